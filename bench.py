@@ -1,0 +1,335 @@
+"""Benchmark: RK-stage DOF updates/s of the DGSEM Euler residual + SSP-RK3.
+
+Workload (one "step" = one SSP-RK3 step = dt reduction + 3 stages):
+  isentropic vortex on the periodic box [0,10]^3 meshed with 64^3 uniform
+  Hex8 cells, DGSEM p = 3 (64 GLL nodes/cell), Rusanov flux, SSP-RK3,
+  CFL 0.1, FP64 (plain form).  L = 83,886,080 DOFs; a step updates 3 L.
+
+Arms
+  default          the GPU library (libmcfd.so) through its C ABI.
+                   value: device-resident stepping (mcfd_advance, dt on the
+                   device, CUDA-graph replay), CUDA events on the handle stream.
+                   e2e: per step mcfd_set_solution from pinned host memory,
+                   one step, mcfd_get_solution to pinned host memory.
+  --impl reference the reference algorithm restated on the CPU (the oracle,
+                   OpenMP over all host cores) on a bounded sample of the same
+                   workload (the 16^3 mesh of the same case).
+
+N > 1 GPUs run independent replicas (the path is single-GPU by design):
+value = sum over ranks / max time over ranks ("scaling": "weak").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "RK-stage DOF updates/s on 1 GB300: plain FP64 vs mixed, at stated L2 error"
+UNIT = "DOF-updates/s"
+N_CELLS_1D = 64
+DEGREE = 3
+CFL = 0.1
+SAMPLE_1D = 16
+K = 5
+
+
+def workload(n1d=N_CELLS_1D):
+    return {
+        "workload": f"isentropic vortex, periodic [0,10]^3, {n1d}^3 Hex8, DGSEM p={DEGREE}, Rusanov, SSP-RK3, CFL {CFL}",
+        "cells": n1d ** 3,
+        "dofs": n1d ** 3 * (DEGREE + 1) ** 3 * K,
+        "form": "plain FP64",
+        "step": "dt reduction + 3 RK stages",
+        "l2_flush": "inputs larger than L2 (solution column 671 MB, geometry 1.3 GB)",
+    }
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during a timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.file, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or self.file is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.file.flush()
+        rows = [r.split(",") for r in Path(self.file.name).read_text().splitlines() if r.strip()]
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [c.strip() for c in r]
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def fp64_peak_tflops(torch, device) -> float:
+    """cuBLAS DGEMM throughput (best of 3), the FP64 denominator."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=device)
+    b = torch.randn(n, n, dtype=torch.float64, device=device)
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = max(best, 2 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    del a, b
+    return best
+
+
+def cpu_sample(steps_min=1, seconds=12.0, max_steps=200, threads=None, fixed_steps=None):
+    """The oracle on the 16^3 sample of the workload, all host cores."""
+    import oracle.orc as orc
+    from pvcriemannsolvers_gb300 import cases, mesh as meshlib
+    orc.build()
+    threads = threads or os.cpu_count() or 1
+    orc.set_threads(threads)
+    m = meshlib.box((SAMPLE_1D,) * 3, lengths=(10.0,) * 3, periodic=(True,) * 3)
+    om = orc.Mesh(m, DEGREE)
+    x = meshlib.node_coordinates(m, DEGREE).reshape(-1, 3)
+    u = cases.vortex_ic(x).ravel()
+    L = u.size
+    t, n, t0 = 0.0, 0, time.perf_counter()
+    while True:
+        dt = om.time_step(u, 1e9, 3, CFL)
+        u = om.rk_update(orc.RUSANOV, 3, t, dt, u)
+        t += dt
+        n += 1
+        el = time.perf_counter() - t0
+        if fixed_steps is not None:
+            if n >= fixed_steps:
+                break
+        elif (n >= steps_min and el >= seconds) or n >= max_steps:
+            break
+    el = time.perf_counter() - t0
+    return {"value": 3 * L * n / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{SAMPLE_1D}^3 cells of the same case (L = {L} DOFs), {n} SSP-RK3 steps, "
+                      f"{el:.1f} s, oracle (plain C restatement, OpenMP)", "seconds": el, "steps": n}
+
+
+def density_l2_vs_exact(sol, mesh, t):
+    """Relative L2 of density against the advected vortex, GLL-weighted."""
+    from pvcriemannsolvers_gb300 import cases, mesh as meshlib
+    q = DEGREE + 1
+    x = meshlib.node_coordinates(mesh, DEGREE).reshape(-1, 3)
+    rho_exact = cases.vortex_prim(x, t)[0]
+    rho = sol.reshape(-1, K)[:, 0]
+    w1 = {4: np.array([1 / 6, 5 / 6, 5 / 6, 1 / 6])}[q]
+    w = np.einsum("i,j,k->ijk", w1, w1, w1).ravel()
+    w = np.tile(w, mesh.n_cells)
+    return float(math.sqrt(np.sum(w * (rho - rho_exact) ** 2) / np.sum(w * rho_exact ** 2)))
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    res = cpu_sample(threads=os.cpu_count(), fixed_steps=args.warmup + args.steps)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": res["value"], "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": res["seconds"] / res["steps"] * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload(SAMPLE_1D),
+        "cpu_baseline": {k: res[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": res["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, rank, world, local_rank):
+    import torch
+    from pvcriemannsolvers_gb300 import Lobatto, build, cases, mesh as meshlib
+    build.build()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    m = meshlib.box((N_CELLS_1D,) * 3, lengths=(10.0,) * 3, periodic=(True,) * 3)
+    sysm = Lobatto(m, DEGREE, "rusanov", cfl=CFL, device=local_rank)
+    stream = torch.cuda.Stream(device=dev)
+    sysm.set_stream(stream.cuda_stream)
+    x = meshlib.node_coordinates(m, DEGREE).reshape(-1, 3)
+    u0 = np.ascontiguousarray(cases.vortex_ic(x).ravel())
+    del x
+    L = u0.size
+    sysm.SetSolutionColumn(u0)
+    # warm-up (also builds the step graph)
+    t = sysm.advance(args.warmup, 1e9, 3, 0.0)
+    sysm.synchronize()
+    # ---- device-resident timed region
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    launches0 = sysm.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clocks:
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            t = sysm.advance(args.steps, 1e9, 3, t)
+            e1.record(stream)
+        e1.synchronize()
+        torch.cuda.synchronize(dev)
+    launches = sysm.launch_count() - launches0
+    ms = e0.elapsed_time(e1)
+    if dist:
+        tt = torch.tensor([ms], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    value = 3 * L * args.steps * world / (ms * 1e-3)
+    sol = sysm.GetSolutionColumn()
+    l2_exact = density_l2_vs_exact(sol, m, t)
+    # ---- kernel times for the roofline (CUDA events on the handle stream)
+    kt = sysm.kernel_times(reps=5)
+    # ---- end to end through the C ABI with pinned host buffers
+    host_in = torch.empty(L, dtype=torch.float64, pin_memory=True).numpy()
+    host_out = torch.empty(L, dtype=torch.float64, pin_memory=True).numpy()
+    host_in[:] = sol
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    te = t
+    for _ in range(args.steps):
+        sysm.SetSolutionColumn(host_in)
+        te = sysm.advance(1, 1e9, 3, te)
+        sysm.get_solution_into(host_out)
+    torch.cuda.synchronize(dev)
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        tt = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    e2e_value = 3 * L * args.steps * world / e2e_s
+    # ---- roofline of the dominant kernel
+    hbm_peak, peak_src = measured_peaks()
+    fp64_peak = fp64_peak_tflops(torch, dev)
+    cells = m.n_cells
+    N = (DEGREE + 1) ** 3
+    dom = "cell_update" if kt["cell_update"] >= kt["face_flux"] else "face_flux"
+    if dom == "cell_update":
+        alg_bytes = 24 * L + (192 + 24) * cells
+        alg_flops = (130 / K + 6 * (DEGREE + 1) + 4) * L
+    else:
+        qf = (DEGREE + 1) ** 2
+        alg_bytes = 2 * K * 8 * 3 * cells * qf + K * 8 * 3 * cells * qf
+        alg_flops = 3 * qf * 60 / (N * K) * L
+    t_dom = kt[dom] * 1e-3
+    achieved = alg_bytes / t_dom / 1e9
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+                "traffic": None, "alg_bytes_per_launch": alg_bytes, "launch_ms": kt[dom],
+                "fp64": {"achieved": alg_flops / t_dom / 1e12, "peak": fp64_peak, "unit": "TFLOP/s",
+                         "frac": alg_flops / t_dom / 1e12 / fp64_peak,
+                         "peak_source": "measured in this run: cuBLAS DGEMM 4096^3",
+                         "alg_flops_per_launch": alg_flops},
+                "binding": "fp64 pipe (see fp64.frac)", "kernel_ms": kt}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_sample()
+        cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload(),
+            "accuracy": {"density_rel_l2_vs_exact": l2_exact, "t_end": t},
+            "clocks": clocks.summary(),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * L, "d2h_bytes_per_step": 8 * L,
+                    "path": "mcfd_set_solution (pinned host) + mcfd_advance(1) + mcfd_get_solution (pinned host)"},
+            "gpu_launches": launches,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    sysm.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    run_gpu(args, rank, world, local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

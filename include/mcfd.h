@@ -1,0 +1,216 @@
+/*
+ * mcfd.h -- C ABI of the GB300-native DG/DGSEM residual and SSP Runge-Kutta
+ * update for the 3D Euler equations (miniCFD's mini::spatial / mini::temporal
+ * hot path), for sm_103a.
+ *
+ * Every entry point takes plain pointers and sizes and returns an int status
+ * (MCFD_OK == 0).  One handle owns the device copy of one mesh and its
+ * solution column; it is used by one host thread at a time, and calls on one
+ * handle are ordered on the handle's CUDA stream.
+ *
+ * Column layout (identical to the reference so Set/GetSolutionColumn are a
+ * drop-in): for cell c (in mesh order), node q (i*Q*Q + j*Q + k, i outer) and
+ * component k (rho, rho*u, rho*v, rho*w, rho*E):
+ *     column[c * 5 * N + q * 5 + k],   N = (p + 1)^3   (DGSEM)
+ * which is the memcpy of the per-cell Eigen K x N column-major coefficient
+ * block in the reference (include/mini/polynomial/expansion.hpp:83-90) placed
+ * at Part::GetCellDataOffset (include/mini/mesh/part.hpp:784-797).
+ *
+ * Reference interfaces replaced (pvcStillInGradSchool/pvcRiemannSolvers):
+ *   include/mini/temporal/ode.hpp:17-48     System<Scalar> virtual quartet
+ *   include/mini/temporal/ode.hpp:92-133    Solver / Euler
+ *   include/mini/temporal/rk.hpp:10-57      RungeKutta<1|2|3>
+ *   include/mini/spatial/fem.hpp:196-258    BC registration, Set/Get columns
+ *   include/mini/spatial/fem.hpp:417-435    GetTimeStep
+ *   include/mini/spatial/dg/lobatto.hpp     dg::Lobatto (DGSEM) residual
+ *   include/mini/riemann/rotated/euler.hpp  rotated Riemann/BC fluxes
+ *   include/mini/spatial/with_limiter.hpp   limiter after SetSolutionColumn
+ */
+#ifndef MCFD_H_
+#define MCFD_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MCFD_ABI_VERSION 1
+#define MCFD_K 5
+
+/* Status codes. */
+enum mcfd_status {
+  MCFD_OK = 0,
+  MCFD_ERR_ARGUMENT = 1,      /* bad argument or size mismatch */
+  MCFD_ERR_MESH = 2,          /* inconsistent mesh (index or face matching) */
+  MCFD_ERR_CUDA = 3,          /* CUDA runtime error (message in last_error) */
+  MCFD_ERR_STATE = 4,         /* non-finite value produced by a kernel */
+  MCFD_ERR_NOT_CONVERGED = 5, /* Exact solver hit its iteration cap */
+  MCFD_ERR_UNSUPPORTED = 6,   /* option combination not built */
+  MCFD_ERR_NO_DEVICE = 7      /* no CUDA device / wrong architecture */
+};
+
+/* Riemann solvers.  Exact / HLLC / AUSM follow
+ * include/mini/riemann/euler/{exact,hllc,ausm}.hpp; Roe and Rusanov follow the
+ * reference's 1D prototype python/riemann.py:405-476 extended to 3D. */
+enum mcfd_riemann {
+  MCFD_EXACT = 0,
+  MCFD_HLLC = 1,
+  MCFD_AUSM = 2,
+  MCFD_ROE = 3,
+  MCFD_RUSANOV = 4
+};
+
+/* Boundary kinds (include/mini/spatial/fem.hpp:196-222 registry,
+ * include/mini/riemann/rotated/euler.hpp:144-318 fluxes). */
+enum mcfd_bc_kind {
+  MCFD_BC_NONE = 0,
+  MCFD_BC_INVISCID_WALL = 1,     /* SetInviscidWall */
+  MCFD_BC_SUPERSONIC_INLET = 2,  /* SetSupersonicInlet(value) */
+  MCFD_BC_SUPERSONIC_OUTLET = 3, /* SetSupersonicOutlet */
+  MCFD_BC_SUBSONIC_INLET = 4,    /* SetSubsonicInlet(p0, cos x/y/z, T0) */
+  MCFD_BC_SUBSONIC_OUTLET = 5,   /* SetSubsonicOutlet(value[4] = p) */
+  MCFD_BC_SMART = 6              /* SetSmartBoundary(value) */
+};
+
+/* The reference passes a std::function<Value(Global, double t)> per boundary
+ * name.  The ABI carries that function as a small program evaluated on the
+ * device at every boundary face point and stage time:
+ *   CONSTANT:     value = a
+ *   MOVING_SPLIT: value = (x[axis] - speed * t) < position ? a : b
+ * (the second form is the moving-shock boundary of demo/euler/riemann2d.cpp).
+ * a and b are conservative states, or for SUBSONIC_INLET the tuple
+ * (p_total, cos_x, cos_y, cos_z, T_total), as in the reference. */
+enum mcfd_state_program {
+  MCFD_STATE_CONSTANT = 0,
+  MCFD_STATE_MOVING_SPLIT = 1
+};
+
+typedef struct mcfd_bc_state {
+  int32_t kind;    /* enum mcfd_bc_kind */
+  int32_t program; /* enum mcfd_state_program */
+  int32_t axis;    /* 0, 1, 2 (MOVING_SPLIT only) */
+  int32_t reserved;
+  double position;
+  double speed;
+  double a[MCFD_K];
+  double b[MCFD_K];
+} mcfd_bc_state;
+
+enum mcfd_cell_type { MCFD_HEX8 = 0, MCFD_TET4 = 1 };
+
+/* Unstructured mesh, the input that replaces mesh::part::Part
+ * (include/mini/mesh/part.hpp:97-291):
+ *   xyz          [n_nodes][3] node coordinates
+ *   cell_nodes   [n_cells][8] node ids in CGNS order (Hex8)
+ *   cell_type    [n_cells] enum mcfd_cell_type, or NULL for all Hex8
+ *   face_cells   [n_faces][2] holder, sharer (-1 on a boundary).  The face
+ *                normal points from the holder to the sharer (outward on a
+ *                boundary), as in part.hpp:1518-1538.
+ *   face_sides   [n_faces][2] local face index (0..5, the order of
+ *                coordinate/hexahedron.hpp:378-389) in the holder and sharer
+ *   face_group   [n_faces] boundary group id (>= 0) or -1 for interior faces
+ *   face_shift   [n_faces][3] or NULL: periodic translation such that
+ *                x(sharer side) + shift = x(holder side).  The reference has
+ *                no periodic boundary; a periodic face here is an ordinary
+ *                interior face whose sharer is found through this shift. */
+typedef struct mcfd_mesh_desc {
+  int64_t n_nodes;
+  const double *xyz;
+  int64_t n_cells;
+  const int64_t *cell_nodes;
+  const int32_t *cell_type;
+  int64_t n_faces;
+  const int64_t *face_cells;
+  const int32_t *face_sides;
+  const int32_t *face_group;
+  const double *face_shift;
+} mcfd_mesh_desc;
+
+enum mcfd_scheme { MCFD_DGSEM = 0 };
+enum mcfd_precision { MCFD_FP64 = 0, MCFD_MIXED = 1 };
+
+typedef struct mcfd_options {
+  int32_t degree;    /* polynomial degree p (1..3) */
+  int32_t scheme;    /* enum mcfd_scheme */
+  int32_t riemann;   /* enum mcfd_riemann */
+  int32_t precision; /* enum mcfd_precision */
+  double cfl;        /* <= 0: the reference table fem.hpp:26-37 */
+  int32_t device;    /* CUDA device ordinal */
+  int32_t reserved[7];
+} mcfd_options;
+
+typedef struct mcfd_handle mcfd_handle;
+
+/* Library identification. */
+int mcfd_abi_version(void);
+
+/* Builds the device-resident mesh and geometry.  Replaces the construction
+ * of spatial::FiniteElement / dg::Lobatto (fem.hpp:95-115, lobatto.hpp:113-125):
+ * Riemann frames per face point and face-point to cell-node matching. */
+int mcfd_create(const mcfd_mesh_desc *mesh, const mcfd_options *options,
+                mcfd_handle **out);
+int mcfd_destroy(mcfd_handle *h);
+
+/* Length of the solution column (Part::GetCellDataSize, part.hpp:793-797). */
+int64_t mcfd_column_size(const mcfd_handle *h);
+
+/* Boundary registration for one face group (fem.hpp:196-222). */
+int mcfd_set_bc(mcfd_handle *h, int32_t group, const mcfd_bc_state *state);
+
+/* System<Scalar> quartet (ode.hpp:17-48): host columns of length n. */
+int mcfd_set_time(mcfd_handle *h, double t);
+int mcfd_set_solution(mcfd_handle *h, const double *column, int64_t n);
+int mcfd_get_solution(mcfd_handle *h, double *column, int64_t n);
+/* GetResidualColumn of dg::Lobatto incl. the lumped mass divide
+ * (fem.hpp:248-258, lobatto.hpp:143-158). */
+int mcfd_residual(mcfd_handle *h, double *residual, int64_t n);
+
+/* Same three calls on caller-owned device memory (no host copies). */
+int mcfd_set_solution_device(mcfd_handle *h, const double *d_column, int64_t n);
+int mcfd_get_solution_device(mcfd_handle *h, double *d_column, int64_t n);
+int mcfd_residual_device(mcfd_handle *h, double *d_residual, int64_t n);
+
+/* FiniteElement::GetTimeStep(dt_guess, rk_order) (fem.hpp:417-435). */
+int mcfd_time_step(mcfd_handle *h, double dt_guess, int32_t rk_order,
+                   double *dt);
+
+/* RungeKutta<order>::Update(system, t, dt) (rk.hpp:16-49), fused on device. */
+int mcfd_rk_step(mcfd_handle *h, double t, double dt, int32_t order);
+
+/* The driver loop of demo/euler/sourceless.cpp:187-215 without I/O:
+ * n_steps x { dt = GetTimeStep(dt_guess, order); Update(t, dt); t += dt },
+ * with dt and t kept on the device (no host round trip per step).  *t is the
+ * start time on entry and the end time on return. */
+int mcfd_advance(mcfd_handle *h, int32_t n_steps, double dt_guess,
+                 int32_t rk_order, double *t);
+
+/* Use a caller-provided cudaStream_t (NULL = the handle's own stream). */
+int mcfd_set_stream(mcfd_handle *h, void *cuda_stream);
+int mcfd_synchronize(mcfd_handle *h);
+
+/* Face-point to cell-node maps (lobatto.hpp:54-78 i_node_on_holder_ /
+ * i_node_on_sharer_), [n_faces][(p+1)^2] each; sharer entries of boundary
+ * faces are -1.  For indexing parity checks. */
+int mcfd_face_node_maps(const mcfd_handle *h, int16_t *holder, int16_t *sharer);
+
+/* Kernel launches issued by this handle since creation. */
+int64_t mcfd_launch_count(const mcfd_handle *h);
+
+/* Instrumentation (the reference times with MPI_Wtime in
+ * demo/euler/sourceless.cpp:94-215): average device time in milliseconds of
+ * one launch of each kernel of an SSP-RK3 stage, measured with CUDA events on
+ * the handle's stream over `reps` launches on the current solution (which is
+ * left unchanged).  out_ms[0] = dt reduction, [1] = face fluxes,
+ * [2] = cell update (volume + lift + mass + stage), [3] = whole RK3 step. */
+int mcfd_kernel_times(mcfd_handle *h, int32_t reps, double *out_ms);
+
+/* Message describing the last failure on this handle (or of mcfd_create when
+ * h is NULL).  Valid until the next call on the handle. */
+const char *mcfd_last_error(const mcfd_handle *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MCFD_H_ */

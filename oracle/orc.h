@@ -1,0 +1,129 @@
+/*
+ * CPU restatement of miniCFD's DG/DGSEM residual + SSP-RK path (the ORACLE).
+ *
+ * This is TEST INFRASTRUCTURE.  It is the parity checker for the GPU library
+ * and the timed CPU baseline.  Only tests/, __graft_entry__.smoke() and the
+ * cpu_baseline / reference legs of bench.py load it.  The product library
+ * never links, loads or calls it.
+ *
+ * Every routine restates one reference routine (file:line in the reference
+ * project pvcStillInGradSchool/pvcRiemannSolvers) in plain C, keeping the
+ * reference's operation order where that order is observable:
+ *   gas conversions          include/mini/riemann/euler/types.hpp:186-334
+ *   Exact / HLLC / AUSM      include/mini/riemann/euler/{exact,hllc,ausm}.hpp
+ *   Roe / Lax-Friedrichs     python/riemann.py:405-476 (1D), restated in 3D
+ *   rotated wrapper + BCs    include/mini/riemann/rotated/euler.hpp:42-345
+ *   GLL rule                 include/mini/integrator/lobatto.hpp:37-83
+ *   Lagrange line basis      include/mini/basis/lagrange.hpp:53-142
+ *   Hex8 map / face table    include/mini/coordinate/hexahedron.hpp:353-490
+ *   face frames              include/mini/coordinate/face.hpp:54-62
+ *   quadrature points        include/mini/integrator/element.hpp:102-115
+ *   DGSEM residual           include/mini/spatial/dg/lobatto.hpp:58-302
+ *   residual orchestration   include/mini/spatial/fem.hpp:248-307
+ *   time step                include/mini/spatial/fem.hpp:417-435
+ *   SSP-RK1/2/3              include/mini/temporal/rk.hpp:16-49, ode.hpp:121-133
+ */
+#ifndef MCFD_ORACLE_ORC_H_
+#define MCFD_ORACLE_ORC_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORC_K 5
+
+/* Riemann solver kinds (same numbering as the product's mcfd.h). */
+enum { ORC_EXACT = 0, ORC_HLLC = 1, ORC_AUSM = 2, ORC_ROE = 3, ORC_RUSANOV = 4 };
+
+/* Boundary kinds (same numbering as the product's mcfd.h). */
+enum {
+  ORC_BC_NONE = 0,
+  ORC_BC_INVISCID_WALL = 1,
+  ORC_BC_SUPERSONIC_INLET = 2,
+  ORC_BC_SUPERSONIC_OUTLET = 3,
+  ORC_BC_SUBSONIC_INLET = 4,
+  ORC_BC_SUBSONIC_OUTLET = 5,
+  ORC_BC_SMART = 6
+};
+
+/* Given-state programs for boundaries that need an exterior value. */
+enum { ORC_STATE_CONSTANT = 0, ORC_STATE_MOVING_SPLIT = 1 };
+
+/* One boundary group: kind, and the given value program
+ * value(x, t) = (x[axis] - speed * t) < position ? a : b   (MOVING_SPLIT)
+ * value(x, t) = a                                           (CONSTANT)   */
+typedef struct {
+  int kind;
+  int program;
+  int axis;
+  double position, speed;
+  double a[ORC_K], b[ORC_K];
+} orc_bc;
+
+/* ---- point functions (used by the golden-vector tests) ---- */
+void orc_cons_to_prim(const double *cons, double *prim);
+void orc_prim_to_cons(const double *prim, double *cons);
+void orc_flux_matrix(const double *cons, double *mat15); /* row-major 5x3 */
+double orc_max_speed(const double *cons);
+/* 1D (normal-frame) upwind flux from primitive (rho, u, v, w, p) pairs. */
+void orc_flux_1d(int kind, const double *prim_l, const double *prim_r,
+                 double *flux);
+/* Rotated flux: frame = {normal, tangent, bitangent} row-major 3x3. */
+void orc_flux_rotated(int kind, const double *frame, const double *cons_l,
+                      const double *cons_r, double *flux);
+void orc_flux_boundary(int riemann, int bc_kind, const double *frame,
+                       const double *cons_in, const double *given,
+                       double *flux);
+
+/* ---- mesh + DGSEM ---- */
+typedef struct orc_mesh orc_mesh;
+
+/* The mesh description shared with the product (see include/mcfd.h).
+ * cell_nodes: 8 entries per cell, CGNS order; faces: holder, sharer (-1 on a
+ * boundary), the local face index on each side, the boundary group (-1 for
+ * interior faces) and an optional periodic shift such that
+ * x(sharer side) + shift = x(holder side). */
+orc_mesh *orc_mesh_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
+                          const int64_t *cell_nodes, int64_t n_faces,
+                          const int64_t *face_cells, const int32_t *face_sides,
+                          const int32_t *face_group, const double *face_shift,
+                          int degree);
+void orc_mesh_destroy(orc_mesh *m);
+int64_t orc_column_size(const orc_mesh *m);
+int orc_nodes_per_cell(const orc_mesh *m);
+/* Node matching tables (reference dg/lobatto.hpp:58-78): int16 per face point;
+ * sharer entries of boundary faces are -1. */
+int orc_face_node_maps(const orc_mesh *m, int16_t *holder, int16_t *sharer);
+/* Per node global coordinates [n_cells][N][3] and global weights [n_cells][N]. */
+int orc_node_geometry(const orc_mesh *m, double *xyz, double *weights);
+/* Per face point global coordinates / weights / frames. */
+int orc_face_geometry(const orc_mesh *m, double *xyz, double *weights,
+                      double *frames);
+double orc_cell_length(const orc_mesh *m, int64_t i_cell);
+
+void orc_set_threads(int n);
+int orc_get_threads(void);
+
+/* GetResidualColumn of dg::Lobatto (lumped mass divide included). */
+int orc_dgsem_residual(const orc_mesh *m, int riemann, int n_bc,
+                       const orc_bc *bcs, double t, const double *u, double *r);
+/* FiniteElement::GetTimeStep with an explicit CFL number (cfl <= 0 selects
+ * the reference table cfl_[rk_order][p]). */
+double orc_time_step(const orc_mesh *m, const double *u, double dt_guess,
+                     int rk_order, double cfl);
+/* RungeKutta<order>::Update over the DGSEM system, in place on u. */
+int orc_rk_update(const orc_mesh *m, int riemann, int n_bc, const orc_bc *bcs,
+                  int order, double t, double dt, double *u);
+
+/* RungeKutta<order>::Update on the linear system du/dt = A u (temporal
+ * test physics, reference ode.hpp:55-85); A row-major n x n. */
+int orc_rk_update_linear(int order, int64_t n, const double *a, double t,
+                         double dt, double *u);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MCFD_ORACLE_ORC_H_ */

@@ -1,0 +1,237 @@
+"""ctypes loader of the CPU oracle liborc.so (test infrastructure only).
+
+liborc.so is the plain-C restatement of the reference's DGSEM residual,
+Riemann solvers, time step and Runge-Kutta steppers (see orc.h for the
+reference file:line of every routine).  It is the checker of the GPU library
+and the timed CPU baseline, never the thing measured as the product.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "liborc.so"
+
+EXACT, HLLC, AUSM, ROE, RUSANOV = range(5)
+BC_NONE, BC_INVISCID_WALL, BC_SUPERSONIC_INLET, BC_SUPERSONIC_OUTLET, BC_SUBSONIC_INLET, \
+    BC_SUBSONIC_OUTLET, BC_SMART = range(7)
+STATE_CONSTANT, STATE_MOVING_SPLIT = 0, 1
+
+_D = C.POINTER(C.c_double)
+
+
+class OrcBc(C.Structure):
+    _fields_ = [("kind", C.c_int), ("program", C.c_int), ("axis", C.c_int),
+                ("position", C.c_double), ("speed", C.c_double),
+                ("a", C.c_double * 5), ("b", C.c_double * 5)]
+
+
+def build(force: bool = False) -> Path:
+    """make -C oracle (portable flags; rebuilt on each host)."""
+    srcs = list(HERE.glob("*.c")) + list(HERE.glob("*.h")) + [HERE / "Makefile"]
+    if force or not LIB.exists() or any(p.stat().st_mtime > LIB.stat().st_mtime for p in srcs):
+        subprocess.run(["make", "-s", "-B" if force else "-s", "-C", str(HERE)], check=True)
+    return LIB
+
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        lib = C.CDLL(str(LIB))
+        sig = {
+            "orc_cons_to_prim": (None, [_D, _D]),
+            "orc_prim_to_cons": (None, [_D, _D]),
+            "orc_flux_matrix": (None, [_D, _D]),
+            "orc_max_speed": (C.c_double, [_D]),
+            "orc_flux_1d": (None, [C.c_int, _D, _D, _D]),
+            "orc_flux_rotated": (None, [C.c_int, _D, _D, _D, _D]),
+            "orc_flux_boundary": (None, [C.c_int, C.c_int, _D, _D, _D, _D]),
+            "orc_mesh_create": (C.c_void_p, [C.c_int64, _D, C.c_int64, C.POINTER(C.c_int64), C.c_int64,
+                                             C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                             _D, C.c_int]),
+            "orc_mesh_destroy": (None, [C.c_void_p]),
+            "orc_column_size": (C.c_int64, [C.c_void_p]),
+            "orc_nodes_per_cell": (C.c_int, [C.c_void_p]),
+            "orc_face_node_maps": (C.c_int, [C.c_void_p, C.POINTER(C.c_int16), C.POINTER(C.c_int16)]),
+            "orc_node_geometry": (C.c_int, [C.c_void_p, _D, _D]),
+            "orc_face_geometry": (C.c_int, [C.c_void_p, _D, _D, _D]),
+            "orc_cell_length": (C.c_double, [C.c_void_p, C.c_int64]),
+            "orc_set_threads": (None, [C.c_int]),
+            "orc_get_threads": (C.c_int, []),
+            "orc_dgsem_residual": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(OrcBc), C.c_double, _D, _D]),
+            "orc_time_step": (C.c_double, [C.c_void_p, _D, C.c_double, C.c_int, C.c_double]),
+            "orc_rk_update": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(OrcBc), C.c_int, C.c_double,
+                                        C.c_double, _D]),
+            "orc_rk_update_linear": (C.c_int, [C.c_int, C.c_int64, _D, C.c_double, C.c_double, _D]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(_D)
+
+
+def cons_to_prim(u) -> np.ndarray:
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    out = np.empty(5)
+    load().orc_cons_to_prim(_p(u), _p(out))
+    return out
+
+
+def prim_to_cons(w) -> np.ndarray:
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    out = np.empty(5)
+    load().orc_prim_to_cons(_p(w), _p(out))
+    return out
+
+
+def flux_matrix(u) -> np.ndarray:
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    out = np.empty(15)
+    load().orc_flux_matrix(_p(u), _p(out))
+    return out.reshape(5, 3)
+
+
+def max_speed(u) -> float:
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    return float(load().orc_max_speed(_p(u)))
+
+
+def flux_1d(kind: int, prim_l, prim_r) -> np.ndarray:
+    """Normal-frame flux from primitive (rho, u, v, w, p) states."""
+    l = np.ascontiguousarray(prim_l, dtype=np.float64)
+    r = np.ascontiguousarray(prim_r, dtype=np.float64)
+    out = np.empty(5)
+    load().orc_flux_1d(kind, _p(l), _p(r), _p(out))
+    return out
+
+
+def flux_rotated(kind: int, frame, cons_l, cons_r) -> np.ndarray:
+    f = np.ascontiguousarray(frame, dtype=np.float64).reshape(9)
+    l = np.ascontiguousarray(cons_l, dtype=np.float64)
+    r = np.ascontiguousarray(cons_r, dtype=np.float64)
+    out = np.empty(5)
+    load().orc_flux_rotated(kind, _p(f), _p(l), _p(r), _p(out))
+    return out
+
+
+def flux_boundary(riemann: int, bc_kind: int, frame, cons_in, given) -> np.ndarray:
+    f = np.ascontiguousarray(frame, dtype=np.float64).reshape(9)
+    u = np.ascontiguousarray(cons_in, dtype=np.float64)
+    g = np.ascontiguousarray(given, dtype=np.float64)
+    out = np.empty(5)
+    load().orc_flux_boundary(riemann, bc_kind, _p(f), _p(u), _p(g), _p(out))
+    return out
+
+
+def make_bcs(specs: dict[int, tuple]) -> tuple[int, C.Array]:
+    """specs: group -> (kind, value) with value None, a 5-vector, or an object
+    with axis/position/speed/a/b (moving split)."""
+    n = max(specs) + 1 if specs else 1
+    arr = (OrcBc * n)()
+    for g, (kind, value) in specs.items():
+        b = arr[g]
+        b.kind = kind
+        if value is None:
+            b.program = STATE_CONSTANT
+        elif hasattr(value, "axis"):
+            b.program = STATE_MOVING_SPLIT
+            b.axis, b.position, b.speed = int(value.axis), float(value.position), float(value.speed)
+            for k in range(5):
+                b.a[k] = float(value.a[k])
+                b.b[k] = float(value.b[k])
+        else:
+            b.program = STATE_CONSTANT
+            for k in range(5):
+                b.a[k] = float(value[k])
+    return n, arr
+
+
+class Mesh:
+    """Oracle-side mesh + DGSEM system built from the same description."""
+
+    def __init__(self, mesh, degree: int):
+        lib = load()
+        self._keep = [np.ascontiguousarray(mesh.xyz, dtype=np.float64),
+                      np.ascontiguousarray(mesh.cell_nodes, dtype=np.int64),
+                      np.ascontiguousarray(mesh.face_cells, dtype=np.int64),
+                      np.ascontiguousarray(mesh.face_sides, dtype=np.int32),
+                      np.ascontiguousarray(mesh.face_group, dtype=np.int32),
+                      np.ascontiguousarray(mesh.face_shift, dtype=np.float64)]
+        xyz, cn, fc, fs, fg, fsh = self._keep
+        self._m = lib.orc_mesh_create(xyz.shape[0], _p(xyz), cn.shape[0], cn.ctypes.data_as(C.POINTER(C.c_int64)),
+                                      fc.shape[0], fc.ctypes.data_as(C.POINTER(C.c_int64)),
+                                      fs.ctypes.data_as(C.POINTER(C.c_int32)),
+                                      fg.ctypes.data_as(C.POINTER(C.c_int32)), _p(fsh), degree)
+        if not self._m:
+            raise RuntimeError("oracle rejected the mesh (unmatched face point or bad index)")
+        self.lib = lib
+        self.degree = degree
+        self.n_faces = fc.shape[0]
+        self.n_cells = cn.shape[0]
+        self.column_size = int(lib.orc_column_size(self._m))
+        self.bcs = make_bcs({})
+
+    def __del__(self):
+        if getattr(self, "_m", None):
+            self.lib.orc_mesh_destroy(self._m)
+            self._m = None
+
+    def set_bcs(self, specs: dict[int, tuple]) -> None:
+        self.bcs = make_bcs(specs)
+
+    def face_node_maps(self):
+        qf = (self.degree + 1) ** 2
+        h = np.empty((self.n_faces, qf), dtype=np.int16)
+        s = np.empty((self.n_faces, qf), dtype=np.int16)
+        self.lib.orc_face_node_maps(self._m, h.ctypes.data_as(C.POINTER(C.c_int16)),
+                                    s.ctypes.data_as(C.POINTER(C.c_int16)))
+        return h, s
+
+    def node_geometry(self):
+        n = (self.degree + 1) ** 3
+        xyz = np.empty((self.n_cells, n, 3))
+        w = np.empty((self.n_cells, n))
+        self.lib.orc_node_geometry(self._m, _p(xyz), _p(w))
+        return xyz, w
+
+    def residual(self, riemann: int, u: np.ndarray, t: float = 0.0) -> np.ndarray:
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        r = np.empty_like(u)
+        n, arr = self.bcs
+        self.lib.orc_dgsem_residual(self._m, riemann, n, arr, t, _p(u), _p(r))
+        return r
+
+    def time_step(self, u: np.ndarray, dt_guess: float, rk_order: int, cfl: float = 0.0) -> float:
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        return float(self.lib.orc_time_step(self._m, _p(u), dt_guess, rk_order, cfl))
+
+    def rk_update(self, riemann: int, order: int, t: float, dt: float, u: np.ndarray) -> np.ndarray:
+        u = np.array(u, dtype=np.float64, copy=True)
+        n, arr = self.bcs
+        self.lib.orc_rk_update(self._m, riemann, n, arr, order, t, dt, _p(u))
+        return u
+
+
+def set_threads(n: int) -> None:
+    load().orc_set_threads(n)
+
+
+def rk_update_linear(order: int, a: np.ndarray, t: float, dt: float, u: np.ndarray) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    u = np.array(u, dtype=np.float64, copy=True)
+    load().orc_rk_update_linear(order, u.size, _p(a), t, dt, _p(u))
+    return u

@@ -1,0 +1,701 @@
+// C ABI of the GB300 DGSEM Euler residual + SSP-RK library (include/mcfd.h).
+//
+// mcfd_create ingests an unstructured Hex8 mesh and builds, on the host in
+// FP64, everything the reference's FiniteElement / dg::Lobatto constructors
+// build (spatial/fem.hpp:95-115, spatial/dg/lobatto.hpp:58-125,
+// polynomial/hexahedron.hpp:221-239, integrator/element.hpp:102-115):
+//   * per cell node: the global weight w = w_i w_j w_k det(J) and w J^-1,
+//     stored together with 1/w (the lumped GLL mass);
+//   * per face point: the unit normal of the holder-sorted Quad4 face
+//     (coordinate/face.hpp:54-62) and the face weight w_a w_b |x_a x x_b|;
+//   * face-point -> cell-node maps.  The reference searches every cell node
+//     for one within 1e-12 of the face point (lobatto.hpp:58-78); here the map
+//     follows from the two local face indices and the corner correspondence,
+//     and every matched pair is then checked geometrically;
+//   * per cell and local face the flux slots each face node lifts from.
+// Everything is uploaded once; the solution column stays on the device.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/mcfd.h"
+#include "euler.cuh"
+#include "handle.hpp"
+
+namespace {
+
+using mcfd::BcDev;
+
+thread_local std::string g_create_error;
+
+// Hex8 local corner coordinates and the first four nodes of each face of
+// the CGNS hexahedron (coordinate/hexahedron.hpp:353-389): the face node
+// order fixes the face parametrisation and the outward normal.
+const int kHexLocal[8][3] = {{-1, -1, -1}, {+1, -1, -1}, {+1, +1, -1},
+                             {-1, +1, -1}, {-1, -1, +1}, {+1, -1, +1},
+                             {+1, +1, +1}, {-1, +1, +1}};
+const int kHexFace[6][4] = {{0, 3, 2, 1}, {0, 1, 5, 4}, {1, 2, 6, 5},
+                            {2, 3, 7, 6}, {0, 4, 7, 3}, {4, 5, 6, 7}};
+
+// Gauss-Lobatto rule (integrator/lobatto.hpp:37-83).
+void gll(int q, double *x, double *w) {
+  if (q == 2) {
+    x[0] = -1; x[1] = 1; w[0] = 1; w[1] = 1;
+  } else if (q == 3) {
+    x[0] = -1; x[1] = 0; x[2] = 1;
+    w[0] = 1.0 / 3; w[1] = 4.0 / 3; w[2] = 1.0 / 3;
+  } else {
+    x[0] = -1; x[1] = -std::sqrt(1.0 / 5); x[2] = std::sqrt(1.0 / 5); x[3] = 1;
+    w[0] = 1.0 / 6; w[1] = 5.0 / 6; w[2] = 5.0 / 6; w[3] = 1.0 / 6;
+  }
+}
+
+// Lagrange differentiation matrix D[a][i] = l_i'(x_a) in barycentric form.
+void diff_matrix(int q, const double *x, double *d) {
+  double bw[8];
+  for (int i = 0; i < q; ++i) {
+    double p = 1;
+    for (int j = 0; j < q; ++j)
+      if (j != i) p *= (x[i] - x[j]);
+    bw[i] = 1.0 / p;
+  }
+  for (int a = 0; a < q; ++a) {
+    double diag = 0;
+    for (int i = 0; i < q; ++i) {
+      if (i == a) continue;
+      double v = (bw[i] / bw[a]) / (x[a] - x[i]);
+      d[a * q + i] = v;
+      diag -= v;
+    }
+    d[a * q + a] = diag;
+  }
+}
+
+void hex8_point(const double *xn, double a, double b, double c, double *x,
+                double *jac) {
+  x[0] = x[1] = x[2] = 0;
+  for (int e = 0; e < 9; ++e) jac[e] = 0;
+  for (int v = 0; v < 8; ++v) {
+    double fa = 1 + kHexLocal[v][0] * a, fb = 1 + kHexLocal[v][1] * b,
+           fc = 1 + kHexLocal[v][2] * c;
+    double s = fa * fb * fc / 8;
+    double g[3] = {kHexLocal[v][0] * fb * fc / 8, kHexLocal[v][1] * fa * fc / 8,
+                   kHexLocal[v][2] * fa * fb / 8};
+    for (int d = 0; d < 3; ++d) {
+      x[d] += s * xn[v * 3 + d];
+      for (int r = 0; r < 3; ++r) jac[r * 3 + d] += g[r] * xn[v * 3 + d];
+    }
+  }
+}
+
+void quad4_point(const double *xn, double a, double b, double *x, double *ta,
+                 double *tb) {
+  const int loc[4][2] = {{-1, -1}, {+1, -1}, {+1, +1}, {-1, +1}};
+  for (int d = 0; d < 3; ++d) x[d] = ta[d] = tb[d] = 0;
+  for (int v = 0; v < 4; ++v) {
+    double fa = 1 + loc[v][0] * a, fb = 1 + loc[v][1] * b;
+    for (int d = 0; d < 3; ++d) {
+      x[d] += fa * fb / 4 * xn[v * 3 + d];
+      ta[d] += loc[v][0] * fb / 4 * xn[v * 3 + d];
+      tb[d] += loc[v][1] * fa / 4 * xn[v * 3 + d];
+    }
+  }
+}
+
+// Grid index (i, j, k) of hex corner v on a Q-point GLL grid.
+void corner_grid(int v, int q, int *g) {
+  for (int d = 0; d < 3; ++d) g[d] = (kHexLocal[v][d] + 1) / 2 * (q - 1);
+}
+
+int fail(mcfd_handle *h, int code, const std::string &msg) {
+  if (h) h->err = msg; else g_create_error = msg;
+  return code;
+}
+
+int cuda_fail(mcfd_handle *h, cudaError_t e, const char *what) {
+  return fail(h, MCFD_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CUDA_TRY(h, call)                                  \
+  do {                                                     \
+    cudaError_t e_ = (call);                               \
+    if (e_ != cudaSuccess) return cuda_fail(h, e_, #call); \
+  } while (0)
+
+template <class T>
+int upload(mcfd_handle *h, T **dst, const std::vector<T> &src) {
+  if (src.empty()) { *dst = nullptr; return MCFD_OK; }
+  CUDA_TRY(h, cudaMalloc(dst, sizeof(T) * src.size()));
+  CUDA_TRY(h, cudaMemcpy(*dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice));
+  return MCFD_OK;
+}
+
+void release(mcfd_handle *h) {
+  auto &m = h->mesh;
+  auto &b = h->buf;
+  void *ptrs[] = {m.cell_geo, m.cell_rate, m.cell_flux, m.face_cells,
+                  m.face_group, m.face_geo, m.face_xyz, m.face_map, m.dmat,
+                  m.bcs, b.u, b.u1, b.u2, b.res, b.flux, b.state};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  if (h->step_graph) cudaGraphExecDestroy(h->step_graph);
+  if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+}
+
+int check_status(mcfd_handle *h) {
+  mcfd::DevState st;
+  CUDA_TRY(h, cudaMemcpyAsync(&st, h->buf.state, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  CUDA_TRY(h, cudaGetLastError());
+  if (st.status) {
+    unsigned zero = 0;
+    CUDA_TRY(h, cudaMemcpy(&h->buf.state->status, &zero, sizeof(zero), cudaMemcpyHostToDevice));
+    if (st.status & mcfd::kStatusNotConverged)
+      return fail(h, MCFD_ERR_NOT_CONVERGED, "Exact Riemann solver reached its iteration cap");
+    return fail(h, MCFD_ERR_STATE, "a kernel produced a non-finite value");
+  }
+  return MCFD_OK;
+}
+
+double cfl_table(int rk_order, int p) {
+  // spatial/fem.hpp:26-37
+  static const double cfl[5][9] = {
+      {1.000},
+      {1.000, 0.333},
+      {1.000, 0.333, 0.209, 0.130, 0.089, 0.066, 0.051, 0.040, 0.033},
+      {1.256, 0.409, 0.209, 0.130, 0.089, 0.066, 0.051, 0.040, 0.033},
+      {1.392, 0.464, 0.235, 0.145, 0.100, 0.073, 0.056, 0.045, 0.037}};
+  rk_order = std::min(std::max(rk_order, 0), 4);
+  return cfl[rk_order][std::min(p, 8)];
+}
+
+int build_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
+  auto &m = h->mesh;
+  m.p = degree;
+  m.q = degree + 1;
+  m.n = m.q * m.q * m.q;
+  m.qf = m.q * m.q;
+  m.n_cells = d->n_cells;
+  m.n_faces = d->n_faces;
+  m.n_points = d->n_faces * m.qf;
+  m.column = d->n_cells * mcfd::kK * m.n;
+  const int Q = m.q, N = m.n, QF = m.qf;
+  double xq[4], wq[4], dm[16];
+  gll(Q, xq, wq);
+  diff_matrix(Q, xq, dm);
+  for (int64_t c = 0; c < d->n_cells; ++c) {
+    if (d->cell_type && d->cell_type[c] != MCFD_HEX8)
+      return fail(h, MCFD_ERR_UNSUPPORTED, "only Hex8 cells are supported by the DGSEM scheme");
+    for (int v = 0; v < 8; ++v) {
+      int64_t id = d->cell_nodes[c * 8 + v];
+      if (id < 0 || id >= d->n_nodes)
+        return fail(h, MCFD_ERR_MESH, "cell node index out of range in cell " + std::to_string(c));
+    }
+  }
+  // ---- per node geometry
+  std::vector<double> geo((size_t)d->n_cells * N * 10);
+  std::vector<double> rate(d->n_cells);
+  int bad_jac = 0;
+#pragma omp parallel for schedule(static)
+  for (int64_t c = 0; c < d->n_cells; ++c) {
+    double xn[24];
+    for (int v = 0; v < 8; ++v)
+      for (int e = 0; e < 3; ++e) xn[v * 3 + e] = d->xyz[d->cell_nodes[c * 8 + v] * 3 + e];
+    double volume = 0;
+    for (int i = 0; i < Q; ++i)
+      for (int j = 0; j < Q; ++j)
+        for (int k = 0; k < Q; ++k) {
+          double x[3], J[9];
+          hex8_point(xn, xq[i], xq[j], xq[k], x, J);
+          double det = J[0] * (J[4] * J[8] - J[5] * J[7]) -
+                       J[1] * (J[3] * J[8] - J[5] * J[6]) +
+                       J[2] * (J[3] * J[7] - J[4] * J[6]);
+          if (!(det > 0)) bad_jac = 1;
+          double w = wq[i] * wq[j] * wq[k] * det;
+          volume += w;
+          // w * J^-1 = (w / det) * adj(J)
+          double s = w / det;
+          double *g = &geo[((size_t)c * N + (i * Q + j) * Q + k) * 10];
+          g[0] = s * (J[4] * J[8] - J[5] * J[7]);
+          g[1] = s * (J[2] * J[7] - J[1] * J[8]);
+          g[2] = s * (J[1] * J[5] - J[2] * J[4]);
+          g[3] = s * (J[5] * J[6] - J[3] * J[8]);
+          g[4] = s * (J[0] * J[8] - J[2] * J[6]);
+          g[5] = s * (J[2] * J[3] - J[0] * J[5]);
+          g[6] = s * (J[3] * J[7] - J[4] * J[6]);
+          g[7] = s * (J[1] * J[6] - J[0] * J[7]);
+          g[8] = s * (J[0] * J[4] - J[1] * J[3]);
+          g[9] = 1.0 / w;
+        }
+    rate[c] = 1.0 / (std::cbrt(volume) * 0.5);
+  }
+  if (bad_jac) return fail(h, MCFD_ERR_MESH, "non-positive Jacobian determinant at a cell node");
+  // ---- faces
+  std::vector<int2> fcells(d->n_faces);
+  std::vector<int32_t> fgroup(d->n_faces);
+  std::vector<double4> fgeo(m.n_points);
+  std::vector<double> fxyz(m.n_points * 3);
+  std::vector<short2> fmap(m.n_points);
+  m.map_h.assign(m.n_points, -1);
+  m.map_s.assign(m.n_points, -1);
+  std::vector<int32_t> cflux((size_t)d->n_cells * 6 * QF, INT32_MIN);
+  int max_group = -1;
+  std::string mesh_error;
+  for (int64_t f = 0; f < d->n_faces; ++f) {
+    int64_t hc = d->face_cells[f * 2], sc = d->face_cells[f * 2 + 1];
+    int sh = d->face_sides[f * 2], ss = d->face_sides[f * 2 + 1];
+    if (hc < 0 || hc >= d->n_cells || sh < 0 || sh > 5 || sc >= d->n_cells ||
+        (sc >= 0 && (ss < 0 || ss > 5)) || hc > INT32_MAX) {
+      return fail(h, MCFD_ERR_MESH, "bad face record " + std::to_string(f));
+    }
+    fcells[f] = make_int2((int)hc, (int)sc);
+    fgroup[f] = d->face_group ? d->face_group[f] : -1;
+    if (sc < 0) max_group = std::max(max_group, fgroup[f]);
+  }
+  m.n_groups = max_group + 1;
+#pragma omp parallel for schedule(static)
+  for (int64_t f = 0; f < d->n_faces; ++f) {
+    int64_t hc = d->face_cells[f * 2], sc = d->face_cells[f * 2 + 1];
+    int sh = d->face_sides[f * 2], ss = d->face_sides[f * 2 + 1];
+    double xn[12];
+    int hg[4][3];
+    for (int v = 0; v < 4; ++v) {
+      int hv = kHexFace[sh][v];
+      corner_grid(hv, Q, hg[v]);
+      for (int e = 0; e < 3; ++e) xn[v * 3 + e] = d->xyz[d->cell_nodes[hc * 8 + hv] * 3 + e];
+    }
+    double shift[3] = {0, 0, 0};
+    if (d->face_shift)
+      for (int e = 0; e < 3; ++e) shift[e] = d->face_shift[f * 3 + e];
+    // sharer corner matched to each holder face corner
+    int sg[4][3];
+    if (sc >= 0) {
+      for (int v = 0; v < 4; ++v) {
+        int64_t hid = d->cell_nodes[hc * 8 + kHexFace[sh][v]];
+        int best = -1;
+        double best_d = 1e300;
+        for (int w = 0; w < 4; ++w) {
+          int sv = kHexFace[ss][w];
+          int64_t sid = d->cell_nodes[sc * 8 + sv];
+          double dd = 0;
+          for (int e = 0; e < 3; ++e) {
+            double diff = d->xyz[sid * 3 + e] + shift[e] - d->xyz[hid * 3 + e];
+            dd += diff * diff;
+          }
+          if (sid == hid && !d->face_shift) dd = -1;
+          if (dd < best_d) { best_d = dd; best = sv; }
+        }
+        corner_grid(best, Q, sg[v]);
+      }
+    }
+    double scale = 0;
+    for (int e = 0; e < 12; ++e) scale = std::max(scale, std::fabs(xn[e]));
+    double tol = 1e-10 * (1 + scale);
+    for (int a = 0; a < Q; ++a)
+      for (int b = 0; b < Q; ++b) {
+        int fp = a * Q + b;
+        int64_t pt = f * QF + fp;
+        double x[3], ta[3], tb[3];
+        quad4_point(xn, xq[a], xq[b], x, ta, tb);
+        double nrm[3] = {ta[1] * tb[2] - ta[2] * tb[1], ta[2] * tb[0] - ta[0] * tb[2],
+                         ta[0] * tb[1] - ta[1] * tb[0]};
+        double area = std::sqrt(nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2]);
+        fgeo[pt] = make_double4(nrm[0] / area, nrm[1] / area, nrm[2] / area,
+                                wq[a] * wq[b] * area);
+        for (int e = 0; e < 3; ++e) fxyz[pt * 3 + e] = x[e];
+        int gi[3], node_h, node_s = -1;
+        for (int e = 0; e < 3; ++e)
+          gi[e] = hg[0][e] + a * (hg[1][e] - hg[0][e]) / (Q - 1) + b * (hg[3][e] - hg[0][e]) / (Q - 1);
+        node_h = (gi[0] * Q + gi[1]) * Q + gi[2];
+        if (sc >= 0) {
+          for (int e = 0; e < 3; ++e)
+            gi[e] = sg[0][e] + a * (sg[1][e] - sg[0][e]) / (Q - 1) + b * (sg[3][e] - sg[0][e]) / (Q - 1);
+          node_s = (gi[0] * Q + gi[1]) * Q + gi[2];
+        }
+        m.map_h[pt] = (int16_t)node_h;
+        m.map_s[pt] = (int16_t)node_s;
+        fmap[pt] = make_short2((short)node_h, (short)node_s);
+      }
+  }
+  // geometric check of every matched pair and flux-slot table
+  for (int64_t f = 0; f < d->n_faces && mesh_error.empty(); ++f) {
+    int64_t hc = d->face_cells[f * 2], sc = d->face_cells[f * 2 + 1];
+    int sh = d->face_sides[f * 2], ss = d->face_sides[f * 2 + 1];
+    for (int fp = 0; fp < QF; ++fp) {
+      int64_t pt = f * QF + fp;
+      int sides[2] = {sh, ss};
+      int64_t cells[2] = {hc, sc};
+      int nodes[2] = {m.map_h[pt], m.map_s[pt]};
+      for (int s = 0; s < 2; ++s) {
+        if (cells[s] < 0) continue;
+        int node = nodes[s];
+        int i = node / QF, j = (node / Q) % Q, k = node % Q;
+        int t;
+        switch (sides[s]) {
+          case 0: t = (k == 0) ? i * Q + j : -1; break;
+          case 5: t = (k == Q - 1) ? i * Q + j : -1; break;
+          case 1: t = (j == 0) ? i * Q + k : -1; break;
+          case 3: t = (j == Q - 1) ? i * Q + k : -1; break;
+          case 4: t = (i == 0) ? j * Q + k : -1; break;
+          default: t = (i == Q - 1) ? j * Q + k : -1; break;
+        }
+        if (t < 0) { mesh_error = "face node off its local face at face " + std::to_string(f); break; }
+        int32_t &slot = cflux[((size_t)cells[s] * 6 + sides[s]) * QF + t];
+        if (slot != INT32_MIN) { mesh_error = "cell face used twice at face " + std::to_string(f); break; }
+        if (pt > INT32_MAX) { mesh_error = "too many face points"; break; }
+        slot = s == 0 ? (int32_t)pt : ~(int32_t)pt;
+      }
+      if (!mesh_error.empty()) break;
+    }
+  }
+  if (!mesh_error.empty()) return fail(h, MCFD_ERR_MESH, mesh_error);
+  // verify matched positions: face point == holder node == sharer node (+shift)
+  int bad_match = 0;
+#pragma omp parallel for schedule(static)
+  for (int64_t f = 0; f < d->n_faces; ++f) {
+    int64_t hc = d->face_cells[f * 2], sc = d->face_cells[f * 2 + 1];
+    double xh[24], xs[24];
+    for (int v = 0; v < 8; ++v)
+      for (int e = 0; e < 3; ++e) {
+        xh[v * 3 + e] = d->xyz[d->cell_nodes[hc * 8 + v] * 3 + e];
+        if (sc >= 0) xs[v * 3 + e] = d->xyz[d->cell_nodes[sc * 8 + v] * 3 + e];
+      }
+    double shift[3] = {0, 0, 0};
+    if (d->face_shift)
+      for (int e = 0; e < 3; ++e) shift[e] = d->face_shift[f * 3 + e];
+    for (int fp = 0; fp < QF; ++fp) {
+      int64_t pt = f * QF + fp;
+      const double *x = &fxyz[pt * 3];
+      double scale = 1 + std::fabs(x[0]) + std::fabs(x[1]) + std::fabs(x[2]);
+      double p[3], J[9];
+      int node = m.map_h[pt];
+      hex8_point(xh, xq[node / QF], xq[(node / Q) % Q], xq[node % Q], p, J);
+      double e2 = 0;
+      for (int e = 0; e < 3; ++e) e2 += (p[e] - x[e]) * (p[e] - x[e]);
+      if (std::sqrt(e2) > 1e-10 * scale) bad_match = 1;
+      if (sc >= 0) {
+        node = m.map_s[pt];
+        hex8_point(xs, xq[node / QF], xq[(node / Q) % Q], xq[node % Q], p, J);
+        e2 = 0;
+        for (int e = 0; e < 3; ++e) e2 += (p[e] + shift[e] - x[e]) * (p[e] + shift[e] - x[e]);
+        if (std::sqrt(e2) > 1e-10 * scale) bad_match = 1;
+      }
+    }
+  }
+  if (bad_match) return fail(h, MCFD_ERR_MESH, "a face point matches no node of its cells");
+  // ---- upload
+  int rc;
+  if ((rc = upload(h, &m.cell_geo, geo))) return rc;
+  if ((rc = upload(h, &m.cell_rate, rate))) return rc;
+  if ((rc = upload(h, &m.cell_flux, cflux))) return rc;
+  if ((rc = upload(h, &m.face_cells, fcells))) return rc;
+  if ((rc = upload(h, &m.face_group, fgroup))) return rc;
+  if ((rc = upload(h, &m.face_geo, fgeo))) return rc;
+  if ((rc = upload(h, &m.face_xyz, fxyz))) return rc;
+  if ((rc = upload(h, &m.face_map, fmap))) return rc;
+  std::vector<double> dvec(dm, dm + Q * Q);
+  if ((rc = upload(h, &m.dmat, dvec))) return rc;
+  m.host_bcs.assign(std::max(m.n_groups, 1), BcDev{});
+  if ((rc = upload(h, &m.bcs, m.host_bcs))) return rc;
+  return MCFD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mcfd_abi_version(void) { return MCFD_ABI_VERSION; }
+
+const char *mcfd_last_error(const mcfd_handle *h) {
+  return h ? h->err.c_str() : g_create_error.c_str();
+}
+
+int mcfd_create(const mcfd_mesh_desc *mesh, const mcfd_options *options,
+                mcfd_handle **out) {
+  g_create_error.clear();
+  if (!mesh || !options || !out) return fail(nullptr, MCFD_ERR_ARGUMENT, "null argument");
+  *out = nullptr;
+  if (mesh->n_cells <= 0 || mesh->n_nodes <= 0 || !mesh->xyz || !mesh->cell_nodes ||
+      (mesh->n_faces > 0 && (!mesh->face_cells || !mesh->face_sides)))
+    return fail(nullptr, MCFD_ERR_ARGUMENT, "incomplete mesh description");
+  if (options->degree < 1 || options->degree > 3)
+    return fail(nullptr, MCFD_ERR_UNSUPPORTED, "degree must be 1, 2 or 3");
+  if (options->scheme != MCFD_DGSEM)
+    return fail(nullptr, MCFD_ERR_UNSUPPORTED, "unknown scheme");
+  if (options->riemann < MCFD_EXACT || options->riemann > MCFD_RUSANOV)
+    return fail(nullptr, MCFD_ERR_ARGUMENT, "unknown Riemann solver");
+  if (options->precision != MCFD_FP64)
+    return fail(nullptr, MCFD_ERR_UNSUPPORTED, "precision form not built");
+  int n_dev = 0;
+  if (cudaGetDeviceCount(&n_dev) != cudaSuccess || n_dev <= options->device || options->device < 0)
+    return fail(nullptr, MCFD_ERR_NO_DEVICE, "no CUDA device available");
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, options->device) != cudaSuccess || prop.major < 10)
+    return fail(nullptr, MCFD_ERR_NO_DEVICE, "device is not a Blackwell-class GPU");
+  mcfd_handle *h = new (std::nothrow) mcfd_handle();
+  if (!h) return fail(nullptr, MCFD_ERR_ARGUMENT, "out of host memory");
+  h->device = options->device;
+  h->opt.riemann = options->riemann;
+  h->opt.precision = options->precision;
+  h->opt.cfl = options->cfl;
+  int rc = MCFD_OK;
+  if (cudaSetDevice(h->device) != cudaSuccess) rc = fail(h, MCFD_ERR_CUDA, "cudaSetDevice failed");
+  if (!rc && cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+    rc = fail(h, MCFD_ERR_CUDA, "cudaStreamCreate failed");
+  h->own_stream = true;
+  if (!rc) rc = build_mesh(h, mesh, options->degree);
+  if (!rc) {
+    size_t col = sizeof(double) * h->mesh.column;
+    cudaError_t e = cudaMalloc(&h->buf.u, col);
+    if (e == cudaSuccess) e = cudaMalloc(&h->buf.u1, col);
+    if (e == cudaSuccess) e = cudaMalloc(&h->buf.u2, col);
+    if (e == cudaSuccess) e = cudaMalloc(&h->buf.res, col);
+    if (e == cudaSuccess) e = cudaMalloc(&h->buf.flux, sizeof(double) * mcfd::kK * std::max<int64_t>(h->mesh.n_points, 1));
+    if (e == cudaSuccess) e = cudaMalloc(&h->buf.state, sizeof(mcfd::DevState));
+    if (e == cudaSuccess) e = cudaMemset(h->buf.u, 0, col);
+    if (e == cudaSuccess) e = cudaMemset(h->buf.state, 0, sizeof(mcfd::DevState));
+    if (e != cudaSuccess) rc = cuda_fail(h, e, "device allocation");
+  }
+  if (rc) {
+    g_create_error = h->err;
+    release(h);
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return MCFD_OK;
+}
+
+int mcfd_destroy(mcfd_handle *h) {
+  if (!h) return MCFD_ERR_ARGUMENT;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  release(h);
+  delete h;
+  return MCFD_OK;
+}
+
+int64_t mcfd_column_size(const mcfd_handle *h) { return h ? h->mesh.column : -1; }
+
+int mcfd_set_bc(mcfd_handle *h, int32_t group, const mcfd_bc_state *s) {
+  if (!h || !s) return MCFD_ERR_ARGUMENT;
+  if (group < 0 || group >= h->mesh.n_groups)
+    return fail(h, MCFD_ERR_ARGUMENT, "boundary group out of range");
+  if (s->kind < MCFD_BC_NONE || s->kind > MCFD_BC_SMART ||
+      (s->program != MCFD_STATE_CONSTANT && s->program != MCFD_STATE_MOVING_SPLIT) ||
+      s->axis < 0 || s->axis > 2)
+    return fail(h, MCFD_ERR_ARGUMENT, "bad boundary description");
+  BcDev bc{};
+  bc.kind = s->kind;
+  bc.program = s->program;
+  bc.axis = s->axis;
+  bc.position = s->position;
+  bc.speed = s->speed;
+  for (int k = 0; k < 5; ++k) { bc.a[k] = s->a[k]; bc.b[k] = s->b[k]; }
+  h->mesh.host_bcs[group] = bc;
+  cudaSetDevice(h->device);
+  CUDA_TRY(h, cudaMemcpyAsync(h->mesh.bcs + group, &h->mesh.host_bcs[group], sizeof(BcDev),
+                              cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  return MCFD_OK;
+}
+
+int mcfd_set_time(mcfd_handle *h, double t) {
+  if (!h) return MCFD_ERR_ARGUMENT;
+  h->t_host = t;
+  return MCFD_OK;
+}
+
+static int copy_column(mcfd_handle *h, void *dst, const void *src, int64_t n,
+                       cudaMemcpyKind kind) {
+  if (!h || !dst || !src) return MCFD_ERR_ARGUMENT;
+  if (n != h->mesh.column) return fail(h, MCFD_ERR_ARGUMENT, "column size mismatch");
+  cudaSetDevice(h->device);
+  CUDA_TRY(h, cudaMemcpyAsync(dst, src, sizeof(double) * n, kind, h->stream));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  return MCFD_OK;
+}
+
+int mcfd_set_solution(mcfd_handle *h, const double *column, int64_t n) {
+  if (!h) return MCFD_ERR_ARGUMENT;
+  return copy_column(h, h->buf.u, column, n, cudaMemcpyHostToDevice);
+}
+
+int mcfd_get_solution(mcfd_handle *h, double *column, int64_t n) {
+  if (!h) return MCFD_ERR_ARGUMENT;
+  return copy_column(h, column, h->buf.u, n, cudaMemcpyDeviceToHost);
+}
+
+int mcfd_set_solution_device(mcfd_handle *h, const double *d_column, int64_t n) {
+  if (!h) return MCFD_ERR_ARGUMENT;
+  return copy_column(h, h->buf.u, d_column, n, cudaMemcpyDeviceToDevice);
+}
+
+int mcfd_get_solution_device(mcfd_handle *h, double *d_column, int64_t n) {
+  if (!h) return MCFD_ERR_ARGUMENT;
+  return copy_column(h, d_column, h->buf.u, n, cudaMemcpyDeviceToDevice);
+}
+
+static int residual_into(mcfd_handle *h, double *dst, int64_t n, cudaMemcpyKind kind) {
+  if (!h || !dst) return MCFD_ERR_ARGUMENT;
+  if (n != h->mesh.column) return fail(h, MCFD_ERR_ARGUMENT, "column size mismatch");
+  cudaSetDevice(h->device);
+  h->launches += mcfd::launch_set_state(h, h->t_host, 0.0, 0.0, 0.0, 1);
+  h->launches += mcfd::launch_face_flux(h, h->buf.u, 0.0);
+  h->launches += mcfd::launch_cell_update(h, mcfd::kStageResidual, h->buf.u, nullptr, h->buf.res, 0);
+  CUDA_TRY(h, cudaGetLastError());
+  CUDA_TRY(h, cudaMemcpyAsync(dst, h->buf.res, sizeof(double) * n, kind, h->stream));
+  return check_status(h);
+}
+
+int mcfd_residual(mcfd_handle *h, double *residual, int64_t n) {
+  return residual_into(h, residual, n, cudaMemcpyDeviceToHost);
+}
+
+int mcfd_residual_device(mcfd_handle *h, double *d_residual, int64_t n) {
+  return residual_into(h, d_residual, n, cudaMemcpyDeviceToDevice);
+}
+
+int mcfd_time_step(mcfd_handle *h, double dt_guess, int32_t rk_order, double *dt) {
+  if (!h || !dt) return MCFD_ERR_ARGUMENT;
+  cudaSetDevice(h->device);
+  double cfl = h->opt.cfl > 0 ? h->opt.cfl : cfl_table(rk_order, h->mesh.p);
+  h->launches += mcfd::launch_set_state(h, h->t_host, 0.0, dt_guess, cfl, 1);
+  h->launches += mcfd::launch_dt(h, h->buf.u);
+  CUDA_TRY(h, cudaGetLastError());
+  mcfd::DevState st;
+  CUDA_TRY(h, cudaMemcpyAsync(&st, h->buf.state, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  *dt = st.dt;
+  return MCFD_OK;
+}
+
+int mcfd_rk_step(mcfd_handle *h, double t, double dt, int32_t order) {
+  if (!h || order < 1 || order > 3) return h ? fail(h, MCFD_ERR_ARGUMENT, "order must be 1, 2 or 3") : MCFD_ERR_ARGUMENT;
+  cudaSetDevice(h->device);
+  h->launches += mcfd::launch_set_state(h, t, dt, dt, 0.0, 0);
+  h->launches += mcfd::launch_rk_stage_sequence(h, order);
+  CUDA_TRY(h, cudaGetLastError());
+  h->t_host = t + dt;
+  return check_status(h);
+}
+
+int mcfd_advance(mcfd_handle *h, int32_t n_steps, double dt_guess, int32_t rk_order, double *t) {
+  if (!h || !t || n_steps < 0 || rk_order < 1 || rk_order > 3) return MCFD_ERR_ARGUMENT;
+  cudaSetDevice(h->device);
+  double cfl = h->opt.cfl > 0 ? h->opt.cfl : cfl_table(rk_order, h->mesh.p);
+  h->launches += mcfd::launch_set_state(h, *t, 0.0, dt_guess, cfl, 1);
+  CUDA_TRY(h, cudaGetLastError());
+  if (!h->step_graph || h->step_graph_order != rk_order) {
+    if (h->step_graph) { cudaGraphExecDestroy(h->step_graph); h->step_graph = nullptr; }
+    cudaGraph_t graph;
+    CUDA_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    int n = mcfd::launch_dt(h, h->buf.u);
+    n += mcfd::launch_rk_stage_sequence(h, rk_order);
+    cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&h->step_graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaGraphInstantiate");
+    h->step_graph_order = rk_order;
+    h->step_graph_kernels = n;
+  }
+  for (int s = 0; s < n_steps; ++s) {
+    CUDA_TRY(h, cudaGraphLaunch(h->step_graph, h->stream));
+    h->launches += h->step_graph_kernels;
+  }
+  mcfd::DevState st;
+  CUDA_TRY(h, cudaMemcpyAsync(&st, h->buf.state, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+  int rc = check_status(h);
+  *t = st.t;
+  h->t_host = st.t;
+  return rc;
+}
+
+int mcfd_set_stream(mcfd_handle *h, void *cuda_stream) {
+  if (!h) return MCFD_ERR_ARGUMENT;
+  cudaSetDevice(h->device);
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  if (cuda_stream) {
+    if (h->own_stream) cudaStreamDestroy(h->stream);
+    h->stream = (cudaStream_t)cuda_stream;
+    h->own_stream = false;
+  } else if (!h->own_stream) {
+    CUDA_TRY(h, cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    h->own_stream = true;
+  }
+  return MCFD_OK;
+}
+
+int mcfd_synchronize(mcfd_handle *h) {
+  if (!h) return MCFD_ERR_ARGUMENT;
+  cudaSetDevice(h->device);
+  return check_status(h);
+}
+
+int mcfd_face_node_maps(const mcfd_handle *h, int16_t *holder, int16_t *sharer) {
+  if (!h || !holder || !sharer) return MCFD_ERR_ARGUMENT;
+  std::memcpy(holder, h->mesh.map_h.data(), sizeof(int16_t) * h->mesh.map_h.size());
+  std::memcpy(sharer, h->mesh.map_s.data(), sizeof(int16_t) * h->mesh.map_s.size());
+  return MCFD_OK;
+}
+
+int64_t mcfd_launch_count(const mcfd_handle *h) { return h ? h->launches : -1; }
+
+int mcfd_kernel_times(mcfd_handle *h, int32_t reps, double *out_ms) {
+  if (!h || !out_ms || reps < 1) return MCFD_ERR_ARGUMENT;
+  cudaSetDevice(h->device);
+  cudaEvent_t e0, e1;
+  CUDA_TRY(h, cudaEventCreate(&e0));
+  CUDA_TRY(h, cudaEventCreate(&e1));
+  auto &b = h->buf;
+  double cfl = h->opt.cfl > 0 ? h->opt.cfl : cfl_table(3, h->mesh.p);
+  h->launches += mcfd::launch_set_state(h, h->t_host, 0.0, 1e300, cfl, 1);
+  float ms = 0;
+  // dt reduction (reads u)
+  CUDA_TRY(h, cudaEventRecord(e0, h->stream));
+  for (int r = 0; r < reps; ++r) h->launches += mcfd::launch_dt(h, b.u);
+  CUDA_TRY(h, cudaEventRecord(e1, h->stream));
+  CUDA_TRY(h, cudaEventSynchronize(e1));
+  CUDA_TRY(h, cudaEventElapsedTime(&ms, e0, e1));
+  out_ms[0] = ms / reps;
+  // face fluxes of the current solution
+  CUDA_TRY(h, cudaEventRecord(e0, h->stream));
+  for (int r = 0; r < reps; ++r) h->launches += mcfd::launch_face_flux(h, b.u, 0.0);
+  CUDA_TRY(h, cudaEventRecord(e1, h->stream));
+  CUDA_TRY(h, cudaEventSynchronize(e1));
+  CUDA_TRY(h, cudaEventElapsedTime(&ms, e0, e1));
+  out_ms[1] = ms / reps;
+  // cell update in the middle-stage form (reads u_in and u0, writes u_out)
+  CUDA_TRY(h, cudaEventRecord(e0, h->stream));
+  for (int r = 0; r < reps; ++r)
+    h->launches += mcfd::launch_cell_update(h, mcfd::kStageRk3Mid, b.u, b.u, b.u2, 0);
+  CUDA_TRY(h, cudaEventRecord(e1, h->stream));
+  CUDA_TRY(h, cudaEventSynchronize(e1));
+  CUDA_TRY(h, cudaEventElapsedTime(&ms, e0, e1));
+  out_ms[2] = ms / reps;
+  // one whole step on a copy of the solution (u is restored afterwards)
+  CUDA_TRY(h, cudaMemcpyAsync(b.res, b.u, sizeof(double) * h->mesh.column, cudaMemcpyDeviceToDevice, h->stream));
+  CUDA_TRY(h, cudaEventRecord(e0, h->stream));
+  for (int r = 0; r < reps; ++r) {
+    h->launches += mcfd::launch_dt(h, b.u);
+    h->launches += mcfd::launch_rk_stage_sequence(h, 3);
+  }
+  CUDA_TRY(h, cudaEventRecord(e1, h->stream));
+  CUDA_TRY(h, cudaEventSynchronize(e1));
+  CUDA_TRY(h, cudaEventElapsedTime(&ms, e0, e1));
+  out_ms[3] = ms / reps;
+  CUDA_TRY(h, cudaMemcpyAsync(b.u, b.res, sizeof(double) * h->mesh.column, cudaMemcpyDeviceToDevice, h->stream));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return check_status(h);
+}
+
+}  // extern "C"

@@ -1,0 +1,375 @@
+// DGSEM (dg::Lobatto, kLocal = false) residual and SSP-RK stages on sm_103a,
+// plain FP64 form.
+//
+// Per RK stage two kernels run over device-resident data:
+//   face_flux_kernel   one thread per face point: gathers the holder and
+//                      sharer node states, evaluates the rotated Riemann (or
+//                      boundary) flux in the global frame, scales it by the
+//                      face weight and writes it to a face-point flux buffer.
+//                      (spatial/dg/lobatto.hpp:171-302)
+//   cell_update_kernel one thread per cell node: contravariant volume flux
+//                      F * (w J^-1) to shared memory, sum-factorised GLL
+//                      differentiation (equal to the reference's dense
+//                      F * J^-1 grad(phi) product, lobatto.hpp:161-170),
+//                      gather of the <= 3 face fluxes this node lifts
+//                      (atomic-free, deterministic), lumped mass divide
+//                      (lobatto.hpp:143-158) and the RK stage combination
+//                      (temporal/rk.hpp:16-49), written in one pass.
+// The time step (spatial/fem.hpp:417-435) is a max-reduction of
+// max_speed / length over all nodes plus a one-thread finalisation; dt and t
+// stay in device memory.
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <cstdint>
+
+#include "euler.cuh"
+#include "handle.hpp"
+
+namespace mcfd {
+namespace {
+
+template <int Q>
+struct CellCfg {
+  static constexpr int kN = Q * Q * Q;
+  static constexpr int kCells = (Q == 4) ? 4 : (Q == 3 ? 9 : 32);
+  static constexpr int kThreads = kCells * kN;
+};
+
+struct FaceArgs {
+  const double *u;
+  const int2 *face_cells;
+  const int32_t *face_group;
+  const double4 *face_geo;
+  const double *face_xyz;
+  const short2 *face_map;
+  const BcDev *bcs;
+  double *flux;
+  DevState *state;
+  double stage_c;
+  int64_t n_points;
+  int n_groups;
+};
+
+struct CellArgs {
+  const double *u_in;
+  const double *u0;
+  double *u_out;
+  const double *cell_geo;
+  const int32_t *cell_flux;
+  const double *flux;
+  const double *dmat;
+  DevState *state;
+  int64_t n_cells;
+  int advance_time;
+};
+
+__device__ __forceinline__ void given_value(const BcDev &bc, const double *x,
+                                            double t, double *g) {
+  const double *src = bc.a;
+  if (bc.program == 1 && (x[bc.axis] - bc.speed * t) >= bc.position) src = bc.b;
+#pragma unroll
+  for (int k = 0; k < kK; ++k) g[k] = src[k];
+}
+
+template <int Q, int R>
+__global__ void __launch_bounds__(256) face_flux_kernel(FaceArgs a) {
+  constexpr int QF = Q * Q, KN = kK * Q * Q * Q;
+  int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= a.n_points) return;
+  int64_t f = gid / QF;
+  int2 cells = a.face_cells[f];
+  short2 map = a.face_map[gid];
+  double4 g = a.face_geo[gid];
+  double n[3] = {g.x, g.y, g.z};
+  const double *uh = a.u + (int64_t)cells.x * KN + map.x * kK;
+  Prim l = cons_to_prim(uh[0], uh[1], uh[2], uh[3], uh[4]);
+  double out[kK];
+  bool not_converged = false;
+  if (cells.y >= 0) {
+    const double *us = a.u + (int64_t)cells.y * KN + map.y * kK;
+    Prim r = cons_to_prim(us[0], us[1], us[2], us[3], us[4]);
+    flux_upwind<R>(l, r, n, out, &not_converged);
+  } else {
+    int grp = a.face_group[f];
+    if (grp >= 0 && grp < a.n_groups && a.bcs[grp].kind != kBcNone) {
+      const BcDev &bc = a.bcs[grp];
+      double t = a.state->t + a.stage_c * a.state->dt;
+      double given[kK];
+      given_value(bc, a.face_xyz + gid * 3, t, given);
+      flux_boundary<R>(bc.kind, l, given, n, out, &not_converged);
+    } else {
+#pragma unroll
+      for (int k = 0; k < kK; ++k) out[k] = 0;
+    }
+  }
+  if (not_converged) atomicOr(&a.state->status, (unsigned)kStatusNotConverged);
+  double *dst = a.flux + gid * kK;
+#pragma unroll
+  for (int k = 0; k < kK; ++k) dst[k] = out[k] * g.w;
+}
+
+template <int Q, int STAGE>
+__global__ void __launch_bounds__(CellCfg<Q>::kThreads)
+cell_update_kernel(CellArgs a) {
+  constexpr int N = Q * Q * Q, QF = Q * Q, KN = kK * N;
+  constexpr int CPB = CellCfg<Q>::kCells;
+  __shared__ double s_ft[CPB][15][N];
+  __shared__ double s_d[Q * Q];
+  const int tid = threadIdx.x;
+  if (tid < Q * Q) s_d[tid] = a.dmat[tid];
+  const int lc = tid / N, q = tid - lc * N;
+  const int64_t c = (int64_t)blockIdx.x * CPB + lc;
+  const bool active = c < a.n_cells;
+  double uq[kK];
+  if (active) {
+    const double *up = a.u_in + c * KN + q * kK;
+#pragma unroll
+    for (int k = 0; k < kK; ++k) uq[k] = up[k];
+    const double *geo = a.cell_geo + (c * N + q) * 10;
+    double A[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) A[e] = geo[e];
+    Prim w = cons_to_prim(uq[0], uq[1], uq[2], uq[3], uq[4]);
+    // Contravariant flux Ft[:, e] = sum_d F[:, d] A[d][e], F = GetFluxMatrix
+    // (types.hpp:322-333).  With V_e = sum_d u_d A[d][e]:
+    //   Ft[0][e] = rho V_e, Ft[1+x][e] = m_x V_e + p A[x][e], Ft[4][e] = (E+p) V_e
+    // A clamped state (zero primitives) keeps only the mass row m . A.
+    double ft[15];
+    if (w.rho != 0) {
+#pragma unroll
+      for (int e = 0; e < 3; ++e) {
+        double ve = w.u * A[0 * 3 + e] + w.v * A[1 * 3 + e] + w.w * A[2 * 3 + e];
+        ft[0 * 3 + e] = w.rho * ve;
+        ft[1 * 3 + e] = uq[1] * ve + w.p * A[0 * 3 + e];
+        ft[2 * 3 + e] = uq[2] * ve + w.p * A[1 * 3 + e];
+        ft[3 * 3 + e] = uq[3] * ve + w.p * A[2 * 3 + e];
+        ft[4 * 3 + e] = (uq[4] + w.p) * ve;
+      }
+    } else {
+#pragma unroll
+      for (int e = 0; e < 3; ++e) {
+        ft[e] = uq[1] * A[0 * 3 + e] + uq[2] * A[1 * 3 + e] + uq[3] * A[2 * 3 + e];
+#pragma unroll
+        for (int r = 1; r < kK; ++r) ft[r * 3 + e] = 0;
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < 15; ++r) s_ft[lc][r][q] = ft[r];
+  }
+  __syncthreads();
+  if (!active) return;
+  const int i = q / QF, j = (q / Q) % Q, k = q % Q;
+  double res[kK];
+#pragma unroll
+  for (int r = 0; r < kK; ++r) {
+    double s = 0;
+#pragma unroll
+    for (int m = 0; m < Q; ++m) {
+      s += s_ft[lc][r * 3 + 0][(m * Q + j) * Q + k] * s_d[m * Q + i];
+      s += s_ft[lc][r * 3 + 1][(i * Q + m) * Q + k] * s_d[m * Q + j];
+      s += s_ft[lc][r * 3 + 2][(i * Q + j) * Q + m] * s_d[m * Q + k];
+    }
+    res[r] = s;
+  }
+  // Surface terms: holder -= flux, sharer += flux (lobatto.hpp:184-189).
+  const int32_t *cf = a.cell_flux + c * 6 * QF;
+  auto lift = [&](int side, int t) {
+    int32_t v = cf[side * QF + t];
+    if (v == INT32_MIN) return;
+    const double *fl = a.flux + (int64_t)(v >= 0 ? v : ~v) * kK;
+    if (v >= 0) {
+#pragma unroll
+      for (int r = 0; r < kK; ++r) res[r] -= fl[r];
+    } else {
+#pragma unroll
+      for (int r = 0; r < kK; ++r) res[r] += fl[r];
+    }
+  };
+  if (k == 0) lift(0, i * Q + j);
+  if (k == Q - 1) lift(5, i * Q + j);
+  if (j == 0) lift(1, i * Q + k);
+  if (j == Q - 1) lift(3, i * Q + k);
+  if (i == 0) lift(4, j * Q + k);
+  if (i == Q - 1) lift(2, j * Q + k);
+  const double inv_w = a.cell_geo[(c * N + q) * 10 + 9];
+  double *out = a.u_out + c * KN + q * kK;
+  bool bad = false;
+  if (STAGE == kStageResidual) {
+#pragma unroll
+    for (int r = 0; r < kK; ++r) {
+      double v = res[r] * inv_w;
+      bad |= !isfinite(v);
+      out[r] = v;
+    }
+  } else {
+    const double dt = a.state->dt;
+#pragma unroll
+    for (int r = 0; r < kK; ++r) {
+      double next = uq[r] + (res[r] * inv_w) * dt;
+      double v;
+      if (STAGE == kStageEuler) {
+        v = next;
+      } else if (STAGE == kStageRk2Last) {
+        v = (next + a.u0[c * KN + q * kK + r]) * 0.5;
+      } else if (STAGE == kStageRk3Mid) {
+        v = (a.u0[c * KN + q * kK + r] * 3 + next) * 0.25;
+      } else {  // kStageRk3Last; division by 3 as a multiplication
+        v = (next * 2 + a.u0[c * KN + q * kK + r]) * (1.0 / 3.0);
+      }
+      bad |= !isfinite(v);
+      out[r] = v;
+    }
+  }
+  if (bad) atomicOr(&a.state->status, (unsigned)kStatusNonFinite);
+  if (a.advance_time && blockIdx.x == 0 && tid == 0) a.state->t += a.state->dt;
+}
+
+// dt: max over nodes of max(1e-5, max_speed) / length, as the bit pattern of
+// a positive double (monotone as an unsigned integer).
+template <int Q>
+__global__ void __launch_bounds__(256)
+dt_reduce_kernel(const double *u, const double *cell_rate, int64_t n_nodes,
+                 DevState *state) {
+  constexpr int N = Q * Q * Q;
+  int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double rate = 0;
+  if (gid < n_nodes) {
+    const double *p = u + gid * kK;
+    Prim w = cons_to_prim(p[0], p[1], p[2], p[3], p[4]);
+    double c = sound_speed(w);
+    double speed = c + sqrt(w.u * w.u + w.v * w.v + w.w * w.w);
+    rate = fmax(speed, 1e-5) * cell_rate[gid / N];
+  }
+  for (int o = 16; o > 0; o >>= 1) rate = fmax(rate, __shfl_xor_sync(0xffffffffu, rate, o));
+  if ((threadIdx.x & 31) == 0 && rate > 0)
+    atomicMax(&state->max_rate_bits, (unsigned long long)__double_as_longlong(rate));
+}
+
+__global__ void dt_finalize_kernel(DevState *state) {
+  double max_rate = __longlong_as_double((long long)state->max_rate_bits);
+  double min_dt = max_rate > 0 ? 1.0 / max_rate : 1.e+100;
+  double dt = state->cfl * min_dt;
+  state->dt = fmin(dt, state->dt_guess);
+  state->max_rate_bits = 0ull;
+}
+
+__global__ void set_state_kernel(DevState *state, double t, double dt,
+                                 double dt_guess, double cfl, int reset_rate) {
+  state->t = t;
+  state->dt = dt;
+  state->dt_guess = dt_guess;
+  state->cfl = cfl;
+  if (reset_rate) state->max_rate_bits = 0ull;
+}
+
+template <int Q, int R>
+void face_launch(mcfd_handle *h, const FaceArgs &fa) {
+  int64_t blocks = (fa.n_points + 255) / 256;
+  face_flux_kernel<Q, R><<<(unsigned)blocks, 256, 0, h->stream>>>(fa);
+}
+
+template <int Q>
+void face_dispatch_r(mcfd_handle *h, const FaceArgs &fa) {
+  switch (h->opt.riemann) {
+    case kExact: face_launch<Q, kExact>(h, fa); break;
+    case kHllc: face_launch<Q, kHllc>(h, fa); break;
+    case kAusm: face_launch<Q, kAusm>(h, fa); break;
+    case kRoe: face_launch<Q, kRoe>(h, fa); break;
+    default: face_launch<Q, kRusanov>(h, fa); break;
+  }
+}
+
+template <int Q, int S>
+void cell_launch(mcfd_handle *h, const CellArgs &ca) {
+  constexpr int CPB = CellCfg<Q>::kCells;
+  int64_t blocks = (ca.n_cells + CPB - 1) / CPB;
+  cell_update_kernel<Q, S><<<(unsigned)blocks, CellCfg<Q>::kThreads, 0, h->stream>>>(ca);
+}
+
+template <int Q>
+void cell_dispatch_s(mcfd_handle *h, int stage, const CellArgs &ca) {
+  switch (stage) {
+    case kStageEuler: cell_launch<Q, kStageEuler>(h, ca); break;
+    case kStageRk2Last: cell_launch<Q, kStageRk2Last>(h, ca); break;
+    case kStageRk3Mid: cell_launch<Q, kStageRk3Mid>(h, ca); break;
+    case kStageRk3Last: cell_launch<Q, kStageRk3Last>(h, ca); break;
+    default: cell_launch<Q, kStageResidual>(h, ca); break;
+  }
+}
+
+}  // namespace
+
+int launch_set_state(mcfd_handle *h, double t, double dt, double dt_guess,
+                     double cfl, int reset_rate) {
+  set_state_kernel<<<1, 1, 0, h->stream>>>(h->buf.state, t, dt, dt_guess, cfl,
+                                           reset_rate);
+  return 1;
+}
+
+int launch_face_flux(mcfd_handle *h, const double *u, double stage_c) {
+  const Mesh &m = h->mesh;
+  FaceArgs fa{u, m.face_cells, m.face_group, m.face_geo, m.face_xyz,
+              m.face_map, m.bcs, h->buf.flux, h->buf.state, stage_c,
+              m.n_points, m.n_groups};
+  if (m.n_points == 0) return 0;
+  switch (m.q) {
+    case 2: face_dispatch_r<2>(h, fa); break;
+    case 3: face_dispatch_r<3>(h, fa); break;
+    default: face_dispatch_r<4>(h, fa); break;
+  }
+  return 1;
+}
+
+int launch_cell_update(mcfd_handle *h, int stage, const double *u_in,
+                       const double *u0, double *u_out, int advance_time) {
+  const Mesh &m = h->mesh;
+  CellArgs ca{u_in, u0, u_out, m.cell_geo, m.cell_flux, h->buf.flux, m.dmat,
+              h->buf.state, m.n_cells, advance_time};
+  switch (m.q) {
+    case 2: cell_dispatch_s<2>(h, stage, ca); break;
+    case 3: cell_dispatch_s<3>(h, stage, ca); break;
+    default: cell_dispatch_s<4>(h, stage, ca); break;
+  }
+  return 1;
+}
+
+int launch_dt(mcfd_handle *h, const double *u) {
+  const Mesh &m = h->mesh;
+  int64_t nodes = m.n_cells * m.n;
+  unsigned blocks = (unsigned)((nodes + 255) / 256);
+  switch (m.q) {
+    case 2: dt_reduce_kernel<2><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state); break;
+    case 3: dt_reduce_kernel<3><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state); break;
+    default: dt_reduce_kernel<4><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state); break;
+  }
+  dt_finalize_kernel<<<1, 1, 0, h->stream>>>(h->buf.state);
+  return 2;
+}
+
+// The stages of RungeKutta<order>::Update with the result left in buf.u.
+// Stage times: t, t + dt, t + dt/2 (rk.hpp:34-42).  The last stage also
+// advances the device time by dt.
+int launch_rk_stage_sequence(mcfd_handle *h, int order) {
+  Buffers &b = h->buf;
+  int n = 0;
+  if (order == 1) {
+    n += launch_face_flux(h, b.u, 0.0);
+    n += launch_cell_update(h, kStageEuler, b.u, nullptr, b.u, 1);
+  } else if (order == 2) {
+    n += launch_face_flux(h, b.u, 0.0);
+    n += launch_cell_update(h, kStageEuler, b.u, nullptr, b.u1, 0);
+    n += launch_face_flux(h, b.u1, 1.0);
+    n += launch_cell_update(h, kStageRk2Last, b.u1, b.u, b.u, 1);
+  } else {
+    n += launch_face_flux(h, b.u, 0.0);
+    n += launch_cell_update(h, kStageEuler, b.u, nullptr, b.u1, 0);
+    n += launch_face_flux(h, b.u1, 1.0);
+    n += launch_cell_update(h, kStageRk3Mid, b.u1, b.u, b.u2, 0);
+    n += launch_face_flux(h, b.u2, 0.5);
+    n += launch_cell_update(h, kStageRk3Last, b.u2, b.u, b.u, 1);
+  }
+  return n;
+}
+
+}  // namespace mcfd

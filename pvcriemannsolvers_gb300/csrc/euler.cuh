@@ -1,0 +1,526 @@
+// Ideal-gas Euler physics for the device kernels (and host helpers).
+//
+// All functions work in the GLOBAL frame with the unit face normal only.  The
+// reference rotates momenta into an orthonormal frame (n, t, b), calls a 1D
+// solver with passive tangential velocities and rotates the flux back
+// (include/mini/riemann/rotated/euler.hpp:68-88, 117-159).  Every solver used
+// here is invariant under rotations about n, so with u_t = u - (u.n) n the
+// rotated flux equals
+//     F = F_1D[mass, normal momentum, energy] + (tangential part carried by
+//         the upwind/star state)
+// evaluated directly in global coordinates.  This needs 3 normal components
+// per face point instead of a 9-entry frame and skips both rotations; the
+// results agree with the rotated form to rounding.
+//
+// Sources restated (pvcStillInGradSchool/pvcRiemannSolvers):
+//   gas                include/mini/riemann/euler/types.hpp:186-334
+//   Exact              include/mini/riemann/euler/exact.hpp:44-320
+//   HLLC               include/mini/riemann/euler/hllc.hpp:30-109
+//   AUSM               include/mini/riemann/euler/ausm.hpp:146-187
+//   Roe, Rusanov       python/riemann.py:405-476 (1D), here in 3D
+//   boundary fluxes    include/mini/riemann/rotated/euler.hpp:144-318
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+
+#ifdef __CUDACC__
+#define MCFD_HD __host__ __device__ __forceinline__
+#else
+#define MCFD_HD inline
+#endif
+
+namespace mcfd {
+
+constexpr int kK = 5;
+constexpr double kGamma = 1.4;
+constexpr double kGasR = 287.05;
+constexpr double kGm1 = kGamma - 1.0;             // GammaMinusOne
+constexpr double kGp1 = kGamma + 1.0;             // GammaPlusOne
+constexpr double kOneOverGm1 = 1.0 / kGm1;        // OneOverGammaMinusOne
+constexpr double kGm1Under2 = 2 / kGm1;           // GammaMinusOneUnderTwo
+constexpr double kGm1Over2 = kGm1 / 2;            // GammaMinusOneOverTwo
+constexpr double kGp1Over2 = kGp1 / 2;            // GammaPlusOneOverTwo
+constexpr double kGp1Over4 = kGp1 / 4;            // GammaPlusOneOverFour
+constexpr double kOneOverGamma = 1 / kGamma;      // OneOverGamma
+constexpr double kGammaOverGm1 = kGamma / kGm1;   // GammaOverGammaMinusOne
+
+enum Riemann { kExact = 0, kHllc = 1, kAusm = 2, kRoe = 3, kRusanov = 4 };
+enum BcKind {
+  kBcNone = 0, kBcInviscidWall = 1, kBcSupersonicInlet = 2,
+  kBcSupersonicOutlet = 3, kBcSubsonicInlet = 4, kBcSubsonicOutlet = 5,
+  kBcSmart = 6
+};
+
+// Status bits raised by kernels (read back by the host).
+enum StatusBits : unsigned {
+  kStatusNonFinite = 1u,
+  kStatusNotConverged = 2u,
+  kStatusTimeout = 4u,
+};
+
+struct Prim {
+  double rho, u, v, w, p;
+};
+
+// ConservativeToPrimitive with SetZeroIfNegative (types.hpp:194-202,288-301):
+// a negative density or (first) energy, or a negative pressure after the
+// conversion, zeroes the whole primitive state.  The three velocity
+// divisions share one reciprocal.
+MCFD_HD Prim cons_to_prim(double r, double mx, double my, double mz,
+                          double e) {
+  Prim w{r, mx, my, mz, e};
+  if (r < 0 || e < 0) return Prim{0, 0, 0, 0, 0};
+  if (r != 0) {
+    double inv = 1.0 / r;
+    w.u = mx * inv;
+    w.v = my * inv;
+    w.w = mz * inv;
+    double ke = 0.5 * (w.u * w.u + w.v * w.v + w.w * w.w);
+    w.p = (e - r * ke) * kGm1;
+    if (w.p < 0) return Prim{0, 0, 0, 0, 0};
+  }
+  return w;
+}
+
+MCFD_HD double kinetic(const Prim &w) {
+  return 0.5 * (w.u * w.u + w.v * w.v + w.w * w.w);
+}
+
+// GetSpeedOfSound(rho, p) (types.hpp:252-254).
+MCFD_HD double sound_speed(const Prim &w) {
+  return (w.rho > 0 && w.p > 0) ? sqrt(kGamma * w.p / w.rho) : 0.0;
+}
+
+// Total energy of a primitive state (PrimitiveToConservative, types.hpp:302-311).
+MCFD_HD double prim_energy(const Prim &w) {
+  return w.p * kOneOverGm1 + w.rho * kinetic(w);
+}
+
+// Physical flux through unit normal n, from a primitive state:
+// the global-frame form of PrimitiveToFlux in the normal frame.
+MCFD_HD void normal_flux(const Prim &w, double e, const double *n, double un,
+                         double *f) {
+  f[0] = w.rho * un;
+  f[1] = w.rho * w.u * un + w.p * n[0];
+  f[2] = w.rho * w.v * un + w.p * n[1];
+  f[3] = w.rho * w.w * un + w.p * n[2];
+  f[4] = (e + w.p) * un;
+}
+
+// ---------------------------------------------------------------- Rusanov
+// Local Lax-Friedrichs (python/riemann.py:457-476): average flux minus
+// lambda_max / 2 * (U_R - U_L), lambda_max = max(|u_n| + a) over both sides.
+MCFD_HD void flux_rusanov(const Prim &l, const Prim &r, const double *n,
+                          double *f) {
+  double unl = l.u * n[0] + l.v * n[1] + l.w * n[2];
+  double unr = r.u * n[0] + r.v * n[1] + r.w * n[2];
+  double el = prim_energy(l), er = prim_energy(r);
+  double fl[kK], fr[kK];
+  normal_flux(l, el, n, unl, fl);
+  normal_flux(r, er, n, unr, fr);
+  double lam = fmax(fabs(unl) + sound_speed(l), fabs(unr) + sound_speed(r));
+  double h = 0.5 * lam;
+  f[0] = 0.5 * (fr[0] + fl[0]) - h * (r.rho - l.rho);
+  f[1] = 0.5 * (fr[1] + fl[1]) - h * (r.rho * r.u - l.rho * l.u);
+  f[2] = 0.5 * (fr[2] + fl[2]) - h * (r.rho * r.v - l.rho * l.v);
+  f[3] = 0.5 * (fr[3] + fl[3]) - h * (r.rho * r.w - l.rho * l.w);
+  f[4] = 0.5 * (fr[4] + fl[4]) - h * (er - el);
+}
+
+// ---------------------------------------------------------------- HLLC
+// hllc.hpp:30-109 with the star state's tangential velocity carried from
+// the side it is built on.
+MCFD_HD double hllc_q(double p_estimate, double p_k) {
+  if (p_estimate <= p_k) return 1.0;
+  double temp = 1 + kGp1Over2 * (p_estimate / p_k - 1) / kGamma;
+  return sqrt(temp);
+}
+
+MCFD_HD void hllc_star(const Prim &s, double un, double e, const double *n,
+                       double wave_k, double wave_star, double *f) {
+  normal_flux(s, e, n, un, f);
+  double temp = s.rho * (wave_k - un) / (wave_k - wave_star);
+  double es = e / s.rho + (wave_star - un) *
+      (wave_star + s.p / (s.rho * (wave_k - un)));
+  es *= temp;
+  // star momentum = temp * (wave_star n + u_t), u_t = u - un n
+  double dm = temp * (wave_star - un);
+  double sm0 = temp * s.u + dm * n[0];
+  double sm1 = temp * s.v + dm * n[1];
+  double sm2 = temp * s.w + dm * n[2];
+  f[0] += wave_k * (temp - s.rho);
+  f[1] += wave_k * (sm0 - s.rho * s.u);
+  f[2] += wave_k * (sm1 - s.rho * s.v);
+  f[3] += wave_k * (sm2 - s.rho * s.w);
+  f[4] += wave_k * (es - e);
+}
+
+MCFD_HD void flux_hllc(const Prim &l, const Prim &r, const double *n,
+                       double *f) {
+  double unl = l.u * n[0] + l.v * n[1] + l.w * n[2];
+  double unr = r.u * n[0] + r.v * n[1] + r.w * n[2];
+  double rho_average = (l.rho + r.rho) / 2;
+  double a_left = sound_speed(l), a_right = sound_speed(r);
+  double a_average = (a_left + a_right) / 2;
+  double p_pvrs = (l.p + r.p - (unr - unl) * rho_average * a_average) / 2;
+  double p_estimate = fmax(0.0, p_pvrs);
+  double wave_left = unl - a_left * hllc_q(p_estimate, l.p);
+  double wave_right = unr + a_right * hllc_q(p_estimate, r.p);
+  double wave_star = (r.p - l.p + l.rho * unl * (wave_left - unl) -
+                      r.rho * unr * (wave_right - unr)) /
+                     (l.rho * (wave_left - unl) - r.rho * (wave_right - unr));
+  if (0.0 <= wave_left) {
+    normal_flux(l, prim_energy(l), n, unl, f);
+  } else if (wave_right <= 0.0) {
+    normal_flux(r, prim_energy(r), n, unr, f);
+  } else if (0.0 <= wave_star) {
+    hllc_star(l, unl, prim_energy(l), n, wave_left, wave_star, f);
+  } else if (wave_star < 0.0) {
+    hllc_star(r, unr, prim_energy(r), n, wave_right, wave_star, f);
+  } else {
+    for (int k = 0; k < kK; ++k) f[k] = NAN;
+  }
+}
+
+// ---------------------------------------------------------------- AUSM
+// ausm.hpp:146-187: F = rho a M+- (1, u, v, w, h) + p+- n.
+MCFD_HD void ausm_signed(bool negative, const Prim &s, const double *n,
+                         double *f) {
+  double a = sound_speed(s);
+  double h = a * a / kGm1 + kinetic(s);
+  double un = s.u * n[0] + s.v * n[1] + s.w * n[2];
+  double mach = un / a;
+  double p = s.p;
+  double signed_mach = (1 + (negative ? -mach : mach)) * 0.5;
+  if (mach >= -1 && mach <= 1) {
+    double m2 = signed_mach * signed_mach;
+    mach = negative ? -m2 : m2;
+    p *= signed_mach;
+  } else if (signed_mach < 0) {
+    mach = 0.0;
+    p = 0.0;
+  }
+  double scale = s.rho * a * mach;
+  f[0] += scale;
+  f[1] += scale * s.u + p * n[0];
+  f[2] += scale * s.v + p * n[1];
+  f[3] += scale * s.w + p * n[2];
+  f[4] += scale * h;
+}
+
+MCFD_HD void flux_ausm(const Prim &l, const Prim &r, const double *n,
+                       double *f) {
+  for (int k = 0; k < kK; ++k) f[k] = 0;
+  ausm_signed(false, l, n, f);
+  ausm_signed(true, r, n, f);
+}
+
+// ---------------------------------------------------------------- Roe
+// python/riemann.py:405-455 in 3D: acoustic waves u_n -/+ a, the entropy
+// wave and two shear waves at u_n; no entropy fix.
+MCFD_HD void flux_roe(const Prim &l, const Prim &r, const double *n,
+                      double *f) {
+  double unl = l.u * n[0] + l.v * n[1] + l.w * n[2];
+  double unr = r.u * n[0] + r.v * n[1] + r.w * n[2];
+  double el = prim_energy(l), er = prim_energy(r);
+  double fl[kK], fr[kK];
+  normal_flux(l, el, n, unl, fl);
+  normal_flux(r, er, n, unr, fr);
+  for (int k = 0; k < kK; ++k) f[k] = (fl[k] + fr[k]) / 2;
+  double h0_l = kGamma * l.p / l.rho / kGm1 + kinetic(l);
+  double h0_r = kGamma * r.p / r.rho / kGm1 + kinetic(r);
+  double sl = sqrt(l.rho), sr = sqrt(r.rho);
+  double inv_sum = 1.0 / (sl + sr);
+  double rho = sl * sr;
+  double u = (sl * l.u + sr * r.u) * inv_sum;
+  double v = (sl * l.v + sr * r.v) * inv_sum;
+  double w = (sl * l.w + sr * r.w) * inv_sum;
+  double h0 = (sl * h0_l + sr * h0_r) * inv_sum;
+  double un = u * n[0] + v * n[1] + w * n[2];
+  double ke = (u * u + v * v + w * w) / 2;
+  double aa = kGm1 * (h0 - ke);
+  double a = sqrt(aa);
+  double ua = un * a;
+  double p_jump = r.p - l.p;
+  double u_jump = unr - unl;
+  double inv_2aa = 1.0 / (2 * aa);
+  // wave u_n - a: r = (1, u - a n, h0 - u_n a)
+  double s1 = 0.5 * ((p_jump - rho * a * u_jump) * inv_2aa) * fabs(un - a);
+  // entropy wave u_n: r = (1, u, ke)
+  double s2 = 0.5 * ((r.rho - l.rho) - p_jump * (2 * inv_2aa)) * fabs(un);
+  // wave u_n + a: r = (1, u + a n, h0 + u_n a)
+  double s5 = 0.5 * ((p_jump + rho * a * u_jump) * inv_2aa) * fabs(un + a);
+  // shear waves u_n: tangential velocity jump times rho
+  double dv0 = r.u - l.u, dv1 = r.v - l.v, dv2 = r.w - l.w;
+  double dvn = dv0 * n[0] + dv1 * n[1] + dv2 * n[2];
+  double st = 0.5 * rho * fabs(un);
+  double t0 = st * (dv0 - dvn * n[0]);
+  double t1 = st * (dv1 - dvn * n[1]);
+  double t2 = st * (dv2 - dvn * n[2]);
+  f[0] -= s1 + s2 + s5;
+  f[1] -= s1 * (u - a * n[0]) + s2 * u + s5 * (u + a * n[0]) + t0;
+  f[2] -= s1 * (v - a * n[1]) + s2 * v + s5 * (v + a * n[1]) + t1;
+  f[3] -= s1 * (w - a * n[2]) + s2 * w + s5 * (w + a * n[2]) + t2;
+  f[4] -= s1 * (h0 - ua) + s2 * ke + s5 * (h0 + ua) +
+          (t0 * u + t1 * v + t2 * w);
+}
+
+// ---------------------------------------------------------------- Exact
+// exact.hpp:62-320 on the normal component; the tangential velocity comes
+// from the left state if u* > 0 else the right (SetPassiveScalars).  The
+// reference keeps u* as solver state across calls and leaves it untouched in
+// vacuum branches; here (as for a freshly built solver) it is 0 there.
+// The root finder is capped at kExactMaxIter iterations per loop; reaching
+// the cap sets *not_converged.
+constexpr int kExactMaxIter = 256;
+
+struct Exact1D {
+  double rho, u, p;  // normal-frame state on the t axis
+};
+
+MCFD_HD double ex_sound(double rho, double p) {
+  return (rho > 0 && p > 0) ? sqrt(kGamma * p / rho) : 0.0;
+}
+
+struct SpeedChange {
+  double rho_before, p_before, a_before, p_const;
+  MCFD_HD SpeedChange(double rho, double p)
+      : rho_before(rho), p_before(p),
+        a_before(rho == 0 ? 0 : ex_sound(rho, p)),
+        p_const(p * kGm1Over2) {}
+  MCFD_HD double P(double p_after) const { return kGp1Over2 * p_after + p_const; }
+  MCFD_HD double value(double p_after) const {
+    if (p_after >= p_before) {
+      double divisor = sqrt(rho_before * P(p_after));
+      return (p_after - p_before) / divisor;
+    }
+    double v = pow(p_after / p_before, kGm1Over2 / kGamma) - 1;
+    return v * (kGm1Under2 * a_before);
+  }
+  MCFD_HD double prime(double p_after) const {
+    if (p_after >= p_before) {
+      double p = P(p_after);
+      double v = kGp1Over4 * (p_before - p_after);
+      double divisor = sqrt(rho_before * p);
+      return (1 + v / p) / divisor;
+    }
+    double divisor = rho_before * a_before;
+    return pow(p_after / p_before, -kGp1Over2 / kGamma) / divisor;
+  }
+};
+
+MCFD_HD Exact1D ex_inside_expansion(double gri_1, double gri_2) {
+  constexpr double r = kGm1 / kGp1;
+  double a = r * gri_2;
+  double a_square = a * a;
+  double rho = pow(a_square / gri_1 * kOneOverGamma, kOneOverGm1);
+  return Exact1D{rho, a, a_square * rho * kOneOverGamma};
+}
+
+MCFD_HD Exact1D ex_near_shock(int field, const Exact1D &before,
+                              Exact1D after) {
+  double u = before.u;
+  double divisor = (after.u - before.u) * before.rho;
+  u += (divisor != 0 ? (after.p - before.p) / divisor : before.u);
+  bool after_shock = field == 1 ? (u < 0) : (u > 0);
+  if (after_shock) {
+    after.rho = before.rho * ((before.u - u) / (after.u - u));
+    return after;
+  }
+  return before;
+}
+
+MCFD_HD Exact1D ex_near_expansion(int field, const Exact1D &before,
+                                  Exact1D after) {
+  double a_before = ex_sound(before.rho, before.p);
+  double gri_1 = before.p / pow(before.rho, kGamma);
+  double gri_2, a_after;
+  if (field == 1) {
+    gri_2 = before.u + kGm1Under2 * a_before;
+    a_after = a_before + kGm1Over2 * (before.u - after.u);
+  } else {
+    gri_2 = before.u - kGm1Under2 * a_before;
+    a_after = a_before - kGm1Over2 * (before.u - after.u);
+  }
+  bool after_wave = field == 1 ? (after.u - a_after < 0) : (after.u + a_after > 0);
+  bool before_wave = field == 1 ? (before.u - a_before > 0)
+                                : (before.u + a_before < 0);
+  if (after_wave) {
+    after.rho = kGamma * after.p / (a_after * a_after);
+    return after;
+  } else if (before_wave) {
+    return before;
+  }
+  return ex_inside_expansion(gri_1, gri_2);
+}
+
+MCFD_HD Exact1D ex_near_vacuum(const Exact1D &l, const Exact1D &r) {
+  double left_a = ex_sound(l.rho, l.p);
+  if (l.u > left_a) return l;
+  double right_a = ex_sound(r.rho, r.p);
+  if (r.u + right_a < 0) return r;
+  double gri_1 = l.p / pow(l.rho, kGamma);
+  double gri_2 = l.u + left_a * kGm1Under2;
+  if (gri_2 >= 0) return ex_inside_expansion(gri_1, gri_2);
+  gri_1 = r.p / pow(r.rho, kGamma);
+  gri_2 = r.u - right_a * kGm1Under2;
+  if (gri_2 < 0) return ex_inside_expansion(gri_1, gri_2);
+  return Exact1D{0, 0, 0};
+}
+
+MCFD_HD Exact1D exact_upwind(const Exact1D &l, const Exact1D &r,
+                             double *star_u, bool *not_converged) {
+  *star_u = 0.0;
+  if (l.rho > 0) {
+    if (!(r.rho > 0)) {
+      double a_left = ex_sound(l.rho, l.p);
+      if (l.u >= a_left) return l;
+      double u_star = l.u + a_left * kGm1Under2;
+      if (u_star <= 0) return Exact1D{0, 0, 0};
+      return ex_inside_expansion(l.p / pow(l.rho, kGamma), u_star);
+    }
+  } else {
+    if (r.rho > 0) {
+      double a_right = ex_sound(r.rho, r.p);
+      if (r.u + a_right <= 0) return r;
+      double u_star = r.u - a_right * kGm1Under2;
+      if (u_star >= 0) return Exact1D{0, 0, 0};
+      return ex_inside_expansion(r.p / pow(r.rho, kGamma), u_star);
+    }
+    return Exact1D{0, 0, 0};
+  }
+  double du = r.u - l.u;
+  SpeedChange cl(l.rho, l.p), cr(r.rho, r.p);
+  if (cl.value(0) + cr.value(0) + du < 0) {
+    // FindRoot (exact.hpp:140-152), both loops capped
+    double x = l.p;
+    int it = 0;
+    while (cl.value(x) + cr.value(x) + du > 0 && it < kExactMaxIter) {
+      x *= 0.5;
+      ++it;
+    }
+    if (it == kExactMaxIter) *not_converged = true;
+    it = 0;
+    double fx;
+    while ((fx = cl.value(x) + cr.value(x) + du) < -1e-8 && it < kExactMaxIter) {
+      x -= fx / (cl.prime(x) + cr.prime(x));
+      ++it;
+    }
+    if (it == kExactMaxIter) *not_converged = true;
+    Exact1D star{0, 0, x};
+    star.u = 0.5 * (r.u + cr.value(x) + l.u - cl.value(x));
+    *star_u = star.u;
+    if (0 < star.u) {
+      return star.p >= l.p ? ex_near_shock(1, l, star)
+                           : ex_near_expansion(1, l, star);
+    }
+    return star.p >= r.p ? ex_near_shock(3, r, star)
+                         : ex_near_expansion(3, r, star);
+  }
+  return ex_near_vacuum(l, r);
+}
+
+MCFD_HD void flux_exact(const Prim &l, const Prim &r, const double *n,
+                        double *f, bool *not_converged) {
+  double unl = l.u * n[0] + l.v * n[1] + l.w * n[2];
+  double unr = r.u * n[0] + r.v * n[1] + r.w * n[2];
+  double star_u;
+  Exact1D s = exact_upwind(Exact1D{l.rho, unl, l.p}, Exact1D{r.rho, unr, r.p},
+                           &star_u, not_converged);
+  const Prim &t = star_u > 0 ? l : r;
+  double untan = star_u > 0 ? unl : unr;
+  // velocity = s.u n + (u_t of the passive side)
+  Prim w;
+  w.rho = s.rho;
+  w.p = s.p;
+  w.u = t.u + (s.u - untan) * n[0];
+  w.v = t.v + (s.u - untan) * n[1];
+  w.w = t.w + (s.u - untan) * n[2];
+  normal_flux(w, prim_energy(w), n, s.u, f);
+}
+
+// Upwind flux F(U_L, U_R; n) of a rotated solver (rotated/euler.hpp:153-159).
+template <int R>
+MCFD_HD void flux_upwind(const Prim &l, const Prim &r, const double *n,
+                         double *f, bool *not_converged) {
+  if constexpr (R == kRusanov) {
+    flux_rusanov(l, r, n, f);
+  } else if constexpr (R == kHllc) {
+    flux_hllc(l, r, n, f);
+  } else if constexpr (R == kAusm) {
+    flux_ausm(l, r, n, f);
+  } else if constexpr (R == kRoe) {
+    flux_roe(l, r, n, f);
+  } else {
+    flux_exact(l, r, n, f, not_converged);
+  }
+}
+
+// Boundary fluxes (rotated/euler.hpp:144-318) for the holder side state `in`
+// and the given value `g` at the face point.
+template <int R>
+MCFD_HD void flux_boundary(int kind, const Prim &in, const double *g,
+                           const double *n, double *f, bool *not_converged) {
+  switch (kind) {
+    case kBcInviscidWall:
+      f[0] = 0;
+      f[1] = in.p * n[0];
+      f[2] = in.p * n[1];
+      f[3] = in.p * n[2];
+      f[4] = 0;
+      break;
+    case kBcSupersonicInlet: {
+      Prim w = cons_to_prim(g[0], g[1], g[2], g[3], g[4]);
+      double un = w.u * n[0] + w.v * n[1] + w.w * n[2];
+      normal_flux(w, prim_energy(w), n, un, f);
+      break;
+    }
+    case kBcSupersonicOutlet: {
+      double un = in.u * n[0] + in.v * n[1] + in.w * n[2];
+      normal_flux(in, prim_energy(in), n, un, f);
+      break;
+    }
+    case kBcSubsonicInlet: {
+      // Carlson (2011) 2.7 as in rotated/euler.hpp:181-236
+      double c_interior = sound_speed(in);
+      double un_in = in.u * n[0] + in.v * n[1] + in.w * n[2];
+      double riemann_interior = -un_in - c_interior * kGm1Under2;
+      double A = n[0] * g[1] + n[1] * g[2] + n[2] * g[3];
+      double sa = A * A;
+      double gamma_times_r = kGamma * kGasR;
+      double qa = sa + kGm1Under2;
+      double qb = riemann_interior;
+      double qc = kGm1Over2 * (riemann_interior * riemann_interior) -
+                  sa * gamma_times_r * g[4];
+      double sd = sqrt(qb * qb - qa * qc);
+      double c_b = fmax((-qb + sd) / qa, (-qb - sd) / qa);
+      double t_b = (c_b * c_b) / gamma_times_r;
+      double mach = sqrt((g[4] / t_b - 1) / kGm1Over2);
+      double p_b = g[0] / pow(1 + kGm1Over2 * mach * mach, kGammaOverGm1);
+      double speed = mach * c_b;
+      Prim w{p_b / kGasR / t_b, g[1] * speed, g[2] * speed, g[3] * speed, p_b};
+      double un = w.u * n[0] + w.v * n[1] + w.w * n[2];
+      normal_flux(w, prim_energy(w), n, un, f);
+      break;
+    }
+    case kBcSubsonicOutlet: {
+      double rt = in.p / in.rho;
+      Prim w = in;
+      w.p = g[4];
+      w.rho = w.p / rt;
+      double un = w.u * n[0] + w.v * n[1] + w.w * n[2];
+      normal_flux(w, prim_energy(w), n, un, f);
+      break;
+    }
+    case kBcSmart: {
+      Prim w = cons_to_prim(g[0], g[1], g[2], g[3], g[4]);
+      flux_upwind<R>(in, w, n, f, not_converged);
+      break;
+    }
+    default:
+      for (int k = 0; k < kK; ++k) f[k] = 0;
+  }
+}
+
+}  // namespace mcfd

@@ -1,0 +1,111 @@
+// Internal state of one mcfd handle: device-resident mesh tables, geometry,
+// solution buffers and launch parameters.  Shared by the C-ABI layer
+// (api.cpp) and the kernel launchers (dgsem.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace mcfd {
+
+// Device-side scalars of the time loop.  t and dt live on the device so a
+// whole step (dt reduction + 3 stages) runs without a host round trip.
+struct DevState {
+  double t;               // current time (start of the step)
+  double dt;              // current step size
+  double dt_guess;        // upper bound passed by the caller
+  double cfl;             // CFL number used by the dt kernels
+  unsigned long long max_rate_bits;  // max over cells of max_speed / length (bits of a positive double)
+  unsigned int status;    // StatusBits
+  unsigned int pad;
+};
+
+// One boundary group on the device (mirror of mcfd_bc_state).
+struct BcDev {
+  int kind, program, axis, pad;
+  double position, speed;
+  double a[5], b[5];
+};
+
+// Stage combinations of RungeKutta<1|2|3> (temporal/rk.hpp:16-49):
+//   kStageEuler:    u + R dt                          (Euler::NextSolution)
+//   kStageRk2Last:  ((u + R dt) + u0) * 0.5
+//   kStageRk3Mid:   (u0 * 3 + (u + R dt)) / 4
+//   kStageRk3Last:  ((u + R dt) * 2 + u0) / 3
+//   kStageResidual: R                                 (GetResidualColumn)
+enum Stage {
+  kStageEuler = 0,
+  kStageRk2Last = 1,
+  kStageRk3Mid = 2,
+  kStageRk3Last = 3,
+  kStageResidual = 4,
+};
+
+struct Mesh {
+  int p = 0, q = 0, n = 0, qf = 0;  // degree, line points, nodes/cell, points/face
+  int64_t n_cells = 0, n_faces = 0, n_points = 0, column = 0;
+  int n_groups = 0;
+  // device arrays
+  double *cell_geo = nullptr;       // [cells][N][10]: w*J^-1 (3x3 row-major), 1/w
+  double *cell_rate = nullptr;      // [cells] 1 / length  (length = cbrt(V)/2)
+  int32_t *cell_flux = nullptr;     // [cells][6][QF] flux slot: >=0 subtract, <0 add (~slot), INT32_MIN none
+  int2 *face_cells = nullptr;       // [faces] holder, sharer
+  int32_t *face_group = nullptr;    // [faces]
+  double4 *face_geo = nullptr;      // [points] unit normal, weight
+  double *face_xyz = nullptr;       // [points][3]
+  short2 *face_map = nullptr;       // [points] holder node, sharer node
+  double *dmat = nullptr;           // [Q][Q] D[a][i] = l_i'(x_a)
+  BcDev *bcs = nullptr;             // [n_groups]
+  // host copies for parity queries
+  std::vector<int16_t> map_h, map_s;
+  std::vector<BcDev> host_bcs;
+};
+
+struct Buffers {
+  double *u = nullptr;     // current solution
+  double *u1 = nullptr;    // stage buffers
+  double *u2 = nullptr;
+  double *res = nullptr;   // residual output
+  double *flux = nullptr;  // [points][5] face flux scratch
+  DevState *state = nullptr;
+};
+
+struct Options {
+  int riemann = 4;
+  int precision = 0;
+  double cfl = 0;
+};
+
+}  // namespace mcfd
+
+struct mcfd_handle {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  mcfd::Options opt;
+  mcfd::Mesh mesh;
+  mcfd::Buffers buf;
+  double t_host = 0;
+  int64_t launches = 0;
+  std::string err;
+  // CUDA graph of one SSP-RK3 step (dt + 3 stages), built on first use
+  cudaGraphExec_t step_graph = nullptr;
+  int step_graph_order = 0;
+  int step_graph_kernels = 0;
+};
+
+namespace mcfd {
+
+// Kernel launchers (dgsem.cu).  Each returns the number of kernels launched.
+int launch_set_state(mcfd_handle *h, double t, double dt, double dt_guess,
+                     double cfl, int reset_rate);
+int launch_face_flux(mcfd_handle *h, const double *u, double stage_c);
+int launch_cell_update(mcfd_handle *h, int stage, const double *u_in,
+                       const double *u0, double *u_out, int advance_time);
+int launch_dt(mcfd_handle *h, const double *u);
+int launch_rk_stage_sequence(mcfd_handle *h, int order);
+
+}  // namespace mcfd

@@ -1,0 +1,181 @@
+"""Synthetic unstructured meshes in the mcfd_mesh_desc format.
+
+The reference reads CGNS files partitioned by METIS (include/mini/mesh/part.hpp);
+here the benchmark meshes are generated: a box of nx x ny x nz Hex8 cells with
+optional periodic axes and optional jitter of interior nodes.  The output is a
+plain unstructured description (node coordinates, CGNS-ordered cell nodes and
+a face list with holder/sharer, local face indices, boundary groups and
+periodic shifts), so nothing downstream relies on the structure.
+
+Face conventions (coordinate/hexahedron.hpp:378-389): local face 0 is
+zeta = -1 (z-), 1 eta = -1 (y-), 2 xi = +1 (x+), 3 eta = +1 (y+),
+4 xi = -1 (x-), 5 zeta = +1 (z+).  The holder of an interior face is the cell
+with the lower id; its face normal points to the sharer (part.hpp:957-967).
+Boundary groups of a non-periodic box: 0 x-, 1 x+, 2 y-, 3 y+, 4 z-, 5 z+.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+# local face index of the lower / upper side of each axis
+LOWER_SIDE = (4, 1, 0)
+UPPER_SIDE = (2, 3, 5)
+
+
+@dataclass
+class Mesh:
+    xyz: np.ndarray          # [n_nodes, 3] float64
+    cell_nodes: np.ndarray   # [n_cells, 8] int64
+    face_cells: np.ndarray   # [n_faces, 2] int64
+    face_sides: np.ndarray   # [n_faces, 2] int32
+    face_group: np.ndarray   # [n_faces] int32
+    face_shift: np.ndarray   # [n_faces, 3] float64
+    cell_type: np.ndarray | None = None
+    shape: tuple = ()
+    lengths: tuple = ()
+    origin: tuple = ()
+    periodic: tuple = ()
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def n_cells(self) -> int:
+        return int(self.cell_nodes.shape[0])
+
+    @property
+    def n_faces(self) -> int:
+        return int(self.face_cells.shape[0])
+
+    def cell_centers(self) -> np.ndarray:
+        return self.xyz[self.cell_nodes].mean(axis=1)
+
+
+def box(shape, lengths=(1.0, 1.0, 1.0), origin=(0.0, 0.0, 0.0),
+        periodic=(False, False, False), jitter: float = 0.0, seed: int = 0) -> Mesh:
+    """nx x ny x nz Hex8 cells on [origin, origin + lengths].
+
+    jitter > 0 moves every node strictly inside the box by U(-jitter h, jitter h)
+    per axis (h = cell size along that axis), drawn from numpy's PCG64 with
+    ``seed``; boundary nodes stay put so periodic faces still match by a shift.
+    """
+    nx, ny, nz = (int(s) for s in shape)
+    L = np.asarray(lengths, dtype=np.float64)
+    O = np.asarray(origin, dtype=np.float64)
+    h = L / np.array([nx, ny, nz], dtype=np.float64)
+    ii, jj, kk = np.meshgrid(np.arange(nx + 1), np.arange(ny + 1), np.arange(nz + 1), indexing="ij")
+    # node id = (k * (ny+1) + j) * (nx+1) + i
+    xyz = np.empty(((nx + 1) * (ny + 1) * (nz + 1), 3), dtype=np.float64)
+    nid = ((kk * (ny + 1) + jj) * (nx + 1) + ii).ravel()
+    xyz[nid, 0] = O[0] + ii.ravel() * h[0]
+    xyz[nid, 1] = O[1] + jj.ravel() * h[1]
+    xyz[nid, 2] = O[2] + kk.ravel() * h[2]
+    # exact end points
+    xyz[nid[ii.ravel() == nx], 0] = O[0] + L[0]
+    xyz[nid[jj.ravel() == ny], 1] = O[1] + L[1]
+    xyz[nid[kk.ravel() == nz], 2] = O[2] + L[2]
+    if jitter > 0:
+        rng = np.random.default_rng(seed)
+        inner = ((ii > 0) & (ii < nx) & (jj > 0) & (jj < ny) & (kk > 0) & (kk < nz)).ravel()
+        ids = nid[inner]
+        ids.sort()
+        xyz[ids] += rng.uniform(-jitter, jitter, size=(ids.size, 3)) * h
+    ci, cj, ck = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    ci, cj, ck = ci.ravel(), cj.ravel(), ck.ravel()
+    cid = (ck * ny + cj) * nx + ci
+    order = np.argsort(cid)
+    ci, cj, ck = ci[order], cj[order], ck[order]
+
+    def node(i, j, k):
+        return (k * (ny + 1) + j) * (nx + 1) + i
+
+    cell_nodes = np.stack([
+        node(ci, cj, ck), node(ci + 1, cj, ck), node(ci + 1, cj + 1, ck), node(ci, cj + 1, ck),
+        node(ci, cj, ck + 1), node(ci + 1, cj, ck + 1), node(ci + 1, cj + 1, ck + 1), node(ci, cj + 1, ck + 1),
+    ], axis=1).astype(np.int64)
+
+    def cell(i, j, k):
+        return (k * ny + j) * nx + i
+
+    n = (nx, ny, nz)
+    holders, sharers, hsides, ssides, shifts = [], [], [], [], []
+    groups_b, holders_b, sides_b = [], [], []
+    idx = (ci, cj, ck)
+    for ax in range(3):
+        ijk = [ci, cj, ck]
+        inner = idx[ax] < n[ax] - 1
+        nb = list(ijk)
+        nb[ax] = idx[ax] + 1
+        a = cell(*[v[inner] for v in ijk])
+        b = cell(*[v[inner] for v in nb])
+        holders.append(a); sharers.append(b)
+        hsides.append(np.full(a.size, UPPER_SIDE[ax])); ssides.append(np.full(a.size, LOWER_SIDE[ax]))
+        shifts.append(np.zeros((a.size, 3)))
+        last = idx[ax] == n[ax] - 1
+        first = idx[ax] == 0
+        if periodic[ax]:
+            lo = cell(*[v[first] for v in ijk])
+            hi_ijk = [v[first].copy() for v in ijk]
+            hi_ijk[ax] = np.full(hi_ijk[ax].shape, n[ax] - 1)
+            hi = cell(*hi_ijk)
+            # holder = lower cell id = the cell at index 0 along the axis
+            sh = np.zeros((lo.size, 3))
+            sh[:, ax] = -L[ax]
+            holders.append(lo); sharers.append(hi)
+            hsides.append(np.full(lo.size, LOWER_SIDE[ax])); ssides.append(np.full(lo.size, UPPER_SIDE[ax]))
+            shifts.append(sh)
+        else:
+            lo = cell(*[v[first] for v in ijk])
+            hi = cell(*[v[last] for v in ijk])
+            holders_b += [lo, hi]
+            sides_b += [np.full(lo.size, LOWER_SIDE[ax]), np.full(hi.size, UPPER_SIDE[ax])]
+            groups_b += [np.full(lo.size, 2 * ax), np.full(hi.size, 2 * ax + 1)]
+    h_i = np.concatenate(holders); s_i = np.concatenate(sharers)
+    hs_i = np.concatenate(hsides); ss_i = np.concatenate(ssides)
+    sh_i = np.concatenate(shifts)
+    o = np.lexsort((hs_i, h_i))  # interior faces sorted by (holder, side)
+    face_cells = [np.stack([h_i[o], s_i[o]], axis=1)]
+    face_sides = [np.stack([hs_i[o], ss_i[o]], axis=1)]
+    face_group = [np.full(o.size, -1)]
+    face_shift = [sh_i[o]]
+    if holders_b:
+        hb = np.concatenate(holders_b); sb = np.concatenate(sides_b); gb = np.concatenate(groups_b)
+        ob = np.lexsort((hb, gb))  # boundary faces by (group, holder)
+        face_cells.append(np.stack([hb[ob], np.full(ob.size, -1)], axis=1))
+        face_sides.append(np.stack([sb[ob], np.full(ob.size, -1)], axis=1))
+        face_group.append(gb[ob])
+        face_shift.append(np.zeros((ob.size, 3)))
+    return Mesh(
+        xyz=np.ascontiguousarray(xyz),
+        cell_nodes=np.ascontiguousarray(cell_nodes),
+        face_cells=np.ascontiguousarray(np.concatenate(face_cells).astype(np.int64)),
+        face_sides=np.ascontiguousarray(np.concatenate(face_sides).astype(np.int32)),
+        face_group=np.ascontiguousarray(np.concatenate(face_group).astype(np.int32)),
+        face_shift=np.ascontiguousarray(np.concatenate(face_shift).astype(np.float64)),
+        shape=(nx, ny, nz), lengths=tuple(L), origin=tuple(O), periodic=tuple(periodic),
+    )
+
+
+def gll_points(q: int) -> np.ndarray:
+    """Gauss-Lobatto points on [-1, 1] (integrator/lobatto.hpp:37-83)."""
+    if q == 2:
+        return np.array([-1.0, 1.0])
+    if q == 3:
+        return np.array([-1.0, 0.0, 1.0])
+    if q == 4:
+        s = np.sqrt(1.0 / 5)
+        return np.array([-1.0, -s, s, 1.0])
+    raise ValueError("q must be 2, 3 or 4")
+
+
+def node_coordinates(mesh: Mesh, degree: int) -> np.ndarray:
+    """Global coordinates of the (p+1)^3 GLL nodes of every cell, [cells, N, 3],
+    node order i*Q*Q + j*Q + k (integrator/hexahedron.hpp:66-80)."""
+    x = gll_points(degree + 1)
+    a, b, c = np.meshgrid(x, x, x, indexing="ij")
+    loc = np.stack([a.ravel(), b.ravel(), c.ravel()], axis=1)  # [N, 3]
+    corners = np.array([[-1, -1, -1], [1, -1, -1], [1, 1, -1], [-1, 1, -1],
+                        [-1, -1, 1], [1, -1, 1], [1, 1, 1], [-1, 1, 1]], dtype=np.float64)
+    shape = np.prod(1 + loc[:, None, :] * corners[None, :, :], axis=2) / 8  # [N, 8]
+    xn = mesh.xyz[mesh.cell_nodes]  # [cells, 8, 3]
+    return np.einsum("nv,cvd->cnd", shape, xn)

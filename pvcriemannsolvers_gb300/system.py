@@ -1,0 +1,241 @@
+"""Host-side mirror of the reference's temporal / spatial interface.
+
+``Lobatto`` plays the role of ``mini::spatial::dg::Lobatto`` (a
+``mini::temporal::System``) and ``RungeKutta`` the role of
+``mini::temporal::RungeKutta<order>``; both drive the GPU library through the
+C ABI of include/mcfd.h.  Method names and argument meanings follow the
+reference:
+
+  System::SetTime / SetSolutionColumn / GetSolutionColumn / GetResidualColumn
+      include/mini/temporal/ode.hpp:17-48
+  FiniteElement::GetTimeStep(dt_guess, rk_order)      spatial/fem.hpp:417-435
+  FiniteElement::Set<Boundary>(name, func)            spatial/fem.hpp:196-222
+  FiniteElement::Approximate(func)                    spatial/fem.hpp:147-154
+  Solver::Update(system, t_curr, dt)                  temporal/ode.hpp:92-105
+
+Boundary "names" are the integer face groups of the mesh description.  A
+boundary value is a constant conservative state, or a ``MovingSplit``
+(value = a if x[axis] - speed * t < position else b), the two forms the
+reference's drivers use (demo/euler/shock_tube.cpp, demo/euler/riemann2d.cpp).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import Callable
+
+import numpy as np
+
+from . import capi
+from .mesh import Mesh, node_coordinates
+
+
+@dataclass
+class MovingSplit:
+    axis: int
+    position: float
+    speed: float
+    a: np.ndarray
+    b: np.ndarray
+
+
+def _bc_state(kind: int, value) -> capi.BcState:
+    s = capi.BcState()
+    s.kind = kind
+    if value is None:
+        s.program = capi.STATE_CONSTANT
+    elif isinstance(value, MovingSplit):
+        s.program = capi.STATE_MOVING_SPLIT
+        s.axis = int(value.axis)
+        s.position = float(value.position)
+        s.speed = float(value.speed)
+        for k in range(5):
+            s.a[k] = float(value.a[k])
+            s.b[k] = float(value.b[k])
+    else:
+        v = np.asarray(value, dtype=np.float64)
+        if v.shape != (5,):
+            raise ValueError("a boundary value is a 5-component state")
+        s.program = capi.STATE_CONSTANT
+        for k in range(5):
+            s.a[k] = float(v[k])
+    return s
+
+
+class Lobatto:
+    """DGSEM (dg::Lobatto, kLocal = false) Euler system on one GPU."""
+
+    def __init__(self, mesh: Mesh, degree: int, riemann: str | int = "rusanov",
+                 cfl: float = 0.0, device: int = 0):
+        lib = capi.load()
+        self.mesh = mesh
+        self.degree = int(degree)
+        self.riemann = capi.RIEMANN[riemann] if isinstance(riemann, str) else int(riemann)
+        self._keep = [
+            np.ascontiguousarray(mesh.xyz, dtype=np.float64),
+            np.ascontiguousarray(mesh.cell_nodes, dtype=np.int64),
+            np.ascontiguousarray(mesh.face_cells, dtype=np.int64),
+            np.ascontiguousarray(mesh.face_sides, dtype=np.int32),
+            np.ascontiguousarray(mesh.face_group, dtype=np.int32),
+            np.ascontiguousarray(mesh.face_shift, dtype=np.float64),
+        ]
+        xyz, cn, fc, fs, fg, fsh = self._keep
+        desc = capi.MeshDesc()
+        desc.n_nodes = xyz.shape[0]
+        desc.xyz = capi.dptr(xyz)
+        desc.n_cells = cn.shape[0]
+        desc.cell_nodes = cn.ctypes.data_as(C.POINTER(C.c_int64))
+        desc.cell_type = None
+        desc.n_faces = fc.shape[0]
+        desc.face_cells = fc.ctypes.data_as(C.POINTER(C.c_int64))
+        desc.face_sides = fs.ctypes.data_as(C.POINTER(C.c_int32))
+        desc.face_group = fg.ctypes.data_as(C.POINTER(C.c_int32))
+        desc.face_shift = capi.dptr(fsh)
+        opt = capi.Options()
+        opt.degree = self.degree
+        opt.scheme = capi.DGSEM
+        opt.riemann = self.riemann
+        opt.precision = capi.FP64
+        opt.cfl = float(cfl)
+        opt.device = int(device)
+        h = C.c_void_p()
+        capi.check(lib.mcfd_create(C.byref(desc), C.byref(opt), C.byref(h)), None)
+        self._h = h
+        self._lib = lib
+        self.column_size = int(lib.mcfd_column_size(h))
+        self.n_nodes_per_cell = (self.degree + 1) ** 3
+
+    # -- lifetime
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.mcfd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _check(self, code: int) -> None:
+        capi.check(code, self._h)
+
+    # -- boundary registration (fem.hpp:196-222)
+    def SetInviscidWall(self, group: int) -> None:
+        self._check(self._lib.mcfd_set_bc(self._h, group, C.byref(_bc_state(capi.BC_INVISCID_WALL, None))))
+
+    def SetSupersonicOutlet(self, group: int) -> None:
+        self._check(self._lib.mcfd_set_bc(self._h, group, C.byref(_bc_state(capi.BC_SUPERSONIC_OUTLET, None))))
+
+    def SetSupersonicInlet(self, group: int, value) -> None:
+        self._check(self._lib.mcfd_set_bc(self._h, group, C.byref(_bc_state(capi.BC_SUPERSONIC_INLET, value))))
+
+    def SetSubsonicInlet(self, group: int, value) -> None:
+        self._check(self._lib.mcfd_set_bc(self._h, group, C.byref(_bc_state(capi.BC_SUBSONIC_INLET, value))))
+
+    def SetSubsonicOutlet(self, group: int, value) -> None:
+        self._check(self._lib.mcfd_set_bc(self._h, group, C.byref(_bc_state(capi.BC_SUBSONIC_OUTLET, value))))
+
+    def SetSmartBoundary(self, group: int, value) -> None:
+        self._check(self._lib.mcfd_set_bc(self._h, group, C.byref(_bc_state(capi.BC_SMART, value))))
+
+    # -- System quartet (ode.hpp:17-48)
+    def SetTime(self, t_curr: float) -> None:
+        self._check(self._lib.mcfd_set_time(self._h, float(t_curr)))
+
+    def SetSolutionColumn(self, column: np.ndarray) -> None:
+        col = np.ascontiguousarray(column, dtype=np.float64)
+        self._check(self._lib.mcfd_set_solution(self._h, capi.dptr(col), col.size))
+
+    def GetSolutionColumn(self) -> np.ndarray:
+        out = np.empty(self.column_size, dtype=np.float64)
+        self._check(self._lib.mcfd_get_solution(self._h, capi.dptr(out), out.size))
+        return out
+
+    def get_solution_into(self, out: np.ndarray) -> None:
+        """GetSolutionColumn into a caller-owned (e.g. pinned) float64 buffer."""
+        if out.dtype != np.float64 or not out.flags.c_contiguous or out.size != self.column_size:
+            raise ValueError("out must be a contiguous float64 array of the column size")
+        self._check(self._lib.mcfd_get_solution(self._h, capi.dptr(out), out.size))
+
+    def GetResidualColumn(self) -> np.ndarray:
+        out = np.empty(self.column_size, dtype=np.float64)
+        self._check(self._lib.mcfd_residual(self._h, capi.dptr(out), out.size))
+        return out
+
+    # -- device-pointer variants (torch tensors or raw addresses)
+    def set_solution_device(self, ptr: int, n: int) -> None:
+        self._check(self._lib.mcfd_set_solution_device(self._h, C.c_void_p(ptr), n))
+
+    def get_solution_device(self, ptr: int, n: int) -> None:
+        self._check(self._lib.mcfd_get_solution_device(self._h, C.c_void_p(ptr), n))
+
+    def residual_device(self, ptr: int, n: int) -> None:
+        self._check(self._lib.mcfd_residual_device(self._h, C.c_void_p(ptr), n))
+
+    # -- spatial extras
+    def GetTimeStep(self, dt_guess: float, rk_order: int) -> float:
+        dt = C.c_double()
+        self._check(self._lib.mcfd_time_step(self._h, float(dt_guess), int(rk_order), C.byref(dt)))
+        return dt.value
+
+    def Approximate(self, func: Callable[[np.ndarray], np.ndarray]) -> None:
+        """Interpolate func (vectorised over [M, 3] points -> [M, 5]) at the
+        GLL nodes (polynomial/hexahedron.hpp:642-648) and load it."""
+        x = node_coordinates(self.mesh, self.degree).reshape(-1, 3)
+        self.SetSolutionColumn(np.ascontiguousarray(func(x), dtype=np.float64).ravel())
+
+    def node_coordinates(self) -> np.ndarray:
+        return node_coordinates(self.mesh, self.degree)
+
+    def face_node_maps(self) -> tuple[np.ndarray, np.ndarray]:
+        qf = (self.degree + 1) ** 2
+        h = np.empty((self.mesh.n_faces, qf), dtype=np.int16)
+        s = np.empty((self.mesh.n_faces, qf), dtype=np.int16)
+        self._check(self._lib.mcfd_face_node_maps(
+            self._h, h.ctypes.data_as(C.POINTER(C.c_int16)), s.ctypes.data_as(C.POINTER(C.c_int16))))
+        return h, s
+
+    def launch_count(self) -> int:
+        return int(self._lib.mcfd_launch_count(self._h))
+
+    def advance(self, n_steps: int, dt_guess: float, rk_order: int, t: float) -> float:
+        """n_steps x {dt = GetTimeStep; Update(t, dt)} with dt, t on device."""
+        tt = C.c_double(float(t))
+        self._check(self._lib.mcfd_advance(self._h, int(n_steps), float(dt_guess), int(rk_order), C.byref(tt)))
+        return tt.value
+
+    def kernel_times(self, reps: int = 10) -> dict:
+        """Average CUDA-event milliseconds per launch of each stage kernel."""
+        out = (C.c_double * 4)()
+        self._check(self._lib.mcfd_kernel_times(self._h, int(reps), out))
+        return {"dt": out[0], "face_flux": out[1], "cell_update": out[2], "rk3_step": out[3]}
+
+    def synchronize(self) -> None:
+        self._check(self._lib.mcfd_synchronize(self._h))
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        self._check(self._lib.mcfd_set_stream(self._h, C.c_void_p(stream_ptr or 0)))
+
+
+class RungeKutta:
+    """mini::temporal::RungeKutta<order> (rk.hpp:10-57) over a Lobatto system:
+    the whole update runs as fused device stages."""
+
+    def __init__(self, order: int):
+        if order not in (1, 2, 3):
+            raise ValueError("order must be 1, 2 or 3")
+        self.order = order
+
+    def Update(self, system: Lobatto, t_curr: float, dt: float) -> None:
+        system._check(system._lib.mcfd_rk_step(system.handle, float(t_curr), float(dt), self.order))

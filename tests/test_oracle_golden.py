@@ -1,0 +1,215 @@
+"""Pins the CPU oracle to the reference's own known-answer tests.
+
+* C++ KATs of test/riemann/euler/{exact,hllc,ausm}.cpp (transcribed into
+  tests/golden/riemann_kat.json by tests/golden/make_golden.py, which checks
+  the transcription against the reference source),
+* Roe / Lax-Friedrichs fluxes of the reference's Python prototype
+  (python/riemann.py:405-476) on seeded states (tests/golden/python_fluxes.json),
+* frame invariance and the inviscid-wall flux of test/riemann/rotated/euler.cpp,
+* the RK1/2/3 closed forms of test/temporal/rk.cpp (bit-exact),
+* GLL exactness (test/integrator/lobatto.cpp) through the mesh geometry.
+"""
+import json
+import math
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle.orc as orc
+from pvcriemannsolvers_gb300 import cases, mesh as meshlib
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+KAT = json.loads((GOLDEN / "riemann_kat.json").read_text())
+PYF = json.loads((GOLDEN / "python_fluxes.json").read_text())
+SOLVER = {"exact": orc.EXACT, "hllc": orc.HLLC, "ausm": orc.AUSM}
+G = 1.4
+
+
+def to3d(state, dim):
+    """1D (rho,u,p) / 2D (rho,u,v,p) / 3D (rho,u,v,w,p) -> 3D primitive."""
+    s = list(state)
+    if dim == 1:
+        return [s[0], s[1], 0.0, 0.0, s[2]]
+    if dim == 2:
+        return [s[0], s[1], s[2], 0.0, s[3]]
+    return s
+
+
+def flux_of(prim):
+    """GetFlux of a 3D primitive in the normal frame (types.hpp:312-321)."""
+    rho, u, v, w, p = prim
+    e = p / (G - 1) + 0.5 * rho * (u * u + v * v + w * w)
+    return np.array([rho * u, rho * u * u + p, rho * v * u, rho * w * u, (e + p) * u])
+
+
+def components(dim):
+    # compared flux components per dimension: mass, momX, (momY, momZ), energy
+    return {1: [0, 1, 4], 2: [0, 1, 2, 4], 3: [0, 1, 2, 3, 4]}[dim]
+
+
+@pytest.mark.parametrize("case", KAT["cases"], ids=lambda c: f"{c['solver']}{c['dim']}d:{c['src'].split('/')[-1]}:{c['line']}")
+def test_riemann_kat(case):
+    dim = case["dim"]
+    got = orc.flux_1d(SOLVER[case["solver"]], to3d(case["left"], dim), to3d(case["right"], dim))
+    want = flux_of(to3d(case["expect"], dim))
+    for comp, eps in zip(components(dim), case["eps"] if dim != 1 else case["eps"]):
+        pass
+    comps = components(dim)
+    # eps lists follow (mass, momX, [momY, momZ], energy) for "ratio" with
+    # dim 1: [mass, momX, energy]; "near" uses one eps for all.
+    for i, c in enumerate(comps):
+        eps = case["eps"][i]
+        x, y = want[c], got[c]
+        if case["cmp"] == "near":
+            if x == 0:
+                assert y == 0, (c, x, y)
+            else:
+                assert abs(y / x - 1) <= eps, (c, x, y)
+        else:
+            denom = max(abs(x), abs(y))
+            assert denom == 0 or abs(x - y) / denom <= eps, (c, x, y)
+
+
+@pytest.mark.parametrize("case", KAT["vacuum"], ids=lambda c: f"vacuum:{c['line']}")
+def test_exact_vacuum_kat(case):
+    dim = case["dim"]
+    left, right = to3d(case["left"], dim), to3d(case["right"], dim)
+    got = orc.flux_1d(orc.EXACT, left, right)
+    if case["expect"] == "left":
+        want = flux_of(left)
+    elif case["expect"] == "right":
+        want = flux_of(right)
+    else:
+        want = flux_of(to3d(case["expect"], dim))
+    for c in components(dim):
+        assert abs(got[c] - want[c]) <= case["atol"] * (1 if case["atol"] > 0 else 1) or got[c] == want[c], (c, got, want)
+
+
+@pytest.mark.parametrize("i", range(len(PYF["cases"])))
+@pytest.mark.parametrize("solver", ["roe", "lax_friedrichs"])
+def test_python_prototype_fluxes(i, solver):
+    case = PYF["cases"][i]
+    l = [case["left"][0], case["left"][1], 0.0, 0.0, case["left"][2]]
+    r = [case["right"][0], case["right"][1], 0.0, 0.0, case["right"][2]]
+    kind = orc.ROE if solver == "roe" else orc.RUSANOV
+    got = orc.flux_1d(kind, l, r)[[0, 1, 4]]
+    want = np.array(case[solver])
+    np.testing.assert_allclose(got, want, rtol=1e-13, atol=1e-13)
+
+
+def _frame(n):
+    n = np.asarray(n, float) / np.linalg.norm(n)
+    t = np.cross(n, [0.3, 0.7, 0.2]); t /= np.linalg.norm(t)
+    b = np.cross(n, t)
+    return np.stack([n, t, b])
+
+
+@pytest.mark.parametrize("kind", [orc.EXACT, orc.HLLC, orc.AUSM, orc.ROE, orc.RUSANOV])
+def test_rotated_frame_invariance(kind):
+    """test/riemann/rotated/euler.cpp:80-151: a rotated solver applied in a
+    frame equals the 1D solver on the rotated states (and the Sod KAT holds
+    for the identity frame and its mirror)."""
+    rng = np.random.default_rng(7)
+    for _ in range(64):
+        n = rng.normal(size=3)
+        f = _frame(n)
+        wl = [rng.uniform(0.5, 2), *rng.uniform(-1, 1, 3), rng.uniform(0.5, 2)]
+        wr = [rng.uniform(0.5, 2), *rng.uniform(-1, 1, 3), rng.uniform(0.5, 2)]
+        ul, ur = orc.prim_to_cons(wl), orc.prim_to_cons(wr)
+        got = orc.flux_rotated(kind, f, ul, ur)
+        # rotate primitives into the frame, 1D flux, rotate back
+        nl = [wl[0], *(f @ np.array(wl[1:4])), wl[4]]
+        nr = [wr[0], *(f @ np.array(wr[1:4])), wr[4]]
+        f1 = orc.flux_1d(kind, nl, nr)
+        want = np.array([f1[0], *(f.T @ f1[1:4]), f1[4]])
+        np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-12)
+
+
+def test_inviscid_wall_flux():
+    """rotated/euler.cpp:160-174 and test/riemann/rotated/euler.cpp:122-149:
+    the wall flux is (0, p n, 0)."""
+    rng = np.random.default_rng(31415926)
+    for _ in range(128):
+        ang = math.radians(180 * rng.uniform())
+        f = np.array([[1, 0, 0], [0, math.cos(ang), math.sin(ang)], [0, -math.sin(ang), math.cos(ang)]], float)
+        rho = 1.29 * (1 + rng.uniform(-1, 1) * 0.05)
+        w = [rho, 10 * rng.uniform(-1, 1), 20 * rng.uniform(-1, 1), 30 * rng.uniform(-1, 1),
+             101325 * (1 + rng.uniform(-1, 1) * 0.05)]
+        flux = orc.flux_boundary(orc.RUSANOV, orc.BC_INVISCID_WALL, f, orc.prim_to_cons(w), np.zeros(5))
+        assert abs(flux[1] - w[4]) <= 1e-10 * w[4]
+        assert flux[0] == 0 and flux[2] == 0 and flux[3] == 0 and flux[4] == 0
+
+
+def test_consistency_equal_states():
+    """hllc.cpp:35-44 / ausm.cpp:35-44: F(U, U) = F(U) for random states."""
+    rng = np.random.default_rng(31415926)
+    for _ in range(32):
+        w = [rng.uniform(0.1, 1), rng.uniform(0, 1), rng.uniform(-1, 1), rng.uniform(-1, 1), rng.uniform(0.1, 1)]
+        for kind in (orc.EXACT, orc.HLLC, orc.AUSM, orc.ROE, orc.RUSANOV):
+            got = orc.flux_1d(kind, w, w)
+            np.testing.assert_allclose(got, flux_of(w), rtol=1e-13, atol=1e-15)
+
+
+def test_gas_conversions():
+    """types.cpp:54-67: PrimitiveToConservative / ConservativeToPrimitive round trip,
+    and the SetZeroIfNegative clamp."""
+    w = [1.29, 3.0, -4.0, 5.0, 101325.0]
+    u = orc.prim_to_cons(w)
+    np.testing.assert_allclose(orc.cons_to_prim(u), w, rtol=1e-15)
+    assert np.all(orc.cons_to_prim([-1.0, 1, 1, 1, 5]) == 0)
+    assert np.all(orc.cons_to_prim([1.0, 10, 0, 0, 1.0]) == 0)  # p < 0 after conversion
+    fm = orc.flux_matrix(u)
+    assert fm.shape == (5, 3)
+    np.testing.assert_allclose(fm[:, 0], flux_of(w), rtol=1e-14)
+
+
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_rk_closed_forms(order):
+    """test/temporal/rk.cpp:21-70: RungeKutta<order> on du/dt = A u equals the
+    closed form evaluated with the same operations, bit for bit."""
+    rng = np.random.default_rng(31415926)
+    n = 10
+    a = rng.uniform(-1, 1, (n, n))
+    u0 = rng.uniform(-1, 1, n)
+    t, dt = rng.uniform(), rng.uniform()
+    got = orc.rk_update_linear(order, a, t, dt, u0)
+
+    def step(u):
+        r = np.array([sum(a[i, j] * u[j] for j in range(n)) for i in range(n)])
+        return u + r * dt
+
+    u1 = step(u0)
+    if order == 1:
+        want = u1
+    elif order == 2:
+        want = (step(u1) + u0) * 0.5
+    else:
+        u2 = (u0 * 3 + step(u1)) / 4
+        want = (step(u2) * 2 + u0) / 3
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("p", [1, 2, 3])
+def test_gll_volume_and_polynomial_exactness(p):
+    """test/integrator/lobatto.cpp: a Q-point GLL rule integrates degree
+    2Q-3 exactly; here through the oracle's node weights on an affine box."""
+    m = meshlib.box((2, 3, 2), lengths=(1.0, 1.5, 0.5), origin=(0.1, -0.2, 0.3))
+    om = orc.Mesh(m, p)
+    xyz, w = om.node_geometry()
+    assert abs(w.sum() - 0.75) < 1e-14
+    deg = 2 * (p + 1) - 3
+    f = xyz[..., 0] ** deg
+    exact = (1.1 ** (deg + 1) - 0.1 ** (deg + 1)) / (deg + 1) * 1.5 * 0.5
+    assert abs((w * f).sum() - exact) < 1e-12
+
+
+def test_freestream_preservation():
+    """A uniform state has zero residual on an affine periodic mesh."""
+    m = meshlib.box((3, 2, 2), lengths=(1, 2, 3), periodic=(True, True, True))
+    for p in (1, 2, 3):
+        om = orc.Mesh(m, p)
+        x = meshlib.node_coordinates(m, p).reshape(-1, 3)
+        u = cases.prim_to_cons(np.ones(len(x)), 0.3, -0.2, 0.5, 1.0).ravel()
+        for kind in (orc.EXACT, orc.HLLC, orc.AUSM, orc.ROE, orc.RUSANOV):
+            assert np.abs(om.residual(kind, u)).max() < 1e-12
