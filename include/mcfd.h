@@ -172,6 +172,26 @@ int mcfd_set_solution_device(mcfd_handle *h, const double *d_column, int64_t n);
 int mcfd_get_solution_device(mcfd_handle *h, double *d_column, int64_t n);
 int mcfd_residual_device(mcfd_handle *h, double *d_residual, int64_t n);
 
+/* Residual that allocates nothing.  No counterpart in the reference.
+ *
+ * For callers that cannot call cudaMalloc while they run: a host program that
+ * hands all device memory to its own pool at start-up and forbids further
+ * allocations, or a time-critical loop where the implicit device
+ * synchronisation of cudaMalloc/cudaFree is not acceptable.  The caller
+ * passes the input column d_u and the output d_residual (device pointers,
+ * length n = mcfd_column_size); the face-flux scratch is a fixed 16 MiB
+ * device array inside the library (2,097,152 doubles, i.e. meshes with at
+ * most 419,430 face points; larger meshes are rejected with
+ * MCFD_ERR_ARGUMENT).  Every GPU that loads the library holds that array
+ * until the process exits.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) and should come before any stream
+ * capture.  All calls share the array and it keeps the last call's contents;
+ * every scratch entry is written before it is read within a call, so nothing
+ * needs clearing, but calls that overlap on the GPU (other threads or
+ * streams) race on it.  Results equal mcfd_residual_device. */
+int mcfd_residual_device_noalloc(mcfd_handle *h, const double *d_u,
+                                 double *d_residual, int64_t n);
+
 /* FiniteElement::GetTimeStep(dt_guess, rk_order) (fem.hpp:417-435). */
 int mcfd_time_step(mcfd_handle *h, double dt_guess, int32_t rk_order,
                    double *dt);

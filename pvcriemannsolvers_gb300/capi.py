@@ -83,6 +83,7 @@ SIGNATURES = {
     "mcfd_set_solution_device": (C.c_int, [_P, _P, C.c_int64]),
     "mcfd_get_solution_device": (C.c_int, [_P, _P, C.c_int64]),
     "mcfd_residual_device": (C.c_int, [_P, _P, C.c_int64]),
+    "mcfd_residual_device_noalloc": (C.c_int, [_P, _P, _P, C.c_int64]),
     "mcfd_time_step": (C.c_int, [_P, C.c_double, C.c_int32, _D]),
     "mcfd_rk_step": (C.c_int, [_P, C.c_double, C.c_double, C.c_int32]),
     "mcfd_advance": (C.c_int, [_P, C.c_int32, C.c_double, C.c_int32, _D]),

@@ -563,6 +563,28 @@ int mcfd_residual_device(mcfd_handle *h, double *d_residual, int64_t n) {
   return residual_into(h, d_residual, n, cudaMemcpyDeviceToDevice);
 }
 
+int mcfd_residual_device_noalloc(mcfd_handle *h, const double *d_u,
+                                 double *d_residual, int64_t n) {
+  if (!h || !d_u || !d_residual) return MCFD_ERR_ARGUMENT;
+  if (n != h->mesh.column) return fail(h, MCFD_ERR_ARGUMENT, "column size mismatch");
+  if (h->mesh.n_points * mcfd::kK > mcfd::kStaticFluxCapacity)
+    return fail(h, MCFD_ERR_ARGUMENT,
+                "mesh too large for the no-allocation residual: " +
+                    std::to_string(h->mesh.n_points) + " face points need " +
+                    std::to_string(h->mesh.n_points * mcfd::kK) +
+                    " scratch doubles, the static capacity is " +
+                    std::to_string(mcfd::kStaticFluxCapacity) + " (16 MiB)");
+  CUDA_TRY(h, cudaSetDevice(h->device));
+  double *scratch = nullptr;
+  std::string why;
+  if (mcfd::static_flux_scratch(h->device, &scratch, &why))
+    return fail(h, MCFD_ERR_CUDA, why);
+  h->launches += mcfd::launch_set_state(h, h->t_host, 0.0, 0.0, 0.0, 1);
+  h->launches += mcfd::launch_residual_static_scratch(h, d_u, d_residual, scratch);
+  CUDA_TRY(h, cudaGetLastError());
+  return check_status(h);
+}
+
 int mcfd_time_step(mcfd_handle *h, double dt_guess, int32_t rk_order, double *dt) {
   if (!h || !dt) return MCFD_ERR_ARGUMENT;
   cudaSetDevice(h->device);

@@ -22,6 +22,8 @@
 
 #include <climits>
 #include <cstdint>
+#include <mutex>
+#include <string>
 
 #include "euler.cuh"
 #include "handle.hpp"
@@ -345,6 +347,72 @@ int launch_dt(mcfd_handle *h, const double *u) {
   }
   dt_finalize_kernel<<<1, 1, 0, h->stream>>>(h->buf.state);
   return 2;
+}
+
+// ---------------------------------------------------------------------------
+// Residual for callers that cannot allocate device memory.
+//
+// The face-flux scratch of this variant is a fixed file-scope device array
+// instead of the handle's allocated buffer.  Host code must not pass the
+// symbol itself to a kernel (on the host it names a host-side stand-in), so
+// the device address is fetched with cudaGetSymbolAddress once per device,
+// with that device current, on the first call, and cached.
+namespace {
+__device__ __align__(256) double g_static_face_flux[kStaticFluxCapacity];
+
+struct StaticScratchSlot {
+  double *ptr = nullptr;
+  bool ready = false;
+};
+constexpr int kMaxDevices = 64;
+StaticScratchSlot g_static_slots[kMaxDevices];
+std::mutex g_static_mutex;
+}  // namespace
+
+int static_flux_scratch(int device, double **ptr, std::string *err) {
+  if (device < 0 || device >= kMaxDevices) {
+    *err = "device ordinal out of range for the static scratch table";
+    return 1;
+  }
+  std::lock_guard<std::mutex> lock(g_static_mutex);
+  StaticScratchSlot &slot = g_static_slots[device];
+  if (!slot.ready) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_static_face_flux);
+    if (e != cudaSuccess) {
+      *err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
+      return 1;
+    }
+    slot.ptr = static_cast<double *>(p);
+    slot.ready = true;
+  }
+  *ptr = slot.ptr;
+  return 0;
+}
+
+int launch_residual_static_scratch(mcfd_handle *h, const double *d_u,
+                                   double *d_r, double *scratch) {
+  const Mesh &m = h->mesh;
+  FaceArgs fa{d_u, m.face_cells, m.face_group, m.face_geo, m.face_xyz,
+              m.face_map, m.bcs, scratch, h->buf.state, 0.0,
+              m.n_points, m.n_groups};
+  CellArgs ca{d_u, nullptr, d_r, m.cell_geo, m.cell_flux, scratch, m.dmat,
+              h->buf.state, m.n_cells, 0};
+  int n = 0;
+  if (m.n_points > 0) {
+    switch (m.q) {
+      case 2: face_dispatch_r<2>(h, fa); break;
+      case 3: face_dispatch_r<3>(h, fa); break;
+      default: face_dispatch_r<4>(h, fa); break;
+    }
+    ++n;
+  }
+  switch (m.q) {
+    case 2: cell_dispatch_s<2>(h, kStageResidual, ca); break;
+    case 3: cell_dispatch_s<3>(h, kStageResidual, ca); break;
+    default: cell_dispatch_s<4>(h, kStageResidual, ca); break;
+  }
+  return n + 1;
 }
 
 // The stages of RungeKutta<order>::Update with the result left in buf.u.

@@ -108,4 +108,12 @@ int launch_cell_update(mcfd_handle *h, int stage, const double *u_in,
 int launch_dt(mcfd_handle *h, const double *u);
 int launch_rk_stage_sequence(mcfd_handle *h, int order);
 
+// Residual whose face-flux scratch is a fixed file-scope device array
+// (mcfd_residual_device_noalloc).  Capacity in doubles: 2 Mi = 16 MiB, i.e.
+// at most 419,430 face points (5 doubles each).
+constexpr int64_t kStaticFluxCapacity = 2 * 1024 * 1024;
+int static_flux_scratch(int device, double **ptr, std::string *err);
+int launch_residual_static_scratch(mcfd_handle *h, const double *d_u,
+                                   double *d_r, double *scratch);
+
 }  // namespace mcfd
