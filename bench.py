@@ -203,7 +203,7 @@ def run_gpu(args, rank, world, local_rank):
         import torch.distributed as dist
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
-    m = meshlib.box((N_CELLS_1D,) * 3, lengths=(10.0,) * 3, periodic=(True,) * 3)
+    m = meshlib.box((args.cells,) * 3, lengths=(10.0,) * 3, periodic=(True,) * 3)
     sysm = Lobatto(m, DEGREE, "rusanov", cfl=CFL, device=local_rank)
     stream = torch.cuda.Stream(device=dev)
     sysm.set_stream(stream.cuda_stream)
@@ -291,7 +291,7 @@ def run_gpu(args, rank, world, local_rank):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": workload(),
+            "config": workload(args.cells),
             "accuracy": {"density_rel_l2_vs_exact": l2_exact, "t_end": t},
             "clocks": clocks.summary(),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * L, "d2h_bytes_per_step": 8 * L,
@@ -311,6 +311,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--cells", type=int, default=N_CELLS_1D, help="cells per direction (profiling runs a smaller case)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
