@@ -194,28 +194,17 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def run_gpu(args, rank, world, local_rank):
-    import torch
-    from pvcriemannsolvers_gb300 import Lobatto, build, cases, mesh as meshlib
-    build.build()
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-    torch.cuda.set_device(local_rank)
-    dev = torch.device("cuda", local_rank)
-    m = meshlib.box((args.cells,) * 3, lengths=(10.0,) * 3, periodic=(True,) * 3)
-    sysm = Lobatto(m, DEGREE, "rusanov", cfl=CFL, device=local_rank)
+def measure_form(args, torch, dist, dev, local_rank, m, u0, precision):
+    """Time one precision form: device-resident stepping, kernel times, e2e."""
+    from pvcriemannsolvers_gb300 import Lobatto
+    world = dist.get_world_size() if dist else 1
+    sysm = Lobatto(m, DEGREE, "rusanov", cfl=CFL, device=local_rank, precision=precision)
     stream = torch.cuda.Stream(device=dev)
     sysm.set_stream(stream.cuda_stream)
-    x = meshlib.node_coordinates(m, DEGREE).reshape(-1, 3)
-    u0 = np.ascontiguousarray(cases.vortex_ic(x).ravel())
-    del x
     L = u0.size
     sysm.SetSolutionColumn(u0)
-    # warm-up (also builds the step graph)
     t = sysm.advance(args.warmup, 1e9, 3, 0.0)
     sysm.synchronize()
-    # ---- device-resident timed region
     if dist:
         dist.barrier()
     torch.cuda.synchronize(dev)
@@ -234,12 +223,9 @@ def run_gpu(args, rank, world, local_rank):
         tt = torch.tensor([ms], dtype=torch.float64, device=dev)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         ms = float(tt.item())
-    value = 3 * L * args.steps * world / (ms * 1e-3)
     sol = sysm.GetSolutionColumn()
-    l2_exact = density_l2_vs_exact(sol, m, t)
-    # ---- kernel times for the roofline (CUDA events on the handle stream)
     kt = sysm.kernel_times(reps=5)
-    # ---- end to end through the C ABI with pinned host buffers
+    # end to end through the C ABI with pinned host buffers
     host_in = torch.empty(L, dtype=torch.float64, pin_memory=True).numpy()
     host_out = torch.empty(L, dtype=torch.float64, pin_memory=True).numpy()
     host_in[:] = sol
@@ -258,50 +244,90 @@ def run_gpu(args, rank, world, local_rank):
         tt = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         e2e_s = float(tt.item())
-    e2e_value = 3 * L * args.steps * world / e2e_s
-    # ---- roofline of the dominant kernel
-    hbm_peak, peak_src = measured_peaks()
-    fp64_peak = fp64_peak_tflops(torch, dev)
-    cells = m.n_cells
+    sysm.close()
+    return {"value": 3 * L * args.steps * world / (ms * 1e-3), "ms_per_step": ms / args.steps,
+            "e2e": 3 * L * args.steps * world / e2e_s, "launches": launches, "kernel_ms": kt,
+            "clocks": clocks.summary(), "solution": sol, "t": t}
+
+
+def roofline_of(kt, L, cells, hbm_peak, peak_src, fp64_peak, precision):
+    """Roofline of the dominant kernel (SURVEY 8(d) algorithmic counts)."""
     N = (DEGREE + 1) ** 3
+    qf = (DEGREE + 1) ** 2
     dom = "cell_update" if kt["cell_update"] >= kt["face_flux"] else "face_flux"
     if dom == "cell_update":
         alg_bytes = 24 * L + (192 + 24) * cells
-        alg_flops = (130 / K + 6 * (DEGREE + 1) + 4) * L
+        alg_flops = (4 if precision == "mixed" else (130 / K + 6 * (DEGREE + 1) + 4)) * L
     else:
-        qf = (DEGREE + 1) ** 2
         alg_bytes = 2 * K * 8 * 3 * cells * qf + K * 8 * 3 * cells * qf
         alg_flops = 3 * qf * 60 / (N * K) * L
     t_dom = kt[dom] * 1e-3
     achieved = alg_bytes / t_dom / 1e9
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved / hbm_peak, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
-                "traffic": None, "alg_bytes_per_launch": alg_bytes, "launch_ms": kt[dom],
-                "fp64": {"achieved": alg_flops / t_dom / 1e12, "peak": fp64_peak, "unit": "TFLOP/s",
-                         "frac": alg_flops / t_dom / 1e12 / fp64_peak,
-                         "peak_source": "measured in this run: cuBLAS DGEMM 4096^3",
-                         "alg_flops_per_launch": alg_flops},
-                "binding": "fp64 pipe (see fp64.frac)", "kernel_ms": kt}
+    return {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+            "frac": achieved / hbm_peak, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+            "traffic": None, "alg_bytes_per_launch": alg_bytes, "launch_ms": kt[dom],
+            "fp64": {"achieved": alg_flops / t_dom / 1e12, "peak": fp64_peak, "unit": "TFLOP/s",
+                     "frac": alg_flops / t_dom / 1e12 / fp64_peak,
+                     "peak_source": "measured in this run: cuBLAS DGEMM 4096^3",
+                     "alg_flops_per_launch": alg_flops},
+            "binding": "fp64 pipe (see fp64.frac)", "kernel_ms": kt}
+
+
+def run_gpu(args, rank, world, local_rank):
+    import torch
+    from pvcriemannsolvers_gb300 import build, cases, mesh as meshlib
+    build.build()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    m = meshlib.box((args.cells,) * 3, lengths=(10.0,) * 3, periodic=(True,) * 3)
+    x = meshlib.node_coordinates(m, DEGREE).reshape(-1, 3)
+    u0 = np.ascontiguousarray(cases.vortex_ic(x).ravel())
+    del x
+    L = u0.size
+    forms = ["fp64", "mixed"] if args.form == "both" else [args.form]
+    res = {f: measure_form(args, torch, dist, dev, local_rank, m, u0, f) for f in forms}
+    head = "mixed" if "mixed" in res else "fp64"
+    r = res[head]
+    accuracy = {"density_rel_l2_vs_exact": density_l2_vs_exact(r["solution"], m, r["t"]), "t_end": r["t"],
+                "steps": args.warmup + args.steps}
+    if "fp64" in res and "mixed" in res:
+        a, b = res["mixed"]["solution"].reshape(-1, K)[:, 0], res["fp64"]["solution"].reshape(-1, K)[:, 0]
+        accuracy["mixed_vs_fp64_density_rel_l2"] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+        accuracy["fp64_density_rel_l2_vs_exact"] = density_l2_vs_exact(res["fp64"]["solution"], m, res["fp64"]["t"])
+    hbm_peak, peak_src = measured_peaks()
+    fp64_peak = fp64_peak_tflops(torch, dev)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_sample()
         cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
     if rank == 0:
+        cfg = workload(args.cells)
+        cfg["form"] = "mixed (FP32 volume flux + contraction; FP64 Riemann fluxes, lift, RK)" if head == "mixed" \
+            else "plain FP64"
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": workload(args.cells),
-            "accuracy": {"density_rel_l2_vs_exact": l2_exact, "t_end": t},
-            "clocks": clocks.summary(),
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * L, "d2h_bytes_per_step": 8 * L,
+            "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64+f32" if head == "mixed" else "f64", "data": "synthetic",
+            "config": cfg,
+            "accuracy": accuracy,
+            "clocks": r["clocks"],
+            "e2e": {"value": r["e2e"], "unit": UNIT, "h2d_bytes_per_step": 8 * L, "d2h_bytes_per_step": 8 * L,
                     "path": "mcfd_set_solution (pinned host) + mcfd_advance(1) + mcfd_get_solution (pinned host)"},
-            "gpu_launches": launches,
-            "roofline": roofline,
+            "gpu_launches": r["launches"],
+            "roofline": roofline_of(r["kernel_ms"], L, m.n_cells, hbm_peak, peak_src, fp64_peak, head),
             "cpu_baseline": cpu,
         }
+        if head == "mixed" and "fp64" in res:
+            p = res["fp64"]
+            line["plain_fp64"] = {"value": p["value"], "ms_per_step": p["ms_per_step"], "e2e": p["e2e"],
+                                  "gpu_launches": p["launches"], "clocks": p["clocks"],
+                                  "roofline": roofline_of(p["kernel_ms"], L, m.n_cells, hbm_peak, peak_src,
+                                                          fp64_peak, "fp64")}
         print(json.dumps(line), flush=True)
-    sysm.close()
 
 
 def main():
@@ -312,6 +338,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--cells", type=int, default=N_CELLS_1D, help="cells per direction (profiling runs a smaller case)")
+    ap.add_argument("--form", default="both", choices=["both", "fp64", "mixed"],
+                    help="precision form(s) to time; the line's value is the mixed form when timed")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -140,7 +140,7 @@ int upload(mcfd_handle *h, T **dst, const std::vector<T> &src) {
 void release(mcfd_handle *h) {
   auto &m = h->mesh;
   auto &b = h->buf;
-  void *ptrs[] = {m.cell_geo, m.cell_rate, m.cell_flux, m.face_cells,
+  void *ptrs[] = {m.cell_geo, m.cell_geo32, m.cell_rate, m.cell_flux, m.face_cells,
                   m.face_group, m.face_geo, m.face_xyz, m.face_map, m.dmat,
                   m.bcs, b.u, b.u1, b.u2, b.res, b.flux, b.state};
   for (void *p : ptrs)
@@ -392,6 +392,13 @@ int build_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
   if (bad_match) return fail(h, MCFD_ERR_MESH, "a face point matches no node of its cells");
   // ---- upload
   int rc;
+  if (h->opt.precision == MCFD_MIXED) {
+    std::vector<float> geo32((size_t)d->n_cells * N * 10);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < d->n_cells * N; ++i)
+      for (int e = 0; e < 10; ++e) geo32[(size_t)i * 10 + e] = (float)geo[(size_t)i * 10 + e];
+    if ((rc = upload(h, &m.cell_geo32, geo32))) return rc;
+  }
   if ((rc = upload(h, &m.cell_geo, geo))) return rc;
   if ((rc = upload(h, &m.cell_rate, rate))) return rc;
   if ((rc = upload(h, &m.cell_flux, cflux))) return rc;
@@ -431,8 +438,8 @@ int mcfd_create(const mcfd_mesh_desc *mesh, const mcfd_options *options,
     return fail(nullptr, MCFD_ERR_UNSUPPORTED, "unknown scheme");
   if (options->riemann < MCFD_EXACT || options->riemann > MCFD_RUSANOV)
     return fail(nullptr, MCFD_ERR_ARGUMENT, "unknown Riemann solver");
-  if (options->precision != MCFD_FP64)
-    return fail(nullptr, MCFD_ERR_UNSUPPORTED, "precision form not built");
+  if (options->precision != MCFD_FP64 && options->precision != MCFD_MIXED)
+    return fail(nullptr, MCFD_ERR_UNSUPPORTED, "unknown precision form");
   int n_dev = 0;
   if (cudaGetDeviceCount(&n_dev) != cudaSuccess || n_dev <= options->device || options->device < 0)
     return fail(nullptr, MCFD_ERR_NO_DEVICE, "no CUDA device available");

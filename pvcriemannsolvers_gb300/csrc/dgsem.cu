@@ -66,6 +66,46 @@ struct CellArgs {
   int advance_time;
 };
 
+// FP64 <-> FP32 conversions on the integer pipes.  On this part the FP64
+// unit is the bottleneck and hardware F2F conversions issue there; these
+// follow the IEEE-754 binary64/binary32 layouts (round to nearest even) and
+// hand zeros, subnormals, infinities and NaNs (rare here) to the hardware
+// conversion.
+__device__ __forceinline__ float f64_to_f32(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7ff) - 1023 + 127;
+  if (e <= 0 || e >= 255) return __double2float_rn(x);
+  const unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
+  const unsigned long long rounded = mant + 0xFFFFFFFull + ((mant >> 29) & 1ull);
+  // a mantissa carry (rounded >> 29 == 2^23) increments the exponent field
+  const unsigned bits = ((unsigned)e << 23) + (unsigned)(rounded >> 29);
+  return __uint_as_float(((unsigned)(b >> 32) & 0x80000000u) | bits);
+}
+
+__device__ __forceinline__ double f32_to_f64(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) {
+    if ((b & 0x7fffffffu) == 0u) return __longlong_as_double((long long)(b & 0x80000000u) << 32);
+    return (double)f;
+  }
+  const unsigned long long r = ((unsigned long long)(b & 0x80000000u) << 32) |
+                               ((unsigned long long)(e + (1023u - 127u)) << 52) |
+                               ((unsigned long long)(b & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)r);
+}
+
+// x < 0 for a finite or infinite double, tested on the bit pattern.
+__device__ __forceinline__ bool negative64(double x) {
+  const long long b = __double_as_longlong(x);
+  return b < 0 && (b << 1) != 0;
+}
+
+// isfinite on the bit pattern (exponent field not all ones).
+__device__ __forceinline__ bool finite64(double x) {
+  return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff;
+}
+
 __device__ __forceinline__ void given_value(const BcDev &bc, const double *x,
                                             double t, double *g) {
   const double *src = bc.a;
@@ -85,14 +125,25 @@ __global__ void __launch_bounds__(256) face_flux_kernel(FaceArgs a) {
   double4 g = a.face_geo[gid];
   double n[3] = {g.x, g.y, g.z};
   const double *uh = a.u + (int64_t)cells.x * KN + map.x * kK;
-  Prim l = cons_to_prim(uh[0], uh[1], uh[2], uh[3], uh[4]);
+  double ch[kK];
+#pragma unroll
+  for (int k = 0; k < kK; ++k) ch[k] = uh[k];
   double out[kK];
   bool not_converged = false;
   if (cells.y >= 0) {
     const double *us = a.u + (int64_t)cells.y * KN + map.y * kK;
-    Prim r = cons_to_prim(us[0], us[1], us[2], us[3], us[4]);
-    flux_upwind<R>(l, r, n, out, &not_converged);
+    double cs[kK];
+#pragma unroll
+    for (int k = 0; k < kK; ++k) cs[k] = us[k];
+    if constexpr (R == kRusanov) {
+      flux_rusanov_cons(ch, cs, n, out);
+    } else {
+      Prim l = cons_to_prim(ch[0], ch[1], ch[2], ch[3], ch[4]);
+      Prim r = cons_to_prim(cs[0], cs[1], cs[2], cs[3], cs[4]);
+      flux_upwind<R>(l, r, n, out, &not_converged);
+    }
   } else {
+    Prim l = cons_to_prim(ch[0], ch[1], ch[2], ch[3], ch[4]);
     int grp = a.face_group[f];
     if (grp >= 0 && grp < a.n_groups && a.bcs[grp].kind != kBcNone) {
       const BcDev &bc = a.bcs[grp];
@@ -134,27 +185,24 @@ cell_update_kernel(CellArgs a) {
     for (int e = 0; e < 9; ++e) A[e] = geo[e];
     Prim w = cons_to_prim(uq[0], uq[1], uq[2], uq[3], uq[4]);
     // Contravariant flux Ft[:, e] = sum_d F[:, d] A[d][e], F = GetFluxMatrix
-    // (types.hpp:322-333).  With V_e = sum_d u_d A[d][e]:
-    //   Ft[0][e] = rho V_e, Ft[1+x][e] = m_x V_e + p A[x][e], Ft[4][e] = (E+p) V_e
-    // A clamped state (zero primitives) keeps only the mass row m . A.
+    // (types.hpp:322-333).  With V_e = sum_d u_d A[d][e] (u = primitive
+    // velocity) and m the conservative momentum:
+    //   Ft[0][e] = m . A[:, e], Ft[1+x][e] = m_x V_e + p A[x][e],
+    //   Ft[4][e] = (E + p) V_e.
+    // For a converted state (rho > 0) the mass row equals rho V_e; clamped
+    // (all-zero primitives) and rho == 0 (unconverted) states take the
+    // general form.
     double ft[15];
-    if (w.rho != 0) {
+    const bool converted = w.rho != 0;
 #pragma unroll
-      for (int e = 0; e < 3; ++e) {
-        double ve = w.u * A[0 * 3 + e] + w.v * A[1 * 3 + e] + w.w * A[2 * 3 + e];
-        ft[0 * 3 + e] = w.rho * ve;
-        ft[1 * 3 + e] = uq[1] * ve + w.p * A[0 * 3 + e];
-        ft[2 * 3 + e] = uq[2] * ve + w.p * A[1 * 3 + e];
-        ft[3 * 3 + e] = uq[3] * ve + w.p * A[2 * 3 + e];
-        ft[4 * 3 + e] = (uq[4] + w.p) * ve;
-      }
-    } else {
-#pragma unroll
-      for (int e = 0; e < 3; ++e) {
-        ft[e] = uq[1] * A[0 * 3 + e] + uq[2] * A[1 * 3 + e] + uq[3] * A[2 * 3 + e];
-#pragma unroll
-        for (int r = 1; r < kK; ++r) ft[r * 3 + e] = 0;
-      }
+    for (int e = 0; e < 3; ++e) {
+      double ve = w.u * A[0 * 3 + e] + w.v * A[1 * 3 + e] + w.w * A[2 * 3 + e];
+      ft[0 * 3 + e] = converted ? w.rho * ve
+                                : uq[1] * A[0 * 3 + e] + uq[2] * A[1 * 3 + e] + uq[3] * A[2 * 3 + e];
+      ft[1 * 3 + e] = uq[1] * ve + w.p * A[0 * 3 + e];
+      ft[2 * 3 + e] = uq[2] * ve + w.p * A[1 * 3 + e];
+      ft[3 * 3 + e] = uq[3] * ve + w.p * A[2 * 3 + e];
+      ft[4 * 3 + e] = (uq[4] + w.p) * ve;
     }
 #pragma unroll
     for (int r = 0; r < 15; ++r) s_ft[lc][r][q] = ft[r];
@@ -227,6 +275,126 @@ cell_update_kernel(CellArgs a) {
   if (a.advance_time && blockIdx.x == 0 && tid == 0) a.state->t += a.state->dt;
 }
 
+// Mixed-precision form of cell_update_kernel.  In FP32: the volume flux and
+// its contravariant transform (FP32 copy of w J^-1), the sum-factorised GLL
+// differentiation, the lift of the (FP64-computed) face fluxes and the
+// mass-scaled increment dt * R / w.  In FP64: the sign checks of density and
+// energy (exact, on the bit patterns), the stage accumulation u + dt R and the
+// RK combinations.  Conversions between the two formats run on the integer
+// pipes, so a node issues ~15 FP64 instructions instead of ~145.
+template <int Q, int STAGE>
+__global__ void __launch_bounds__(CellCfg<Q>::kThreads)
+cell_update_mixed_kernel(CellArgs a, const float *__restrict__ geo32) {
+  constexpr int N = Q * Q * Q, QF = Q * Q, KN = kK * N;
+  constexpr int CPB = CellCfg<Q>::kCells;
+  __shared__ float s_ft[CPB][15][N];
+  __shared__ float s_d[Q * Q];
+  const int tid = threadIdx.x;
+  if (tid < Q * Q) s_d[tid] = f64_to_f32(a.dmat[tid]);
+  const int lc = tid / N, q = tid - lc * N;
+  const int64_t c = (int64_t)blockIdx.x * CPB + lc;
+  const bool active = c < a.n_cells;
+  double uq[kK];
+  float inv_w = 0.f;
+  if (active) {
+    const double *up = a.u_in + c * KN + q * kK;
+#pragma unroll
+    for (int k = 0; k < kK; ++k) uq[k] = up[k];
+    const float *g = geo32 + (c * N + q) * 10;
+    float A[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) A[e] = g[e];
+    inv_w = g[9];
+    const float r = f64_to_f32(uq[0]), mx = f64_to_f32(uq[1]), my = f64_to_f32(uq[2]),
+                mz = f64_to_f32(uq[3]), en = f64_to_f32(uq[4]);
+    // ConservativeToPrimitive with its clamp; rho < 0 and E < 0 are decided
+    // on the FP64 values, p < 0 in FP32.
+    float pr = r, u = mx, v = my, w = mz, p = en;
+    if (negative64(uq[0]) || negative64(uq[4])) {
+      pr = u = v = w = p = 0.f;
+    } else if (uq[0] != 0) {
+      float inv = 1.0f / r;
+      u = mx * inv; v = my * inv; w = mz * inv;
+      p = (en - r * (0.5f * (u * u + v * v + w * w))) * (float)kGm1;
+      if (p < 0.f) pr = u = v = w = p = 0.f;
+    }
+    const bool converted = pr != 0.f;
+    float ft[15];
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+      float ve = u * A[0 * 3 + e] + v * A[1 * 3 + e] + w * A[2 * 3 + e];
+      ft[0 * 3 + e] = converted ? pr * ve
+                                : mx * A[0 * 3 + e] + my * A[1 * 3 + e] + mz * A[2 * 3 + e];
+      ft[1 * 3 + e] = mx * ve + p * A[0 * 3 + e];
+      ft[2 * 3 + e] = my * ve + p * A[1 * 3 + e];
+      ft[3 * 3 + e] = mz * ve + p * A[2 * 3 + e];
+      ft[4 * 3 + e] = (en + p) * ve;
+    }
+#pragma unroll
+    for (int rr = 0; rr < 15; ++rr) s_ft[lc][rr][q] = ft[rr];
+  }
+  __syncthreads();
+  if (!active) return;
+  const int i = q / QF, j = (q / Q) % Q, k = q % Q;
+  float res[kK];
+#pragma unroll
+  for (int rr = 0; rr < kK; ++rr) {
+    float s = 0.f;
+#pragma unroll
+    for (int m = 0; m < Q; ++m) {
+      s = fmaf(s_ft[lc][rr * 3 + 0][(m * Q + j) * Q + k], s_d[m * Q + i], s);
+      s = fmaf(s_ft[lc][rr * 3 + 1][(i * Q + m) * Q + k], s_d[m * Q + j], s);
+      s = fmaf(s_ft[lc][rr * 3 + 2][(i * Q + j) * Q + m], s_d[m * Q + k], s);
+    }
+    res[rr] = s;
+  }
+  const int32_t *cf = a.cell_flux + c * 6 * QF;
+  auto lift = [&](int side, int t) {
+    int32_t vv = cf[side * QF + t];
+    if (vv == INT32_MIN) return;
+    const double *fl = a.flux + (int64_t)(vv >= 0 ? vv : ~vv) * kK;
+    const float sign = vv >= 0 ? -1.f : 1.f;
+#pragma unroll
+    for (int rr = 0; rr < kK; ++rr) res[rr] = fmaf(sign, f64_to_f32(fl[rr]), res[rr]);
+  };
+  if (k == 0) lift(0, i * Q + j);
+  if (k == Q - 1) lift(5, i * Q + j);
+  if (j == 0) lift(1, i * Q + k);
+  if (j == Q - 1) lift(3, i * Q + k);
+  if (i == 0) lift(4, j * Q + k);
+  if (i == Q - 1) lift(2, j * Q + k);
+  double *out = a.u_out + c * KN + q * kK;
+  bool bad = false;
+  if (STAGE == kStageResidual) {
+#pragma unroll
+    for (int rr = 0; rr < kK; ++rr) {
+      double val = f32_to_f64(res[rr] * inv_w);
+      bad |= !finite64(val);
+      out[rr] = val;
+    }
+  } else {
+    const float wdt = inv_w * f64_to_f32(a.state->dt);
+#pragma unroll
+    for (int rr = 0; rr < kK; ++rr) {
+      double next = uq[rr] + f32_to_f64(res[rr] * wdt);
+      double val;
+      if (STAGE == kStageEuler) {
+        val = next;
+      } else if (STAGE == kStageRk2Last) {
+        val = (next + a.u0[c * KN + q * kK + rr]) * 0.5;
+      } else if (STAGE == kStageRk3Mid) {
+        val = (a.u0[c * KN + q * kK + rr] * 3 + next) * 0.25;
+      } else {
+        val = (next * 2 + a.u0[c * KN + q * kK + rr]) * (1.0 / 3.0);
+      }
+      bad |= !finite64(val);
+      out[rr] = val;
+    }
+  }
+  if (bad) atomicOr(&a.state->status, (unsigned)kStatusNonFinite);
+  if (a.advance_time && blockIdx.x == 0 && tid == 0) a.state->t += a.state->dt;
+}
+
 // dt: max over nodes of max(1e-5, max_speed) / length, as the bit pattern of
 // a positive double (monotone as an unsigned integer).
 template <int Q>
@@ -242,6 +410,35 @@ dt_reduce_kernel(const double *u, const double *cell_rate, int64_t n_nodes,
     double c = sound_speed(w);
     double speed = c + sqrt(w.u * w.u + w.v * w.v + w.w * w.w);
     rate = fmax(speed, 1e-5) * cell_rate[gid / N];
+  }
+  for (int o = 16; o > 0; o >>= 1) rate = fmax(rate, __shfl_xor_sync(0xffffffffu, rate, o));
+  if ((threadIdx.x & 31) == 0 && rate > 0)
+    atomicMax(&state->max_rate_bits, (unsigned long long)__double_as_longlong(rate));
+}
+
+// Mixed-precision dt reduction: wave speeds in FP32.
+template <int Q>
+__global__ void __launch_bounds__(256)
+dt_reduce_mixed_kernel(const double *u, const double *cell_rate, int64_t n_nodes,
+                       DevState *state) {
+  constexpr int N = Q * Q * Q;
+  int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double rate = 0;
+  if (gid < n_nodes) {
+    const double *p = u + gid * kK;
+    float r = (float)p[0], mx = (float)p[1], my = (float)p[2], mz = (float)p[3],
+          en = (float)p[4];
+    float speed = 0.f;
+    if (r > 0.f && en >= 0.f) {
+      float inv = 1.0f / r;
+      float uu = (mx * mx + my * my + mz * mz) * inv * inv;
+      float pp = (en - 0.5f * r * uu) * (float)kGm1;
+      float c = pp > 0.f ? sqrtf((float)kGamma * pp * inv) : 0.f;
+      speed = pp >= 0.f ? c + sqrtf(uu) : 0.f;
+    } else if (r == 0.f && en >= 0.f) {
+      speed = sqrtf(mx * mx + my * my + mz * mz);
+    }
+    rate = (double)fmaxf(speed, 1e-5f) * cell_rate[gid / N];
   }
   for (int o = 16; o > 0; o >>= 1) rate = fmax(rate, __shfl_xor_sync(0xffffffffu, rate, o));
   if ((threadIdx.x & 31) == 0 && rate > 0)
@@ -289,8 +486,26 @@ void cell_launch(mcfd_handle *h, const CellArgs &ca) {
   cell_update_kernel<Q, S><<<(unsigned)blocks, CellCfg<Q>::kThreads, 0, h->stream>>>(ca);
 }
 
+template <int Q, int S>
+void cell_launch_mixed(mcfd_handle *h, const CellArgs &ca) {
+  constexpr int CPB = CellCfg<Q>::kCells;
+  int64_t blocks = (ca.n_cells + CPB - 1) / CPB;
+  cell_update_mixed_kernel<Q, S><<<(unsigned)blocks, CellCfg<Q>::kThreads, 0, h->stream>>>(
+      ca, h->mesh.cell_geo32);
+}
+
 template <int Q>
 void cell_dispatch_s(mcfd_handle *h, int stage, const CellArgs &ca) {
+  if (h->opt.precision == 1) {
+    switch (stage) {
+      case kStageEuler: cell_launch_mixed<Q, kStageEuler>(h, ca); break;
+      case kStageRk2Last: cell_launch_mixed<Q, kStageRk2Last>(h, ca); break;
+      case kStageRk3Mid: cell_launch_mixed<Q, kStageRk3Mid>(h, ca); break;
+      case kStageRk3Last: cell_launch_mixed<Q, kStageRk3Last>(h, ca); break;
+      default: cell_launch_mixed<Q, kStageResidual>(h, ca); break;
+    }
+    return;
+  }
   switch (stage) {
     case kStageEuler: cell_launch<Q, kStageEuler>(h, ca); break;
     case kStageRk2Last: cell_launch<Q, kStageRk2Last>(h, ca); break;
@@ -340,6 +555,15 @@ int launch_dt(mcfd_handle *h, const double *u) {
   const Mesh &m = h->mesh;
   int64_t nodes = m.n_cells * m.n;
   unsigned blocks = (unsigned)((nodes + 255) / 256);
+  if (h->opt.precision == 1) {
+    switch (m.q) {
+      case 2: dt_reduce_mixed_kernel<2><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state); break;
+      case 3: dt_reduce_mixed_kernel<3><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state); break;
+      default: dt_reduce_mixed_kernel<4><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state); break;
+    }
+    dt_finalize_kernel<<<1, 1, 0, h->stream>>>(h->buf.state);
+    return 2;
+  }
   switch (m.q) {
     case 2: dt_reduce_kernel<2><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state); break;
     case 3: dt_reduce_kernel<3><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state); break;

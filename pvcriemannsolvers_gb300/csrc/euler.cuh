@@ -61,7 +61,12 @@ enum StatusBits : unsigned {
 
 struct Prim {
   double rho, u, v, w, p;
+  double rinv;  // 1 / rho when rho > 0, else 0 (saves divisions downstream)
 };
+
+MCFD_HD Prim make_prim(double rho, double u, double v, double w, double p) {
+  return Prim{rho, u, v, w, p, rho > 0 ? 1.0 / rho : 0.0};
+}
 
 // ConservativeToPrimitive with SetZeroIfNegative (types.hpp:194-202,288-301):
 // a negative density or (first) energy, or a negative pressure after the
@@ -69,16 +74,17 @@ struct Prim {
 // divisions share one reciprocal.
 MCFD_HD Prim cons_to_prim(double r, double mx, double my, double mz,
                           double e) {
-  Prim w{r, mx, my, mz, e};
-  if (r < 0 || e < 0) return Prim{0, 0, 0, 0, 0};
+  Prim w{r, mx, my, mz, e, 0.0};
+  if (r < 0 || e < 0) return Prim{0, 0, 0, 0, 0, 0};
   if (r != 0) {
     double inv = 1.0 / r;
+    w.rinv = inv;
     w.u = mx * inv;
     w.v = my * inv;
     w.w = mz * inv;
     double ke = 0.5 * (w.u * w.u + w.v * w.v + w.w * w.w);
     w.p = (e - r * ke) * kGm1;
-    if (w.p < 0) return Prim{0, 0, 0, 0, 0};
+    if (w.p < 0) return Prim{0, 0, 0, 0, 0, 0};
   }
   return w;
 }
@@ -89,7 +95,7 @@ MCFD_HD double kinetic(const Prim &w) {
 
 // GetSpeedOfSound(rho, p) (types.hpp:252-254).
 MCFD_HD double sound_speed(const Prim &w) {
-  return (w.rho > 0 && w.p > 0) ? sqrt(kGamma * w.p / w.rho) : 0.0;
+  return (w.rho > 0 && w.p > 0) ? sqrt(kGamma * w.p * w.rinv) : 0.0;
 }
 
 // Total energy of a primitive state (PrimitiveToConservative, types.hpp:302-311).
@@ -109,6 +115,33 @@ MCFD_HD void normal_flux(const Prim &w, double e, const double *n, double un,
 }
 
 // ---------------------------------------------------------------- Rusanov
+// Rusanov on conservative inputs: for a converted state (rho > 0, p >= 0)
+// F_n = (m.n, m (m.n)/rho + p n, (E + p)(m.n)/rho) and U is the input itself,
+// so no velocity vector is formed (u = m/rho appears only through m.n/rho).
+// Degenerate (clamped or rho == 0) states fall back to the primitive form.
+// Equal to flux_rusanov on the converted primitives up to rounding.
+MCFD_HD bool rusanov_side(const double *c, const double *n, double *f,
+                          double *speed) {
+  double r = c[0], e = c[4];
+  if (!(r > 0) || e < 0) return false;
+  double rinv = 1.0 / r;
+  double m2 = c[1] * c[1] + c[2] * c[2] + c[3] * c[3];
+  double p = (e - 0.5 * m2 * rinv) * kGm1;
+  if (p < 0) return false;
+  double mn = c[1] * n[0] + c[2] * n[1] + c[3] * n[2];
+  double un = mn * rinv;
+  f[0] = mn;
+  f[1] = c[1] * un + p * n[0];
+  f[2] = c[2] * un + p * n[1];
+  f[3] = c[3] * un + p * n[2];
+  f[4] = (e + p) * un;
+  *speed = fabs(un) + (p > 0 ? sqrt(kGamma * p * rinv) : 0.0);
+  return true;
+}
+
+MCFD_HD void flux_rusanov_cons(const double *cl, const double *cr,
+                               const double *n, double *f);
+
 // Local Lax-Friedrichs (python/riemann.py:457-476): average flux minus
 // lambda_max / 2 * (U_R - U_L), lambda_max = max(|u_n| + a) over both sides.
 MCFD_HD void flux_rusanov(const Prim &l, const Prim &r, const double *n,
@@ -126,6 +159,19 @@ MCFD_HD void flux_rusanov(const Prim &l, const Prim &r, const double *n,
   f[2] = 0.5 * (fr[2] + fl[2]) - h * (r.rho * r.v - l.rho * l.v);
   f[3] = 0.5 * (fr[3] + fl[3]) - h * (r.rho * r.w - l.rho * l.w);
   f[4] = 0.5 * (fr[4] + fl[4]) - h * (er - el);
+}
+
+MCFD_HD void flux_rusanov_cons(const double *cl, const double *cr,
+                               const double *n, double *f) {
+  double fl[kK], fr[kK], sl, sr;
+  if (rusanov_side(cl, n, fl, &sl) && rusanov_side(cr, n, fr, &sr)) {
+    double h = 0.5 * fmax(sl, sr);
+#pragma unroll
+    for (int k = 0; k < kK; ++k) f[k] = 0.5 * (fr[k] + fl[k]) - h * (cr[k] - cl[k]);
+    return;
+  }
+  flux_rusanov(cons_to_prim(cl[0], cl[1], cl[2], cl[3], cl[4]),
+               cons_to_prim(cr[0], cr[1], cr[2], cr[3], cr[4]), n, f);
 }
 
 // ---------------------------------------------------------------- HLLC
@@ -228,8 +274,8 @@ MCFD_HD void flux_roe(const Prim &l, const Prim &r, const double *n,
   normal_flux(l, el, n, unl, fl);
   normal_flux(r, er, n, unr, fr);
   for (int k = 0; k < kK; ++k) f[k] = (fl[k] + fr[k]) / 2;
-  double h0_l = kGamma * l.p / l.rho / kGm1 + kinetic(l);
-  double h0_r = kGamma * r.p / r.rho / kGm1 + kinetic(r);
+  double h0_l = kGammaOverGm1 * l.p * l.rinv + kinetic(l);
+  double h0_r = kGammaOverGm1 * r.p * r.rinv + kinetic(r);
   double sl = sqrt(l.rho), sr = sqrt(r.rho);
   double inv_sum = 1.0 / (sl + sr);
   double rho = sl * sr;
@@ -433,6 +479,7 @@ MCFD_HD void flux_exact(const Prim &l, const Prim &r, const double *n,
   // velocity = s.u n + (u_t of the passive side)
   Prim w;
   w.rho = s.rho;
+  w.rinv = s.rho > 0 ? 1.0 / s.rho : 0.0;
   w.p = s.p;
   w.u = t.u + (s.u - untan) * n[0];
   w.v = t.v + (s.u - untan) * n[1];
@@ -499,7 +546,7 @@ MCFD_HD void flux_boundary(int kind, const Prim &in, const double *g,
       double mach = sqrt((g[4] / t_b - 1) / kGm1Over2);
       double p_b = g[0] / pow(1 + kGm1Over2 * mach * mach, kGammaOverGm1);
       double speed = mach * c_b;
-      Prim w{p_b / kGasR / t_b, g[1] * speed, g[2] * speed, g[3] * speed, p_b};
+      Prim w = make_prim(p_b / kGasR / t_b, g[1] * speed, g[2] * speed, g[3] * speed, p_b);
       double un = w.u * n[0] + w.v * n[1] + w.w * n[2];
       normal_flux(w, prim_energy(w), n, un, f);
       break;
@@ -509,6 +556,7 @@ MCFD_HD void flux_boundary(int kind, const Prim &in, const double *g,
       Prim w = in;
       w.p = g[4];
       w.rho = w.p / rt;
+      w.rinv = w.rho > 0 ? 1.0 / w.rho : 0.0;
       double un = w.u * n[0] + w.v * n[1] + w.w * n[2];
       normal_flux(w, prim_energy(w), n, un, f);
       break;

@@ -50,6 +50,7 @@ struct Mesh {
   int n_groups = 0;
   // device arrays
   double *cell_geo = nullptr;       // [cells][N][10]: w*J^-1 (3x3 row-major), 1/w
+  float *cell_geo32 = nullptr;      // [cells][N][10]: FP32 w*J^-1, 1/w (mixed form only)
   double *cell_rate = nullptr;      // [cells] 1 / length  (length = cbrt(V)/2)
   int32_t *cell_flux = nullptr;     // [cells][6][QF] flux slot: >=0 subtract, <0 add (~slot), INT32_MIN none
   int2 *face_cells = nullptr;       // [faces] holder, sharer

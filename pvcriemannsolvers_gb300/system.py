@@ -66,10 +66,15 @@ class Lobatto:
     """DGSEM (dg::Lobatto, kLocal = false) Euler system on one GPU."""
 
     def __init__(self, mesh: Mesh, degree: int, riemann: str | int = "rusanov",
-                 cfl: float = 0.0, device: int = 0):
+                 cfl: float = 0.0, device: int = 0, precision: str = "fp64"):
+        """precision: "fp64" (plain form) or "mixed" (FP32 volume flux and
+        contraction; FP64 Riemann fluxes, lift and RK accumulation)."""
         lib = capi.load()
         self.mesh = mesh
         self.degree = int(degree)
+        if precision not in ("fp64", "mixed"):
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        self.precision = precision
         self.riemann = capi.RIEMANN[riemann] if isinstance(riemann, str) else int(riemann)
         self._keep = [
             np.ascontiguousarray(mesh.xyz, dtype=np.float64),
@@ -95,7 +100,7 @@ class Lobatto:
         opt.degree = self.degree
         opt.scheme = capi.DGSEM
         opt.riemann = self.riemann
-        opt.precision = capi.FP64
+        opt.precision = capi.FP64 if precision == "fp64" else capi.MIXED
         opt.cfl = float(cfl)
         opt.device = int(device)
         h = C.c_void_p()
