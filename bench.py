@@ -250,8 +250,19 @@ def measure_form(args, torch, dist, dev, local_rank, m, u0, precision):
             "clocks": clocks.summary(), "solution": sol, "t": t}
 
 
+# DRAM bytes (read + write) per launch measured by one ncu capture on the
+# 40^3 p = 3 case (64 000 cells); scaled linearly with the cell count.
+NCU_TRAFFIC_40 = {
+    ("mixed", "face_flux"): 280.143872e6 + 97.142016e6,
+    ("mixed", "cell_update"): 476.211456e6 + 140.708608e6,
+    ("fp64", "face_flux"): 280.143872e6 + 97.142016e6,
+    ("fp64", "cell_update"): 640.078336e6 + 146.893312e6,
+}
+NCU_CELLS = 40 ** 3
+
+
 def roofline_of(kt, L, cells, hbm_peak, peak_src, fp64_peak, precision):
-    """Roofline of the dominant kernel (SURVEY 8(d) algorithmic counts)."""
+    """Roofline of the dominant kernel (algorithmic counts per launch)."""
     N = (DEGREE + 1) ** 3
     qf = (DEGREE + 1) ** 2
     dom = "cell_update" if kt["cell_update"] >= kt["face_flux"] else "face_flux"
@@ -263,9 +274,12 @@ def roofline_of(kt, L, cells, hbm_peak, peak_src, fp64_peak, precision):
         alg_flops = 3 * qf * 60 / (N * K) * L
     t_dom = kt[dom] * 1e-3
     achieved = alg_bytes / t_dom / 1e9
+    traffic = NCU_TRAFFIC_40.get((precision, dom))
+    traffic = traffic * cells / NCU_CELLS if traffic is not None and DEGREE == 3 else None
     return {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
             "frac": achieved / hbm_peak, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
-            "traffic": None, "alg_bytes_per_launch": alg_bytes, "launch_ms": kt[dom],
+            "traffic": traffic, "traffic_source": "ncu dram__bytes_read+write on 40^3, scaled by cells",
+            "alg_bytes_per_launch": alg_bytes, "launch_ms": kt[dom],
             "fp64": {"achieved": alg_flops / t_dom / 1e12, "peak": fp64_peak, "unit": "TFLOP/s",
                      "frac": alg_flops / t_dom / 1e12 / fp64_peak,
                      "peak_source": "measured in this run: cuBLAS DGEMM 4096^3",

@@ -67,32 +67,38 @@ struct CellArgs {
 };
 
 // FP64 <-> FP32 conversions on the integer pipes.  On this part the FP64
-// unit is the bottleneck and hardware F2F conversions issue there; these
-// follow the IEEE-754 binary64/binary32 layouts (round to nearest even) and
-// hand zeros, subnormals, infinities and NaNs (rare here) to the hardware
-// conversion.
+// unit is the bottleneck and hardware F2F conversions issue there.  These
+// follow the IEEE-754 binary64/binary32 layouts with branch-free selects:
+// round to nearest even, subnormal results flushed to a signed zero,
+// overflow to infinity, NaN kept NaN.
 __device__ __forceinline__ float f64_to_f32(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const int e = (int)((b >> 52) & 0x7ff) - 1023 + 127;
-  if (e <= 0 || e >= 255) return __double2float_rn(x);
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  const int ex = (int)((b >> 52) & 0x7ff);
+  const int e = ex - (1023 - 127);
   const unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
   const unsigned long long rounded = mant + 0xFFFFFFFull + ((mant >> 29) & 1ull);
   // a mantissa carry (rounded >> 29 == 2^23) increments the exponent field
-  const unsigned bits = ((unsigned)e << 23) + (unsigned)(rounded >> 29);
-  return __uint_as_float(((unsigned)(b >> 32) & 0x80000000u) | bits);
+  unsigned bits = ((unsigned)e << 23) + (unsigned)(rounded >> 29);
+  bits = e <= 0 ? 0u : bits;
+  const unsigned special = 0x7f800000u | ((ex == 0x7ff && mant != 0ull) ? 0x400000u : 0u);
+  bits = e >= 255 ? special : bits;
+  return __uint_as_float(sign | bits);
 }
 
 __device__ __forceinline__ double f32_to_f64(float f) {
   const unsigned b = __float_as_uint(f);
   const unsigned e = (b >> 23) & 0xffu;
-  if (e == 0u || e == 0xffu) {
-    if ((b & 0x7fffffffu) == 0u) return __longlong_as_double((long long)(b & 0x80000000u) << 32);
-    return (double)f;
-  }
-  const unsigned long long r = ((unsigned long long)(b & 0x80000000u) << 32) |
-                               ((unsigned long long)(e + (1023u - 127u)) << 52) |
-                               ((unsigned long long)(b & 0x7fffffu) << 29);
-  return __longlong_as_double((long long)r);
+  const unsigned long long m = (unsigned long long)(b & 0x7fffffu) << 29;
+  unsigned long long r = ((unsigned long long)(e + (1023u - 127u)) << 52) | m;
+  r = e == 0u ? 0ull : r;
+  r = e == 0xffu ? ((0x7ffull << 52) | m) : r;
+  return __longlong_as_double((long long)(r | ((unsigned long long)(b & 0x80000000u) << 32)));
+}
+
+// x != 0 on the bit pattern.
+__device__ __forceinline__ bool nonzero64(double x) {
+  return (__double_as_longlong(x) << 1) != 0;
 }
 
 // x < 0 for a finite or infinite double, tested on the bit pattern.
@@ -136,7 +142,12 @@ __global__ void __launch_bounds__(256) face_flux_kernel(FaceArgs a) {
 #pragma unroll
     for (int k = 0; k < kK; ++k) cs[k] = us[k];
     if constexpr (R == kRusanov) {
-      flux_rusanov_cons(ch, cs, n, out);
+      // already multiplied by the face weight
+      flux_rusanov_cons_weighted(ch, cs, n, g.w, out);
+      double *dst = a.flux + gid * kK;
+#pragma unroll
+      for (int k = 0; k < kK; ++k) dst[k] = out[k];
+      return;
     } else {
       Prim l = cons_to_prim(ch[0], ch[1], ch[2], ch[3], ch[4]);
       Prim r = cons_to_prim(cs[0], cs[1], cs[2], cs[3], cs[4]);
@@ -312,7 +323,7 @@ cell_update_mixed_kernel(CellArgs a, const float *__restrict__ geo32) {
     float pr = r, u = mx, v = my, w = mz, p = en;
     if (negative64(uq[0]) || negative64(uq[4])) {
       pr = u = v = w = p = 0.f;
-    } else if (uq[0] != 0) {
+    } else if (nonzero64(uq[0])) {
       float inv = 1.0f / r;
       u = mx * inv; v = my * inv; w = mz * inv;
       p = (en - r * (0.5f * (u * u + v * v + w * w))) * (float)kGm1;
