@@ -123,6 +123,31 @@ int orc_rk_update(const orc_mesh *m, int riemann, int n_bc, const orc_bc *bcs,
 int orc_rk_update_linear(int order, int64_t n, const double *a, double t,
                          double dt, double *u);
 
+/* ---- WENO limiter on DGSEM cells (orc_weno.c) ---- */
+enum { ORC_LIMITER_NONE = 0, ORC_LIMITER_LAZY = 1, ORC_LIMITER_DETECT_LAZY = 2 };
+typedef struct orc_limiter orc_limiter;
+orc_limiter *orc_limiter_create(const orc_mesh *m);
+void orc_limiter_destroy(orc_limiter *l);
+int orc_modal_count(int p);
+int orc_limiter_modal_count(const orc_limiter *l);
+/* modal coefficients [cells][K][M] of a nodal column */
+void orc_limiter_modal(const orc_limiter *l, const double *u, double *modal);
+/* limiter::Reconstruct in place; returns the number of reconstructed cells */
+int64_t orc_limit(const orc_limiter *l, int mode, double w0, double eps,
+                  double *u);
+/* GetSmoothness (weno.hpp:78-95) of modal coeff cm [K][M] on cell c */
+void orc_limiter_smoothness(const orc_limiter *l, int64_t c, const double *cm,
+                            double *beta);
+/* jump-detector flags [cells]; returns the troubled count */
+int64_t orc_limiter_troubled(const orc_limiter *l, const double *u,
+                             char *flags);
+/* RungeKutta<order>::Update on WithLimiter<dg::Lobatto>: the limiter runs
+ * after every SetSolutionColumn (spatial/with_limiter.hpp:56-59). */
+int orc_rk_update_limited(const orc_mesh *m, int riemann, int n_bc,
+                          const orc_bc *bcs, int order, double t, double dt,
+                          double *u, const orc_limiter *l, int mode, double w0,
+                          double eps);
+
 #ifdef __cplusplus
 }
 #endif

@@ -235,3 +235,72 @@ def rk_update_linear(order: int, a: np.ndarray, t: float, dt: float, u: np.ndarr
     u = np.array(u, dtype=np.float64, copy=True)
     load().orc_rk_update_linear(order, u.size, _p(a), t, dt, _p(u))
     return u
+
+
+LIMITER_NONE, LIMITER_LAZY, LIMITER_DETECT_LAZY = 0, 1, 2
+
+
+def _limiter_sigs(lib):
+    sig = {
+        "orc_limiter_create": (C.c_void_p, [C.c_void_p]),
+        "orc_limiter_destroy": (None, [C.c_void_p]),
+        "orc_modal_count": (C.c_int, [C.c_int]),
+        "orc_limiter_modal": (None, [C.c_void_p, _D, _D]),
+        "orc_limit": (C.c_int64, [C.c_void_p, C.c_int, C.c_double, C.c_double, _D]),
+        "orc_limiter_troubled": (C.c_int64, [C.c_void_p, _D, C.c_char_p]),
+        "orc_limiter_smoothness": (None, [C.c_void_p, C.c_int64, _D, _D]),
+        "orc_rk_update_limited": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(OrcBc), C.c_int, C.c_double,
+                                            C.c_double, _D, C.c_void_p, C.c_int, C.c_double, C.c_double]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+class Limiter:
+    """WENO limiter (weno::Lazy reconstruct, optional weno::Eigen detector) on
+    the DGSEM cells of an oracle Mesh."""
+
+    def __init__(self, mesh: "Mesh", mode: int = LIMITER_LAZY, w0: float = 0.001, eps: float = 1e-6):
+        self.lib = load()
+        _limiter_sigs(self.lib)
+        self.mesh = mesh
+        self._l = self.lib.orc_limiter_create(mesh._m)
+        self.mode, self.w0, self.eps = mode, w0, eps
+        self.m = int(self.lib.orc_modal_count(mesh.degree))
+
+    def __del__(self):
+        if getattr(self, "_l", None):
+            self.lib.orc_limiter_destroy(self._l)
+            self._l = None
+
+    def modal(self, u: np.ndarray) -> np.ndarray:
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        out = np.empty((self.mesh.n_cells, 5, self.m))
+        self.lib.orc_limiter_modal(self._l, _p(u), _p(out))
+        return out
+
+    def limit(self, u: np.ndarray) -> tuple[np.ndarray, int]:
+        u = np.array(u, dtype=np.float64, copy=True)
+        n = self.lib.orc_limit(self._l, self.mode, self.w0, self.eps, _p(u))
+        return u, int(n)
+
+    def troubled(self, u: np.ndarray) -> np.ndarray:
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        flags = C.create_string_buffer(self.mesh.n_cells)
+        self.lib.orc_limiter_troubled(self._l, _p(u), flags)
+        return np.frombuffer(flags.raw, dtype=np.int8).astype(bool)
+
+    def smoothness(self, cell: int, modal_coeff: np.ndarray) -> np.ndarray:
+        cm = np.ascontiguousarray(modal_coeff, dtype=np.float64)
+        beta = np.empty(5)
+        self.lib.orc_limiter_smoothness(self._l, cell, _p(cm), _p(beta))
+        return beta
+
+    def rk_update(self, riemann: int, order: int, t: float, dt: float, u: np.ndarray) -> np.ndarray:
+        u = np.array(u, dtype=np.float64, copy=True)
+        n, arr = self.mesh.bcs
+        self.lib.orc_rk_update_limited(self.mesh._m, riemann, n, arr, order, t, dt, _p(u), self._l,
+                                       self.mode, self.w0, self.eps)
+        return u

@@ -34,6 +34,7 @@
 #endif
 
 #include "orc.h"
+#include "orc_internal.h"
 
 #define K ORC_K
 #define MAXQ 6
@@ -237,6 +238,7 @@ struct orc_mesh {
   double *node_w;     /* [cells][N]  global weights */
   double *grad;       /* [cells][N][3][N]  basis global gradients */
   double *length;     /* [cells] */
+  double *cell_center; /* [cells][3] Hex8 LocalToGlobal(0, 0, 0) */
   /* per face */
   int64_t *face_cells; /* [faces][2] */
   int32_t *face_group; /* [faces] */
@@ -247,12 +249,20 @@ struct orc_mesh {
 };
 
 int64_t orc_column_size(const orc_mesh *m) { return m->n_cells * m->n * K; }
+int orc_mesh_degree(const orc_mesh *m) { return m->p; }
+int64_t orc_mesh_cells(const orc_mesh *m) { return m->n_cells; }
+int64_t orc_mesh_faces(const orc_mesh *m) { return m->n_faces; }
+const int64_t *orc_mesh_face_cells(const orc_mesh *m) { return m->face_cells; }
+void orc_cell_centers(const orc_mesh *m, double *center) {
+  for (int64_t c = 0; c < m->n_cells; ++c)
+    for (int d = 0; d < 3; ++d) center[c * 3 + d] = m->cell_center[c * 3 + d];
+}
 int orc_nodes_per_cell(const orc_mesh *m) { return m->n; }
 double orc_cell_length(const orc_mesh *m, int64_t c) { return m->length[c]; }
 
 void orc_mesh_destroy(orc_mesh *m) {
   if (!m) return;
-  free(m->node_xyz); free(m->node_w); free(m->grad); free(m->length);
+  free(m->node_xyz); free(m->node_w); free(m->grad); free(m->length); free(m->cell_center);
   free(m->face_cells); free(m->face_group); free(m->face_xyz); free(m->face_w);
   free(m->face_frame); free(m->map_h); free(m->map_s);
   free(m);
@@ -283,6 +293,7 @@ orc_mesh *orc_mesh_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
   m->node_w = (double *)malloc(sizeof(double) * n_cells * N);
   m->grad = (double *)malloc(sizeof(double) * n_cells * N * 3 * N);
   m->length = (double *)malloc(sizeof(double) * n_cells);
+  m->cell_center = (double *)malloc(sizeof(double) * n_cells * 3);
   int bad = 0;
 #pragma omp parallel for schedule(static) num_threads(orc_get_threads())
   for (int64_t c = 0; c < n_cells; ++c) {
@@ -293,6 +304,8 @@ orc_mesh *orc_mesh_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
       for (int d = 0; d < 3; ++d) xn[v * 3 + d] = xyz[id * 3 + d];
     }
     double volume = 0;
+    const double zero[3] = {0, 0, 0};
+    hex8_global(xn, zero, &m->cell_center[c * 3]);
     for (int i = 0; i < Q; ++i)
       for (int j = 0; j < Q; ++j)
         for (int k = 0; k < Q; ++k) {
@@ -553,16 +566,21 @@ static void next_solution(residual_fn fn, void *ctx, int64_t L, double t,
   for (int64_t i = 0; i < L; ++i) u_next[i] = u[i] + r[i] * dt;
 }
 
+/* Hook run after every SetSolutionColumn (the limiter of WithLimiter). */
+typedef void (*set_hook)(void *ctx, double *u);
+
 static int rk_update(residual_fn fn, void *ctx, int64_t L, int order, double t,
-                     double dt, double *u) {
+                     double dt, double *u, set_hook hook, void *hook_ctx) {
   double *u_curr = (double *)malloc(sizeof(double) * L);
   double *u_tmp = (double *)malloc(sizeof(double) * L);
   double *r = (double *)malloc(sizeof(double) * L);
   memcpy(u_curr, u, sizeof(double) * L);
   if (order == 1) {
     next_solution(fn, ctx, L, t, dt, u_curr, u, r);
+    if (hook) hook(hook_ctx, u);
   } else if (order == 2) {  /* rk.hpp:21-29 */
     next_solution(fn, ctx, L, t, dt, u_curr, u, r);
+    if (hook) hook(hook_ctx, u);
     next_solution(fn, ctx, L, t + dt, dt, u, u_tmp, r);
     for (int64_t i = 0; i < L; ++i) {
       double v = u_tmp[i];
@@ -570,8 +588,10 @@ static int rk_update(residual_fn fn, void *ctx, int64_t L, int order, double t,
       v *= 0.5;
       u[i] = v;
     }
+    if (hook) hook(hook_ctx, u);
   } else {  /* rk.hpp:31-49 */
     next_solution(fn, ctx, L, t, dt, u_curr, u, r);
+    if (hook) hook(hook_ctx, u);
     next_solution(fn, ctx, L, t + dt, dt, u, u_tmp, r);
     for (int64_t i = 0; i < L; ++i) {
       double v = u_curr[i];
@@ -580,6 +600,7 @@ static int rk_update(residual_fn fn, void *ctx, int64_t L, int order, double t,
       v /= 4;
       u[i] = v;
     }
+    if (hook) hook(hook_ctx, u);
     next_solution(fn, ctx, L, t + dt / 2, dt, u, u_tmp, r);
     for (int64_t i = 0; i < L; ++i) {
       double v = u_tmp[i];
@@ -588,9 +609,21 @@ static int rk_update(residual_fn fn, void *ctx, int64_t L, int order, double t,
       v /= 3;
       u[i] = v;
     }
+    if (hook) hook(hook_ctx, u);
   }
   free(u_curr); free(u_tmp); free(r);
   return 0;
+}
+
+typedef struct {
+  const orc_limiter *l;
+  int mode;
+  double w0, eps;
+} limit_ctx;
+
+static void limit_hook(void *ctx, double *u) {
+  limit_ctx *c = (limit_ctx *)ctx;
+  orc_limit(c->l, c->mode, c->w0, c->eps, u);
 }
 
 typedef struct {
@@ -607,7 +640,18 @@ static int dg_residual_fn(void *ctx, double t, const double *u, double *r) {
 int orc_rk_update(const orc_mesh *m, int riemann, int n_bc, const orc_bc *bcs,
                   int order, double t, double dt, double *u) {
   dg_ctx ctx = {m, riemann, n_bc, bcs};
-  return rk_update(dg_residual_fn, &ctx, orc_column_size(m), order, t, dt, u);
+  return rk_update(dg_residual_fn, &ctx, orc_column_size(m), order, t, dt, u,
+                   NULL, NULL);
+}
+
+int orc_rk_update_limited(const orc_mesh *m, int riemann, int n_bc,
+                          const orc_bc *bcs, int order, double t, double dt,
+                          double *u, const orc_limiter *l, int mode, double w0,
+                          double eps) {
+  dg_ctx ctx = {m, riemann, n_bc, bcs};
+  limit_ctx lc = {l, mode, w0, eps};
+  return rk_update(dg_residual_fn, &ctx, orc_column_size(m), order, t, dt, u,
+                   (l && mode != ORC_LIMITER_NONE) ? limit_hook : NULL, &lc);
 }
 
 typedef struct {
@@ -629,5 +673,5 @@ static int lin_residual_fn(void *ctx, double t, const double *u, double *r) {
 int orc_rk_update_linear(int order, int64_t n, const double *a, double t,
                          double dt, double *u) {
   lin_ctx ctx = {n, a};
-  return rk_update(lin_residual_fn, &ctx, n, order, t, dt, u);
+  return rk_update(lin_residual_fn, &ctx, n, order, t, dt, u, NULL, NULL);
 }

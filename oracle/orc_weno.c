@@ -1,0 +1,387 @@
+/*
+ * ORACLE (test infrastructure only): WENO limiter on DGSEM cells, restated
+ * from the reference project.  Parity checker and CPU baseline; the product
+ * library never calls it.
+ *
+ *   per-cell modal basis: Taylor monomials about the cell centre
+ *       (basis/taylor.hpp:79-218, index order constant/index.hpp via
+ *       taylor.hpp:40-55), orthonormalised by the cell's quadrature
+ *       (basis/linear.hpp:86-110, integrator/function.hpp:139-172)
+ *   nodal <-> modal: modal = nodal * modal_to_nodal, modal_to_nodal[n][m] =
+ *       w_n psi_m(x_n); nodal = modal evaluated at the nodes
+ *       (polynomial/extrapolation.hpp:59-89, 114-125)
+ *   projection average and offset: polynomial/projection.hpp:45-51, 260-264
+ *   smoothness beta: limiter/weno.hpp:25-95
+ *   Lazy reconstruct: limiter/weno.hpp:97-195
+ *   Eigen (jump) detector: limiter/weno.hpp:230-258
+ *   detect all, reconstruct all, then write back: limiter/reconstruct.hpp:21-54
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "orc.h"
+#include "orc_internal.h"
+
+#define K ORC_K
+
+/* exponents (x, y, z) of the Taylor monomials in the reference's order */
+static const int kTaylorExp[20][3] = {
+    {0, 0, 0},
+    {1, 0, 0}, {0, 1, 0}, {0, 0, 1},
+    {2, 0, 0}, {1, 1, 0}, {1, 0, 1}, {0, 2, 0}, {0, 1, 1}, {0, 0, 2},
+    {3, 0, 0}, {2, 1, 0}, {2, 0, 1}, {1, 2, 0}, {1, 1, 1}, {1, 0, 2},
+    {0, 3, 0}, {0, 2, 1}, {0, 1, 2}, {0, 0, 3}};
+
+int orc_modal_count(int p) { return (p + 1) * (p + 2) * (p + 3) / 6; }
+
+static double ipow(double x, int e) {
+  double r = 1;
+  for (int i = 0; i < e; ++i) r *= x;
+  return r;
+}
+
+static void taylor_values(int M, const double *d, double *t) {
+  for (int j = 0; j < M; ++j)
+    t[j] = ipow(d[0], kTaylorExp[j][0]) * ipow(d[1], kTaylorExp[j][1]) *
+           ipow(d[2], kTaylorExp[j][2]);
+}
+
+static double falling(int e, int a) { /* e! / (e - a)! */
+  double r = 1;
+  for (int i = 0; i < a; ++i) r *= (e - i);
+  return r;
+}
+
+/* GetPartialDerivatives: column a = d^alpha_a p (x), column 0 = 0. */
+static void taylor_pdv(int M, const double *d, const double *tc, double *out) {
+  out[0] = 0;
+  for (int a = 1; a < M; ++a) {
+    double s = 0;
+    for (int j = 0; j < M; ++j) {
+      int ok = 1;
+      double f = 1;
+      for (int dd = 0; dd < 3; ++dd) {
+        int e = kTaylorExp[j][dd], al = kTaylorExp[a][dd];
+        if (e < al) { ok = 0; break; }
+        f *= falling(e, al) * ipow(d[dd], e - al);
+      }
+      if (ok) s += tc[j] * f;
+    }
+    out[a] = s;
+  }
+}
+
+static int degree_of(int j) {
+  return kTaylorExp[j][0] + kTaylorExp[j][1] + kTaylorExp[j][2];
+}
+
+struct orc_limiter {
+  int p, n, m;
+  int64_t n_cells;
+  double *center;  /* [cells][3] */
+  double *s;       /* [cells][M][M] lower triangular */
+  double *psi;     /* [cells][N][M] basis values at own nodes */
+  double *w;       /* [cells][N] global weights */
+  double *xyz;     /* [cells][N][3] */
+  double *volume;  /* [cells] */
+  int *adj;        /* [cells][6] */
+  int *n_adj;      /* [cells] */
+};
+
+orc_limiter *orc_limiter_create(const orc_mesh *mesh) {
+  const int p = orc_mesh_degree(mesh), N = orc_nodes_per_cell(mesh);
+  const int M = orc_modal_count(p);
+  const int64_t C = orc_mesh_cells(mesh);
+  orc_limiter *l = (orc_limiter *)calloc(1, sizeof(orc_limiter));
+  l->p = p; l->n = N; l->m = M; l->n_cells = C;
+  l->center = (double *)malloc(sizeof(double) * C * 3);
+  l->s = (double *)calloc(C * M * M, sizeof(double));
+  l->psi = (double *)malloc(sizeof(double) * C * N * M);
+  l->w = (double *)malloc(sizeof(double) * C * N);
+  l->xyz = (double *)malloc(sizeof(double) * C * N * 3);
+  l->volume = (double *)malloc(sizeof(double) * C);
+  l->adj = (int *)malloc(sizeof(int) * C * 6);
+  l->n_adj = (int *)calloc(C, sizeof(int));
+  orc_node_geometry(mesh, l->xyz, l->w);
+  orc_cell_centers(mesh, l->center);
+  /* adjacency in face order (part.hpp:957-960 appends per local face) */
+  const int64_t F = orc_mesh_faces(mesh);
+  const int64_t *fc = orc_mesh_face_cells(mesh);
+  for (int64_t f = 0; f < F; ++f) {
+    int64_t h = fc[f * 2], s = fc[f * 2 + 1];
+    if (s < 0) continue;
+    if (l->n_adj[h] < 6) l->adj[h * 6 + l->n_adj[h]++] = (int)s;
+    if (l->n_adj[s] < 6) l->adj[s * 6 + l->n_adj[s]++] = (int)h;
+  }
+#pragma omp parallel for schedule(static) num_threads(orc_get_threads())
+  for (int64_t c = 0; c < C; ++c) {
+    double A[20 * 20] = {0}, T[64 * 20];
+    double *S = &l->s[c * M * M];
+    const double *W = &l->w[c * N];
+    double vol = 0;
+    for (int q = 0; q < N; ++q) {
+      double d[3];
+      for (int e = 0; e < 3; ++e) d[e] = l->xyz[(c * N + q) * 3 + e] - l->center[c * 3 + e];
+      taylor_values(M, d, &T[q * M]);
+      vol += W[q];
+    }
+    l->volume[c] = vol;
+    /* A = Integrate(T T^T) with global weights */
+    for (int i = 0; i < M; ++i)
+      for (int j = 0; j < M; ++j) {
+        double s = 0;
+        for (int q = 0; q < N; ++q) s += T[q * M + i] * T[q * M + j] * W[q];
+        A[i * M + j] = s;
+      }
+    /* OrthoNormalize (integrator/function.hpp:139-172) */
+    for (int i = 0; i < M; ++i)
+      for (int j = 0; j < M; ++j) S[i * M + j] = (i == j);
+    S[0] = 1 / sqrt(A[0]);
+    for (int i = 1; i < M; ++i) {
+      for (int j = 0; j < i; ++j) {
+        double temp = 0;
+        for (int k = 0; k <= j; ++k) temp += S[j * M + k] * A[k * M + i];
+        for (int ll = 0; ll <= j; ++ll) S[i * M + ll] -= temp * S[j * M + ll];
+      }
+      double norm_sq = 0;
+      for (int j = 0; j <= i; ++j) {
+        double sum = 0, sij = S[i * M + j];
+        for (int k = 0; k < j; ++k) sum += 2 * S[i * M + k] * A[k * M + j];
+        norm_sq += sij * (sij * A[j * M + j] + sum);
+      }
+      double inv = sqrt(norm_sq);
+      for (int j = 0; j < M; ++j) S[i * M + j] /= inv;
+    }
+    for (int q = 0; q < N; ++q)
+      for (int m = 0; m < M; ++m) {
+        double s = 0;
+        for (int j = 0; j <= m; ++j) s += S[m * M + j] * T[q * M + j];
+        l->psi[(c * N + q) * M + m] = s;
+      }
+  }
+  return l;
+}
+
+void orc_limiter_destroy(orc_limiter *l) {
+  if (!l) return;
+  free(l->center); free(l->s); free(l->psi); free(l->w); free(l->xyz);
+  free(l->volume); free(l->adj); free(l->n_adj);
+  free(l);
+}
+
+int orc_limiter_modal_count(const orc_limiter *l) { return l->m; }
+
+/* ProjectionWrapper GlobalToValue of cell c with modal coeff cm (K x M). */
+static void modal_value(const orc_limiter *l, int64_t c, const double *cm,
+                        const double *x, double *v) {
+  const int M = l->m;
+  double d[3], t[20], psi[20];
+  for (int e = 0; e < 3; ++e) d[e] = x[e] - l->center[c * 3 + e];
+  taylor_values(M, d, t);
+  const double *S = &l->s[c * M * M];
+  for (int m = 0; m < M; ++m) {
+    double s = 0;
+    for (int j = 0; j <= m; ++j) s += S[m * M + j] * t[j];
+    psi[m] = s;
+  }
+  for (int k = 0; k < K; ++k) {
+    double s = 0;
+    for (int m = 0; m < M; ++m) s += cm[k * M + m] * psi[m];
+    v[k] = s;
+  }
+}
+
+/* UpdateModalCoeff: modal (K x M) = nodal values (K x N) * modal_to_nodal. */
+void orc_limiter_modal(const orc_limiter *l, const double *u, double *modal) {
+  const int N = l->n, M = l->m;
+#pragma omp parallel for schedule(static) num_threads(orc_get_threads())
+  for (int64_t c = 0; c < l->n_cells; ++c) {
+    for (int k = 0; k < K; ++k)
+      for (int m = 0; m < M; ++m) {
+        double s = 0;
+        for (int q = 0; q < N; ++q)
+          s += u[(c * N + q) * K + k] * (l->w[c * N + q] * l->psi[(c * N + q) * M + m]);
+        modal[(c * K + k) * M + m] = s;
+      }
+  }
+}
+
+/* GetSmoothness (weno.hpp:78-95) of modal coeff cm on cell c. */
+static void smoothness(const orc_limiter *l, int64_t c, const double *cm,
+                       double *beta) {
+  const int N = l->n, M = l->m, P = l->p;
+  const double *S = &l->s[c * M * M];
+  double tc[K * 20], integral[K * 20];
+  for (int k = 0; k < K; ++k)
+    for (int j = 0; j < M; ++j) {
+      double s = 0;
+      for (int m = j; m < M; ++m) s += cm[k * M + m] * S[m * M + j];
+      tc[k * M + j] = s;
+    }
+  memset(integral, 0, sizeof(integral));
+  for (int q = 0; q < N; ++q) {
+    double d[3], pdv[20];
+    for (int e = 0; e < 3; ++e) d[e] = l->xyz[(c * N + q) * 3 + e] - l->center[c * 3 + e];
+    double w = l->w[c * N + q];
+    for (int k = 0; k < K; ++k) {
+      taylor_pdv(M, d, &tc[k * M], pdv);
+      for (int a = 0; a < M; ++a) integral[k * M + a] += pdv[a] * pdv[a] * w;
+    }
+  }
+  double s00 = S[0];
+  double volume = 1 / (s00 * s00);
+  for (int k = 0; k < K; ++k) {
+    double b = 0;
+    for (int deg = 1; deg <= P; ++deg) {
+      double kf = tgamma(deg + 1);
+      double weight = pow(volume, deg * 2. / 3 - 1) / (kf * kf);
+      double s = 0;
+      for (int a = 1; a < M; ++a)
+        if (degree_of(a) == deg) s += integral[k * M + a];
+      b += s * weight;
+    }
+    beta[k] = b;
+  }
+}
+
+void orc_limiter_smoothness(const orc_limiter *l, int64_t c, const double *cm,
+                            double *beta) {
+  smoothness(l, c, cm, beta);
+}
+
+/* weno::Eigen::IsNotSmooth (weno.hpp:230-258). */
+static int is_not_smooth(const orc_limiter *l, int64_t c, const double *modal) {
+  const int M = l->m, P = l->p;
+  const int comps[2] = {0, K - 1};
+  const double *cm = &modal[c * K * M];
+  double s00 = l->s[c * M * M];
+  double max_abs[K], sum_abs[K] = {0, 0, 0, 0, 0}, mine[K];
+  for (int k = 0; k < K; ++k) max_abs[k] = cm[k * M] * s00;
+  for (int i = 0; i < 2; ++i) max_abs[comps[i]] = fmax(1e-9, fabs(max_abs[comps[i]]));
+  modal_value(l, c, cm, &l->center[c * 3], mine);
+  for (int a = 0; a < l->n_adj[c]; ++a) {
+    int64_t b = l->adj[c * 6 + a];
+    const double *cb = &modal[b * K * M];
+    double adjv[K];
+    modal_value(l, b, cb, &l->center[c * 3], adjv);
+    double bs00 = l->s[b * M * M];
+    for (int i = 0; i < 2; ++i) {
+      int k = comps[i];
+      sum_abs[k] += fabs(mine[k] - adjv[k]);
+      max_abs[k] = fmax(max_abs[k], fabs(cb[k * M] * bs00));
+    }
+  }
+  double volume_power = (P + 1.0) / 2.0 / 3;
+  double divisor = pow(l->volume[c], volume_power) * l->n_adj[c];
+  double ref = P < 3 ? 1.0 : 3.0;
+  for (int i = 0; i < 2; ++i) {
+    int k = comps[i];
+    if (sum_abs[k] / max_abs[k] / divisor > ref) return 1;
+  }
+  return 0;
+}
+
+/* weno::Lazy::Reconstruct (weno.hpp:125-194) of cell c -> new modal coeff. */
+static void lazy_reconstruct(const orc_limiter *l, int64_t c,
+                             const double *modal, double w0, double eps,
+                             double *out) {
+  const int N = l->n, M = l->m;
+  const int n_adj = l->n_adj[c];
+  double cand[7][K * 20];
+  const double *own = &modal[c * K * M];
+  double s00 = l->s[c * M * M];
+  /* Borrow: neighbours projected onto my basis, shifted to my average */
+  for (int a = 0; a < n_adj; ++a) {
+    int64_t b = l->adj[c * 6 + a];
+    double *pj = cand[a];
+    memset(pj, 0, sizeof(double) * K * M);
+    for (int q = 0; q < N; ++q) {
+      double v[K];
+      modal_value(l, b, &modal[b * K * M], &l->xyz[(c * N + q) * 3], v);
+      double w = l->w[c * N + q];
+      for (int k = 0; k < K; ++k)
+        for (int m = 0; m < M; ++m) pj[k * M + m] += v[k] * l->psi[(c * N + q) * M + m] * w;
+    }
+    for (int k = 0; k < K; ++k) {
+      double my_avg = own[k * M] * s00;
+      double adj_avg = pj[k * M] * s00;
+      pj[k * M] += (my_avg - adj_avg) / s00;
+    }
+  }
+  memcpy(cand[n_adj], own, sizeof(double) * K * M);
+  /* weights */
+  double weights[7][K], sum[K] = {0, 0, 0, 0, 0};
+  for (int i = 0; i <= n_adj; ++i)
+    for (int k = 0; k < K; ++k) weights[i][k] = w0;
+  for (int k = 0; k < K; ++k) {
+    weights[n_adj][k] *= -n_adj;
+    weights[n_adj][k] += 1.0;
+  }
+  for (int i = 0; i <= n_adj; ++i) {
+    double beta[K];
+    smoothness(l, c, cand[i], beta);
+    for (int k = 0; k < K; ++k) {
+      double b = beta[k] + eps;
+      b *= b;
+      weights[i][k] /= b;
+    }
+  }
+  for (int i = 0; i <= n_adj; ++i)
+    for (int k = 0; k < K; ++k) sum[k] += weights[i][k];
+  for (int i = 0; i <= n_adj; ++i)
+    for (int k = 0; k < K; ++k) weights[i][k] /= sum[k];
+  for (int k = 0; k < K; ++k)
+    for (int m = 0; m < M; ++m) out[k * M + m] = cand[n_adj][k * M + m] * weights[n_adj][k];
+  for (int i = 0; i < n_adj; ++i)
+    for (int k = 0; k < K; ++k)
+      for (int m = 0; m < M; ++m) out[k * M + m] += cand[i][k * M + m] * weights[i][k];
+}
+
+/* limiter::Reconstruct (reconstruct.hpp:21-54) in place on the nodal column.
+ * mode: ORC_LIMITER_LAZY (every cell) or ORC_LIMITER_DETECT_LAZY (cells the
+ * jump detector flags).  Returns the number of reconstructed cells. */
+int64_t orc_limit(const orc_limiter *l, int mode, double w0, double eps,
+                  double *u) {
+  const int N = l->n, M = l->m;
+  const int64_t C = l->n_cells;
+  double *modal = (double *)malloc(sizeof(double) * C * K * M);
+  double *fresh = (double *)malloc(sizeof(double) * C * K * M);
+  char *troubled = (char *)calloc(C, 1);
+  orc_limiter_modal(l, u, modal);
+  int64_t count = 0;
+#pragma omp parallel for schedule(dynamic, 16) reduction(+ : count) num_threads(orc_get_threads())
+  for (int64_t c = 0; c < C; ++c) {
+    troubled[c] = mode == ORC_LIMITER_LAZY ? 1 : (char)is_not_smooth(l, c, modal);
+    if (troubled[c]) {
+      lazy_reconstruct(l, c, modal, w0, eps, &fresh[c * K * M]);
+      ++count;
+    }
+  }
+  /* SetCoeff(modal) -> UpdateNodalCoeff: nodal = modal at the nodes */
+#pragma omp parallel for schedule(static) num_threads(orc_get_threads())
+  for (int64_t c = 0; c < C; ++c) {
+    if (!troubled[c]) continue;
+    for (int q = 0; q < N; ++q)
+      for (int k = 0; k < K; ++k) {
+        double s = 0;
+        for (int m = 0; m < M; ++m) s += fresh[(c * K + k) * M + m] * l->psi[(c * N + q) * M + m];
+        u[(c * N + q) * K + k] = s;
+      }
+  }
+  free(modal); free(fresh); free(troubled);
+  return count;
+}
+
+int64_t orc_limiter_troubled(const orc_limiter *l, const double *u, char *flags) {
+  const int M = l->m;
+  double *modal = (double *)malloc(sizeof(double) * l->n_cells * K * M);
+  orc_limiter_modal(l, u, modal);
+  int64_t count = 0;
+  for (int64_t c = 0; c < l->n_cells; ++c) {
+    flags[c] = (char)is_not_smooth(l, c, modal);
+    count += flags[c];
+  }
+  free(modal);
+  return count;
+}

@@ -1,0 +1,89 @@
+"""The oracle's WENO limiter against the reference's limiter tests.
+
+* smoothness indicator of the Taylor monomials on [-1,1]^3
+  (test/limiter/weno.cpp:45-88: first-order monomials give volume * w1,
+  x^2 gives 32/3 w1 + 32 w2, xy gives 16/3 w1 + 8 w2),
+* cell averages are preserved by the reconstruction
+  (test/limiter/weno.cpp:172-176, 301-305: 1e-13),
+* a globally linear field is reproduced exactly (every candidate equals it),
+* the jump detector flags the cells next to a discontinuity only.
+"""
+import numpy as np
+import pytest
+
+import oracle.orc as orc
+from pvcriemannsolvers_gb300 import cases, mesh as meshlib
+
+EXPS = [(1, 0, 0), (0, 1, 0), (0, 0, 1), (2, 0, 0), (1, 1, 0), (1, 0, 1), (0, 2, 0), (0, 1, 1), (0, 0, 2)]
+
+
+def monomial_field(x, exps):
+    return np.stack([x[:, 0] ** a * x[:, 1] ** b * x[:, 2] ** c for a, b, c in exps], axis=1)
+
+
+def test_smoothness_kat():
+    m = meshlib.box((1, 1, 1), lengths=(2, 2, 2), origin=(-1, -1, -1))
+    om = orc.Mesh(m, 2)
+    lim = orc.Limiter(om)
+    x = meshlib.node_coordinates(m, 2).reshape(-1, 3)
+    volume = 8.0
+    w1 = volume ** (2 / 3 - 1)
+    w2 = volume ** (4 / 3 - 1) / 4
+    want = {(1, 0, 0): volume * w1, (0, 1, 0): volume * w1, (0, 0, 1): volume * w1,
+            (2, 0, 0): 32 / 3 * w1 + 32 * w2, (0, 2, 0): 32 / 3 * w1 + 32 * w2, (0, 0, 2): 32 / 3 * w1 + 32 * w2,
+            (1, 1, 0): 16 / 3 * w1 + 8 * w2, (1, 0, 1): 16 / 3 * w1 + 8 * w2, (0, 1, 1): 16 / 3 * w1 + 8 * w2}
+    for group in (EXPS[:5], EXPS[4:]):
+        u = monomial_field(x, group).ravel()
+        beta = lim.smoothness(0, lim.modal(u)[0])
+        for e, b in zip(group, beta):
+            assert abs(b - want[e]) < 1e-12, (e, b, want[e])
+    # a constant has zero smoothness indicator
+    u = np.ones((x.shape[0], 5)).ravel()
+    assert np.abs(lim.smoothness(0, lim.modal(u)[0])).max() < 1e-14
+
+
+def cell_averages(om, u):
+    _, w = om.node_geometry()
+    uu = u.reshape(w.shape[0], w.shape[1], 5)
+    return (uu * w[..., None]).sum(axis=1) / w.sum(axis=1)[:, None]
+
+
+@pytest.mark.parametrize("p", [1, 2, 3])
+def test_lazy_preserves_cell_averages(p):
+    m = meshlib.box((5, 4, 3), lengths=(1, 0.8, 0.6), jitter=0.1, seed=2)
+    om = orc.Mesh(m, p)
+    lim = orc.Limiter(om, orc.LIMITER_LAZY)
+    x = meshlib.node_coordinates(m, p).reshape(-1, 3)
+    rng = np.random.default_rng(p)
+    u = cases.prim_to_cons(1 + 0.3 * rng.uniform(-1, 1, len(x)), 0.2, 0.1, 0.0, 1 + 0.3 * rng.uniform(-1, 1, len(x))).ravel()
+    # first make u a modal (total degree p) field, as after any limiter pass
+    u1, n1 = lim.limit(u)
+    assert n1 == m.n_cells
+    u2, _ = lim.limit(u1)
+    np.testing.assert_allclose(cell_averages(om, u2), cell_averages(om, u1), rtol=0, atol=1e-13)
+
+
+def test_lazy_reproduces_linear_fields():
+    m = meshlib.box((4, 3, 3), lengths=(1, 0.8, 0.6), jitter=0.1, seed=5)
+    for p in (1, 2):
+        om = orc.Mesh(m, p)
+        lim = orc.Limiter(om, orc.LIMITER_LAZY)
+        x = meshlib.node_coordinates(m, p).reshape(-1, 3)
+        u = cases.prim_to_cons(1 + 0.1 * x[:, 0] - 0.2 * x[:, 1], 0.0, 0.0, 0.0, 1 + 0.05 * x[:, 2]).ravel()
+        # density and energy are linear in x here; momentum is zero
+        v, _ = lim.limit(u)
+        np.testing.assert_allclose(v, u, rtol=0, atol=1e-12)
+
+
+def test_jump_detector_flags_cells_next_to_a_shock():
+    m = meshlib.box((12, 2, 2), lengths=(1, 0.2, 0.2))
+    om = orc.Mesh(m, 2)
+    lim = orc.Limiter(om, orc.LIMITER_DETECT_LAZY)
+    x = meshlib.node_coordinates(m, 2).reshape(-1, 3)
+    smooth = cases.prim_to_cons(1 + 0.01 * x[:, 0], 0, 0, 0, 1.0).ravel()
+    assert not lim.troubled(smooth).any()
+    sod = cases.sod_ic(x).ravel()
+    flags = lim.troubled(sod)
+    centers = m.cell_centers()[:, 0]
+    assert flags.any()
+    assert np.all(np.abs(centers[flags] - 0.5) < 2 / 12)  # within two cells of the jump
