@@ -131,6 +131,19 @@ typedef struct mcfd_mesh_desc {
 enum mcfd_scheme { MCFD_DGSEM = 0 };
 enum mcfd_precision { MCFD_FP64 = 0, MCFD_MIXED = 1 };
 
+/* Limiter applied after every solution update (spatial/with_limiter.hpp:56-65):
+ *   LAZY:        weno::Lazy on every cell (limiter/weno.hpp:97-195)
+ *   DETECT_LAZY: weno::Lazy reconstruction on the cells that the jump
+ *                detector of weno::Eigen::IsNotSmooth flags
+ *                (limiter/weno.hpp:230-258)
+ * The modal basis is the per-cell orthonormalised Taylor basis of
+ * polynomial::Extrapolation (polynomial/extrapolation.hpp). */
+enum mcfd_limiter {
+  MCFD_LIMITER_NONE = 0,
+  MCFD_LIMITER_LAZY = 1,
+  MCFD_LIMITER_DETECT_LAZY = 2
+};
+
 typedef struct mcfd_options {
   int32_t degree;    /* polynomial degree p (1..3) */
   int32_t scheme;    /* enum mcfd_scheme */
@@ -138,7 +151,10 @@ typedef struct mcfd_options {
   int32_t precision; /* enum mcfd_precision */
   double cfl;        /* <= 0: the reference table fem.hpp:26-37 */
   int32_t device;    /* CUDA device ordinal */
-  int32_t reserved[7];
+  int32_t limiter;   /* enum mcfd_limiter */
+  double weno_w0;    /* linear weight of a neighbour; <= 0 selects 0.001 */
+  double weno_eps;   /* smoothness offset; <= 0 selects 1e-6 */
+  int32_t reserved[4];
 } mcfd_options;
 
 typedef struct mcfd_handle mcfd_handle;
@@ -205,6 +221,14 @@ int mcfd_rk_step(mcfd_handle *h, double t, double dt, int32_t order);
  * start time on entry and the end time on return. */
 int mcfd_advance(mcfd_handle *h, int32_t n_steps, double dt_guess,
                  int32_t rk_order, double *t);
+
+/* limiter::Reconstruct(part, limiter) (limiter/reconstruct.hpp:21-54) on the
+ * current solution with the handle's limiter (no-op when none is set).
+ * *troubled (may be NULL) receives the number of reconstructed cells. */
+int mcfd_limit(mcfd_handle *h, int64_t *troubled);
+
+/* Cells reconstructed by limiter passes since the last call (reset on read). */
+int mcfd_troubled_cells(mcfd_handle *h, int64_t *count);
 
 /* Use a caller-provided cudaStream_t (NULL = the handle's own stream). */
 int mcfd_set_stream(mcfd_handle *h, void *cuda_stream);

@@ -242,6 +242,7 @@ struct orc_mesh {
   /* per face */
   int64_t *face_cells; /* [faces][2] */
   int32_t *face_group; /* [faces] */
+  double *face_shift;  /* [faces][3] periodic shift (zeros when absent) */
   double *face_xyz;    /* [faces][QF][3] */
   double *face_w;      /* [faces][QF] */
   double *face_frame;  /* [faces][QF][9] */
@@ -253,6 +254,7 @@ int orc_mesh_degree(const orc_mesh *m) { return m->p; }
 int64_t orc_mesh_cells(const orc_mesh *m) { return m->n_cells; }
 int64_t orc_mesh_faces(const orc_mesh *m) { return m->n_faces; }
 const int64_t *orc_mesh_face_cells(const orc_mesh *m) { return m->face_cells; }
+const double *orc_mesh_face_shift(const orc_mesh *m) { return m->face_shift; }
 void orc_cell_centers(const orc_mesh *m, double *center) {
   for (int64_t c = 0; c < m->n_cells; ++c)
     for (int d = 0; d < 3; ++d) center[c * 3 + d] = m->cell_center[c * 3 + d];
@@ -263,6 +265,7 @@ double orc_cell_length(const orc_mesh *m, int64_t c) { return m->length[c]; }
 void orc_mesh_destroy(orc_mesh *m) {
   if (!m) return;
   free(m->node_xyz); free(m->node_w); free(m->grad); free(m->length); free(m->cell_center);
+  free(m->face_shift);
   free(m->face_cells); free(m->face_group); free(m->face_xyz); free(m->face_w);
   free(m->face_frame); free(m->map_h); free(m->map_s);
   free(m);
@@ -342,6 +345,8 @@ orc_mesh *orc_mesh_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
   m->map_s = (int16_t *)malloc(sizeof(int16_t) * n_faces * QF);
   memcpy(m->face_cells, face_cells, sizeof(int64_t) * n_faces * 2);
   memcpy(m->face_group, face_group, sizeof(int32_t) * n_faces);
+  m->face_shift = (double *)calloc(n_faces * 3 + 1, sizeof(double));
+  if (face_shift) memcpy(m->face_shift, face_shift, sizeof(double) * n_faces * 3);
 #pragma omp parallel for schedule(static) num_threads(orc_get_threads())
   for (int64_t f = 0; f < n_faces; ++f) {
     int64_t h = face_cells[f * 2], s = face_cells[f * 2 + 1];

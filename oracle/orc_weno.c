@@ -87,6 +87,9 @@ struct orc_limiter {
   double *volume;  /* [cells] */
   int *adj;        /* [cells][6] */
   int *n_adj;      /* [cells] */
+  double *adj_shift; /* [cells][6][3]: a point x of this cell is x - shift in
+                        the neighbour's frame (periodic faces; the reference
+                        has none, so its shift is always zero) */
 };
 
 orc_limiter *orc_limiter_create(const orc_mesh *mesh) {
@@ -103,16 +106,24 @@ orc_limiter *orc_limiter_create(const orc_mesh *mesh) {
   l->volume = (double *)malloc(sizeof(double) * C);
   l->adj = (int *)malloc(sizeof(int) * C * 6);
   l->n_adj = (int *)calloc(C, sizeof(int));
+  l->adj_shift = (double *)calloc(C * 6 * 3, sizeof(double));
   orc_node_geometry(mesh, l->xyz, l->w);
   orc_cell_centers(mesh, l->center);
   /* adjacency in face order (part.hpp:957-960 appends per local face) */
   const int64_t F = orc_mesh_faces(mesh);
   const int64_t *fc = orc_mesh_face_cells(mesh);
+  const double *fs = orc_mesh_face_shift(mesh);
   for (int64_t f = 0; f < F; ++f) {
     int64_t h = fc[f * 2], s = fc[f * 2 + 1];
     if (s < 0) continue;
-    if (l->n_adj[h] < 6) l->adj[h * 6 + l->n_adj[h]++] = (int)s;
-    if (l->n_adj[s] < 6) l->adj[s * 6 + l->n_adj[s]++] = (int)h;
+    if (l->n_adj[h] < 6) {
+      for (int e = 0; e < 3; ++e) l->adj_shift[(h * 6 + l->n_adj[h]) * 3 + e] = fs[f * 3 + e];
+      l->adj[h * 6 + l->n_adj[h]++] = (int)s;
+    }
+    if (l->n_adj[s] < 6) {
+      for (int e = 0; e < 3; ++e) l->adj_shift[(s * 6 + l->n_adj[s]) * 3 + e] = -fs[f * 3 + e];
+      l->adj[s * 6 + l->n_adj[s]++] = (int)h;
+    }
   }
 #pragma omp parallel for schedule(static) num_threads(orc_get_threads())
   for (int64_t c = 0; c < C; ++c) {
@@ -166,7 +177,7 @@ orc_limiter *orc_limiter_create(const orc_mesh *mesh) {
 void orc_limiter_destroy(orc_limiter *l) {
   if (!l) return;
   free(l->center); free(l->s); free(l->psi); free(l->w); free(l->xyz);
-  free(l->volume); free(l->adj); free(l->n_adj);
+  free(l->volume); free(l->adj); free(l->n_adj); free(l->adj_shift);
   free(l);
 }
 
@@ -263,8 +274,10 @@ static int is_not_smooth(const orc_limiter *l, int64_t c, const double *modal) {
   for (int a = 0; a < l->n_adj[c]; ++a) {
     int64_t b = l->adj[c * 6 + a];
     const double *cb = &modal[b * K * M];
-    double adjv[K];
-    modal_value(l, b, cb, &l->center[c * 3], adjv);
+    const double *sh = &l->adj_shift[(c * 6 + a) * 3];
+    double adjv[K], xc[3];
+    for (int e = 0; e < 3; ++e) xc[e] = l->center[c * 3 + e] - sh[e];
+    modal_value(l, b, cb, xc, adjv);
     double bs00 = l->s[b * M * M];
     for (int i = 0; i < 2; ++i) {
       int k = comps[i];
@@ -294,11 +307,13 @@ static void lazy_reconstruct(const orc_limiter *l, int64_t c,
   /* Borrow: neighbours projected onto my basis, shifted to my average */
   for (int a = 0; a < n_adj; ++a) {
     int64_t b = l->adj[c * 6 + a];
+    const double *sh = &l->adj_shift[(c * 6 + a) * 3];
     double *pj = cand[a];
     memset(pj, 0, sizeof(double) * K * M);
     for (int q = 0; q < N; ++q) {
-      double v[K];
-      modal_value(l, b, &modal[b * K * M], &l->xyz[(c * N + q) * 3], v);
+      double v[K], xq[3];
+      for (int e = 0; e < 3; ++e) xq[e] = l->xyz[(c * N + q) * 3 + e] - sh[e];
+      modal_value(l, b, &modal[b * K * M], xq, v);
       double w = l->w[c * N + q];
       for (int k = 0; k < K; ++k)
         for (int m = 0; m < M; ++m) pj[k * M + m] += v[k] * l->psi[(c * N + q) * M + m] * w;

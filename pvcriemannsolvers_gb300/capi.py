@@ -49,7 +49,10 @@ class Options(C.Structure):
         ("precision", C.c_int32),
         ("cfl", C.c_double),
         ("device", C.c_int32),
-        ("reserved", C.c_int32 * 7),
+        ("limiter", C.c_int32),
+        ("weno_w0", C.c_double),
+        ("weno_eps", C.c_double),
+        ("reserved", C.c_int32 * 4),
     ]
 
 
@@ -92,7 +95,10 @@ SIGNATURES = {
     "mcfd_face_node_maps": (C.c_int, [_P, C.POINTER(C.c_int16), C.POINTER(C.c_int16)]),
     "mcfd_launch_count": (C.c_int64, [_P]),
     "mcfd_kernel_times": (C.c_int, [_P, C.c_int32, _D]),
+    "mcfd_limit": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "mcfd_troubled_cells": (C.c_int, [_P, C.POINTER(C.c_int64)]),
 }
+LIMITER = {"none": 0, "lazy": 1, "detect_lazy": 2}
 
 _lib = None
 

@@ -145,6 +145,11 @@ void release(mcfd_handle *h) {
                   m.bcs, b.u, b.u1, b.u2, b.res, b.flux, b.state};
   for (void *p : ptrs)
     if (p) cudaFree(p);
+  auto &l = h->lim;
+  void *lptrs[] = {l.psi, l.mn, l.proj, l.beta, l.eval, l.s00, l.divisor, l.adj,
+                   l.modal, l.troubled};
+  for (void *p : lptrs)
+    if (p) cudaFree(p);
   if (h->step_graph) cudaGraphExecDestroy(h->step_graph);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
 }
@@ -414,6 +419,222 @@ int build_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
   return MCFD_OK;
 }
 
+// ---------------------------------------------------------------------------
+// WENO limiter tables.  The modal basis of a cell (polynomial::Projection in
+// polynomial::Extrapolation) is the set of Taylor monomials of total degree
+// <= p about the cell centre, orthonormalised under the cell's own quadrature
+// (the GLL nodes with weights w = w_i w_j w_k det J).  With A the Gram matrix
+// of the monomials and A = L L^T its Cholesky factorisation, the basis is
+// psi = L^-1 T: the unique lower-triangular orthonormalisation, i.e. the one
+// the reference's Gram-Schmidt produces (integrator/function.hpp:139-172).
+
+// exponents (x, y, z) of the Taylor monomials in the reference's order
+// (basis/taylor.hpp:40-55, 200-218)
+const int kTaylorExp[20][3] = {
+    {0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {2, 0, 0}, {1, 1, 0}, {1, 0, 1},
+    {0, 2, 0}, {0, 1, 1}, {0, 0, 2}, {3, 0, 0}, {2, 1, 0}, {2, 0, 1}, {1, 2, 0},
+    {1, 1, 1}, {1, 0, 2}, {0, 3, 0}, {0, 2, 1}, {0, 1, 2}, {0, 0, 3}};
+
+double ipow(double x, int e) {
+  double r = 1;
+  for (int i = 0; i < e; ++i) r *= x;
+  return r;
+}
+
+// d^alpha T_j at offset d, alpha = exponents of monomial a
+double taylor_derivative(int j, int a, const double *d) {
+  double f = 1;
+  for (int e = 0; e < 3; ++e) {
+    int ej = kTaylorExp[j][e], ea = kTaylorExp[a][e];
+    if (ej < ea) return 0;
+    double fall = 1;
+    for (int i = 0; i < ea; ++i) fall *= (ej - i);
+    f *= fall * ipow(d[e], ej - ea);
+  }
+  return f;
+}
+
+struct CellBasis {
+  double center[3];
+  double s[20 * 20];  // psi_m = sum_j s[m][j] T_j(x - center), lower triangular
+};
+
+void basis_values(const CellBasis &b, int M, const double *x, double *psi) {
+  double d[3] = {x[0] - b.center[0], x[1] - b.center[1], x[2] - b.center[2]};
+  double t[20];
+  for (int j = 0; j < M; ++j) t[j] = taylor_derivative(j, 0, d);
+  for (int m = 0; m < M; ++m) {
+    double s = 0;
+    for (int j = 0; j <= m; ++j) s += b.s[m * M + j] * t[j];
+    psi[m] = s;
+  }
+}
+
+int build_limiter(mcfd_handle *h, const mcfd_mesh_desc *d, int kind, double w0,
+                  double eps) {
+  auto &m = h->mesh;
+  auto &l = h->lim;
+  const int Q = m.q, N = m.n, p = m.p;
+  const int M = (p + 1) * (p + 2) * (p + 3) / 6;
+  l.kind = kind;
+  l.m = M;
+  l.w0 = w0 > 0 ? w0 : 0.001;
+  l.eps = eps > 0 ? eps : 1e-6;
+  const int64_t C = d->n_cells;
+  double xq[4], wq[4];
+  gll(Q, xq, wq);
+  // adjacency in face order with periodic shifts (a point x of the cell is
+  // x - shift in the neighbour's frame)
+  std::vector<int32_t> adj((size_t)C * 6, -1);
+  std::vector<double> adj_shift((size_t)C * 6 * 3, 0.0);
+  std::vector<int> n_adj(C, 0);
+  for (int64_t f = 0; f < d->n_faces; ++f) {
+    int64_t hc = d->face_cells[f * 2], sc = d->face_cells[f * 2 + 1];
+    if (sc < 0) continue;
+    double sh[3] = {0, 0, 0};
+    if (d->face_shift)
+      for (int e = 0; e < 3; ++e) sh[e] = d->face_shift[f * 3 + e];
+    if (n_adj[hc] < 6) {
+      for (int e = 0; e < 3; ++e) adj_shift[((size_t)hc * 6 + n_adj[hc]) * 3 + e] = sh[e];
+      adj[(size_t)hc * 6 + n_adj[hc]++] = (int32_t)sc;
+    }
+    if (n_adj[sc] < 6) {
+      for (int e = 0; e < 3; ++e) adj_shift[((size_t)sc * 6 + n_adj[sc]) * 3 + e] = -sh[e];
+      adj[(size_t)sc * 6 + n_adj[sc]++] = (int32_t)hc;
+    }
+  }
+  std::vector<CellBasis> basis(C);
+  std::vector<double> node_x((size_t)C * N * 3), node_w((size_t)C * N), volume(C);
+  std::vector<double> psi((size_t)C * N * M), mn((size_t)C * N * M);
+  std::vector<double> beta((size_t)C * M * M), s00(C), divisor(C);
+  int bad = 0;
+#pragma omp parallel for schedule(static)
+  for (int64_t c = 0; c < C; ++c) {
+    double xn[24], J[9];
+    for (int v = 0; v < 8; ++v)
+      for (int e = 0; e < 3; ++e) xn[v * 3 + e] = d->xyz[d->cell_nodes[c * 8 + v] * 3 + e];
+    CellBasis &b = basis[c];
+    hex8_point(xn, 0, 0, 0, b.center, J);
+    double vol = 0;
+    for (int i = 0; i < Q; ++i)
+      for (int j = 0; j < Q; ++j)
+        for (int k = 0; k < Q; ++k) {
+          int q = (i * Q + j) * Q + k;
+          double *x = &node_x[((size_t)c * N + q) * 3];
+          hex8_point(xn, xq[i], xq[j], xq[k], x, J);
+          double det = J[0] * (J[4] * J[8] - J[5] * J[7]) - J[1] * (J[3] * J[8] - J[5] * J[6]) +
+                       J[2] * (J[3] * J[7] - J[4] * J[6]);
+          node_w[(size_t)c * N + q] = wq[i] * wq[j] * wq[k] * det;
+          vol += node_w[(size_t)c * N + q];
+        }
+    volume[c] = vol;
+    // Gram matrix of the monomials and its Cholesky factor L (A = L L^T)
+    std::vector<double> T((size_t)N * M), A((size_t)M * M, 0.0), L((size_t)M * M, 0.0);
+    for (int q = 0; q < N; ++q) {
+      const double *x = &node_x[((size_t)c * N + q) * 3];
+      double dd[3] = {x[0] - b.center[0], x[1] - b.center[1], x[2] - b.center[2]};
+      for (int j = 0; j < M; ++j) T[q * M + j] = taylor_derivative(j, 0, dd);
+    }
+    for (int i = 0; i < M; ++i)
+      for (int j = 0; j < M; ++j) {
+        double s = 0;
+        for (int q = 0; q < N; ++q) s += node_w[(size_t)c * N + q] * T[q * M + i] * T[q * M + j];
+        A[i * M + j] = s;
+      }
+    for (int i = 0; i < M; ++i) {
+      for (int j = 0; j <= i; ++j) {
+        double s = A[i * M + j];
+        for (int k = 0; k < j; ++k) s -= L[i * M + k] * L[j * M + k];
+        if (i == j) {
+          if (!(s > 0)) { bad = 1; s = 1; }
+          L[i * M + i] = std::sqrt(s);
+        } else {
+          L[i * M + j] = s / L[j * M + j];
+        }
+      }
+    }
+    // S = L^-1 (lower triangular, forward substitution per column)
+    for (int i = 0; i < M * M; ++i) b.s[i] = 0;
+    for (int col = 0; col < M; ++col) {
+      for (int i = col; i < M; ++i) {
+        double s = (i == col) ? 1.0 : 0.0;
+        for (int k = col; k < i; ++k) s -= L[i * M + k] * b.s[k * M + col];
+        b.s[i * M + col] = s / L[i * M + i];
+      }
+    }
+    s00[c] = b.s[0];
+    for (int q = 0; q < N; ++q) {
+      double *pq = &psi[((size_t)c * N + q) * M];
+      basis_values(b, M, &node_x[((size_t)c * N + q) * 3], pq);
+      for (int mm = 0; mm < M; ++mm) mn[((size_t)c * N + q) * M + mm] = node_w[(size_t)c * N + q] * pq[mm];
+    }
+    // smoothness quadratic form: sum over derivative multi-indices a (|a| >= 1)
+    // of weight(|a|) * integral of d^a psi_m d^a psi_m' (limiter/weno.hpp:25-95)
+    double measure = 1 / (b.s[0] * b.s[0]);
+    double weight[4] = {0, 0, 0, 0};
+    for (int deg = 1; deg <= p; ++deg) {
+      double kf = std::tgamma(deg + 1);
+      weight[deg] = std::pow(measure, deg * 2. / 3 - 1) / (kf * kf);
+    }
+    double *B = &beta[(size_t)c * M * M];
+    for (int i = 0; i < M * M; ++i) B[i] = 0;
+    std::vector<double> dpsi(M);
+    for (int q = 0; q < N; ++q) {
+      const double *x = &node_x[((size_t)c * N + q) * 3];
+      double dd[3] = {x[0] - b.center[0], x[1] - b.center[1], x[2] - b.center[2]};
+      double wgt = node_w[(size_t)c * N + q];
+      for (int a = 1; a < M; ++a) {
+        int deg = kTaylorExp[a][0] + kTaylorExp[a][1] + kTaylorExp[a][2];
+        for (int mm = 0; mm < M; ++mm) {
+          double s = 0;
+          for (int j = 0; j <= mm; ++j) s += b.s[mm * M + j] * taylor_derivative(j, a, dd);
+          dpsi[mm] = s;
+        }
+        for (int i = 0; i < M; ++i)
+          for (int j = 0; j < M; ++j) B[i * M + j] += wgt * weight[deg] * dpsi[i] * dpsi[j];
+      }
+    }
+    divisor[c] = std::pow(vol, (p + 1.0) / 2.0 / 3) * n_adj[c];
+  }
+  if (bad) return fail(h, MCFD_ERR_MESH, "degenerate cell: modal basis Gram matrix not positive definite");
+  // neighbour projections and basis values at the cell centre
+  std::vector<double> proj((size_t)C * 6 * M * M, 0.0), eval((size_t)C * 7 * M, 0.0);
+#pragma omp parallel for schedule(static)
+  for (int64_t c = 0; c < C; ++c) {
+    std::vector<double> pb(M);
+    for (int s = 0; s < 6; ++s) {
+      int32_t nb = adj[(size_t)c * 6 + s];
+      if (nb < 0) continue;
+      const double *sh = &adj_shift[((size_t)c * 6 + s) * 3];
+      double *P = &proj[(((size_t)c * 6 + s) * M) * M];
+      for (int q = 0; q < N; ++q) {
+        const double *x = &node_x[((size_t)c * N + q) * 3];
+        double xs[3] = {x[0] - sh[0], x[1] - sh[1], x[2] - sh[2]};
+        basis_values(basis[nb], M, xs, pb.data());
+        const double *mq = &mn[((size_t)c * N + q) * M];
+        for (int i = 0; i < M; ++i)
+          for (int j = 0; j < M; ++j) P[i * M + j] += pb[i] * mq[j];
+      }
+      double xc[3] = {basis[c].center[0] - sh[0], basis[c].center[1] - sh[1], basis[c].center[2] - sh[2]};
+      basis_values(basis[nb], M, xc, &eval[((size_t)c * 7 + s) * M]);
+    }
+    basis_values(basis[c], M, basis[c].center, &eval[((size_t)c * 7 + 6) * M]);
+  }
+  int rc;
+  if ((rc = upload(h, &l.psi, psi))) return rc;
+  if ((rc = upload(h, &l.mn, mn))) return rc;
+  if ((rc = upload(h, &l.proj, proj))) return rc;
+  if ((rc = upload(h, &l.beta, beta))) return rc;
+  if ((rc = upload(h, &l.eval, eval))) return rc;
+  if ((rc = upload(h, &l.s00, s00))) return rc;
+  if ((rc = upload(h, &l.divisor, divisor))) return rc;
+  if ((rc = upload(h, &l.adj, adj))) return rc;
+  CUDA_TRY(h, cudaMalloc(&l.modal, sizeof(double) * C * mcfd::kK * M));
+  CUDA_TRY(h, cudaMalloc(&l.troubled, sizeof(unsigned long long)));
+  CUDA_TRY(h, cudaMemset(l.troubled, 0, sizeof(unsigned long long)));
+  return MCFD_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -458,6 +679,12 @@ int mcfd_create(const mcfd_mesh_desc *mesh, const mcfd_options *options,
     rc = fail(h, MCFD_ERR_CUDA, "cudaStreamCreate failed");
   h->own_stream = true;
   if (!rc) rc = build_mesh(h, mesh, options->degree);
+  if (!rc && options->limiter != MCFD_LIMITER_NONE) {
+    if (options->limiter != MCFD_LIMITER_LAZY && options->limiter != MCFD_LIMITER_DETECT_LAZY)
+      rc = fail(h, MCFD_ERR_ARGUMENT, "unknown limiter");
+    else
+      rc = build_limiter(h, mesh, options->limiter, options->weno_w0, options->weno_eps);
+  }
   if (!rc) {
     size_t col = sizeof(double) * h->mesh.column;
     cudaError_t e = cudaMalloc(&h->buf.u, col);
@@ -530,9 +757,45 @@ static int copy_column(mcfd_handle *h, void *dst, const void *src, int64_t n,
   return MCFD_OK;
 }
 
+// WithLimiter::SetSolutionColumn runs the limiter after setting the column
+// (spatial/with_limiter.hpp:56-59).
+static int limit_current(mcfd_handle *h) {
+  if (h->lim.kind == MCFD_LIMITER_NONE) return MCFD_OK;
+  h->launches += mcfd::launch_limiter(h, h->buf.u);
+  CUDA_TRY(h, cudaGetLastError());
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  return MCFD_OK;
+}
+
 int mcfd_set_solution(mcfd_handle *h, const double *column, int64_t n) {
   if (!h) return MCFD_ERR_ARGUMENT;
-  return copy_column(h, h->buf.u, column, n, cudaMemcpyHostToDevice);
+  int rc = copy_column(h, h->buf.u, column, n, cudaMemcpyHostToDevice);
+  return rc ? rc : limit_current(h);
+}
+
+int mcfd_limit(mcfd_handle *h, int64_t *troubled) {
+  if (!h) return MCFD_ERR_ARGUMENT;
+  cudaSetDevice(h->device);
+  int64_t before = 0, after = 0;
+  if (h->lim.kind != MCFD_LIMITER_NONE) {
+    CUDA_TRY(h, cudaMemcpy(&before, h->lim.troubled, sizeof(before), cudaMemcpyDeviceToHost));
+    int rc = limit_current(h);
+    if (rc) return rc;
+    CUDA_TRY(h, cudaMemcpy(&after, h->lim.troubled, sizeof(after), cudaMemcpyDeviceToHost));
+  }
+  if (troubled) *troubled = after - before;
+  return MCFD_OK;
+}
+
+int mcfd_troubled_cells(mcfd_handle *h, int64_t *count) {
+  if (!h || !count) return MCFD_ERR_ARGUMENT;
+  *count = 0;
+  if (h->lim.kind == MCFD_LIMITER_NONE) return MCFD_OK;
+  cudaSetDevice(h->device);
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  CUDA_TRY(h, cudaMemcpy(count, h->lim.troubled, sizeof(*count), cudaMemcpyDeviceToHost));
+  CUDA_TRY(h, cudaMemset(h->lim.troubled, 0, sizeof(unsigned long long)));
+  return MCFD_OK;
 }
 
 int mcfd_get_solution(mcfd_handle *h, double *column, int64_t n) {
@@ -542,7 +805,8 @@ int mcfd_get_solution(mcfd_handle *h, double *column, int64_t n) {
 
 int mcfd_set_solution_device(mcfd_handle *h, const double *d_column, int64_t n) {
   if (!h) return MCFD_ERR_ARGUMENT;
-  return copy_column(h, h->buf.u, d_column, n, cudaMemcpyDeviceToDevice);
+  int rc = copy_column(h, h->buf.u, d_column, n, cudaMemcpyDeviceToDevice);
+  return rc ? rc : limit_current(h);
 }
 
 int mcfd_get_solution_device(mcfd_handle *h, double *d_column, int64_t n) {

@@ -656,21 +656,29 @@ int launch_residual_static_scratch(mcfd_handle *h, const double *d_u,
 int launch_rk_stage_sequence(mcfd_handle *h, int order) {
   Buffers &b = h->buf;
   int n = 0;
+  // Each stage result is a SetSolutionColumn in the reference, which runs the
+  // limiter when one is installed (spatial/with_limiter.hpp:56-59).
   if (order == 1) {
     n += launch_face_flux(h, b.u, 0.0);
     n += launch_cell_update(h, kStageEuler, b.u, nullptr, b.u, 1);
+    n += launch_limiter(h, b.u);
   } else if (order == 2) {
     n += launch_face_flux(h, b.u, 0.0);
     n += launch_cell_update(h, kStageEuler, b.u, nullptr, b.u1, 0);
+    n += launch_limiter(h, b.u1);
     n += launch_face_flux(h, b.u1, 1.0);
     n += launch_cell_update(h, kStageRk2Last, b.u1, b.u, b.u, 1);
+    n += launch_limiter(h, b.u);
   } else {
     n += launch_face_flux(h, b.u, 0.0);
     n += launch_cell_update(h, kStageEuler, b.u, nullptr, b.u1, 0);
+    n += launch_limiter(h, b.u1);
     n += launch_face_flux(h, b.u1, 1.0);
     n += launch_cell_update(h, kStageRk3Mid, b.u1, b.u, b.u2, 0);
+    n += launch_limiter(h, b.u2);
     n += launch_face_flux(h, b.u2, 0.5);
     n += launch_cell_update(h, kStageRk3Last, b.u2, b.u, b.u, 1);
+    n += launch_limiter(h, b.u);
   }
   return n;
 }

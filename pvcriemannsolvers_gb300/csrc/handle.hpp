@@ -65,6 +65,25 @@ struct Mesh {
   std::vector<BcDev> host_bcs;
 };
 
+// Device tables of the WENO limiter (built when a limiter is requested).
+// M = (p+1)(p+2)(p+3)/6 modal basis functions per cell.
+struct Limiter {
+  int kind = 0;              // mcfd_limiter
+  int m = 0;                 // modal basis size
+  double w0 = 0.001, eps = 1e-6;
+  double *psi = nullptr;     // [cells][N][M] orthonormal basis at the cell's nodes
+  double *mn = nullptr;      // [cells][N][M] w_n psi_m(x_n) (modal_to_nodal)
+  double *proj = nullptr;    // [cells][6][M][M] neighbour -> own basis projection
+  double *beta = nullptr;    // [cells][M][M] smoothness quadratic form
+  double *eval = nullptr;    // [cells][7][M] basis values at this cell's centre:
+                             //   slots 0..5 neighbour bases, slot 6 own basis
+  double *s00 = nullptr;     // [cells] S(0,0) of the own basis
+  double *divisor = nullptr; // [cells] volume^((p+1)/6) * n_adj (jump detector)
+  int32_t *adj = nullptr;    // [cells][6] neighbour cells (-1 = none), face order
+  double *modal = nullptr;   // [cells][K][M] scratch: modal coefficients
+  unsigned long long *troubled = nullptr;  // counter of reconstructed cells
+};
+
 struct Buffers {
   double *u = nullptr;     // current solution
   double *u1 = nullptr;    // stage buffers
@@ -89,6 +108,7 @@ struct mcfd_handle {
   mcfd::Options opt;
   mcfd::Mesh mesh;
   mcfd::Buffers buf;
+  mcfd::Limiter lim;
   double t_host = 0;
   int64_t launches = 0;
   std::string err;
@@ -108,6 +128,8 @@ int launch_cell_update(mcfd_handle *h, int stage, const double *u_in,
                        const double *u0, double *u_out, int advance_time);
 int launch_dt(mcfd_handle *h, const double *u);
 int launch_rk_stage_sequence(mcfd_handle *h, int order);
+// WENO limiter pass on a solution buffer, in place (weno.cu).
+int launch_limiter(mcfd_handle *h, double *u);
 
 // Residual whose face-flux scratch is a fixed file-scope device array
 // (mcfd_residual_device_noalloc).  Capacity in doubles: 2 Mi = 16 MiB, i.e.

@@ -66,9 +66,13 @@ class Lobatto:
     """DGSEM (dg::Lobatto, kLocal = false) Euler system on one GPU."""
 
     def __init__(self, mesh: Mesh, degree: int, riemann: str | int = "rusanov",
-                 cfl: float = 0.0, device: int = 0, precision: str = "fp64"):
+                 cfl: float = 0.0, device: int = 0, precision: str = "fp64",
+                 limiter: str = "none", weno_w0: float = 0.001, weno_eps: float = 1e-6):
         """precision: "fp64" (plain form) or "mixed" (FP32 volume flux and
-        contraction; FP64 Riemann fluxes, lift and RK accumulation)."""
+        contraction; FP64 Riemann fluxes, lift and RK accumulation).
+        limiter: "none", "lazy" (weno::Lazy on every cell) or "detect_lazy"
+        (weno::Lazy on the cells the weno::Eigen jump detector flags), run
+        after every solution update as WithLimiter does."""
         lib = capi.load()
         self.mesh = mesh
         self.degree = int(degree)
@@ -103,6 +107,10 @@ class Lobatto:
         opt.precision = capi.FP64 if precision == "fp64" else capi.MIXED
         opt.cfl = float(cfl)
         opt.device = int(device)
+        opt.limiter = capi.LIMITER[limiter]
+        opt.weno_w0 = float(weno_w0)
+        opt.weno_eps = float(weno_eps)
+        self.limiter = limiter
         h = C.c_void_p()
         capi.check(lib.mcfd_create(C.byref(desc), C.byref(opt), C.byref(h)), None)
         self._h = h
@@ -219,6 +227,19 @@ class Lobatto:
         tt = C.c_double(float(t))
         self._check(self._lib.mcfd_advance(self._h, int(n_steps), float(dt_guess), int(rk_order), C.byref(tt)))
         return tt.value
+
+    def Limit(self) -> int:
+        """limiter::Reconstruct on the current solution; returns the number of
+        reconstructed cells."""
+        n = C.c_int64()
+        self._check(self._lib.mcfd_limit(self._h, C.byref(n)))
+        return n.value
+
+    def troubled_cells(self) -> int:
+        """Cells reconstructed since the previous call."""
+        n = C.c_int64()
+        self._check(self._lib.mcfd_troubled_cells(self._h, C.byref(n)))
+        return n.value
 
     def kernel_times(self, reps: int = 10) -> dict:
         """Average CUDA-event milliseconds per launch of each stage kernel."""

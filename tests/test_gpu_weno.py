@@ -1,0 +1,99 @@
+"""GPU WENO limiter (through the C ABI) against the oracle's restatement of
+limiter::Reconstruct with weno::Lazy / the weno::Eigen jump detector.
+
+Bar: 1e-12 relative L2 on the limited column and on limited SSP-RK3 steps;
+identical troubled-cell counts.
+"""
+import numpy as np
+import pytest
+
+import oracle.orc as orc
+from pvcriemannsolvers_gb300 import Lobatto, RungeKutta, cases, mesh as meshlib
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-12
+MODES = {"lazy": orc.LIMITER_LAZY, "detect_lazy": orc.LIMITER_DETECT_LAZY}
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def sod_like(x, rng):
+    base = cases.sod_ic(x)
+    noise = 1 + 0.02 * rng.uniform(-1, 1, (x.shape[0], 1))
+    return (base * noise).ravel()
+
+
+@pytest.mark.parametrize("mode", list(MODES))
+@pytest.mark.parametrize("p", [1, 2, 3])
+@pytest.mark.parametrize("periodic", [False, True])
+def test_limiter_parity(gpu, mode, p, periodic):
+    m = meshlib.box((8, 3, 2), lengths=(1.0, 0.3, 0.2), periodic=(periodic,) * 3, jitter=0.1, seed=4)
+    x = meshlib.node_coordinates(m, p).reshape(-1, 3)
+    u = sod_like(x, np.random.default_rng(p))
+    s = Lobatto(m, p, "roe", limiter=mode)
+    om = orc.Mesh(m, p)
+    lim = orc.Limiter(om, MODES[mode])
+    s.SetSolutionColumn(u)            # WithLimiter::SetSolutionColumn limits
+    got = s.GetSolutionColumn()
+    want, n_orc = lim.limit(u)
+    assert s.troubled_cells() == n_orc
+    if mode == "detect_lazy":
+        assert 0 < n_orc < m.n_cells
+    assert rel_l2(got, want) <= RTOL, rel_l2(got, want)
+    s.close()
+
+
+@pytest.mark.parametrize("mode", list(MODES))
+def test_limited_rk3_parity(gpu, mode):
+    """SSP-RK3 on WithLimiter<dg::Lobatto> (Sod tube, Roe, p = 2): the limiter
+    runs after every stage."""
+    p = 2
+    m = cases.sod_mesh(20, 2, 2)
+    x = meshlib.node_coordinates(m, p).reshape(-1, 3)
+    u0 = cases.sod_ic(x).ravel()
+    s = Lobatto(m, p, "roe", limiter=mode)
+    cases.sod_bc(s)
+    om = orc.Mesh(m, p)
+    om.set_bcs({0: (orc.BC_SMART, cases.SOD_LEFT), 1: (orc.BC_SMART, cases.SOD_RIGHT),
+                2: (orc.BC_INVISCID_WALL, None), 3: (orc.BC_INVISCID_WALL, None),
+                4: (orc.BC_INVISCID_WALL, None), 5: (orc.BC_INVISCID_WALL, None)})
+    lim = orc.Limiter(om, MODES[mode])
+    s.SetSolutionColumn(u0)
+    u, _ = lim.limit(u0)
+    t = 0.0
+    for _ in range(3):
+        dt = om.time_step(u, 1.0, 3, 0.1)
+        RungeKutta(3).Update(s, t, dt)
+        u = lim.rk_update(orc.ROE, 3, t, dt, u)
+        t += dt
+    err = rel_l2(s.GetSolutionColumn(), u)
+    assert err <= RTOL, err
+    s.close()
+
+
+def test_limiter_keeps_advance_graph_consistent(gpu):
+    """mcfd_advance (graph-captured step incl. limiter passes) equals the
+    step-by-step fused update."""
+    p = 2
+    m = cases.sod_mesh(16, 2, 2)
+    x = meshlib.node_coordinates(m, p).reshape(-1, 3)
+    u0 = cases.sod_ic(x).ravel()
+    out = []
+    for fused in (True, False):
+        s = Lobatto(m, p, "roe", cfl=0.1, limiter="lazy")
+        cases.sod_bc(s)
+        s.SetSolutionColumn(u0)
+        if fused:
+            s.advance(3, 1e9, 3, 0.0)
+        else:
+            t = 0.0
+            for _ in range(3):
+                dt = s.GetTimeStep(1e9, 3)
+                RungeKutta(3).Update(s, t, dt)
+                t += dt
+        out.append(s.GetSolutionColumn())
+        s.close()
+    assert rel_l2(out[0], out[1]) <= 1e-14
