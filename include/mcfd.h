@@ -128,7 +128,12 @@ typedef struct mcfd_mesh_desc {
   const double *face_shift;
 } mcfd_mesh_desc;
 
-enum mcfd_scheme { MCFD_DGSEM = 0 };
+/* Spatial schemes on GLL-collocated hexahedra:
+ *   DGSEM: dg::Lobatto, weak form with lumped mass (spatial/dg/lobatto.hpp)
+ *   FR:    fr::Lobatto, flux reconstruction with Huynh's g2 correction
+ *          (spatial/fr/general.hpp, spatial/fr/lobatto.hpp, basis/vincent.hpp);
+ *          its time step is twice the DGSEM one (fr/lobatto.hpp:220-222). */
+enum mcfd_scheme { MCFD_DGSEM = 0, MCFD_FR = 1 };
 enum mcfd_precision { MCFD_FP64 = 0, MCFD_MIXED = 1 };
 
 /* Limiter applied after every solution update (spatial/with_limiter.hpp:56-65):

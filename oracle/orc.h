@@ -107,7 +107,13 @@ double orc_cell_length(const orc_mesh *m, int64_t i_cell);
 void orc_set_threads(int n);
 int orc_get_threads(void);
 
-/* GetResidualColumn of dg::Lobatto (lumped mass divide included). */
+/* Spatial scheme of a mesh's residual: dg::Lobatto (default) or fr::Lobatto
+ * with Huynh's g2 correction (spatial/fr/lobatto.hpp). */
+enum { ORC_SCHEME_DGSEM = 0, ORC_SCHEME_FR = 1 };
+void orc_mesh_set_scheme(orc_mesh *m, int scheme);
+
+/* GetResidualColumn of dg::Lobatto (lumped mass divide included) or of
+ * fr::Lobatto (divided by det J), by the mesh's scheme. */
 int orc_dgsem_residual(const orc_mesh *m, int riemann, int n_bc,
                        const orc_bc *bcs, double t, const double *u, double *r);
 /* FiniteElement::GetTimeStep with an explicit CFL number (cfl <= 0 selects

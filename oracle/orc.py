@@ -71,6 +71,7 @@ def load() -> C.CDLL:
             "orc_rk_update": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(OrcBc), C.c_int, C.c_double,
                                         C.c_double, _D]),
             "orc_rk_update_linear": (C.c_int, [C.c_int, C.c_int64, _D, C.c_double, C.c_double, _D]),
+            "orc_mesh_set_scheme": (None, [C.c_void_p, C.c_int]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -163,7 +164,7 @@ def make_bcs(specs: dict[int, tuple]) -> tuple[int, C.Array]:
 class Mesh:
     """Oracle-side mesh + DGSEM system built from the same description."""
 
-    def __init__(self, mesh, degree: int):
+    def __init__(self, mesh, degree: int, scheme: str = "dgsem"):
         lib = load()
         self._keep = [np.ascontiguousarray(mesh.xyz, dtype=np.float64),
                       np.ascontiguousarray(mesh.cell_nodes, dtype=np.int64),
@@ -184,6 +185,8 @@ class Mesh:
         self.n_cells = cn.shape[0]
         self.column_size = int(lib.orc_column_size(self._m))
         self.bcs = make_bcs({})
+        if scheme == "fr":
+            lib.orc_mesh_set_scheme(self._m, 1)
 
     def __del__(self):
         if getattr(self, "_m", None):

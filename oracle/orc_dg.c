@@ -239,6 +239,10 @@ struct orc_mesh {
   double *grad;       /* [cells][N][3][N]  basis global gradients */
   double *length;     /* [cells] */
   double *cell_center; /* [cells][3] Hex8 LocalToGlobal(0, 0, 0) */
+  double *jdi;        /* [cells][N][9] det(J) J^-1 (GetJacobianAssociated) */
+  double *detj;       /* [cells][N] det(J) */
+  int32_t *face_sides; /* [faces][2] local face index in holder / sharer */
+  int scheme;          /* ORC_SCHEME_DGSEM or ORC_SCHEME_FR */
   /* per face */
   int64_t *face_cells; /* [faces][2] */
   int32_t *face_group; /* [faces] */
@@ -265,7 +269,7 @@ double orc_cell_length(const orc_mesh *m, int64_t c) { return m->length[c]; }
 void orc_mesh_destroy(orc_mesh *m) {
   if (!m) return;
   free(m->node_xyz); free(m->node_w); free(m->grad); free(m->length); free(m->cell_center);
-  free(m->face_shift);
+  free(m->face_shift); free(m->jdi); free(m->detj); free(m->face_sides);
   free(m->face_cells); free(m->face_group); free(m->face_xyz); free(m->face_w);
   free(m->face_frame); free(m->map_h); free(m->map_s);
   free(m);
@@ -297,6 +301,11 @@ orc_mesh *orc_mesh_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
   m->grad = (double *)malloc(sizeof(double) * n_cells * N * 3 * N);
   m->length = (double *)malloc(sizeof(double) * n_cells);
   m->cell_center = (double *)malloc(sizeof(double) * n_cells * 3);
+  m->jdi = (double *)malloc(sizeof(double) * n_cells * N * 9);
+  m->detj = (double *)malloc(sizeof(double) * n_cells * N);
+  m->face_sides = (int32_t *)malloc(sizeof(int32_t) * (n_faces * 2 + 1));
+  if (n_faces) memcpy(m->face_sides, face_sides, sizeof(int32_t) * n_faces * 2);
+  m->scheme = ORC_SCHEME_DGSEM;
   int bad = 0;
 #pragma omp parallel for schedule(static) num_threads(orc_get_threads())
   for (int64_t c = 0; c < n_cells; ++c) {
@@ -322,6 +331,8 @@ orc_mesh *orc_mesh_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
           m->node_w[c * N + qn] = w;
           volume += w;
           inv3(jac, inv);
+          m->detj[c * N + qn] = det;
+          for (int e = 0; e < 9; ++e) m->jdi[(c * N + qn) * 9 + e] = det * inv[e];
           /* local gradients of every basis function at node (i,j,k) */
           double *g = &m->grad[((c * N + qn) * 3) * N];
           for (int r = 0; r < 3; ++r)
@@ -432,9 +443,124 @@ static void given_value(const orc_bc *bc, const double *x, double t,
   memcpy(v, src, sizeof(double) * K);
 }
 
+void orc_mesh_set_scheme(orc_mesh *m, int scheme) { m->scheme = scheme; }
+
+/* Vincent::LocalToRightDerivative(1) with c_next = HuynhLumpingLobatto(p)
+ * (basis/vincent.hpp:30-32, 73-89): Legendre derivatives by the recurrence
+ * P'_{k+1}(x) = (k+1) P_k(x) + x P'_k(x) at x = 1, where P_k(1) = 1. */
+static double fr_g_prime(int p) {
+  double c_next = p / (2.0 * p + 1), c_prev = 1 - c_next;
+  double prev = 0, curr = 0, next = 0;
+  for (int k = 0; k <= p; ++k) {
+    if (k > 0) { prev = curr; curr = next; }
+    next = (k + 1) * 1.0 + 1.0 * curr;
+  }
+  return 0.5 * (curr + c_prev * prev + c_next * next);
+}
+
+/* fr::Lobatto residual (spatial/fr/general.hpp:249-288, fr/lobatto.hpp:66-433):
+ * residual[q] -= div of the interpolated contravariant flux at node q; at
+ * every flux point the holder (sharer) node gets
+ *   -= g'(+-1) (F_upwind * scale - F_contravariant[:, dir])
+ * with scale = +-|det(J) J^-1 e_dir|; finally residual /= det(J). */
+static int fr_residual(const orc_mesh *m, int riemann, int n_bc,
+                       const orc_bc *bcs, double t, const double *u,
+                       double *r) {
+  const int Q = m->q, N = m->n, QF = m->qf, KN = K * m->n;
+  int64_t L = orc_column_size(m);
+  memset(r, 0, sizeof(double) * L);
+  const double g1 = fr_g_prime(m->p);
+  double *cflux = (double *)malloc(sizeof(double) * m->n_cells * N * 15);
+  /* AddFluxDivergence */
+#pragma omp parallel for schedule(static) num_threads(orc_get_threads())
+  for (int64_t c = 0; c < m->n_cells; ++c) {
+    const double *uc = u + c * KN;
+    double *fc = cflux + c * N * 15;
+    for (int q = 0; q < N; ++q) {
+      double f[15];
+      orc_flux_matrix(uc + q * K, f);
+      const double *jd = &m->jdi[(c * N + q) * 9];
+      for (int k = 0; k < K; ++k)
+        for (int e = 0; e < 3; ++e)
+          fc[q * 15 + k * 3 + e] = f[k * 3 + 0] * jd[0 * 3 + e] + f[k * 3 + 1] * jd[1 * 3 + e] +
+                                   f[k * 3 + 2] * jd[2 * 3 + e];
+    }
+    for (int q = 0; q < N; ++q) {
+      int i = q / QF, j = (q / Q) % Q, l = q % Q;
+      double value[K] = {0, 0, 0, 0, 0};
+      for (int kb = 0; kb < N; ++kb) {
+        int a = kb / QF, b = (kb / Q) % Q, cc = kb % Q;
+        double g0 = (b == j && cc == l) ? m->d[i * Q + a] : 0;
+        double gy = (a == i && cc == l) ? m->d[j * Q + b] : 0;
+        double gz = (a == i && b == j) ? m->d[l * Q + cc] : 0;
+        for (int k = 0; k < K; ++k)
+          value[k] += fc[kb * 15 + k * 3 + 0] * g0 + fc[kb * 15 + k * 3 + 1] * gy +
+                      fc[kb * 15 + k * 3 + 2] * gz;
+      }
+      for (int k = 0; k < K; ++k) r[c * KN + q * K + k] -= value[k];
+    }
+  }
+  /* face corrections; dir and sign of each local face (fr/lobatto.hpp:81-152) */
+  static const int kDir[6] = {2, 1, 0, 1, 0, 2};
+  static const double kSign[6] = {-1, -1, +1, +1, -1, +1};
+  for (int64_t f = 0; f < m->n_faces; ++f) {
+    int64_t h = m->face_cells[f * 2], s = m->face_cells[f * 2 + 1];
+    int g = m->face_group[f];
+    if (s < 0 && !(g >= 0 && g < n_bc && bcs[g].kind != ORC_BC_NONE)) continue;
+    int sh = m->face_sides[f * 2], ss = s >= 0 ? m->face_sides[f * 2 + 1] : 0;
+    for (int fp = 0; fp < QF; ++fp) {
+      const double *fr = &m->face_frame[(f * QF + fp) * 9];
+      int nh = m->map_h[f * QF + fp];
+      const double *uh = u + h * KN + nh * K;
+      double flux[K];
+      if (s >= 0) {
+        const double *us = u + s * KN + m->map_s[f * QF + fp] * K;
+        orc_flux_rotated(riemann, fr, uh, us, flux);
+      } else {
+        double given[K];
+        given_value(&bcs[g], &m->face_xyz[(f * QF + fp) * 3], t, given);
+        orc_flux_boundary(riemann, bcs[g].kind, fr, uh, given, flux);
+      }
+      {
+        const double *jd = &m->jdi[(h * N + nh) * 9];
+        int dir = kDir[sh];
+        double nrm = sqrt(jd[0 * 3 + dir] * jd[0 * 3 + dir] + jd[1 * 3 + dir] * jd[1 * 3 + dir] +
+                          jd[2 * 3 + dir] * jd[2 * 3 + dir]);
+        double scale = kSign[sh] * nrm, gp = kSign[sh] * g1;
+        for (int k = 0; k < K; ++k) {
+          double fh = flux[k] * scale - cflux[(h * N + nh) * 15 + k * 3 + dir];
+          r[h * KN + nh * K + k] -= fh * gp;
+        }
+      }
+      if (s >= 0) {
+        int ns = m->map_s[f * QF + fp];
+        const double *jd = &m->jdi[(s * N + ns) * 9];
+        int dir = kDir[ss];
+        double nrm = sqrt(jd[0 * 3 + dir] * jd[0 * 3 + dir] + jd[1 * 3 + dir] * jd[1 * 3 + dir] +
+                          jd[2 * 3 + dir] * jd[2 * 3 + dir]);
+        double scale = kSign[ss] * nrm, gp = kSign[ss] * g1;
+        for (int k = 0; k < K; ++k) {
+          double fs = flux[k] * (-scale) - cflux[(s * N + ns) * 15 + k * 3 + dir];
+          r[s * KN + ns * K + k] -= fs * gp;
+        }
+      }
+    }
+  }
+  free(cflux);
+  /* divide by det(J) (fr/general.hpp:249-268) */
+#pragma omp parallel for schedule(static) num_threads(orc_get_threads())
+  for (int64_t c = 0; c < m->n_cells; ++c)
+    for (int q = 0; q < N; ++q) {
+      double scale = 1.0 / m->detj[c * N + q];
+      for (int k = 0; k < K; ++k) r[c * KN + q * K + k] *= scale;
+    }
+  return 0;
+}
+
 int orc_dgsem_residual(const orc_mesh *m, int riemann, int n_bc,
                        const orc_bc *bcs, double t, const double *u,
                        double *r) {
+  if (m->scheme == ORC_SCHEME_FR) return fr_residual(m, riemann, n_bc, bcs, t, u, r);
   const int N = m->n, QF = m->qf, KN = K * m->n;
   int64_t L = orc_column_size(m);
   memset(r, 0, sizeof(double) * L);
@@ -555,7 +681,10 @@ double orc_time_step(const orc_mesh *m, const double *u, double dt_guess,
     cfl = kCfl[ro][pp];
   }
   double dt = cfl * min_dt;
-  return fmin(dt, dt_guess);
+  dt = fmin(dt, dt_guess);
+  /* fr::Lobatto::GetTimeStep doubles the base step (fr/lobatto.hpp:220-222) */
+  if (m->scheme == ORC_SCHEME_FR) dt = fmin(dt_guess, 2.0 * dt);
+  return dt;
 }
 
 /* ---------------- Runge-Kutta over a generic residual ---------------- */

@@ -22,7 +22,7 @@ BC_NONE, BC_INVISCID_WALL, BC_SUPERSONIC_INLET, BC_SUPERSONIC_OUTLET, BC_SUBSONI
     BC_SUBSONIC_OUTLET, BC_SMART = range(7)
 STATE_CONSTANT, STATE_MOVING_SPLIT = 0, 1
 HEX8, TET4 = 0, 1
-DGSEM = 0
+DGSEM, FR = 0, 1
 FP64, MIXED = 0, 1
 
 

@@ -109,6 +109,15 @@ void quad4_point(const double *xn, double a, double b, double *x, double *ta,
   }
 }
 
+// Slope at xi = 1 of Huynh's g2 correction function g_R = (P_p + c_prev
+// P_{p-1} + c_next P_{p+1}) / 2 with c_next = p / (2p + 1)
+// (basis/vincent.hpp:30-32, 57-61): P_n'(1) = n (n + 1) / 2.
+double fr_correction_slope(int p) {
+  double c_next = p / (2.0 * p + 1), c_prev = 1 - c_next;
+  auto dp = [](int n) { return n * (n + 1) / 2.0; };
+  return 0.5 * (dp(p) + c_prev * dp(p - 1) + c_next * dp(p + 1));
+}
+
 // Grid index (i, j, k) of hex corner v on a Q-point GLL grid.
 void corner_grid(int v, int q, int *g) {
   for (int d = 0; d < 3; ++d) g[d] = (kHexLocal[v][d] + 1) / 2 * (q - 1);
@@ -225,8 +234,10 @@ int build_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
           if (!(det > 0)) bad_jac = 1;
           double w = wq[i] * wq[j] * wq[k] * det;
           volume += w;
-          // w * J^-1 = (w / det) * adj(J)
-          double s = w / det;
+          // DGSEM: w J^-1 = (w / det) adj(J) and the lumped mass 1/w.
+          // FR: det(J) J^-1 = adj(J) (GetJacobianAssociated) and 1/det(J).
+          const bool fr = h->opt.scheme == MCFD_FR;
+          double s = fr ? 1.0 : w / det;
           double *g = &geo[((size_t)c * N + (i * Q + j) * Q + k) * 10];
           g[0] = s * (J[4] * J[8] - J[5] * J[7]);
           g[1] = s * (J[2] * J[7] - J[1] * J[8]);
@@ -237,7 +248,7 @@ int build_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
           g[6] = s * (J[3] * J[7] - J[4] * J[6]);
           g[7] = s * (J[1] * J[6] - J[0] * J[7]);
           g[8] = s * (J[0] * J[4] - J[1] * J[3]);
-          g[9] = 1.0 / w;
+          g[9] = fr ? 1.0 / det : 1.0 / w;
         }
     rate[c] = 1.0 / (std::cbrt(volume) * 0.5);
   }
@@ -312,8 +323,10 @@ int build_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
         double nrm[3] = {ta[1] * tb[2] - ta[2] * tb[1], ta[2] * tb[0] - ta[0] * tb[2],
                          ta[0] * tb[1] - ta[1] * tb[0]};
         double area = std::sqrt(nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2]);
+        // DGSEM lifts the flux with the face quadrature weight; FR scales it
+        // by the area element |det(J) J^-1 e_dir| of the flux point.
         fgeo[pt] = make_double4(nrm[0] / area, nrm[1] / area, nrm[2] / area,
-                                wq[a] * wq[b] * area);
+                                h->opt.scheme == MCFD_FR ? area : wq[a] * wq[b] * area);
         for (int e = 0; e < 3; ++e) fxyz[pt * 3 + e] = x[e];
         int gi[3], node_h, node_s = -1;
         for (int e = 0; e < 3; ++e)
@@ -655,7 +668,7 @@ int mcfd_create(const mcfd_mesh_desc *mesh, const mcfd_options *options,
     return fail(nullptr, MCFD_ERR_ARGUMENT, "incomplete mesh description");
   if (options->degree < 1 || options->degree > 3)
     return fail(nullptr, MCFD_ERR_UNSUPPORTED, "degree must be 1, 2 or 3");
-  if (options->scheme != MCFD_DGSEM)
+  if (options->scheme != MCFD_DGSEM && options->scheme != MCFD_FR)
     return fail(nullptr, MCFD_ERR_UNSUPPORTED, "unknown scheme");
   if (options->riemann < MCFD_EXACT || options->riemann > MCFD_RUSANOV)
     return fail(nullptr, MCFD_ERR_ARGUMENT, "unknown Riemann solver");
@@ -673,6 +686,8 @@ int mcfd_create(const mcfd_mesh_desc *mesh, const mcfd_options *options,
   h->opt.riemann = options->riemann;
   h->opt.precision = options->precision;
   h->opt.cfl = options->cfl;
+  h->opt.scheme = options->scheme;
+  h->opt.fr_g1 = fr_correction_slope(options->degree);
   int rc = MCFD_OK;
   if (cudaSetDevice(h->device) != cudaSuccess) rc = fail(h, MCFD_ERR_CUDA, "cudaSetDevice failed");
   if (!rc && cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)

@@ -51,7 +51,13 @@ struct FaceArgs {
   double stage_c;
   int64_t n_points;
   int n_groups;
+  int fr;  // flux reconstruction: mark faces without a boundary condition
 };
+
+// FR: a boundary face point without a registered boundary gets no correction
+// (the reference skips such faces); the face kernel marks its flux with this
+// NaN payload and the FR lift skips it.
+constexpr unsigned long long kNoFluxBits = 0x7ff8dead0000beefull;
 
 struct CellArgs {
   const double *u_in;
@@ -64,7 +70,16 @@ struct CellArgs {
   DevState *state;
   int64_t n_cells;
   int advance_time;
+  int fr;     // 0: dg::Lobatto (weak form), 1: fr::Lobatto (Huynh g2)
+  double g1;  // FR: g_R'(1) of the Huynh g2 correction
 };
+
+// FR: axis and orientation of each local hex face (fr/lobatto.hpp:81-152)
+// sides 0..5 -> axes 2, 1, 0, 1, 0, 2 (one nibble per side, side 0 lowest)
+__device__ __forceinline__ int fr_dir(int side) { return (0x201012 >> (4 * side)) & 0xf; }
+__device__ __forceinline__ double fr_sign(int side) {
+  return ((0x2c >> side) & 1) ? 1.0 : -1.0;  // + for faces 2, 3, 5
+}
 
 // FP64 <-> FP32 conversions on the integer pipes.  On this part the FP64
 // unit is the bottleneck and hardware F2F conversions issue there.  These
@@ -165,6 +180,7 @@ __global__ void __launch_bounds__(256) face_flux_kernel(FaceArgs a) {
     } else {
 #pragma unroll
       for (int k = 0; k < kK; ++k) out[k] = 0;
+      if (a.fr) out[0] = __longlong_as_double((long long)kNoFluxBits);
     }
   }
   if (not_converged) atomicOr(&a.state->status, (unsigned)kStatusNotConverged);
@@ -222,23 +238,52 @@ cell_update_kernel(CellArgs a) {
   if (!active) return;
   const int i = q / QF, j = (q / Q) % Q, k = q % Q;
   double res[kK];
+  if (!a.fr) {
+    // weak form: sum_q Ft_q . grad(phi_n)(x_q)
 #pragma unroll
-  for (int r = 0; r < kK; ++r) {
-    double s = 0;
+    for (int r = 0; r < kK; ++r) {
+      double s = 0;
 #pragma unroll
-    for (int m = 0; m < Q; ++m) {
-      s += s_ft[lc][r * 3 + 0][(m * Q + j) * Q + k] * s_d[m * Q + i];
-      s += s_ft[lc][r * 3 + 1][(i * Q + m) * Q + k] * s_d[m * Q + j];
-      s += s_ft[lc][r * 3 + 2][(i * Q + j) * Q + m] * s_d[m * Q + k];
+      for (int m = 0; m < Q; ++m) {
+        s += s_ft[lc][r * 3 + 0][(m * Q + j) * Q + k] * s_d[m * Q + i];
+        s += s_ft[lc][r * 3 + 1][(i * Q + m) * Q + k] * s_d[m * Q + j];
+        s += s_ft[lc][r * 3 + 2][(i * Q + j) * Q + m] * s_d[m * Q + k];
+      }
+      res[r] = s;
     }
-    res[r] = s;
+  } else {
+    // FR: minus the divergence of the interpolated contravariant flux at the
+    // node (fr/general.hpp:271-288)
+#pragma unroll
+    for (int r = 0; r < kK; ++r) {
+      double s = 0;
+#pragma unroll
+      for (int m = 0; m < Q; ++m) {
+        s -= s_ft[lc][r * 3 + 0][(m * Q + j) * Q + k] * s_d[i * Q + m];
+        s -= s_ft[lc][r * 3 + 1][(i * Q + m) * Q + k] * s_d[j * Q + m];
+        s -= s_ft[lc][r * 3 + 2][(i * Q + j) * Q + m] * s_d[k * Q + m];
+      }
+      res[r] = s;
+    }
   }
-  // Surface terms: holder -= flux, sharer += flux (lobatto.hpp:184-189).
+  // Surface terms.  DG: holder -= flux, sharer += flux (lobatto.hpp:184-189).
+  // FR: -= g'(1) (F_out |n| - sigma Ft[:, dir]) at the node
+  // (fr/lobatto.hpp:232-251, fr/general.hpp:296-315).
   const int32_t *cf = a.cell_flux + c * 6 * QF;
   auto lift = [&](int side, int t) {
     int32_t v = cf[side * QF + t];
     if (v == INT32_MIN) return;
     const double *fl = a.flux + (int64_t)(v >= 0 ? v : ~v) * kK;
+    if (a.fr) {
+      const long long b0 = __double_as_longlong(fl[0]);
+      if (((b0 >> 52) & 0x7ff) == 0x7ff && (b0 & 0xFFFFFFFFFFFFFll)) return;  // no boundary
+      const int dir = fr_dir(side);
+      const double sigma = fr_sign(side), out_sign = v >= 0 ? 1.0 : -1.0;
+#pragma unroll
+      for (int r = 0; r < kK; ++r)
+        res[r] -= a.g1 * (out_sign * fl[r] - sigma * s_ft[lc][r * 3 + dir][q]);
+      return;
+    }
     if (v >= 0) {
 #pragma unroll
       for (int r = 0; r < kK; ++r) res[r] -= fl[r];
@@ -348,22 +393,47 @@ cell_update_mixed_kernel(CellArgs a, const float *__restrict__ geo32) {
   if (!active) return;
   const int i = q / QF, j = (q / Q) % Q, k = q % Q;
   float res[kK];
+  if (!a.fr) {
 #pragma unroll
-  for (int rr = 0; rr < kK; ++rr) {
-    float s = 0.f;
+    for (int rr = 0; rr < kK; ++rr) {
+      float s = 0.f;
 #pragma unroll
-    for (int m = 0; m < Q; ++m) {
-      s = fmaf(s_ft[lc][rr * 3 + 0][(m * Q + j) * Q + k], s_d[m * Q + i], s);
-      s = fmaf(s_ft[lc][rr * 3 + 1][(i * Q + m) * Q + k], s_d[m * Q + j], s);
-      s = fmaf(s_ft[lc][rr * 3 + 2][(i * Q + j) * Q + m], s_d[m * Q + k], s);
+      for (int m = 0; m < Q; ++m) {
+        s = fmaf(s_ft[lc][rr * 3 + 0][(m * Q + j) * Q + k], s_d[m * Q + i], s);
+        s = fmaf(s_ft[lc][rr * 3 + 1][(i * Q + m) * Q + k], s_d[m * Q + j], s);
+        s = fmaf(s_ft[lc][rr * 3 + 2][(i * Q + j) * Q + m], s_d[m * Q + k], s);
+      }
+      res[rr] = s;
     }
-    res[rr] = s;
+  } else {
+#pragma unroll
+    for (int rr = 0; rr < kK; ++rr) {
+      float s = 0.f;
+#pragma unroll
+      for (int m = 0; m < Q; ++m) {
+        s = fmaf(-s_ft[lc][rr * 3 + 0][(m * Q + j) * Q + k], s_d[i * Q + m], s);
+        s = fmaf(-s_ft[lc][rr * 3 + 1][(i * Q + m) * Q + k], s_d[j * Q + m], s);
+        s = fmaf(-s_ft[lc][rr * 3 + 2][(i * Q + j) * Q + m], s_d[k * Q + m], s);
+      }
+      res[rr] = s;
+    }
   }
   const int32_t *cf = a.cell_flux + c * 6 * QF;
+  const float g1 = f64_to_f32(a.g1);
   auto lift = [&](int side, int t) {
     int32_t vv = cf[side * QF + t];
     if (vv == INT32_MIN) return;
     const double *fl = a.flux + (int64_t)(vv >= 0 ? vv : ~vv) * kK;
+    if (a.fr) {
+      const long long b0 = __double_as_longlong(fl[0]);
+      if (((b0 >> 52) & 0x7ff) == 0x7ff && (b0 & 0xFFFFFFFFFFFFFll)) return;  // no boundary
+      const int dir = fr_dir(side);
+      const float sigma = fr_sign(side) > 0 ? 1.f : -1.f, out_sign = vv >= 0 ? 1.f : -1.f;
+#pragma unroll
+      for (int rr = 0; rr < kK; ++rr)
+        res[rr] -= g1 * (out_sign * f64_to_f32(fl[rr]) - sigma * s_ft[lc][rr * 3 + dir][q]);
+      return;
+    }
     const float sign = vv >= 0 ? -1.f : 1.f;
 #pragma unroll
     for (int rr = 0; rr < kK; ++rr) res[rr] = fmaf(sign, f64_to_f32(fl[rr]), res[rr]);
@@ -456,11 +526,14 @@ dt_reduce_mixed_kernel(const double *u, const double *cell_rate, int64_t n_nodes
     atomicMax(&state->max_rate_bits, (unsigned long long)__double_as_longlong(rate));
 }
 
-__global__ void dt_finalize_kernel(DevState *state) {
+__global__ void dt_finalize_kernel(DevState *state, int fr) {
   double max_rate = __longlong_as_double((long long)state->max_rate_bits);
   double min_dt = max_rate > 0 ? 1.0 / max_rate : 1.e+100;
   double dt = state->cfl * min_dt;
-  state->dt = fmin(dt, state->dt_guess);
+  dt = fmin(dt, state->dt_guess);
+  // fr::Lobatto::GetTimeStep doubles the base step (fr/lobatto.hpp:220-222)
+  if (fr) dt = fmin(state->dt_guess, 2.0 * dt);
+  state->dt = dt;
   state->max_rate_bits = 0ull;
 }
 
@@ -539,7 +612,7 @@ int launch_face_flux(mcfd_handle *h, const double *u, double stage_c) {
   const Mesh &m = h->mesh;
   FaceArgs fa{u, m.face_cells, m.face_group, m.face_geo, m.face_xyz,
               m.face_map, m.bcs, h->buf.flux, h->buf.state, stage_c,
-              m.n_points, m.n_groups};
+              m.n_points, m.n_groups, h->opt.scheme == 1};
   if (m.n_points == 0) return 0;
   switch (m.q) {
     case 2: face_dispatch_r<2>(h, fa); break;
@@ -553,7 +626,7 @@ int launch_cell_update(mcfd_handle *h, int stage, const double *u_in,
                        const double *u0, double *u_out, int advance_time) {
   const Mesh &m = h->mesh;
   CellArgs ca{u_in, u0, u_out, m.cell_geo, m.cell_flux, h->buf.flux, m.dmat,
-              h->buf.state, m.n_cells, advance_time};
+              h->buf.state, m.n_cells, advance_time, h->opt.scheme == 1, h->opt.fr_g1};
   switch (m.q) {
     case 2: cell_dispatch_s<2>(h, stage, ca); break;
     case 3: cell_dispatch_s<3>(h, stage, ca); break;
@@ -572,7 +645,7 @@ int launch_dt(mcfd_handle *h, const double *u) {
       case 3: dt_reduce_mixed_kernel<3><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state); break;
       default: dt_reduce_mixed_kernel<4><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state); break;
     }
-    dt_finalize_kernel<<<1, 1, 0, h->stream>>>(h->buf.state);
+    dt_finalize_kernel<<<1, 1, 0, h->stream>>>(h->buf.state, h->opt.scheme == 1);
     return 2;
   }
   switch (m.q) {
@@ -580,7 +653,7 @@ int launch_dt(mcfd_handle *h, const double *u) {
     case 3: dt_reduce_kernel<3><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state); break;
     default: dt_reduce_kernel<4><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state); break;
   }
-  dt_finalize_kernel<<<1, 1, 0, h->stream>>>(h->buf.state);
+  dt_finalize_kernel<<<1, 1, 0, h->stream>>>(h->buf.state, h->opt.scheme == 1);
   return 2;
 }
 
@@ -630,9 +703,9 @@ int launch_residual_static_scratch(mcfd_handle *h, const double *d_u,
   const Mesh &m = h->mesh;
   FaceArgs fa{d_u, m.face_cells, m.face_group, m.face_geo, m.face_xyz,
               m.face_map, m.bcs, scratch, h->buf.state, 0.0,
-              m.n_points, m.n_groups};
+              m.n_points, m.n_groups, h->opt.scheme == 1};
   CellArgs ca{d_u, nullptr, d_r, m.cell_geo, m.cell_flux, scratch, m.dmat,
-              h->buf.state, m.n_cells, 0};
+              h->buf.state, m.n_cells, 0, h->opt.scheme == 1, h->opt.fr_g1};
   int n = 0;
   if (m.n_points > 0) {
     switch (m.q) {

@@ -96,7 +96,9 @@ struct Buffers {
 struct Options {
   int riemann = 4;
   int precision = 0;
+  int scheme = 0;     // 0 dg::Lobatto (DGSEM), 1 fr::Lobatto (Huynh g2)
   double cfl = 0;
+  double fr_g1 = 0;   // g_R'(1) of the FR correction function
 };
 
 }  // namespace mcfd

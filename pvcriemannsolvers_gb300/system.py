@@ -67,7 +67,8 @@ class Lobatto:
 
     def __init__(self, mesh: Mesh, degree: int, riemann: str | int = "rusanov",
                  cfl: float = 0.0, device: int = 0, precision: str = "fp64",
-                 limiter: str = "none", weno_w0: float = 0.001, weno_eps: float = 1e-6):
+                 limiter: str = "none", weno_w0: float = 0.001, weno_eps: float = 1e-6,
+                 scheme: str = "dgsem"):
         """precision: "fp64" (plain form) or "mixed" (FP32 volume flux and
         contraction; FP64 Riemann fluxes, lift and RK accumulation).
         limiter: "none", "lazy" (weno::Lazy on every cell) or "detect_lazy"
@@ -102,7 +103,10 @@ class Lobatto:
         desc.face_shift = capi.dptr(fsh)
         opt = capi.Options()
         opt.degree = self.degree
-        opt.scheme = capi.DGSEM
+        if scheme not in ("dgsem", "fr"):
+            raise ValueError("scheme must be 'dgsem' (dg::Lobatto) or 'fr' (fr::Lobatto)")
+        self.scheme = scheme
+        opt.scheme = capi.DGSEM if scheme == "dgsem" else capi.FR
         opt.riemann = self.riemann
         opt.precision = capi.FP64 if precision == "fp64" else capi.MIXED
         opt.cfl = float(cfl)

@@ -169,3 +169,40 @@ def test_bad_inputs_fail_loudly(gpu):
     with pytest.raises(capi.McfdError):
         Lobatto(bad, 2, "rusanov")
     s.close()
+
+
+@pytest.mark.parametrize("riemann", ["rusanov", "roe", "hllc", "exact"])
+@pytest.mark.parametrize("p", [1, 2, 3])
+@pytest.mark.parametrize("periodic,jitter", [((True, True, True), 0.1), ((False, False, False), 0.1)])
+def test_fr_residual_parity(gpu, riemann, p, periodic, jitter):
+    """fr::Lobatto (Huynh g2) residual against the oracle's FR restatement."""
+    m = meshlib.box((4, 3, 3), lengths=(1.0, 0.8, 0.6), periodic=periodic, jitter=jitter, seed=0)
+    s = Lobatto(m, p, riemann, scheme="fr")
+    om = orc.Mesh(m, p, "fr")
+    groups = sorted(set(int(g) for g in m.face_group if g >= 0))
+    apply_bcs(s, om, bc_specs(), groups)
+    u = random_state(m.n_cells * (p + 1) ** 3, seed=p + 10)
+    s.SetSolutionColumn(u)
+    s.SetTime(0.2)
+    err = rel_l2(s.GetResidualColumn(), om.residual(KINDS[riemann], u, 0.2))
+    assert err <= RTOL, err
+    s.close()
+
+
+def test_fr_rk_and_time_step_parity(gpu):
+    m = meshlib.box((4, 4, 3), lengths=(10.0,) * 3, periodic=(True,) * 3, jitter=0.05, seed=2)
+    p = 3
+    s = Lobatto(m, p, "rusanov", cfl=0.1, scheme="fr")
+    om = orc.Mesh(m, p, "fr")
+    x = meshlib.node_coordinates(m, p).reshape(-1, 3)
+    u = cases.vortex_ic(x).ravel()
+    s.SetSolutionColumn(u)
+    t_end = s.advance(3, 1e9, 3, 0.0)
+    t = 0.0
+    for _ in range(3):
+        dt = om.time_step(u, 1e9, 3, 0.1)
+        u = om.rk_update(orc.RUSANOV, 3, t, dt, u)
+        t += dt
+    assert abs(t_end - t) <= 1e-13 * t
+    assert rel_l2(s.GetSolutionColumn(), u) <= RTOL
+    s.close()

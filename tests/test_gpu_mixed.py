@@ -102,3 +102,20 @@ def test_mixed_convergence_order_preserved(gpu):
     order = {k: math.log2(v[0] / v[1]) for k, v in errs.items()}
     assert order["fp64"] > 2.5, errs
     assert abs(order["mixed"] - order["fp64"]) < 0.1, (order, errs)
+
+
+def test_mixed_fr_vortex_density_error(gpu):
+    """fr::Lobatto in the mixed form: 50 steps on 8^3 against the FP64 FR path."""
+    m = cases.vortex_mesh(8)
+    x = meshlib.node_coordinates(m, 3).reshape(-1, 3)
+    u0 = cases.vortex_ic(x).ravel()
+    out = {}
+    for prec in ("fp64", "mixed"):
+        s = Lobatto(m, 3, "rusanov", cfl=0.1, precision=prec, scheme="fr")
+        s.SetSolutionColumn(u0)
+        t = s.advance(50, 1e9, 3, 0.0)
+        out[prec] = (s.GetSolutionColumn(), t)
+        s.close()
+    assert abs(out["mixed"][1] - out["fp64"][1]) <= 1e-6 * out["fp64"][1]
+    err = density_l2(out["mixed"][0], out["fp64"][0])
+    assert err <= MIXED_L2_BAR, err

@@ -97,3 +97,29 @@ def test_limiter_keeps_advance_graph_consistent(gpu):
         out.append(s.GetSolutionColumn())
         s.close()
     assert rel_l2(out[0], out[1]) <= 1e-14
+
+
+def test_limited_fr_rk3_parity(gpu):
+    """WithLimiter<fr::Lobatto>: the same Sod tube with the FR scheme."""
+    p = 2
+    m = cases.sod_mesh(20, 2, 2)
+    x = meshlib.node_coordinates(m, p).reshape(-1, 3)
+    u0 = cases.sod_ic(x).ravel()
+    s = Lobatto(m, p, "roe", limiter="detect_lazy", scheme="fr")
+    cases.sod_bc(s)
+    om = orc.Mesh(m, p, "fr")
+    om.set_bcs({0: (orc.BC_SMART, cases.SOD_LEFT), 1: (orc.BC_SMART, cases.SOD_RIGHT),
+                2: (orc.BC_INVISCID_WALL, None), 3: (orc.BC_INVISCID_WALL, None),
+                4: (orc.BC_INVISCID_WALL, None), 5: (orc.BC_INVISCID_WALL, None)})
+    lim = orc.Limiter(om, MODES["detect_lazy"])
+    s.SetSolutionColumn(u0)
+    u, _ = lim.limit(u0)
+    t = 0.0
+    for _ in range(3):
+        dt = om.time_step(u, 1.0, 3, 0.1)
+        RungeKutta(3).Update(s, t, dt)
+        u = lim.rk_update(orc.ROE, 3, t, dt, u)
+        t += dt
+    err = rel_l2(s.GetSolutionColumn(), u)
+    assert err <= RTOL, err
+    s.close()

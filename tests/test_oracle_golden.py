@@ -213,3 +213,18 @@ def test_freestream_preservation():
         u = cases.prim_to_cons(np.ones(len(x)), 0.3, -0.2, 0.5, 1.0).ravel()
         for kind in (orc.EXACT, orc.HLLC, orc.AUSM, orc.ROE, orc.RUSANOV):
             assert np.abs(om.residual(kind, u)).max() < 1e-12
+
+
+@pytest.mark.parametrize("p", [1, 2, 3])
+def test_fr_lobatto_equals_dgsem_residual(p):
+    """FR with Huynh's g2 correction on GLL points is DGSEM
+    (test/spatial/fr.cpp:82-97 checks FR::General == FR::Lobatto to 1e-15;
+    test/spatial/dg.cpp:196-259 compares FEM and SEM residual pieces): the
+    oracle's two restatements agree to rounding on a jittered periodic mesh."""
+    m = meshlib.box((3, 3, 2), lengths=(10, 10, 10), periodic=(True,) * 3, jitter=0.05, seed=1)
+    x = meshlib.node_coordinates(m, p).reshape(-1, 3)
+    u = cases.vortex_ic(x).ravel()
+    for kind in (orc.RUSANOV, orc.ROE, orc.HLLC):
+        a = orc.Mesh(m, p).residual(kind, u)
+        b = orc.Mesh(m, p, "fr").residual(kind, u)
+        assert np.linalg.norm(a - b) / np.linalg.norm(a) < 1e-13
