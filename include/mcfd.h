@@ -103,13 +103,17 @@ enum mcfd_cell_type { MCFD_HEX8 = 0, MCFD_TET4 = 1 };
 /* Unstructured mesh, the input that replaces mesh::part::Part
  * (include/mini/mesh/part.hpp:97-291):
  *   xyz          [n_nodes][3] node coordinates
- *   cell_nodes   [n_cells][8] node ids in CGNS order (Hex8)
- *   cell_type    [n_cells] enum mcfd_cell_type, or NULL for all Hex8
+ *   cell_nodes   [n_cells][8] node ids in CGNS order; a Tet4 cell uses the
+ *                first 4 slots (the rest are ignored)
+ *   cell_type    [n_cells] enum mcfd_cell_type, or NULL for all Hex8.
+ *                Tet4 cells are accepted by the MODAL scheme only.
  *   face_cells   [n_faces][2] holder, sharer (-1 on a boundary).  The face
  *                normal points from the holder to the sharer (outward on a
  *                boundary), as in part.hpp:1518-1538.
- *   face_sides   [n_faces][2] local face index (0..5, the order of
- *                coordinate/hexahedron.hpp:378-389) in the holder and sharer
+ *   face_sides   [n_faces][2] local face index in the holder and sharer:
+ *                Hex8 0..5 in the order of coordinate/hexahedron.hpp:378-389,
+ *                Tet4 0..3 in the order of Tetrahedron4::faces_
+ *                (coordinate/tetrahedron.hpp:141-147)
  *   face_group   [n_faces] boundary group id (>= 0) or -1 for interior faces
  *   face_shift   [n_faces][3] or NULL: periodic translation such that
  *                x(sharer side) + shift = x(holder side).  The reference has
@@ -128,12 +132,21 @@ typedef struct mcfd_mesh_desc {
   const double *face_shift;
 } mcfd_mesh_desc;
 
-/* Spatial schemes on GLL-collocated hexahedra:
+/* Spatial schemes:
  *   DGSEM: dg::Lobatto, weak form with lumped mass (spatial/dg/lobatto.hpp)
+ *          on GLL-collocated hexahedra
  *   FR:    fr::Lobatto, flux reconstruction with Huynh's g2 correction
  *          (spatial/fr/general.hpp, spatial/fr/lobatto.hpp, basis/vincent.hpp);
- *          its time step is twice the DGSEM one (fr/lobatto.hpp:220-222). */
-enum mcfd_scheme { MCFD_DGSEM = 0, MCFD_FR = 1 };
+ *          its time step is twice the DGSEM one (fr/lobatto.hpp:220-222)
+ *   MODAL: dg::General over polynomial::Projection (spatial/dg/general.hpp,
+ *          polynomial/projection.hpp) on Hex8 and Tet4 cells: per-cell
+ *          orthonormal Taylor basis, column block [M][K] per cell with
+ *          M = (p+1)(p+2)(p+3)/6.  Quadrature: Hex8 Gauss-Legendre (p+1)^3,
+ *          Quad4 faces (p+1)^2; Tet4 14 points (p <= 2) or 24 points (p = 3),
+ *          Tri3 faces 6 points (p <= 2) or 12 points (p = 3)
+ *          (integrator/{legendre,tetrahedron,triangle}.hpp).  FP64 only, no
+ *          limiter. */
+enum mcfd_scheme { MCFD_DGSEM = 0, MCFD_FR = 1, MCFD_MODAL = 2 };
 enum mcfd_precision { MCFD_FP64 = 0, MCFD_MIXED = 1 };
 
 /* Limiter applied after every solution update (spatial/with_limiter.hpp:56-65):
@@ -254,6 +267,20 @@ int64_t mcfd_launch_count(const mcfd_handle *h);
  * left unchanged).  out_ms[0] = dt reduction, [1] = face fluxes,
  * [2] = cell update (volume + lift + mass + stage), [3] = whole RK3 step. */
 int mcfd_kernel_times(mcfd_handle *h, int32_t reps, double *out_ms);
+
+/* Approximate (spatial/fem.hpp:147-154 -> Projection::Approximate,
+ * polynomial/projection.hpp:28-42) of the MODAL scheme, split so that the
+ * initial-value function runs on the caller's side:
+ *   mcfd_point_count   number of volume quadrature points (all cells, cell by
+ *                      cell in integrator order)
+ *   mcfd_points        their global coordinates [n][3]
+ *   mcfd_project       sets the solution to the projection of the values
+ *                      [n][K] given at those points (coeff = sum_q f_q psi w_q)
+ * Nodal schemes return MCFD_ERR_UNSUPPORTED (their Approximate is the value
+ * at each node, i.e. mcfd_set_solution). */
+int64_t mcfd_point_count(const mcfd_handle *h);
+int mcfd_points(const mcfd_handle *h, double *xyz, int64_t n);
+int mcfd_project(mcfd_handle *h, const double *values, int64_t n);
 
 /* Message describing the last failure on this handle (or of mcfd_create when
  * h is NULL).  Valid until the next call on the handle. */

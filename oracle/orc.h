@@ -154,6 +154,39 @@ int orc_rk_update_limited(const orc_mesh *m, int riemann, int n_bc,
                           double *u, const orc_limiter *l, int mode, double w0,
                           double eps);
 
+/* ---- modal DG: dg::General over Projection on Hex8 / Tet4 (orc_modal.c) ---- */
+enum { ORC_CELL_HEX8 = 0, ORC_CELL_TET4 = 1 };
+typedef struct orc_modal orc_modal;
+/* Same mesh description as orc_mesh_create plus cell types (NULL: all Hex8);
+ * a Tet4 cell uses the first 4 of its 8 cell_nodes entries (CGNS order) and
+ * local faces 0..3 of Tetrahedron4::faces_.  Column layout per cell: [M][K]. */
+orc_modal *orc_modal_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
+                            const int64_t *cell_nodes, const int32_t *cell_type,
+                            int64_t n_faces, const int64_t *face_cells,
+                            const int32_t *face_sides, const int32_t *face_group,
+                            const double *face_shift, int degree);
+void orc_modal_destroy(orc_modal *m);
+int64_t orc_modal_column_size(const orc_modal *m);
+int orc_modal_basis_count(const orc_modal *m);
+/* volume quadrature points of all cells, cell by cell in integrator order */
+int64_t orc_modal_point_count(const orc_modal *m);
+int orc_modal_points(const orc_modal *m, double *xyz, double *weights);
+int64_t orc_modal_face_point_count(const orc_modal *m);
+int orc_modal_face_points(const orc_modal *m, double *xyz, double *weights,
+                          double *frames);
+double orc_modal_cell_length(const orc_modal *m, int64_t c);
+/* solution values [points][K] at the volume points */
+int orc_modal_values(const orc_modal *m, const double *u, double *values);
+/* Approximate from values [points][K] at the volume points */
+int orc_modal_project(const orc_modal *m, const double *values, double *u);
+int orc_modal_residual(const orc_modal *m, int riemann, int n_bc,
+                       const orc_bc *bcs, double t, const double *u, double *r);
+double orc_modal_time_step(const orc_modal *m, const double *u, double dt_guess,
+                           int rk_order, double cfl);
+int orc_modal_rk_update(const orc_modal *m, int riemann, int n_bc,
+                        const orc_bc *bcs, int order, double t, double dt,
+                        double *u);
+
 #ifdef __cplusplus
 }
 #endif

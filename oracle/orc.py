@@ -307,3 +307,112 @@ class Limiter:
         self.lib.orc_rk_update_limited(self.mesh._m, riemann, n, arr, order, t, dt, _p(u), self._l,
                                        self.mode, self.w0, self.eps)
         return u
+
+
+def _modal_sigs(lib):
+    P64, P32 = C.POINTER(C.c_int64), C.POINTER(C.c_int32)
+    sig = {
+        "orc_modal_create": (C.c_void_p, [C.c_int64, _D, C.c_int64, P64, P32, C.c_int64, P64, P32, P32,
+                                          _D, C.c_int]),
+        "orc_modal_destroy": (None, [C.c_void_p]),
+        "orc_modal_column_size": (C.c_int64, [C.c_void_p]),
+        "orc_modal_basis_count": (C.c_int, [C.c_void_p]),
+        "orc_modal_point_count": (C.c_int64, [C.c_void_p]),
+        "orc_modal_points": (C.c_int, [C.c_void_p, _D, _D]),
+        "orc_modal_face_point_count": (C.c_int64, [C.c_void_p]),
+        "orc_modal_face_points": (C.c_int, [C.c_void_p, _D, _D, _D]),
+        "orc_modal_cell_length": (C.c_double, [C.c_void_p, C.c_int64]),
+        "orc_modal_values": (C.c_int, [C.c_void_p, _D, _D]),
+        "orc_modal_project": (C.c_int, [C.c_void_p, _D, _D]),
+        "orc_modal_residual": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(OrcBc), C.c_double, _D, _D]),
+        "orc_modal_time_step": (C.c_double, [C.c_void_p, _D, C.c_double, C.c_int, C.c_double]),
+        "orc_modal_rk_update": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(OrcBc), C.c_int, C.c_double,
+                                          C.c_double, _D]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+class Modal:
+    """Oracle-side modal DG system (dg::General over Projection) on a Hex8 /
+    Tet4 mesh description; column layout per cell [M][5]."""
+
+    def __init__(self, mesh, degree: int):
+        lib = load()
+        _modal_sigs(lib)
+        ct = mesh.cell_type if mesh.cell_type is not None else np.zeros(mesh.n_cells, np.int32)
+        self._keep = [np.ascontiguousarray(mesh.xyz, dtype=np.float64),
+                      np.ascontiguousarray(mesh.cell_nodes, dtype=np.int64),
+                      np.ascontiguousarray(ct, dtype=np.int32),
+                      np.ascontiguousarray(mesh.face_cells, dtype=np.int64),
+                      np.ascontiguousarray(mesh.face_sides, dtype=np.int32),
+                      np.ascontiguousarray(mesh.face_group, dtype=np.int32),
+                      np.ascontiguousarray(mesh.face_shift, dtype=np.float64)]
+        xyz, cn, ct, fc, fs, fg, fsh = self._keep
+        P64, P32 = C.POINTER(C.c_int64), C.POINTER(C.c_int32)
+        self._m = lib.orc_modal_create(xyz.shape[0], _p(xyz), cn.shape[0], cn.ctypes.data_as(P64),
+                                       ct.ctypes.data_as(P32), fc.shape[0], fc.ctypes.data_as(P64),
+                                       fs.ctypes.data_as(P32), fg.ctypes.data_as(P32), _p(fsh), degree)
+        if not self._m:
+            raise RuntimeError("oracle rejected the modal mesh")
+        self.lib = lib
+        self.degree = degree
+        self.n_cells = cn.shape[0]
+        self.m = int(lib.orc_modal_basis_count(self._m))
+        self.column_size = int(lib.orc_modal_column_size(self._m))
+        self.n_points = int(lib.orc_modal_point_count(self._m))
+        self.bcs = make_bcs({})
+
+    def __del__(self):
+        if getattr(self, "_m", None):
+            self.lib.orc_modal_destroy(self._m)
+            self._m = None
+
+    def set_bcs(self, specs: dict[int, tuple]) -> None:
+        self.bcs = make_bcs(specs)
+
+    def points(self):
+        xyz = np.empty((self.n_points, 3))
+        w = np.empty(self.n_points)
+        self.lib.orc_modal_points(self._m, _p(xyz), _p(w))
+        return xyz, w
+
+    def face_points(self):
+        n = int(self.lib.orc_modal_face_point_count(self._m))
+        xyz, w, fr = np.empty((n, 3)), np.empty(n), np.empty((n, 3, 3))
+        self.lib.orc_modal_face_points(self._m, _p(xyz), _p(w), _p(fr))
+        return xyz, w, fr
+
+    def cell_length(self, c: int) -> float:
+        return float(self.lib.orc_modal_cell_length(self._m, c))
+
+    def values(self, u: np.ndarray) -> np.ndarray:
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        v = np.empty((self.n_points, 5))
+        self.lib.orc_modal_values(self._m, _p(u), _p(v))
+        return v
+
+    def project(self, values: np.ndarray) -> np.ndarray:
+        values = np.ascontiguousarray(values, dtype=np.float64).reshape(self.n_points, 5)
+        u = np.empty(self.column_size)
+        self.lib.orc_modal_project(self._m, _p(values), _p(u))
+        return u
+
+    def residual(self, riemann: int, u: np.ndarray, t: float = 0.0) -> np.ndarray:
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        r = np.empty_like(u)
+        n, arr = self.bcs
+        self.lib.orc_modal_residual(self._m, riemann, n, arr, t, _p(u), _p(r))
+        return r
+
+    def time_step(self, u: np.ndarray, dt_guess: float, rk_order: int, cfl: float = 0.0) -> float:
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        return float(self.lib.orc_modal_time_step(self._m, _p(u), dt_guess, rk_order, cfl))
+
+    def rk_update(self, riemann: int, order: int, t: float, dt: float, u: np.ndarray) -> np.ndarray:
+        u = np.array(u, dtype=np.float64, copy=True)
+        n, arr = self.bcs
+        self.lib.orc_modal_rk_update(self._m, riemann, n, arr, order, t, dt, _p(u))
+        return u

@@ -689,10 +689,9 @@ double orc_time_step(const orc_mesh *m, const double *u, double dt_guess,
 
 /* ---------------- Runge-Kutta over a generic residual ---------------- */
 
-typedef int (*residual_fn)(void *ctx, double t, const double *u, double *r);
 
 /* Euler::NextSolution: u_next = u + (R(u) * dt)   (ode.hpp:121-128) */
-static void next_solution(residual_fn fn, void *ctx, int64_t L, double t,
+static void next_solution(orc_residual_fn fn, void *ctx, int64_t L, double t,
                           double dt, const double *u, double *u_next,
                           double *r) {
   fn(ctx, t, u, r);
@@ -700,11 +699,8 @@ static void next_solution(residual_fn fn, void *ctx, int64_t L, double t,
   for (int64_t i = 0; i < L; ++i) u_next[i] = u[i] + r[i] * dt;
 }
 
-/* Hook run after every SetSolutionColumn (the limiter of WithLimiter). */
-typedef void (*set_hook)(void *ctx, double *u);
-
-static int rk_update(residual_fn fn, void *ctx, int64_t L, int order, double t,
-                     double dt, double *u, set_hook hook, void *hook_ctx) {
+int orc_rk_generic(orc_residual_fn fn, void *ctx, int64_t L, int order, double t,
+                     double dt, double *u, orc_set_hook hook, void *hook_ctx) {
   double *u_curr = (double *)malloc(sizeof(double) * L);
   double *u_tmp = (double *)malloc(sizeof(double) * L);
   double *r = (double *)malloc(sizeof(double) * L);
@@ -774,7 +770,7 @@ static int dg_residual_fn(void *ctx, double t, const double *u, double *r) {
 int orc_rk_update(const orc_mesh *m, int riemann, int n_bc, const orc_bc *bcs,
                   int order, double t, double dt, double *u) {
   dg_ctx ctx = {m, riemann, n_bc, bcs};
-  return rk_update(dg_residual_fn, &ctx, orc_column_size(m), order, t, dt, u,
+  return orc_rk_generic(dg_residual_fn, &ctx, orc_column_size(m), order, t, dt, u,
                    NULL, NULL);
 }
 
@@ -784,7 +780,7 @@ int orc_rk_update_limited(const orc_mesh *m, int riemann, int n_bc,
                           double eps) {
   dg_ctx ctx = {m, riemann, n_bc, bcs};
   limit_ctx lc = {l, mode, w0, eps};
-  return rk_update(dg_residual_fn, &ctx, orc_column_size(m), order, t, dt, u,
+  return orc_rk_generic(dg_residual_fn, &ctx, orc_column_size(m), order, t, dt, u,
                    (l && mode != ORC_LIMITER_NONE) ? limit_hook : NULL, &lc);
 }
 
@@ -807,5 +803,5 @@ static int lin_residual_fn(void *ctx, double t, const double *u, double *r) {
 int orc_rk_update_linear(int order, int64_t n, const double *a, double t,
                          double dt, double *u) {
   lin_ctx ctx = {n, a};
-  return rk_update(lin_residual_fn, &ctx, n, order, t, dt, u, NULL, NULL);
+  return orc_rk_generic(lin_residual_fn, &ctx, n, order, t, dt, u, NULL, NULL);
 }

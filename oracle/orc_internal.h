@@ -15,4 +15,18 @@ const double *orc_mesh_face_shift(const orc_mesh *m);
 /* Hex8 LocalToGlobal(0, 0, 0) of every cell, [cells][3]. */
 void orc_cell_centers(const orc_mesh *m, double *center);
 
+/* Taylor monomials about a centre (basis/taylor.hpp:198-218), t [M] at the
+ * offset d = x - centre; gradients g [3][M]. */
+void orc_taylor_values(int M, const double *d, double *t);
+void orc_taylor_grad(int M, const double *d, double *g);
+/* OrthoNormalize (integrator/function.hpp:139-172). */
+void orc_orthonormalize(int M, int nq, const double *T, const double *W, double *S);
+
+/* RungeKutta<order>::Update (temporal/rk.hpp:16-49) over any residual; the
+ * hook runs after every SetSolutionColumn. */
+typedef int (*orc_residual_fn)(void *ctx, double t, const double *u, double *r);
+typedef void (*orc_set_hook)(void *ctx, double *u);
+int orc_rk_generic(orc_residual_fn fn, void *ctx, int64_t L, int order, double t,
+                   double dt, double *u, orc_set_hook hook, void *hook_ctx);
+
 #endif /* MCFD_ORACLE_ORC_INTERNAL_H_ */

@@ -41,10 +41,56 @@ static double ipow(double x, int e) {
   return r;
 }
 
-static void taylor_values(int M, const double *d, double *t) {
+void orc_taylor_values(int M, const double *d, double *t) {
   for (int j = 0; j < M; ++j)
     t[j] = ipow(d[0], kTaylorExp[j][0]) * ipow(d[1], kTaylorExp[j][1]) *
            ipow(d[2], kTaylorExp[j][2]);
+}
+
+/* Taylor::GetGradValue with the identity coefficient: g[d][j] = d T_j / d x_d. */
+void orc_taylor_grad(int M, const double *d, double *g) {
+  for (int dd = 0; dd < 3; ++dd)
+    for (int j = 0; j < M; ++j) {
+      int e = kTaylorExp[j][dd];
+      if (e == 0) { g[dd * M + j] = 0; continue; }
+      double v = e;
+      for (int o = 0; o < 3; ++o) v *= ipow(d[o], kTaylorExp[j][o] - (o == dd));
+      g[dd * M + j] = v;
+    }
+}
+
+/* OrthoNormalize (integrator/function.hpp:139-172): the lower-triangular S
+ * whose rows are the Gram-Schmidt orthonormalised Taylor monomials under the
+ * quadrature (T [nq][M] monomial values, w [nq] global weights); S [M][M]. */
+void orc_orthonormalize(int M, int nq, const double *T, const double *W, double *S) {
+  double A[20 * 20] = {0};
+  const int N = nq;
+  /* A = Integrate(T T^T) with global weights */
+  for (int i = 0; i < M; ++i)
+    for (int j = 0; j < M; ++j) {
+      double s = 0;
+      for (int q = 0; q < N; ++q) s += T[q * M + i] * T[q * M + j] * W[q];
+      A[i * M + j] = s;
+    }
+  /* OrthoNormalize (integrator/function.hpp:139-172) */
+  for (int i = 0; i < M; ++i)
+    for (int j = 0; j < M; ++j) S[i * M + j] = (i == j);
+  S[0] = 1 / sqrt(A[0]);
+  for (int i = 1; i < M; ++i) {
+    for (int j = 0; j < i; ++j) {
+      double temp = 0;
+      for (int k = 0; k <= j; ++k) temp += S[j * M + k] * A[k * M + i];
+      for (int ll = 0; ll <= j; ++ll) S[i * M + ll] -= temp * S[j * M + ll];
+    }
+    double norm_sq = 0;
+    for (int j = 0; j <= i; ++j) {
+      double sum = 0, sij = S[i * M + j];
+      for (int k = 0; k < j; ++k) sum += 2 * S[i * M + k] * A[k * M + j];
+      norm_sq += sij * (sij * A[j * M + j] + sum);
+    }
+    double inv = sqrt(norm_sq);
+    for (int j = 0; j < M; ++j) S[i * M + j] /= inv;
+  }
 }
 
 static double falling(int e, int a) { /* e! / (e - a)! */
@@ -127,43 +173,18 @@ orc_limiter *orc_limiter_create(const orc_mesh *mesh) {
   }
 #pragma omp parallel for schedule(static) num_threads(orc_get_threads())
   for (int64_t c = 0; c < C; ++c) {
-    double A[20 * 20] = {0}, T[64 * 20];
+    double T[64 * 20];
     double *S = &l->s[c * M * M];
     const double *W = &l->w[c * N];
     double vol = 0;
     for (int q = 0; q < N; ++q) {
       double d[3];
       for (int e = 0; e < 3; ++e) d[e] = l->xyz[(c * N + q) * 3 + e] - l->center[c * 3 + e];
-      taylor_values(M, d, &T[q * M]);
+      orc_taylor_values(M, d, &T[q * M]);
       vol += W[q];
     }
     l->volume[c] = vol;
-    /* A = Integrate(T T^T) with global weights */
-    for (int i = 0; i < M; ++i)
-      for (int j = 0; j < M; ++j) {
-        double s = 0;
-        for (int q = 0; q < N; ++q) s += T[q * M + i] * T[q * M + j] * W[q];
-        A[i * M + j] = s;
-      }
-    /* OrthoNormalize (integrator/function.hpp:139-172) */
-    for (int i = 0; i < M; ++i)
-      for (int j = 0; j < M; ++j) S[i * M + j] = (i == j);
-    S[0] = 1 / sqrt(A[0]);
-    for (int i = 1; i < M; ++i) {
-      for (int j = 0; j < i; ++j) {
-        double temp = 0;
-        for (int k = 0; k <= j; ++k) temp += S[j * M + k] * A[k * M + i];
-        for (int ll = 0; ll <= j; ++ll) S[i * M + ll] -= temp * S[j * M + ll];
-      }
-      double norm_sq = 0;
-      for (int j = 0; j <= i; ++j) {
-        double sum = 0, sij = S[i * M + j];
-        for (int k = 0; k < j; ++k) sum += 2 * S[i * M + k] * A[k * M + j];
-        norm_sq += sij * (sij * A[j * M + j] + sum);
-      }
-      double inv = sqrt(norm_sq);
-      for (int j = 0; j < M; ++j) S[i * M + j] /= inv;
-    }
+    orc_orthonormalize(M, N, T, W, S);
     for (int q = 0; q < N; ++q)
       for (int m = 0; m < M; ++m) {
         double s = 0;
@@ -189,7 +210,7 @@ static void modal_value(const orc_limiter *l, int64_t c, const double *cm,
   const int M = l->m;
   double d[3], t[20], psi[20];
   for (int e = 0; e < 3; ++e) d[e] = x[e] - l->center[c * 3 + e];
-  taylor_values(M, d, t);
+  orc_taylor_values(M, d, t);
   const double *S = &l->s[c * M * M];
   for (int m = 0; m < M; ++m) {
     double s = 0;

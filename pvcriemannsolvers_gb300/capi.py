@@ -22,7 +22,8 @@ BC_NONE, BC_INVISCID_WALL, BC_SUPERSONIC_INLET, BC_SUPERSONIC_OUTLET, BC_SUBSONI
     BC_SUBSONIC_OUTLET, BC_SMART = range(7)
 STATE_CONSTANT, STATE_MOVING_SPLIT = 0, 1
 HEX8, TET4 = 0, 1
-DGSEM, FR = 0, 1
+DGSEM, FR, MODAL = 0, 1, 2
+SCHEME = {"dgsem": DGSEM, "fr": FR, "modal": MODAL}
 FP64, MIXED = 0, 1
 
 
@@ -97,6 +98,9 @@ SIGNATURES = {
     "mcfd_kernel_times": (C.c_int, [_P, C.c_int32, _D]),
     "mcfd_limit": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "mcfd_troubled_cells": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "mcfd_point_count": (C.c_int64, [_P]),
+    "mcfd_points": (C.c_int, [_P, _D, C.c_int64]),
+    "mcfd_project": (C.c_int, [_P, _D, C.c_int64]),
 }
 LIMITER = {"none": 0, "lazy": 1, "detect_lazy": 2}
 

@@ -159,6 +159,11 @@ void release(mcfd_handle *h) {
                    l.modal, l.troubled};
   for (void *p : lptrs)
     if (p) cudaFree(p);
+  auto &md = h->modal;
+  void *mptrs[] = {md.center, md.s, md.vol_off, md.vol, md.cell_faces, md.face_off,
+                   md.point_face, md.fpt, md.fnrm, md.fshift, md.taylor, md.values};
+  for (void *p : mptrs)
+    if (p) cudaFree(p);
   if (h->step_graph) cudaGraphExecDestroy(h->step_graph);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
 }
@@ -668,8 +673,12 @@ int mcfd_create(const mcfd_mesh_desc *mesh, const mcfd_options *options,
     return fail(nullptr, MCFD_ERR_ARGUMENT, "incomplete mesh description");
   if (options->degree < 1 || options->degree > 3)
     return fail(nullptr, MCFD_ERR_UNSUPPORTED, "degree must be 1, 2 or 3");
-  if (options->scheme != MCFD_DGSEM && options->scheme != MCFD_FR)
+  if (options->scheme != MCFD_DGSEM && options->scheme != MCFD_FR && options->scheme != MCFD_MODAL)
     return fail(nullptr, MCFD_ERR_UNSUPPORTED, "unknown scheme");
+  if (options->scheme == MCFD_MODAL &&
+      (options->precision != MCFD_FP64 || options->limiter != MCFD_LIMITER_NONE))
+    return fail(nullptr, MCFD_ERR_UNSUPPORTED,
+                "the modal scheme is built in FP64 without a limiter");
   if (options->riemann < MCFD_EXACT || options->riemann > MCFD_RUSANOV)
     return fail(nullptr, MCFD_ERR_ARGUMENT, "unknown Riemann solver");
   if (options->precision != MCFD_FP64 && options->precision != MCFD_MIXED)
@@ -693,7 +702,9 @@ int mcfd_create(const mcfd_mesh_desc *mesh, const mcfd_options *options,
   if (!rc && cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
     rc = fail(h, MCFD_ERR_CUDA, "cudaStreamCreate failed");
   h->own_stream = true;
-  if (!rc) rc = build_mesh(h, mesh, options->degree);
+  if (!rc)
+    rc = options->scheme == MCFD_MODAL ? mcfd::build_modal_mesh(h, mesh, options->degree)
+                                       : build_mesh(h, mesh, options->degree);
   if (!rc && options->limiter != MCFD_LIMITER_NONE) {
     if (options->limiter != MCFD_LIMITER_LAZY && options->limiter != MCFD_LIMITER_DETECT_LAZY)
       rc = fail(h, MCFD_ERR_ARGUMENT, "unknown limiter");
@@ -853,6 +864,8 @@ int mcfd_residual_device_noalloc(mcfd_handle *h, const double *d_u,
                                  double *d_residual, int64_t n) {
   if (!h || !d_u || !d_residual) return MCFD_ERR_ARGUMENT;
   if (n != h->mesh.column) return fail(h, MCFD_ERR_ARGUMENT, "column size mismatch");
+  if (h->opt.scheme == MCFD_MODAL)
+    return fail(h, MCFD_ERR_UNSUPPORTED, "the no-allocation residual covers the nodal schemes");
   if (h->mesh.n_points * mcfd::kK > mcfd::kStaticFluxCapacity)
     return fail(h, MCFD_ERR_ARGUMENT,
                 "mesh too large for the no-allocation residual: " +
@@ -950,12 +963,42 @@ int mcfd_synchronize(mcfd_handle *h) {
 
 int mcfd_face_node_maps(const mcfd_handle *h, int16_t *holder, int16_t *sharer) {
   if (!h || !holder || !sharer) return MCFD_ERR_ARGUMENT;
+  if (h->opt.scheme == MCFD_MODAL) return MCFD_ERR_UNSUPPORTED;
   std::memcpy(holder, h->mesh.map_h.data(), sizeof(int16_t) * h->mesh.map_h.size());
   std::memcpy(sharer, h->mesh.map_s.data(), sizeof(int16_t) * h->mesh.map_s.size());
   return MCFD_OK;
 }
 
 int64_t mcfd_launch_count(const mcfd_handle *h) { return h ? h->launches : -1; }
+
+int64_t mcfd_point_count(const mcfd_handle *h) {
+  if (!h) return -1;
+  return h->opt.scheme == MCFD_MODAL ? h->modal.n_vol : 0;
+}
+
+int mcfd_points(const mcfd_handle *h, double *xyz, int64_t n) {
+  if (!h || !xyz) return MCFD_ERR_ARGUMENT;
+  if (h->opt.scheme != MCFD_MODAL) return MCFD_ERR_UNSUPPORTED;
+  if (n != h->modal.n_vol) return MCFD_ERR_ARGUMENT;
+  std::memcpy(xyz, h->modal.host_points.data(), sizeof(double) * 3 * n);
+  return MCFD_OK;
+}
+
+int mcfd_project(mcfd_handle *h, const double *values, int64_t n) {
+  if (!h || !values) return MCFD_ERR_ARGUMENT;
+  if (h->opt.scheme != MCFD_MODAL)
+    return fail(h, MCFD_ERR_UNSUPPORTED, "mcfd_project belongs to the modal scheme");
+  if (n != h->modal.n_vol) return fail(h, MCFD_ERR_ARGUMENT, "point count mismatch");
+  cudaSetDevice(h->device);
+  if (!h->modal.values)
+    CUDA_TRY(h, cudaMalloc(&h->modal.values, sizeof(double) * mcfd::kK * n));
+  CUDA_TRY(h, cudaMemcpyAsync(h->modal.values, values, sizeof(double) * mcfd::kK * n,
+                              cudaMemcpyHostToDevice, h->stream));
+  h->launches += mcfd::launch_modal_project(h, h->buf.u);
+  CUDA_TRY(h, cudaGetLastError());
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  return MCFD_OK;
+}
 
 int mcfd_kernel_times(mcfd_handle *h, int32_t reps, double *out_ms) {
   if (!h || !out_ms || reps < 1) return MCFD_ERR_ARGUMENT;

@@ -609,6 +609,7 @@ int launch_set_state(mcfd_handle *h, double t, double dt, double dt_guess,
 }
 
 int launch_face_flux(mcfd_handle *h, const double *u, double stage_c) {
+  if (h->opt.scheme == kSchemeModal) return launch_modal_face_flux(h, u, stage_c);
   const Mesh &m = h->mesh;
   FaceArgs fa{u, m.face_cells, m.face_group, m.face_geo, m.face_xyz,
               m.face_map, m.bcs, h->buf.flux, h->buf.state, stage_c,
@@ -624,6 +625,8 @@ int launch_face_flux(mcfd_handle *h, const double *u, double stage_c) {
 
 int launch_cell_update(mcfd_handle *h, int stage, const double *u_in,
                        const double *u0, double *u_out, int advance_time) {
+  if (h->opt.scheme == kSchemeModal)
+    return launch_modal_cell_update(h, stage, u_in, u0, u_out, advance_time);
   const Mesh &m = h->mesh;
   CellArgs ca{u_in, u0, u_out, m.cell_geo, m.cell_flux, h->buf.flux, m.dmat,
               h->buf.state, m.n_cells, advance_time, h->opt.scheme == 1, h->opt.fr_g1};
@@ -636,6 +639,7 @@ int launch_cell_update(mcfd_handle *h, int stage, const double *u_in,
 }
 
 int launch_dt(mcfd_handle *h, const double *u) {
+  if (h->opt.scheme == kSchemeModal) return launch_modal_dt(h, u);
   const Mesh &m = h->mesh;
   int64_t nodes = m.n_cells * m.n;
   unsigned blocks = (unsigned)((nodes + 255) / 256);

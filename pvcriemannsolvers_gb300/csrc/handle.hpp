@@ -9,6 +9,8 @@
 #include <string>
 #include <vector>
 
+struct mcfd_mesh_desc;
+
 namespace mcfd {
 
 // Device-side scalars of the time loop.  t and dt live on the device so a
@@ -84,6 +86,28 @@ struct Limiter {
   unsigned long long *troubled = nullptr;  // counter of reconstructed cells
 };
 
+// Modal DG tables (dg::General over Projection, Hex8 and Tet4 cells).
+// Cell c's basis is psi = S_c T(x - centre_c) with T the M Taylor monomials;
+// kernels work with the Taylor coefficients a = S^T u of the stage input and
+// accumulate the residual against T, then apply S once per cell.
+struct Modal {
+  int m = 0;                        // basis size M
+  int64_t n_vol = 0, n_fpts = 0;    // volume / face quadrature points
+  double4 *center = nullptr;        // [cells] centre, 1 / length
+  double *s = nullptr;              // [cells][M (M + 1) / 2] packed rows of S
+  int32_t *vol_off = nullptr;       // [cells + 1]
+  double4 *vol = nullptr;           // [volume points] x - centre, global weight
+  int32_t *cell_faces = nullptr;    // [cells][6] 2 face + (1 on the sharer side), -1 none
+  int32_t *face_off = nullptr;      // [faces + 1]
+  int32_t *point_face = nullptr;    // [face points] face id
+  double4 *fpt = nullptr;           // [face points] x, global weight
+  double4 *fnrm = nullptr;          // [face points] unit normal (holder -> sharer)
+  double4 *fshift = nullptr;        // [faces] periodic shift: sharer sees x - shift
+  double *taylor = nullptr;         // [cells][M][K] Taylor coefficients of a stage input
+  double *values = nullptr;         // [volume points][K] scratch of mcfd_project
+  std::vector<double> host_points;  // [volume points][3] global coordinates
+};
+
 struct Buffers {
   double *u = nullptr;     // current solution
   double *u1 = nullptr;    // stage buffers
@@ -96,7 +120,7 @@ struct Buffers {
 struct Options {
   int riemann = 4;
   int precision = 0;
-  int scheme = 0;     // 0 dg::Lobatto (DGSEM), 1 fr::Lobatto (Huynh g2)
+  int scheme = 0;     // 0 dg::Lobatto (DGSEM), 1 fr::Lobatto (Huynh g2), 2 dg::General (modal)
   double cfl = 0;
   double fr_g1 = 0;   // g_R'(1) of the FR correction function
 };
@@ -111,6 +135,7 @@ struct mcfd_handle {
   mcfd::Mesh mesh;
   mcfd::Buffers buf;
   mcfd::Limiter lim;
+  mcfd::Modal modal;
   double t_host = 0;
   int64_t launches = 0;
   std::string err;
@@ -132,6 +157,17 @@ int launch_dt(mcfd_handle *h, const double *u);
 int launch_rk_stage_sequence(mcfd_handle *h, int order);
 // WENO limiter pass on a solution buffer, in place (weno.cu).
 int launch_limiter(mcfd_handle *h, double *u);
+
+// Modal DG (modal.cu): the same stage interface as the nodal launchers.
+constexpr int kSchemeModal = 2;
+int launch_modal_face_flux(mcfd_handle *h, const double *u, double stage_c);
+int launch_modal_cell_update(mcfd_handle *h, int stage, const double *u_in,
+                             const double *u0, double *u_out, int advance_time);
+int launch_modal_dt(mcfd_handle *h, const double *u);
+// Projection::Approximate from values [volume points][K] in modal.values.
+int launch_modal_project(mcfd_handle *h, double *u);
+// Host set-up of the modal tables (modal_setup.cpp); returns an mcfd status.
+int build_modal_mesh(mcfd_handle *h, const ::mcfd_mesh_desc *d, int degree);
 
 // Residual whose face-flux scratch is a fixed file-scope device array
 // (mcfd_residual_device_noalloc).  Capacity in doubles: 2 Mi = 16 MiB, i.e.

@@ -1,0 +1,488 @@
+// Modal DG (dg::General over polynomial::Projection) on Hex8 and Tet4 cells,
+// FP64, on sm_103a.
+//
+// The reference evaluates, at every quadrature point, the cell's orthonormal
+// basis psi = S T(x - centre) (T the M Taylor monomials, S lower triangular)
+// and its gradient, and adds F . grad(psi) w (volume, spatial/dg/general.hpp:
+// 58-69) and -F^ w psi (faces, general.hpp:70-202) to the K x M block.  Here
+// the same sums are reassociated through S:
+//   u(x)   = sum_m c_m psi_m(x) = sum_j a_j T_j(x - centre),   a = S^T c
+//   R_m    = sum_j S_mj Rt_j,   Rt_j = sum_q w F . grad T_j - sum_f w F^ T_j
+// so a point costs one K x M contraction with the Taylor coefficients a and a
+// sparse update of Rt (each monomial has at most three non-zero partials);
+// S is applied once per cell.  Per RK stage three kernels run:
+//   modal_taylor_kernel  a = S^T c of the stage input, one thread per
+//                        (cell, monomial, component)
+//   modal_face_kernel    one thread per face point: u on both sides from a,
+//                        the rotated Riemann or boundary flux, times w
+//   modal_cell_kernel    one thread per cell: volume quadrature, lift of its
+//                        <= 6 faces' point fluxes (gathered, atomic-free),
+//                        R = S Rt and the RK stage combination
+// The time step follows fem.hpp:417-435 with the Projection quirk that
+// GetValue(i) for i < M reads the value at quadrature point i.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "euler.cuh"
+#include "handle.hpp"
+
+namespace mcfd {
+namespace {
+
+// Threads per block of the cell kernel: its shared Taylor coefficients take
+// K M doubles per thread (at most 25.6 KB per block).
+template <int M>
+struct ModalCfg {
+  static constexpr int kBlock = M == 20 ? 32 : 64;
+};
+
+// Taylor monomials at offset (x, y, z) in the reference's order
+// (basis/taylor.hpp:198-218).
+template <int M>
+__device__ __forceinline__ void taylor_values(double x, double y, double z, double *t) {
+  t[0] = 1.0;
+  t[1] = x; t[2] = y; t[3] = z;
+  if constexpr (M >= 10) {
+    t[4] = x * x; t[5] = x * y; t[6] = x * z;
+    t[7] = y * y; t[8] = y * z; t[9] = z * z;
+  }
+  if constexpr (M >= 20) {
+    t[10] = x * t[4]; t[11] = x * t[5]; t[12] = x * t[6];
+    t[13] = x * t[7]; t[14] = x * t[8]; t[15] = x * t[9];
+    t[16] = y * t[7]; t[17] = y * t[8]; t[18] = y * t[9];
+    t[19] = z * t[9];
+  }
+}
+
+// rt[j] += gx dT_j/dx + gy dT_j/dy + gz dT_j/dz at offset (x, y, z), t the
+// monomial values there (basis/taylor.hpp:387-472).
+template <int M>
+__device__ __forceinline__ void add_gradient(const double *t, double gx, double gy,
+                                             double gz, double *rt) {
+  rt[1] += gx;
+  rt[2] += gy;
+  rt[3] += gz;
+  if constexpr (M >= 10) {
+    const double x = t[1], y = t[2], z = t[3];
+    rt[4] += gx * (2 * x);
+    rt[5] += gx * y + gy * x;
+    rt[6] += gx * z + gz * x;
+    rt[7] += gy * (2 * y);
+    rt[8] += gy * z + gz * y;
+    rt[9] += gz * (2 * z);
+  }
+  if constexpr (M >= 20) {
+    const double xx = t[4], xy = t[5], xz = t[6], yy = t[7], yz = t[8], zz = t[9];
+    rt[10] += gx * (3 * xx);
+    rt[11] += gx * (2 * xy) + gy * xx;
+    rt[12] += gx * (2 * xz) + gz * xx;
+    rt[13] += gx * yy + gy * (2 * xy);
+    rt[14] += gx * yz + gy * xz + gz * xy;
+    rt[15] += gx * zz + gz * (2 * xz);
+    rt[16] += gy * (3 * yy);
+    rt[17] += gy * (2 * yz) + gz * yy;
+    rt[18] += gy * zz + gz * (2 * yz);
+    rt[19] += gz * (3 * zz);
+  }
+}
+
+__device__ __forceinline__ void modal_given(const BcDev &bc, double x, double y,
+                                            double z, double t, double *g) {
+  const double pos[3] = {x, y, z};
+  const double *src = bc.a;
+  if (bc.program == 1 && (pos[bc.axis] - bc.speed * t) >= bc.position) src = bc.b;
+#pragma unroll
+  for (int k = 0; k < kK; ++k) g[k] = src[k];
+}
+
+// a[c][j][k] = sum_{m >= j} S[m][j] u[c][m][k]
+template <int M>
+__global__ void __launch_bounds__(256)
+modal_taylor_kernel(const double *u, const double *s, double *a, int64_t n) {
+  constexpr int KM = kK * M, NS = M * (M + 1) / 2;
+  int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= n) return;
+  const int64_t c = gid / KM;
+  const int r = (int)(gid - c * KM), j = r / kK, k = r - j * kK;
+  const double *uc = u + c * KM;
+  const double *sc = s + c * NS;
+  double acc = 0;
+  for (int m = j; m < M; ++m) acc += sc[m * (m + 1) / 2 + j] * uc[m * kK + k];
+  a[gid] = acc;
+}
+
+struct ModalFaceArgs {
+  const double *taylor;
+  const double4 *center;
+  const int2 *face_cells;
+  const int32_t *face_group;
+  const int32_t *point_face;
+  const double4 *fpt, *fnrm, *fshift;
+  const BcDev *bcs;
+  double *flux;
+  DevState *state;
+  double stage_c;
+  int64_t n_points;
+  int n_groups;
+};
+
+template <int M>
+__device__ __forceinline__ void eval_taylor(const double *a, const double *t, double *u) {
+#pragma unroll
+  for (int k = 0; k < kK; ++k) {
+    double s = 0;
+#pragma unroll
+    for (int j = 0; j < M; ++j) s += a[j * kK + k] * t[j];
+    u[k] = s;
+  }
+}
+
+template <int M, int R>
+__global__ void __launch_bounds__(256) modal_face_kernel(ModalFaceArgs a) {
+  int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= a.n_points) return;
+  const int f = a.point_face[gid];
+  const int2 cells = a.face_cells[f];
+  const double4 x = a.fpt[gid];
+  const double4 nv = a.fnrm[gid];
+  const double n[3] = {nv.x, nv.y, nv.z};
+  const double4 ch = a.center[cells.x];
+  double t[M], uh[kK], out[kK];
+  taylor_values<M>(x.x - ch.x, x.y - ch.y, x.z - ch.z, t);
+  eval_taylor<M>(a.taylor + (int64_t)cells.x * M * kK, t, uh);
+  bool not_converged = false;
+  Prim l = cons_to_prim(uh[0], uh[1], uh[2], uh[3], uh[4]);
+  if (cells.y >= 0) {
+    const double4 sh = a.fshift[f];
+    const double4 cs = a.center[cells.y];
+    double us[kK];
+    taylor_values<M>((x.x - sh.x) - cs.x, (x.y - sh.y) - cs.y, (x.z - sh.z) - cs.z, t);
+    eval_taylor<M>(a.taylor + (int64_t)cells.y * M * kK, t, us);
+    Prim r = cons_to_prim(us[0], us[1], us[2], us[3], us[4]);
+    flux_upwind<R>(l, r, n, out, &not_converged);
+  } else {
+    const int grp = a.face_group[f];
+    if (grp >= 0 && grp < a.n_groups && a.bcs[grp].kind != kBcNone) {
+      const BcDev &bc = a.bcs[grp];
+      double given[kK];
+      modal_given(bc, x.x, x.y, x.z, a.state->t + a.stage_c * a.state->dt, given);
+      flux_boundary<R>(bc.kind, l, given, n, out, &not_converged);
+    } else {
+#pragma unroll
+      for (int k = 0; k < kK; ++k) out[k] = 0;
+    }
+  }
+  if (not_converged) atomicOr(&a.state->status, (unsigned)kStatusNotConverged);
+  double *dst = a.flux + gid * kK;
+#pragma unroll
+  for (int k = 0; k < kK; ++k) dst[k] = out[k] * x.w;
+}
+
+struct ModalCellArgs {
+  const double *u_in, *u0;
+  double *u_out;
+  const double *taylor;
+  const double *s;
+  const double4 *center;
+  const int32_t *vol_off;
+  const double4 *vol;
+  const int32_t *cell_faces;
+  const int32_t *face_off;
+  const double4 *fpt, *fshift;
+  const double *flux;
+  DevState *state;
+  int64_t n_cells;
+  int advance_time;
+};
+
+template <int M, int STAGE>
+__global__ void __launch_bounds__(ModalCfg<M>::kBlock) modal_cell_kernel(ModalCellArgs a) {
+  constexpr int KM = kK * M, NS = M * (M + 1) / 2, kCellBlock = ModalCfg<M>::kBlock;
+  // thread-private Taylor coefficients, column per thread (conflict-free)
+  __shared__ double s_a[KM][kCellBlock];
+  const int tid = threadIdx.x;
+  const int64_t c = (int64_t)blockIdx.x * kCellBlock + tid;
+  if (c >= a.n_cells) return;
+  {
+    const double *ac = a.taylor + c * KM;
+#pragma unroll
+    for (int i = 0; i < KM; ++i) s_a[i][tid] = ac[i];
+  }
+  double rt[kK][M];
+#pragma unroll
+  for (int k = 0; k < kK; ++k)
+#pragma unroll
+    for (int j = 0; j < M; ++j) rt[k][j] = 0;
+  // volume: sum_q w F(u_q) . grad T(x_q)
+  const int q0 = a.vol_off[c], q1 = a.vol_off[c + 1];
+  for (int q = q0; q < q1; ++q) {
+    const double4 g = a.vol[q];
+    double t[M], u[kK];
+    taylor_values<M>(g.x, g.y, g.z, t);
+#pragma unroll
+    for (int k = 0; k < kK; ++k) {
+      double s = 0;
+#pragma unroll
+      for (int j = 0; j < M; ++j) s += s_a[j * kK + k][tid] * t[j];
+      u[k] = s;
+    }
+    // GetFluxMatrix (types.hpp:322-333); mass row = momentum, which for a
+    // converted state equals rho * velocity
+    const Prim w = cons_to_prim(u[0], u[1], u[2], u[3], u[4]);
+    const bool converted = w.rho != 0;
+    const double vel[3] = {w.u, w.v, w.w};
+    double f[kK][3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      f[0][d] = converted ? w.rho * vel[d] : u[1 + d];
+      f[1][d] = u[1] * vel[d] + (d == 0 ? w.p : 0.0);
+      f[2][d] = u[2] * vel[d] + (d == 1 ? w.p : 0.0);
+      f[3][d] = u[3] * vel[d] + (d == 2 ? w.p : 0.0);
+      f[4][d] = (u[4] + w.p) * vel[d];
+    }
+#pragma unroll
+    for (int k = 0; k < kK; ++k)
+      add_gradient<M>(t, f[k][0] * g.w, f[k][1] * g.w, f[k][2] * g.w, rt[k]);
+  }
+  // faces: holder -= w F^ T(x - centre), sharer += w F^ T(x - shift - centre)
+  const double4 ctr = a.center[c];
+  for (int slot = 0; slot < 6; ++slot) {
+    const int code = a.cell_faces[c * 6 + slot];
+    if (code < 0) continue;
+    const int f = code >> 1;
+    const bool sharer = code & 1;
+    double4 sh = make_double4(0, 0, 0, 0);
+    if (sharer) sh = a.fshift[f];
+    const int p0 = a.face_off[f], p1 = a.face_off[f + 1];
+    for (int p = p0; p < p1; ++p) {
+      const double4 x = a.fpt[p];
+      double t[M];
+      taylor_values<M>((x.x - sh.x) - ctr.x, (x.y - sh.y) - ctr.y, (x.z - sh.z) - ctr.z, t);
+      const double *fl = a.flux + (int64_t)p * kK;
+#pragma unroll
+      for (int k = 0; k < kK; ++k) {
+        const double v = sharer ? fl[k] : -fl[k];
+#pragma unroll
+        for (int j = 0; j < M; ++j) rt[k][j] += v * t[j];
+      }
+    }
+  }
+  // R = S Rt, then the stage combination (temporal/rk.hpp:16-49)
+  const double *sc = a.s + c * NS;
+  const double *uin = a.u_in + c * KM;
+  double *out = a.u_out + c * KM;
+  const double dt = STAGE == kStageResidual ? 0.0 : a.state->dt;
+  bool bad = false;
+#pragma unroll
+  for (int m = 0; m < M; ++m) {
+    double srow[M];
+#pragma unroll
+    for (int j = 0; j <= m; ++j) srow[j] = sc[m * (m + 1) / 2 + j];
+#pragma unroll
+    for (int k = 0; k < kK; ++k) {
+      double r = 0;
+#pragma unroll
+      for (int j = 0; j <= m; ++j) r += srow[j] * rt[k][j];
+      double v;
+      if (STAGE == kStageResidual) {
+        v = r;
+      } else {
+        const double next = uin[m * kK + k] + r * dt;
+        if (STAGE == kStageEuler) {
+          v = next;
+        } else if (STAGE == kStageRk2Last) {
+          v = (next + a.u0[c * KM + m * kK + k]) * 0.5;
+        } else if (STAGE == kStageRk3Mid) {
+          v = (a.u0[c * KM + m * kK + k] * 3 + next) * 0.25;
+        } else {
+          v = (next * 2 + a.u0[c * KM + m * kK + k]) * (1.0 / 3.0);
+        }
+      }
+      bad |= !isfinite(v);
+      out[m * kK + k] = v;
+    }
+  }
+  if (bad) atomicOr(&a.state->status, (unsigned)kStatusNonFinite);
+  if (a.advance_time && c == 0) a.state->t += a.state->dt;
+}
+
+// max over the first M quadrature points of (|u| + c) / length, per cell
+// (fem.hpp:417-435 with Projection::GetValue(i), projection.hpp:109-118)
+template <int M>
+__global__ void __launch_bounds__(256)
+modal_dt_kernel(const double *u, const double *s, const double4 *center,
+                const int32_t *vol_off, const double4 *vol, int64_t n_cells,
+                DevState *state) {
+  constexpr int KM = kK * M, NS = M * (M + 1) / 2;
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double rate = 0;
+  if (c < n_cells) {
+    const double *sc = s + c * NS;
+    const double *uc = u + c * KM;
+    double max_speed = 1e-5;
+    const int q0 = vol_off[c];
+    for (int i = 0; i < M; ++i) {
+      const double4 g = vol[q0 + i];
+      double t[M], psi[M], v[kK];
+      taylor_values<M>(g.x, g.y, g.z, t);
+#pragma unroll
+      for (int m = 0; m < M; ++m) {
+        double acc = 0;
+#pragma unroll
+        for (int j = 0; j <= m; ++j) acc += sc[m * (m + 1) / 2 + j] * t[j];
+        psi[m] = acc;
+      }
+#pragma unroll
+      for (int k = 0; k < kK; ++k) {
+        double acc = 0;
+#pragma unroll
+        for (int m = 0; m < M; ++m) acc += uc[m * kK + k] * psi[m];
+        v[k] = acc;
+      }
+      const Prim w = cons_to_prim(v[0], v[1], v[2], v[3], v[4]);
+      const double speed = sound_speed(w) + sqrt(w.u * w.u + w.v * w.v + w.w * w.w);
+      max_speed = fmax(max_speed, speed);
+    }
+    rate = max_speed * center[c].w;
+  }
+  for (int o = 16; o > 0; o >>= 1) rate = fmax(rate, __shfl_xor_sync(0xffffffffu, rate, o));
+  if ((threadIdx.x & 31) == 0 && rate > 0)
+    atomicMax(&state->max_rate_bits, (unsigned long long)__double_as_longlong(rate));
+}
+
+__global__ void modal_dt_finalize_kernel(DevState *state) {
+  const double max_rate = __longlong_as_double((long long)state->max_rate_bits);
+  const double min_dt = max_rate > 0 ? 1.0 / max_rate : 1.e+100;
+  state->dt = fmin(state->cfl * min_dt, state->dt_guess);
+  state->max_rate_bits = 0ull;
+}
+
+// Projection::Approximate (projection.hpp:28-42): coeff = sum_q (f_q psi(x_q)) w_q
+template <int M>
+__global__ void __launch_bounds__(256)
+modal_project_kernel(const double *values, const double *s, const int32_t *vol_off,
+                     const double4 *vol, double *u, int64_t n) {
+  constexpr int KM = kK * M, NS = M * (M + 1) / 2;
+  int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= n) return;
+  const int64_t c = gid / KM;
+  const int r = (int)(gid - c * KM), m = r / kK, k = r - m * kK;
+  const double *sc = s + c * NS;
+  double acc = 0;
+  for (int q = vol_off[c]; q < vol_off[c + 1]; ++q) {
+    const double4 g = vol[q];
+    double t[M];
+    taylor_values<M>(g.x, g.y, g.z, t);
+    double psi = 0;
+    for (int j = 0; j <= m; ++j) psi += sc[m * (m + 1) / 2 + j] * t[j];
+    acc += values[(int64_t)q * kK + k] * psi * g.w;
+  }
+  u[gid] = acc;
+}
+
+template <int M>
+int taylor_launch(mcfd_handle *h, const double *u) {
+  const int64_t n = h->mesh.n_cells * kK * M;
+  modal_taylor_kernel<M><<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(
+      u, h->modal.s, h->modal.taylor, n);
+  return 1;
+}
+
+template <int M, int R>
+void modal_face_launch(mcfd_handle *h, const ModalFaceArgs &fa) {
+  modal_face_kernel<M, R><<<(unsigned)((fa.n_points + 255) / 256), 256, 0, h->stream>>>(fa);
+}
+
+template <int M>
+void modal_face_dispatch(mcfd_handle *h, const ModalFaceArgs &fa) {
+  switch (h->opt.riemann) {
+    case kExact: modal_face_launch<M, kExact>(h, fa); break;
+    case kHllc: modal_face_launch<M, kHllc>(h, fa); break;
+    case kAusm: modal_face_launch<M, kAusm>(h, fa); break;
+    case kRoe: modal_face_launch<M, kRoe>(h, fa); break;
+    default: modal_face_launch<M, kRusanov>(h, fa); break;
+  }
+}
+
+template <int M, int S>
+void modal_cell_launch(mcfd_handle *h, const ModalCellArgs &ca) {
+  constexpr int B = ModalCfg<M>::kBlock;
+  const int64_t blocks = (ca.n_cells + B - 1) / B;
+  modal_cell_kernel<M, S><<<(unsigned)blocks, B, 0, h->stream>>>(ca);
+}
+
+template <int M>
+void modal_cell_dispatch(mcfd_handle *h, int stage, const ModalCellArgs &ca) {
+  switch (stage) {
+    case kStageEuler: modal_cell_launch<M, kStageEuler>(h, ca); break;
+    case kStageRk2Last: modal_cell_launch<M, kStageRk2Last>(h, ca); break;
+    case kStageRk3Mid: modal_cell_launch<M, kStageRk3Mid>(h, ca); break;
+    case kStageRk3Last: modal_cell_launch<M, kStageRk3Last>(h, ca); break;
+    default: modal_cell_launch<M, kStageResidual>(h, ca); break;
+  }
+}
+
+}  // namespace
+
+int launch_modal_face_flux(mcfd_handle *h, const double *u, double stage_c) {
+  const Mesh &m = h->mesh;
+  const Modal &md = h->modal;
+  int n = 0;
+  switch (md.m) {
+    case 4: n += taylor_launch<4>(h, u); break;
+    case 10: n += taylor_launch<10>(h, u); break;
+    default: n += taylor_launch<20>(h, u); break;
+  }
+  if (md.n_fpts == 0) return n;
+  ModalFaceArgs fa{md.taylor, md.center, m.face_cells, m.face_group, md.point_face,
+                   md.fpt, md.fnrm, md.fshift, m.bcs, h->buf.flux, h->buf.state,
+                   stage_c, md.n_fpts, m.n_groups};
+  switch (md.m) {
+    case 4: modal_face_dispatch<4>(h, fa); break;
+    case 10: modal_face_dispatch<10>(h, fa); break;
+    default: modal_face_dispatch<20>(h, fa); break;
+  }
+  return n + 1;
+}
+
+int launch_modal_cell_update(mcfd_handle *h, int stage, const double *u_in,
+                             const double *u0, double *u_out, int advance_time) {
+  const Modal &md = h->modal;
+  ModalCellArgs ca{u_in, u0, u_out, md.taylor, md.s, md.center, md.vol_off, md.vol,
+                   md.cell_faces, md.face_off, md.fpt, md.fshift, h->buf.flux,
+                   h->buf.state, h->mesh.n_cells, advance_time};
+  switch (md.m) {
+    case 4: modal_cell_dispatch<4>(h, stage, ca); break;
+    case 10: modal_cell_dispatch<10>(h, stage, ca); break;
+    default: modal_cell_dispatch<20>(h, stage, ca); break;
+  }
+  return 1;
+}
+
+int launch_modal_dt(mcfd_handle *h, const double *u) {
+  const Modal &md = h->modal;
+  const int64_t C = h->mesh.n_cells;
+  const unsigned blocks = (unsigned)((C + 255) / 256);
+  switch (md.m) {
+    case 4: modal_dt_kernel<4><<<blocks, 256, 0, h->stream>>>(u, md.s, md.center, md.vol_off, md.vol, C, h->buf.state); break;
+    case 10: modal_dt_kernel<10><<<blocks, 256, 0, h->stream>>>(u, md.s, md.center, md.vol_off, md.vol, C, h->buf.state); break;
+    default: modal_dt_kernel<20><<<blocks, 256, 0, h->stream>>>(u, md.s, md.center, md.vol_off, md.vol, C, h->buf.state); break;
+  }
+  modal_dt_finalize_kernel<<<1, 1, 0, h->stream>>>(h->buf.state);
+  return 2;
+}
+
+int launch_modal_project(mcfd_handle *h, double *u) {
+  const Modal &md = h->modal;
+  const int64_t n = h->mesh.column;
+  const unsigned blocks = (unsigned)((n + 255) / 256);
+  switch (md.m) {
+    case 4: modal_project_kernel<4><<<blocks, 256, 0, h->stream>>>(md.values, md.s, md.vol_off, md.vol, u, n); break;
+    case 10: modal_project_kernel<10><<<blocks, 256, 0, h->stream>>>(md.values, md.s, md.vol_off, md.vol, u, n); break;
+    default: modal_project_kernel<20><<<blocks, 256, 0, h->stream>>>(md.values, md.s, md.vol_off, md.vol, u, n); break;
+  }
+  return 1;
+}
+
+}  // namespace mcfd

@@ -179,3 +179,149 @@ def node_coordinates(mesh: Mesh, degree: int) -> np.ndarray:
     shape = np.prod(1 + loc[:, None, :] * corners[None, :, :], axis=2) / 8  # [N, 8]
     xn = mesh.xyz[mesh.cell_nodes]  # [cells, 8, 3]
     return np.einsum("nv,cvd->cnd", shape, xn)
+
+
+# Tetrahedron4::faces_ (coordinate/tetrahedron.hpp:141-147): local face ->
+# cell node slots, ordered so the normal points out of a positively oriented
+# (CGNS) tetrahedron.
+TET_FACES = np.array([[0, 2, 1], [0, 1, 3], [0, 3, 2], [1, 2, 3]], dtype=np.int64)
+HEX8, TET4 = 0, 1
+
+# Kuhn split of a hex into 6 tetrahedra sharing the (0,0,0)-(1,1,1) diagonal:
+# for each axis permutation (a, b, c) the path 0 -> e_a -> e_a + e_b -> 1.
+# Corner slot of offset (dx, dy, dz) in a CGNS Hex8: see box().
+_HEX_SLOT = {(0, 0, 0): 0, (1, 0, 0): 1, (1, 1, 0): 2, (0, 1, 0): 3,
+             (0, 0, 1): 4, (1, 0, 1): 5, (1, 1, 1): 6, (0, 1, 1): 7}
+
+
+def _kuhn_tets():
+    import itertools
+    tets = []
+    for perm in itertools.permutations(range(3)):
+        path = [(0, 0, 0)]
+        cur = [0, 0, 0]
+        for ax in perm:
+            cur[ax] = 1
+            path.append(tuple(cur))
+        slots = [_HEX_SLOT[v] for v in path]
+        # positive orientation: det[v1 - v0, v2 - v0, v3 - v0] > 0
+        v = np.array(path, dtype=np.float64)
+        if np.linalg.det(v[1:] - v[0]) < 0:
+            slots[1], slots[2] = slots[2], slots[1]
+        tets.append(slots)
+    return np.array(tets, dtype=np.int64)
+
+
+KUHN_TETS = _kuhn_tets()
+
+
+def tet_box(shape, lengths=(1.0, 1.0, 1.0), origin=(0.0, 0.0, 0.0),
+            periodic=(False, False, False), jitter: float = 0.0, seed: int = 0) -> Mesh:
+    """nx x ny x nz hexes of box() each split into 6 Tet4 cells (Kuhn split,
+    conforming across cells and across periodic boundaries).
+
+    cell_nodes keeps 8 slots per cell: the 4 tetrahedron nodes in CGNS order
+    followed by -1.  Faces use the local face numbering of TET_FACES; holders
+    are the lower cell id of each interior face, boundary groups as in box().
+    """
+    hexes = box(shape, lengths, origin, periodic, jitter, seed)
+    nx, ny, nz = hexes.shape
+    L = np.asarray(hexes.lengths)
+    cn = hexes.cell_nodes[:, KUHN_TETS].reshape(-1, 4)           # [6 * cells, 4]
+    n_cells = cn.shape[0]
+    cell_nodes = np.full((n_cells, 8), -1, dtype=np.int64)
+    cell_nodes[:, :4] = cn
+    # node lattice indices and periodic canonical ids
+    nid = np.arange(hexes.xyz.shape[0], dtype=np.int64)
+    ii = nid % (nx + 1)
+    jj = (nid // (nx + 1)) % (ny + 1)
+    kk = nid // ((nx + 1) * (ny + 1))
+    ci = np.where(periodic[0], ii % nx, ii) if periodic[0] else ii
+    cj = np.where(periodic[1], jj % ny, jj) if periodic[1] else jj
+    ck = np.where(periodic[2], kk % nz, kk) if periodic[2] else kk
+    canon = (ck * (ny + 1) + cj) * (nx + 1) + ci
+    # all (cell, side) faces
+    fn = cn[:, TET_FACES]                                        # [cells, 4, 3]
+    cells = np.repeat(np.arange(n_cells, dtype=np.int64), 4)
+    sides = np.tile(np.arange(4, dtype=np.int64), n_cells)
+    fn = fn.reshape(-1, 3)
+    key = np.sort(canon[fn], axis=1)
+    order = np.lexsort((cells, key[:, 2], key[:, 1], key[:, 0]))
+    key, cells, sides, fn = key[order], cells[order], sides[order], fn[order]
+    same = np.all(key[1:] == key[:-1], axis=1)
+    first = np.flatnonzero(same)                                 # pairs (first, first + 1)
+    paired = np.zeros(key.shape[0], dtype=bool)
+    paired[first] = True
+    paired[first + 1] = True
+    # interior faces: holder = lower cell id (the sort puts it first)
+    h, s = cells[first], cells[first + 1]
+    hs, ss = sides[first], sides[first + 1]
+    ch = hexes.xyz[fn[first]].mean(axis=1)
+    cs = hexes.xyz[fn[first + 1]].mean(axis=1)
+    shift = np.round((ch - cs) / L) * L
+    o = np.lexsort((hs, h))
+    face_cells = [np.stack([h[o], s[o]], axis=1)]
+    face_sides = [np.stack([hs[o], ss[o]], axis=1)]
+    face_group = [np.full(o.size, -1)]
+    face_shift = [shift[o]]
+    # boundary faces: group from the plane that holds all three nodes
+    lone = np.flatnonzero(~paired)
+    if lone.size:
+        bn = fn[lone]
+        grp = np.full(lone.size, -1, dtype=np.int64)
+        for ax, (idx, n) in enumerate(((ii, nx), (jj, ny), (kk, nz))):
+            v = idx[bn]
+            grp = np.where(np.all(v == 0, axis=1), 2 * ax, grp)
+            grp = np.where(np.all(v == n, axis=1), 2 * ax + 1, grp)
+        if np.any(grp < 0):
+            raise ValueError("unmatched interior tetrahedron face")
+        hb, sb = cells[lone], sides[lone]
+        ob = np.lexsort((hb, grp))
+        face_cells.append(np.stack([hb[ob], np.full(ob.size, -1)], axis=1))
+        face_sides.append(np.stack([sb[ob], np.full(ob.size, -1)], axis=1))
+        face_group.append(grp[ob])
+        face_shift.append(np.zeros((ob.size, 3)))
+    return Mesh(
+        xyz=hexes.xyz,
+        cell_nodes=cell_nodes,
+        face_cells=np.ascontiguousarray(np.concatenate(face_cells).astype(np.int64)),
+        face_sides=np.ascontiguousarray(np.concatenate(face_sides).astype(np.int32)),
+        face_group=np.ascontiguousarray(np.concatenate(face_group).astype(np.int32)),
+        face_shift=np.ascontiguousarray(np.concatenate(face_shift).astype(np.float64)),
+        cell_type=np.full(n_cells, TET4, dtype=np.int32),
+        shape=hexes.shape, lengths=hexes.lengths, origin=hexes.origin, periodic=hexes.periodic,
+    )
+
+
+def concat(*meshes: Mesh) -> Mesh:
+    """Disjoint union of meshes (independent blocks in one description):
+    node and cell ids are offset; boundary groups of block b become
+    b * 6 + group."""
+    xyz, cn, fc, fs, fg, fsh, ct = [], [], [], [], [], [], []
+    n_off = c_off = 0
+    for b, m in enumerate(meshes):
+        xyz.append(m.xyz)
+        nodes = m.cell_nodes.copy()
+        nodes[nodes >= 0] += n_off
+        cn.append(nodes)
+        f = m.face_cells.copy()
+        f[f >= 0] += c_off
+        fc.append(f)
+        fs.append(m.face_sides)
+        g = m.face_group.copy()
+        g[g >= 0] += 6 * b
+        fg.append(g)
+        fsh.append(m.face_shift)
+        ct.append(m.cell_type if m.cell_type is not None else np.full(m.n_cells, HEX8, dtype=np.int32))
+        n_off += m.xyz.shape[0]
+        c_off += m.n_cells
+    return Mesh(
+        xyz=np.ascontiguousarray(np.concatenate(xyz)),
+        cell_nodes=np.ascontiguousarray(np.concatenate(cn)),
+        face_cells=np.ascontiguousarray(np.concatenate(fc)),
+        face_sides=np.ascontiguousarray(np.concatenate(fs)),
+        face_group=np.ascontiguousarray(np.concatenate(fg)),
+        face_shift=np.ascontiguousarray(np.concatenate(fsh)),
+        cell_type=np.ascontiguousarray(np.concatenate(ct).astype(np.int32)),
+        meta={"blocks": [m.n_cells for m in meshes]},
+    )

@@ -88,14 +88,15 @@ class Lobatto:
             np.ascontiguousarray(mesh.face_sides, dtype=np.int32),
             np.ascontiguousarray(mesh.face_group, dtype=np.int32),
             np.ascontiguousarray(mesh.face_shift, dtype=np.float64),
+            None if mesh.cell_type is None else np.ascontiguousarray(mesh.cell_type, dtype=np.int32),
         ]
-        xyz, cn, fc, fs, fg, fsh = self._keep
+        xyz, cn, fc, fs, fg, fsh, ct = self._keep
         desc = capi.MeshDesc()
         desc.n_nodes = xyz.shape[0]
         desc.xyz = capi.dptr(xyz)
         desc.n_cells = cn.shape[0]
         desc.cell_nodes = cn.ctypes.data_as(C.POINTER(C.c_int64))
-        desc.cell_type = None
+        desc.cell_type = None if ct is None else ct.ctypes.data_as(C.POINTER(C.c_int32))
         desc.n_faces = fc.shape[0]
         desc.face_cells = fc.ctypes.data_as(C.POINTER(C.c_int64))
         desc.face_sides = fs.ctypes.data_as(C.POINTER(C.c_int32))
@@ -103,10 +104,11 @@ class Lobatto:
         desc.face_shift = capi.dptr(fsh)
         opt = capi.Options()
         opt.degree = self.degree
-        if scheme not in ("dgsem", "fr"):
-            raise ValueError("scheme must be 'dgsem' (dg::Lobatto) or 'fr' (fr::Lobatto)")
+        if scheme not in capi.SCHEME:
+            raise ValueError("scheme must be 'dgsem' (dg::Lobatto), 'fr' (fr::Lobatto) "
+                             "or 'modal' (dg::General over Projection)")
         self.scheme = scheme
-        opt.scheme = capi.DGSEM if scheme == "dgsem" else capi.FR
+        opt.scheme = capi.SCHEME[scheme]
         opt.riemann = self.riemann
         opt.precision = capi.FP64 if precision == "fp64" else capi.MIXED
         opt.cfl = float(cfl)
@@ -121,6 +123,8 @@ class Lobatto:
         self._lib = lib
         self.column_size = int(lib.mcfd_column_size(h))
         self.n_nodes_per_cell = (self.degree + 1) ** 3
+        if scheme == "modal":
+            self.n_nodes_per_cell = (self.degree + 1) * (self.degree + 2) * (self.degree + 3) // 6
 
     # -- lifetime
     def close(self) -> None:
@@ -256,6 +260,41 @@ class Lobatto:
 
     def set_stream(self, stream_ptr: int | None) -> None:
         self._check(self._lib.mcfd_set_stream(self._h, C.c_void_p(stream_ptr or 0)))
+
+
+class General(Lobatto):
+    """Modal DG (dg::General over polynomial::Projection) Euler system on one
+    GPU, on Hex8 and Tet4 cells.  The column holds, per cell, the M x 5
+    coefficients on the cell's orthonormal Taylor basis (m-major)."""
+
+    def __init__(self, mesh: Mesh, degree: int, riemann: str | int = "rusanov",
+                 cfl: float = 0.0, device: int = 0):
+        super().__init__(mesh, degree, riemann, cfl=cfl, device=device, scheme="modal")
+        self.n_points = int(self._lib.mcfd_point_count(self._h))
+
+    def points(self) -> np.ndarray:
+        """Global coordinates [n_points, 3] of the volume quadrature points."""
+        out = np.empty((self.n_points, 3), dtype=np.float64)
+        self._check(self._lib.mcfd_points(self._h, capi.dptr(out), self.n_points))
+        return out
+
+    def project(self, values: np.ndarray) -> None:
+        """Load the projection of values [n_points, 5] given at points()."""
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        if v.size != self.n_points * 5:
+            raise ValueError("values must hold 5 components per quadrature point")
+        self._check(self._lib.mcfd_project(self._h, capi.dptr(v), self.n_points))
+
+    def Approximate(self, func: Callable[[np.ndarray], np.ndarray]) -> None:
+        """Projection::Approximate (polynomial/projection.hpp:28-42) of func
+        (vectorised over [M, 3] points -> [M, 5])."""
+        self.project(func(self.points()))
+
+    def node_coordinates(self) -> np.ndarray:
+        raise NotImplementedError("the modal scheme has no nodes; use points()")
+
+    def face_node_maps(self):
+        raise NotImplementedError("the modal scheme evaluates both sides at each face point")
 
 
 class RungeKutta:
