@@ -287,6 +287,169 @@ def roofline_of(kt, L, cells, hbm_peak, peak_src, fp64_peak, precision):
             "binding": "fp64 pipe (see fp64.frac)", "kernel_ms": kt}
 
 
+# ---------------------------------------------------------------------------
+# Mixed hex + tet box: modal DG (dg::General over Projection), p = 2, HLLC.
+# Two independent periodic unit-cube blocks: 100^3 Hex8 and 64^3 x 6 Tet4
+# (Kuhn split), interior nodes jittered U(-0.1 h, 0.1 h), seed 0; 2,572,864
+# cells, M = 10, L = 128,643,200.  rho = 1 + 0.2 sin(2 pi x) cos(2 pi y),
+# u = (0.5, 0.3, 0.1), p = 1; CFL from the reference table (0.209).
+MIXED_HEX_1D, MIXED_TET_1D, MIXED_DEGREE, MIXED_SAMPLE = 100, 64, 2, (12, 8)
+C_HLLC = 120
+
+
+def mixed_box_mesh(n_hex, n_tet):
+    from pvcriemannsolvers_gb300 import mesh as meshlib
+    a = meshlib.box((n_hex,) * 3, periodic=(True,) * 3, jitter=0.1, seed=0)
+    b = meshlib.tet_box((n_tet,) * 3, periodic=(True,) * 3, jitter=0.1, seed=0)
+    return meshlib.concat(a, b)
+
+
+def mixed_box_ic(x):
+    from pvcriemannsolvers_gb300 import cases
+    rho = 1 + 0.2 * np.sin(2 * np.pi * x[:, 0]) * np.cos(2 * np.pi * x[:, 1])
+    n = rho.size
+    return cases.prim_to_cons(rho, np.full(n, 0.5), np.full(n, 0.3), np.full(n, 0.1), np.ones(n))
+
+
+def mixed_box_config(n_hex, n_tet):
+    cells = n_hex ** 3 + 6 * n_tet ** 3
+    m = (MIXED_DEGREE + 1) * (MIXED_DEGREE + 2) * (MIXED_DEGREE + 3) // 6
+    return {"workload": f"mixed box: periodic unit cube {n_hex}^3 Hex8 + periodic unit cube {n_tet}^3 x 6 Tet4, "
+                        f"jitter 0.1 h, modal DG p={MIXED_DEGREE} (dg::General + Projection), HLLC, SSP-RK3, "
+                        f"CFL 0.209 (reference table)",
+            "cells": cells, "dofs": cells * m * K, "form": "plain FP64",
+            "quadrature": "Hex8 Gauss 3^3 / Quad4 3^2; Tet4 14 points / Tri3 6 points",
+            "step": "dt reduction + 3 RK stages (3 kernels each)",
+            "l2_flush": "inputs larger than L2 (solution column 1.03 GB)"}
+
+
+def mixed_box_cpu_sample(seconds=12.0, threads=None, fixed_steps=None):
+    import oracle.orc as orc
+    orc.build()
+    threads = threads or os.cpu_count() or 1
+    orc.set_threads(threads)
+    m = mixed_box_mesh(*MIXED_SAMPLE)
+    o = orc.Modal(m, MIXED_DEGREE)
+    x, _ = o.points()
+    u = o.project(mixed_box_ic(x))
+    L = u.size
+    t, n, t0 = 0.0, 0, time.perf_counter()
+    while True:
+        dt = o.time_step(u, 1e9, 3, 0.0)
+        u = o.rk_update(orc.HLLC, 3, t, dt, u)
+        t += dt
+        n += 1
+        el = time.perf_counter() - t0
+        if (fixed_steps is not None and n >= fixed_steps) or (fixed_steps is None and el >= seconds):
+            break
+    el = time.perf_counter() - t0
+    return {"value": 3 * L * n / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"mixed box {MIXED_SAMPLE[0]}^3 Hex8 + {MIXED_SAMPLE[1]}^3 x 6 Tet4 (L = {L} DOFs), "
+                      f"{n} SSP-RK3 steps, {el:.1f} s, oracle (plain C restatement, OpenMP)",
+            "seconds": el, "steps": n}
+
+
+def modal_roofline(kt, m, L, fp64_peak, hbm_peak, peak_src):
+    """Algorithmic counts of the modal kernels (per launch).
+    cell kernel: volume 2 K 3 M per quadrature point (F . grad psi), lift
+    2 K M per face point and side, stage 4 per DOF; bytes: 3 column
+    accesses + Hex8 192 B / Tet4 96 B of geometry + 4 B per face slot.
+    face kernel: 2 x 2 K M (both traces) + c_R per face point."""
+    M = (MIXED_DEGREE + 1) * (MIXED_DEGREE + 2) * (MIXED_DEGREE + 3) // 6
+    Q = MIXED_DEGREE + 1
+    ct = m.cell_type
+    n_hex = int((ct == 0).sum())
+    n_tet = int((ct == 1).sum())
+    nq = n_hex * Q ** 3 + n_tet * 14
+    interior = m.face_cells[:, 1] >= 0
+    fq_face = np.where(ct[m.face_cells[:, 0]] == 0, Q * Q, 6)
+    face_pts = int(fq_face.sum())
+    face_sides = int(fq_face.sum() + fq_face[interior].sum())
+    cell_flops = 2 * K * 3 * M * nq + 2 * K * M * face_sides + 4 * L
+    face_flops = face_pts * (4 * K * M + C_HLLC)
+    cell_bytes = 24 * L + 192 * n_hex + 96 * n_tet + 4 * (6 * n_hex + 4 * n_tet)
+    dom = "cell_update" if kt["cell_update"] >= kt["face_flux"] else "face_flux"
+    flops = cell_flops if dom == "cell_update" else face_flops
+    t = kt[dom] * 1e-3
+    ach = flops / t / 1e12
+    return {"bound": "fp64", "kernel": dom, "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
+            "frac": ach / fp64_peak, "peak_source": "measured in this run: cuBLAS DGEMM 4096^3",
+            "traffic": None, "alg_flops_per_launch": flops, "launch_ms": kt[dom],
+            "hbm": {"alg_bytes_per_launch": cell_bytes, "achieved": cell_bytes / (kt["cell_update"] * 1e-3) / 1e9,
+                    "peak": hbm_peak, "unit": "GB/s", "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)"},
+            "kernel_ms": kt,
+            "note": "face_flux includes the Taylor-coefficient kernel a = S^T c"}
+
+
+def run_mixed_box(args, rank, world, local_rank):
+    import torch
+    from pvcriemannsolvers_gb300 import General, build
+    build.build()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    n_hex, n_tet = args.mixed_cells
+    m = mixed_box_mesh(n_hex, n_tet)
+    sysm = General(m, MIXED_DEGREE, "hllc", device=local_rank)
+    stream = torch.cuda.Stream(device=dev)
+    sysm.set_stream(stream.cuda_stream)
+    sysm.project(mixed_box_ic(sysm.points()))
+    u0 = sysm.GetSolutionColumn()
+    L = u0.size
+    t = sysm.advance(args.warmup, 1e9, 3, 0.0)
+    sysm.synchronize()
+    torch.cuda.synchronize(dev)
+    launches0 = sysm.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clocks:
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            t = sysm.advance(args.steps, 1e9, 3, t)
+            e1.record(stream)
+        e1.synchronize()
+    launches = sysm.launch_count() - launches0
+    ms = e0.elapsed_time(e1)
+    sol = sysm.GetSolutionColumn()
+    kt = sysm.kernel_times(reps=3)
+    host_in = torch.empty(L, dtype=torch.float64, pin_memory=True).numpy()
+    host_out = torch.empty(L, dtype=torch.float64, pin_memory=True).numpy()
+    host_in[:] = sol
+    e2e_steps = max(1, min(args.steps, 10))
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    te = t
+    for _ in range(e2e_steps):
+        sysm.SetSolutionColumn(host_in)
+        te = sysm.advance(1, 1e9, 3, te)
+        sysm.get_solution_into(host_out)
+    torch.cuda.synchronize(dev)
+    e2e_s = time.perf_counter() - t0
+    sysm.close()
+    hbm_peak, peak_src = measured_peaks()
+    fp64_peak = fp64_peak_tflops(torch, dev)
+    cpu = None
+    if not args.no_cpu:
+        cpu = mixed_box_cpu_sample()
+        cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    rho = sol.reshape(-1, K)
+    line = {
+        "metric": METRIC, "value": 3 * L * args.steps / (ms * 1e-3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": mixed_box_config(n_hex, n_tet),
+        "accuracy": {"t_end": t, "finite": bool(np.isfinite(sol).all()),
+                     "mean_density_coeff_drift": float(abs(rho[:, 0].sum() - u0.reshape(-1, K)[:, 0].sum()))},
+        "clocks": clocks.summary(),
+        "e2e": {"value": 3 * L * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * L,
+                "d2h_bytes_per_step": 8 * L, "steps": e2e_steps,
+                "path": "mcfd_set_solution (pinned host) + mcfd_advance(1) + mcfd_get_solution (pinned host)"},
+        "gpu_launches": launches,
+        "roofline": modal_roofline(kt, m, L, fp64_peak, hbm_peak, peak_src),
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_gpu(args, rank, world, local_rank):
     import torch
     from pvcriemannsolvers_gb300 import build, cases, mesh as meshlib
@@ -354,6 +517,10 @@ def main():
     ap.add_argument("--cells", type=int, default=N_CELLS_1D, help="cells per direction (profiling runs a smaller case)")
     ap.add_argument("--form", default="both", choices=["both", "fp64", "mixed"],
                     help="precision form(s) to time; the line's value is the mixed form when timed")
+    ap.add_argument("--workload", default="vortex", choices=["vortex", "mixed_box"],
+                    help="vortex: the headline DGSEM case; mixed_box: modal DG on hex + tet blocks")
+    ap.add_argument("--mixed-cells", type=int, nargs=2, default=[MIXED_HEX_1D, MIXED_TET_1D],
+                    metavar=("HEX_1D", "TET_1D"), help="block sizes of the mixed box")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -362,6 +529,9 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload == "mixed_box":
+        run_mixed_box(args, rank, world, local_rank)
         return
     if world > 1:
         import torch
