@@ -282,6 +282,34 @@ int64_t mcfd_point_count(const mcfd_handle *h);
 int mcfd_points(const mcfd_handle *h, double *xyz, int64_t n);
 int mcfd_project(mcfd_handle *h, const double *values, int64_t n);
 
+/* Batching (no reference counterpart: in the reference every case is its own
+ * run of the demo/euler/sourceless.cpp:187-215 loop).
+ *
+ * mcfd_set_cases splits one handle's mesh into independent cases: cells
+ * [case_offsets[k], case_offsets[k+1]) form case k (n_cases <= 1024, no face
+ * may join two cases; a disjoint union of meshes qualifies).  From then on
+ * every case takes its own time step (GetTimeStep over its own cells) and
+ * keeps its own time, starting at 0: mcfd_advance steps all cases at once and
+ * returns the smallest case time, mcfd_rk_step applies the given (t, dt) to
+ * every case, boundary values are evaluated at each case's own time, and
+ * mcfd_time_step reports the smallest case step.
+ * mcfd_case_times copies the case times (and, when dt is not NULL, the last
+ * steps) to the host. */
+int mcfd_set_cases(mcfd_handle *h, int32_t n_cases, const int64_t *case_offsets);
+int mcfd_case_times(mcfd_handle *h, double *t, double *dt, int32_t n);
+
+/* An ensemble steps several handles (e.g. one per scheme and degree) with one
+ * CUDA graph per step: the replay forks to every member's stream, runs its dt
+ * reduction and RK stages, and joins, so members run concurrently.  Members
+ * share one device, stay owned by the caller, and must outlive the ensemble;
+ * reconfiguring a member (cases, limiter, stream) after the first advance is
+ * not allowed. */
+typedef struct mcfd_ensemble mcfd_ensemble;
+int mcfd_ensemble_create(mcfd_handle *const *handles, int32_t n, mcfd_ensemble **out);
+int mcfd_ensemble_advance(mcfd_ensemble *e, int32_t n_steps, double dt_guess, int32_t rk_order);
+int mcfd_ensemble_destroy(mcfd_ensemble *e);
+const char *mcfd_ensemble_last_error(const mcfd_ensemble *e);
+
 /* Message describing the last failure on this handle (or of mcfd_create when
  * h is NULL).  Valid until the next call on the handle. */
 const char *mcfd_last_error(const mcfd_handle *h);

@@ -159,6 +159,10 @@ void release(mcfd_handle *h) {
                    l.modal, l.troubled};
   for (void *p : lptrs)
     if (p) cudaFree(p);
+  auto &cs = h->cases;
+  void *cptrs[] = {cs.cell_case, cs.t, cs.dt, cs.rate};
+  for (void *p : cptrs)
+    if (p) cudaFree(p);
   auto &md = h->modal;
   void *mptrs[] = {md.center, md.s, md.vol_off, md.vol, md.cell_faces, md.face_off,
                    md.point_face, md.fpt, md.fnrm, md.fshift, md.taylor, md.values};
@@ -902,6 +906,7 @@ int mcfd_rk_step(mcfd_handle *h, double t, double dt, int32_t order) {
   if (!h || order < 1 || order > 3) return h ? fail(h, MCFD_ERR_ARGUMENT, "order must be 1, 2 or 3") : MCFD_ERR_ARGUMENT;
   cudaSetDevice(h->device);
   h->launches += mcfd::launch_set_state(h, t, dt, dt, 0.0, 0);
+  h->launches += mcfd::launch_set_cases(h, t, dt);
   h->launches += mcfd::launch_rk_stage_sequence(h, order);
   CUDA_TRY(h, cudaGetLastError());
   h->t_host = t + dt;
@@ -940,6 +945,143 @@ int mcfd_advance(mcfd_handle *h, int32_t n_steps, double dt_guess, int32_t rk_or
   return rc;
 }
 
+}  // extern "C"
+
+// Ensemble: several handles stepped by one CUDA graph per step.  The graph
+// forks from the ensemble's stream to every member's stream, captures the
+// member's dt reduction and RK stages there, and joins back, so members with
+// different schemes or degrees run concurrently inside one replay.
+struct mcfd_ensemble {
+  std::vector<mcfd_handle *> members;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> join;
+  cudaGraphExec_t graph = nullptr;
+  int order = 0;
+  std::vector<int> kernels;
+  std::string err;
+};
+
+namespace {
+
+int ens_fail(mcfd_ensemble *e, int code, const std::string &msg) {
+  if (e) e->err = msg; else g_create_error = msg;
+  return code;
+}
+
+void ens_release(mcfd_ensemble *e) {
+  if (e->graph) cudaGraphExecDestroy(e->graph);
+  for (cudaEvent_t ev : e->join)
+    if (ev) cudaEventDestroy(ev);
+  if (e->fork) cudaEventDestroy(e->fork);
+  if (e->stream) cudaStreamDestroy(e->stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+int mcfd_ensemble_create(mcfd_handle *const *handles, int32_t n, mcfd_ensemble **out) {
+  g_create_error.clear();
+  if (!handles || !out || n < 1) return ens_fail(nullptr, MCFD_ERR_ARGUMENT, "null or empty member list");
+  *out = nullptr;
+  for (int32_t i = 0; i < n; ++i) {
+    if (!handles[i]) return ens_fail(nullptr, MCFD_ERR_ARGUMENT, "null member");
+    if (handles[i]->device != handles[0]->device)
+      return ens_fail(nullptr, MCFD_ERR_ARGUMENT, "ensemble members must share one device");
+    for (int32_t j = 0; j < i; ++j)
+      if (handles[j] == handles[i]) return ens_fail(nullptr, MCFD_ERR_ARGUMENT, "a handle appears twice");
+  }
+  mcfd_ensemble *e = new (std::nothrow) mcfd_ensemble();
+  if (!e) return ens_fail(nullptr, MCFD_ERR_ARGUMENT, "out of host memory");
+  e->members.assign(handles, handles + n);
+  e->device = handles[0]->device;
+  e->join.assign(n, nullptr);
+  cudaError_t err = cudaSetDevice(e->device);
+  if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
+  if (err == cudaSuccess) err = cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming);
+  for (int32_t i = 0; i < n && err == cudaSuccess; ++i)
+    err = cudaEventCreateWithFlags(&e->join[i], cudaEventDisableTiming);
+  if (err != cudaSuccess) {
+    g_create_error = std::string("ensemble set-up: ") + cudaGetErrorString(err);
+    ens_release(e);
+    delete e;
+    return MCFD_ERR_CUDA;
+  }
+  *out = e;
+  return MCFD_OK;
+}
+
+int mcfd_ensemble_destroy(mcfd_ensemble *e) {
+  if (!e) return MCFD_ERR_ARGUMENT;
+  cudaSetDevice(e->device);
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  ens_release(e);
+  delete e;
+  return MCFD_OK;
+}
+
+const char *mcfd_ensemble_last_error(const mcfd_ensemble *e) {
+  return e ? e->err.c_str() : g_create_error.c_str();
+}
+
+int mcfd_ensemble_advance(mcfd_ensemble *e, int32_t n_steps, double dt_guess, int32_t rk_order) {
+  if (!e || n_steps < 0 || rk_order < 1 || rk_order > 3) return MCFD_ERR_ARGUMENT;
+  cudaSetDevice(e->device);
+  // per-member step bounds, ordered before the replays
+  for (mcfd_handle *h : e->members) {
+    double cfl = h->opt.cfl > 0 ? h->opt.cfl : cfl_table(rk_order, h->mesh.p);
+    h->launches += mcfd::launch_set_state(h, h->t_host, 0.0, dt_guess, cfl, 1);
+    cudaError_t err = cudaGetLastError();
+    if (err == cudaSuccess) err = cudaStreamSynchronize(h->stream);
+    if (err != cudaSuccess) return ens_fail(e, MCFD_ERR_CUDA, std::string("member set-up: ") + cudaGetErrorString(err));
+  }
+  if (!e->graph || e->order != rk_order) {
+    if (e->graph) { cudaGraphExecDestroy(e->graph); e->graph = nullptr; }
+    e->kernels.assign(e->members.size(), 0);
+    cudaGraph_t graph;
+    cudaError_t err = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
+    if (err == cudaSuccess) err = cudaEventRecord(e->fork, e->stream);
+    for (size_t i = 0; i < e->members.size() && err == cudaSuccess; ++i) {
+      mcfd_handle *h = e->members[i];
+      err = cudaStreamWaitEvent(h->stream, e->fork, 0);
+      if (err != cudaSuccess) break;
+      int k = mcfd::launch_dt(h, h->buf.u);
+      k += mcfd::launch_rk_stage_sequence(h, rk_order);
+      e->kernels[i] = k;
+      err = cudaEventRecord(e->join[i], h->stream);
+      if (err == cudaSuccess) err = cudaStreamWaitEvent(e->stream, e->join[i], 0);
+    }
+    cudaError_t end = cudaStreamEndCapture(e->stream, &graph);
+    if (err == cudaSuccess) err = end;
+    if (err != cudaSuccess) return ens_fail(e, MCFD_ERR_CUDA, std::string("ensemble capture: ") + cudaGetErrorString(err));
+    err = cudaGraphInstantiate(&e->graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (err != cudaSuccess) return ens_fail(e, MCFD_ERR_CUDA, std::string("ensemble graph: ") + cudaGetErrorString(err));
+    e->order = rk_order;
+  }
+  for (int s = 0; s < n_steps; ++s) {
+    cudaError_t err = cudaGraphLaunch(e->graph, e->stream);
+    if (err != cudaSuccess) return ens_fail(e, MCFD_ERR_CUDA, std::string("cudaGraphLaunch: ") + cudaGetErrorString(err));
+  }
+  cudaError_t err = cudaStreamSynchronize(e->stream);
+  if (err != cudaSuccess) return ens_fail(e, MCFD_ERR_CUDA, std::string("ensemble replay: ") + cudaGetErrorString(err));
+  int rc = MCFD_OK;
+  for (size_t i = 0; i < e->members.size(); ++i) {
+    mcfd_handle *h = e->members[i];
+    h->launches += (int64_t)e->kernels[i] * n_steps;
+    mcfd::DevState st;
+    if (cudaMemcpy(&st, h->buf.state, sizeof(st), cudaMemcpyDeviceToHost) == cudaSuccess) h->t_host = st.t;
+    int r = check_status(h);
+    if (r && !rc) {
+      rc = r;
+      e->err = "member " + std::to_string(i) + ": " + h->err;
+    }
+  }
+  return rc;
+}
+
 int mcfd_set_stream(mcfd_handle *h, void *cuda_stream) {
   if (!h) return MCFD_ERR_ARGUMENT;
   cudaSetDevice(h->device);
@@ -970,6 +1112,56 @@ int mcfd_face_node_maps(const mcfd_handle *h, int16_t *holder, int16_t *sharer) 
 }
 
 int64_t mcfd_launch_count(const mcfd_handle *h) { return h ? h->launches : -1; }
+
+int mcfd_set_cases(mcfd_handle *h, int32_t n_cases, const int64_t *case_offsets) {
+  if (!h || n_cases < 1 || !case_offsets) return MCFD_ERR_ARGUMENT;
+  const int64_t C = h->mesh.n_cells;
+  if (n_cases > 1024) return fail(h, MCFD_ERR_UNSUPPORTED, "at most 1024 cases per handle");
+  if (case_offsets[0] != 0 || case_offsets[n_cases] != C)
+    return fail(h, MCFD_ERR_ARGUMENT, "case offsets must run from 0 to the cell count");
+  std::vector<int32_t> cell_case(C);
+  for (int32_t k = 0; k < n_cases; ++k) {
+    if (case_offsets[k + 1] <= case_offsets[k])
+      return fail(h, MCFD_ERR_ARGUMENT, "case offsets must increase strictly");
+    for (int64_t c = case_offsets[k]; c < case_offsets[k + 1]; ++c) cell_case[c] = k;
+  }
+  cudaSetDevice(h->device);
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  // no face may join two cases
+  if (h->mesh.n_faces > 0) {
+    std::vector<int2> fc(h->mesh.n_faces);
+    CUDA_TRY(h, cudaMemcpy(fc.data(), h->mesh.face_cells, sizeof(int2) * fc.size(), cudaMemcpyDeviceToHost));
+    for (const int2 &f : fc)
+      if (f.y >= 0 && cell_case[f.x] != cell_case[f.y])
+        return fail(h, MCFD_ERR_MESH, "a face joins two cases");
+  }
+  auto &cs = h->cases;
+  void *old[] = {cs.cell_case, cs.t, cs.dt, cs.rate};
+  for (void *p : old)
+    if (p) cudaFree(p);
+  cs = mcfd::Cases{};
+  int rc;
+  if ((rc = upload(h, &cs.cell_case, cell_case))) return rc;
+  std::vector<double> zeros(n_cases, 0.0);
+  if ((rc = upload(h, &cs.t, zeros))) return rc;
+  if ((rc = upload(h, &cs.dt, zeros))) return rc;
+  std::vector<unsigned long long> zr(n_cases, 0ull);
+  if ((rc = upload(h, &cs.rate, zr))) return rc;
+  cs.offsets.assign(case_offsets, case_offsets + n_cases + 1);
+  cs.n = n_cases;
+  if (h->step_graph) { cudaGraphExecDestroy(h->step_graph); h->step_graph = nullptr; }
+  return MCFD_OK;
+}
+
+int mcfd_case_times(mcfd_handle *h, double *t, double *dt, int32_t n) {
+  if (!h || !t || n != h->cases.n || n < 1) return MCFD_ERR_ARGUMENT;
+  cudaSetDevice(h->device);
+  CUDA_TRY(h, cudaMemcpyAsync(t, h->cases.t, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
+  if (dt)
+    CUDA_TRY(h, cudaMemcpyAsync(dt, h->cases.dt, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  return MCFD_OK;
+}
 
 int64_t mcfd_point_count(const mcfd_handle *h) {
   if (!h) return -1;

@@ -52,6 +52,7 @@ struct FaceArgs {
   int64_t n_points;
   int n_groups;
   int fr;  // flux reconstruction: mark faces without a boundary condition
+  CaseView cs;
 };
 
 // FR: a boundary face point without a registered boundary gets no correction
@@ -72,7 +73,23 @@ struct CellArgs {
   int advance_time;
   int fr;     // 0: dg::Lobatto (weak form), 1: fr::Lobatto (Huynh g2)
   double g1;  // FR: g_R'(1) of the Huynh g2 correction
+  CaseView cs;
 };
+
+// Step of the case that owns cell c (the handle's step without cases).
+__device__ __forceinline__ double cell_dt(const CaseView &cs, const DevState *state, int64_t c) {
+  return cs.dt ? cs.dt[cs.cell_case[c]] : state->dt;
+}
+
+// Stage time t + stage_c dt of the case that owns cell c.
+__device__ __forceinline__ double stage_time(const CaseView &cs, const DevState *state,
+                                             int64_t c, double stage_c) {
+  if (cs.t) {
+    const int k = cs.cell_case[c];
+    return cs.t[k] + stage_c * cs.dt[k];
+  }
+  return state->t + stage_c * state->dt;
+}
 
 // FR: axis and orientation of each local hex face (fr/lobatto.hpp:81-152)
 // sides 0..5 -> axes 2, 1, 0, 1, 0, 2 (one nibble per side, side 0 lowest)
@@ -173,7 +190,7 @@ __global__ void __launch_bounds__(256) face_flux_kernel(FaceArgs a) {
     int grp = a.face_group[f];
     if (grp >= 0 && grp < a.n_groups && a.bcs[grp].kind != kBcNone) {
       const BcDev &bc = a.bcs[grp];
-      double t = a.state->t + a.stage_c * a.state->dt;
+      double t = stage_time(a.cs, a.state, cells.x, a.stage_c);
       double given[kK];
       given_value(bc, a.face_xyz + gid * 3, t, given);
       flux_boundary<R>(bc.kind, l, given, n, out, &not_converged);
@@ -309,7 +326,7 @@ cell_update_kernel(CellArgs a) {
       out[r] = v;
     }
   } else {
-    const double dt = a.state->dt;
+    const double dt = cell_dt(a.cs, a.state, c);
 #pragma unroll
     for (int r = 0; r < kK; ++r) {
       double next = uq[r] + (res[r] * inv_w) * dt;
@@ -328,7 +345,7 @@ cell_update_kernel(CellArgs a) {
     }
   }
   if (bad) atomicOr(&a.state->status, (unsigned)kStatusNonFinite);
-  if (a.advance_time && blockIdx.x == 0 && tid == 0) a.state->t += a.state->dt;
+  if (a.advance_time && !a.cs.dt && blockIdx.x == 0 && tid == 0) a.state->t += a.state->dt;
 }
 
 // Mixed-precision form of cell_update_kernel.  In FP32: the volume flux and
@@ -454,7 +471,7 @@ cell_update_mixed_kernel(CellArgs a, const float *__restrict__ geo32) {
       out[rr] = val;
     }
   } else {
-    const float wdt = inv_w * f64_to_f32(a.state->dt);
+    const float wdt = inv_w * f64_to_f32(cell_dt(a.cs, a.state, c));
 #pragma unroll
     for (int rr = 0; rr < kK; ++rr) {
       double next = uq[rr] + f32_to_f64(res[rr] * wdt);
@@ -473,15 +490,36 @@ cell_update_mixed_kernel(CellArgs a, const float *__restrict__ geo32) {
     }
   }
   if (bad) atomicOr(&a.state->status, (unsigned)kStatusNonFinite);
-  if (a.advance_time && blockIdx.x == 0 && tid == 0) a.state->t += a.state->dt;
+  if (a.advance_time && !a.cs.dt && blockIdx.x == 0 && tid == 0) a.state->t += a.state->dt;
 }
 
 // dt: max over nodes of max(1e-5, max_speed) / length, as the bit pattern of
 // a positive double (monotone as an unsigned integer).
+// Max of `rate` into the handle's word, or into the word of each lane's case.
+// Cases are contiguous runs of cells, so almost every warp is uniform.
+__device__ __forceinline__ void reduce_rate(double rate, int key, DevState *state,
+                                            unsigned long long *case_rate) {
+  if (case_rate) {
+    const int key0 = __shfl_sync(0xffffffffu, key, 0);
+    if (__all_sync(0xffffffffu, key == key0)) {
+      for (int o = 16; o > 0; o >>= 1) rate = fmax(rate, __shfl_xor_sync(0xffffffffu, rate, o));
+      if ((threadIdx.x & 31) == 0 && key0 >= 0 && rate > 0)
+        atomicMax(&case_rate[key0], (unsigned long long)__double_as_longlong(rate));
+    } else if (key >= 0 && rate > 0) {
+      atomicMax(&case_rate[key], (unsigned long long)__double_as_longlong(rate));
+    }
+    return;
+  }
+  for (int o = 16; o > 0; o >>= 1) rate = fmax(rate, __shfl_xor_sync(0xffffffffu, rate, o));
+  if ((threadIdx.x & 31) == 0 && rate > 0)
+    atomicMax(&state->max_rate_bits, (unsigned long long)__double_as_longlong(rate));
+}
+
 template <int Q>
 __global__ void __launch_bounds__(256)
 dt_reduce_kernel(const double *u, const double *cell_rate, int64_t n_nodes,
-                 DevState *state) {
+                 DevState *state, const int32_t *cell_case,
+                 unsigned long long *case_rate) {
   constexpr int N = Q * Q * Q;
   int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double rate = 0;
@@ -492,16 +530,15 @@ dt_reduce_kernel(const double *u, const double *cell_rate, int64_t n_nodes,
     double speed = c + sqrt(w.u * w.u + w.v * w.v + w.w * w.w);
     rate = fmax(speed, 1e-5) * cell_rate[gid / N];
   }
-  for (int o = 16; o > 0; o >>= 1) rate = fmax(rate, __shfl_xor_sync(0xffffffffu, rate, o));
-  if ((threadIdx.x & 31) == 0 && rate > 0)
-    atomicMax(&state->max_rate_bits, (unsigned long long)__double_as_longlong(rate));
+  reduce_rate(rate, (case_rate && gid < n_nodes) ? cell_case[gid / N] : -1, state, case_rate);
 }
 
 // Mixed-precision dt reduction: wave speeds in FP32.
 template <int Q>
 __global__ void __launch_bounds__(256)
 dt_reduce_mixed_kernel(const double *u, const double *cell_rate, int64_t n_nodes,
-                       DevState *state) {
+                       DevState *state, const int32_t *cell_case,
+                       unsigned long long *case_rate) {
   constexpr int N = Q * Q * Q;
   int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double rate = 0;
@@ -521,9 +558,7 @@ dt_reduce_mixed_kernel(const double *u, const double *cell_rate, int64_t n_nodes
     }
     rate = (double)fmaxf(speed, 1e-5f) * cell_rate[gid / N];
   }
-  for (int o = 16; o > 0; o >>= 1) rate = fmax(rate, __shfl_xor_sync(0xffffffffu, rate, o));
-  if ((threadIdx.x & 31) == 0 && rate > 0)
-    atomicMax(&state->max_rate_bits, (unsigned long long)__double_as_longlong(rate));
+  reduce_rate(rate, (case_rate && gid < n_nodes) ? cell_case[gid / N] : -1, state, case_rate);
 }
 
 __global__ void dt_finalize_kernel(DevState *state, int fr) {
@@ -535,6 +570,57 @@ __global__ void dt_finalize_kernel(DevState *state, int fr) {
   if (fr) dt = fmin(state->dt_guess, 2.0 * dt);
   state->dt = dt;
   state->max_rate_bits = 0ull;
+}
+
+// Per-case finalisation (one block): dt_k from each case's maximum rate, the
+// handle's dt = min over cases (what mcfd_time_step reports).
+__global__ void dt_finalize_cases_kernel(DevState *state, unsigned long long *case_rate,
+                                         double *case_dt, int n, int fr) {
+  __shared__ double s_min[32];
+  double local = 1.e+300;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const double max_rate = __longlong_as_double((long long)case_rate[k]);
+    const double min_dt = max_rate > 0 ? 1.0 / max_rate : 1.e+100;
+    double dt = fmin(state->cfl * min_dt, state->dt_guess);
+    if (fr) dt = fmin(state->dt_guess, 2.0 * dt);
+    case_dt[k] = dt;
+    case_rate[k] = 0ull;
+    local = fmin(local, dt);
+  }
+  for (int o = 16; o > 0; o >>= 1) local = fmin(local, __shfl_xor_sync(0xffffffffu, local, o));
+  if ((threadIdx.x & 31) == 0) s_min[threadIdx.x >> 5] = local;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = s_min[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmin(m, s_min[w]);
+    state->dt = m;
+  }
+}
+
+// After the last stage: t_k += dt_k; the handle's t = min over cases.
+__global__ void advance_cases_kernel(DevState *state, double *case_t, const double *case_dt,
+                                     int n) {
+  __shared__ double s_min[32];
+  double local = 1.e+300;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    case_t[k] += case_dt[k];
+    local = fmin(local, case_t[k]);
+  }
+  for (int o = 16; o > 0; o >>= 1) local = fmin(local, __shfl_xor_sync(0xffffffffu, local, o));
+  if ((threadIdx.x & 31) == 0) s_min[threadIdx.x >> 5] = local;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = s_min[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmin(m, s_min[w]);
+    state->t = m;
+  }
+}
+
+__global__ void set_cases_kernel(double *case_t, double *case_dt, int n, double t, double dt) {
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    case_t[k] = t;
+    case_dt[k] = dt;
+  }
 }
 
 __global__ void set_state_kernel(DevState *state, double t, double dt,
@@ -613,7 +699,7 @@ int launch_face_flux(mcfd_handle *h, const double *u, double stage_c) {
   const Mesh &m = h->mesh;
   FaceArgs fa{u, m.face_cells, m.face_group, m.face_geo, m.face_xyz,
               m.face_map, m.bcs, h->buf.flux, h->buf.state, stage_c,
-              m.n_points, m.n_groups, h->opt.scheme == 1};
+              m.n_points, m.n_groups, h->opt.scheme == 1, case_view(h)};
   if (m.n_points == 0) return 0;
   switch (m.q) {
     case 2: face_dispatch_r<2>(h, fa); break;
@@ -629,11 +715,24 @@ int launch_cell_update(mcfd_handle *h, int stage, const double *u_in,
     return launch_modal_cell_update(h, stage, u_in, u0, u_out, advance_time);
   const Mesh &m = h->mesh;
   CellArgs ca{u_in, u0, u_out, m.cell_geo, m.cell_flux, h->buf.flux, m.dmat,
-              h->buf.state, m.n_cells, advance_time, h->opt.scheme == 1, h->opt.fr_g1};
+              h->buf.state, m.n_cells, advance_time, h->opt.scheme == 1, h->opt.fr_g1,
+              case_view(h)};
   switch (m.q) {
     case 2: cell_dispatch_s<2>(h, stage, ca); break;
     case 3: cell_dispatch_s<3>(h, stage, ca); break;
     default: cell_dispatch_s<4>(h, stage, ca); break;
+  }
+  return 1;
+}
+
+// Finalisation of a dt reduction: the handle's word, or one word per case.
+int launch_dt_finalize(mcfd_handle *h) {
+  const int fr = h->opt.scheme == 1;
+  if (h->cases.n) {
+    dt_finalize_cases_kernel<<<1, 1024, 0, h->stream>>>(h->buf.state, h->cases.rate,
+                                                      h->cases.dt, h->cases.n, fr);
+  } else {
+    dt_finalize_kernel<<<1, 1, 0, h->stream>>>(h->buf.state, fr);
   }
   return 1;
 }
@@ -643,22 +742,34 @@ int launch_dt(mcfd_handle *h, const double *u) {
   const Mesh &m = h->mesh;
   int64_t nodes = m.n_cells * m.n;
   unsigned blocks = (unsigned)((nodes + 255) / 256);
+  const int32_t *cc = h->cases.cell_case;
+  unsigned long long *cr = h->cases.n ? h->cases.rate : nullptr;
   if (h->opt.precision == 1) {
     switch (m.q) {
-      case 2: dt_reduce_mixed_kernel<2><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state); break;
-      case 3: dt_reduce_mixed_kernel<3><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state); break;
-      default: dt_reduce_mixed_kernel<4><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state); break;
+      case 2: dt_reduce_mixed_kernel<2><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr); break;
+      case 3: dt_reduce_mixed_kernel<3><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr); break;
+      default: dt_reduce_mixed_kernel<4><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr); break;
     }
-    dt_finalize_kernel<<<1, 1, 0, h->stream>>>(h->buf.state, h->opt.scheme == 1);
-    return 2;
+  } else {
+    switch (m.q) {
+      case 2: dt_reduce_kernel<2><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr); break;
+      case 3: dt_reduce_kernel<3><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr); break;
+      default: dt_reduce_kernel<4><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr); break;
+    }
   }
-  switch (m.q) {
-    case 2: dt_reduce_kernel<2><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state); break;
-    case 3: dt_reduce_kernel<3><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state); break;
-    default: dt_reduce_kernel<4><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state); break;
-  }
-  dt_finalize_kernel<<<1, 1, 0, h->stream>>>(h->buf.state, h->opt.scheme == 1);
-  return 2;
+  return 1 + launch_dt_finalize(h);
+}
+
+int launch_advance_cases(mcfd_handle *h) {
+  if (!h->cases.n) return 0;
+  advance_cases_kernel<<<1, 1024, 0, h->stream>>>(h->buf.state, h->cases.t, h->cases.dt, h->cases.n);
+  return 1;
+}
+
+int launch_set_cases(mcfd_handle *h, double t, double dt) {
+  if (!h->cases.n) return 0;
+  set_cases_kernel<<<1, 1024, 0, h->stream>>>(h->cases.t, h->cases.dt, h->cases.n, t, dt);
+  return 1;
 }
 
 // ---------------------------------------------------------------------------
@@ -707,9 +818,9 @@ int launch_residual_static_scratch(mcfd_handle *h, const double *d_u,
   const Mesh &m = h->mesh;
   FaceArgs fa{d_u, m.face_cells, m.face_group, m.face_geo, m.face_xyz,
               m.face_map, m.bcs, scratch, h->buf.state, 0.0,
-              m.n_points, m.n_groups, h->opt.scheme == 1};
+              m.n_points, m.n_groups, h->opt.scheme == 1, case_view(h)};
   CellArgs ca{d_u, nullptr, d_r, m.cell_geo, m.cell_flux, scratch, m.dmat,
-              h->buf.state, m.n_cells, 0, h->opt.scheme == 1, h->opt.fr_g1};
+              h->buf.state, m.n_cells, 0, h->opt.scheme == 1, h->opt.fr_g1, case_view(h)};
   int n = 0;
   if (m.n_points > 0) {
     switch (m.q) {
@@ -757,7 +868,7 @@ int launch_rk_stage_sequence(mcfd_handle *h, int order) {
     n += launch_cell_update(h, kStageRk3Last, b.u2, b.u, b.u, 1);
     n += launch_limiter(h, b.u);
   }
-  return n;
+  return n + launch_advance_cases(h);
 }
 
 }  // namespace mcfd

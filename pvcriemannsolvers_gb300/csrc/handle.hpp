@@ -108,6 +108,26 @@ struct Modal {
   std::vector<double> host_points;  // [volume points][3] global coordinates
 };
 
+// Independent cases inside one handle (an ensemble member: disjoint meshes
+// concatenated).  Cells [offsets[k], offsets[k+1]) form case k; no face
+// joins two cases.  Every case has its own time step (the minimum over its
+// cells) and its own time.
+struct Cases {
+  int n = 0;
+  int32_t *cell_case = nullptr;        // [cells] case id
+  double *t = nullptr;                 // [n] time of each case
+  double *dt = nullptr;                // [n] current step of each case
+  unsigned long long *rate = nullptr;  // [n] max of max_speed / length (bits)
+  std::vector<int64_t> offsets;        // [n + 1] host copy
+};
+
+// Case fields of the kernel argument blocks (all null without cases).
+struct CaseView {
+  const int32_t *cell_case;
+  const double *t;
+  const double *dt;
+};
+
 struct Buffers {
   double *u = nullptr;     // current solution
   double *u1 = nullptr;    // stage buffers
@@ -136,6 +156,7 @@ struct mcfd_handle {
   mcfd::Buffers buf;
   mcfd::Limiter lim;
   mcfd::Modal modal;
+  mcfd::Cases cases;
   double t_host = 0;
   int64_t launches = 0;
   std::string err;
@@ -154,9 +175,20 @@ int launch_face_flux(mcfd_handle *h, const double *u, double stage_c);
 int launch_cell_update(mcfd_handle *h, int stage, const double *u_in,
                        const double *u0, double *u_out, int advance_time);
 int launch_dt(mcfd_handle *h, const double *u);
+// dt finalisation after a max-rate reduction (handle word or per case).
+int launch_dt_finalize(mcfd_handle *h);
 int launch_rk_stage_sequence(mcfd_handle *h, int order);
 // WENO limiter pass on a solution buffer, in place (weno.cu).
 int launch_limiter(mcfd_handle *h, double *u);
+
+// Cases (dgsem.cu): per-case time advance after the last stage, and the
+// per-case stage time / step set by mcfd_rk_step.
+int launch_advance_cases(mcfd_handle *h);
+int launch_set_cases(mcfd_handle *h, double t, double dt);
+inline CaseView case_view(const mcfd_handle *h) {
+  if (h->cases.n == 0) return CaseView{nullptr, nullptr, nullptr};
+  return CaseView{h->cases.cell_case, h->cases.t, h->cases.dt};
+}
 
 // Modal DG (modal.cu): the same stage interface as the nodal launchers.
 constexpr int kSchemeModal = 2;

@@ -125,6 +125,7 @@ struct ModalFaceArgs {
   double stage_c;
   int64_t n_points;
   int n_groups;
+  CaseView cs;
 };
 
 template <int M>
@@ -166,7 +167,12 @@ __global__ void __launch_bounds__(256) modal_face_kernel(ModalFaceArgs a) {
     if (grp >= 0 && grp < a.n_groups && a.bcs[grp].kind != kBcNone) {
       const BcDev &bc = a.bcs[grp];
       double given[kK];
-      modal_given(bc, x.x, x.y, x.z, a.state->t + a.stage_c * a.state->dt, given);
+      double t = a.state->t + a.stage_c * a.state->dt;
+      if (a.cs.t) {
+        const int k = a.cs.cell_case[cells.x];
+        t = a.cs.t[k] + a.stage_c * a.cs.dt[k];
+      }
+      modal_given(bc, x.x, x.y, x.z, t, given);
       flux_boundary<R>(bc.kind, l, given, n, out, &not_converged);
     } else {
 #pragma unroll
@@ -194,6 +200,7 @@ struct ModalCellArgs {
   DevState *state;
   int64_t n_cells;
   int advance_time;
+  CaseView cs;
 };
 
 template <int M, int STAGE>
@@ -272,7 +279,8 @@ __global__ void __launch_bounds__(ModalCfg<M>::kBlock) modal_cell_kernel(ModalCe
   const double *sc = a.s + c * NS;
   const double *uin = a.u_in + c * KM;
   double *out = a.u_out + c * KM;
-  const double dt = STAGE == kStageResidual ? 0.0 : a.state->dt;
+  const double dt = STAGE == kStageResidual ? 0.0
+                    : (a.cs.dt ? a.cs.dt[a.cs.cell_case[c]] : a.state->dt);
   bool bad = false;
 #pragma unroll
   for (int m = 0; m < M; ++m) {
@@ -304,7 +312,7 @@ __global__ void __launch_bounds__(ModalCfg<M>::kBlock) modal_cell_kernel(ModalCe
     }
   }
   if (bad) atomicOr(&a.state->status, (unsigned)kStatusNonFinite);
-  if (a.advance_time && c == 0) a.state->t += a.state->dt;
+  if (a.advance_time && !a.cs.dt && c == 0) a.state->t += a.state->dt;
 }
 
 // max over the first M quadrature points of (|u| + c) / length, per cell
@@ -313,7 +321,7 @@ template <int M>
 __global__ void __launch_bounds__(256)
 modal_dt_kernel(const double *u, const double *s, const double4 *center,
                 const int32_t *vol_off, const double4 *vol, int64_t n_cells,
-                DevState *state) {
+                DevState *state, const int32_t *cell_case, unsigned long long *case_rate) {
   constexpr int KM = kK * M, NS = M * (M + 1) / 2;
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double rate = 0;
@@ -346,16 +354,23 @@ modal_dt_kernel(const double *u, const double *s, const double4 *center,
     }
     rate = max_speed * center[c].w;
   }
+  // max into the handle's word, or into each cell's case word (cases are
+  // contiguous cell runs, so warps are almost always uniform)
+  if (case_rate) {
+    const int key = c < n_cells ? cell_case[c] : -1;
+    const int key0 = __shfl_sync(0xffffffffu, key, 0);
+    if (__all_sync(0xffffffffu, key == key0)) {
+      for (int o = 16; o > 0; o >>= 1) rate = fmax(rate, __shfl_xor_sync(0xffffffffu, rate, o));
+      if ((threadIdx.x & 31) == 0 && key0 >= 0 && rate > 0)
+        atomicMax(&case_rate[key0], (unsigned long long)__double_as_longlong(rate));
+    } else if (key >= 0 && rate > 0) {
+      atomicMax(&case_rate[key], (unsigned long long)__double_as_longlong(rate));
+    }
+    return;
+  }
   for (int o = 16; o > 0; o >>= 1) rate = fmax(rate, __shfl_xor_sync(0xffffffffu, rate, o));
   if ((threadIdx.x & 31) == 0 && rate > 0)
     atomicMax(&state->max_rate_bits, (unsigned long long)__double_as_longlong(rate));
-}
-
-__global__ void modal_dt_finalize_kernel(DevState *state) {
-  const double max_rate = __longlong_as_double((long long)state->max_rate_bits);
-  const double min_dt = max_rate > 0 ? 1.0 / max_rate : 1.e+100;
-  state->dt = fmin(state->cfl * min_dt, state->dt_guess);
-  state->max_rate_bits = 0ull;
 }
 
 // Projection::Approximate (projection.hpp:28-42): coeff = sum_q (f_q psi(x_q)) w_q
@@ -437,7 +452,7 @@ int launch_modal_face_flux(mcfd_handle *h, const double *u, double stage_c) {
   if (md.n_fpts == 0) return n;
   ModalFaceArgs fa{md.taylor, md.center, m.face_cells, m.face_group, md.point_face,
                    md.fpt, md.fnrm, md.fshift, m.bcs, h->buf.flux, h->buf.state,
-                   stage_c, md.n_fpts, m.n_groups};
+                   stage_c, md.n_fpts, m.n_groups, case_view(h)};
   switch (md.m) {
     case 4: modal_face_dispatch<4>(h, fa); break;
     case 10: modal_face_dispatch<10>(h, fa); break;
@@ -451,7 +466,7 @@ int launch_modal_cell_update(mcfd_handle *h, int stage, const double *u_in,
   const Modal &md = h->modal;
   ModalCellArgs ca{u_in, u0, u_out, md.taylor, md.s, md.center, md.vol_off, md.vol,
                    md.cell_faces, md.face_off, md.fpt, md.fshift, h->buf.flux,
-                   h->buf.state, h->mesh.n_cells, advance_time};
+                   h->buf.state, h->mesh.n_cells, advance_time, case_view(h)};
   switch (md.m) {
     case 4: modal_cell_dispatch<4>(h, stage, ca); break;
     case 10: modal_cell_dispatch<10>(h, stage, ca); break;
@@ -464,13 +479,14 @@ int launch_modal_dt(mcfd_handle *h, const double *u) {
   const Modal &md = h->modal;
   const int64_t C = h->mesh.n_cells;
   const unsigned blocks = (unsigned)((C + 255) / 256);
+  const int32_t *cc = h->cases.cell_case;
+  unsigned long long *cr = h->cases.n ? h->cases.rate : nullptr;
   switch (md.m) {
-    case 4: modal_dt_kernel<4><<<blocks, 256, 0, h->stream>>>(u, md.s, md.center, md.vol_off, md.vol, C, h->buf.state); break;
-    case 10: modal_dt_kernel<10><<<blocks, 256, 0, h->stream>>>(u, md.s, md.center, md.vol_off, md.vol, C, h->buf.state); break;
-    default: modal_dt_kernel<20><<<blocks, 256, 0, h->stream>>>(u, md.s, md.center, md.vol_off, md.vol, C, h->buf.state); break;
+    case 4: modal_dt_kernel<4><<<blocks, 256, 0, h->stream>>>(u, md.s, md.center, md.vol_off, md.vol, C, h->buf.state, cc, cr); break;
+    case 10: modal_dt_kernel<10><<<blocks, 256, 0, h->stream>>>(u, md.s, md.center, md.vol_off, md.vol, C, h->buf.state, cc, cr); break;
+    default: modal_dt_kernel<20><<<blocks, 256, 0, h->stream>>>(u, md.s, md.center, md.vol_off, md.vol, C, h->buf.state, cc, cr); break;
   }
-  modal_dt_finalize_kernel<<<1, 1, 0, h->stream>>>(h->buf.state);
-  return 2;
+  return 1 + launch_dt_finalize(h);
 }
 
 int launch_modal_project(mcfd_handle *h, double *u) {

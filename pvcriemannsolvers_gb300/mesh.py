@@ -249,6 +249,11 @@ def tet_box(shape, lengths=(1.0, 1.0, 1.0), origin=(0.0, 0.0, 0.0),
     order = np.lexsort((cells, key[:, 2], key[:, 1], key[:, 0]))
     key, cells, sides, fn = key[order], cells[order], sides[order], fn[order]
     same = np.all(key[1:] == key[:-1], axis=1)
+    if np.any(same[1:] & same[:-1]):
+        # three faces share one periodic node set: the wrap is too short to
+        # tell the faces apart by their nodes
+        raise ValueError("periodic tetrahedral box too small: use at least 3 cells along "
+                         "all but one periodic axis")
     first = np.flatnonzero(same)                                 # pairs (first, first + 1)
     paired = np.zeros(key.shape[0], dtype=bool)
     paired[first] = True

@@ -258,6 +258,20 @@ class Lobatto:
     def synchronize(self) -> None:
         self._check(self._lib.mcfd_synchronize(self._h))
 
+    # -- batching: independent cases inside this handle
+    def set_cases(self, case_offsets) -> None:
+        """Cells [offsets[k], offsets[k+1]) form case k, with its own dt and t."""
+        off = np.ascontiguousarray(case_offsets, dtype=np.int64)
+        self._check(self._lib.mcfd_set_cases(self._h, off.size - 1, off.ctypes.data_as(C.POINTER(C.c_int64))))
+        self.n_cases = off.size - 1
+
+    def case_times(self) -> tuple[np.ndarray, np.ndarray]:
+        """(t, last dt) of every case."""
+        t = np.empty(self.n_cases)
+        dt = np.empty(self.n_cases)
+        self._check(self._lib.mcfd_case_times(self._h, capi.dptr(t), capi.dptr(dt), self.n_cases))
+        return t, dt
+
     def set_stream(self, stream_ptr: int | None) -> None:
         self._check(self._lib.mcfd_set_stream(self._h, C.c_void_p(stream_ptr or 0)))
 
@@ -295,6 +309,38 @@ class General(Lobatto):
 
     def face_node_maps(self):
         raise NotImplementedError("the modal scheme evaluates both sides at each face point")
+
+
+class Ensemble:
+    """Several systems stepped by one CUDA graph per step (mcfd_ensemble)."""
+
+    def __init__(self, systems):
+        self._lib = capi.load()
+        self.systems = list(systems)
+        arr = (C.c_void_p * len(self.systems))(*[s.handle.value for s in self.systems])
+        e = C.c_void_p()
+        code = self._lib.mcfd_ensemble_create(arr, len(self.systems), C.byref(e))
+        if code != capi.OK:
+            msg = self._lib.mcfd_ensemble_last_error(None)
+            raise capi.McfdError(code, msg.decode() if msg else "")
+        self._e = e
+
+    def advance(self, n_steps: int, dt_guess: float, rk_order: int) -> None:
+        code = self._lib.mcfd_ensemble_advance(self._e, int(n_steps), float(dt_guess), int(rk_order))
+        if code != capi.OK:
+            msg = self._lib.mcfd_ensemble_last_error(self._e)
+            raise capi.McfdError(code, msg.decode() if msg else "")
+
+    def close(self) -> None:
+        if getattr(self, "_e", None):
+            self._lib.mcfd_ensemble_destroy(self._e)
+            self._e = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class RungeKutta:

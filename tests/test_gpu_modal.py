@@ -137,7 +137,7 @@ def test_modal_advance_matches_oracle_loop(gpu):
 
 
 def test_modal_rejections(gpu):
-    m = meshlib.tet_box((2, 2, 2), periodic=(True,) * 3)
+    m = meshlib.tet_box((3, 3, 2), periodic=(True,) * 3)
     with pytest.raises(capi.McfdError):
         Lobatto(m, 2)                            # Tet4 cells need the modal scheme
     hexes = meshlib.box((2, 2, 2), periodic=(True,) * 3)

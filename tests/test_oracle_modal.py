@@ -116,3 +116,8 @@ def test_tet_mesh_is_conforming_and_oriented():
     sh = m.face_shift[m.face_group < 0]
     assert set(np.unique(np.round(sh, 12)).tolist()) <= {-1.0, 0.0}
     assert np.all(sh[:, 1] == 0)
+
+
+def test_tet_box_rejects_ambiguous_periodic_wrap():
+    with pytest.raises(ValueError):
+        meshlib.tet_box((2, 2, 2), periodic=(True,) * 3)
