@@ -450,6 +450,202 @@ def run_mixed_box(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# Ensemble: 64 independent periodic unit-cube cases (numpy PCG64 seed 1):
+# element counts log-uniform in [4k, 200k]; each case Hex8 or 6-tet-split
+# (fair draw), p in {1, 2, 3} (uniform draw); Hex8 cases use DGSEM or modal
+# DG (fair draw), Tet4 cases modal DG; Rusanov; rho = 1 + sum_{m=1..3}
+# a_m sin(2 pi k_m . x + phi_m), a_m ~ U(0, 0.1), |k_m|_inf <= 3,
+# phi_m ~ U(0, 2 pi); uniform velocity, direction on the sphere, magnitude
+# U(0, 0.5); p = 1.  Cases of one (scheme, p) share a handle (mcfd_set_cases,
+# own dt and t per case); the handles form one mcfd_ensemble (one CUDA graph
+# per step, forked over the handles' streams).
+ENSEMBLE_CASES = 64
+
+
+def ensemble_spec(n_cases=ENSEMBLE_CASES, seed=1, scale=1.0):
+    rng = np.random.default_rng(seed)
+    specs = []
+    for k in range(n_cases):
+        count = float(np.exp(rng.uniform(np.log(4000), np.log(200000)))) * scale
+        tet = bool(rng.integers(0, 2))
+        p = int(rng.integers(1, 4))
+        modal_hex = bool(rng.integers(0, 2))
+        waves = [(rng.uniform(0, 0.1), rng.integers(-3, 4, 3), rng.uniform(0, 2 * np.pi)) for _ in range(3)]
+        d = rng.normal(size=3)
+        vel = rng.uniform(0, 0.5) * d / np.linalg.norm(d)
+        n = max(3, int(round((count / 6) ** (1 / 3)))) if tet else max(3, int(round(count ** (1 / 3))))
+        scheme = "modal" if (tet or modal_hex) else "dgsem"
+        specs.append({"case": k, "tet": tet, "p": p, "scheme": scheme, "n": n, "waves": waves, "vel": vel})
+    return specs
+
+
+def ensemble_state(x, spec):
+    from pvcriemannsolvers_gb300 import cases
+    rho = np.ones(len(x))
+    for a, kv, phi in spec["waves"]:
+        rho += a * np.sin(2 * np.pi * (x @ kv) + phi)
+    n = len(x)
+    v = spec["vel"]
+    return cases.prim_to_cons(rho, np.full(n, v[0]), np.full(n, v[1]), np.full(n, v[2]), np.ones(n))
+
+
+def ensemble_mesh(spec):
+    from pvcriemannsolvers_gb300 import mesh as meshlib
+    make = meshlib.tet_box if spec["tet"] else meshlib.box
+    return make((spec["n"],) * 3, periodic=(True,) * 3)
+
+
+def build_ensemble(specs, device=0):
+    """Group the cases by (scheme, p); one handle per group with its cases."""
+    from pvcriemannsolvers_gb300 import General, Lobatto, mesh as meshlib
+    groups = {}
+    for sp in specs:
+        groups.setdefault((sp["scheme"], sp["p"]), []).append(sp)
+    members = []
+    for (scheme, p), sps in sorted(groups.items()):
+        meshes = [ensemble_mesh(sp) for sp in sps]
+        m = meshlib.concat(*meshes)
+        sysm = General(m, p, "rusanov", device=device) if scheme == "modal" else \
+            Lobatto(m, p, "rusanov", device=device)
+        if scheme == "modal":
+            # volume points come cell by cell; a case's cells are one type
+            pts = sysm.points()
+            vals, off = [], 0
+            for q, sp in zip(meshes, sps):
+                ppc = (p + 1) ** 3 if not sp["tet"] else (14 if p <= 2 else 24)
+                n = q.n_cells * ppc
+                vals.append(ensemble_state(pts[off:off + n], sp))
+                off += n
+            sysm.project(np.concatenate(vals))
+        else:
+            cols = [ensemble_state(meshlib.node_coordinates(q, p).reshape(-1, 3), sp).ravel()
+                    for q, sp in zip(meshes, sps)]
+            sysm.SetSolutionColumn(np.concatenate(cols))
+        sysm.set_cases(np.concatenate([[0], np.cumsum([q.n_cells for q in meshes])]))
+        members.append({"scheme": scheme, "p": p, "system": sysm, "cases": len(sps),
+                        "cells": m.n_cells, "dofs": sysm.column_size})
+    return members
+
+
+def ensemble_cpu_sample(specs, seconds=12.0, threads=None):
+    """The oracle on the smallest cases of the ensemble, one after another."""
+    import oracle.orc as orc
+    orc.build()
+    threads = threads or os.cpu_count() or 1
+    orc.set_threads(threads)
+    from pvcriemannsolvers_gb300 import mesh as meshlib
+    done, dofs_steps, t0 = 0, 0, time.perf_counter()
+    for sp in sorted(specs, key=lambda s: s["n"] ** 3 * (6 if s["tet"] else 1)):
+        q = ensemble_mesh(sp)
+        if sp["scheme"] == "modal":
+            o = orc.Modal(q, sp["p"])
+            u = o.project(ensemble_state(o.points()[0], sp))
+        else:
+            o = orc.Mesh(q, sp["p"])
+            u = ensemble_state(meshlib.node_coordinates(q, sp["p"]).reshape(-1, 3), sp).ravel()
+        t = 0.0
+        for _ in range(2):
+            dt = o.time_step(u, 1e9, 3, 0.0)
+            u = o.rk_update(orc.RUSANOV, 3, t, dt, u)
+            t += dt
+            dofs_steps += 3 * u.size
+        done += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    el = time.perf_counter() - t0
+    return {"value": dofs_steps / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"the {done} smallest ensemble cases, 2 SSP-RK3 steps each, {el:.1f} s, "
+                      f"oracle (plain C restatement, OpenMP)"}
+
+
+def run_ensemble(args, rank, world, local_rank):
+    import torch
+    from pvcriemannsolvers_gb300 import Ensemble, build
+    build.build()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    specs = ensemble_spec(scale=args.ensemble_scale)
+    members = build_ensemble(specs, device=local_rank)
+    ens = Ensemble([mb["system"] for mb in members])
+    stream = torch.cuda.Stream(device=dev)
+    ens.set_stream(stream.cuda_stream)
+    L = sum(mb["dofs"] for mb in members)
+    ens.advance(args.warmup, 1e9, 3)
+    torch.cuda.synchronize(dev)
+    launches0 = sum(mb["system"].launch_count() for mb in members)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clocks:
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            ens.advance(args.steps, 1e9, 3)
+            e1.record(stream)
+        e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = sum(mb["system"].launch_count() for mb in members) - launches0
+    # end to end: every member's column from / to pinned host memory each step
+    hosts = []
+    for mb in members:
+        n = mb["dofs"]
+        hin = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+        hout = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+        hin[:] = mb["system"].GetSolutionColumn()
+        hosts.append((hin, hout))
+    e2e_steps = max(1, min(args.steps, 10))
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for mb, (hin, _) in zip(members, hosts):
+            mb["system"].SetSolutionColumn(hin)
+        ens.advance(1, 1e9, 3)
+        for mb, (_, hout) in zip(members, hosts):
+            mb["system"].get_solution_into(hout)
+    torch.cuda.synchronize(dev)
+    e2e_s = time.perf_counter() - t0
+    per_member = []
+    for mb in members:
+        kt = mb["system"].kernel_times(reps=3)
+        t_cases, _ = mb["system"].case_times()
+        per_member.append({"scheme": mb["scheme"], "p": mb["p"], "cases": mb["cases"], "cells": mb["cells"],
+                           "dofs": mb["dofs"], "kernel_ms": kt, "case_t_min": float(t_cases.min()),
+                           "case_t_max": float(t_cases.max())})
+    ens.close()
+    for mb in members:
+        mb["system"].close()
+    fp64_peak = fp64_peak_tflops(torch, dev)
+    hbm_peak, peak_src = measured_peaks()
+    dom = max(per_member, key=lambda r: r["kernel_ms"]["rk3_step"])
+    cpu = None
+    if not args.no_cpu:
+        cpu = ensemble_cpu_sample(specs)
+    line = {
+        "metric": METRIC, "value": 3 * L * args.steps / (ms * 1e-3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"ensemble of {len(specs)} periodic unit-cube cases (seed 1), counts log-uniform "
+                               f"in [4k, 200k] x {args.ensemble_scale}, Hex8 DGSEM / Hex8 modal / Tet4 modal, "
+                               f"p in 1..3, Rusanov, SSP-RK3, own dt per case",
+                   "cases": len(specs), "cells": sum(mb["cells"] for mb in members), "dofs": L,
+                   "handles": len(members), "form": "plain FP64",
+                   "step": "one CUDA graph per step: every handle's dt reduction + 3 RK stages",
+                   "l2_flush": f"inputs larger than L2 (all columns {8 * L / 1e9:.2f} GB)"},
+        "clocks": clocks.summary(),
+        "e2e": {"value": 3 * L * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * L,
+                "d2h_bytes_per_step": 8 * L, "steps": e2e_steps,
+                "path": "mcfd_set_solution per handle + mcfd_ensemble_advance(1) + mcfd_get_solution per handle"},
+        "gpu_launches": launches,
+        "members": per_member,
+        "roofline": {"bound": "fp64", "kernel": f"step of the {dom['scheme']} p={dom['p']} handle",
+                     "achieved": None, "peak": fp64_peak, "unit": "TFLOP/s", "frac": None,
+                     "traffic": None, "peak_source": "measured in this run: cuBLAS DGEMM 4096^3",
+                     "hbm_peak": hbm_peak, "hbm_peak_source": peak_src,
+                     "note": "per-kernel rooflines of these kernels: the vortex and mixed-box lines"},
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_gpu(args, rank, world, local_rank):
     import torch
     from pvcriemannsolvers_gb300 import build, cases, mesh as meshlib
@@ -517,8 +713,11 @@ def main():
     ap.add_argument("--cells", type=int, default=N_CELLS_1D, help="cells per direction (profiling runs a smaller case)")
     ap.add_argument("--form", default="both", choices=["both", "fp64", "mixed"],
                     help="precision form(s) to time; the line's value is the mixed form when timed")
-    ap.add_argument("--workload", default="vortex", choices=["vortex", "mixed_box"],
-                    help="vortex: the headline DGSEM case; mixed_box: modal DG on hex + tet blocks")
+    ap.add_argument("--workload", default="vortex", choices=["vortex", "mixed_box", "ensemble"],
+                    help="vortex: the headline DGSEM case; mixed_box: modal DG on hex + tet blocks; "
+                         "ensemble: 64 independent cases in one graph per step")
+    ap.add_argument("--ensemble-scale", type=float, default=1.0,
+                    help="scale of the ensemble's element counts (profiling runs a smaller case)")
     ap.add_argument("--mixed-cells", type=int, nargs=2, default=[MIXED_HEX_1D, MIXED_TET_1D],
                     metavar=("HEX_1D", "TET_1D"), help="block sizes of the mixed box")
     args = ap.parse_args()
@@ -532,6 +731,9 @@ def main():
         return
     if args.workload == "mixed_box":
         run_mixed_box(args, rank, world, local_rank)
+        return
+    if args.workload == "ensemble":
+        run_ensemble(args, rank, world, local_rank)
         return
     if world > 1:
         import torch

@@ -308,6 +308,9 @@ typedef struct mcfd_ensemble mcfd_ensemble;
 int mcfd_ensemble_create(mcfd_handle *const *handles, int32_t n, mcfd_ensemble **out);
 int mcfd_ensemble_advance(mcfd_ensemble *e, int32_t n_steps, double dt_guess, int32_t rk_order);
 int mcfd_ensemble_destroy(mcfd_ensemble *e);
+/* Replays go to the caller's stream from now on (the ensemble's own stream is
+ * released); the caller keeps ownership of the stream. */
+int mcfd_ensemble_set_stream(mcfd_ensemble *e, void *cuda_stream);
 const char *mcfd_ensemble_last_error(const mcfd_ensemble *e);
 
 /* Message describing the last failure on this handle (or of mcfd_create when

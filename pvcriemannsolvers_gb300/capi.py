@@ -103,6 +103,7 @@ SIGNATURES = {
     "mcfd_ensemble_create": (C.c_int, [C.POINTER(_P), C.c_int32, C.POINTER(_P)]),
     "mcfd_ensemble_advance": (C.c_int, [_P, C.c_int32, C.c_double, C.c_int32]),
     "mcfd_ensemble_destroy": (C.c_int, [_P]),
+    "mcfd_ensemble_set_stream": (C.c_int, [_P, _P]),
     "mcfd_ensemble_last_error": (C.c_char_p, [_P]),
     "mcfd_point_count": (C.c_int64, [_P]),
     "mcfd_points": (C.c_int, [_P, _D, C.c_int64]),

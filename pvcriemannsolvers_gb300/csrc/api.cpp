@@ -955,6 +955,7 @@ struct mcfd_ensemble {
   std::vector<mcfd_handle *> members;
   int device = 0;
   cudaStream_t stream = nullptr;
+  bool own_stream = true;
   cudaEvent_t fork = nullptr;
   std::vector<cudaEvent_t> join;
   cudaGraphExec_t graph = nullptr;
@@ -975,7 +976,7 @@ void ens_release(mcfd_ensemble *e) {
   for (cudaEvent_t ev : e->join)
     if (ev) cudaEventDestroy(ev);
   if (e->fork) cudaEventDestroy(e->fork);
-  if (e->stream) cudaStreamDestroy(e->stream);
+  if (e->stream && e->own_stream) cudaStreamDestroy(e->stream);
 }
 
 }  // namespace
@@ -1019,6 +1020,17 @@ int mcfd_ensemble_destroy(mcfd_ensemble *e) {
   if (e->stream) cudaStreamSynchronize(e->stream);
   ens_release(e);
   delete e;
+  return MCFD_OK;
+}
+
+int mcfd_ensemble_set_stream(mcfd_ensemble *e, void *cuda_stream) {
+  if (!e || !cuda_stream) return MCFD_ERR_ARGUMENT;
+  cudaSetDevice(e->device);
+  cudaError_t err = cudaStreamSynchronize(e->stream);
+  if (err != cudaSuccess) return ens_fail(e, MCFD_ERR_CUDA, cudaGetErrorString(err));
+  cudaStreamDestroy(e->stream);
+  e->stream = (cudaStream_t)cuda_stream;
+  e->own_stream = false;
   return MCFD_OK;
 }
 

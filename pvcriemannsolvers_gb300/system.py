@@ -331,6 +331,12 @@ class Ensemble:
             msg = self._lib.mcfd_ensemble_last_error(self._e)
             raise capi.McfdError(code, msg.decode() if msg else "")
 
+    def set_stream(self, stream_ptr: int) -> None:
+        code = self._lib.mcfd_ensemble_set_stream(self._e, C.c_void_p(stream_ptr))
+        if code != capi.OK:
+            msg = self._lib.mcfd_ensemble_last_error(self._e)
+            raise capi.McfdError(code, msg.decode() if msg else "")
+
     def close(self) -> None:
         if getattr(self, "_e", None):
             self._lib.mcfd_ensemble_destroy(self._e)
