@@ -30,11 +30,15 @@
 namespace mcfd {
 namespace {
 
-// Threads per block of the cell kernel: its shared Taylor coefficients take
-// K M doubles per thread (at most 25.6 KB per block).
+// Cell-kernel storage: the Taylor coefficients sit in shared memory, one
+// column of a [K M][block] array per thread (conflict-free, at most 25.6 KB
+// per block); the K x M residual accumulators stay in registers.  At M = 20
+// part of them spills to L1, which measured faster (25 ms against 40 ms per
+// launch on the ensemble's p = 3 handle) than keeping them in shared memory.
 template <int M>
 struct ModalCfg {
   static constexpr int kBlock = M == 20 ? 32 : 64;
+  static constexpr int kSmemBytes = kK * M * kBlock * 8;
 };
 
 // Taylor monomials at offset (x, y, z) in the reference's order
@@ -57,33 +61,34 @@ __device__ __forceinline__ void taylor_values(double x, double y, double z, doub
 
 // rt[j] += gx dT_j/dx + gy dT_j/dy + gz dT_j/dz at offset (x, y, z), t the
 // monomial values there (basis/taylor.hpp:387-472).
-template <int M>
+// `rt(j)` yields the accumulator of monomial j (registers or shared memory).
+template <int M, class R>
 __device__ __forceinline__ void add_gradient(const double *t, double gx, double gy,
-                                             double gz, double *rt) {
-  rt[1] += gx;
-  rt[2] += gy;
-  rt[3] += gz;
+                                             double gz, R &&rt) {
+  rt(1) += gx;
+  rt(2) += gy;
+  rt(3) += gz;
   if constexpr (M >= 10) {
     const double x = t[1], y = t[2], z = t[3];
-    rt[4] += gx * (2 * x);
-    rt[5] += gx * y + gy * x;
-    rt[6] += gx * z + gz * x;
-    rt[7] += gy * (2 * y);
-    rt[8] += gy * z + gz * y;
-    rt[9] += gz * (2 * z);
+    rt(4) += gx * (2 * x);
+    rt(5) += gx * y + gy * x;
+    rt(6) += gx * z + gz * x;
+    rt(7) += gy * (2 * y);
+    rt(8) += gy * z + gz * y;
+    rt(9) += gz * (2 * z);
   }
   if constexpr (M >= 20) {
     const double xx = t[4], xy = t[5], xz = t[6], yy = t[7], yz = t[8], zz = t[9];
-    rt[10] += gx * (3 * xx);
-    rt[11] += gx * (2 * xy) + gy * xx;
-    rt[12] += gx * (2 * xz) + gz * xx;
-    rt[13] += gx * yy + gy * (2 * xy);
-    rt[14] += gx * yz + gy * xz + gz * xy;
-    rt[15] += gx * zz + gz * (2 * xz);
-    rt[16] += gy * (3 * yy);
-    rt[17] += gy * (2 * yz) + gz * yy;
-    rt[18] += gy * zz + gz * (2 * yz);
-    rt[19] += gz * (3 * zz);
+    rt(10) += gx * (3 * xx);
+    rt(11) += gx * (2 * xy) + gy * xx;
+    rt(12) += gx * (2 * xz) + gz * xx;
+    rt(13) += gx * yy + gy * (2 * xy);
+    rt(14) += gx * yz + gy * xz + gz * xy;
+    rt(15) += gx * zz + gz * (2 * xz);
+    rt(16) += gy * (3 * yy);
+    rt(17) += gy * (2 * yz) + gz * yy;
+    rt(18) += gy * zz + gz * (2 * yz);
+    rt(19) += gz * (3 * zz);
   }
 }
 
@@ -206,21 +211,20 @@ struct ModalCellArgs {
 template <int M, int STAGE>
 __global__ void __launch_bounds__(ModalCfg<M>::kBlock) modal_cell_kernel(ModalCellArgs a) {
   constexpr int KM = kK * M, NS = M * (M + 1) / 2, kCellBlock = ModalCfg<M>::kBlock;
-  // thread-private Taylor coefficients, column per thread (conflict-free)
-  __shared__ double s_a[KM][kCellBlock];
+  extern __shared__ double s_dyn[];  // [KM][block] Taylor coefficients
   const int tid = threadIdx.x;
   const int64_t c = (int64_t)blockIdx.x * kCellBlock + tid;
   if (c >= a.n_cells) return;
-  {
-    const double *ac = a.taylor + c * KM;
-#pragma unroll
-    for (int i = 0; i < KM; ++i) s_a[i][tid] = ac[i];
-  }
+  const double *ac = a.taylor + c * KM;
   double rt[kK][M];
+  auto coef = [&](int i) -> double { return s_dyn[i * kCellBlock + tid]; };
+  auto RT = [&](int k, int j) -> double & { return rt[k][j]; };
+#pragma unroll
+  for (int i = 0; i < KM; ++i) s_dyn[i * kCellBlock + tid] = ac[i];
 #pragma unroll
   for (int k = 0; k < kK; ++k)
 #pragma unroll
-    for (int j = 0; j < M; ++j) rt[k][j] = 0;
+    for (int j = 0; j < M; ++j) RT(k, j) = 0;
   // volume: sum_q w F(u_q) . grad T(x_q)
   const int q0 = a.vol_off[c], q1 = a.vol_off[c + 1];
   for (int q = q0; q < q1; ++q) {
@@ -231,7 +235,7 @@ __global__ void __launch_bounds__(ModalCfg<M>::kBlock) modal_cell_kernel(ModalCe
     for (int k = 0; k < kK; ++k) {
       double s = 0;
 #pragma unroll
-      for (int j = 0; j < M; ++j) s += s_a[j * kK + k][tid] * t[j];
+      for (int j = 0; j < M; ++j) s += coef(j * kK + k) * t[j];
       u[k] = s;
     }
     // GetFluxMatrix (types.hpp:322-333); mass row = momentum, which for a
@@ -250,7 +254,8 @@ __global__ void __launch_bounds__(ModalCfg<M>::kBlock) modal_cell_kernel(ModalCe
     }
 #pragma unroll
     for (int k = 0; k < kK; ++k)
-      add_gradient<M>(t, f[k][0] * g.w, f[k][1] * g.w, f[k][2] * g.w, rt[k]);
+      add_gradient<M>(t, f[k][0] * g.w, f[k][1] * g.w, f[k][2] * g.w,
+                      [&](int j) -> double & { return RT(k, j); });
   }
   // faces: holder -= w F^ T(x - centre), sharer += w F^ T(x - shift - centre)
   const double4 ctr = a.center[c];
@@ -271,7 +276,7 @@ __global__ void __launch_bounds__(ModalCfg<M>::kBlock) modal_cell_kernel(ModalCe
       for (int k = 0; k < kK; ++k) {
         const double v = sharer ? fl[k] : -fl[k];
 #pragma unroll
-        for (int j = 0; j < M; ++j) rt[k][j] += v * t[j];
+        for (int j = 0; j < M; ++j) RT(k, j) += v * t[j];
       }
     }
   }
@@ -291,7 +296,7 @@ __global__ void __launch_bounds__(ModalCfg<M>::kBlock) modal_cell_kernel(ModalCe
     for (int k = 0; k < kK; ++k) {
       double r = 0;
 #pragma unroll
-      for (int j = 0; j <= m; ++j) r += srow[j] * rt[k][j];
+      for (int j = 0; j <= m; ++j) r += srow[j] * RT(k, j);
       double v;
       if (STAGE == kStageResidual) {
         v = r;
@@ -315,13 +320,41 @@ __global__ void __launch_bounds__(ModalCfg<M>::kBlock) modal_cell_kernel(ModalCe
   if (a.advance_time && !a.cs.dt && c == 0) a.state->t += a.state->dt;
 }
 
+// max of `rate` into the handle's word, or into each cell's case word (cases
+// are contiguous cell runs, so warps are almost always uniform)
+__device__ __forceinline__ void reduce_cell_rate(double rate, int64_t c, int64_t n_cells,
+                                                 DevState *state, const int32_t *cell_case,
+                                                 unsigned long long *case_rate) {
+  if (case_rate) {
+    const int key = c < n_cells ? cell_case[c] : -1;
+    const int key0 = __shfl_sync(0xffffffffu, key, 0);
+    if (__all_sync(0xffffffffu, key == key0)) {
+      for (int o = 16; o > 0; o >>= 1) rate = fmax(rate, __shfl_xor_sync(0xffffffffu, rate, o));
+      if ((threadIdx.x & 31) == 0 && key0 >= 0 && rate > 0)
+        atomicMax(&case_rate[key0], (unsigned long long)__double_as_longlong(rate));
+    } else if (key >= 0 && rate > 0) {
+      atomicMax(&case_rate[key], (unsigned long long)__double_as_longlong(rate));
+    }
+    return;
+  }
+  for (int o = 16; o > 0; o >>= 1) rate = fmax(rate, __shfl_xor_sync(0xffffffffu, rate, o));
+  if ((threadIdx.x & 31) == 0 && rate > 0)
+    atomicMax(&state->max_rate_bits, (unsigned long long)__double_as_longlong(rate));
+}
+
+__device__ __forceinline__ double point_speed(const double *v) {
+  const Prim w = cons_to_prim(v[0], v[1], v[2], v[3], v[4]);
+  return sound_speed(w) + sqrt(w.u * w.u + w.v * w.v + w.w * w.w);
+}
+
 // max over the first M quadrature points of (|u| + c) / length, per cell
-// (fem.hpp:417-435 with Projection::GetValue(i), projection.hpp:109-118)
+// (fem.hpp:417-435 with Projection::GetValue(i), projection.hpp:109-118):
+// the value as the reference forms it, c . (S T(x_i - centre))
 template <int M>
 __global__ void __launch_bounds__(256)
-modal_dt_kernel(const double *u, const double *s, const double4 *center,
-                const int32_t *vol_off, const double4 *vol, int64_t n_cells,
-                DevState *state, const int32_t *cell_case, unsigned long long *case_rate) {
+modal_dt_basis_kernel(const double *u, const double *s, const double4 *center,
+                      const int32_t *vol_off, const double4 *vol, int64_t n_cells,
+                      DevState *state, const int32_t *cell_case, unsigned long long *case_rate) {
   constexpr int KM = kK * M, NS = M * (M + 1) / 2;
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double rate = 0;
@@ -348,29 +381,37 @@ modal_dt_kernel(const double *u, const double *s, const double4 *center,
         for (int m = 0; m < M; ++m) acc += uc[m * kK + k] * psi[m];
         v[k] = acc;
       }
-      const Prim w = cons_to_prim(v[0], v[1], v[2], v[3], v[4]);
-      const double speed = sound_speed(w) + sqrt(w.u * w.u + w.v * w.v + w.w * w.w);
-      max_speed = fmax(max_speed, speed);
+      max_speed = fmax(max_speed, point_speed(v));
     }
     rate = max_speed * center[c].w;
   }
-  // max into the handle's word, or into each cell's case word (cases are
-  // contiguous cell runs, so warps are almost always uniform)
-  if (case_rate) {
-    const int key = c < n_cells ? cell_case[c] : -1;
-    const int key0 = __shfl_sync(0xffffffffu, key, 0);
-    if (__all_sync(0xffffffffu, key == key0)) {
-      for (int o = 16; o > 0; o >>= 1) rate = fmax(rate, __shfl_xor_sync(0xffffffffu, rate, o));
-      if ((threadIdx.x & 31) == 0 && key0 >= 0 && rate > 0)
-        atomicMax(&case_rate[key0], (unsigned long long)__double_as_longlong(rate));
-    } else if (key >= 0 && rate > 0) {
-      atomicMax(&case_rate[key], (unsigned long long)__double_as_longlong(rate));
+  reduce_cell_rate(rate, c, n_cells, state, cell_case, case_rate);
+}
+
+// The same maximum from the Taylor coefficients a = S^T c of the input:
+// u(x_i) = a . T(x_i - centre), reassociated (rounding-level difference).
+template <int M>
+__global__ void __launch_bounds__(256)
+modal_dt_kernel(const double *taylor, const double4 *center,
+                const int32_t *vol_off, const double4 *vol, int64_t n_cells,
+                DevState *state, const int32_t *cell_case, unsigned long long *case_rate) {
+  constexpr int KM = kK * M;
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double rate = 0;
+  if (c < n_cells) {
+    const double *ac = taylor + c * KM;
+    double max_speed = 1e-5;
+    const int q0 = vol_off[c];
+    for (int i = 0; i < M; ++i) {
+      const double4 g = vol[q0 + i];
+      double t[M], v[kK];
+      taylor_values<M>(g.x, g.y, g.z, t);
+      eval_taylor<M>(ac, t, v);
+      max_speed = fmax(max_speed, point_speed(v));
     }
-    return;
+    rate = max_speed * center[c].w;
   }
-  for (int o = 16; o > 0; o >>= 1) rate = fmax(rate, __shfl_xor_sync(0xffffffffu, rate, o));
-  if ((threadIdx.x & 31) == 0 && rate > 0)
-    atomicMax(&state->max_rate_bits, (unsigned long long)__double_as_longlong(rate));
+  reduce_cell_rate(rate, c, n_cells, state, cell_case, case_rate);
 }
 
 // Projection::Approximate (projection.hpp:28-42): coeff = sum_q (f_q psi(x_q)) w_q
@@ -422,9 +463,10 @@ void modal_face_dispatch(mcfd_handle *h, const ModalFaceArgs &fa) {
 
 template <int M, int S>
 void modal_cell_launch(mcfd_handle *h, const ModalCellArgs &ca) {
-  constexpr int B = ModalCfg<M>::kBlock;
+  constexpr int B = ModalCfg<M>::kBlock, SMEM = ModalCfg<M>::kSmemBytes;
+  static_assert(SMEM <= 48 * 1024, "cell kernel shared memory above the default limit");
   const int64_t blocks = (ca.n_cells + B - 1) / B;
-  modal_cell_kernel<M, S><<<(unsigned)blocks, B, 0, h->stream>>>(ca);
+  modal_cell_kernel<M, S><<<(unsigned)blocks, B, SMEM, h->stream>>>(ca);
 }
 
 template <int M>
@@ -481,10 +523,15 @@ int launch_modal_dt(mcfd_handle *h, const double *u) {
   const unsigned blocks = (unsigned)((C + 255) / 256);
   const int32_t *cc = h->cases.cell_case;
   unsigned long long *cr = h->cases.n ? h->cases.rate : nullptr;
+  // values at the first M quadrature points: c . psi(x_i) up to M = 10; at
+  // M = 20 through the Taylor coefficients (3050 instead of 6200 FMAs per cell)
   switch (md.m) {
-    case 4: modal_dt_kernel<4><<<blocks, 256, 0, h->stream>>>(u, md.s, md.center, md.vol_off, md.vol, C, h->buf.state, cc, cr); break;
-    case 10: modal_dt_kernel<10><<<blocks, 256, 0, h->stream>>>(u, md.s, md.center, md.vol_off, md.vol, C, h->buf.state, cc, cr); break;
-    default: modal_dt_kernel<20><<<blocks, 256, 0, h->stream>>>(u, md.s, md.center, md.vol_off, md.vol, C, h->buf.state, cc, cr); break;
+    case 4: modal_dt_basis_kernel<4><<<blocks, 256, 0, h->stream>>>(u, md.s, md.center, md.vol_off, md.vol, C, h->buf.state, cc, cr); break;
+    case 10: modal_dt_basis_kernel<10><<<blocks, 256, 0, h->stream>>>(u, md.s, md.center, md.vol_off, md.vol, C, h->buf.state, cc, cr); break;
+    default:
+      taylor_launch<20>(h, u);
+      modal_dt_kernel<20><<<blocks, 256, 0, h->stream>>>(md.taylor, md.center, md.vol_off, md.vol, C, h->buf.state, cc, cr);
+      return 2 + launch_dt_finalize(h);
   }
   return 1 + launch_dt_finalize(h);
 }
