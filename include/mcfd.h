@@ -159,7 +159,11 @@ enum mcfd_precision { MCFD_FP64 = 0, MCFD_MIXED = 1 };
 enum mcfd_limiter {
   MCFD_LIMITER_NONE = 0,
   MCFD_LIMITER_LAZY = 1,
-  MCFD_LIMITER_DETECT_LAZY = 2
+  MCFD_LIMITER_DETECT_LAZY = 2,
+  MCFD_LIMITER_EIGEN = 3   /* weno::Eigen: the jump detector, then the
+                              characteristic-wise reconstruction in each
+                              adjacent face's frame, averaged with the
+                              neighbours' volumes (limiter/weno.hpp:259-348) */
 };
 
 typedef struct mcfd_options {

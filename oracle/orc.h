@@ -130,7 +130,15 @@ int orc_rk_update_linear(int order, int64_t n, const double *a, double t,
                          double dt, double *u);
 
 /* ---- WENO limiter on DGSEM cells (orc_weno.c) ---- */
-enum { ORC_LIMITER_NONE = 0, ORC_LIMITER_LAZY = 1, ORC_LIMITER_DETECT_LAZY = 2 };
+/* LAZY: weno::Lazy on every cell; DETECT_LAZY: Lazy reconstruction of the
+ * cells the weno::Eigen jump detector flags; EIGEN: weno::Eigen (jump
+ * detector + characteristic-wise reconstruction, limiter/weno.hpp:196-348). */
+enum { ORC_LIMITER_NONE = 0, ORC_LIMITER_LAZY = 1, ORC_LIMITER_DETECT_LAZY = 2, ORC_LIMITER_EIGEN = 3,
+       /* tests only: the characteristic reconstruction on every cell */
+       ORC_LIMITER_EIGEN_ALL = 4 };
+/* EigenMatrices (riemann/euler/eigen.hpp:27-56) of a conservative state in
+ * the frame {nu, mu, pi} (rows of frame9); L, R row-major 5x5. */
+void orc_eigen_matrices(const double *cons, const double *frame9, double *L, double *R);
 typedef struct orc_limiter orc_limiter;
 orc_limiter *orc_limiter_create(const orc_mesh *m);
 void orc_limiter_destroy(orc_limiter *l);

@@ -240,7 +240,20 @@ def rk_update_linear(order: int, a: np.ndarray, t: float, dt: float, u: np.ndarr
     return u
 
 
-LIMITER_NONE, LIMITER_LAZY, LIMITER_DETECT_LAZY = 0, 1, 2
+LIMITER_NONE, LIMITER_LAZY, LIMITER_DETECT_LAZY, LIMITER_EIGEN, LIMITER_EIGEN_ALL = 0, 1, 2, 3, 4
+
+
+def eigen_matrices(cons, frame):
+    """EigenMatrices (riemann/euler/eigen.hpp:27-56): L, R of a conservative
+    state in the frame rows (normal, tangent, bitangent)."""
+    lib = load()
+    lib.orc_eigen_matrices.restype = None
+    lib.orc_eigen_matrices.argtypes = [_D, _D, _D, _D]
+    cons = np.ascontiguousarray(cons, dtype=np.float64)
+    frame = np.ascontiguousarray(frame, dtype=np.float64)
+    L, R = np.empty((5, 5)), np.empty((5, 5))
+    lib.orc_eigen_matrices(_p(cons), _p(frame), _p(L), _p(R))
+    return L, R
 
 
 def _limiter_sigs(lib):

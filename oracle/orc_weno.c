@@ -14,6 +14,9 @@
  *   smoothness beta: limiter/weno.hpp:25-95
  *   Lazy reconstruct: limiter/weno.hpp:97-195
  *   Eigen (jump) detector: limiter/weno.hpp:230-258
+ *   Eigen characteristic-wise reconstruction: limiter/weno.hpp:259-348,
+ *       EigenMatrices riemann/euler/eigen.hpp:27-56 in the frame of the
+ *       face's first quadrature point (rotated/euler.hpp:330-338)
  *   detect all, reconstruct all, then write back: limiter/reconstruct.hpp:21-54
  */
 #include <math.h>
@@ -136,6 +139,8 @@ struct orc_limiter {
   double *adj_shift; /* [cells][6][3]: a point x of this cell is x - shift in
                         the neighbour's frame (periodic faces; the reference
                         has none, so its shift is always zero) */
+  double *adj_frame; /* [cells][6][9]: normal frame of the shared face at its
+                        first quadrature point (holder -> sharer) */
 };
 
 orc_limiter *orc_limiter_create(const orc_mesh *mesh) {
@@ -153,6 +158,10 @@ orc_limiter *orc_limiter_create(const orc_mesh *mesh) {
   l->adj = (int *)malloc(sizeof(int) * C * 6);
   l->n_adj = (int *)calloc(C, sizeof(int));
   l->adj_shift = (double *)calloc(C * 6 * 3, sizeof(double));
+  l->adj_frame = (double *)calloc(C * 6 * 9, sizeof(double));
+  const int QF = (p + 1) * (p + 1);
+  double *frames = (double *)malloc(sizeof(double) * (orc_mesh_faces(mesh) * QF * 9 + 1));
+  orc_face_geometry(mesh, NULL, NULL, frames);
   orc_node_geometry(mesh, l->xyz, l->w);
   orc_cell_centers(mesh, l->center);
   /* adjacency in face order (part.hpp:957-960 appends per local face) */
@@ -164,13 +173,16 @@ orc_limiter *orc_limiter_create(const orc_mesh *mesh) {
     if (s < 0) continue;
     if (l->n_adj[h] < 6) {
       for (int e = 0; e < 3; ++e) l->adj_shift[(h * 6 + l->n_adj[h]) * 3 + e] = fs[f * 3 + e];
+      memcpy(&l->adj_frame[(h * 6 + l->n_adj[h]) * 9], &frames[f * QF * 9], sizeof(double) * 9);
       l->adj[h * 6 + l->n_adj[h]++] = (int)s;
     }
     if (l->n_adj[s] < 6) {
       for (int e = 0; e < 3; ++e) l->adj_shift[(s * 6 + l->n_adj[s]) * 3 + e] = -fs[f * 3 + e];
+      memcpy(&l->adj_frame[(s * 6 + l->n_adj[s]) * 9], &frames[f * QF * 9], sizeof(double) * 9);
       l->adj[s * 6 + l->n_adj[s]++] = (int)h;
     }
   }
+  free(frames);
 #pragma omp parallel for schedule(static) num_threads(orc_get_threads())
   for (int64_t c = 0; c < C; ++c) {
     double T[64 * 20];
@@ -198,7 +210,7 @@ orc_limiter *orc_limiter_create(const orc_mesh *mesh) {
 void orc_limiter_destroy(orc_limiter *l) {
   if (!l) return;
   free(l->center); free(l->s); free(l->psi); free(l->w); free(l->xyz);
-  free(l->volume); free(l->adj); free(l->n_adj); free(l->adj_shift);
+  free(l->volume); free(l->adj); free(l->n_adj); free(l->adj_shift); free(l->adj_frame);
   free(l);
 }
 
@@ -374,6 +386,123 @@ static void lazy_reconstruct(const orc_limiter *l, int64_t c,
       for (int m = 0; m < M; ++m) out[k * M + m] += cand[i][k * M + m] * weights[i][k];
 }
 
+void orc_eigen_matrices(const double *cons, const double *frame9, double *L, double *R) {
+  double prim[K];
+  orc_cons_to_prim(cons, prim);
+  const double *nu = &frame9[0], *mu = &frame9[3], *pi = &frame9[6];
+  const double gamma = 1.4;
+  double u_x = prim[1], u_y = prim[2], u_z = prim[3];
+  double u_nu = (u_x * nu[0] + u_y * nu[1] + u_z * nu[2]);
+  double u_mu = (u_x * mu[0] + u_y * mu[1] + u_z * mu[2]);
+  double u_pi = (u_x * pi[0] + u_y * pi[1] + u_z * pi[2]);
+  double a = sqrt(gamma * prim[4] / prim[0]);
+  double ek = (u_x * u_x + u_y * u_y + u_z * u_z) / 2;
+  double e0 = a * a * (1 / (gamma - 1));
+  double h0 = e0 + ek;
+  const double Rc[5][5] = {
+      {1, u_x - a * nu[0], u_y - a * nu[1], u_z - a * nu[2], h0 - a * u_nu},
+      {1, u_x, u_y, u_z, ek},
+      {0, mu[0], mu[1], mu[2], u_mu},
+      {0, pi[0], pi[1], pi[2], u_pi},
+      {1, u_x + a * nu[0], u_y + a * nu[1], u_z + a * nu[2], h0 + a * u_nu}};
+  double b1 = 1 / e0, b2 = b1 * ek;
+  const double Lc[5][5] = {
+      {(b2 + u_nu / a) / 2, 1 - b2, -u_mu, -u_pi, (b2 - u_nu / a) / 2},
+      {-(b1 * u_x + nu[0] / a) / 2, b1 * u_x, mu[0], pi[0], -(b1 * u_x - nu[0] / a) / 2},
+      {-(b1 * u_y + nu[1] / a) / 2, b1 * u_y, mu[1], pi[1], -(b1 * u_y - nu[1] / a) / 2},
+      {-(b1 * u_z + nu[2] / a) / 2, b1 * u_z, mu[2], pi[2], -(b1 * u_z - nu[2] / a) / 2},
+      {b1 / 2, -b1, 0, 0, b1 / 2}};
+  /* the reference fills columns: X.col(j) << rows 0..4 */
+  for (int i = 0; i < 5; ++i)
+    for (int j = 0; j < 5; ++j) {
+      R[i * 5 + j] = Rc[j][i];
+      L[i * 5 + j] = Lc[j][i];
+    }
+}
+
+/* weno::Eigen::Reconstruct (weno.hpp:259-348) of cell c -> new modal coeff. */
+static void eigen_reconstruct(const orc_limiter *l, int64_t c,
+                              const double *modal, double w0, double eps,
+                              double *out) {
+  const int N = l->n, M = l->m;
+  const int n_adj = l->n_adj[c];
+  double cand[7][K * 20], rot[7][K * 20];
+  const double *own = &modal[c * K * M];
+  double s00 = l->s[c * M * M];
+  /* Borrow (weno.hpp:275-291), as in Lazy */
+  for (int a = 0; a < n_adj; ++a) {
+    int64_t b = l->adj[c * 6 + a];
+    const double *sh = &l->adj_shift[(c * 6 + a) * 3];
+    double *pj = cand[a];
+    memset(pj, 0, sizeof(double) * K * M);
+    for (int q = 0; q < N; ++q) {
+      double v[K], xq[3];
+      for (int e = 0; e < 3; ++e) xq[e] = l->xyz[(c * N + q) * 3 + e] - sh[e];
+      modal_value(l, b, &modal[b * K * M], xq, v);
+      double w = l->w[c * N + q];
+      for (int k = 0; k < K; ++k)
+        for (int m = 0; m < M; ++m) pj[k * M + m] += v[k] * l->psi[(c * N + q) * M + m] * w;
+    }
+    for (int k = 0; k < K; ++k) {
+      double my_avg = own[k * M] * s00;
+      double adj_avg = pj[k * M] * s00;
+      pj[k * M] += (my_avg - adj_avg) / s00;
+    }
+  }
+  memcpy(cand[n_adj], own, sizeof(double) * K * M);
+  double big_u[K];
+  for (int k = 0; k < K; ++k) big_u[k] = own[k * M] * s00;
+  double acc[K * 20];
+  memset(acc, 0, sizeof(acc));
+  double total_volume = 0.0;
+  /* ReconstructOnFace for every adjacent face (weno.hpp:297-336) */
+  for (int f = 0; f < n_adj; ++f) {
+    double L[25], R[25];
+    orc_eigen_matrices(big_u, &l->adj_frame[(c * 6 + f) * 9], L, R);
+    double weights[7][K], sum[K] = {0, 0, 0, 0, 0};
+    for (int i = 0; i <= n_adj; ++i)
+      for (int k = 0; k < K; ++k) weights[i][k] = w0;
+    for (int k = 0; k < K; ++k) {
+      weights[n_adj][k] *= -n_adj;
+      weights[n_adj][k] += 1.0;
+    }
+    for (int i = 0; i <= n_adj; ++i) {
+      for (int k = 0; k < K; ++k)
+        for (int m = 0; m < M; ++m) {
+          double s = 0;
+          for (int j = 0; j < K; ++j) s += L[k * 5 + j] * cand[i][j * M + m];
+          rot[i][k * M + m] = s;
+        }
+      double beta[K];
+      smoothness(l, c, rot[i], beta);
+      for (int k = 0; k < K; ++k) {
+        double b = beta[k] + eps;
+        b *= b;
+        weights[i][k] /= b;
+      }
+    }
+    for (int i = 0; i <= n_adj; ++i)
+      for (int k = 0; k < K; ++k) sum[k] += weights[i][k];
+    for (int i = 0; i <= n_adj; ++i)
+      for (int k = 0; k < K; ++k) weights[i][k] /= sum[k];
+    double nw[K * 20];
+    for (int k = 0; k < K; ++k)
+      for (int m = 0; m < M; ++m) nw[k * M + m] = rot[n_adj][k * M + m] * weights[n_adj][k];
+    for (int i = 0; i < n_adj; ++i)
+      for (int k = 0; k < K; ++k)
+        for (int m = 0; m < M; ++m) nw[k * M + m] += rot[i][k * M + m] * weights[i][k];
+    double adj_volume = l->volume[l->adj[c * 6 + f]];
+    for (int k = 0; k < K; ++k)
+      for (int m = 0; m < M; ++m) {
+        double s = 0;
+        for (int j = 0; j < K; ++j) s += R[k * 5 + j] * nw[j * M + m];
+        acc[k * M + m] += s * adj_volume;
+      }
+    total_volume += adj_volume;
+  }
+  for (int i = 0; i < K * M; ++i) out[i] = acc[i] / total_volume;
+}
+
 /* limiter::Reconstruct (reconstruct.hpp:21-54) in place on the nodal column.
  * mode: ORC_LIMITER_LAZY (every cell) or ORC_LIMITER_DETECT_LAZY (cells the
  * jump detector flags).  Returns the number of reconstructed cells. */
@@ -388,9 +517,13 @@ int64_t orc_limit(const orc_limiter *l, int mode, double w0, double eps,
   int64_t count = 0;
 #pragma omp parallel for schedule(dynamic, 16) reduction(+ : count) num_threads(orc_get_threads())
   for (int64_t c = 0; c < C; ++c) {
-    troubled[c] = mode == ORC_LIMITER_LAZY ? 1 : (char)is_not_smooth(l, c, modal);
+    troubled[c] = (mode == ORC_LIMITER_LAZY || mode == ORC_LIMITER_EIGEN_ALL)
+                      ? 1 : (char)is_not_smooth(l, c, modal);
     if (troubled[c]) {
-      lazy_reconstruct(l, c, modal, w0, eps, &fresh[c * K * M]);
+      if (mode == ORC_LIMITER_EIGEN || mode == ORC_LIMITER_EIGEN_ALL)
+        eigen_reconstruct(l, c, modal, w0, eps, &fresh[c * K * M]);
+      else
+        lazy_reconstruct(l, c, modal, w0, eps, &fresh[c * K * M]);
       ++count;
     }
   }

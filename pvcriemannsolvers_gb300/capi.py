@@ -109,7 +109,7 @@ SIGNATURES = {
     "mcfd_points": (C.c_int, [_P, _D, C.c_int64]),
     "mcfd_project": (C.c_int, [_P, _D, C.c_int64]),
 }
-LIMITER = {"none": 0, "lazy": 1, "detect_lazy": 2}
+LIMITER = {"none": 0, "lazy": 1, "detect_lazy": 2, "eigen": 3}
 
 _lib = None
 

@@ -156,7 +156,7 @@ void release(mcfd_handle *h) {
     if (p) cudaFree(p);
   auto &l = h->lim;
   void *lptrs[] = {l.psi, l.mn, l.proj, l.beta, l.eval, l.s00, l.divisor, l.adj,
-                   l.modal, l.troubled};
+                   l.frame, l.volume, l.modal, l.troubled};
   for (void *p : lptrs)
     if (p) cudaFree(p);
   auto &cs = h->cases;
@@ -509,6 +509,7 @@ int build_limiter(mcfd_handle *h, const mcfd_mesh_desc *d, int kind, double w0,
   // x - shift in the neighbour's frame)
   std::vector<int32_t> adj((size_t)C * 6, -1);
   std::vector<double> adj_shift((size_t)C * 6 * 3, 0.0);
+  std::vector<double> adj_frame((size_t)C * 6 * 9, 0.0);
   std::vector<int> n_adj(C, 0);
   for (int64_t f = 0; f < d->n_faces; ++f) {
     int64_t hc = d->face_cells[f * 2], sc = d->face_cells[f * 2 + 1];
@@ -516,12 +517,30 @@ int build_limiter(mcfd_handle *h, const mcfd_mesh_desc *d, int kind, double w0,
     double sh[3] = {0, 0, 0};
     if (d->face_shift)
       for (int e = 0; e < 3; ++e) sh[e] = d->face_shift[f * 3 + e];
+    // frame of the face at its first GLL point, local (-1, -1) on the
+    // holder's face (coordinate/face.hpp:54-62): normal, tangent, bitangent
+    double xn[12], x[3], ta[3], tb[3], fr[9];
+    const int side = d->face_sides[f * 2];
+    for (int v = 0; v < 4; ++v)
+      for (int e = 0; e < 3; ++e) xn[v * 3 + e] = d->xyz[d->cell_nodes[hc * 8 + kHexFace[side][v]] * 3 + e];
+    quad4_point(xn, -1.0, -1.0, x, ta, tb);
+    fr[0] = ta[1] * tb[2] - ta[2] * tb[1];
+    fr[1] = ta[2] * tb[0] - ta[0] * tb[2];
+    fr[2] = ta[0] * tb[1] - ta[1] * tb[0];
+    const double nn = std::sqrt(fr[0] * fr[0] + fr[1] * fr[1] + fr[2] * fr[2]);
+    const double tn = std::sqrt(ta[0] * ta[0] + ta[1] * ta[1] + ta[2] * ta[2]);
+    for (int e = 0; e < 3; ++e) { fr[e] /= nn; fr[3 + e] = ta[e] / tn; }
+    fr[6] = fr[1] * fr[5] - fr[2] * fr[4];
+    fr[7] = fr[2] * fr[3] - fr[0] * fr[5];
+    fr[8] = fr[0] * fr[4] - fr[1] * fr[3];
     if (n_adj[hc] < 6) {
       for (int e = 0; e < 3; ++e) adj_shift[((size_t)hc * 6 + n_adj[hc]) * 3 + e] = sh[e];
+      for (int e = 0; e < 9; ++e) adj_frame[((size_t)hc * 6 + n_adj[hc]) * 9 + e] = fr[e];
       adj[(size_t)hc * 6 + n_adj[hc]++] = (int32_t)sc;
     }
     if (n_adj[sc] < 6) {
       for (int e = 0; e < 3; ++e) adj_shift[((size_t)sc * 6 + n_adj[sc]) * 3 + e] = -sh[e];
+      for (int e = 0; e < 9; ++e) adj_frame[((size_t)sc * 6 + n_adj[sc]) * 9 + e] = fr[e];
       adj[(size_t)sc * 6 + n_adj[sc]++] = (int32_t)hc;
     }
   }
@@ -651,6 +670,8 @@ int build_limiter(mcfd_handle *h, const mcfd_mesh_desc *d, int kind, double w0,
   if ((rc = upload(h, &l.s00, s00))) return rc;
   if ((rc = upload(h, &l.divisor, divisor))) return rc;
   if ((rc = upload(h, &l.adj, adj))) return rc;
+  if ((rc = upload(h, &l.frame, adj_frame))) return rc;
+  if ((rc = upload(h, &l.volume, volume))) return rc;
   CUDA_TRY(h, cudaMalloc(&l.modal, sizeof(double) * C * mcfd::kK * M));
   CUDA_TRY(h, cudaMalloc(&l.troubled, sizeof(unsigned long long)));
   CUDA_TRY(h, cudaMemset(l.troubled, 0, sizeof(unsigned long long)));
@@ -710,7 +731,8 @@ int mcfd_create(const mcfd_mesh_desc *mesh, const mcfd_options *options,
     rc = options->scheme == MCFD_MODAL ? mcfd::build_modal_mesh(h, mesh, options->degree)
                                        : build_mesh(h, mesh, options->degree);
   if (!rc && options->limiter != MCFD_LIMITER_NONE) {
-    if (options->limiter != MCFD_LIMITER_LAZY && options->limiter != MCFD_LIMITER_DETECT_LAZY)
+    if (options->limiter != MCFD_LIMITER_LAZY && options->limiter != MCFD_LIMITER_DETECT_LAZY &&
+        options->limiter != MCFD_LIMITER_EIGEN)
       rc = fail(h, MCFD_ERR_ARGUMENT, "unknown limiter");
     else
       rc = build_limiter(h, mesh, options->limiter, options->weno_w0, options->weno_eps);

@@ -82,6 +82,9 @@ struct Limiter {
   double *s00 = nullptr;     // [cells] S(0,0) of the own basis
   double *divisor = nullptr; // [cells] volume^((p+1)/6) * n_adj (jump detector)
   int32_t *adj = nullptr;    // [cells][6] neighbour cells (-1 = none), face order
+  double *frame = nullptr;   // [cells][6][9] frame of the shared face at its first
+                             //   point: normal, tangent, bitangent (weno::Eigen)
+  double *volume = nullptr;  // [cells] cell volume (weno::Eigen face weights)
   double *modal = nullptr;   // [cells][K][M] scratch: modal coefficients
   unsigned long long *troubled = nullptr;  // counter of reconstructed cells
 };

@@ -18,6 +18,11 @@
 //                            squared partial derivatives; same quadratic form),
 //                            nonlinear weights, and the new nodal values
 //                            (UpdateNodalCoeff), written in place.
+// MODE 3 (weno::Eigen, limiter/weno.hpp:259-348) reconstructs characteristic-
+// wise instead: for every adjacent face the candidates are mapped by L of the
+// Euler eigen-system at the cell average in the face's frame (first quadrature
+// point, rotated/euler.hpp:330-338), weighted per characteristic field, mapped
+// back by R, and the face results are averaged with the neighbours' volumes.
 // Every cell reads the modal buffer only, so the in-place write is safe and
 // the pass is Jacobi-like, as in limiter::Reconstruct (all new projections
 // are computed before any is written back).
@@ -41,6 +46,8 @@ struct WenoArgs {
   const double *s00;
   const double *divisor;
   const int32_t *adj;
+  const double *frame;   // [cells][6][9] face frame at its first point (MODE 3)
+  const double *volume;  // [cells] (MODE 3)
   unsigned long long *troubled;
   int64_t n_cells;
   double w0, eps, smooth_ref;
@@ -63,6 +70,135 @@ weno_modal_kernel(const double *__restrict__ u, const double *__restrict__ mn,
   modal[gid] = s;
 }
 
+// EigenMatrices (riemann/euler/eigen.hpp:27-56) of the conservative state u
+// in the frame {nu, mu, pi}; L and R row-major.  One thread.
+__device__ void eigen_matrices(const double *u, const double *nu, const double *mu,
+                               const double *pi, double *L, double *R) {
+  const Prim w = cons_to_prim(u[0], u[1], u[2], u[3], u[4]);
+  const double ux = w.u, uy = w.v, uz = w.w;
+  const double u_nu = ux * nu[0] + uy * nu[1] + uz * nu[2];
+  const double u_mu = ux * mu[0] + uy * mu[1] + uz * mu[2];
+  const double u_pi = ux * pi[0] + uy * pi[1] + uz * pi[2];
+  const double a = sqrt(kGamma * w.p / w.rho);
+  const double ek = (ux * ux + uy * uy + uz * uz) / 2;
+  const double e0 = a * a * (1 / kGm1);
+  const double h0 = e0 + ek;
+  const double vel[3] = {ux, uy, uz};
+  // columns: u - a, u (entropy), two shear waves, u + a
+  R[0 * 5 + 0] = 1; R[0 * 5 + 1] = 1; R[0 * 5 + 2] = 0; R[0 * 5 + 3] = 0; R[0 * 5 + 4] = 1;
+  for (int d = 0; d < 3; ++d) {
+    R[(1 + d) * 5 + 0] = vel[d] - a * nu[d];
+    R[(1 + d) * 5 + 1] = vel[d];
+    R[(1 + d) * 5 + 2] = mu[d];
+    R[(1 + d) * 5 + 3] = pi[d];
+    R[(1 + d) * 5 + 4] = vel[d] + a * nu[d];
+  }
+  R[4 * 5 + 0] = h0 - a * u_nu; R[4 * 5 + 1] = ek; R[4 * 5 + 2] = u_mu; R[4 * 5 + 3] = u_pi;
+  R[4 * 5 + 4] = h0 + a * u_nu;
+  const double b1 = 1 / e0, b2 = b1 * ek;
+  L[0 * 5 + 0] = (b2 + u_nu / a) / 2;
+  L[1 * 5 + 0] = 1 - b2;
+  L[2 * 5 + 0] = -u_mu;
+  L[3 * 5 + 0] = -u_pi;
+  L[4 * 5 + 0] = (b2 - u_nu / a) / 2;
+  for (int d = 0; d < 3; ++d) {
+    L[0 * 5 + 1 + d] = -(b1 * vel[d] + nu[d] / a) / 2;
+    L[1 * 5 + 1 + d] = b1 * vel[d];
+    L[2 * 5 + 1 + d] = mu[d];
+    L[3 * 5 + 1 + d] = pi[d];
+    L[4 * 5 + 1 + d] = -(b1 * vel[d] - nu[d] / a) / 2;
+  }
+  L[0 * 5 + 4] = b1 / 2; L[1 * 5 + 4] = -b1; L[2 * 5 + 4] = 0; L[3 * 5 + 4] = 0;
+  L[4 * 5 + 4] = b1 / 2;
+}
+
+// weno::Eigen reconstruction of cell c from its candidates (slots 0..n_adj-1
+// neighbours, slot 6 own) into s_new; all 64 threads take part.
+template <int M, class Args>
+__device__ void eigen_reconstruct(const Args &a, int64_t c, int n_adj,
+                                  double (*s_cand)[kK][M], double (*s_beta)[kK],
+                                  double (*s_new)[M]) {
+  __shared__ double s_L[25], s_R[25];
+  __shared__ double s_rot[7][kK][M];
+  __shared__ double s_acc[kK][M];
+  __shared__ double s_total, s_vol;
+  const int t = threadIdx.x;
+  const double *B = a.beta + c * M * M;
+  for (int i = t; i < kK * M; i += blockDim.x) s_acc[i / M][i % M] = 0;
+  if (t == 0) s_total = 0;
+  __syncthreads();
+  for (int f = 0; f < n_adj; ++f) {
+    if (t == 0) {
+      const double s00 = a.s00[c];
+      double big_u[kK];
+      for (int k = 0; k < kK; ++k) big_u[k] = s_cand[6][k][0] * s00;
+      const double *fr = a.frame + (c * 6 + f) * 9;
+      eigen_matrices(big_u, fr, fr + 3, fr + 6, s_L, s_R);
+      s_vol = a.volume[a.adj[c * 6 + f]];
+    }
+    __syncthreads();
+    // L applied to every candidate (ProjectionWrapper::LeftMultiply)
+    for (int i = t; i < (n_adj + 1) * kK * M; i += blockDim.x) {
+      const int slot = i / (kK * M), r = i - slot * kK * M, k = r / M, m = r - k * M;
+      const int src = slot < n_adj ? slot : 6;
+      double v = 0;
+#pragma unroll
+      for (int j = 0; j < kK; ++j) v += s_L[k * 5 + j] * s_cand[src][j][m];
+      s_rot[src][k][m] = v;
+    }
+    __syncthreads();
+    if (t < 7 * kK) {
+      const int slot = t / kK, k = t - slot * kK;
+      if (slot == 6 || slot < n_adj) {
+        double b = 0;
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+          double row = 0;
+#pragma unroll
+          for (int j = 0; j < M; ++j) row += B[m * M + j] * s_rot[slot][k][j];
+          b += s_rot[slot][k][m] * row;
+        }
+        s_beta[slot][k] = b;
+      }
+    }
+    __syncthreads();
+    if (t < kK) {
+      const int k = t;
+      double w[7];
+      for (int s = 0; s < n_adj; ++s) w[s] = a.w0;
+      double ws = a.w0;
+      ws *= -n_adj;
+      ws += 1.0;
+      w[n_adj] = ws;
+      double sum = 0;
+      for (int s = 0; s <= n_adj; ++s) {
+        double b = (s < n_adj ? s_beta[s][k] : s_beta[6][k]) + a.eps;
+        b *= b;
+        w[s] /= b;
+      }
+      for (int s = 0; s <= n_adj; ++s) sum += w[s];
+      for (int s = 0; s <= n_adj; ++s) w[s] /= sum;
+      for (int m = 0; m < M; ++m) {
+        double v = s_rot[6][k][m] * w[n_adj];
+        for (int s = 0; s < n_adj; ++s) v += s_rot[s][k][m] * w[s];
+        s_new[k][m] = v;
+      }
+    }
+    __syncthreads();
+    // back to conservative variables, weighted by the neighbour's volume
+    for (int i = t; i < kK * M; i += blockDim.x) {
+      const int k = i / M, m = i - k * M;
+      double v = 0;
+#pragma unroll
+      for (int j = 0; j < kK; ++j) v += s_R[k * 5 + j] * s_new[j][m];
+      s_acc[k][m] += v * s_vol;
+    }
+    if (t == 0) s_total += s_vol;
+    __syncthreads();
+  }
+  for (int i = t; i < kK * M; i += blockDim.x) s_new[i / M][i % M] = s_acc[i / M][i % M] / s_total;
+}
+
 template <int N, int M, int MODE>
 __global__ void __launch_bounds__(64) weno_reconstruct_kernel(WenoArgs a) {
   const int64_t c = blockIdx.x;
@@ -80,7 +216,7 @@ __global__ void __launch_bounds__(64) weno_reconstruct_kernel(WenoArgs a) {
     for (int s = 0; s < 6; ++s) n += s_adj[s] >= 0;
     s_nadj = n;
     int troubled = 1;
-    if (MODE == 2) {
+    if (MODE >= 2) {
       // weno::Eigen::IsNotSmooth on density and energy (weno.hpp:230-258)
       troubled = 0;
       const double s00 = a.s00[c];
@@ -133,6 +269,9 @@ __global__ void __launch_bounds__(64) weno_reconstruct_kernel(WenoArgs a) {
     }
   }
   __syncthreads();
+  if constexpr (MODE == 3) {
+    eigen_reconstruct<M>(a, c, n_adj, s_cand, s_beta, s_new);
+  } else {
   // smoothness indicators beta = c^T B c (weno.hpp:25-95)
   if (t < 7 * kK) {
     const int slot = t / kK, k = t - slot * kK;
@@ -173,6 +312,7 @@ __global__ void __launch_bounds__(64) weno_reconstruct_kernel(WenoArgs a) {
       s_new[k][m] = v;
     }
   }
+  }
   __syncthreads();
   // UpdateNodalCoeff: nodal values = modal expansion at the nodes
   const double *pc = a.psi + c * N * M;
@@ -197,11 +337,13 @@ void limiter_dispatch(mcfd_handle *h, double *u) {
   weno_modal_kernel<N, M><<<(unsigned)((total + 255) / 256), 256, 0, h->stream>>>(
       u, l.mn, l.modal, mesh.n_cells);
   WenoArgs wa{u, l.modal, l.psi, l.proj, l.beta, l.eval, l.s00, l.divisor, l.adj,
-              l.troubled, mesh.n_cells, l.w0, l.eps, (Q - 1) < 3 ? 1.0 : 3.0};
+              l.frame, l.volume, l.troubled, mesh.n_cells, l.w0, l.eps, (Q - 1) < 3 ? 1.0 : 3.0};
   if (l.kind == 1 /* MCFD_LIMITER_LAZY */)
     weno_reconstruct_kernel<N, M, 1><<<(unsigned)mesh.n_cells, 64, 0, h->stream>>>(wa);
-  else
+  else if (l.kind == 2 /* MCFD_LIMITER_DETECT_LAZY */)
     weno_reconstruct_kernel<N, M, 2><<<(unsigned)mesh.n_cells, 64, 0, h->stream>>>(wa);
+  else
+    weno_reconstruct_kernel<N, M, 3><<<(unsigned)mesh.n_cells, 64, 0, h->stream>>>(wa);
 }
 
 }  // namespace

@@ -87,3 +87,44 @@ def test_jump_detector_flags_cells_next_to_a_shock():
     centers = m.cell_centers()[:, 0]
     assert flags.any()
     assert np.all(np.abs(centers[flags] - 0.5) < 2 / 12)  # within two cells of the jump
+
+
+def test_eigen_matrices_are_inverse():
+    """test/riemann/euler/eigen.cpp:13-23: L R = R L = I to 1e-15 (scaled)."""
+    rng = np.random.default_rng(31415926)
+    for _ in range(32):
+        prim = [rng.uniform(0.5, 2), *rng.uniform(-1, 1, 3), rng.uniform(0.5, 2)]
+        n = rng.normal(size=3)
+        n /= np.linalg.norm(n)
+        t = np.cross(n, rng.normal(size=3))
+        t /= np.linalg.norm(t)
+        frame = np.stack([n, t, np.cross(n, t)])
+        L, R = orc.eigen_matrices(orc.prim_to_cons(prim), frame)
+        assert np.abs(L @ R - np.eye(5)).max() < 1e-14
+        assert np.abs(R @ L - np.eye(5)).max() < 1e-14
+
+
+@pytest.mark.parametrize("p", [1, 2, 3])
+def test_eigen_reconstruction_preserves_means_and_linear_fields(p):
+    """weno::Eigen reconstruction (on every cell) keeps every cell average: the
+    candidates share it, the weights of a component sum to one and R L = I.
+    A linear field is reproduced: every candidate is the same polynomial."""
+    m = meshlib.box((4, 3, 3), lengths=(1.0, 1.0, 1.0), periodic=(False,) * 3, jitter=0.1, seed=2)
+    om = orc.Mesh(m, p)
+    lim = orc.Limiter(om, orc.LIMITER_EIGEN_ALL)
+    x = meshlib.node_coordinates(m, p).reshape(-1, 3)
+    rng = np.random.default_rng(p)
+    n = len(x)
+    rho = 1 + 0.5 * (x[:, 0] > 0.5) + 0.05 * rng.uniform(-1, 1, n)
+    u = cases.prim_to_cons(rho, np.full(n, 0.2), np.full(n, -0.1), np.zeros(n),
+                           1 + 0.3 * (x[:, 1] > 0.4)).ravel()
+    before = lim.modal(u)
+    out, count = lim.limit(u)
+    assert count == m.n_cells
+    after = lim.modal(out)
+    assert np.abs(after[:, :, 0] - before[:, :, 0]).max() < 1e-12 * np.abs(before[:, :, 0]).max()
+    assert not np.allclose(after, before)
+    lin = cases.prim_to_cons(1 + 0.1 * x[:, 0], np.full(n, 0.2), np.full(n, 0.1), np.zeros(n),
+                             1 + 0.05 * x[:, 1]).ravel()
+    out_l, _ = lim.limit(lin)
+    assert np.abs(out_l - lin).max() < 1e-12 * np.abs(lin).max()
