@@ -152,7 +152,9 @@ __device__ __forceinline__ void given_value(const BcDev &bc, const double *x,
   for (int k = 0; k < kK; ++k) g[k] = src[k];
 }
 
-template <int Q, int R>
+// FAST_SQRT (the mixed form): the Rusanov wave speed's square root from an
+// FP32 seed and one FP64 Newton step (sqrt_seeded, relative error ~1e-13).
+template <int Q, int R, bool FAST_SQRT>
 __global__ void __launch_bounds__(256) face_flux_kernel(FaceArgs a) {
   constexpr int QF = Q * Q, KN = kK * Q * Q * Q;
   int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -175,7 +177,7 @@ __global__ void __launch_bounds__(256) face_flux_kernel(FaceArgs a) {
     for (int k = 0; k < kK; ++k) cs[k] = us[k];
     if constexpr (R == kRusanov) {
       // already multiplied by the face weight
-      flux_rusanov_cons_weighted(ch, cs, n, g.w, out);
+      flux_rusanov_cons_weighted<FAST_SQRT>(ch, cs, n, g.w, out);
       double *dst = a.flux + gid * kK;
 #pragma unroll
       for (int k = 0; k < kK; ++k) dst[k] = out[k];
@@ -635,7 +637,13 @@ __global__ void set_state_kernel(DevState *state, double t, double dt,
 template <int Q, int R>
 void face_launch(mcfd_handle *h, const FaceArgs &fa) {
   int64_t blocks = (fa.n_points + 255) / 256;
-  face_flux_kernel<Q, R><<<(unsigned)blocks, 256, 0, h->stream>>>(fa);
+  if constexpr (R == kRusanov) {
+    if (h->opt.precision == 1) {
+      face_flux_kernel<Q, R, true><<<(unsigned)blocks, 256, 0, h->stream>>>(fa);
+      return;
+    }
+  }
+  face_flux_kernel<Q, R, false><<<(unsigned)blocks, 256, 0, h->stream>>>(fa);
 }
 
 template <int Q>

@@ -142,18 +142,52 @@ __device__ __forceinline__ double rcp_newton(double x) {
   d = fma(-x, y, 1.0);
   return fma(y, d, y);
 }
+// Square root for the mixed form's wave speed: one Newton-Raphson step on
+// the reciprocal square root, y <- y + y (1 - x y^2) / 2, from the FP32
+// hardware estimate of 1/sqrt(x) (relative error below 3e-7, so ~1.4e-13
+// after the step), then sqrt(x) = x y.  Outside the normal FP32 range the
+// FP64 square root is used.
+__device__ __forceinline__ double sqrt_seeded(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7ff) - (1023 - 127);
+  if (e <= 1 || e >= 253) return sqrt(x);
+  const unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
+  const float xf = __uint_as_float(((unsigned)e << 23) + (unsigned)(mant >> 29));
+  const unsigned yb = __float_as_uint(rsqrtf(xf));
+  const unsigned ye = (yb >> 23) & 0xffu;
+  const double y0 = __longlong_as_double((long long)(
+      ((unsigned long long)(ye + (1023u - 127u)) << 52) |
+      ((unsigned long long)(yb & 0x7fffffu) << 29)));
+  const double r = fma(-(x * y0), y0, 1.0);
+  const double y1 = fma(y0 * r, 0.5, y0);
+  return x * y1;
+}
+
+// Sign tests on the bit patterns (integer pipes): x > 0 and x < 0 for
+// finite or infinite x.
+__device__ __forceinline__ bool bits_positive(double x) { return __double_as_longlong(x) > 0; }
+__device__ __forceinline__ bool bits_negative(double x) {
+  const long long b = __double_as_longlong(x);
+  return b < 0 && (b << 1) != 0;
+}
 #else
 inline double rcp_newton(double x) { return 1.0 / x; }
+inline double sqrt_seeded(double x) { return std::sqrt(x); }
+inline bool bits_positive(double x) { return x > 0; }
+inline bool bits_negative(double x) { return x < 0; }
 #endif
 
+// One side of the conservative-form Rusanov flux.  FAST_SQRT (the mixed
+// form) takes the sound speed from sqrt_seeded.
+template <bool FAST_SQRT = false>
 MCFD_HD bool rusanov_side(const double *c, const double *n, double *f,
                           double *speed) {
   double r = c[0], e = c[4];
-  if (!(r > 0) || e < 0) return false;
+  if (!bits_positive(r) || bits_negative(e)) return false;
   double rinv = rcp_newton(r);
   double m2 = c[1] * c[1] + c[2] * c[2] + c[3] * c[3];
   double p = (e - 0.5 * m2 * rinv) * kGm1;
-  if (p < 0) return false;
+  if (bits_negative(p)) return false;
   double mn = c[1] * n[0] + c[2] * n[1] + c[3] * n[2];
   double un = mn * rinv;
   f[0] = mn;
@@ -161,13 +195,19 @@ MCFD_HD bool rusanov_side(const double *c, const double *n, double *f,
   f[2] = c[2] * un + p * n[1];
   f[3] = c[3] * un + p * n[2];
   f[4] = (e + p) * un;
-  *speed = (p > 0 ? sqrt(kGamma * p * rinv) : 0.0);  // sound speed; caller adds |un|
+  const double c2 = kGamma * p * rinv;
+  if constexpr (FAST_SQRT) {
+    *speed = bits_positive(p) ? sqrt_seeded(c2) : 0.0;  // sound speed; caller adds |un|
+  } else {
+    *speed = bits_positive(p) ? sqrt(c2) : 0.0;
+  }
   speed[1] = fabs(un);
   return true;
 }
 
 MCFD_HD void flux_rusanov_cons(const double *cl, const double *cr,
                                const double *n, double *f);
+template <bool FAST_SQRT = false>
 MCFD_HD void flux_rusanov_cons_weighted(const double *cl, const double *cr,
                                         const double *n, double w, double *f);
 
@@ -208,12 +248,13 @@ MCFD_HD void flux_rusanov_cons(const double *cl, const double *cr,
 // fluxes and |u.nh| + a|nh| = (w/2)(|u.n| + a), so
 //   w F_hat = F_L(nh) + F_R(nh) - lambda(nh) (U_R - U_L)
 // without the separate averaging and weighting multiplies.
+template <bool FAST_SQRT>
 MCFD_HD void flux_rusanov_cons_weighted(const double *cl, const double *cr,
                                         const double *n, double w, double *f) {
   const double hw = 0.5 * w;
   const double nh[3] = {hw * n[0], hw * n[1], hw * n[2]};
   double fl[kK], fr[kK], sl[2], sr[2];
-  if (rusanov_side(cl, nh, fl, sl) && rusanov_side(cr, nh, fr, sr)) {
+  if (rusanov_side<FAST_SQRT>(cl, nh, fl, sl) && rusanov_side<FAST_SQRT>(cr, nh, fr, sr)) {
     double lam = fmax(fma(sl[0], hw, sl[1]), fma(sr[0], hw, sr[1]));
 #pragma unroll
     for (int k = 0; k < kK; ++k) f[k] = (fr[k] + fl[k]) - lam * (cr[k] - cl[k]);
