@@ -646,6 +646,134 @@ def run_ensemble(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# Four-quadrant Riemann problem (demo/euler/riemann2d.cpp:5-53): 256 x 256 x
+# 16 Hex8 on [0,1]^2 x [0,0.0625], DGSEM p = 2, Roe, SSP-RK3 at the reference
+# CFL table value (0.209), weno::Eigen limiter (jump detector + characteristic
+# reconstruction) after every stage; walls on top/right/front/back, moving-
+# shock smart states left/bottom.  Both precision forms; the troubled
+# fraction is reconstructions per cell per limiter pass.
+QUAD_DEGREE = 2
+QUAD_SAMPLE = (32, 32, 2)
+
+
+def quadrant_oracle_bcs():
+    import oracle.orc as orc
+    from pvcriemannsolvers_gb300 import MovingSplit, cases
+    return {0: (orc.BC_SMART, MovingSplit(axis=1, position=0.8, speed=cases.SPEED_BC, a=cases.Q_C, b=cases.Q_B)),
+            1: (orc.BC_INVISCID_WALL, None),
+            2: (orc.BC_SMART, MovingSplit(axis=0, position=0.8, speed=cases.SPEED_CD, a=cases.Q_C, b=cases.Q_D)),
+            3: (orc.BC_INVISCID_WALL, None), 4: (orc.BC_INVISCID_WALL, None), 5: (orc.BC_INVISCID_WALL, None)}
+
+
+def quadrant_cpu_sample(seconds=12.0, threads=None):
+    import oracle.orc as orc
+    from pvcriemannsolvers_gb300 import cases, mesh as meshlib
+    orc.build()
+    threads = threads or os.cpu_count() or 1
+    orc.set_threads(threads)
+    m = cases.quadrant_mesh(*QUAD_SAMPLE)
+    om = orc.Mesh(m, QUAD_DEGREE)
+    om.set_bcs(quadrant_oracle_bcs())
+    lim = orc.Limiter(om, orc.LIMITER_EIGEN)
+    u, _ = lim.limit(cases.quadrant_ic(meshlib.node_coordinates(m, QUAD_DEGREE).reshape(-1, 3)).ravel())
+    t, n, t0 = 0.0, 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        dt = om.time_step(u, 1.0, 3, 0.0)
+        u = lim.rk_update(orc.ROE, 3, t, dt, u)
+        t += dt
+        n += 1
+    el = time.perf_counter() - t0
+    return {"value": 3 * u.size * n / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{QUAD_SAMPLE[0]}x{QUAD_SAMPLE[1]}x{QUAD_SAMPLE[2]} cells of the same case "
+                      f"(L = {u.size} DOFs), {n} SSP-RK3 steps with the limiter, {el:.1f} s, oracle (OpenMP)"}
+
+
+def run_quadrant(args, rank, world, local_rank):
+    import torch
+    from pvcriemannsolvers_gb300 import Lobatto, build, cases, mesh as meshlib
+    build.build()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    nx, ny, nz = args.quadrant_cells
+    m = cases.quadrant_mesh(nx, ny, nz)
+    u0 = np.ascontiguousarray(cases.quadrant_ic(meshlib.node_coordinates(m, QUAD_DEGREE).reshape(-1, 3)).ravel())
+    L = u0.size
+    res = {}
+    for form in ("fp64", "mixed"):
+        sysm = Lobatto(m, QUAD_DEGREE, "roe", device=local_rank, precision=form, limiter="eigen")
+        cases.quadrant_bc(sysm)
+        stream = torch.cuda.Stream(device=dev)
+        sysm.set_stream(stream.cuda_stream)
+        sysm.SetSolutionColumn(u0)
+        t = sysm.advance(args.warmup, 1.0, 3, 0.0)
+        sysm.troubled_cells()
+        torch.cuda.synchronize(dev)
+        launches0 = sysm.launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(local_rank) as clocks:
+            with torch.cuda.stream(stream):
+                e0.record(stream)
+                t = sysm.advance(args.steps, 1.0, 3, t)
+                e1.record(stream)
+            e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        troubled = sysm.troubled_cells()
+        launches = sysm.launch_count() - launches0
+        sol = sysm.GetSolutionColumn()
+        kt = sysm.kernel_times(reps=3)
+        host_in = torch.empty(L, dtype=torch.float64, pin_memory=True).numpy()
+        host_out = torch.empty(L, dtype=torch.float64, pin_memory=True).numpy()
+        host_in[:] = sol
+        e2e_steps = max(1, min(args.steps, 10))
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        te = t
+        for _ in range(e2e_steps):
+            sysm.SetSolutionColumn(host_in)
+            te = sysm.advance(1, 1.0, 3, te)
+            sysm.get_solution_into(host_out)
+        torch.cuda.synchronize(dev)
+        e2e_s = time.perf_counter() - t0
+        sysm.close()
+        res[form] = {"value": 3 * L * args.steps / (ms * 1e-3), "ms_per_step": ms / args.steps,
+                     "e2e": 3 * L * e2e_steps / e2e_s, "launches": launches, "kernel_ms": kt,
+                     "clocks": clocks.summary(), "t": t, "solution": sol,
+                     "troubled_fraction": troubled / (3.0 * args.steps * m.n_cells)}
+    fp64_peak = fp64_peak_tflops(torch, dev)
+    a, b = res["mixed"]["solution"].reshape(-1, K)[:, 0], res["fp64"]["solution"].reshape(-1, K)[:, 0]
+    cpu = None
+    if not args.no_cpu:
+        cpu = quadrant_cpu_sample()
+    r = res["mixed"]
+    line = {
+        "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
+        "config": {"workload": f"four-quadrant Riemann problem, {nx}x{ny}x{nz} Hex8, DGSEM p={QUAD_DEGREE}, Roe, "
+                               f"SSP-RK3, CFL 0.209, weno::Eigen limiter after every stage",
+                   "cells": m.n_cells, "dofs": L,
+                   "form": "mixed (FP32 volume flux + contraction; FP64 Riemann fluxes, limiter, RK)",
+                   "step": "dt reduction + 3 x (RK stage + limiter pass)",
+                   "l2_flush": "inputs larger than L2 (solution column 1.13 GB)"},
+        "accuracy": {"t_end": r["t"], "mixed_vs_fp64_density_rel_l2": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
+                     "troubled_fraction_mixed": r["troubled_fraction"],
+                     "troubled_fraction_fp64": res["fp64"]["troubled_fraction"]},
+        "clocks": r["clocks"],
+        "e2e": {"value": r["e2e"], "unit": UNIT, "h2d_bytes_per_step": 8 * L, "d2h_bytes_per_step": 8 * L,
+                "path": "mcfd_set_solution (pinned host) + mcfd_advance(1) + mcfd_get_solution (pinned host)"},
+        "gpu_launches": r["launches"],
+        "plain_fp64": {k: res["fp64"][k] for k in ("value", "ms_per_step", "e2e", "launches", "kernel_ms", "clocks")},
+        "roofline": {"bound": "fp64", "kernel": "step", "kernel_ms": r["kernel_ms"], "peak": fp64_peak,
+                     "unit": "TFLOP/s", "achieved": None, "frac": None, "traffic": None,
+                     "peak_source": "measured in this run: cuBLAS DGEMM 4096^3",
+                     "note": "per-kernel rooflines of the DGSEM kernels: the vortex line"},
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_gpu(args, rank, world, local_rank):
     import torch
     from pvcriemannsolvers_gb300 import build, cases, mesh as meshlib
@@ -713,9 +841,11 @@ def main():
     ap.add_argument("--cells", type=int, default=N_CELLS_1D, help="cells per direction (profiling runs a smaller case)")
     ap.add_argument("--form", default="both", choices=["both", "fp64", "mixed"],
                     help="precision form(s) to time; the line's value is the mixed form when timed")
-    ap.add_argument("--workload", default="vortex", choices=["vortex", "mixed_box", "ensemble"],
+    ap.add_argument("--workload", default="vortex", choices=["vortex", "mixed_box", "ensemble", "quadrant"],
                     help="vortex: the headline DGSEM case; mixed_box: modal DG on hex + tet blocks; "
                          "ensemble: 64 independent cases in one graph per step")
+    ap.add_argument("--quadrant-cells", type=int, nargs=3, default=[256, 256, 16], metavar=("NX", "NY", "NZ"),
+                    help="mesh of the four-quadrant workload")
     ap.add_argument("--ensemble-scale", type=float, default=1.0,
                     help="scale of the ensemble's element counts (profiling runs a smaller case)")
     ap.add_argument("--mixed-cells", type=int, nargs=2, default=[MIXED_HEX_1D, MIXED_TET_1D],
@@ -734,6 +864,9 @@ def main():
         return
     if args.workload == "ensemble":
         run_ensemble(args, rank, world, local_rank)
+        return
+    if args.workload == "quadrant":
+        run_quadrant(args, rank, world, local_rank)
         return
     if world > 1:
         import torch
