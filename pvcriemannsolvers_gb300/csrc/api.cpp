@@ -151,12 +151,12 @@ void release(mcfd_handle *h) {
   auto &b = h->buf;
   void *ptrs[] = {m.cell_geo, m.cell_geo32, m.cell_rate, m.cell_flux, m.face_cells,
                   m.face_group, m.face_geo, m.face_xyz, m.face_map, m.dmat,
-                  m.bcs, b.u, b.u1, b.u2, b.res, b.flux, b.state};
+                  m.bcs, b.u, b.u1, b.u2, b.res, b.flux, b.trace, b.state};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   auto &l = h->lim;
   void *lptrs[] = {l.psi, l.mn, l.proj, l.beta, l.eval, l.s00, l.divisor, l.adj,
-                   l.frame, l.volume, l.modal, l.troubled};
+                   l.frame, l.volume, l.modal, l.list, l.list_count, l.troubled};
   for (void *p : lptrs)
     if (p) cudaFree(p);
   auto &cs = h->cases;
@@ -673,6 +673,8 @@ int build_limiter(mcfd_handle *h, const mcfd_mesh_desc *d, int kind, double w0,
   if ((rc = upload(h, &l.frame, adj_frame))) return rc;
   if ((rc = upload(h, &l.volume, volume))) return rc;
   CUDA_TRY(h, cudaMalloc(&l.modal, sizeof(double) * C * mcfd::kK * M));
+  CUDA_TRY(h, cudaMalloc(&l.list, sizeof(int32_t) * C));
+  CUDA_TRY(h, cudaMalloc(&l.list_count, sizeof(unsigned)));
   CUDA_TRY(h, cudaMalloc(&l.troubled, sizeof(unsigned long long)));
   CUDA_TRY(h, cudaMemset(l.troubled, 0, sizeof(unsigned long long)));
   return MCFD_OK;
@@ -747,6 +749,12 @@ int mcfd_create(const mcfd_mesh_desc *mesh, const mcfd_options *options,
     if (e == cudaSuccess) e = cudaMalloc(&h->buf.state, sizeof(mcfd::DevState));
     if (e == cudaSuccess) e = cudaMemset(h->buf.u, 0, col);
     if (e == cudaSuccess) e = cudaMemset(h->buf.state, 0, sizeof(mcfd::DevState));
+    // node traces for the Rusanov face flux of the nodal schemes (a limiter
+    // rewrites states after the cell kernel, so it turns them off)
+    h->use_trace = options->scheme != MCFD_MODAL && options->riemann == MCFD_RUSANOV &&
+                   options->limiter == MCFD_LIMITER_NONE;
+    if (e == cudaSuccess && h->use_trace)
+      e = cudaMalloc(&h->buf.trace, sizeof(double) * 3 * h->mesh.n_cells * h->mesh.n);
     if (e != cudaSuccess) rc = cuda_fail(h, e, "device allocation");
   }
   if (rc) {
@@ -803,6 +811,7 @@ static int copy_column(mcfd_handle *h, void *dst, const void *src, int64_t n,
                        cudaMemcpyKind kind) {
   if (!h || !dst || !src) return MCFD_ERR_ARGUMENT;
   if (n != h->mesh.column) return fail(h, MCFD_ERR_ARGUMENT, "column size mismatch");
+  mcfd::invalidate_trace(h, (const double *)dst);
   cudaSetDevice(h->device);
   CUDA_TRY(h, cudaMemcpyAsync(dst, src, sizeof(double) * n, kind, h->stream));
   CUDA_TRY(h, cudaStreamSynchronize(h->stream));
@@ -940,6 +949,9 @@ int mcfd_advance(mcfd_handle *h, int32_t n_steps, double dt_guess, int32_t rk_or
   cudaSetDevice(h->device);
   double cfl = h->opt.cfl > 0 ? h->opt.cfl : cfl_table(rk_order, h->mesh.p);
   h->launches += mcfd::launch_set_state(h, *t, 0.0, dt_guess, cfl, 1);
+  // the captured step reads the trace of u in its first stage and leaves the
+  // trace of the new u behind; make it current before capture and replay
+  if (h->use_trace && h->trace_for != h->buf.u) h->launches += mcfd::launch_trace(h, h->buf.u);
   CUDA_TRY(h, cudaGetLastError());
   if (!h->step_graph || h->step_graph_order != rk_order) {
     if (h->step_graph) { cudaGraphExecDestroy(h->step_graph); h->step_graph = nullptr; }
@@ -1067,6 +1079,7 @@ int mcfd_ensemble_advance(mcfd_ensemble *e, int32_t n_steps, double dt_guess, in
   for (mcfd_handle *h : e->members) {
     double cfl = h->opt.cfl > 0 ? h->opt.cfl : cfl_table(rk_order, h->mesh.p);
     h->launches += mcfd::launch_set_state(h, h->t_host, 0.0, dt_guess, cfl, 1);
+    if (h->use_trace && h->trace_for != h->buf.u) h->launches += mcfd::launch_trace(h, h->buf.u);
     cudaError_t err = cudaGetLastError();
     if (err == cudaSuccess) err = cudaStreamSynchronize(h->stream);
     if (err != cudaSuccess) return ens_fail(e, MCFD_ERR_CUDA, std::string("member set-up: ") + cudaGetErrorString(err));
@@ -1235,6 +1248,7 @@ int mcfd_kernel_times(mcfd_handle *h, int32_t reps, double *out_ms) {
   auto &b = h->buf;
   double cfl = h->opt.cfl > 0 ? h->opt.cfl : cfl_table(3, h->mesh.p);
   h->launches += mcfd::launch_set_state(h, h->t_host, 0.0, 1e300, cfl, 1);
+  if (h->use_trace && h->trace_for != b.u) h->launches += mcfd::launch_trace(h, b.u);
   float ms = 0;
   // dt reduction (reads u)
   CUDA_TRY(h, cudaEventRecord(e0, h->stream));
@@ -1260,6 +1274,7 @@ int mcfd_kernel_times(mcfd_handle *h, int32_t reps, double *out_ms) {
   out_ms[2] = ms / reps;
   // one whole step on a copy of the solution (u is restored afterwards)
   CUDA_TRY(h, cudaMemcpyAsync(b.res, b.u, sizeof(double) * h->mesh.column, cudaMemcpyDeviceToDevice, h->stream));
+  if (h->use_trace && h->trace_for != b.u) h->launches += mcfd::launch_trace(h, b.u);
   CUDA_TRY(h, cudaEventRecord(e0, h->stream));
   for (int r = 0; r < reps; ++r) {
     h->launches += mcfd::launch_dt(h, b.u);
@@ -1270,6 +1285,7 @@ int mcfd_kernel_times(mcfd_handle *h, int32_t reps, double *out_ms) {
   CUDA_TRY(h, cudaEventElapsedTime(&ms, e0, e1));
   out_ms[3] = ms / reps;
   CUDA_TRY(h, cudaMemcpyAsync(b.u, b.res, sizeof(double) * h->mesh.column, cudaMemcpyDeviceToDevice, h->stream));
+  mcfd::invalidate_trace(h, b.u);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return check_status(h);

@@ -53,6 +53,7 @@ struct FaceArgs {
   int n_groups;
   int fr;  // flux reconstruction: mark faces without a boundary condition
   CaseView cs;
+  const double *trace;  // node traces of u (Rusanov), or null
 };
 
 // FR: a boundary face point without a registered boundary gets no correction
@@ -74,6 +75,7 @@ struct CellArgs {
   int fr;     // 0: dg::Lobatto (weak form), 1: fr::Lobatto (Huynh g2)
   double g1;  // FR: g_R'(1) of the Huynh g2 correction
   CaseView cs;
+  double *trace;  // write the node traces of u_out here (surface nodes), or null
 };
 
 // Step of the case that owns cell c (the handle's step without cases).
@@ -177,7 +179,14 @@ __global__ void __launch_bounds__(256) face_flux_kernel(FaceArgs a) {
     for (int k = 0; k < kK; ++k) cs[k] = us[k];
     if constexpr (R == kRusanov) {
       // already multiplied by the face weight
-      flux_rusanov_cons_weighted<FAST_SQRT>(ch, cs, n, g.w, out);
+      if (a.trace) {
+        const double *th = a.trace + ((int64_t)cells.x * (Q * Q * Q) + map.x) * 3;
+        const double *ts = a.trace + ((int64_t)cells.y * (Q * Q * Q) + map.y) * 3;
+        const double trh[3] = {th[0], th[1], th[2]}, trs[3] = {ts[0], ts[1], ts[2]};
+        flux_rusanov_traced_weighted(ch, trh, cs, trs, n, g.w, out);
+      } else {
+        flux_rusanov_cons_weighted<FAST_SQRT>(ch, cs, n, g.w, out);
+      }
       double *dst = a.flux + gid * kK;
 #pragma unroll
       for (int k = 0; k < kK; ++k) dst[k] = out[k];
@@ -329,6 +338,7 @@ cell_update_kernel(CellArgs a) {
     }
   } else {
     const double dt = cell_dt(a.cs, a.state, c);
+    double nv[kK];
 #pragma unroll
     for (int r = 0; r < kK; ++r) {
       double next = uq[r] + (res[r] * inv_w) * dt;
@@ -344,6 +354,14 @@ cell_update_kernel(CellArgs a) {
       }
       bad |= !isfinite(v);
       out[r] = v;
+      nv[r] = v;
+    }
+    const bool surface = i == 0 || i == Q - 1 || j == 0 || j == Q - 1 || k == 0 || k == Q - 1;
+    if (a.trace && surface) {
+      double tr[3];
+      node_trace<false>(nv, tr);
+      double *dst = a.trace + (c * N + q) * 3;
+      dst[0] = tr[0]; dst[1] = tr[1]; dst[2] = tr[2];
     }
   }
   if (bad) atomicOr(&a.state->status, (unsigned)kStatusNonFinite);
@@ -474,6 +492,7 @@ cell_update_mixed_kernel(CellArgs a, const float *__restrict__ geo32) {
     }
   } else {
     const float wdt = inv_w * f64_to_f32(cell_dt(a.cs, a.state, c));
+    double nv[kK];
 #pragma unroll
     for (int rr = 0; rr < kK; ++rr) {
       double next = uq[rr] + f32_to_f64(res[rr] * wdt);
@@ -489,6 +508,14 @@ cell_update_mixed_kernel(CellArgs a, const float *__restrict__ geo32) {
       }
       bad |= !finite64(val);
       out[rr] = val;
+      nv[rr] = val;
+    }
+    const bool surface = i == 0 || i == Q - 1 || j == 0 || j == Q - 1 || k == 0 || k == Q - 1;
+    if (a.trace && surface) {
+      double tr[3];
+      node_trace<true>(nv, tr);
+      double *dst = a.trace + (c * N + q) * 3;
+      dst[0] = tr[0]; dst[1] = tr[1]; dst[2] = tr[2];
     }
   }
   if (bad) atomicOr(&a.state->status, (unsigned)kStatusNonFinite);
@@ -625,6 +652,19 @@ __global__ void set_cases_kernel(double *case_t, double *case_dt, int n, double 
   }
 }
 
+// Node traces of a state (Buffers::trace), one thread per node.
+template <bool FAST_SQRT>
+__global__ void __launch_bounds__(256)
+trace_kernel(const double *u, double *trace, int64_t n_nodes) {
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= n_nodes) return;
+  double tr[3];
+  node_trace<FAST_SQRT>(u + gid * kK, tr);
+  trace[gid * 3 + 0] = tr[0];
+  trace[gid * 3 + 1] = tr[1];
+  trace[gid * 3 + 2] = tr[2];
+}
+
 __global__ void set_state_kernel(DevState *state, double t, double dt,
                                  double dt_guess, double cfl, int reset_rate) {
   state->t = t;
@@ -707,7 +747,8 @@ int launch_face_flux(mcfd_handle *h, const double *u, double stage_c) {
   const Mesh &m = h->mesh;
   FaceArgs fa{u, m.face_cells, m.face_group, m.face_geo, m.face_xyz,
               m.face_map, m.bcs, h->buf.flux, h->buf.state, stage_c,
-              m.n_points, m.n_groups, h->opt.scheme == 1, case_view(h)};
+              m.n_points, m.n_groups, h->opt.scheme == 1, case_view(h),
+              (h->use_trace && h->trace_for == u) ? h->buf.trace : nullptr};
   if (m.n_points == 0) return 0;
   switch (m.q) {
     case 2: face_dispatch_r<2>(h, fa); break;
@@ -722,9 +763,11 @@ int launch_cell_update(mcfd_handle *h, int stage, const double *u_in,
   if (h->opt.scheme == kSchemeModal)
     return launch_modal_cell_update(h, stage, u_in, u0, u_out, advance_time);
   const Mesh &m = h->mesh;
+  double *trace = (h->use_trace && stage != kStageResidual) ? h->buf.trace : nullptr;
   CellArgs ca{u_in, u0, u_out, m.cell_geo, m.cell_flux, h->buf.flux, m.dmat,
               h->buf.state, m.n_cells, advance_time, h->opt.scheme == 1, h->opt.fr_g1,
-              case_view(h)};
+              case_view(h), trace};
+  if (trace) h->trace_for = u_out;
   switch (m.q) {
     case 2: cell_dispatch_s<2>(h, stage, ca); break;
     case 3: cell_dispatch_s<3>(h, stage, ca); break;
@@ -766,6 +809,18 @@ int launch_dt(mcfd_handle *h, const double *u) {
     }
   }
   return 1 + launch_dt_finalize(h);
+}
+
+int launch_trace(mcfd_handle *h, const double *u) {
+  if (!h->use_trace) return 0;
+  const int64_t nodes = h->mesh.n_cells * h->mesh.n;
+  const unsigned blocks = (unsigned)((nodes + 255) / 256);
+  if (h->opt.precision == 1)
+    trace_kernel<true><<<blocks, 256, 0, h->stream>>>(u, h->buf.trace, nodes);
+  else
+    trace_kernel<false><<<blocks, 256, 0, h->stream>>>(u, h->buf.trace, nodes);
+  h->trace_for = u;
+  return 1;
 }
 
 int launch_advance_cases(mcfd_handle *h) {
@@ -826,9 +881,9 @@ int launch_residual_static_scratch(mcfd_handle *h, const double *d_u,
   const Mesh &m = h->mesh;
   FaceArgs fa{d_u, m.face_cells, m.face_group, m.face_geo, m.face_xyz,
               m.face_map, m.bcs, scratch, h->buf.state, 0.0,
-              m.n_points, m.n_groups, h->opt.scheme == 1, case_view(h)};
+              m.n_points, m.n_groups, h->opt.scheme == 1, case_view(h), nullptr};
   CellArgs ca{d_u, nullptr, d_r, m.cell_geo, m.cell_flux, scratch, m.dmat,
-              h->buf.state, m.n_cells, 0, h->opt.scheme == 1, h->opt.fr_g1, case_view(h)};
+              h->buf.state, m.n_cells, 0, h->opt.scheme == 1, h->opt.fr_g1, case_view(h), nullptr};
   int n = 0;
   if (m.n_points > 0) {
     switch (m.q) {

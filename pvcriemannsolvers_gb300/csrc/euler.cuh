@@ -205,6 +205,56 @@ MCFD_HD bool rusanov_side(const double *c, const double *n, double *f,
   return true;
 }
 
+// The per-node part of rusanov_side, stored once per stage state ("trace"):
+// tr = {1/rho, p, sound speed}; p = -1 marks a state that takes the
+// primitive fallback (non-positive density, negative energy or pressure).
+template <bool FAST_SQRT = false>
+MCFD_HD void node_trace(const double *c, double *tr) {
+  double r = c[0], e = c[4];
+  if (!bits_positive(r) || bits_negative(e)) {
+    tr[0] = 0; tr[1] = -1; tr[2] = 0;
+    return;
+  }
+  double rinv = rcp_newton(r);
+  double m2 = c[1] * c[1] + c[2] * c[2] + c[3] * c[3];
+  double p = (e - 0.5 * m2 * rinv) * kGm1;
+  tr[0] = rinv;
+  if (bits_negative(p)) {
+    tr[1] = -1; tr[2] = 0;
+    return;
+  }
+  const double c2 = kGamma * p * rinv;
+  tr[1] = p;
+  if constexpr (FAST_SQRT) {
+    tr[2] = bits_positive(p) ? sqrt_seeded(c2) : 0.0;
+  } else {
+    tr[2] = bits_positive(p) ? sqrt(c2) : 0.0;
+  }
+}
+
+// rusanov_side with the node's trace supplied.
+MCFD_HD bool rusanov_side_traced(const double *c, const double *tr, const double *n,
+                                 double *f, double *speed) {
+  const double p = tr[1];
+  if (bits_negative(p)) return false;
+  const double rinv = tr[0], e = c[4];
+  double mn = c[1] * n[0] + c[2] * n[1] + c[3] * n[2];
+  double un = mn * rinv;
+  f[0] = mn;
+  f[1] = c[1] * un + p * n[0];
+  f[2] = c[2] * un + p * n[1];
+  f[3] = c[3] * un + p * n[2];
+  f[4] = (e + p) * un;
+  speed[0] = tr[2];
+  speed[1] = fabs(un);
+  return true;
+}
+
+// w * Rusanov(n) from both sides' traces (flux_rusanov_cons_weighted below).
+MCFD_HD void flux_rusanov_traced_weighted(const double *cl, const double *trl,
+                                          const double *cr, const double *trr,
+                                          const double *n, double w, double *f);
+
 MCFD_HD void flux_rusanov_cons(const double *cl, const double *cr,
                                const double *n, double *f);
 template <bool FAST_SQRT = false>
@@ -255,6 +305,24 @@ MCFD_HD void flux_rusanov_cons_weighted(const double *cl, const double *cr,
   const double nh[3] = {hw * n[0], hw * n[1], hw * n[2]};
   double fl[kK], fr[kK], sl[2], sr[2];
   if (rusanov_side<FAST_SQRT>(cl, nh, fl, sl) && rusanov_side<FAST_SQRT>(cr, nh, fr, sr)) {
+    double lam = fmax(fma(sl[0], hw, sl[1]), fma(sr[0], hw, sr[1]));
+#pragma unroll
+    for (int k = 0; k < kK; ++k) f[k] = (fr[k] + fl[k]) - lam * (cr[k] - cl[k]);
+    return;
+  }
+  flux_rusanov(cons_to_prim(cl[0], cl[1], cl[2], cl[3], cl[4]),
+               cons_to_prim(cr[0], cr[1], cr[2], cr[3], cr[4]), n, f);
+#pragma unroll
+  for (int k = 0; k < kK; ++k) f[k] *= w;
+}
+
+MCFD_HD void flux_rusanov_traced_weighted(const double *cl, const double *trl,
+                                          const double *cr, const double *trr,
+                                          const double *n, double w, double *f) {
+  const double hw = 0.5 * w;
+  const double nh[3] = {hw * n[0], hw * n[1], hw * n[2]};
+  double fl[kK], fr[kK], sl[2], sr[2];
+  if (rusanov_side_traced(cl, trl, nh, fl, sl) && rusanov_side_traced(cr, trr, nh, fr, sr)) {
     double lam = fmax(fma(sl[0], hw, sl[1]), fma(sr[0], hw, sr[1]));
 #pragma unroll
     for (int k = 0; k < kK; ++k) f[k] = (fr[k] + fl[k]) - lam * (cr[k] - cl[k]);

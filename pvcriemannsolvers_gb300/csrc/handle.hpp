@@ -86,6 +86,8 @@ struct Limiter {
                              //   point: normal, tangent, bitangent (weno::Eigen)
   double *volume = nullptr;  // [cells] cell volume (weno::Eigen face weights)
   double *modal = nullptr;   // [cells][K][M] scratch: modal coefficients
+  int32_t *list = nullptr;   // [cells] troubled cells of the current pass
+  unsigned *list_count = nullptr;
   unsigned long long *troubled = nullptr;  // counter of reconstructed cells
 };
 
@@ -137,6 +139,10 @@ struct Buffers {
   double *u2 = nullptr;
   double *res = nullptr;   // residual output
   double *flux = nullptr;  // [points][5] face flux scratch
+  // [cells][N][3] 1/rho, p, sound speed of one stage state (Rusanov, nodal
+  // schemes without a limiter): written by the cell kernel that produces the
+  // state, read by the next face kernel instead of recomputing per face point
+  double *trace = nullptr;
   DevState *state = nullptr;
 };
 
@@ -162,6 +168,8 @@ struct mcfd_handle {
   mcfd::Cases cases;
   double t_host = 0;
   int64_t launches = 0;
+  bool use_trace = false;            // see Buffers::trace
+  const double *trace_for = nullptr; // the buffer whose trace buf.trace holds
   std::string err;
   // CUDA graph of one SSP-RK3 step (dt + 3 stages), built on first use
   cudaGraphExec_t step_graph = nullptr;
@@ -178,6 +186,12 @@ int launch_face_flux(mcfd_handle *h, const double *u, double stage_c);
 int launch_cell_update(mcfd_handle *h, int stage, const double *u_in,
                        const double *u0, double *u_out, int advance_time);
 int launch_dt(mcfd_handle *h, const double *u);
+// Trace of a state buffer (Buffers::trace), when the handle uses one.
+int launch_trace(mcfd_handle *h, const double *u);
+// A host-side or limiter write to `u` makes its trace stale.
+inline void invalidate_trace(mcfd_handle *h, const double *u) {
+  if (h->trace_for == u) h->trace_for = nullptr;
+}
 // dt finalisation after a max-rate reduction (handle word or per case).
 int launch_dt_finalize(mcfd_handle *h);
 int launch_rk_stage_sequence(mcfd_handle *h, int order);

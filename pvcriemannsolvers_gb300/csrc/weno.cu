@@ -28,6 +28,7 @@
 // are computed before any is written back).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "euler.cuh"
@@ -199,15 +200,58 @@ __device__ void eigen_reconstruct(const Args &a, int64_t c, int n_adj,
   for (int i = t; i < kK * M; i += blockDim.x) s_new[i / M][i % M] = s_acc[i / M][i % M] / s_total;
 }
 
+// weno::Eigen::IsNotSmooth (weno.hpp:230-258) on density and energy, one
+// thread per cell; flagged cells are appended to the troubled list (their
+// order does not matter: each reconstruction writes only its own cell).
+template <int M>
+__global__ void __launch_bounds__(256)
+weno_detect_kernel(WenoArgs a, int32_t *list, unsigned *count) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.n_cells) return;
+  const double s00 = a.s00[c];
+  const double *ev = a.eval + c * 7 * M;
+  const double *own = a.modal + c * kK * M;
+  int adj[6], n = 0;
+  for (int s = 0; s < 6; ++s) {
+    adj[s] = a.adj[c * 6 + s];
+    n += adj[s] >= 0;
+  }
+  bool troubled = false;
+  const int comps[2] = {0, kK - 1};
+  for (int ci = 0; ci < 2; ++ci) {
+    const int k = comps[ci];
+    double max_abs = fmax(1e-9, fabs(own[k * M] * s00));
+    double mine = 0;
+    for (int m = 0; m < M; ++m) mine += own[k * M + m] * ev[6 * M + m];
+    double sum_abs = 0;
+    for (int s = 0; s < n; ++s) {
+      const int b = adj[s];
+      const double *cb = a.modal + ((int64_t)b * kK + k) * M;
+      double v = 0;
+      for (int m = 0; m < M; ++m) v += cb[m] * ev[s * M + m];
+      sum_abs += fabs(mine - v);
+      max_abs = fmax(max_abs, fabs(cb[0] * a.s00[b]));
+    }
+    if (sum_abs / max_abs / a.divisor[c] > a.smooth_ref) troubled = true;
+  }
+  if (troubled) list[atomicAdd(count, 1u)] = (int32_t)c;
+}
+
+// Reconstruction of the listed cells (every cell when list is null) by a
+// persistent grid of 64-thread blocks, one cell at a time per block.
 template <int N, int M, int MODE>
-__global__ void __launch_bounds__(64) weno_reconstruct_kernel(WenoArgs a) {
-  const int64_t c = blockIdx.x;
+__global__ void __launch_bounds__(64)
+weno_reconstruct_kernel(WenoArgs a, const int32_t *list, const unsigned *count) {
   const int t = threadIdx.x;
   __shared__ double s_cand[7][kK][M];  // slots 0..5 neighbours, 6 own
   __shared__ double s_beta[7][kK];
   __shared__ double s_new[kK][M];
   __shared__ int s_adj[6];
-  __shared__ int s_nadj, s_troubled;
+  __shared__ int s_nadj;
+  const int64_t n_work = list ? (int64_t)*count : a.n_cells;
+  if (blockIdx.x == 0 && t == 0 && n_work > 0) atomicAdd(a.troubled, (unsigned long long)n_work);
+  for (int64_t item = blockIdx.x; item < n_work; item += gridDim.x) {
+  const int64_t c = list ? (int64_t)list[item] : item;
   if (t < 6) s_adj[t] = a.adj[c * 6 + t];
   for (int i = t; i < kK * M; i += blockDim.x) s_cand[6][i / M][i % M] = a.modal[c * kK * M + i];
   __syncthreads();
@@ -215,34 +259,8 @@ __global__ void __launch_bounds__(64) weno_reconstruct_kernel(WenoArgs a) {
     int n = 0;
     for (int s = 0; s < 6; ++s) n += s_adj[s] >= 0;
     s_nadj = n;
-    int troubled = 1;
-    if (MODE >= 2) {
-      // weno::Eigen::IsNotSmooth on density and energy (weno.hpp:230-258)
-      troubled = 0;
-      const double s00 = a.s00[c];
-      const double *ev = a.eval + c * 7 * M;
-      const int comps[2] = {0, kK - 1};
-      for (int ci = 0; ci < 2; ++ci) {
-        const int k = comps[ci];
-        double max_abs = fmax(1e-9, fabs(s_cand[6][k][0] * s00));
-        double mine = 0;
-        for (int m = 0; m < M; ++m) mine += s_cand[6][k][m] * ev[6 * M + m];
-        double sum_abs = 0;
-        for (int s = 0; s < n; ++s) {
-          const int b = s_adj[s];
-          const double *cb = a.modal + ((int64_t)b * kK + k) * M;
-          double v = 0;
-          for (int m = 0; m < M; ++m) v += cb[m] * ev[s * M + m];
-          sum_abs += fabs(mine - v);
-          max_abs = fmax(max_abs, fabs(cb[0] * a.s00[b]));
-        }
-        if (sum_abs / max_abs / a.divisor[c] > a.smooth_ref) troubled = 1;
-      }
-    }
-    s_troubled = troubled;
   }
   __syncthreads();
-  if (!s_troubled) return;
   const int n_adj = s_nadj;
   // Borrow: neighbour coefficients projected onto the own basis, shifted to
   // the own average (weno.hpp:138-166, projection.hpp:260-264)
@@ -324,11 +342,12 @@ __global__ void __launch_bounds__(64) weno_reconstruct_kernel(WenoArgs a) {
     for (int m = 0; m < M; ++m) v += s_new[k][m] * pc[q * M + m];
     uc[q * kK + k] = v;
   }
-  if (t == 0) atomicAdd(a.troubled, 1ull);
+  __syncthreads();  // the shared arrays are reused by the next cell
+  }
 }
 
 template <int Q>
-void limiter_dispatch(mcfd_handle *h, double *u) {
+int limiter_dispatch(mcfd_handle *h, double *u) {
   constexpr int N = Q * Q * Q;
   constexpr int M = Q * (Q + 1) * (Q + 2) / 6;
   const Mesh &mesh = h->mesh;
@@ -338,12 +357,20 @@ void limiter_dispatch(mcfd_handle *h, double *u) {
       u, l.mn, l.modal, mesh.n_cells);
   WenoArgs wa{u, l.modal, l.psi, l.proj, l.beta, l.eval, l.s00, l.divisor, l.adj,
               l.frame, l.volume, l.troubled, mesh.n_cells, l.w0, l.eps, (Q - 1) < 3 ? 1.0 : 3.0};
-  if (l.kind == 1 /* MCFD_LIMITER_LAZY */)
-    weno_reconstruct_kernel<N, M, 1><<<(unsigned)mesh.n_cells, 64, 0, h->stream>>>(wa);
-  else if (l.kind == 2 /* MCFD_LIMITER_DETECT_LAZY */)
-    weno_reconstruct_kernel<N, M, 2><<<(unsigned)mesh.n_cells, 64, 0, h->stream>>>(wa);
+  // persistent grid: 16 blocks of 64 threads per SM on the 152 SMs
+  const unsigned grid = (unsigned)std::min<int64_t>(mesh.n_cells, 152 * 16);
+  if (l.kind == 1 /* MCFD_LIMITER_LAZY: every cell */) {
+    weno_reconstruct_kernel<N, M, 1><<<grid, 64, 0, h->stream>>>(wa, nullptr, nullptr);
+    return 2;
+  }
+  cudaMemsetAsync(l.list_count, 0, sizeof(unsigned), h->stream);
+  weno_detect_kernel<M><<<(unsigned)((mesh.n_cells + 255) / 256), 256, 0, h->stream>>>(
+      wa, l.list, l.list_count);
+  if (l.kind == 2 /* MCFD_LIMITER_DETECT_LAZY */)
+    weno_reconstruct_kernel<N, M, 2><<<grid, 64, 0, h->stream>>>(wa, l.list, l.list_count);
   else
-    weno_reconstruct_kernel<N, M, 3><<<(unsigned)mesh.n_cells, 64, 0, h->stream>>>(wa);
+    weno_reconstruct_kernel<N, M, 3><<<grid, 64, 0, h->stream>>>(wa, l.list, l.list_count);
+  return 3;
 }
 
 }  // namespace
@@ -351,11 +378,10 @@ void limiter_dispatch(mcfd_handle *h, double *u) {
 int launch_limiter(mcfd_handle *h, double *u) {
   if (h->lim.kind == 0) return 0;
   switch (h->mesh.q) {
-    case 2: limiter_dispatch<2>(h, u); break;
-    case 3: limiter_dispatch<3>(h, u); break;
-    default: limiter_dispatch<4>(h, u); break;
+    case 2: return limiter_dispatch<2>(h, u);
+    case 3: return limiter_dispatch<3>(h, u);
+    default: return limiter_dispatch<4>(h, u);
   }
-  return 2;
 }
 
 }  // namespace mcfd
