@@ -71,133 +71,172 @@ weno_modal_kernel(const double *__restrict__ u, const double *__restrict__ mn,
   modal[gid] = s;
 }
 
-// EigenMatrices (riemann/euler/eigen.hpp:27-56) of the conservative state u
-// in the frame {nu, mu, pi}; L and R row-major.  One thread.
-__device__ void eigen_matrices(const double *u, const double *nu, const double *mu,
-                               const double *pi, double *L, double *R) {
-  const Prim w = cons_to_prim(u[0], u[1], u[2], u[3], u[4]);
-  const double ux = w.u, uy = w.v, uz = w.w;
-  const double u_nu = ux * nu[0] + uy * nu[1] + uz * nu[2];
-  const double u_mu = ux * mu[0] + uy * mu[1] + uz * mu[2];
-  const double u_pi = ux * pi[0] + uy * pi[1] + uz * pi[2];
+// One entry of L or R of EigenMatrices (riemann/euler/eigen.hpp:27-56) for
+// the conservative state of primitive w in the frame {nu, mu, pi}:
+// e < 25 is L[e / 5][e % 5], otherwise R[(e - 25) / 5][(e - 25) % 5].
+// Columns of R: u - a, u (entropy), two shear waves, u + a; L = R^-1.
+__device__ double eigen_entry(const Prim &w, const double *nu, const double *mu,
+                              const double *pi, int e) {
+  const double vel[3] = {w.u, w.v, w.w};
+  const double u_nu = vel[0] * nu[0] + vel[1] * nu[1] + vel[2] * nu[2];
   const double a = sqrt(kGamma * w.p / w.rho);
-  const double ek = (ux * ux + uy * uy + uz * uz) / 2;
+  const double ek = (vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]) / 2;
   const double e0 = a * a * (1 / kGm1);
-  const double h0 = e0 + ek;
-  const double vel[3] = {ux, uy, uz};
-  // columns: u - a, u (entropy), two shear waves, u + a
-  R[0 * 5 + 0] = 1; R[0 * 5 + 1] = 1; R[0 * 5 + 2] = 0; R[0 * 5 + 3] = 0; R[0 * 5 + 4] = 1;
-  for (int d = 0; d < 3; ++d) {
-    R[(1 + d) * 5 + 0] = vel[d] - a * nu[d];
-    R[(1 + d) * 5 + 1] = vel[d];
-    R[(1 + d) * 5 + 2] = mu[d];
-    R[(1 + d) * 5 + 3] = pi[d];
-    R[(1 + d) * 5 + 4] = vel[d] + a * nu[d];
+  if (e >= 25) {
+    const int row = (e - 25) / 5, col = (e - 25) % 5;
+    if (row == 0) return (col == 2 || col == 3) ? 0.0 : 1.0;
+    if (row == 4) {
+      const double h0 = e0 + ek;
+      if (col == 0) return h0 - a * u_nu;
+      if (col == 1) return ek;
+      if (col == 2) return vel[0] * mu[0] + vel[1] * mu[1] + vel[2] * mu[2];
+      if (col == 3) return vel[0] * pi[0] + vel[1] * pi[1] + vel[2] * pi[2];
+      return h0 + a * u_nu;
+    }
+    const int d = row - 1;
+    if (col == 0) return vel[d] - a * nu[d];
+    if (col == 1) return vel[d];
+    if (col == 2) return mu[d];
+    if (col == 3) return pi[d];
+    return vel[d] + a * nu[d];
   }
-  R[4 * 5 + 0] = h0 - a * u_nu; R[4 * 5 + 1] = ek; R[4 * 5 + 2] = u_mu; R[4 * 5 + 3] = u_pi;
-  R[4 * 5 + 4] = h0 + a * u_nu;
+  const int row = e / 5, col = e % 5;
   const double b1 = 1 / e0, b2 = b1 * ek;
-  L[0 * 5 + 0] = (b2 + u_nu / a) / 2;
-  L[1 * 5 + 0] = 1 - b2;
-  L[2 * 5 + 0] = -u_mu;
-  L[3 * 5 + 0] = -u_pi;
-  L[4 * 5 + 0] = (b2 - u_nu / a) / 2;
-  for (int d = 0; d < 3; ++d) {
-    L[0 * 5 + 1 + d] = -(b1 * vel[d] + nu[d] / a) / 2;
-    L[1 * 5 + 1 + d] = b1 * vel[d];
-    L[2 * 5 + 1 + d] = mu[d];
-    L[3 * 5 + 1 + d] = pi[d];
-    L[4 * 5 + 1 + d] = -(b1 * vel[d] - nu[d] / a) / 2;
+  if (col == 0) {
+    if (row == 0) return (b2 + u_nu / a) / 2;
+    if (row == 1) return 1 - b2;
+    if (row == 2) return -(vel[0] * mu[0] + vel[1] * mu[1] + vel[2] * mu[2]);
+    if (row == 3) return -(vel[0] * pi[0] + vel[1] * pi[1] + vel[2] * pi[2]);
+    return (b2 - u_nu / a) / 2;
   }
-  L[0 * 5 + 4] = b1 / 2; L[1 * 5 + 4] = -b1; L[2 * 5 + 4] = 0; L[3 * 5 + 4] = 0;
-  L[4 * 5 + 4] = b1 / 2;
+  if (col == 4) {
+    if (row == 0 || row == 4) return b1 / 2;
+    if (row == 1) return -b1;
+    return 0.0;
+  }
+  const int d = col - 1;
+  if (row == 0) return -(b1 * vel[d] + nu[d] / a) / 2;
+  if (row == 1) return b1 * vel[d];
+  if (row == 2) return mu[d];
+  if (row == 3) return pi[d];
+  return -(b1 * vel[d] - nu[d] / a) / 2;
 }
 
 // weno::Eigen reconstruction of cell c from its candidates (slots 0..n_adj-1
-// neighbours, slot 6 own) into s_new; all 64 threads take part.
+// neighbours, slot 6 own) into s_new, all adjacent faces at once so that the
+// 64 threads stay busy:
+//   G_i = C_i B C_i^T     (K x K, face-independent) for each candidate
+//   L_f, R_f              every entry of every face's eigen-matrices
+//   beta[f][i][k] = L_f[k] G_i L_f[k]^T   (= GetSmoothness of L_f C_i)
+//   w[f][i][k]            the reference's weights per face and field
+//   nw[f] = sum_i w[f][i] (L_f C_i),  new = sum_f vol_f R_f nw[f] / sum_f vol_f
 template <int M, class Args>
 __device__ void eigen_reconstruct(const Args &a, int64_t c, int n_adj,
-                                  double (*s_cand)[kK][M], double (*s_beta)[kK],
-                                  double (*s_new)[M]) {
-  __shared__ double s_L[25], s_R[25];
-  __shared__ double s_rot[7][kK][M];
-  __shared__ double s_acc[kK][M];
-  __shared__ double s_total, s_vol;
-  const int t = threadIdx.x;
+                                  double (*s_cand)[kK][M], double (*s_new)[M]) {
+  __shared__ double s_cb[7][kK][M];     // C_i B
+  __shared__ double s_G[7][kK][kK];
+  __shared__ double s_LR[6][50];        // per face: L (25) then R (25)
+  __shared__ double s_beta[6][7][kK];
+  __shared__ double s_w[6][7][kK];
+  __shared__ double s_nw[6][kK][M];
+  __shared__ double s_vol[6];
+  const int t = threadIdx.x, nt = blockDim.x;
+  const int nc = n_adj + 1;  // candidates: 0..n_adj-1 neighbours, then own (slot 6)
   const double *B = a.beta + c * M * M;
-  for (int i = t; i < kK * M; i += blockDim.x) s_acc[i / M][i % M] = 0;
-  if (t == 0) s_total = 0;
-  __syncthreads();
-  for (int f = 0; f < n_adj; ++f) {
-    if (t == 0) {
-      const double s00 = a.s00[c];
-      double big_u[kK];
-      for (int k = 0; k < kK; ++k) big_u[k] = s_cand[6][k][0] * s00;
-      const double *fr = a.frame + (c * 6 + f) * 9;
-      eigen_matrices(big_u, fr, fr + 3, fr + 6, s_L, s_R);
-      s_vol = a.volume[a.adj[c * 6 + f]];
-    }
-    __syncthreads();
-    // L applied to every candidate (ProjectionWrapper::LeftMultiply)
-    for (int i = t; i < (n_adj + 1) * kK * M; i += blockDim.x) {
-      const int slot = i / (kK * M), r = i - slot * kK * M, k = r / M, m = r - k * M;
-      const int src = slot < n_adj ? slot : 6;
-      double v = 0;
-#pragma unroll
-      for (int j = 0; j < kK; ++j) v += s_L[k * 5 + j] * s_cand[src][j][m];
-      s_rot[src][k][m] = v;
-    }
-    __syncthreads();
-    if (t < 7 * kK) {
-      const int slot = t / kK, k = t - slot * kK;
-      if (slot == 6 || slot < n_adj) {
-        double b = 0;
-#pragma unroll
-        for (int m = 0; m < M; ++m) {
-          double row = 0;
-#pragma unroll
-          for (int j = 0; j < M; ++j) row += B[m * M + j] * s_rot[slot][k][j];
-          b += s_rot[slot][k][m] * row;
-        }
-        s_beta[slot][k] = b;
-      }
-    }
-    __syncthreads();
-    if (t < kK) {
-      const int k = t;
-      double w[7];
-      for (int s = 0; s < n_adj; ++s) w[s] = a.w0;
-      double ws = a.w0;
-      ws *= -n_adj;
-      ws += 1.0;
-      w[n_adj] = ws;
-      double sum = 0;
-      for (int s = 0; s <= n_adj; ++s) {
-        double b = (s < n_adj ? s_beta[s][k] : s_beta[6][k]) + a.eps;
-        b *= b;
-        w[s] /= b;
-      }
-      for (int s = 0; s <= n_adj; ++s) sum += w[s];
-      for (int s = 0; s <= n_adj; ++s) w[s] /= sum;
-      for (int m = 0; m < M; ++m) {
-        double v = s_rot[6][k][m] * w[n_adj];
-        for (int s = 0; s < n_adj; ++s) v += s_rot[s][k][m] * w[s];
-        s_new[k][m] = v;
-      }
-    }
-    __syncthreads();
-    // back to conservative variables, weighted by the neighbour's volume
-    for (int i = t; i < kK * M; i += blockDim.x) {
-      const int k = i / M, m = i - k * M;
-      double v = 0;
-#pragma unroll
-      for (int j = 0; j < kK; ++j) v += s_R[k * 5 + j] * s_new[j][m];
-      s_acc[k][m] += v * s_vol;
-    }
-    if (t == 0) s_total += s_vol;
-    __syncthreads();
+  // C_i B and the face data
+  for (int i = t; i < nc * kK * M; i += nt) {
+    const int cand = i / (kK * M), r = i - cand * kK * M, k = r / M, m = r - k * M;
+    const int src = cand < n_adj ? cand : 6;
+    double v = 0;
+    for (int j = 0; j < M; ++j) v += s_cand[src][k][j] * B[j * M + m];
+    s_cb[cand][k][m] = v;
   }
-  for (int i = t; i < kK * M; i += blockDim.x) s_new[i / M][i % M] = s_acc[i / M][i % M] / s_total;
+  {
+    const double s00 = a.s00[c];
+    const Prim w = cons_to_prim(s_cand[6][0][0] * s00, s_cand[6][1][0] * s00, s_cand[6][2][0] * s00,
+                                s_cand[6][3][0] * s00, s_cand[6][4][0] * s00);
+    for (int i = t; i < n_adj * 50; i += nt) {
+      const int f = i / 50, e = i - f * 50;
+      const double *fr = a.frame + (c * 6 + f) * 9;
+      s_LR[f][e] = eigen_entry(w, fr, fr + 3, fr + 6, e);
+    }
+    if (t < n_adj) s_vol[t] = a.volume[a.adj[c * 6 + t]];
+  }
+  __syncthreads();
+  for (int i = t; i < nc * kK * kK; i += nt) {
+    const int cand = i / (kK * kK), r = i - cand * kK * kK, j = r / kK, l = r - j * kK;
+    const int src = cand < n_adj ? cand : 6;
+    double v = 0;
+    for (int m = 0; m < M; ++m) v += s_cb[cand][j][m] * s_cand[src][l][m];
+    s_G[cand][j][l] = v;
+  }
+  __syncthreads();
+  for (int i = t; i < n_adj * nc * kK; i += nt) {
+    const int f = i / (nc * kK), r = i - f * nc * kK, cand = r / kK, k = r - cand * kK;
+    const double *Lk = &s_LR[f][k * 5];
+    double b = 0;
+#pragma unroll
+    for (int j = 0; j < kK; ++j) {
+      double row = 0;
+#pragma unroll
+      for (int l = 0; l < kK; ++l) row += s_G[cand][j][l] * Lk[l];
+      b += Lk[j] * row;
+    }
+    s_beta[f][cand][k] = b;
+  }
+  __syncthreads();
+  // weights (weno.hpp:306-326): w0 for the neighbours, 1 - n w0 for the own
+  // candidate, divided by (beta + eps)^2, normalised per field
+  for (int i = t; i < n_adj * kK; i += nt) {
+    const int f = i / kK, k = i - f * kK;
+    double sum = 0;
+    for (int cand = 0; cand < nc; ++cand) {
+      double w = a.w0;
+      if (cand == n_adj) {
+        w *= -n_adj;
+        w += 1.0;
+      }
+      double b = s_beta[f][cand][k] + a.eps;
+      b *= b;
+      w /= b;
+      s_w[f][cand][k] = w;
+      sum += w;
+    }
+    for (int cand = 0; cand < nc; ++cand) s_w[f][cand][k] /= sum;
+  }
+  __syncthreads();
+  // nw[f] = w_own (L_f C_own) + sum_i w_i (L_f C_i)   (weno.hpp:327-333)
+  for (int i = t; i < n_adj * kK * M; i += nt) {
+    const int f = i / (kK * M), r = i - f * kK * M, k = r / M, m = r - k * M;
+    const double *Lk = &s_LR[f][k * 5];
+    double lc = 0;
+#pragma unroll
+    for (int j = 0; j < kK; ++j) lc += Lk[j] * s_cand[6][j][m];
+    double v = lc * s_w[f][n_adj][k];
+    for (int cand = 0; cand < n_adj; ++cand) {
+      lc = 0;
+#pragma unroll
+      for (int j = 0; j < kK; ++j) lc += Lk[j] * s_cand[cand][j][m];
+      v += lc * s_w[f][cand][k];
+    }
+    s_nw[f][k][m] = v;
+  }
+  __syncthreads();
+  // back to conservative variables, volume-weighted over the faces
+  // (weno.hpp:334-347)
+  for (int i = t; i < kK * M; i += nt) {
+    const int k = i / M, m = i - k * M;
+    double acc = 0, total = 0;
+    for (int f = 0; f < n_adj; ++f) {
+      double v = 0;
+#pragma unroll
+      for (int j = 0; j < kK; ++j) v += s_LR[f][25 + k * 5 + j] * s_nw[f][j][m];
+      acc += v * s_vol[f];
+      total += s_vol[f];
+    }
+    s_new[k][m] = acc / total;
+  }
+  __syncthreads();
 }
 
 // weno::Eigen::IsNotSmooth (weno.hpp:230-258) on density and energy, one
@@ -288,7 +327,7 @@ weno_reconstruct_kernel(WenoArgs a, const int32_t *list, const unsigned *count) 
   }
   __syncthreads();
   if constexpr (MODE == 3) {
-    eigen_reconstruct<M>(a, c, n_adj, s_cand, s_beta, s_new);
+    eigen_reconstruct<M>(a, c, n_adj, s_cand, s_new);
   } else {
   // smoothness indicators beta = c^T B c (weno.hpp:25-95)
   if (t < 7 * kK) {
