@@ -251,12 +251,12 @@ def measure_form(args, torch, dist, dev, local_rank, m, u0, precision):
 
 
 # DRAM bytes (read + write) per launch measured by one ncu capture on the
-# 40^3 p = 3 case (64 000 cells); scaled linearly with the cell count.
+# 40^3 p = 3 case (64 000 cells); scaled linearly with the cell count.  Mixed
+# form: profiles/mixed_kernels_vortex40_p3.md (traced face kernel, cell
+# kernel writing the node traces).
 NCU_TRAFFIC_40 = {
-    ("mixed", "face_flux"): 280.143872e6 + 97.142016e6,
-    ("mixed", "cell_update"): 476.211456e6 + 140.708608e6,
-    ("fp64", "face_flux"): 280.143872e6 + 97.142016e6,
-    ("fp64", "cell_update"): 640.078336e6 + 146.893312e6,
+    ("mixed", "face_flux"): 380.929024e6 + 102.737152e6,
+    ("mixed", "cell_update"): 491.185664e6 + 220.190208e6,
 }
 NCU_CELLS = 40 ** 3
 
