@@ -144,8 +144,8 @@ typedef struct mcfd_mesh_desc {
  *          M = (p+1)(p+2)(p+3)/6.  Quadrature: Hex8 Gauss-Legendre (p+1)^3,
  *          Quad4 faces (p+1)^2; Tet4 14 points (p <= 2) or 24 points (p = 3),
  *          Tri3 faces 6 points (p <= 2) or 12 points (p = 3)
- *          (integrator/{legendre,tetrahedron,triangle}.hpp).  FP64 only, no
- *          limiter. */
+ *          (integrator/{legendre,tetrahedron,triangle}.hpp).  FP64 or mixed
+ *          (FP32 contractions, FP64 face states / Riemann / RK); no limiter. */
 enum mcfd_scheme { MCFD_DGSEM = 0, MCFD_FR = 1, MCFD_MODAL = 2 };
 enum mcfd_precision { MCFD_FP64 = 0, MCFD_MIXED = 1 };
 

@@ -165,7 +165,8 @@ void release(mcfd_handle *h) {
     if (p) cudaFree(p);
   auto &md = h->modal;
   void *mptrs[] = {md.center, md.s, md.vol_off, md.vol, md.cell_faces, md.face_off,
-                   md.point_face, md.fpt, md.fnrm, md.fshift, md.taylor, md.values};
+                   md.point_face, md.fpt, md.fnrm, md.fshift, md.taylor, md.values,
+                   md.s32, md.vol32, md.foff32, md.taylor32};
   for (void *p : mptrs)
     if (p) cudaFree(p);
   if (h->step_graph) cudaGraphExecDestroy(h->step_graph);
@@ -702,10 +703,8 @@ int mcfd_create(const mcfd_mesh_desc *mesh, const mcfd_options *options,
     return fail(nullptr, MCFD_ERR_UNSUPPORTED, "degree must be 1, 2 or 3");
   if (options->scheme != MCFD_DGSEM && options->scheme != MCFD_FR && options->scheme != MCFD_MODAL)
     return fail(nullptr, MCFD_ERR_UNSUPPORTED, "unknown scheme");
-  if (options->scheme == MCFD_MODAL &&
-      (options->precision != MCFD_FP64 || options->limiter != MCFD_LIMITER_NONE))
-    return fail(nullptr, MCFD_ERR_UNSUPPORTED,
-                "the modal scheme is built in FP64 without a limiter");
+  if (options->scheme == MCFD_MODAL && options->limiter != MCFD_LIMITER_NONE)
+    return fail(nullptr, MCFD_ERR_UNSUPPORTED, "the modal scheme is built without a limiter");
   if (options->riemann < MCFD_EXACT || options->riemann > MCFD_RUSANOV)
     return fail(nullptr, MCFD_ERR_ARGUMENT, "unknown Riemann solver");
   if (options->precision != MCFD_FP64 && options->precision != MCFD_MIXED)

@@ -100,52 +100,6 @@ __device__ __forceinline__ double fr_sign(int side) {
   return ((0x2c >> side) & 1) ? 1.0 : -1.0;  // + for faces 2, 3, 5
 }
 
-// FP64 <-> FP32 conversions on the integer pipes.  On this part the FP64
-// unit is the bottleneck and hardware F2F conversions issue there.  These
-// follow the IEEE-754 binary64/binary32 layouts with branch-free selects:
-// round to nearest even, subnormal results flushed to a signed zero,
-// overflow to infinity, NaN kept NaN.
-__device__ __forceinline__ float f64_to_f32(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
-  const int ex = (int)((b >> 52) & 0x7ff);
-  const int e = ex - (1023 - 127);
-  const unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
-  const unsigned long long rounded = mant + 0xFFFFFFFull + ((mant >> 29) & 1ull);
-  // a mantissa carry (rounded >> 29 == 2^23) increments the exponent field
-  unsigned bits = ((unsigned)e << 23) + (unsigned)(rounded >> 29);
-  bits = e <= 0 ? 0u : bits;
-  const unsigned special = 0x7f800000u | ((ex == 0x7ff && mant != 0ull) ? 0x400000u : 0u);
-  bits = e >= 255 ? special : bits;
-  return __uint_as_float(sign | bits);
-}
-
-__device__ __forceinline__ double f32_to_f64(float f) {
-  const unsigned b = __float_as_uint(f);
-  const unsigned e = (b >> 23) & 0xffu;
-  const unsigned long long m = (unsigned long long)(b & 0x7fffffu) << 29;
-  unsigned long long r = ((unsigned long long)(e + (1023u - 127u)) << 52) | m;
-  r = e == 0u ? 0ull : r;
-  r = e == 0xffu ? ((0x7ffull << 52) | m) : r;
-  return __longlong_as_double((long long)(r | ((unsigned long long)(b & 0x80000000u) << 32)));
-}
-
-// x != 0 on the bit pattern.
-__device__ __forceinline__ bool nonzero64(double x) {
-  return (__double_as_longlong(x) << 1) != 0;
-}
-
-// x < 0 for a finite or infinite double, tested on the bit pattern.
-__device__ __forceinline__ bool negative64(double x) {
-  const long long b = __double_as_longlong(x);
-  return b < 0 && (b << 1) != 0;
-}
-
-// isfinite on the bit pattern (exponent field not all ones).
-__device__ __forceinline__ bool finite64(double x) {
-  return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff;
-}
-
 __device__ __forceinline__ void given_value(const BcDev &bc, const double *x,
                                             double t, double *g) {
   const double *src = bc.a;

@@ -110,6 +110,11 @@ struct Modal {
   double4 *fshift = nullptr;        // [faces] periodic shift: sharer sees x - shift
   double *taylor = nullptr;         // [cells][M][K] Taylor coefficients of a stage input
   double *values = nullptr;         // [volume points][K] scratch of mcfd_project
+  // mixed form: FP32 copies for the contractions
+  float *s32 = nullptr;             // [cells][M (M + 1) / 2]
+  float4 *vol32 = nullptr;          // [volume points] x - centre, global weight
+  float4 *foff32 = nullptr;         // [face points][2] x - centre (holder), x - shift - centre (sharer)
+  float *taylor32 = nullptr;        // [cells][M][K]
   std::vector<double> host_points;  // [volume points][3] global coordinates
 };
 

@@ -43,9 +43,9 @@ struct ModalCfg {
 
 // Taylor monomials at offset (x, y, z) in the reference's order
 // (basis/taylor.hpp:198-218).
-template <int M>
-__device__ __forceinline__ void taylor_values(double x, double y, double z, double *t) {
-  t[0] = 1.0;
+template <int M, class Real>
+__device__ __forceinline__ void taylor_values(Real x, Real y, Real z, Real *t) {
+  t[0] = Real(1);
   t[1] = x; t[2] = y; t[3] = z;
   if constexpr (M >= 10) {
     t[4] = x * x; t[5] = x * y; t[6] = x * z;
@@ -62,9 +62,9 @@ __device__ __forceinline__ void taylor_values(double x, double y, double z, doub
 // rt[j] += gx dT_j/dx + gy dT_j/dy + gz dT_j/dz at offset (x, y, z), t the
 // monomial values there (basis/taylor.hpp:387-472).
 // `rt(j)` yields the accumulator of monomial j (registers or shared memory).
-template <int M, class R>
-__device__ __forceinline__ void add_gradient(const double *t, double gx, double gy,
-                                             double gz, R &&rt) {
+template <int M, class Real, class R>
+__device__ __forceinline__ void add_gradient(const Real *t, Real gx, Real gy, Real gz,
+                                             R &&rt) {
   rt(1) += gx;
   rt(2) += gy;
   rt(3) += gz;
@@ -133,11 +133,11 @@ struct ModalFaceArgs {
   CaseView cs;
 };
 
-template <int M>
-__device__ __forceinline__ void eval_taylor(const double *a, const double *t, double *u) {
+template <int M, class Real>
+__device__ __forceinline__ void eval_taylor(const Real *a, const Real *t, Real *u) {
 #pragma unroll
   for (int k = 0; k < kK; ++k) {
-    double s = 0;
+    Real s = 0;
 #pragma unroll
     for (int j = 0; j < M; ++j) s += a[j * kK + k] * t[j];
     u[k] = s;
@@ -437,6 +437,321 @@ modal_project_kernel(const double *values, const double *s, const int32_t *vol_o
   u[gid] = acc;
 }
 
+// ---------------------------------------------------------------------------
+// Mixed form: the contractions (Taylor coefficients, values at quadrature
+// points, volume flux, residual accumulation, S Rt) in FP32 on FP32 copies of
+// S and of the point offsets; FP64 for the face states handed to the Riemann
+// solver, the Riemann / boundary flux itself, the positivity decisions of the
+// face states and the RK accumulation u + dt R and combinations.  FP64 <-> FP32
+// conversions run on the integer pipes (f64_to_f32 / f32_to_f64).
+
+// a32 = S^T c in FP32, one thread per (cell, component)
+template <int M>
+__global__ void __launch_bounds__(256)
+modal_taylor32_kernel(const double *u, const float *s32, float *a32, int64_t n) {
+  constexpr int KM = kK * M, NS = M * (M + 1) / 2;
+  int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= n) return;
+  const int64_t c = gid / kK;
+  const int k = (int)(gid - c * kK);
+  const double *uc = u + c * KM;
+  const float *sc = s32 + c * NS;
+  float cf[M];
+#pragma unroll
+  for (int m = 0; m < M; ++m) cf[m] = f64_to_f32(uc[m * kK + k]);
+  float *ac = a32 + c * KM;
+#pragma unroll
+  for (int j = 0; j < M; ++j) {
+    float acc = 0.f;
+#pragma unroll
+    for (int m = j; m < M; ++m) acc = fmaf(sc[m * (m + 1) / 2 + j], cf[m], acc);
+    ac[j * kK + k] = acc;
+  }
+}
+
+struct ModalFace32Args {
+  const float *taylor32;
+  const int2 *face_cells;
+  const int32_t *face_group;
+  const int32_t *point_face;
+  const double4 *fpt, *fnrm;
+  const float4 *foff32;
+  const BcDev *bcs;
+  float *flux32;
+  DevState *state;
+  double stage_c;
+  int64_t n_points;
+  int n_groups;
+  CaseView cs;
+};
+
+template <int M, int R>
+__global__ void __launch_bounds__(256) modal_face32_kernel(ModalFace32Args a) {
+  int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= a.n_points) return;
+  const int f = a.point_face[gid];
+  const int2 cells = a.face_cells[f];
+  const double4 x = a.fpt[gid];
+  const double4 nv = a.fnrm[gid];
+  const double n[3] = {nv.x, nv.y, nv.z};
+  const float4 oh = a.foff32[gid * 2];
+  float t[M], v[kK];
+  double uh[kK], out[kK];
+  taylor_values<M, float>(oh.x, oh.y, oh.z, t);
+  eval_taylor<M, float>(a.taylor32 + (int64_t)cells.x * M * kK, t, v);
+#pragma unroll
+  for (int k = 0; k < kK; ++k) uh[k] = f32_to_f64(v[k]);
+  bool not_converged = false;
+  Prim l = cons_to_prim(uh[0], uh[1], uh[2], uh[3], uh[4]);
+  if (cells.y >= 0) {
+    const float4 os = a.foff32[gid * 2 + 1];
+    double us[kK];
+    taylor_values<M, float>(os.x, os.y, os.z, t);
+    eval_taylor<M, float>(a.taylor32 + (int64_t)cells.y * M * kK, t, v);
+#pragma unroll
+    for (int k = 0; k < kK; ++k) us[k] = f32_to_f64(v[k]);
+    Prim r = cons_to_prim(us[0], us[1], us[2], us[3], us[4]);
+    flux_upwind<R>(l, r, n, out, &not_converged);
+  } else {
+    const int grp = a.face_group[f];
+    if (grp >= 0 && grp < a.n_groups && a.bcs[grp].kind != kBcNone) {
+      const BcDev &bc = a.bcs[grp];
+      double given[kK];
+      double tt = a.state->t + a.stage_c * a.state->dt;
+      if (a.cs.t) {
+        const int k = a.cs.cell_case[cells.x];
+        tt = a.cs.t[k] + a.stage_c * a.cs.dt[k];
+      }
+      modal_given(bc, x.x, x.y, x.z, tt, given);
+      flux_boundary<R>(bc.kind, l, given, n, out, &not_converged);
+    } else {
+#pragma unroll
+      for (int k = 0; k < kK; ++k) out[k] = 0;
+    }
+  }
+  if (not_converged) atomicOr(&a.state->status, (unsigned)kStatusNotConverged);
+  float *dst = a.flux32 + gid * kK;
+#pragma unroll
+  for (int k = 0; k < kK; ++k) dst[k] = f64_to_f32(out[k] * x.w);
+}
+
+struct ModalCell32Args {
+  const double *u_in, *u0;
+  double *u_out;
+  const float *taylor32;
+  const float *s32;
+  const int32_t *vol_off;
+  const float4 *vol32;
+  const int32_t *cell_faces;
+  const int32_t *face_off;
+  const float4 *foff32;
+  const float *flux32;
+  DevState *state;
+  int64_t n_cells;
+  int advance_time;
+  CaseView cs;
+};
+
+template <int M>
+struct ModalCfg32 {
+  static constexpr int kBlock = 64;
+};
+
+template <int M, int STAGE>
+__global__ void __launch_bounds__(ModalCfg32<M>::kBlock) modal_cell32_kernel(ModalCell32Args a) {
+  constexpr int KM = kK * M, NS = M * (M + 1) / 2, B = ModalCfg32<M>::kBlock;
+  __shared__ float s_a[KM][B];  // thread-private Taylor coefficients
+  const int tid = threadIdx.x;
+  const int64_t c = (int64_t)blockIdx.x * B + tid;
+  if (c >= a.n_cells) return;
+  {
+    const float *ac = a.taylor32 + c * KM;
+#pragma unroll
+    for (int i = 0; i < KM; ++i) s_a[i][tid] = ac[i];
+  }
+  float rt[kK][M];
+#pragma unroll
+  for (int k = 0; k < kK; ++k)
+#pragma unroll
+    for (int j = 0; j < M; ++j) rt[k][j] = 0.f;
+  // volume: sum_q w F(u_q) . grad T(x_q), all FP32 (types.hpp:288-333 with
+  // the positivity clamp)
+  const int q0 = a.vol_off[c], q1 = a.vol_off[c + 1];
+  for (int q = q0; q < q1; ++q) {
+    const float4 g = a.vol32[q];
+    float t[M], u[kK];
+    taylor_values<M, float>(g.x, g.y, g.z, t);
+#pragma unroll
+    for (int k = 0; k < kK; ++k) {
+      float s = 0.f;
+#pragma unroll
+      for (int j = 0; j < M; ++j) s = fmaf(s_a[j * kK + k][tid], t[j], s);
+      u[k] = s;
+    }
+    float rho = u[0], vx = u[1], vy = u[2], vz = u[3], p = u[4];
+    if (u[0] < 0.f || u[4] < 0.f) {
+      rho = vx = vy = vz = p = 0.f;
+    } else if (u[0] != 0.f) {
+      const float inv = 1.0f / u[0];
+      vx = u[1] * inv; vy = u[2] * inv; vz = u[3] * inv;
+      p = (u[4] - u[0] * (0.5f * (vx * vx + vy * vy + vz * vz))) * (float)kGm1;
+      if (p < 0.f) rho = vx = vy = vz = p = 0.f;
+    }
+    const bool converted = rho != 0.f;
+    const float vel[3] = {vx, vy, vz};
+    float f[kK][3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      f[0][d] = converted ? rho * vel[d] : u[1 + d];
+      f[1][d] = u[1] * vel[d] + (d == 0 ? p : 0.f);
+      f[2][d] = u[2] * vel[d] + (d == 1 ? p : 0.f);
+      f[3][d] = u[3] * vel[d] + (d == 2 ? p : 0.f);
+      f[4][d] = (u[4] + p) * vel[d];
+    }
+#pragma unroll
+    for (int k = 0; k < kK; ++k)
+      add_gradient<M, float>(t, f[k][0] * g.w, f[k][1] * g.w, f[k][2] * g.w,
+                             [&](int j) -> float & { return rt[k][j]; });
+  }
+  // faces: holder -= w F^ T, sharer += w F^ T (FP32 lift of the FP64 flux)
+  for (int slot = 0; slot < 6; ++slot) {
+    const int code = a.cell_faces[c * 6 + slot];
+    if (code < 0) continue;
+    const int f = code >> 1;
+    const int side = code & 1;
+    const int p0 = a.face_off[f], p1 = a.face_off[f + 1];
+    for (int p = p0; p < p1; ++p) {
+      const float4 o = a.foff32[(int64_t)p * 2 + side];
+      float t[M];
+      taylor_values<M, float>(o.x, o.y, o.z, t);
+      const float *fl = a.flux32 + (int64_t)p * kK;
+#pragma unroll
+      for (int k = 0; k < kK; ++k) {
+        const float v = side ? fl[k] : -fl[k];
+#pragma unroll
+        for (int j = 0; j < M; ++j) rt[k][j] = fmaf(v, t[j], rt[k][j]);
+      }
+    }
+  }
+  // R = S Rt in FP32; u + dt R and the RK combinations in FP64
+  const float *sc = a.s32 + c * NS;
+  const double *uin = a.u_in + c * KM;
+  double *out = a.u_out + c * KM;
+  const double dt = STAGE == kStageResidual ? 0.0
+                    : (a.cs.dt ? a.cs.dt[a.cs.cell_case[c]] : a.state->dt);
+  const float dt32 = f64_to_f32(dt);
+  bool bad = false;
+#pragma unroll
+  for (int m = 0; m < M; ++m) {
+    float srow[M];
+#pragma unroll
+    for (int j = 0; j <= m; ++j) srow[j] = sc[m * (m + 1) / 2 + j];
+#pragma unroll
+    for (int k = 0; k < kK; ++k) {
+      float r = 0.f;
+#pragma unroll
+      for (int j = 0; j <= m; ++j) r = fmaf(srow[j], rt[k][j], r);
+      double v;
+      if (STAGE == kStageResidual) {
+        v = f32_to_f64(r);
+      } else {
+        const double next = uin[m * kK + k] + f32_to_f64(r * dt32);
+        if (STAGE == kStageEuler) {
+          v = next;
+        } else if (STAGE == kStageRk2Last) {
+          v = (next + a.u0[c * KM + m * kK + k]) * 0.5;
+        } else if (STAGE == kStageRk3Mid) {
+          v = (a.u0[c * KM + m * kK + k] * 3 + next) * 0.25;
+        } else {
+          v = (next * 2 + a.u0[c * KM + m * kK + k]) * (1.0 / 3.0);
+        }
+      }
+      bad |= !finite64(v);
+      out[m * kK + k] = v;
+    }
+  }
+  if (bad) atomicOr(&a.state->status, (unsigned)kStatusNonFinite);
+  if (a.advance_time && !a.cs.dt && c == 0) a.state->t += a.state->dt;
+}
+
+// Mixed-form time step: values at the first M quadrature points from the
+// FP32 Taylor coefficients, wave speeds in FP32.
+template <int M>
+__global__ void __launch_bounds__(256)
+modal_dt32_kernel(const float *taylor32, const double4 *center, const int32_t *vol_off,
+                  const float4 *vol32, int64_t n_cells, DevState *state,
+                  const int32_t *cell_case, unsigned long long *case_rate) {
+  constexpr int KM = kK * M;
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double rate = 0;
+  if (c < n_cells) {
+    const float *ac = taylor32 + c * KM;
+    float max_speed = 1e-5f;
+    const int q0 = vol_off[c];
+    for (int i = 0; i < M; ++i) {
+      const float4 g = vol32[q0 + i];
+      float t[M], v[kK];
+      taylor_values<M, float>(g.x, g.y, g.z, t);
+      eval_taylor<M, float>(ac, t, v);
+      float speed = 0.f;
+      if (v[0] > 0.f && v[4] >= 0.f) {
+        const float inv = 1.0f / v[0];
+        const float uu = (v[1] * v[1] + v[2] * v[2] + v[3] * v[3]) * inv * inv;
+        const float pp = (v[4] - 0.5f * v[0] * uu) * (float)kGm1;
+        const float cs = pp > 0.f ? sqrtf((float)kGamma * pp * inv) : 0.f;
+        speed = pp >= 0.f ? cs + sqrtf(uu) : 0.f;
+      } else if (v[0] == 0.f && v[4] >= 0.f) {
+        speed = sqrtf(v[1] * v[1] + v[2] * v[2] + v[3] * v[3]);
+      }
+      max_speed = fmaxf(max_speed, speed);
+    }
+    rate = (double)max_speed * center[c].w;
+  }
+  reduce_cell_rate(rate, c, n_cells, state, cell_case, case_rate);
+}
+
+template <int M>
+int taylor32_launch(mcfd_handle *h, const double *u) {
+  const int64_t n = h->mesh.n_cells * kK;
+  modal_taylor32_kernel<M><<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(
+      u, h->modal.s32, h->modal.taylor32, n);
+  return 1;
+}
+
+template <int M, int R>
+void modal_face32_launch(mcfd_handle *h, const ModalFace32Args &fa) {
+  modal_face32_kernel<M, R><<<(unsigned)((fa.n_points + 255) / 256), 256, 0, h->stream>>>(fa);
+}
+
+template <int M>
+void modal_face32_dispatch(mcfd_handle *h, const ModalFace32Args &fa) {
+  switch (h->opt.riemann) {
+    case kExact: modal_face32_launch<M, kExact>(h, fa); break;
+    case kHllc: modal_face32_launch<M, kHllc>(h, fa); break;
+    case kAusm: modal_face32_launch<M, kAusm>(h, fa); break;
+    case kRoe: modal_face32_launch<M, kRoe>(h, fa); break;
+    default: modal_face32_launch<M, kRusanov>(h, fa); break;
+  }
+}
+
+template <int M, int S>
+void modal_cell32_launch(mcfd_handle *h, const ModalCell32Args &ca) {
+  constexpr int B = ModalCfg32<M>::kBlock;
+  const int64_t blocks = (ca.n_cells + B - 1) / B;
+  modal_cell32_kernel<M, S><<<(unsigned)blocks, B, 0, h->stream>>>(ca);
+}
+
+template <int M>
+void modal_cell32_dispatch(mcfd_handle *h, int stage, const ModalCell32Args &ca) {
+  switch (stage) {
+    case kStageEuler: modal_cell32_launch<M, kStageEuler>(h, ca); break;
+    case kStageRk2Last: modal_cell32_launch<M, kStageRk2Last>(h, ca); break;
+    case kStageRk3Mid: modal_cell32_launch<M, kStageRk3Mid>(h, ca); break;
+    case kStageRk3Last: modal_cell32_launch<M, kStageRk3Last>(h, ca); break;
+    default: modal_cell32_launch<M, kStageResidual>(h, ca); break;
+  }
+}
+
 template <int M>
 int taylor_launch(mcfd_handle *h, const double *u) {
   const int64_t n = h->mesh.n_cells * kK * M;
@@ -486,6 +801,23 @@ int launch_modal_face_flux(mcfd_handle *h, const double *u, double stage_c) {
   const Mesh &m = h->mesh;
   const Modal &md = h->modal;
   int n = 0;
+  if (h->opt.precision == 1) {
+    switch (md.m) {
+      case 4: n += taylor32_launch<4>(h, u); break;
+      case 10: n += taylor32_launch<10>(h, u); break;
+      default: n += taylor32_launch<20>(h, u); break;
+    }
+    if (md.n_fpts == 0) return n;
+    ModalFace32Args fa{md.taylor32, m.face_cells, m.face_group, md.point_face, md.fpt, md.fnrm,
+                       md.foff32, m.bcs, reinterpret_cast<float *>(h->buf.flux), h->buf.state,
+                       stage_c, md.n_fpts, m.n_groups, case_view(h)};
+    switch (md.m) {
+      case 4: modal_face32_dispatch<4>(h, fa); break;
+      case 10: modal_face32_dispatch<10>(h, fa); break;
+      default: modal_face32_dispatch<20>(h, fa); break;
+    }
+    return n + 1;
+  }
   switch (md.m) {
     case 4: n += taylor_launch<4>(h, u); break;
     case 10: n += taylor_launch<10>(h, u); break;
@@ -506,6 +838,18 @@ int launch_modal_face_flux(mcfd_handle *h, const double *u, double stage_c) {
 int launch_modal_cell_update(mcfd_handle *h, int stage, const double *u_in,
                              const double *u0, double *u_out, int advance_time) {
   const Modal &md = h->modal;
+  if (h->opt.precision == 1) {
+    ModalCell32Args ca{u_in, u0, u_out, md.taylor32, md.s32, md.vol_off, md.vol32,
+                       md.cell_faces, md.face_off, md.foff32,
+                       reinterpret_cast<const float *>(h->buf.flux), h->buf.state,
+                       h->mesh.n_cells, advance_time, case_view(h)};
+    switch (md.m) {
+      case 4: modal_cell32_dispatch<4>(h, stage, ca); break;
+      case 10: modal_cell32_dispatch<10>(h, stage, ca); break;
+      default: modal_cell32_dispatch<20>(h, stage, ca); break;
+    }
+    return 1;
+  }
   ModalCellArgs ca{u_in, u0, u_out, md.taylor, md.s, md.center, md.vol_off, md.vol,
                    md.cell_faces, md.face_off, md.fpt, md.fshift, h->buf.flux,
                    h->buf.state, h->mesh.n_cells, advance_time, case_view(h)};
@@ -523,6 +867,18 @@ int launch_modal_dt(mcfd_handle *h, const double *u) {
   const unsigned blocks = (unsigned)((C + 255) / 256);
   const int32_t *cc = h->cases.cell_case;
   unsigned long long *cr = h->cases.n ? h->cases.rate : nullptr;
+  if (h->opt.precision == 1) {
+    int n = 0;
+    switch (md.m) {
+      case 4: n += taylor32_launch<4>(h, u);
+        modal_dt32_kernel<4><<<blocks, 256, 0, h->stream>>>(md.taylor32, md.center, md.vol_off, md.vol32, C, h->buf.state, cc, cr); break;
+      case 10: n += taylor32_launch<10>(h, u);
+        modal_dt32_kernel<10><<<blocks, 256, 0, h->stream>>>(md.taylor32, md.center, md.vol_off, md.vol32, C, h->buf.state, cc, cr); break;
+      default: n += taylor32_launch<20>(h, u);
+        modal_dt32_kernel<20><<<blocks, 256, 0, h->stream>>>(md.taylor32, md.center, md.vol_off, md.vol32, C, h->buf.state, cc, cr); break;
+    }
+    return n + 1 + launch_dt_finalize(h);
+  }
   // values at the first M quadrature points: c . psi(x_i) up to M = 10; at
   // M = 20 through the Taylor coefficients (3050 instead of 6200 FMAs per cell)
   switch (md.m) {

@@ -444,6 +444,35 @@ int build_modal_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
   if ((rc = upload(h, &md.fshift, fshift))) return rc;
   if ((rc = upload(h, &m.face_cells, fcells))) return rc;
   if ((rc = upload(h, &m.face_group, fgroup))) return rc;
+  if (h->opt.precision == MCFD_MIXED) {
+    // FP32 copies for the mixed form's contractions
+    std::vector<float> s32(S.size());
+    for (size_t i = 0; i < S.size(); ++i) s32[i] = (float)S[i];
+    std::vector<float4> vol32(NV);
+    for (int64_t q = 0; q < NV; ++q)
+      vol32[q] = make_float4((float)vol[q].x, (float)vol[q].y, (float)vol[q].z, (float)vol[q].w);
+    std::vector<float4> foff32((size_t)NF * 2);
+#pragma omp parallel for schedule(static)
+    for (int64_t f = 0; f < F; ++f) {
+      const int64_t hc = fcells[f].x, sc = fcells[f].y;
+      for (int32_t q = face_off[f]; q < face_off[f + 1]; ++q) {
+        const double4 x = fpt[q];
+        foff32[(size_t)q * 2] = make_float4((float)(x.x - center[hc].x), (float)(x.y - center[hc].y),
+                                            (float)(x.z - center[hc].z), 0.f);
+        if (sc >= 0)
+          foff32[(size_t)q * 2 + 1] =
+              make_float4((float)((x.x - fshift[f].x) - center[sc].x), (float)((x.y - fshift[f].y) - center[sc].y),
+                          (float)((x.z - fshift[f].z) - center[sc].z), 0.f);
+        else
+          foff32[(size_t)q * 2 + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+    if ((rc = upload(h, &md.s32, s32))) return rc;
+    if ((rc = upload(h, &md.vol32, vol32))) return rc;
+    if ((rc = upload(h, &md.foff32, foff32))) return rc;
+    cudaError_t e32 = cudaMalloc(&md.taylor32, sizeof(float) * m.column);
+    if (e32 != cudaSuccess) return fail(h, MCFD_ERR_CUDA, std::string("modal tables: ") + cudaGetErrorString(e32));
+  }
   cudaError_t e = cudaMalloc(&md.taylor, sizeof(double) * m.column);
   if (e != cudaSuccess) return fail(h, MCFD_ERR_CUDA, std::string("modal tables: ") + cudaGetErrorString(e));
   m.host_bcs.assign(std::max(m.n_groups, 1), BcDev{});

@@ -282,8 +282,12 @@ class General(Lobatto):
     coefficients on the cell's orthonormal Taylor basis (m-major)."""
 
     def __init__(self, mesh: Mesh, degree: int, riemann: str | int = "rusanov",
-                 cfl: float = 0.0, device: int = 0):
-        super().__init__(mesh, degree, riemann, cfl=cfl, device=device, scheme="modal")
+                 cfl: float = 0.0, device: int = 0, precision: str = "fp64"):
+        """precision: "fp64", or "mixed" (FP32 contractions on FP32 copies of
+        the basis and point offsets; FP64 face states, Riemann fluxes and RK
+        accumulation)."""
+        super().__init__(mesh, degree, riemann, cfl=cfl, device=device, scheme="modal",
+                         precision=precision)
         self.n_points = int(self._lib.mcfd_point_count(self._h))
 
     def points(self) -> np.ndarray:

@@ -144,4 +144,35 @@ def test_modal_rejections(gpu):
     with pytest.raises(capi.McfdError):
         Lobatto(hexes, 2, limiter="lazy", scheme="modal")
     with pytest.raises(capi.McfdError):
-        Lobatto(hexes, 2, precision="mixed", scheme="modal")
+        Lobatto(hexes, 2, precision="mixed", limiter="lazy", scheme="modal")
+
+
+@pytest.mark.parametrize("kind", ["hex", "tet", "mixed"])
+@pytest.mark.parametrize("p", [1, 2, 3])
+def test_modal_mixed_form_accuracy(gpu, kind, p):
+    """Mixed modal form (FP32 contractions, FP64 Riemann and RK): residual
+    within 1e-4 of the oracle (the residual of this near-uniform field is
+    ~1e-3 of the fluxes whose FP32 contraction error it inherits), and 20
+    SSP-RK3 steps within 1e-6 density L2 of the FP64 GPU path (the bar of the
+    mixed form)."""
+    m = make_mesh(kind, (True, True, True), seed=3)
+    o = orc.Modal(m, p)
+    x, _ = o.points()
+    u0 = o.project(smooth_values(x, 5))
+    s = General(m, p, "hllc", precision="mixed")
+    s.SetSolutionColumn(u0)
+    r = s.GetResidualColumn()
+    assert rel_l2(r, o.residual(orc.HLLC, u0)) < 1e-4
+    out = {}
+    for prec in ("fp64", "mixed"):
+        sys_ = General(m, p, "hllc", precision=prec)
+        sys_.SetSolutionColumn(u0)
+        t = sys_.advance(20, 1e9, 3, 0.0)
+        out[prec] = (sys_.GetSolutionColumn(), t)
+        sys_.close()
+    a = out["mixed"][0].reshape(-1, 5)
+    b = out["fp64"][0].reshape(-1, 5)
+    # density coefficients on the orthonormal basis: their L2 is the field's L2
+    assert np.linalg.norm(a[:, 0] - b[:, 0]) / np.linalg.norm(b[:, 0]) <= 1e-6
+    assert abs(out["mixed"][1] - out["fp64"][1]) <= 1e-6 * out["fp64"][1]
+    s.close()
