@@ -64,8 +64,14 @@ struct Prim {
   double rinv;  // 1 / rho when rho > 0, else 0 (saves divisions downstream)
 };
 
+#ifdef __CUDA_ARCH__
+__device__ __forceinline__ double rcp_newton(double x);
+#else
+inline double rcp_newton(double x);
+#endif
+
 MCFD_HD Prim make_prim(double rho, double u, double v, double w, double p) {
-  return Prim{rho, u, v, w, p, rho > 0 ? 1.0 / rho : 0.0};
+  return Prim{rho, u, v, w, p, rho > 0 ? rcp_newton(rho) : 0.0};
 }
 
 // ConservativeToPrimitive with SetZeroIfNegative (types.hpp:194-202,288-301):
@@ -77,7 +83,7 @@ MCFD_HD Prim cons_to_prim(double r, double mx, double my, double mz,
   Prim w{r, mx, my, mz, e, 0.0};
   if (r < 0 || e < 0) return Prim{0, 0, 0, 0, 0, 0};
   if (r != 0) {
-    double inv = 1.0 / r;
+    double inv = rcp_newton(r);
     w.rinv = inv;
     w.u = mx * inv;
     w.v = my * inv;
@@ -216,8 +222,15 @@ __device__ __forceinline__ bool bits_negative(double x) {
   const long long b = __double_as_longlong(x);
   return b < 0 && (b << 1) != 0;
 }
+// 1/x of either sign: rcp_newton of |x| with x's sign.
+__device__ __forceinline__ double rcp_signed(double x) {
+  const long long b = __double_as_longlong(x);
+  const double y = rcp_newton(__longlong_as_double(b & 0x7fffffffffffffffll));
+  return __longlong_as_double(__double_as_longlong(y) ^ (b & (long long)0x8000000000000000ull));
+}
 #else
 inline double rcp_newton(double x) { return 1.0 / x; }
+inline double rcp_signed(double x) { return 1.0 / x; }
 inline double sqrt_seeded(double x) { return std::sqrt(x); }
 inline bool bits_positive(double x) { return x > 0; }
 inline bool bits_negative(double x) { return x < 0; }
@@ -385,16 +398,16 @@ MCFD_HD void flux_rusanov_traced_weighted(const double *cl, const double *trl,
 // the side it is built on.
 MCFD_HD double hllc_q(double p_estimate, double p_k) {
   if (p_estimate <= p_k) return 1.0;
-  double temp = 1 + kGp1Over2 * (p_estimate / p_k - 1) / kGamma;
+  double temp = 1 + kGp1Over2 * (p_estimate * rcp_newton(p_k) - 1) * kOneOverGamma;
   return sqrt(temp);
 }
 
 MCFD_HD void hllc_star(const Prim &s, double un, double e, const double *n,
                        double wave_k, double wave_star, double *f) {
   normal_flux(s, e, n, un, f);
-  double temp = s.rho * (wave_k - un) / (wave_k - wave_star);
-  double es = e / s.rho + (wave_star - un) *
-      (wave_star + s.p / (s.rho * (wave_k - un)));
+  double temp = s.rho * (wave_k - un) * rcp_signed(wave_k - wave_star);
+  double es = e * s.rinv + (wave_star - un) *
+      (wave_star + s.p * rcp_signed(s.rho * (wave_k - un)));
   es *= temp;
   // star momentum = temp * (wave_star n + u_t), u_t = u - un n
   double dm = temp * (wave_star - un);
@@ -420,8 +433,8 @@ MCFD_HD void flux_hllc(const Prim &l, const Prim &r, const double *n,
   double wave_left = unl - a_left * hllc_q(p_estimate, l.p);
   double wave_right = unr + a_right * hllc_q(p_estimate, r.p);
   double wave_star = (r.p - l.p + l.rho * unl * (wave_left - unl) -
-                      r.rho * unr * (wave_right - unr)) /
-                     (l.rho * (wave_left - unl) - r.rho * (wave_right - unr));
+                      r.rho * unr * (wave_right - unr)) *
+                     rcp_signed(l.rho * (wave_left - unl) - r.rho * (wave_right - unr));
   if (0.0 <= wave_left) {
     normal_flux(l, prim_energy(l), n, unl, f);
   } else if (wave_right <= 0.0) {
@@ -483,7 +496,7 @@ MCFD_HD void flux_roe(const Prim &l, const Prim &r, const double *n,
   double h0_l = kGammaOverGm1 * l.p * l.rinv + kinetic(l);
   double h0_r = kGammaOverGm1 * r.p * r.rinv + kinetic(r);
   double sl = sqrt(l.rho), sr = sqrt(r.rho);
-  double inv_sum = 1.0 / (sl + sr);
+  double inv_sum = rcp_newton(sl + sr);
   double rho = sl * sr;
   double u = (sl * l.u + sr * r.u) * inv_sum;
   double v = (sl * l.v + sr * r.v) * inv_sum;
@@ -496,7 +509,7 @@ MCFD_HD void flux_roe(const Prim &l, const Prim &r, const double *n,
   double ua = un * a;
   double p_jump = r.p - l.p;
   double u_jump = unr - unl;
-  double inv_2aa = 1.0 / (2 * aa);
+  double inv_2aa = rcp_newton(2 * aa);
   // wave u_n - a: r = (1, u - a n, h0 - u_n a)
   double s1 = 0.5 * ((p_jump - rho * a * u_jump) * inv_2aa) * fabs(un - a);
   // entropy wave u_n: r = (1, u, ke)
