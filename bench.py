@@ -178,6 +178,30 @@ def density_l2_vs_exact(sol, mesh, t):
     return float(math.sqrt(np.sum(w * (rho - rho_exact) ** 2) / np.sum(w * rho_exact ** 2)))
 
 
+def convergence(forms, device, dt_cfl, n_steps, finest):
+    """Density L2 against the exact vortex on 16^3, 32^3 and the timed mesh
+    after the same number of steps of one fixed dt (half the finest mesh's
+    CFL step, so every mesh runs the same times): the observed order of
+    both forms."""
+    from pvcriemannsolvers_gb300 import Lobatto, cases, mesh as meshlib
+    dt = 0.5 * dt_cfl
+    out = {"dt": dt, "steps": n_steps, "t_end": dt * n_steps}
+    sizes = [n for n in (16, 32) if n < finest] + [finest]
+    for form in forms:
+        errs = []
+        for n1d in sizes:
+            m = meshlib.box((n1d,) * 3, lengths=(10.0,) * 3, periodic=(True,) * 3)
+            s = Lobatto(m, DEGREE, "rusanov", cfl=CFL, device=device, precision=form)
+            s.SetSolutionColumn(cases.vortex_ic(meshlib.node_coordinates(m, DEGREE).reshape(-1, 3)).ravel())
+            t = s.advance(n_steps, dt, 3, 0.0)
+            errs.append(density_l2_vs_exact(s.GetSolutionColumn(), m, t))
+            s.close()
+        orders = [math.log2(errs[i] / errs[i + 1]) * math.log(2) / math.log(sizes[i + 1] / sizes[i])
+                  for i in range(len(errs) - 1)]
+        out[form] = {"cells_1d": sizes, "density_rel_l2_vs_exact": errs, "observed_order": orders}
+    return out
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -817,6 +841,8 @@ def run_gpu(args, rank, world, local_rank):
         a, b = res["mixed"]["solution"].reshape(-1, K)[:, 0], res["fp64"]["solution"].reshape(-1, K)[:, 0]
         accuracy["mixed_vs_fp64_density_rel_l2"] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
         accuracy["fp64_density_rel_l2_vs_exact"] = density_l2_vs_exact(res["fp64"]["solution"], m, res["fp64"]["t"])
+    accuracy["convergence"] = convergence(forms, local_rank, r["t"] / (args.warmup + args.steps),
+                                          args.warmup + args.steps, args.cells)
     hbm_peak, peak_src = measured_peaks()
     fp64_peak = fp64_peak_tflops(torch, dev)
     cpu = None
