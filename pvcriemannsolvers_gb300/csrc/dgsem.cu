@@ -54,7 +54,23 @@ struct FaceArgs {
   int fr;  // flux reconstruction: mark faces without a boundary condition
   CaseView cs;
   const double *trace;  // node traces of u (Rusanov), or null
+  int f32_out;          // mixed form: the flux buffer holds FP32 values
 };
+
+// Face-point flux store: FP64, or FP32 for the mixed form's FP32 lift (one
+// conversion per face point instead of one per lifting cell).
+__device__ __forceinline__ void store_flux(double *flux, int f32_out, int64_t gid,
+                                           const double *v) {
+  if (f32_out) {
+    float *d = reinterpret_cast<float *>(flux) + gid * kK;
+#pragma unroll
+    for (int k = 0; k < kK; ++k) d[k] = f64_to_f32(v[k]);
+  } else {
+    double *d = flux + gid * kK;
+#pragma unroll
+    for (int k = 0; k < kK; ++k) d[k] = v[k];
+  }
+}
 
 // FR: a boundary face point without a registered boundary gets no correction
 // (the reference skips such faces); the face kernel marks its flux with this
@@ -141,9 +157,7 @@ __global__ void __launch_bounds__(256) face_flux_kernel(FaceArgs a) {
       } else {
         flux_rusanov_cons_weighted<FAST_SQRT>(ch, cs, n, g.w, out);
       }
-      double *dst = a.flux + gid * kK;
-#pragma unroll
-      for (int k = 0; k < kK; ++k) dst[k] = out[k];
+      store_flux(a.flux, a.f32_out, gid, out);
       return;
     } else {
       Prim l = cons_to_prim(ch[0], ch[1], ch[2], ch[3], ch[4]);
@@ -166,9 +180,9 @@ __global__ void __launch_bounds__(256) face_flux_kernel(FaceArgs a) {
     }
   }
   if (not_converged) atomicOr(&a.state->status, (unsigned)kStatusNotConverged);
-  double *dst = a.flux + gid * kK;
 #pragma unroll
-  for (int k = 0; k < kK; ++k) dst[k] = out[k] * g.w;
+  for (int k = 0; k < kK; ++k) out[k] *= g.w;
+  store_flux(a.flux, a.f32_out, gid, out);
 }
 
 template <int Q, int STAGE>
@@ -410,24 +424,25 @@ cell_update_mixed_kernel(CellArgs a, const float *__restrict__ geo32) {
     }
   }
   const int32_t *cf = a.cell_flux + c * 6 * QF;
-  const float g1 = f64_to_f32(a.g1);
+  const float g1 = a.fr ? f64_to_f32(a.g1) : 0.f;
   auto lift = [&](int side, int t) {
     int32_t vv = cf[side * QF + t];
     if (vv == INT32_MIN) return;
-    const double *fl = a.flux + (int64_t)(vv >= 0 ? vv : ~vv) * kK;
+    // FP32 face fluxes (the face kernel converts once per face point)
+    const float *fl = reinterpret_cast<const float *>(a.flux) + (int64_t)(vv >= 0 ? vv : ~vv) * kK;
     if (a.fr) {
-      const long long b0 = __double_as_longlong(fl[0]);
-      if (((b0 >> 52) & 0x7ff) == 0x7ff && (b0 & 0xFFFFFFFFFFFFFll)) return;  // no boundary
+      const unsigned b0 = __float_as_uint(fl[0]);
+      if (((b0 >> 23) & 0xffu) == 0xffu && (b0 & 0x7fffffu)) return;  // no boundary
       const int dir = fr_dir(side);
       const float sigma = fr_sign(side) > 0 ? 1.f : -1.f, out_sign = vv >= 0 ? 1.f : -1.f;
 #pragma unroll
       for (int rr = 0; rr < kK; ++rr)
-        res[rr] -= g1 * (out_sign * f64_to_f32(fl[rr]) - sigma * s_ft[lc][rr * 3 + dir][q]);
+        res[rr] -= g1 * (out_sign * fl[rr] - sigma * s_ft[lc][rr * 3 + dir][q]);
       return;
     }
     const float sign = vv >= 0 ? -1.f : 1.f;
 #pragma unroll
-    for (int rr = 0; rr < kK; ++rr) res[rr] = fmaf(sign, f64_to_f32(fl[rr]), res[rr]);
+    for (int rr = 0; rr < kK; ++rr) res[rr] = fmaf(sign, fl[rr], res[rr]);
   };
   if (k == 0) lift(0, i * Q + j);
   if (k == Q - 1) lift(5, i * Q + j);
@@ -702,7 +717,8 @@ int launch_face_flux(mcfd_handle *h, const double *u, double stage_c) {
   FaceArgs fa{u, m.face_cells, m.face_group, m.face_geo, m.face_xyz,
               m.face_map, m.bcs, h->buf.flux, h->buf.state, stage_c,
               m.n_points, m.n_groups, h->opt.scheme == 1, case_view(h),
-              (h->use_trace && h->trace_for == u) ? h->buf.trace : nullptr};
+              (h->use_trace && h->trace_for == u) ? h->buf.trace : nullptr,
+              h->opt.precision == 1};
   if (m.n_points == 0) return 0;
   switch (m.q) {
     case 2: face_dispatch_r<2>(h, fa); break;
@@ -835,7 +851,8 @@ int launch_residual_static_scratch(mcfd_handle *h, const double *d_u,
   const Mesh &m = h->mesh;
   FaceArgs fa{d_u, m.face_cells, m.face_group, m.face_geo, m.face_xyz,
               m.face_map, m.bcs, scratch, h->buf.state, 0.0,
-              m.n_points, m.n_groups, h->opt.scheme == 1, case_view(h), nullptr};
+              m.n_points, m.n_groups, h->opt.scheme == 1, case_view(h), nullptr,
+              h->opt.precision == 1};
   CellArgs ca{d_u, nullptr, d_r, m.cell_geo, m.cell_flux, scratch, m.dmat,
               h->buf.state, m.n_cells, 0, h->opt.scheme == 1, h->opt.fr_g1, case_view(h), nullptr};
   int n = 0;
