@@ -317,6 +317,18 @@ int mcfd_ensemble_destroy(mcfd_ensemble *e);
 int mcfd_ensemble_set_stream(mcfd_ensemble *e, void *cuda_stream);
 const char *mcfd_ensemble_last_error(const mcfd_ensemble *e);
 
+/* Launch-shape autotuner (no reference counterpart).  Times the candidate
+ * launch shapes of this handle's kernels on its own mesh and current solution
+ * (face-flux and dt-reduction block sizes 128 / 256 / 512; persistent limiter
+ * grid of 4 / 8 / 16 / 32 blocks per SM), keeps the fastest and re-captures
+ * the step graph on the next mcfd_advance.  With cache_path, the choice is
+ * first looked up in that file (one JSON object per line, keyed by scheme,
+ * degree, precision, solver, limiter and cell-count bucket) and otherwise
+ * appended to it.  choice (NULL or [4]): face block, dt block, limiter blocks
+ * per SM, 1 when taken from the cache.  Tune members before building an
+ * ensemble from them. */
+int mcfd_autotune(mcfd_handle *h, const char *cache_path, int32_t *choice);
+
 /* Message describing the last failure on this handle (or of mcfd_create when
  * h is NULL).  Valid until the next call on the handle. */
 const char *mcfd_last_error(const mcfd_handle *h);

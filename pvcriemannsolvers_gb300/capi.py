@@ -105,6 +105,7 @@ SIGNATURES = {
     "mcfd_ensemble_destroy": (C.c_int, [_P]),
     "mcfd_ensemble_set_stream": (C.c_int, [_P, _P]),
     "mcfd_ensemble_last_error": (C.c_char_p, [_P]),
+    "mcfd_autotune": (C.c_int, [_P, C.c_char_p, C.POINTER(C.c_int32)]),
     "mcfd_point_count": (C.c_int64, [_P]),
     "mcfd_points": (C.c_int, [_P, _D, C.c_int64]),
     "mcfd_project": (C.c_int, [_P, _D, C.c_int64]),

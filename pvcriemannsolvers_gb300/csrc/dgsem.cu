@@ -127,7 +127,7 @@ __device__ __forceinline__ void given_value(const BcDev &bc, const double *x,
 // FAST_SQRT (the mixed form): the Rusanov wave speed's square root from an
 // FP32 seed and one FP64 Newton step (sqrt_seeded, relative error ~1e-13).
 template <int Q, int R, bool FAST_SQRT>
-__global__ void __launch_bounds__(256) face_flux_kernel(FaceArgs a) {
+__global__ void __launch_bounds__(512) face_flux_kernel(FaceArgs a) {
   constexpr int QF = Q * Q, KN = kK * Q * Q * Q;
   int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= a.n_points) return;
@@ -514,7 +514,7 @@ __device__ __forceinline__ void reduce_rate(double rate, int key, DevState *stat
 }
 
 template <int Q>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(512)
 dt_reduce_kernel(const double *u, const double *cell_rate, int64_t n_nodes,
                  DevState *state, const int32_t *cell_case,
                  unsigned long long *case_rate) {
@@ -533,7 +533,7 @@ dt_reduce_kernel(const double *u, const double *cell_rate, int64_t n_nodes,
 
 // Mixed-precision dt reduction: wave speeds in FP32.
 template <int Q>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(512)
 dt_reduce_mixed_kernel(const double *u, const double *cell_rate, int64_t n_nodes,
                        DevState *state, const int32_t *cell_case,
                        unsigned long long *case_rate) {
@@ -645,14 +645,15 @@ __global__ void set_state_kernel(DevState *state, double t, double dt,
 
 template <int Q, int R>
 void face_launch(mcfd_handle *h, const FaceArgs &fa) {
-  int64_t blocks = (fa.n_points + 255) / 256;
+  const int bs = h->tune.face_block;
+  int64_t blocks = (fa.n_points + bs - 1) / bs;
   if constexpr (R == kRusanov) {
     if (h->opt.precision == 1) {
-      face_flux_kernel<Q, R, true><<<(unsigned)blocks, 256, 0, h->stream>>>(fa);
+      face_flux_kernel<Q, R, true><<<(unsigned)blocks, bs, 0, h->stream>>>(fa);
       return;
     }
   }
-  face_flux_kernel<Q, R, false><<<(unsigned)blocks, 256, 0, h->stream>>>(fa);
+  face_flux_kernel<Q, R, false><<<(unsigned)blocks, bs, 0, h->stream>>>(fa);
 }
 
 template <int Q>
@@ -762,20 +763,21 @@ int launch_dt(mcfd_handle *h, const double *u) {
   if (h->opt.scheme == kSchemeModal) return launch_modal_dt(h, u);
   const Mesh &m = h->mesh;
   int64_t nodes = m.n_cells * m.n;
-  unsigned blocks = (unsigned)((nodes + 255) / 256);
+  const int bs = h->tune.dt_block;
+  unsigned blocks = (unsigned)((nodes + bs - 1) / bs);
   const int32_t *cc = h->cases.cell_case;
   unsigned long long *cr = h->cases.n ? h->cases.rate : nullptr;
   if (h->opt.precision == 1) {
     switch (m.q) {
-      case 2: dt_reduce_mixed_kernel<2><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr); break;
-      case 3: dt_reduce_mixed_kernel<3><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr); break;
-      default: dt_reduce_mixed_kernel<4><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr); break;
+      case 2: dt_reduce_mixed_kernel<2><<<blocks, bs, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr); break;
+      case 3: dt_reduce_mixed_kernel<3><<<blocks, bs, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr); break;
+      default: dt_reduce_mixed_kernel<4><<<blocks, bs, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr); break;
     }
   } else {
     switch (m.q) {
-      case 2: dt_reduce_kernel<2><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr); break;
-      case 3: dt_reduce_kernel<3><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr); break;
-      default: dt_reduce_kernel<4><<<blocks, 256, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr); break;
+      case 2: dt_reduce_kernel<2><<<blocks, bs, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr); break;
+      case 3: dt_reduce_kernel<3><<<blocks, bs, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr); break;
+      default: dt_reduce_kernel<4><<<blocks, bs, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr); break;
     }
   }
   return 1 + launch_dt_finalize(h);

@@ -161,8 +161,19 @@ struct Options {
 
 }  // namespace mcfd
 
+namespace mcfd {
+// Launch shapes chosen by mcfd_autotune (defaults until it runs).
+struct Tune {
+  int face_block = 256;            // threads per block of the face kernels
+  int dt_block = 256;              // threads per block of the dt reductions
+  int limiter_blocks_per_sm = 16;  // persistent reconstruction grid width
+  bool tuned = false;
+};
+}  // namespace mcfd
+
 struct mcfd_handle {
   int device = 0;
+  mcfd::Tune tune;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   mcfd::Options opt;

@@ -145,7 +145,7 @@ __device__ __forceinline__ void eval_taylor(const Real *a, const Real *t, Real *
 }
 
 template <int M, int R>
-__global__ void __launch_bounds__(256) modal_face_kernel(ModalFaceArgs a) {
+__global__ void __launch_bounds__(512) modal_face_kernel(ModalFaceArgs a) {
   int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= a.n_points) return;
   const int f = a.point_face[gid];
@@ -351,7 +351,7 @@ __device__ __forceinline__ double point_speed(const double *v) {
 // (fem.hpp:417-435 with Projection::GetValue(i), projection.hpp:109-118):
 // the value as the reference forms it, c . (S T(x_i - centre))
 template <int M>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(512)
 modal_dt_basis_kernel(const double *u, const double *s, const double4 *center,
                       const int32_t *vol_off, const double4 *vol, int64_t n_cells,
                       DevState *state, const int32_t *cell_case, unsigned long long *case_rate) {
@@ -391,7 +391,7 @@ modal_dt_basis_kernel(const double *u, const double *s, const double4 *center,
 // The same maximum from the Taylor coefficients a = S^T c of the input:
 // u(x_i) = a . T(x_i - centre), reassociated (rounding-level difference).
 template <int M>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(512)
 modal_dt_kernel(const double *taylor, const double4 *center,
                 const int32_t *vol_off, const double4 *vol, int64_t n_cells,
                 DevState *state, const int32_t *cell_case, unsigned long long *case_rate) {
@@ -486,7 +486,7 @@ struct ModalFace32Args {
 };
 
 template <int M, int R>
-__global__ void __launch_bounds__(256) modal_face32_kernel(ModalFace32Args a) {
+__global__ void __launch_bounds__(512) modal_face32_kernel(ModalFace32Args a) {
   int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= a.n_points) return;
   const int f = a.point_face[gid];
@@ -677,7 +677,7 @@ __global__ void __launch_bounds__(ModalCfg32<M>::kBlock) modal_cell32_kernel(Mod
 // Mixed-form time step: values at the first M quadrature points from the
 // FP32 Taylor coefficients, wave speeds in FP32.
 template <int M>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(512)
 modal_dt32_kernel(const float *taylor32, const double4 *center, const int32_t *vol_off,
                   const float4 *vol32, int64_t n_cells, DevState *state,
                   const int32_t *cell_case, unsigned long long *case_rate) {
@@ -720,7 +720,8 @@ int taylor32_launch(mcfd_handle *h, const double *u) {
 
 template <int M, int R>
 void modal_face32_launch(mcfd_handle *h, const ModalFace32Args &fa) {
-  modal_face32_kernel<M, R><<<(unsigned)((fa.n_points + 255) / 256), 256, 0, h->stream>>>(fa);
+  const int bs = h->tune.face_block;
+  modal_face32_kernel<M, R><<<(unsigned)((fa.n_points + bs - 1) / bs), bs, 0, h->stream>>>(fa);
 }
 
 template <int M>
@@ -762,7 +763,8 @@ int taylor_launch(mcfd_handle *h, const double *u) {
 
 template <int M, int R>
 void modal_face_launch(mcfd_handle *h, const ModalFaceArgs &fa) {
-  modal_face_kernel<M, R><<<(unsigned)((fa.n_points + 255) / 256), 256, 0, h->stream>>>(fa);
+  const int bs = h->tune.face_block;
+  modal_face_kernel<M, R><<<(unsigned)((fa.n_points + bs - 1) / bs), bs, 0, h->stream>>>(fa);
 }
 
 template <int M>
@@ -864,29 +866,30 @@ int launch_modal_cell_update(mcfd_handle *h, int stage, const double *u_in,
 int launch_modal_dt(mcfd_handle *h, const double *u) {
   const Modal &md = h->modal;
   const int64_t C = h->mesh.n_cells;
-  const unsigned blocks = (unsigned)((C + 255) / 256);
+  const int bs = h->tune.dt_block;
+  const unsigned blocks = (unsigned)((C + bs - 1) / bs);
   const int32_t *cc = h->cases.cell_case;
   unsigned long long *cr = h->cases.n ? h->cases.rate : nullptr;
   if (h->opt.precision == 1) {
     int n = 0;
     switch (md.m) {
       case 4: n += taylor32_launch<4>(h, u);
-        modal_dt32_kernel<4><<<blocks, 256, 0, h->stream>>>(md.taylor32, md.center, md.vol_off, md.vol32, C, h->buf.state, cc, cr); break;
+        modal_dt32_kernel<4><<<blocks, bs, 0, h->stream>>>(md.taylor32, md.center, md.vol_off, md.vol32, C, h->buf.state, cc, cr); break;
       case 10: n += taylor32_launch<10>(h, u);
-        modal_dt32_kernel<10><<<blocks, 256, 0, h->stream>>>(md.taylor32, md.center, md.vol_off, md.vol32, C, h->buf.state, cc, cr); break;
+        modal_dt32_kernel<10><<<blocks, bs, 0, h->stream>>>(md.taylor32, md.center, md.vol_off, md.vol32, C, h->buf.state, cc, cr); break;
       default: n += taylor32_launch<20>(h, u);
-        modal_dt32_kernel<20><<<blocks, 256, 0, h->stream>>>(md.taylor32, md.center, md.vol_off, md.vol32, C, h->buf.state, cc, cr); break;
+        modal_dt32_kernel<20><<<blocks, bs, 0, h->stream>>>(md.taylor32, md.center, md.vol_off, md.vol32, C, h->buf.state, cc, cr); break;
     }
     return n + 1 + launch_dt_finalize(h);
   }
   // values at the first M quadrature points: c . psi(x_i) up to M = 10; at
   // M = 20 through the Taylor coefficients (3050 instead of 6200 FMAs per cell)
   switch (md.m) {
-    case 4: modal_dt_basis_kernel<4><<<blocks, 256, 0, h->stream>>>(u, md.s, md.center, md.vol_off, md.vol, C, h->buf.state, cc, cr); break;
-    case 10: modal_dt_basis_kernel<10><<<blocks, 256, 0, h->stream>>>(u, md.s, md.center, md.vol_off, md.vol, C, h->buf.state, cc, cr); break;
+    case 4: modal_dt_basis_kernel<4><<<blocks, bs, 0, h->stream>>>(u, md.s, md.center, md.vol_off, md.vol, C, h->buf.state, cc, cr); break;
+    case 10: modal_dt_basis_kernel<10><<<blocks, bs, 0, h->stream>>>(u, md.s, md.center, md.vol_off, md.vol, C, h->buf.state, cc, cr); break;
     default:
       taylor_launch<20>(h, u);
-      modal_dt_kernel<20><<<blocks, 256, 0, h->stream>>>(md.taylor, md.center, md.vol_off, md.vol, C, h->buf.state, cc, cr);
+      modal_dt_kernel<20><<<blocks, bs, 0, h->stream>>>(md.taylor, md.center, md.vol_off, md.vol, C, h->buf.state, cc, cr);
       return 2 + launch_dt_finalize(h);
   }
   return 1 + launch_dt_finalize(h);

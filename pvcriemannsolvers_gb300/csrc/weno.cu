@@ -396,8 +396,11 @@ int limiter_dispatch(mcfd_handle *h, double *u) {
       u, l.mn, l.modal, mesh.n_cells);
   WenoArgs wa{u, l.modal, l.psi, l.proj, l.beta, l.eval, l.s00, l.divisor, l.adj,
               l.frame, l.volume, l.troubled, mesh.n_cells, l.w0, l.eps, (Q - 1) < 3 ? 1.0 : 3.0};
-  // persistent grid: 16 blocks of 64 threads per SM on the 152 SMs
-  const unsigned grid = (unsigned)std::min<int64_t>(mesh.n_cells, 152 * 16);
+  // persistent grid: limiter_blocks_per_sm blocks of 64 threads per SM
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+  const unsigned grid =
+      (unsigned)std::min<int64_t>(mesh.n_cells, (int64_t)std::max(sms, 1) * h->tune.limiter_blocks_per_sm);
   if (l.kind == 1 /* MCFD_LIMITER_LAZY: every cell */) {
     weno_reconstruct_kernel<N, M, 1><<<grid, 64, 0, h->stream>>>(wa, nullptr, nullptr);
     return 2;

@@ -258,6 +258,15 @@ class Lobatto:
     def synchronize(self) -> None:
         self._check(self._lib.mcfd_synchronize(self._h))
 
+    def autotune(self, cache_path: str | None = None) -> dict:
+        """mcfd_autotune: pick the fastest launch shapes on this mesh and
+        solution (optionally through a JSON-lines cache file)."""
+        out = (C.c_int32 * 4)()
+        path = cache_path.encode() if cache_path else None
+        self._check(self._lib.mcfd_autotune(self._h, path, out))
+        return {"face_block": out[0], "dt_block": out[1], "limiter_blocks_per_sm": out[2],
+                "from_cache": bool(out[3])}
+
     # -- batching: independent cases inside this handle
     def set_cases(self, case_offsets) -> None:
         """Cells [offsets[k], offsets[k+1]) form case k, with its own dt and t."""
