@@ -227,6 +227,7 @@ def measure_form(args, torch, dist, dev, local_rank, m, u0, precision):
     sysm.set_stream(stream.cuda_stream)
     L = u0.size
     sysm.SetSolutionColumn(u0)
+    tune = sysm.autotune()
     t = sysm.advance(args.warmup, 1e9, 3, 0.0)
     sysm.synchronize()
     if dist:
@@ -271,7 +272,7 @@ def measure_form(args, torch, dist, dev, local_rank, m, u0, precision):
     sysm.close()
     return {"value": 3 * L * args.steps * world / (ms * 1e-3), "ms_per_step": ms / args.steps,
             "e2e": 3 * L * args.steps * world / e2e_s, "launches": launches, "kernel_ms": kt,
-            "clocks": clocks.summary(), "solution": sol, "t": t}
+            "clocks": clocks.summary(), "solution": sol, "t": t, "autotune": tune}
 
 
 # DRAM bytes (read + write) per launch measured by one ncu capture on the
@@ -425,6 +426,7 @@ def run_mixed_box(args, rank, world, local_rank):
         else:
             sysm.SetSolutionColumn(u0)
         L = u0.size
+        sysm.autotune()
         t = sysm.advance(args.warmup, 1e9, 3, 0.0)
         sysm.synchronize()
         torch.cuda.synchronize(dev)
@@ -610,6 +612,8 @@ def run_ensemble(args, rank, world, local_rank):
     dev = torch.device("cuda", local_rank)
     specs = ensemble_spec(scale=args.ensemble_scale)
     members = build_ensemble(specs, device=local_rank)
+    for mb in members:
+        mb["system"].autotune()
     ens = Ensemble([mb["system"] for mb in members])
     stream = torch.cuda.Stream(device=dev)
     ens.set_stream(stream.cuda_stream)
@@ -749,6 +753,7 @@ def run_quadrant(args, rank, world, local_rank):
         stream = torch.cuda.Stream(device=dev)
         sysm.set_stream(stream.cuda_stream)
         sysm.SetSolutionColumn(u0)
+        sysm.autotune()
         t = sysm.advance(args.warmup, 1.0, 3, 0.0)
         sysm.troubled_cells()
         torch.cuda.synchronize(dev)
@@ -866,6 +871,7 @@ def run_gpu(args, rank, world, local_rank):
             "e2e": {"value": r["e2e"], "unit": UNIT, "h2d_bytes_per_step": 8 * L, "d2h_bytes_per_step": 8 * L,
                     "path": "mcfd_set_solution (pinned host) + mcfd_advance(1) + mcfd_get_solution (pinned host)"},
             "gpu_launches": r["launches"],
+            "autotune": r["autotune"],
             "roofline": roofline_of(r["kernel_ms"], L, m.n_cells, hbm_peak, peak_src, fp64_peak, head),
             "cpu_baseline": cpu,
         }
