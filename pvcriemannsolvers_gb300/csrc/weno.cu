@@ -54,21 +54,27 @@ struct WenoArgs {
   double w0, eps, smooth_ref;
 };
 
+// one thread per (cell, mode): all five components, so each modal_to_nodal
+// entry is loaded once
 template <int N, int M>
 __global__ void __launch_bounds__(256)
 weno_modal_kernel(const double *__restrict__ u, const double *__restrict__ mn,
                   double *__restrict__ modal, int64_t n_cells) {
   int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (gid >= n_cells * kK * M) return;
-  const int64_t c = gid / (kK * M);
-  const int r = (int)(gid - c * kK * M);
-  const int k = r / M, m = r - k * M;
+  if (gid >= n_cells * M) return;
+  const int64_t c = gid / M;
+  const int m = (int)(gid - c * M);
   const double *uc = u + c * kK * N;
   const double *mc = mn + c * N * M;
-  double s = 0;
-#pragma unroll 4
-  for (int q = 0; q < N; ++q) s += uc[q * kK + k] * mc[q * M + m];
-  modal[gid] = s;
+  double s[kK] = {0, 0, 0, 0, 0};
+#pragma unroll 3
+  for (int q = 0; q < N; ++q) {
+    const double w = mc[q * M + m];
+#pragma unroll
+    for (int k = 0; k < kK; ++k) s[k] += uc[q * kK + k] * w;
+  }
+#pragma unroll
+  for (int k = 0; k < kK; ++k) modal[(c * kK + k) * M + m] = s[k];
 }
 
 // One entry of L or R of EigenMatrices (riemann/euler/eigen.hpp:27-56) for
@@ -391,7 +397,7 @@ int limiter_dispatch(mcfd_handle *h, double *u) {
   constexpr int M = Q * (Q + 1) * (Q + 2) / 6;
   const Mesh &mesh = h->mesh;
   Limiter &l = h->lim;
-  int64_t total = mesh.n_cells * kK * M;
+  int64_t total = mesh.n_cells * M;
   weno_modal_kernel<N, M><<<(unsigned)((total + 255) / 256), 256, 0, h->stream>>>(
       u, l.mn, l.modal, mesh.n_cells);
   WenoArgs wa{u, l.modal, l.psi, l.proj, l.beta, l.eval, l.s00, l.divisor, l.adj,
