@@ -9,8 +9,10 @@ Arms
   default          the GPU library (libmcfd.so) through its C ABI.
                    value: device-resident stepping (mcfd_advance, dt on the
                    device, CUDA-graph replay), CUDA events on the handle stream.
-                   e2e: per step mcfd_set_solution from pinned host memory,
-                   one step, mcfd_get_solution to pinned host memory.
+                   e2e: per step the column in from pinned host memory, one
+                   step, the column back to pinned host memory, streamed
+                   (mcfd_stream_step: neighbouring steps' copies overlap the
+                   compute); the sequential set/advance/get figure beside it.
   --impl reference the reference algorithm restated on the CPU (the oracle,
                    OpenMP over all host cores) on a bounded sample of the same
                    workload (the 16^3 mesh of the same case).
@@ -218,6 +220,56 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def e2e_runs(torch, dev, sysm, sol, t, steps, dt_guess, dist=None):
+    """End-to-end stepping through the C ABI from / to pinned host memory.
+
+    streamed:   mcfd_stream_step per step (the upload of step k+1 and the
+                download of step k-1 overlap step k's compute), closed by
+                mcfd_stream_end, which waits for the last download.
+    sequential: mcfd_set_solution + mcfd_advance(1) + mcfd_get_solution.
+    Every step copies the whole column in from and back to pinned host
+    memory in both.  Returns (streamed seconds, sequential seconds)."""
+    L = sol.size
+    host_in = torch.empty(L, dtype=torch.float64, pin_memory=True).numpy()
+    host_out = torch.empty(L, dtype=torch.float64, pin_memory=True).numpy()
+    host_in[:] = sol
+    # set-up, untimed: the device staging and the two job graphs
+    sysm.stream_begin()
+    sysm.stream_step(host_in, host_out, t, 1, dt_guess, 3)
+    sysm.stream_step(host_in, host_out, t, 1, dt_guess, 3)
+    sysm.stream_end()
+    out = []
+    for mode in ("streamed", "sequential"):
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        if mode == "streamed":
+            sysm.stream_begin()
+            for _ in range(steps):
+                sysm.stream_step(host_in, host_out, t, 1, dt_guess, 3)
+            sysm.stream_end()
+        else:
+            te = t
+            for _ in range(steps):
+                sysm.SetSolutionColumn(host_in)
+                te = sysm.advance(1, dt_guess, 3, te)
+                sysm.get_solution_into(host_out)
+        torch.cuda.synchronize(dev)
+        el = time.perf_counter() - t0
+        if dist:
+            tt = torch.tensor([el], dtype=torch.float64, device=dev)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            el = float(tt.item())
+        out.append(el)
+    return out[0], out[1]
+
+
+E2E_PATH = ("mcfd_stream_step per step (pinned host column in, one SSP-RK3 step, pinned host column out; "
+            "the copies of neighbouring steps overlap the compute), mcfd_stream_end")
+E2E_SEQ_PATH = "mcfd_set_solution (pinned host) + mcfd_advance(1) + mcfd_get_solution (pinned host)"
+
+
 def measure_form(args, torch, dist, dev, local_rank, m, u0, precision):
     """Time one precision form: device-resident stepping, kernel times, e2e."""
     from pvcriemannsolvers_gb300 import Lobatto
@@ -251,27 +303,11 @@ def measure_form(args, torch, dist, dev, local_rank, m, u0, precision):
     sol = sysm.GetSolutionColumn()
     kt = sysm.kernel_times(reps=5)
     # end to end through the C ABI with pinned host buffers
-    host_in = torch.empty(L, dtype=torch.float64, pin_memory=True).numpy()
-    host_out = torch.empty(L, dtype=torch.float64, pin_memory=True).numpy()
-    host_in[:] = sol
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize(dev)
-    t0 = time.perf_counter()
-    te = t
-    for _ in range(args.steps):
-        sysm.SetSolutionColumn(host_in)
-        te = sysm.advance(1, 1e9, 3, te)
-        sysm.get_solution_into(host_out)
-    torch.cuda.synchronize(dev)
-    e2e_s = time.perf_counter() - t0
-    if dist:
-        tt = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
+    e2e_s, seq_s = e2e_runs(torch, dev, sysm, sol, t, args.steps, 1e9, dist)
     sysm.close()
     return {"value": 3 * L * args.steps * world / (ms * 1e-3), "ms_per_step": ms / args.steps,
-            "e2e": 3 * L * args.steps * world / e2e_s, "launches": launches, "kernel_ms": kt,
+            "e2e": 3 * L * args.steps * world / e2e_s, "e2e_sequential": 3 * L * args.steps * world / seq_s,
+            "launches": launches, "kernel_ms": kt,
             "clocks": clocks.summary(), "solution": sol, "t": t, "autotune": tune}
 
 
@@ -442,22 +478,12 @@ def run_mixed_box(args, rank, world, local_rank):
         ms = e0.elapsed_time(e1)
         sol = sysm.GetSolutionColumn()
         kt = sysm.kernel_times(reps=3)
-        host_in = torch.empty(L, dtype=torch.float64, pin_memory=True).numpy()
-        host_out = torch.empty(L, dtype=torch.float64, pin_memory=True).numpy()
-        host_in[:] = sol
-        e2e_steps = max(1, min(args.steps, 10))
-        torch.cuda.synchronize(dev)
-        t0 = time.perf_counter()
-        te = t
-        for _ in range(e2e_steps):
-            sysm.SetSolutionColumn(host_in)
-            te = sysm.advance(1, 1e9, 3, te)
-            sysm.get_solution_into(host_out)
-        torch.cuda.synchronize(dev)
-        e2e_s = time.perf_counter() - t0
+        e2e_steps = max(1, min(args.steps, 20))
+        e2e_s, seq_s = e2e_runs(torch, dev, sysm, sol, t, e2e_steps, 1e9)
         sysm.close()
         res[form] = {"value": 3 * L * args.steps / (ms * 1e-3), "ms_per_step": ms / args.steps,
-                     "e2e": 3 * L * e2e_steps / e2e_s, "launches": launches, "kernel_ms": kt,
+                     "e2e": 3 * L * e2e_steps / e2e_s, "e2e_sequential": 3 * L * e2e_steps / seq_s,
+                     "launches": launches, "kernel_ms": kt,
                      "clocks": clocks.summary(), "t": t, "solution": sol, "e2e_steps": e2e_steps}
     hbm_peak, peak_src = measured_peaks()
     fp64_peak = fp64_peak_tflops(torch, dev)
@@ -481,10 +507,11 @@ def run_mixed_box(args, rank, world, local_rank):
                      "note": "density coefficients on each cell's orthonormal basis (their L2 is the field L2)"},
         "clocks": r["clocks"],
         "e2e": {"value": r["e2e"], "unit": UNIT, "h2d_bytes_per_step": 8 * L,
-                "d2h_bytes_per_step": 8 * L, "steps": r["e2e_steps"],
-                "path": "mcfd_set_solution (pinned host) + mcfd_advance(1) + mcfd_get_solution (pinned host)"},
+                "d2h_bytes_per_step": 8 * L, "steps": r["e2e_steps"], "path": E2E_PATH,
+                "sequential": {"value": r["e2e_sequential"], "path": E2E_SEQ_PATH}},
         "gpu_launches": r["launches"],
-        "plain_fp64": {k: res["fp64"][k] for k in ("value", "ms_per_step", "e2e", "launches", "kernel_ms", "clocks")},
+        "plain_fp64": {k: res["fp64"][k] for k in ("value", "ms_per_step", "e2e", "e2e_sequential", "launches",
+                                                   "kernel_ms", "clocks")},
         "roofline": modal_roofline(res["fp64"]["kernel_ms"], m, L, fp64_peak, hbm_peak, peak_src),
         "cpu_baseline": cpu,
     }
@@ -770,22 +797,12 @@ def run_quadrant(args, rank, world, local_rank):
         launches = sysm.launch_count() - launches0
         sol = sysm.GetSolutionColumn()
         kt = sysm.kernel_times(reps=3)
-        host_in = torch.empty(L, dtype=torch.float64, pin_memory=True).numpy()
-        host_out = torch.empty(L, dtype=torch.float64, pin_memory=True).numpy()
-        host_in[:] = sol
-        e2e_steps = max(1, min(args.steps, 10))
-        torch.cuda.synchronize(dev)
-        t0 = time.perf_counter()
-        te = t
-        for _ in range(e2e_steps):
-            sysm.SetSolutionColumn(host_in)
-            te = sysm.advance(1, 1.0, 3, te)
-            sysm.get_solution_into(host_out)
-        torch.cuda.synchronize(dev)
-        e2e_s = time.perf_counter() - t0
+        e2e_steps = max(1, min(args.steps, 20))
+        e2e_s, seq_s = e2e_runs(torch, dev, sysm, sol, t, e2e_steps, 1.0)
         sysm.close()
         res[form] = {"value": 3 * L * args.steps / (ms * 1e-3), "ms_per_step": ms / args.steps,
-                     "e2e": 3 * L * e2e_steps / e2e_s, "launches": launches, "kernel_ms": kt,
+                     "e2e": 3 * L * e2e_steps / e2e_s, "e2e_sequential": 3 * L * e2e_steps / seq_s,
+                     "launches": launches, "kernel_ms": kt,
                      "clocks": clocks.summary(), "t": t, "solution": sol,
                      "troubled_fraction": troubled / (3.0 * args.steps * m.n_cells)}
     fp64_peak = fp64_peak_tflops(torch, dev)
@@ -809,9 +826,11 @@ def run_quadrant(args, rank, world, local_rank):
                      "troubled_fraction_fp64": res["fp64"]["troubled_fraction"]},
         "clocks": r["clocks"],
         "e2e": {"value": r["e2e"], "unit": UNIT, "h2d_bytes_per_step": 8 * L, "d2h_bytes_per_step": 8 * L,
-                "path": "mcfd_set_solution (pinned host) + mcfd_advance(1) + mcfd_get_solution (pinned host)"},
+                "steps": e2e_steps, "path": E2E_PATH,
+                "sequential": {"value": r["e2e_sequential"], "path": E2E_SEQ_PATH}},
         "gpu_launches": r["launches"],
-        "plain_fp64": {k: res["fp64"][k] for k in ("value", "ms_per_step", "e2e", "launches", "kernel_ms", "clocks")},
+        "plain_fp64": {k: res["fp64"][k] for k in ("value", "ms_per_step", "e2e", "e2e_sequential", "launches",
+                                                   "kernel_ms", "clocks")},
         "roofline": {"bound": "fp64", "kernel": "step", "kernel_ms": r["kernel_ms"], "peak": fp64_peak,
                      "unit": "TFLOP/s", "achieved": None, "frac": None, "traffic": None,
                      "peak_source": "measured in this run: cuBLAS DGEMM 4096^3",
@@ -869,7 +888,8 @@ def run_gpu(args, rank, world, local_rank):
             "accuracy": accuracy,
             "clocks": r["clocks"],
             "e2e": {"value": r["e2e"], "unit": UNIT, "h2d_bytes_per_step": 8 * L, "d2h_bytes_per_step": 8 * L,
-                    "path": "mcfd_set_solution (pinned host) + mcfd_advance(1) + mcfd_get_solution (pinned host)"},
+                    "steps": args.steps, "path": E2E_PATH,
+                    "sequential": {"value": r["e2e_sequential"], "path": E2E_SEQ_PATH}},
             "gpu_launches": r["launches"],
             "autotune": r["autotune"],
             "roofline": roofline_of(r["kernel_ms"], L, m.n_cells, hbm_peak, peak_src, fp64_peak, head),
@@ -878,6 +898,7 @@ def run_gpu(args, rank, world, local_rank):
         if head == "mixed" and "fp64" in res:
             p = res["fp64"]
             line["plain_fp64"] = {"value": p["value"], "ms_per_step": p["ms_per_step"], "e2e": p["e2e"],
+                                  "e2e_sequential": p["e2e_sequential"],
                                   "gpu_launches": p["launches"], "clocks": p["clocks"],
                                   "roofline": roofline_of(p["kernel_ms"], L, m.n_cells, hbm_peak, peak_src,
                                                           fp64_peak, "fp64")}

@@ -244,6 +244,26 @@ int mcfd_rk_step(mcfd_handle *h, double t, double dt, int32_t order);
 int mcfd_advance(mcfd_handle *h, int32_t n_steps, double dt_guess,
                  int32_t rk_order, double *t);
 
+/* Streamed stepping: a sequence of jobs, each "load a column from host memory
+ * at time t, mcfd_advance n_steps, store the result to host memory", where
+ * the upload of job k+1 and the download of job k-1 overlap job k's compute
+ * (two device staging slots, one copy stream per direction; each job's graph
+ * steps its input slot straight into its output slot).  The loop of
+ * demo/euler/sourceless.cpp:187-215 with SetSolutionColumn / GetSolutionColumn
+ * around every step, pipelined.  mcfd_stream_step only enqueues: host_in must
+ * stay unchanged and host_out unread until mcfd_stream_end returns.  Use
+ * page-locked host memory for the copies to be asynchronous.  Each job's
+ * result equals mcfd_set_solution(host_in) + mcfd_advance(n_steps, t) +
+ * mcfd_get_solution(host_out); the handle's own solution is not touched.
+ * mcfd_stream_end waits for every job and reports the first kernel status
+ * (non-finite value, Exact-solver cap).  The staging (4 columns) is
+ * allocated by the first mcfd_stream_begin and kept until mcfd_destroy. */
+int mcfd_stream_begin(mcfd_handle *h);
+int mcfd_stream_step(mcfd_handle *h, const double *host_in, double *host_out,
+                     int64_t n, double t, int32_t n_steps, double dt_guess,
+                     int32_t rk_order);
+int mcfd_stream_end(mcfd_handle *h);
+
 /* limiter::Reconstruct(part, limiter) (limiter/reconstruct.hpp:21-54) on the
  * current solution with the handle's limiter (no-op when none is set).
  * *troubled (may be NULL) receives the number of reconstructed cells. */

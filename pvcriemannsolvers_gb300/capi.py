@@ -91,6 +91,9 @@ SIGNATURES = {
     "mcfd_time_step": (C.c_int, [_P, C.c_double, C.c_int32, _D]),
     "mcfd_rk_step": (C.c_int, [_P, C.c_double, C.c_double, C.c_int32]),
     "mcfd_advance": (C.c_int, [_P, C.c_int32, C.c_double, C.c_int32, _D]),
+    "mcfd_stream_begin": (C.c_int, [_P]),
+    "mcfd_stream_step": (C.c_int, [_P, _D, _D, C.c_int64, C.c_double, C.c_int32, C.c_double, C.c_int32]),
+    "mcfd_stream_end": (C.c_int, [_P]),
     "mcfd_set_stream": (C.c_int, [_P, _P]),
     "mcfd_synchronize": (C.c_int, [_P]),
     "mcfd_face_node_maps": (C.c_int, [_P, C.POINTER(C.c_int16), C.POINTER(C.c_int16)]),

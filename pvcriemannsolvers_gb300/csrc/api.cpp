@@ -146,7 +146,24 @@ int upload(mcfd_handle *h, T **dst, const std::vector<T> &src) {
   return MCFD_OK;
 }
 
+// Staging buffers, copy streams and events of streamed stepping.
+void stream_release(mcfd_handle *h) {
+  auto &st = h->streamer;
+  for (int b = 0; b < 2; ++b) {
+    if (st.in[b]) cudaFree(st.in[b]);
+    if (st.out[b]) cudaFree(st.out[b]);
+    cudaEvent_t evs[] = {st.in_ready[b], st.in_free[b], st.out_ready[b], st.out_free[b]};
+    for (cudaEvent_t e : evs)
+      if (e) cudaEventDestroy(e);
+    if (st.graph[b]) cudaGraphExecDestroy(st.graph[b]);
+  }
+  if (st.copy_in) cudaStreamDestroy(st.copy_in);
+  if (st.copy_out) cudaStreamDestroy(st.copy_out);
+  st = mcfd::Streamer{};
+}
+
 void release(mcfd_handle *h) {
+  stream_release(h);
   auto &m = h->mesh;
   auto &b = h->buf;
   void *ptrs[] = {m.cell_geo, m.cell_geo32, m.cell_rate, m.cell_flux, m.face_cells,
@@ -169,7 +186,7 @@ void release(mcfd_handle *h) {
                    md.s32, md.vol32, md.foff32, md.taylor32};
   for (void *p : mptrs)
     if (p) cudaFree(p);
-  if (h->step_graph) cudaGraphExecDestroy(h->step_graph);
+  mcfd::drop_graphs(h);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -943,13 +960,10 @@ int mcfd_rk_step(mcfd_handle *h, double t, double dt, int32_t order) {
   return check_status(h);
 }
 
-int mcfd_advance(mcfd_handle *h, int32_t n_steps, double dt_guess, int32_t rk_order, double *t) {
-  if (!h || !t || n_steps < 0 || rk_order < 1 || rk_order > 3) return MCFD_ERR_ARGUMENT;
-  cudaSetDevice(h->device);
-  double cfl = h->opt.cfl > 0 ? h->opt.cfl : cfl_table(rk_order, h->mesh.p);
-  h->launches += mcfd::launch_set_state(h, *t, 0.0, dt_guess, cfl, 1);
-  // the captured step reads the trace of u in its first stage and leaves the
-  // trace of the new u behind; make it current before capture and replay
+// Capture (once per RK order) the CUDA graph of one step: dt + RK stages.
+// The captured step reads the trace of u in its first stage and leaves the
+// trace of the new u behind, so the trace is made current first.
+static int ensure_step_graph(mcfd_handle *h, int32_t rk_order) {
   if (h->use_trace && h->trace_for != h->buf.u) h->launches += mcfd::launch_trace(h, h->buf.u);
   CUDA_TRY(h, cudaGetLastError());
   if (!h->step_graph || h->step_graph_order != rk_order) {
@@ -966,6 +980,43 @@ int mcfd_advance(mcfd_handle *h, int32_t n_steps, double dt_guess, int32_t rk_or
     h->step_graph_order = rk_order;
     h->step_graph_kernels = n;
   }
+  return MCFD_OK;
+}
+
+// Capture the graph of one streamed job on staging slot b: the limiter on
+// the loaded column (as mcfd_set_solution), its trace, then n_steps x (dt +
+// RK stages), the first step reading in[b] and every step writing out[b].
+static int ensure_job_graph(mcfd_handle *h, int b, int32_t n_steps, int32_t rk_order) {
+  auto &st = h->streamer;
+  if (st.graph[b] && st.graph_order[b] == rk_order && st.graph_steps[b] == n_steps) return MCFD_OK;
+  if (st.graph[b]) { cudaGraphExecDestroy(st.graph[b]); st.graph[b] = nullptr; }
+  cudaGraph_t graph;
+  CUDA_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  int n = mcfd::launch_limiter(h, st.in[b]);
+  n += mcfd::launch_trace(h, st.in[b]);
+  for (int s = 0; s < n_steps; ++s) {
+    const double *src = s == 0 ? st.in[b] : st.out[b];
+    n += mcfd::launch_dt(h, src);
+    n += mcfd::launch_rk_stage_sequence(h, rk_order, src, st.out[b]);
+  }
+  cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(&st.graph[b], graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaGraphInstantiate");
+  st.graph_order[b] = rk_order;
+  st.graph_steps[b] = n_steps;
+  st.graph_kernels[b] = n;
+  return MCFD_OK;
+}
+
+int mcfd_advance(mcfd_handle *h, int32_t n_steps, double dt_guess, int32_t rk_order, double *t) {
+  if (!h || !t || n_steps < 0 || rk_order < 1 || rk_order > 3) return MCFD_ERR_ARGUMENT;
+  cudaSetDevice(h->device);
+  double cfl = h->opt.cfl > 0 ? h->opt.cfl : cfl_table(rk_order, h->mesh.p);
+  h->launches += mcfd::launch_set_state(h, *t, 0.0, dt_guess, cfl, 1);
+  int grc = ensure_step_graph(h, rk_order);
+  if (grc) return grc;
   for (int s = 0; s < n_steps; ++s) {
     CUDA_TRY(h, cudaGraphLaunch(h->step_graph, h->stream));
     h->launches += h->step_graph_kernels;
@@ -976,6 +1027,83 @@ int mcfd_advance(mcfd_handle *h, int32_t n_steps, double dt_guess, int32_t rk_or
   *t = st.t;
   h->t_host = st.t;
   return rc;
+}
+
+int mcfd_stream_begin(mcfd_handle *h) {
+  if (!h) return MCFD_ERR_ARGUMENT;
+  if (h->streamer.on) return MCFD_OK;
+  cudaSetDevice(h->device);
+  auto &st = h->streamer;
+  if (st.copy_out) {  // staging kept from an earlier stream
+    st.on = true;
+    st.k = 0;
+    return MCFD_OK;
+  }
+  const size_t bytes = sizeof(double) * h->mesh.column;
+  cudaError_t e = cudaSuccess;
+  for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+    e = cudaMalloc(&st.in[b], bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&st.out[b], bytes);
+    cudaEvent_t *evs[] = {&st.in_ready[b], &st.in_free[b], &st.out_ready[b], &st.out_free[b]};
+    for (cudaEvent_t *ev : evs)
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+  }
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st.copy_in, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st.copy_out, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    stream_release(h);
+    return cuda_fail(h, e, "stream set-up");
+  }
+  st.on = true;
+  st.k = 0;
+  return MCFD_OK;
+}
+
+int mcfd_stream_step(mcfd_handle *h, const double *host_in, double *host_out, int64_t n,
+                     double t, int32_t n_steps, double dt_guess, int32_t rk_order) {
+  if (!h || !host_in || !host_out || n_steps < 1 || rk_order < 1 || rk_order > 3)
+    return MCFD_ERR_ARGUMENT;
+  if (!h->streamer.on) return fail(h, MCFD_ERR_STATE, "mcfd_stream_begin first");
+  if (n != h->mesh.column) return fail(h, MCFD_ERR_ARGUMENT, "column size mismatch");
+  cudaSetDevice(h->device);
+  auto &st = h->streamer;
+  const int b = (int)(st.k & 1);
+  const size_t bytes = sizeof(double) * n;
+  // upload into in[b] once job k-2 has finished reading it
+  CUDA_TRY(h, cudaStreamWaitEvent(st.copy_in, st.in_free[b], 0));
+  CUDA_TRY(h, cudaMemcpyAsync(st.in[b], host_in, bytes, cudaMemcpyHostToDevice, st.copy_in));
+  CUDA_TRY(h, cudaEventRecord(st.in_ready[b], st.copy_in));
+  // compute in[b] -> out[b] once the upload has landed and the download of
+  // job k-2 has left out[b]
+  CUDA_TRY(h, cudaStreamWaitEvent(h->stream, st.in_ready[b], 0));
+  CUDA_TRY(h, cudaStreamWaitEvent(h->stream, st.out_free[b], 0));
+  double cfl = h->opt.cfl > 0 ? h->opt.cfl : cfl_table(rk_order, h->mesh.p);
+  h->launches += mcfd::launch_set_state(h, t, 0.0, dt_guess, cfl, 1);
+  int grc = ensure_job_graph(h, b, n_steps, rk_order);
+  if (grc) return grc;
+  CUDA_TRY(h, cudaGraphLaunch(st.graph[b], h->stream));
+  h->launches += st.graph_kernels[b];
+  h->trace_for = nullptr;  // the job overwrote the trace buffer
+  CUDA_TRY(h, cudaEventRecord(st.in_free[b], h->stream));
+  CUDA_TRY(h, cudaEventRecord(st.out_ready[b], h->stream));
+  // download once the result is complete
+  CUDA_TRY(h, cudaStreamWaitEvent(st.copy_out, st.out_ready[b], 0));
+  CUDA_TRY(h, cudaMemcpyAsync(host_out, st.out[b], bytes, cudaMemcpyDeviceToHost, st.copy_out));
+  CUDA_TRY(h, cudaEventRecord(st.out_free[b], st.copy_out));
+  ++st.k;
+  return MCFD_OK;
+}
+
+int mcfd_stream_end(mcfd_handle *h) {
+  if (!h) return MCFD_ERR_ARGUMENT;
+  if (!h->streamer.on) return MCFD_OK;
+  cudaSetDevice(h->device);
+  cudaError_t e = cudaStreamSynchronize(h->streamer.copy_in);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->streamer.copy_out);
+  h->streamer.on = false;  // staging buffers, streams and graphs stay for the next stream
+  if (e != cudaSuccess) return cuda_fail(h, e, "stream end");
+  return check_status(h);
 }
 
 }  // extern "C"
@@ -1195,7 +1323,7 @@ int mcfd_set_cases(mcfd_handle *h, int32_t n_cases, const int64_t *case_offsets)
   if ((rc = upload(h, &cs.rate, zr))) return rc;
   cs.offsets.assign(case_offsets, case_offsets + n_cases + 1);
   cs.n = n_cases;
-  if (h->step_graph) { cudaGraphExecDestroy(h->step_graph); h->step_graph = nullptr; }
+  mcfd::drop_graphs(h);
   return MCFD_OK;
 }
 

@@ -877,32 +877,34 @@ int launch_residual_static_scratch(mcfd_handle *h, const double *d_u,
 // The stages of RungeKutta<order>::Update with the result left in buf.u.
 // Stage times: t, t + dt, t + dt/2 (rk.hpp:34-42).  The last stage also
 // advances the device time by dt.
-int launch_rk_stage_sequence(mcfd_handle *h, int order) {
+int launch_rk_stage_sequence(mcfd_handle *h, int order, const double *u_in, double *u_out) {
   Buffers &b = h->buf;
+  const double *u = u_in ? u_in : b.u;
+  double *out = u_out ? u_out : b.u;
   int n = 0;
   // Each stage result is a SetSolutionColumn in the reference, which runs the
   // limiter when one is installed (spatial/with_limiter.hpp:56-59).
   if (order == 1) {
-    n += launch_face_flux(h, b.u, 0.0);
-    n += launch_cell_update(h, kStageEuler, b.u, nullptr, b.u, 1);
-    n += launch_limiter(h, b.u);
+    n += launch_face_flux(h, u, 0.0);
+    n += launch_cell_update(h, kStageEuler, u, nullptr, out, 1);
+    n += launch_limiter(h, out);
   } else if (order == 2) {
-    n += launch_face_flux(h, b.u, 0.0);
-    n += launch_cell_update(h, kStageEuler, b.u, nullptr, b.u1, 0);
+    n += launch_face_flux(h, u, 0.0);
+    n += launch_cell_update(h, kStageEuler, u, nullptr, b.u1, 0);
     n += launch_limiter(h, b.u1);
     n += launch_face_flux(h, b.u1, 1.0);
-    n += launch_cell_update(h, kStageRk2Last, b.u1, b.u, b.u, 1);
-    n += launch_limiter(h, b.u);
+    n += launch_cell_update(h, kStageRk2Last, b.u1, u, out, 1);
+    n += launch_limiter(h, out);
   } else {
-    n += launch_face_flux(h, b.u, 0.0);
-    n += launch_cell_update(h, kStageEuler, b.u, nullptr, b.u1, 0);
+    n += launch_face_flux(h, u, 0.0);
+    n += launch_cell_update(h, kStageEuler, u, nullptr, b.u1, 0);
     n += launch_limiter(h, b.u1);
     n += launch_face_flux(h, b.u1, 1.0);
-    n += launch_cell_update(h, kStageRk3Mid, b.u1, b.u, b.u2, 0);
+    n += launch_cell_update(h, kStageRk3Mid, b.u1, u, b.u2, 0);
     n += launch_limiter(h, b.u2);
     n += launch_face_flux(h, b.u2, 0.5);
-    n += launch_cell_update(h, kStageRk3Last, b.u2, b.u, b.u, 1);
-    n += launch_limiter(h, b.u);
+    n += launch_cell_update(h, kStageRk3Last, b.u2, u, out, 1);
+    n += launch_limiter(h, out);
   }
   return n + launch_advance_cases(h);
 }

@@ -162,6 +162,23 @@ struct Options {
 }  // namespace mcfd
 
 namespace mcfd {
+// Streamed stepping (mcfd_stream_*): double-buffered device staging of the
+// host columns and one copy stream per direction, so that the uploads and
+// downloads of neighbouring jobs overlap the current job's compute.  Job k
+// uses staging slot b = k & 1; its graph steps in[b] into out[b] directly
+// (first stage reads in[b], last stage writes out[b]), so no device copy of
+// the column is made.
+struct Streamer {
+  bool on = false;
+  double *in[2] = {nullptr, nullptr}, *out[2] = {nullptr, nullptr};
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  int graph_order[2] = {0, 0}, graph_steps[2] = {0, 0}, graph_kernels[2] = {0, 0};
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  cudaEvent_t in_ready[2] = {nullptr, nullptr}, in_free[2] = {nullptr, nullptr};
+  cudaEvent_t out_ready[2] = {nullptr, nullptr}, out_free[2] = {nullptr, nullptr};
+  int64_t k = 0;
+};
+
 // Launch shapes chosen by mcfd_autotune (defaults until it runs).
 struct Tune {
   int face_block = 256;            // threads per block of the face kernels
@@ -191,9 +208,17 @@ struct mcfd_handle {
   cudaGraphExec_t step_graph = nullptr;
   int step_graph_order = 0;
   int step_graph_kernels = 0;
+  mcfd::Streamer streamer;
 };
 
 namespace mcfd {
+
+// Drop every captured step graph (launch shapes, cases or pointers changed).
+inline void drop_graphs(mcfd_handle *h) {
+  if (h->step_graph) { cudaGraphExecDestroy(h->step_graph); h->step_graph = nullptr; }
+  for (int b = 0; b < 2; ++b)
+    if (h->streamer.graph[b]) { cudaGraphExecDestroy(h->streamer.graph[b]); h->streamer.graph[b] = nullptr; }
+}
 
 // Kernel launchers (dgsem.cu).  Each returns the number of kernels launched.
 int launch_set_state(mcfd_handle *h, double t, double dt, double dt_guess,
@@ -210,7 +235,9 @@ inline void invalidate_trace(mcfd_handle *h, const double *u) {
 }
 // dt finalisation after a max-rate reduction (handle word or per case).
 int launch_dt_finalize(mcfd_handle *h);
-int launch_rk_stage_sequence(mcfd_handle *h, int order);
+// One RK step's stages from u_in to u_out (both default to buf.u).
+int launch_rk_stage_sequence(mcfd_handle *h, int order, const double *u_in = nullptr,
+                             double *u_out = nullptr);
 // WENO limiter pass on a solution buffer, in place (weno.cu).
 int launch_limiter(mcfd_handle *h, double *u);
 

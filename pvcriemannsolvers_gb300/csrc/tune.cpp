@@ -155,7 +155,7 @@ extern "C" int mcfd_autotune(mcfd_handle *h, const char *cache_path, int32_t *ch
   }
   t.tuned = true;
   h->tune = t;
-  if (h->step_graph) { cudaGraphExecDestroy(h->step_graph); h->step_graph = nullptr; }
+  mcfd::drop_graphs(h);
   if (choice) {
     choice[0] = t.face_block;
     choice[1] = t.dt_block;

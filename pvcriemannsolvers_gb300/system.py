@@ -236,6 +236,24 @@ class Lobatto:
         self._check(self._lib.mcfd_advance(self._h, int(n_steps), float(dt_guess), int(rk_order), C.byref(tt)))
         return tt.value
 
+    # -- streamed stepping (uploads/downloads overlap the neighbouring jobs' compute)
+    def stream_begin(self) -> None:
+        self._check(self._lib.mcfd_stream_begin(self._h))
+
+    def stream_step(self, host_in: np.ndarray, host_out: np.ndarray, t: float, n_steps: int,
+                    dt_guess: float, rk_order: int) -> None:
+        """Enqueue one job: load host_in at time t, advance n_steps, store into
+        host_out.  Both arrays must stay alive (and host_in unchanged) until
+        stream_end; page-locked arrays make the copies asynchronous."""
+        for a in (host_in, host_out):
+            if a.dtype != np.float64 or not a.flags.c_contiguous or a.size != self.column_size:
+                raise ValueError("stream buffers must be contiguous float64 arrays of the column size")
+        self._check(self._lib.mcfd_stream_step(self._h, capi.dptr(host_in), capi.dptr(host_out), host_in.size,
+                                               float(t), int(n_steps), float(dt_guess), int(rk_order)))
+
+    def stream_end(self) -> None:
+        self._check(self._lib.mcfd_stream_end(self._h))
+
     def Limit(self) -> int:
         """limiter::Reconstruct on the current solution; returns the number of
         reconstructed cells."""
