@@ -48,7 +48,8 @@ enum mcfd_status {
   MCFD_ERR_STATE = 4,         /* non-finite value produced by a kernel */
   MCFD_ERR_NOT_CONVERGED = 5, /* Exact solver hit its iteration cap */
   MCFD_ERR_UNSUPPORTED = 6,   /* option combination not built */
-  MCFD_ERR_NO_DEVICE = 7      /* no CUDA device / wrong architecture */
+  MCFD_ERR_NO_DEVICE = 7,     /* no CUDA device / wrong architecture */
+  MCFD_ERR_IO = 8             /* file cannot be written / read / verified */
 };
 
 /* Riemann solvers.  Exact / HLLC / AUSM follow
@@ -263,6 +264,51 @@ int mcfd_stream_step(mcfd_handle *h, const double *host_in, double *host_out,
                      int64_t n, double t, int32_t n_steps, double dt_guess,
                      int32_t rk_order);
 int mcfd_stream_end(mcfd_handle *h);
+
+/* ---- output and restart ----
+ * Writer<Part>::WriteSolutions (mesh/vtk.hpp:526-669): every cell is written
+ * as a disconnected VTK element, Hex8 cells as Hexahedron27 (type 29) and
+ * Tet4 cells as Tetrahedron10 (type 24), carrying the conservative variables
+ * (Density, MomentumX/Y/Z, EnergyStagnationDensity) at the element's VTK
+ * nodes (Writer::Prepare, vtk.hpp:428-493: LocalToGlobalAndValue at the VTK
+ * local coordinates).  Points are cell by cell, 27 or 10 per cell. */
+int mcfd_vtk_point_count(const mcfd_handle *h, int64_t *n_points);
+/* xyz [n_points][3], values [n_points][5], types [n_cells] (host memory). */
+int mcfd_vtk_sample(mcfd_handle *h, double *xyz, double *values, uint8_t *types,
+                    int64_t n_points);
+/* <directory>/<soln_name>.pvtu and <directory>/<soln_name>/0.vtu in the
+ * reference's layout: values ASCII at the stream's default 6 significant
+ * digits, points base64 (binary = 0, as the reference); binary = 1 writes
+ * values, offsets and types base64 as well (full precision).  The
+ * directories are created as needed. */
+int mcfd_write_vtu(mcfd_handle *h, const char *directory, const char *soln_name,
+                   int32_t binary);
+/* The writer alone, on host arrays as mcfd_vtk_sample returns them (types
+ * 29 or 24); needs no device. */
+int mcfd_write_vtu_arrays(const char *directory, const char *soln_name,
+                          int64_t n_points, const double *xyz,
+                          const double *values, int64_t n_cells,
+                          const uint8_t *types, int32_t binary);
+/* Base64 of the VTK binary arrays (mesh/vtk.hpp:21-91 EncodeBase64): writes
+ * the text and a terminating NUL to out (capacity cap) and its length to
+ * *written; out = NULL only queries the length. */
+int mcfd_base64_encode(const uint8_t *data, int64_t n, char *out, int64_t cap,
+                       int64_t *written);
+
+/* Part::GatherSolutions / ScatterSolutions (mesh/part.hpp:380-395,
+ * 1053-1069): the DataOnCells fields, field-major [F][n_cells] with
+ * F = column / n_cells and field i of cell c = value i of the cell's column
+ * block (device pointers, n = column size).  Scatter replaces the solution
+ * without running the limiter, as ScatterFields sets the coefficients. */
+int mcfd_gather_fields(mcfd_handle *h, double *d_fields, int64_t n);
+int mcfd_scatter_fields(mcfd_handle *h, const double *d_fields, int64_t n);
+/* Part::WriteSolutions / ReadSolutions (mesh/part.hpp:1070-1208) with a
+ * binary file in place of CGNS: a header (magic "MCFDRST", version 1,
+ * scheme, degree, F, n_cells, t, 64-bit FNV-1a checksum of the payload over
+ * 8-byte words) and the DataOnCells fields.  Reading checks the header
+ * against the handle and the checksum, scatters the fields and returns t. */
+int mcfd_write_restart(mcfd_handle *h, const char *path, double t);
+int mcfd_read_restart(mcfd_handle *h, const char *path, double *t);
 
 /* limiter::Reconstruct(part, limiter) (limiter/reconstruct.hpp:21-54) on the
  * current solution with the handle's limiter (no-op when none is set).

@@ -195,6 +195,15 @@ int orc_modal_rk_update(const orc_modal *m, int riemann, int n_bc,
                         const orc_bc *bcs, int order, double t, double dt,
                         double *u);
 
+/* ---- output sampling, Writer<Part>::Prepare (mesh/vtk.hpp:428-493) ---- */
+/* nodal mesh: every cell at the 27 VTK Hexahedron27 locals; xyz
+ * [cells][27][3], values [cells][27][K] of the GLL Lagrange interpolant */
+int orc_vtk_sample(const orc_mesh *m, const double *u, double *xyz, double *values);
+/* modal mesh: Hex8 -> Hexahedron27 (type 29), Tet4 -> Tetrahedron10 (type
+ * 24), cell by cell; returns the number of points */
+int64_t orc_modal_vtk_sample(const orc_modal *m, const double *u, double *xyz,
+                             double *values, uint8_t *types);
+
 #ifdef __cplusplus
 }
 #endif

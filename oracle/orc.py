@@ -72,6 +72,7 @@ def load() -> C.CDLL:
                                         C.c_double, _D]),
             "orc_rk_update_linear": (C.c_int, [C.c_int, C.c_int64, _D, C.c_double, C.c_double, _D]),
             "orc_mesh_set_scheme": (None, [C.c_void_p, C.c_int]),
+            "orc_vtk_sample": (C.c_int, [C.c_void_p, _D, _D, _D]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -228,6 +229,14 @@ class Mesh:
         self.lib.orc_rk_update(self._m, riemann, n, arr, order, t, dt, _p(u))
         return u
 
+    def vtk_sample(self, u: np.ndarray):
+        """Writer<Part>::Prepare: (xyz [P, 3], values [P, 5], types [cells])."""
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        xyz = np.empty((self.n_cells * 27, 3))
+        v = np.empty((self.n_cells * 27, 5))
+        self.lib.orc_vtk_sample(self._m, _p(u), _p(xyz), _p(v))
+        return xyz, v, np.full(self.n_cells, 29, dtype=np.uint8)
+
 
 def set_threads(n: int) -> None:
     load().orc_set_threads(n)
@@ -341,6 +350,7 @@ def _modal_sigs(lib):
         "orc_modal_time_step": (C.c_double, [C.c_void_p, _D, C.c_double, C.c_int, C.c_double]),
         "orc_modal_rk_update": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(OrcBc), C.c_int, C.c_double,
                                           C.c_double, _D]),
+        "orc_modal_vtk_sample": (C.c_int64, [C.c_void_p, _D, _D, _D, C.POINTER(C.c_uint8)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -429,3 +439,66 @@ class Modal:
         n, arr = self.bcs
         self.lib.orc_modal_rk_update(self._m, riemann, n, arr, order, t, dt, _p(u))
         return u
+
+    def vtk_sample(self, u: np.ndarray):
+        """Writer<Part>::Prepare: (xyz [P, 3], values [P, 5], types [cells])."""
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        cap = self.n_cells * 27
+        xyz, v = np.empty((cap, 3)), np.empty((cap, 5))
+        types = np.empty(self.n_cells, dtype=np.uint8)
+        n = int(self.lib.orc_modal_vtk_sample(self._m, _p(u), _p(xyz), _p(v),
+                                              types.ctypes.data_as(C.POINTER(C.c_uint8))))
+        return xyz[:n].copy(), v[:n].copy(), types
+
+
+# ---------------------------------------------------------------------------
+# Writer<Part>::WriteSolutions (mesh/vtk.hpp:526-669), restated in Python:
+# the text of the .pvtu index and the .vtu piece written by one rank.
+
+FIELD_NAMES = ("Density", "MomentumX", "MomentumY", "MomentumZ", "EnergyStagnationDensity")
+
+
+def _fmt(x) -> str:
+    """operator<< of a double at the stream defaults (%g, 6 digits)."""
+    return "%g" % x
+
+
+def vtk_inline_binary(data: bytes) -> str:
+    """EncodeBase64 of the UInt64 byte count, then of the bytes (vtk.hpp:641-648)."""
+    import base64
+    import struct
+    return base64.b64encode(struct.pack("<Q", len(data))).decode() + base64.b64encode(data).decode()
+
+
+def pvtu_text(soln_name: str) -> str:
+    lines = ['<VTKFile type="PUnstructuredGrid" version="1.0" byte_order="LittleEndian" header_type="UInt64">',
+             '  <PUnstructuredGrid GhostLevel="1">', "    <PPointData>"]
+    lines += [f'      <PDataArray type="Float64" Name="{f}"/>' for f in FIELD_NAMES]
+    lines += ["    </PPointData>", "    <PCellData>", "    </PCellData>", "    <PPoints>",
+              '      <PDataArray type="Float64" Name="Points" NumberOfComponents="3"/>', "    </PPoints>",
+              f'    <Piece Source="./{soln_name}/0.vtu"/>', "  </PUnstructuredGrid>", "</VTKFile>"]
+    return "\n".join(lines) + "\n"
+
+
+def vtu_text(xyz: np.ndarray, values: np.ndarray, types: np.ndarray) -> str:
+    n_points, n_cells = len(xyz), len(types)
+    out = ['<VTKFile type="UnstructuredGrid" version="1.0" byte_order="LittleEndian" header_type="UInt64">\n',
+           "  <UnstructuredGrid>\n", f'    <Piece NumberOfPoints="{n_points}" NumberOfCells="{n_cells}">\n',
+           "      <PointData>\n"]
+    for k, f in enumerate(FIELD_NAMES):
+        out.append(f'        <DataArray type="Float64" Name="{f}" format="ascii">\n')
+        out.append("".join(_fmt(v) + " " for v in values[:, k]))
+        out.append("\n        </DataArray>\n")
+    out += ["      </PointData>\n", "      <CellData>\n", "      </CellData>\n", "      <Points>\n",
+            '        <DataArray type="Float64" Name="Points" NumberOfComponents="3" format="binary">\n',
+            vtk_inline_binary(np.ascontiguousarray(xyz, dtype="<f8").tobytes()),
+            "\n        </DataArray>\n", "      </Points>\n", "      <Cells>\n",
+            '        <DataArray type="Int32" Name="connectivity" format="ascii">\n',
+            "".join(f"{i} " for i in range(n_points)), "\n        </DataArray>\n",
+            '        <DataArray type="Int32" Name="offsets" format="ascii">\n']
+    sizes = np.where(np.asarray(types) == 29, 27, 10)
+    out.append("".join(f"{o} " for o in np.cumsum(sizes)))
+    out += ["\n        </DataArray>\n", '        <DataArray type="UInt8" Name="types" format="ascii">\n',
+            "".join(f"{int(t)} " for t in types), "\n        </DataArray>\n", "      </Cells>\n",
+            "    </Piece>\n", "  </UnstructuredGrid>\n", "</VTKFile>\n"]
+    return "".join(out)

@@ -239,6 +239,7 @@ struct orc_mesh {
   double *grad;       /* [cells][N][3][N]  basis global gradients */
   double *length;     /* [cells] */
   double *cell_center; /* [cells][3] Hex8 LocalToGlobal(0, 0, 0) */
+  double *corners;    /* [cells][8][3] Hex8 node coordinates */
   double *jdi;        /* [cells][N][9] det(J) J^-1 (GetJacobianAssociated) */
   double *detj;       /* [cells][N] det(J) */
   int32_t *face_sides; /* [faces][2] local face index in holder / sharer */
@@ -269,6 +270,7 @@ double orc_cell_length(const orc_mesh *m, int64_t c) { return m->length[c]; }
 void orc_mesh_destroy(orc_mesh *m) {
   if (!m) return;
   free(m->node_xyz); free(m->node_w); free(m->grad); free(m->length); free(m->cell_center);
+  free(m->corners);
   free(m->face_shift); free(m->jdi); free(m->detj); free(m->face_sides);
   free(m->face_cells); free(m->face_group); free(m->face_xyz); free(m->face_w);
   free(m->face_frame); free(m->map_h); free(m->map_s);
@@ -301,6 +303,7 @@ orc_mesh *orc_mesh_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
   m->grad = (double *)malloc(sizeof(double) * n_cells * N * 3 * N);
   m->length = (double *)malloc(sizeof(double) * n_cells);
   m->cell_center = (double *)malloc(sizeof(double) * n_cells * 3);
+  m->corners = (double *)malloc(sizeof(double) * n_cells * 24);
   m->jdi = (double *)malloc(sizeof(double) * n_cells * N * 9);
   m->detj = (double *)malloc(sizeof(double) * n_cells * N);
   m->face_sides = (int32_t *)malloc(sizeof(int32_t) * (n_faces * 2 + 1));
@@ -317,6 +320,7 @@ orc_mesh *orc_mesh_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
     }
     double volume = 0;
     const double zero[3] = {0, 0, 0};
+    memcpy(&m->corners[c * 24], xn, sizeof(xn));
     hex8_global(xn, zero, &m->cell_center[c * 3]);
     for (int i = 0; i < Q; ++i)
       for (int j = 0; j < Q; ++j)
@@ -804,4 +808,48 @@ int orc_rk_update_linear(int order, int64_t n, const double *a, double t,
                          double dt, double *u) {
   lin_ctx ctx = {n, a};
   return orc_rk_generic(lin_residual_fn, &ctx, n, order, t, dt, u, NULL, NULL);
+}
+
+/* ---- output sampling: Writer<Part>::Prepare (mesh/vtk.hpp:428-493) ---- */
+
+/* VTK Hexahedron27 local coordinates (mesh/vtk.hpp:310-330): corners, edge
+ * midpoints, face centres, centre. */
+const signed char orc_vtk_hex27[27][3] = {
+    {-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1}, {-1, -1, 1}, {1, -1, 1},
+    {1, 1, 1},    {-1, 1, 1},  {0, -1, -1}, {1, 0, -1}, {0, 1, -1},  {-1, 0, -1},
+    {0, -1, 1},   {1, 0, 1},   {0, 1, 1},  {-1, 0, 1},  {-1, -1, 0}, {1, -1, 0},
+    {1, 1, 0},    {-1, 1, 0},  {-1, 0, 0}, {1, 0, 0},   {0, -1, 0},  {0, 1, 0},
+    {0, 0, -1},   {0, 0, 1},   {0, 0, 0}};
+
+/* Lagrange basis on the GLL abscissae at s (basis/lagrange.hpp:53-142). */
+static void lagrange_values(int q, const double *x, double s, double *l) {
+  for (int i = 0; i < q; ++i) {
+    double v = 1;
+    for (int m = 0; m < q; ++m)
+      if (m != i) v *= (s - x[m]) / (x[i] - x[m]);
+    l[i] = v;
+  }
+}
+
+int orc_vtk_sample(const orc_mesh *m, const double *u, double *xyz, double *values) {
+  const int Q = m->q, N = m->n;
+  for (int64_t c = 0; c < m->n_cells; ++c)
+    for (int s = 0; s < 27; ++s) {
+      double loc[3] = {orc_vtk_hex27[s][0], orc_vtk_hex27[s][1], orc_vtk_hex27[s][2]};
+      double *g = &xyz[(c * 27 + s) * 3], *v = &values[(c * 27 + s) * K];
+      hex8_global(&m->corners[c * 24], loc, g);
+      double lx[MAXQ], ly[MAXQ], lz[MAXQ];
+      lagrange_values(Q, m->xq, loc[0], lx);
+      lagrange_values(Q, m->xq, loc[1], ly);
+      lagrange_values(Q, m->xq, loc[2], lz);
+      for (int k = 0; k < K; ++k) v[k] = 0;
+      for (int i = 0; i < Q; ++i)
+        for (int j = 0; j < Q; ++j)
+          for (int kk = 0; kk < Q; ++kk) {
+            const double w = lx[i] * ly[j] * lz[kk];
+            const double *un = &u[(c * N + (i * Q + j) * Q + kk) * K];
+            for (int k = 0; k < K; ++k) v[k] += w * un[k];
+          }
+    }
+  return 0;
 }

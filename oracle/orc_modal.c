@@ -214,6 +214,8 @@ struct orc_modal {
   int64_t *face_cells;
   int32_t *face_group;
   double *face_shift;
+  double *corners;     /* [cells][8][3] (Tet4: first 4) */
+  int32_t *type;       /* [cells] ORC_CELL_* */
 };
 
 int64_t orc_modal_column_size(const orc_modal *m) { return m->n_cells * m->m * K; }
@@ -226,6 +228,7 @@ void orc_modal_destroy(orc_modal *m) {
   free(m->vp_off); free(m->vx); free(m->vw); free(m->center); free(m->s);
   free(m->length); free(m->fp_off); free(m->fx); free(m->fw); free(m->ff);
   free(m->face_cells); free(m->face_group); free(m->face_shift);
+  free(m->corners); free(m->type);
   free(m);
 }
 
@@ -260,6 +263,8 @@ orc_modal *orc_modal_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
   m->center = (double *)malloc(sizeof(double) * n_cells * 3);
   m->s = (double *)calloc(n_cells * M * M, sizeof(double));
   m->length = (double *)malloc(sizeof(double) * n_cells);
+  m->corners = (double *)calloc(n_cells * 24, sizeof(double));
+  m->type = (int32_t *)malloc(sizeof(int32_t) * n_cells);
   double gx[4], gw[4];
   gauss_rule(Q, gx, gw);
   double tx[24][3], tw[24];
@@ -277,6 +282,8 @@ orc_modal *orc_modal_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
       if (id < 0 || id >= n_nodes) { bad = 1; id = 0; }
       for (int d = 0; d < 3; ++d) xn[v * 3 + d] = xyz[id * 3 + d];
     }
+    memcpy(&m->corners[c * 24], xn, sizeof(double) * 3 * nv);
+    m->type[c] = t;
     double *ctr = &m->center[c * 3];
     double *X = &m->vx[m->vp_off[c] * 3], *W = &m->vw[m->vp_off[c]];
     double volume = 0;
@@ -647,4 +654,39 @@ int orc_modal_rk_update(const orc_modal *m, int riemann, int n_bc,
   modal_ctx ctx = {m, riemann, n_bc, bcs};
   return orc_rk_generic(modal_residual_fn, &ctx, orc_modal_column_size(m), order,
                         t, dt, u, NULL, NULL);
+}
+
+/* ---- output sampling: Writer<Part>::Prepare (mesh/vtk.hpp:428-493) ----
+ * Hex8 cells at the VTK Hexahedron27 locals, Tet4 cells at the VTK
+ * Tetrahedron10 locals (vtk.hpp:214-224); global point from the cell map,
+ * value = Projection::GlobalToValue there.  Points cell by cell. */
+extern const signed char orc_vtk_hex27[27][3];
+static const double kTet10[10][3] = {
+    {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {0, 0, 0}, {0.5, 0.5, 0},
+    {0, 0.5, 0.5}, {0.5, 0, 0.5}, {0.5, 0, 0}, {0, 0.5, 0}, {0, 0, 0.5}};
+
+int64_t orc_modal_vtk_sample(const orc_modal *m, const double *u, double *xyz,
+                             double *values, uint8_t *types) {
+  int64_t pt = 0;
+  double psi[MAXM];
+  for (int64_t c = 0; c < m->n_cells; ++c) {
+    const double *xn = &m->corners[c * 24];
+    const int tet = m->type[c] == ORC_CELL_TET4;
+    types[c] = tet ? 24 : 29;
+    const int n = tet ? 10 : 27;
+    for (int s = 0; s < n; ++s, ++pt) {
+      double *g = &xyz[pt * 3];
+      if (!tet) {
+        double loc[3] = {orc_vtk_hex27[s][0], orc_vtk_hex27[s][1], orc_vtk_hex27[s][2]};
+        hex8_global(xn, loc, g);
+      } else {
+        double l0 = kTet10[s][0], l1 = kTet10[s][1], l2 = kTet10[s][2];
+        double l3 = 1.0 - l0 - l1 - l2;
+        for (int d = 0; d < 3; ++d)
+          g[d] = xn[d] * l0 + xn[3 + d] * l1 + xn[6 + d] * l2 + xn[9 + d] * l3;
+      }
+      value_at(m, c, u, g, &values[pt * K], psi);
+    }
+  }
+  return pt;
 }

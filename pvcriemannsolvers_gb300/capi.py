@@ -15,7 +15,7 @@ LIB_PATH = Path(__file__).resolve().parent / "libmcfd.so"
 
 # enum values of include/mcfd.h
 OK = 0
-ERR_ARGUMENT, ERR_MESH, ERR_CUDA, ERR_STATE, ERR_NOT_CONVERGED, ERR_UNSUPPORTED, ERR_NO_DEVICE = range(1, 8)
+ERR_ARGUMENT, ERR_MESH, ERR_CUDA, ERR_STATE, ERR_NOT_CONVERGED, ERR_UNSUPPORTED, ERR_NO_DEVICE, ERR_IO = range(1, 9)
 EXACT, HLLC, AUSM, ROE, RUSANOV = range(5)
 RIEMANN = {"exact": EXACT, "hllc": HLLC, "ausm": AUSM, "roe": ROE, "rusanov": RUSANOV}
 BC_NONE, BC_INVISCID_WALL, BC_SUPERSONIC_INLET, BC_SUPERSONIC_OUTLET, BC_SUBSONIC_INLET, \
@@ -91,6 +91,17 @@ SIGNATURES = {
     "mcfd_time_step": (C.c_int, [_P, C.c_double, C.c_int32, _D]),
     "mcfd_rk_step": (C.c_int, [_P, C.c_double, C.c_double, C.c_int32]),
     "mcfd_advance": (C.c_int, [_P, C.c_int32, C.c_double, C.c_int32, _D]),
+    "mcfd_vtk_point_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "mcfd_vtk_sample": (C.c_int, [_P, _D, _D, C.POINTER(C.c_uint8), C.c_int64]),
+    "mcfd_write_vtu": (C.c_int, [_P, C.c_char_p, C.c_char_p, C.c_int32]),
+    "mcfd_write_vtu_arrays": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int64, _D, _D, C.c_int64,
+                                        C.POINTER(C.c_uint8), C.c_int32]),
+    "mcfd_base64_encode": (C.c_int, [C.POINTER(C.c_uint8), C.c_int64, C.c_char_p, C.c_int64,
+                                     C.POINTER(C.c_int64)]),
+    "mcfd_gather_fields": (C.c_int, [_P, _P, C.c_int64]),
+    "mcfd_scatter_fields": (C.c_int, [_P, _P, C.c_int64]),
+    "mcfd_write_restart": (C.c_int, [_P, C.c_char_p, C.c_double]),
+    "mcfd_read_restart": (C.c_int, [_P, C.c_char_p, _D]),
     "mcfd_stream_begin": (C.c_int, [_P]),
     "mcfd_stream_step": (C.c_int, [_P, _D, _D, C.c_int64, C.c_double, C.c_int32, C.c_double, C.c_int32]),
     "mcfd_stream_end": (C.c_int, [_P]),

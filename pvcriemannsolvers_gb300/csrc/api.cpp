@@ -168,7 +168,7 @@ void release(mcfd_handle *h) {
   auto &b = h->buf;
   void *ptrs[] = {m.cell_geo, m.cell_geo32, m.cell_rate, m.cell_flux, m.face_cells,
                   m.face_group, m.face_geo, m.face_xyz, m.face_map, m.dmat,
-                  m.bcs, b.u, b.u1, b.u2, b.res, b.flux, b.trace, b.state};
+                  m.bcs, m.corners, m.cell_type, b.u, b.u1, b.u2, b.res, b.flux, b.trace, b.state};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   auto &l = h->lim;
@@ -188,6 +188,27 @@ void release(mcfd_handle *h) {
     if (p) cudaFree(p);
   mcfd::drop_graphs(h);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+}
+
+// Cell corners and types for output sampling (Tet4 cells: the first four
+// cell_nodes entries, the rest zero).
+int upload_corners(mcfd_handle *h, const mcfd_mesh_desc *d) {
+  const int64_t nc = d->n_cells;
+  std::vector<double> corners(nc * 24, 0.0);
+  auto &types = h->mesh.host_types;
+  types.assign(nc, 0);
+  for (int64_t c = 0; c < nc; ++c) {
+    const int t = d->cell_type ? d->cell_type[c] : 0;
+    types[c] = (uint8_t)(t == 1 ? 1 : 0);
+    const int nv = t == 1 ? 4 : 8;
+    for (int v = 0; v < nv; ++v) {
+      const int64_t id = d->cell_nodes[c * 8 + v];
+      if (id < 0 || id >= d->n_nodes) return fail(h, MCFD_ERR_ARGUMENT, "cell node index out of range");
+      for (int e = 0; e < 3; ++e) corners[(c * 8 + v) * 3 + e] = d->xyz[id * 3 + e];
+    }
+  }
+  int rc = upload(h, &h->mesh.corners, corners);
+  return rc ? rc : upload(h, &h->mesh.cell_type, types);
 }
 
 int check_status(mcfd_handle *h) {
@@ -230,6 +251,7 @@ int build_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
   const int Q = m.q, N = m.n, QF = m.qf;
   double xq[4], wq[4], dm[16];
   gll(Q, xq, wq);
+  for (int i = 0; i < Q; ++i) h->mesh.xq[i] = xq[i];
   diff_matrix(Q, xq, dm);
   for (int64_t c = 0; c < d->n_cells; ++c) {
     if (d->cell_type && d->cell_type[c] != MCFD_HEX8)
@@ -748,6 +770,7 @@ int mcfd_create(const mcfd_mesh_desc *mesh, const mcfd_options *options,
   if (!rc)
     rc = options->scheme == MCFD_MODAL ? mcfd::build_modal_mesh(h, mesh, options->degree)
                                        : build_mesh(h, mesh, options->degree);
+  if (!rc) rc = upload_corners(h, mesh);
   if (!rc && options->limiter != MCFD_LIMITER_NONE) {
     if (options->limiter != MCFD_LIMITER_LAZY && options->limiter != MCFD_LIMITER_DETECT_LAZY &&
         options->limiter != MCFD_LIMITER_EIGEN)

@@ -62,6 +62,11 @@ struct Mesh {
   short2 *face_map = nullptr;       // [points] holder node, sharer node
   double *dmat = nullptr;           // [Q][Q] D[a][i] = l_i'(x_a)
   BcDev *bcs = nullptr;             // [n_groups]
+  // output sampling (mcfd_vtk_sample): cell corners and types
+  double *corners = nullptr;        // [cells][8][3] corner coordinates (Tet4: first 4)
+  uint8_t *cell_type = nullptr;     // [cells] 0 Hex8, 1 Tet4
+  std::vector<uint8_t> host_types;  // [cells]
+  double xq[4] = {0, 0, 0, 0};      // GLL abscissae of the nodal schemes
   // host copies for parity queries
   std::vector<int16_t> map_h, map_s;
   std::vector<BcDev> host_bcs;
@@ -235,6 +240,14 @@ inline void invalidate_trace(mcfd_handle *h, const double *u) {
 }
 // dt finalisation after a max-rate reduction (handle word or per case).
 int launch_dt_finalize(mcfd_handle *h);
+// Output (output.cu): column <-> DataOnCells fields ([F][cells], F values
+// per cell) and the VTK sample points of every cell (Hex27 / Tet10 locals),
+// written at xyz / values + off[cell] (3 and K doubles per point).
+int launch_fields_transpose(mcfd_handle *h, const double *src, double *dst, int to_fields);
+int launch_vtk_sample(mcfd_handle *h, const double *u, const int64_t *off, double *xyz,
+                      double *values);
+int launch_modal_vtk_sample(mcfd_handle *h, const double *u, const int64_t *off, double *xyz,
+                            double *values);
 // One RK step's stages from u_in to u_out (both default to buf.u).
 int launch_rk_stage_sequence(mcfd_handle *h, int order, const double *u_in = nullptr,
                              double *u_out = nullptr);

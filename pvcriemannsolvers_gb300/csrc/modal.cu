@@ -26,6 +26,7 @@
 
 #include "euler.cuh"
 #include "handle.hpp"
+#include "vtk_locals.cuh"
 
 namespace mcfd {
 namespace {
@@ -797,7 +798,84 @@ void modal_cell_dispatch(mcfd_handle *h, int stage, const ModalCellArgs &ca) {
   }
 }
 
+// Writer<Part>::Prepare (mesh/vtk.hpp:428-493) for the modal scheme: one
+// thread per (cell, VTK node slot); Hex8 cells sample the Hexahedron27
+// locals, Tet4 cells the Tetrahedron10 locals (slots 10..26 idle).  Global
+// point from the cell's map, value = sum_j a_j T_j(x - centre) with the
+// Taylor coefficients a = S^T c (Projection::LocalToGlobalAndValue).
+struct ModalSampleArgs {
+  const double *taylor;
+  const double4 *center;
+  const double *corners;
+  const uint8_t *type;
+  const int64_t *off;
+  double *xyz;
+  double *values;
+  int64_t n_cells;
+};
+
+template <int M>
+__global__ void __launch_bounds__(256) modal_vtk_sample_kernel(ModalSampleArgs a) {
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t c = gid / 27;
+  const int s = (int)(gid - c * 27);
+  if (c >= a.n_cells) return;
+  const bool tet = a.type[c] == 1;
+  if (tet && s >= 10) return;
+  const double *xn = a.corners + c * 24;
+  double g[3];
+  if (!tet) {
+    const double loc[3] = {(double)kVtkHex27[s][0], (double)kVtkHex27[s][1],
+                           (double)kVtkHex27[s][2]};
+    g[0] = g[1] = g[2] = 0;
+#pragma unroll
+    for (int v = 0; v < 8; ++v) {
+      const double w = (1 + kVtkHex27[v][0] * loc[0]) * (1 + kVtkHex27[v][1] * loc[1]) *
+                       (1 + kVtkHex27[v][2] * loc[2]) * 0.125;
+#pragma unroll
+      for (int e = 0; e < 3; ++e) g[e] += xn[v * 3 + e] * w;
+    }
+  } else {
+    // Tetrahedron4 shapes (x, y, z, 1 - x - y - z), coordinate/tetrahedron.hpp:98-103
+    const double l0 = kVtkTet10Half[s][0] * 0.5, l1 = kVtkTet10Half[s][1] * 0.5,
+                 l2 = kVtkTet10Half[s][2] * 0.5;
+    const double l3 = 1.0 - l0 - l1 - l2;
+#pragma unroll
+    for (int e = 0; e < 3; ++e)
+      g[e] = xn[e] * l0 + xn[3 + e] * l1 + xn[6 + e] * l2 + xn[9 + e] * l3;
+  }
+  const double4 ch = a.center[c];
+  double t[M], v[kK];
+  taylor_values<M>(g[0] - ch.x, g[1] - ch.y, g[2] - ch.z, t);
+  eval_taylor<M>(a.taylor + c * M * kK, t, v);
+  const int64_t pt = a.off[c] + s;
+#pragma unroll
+  for (int e = 0; e < 3; ++e) a.xyz[pt * 3 + e] = g[e];
+#pragma unroll
+  for (int e = 0; e < kK; ++e) a.values[pt * kK + e] = v[e];
+}
+
+template <int M>
+int modal_vtk_launch(mcfd_handle *h, const double *u, const ModalSampleArgs &sa) {
+  taylor_launch<M>(h, u);
+  const int64_t threads = h->mesh.n_cells * 27;
+  modal_vtk_sample_kernel<M><<<(unsigned)((threads + 255) / 256), 256, 0, h->stream>>>(sa);
+  return 2;
+}
+
 }  // namespace
+
+int launch_modal_vtk_sample(mcfd_handle *h, const double *u, const int64_t *off, double *xyz,
+                            double *values) {
+  const Modal &md = h->modal;
+  ModalSampleArgs sa{md.taylor, md.center, h->mesh.corners, h->mesh.cell_type, off, xyz, values,
+                     h->mesh.n_cells};
+  switch (md.m) {
+    case 4: return modal_vtk_launch<4>(h, u, sa);
+    case 10: return modal_vtk_launch<10>(h, u, sa);
+    default: return modal_vtk_launch<20>(h, u, sa);
+  }
+}
 
 int launch_modal_face_flux(mcfd_handle *h, const double *u, double stage_c) {
   const Mesh &m = h->mesh;

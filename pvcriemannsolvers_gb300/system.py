@@ -236,6 +236,39 @@ class Lobatto:
         self._check(self._lib.mcfd_advance(self._h, int(n_steps), float(dt_guess), int(rk_order), C.byref(tt)))
         return tt.value
 
+    # -- output and restart (mesh/vtk.hpp Writer, mesh/part.hpp Gather/Scatter/Write/ReadSolutions)
+    def vtk_sample(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """Writer<Part>::Prepare on the current solution: (xyz [P, 3],
+        values [P, 5], VTK cell types [cells]), Hex8 cells as Hexahedron27,
+        Tet4 cells as Tetrahedron10, points cell by cell."""
+        n = C.c_int64()
+        self._check(self._lib.mcfd_vtk_point_count(self._h, C.byref(n)))
+        xyz = np.empty((n.value, 3))
+        values = np.empty((n.value, 5))
+        types = np.empty(self.mesh.n_cells, dtype=np.uint8)
+        self._check(self._lib.mcfd_vtk_sample(self._h, capi.dptr(xyz), capi.dptr(values),
+                                              types.ctypes.data_as(C.POINTER(C.c_uint8)), n.value))
+        return xyz, values, types
+
+    def WriteSolutions(self, directory: str, soln_name: str, binary: bool = False) -> None:
+        """<directory>/<soln_name>.pvtu + <directory>/<soln_name>/0.vtu."""
+        self._check(self._lib.mcfd_write_vtu(self._h, str(directory).encode(), soln_name.encode(),
+                                             int(bool(binary))))
+
+    def gather_fields_device(self, ptr: int, n: int) -> None:
+        self._check(self._lib.mcfd_gather_fields(self._h, C.c_void_p(ptr), n))
+
+    def scatter_fields_device(self, ptr: int, n: int) -> None:
+        self._check(self._lib.mcfd_scatter_fields(self._h, C.c_void_p(ptr), n))
+
+    def write_restart(self, path: str, t: float) -> None:
+        self._check(self._lib.mcfd_write_restart(self._h, str(path).encode(), float(t)))
+
+    def read_restart(self, path: str) -> float:
+        t = C.c_double()
+        self._check(self._lib.mcfd_read_restart(self._h, str(path).encode(), C.byref(t)))
+        return t.value
+
     # -- streamed stepping (uploads/downloads overlap the neighbouring jobs' compute)
     def stream_begin(self) -> None:
         self._check(self._lib.mcfd_stream_begin(self._h))
@@ -391,3 +424,26 @@ class RungeKutta:
 
     def Update(self, system: Lobatto, t_curr: float, dt: float) -> None:
         system._check(system._lib.mcfd_rk_step(system.handle, float(t_curr), float(dt), self.order))
+
+
+def write_vtu_arrays(directory: str, soln_name: str, xyz: np.ndarray, values: np.ndarray,
+                     types: np.ndarray, binary: bool = False) -> None:
+    """The .pvtu / .vtu writer on host arrays (no device needed)."""
+    lib = capi.load()
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    values = np.ascontiguousarray(values, dtype=np.float64)
+    types = np.ascontiguousarray(types, dtype=np.uint8)
+    capi.check(lib.mcfd_write_vtu_arrays(str(directory).encode(), soln_name.encode(), len(xyz),
+                                         capi.dptr(xyz), capi.dptr(values), len(types),
+                                         types.ctypes.data_as(C.POINTER(C.c_uint8)), int(bool(binary))))
+
+
+def base64_encode(data: bytes) -> str:
+    """The library's base64 of VTK binary arrays."""
+    lib = capi.load()
+    buf = (C.c_uint8 * max(len(data), 1)).from_buffer_copy(data if data else b"\0")
+    n = C.c_int64()
+    capi.check(lib.mcfd_base64_encode(buf, len(data), None, 0, C.byref(n)))
+    out = C.create_string_buffer(n.value + 1)
+    capi.check(lib.mcfd_base64_encode(buf, len(data), out, n.value + 1, C.byref(n)))
+    return out.value.decode()
