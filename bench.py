@@ -905,6 +905,87 @@ def run_gpu(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# Output and restart on the headline mesh (64^3 Hex8, DGSEM p = 3, 83.9 M
+# values): the DataOnCells field transposition (Part::GatherSolutions /
+# ScatterSolutions) against HBM, the VTK sampling (Writer::Prepare) and the
+# restart file round trip through the C ABI.
+
+def run_output(args, rank, world, local_rank):
+    import torch
+    from pvcriemannsolvers_gb300 import Lobatto, build, cases, mesh as meshlib
+    build.build()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    m = meshlib.box((args.cells,) * 3, lengths=(10.0,) * 3, periodic=(True,) * 3)
+    u0 = np.ascontiguousarray(cases.vortex_ic(meshlib.node_coordinates(m, DEGREE).reshape(-1, 3)).ravel())
+    L = u0.size
+    sysm = Lobatto(m, DEGREE, "rusanov", cfl=CFL, device=local_rank)
+    stream = torch.cuda.Stream(device=dev)
+    sysm.set_stream(stream.cuda_stream)
+    sysm.SetSolutionColumn(u0)
+    fields = torch.empty(L, dtype=torch.float64, device=dev)
+    launches0 = sysm.launch_count()
+    times = {}
+    with ClockSampler(local_rank) as clocks:
+        for name, fn in (("gather", sysm.gather_fields_device), ("scatter", sysm.scatter_fields_device)):
+            for _ in range(args.warmup):
+                fn(fields.data_ptr(), L)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.steps):
+                fn(fields.data_ptr(), L)
+            e1.record(stream)
+            e1.synchronize()
+            times[name] = e0.elapsed_time(e1) / args.steps
+    launches = sysm.launch_count() - launches0
+    ok = bool(np.array_equal(sysm.GetSolutionColumn(), u0))
+    t0 = time.perf_counter()
+    xyz, values, types = sysm.vtk_sample()
+    sample_s = time.perf_counter() - t0
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "state.rst")
+        t0 = time.perf_counter()
+        sysm.write_restart(path, 0.0)
+        write_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        sysm.read_restart(path)
+        read_s = time.perf_counter() - t0
+    ok = ok and bool(np.array_equal(sysm.GetSolutionColumn(), u0))
+    sysm.close()
+    hbm_peak, peak_src = measured_peaks()
+    gbs = 16.0 * L / (times["gather"] * 1e-3) / 1e9
+    cpu = None
+    if not args.no_cpu:
+        t0 = time.perf_counter()
+        reps = 0
+        while time.perf_counter() - t0 < 5.0:
+            np.ascontiguousarray(u0.reshape(m.n_cells, -1).T)
+            reps += 1
+        el = time.perf_counter() - t0
+        cpu = {"value": 16.0 * L * reps / el / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
+               "sample": f"numpy transpose of the same column, {reps} reps, {el:.1f} s"}
+    line = {
+        "metric": "DataOnCells field gather (column -> fields) bandwidth", "value": gbs, "unit": "GB/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": times["gather"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"output of the vortex {args.cells}^3 Hex8 DGSEM p={DEGREE} column",
+                   "values": L, "cells": m.n_cells, "l2_flush": f"inputs larger than L2 ({8 * L / 1e9:.2f} GB)"},
+        "clocks": clocks.summary(), "gpu_launches": launches, "round_trip_bit_exact": ok,
+        "scatter_ms": times["scatter"], "scatter_gbs": 16.0 * L / (times["scatter"] * 1e-3) / 1e9,
+        "roofline": {"bound": "hbm", "kernel": "fields_transpose_kernel<true>", "achieved": gbs,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak, "traffic": None,
+                     "peak_source": peak_src, "algorithmic_bytes": 16 * L},
+        "e2e": {"vtk_sample_s": sample_s, "vtk_points": len(xyz),
+                "restart_write_s": write_s, "restart_read_s": read_s,
+                "restart_write_gbs": 8 * L / write_s / 1e9, "restart_read_gbs": 8 * L / read_s / 1e9,
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -915,9 +996,11 @@ def main():
     ap.add_argument("--cells", type=int, default=N_CELLS_1D, help="cells per direction (profiling runs a smaller case)")
     ap.add_argument("--form", default="both", choices=["both", "fp64", "mixed"],
                     help="precision form(s) to time; the line's value is the mixed form when timed")
-    ap.add_argument("--workload", default="vortex", choices=["vortex", "mixed_box", "ensemble", "quadrant"],
+    ap.add_argument("--workload", default="vortex",
+                    choices=["vortex", "mixed_box", "ensemble", "quadrant", "output"],
                     help="vortex: the headline DGSEM case; mixed_box: modal DG on hex + tet blocks; "
-                         "ensemble: 64 independent cases in one graph per step")
+                         "ensemble: 64 independent cases in one graph per step; output: field "
+                         "gather/scatter, VTK sampling and restart on the headline column")
     ap.add_argument("--quadrant-cells", type=int, nargs=3, default=[256, 256, 16], metavar=("NX", "NY", "NZ"),
                     help="mesh of the four-quadrant workload")
     ap.add_argument("--ensemble-scale", type=float, default=1.0,
@@ -941,6 +1024,9 @@ def main():
         return
     if args.workload == "quadrant":
         run_quadrant(args, rank, world, local_rank)
+        return
+    if args.workload == "output":
+        run_output(args, rank, world, local_rank)
         return
     if world > 1:
         import torch
