@@ -986,6 +986,69 @@ def run_output(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# Cell numbering: the headline step (mixed form) on the box's lexicographic
+# numbering, on a random renumbering (seed 0) and on the Hilbert order of the
+# random one (mesh.renumber_cells / mcfd_hilbert_order).
+
+def run_reorder(args, rank, world, local_rank):
+    import torch
+    from pvcriemannsolvers_gb300 import Lobatto, build, cases, mesh as meshlib
+    build.build()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    m = meshlib.box((args.cells,) * 3, lengths=(10.0,) * 3, periodic=(True,) * 3)
+    u0 = np.ascontiguousarray(cases.vortex_ic(meshlib.node_coordinates(m, DEGREE).reshape(-1, 3)).ravel())
+    L = u0.size
+    rng = np.random.default_rng(0)
+    shuffle = rng.permutation(m.n_cells)
+    shuffled = meshlib.renumber_cells(m, shuffle)
+    t0 = time.perf_counter()
+    hil = meshlib.hilbert_order(shuffled)
+    order_s = time.perf_counter() - t0
+    variants = {"lexicographic": (m, np.arange(m.n_cells)), "random": (shuffled, shuffle),
+                "hilbert_of_random": (meshlib.renumber_cells(shuffled, hil), shuffle[hil])}
+    res = {}
+    sols = {}
+    for name, (mm, order) in variants.items():
+        sysm = Lobatto(mm, DEGREE, "rusanov", cfl=CFL, device=local_rank, precision="mixed")
+        stream = torch.cuda.Stream(device=dev)
+        sysm.set_stream(stream.cuda_stream)
+        sysm.SetSolutionColumn(np.ascontiguousarray(u0.reshape(m.n_cells, -1)[order].ravel()))
+        sysm.autotune()
+        t = sysm.advance(args.warmup, 1e9, 3, 0.0)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(local_rank) as clocks:
+            with torch.cuda.stream(stream):
+                e0.record(stream)
+                t = sysm.advance(args.steps, 1e9, 3, t)
+                e1.record(stream)
+            e1.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        back = np.empty_like(u0.reshape(m.n_cells, -1))
+        back[order] = sysm.GetSolutionColumn().reshape(m.n_cells, -1)
+        sols[name] = back.ravel()
+        res[name] = {"ms_per_step": ms, "value": 3 * L / (ms * 1e-3), "kernel_ms": sysm.kernel_times(reps=3),
+                     "clocks": clocks.summary()}
+        sysm.close()
+    ref = sols["lexicographic"]
+    agree = {k: float(np.linalg.norm(v - ref) / np.linalg.norm(ref)) for k, v in sols.items()}
+    r = res["hilbert_of_random"]
+    line = {
+        "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
+        "config": {"workload": f"vortex {args.cells}^3 Hex8 DGSEM p={DEGREE} mixed, cells renumbered",
+                   "numbering": "Hilbert order (mcfd_hilbert_order) of a random renumbering",
+                   "l2_flush": f"inputs larger than L2 ({8 * L / 1e9:.2f} GB)"},
+        "clocks": r["clocks"], "hilbert_order_s": order_s,
+        "variants": res, "solution_rel_l2_vs_lexicographic": agree,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -997,7 +1060,7 @@ def main():
     ap.add_argument("--form", default="both", choices=["both", "fp64", "mixed"],
                     help="precision form(s) to time; the line's value is the mixed form when timed")
     ap.add_argument("--workload", default="vortex",
-                    choices=["vortex", "mixed_box", "ensemble", "quadrant", "output"],
+                    choices=["vortex", "mixed_box", "ensemble", "quadrant", "output", "reorder"],
                     help="vortex: the headline DGSEM case; mixed_box: modal DG on hex + tet blocks; "
                          "ensemble: 64 independent cases in one graph per step; output: field "
                          "gather/scatter, VTK sampling and restart on the headline column")
@@ -1027,6 +1090,9 @@ def main():
         return
     if args.workload == "output":
         run_output(args, rank, world, local_rank)
+        return
+    if args.workload == "reorder":
+        run_reorder(args, rank, world, local_rank)
         return
     if world > 1:
         import torch

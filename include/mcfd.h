@@ -265,6 +265,37 @@ int mcfd_stream_step(mcfd_handle *h, const double *host_in, double *host_out,
                      int32_t rk_order);
 int mcfd_stream_end(mcfd_handle *h);
 
+/* ---- mesh ingest ----
+ * Face connectivity from cells alone, as Part::BuildLocalFaces /
+ * BuildBoundaryFaces (mesh/part.hpp:932-1019, 1456-1545) derive it: (cell,
+ * local face) slots are keyed by their sorted node ids; equal keys pair into
+ * interior faces with the lower cell id as holder (the shuffler's
+ * [i_cell_small, i_cell_large] adjacency, mesh/shuffler.hpp:399-421).  Free
+ * slots are boundary faces: bface_nodes [n_bfaces][4] (a triangle's 4th entry
+ * is -1) with bface_group give their groups (free slots not listed get -1);
+ * periodic_groups [n_periodic][2] = (a, b) with periodic_shift [n_periodic][3]
+ * such that x(face of b) + shift = x(face of a) joins the two groups face by
+ * face (matched by centroid) into interior faces.  Output arrays in
+ * mcfd_mesh_desc form with capacity cap >= mcfd_face_slot_count(); order:
+ * interior and periodic faces by (holder, holder side), then boundary faces
+ * by (group, holder, side), ungrouped ones last.  MCFD_ERR_MESH with the
+ * reason in mcfd_build_error() for a face shared by three cells, a boundary
+ * element that is not a free face, or an unmatched periodic face. */
+int64_t mcfd_face_slot_count(int64_t n_cells, const int32_t *cell_type);
+int mcfd_build_faces(int64_t n_nodes, const double *xyz, int64_t n_cells,
+                     const int64_t *cell_nodes, const int32_t *cell_type,
+                     int64_t n_bfaces, const int64_t *bface_nodes,
+                     const int32_t *bface_group, int32_t n_periodic,
+                     const int32_t *periodic_groups, const double *periodic_shift,
+                     int64_t cap, int64_t *face_cells, int32_t *face_sides,
+                     int32_t *face_group, double *face_shift, int64_t *n_faces);
+const char *mcfd_build_error(void);
+/* order[k] = the point (cell centroid) at position k along a 3D Hilbert
+ * curve through the points' bounding cube (21 bits per axis; Skilling 2004).
+ * Renumbering cells in this order (in place of the reference's METIS
+ * shuffle, mesh/shuffler.hpp) keeps face neighbours close in memory. */
+int mcfd_hilbert_order(int64_t n, const double *points, int64_t *order);
+
 /* ---- output and restart ----
  * Writer<Part>::WriteSolutions (mesh/vtk.hpp:526-669): every cell is written
  * as a disconnected VTK element, Hex8 cells as Hexahedron27 (type 29) and

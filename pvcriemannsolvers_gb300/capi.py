@@ -91,6 +91,13 @@ SIGNATURES = {
     "mcfd_time_step": (C.c_int, [_P, C.c_double, C.c_int32, _D]),
     "mcfd_rk_step": (C.c_int, [_P, C.c_double, C.c_double, C.c_int32]),
     "mcfd_advance": (C.c_int, [_P, C.c_int32, C.c_double, C.c_int32, _D]),
+    "mcfd_face_slot_count": (C.c_int64, [C.c_int64, C.POINTER(C.c_int32)]),
+    "mcfd_build_faces": (C.c_int, [C.c_int64, _D, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
+                                   C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.c_int32,
+                                   C.POINTER(C.c_int32), _D, C.c_int64, C.POINTER(C.c_int64),
+                                   C.POINTER(C.c_int32), C.POINTER(C.c_int32), _D, C.POINTER(C.c_int64)]),
+    "mcfd_build_error": (C.c_char_p, []),
+    "mcfd_hilbert_order": (C.c_int, [C.c_int64, _D, C.POINTER(C.c_int64)]),
     "mcfd_vtk_point_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "mcfd_vtk_sample": (C.c_int, [_P, _D, _D, C.POINTER(C.c_uint8), C.c_int64]),
     "mcfd_write_vtu": (C.c_int, [_P, C.c_char_p, C.c_char_p, C.c_int32]),

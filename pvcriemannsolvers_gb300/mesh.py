@@ -330,3 +330,88 @@ def concat(*meshes: Mesh) -> Mesh:
         cell_type=np.ascontiguousarray(np.concatenate(ct).astype(np.int32)),
         meta={"blocks": [m.n_cells for m in meshes]},
     )
+
+
+# ---------------------------------------------------------------------------
+# Mesh ingest through the library's connectivity builder (mcfd_build_faces)
+# and the Hilbert cell order (mcfd_hilbert_order).
+
+def build(xyz, cell_nodes, cell_type=None, bface_nodes=None, bface_group=None,
+          periodic=()) -> Mesh:
+    """Mesh with faces built from the cells alone (Part::BuildLocalFaces /
+    BuildBoundaryFaces).  cell_nodes [cells, 8] (Tet4: first 4, rest -1);
+    bface_nodes [n, 4] boundary elements (triangles end in -1) with groups
+    bface_group; periodic: ((group_a, group_b, shift), ...) with
+    x(face of b) + shift = x(face of a)."""
+    import ctypes as C
+    from . import capi
+    lib = capi.load()
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    cn = np.ascontiguousarray(cell_nodes, dtype=np.int64)
+    ct = None if cell_type is None else np.ascontiguousarray(cell_type, dtype=np.int32)
+    bf = np.ascontiguousarray(np.zeros((0, 4)) if bface_nodes is None else bface_nodes, dtype=np.int64)
+    bg = np.ascontiguousarray(np.zeros(0) if bface_group is None else bface_group, dtype=np.int32)
+    pg = np.ascontiguousarray([[a, b] for a, b, _ in periodic] or np.zeros((0, 2)), dtype=np.int32)
+    ps = np.ascontiguousarray([list(s) for _, _, s in periodic] or np.zeros((0, 3)), dtype=np.float64)
+    P64, P32, PD = C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_double)
+    ct_p = None if ct is None else ct.ctypes.data_as(P32)
+    cap = int(lib.mcfd_face_slot_count(cn.shape[0], ct_p))
+    fc = np.empty((cap, 2), np.int64)
+    fs = np.empty((cap, 2), np.int32)
+    fg = np.empty(cap, np.int32)
+    fsh = np.empty((cap, 3), np.float64)
+    n = C.c_int64()
+    rc = lib.mcfd_build_faces(xyz.shape[0], xyz.ctypes.data_as(PD), cn.shape[0], cn.ctypes.data_as(P64), ct_p,
+                              bf.shape[0], bf.ctypes.data_as(P64), bg.ctypes.data_as(P32), pg.shape[0],
+                              pg.ctypes.data_as(P32), ps.ctypes.data_as(PD), cap, fc.ctypes.data_as(P64),
+                              fs.ctypes.data_as(P32), fg.ctypes.data_as(P32), fsh.ctypes.data_as(PD),
+                              C.byref(n))
+    if rc != 0:
+        raise capi.McfdError(rc, (lib.mcfd_build_error() or b"").decode())
+    k = n.value
+    return Mesh(xyz=xyz, cell_nodes=cn, face_cells=np.ascontiguousarray(fc[:k]),
+                face_sides=np.ascontiguousarray(fs[:k]), face_group=np.ascontiguousarray(fg[:k]),
+                face_shift=np.ascontiguousarray(fsh[:k]), cell_type=ct)
+
+
+def cell_centroids(m: Mesh) -> np.ndarray:
+    """Mean of each cell's corner nodes (8 for Hex8, 4 for Tet4)."""
+    if m.cell_type is None:
+        return m.xyz[m.cell_nodes].mean(axis=1)
+    tet = m.cell_type == TET4
+    out = m.xyz[m.cell_nodes[:, :4].clip(0)].mean(axis=1)
+    out[~tet] = m.xyz[m.cell_nodes[~tet]].mean(axis=1)
+    return out
+
+
+def hilbert_order(m: Mesh) -> np.ndarray:
+    """Cells in the order of a 3D Hilbert curve through their centroids."""
+    import ctypes as C
+    from . import capi
+    pts = np.ascontiguousarray(cell_centroids(m), dtype=np.float64)
+    order = np.empty(m.n_cells, dtype=np.int64)
+    capi.check(capi.load().mcfd_hilbert_order(m.n_cells, pts.ctypes.data_as(C.POINTER(C.c_double)),
+                                              order.ctypes.data_as(C.POINTER(C.c_int64))))
+    return order
+
+
+def renumber_cells(m: Mesh, order: np.ndarray) -> Mesh:
+    """The same mesh with cell k of the result = cell order[k] of m; faces
+    keep their holder / sharer roles and sides and are re-sorted by (new
+    holder, side), boundary faces after interior ones by (group, holder).
+    A column of m maps to the result by column.reshape(cells, -1)[order]."""
+    order = np.asarray(order, dtype=np.int64)
+    new_id = np.empty_like(order)
+    new_id[order] = np.arange(order.size, dtype=np.int64)
+    fc = m.face_cells.copy()
+    fc[:, 0] = new_id[fc[:, 0]]
+    fc[:, 1] = np.where(fc[:, 1] >= 0, new_id[np.maximum(fc[:, 1], 0)], -1)
+    inner = fc[:, 1] >= 0
+    grp = m.face_group.astype(np.int64)
+    key_group = np.where(inner, -1, np.where(grp < 0, np.iinfo(np.int64).max, grp))
+    o = np.lexsort((m.face_sides[:, 0], fc[:, 0], key_group, ~inner))
+    return Mesh(xyz=m.xyz, cell_nodes=np.ascontiguousarray(m.cell_nodes[order]),
+                face_cells=np.ascontiguousarray(fc[o]), face_sides=np.ascontiguousarray(m.face_sides[o]),
+                face_group=np.ascontiguousarray(m.face_group[o]), face_shift=np.ascontiguousarray(m.face_shift[o]),
+                cell_type=None if m.cell_type is None else np.ascontiguousarray(m.cell_type[order]),
+                shape=m.shape, lengths=m.lengths, origin=m.origin, periodic=m.periodic)

@@ -1,0 +1,130 @@
+"""Mesh ingest on the host (no GPU): the library's connectivity builder
+(mcfd_build_faces, the faces of Part::BuildLocalFaces / BuildBoundaryFaces)
+reproduces the generators' face tables index for index from cells and
+boundary elements alone, and the Hilbert cell order (mcfd_hilbert_order)
+is a locality-preserving permutation."""
+import numpy as np
+import pytest
+
+import oracle.orc as orc
+from pvcriemannsolvers_gb300 import capi, cases, mesh as meshlib
+
+HEX_FACE = np.array([[0, 3, 2, 1], [0, 1, 5, 4], [1, 2, 6, 5], [2, 3, 7, 6], [0, 4, 7, 3], [4, 5, 6, 7]])
+
+
+def boundary_elements(m):
+    """Boundary faces of m as element node lists (holder's local face) and groups."""
+    b = m.face_cells[:, 1] < 0
+    cells, sides = m.face_cells[b, 0], m.face_sides[b, 0]
+    nodes = np.full((cells.size, 4), -1, dtype=np.int64)
+    tet = np.zeros(cells.size, bool) if m.cell_type is None else m.cell_type[cells] == meshlib.TET4
+    hx = ~tet
+    nodes[hx] = m.cell_nodes[cells[hx][:, None], HEX_FACE[sides[hx]]]
+    nodes[tet, :3] = m.cell_nodes[cells[tet][:, None], meshlib.TET_FACES[sides[tet]]]
+    return nodes, m.face_group[b]
+
+
+def periodic_spec(m, periodic):
+    L = m.lengths
+    return [(2 * ax, 2 * ax + 1, tuple(-L[ax] if e == ax else 0.0 for e in range(3)))
+            for ax in range(3) if periodic[ax]]
+
+
+def same_faces(a, b):
+    assert np.array_equal(a.face_cells, b.face_cells)
+    assert np.array_equal(a.face_sides, b.face_sides)
+    assert np.array_equal(a.face_group, b.face_group)
+    assert np.array_equal(a.face_shift, b.face_shift)
+
+
+@pytest.mark.parametrize("maker", ["box", "tet_box"])
+@pytest.mark.parametrize("periodic", [(False, False, False), (True, False, True), (True, True, True)])
+def test_builder_reproduces_generators(maker, periodic):
+    make = getattr(meshlib, maker)
+    shape = (4, 3, 5) if maker == "box" else (3, 4, 3)
+    open_mesh = make(shape, lengths=(1.0, 0.8, 1.3), jitter=0.1, seed=7)
+    want = make(shape, lengths=(1.0, 0.8, 1.3), periodic=periodic, jitter=0.1, seed=7)
+    bn, bg = boundary_elements(open_mesh)
+    got = meshlib.build(open_mesh.xyz, open_mesh.cell_nodes, open_mesh.cell_type, bn, bg,
+                        periodic_spec(want, periodic))
+    same_faces(got, want)
+
+
+def canonical(m):
+    """Faces of m as a sorted table (concat orders them block by block)."""
+    t = np.column_stack([m.face_cells, m.face_sides, m.face_group, m.face_shift])
+    return t[np.lexsort(t[:, ::-1].T)]
+
+
+def test_builder_concat_and_ungrouped():
+    m = meshlib.concat(meshlib.box((2, 2, 2), jitter=0.1, seed=1), meshlib.tet_box((3, 3, 3), jitter=0.1, seed=2))
+    bn, bg = boundary_elements(m)
+    assert np.array_equal(canonical(meshlib.build(m.xyz, m.cell_nodes, m.cell_type, bn, bg)), canonical(m))
+    # without boundary elements every free face comes out ungrouped
+    got = meshlib.build(m.xyz, m.cell_nodes, m.cell_type)
+    assert np.all(got.face_group[got.face_cells[:, 1] < 0] == -1)
+    assert (got.face_cells[:, 1] >= 0).sum() == (m.face_cells[:, 1] >= 0).sum()
+
+
+def test_builder_errors():
+    m = meshlib.box((2, 2, 1))
+    bn, bg = boundary_elements(m)
+    with pytest.raises(capi.McfdError, match="more than two"):
+        meshlib.build(m.xyz, np.concatenate([m.cell_nodes, m.cell_nodes[:1]]))
+    inner_face = m.cell_nodes[0, HEX_FACE[2]][None, :]  # shared by cells 0 and 1
+    with pytest.raises(capi.McfdError, match="not a free face"):
+        meshlib.build(m.xyz, m.cell_nodes, None, inner_face, np.array([0], np.int32))
+    with pytest.raises(capi.McfdError, match="no partner"):
+        meshlib.build(m.xyz, m.cell_nodes, None, bn, bg, [(0, 1, (-0.5, 0.0, 0.0))])
+    bad = m.cell_nodes.copy()
+    bad[0, 0] = m.xyz.shape[0]
+    with pytest.raises(capi.McfdError, match="out of range"):
+        meshlib.build(m.xyz, bad)
+
+
+def test_hilbert_order_corners_form_a_gray_path():
+    pts = np.array([[i, j, k] for i in (0, 1) for j in (0, 1) for k in (0, 1)], dtype=float)
+    m = meshlib.Mesh(xyz=pts, cell_nodes=np.repeat(np.arange(8)[:, None], 8, axis=1),
+                     face_cells=np.zeros((0, 2), np.int64), face_sides=np.zeros((0, 2), np.int32),
+                     face_group=np.zeros(0, np.int32), face_shift=np.zeros((0, 3)))
+    order = meshlib.hilbert_order(m)
+    assert sorted(order.tolist()) == list(range(8))
+    steps = np.abs(np.diff(pts[order], axis=0)).sum(axis=1)
+    assert np.all(steps == 1)  # consecutive octants share a face
+
+
+def test_hilbert_order_locality():
+    m = meshlib.box((16, 16, 16))
+    rng = np.random.default_rng(0)
+    shuffled = meshlib.renumber_cells(m, rng.permutation(m.n_cells))
+    order = meshlib.hilbert_order(shuffled)
+    assert np.array_equal(np.sort(order), np.arange(m.n_cells))
+    h = meshlib.renumber_cells(shuffled, order)
+    inner = h.face_cells[:, 1] >= 0
+    gap_h = np.abs(h.face_cells[inner, 0] - h.face_cells[inner, 1]).mean()
+    gap_s = np.abs(shuffled.face_cells[inner, 0] - shuffled.face_cells[inner, 1]).mean()
+    assert gap_h < gap_s / 10
+
+
+@pytest.mark.parametrize("kind", ["hex", "mixed"])
+def test_renumbered_residual_is_permuted(kind):
+    """The oracle's residual on the renumbered mesh is the permuted residual."""
+    if kind == "hex":
+        m = meshlib.box((4, 3, 3), periodic=(True, False, True), jitter=0.1, seed=3)
+        p = 2
+        u = cases.smooth_ic(meshlib.node_coordinates(m, p).reshape(-1, 3)).ravel()
+        order = meshlib.hilbert_order(m)[::-1].copy()
+        r = orc.Mesh(m, p).residual(orc.RUSANOV, u)
+        mm = meshlib.renumber_cells(m, order)
+        r2 = orc.Mesh(mm, p).residual(orc.RUSANOV, u.reshape(m.n_cells, -1)[order].ravel())
+    else:
+        m = meshlib.concat(meshlib.box((2, 2, 2), periodic=(True,) * 3, jitter=0.1, seed=4),
+                           meshlib.tet_box((3, 3, 3), periodic=(True,) * 3, jitter=0.1, seed=5))
+        om = orc.Modal(m, 2)
+        u = om.project(cases.smooth_ic(om.points()[0]))
+        order = np.random.default_rng(1).permutation(m.n_cells)
+        r = om.residual(orc.HLLC, u)
+        mm = meshlib.renumber_cells(m, order)
+        r2 = orc.Modal(mm, 2).residual(orc.HLLC, u.reshape(m.n_cells, -1)[order].ravel())
+    want = r.reshape(m.n_cells, -1)[order].ravel()
+    assert np.linalg.norm(r2 - want) <= 1e-13 * np.linalg.norm(want)
