@@ -290,6 +290,23 @@ int mcfd_build_faces(int64_t n_nodes, const double *xyz, int64_t n_cells,
                      int64_t cap, int64_t *face_cells, int32_t *face_sides,
                      int32_t *face_group, double *face_shift, int64_t *n_faces);
 const char *mcfd_build_error(void);
+/* Legacy VTK unstructured grid reader (ASCII or BINARY; CELLS in the classic
+ * or the version-5 OFFSETS / CONNECTIVITY layout): hexahedra (12) and
+ * tetrahedra (10) become cells in mcfd_mesh_desc form (VTK and CGNS share
+ * their corner order), quads (9) and triangles (5) boundary elements whose
+ * group is the integral CELL_DATA array named group_array (NULL: the first
+ * single-component one; 0 without any).  Feed the result to
+ * mcfd_build_faces.  MCFD_ERR_IO with the reason in mcfd_vtk_error(). */
+typedef struct mcfd_vtk_mesh mcfd_vtk_mesh;
+int mcfd_vtk_read(const char *path, const char *group_array, mcfd_vtk_mesh **out);
+int mcfd_vtk_mesh_sizes(const mcfd_vtk_mesh *m, int64_t *n_nodes, int64_t *n_cells,
+                        int64_t *n_bfaces);
+/* xyz [n_nodes][3], cell_nodes [n_cells][8] (Tet4: 4 then -1), cell_type
+ * [n_cells], bface_nodes [n_bfaces][4] (triangles end in -1), bface_group. */
+int mcfd_vtk_mesh_arrays(const mcfd_vtk_mesh *m, double *xyz, int64_t *cell_nodes,
+                         int32_t *cell_type, int64_t *bface_nodes, int32_t *bface_group);
+void mcfd_vtk_mesh_destroy(mcfd_vtk_mesh *m);
+const char *mcfd_vtk_error(void);
 /* order[k] = the point (cell centroid) at position k along a 3D Hilbert
  * curve through the points' bounding cube (21 bits per axis; Skilling 2004).
  * Renumbering cells in this order (in place of the reference's METIS

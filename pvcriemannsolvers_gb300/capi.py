@@ -97,6 +97,13 @@ SIGNATURES = {
                                    C.POINTER(C.c_int32), _D, C.c_int64, C.POINTER(C.c_int64),
                                    C.POINTER(C.c_int32), C.POINTER(C.c_int32), _D, C.POINTER(C.c_int64)]),
     "mcfd_build_error": (C.c_char_p, []),
+    "mcfd_vtk_read": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(C.c_void_p)]),
+    "mcfd_vtk_mesh_sizes": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                      C.POINTER(C.c_int64)]),
+    "mcfd_vtk_mesh_arrays": (C.c_int, [C.c_void_p, _D, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
+                                       C.POINTER(C.c_int64), C.POINTER(C.c_int32)]),
+    "mcfd_vtk_mesh_destroy": (None, [C.c_void_p]),
+    "mcfd_vtk_error": (C.c_char_p, []),
     "mcfd_hilbert_order": (C.c_int, [C.c_int64, _D, C.POINTER(C.c_int64)]),
     "mcfd_vtk_point_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "mcfd_vtk_sample": (C.c_int, [_P, _D, _D, C.POINTER(C.c_uint8), C.c_int64]),

@@ -1,0 +1,305 @@
+// Mesh ingest: legacy VTK unstructured grids (the reference keeps its input
+// meshes as legacy .vtk files next to the gmsh scripts, input/*.vtk, and
+// converts them to CGNS; CGNS needs HDF5, so this reader is the ingest path
+// here).  ASCII and BINARY (big-endian) files, the classic CELLS layout and
+// the OFFSETS / CONNECTIVITY layout of file version 5.  Hexahedra (VTK type
+// 12) and tetrahedra (10) become cells (VTK and CGNS share their corner
+// order), quadrilaterals (9) and triangles (5) boundary elements; vertices,
+// lines and other types are skipped.  Boundary groups come from an integer
+// (or integral-valued) CELL_DATA array, SCALARS or FIELD, by name or the first
+// one.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/mcfd.h"
+
+struct mcfd_vtk_mesh {
+  std::vector<double> xyz;
+  std::vector<int64_t> cell_nodes;  // [cells][8]
+  std::vector<int32_t> cell_type;   // 0 Hex8, 1 Tet4
+  std::vector<int64_t> bface_nodes; // [bfaces][4]
+  std::vector<int32_t> bface_group;
+};
+
+namespace {
+
+thread_local std::string g_vtk_error;
+
+class Reader {
+ public:
+  explicit Reader(const std::string &path) : in_(path, std::ios::in | std::ios::binary) {}
+  bool ok() const { return (bool)in_; }
+  bool binary = false;
+
+  // next whitespace-separated token (skips blank lines); the whitespace
+  // after it stays in the stream, so line() then takes the rest of the line
+  bool token(std::string *t) {
+    t->clear();
+    while (in_.peek() != EOF && std::isspace(in_.peek())) in_.get();
+    while (in_.peek() != EOF && !std::isspace(in_.peek())) t->push_back((char)in_.get());
+    return !t->empty();
+  }
+  bool line(std::string *l) { return (bool)std::getline(in_, *l); }
+
+  // n values of the declared VTK type into doubles / int64
+  template <class T>
+  bool values(int64_t n, const std::string &type, std::vector<T> *out) {
+    out->resize(n);
+    if (!binary) {
+      std::string t;
+      for (int64_t i = 0; i < n; ++i) {
+        if (!token(&t)) return false;
+        (*out)[i] = (T)std::strtod(t.c_str(), nullptr);
+      }
+      return true;
+    }
+    // binary: skip the single newline after the header line, big-endian data
+    int size = 0;
+    bool real = false;
+    if (type == "float") size = 4, real = true;
+    else if (type == "double") size = 8, real = true;
+    else if (type == "int" || type == "unsigned_int" || type == "vtktypeint32") size = 4;
+    else if (type == "long" || type == "unsigned_long" || type == "vtktypeint64") size = 8;
+    else if (type == "short" || type == "unsigned_short") size = 2;
+    else if (type == "char" || type == "unsigned_char") size = 1;
+    else return false;
+    std::vector<unsigned char> raw((size_t)n * size);
+    if (n > 0 && !in_.read(reinterpret_cast<char *>(raw.data()), (std::streamsize)raw.size())) return false;
+    for (int64_t i = 0; i < n; ++i) {
+      uint64_t v = 0;
+      for (int b = 0; b < size; ++b) v = (v << 8) | raw[(size_t)i * size + b];
+      if (real && size == 4) {
+        float f;
+        const uint32_t w = (uint32_t)v;
+        std::memcpy(&f, &w, 4);
+        (*out)[i] = (T)f;
+      } else if (real) {
+        double d;
+        std::memcpy(&d, &v, 8);
+        (*out)[i] = (T)d;
+      } else {
+        const bool is_signed = type.rfind("unsigned", 0) != 0 && type != "unsigned_char";
+        int64_t s = (int64_t)v;
+        if (is_signed && size < 8 && (v >> (8 * size - 1)) & 1) s = (int64_t)(v | (~0ull << (8 * size)));
+        (*out)[i] = (T)s;
+      }
+    }
+    return true;
+  }
+  // binary data blocks end at the next newline
+  void after_binary() {
+    if (binary) {
+      std::string rest;
+      std::getline(in_, rest);
+    }
+  }
+
+ private:
+  std::ifstream in_;
+};
+
+int vtk_fail(const std::string &msg) {
+  g_vtk_error = msg;
+  return MCFD_ERR_IO;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *mcfd_vtk_error(void) { return g_vtk_error.c_str(); }
+
+int mcfd_vtk_read(const char *path, const char *group_array, mcfd_vtk_mesh **out) {
+  g_vtk_error.clear();
+  if (!path || !out) return MCFD_ERR_ARGUMENT;
+  *out = nullptr;
+  Reader r(path);
+  if (!r.ok()) return vtk_fail(std::string("cannot open ") + path);
+  std::string l;
+  if (!r.line(&l) || l.rfind("# vtk DataFile", 0) != 0) return vtk_fail("not a legacy VTK file");
+  r.line(&l);  // title
+  if (!r.line(&l)) return vtk_fail("truncated header");
+  while (!l.empty() && std::isspace((unsigned char)l.back())) l.pop_back();
+  if (l == "BINARY") r.binary = true;
+  else if (l != "ASCII") return vtk_fail("expected ASCII or BINARY");
+  std::string t, type;
+  if (!r.token(&t) || t != "DATASET" || !r.token(&t) || t != "UNSTRUCTURED_GRID")
+    return vtk_fail("only DATASET UNSTRUCTURED_GRID is read");
+  std::vector<double> xyz;
+  std::vector<int64_t> conn, offsets, types;
+  std::vector<double> groups;
+  int64_t n_points = -1, n_cells = -1, n_attr = -1;
+  bool have_groups = false, cell_data = false;
+  while (r.token(&t)) {
+    if (t == "POINTS") {
+      r.token(&t);
+      n_points = std::atoll(t.c_str());
+      r.token(&type);
+      r.line(&l);
+      if (!r.values(3 * n_points, type, &xyz)) return vtk_fail("bad POINTS block");
+      r.after_binary();
+    } else if (t == "CELLS") {
+      std::string a, b;
+      r.token(&a);
+      r.token(&b);
+      r.line(&l);
+      // classic layout: CELLS n size, then (npts id ...) per cell; version 5:
+      // CELLS n_offsets n_conn, then OFFSETS / CONNECTIVITY blocks
+      std::string next;
+      const int64_t na = std::atoll(a.c_str()), nb = std::atoll(b.c_str());
+      std::vector<int64_t> flat;
+      // peek: version-5 files put the OFFSETS keyword next
+      if (!r.token(&next)) return vtk_fail("truncated CELLS");
+      if (next == "OFFSETS") {
+        r.token(&type);
+        r.line(&l);
+        if (!r.values(na, type, &offsets)) return vtk_fail("bad OFFSETS block");
+        r.after_binary();
+        if (!r.token(&next) || next != "CONNECTIVITY") return vtk_fail("expected CONNECTIVITY");
+        r.token(&type);
+        r.line(&l);
+        if (!r.values(nb, type, &conn)) return vtk_fail("bad CONNECTIVITY block");
+        r.after_binary();
+        n_cells = na - 1;
+        if (n_cells < 0 || offsets.front() != 0 || offsets.back() != nb) return vtk_fail("bad OFFSETS");
+        for (int64_t c = 0; c < n_cells; ++c)
+          if (offsets[c + 1] < offsets[c]) return vtk_fail("bad OFFSETS");
+      } else {
+        n_cells = na;
+        if (r.binary) return vtk_fail("binary classic CELLS layout: write file version 5 (OFFSETS)");
+        if (na < 0 || nb < 1) return vtk_fail("bad CELLS header");
+        flat.resize(nb);
+        flat[0] = std::atoll(next.c_str());
+        for (int64_t i = 1; i < nb; ++i) {
+          if (!r.token(&t)) return vtk_fail("truncated CELLS");
+          flat[i] = std::atoll(t.c_str());
+        }
+        offsets.assign(1, 0);
+        for (int64_t i = 0, c = 0; c < n_cells; ++c) {
+          const int64_t k = flat[i];
+          if (k < 0 || i + 1 + k > nb) return vtk_fail("bad CELLS entry");
+          conn.insert(conn.end(), flat.begin() + i + 1, flat.begin() + i + 1 + k);
+          offsets.push_back((int64_t)conn.size());
+          i += 1 + k;
+        }
+      }
+    } else if (t == "CELL_TYPES") {
+      r.token(&t);
+      const int64_t n = std::atoll(t.c_str());
+      r.line(&l);
+      if (!r.values(n, "int", &types)) return vtk_fail("bad CELL_TYPES block");
+      r.after_binary();
+    } else if (t == "CELL_DATA" || t == "POINT_DATA") {
+      cell_data = t == "CELL_DATA";
+      r.token(&t);
+      n_attr = std::atoll(t.c_str());
+    } else if (t == "SCALARS" && n_attr >= 0) {
+      std::string name;
+      r.token(&name);
+      r.token(&type);
+      r.line(&l);  // optional component count
+      const int nc = std::max(1, std::atoi(l.c_str()));
+      r.token(&t);  // LOOKUP_TABLE
+      r.token(&t);  // its name
+      r.line(&l);
+      std::vector<double> v;
+      if (!r.values(n_attr * nc, type, &v)) return vtk_fail("bad SCALARS block");
+      r.after_binary();
+      if (cell_data && !have_groups && nc == 1 && (!group_array || name == group_array)) {
+        groups = v;
+        have_groups = true;
+      }
+    } else if (t == "FIELD" && n_attr >= 0) {
+      r.token(&t);  // field name
+      r.token(&t);
+      const int n_arrays = std::atoi(t.c_str());
+      r.line(&l);
+      for (int a = 0; a < n_arrays; ++a) {
+        std::string name, snc, snt;
+        r.token(&name);
+        r.token(&snc);
+        r.token(&snt);
+        r.token(&type);
+        r.line(&l);
+        const int64_t nc = std::atoll(snc.c_str()), nt = std::atoll(snt.c_str());
+        std::vector<double> v;
+        if (!r.values(nc * nt, type, &v)) return vtk_fail("bad FIELD array");
+        r.after_binary();
+        if (cell_data && !have_groups && nc == 1 && nt == n_attr && (!group_array || name == group_array)) {
+          groups = v;
+          have_groups = true;
+        }
+      }
+    } else if ((t == "VECTORS" || t == "NORMALS" || t == "TENSORS") && n_attr >= 0) {
+      std::string name;
+      r.token(&name);
+      r.token(&type);
+      r.line(&l);
+      std::vector<double> v;
+      if (!r.values(n_attr * (t == "TENSORS" ? 9 : 3), type, &v)) return vtk_fail("bad attribute block");
+      r.after_binary();
+    } else if (t == "METADATA") {
+      // skip until a blank line
+      while (r.line(&l) && !l.empty()) {}
+    } else {
+      return vtk_fail("unexpected keyword " + t);
+    }
+  }
+  if (n_points < 0 || n_cells < 0 || (int64_t)types.size() != n_cells ||
+      (int64_t)offsets.size() != n_cells + 1)
+    return vtk_fail("POINTS, CELLS and CELL_TYPES are required and must agree");
+  if (have_groups && (int64_t)groups.size() != n_cells) return vtk_fail("CELL_DATA size mismatch");
+  auto *m = new mcfd_vtk_mesh();
+  m->xyz = std::move(xyz);
+  for (int64_t c = 0; c < n_cells; ++c) {
+    const int64_t b = offsets[c], k = offsets[c + 1] - b;
+    auto node = [&](int i) { return conn[b + i]; };
+    for (int64_t i = 0; i < k; ++i)
+      if (node((int)i) < 0 || node((int)i) >= n_points) {
+        delete m;
+        return vtk_fail("cell " + std::to_string(c) + ": node index out of range");
+      }
+    const int vt = (int)types[c];
+    if ((vt == 12 && k == 8) || (vt == 10 && k == 4)) {
+      for (int i = 0; i < 8; ++i) m->cell_nodes.push_back(i < k ? node(i) : -1);
+      m->cell_type.push_back(vt == 10 ? 1 : 0);
+    } else if ((vt == 9 && k == 4) || (vt == 5 && k == 3)) {
+      for (int i = 0; i < 4; ++i) m->bface_nodes.push_back(i < k ? node(i) : -1);
+      const double g = have_groups ? groups[c] : 0.0;
+      m->bface_group.push_back((int32_t)std::lround(g));
+    }
+  }
+  *out = m;
+  return MCFD_OK;
+}
+
+int mcfd_vtk_mesh_sizes(const mcfd_vtk_mesh *m, int64_t *n_nodes, int64_t *n_cells,
+                        int64_t *n_bfaces) {
+  if (!m || !n_nodes || !n_cells || !n_bfaces) return MCFD_ERR_ARGUMENT;
+  *n_nodes = (int64_t)m->xyz.size() / 3;
+  *n_cells = (int64_t)m->cell_type.size();
+  *n_bfaces = (int64_t)m->bface_group.size();
+  return MCFD_OK;
+}
+
+int mcfd_vtk_mesh_arrays(const mcfd_vtk_mesh *m, double *xyz, int64_t *cell_nodes,
+                         int32_t *cell_type, int64_t *bface_nodes, int32_t *bface_group) {
+  if (!m || !xyz || !cell_nodes || !cell_type || (!m->bface_group.empty() && (!bface_nodes || !bface_group)))
+    return MCFD_ERR_ARGUMENT;
+  std::copy(m->xyz.begin(), m->xyz.end(), xyz);
+  std::copy(m->cell_nodes.begin(), m->cell_nodes.end(), cell_nodes);
+  std::copy(m->cell_type.begin(), m->cell_type.end(), cell_type);
+  std::copy(m->bface_nodes.begin(), m->bface_nodes.end(), bface_nodes);
+  std::copy(m->bface_group.begin(), m->bface_group.end(), bface_group);
+  return MCFD_OK;
+}
+
+void mcfd_vtk_mesh_destroy(mcfd_vtk_mesh *m) { delete m; }
+
+}  // extern "C"

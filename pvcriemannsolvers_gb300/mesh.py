@@ -415,3 +415,98 @@ def renumber_cells(m: Mesh, order: np.ndarray) -> Mesh:
                 face_group=np.ascontiguousarray(m.face_group[o]), face_shift=np.ascontiguousarray(m.face_shift[o]),
                 cell_type=None if m.cell_type is None else np.ascontiguousarray(m.cell_type[order]),
                 shape=m.shape, lengths=m.lengths, origin=m.origin, periodic=m.periodic)
+
+
+def boundary_elements(m: Mesh) -> tuple[np.ndarray, np.ndarray]:
+    """Boundary faces of m as element node lists [n, 4] (the holder's local
+    face; triangles end in -1) and their groups."""
+    hex_face = np.array([[0, 3, 2, 1], [0, 1, 5, 4], [1, 2, 6, 5], [2, 3, 7, 6], [0, 4, 7, 3], [4, 5, 6, 7]])
+    b = m.face_cells[:, 1] < 0
+    cells, sides = m.face_cells[b, 0], m.face_sides[b, 0]
+    nodes = np.full((cells.size, 4), -1, dtype=np.int64)
+    tet = np.zeros(cells.size, bool) if m.cell_type is None else m.cell_type[cells] == TET4
+    nodes[~tet] = m.cell_nodes[cells[~tet][:, None], hex_face[sides[~tet]]]
+    nodes[tet, :3] = m.cell_nodes[cells[tet][:, None], TET_FACES[sides[tet]]]
+    return nodes, m.face_group[b].astype(np.int32)
+
+
+def write_vtk(path, m: Mesh, binary: bool = False, classic: bool = False) -> None:
+    """Legacy VTK unstructured grid of m: its cells (Hex8 -> 12, Tet4 -> 10),
+    its boundary faces as quads / triangles (9 / 5) and a CELL_DATA int
+    array "group" (-1 on volume cells).  Version-5 OFFSETS / CONNECTIVITY
+    layout, or the classic CELLS layout with classic=True (ASCII only)."""
+    bn, bg = boundary_elements(m)
+    tet = np.zeros(m.n_cells, bool) if m.cell_type is None else m.cell_type == TET4
+    conn, offs, types = [], [0], []
+    for c in range(m.n_cells):
+        k = 4 if tet[c] else 8
+        conn.append(m.cell_nodes[c, :k]); offs.append(offs[-1] + k); types.append(10 if tet[c] else 12)
+    for f in range(bn.shape[0]):
+        k = 3 if bn[f, 3] < 0 else 4
+        conn.append(bn[f, :k]); offs.append(offs[-1] + k); types.append(5 if k == 3 else 9)
+    conn = np.concatenate(conn).astype(np.int64) if conn else np.zeros(0, np.int64)
+    offs = np.asarray(offs, dtype=np.int64)
+    types = np.asarray(types, dtype=np.int32)
+    groups = np.concatenate([np.full(m.n_cells, -1, np.int32), bg]).astype(np.int32)
+    n = types.size
+    with open(path, "wb") as f:
+        w = lambda s: f.write(s.encode())  # noqa: E731
+        w("# vtk DataFile Version 5.1\nmesh written by pvcriemannsolvers_gb300\n")
+        w("BINARY\n" if binary else "ASCII\n")
+        w("DATASET UNSTRUCTURED_GRID\n")
+        w(f"POINTS {m.xyz.shape[0]} double\n")
+        if binary:
+            f.write(np.ascontiguousarray(m.xyz, dtype=">f8").tobytes()); w("\n")
+        else:
+            w("\n".join(" ".join(repr(float(v)) for v in p) for p in m.xyz) + "\n")
+        if classic:
+            if binary:
+                raise ValueError("the classic CELLS layout is written in ASCII only")
+            w(f"CELLS {n} {n + conn.size}\n")
+            for c in range(n):
+                ids = conn[offs[c]:offs[c + 1]]
+                w(f"{ids.size} " + " ".join(str(int(i)) for i in ids) + "\n")
+        else:
+            w(f"CELLS {n + 1} {conn.size}\n")
+            for name, arr in (("OFFSETS", offs), ("CONNECTIVITY", conn)):
+                w(f"{name} vtktypeint64\n")
+                if binary:
+                    f.write(np.ascontiguousarray(arr, dtype=">i8").tobytes()); w("\n")
+                else:
+                    w(" ".join(str(int(v)) for v in arr) + "\n")
+        w(f"CELL_TYPES {n}\n")
+        if binary:
+            f.write(np.ascontiguousarray(types, dtype=">i4").tobytes()); w("\n")
+        else:
+            w("\n".join(str(int(t)) for t in types) + "\n")
+        w(f"CELL_DATA {n}\nSCALARS group int 1\nLOOKUP_TABLE default\n")
+        if binary:
+            f.write(np.ascontiguousarray(groups, dtype=">i4").tobytes()); w("\n")
+        else:
+            w("\n".join(str(int(g)) for g in groups) + "\n")
+
+
+def read_vtk(path, periodic=(), group_array: str | None = None) -> Mesh:
+    """Mesh from a legacy VTK unstructured grid (mcfd_vtk_read) with faces
+    from the library's connectivity builder; periodic as in build()."""
+    import ctypes as C
+    from . import capi
+    lib = capi.load()
+    h = C.c_void_p()
+    rc = lib.mcfd_vtk_read(str(path).encode(), None if group_array is None else group_array.encode(), C.byref(h))
+    if rc != 0:
+        raise capi.McfdError(rc, (lib.mcfd_vtk_error() or b"").decode())
+    try:
+        nn, nc, nb = C.c_int64(), C.c_int64(), C.c_int64()
+        capi.check(lib.mcfd_vtk_mesh_sizes(h, C.byref(nn), C.byref(nc), C.byref(nb)))
+        xyz = np.empty((nn.value, 3))
+        cn = np.empty((nc.value, 8), np.int64)
+        ct = np.empty(nc.value, np.int32)
+        bf = np.empty((nb.value, 4), np.int64)
+        bg = np.empty(nb.value, np.int32)
+        P64, P32 = C.POINTER(C.c_int64), C.POINTER(C.c_int32)
+        capi.check(lib.mcfd_vtk_mesh_arrays(h, xyz.ctypes.data_as(C.POINTER(C.c_double)), cn.ctypes.data_as(P64),
+                                            ct.ctypes.data_as(P32), bf.ctypes.data_as(P64), bg.ctypes.data_as(P32)))
+    finally:
+        lib.mcfd_vtk_mesh_destroy(h)
+    return build(xyz, cn, ct if np.any(ct == TET4) else None, bf, bg, periodic)

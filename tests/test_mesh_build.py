@@ -128,3 +128,35 @@ def test_renumbered_residual_is_permuted(kind):
         r2 = orc.Modal(mm, 2).residual(orc.HLLC, u.reshape(m.n_cells, -1)[order].ravel())
     want = r.reshape(m.n_cells, -1)[order].ravel()
     assert np.linalg.norm(r2 - want) <= 1e-13 * np.linalg.norm(want)
+
+
+@pytest.mark.parametrize("fmt", ["ascii", "binary", "classic"])
+@pytest.mark.parametrize("maker", ["box", "tet_box"])
+def test_vtk_round_trip(tmp_path, fmt, maker):
+    """A mesh written as legacy VTK and read back through mcfd_vtk_read +
+    mcfd_build_faces has the generator's faces, periodic planes included."""
+    make = getattr(meshlib, maker)
+    periodic = (True, False, True)
+    open_mesh = make((3, 4, 3), lengths=(1.0, 0.8, 1.3), jitter=0.1, seed=9)
+    want = make((3, 4, 3), lengths=(1.0, 0.8, 1.3), periodic=periodic, jitter=0.1, seed=9)
+    path = tmp_path / "m.vtk"
+    meshlib.write_vtk(path, open_mesh, binary=fmt == "binary", classic=fmt == "classic")
+    got = meshlib.read_vtk(path, periodic_spec(want, periodic))
+    assert np.array_equal(got.xyz, open_mesh.xyz)
+    assert np.array_equal(got.cell_nodes, open_mesh.cell_nodes)
+    same_faces(got, want)
+
+
+def test_vtk_reader_errors(tmp_path):
+    bad = tmp_path / "bad.vtk"
+    bad.write_text("not a vtk file\n")
+    with pytest.raises(capi.McfdError, match="legacy VTK"):
+        meshlib.read_vtk(bad)
+    with pytest.raises(capi.McfdError, match="cannot open"):
+        meshlib.read_vtk(tmp_path / "missing.vtk")
+    m = meshlib.box((2, 1, 1))
+    meshlib.write_vtk(bad, m)
+    text = bad.read_text().replace("CELL_TYPES", "CELL_TYPEZ")
+    bad.write_text(text)
+    with pytest.raises(capi.McfdError, match="unexpected keyword"):
+        meshlib.read_vtk(bad)
