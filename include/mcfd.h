@@ -99,15 +99,26 @@ typedef struct mcfd_bc_state {
   double b[MCFD_K];
 } mcfd_bc_state;
 
-enum mcfd_cell_type { MCFD_HEX8 = 0, MCFD_TET4 = 1 };
+/* Element types and their maps (coordinate/hexahedron.hpp Hexahedron8 /
+ * Hexahedron20 / Hexahedron27, coordinate/tetrahedron.hpp Tetrahedron4 /
+ * Tetrahedron10), nodes in CGNS order.  The quadratic types give curved
+ * cells and faces; the hexahedra run every scheme, the tetrahedra the MODAL
+ * scheme; the WENO limiter takes Hex8 cells only. */
+enum mcfd_cell_type {
+  MCFD_HEX8 = 0,
+  MCFD_TET4 = 1,
+  MCFD_HEX27 = 2,
+  MCFD_TET10 = 3,
+  MCFD_HEX20 = 4
+};
 
 /* Unstructured mesh, the input that replaces mesh::part::Part
  * (include/mini/mesh/part.hpp:97-291):
  *   xyz          [n_nodes][3] node coordinates
- *   cell_nodes   [n_cells][8] node ids in CGNS order; a Tet4 cell uses the
- *                first 4 slots (the rest are ignored)
+ *   cell_nodes   [n_cells][cell_node_stride] node ids in CGNS order; a cell
+ *                uses the first 4 / 8 / 10 / 20 / 27 slots of its type (the
+ *                rest are ignored)
  *   cell_type    [n_cells] enum mcfd_cell_type, or NULL for all Hex8.
- *                Tet4 cells are accepted by the MODAL scheme only.
  *   face_cells   [n_faces][2] holder, sharer (-1 on a boundary).  The face
  *                normal points from the holder to the sharer (outward on a
  *                boundary), as in part.hpp:1518-1538.
@@ -131,6 +142,7 @@ typedef struct mcfd_mesh_desc {
   const int32_t *face_sides;
   const int32_t *face_group;
   const double *face_shift;
+  int32_t cell_node_stride; /* slots per cell in cell_nodes; 0 means 8 */
 } mcfd_mesh_desc;
 
 /* Spatial schemes:
@@ -268,7 +280,8 @@ int mcfd_stream_end(mcfd_handle *h);
 /* ---- mesh ingest ----
  * Face connectivity from cells alone, as Part::BuildLocalFaces /
  * BuildBoundaryFaces (mesh/part.hpp:932-1019, 1456-1545) derive it: (cell,
- * local face) slots are keyed by their sorted node ids; equal keys pair into
+ * local face) slots are keyed by their sorted corner ids (cell_nodes with
+ * cell_node_stride slots per cell, 0 meaning 8); equal keys pair into
  * interior faces with the lower cell id as holder (the shuffler's
  * [i_cell_small, i_cell_large] adjacency, mesh/shuffler.hpp:399-421).  Free
  * slots are boundary faces: bface_nodes [n_bfaces][4] (a triangle's 4th entry
@@ -284,7 +297,7 @@ int mcfd_stream_end(mcfd_handle *h);
 int64_t mcfd_face_slot_count(int64_t n_cells, const int32_t *cell_type);
 int mcfd_build_faces(int64_t n_nodes, const double *xyz, int64_t n_cells,
                      const int64_t *cell_nodes, const int32_t *cell_type,
-                     int64_t n_bfaces, const int64_t *bface_nodes,
+                     int32_t cell_node_stride, int64_t n_bfaces, const int64_t *bface_nodes,
                      const int32_t *bface_group, int32_t n_periodic,
                      const int32_t *periodic_groups, const double *periodic_shift,
                      int64_t cap, int64_t *face_cells, int32_t *face_sides,

@@ -82,12 +82,15 @@ void orc_flux_boundary(int riemann, int bc_kind, const double *frame,
 typedef struct orc_mesh orc_mesh;
 
 /* The mesh description shared with the product (see include/mcfd.h).
- * cell_nodes: 8 entries per cell, CGNS order; faces: holder, sharer (-1 on a
+ * cell_nodes: stride entries per cell (0: 8), CGNS order; cell_type NULL
+ * for all Hex8, else ORC_CELL_HEX8 / HEX27 / HEX20 (the Hex27 / Hex20 maps of
+ * coordinate/hexahedron.hpp give curved cells); faces: holder, sharer (-1 on a
  * boundary), the local face index on each side, the boundary group (-1 for
  * interior faces) and an optional periodic shift such that
  * x(sharer side) + shift = x(holder side). */
 orc_mesh *orc_mesh_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
-                          const int64_t *cell_nodes, int64_t n_faces,
+                          const int64_t *cell_nodes, const int32_t *cell_type,
+                          int32_t stride, int64_t n_faces,
                           const int64_t *face_cells, const int32_t *face_sides,
                           const int32_t *face_group, const double *face_shift,
                           int degree);
@@ -163,14 +166,15 @@ int orc_rk_update_limited(const orc_mesh *m, int riemann, int n_bc,
                           double eps);
 
 /* ---- modal DG: dg::General over Projection on Hex8 / Tet4 (orc_modal.c) ---- */
-enum { ORC_CELL_HEX8 = 0, ORC_CELL_TET4 = 1 };
+enum { ORC_CELL_HEX8 = 0, ORC_CELL_TET4 = 1, ORC_CELL_HEX27 = 2, ORC_CELL_TET10 = 3,
+       ORC_CELL_HEX20 = 4 };
 typedef struct orc_modal orc_modal;
 /* Same mesh description as orc_mesh_create plus cell types (NULL: all Hex8);
  * a Tet4 cell uses the first 4 of its 8 cell_nodes entries (CGNS order) and
  * local faces 0..3 of Tetrahedron4::faces_.  Column layout per cell: [M][K]. */
 orc_modal *orc_modal_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
                             const int64_t *cell_nodes, const int32_t *cell_type,
-                            int64_t n_faces, const int64_t *face_cells,
+                            int32_t stride, int64_t n_faces, const int64_t *face_cells,
                             const int32_t *face_sides, const int32_t *face_group,
                             const double *face_shift, int degree);
 void orc_modal_destroy(orc_modal *m);

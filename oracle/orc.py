@@ -54,7 +54,8 @@ def load() -> C.CDLL:
             "orc_flux_1d": (None, [C.c_int, _D, _D, _D]),
             "orc_flux_rotated": (None, [C.c_int, _D, _D, _D, _D]),
             "orc_flux_boundary": (None, [C.c_int, C.c_int, _D, _D, _D, _D]),
-            "orc_mesh_create": (C.c_void_p, [C.c_int64, _D, C.c_int64, C.POINTER(C.c_int64), C.c_int64,
+            "orc_mesh_create": (C.c_void_p, [C.c_int64, _D, C.c_int64, C.POINTER(C.c_int64),
+                                             C.POINTER(C.c_int32), C.c_int32, C.c_int64,
                                              C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                              _D, C.c_int]),
             "orc_mesh_destroy": (None, [C.c_void_p]),
@@ -174,8 +175,10 @@ class Mesh:
                       np.ascontiguousarray(mesh.face_group, dtype=np.int32),
                       np.ascontiguousarray(mesh.face_shift, dtype=np.float64)]
         xyz, cn, fc, fs, fg, fsh = self._keep
+        self._ct = None if mesh.cell_type is None else np.ascontiguousarray(mesh.cell_type, dtype=np.int32)
+        ct_p = None if self._ct is None else self._ct.ctypes.data_as(C.POINTER(C.c_int32))
         self._m = lib.orc_mesh_create(xyz.shape[0], _p(xyz), cn.shape[0], cn.ctypes.data_as(C.POINTER(C.c_int64)),
-                                      fc.shape[0], fc.ctypes.data_as(C.POINTER(C.c_int64)),
+                                      ct_p, cn.shape[1], fc.shape[0], fc.ctypes.data_as(C.POINTER(C.c_int64)),
                                       fs.ctypes.data_as(C.POINTER(C.c_int32)),
                                       fg.ctypes.data_as(C.POINTER(C.c_int32)), _p(fsh), degree)
         if not self._m:
@@ -334,8 +337,8 @@ class Limiter:
 def _modal_sigs(lib):
     P64, P32 = C.POINTER(C.c_int64), C.POINTER(C.c_int32)
     sig = {
-        "orc_modal_create": (C.c_void_p, [C.c_int64, _D, C.c_int64, P64, P32, C.c_int64, P64, P32, P32,
-                                          _D, C.c_int]),
+        "orc_modal_create": (C.c_void_p, [C.c_int64, _D, C.c_int64, P64, P32, C.c_int32, C.c_int64, P64, P32,
+                                          P32, _D, C.c_int]),
         "orc_modal_destroy": (None, [C.c_void_p]),
         "orc_modal_column_size": (C.c_int64, [C.c_void_p]),
         "orc_modal_basis_count": (C.c_int, [C.c_void_p]),
@@ -376,7 +379,7 @@ class Modal:
         xyz, cn, ct, fc, fs, fg, fsh = self._keep
         P64, P32 = C.POINTER(C.c_int64), C.POINTER(C.c_int32)
         self._m = lib.orc_modal_create(xyz.shape[0], _p(xyz), cn.shape[0], cn.ctypes.data_as(P64),
-                                       ct.ctypes.data_as(P32), fc.shape[0], fc.ctypes.data_as(P64),
+                                       ct.ctypes.data_as(P32), cn.shape[1], fc.shape[0], fc.ctypes.data_as(P64),
                                        fs.ctypes.data_as(P32), fg.ctypes.data_as(P32), _p(fsh), degree)
         if not self._m:
             raise RuntimeError("oracle rejected the modal mesh")

@@ -239,7 +239,8 @@ struct orc_mesh {
   double *grad;       /* [cells][N][3][N]  basis global gradients */
   double *length;     /* [cells] */
   double *cell_center; /* [cells][3] Hex8 LocalToGlobal(0, 0, 0) */
-  double *corners;    /* [cells][8][3] Hex8 node coordinates */
+  double *corners;    /* [cells][27][3] node coordinates (the type's first n) */
+  int32_t *type;      /* [cells] ORC_CELL_HEX8 / HEX27 / HEX20 */
   double *jdi;        /* [cells][N][9] det(J) J^-1 (GetJacobianAssociated) */
   double *detj;       /* [cells][N] det(J) */
   int32_t *face_sides; /* [faces][2] local face index in holder / sharer */
@@ -270,7 +271,7 @@ double orc_cell_length(const orc_mesh *m, int64_t c) { return m->length[c]; }
 void orc_mesh_destroy(orc_mesh *m) {
   if (!m) return;
   free(m->node_xyz); free(m->node_w); free(m->grad); free(m->length); free(m->cell_center);
-  free(m->corners);
+  free(m->corners); free(m->type);
   free(m->face_shift); free(m->jdi); free(m->detj); free(m->face_sides);
   free(m->face_cells); free(m->face_group); free(m->face_xyz); free(m->face_w);
   free(m->face_frame); free(m->map_h); free(m->map_s);
@@ -283,7 +284,8 @@ static int near12(const double *a, const double *b) {
 }
 
 orc_mesh *orc_mesh_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
-                          const int64_t *cell_nodes, int64_t n_faces,
+                          const int64_t *cell_nodes, const int32_t *cell_type,
+                          int32_t stride, int64_t n_faces,
                           const int64_t *face_cells, const int32_t *face_sides,
                           const int32_t *face_group, const double *face_shift,
                           int degree) {
@@ -303,7 +305,17 @@ orc_mesh *orc_mesh_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
   m->grad = (double *)malloc(sizeof(double) * n_cells * N * 3 * N);
   m->length = (double *)malloc(sizeof(double) * n_cells);
   m->cell_center = (double *)malloc(sizeof(double) * n_cells * 3);
-  m->corners = (double *)malloc(sizeof(double) * n_cells * 24);
+  m->corners = (double *)calloc(n_cells * 81, sizeof(double));
+  m->type = (int32_t *)malloc(sizeof(int32_t) * n_cells);
+  const int64_t S = stride > 0 ? stride : 8;
+  for (int64_t c = 0; c < n_cells; ++c) {
+    int t = cell_type ? cell_type[c] : ORC_CELL_HEX8;
+    if (orc_type_is_tet(t) || orc_type_nodes(t) == 0 || orc_type_nodes(t) > S) {
+      orc_mesh_destroy(m);
+      return NULL;
+    }
+    m->type[c] = t;
+  }
   m->jdi = (double *)malloc(sizeof(double) * n_cells * N * 9);
   m->detj = (double *)malloc(sizeof(double) * n_cells * N);
   m->face_sides = (int32_t *)malloc(sizeof(int32_t) * (n_faces * 2 + 1));
@@ -312,24 +324,34 @@ orc_mesh *orc_mesh_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
   int bad = 0;
 #pragma omp parallel for schedule(static) num_threads(orc_get_threads())
   for (int64_t c = 0; c < n_cells; ++c) {
-    double xn[24];
-    for (int v = 0; v < 8; ++v) {
-      int64_t id = cell_nodes[c * 8 + v];
+    const int type = m->type[c], nv = orc_type_nodes(type);
+    double xn[81];
+    for (int v = 0; v < nv; ++v) {
+      int64_t id = cell_nodes[c * S + v];
       if (id < 0 || id >= n_nodes) { bad = 1; id = 0; }
       for (int d = 0; d < 3; ++d) xn[v * 3 + d] = xyz[id * 3 + d];
     }
     double volume = 0;
     const double zero[3] = {0, 0, 0};
-    memcpy(&m->corners[c * 24], xn, sizeof(xn));
-    hex8_global(xn, zero, &m->cell_center[c * 3]);
+    memcpy(&m->corners[c * 81], xn, sizeof(double) * 3 * nv);
+    if (type == ORC_CELL_HEX8) {
+      hex8_global(xn, zero, &m->cell_center[c * 3]);
+    } else {
+      double jz[9];
+      orc_map_point(type, xn, zero, &m->cell_center[c * 3], jz);
+    }
     for (int i = 0; i < Q; ++i)
       for (int j = 0; j < Q; ++j)
         for (int k = 0; k < Q; ++k) {
           int qn = (i * Q + j) * Q + k;
           double loc[3] = {m->xq[i], m->xq[j], m->xq[k]};
-          hex8_global(xn, loc, &m->node_xyz[(c * N + qn) * 3]);
           double jac[9], inv[9];
-          hex8_jacobian(xn, loc, jac);
+          if (type == ORC_CELL_HEX8) {
+            hex8_global(xn, loc, &m->node_xyz[(c * N + qn) * 3]);
+            hex8_jacobian(xn, loc, jac);
+          } else {
+            orc_map_point(type, xn, loc, &m->node_xyz[(c * N + qn) * 3], jac);
+          }
           double det = det3(jac);
           double w = m->wq[i] * m->wq[j] * m->wq[k] * det;
           m->node_w[c * N + qn] = w;
@@ -369,8 +391,17 @@ orc_mesh *orc_mesh_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
     if (h < 0 || h >= n_cells || side < 0 || side > 5) { bad = 1; continue; }
     double xn[12];
     for (int v = 0; v < 4; ++v) {
-      int64_t id = cell_nodes[h * 8 + kHexFace[side][v]];
+      int64_t id = cell_nodes[h * S + kHexFace[side][v]];
       for (int d = 0; d < 3; ++d) xn[v * 3 + d] = xyz[id * 3 + d];
+    }
+    /* curved holder: the face's points from the cell map at the face's local
+     * points; tangents J^T dloc/da (corner 0 -> 1) and J^T dloc/db (0 -> 3) */
+    const int htype = m->type[h];
+    double l0[3], da[3], db[3];
+    for (int d = 0; d < 3; ++d) {
+      l0[d] = kHexLocal[kHexFace[side][0]][d];
+      da[d] = (kHexLocal[kHexFace[side][1]][d] - l0[d]) / 2;
+      db[d] = (kHexLocal[kHexFace[side][3]][d] - l0[d]) / 2;
     }
     double shift[3] = {0, 0, 0};
     if (face_shift) for (int d = 0; d < 3; ++d) shift[d] = face_shift[f * 3 + d];
@@ -378,9 +409,19 @@ orc_mesh *orc_mesh_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
       for (int j = 0; j < Q; ++j) {
         int fp = i * Q + j;
         double *gx = &m->face_xyz[(f * QF + fp) * 3];
-        quad4_global(xn, m->xq[i], m->xq[j], gx);
         double jac[6];
-        quad4_jacobian(xn, m->xq[i], m->xq[j], jac);
+        if (htype == ORC_CELL_HEX8) {
+          quad4_global(xn, m->xq[i], m->xq[j], gx);
+          quad4_jacobian(xn, m->xq[i], m->xq[j], jac);
+        } else {
+          double loc[3], J[9];
+          for (int d = 0; d < 3; ++d) loc[d] = l0[d] + (m->xq[i] + 1) * da[d] + (m->xq[j] + 1) * db[d];
+          orc_map_point(htype, &m->corners[h * 81], loc, gx, J);
+          for (int d = 0; d < 3; ++d) {
+            jac[d] = J[0 * 3 + d] * da[0] + J[1 * 3 + d] * da[1] + J[2 * 3 + d] * da[2];
+            jac[3 + d] = J[0 * 3 + d] * db[0] + J[1 * 3 + d] * db[1] + J[2 * 3 + d] * db[2];
+          }
+        }
         double a = jac[0] * jac[0] + jac[1] * jac[1] + jac[2] * jac[2];
         double b = jac[0] * jac[3] + jac[1] * jac[4] + jac[2] * jac[5];
         double cc = jac[3] * jac[3] + jac[4] * jac[4] + jac[5] * jac[5];
@@ -837,7 +878,8 @@ int orc_vtk_sample(const orc_mesh *m, const double *u, double *xyz, double *valu
     for (int s = 0; s < 27; ++s) {
       double loc[3] = {orc_vtk_hex27[s][0], orc_vtk_hex27[s][1], orc_vtk_hex27[s][2]};
       double *g = &xyz[(c * 27 + s) * 3], *v = &values[(c * 27 + s) * K];
-      hex8_global(&m->corners[c * 24], loc, g);
+      double jz[9];
+      orc_map_point(m->type[c], &m->corners[c * 81], loc, g, jz);
       double lx[MAXQ], ly[MAXQ], lz[MAXQ];
       lagrange_values(Q, m->xq, loc[0], lx);
       lagrange_values(Q, m->xq, loc[1], ly);

@@ -29,4 +29,12 @@ typedef void (*orc_set_hook)(void *ctx, double *u);
 int orc_rk_generic(orc_residual_fn fn, void *ctx, int64_t L, int order, double t,
                    double dt, double *u, orc_set_hook hook, void *hook_ctx);
 
+/* Cell maps (orc_geom.c): node count of a type, whether it is a
+ * tetrahedron, the local coordinates of node a, and x(loc) with
+ * jac[r * 3 + d] = d x_d / d loc_r for the type's nodes xn [n][3]. */
+int orc_type_nodes(int type);
+int orc_type_is_tet(int type);
+void orc_local_of_node(int type, int a, double *loc);
+void orc_map_point(int type, const double *xn, const double *loc, double *x, double *jac);
+
 #endif /* MCFD_ORACLE_ORC_INTERNAL_H_ */

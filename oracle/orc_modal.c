@@ -233,18 +233,18 @@ void orc_modal_destroy(orc_modal *m) {
 }
 
 static int cell_points(int type, int p) {
-  if (type == ORC_CELL_HEX8) return (p + 1) * (p + 1) * (p + 1);
+  if (!orc_type_is_tet(type)) return (p + 1) * (p + 1) * (p + 1);
   return p <= 2 ? 14 : 24;
 }
 
 static int face_points(int type, int p) {
-  if (type == ORC_CELL_HEX8) return (p + 1) * (p + 1);
+  if (!orc_type_is_tet(type)) return (p + 1) * (p + 1);
   return p <= 2 ? 6 : 12;
 }
 
 orc_modal *orc_modal_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
                             const int64_t *cell_nodes, const int32_t *cell_type,
-                            int64_t n_faces, const int64_t *face_cells,
+                            int32_t stride, int64_t n_faces, const int64_t *face_cells,
                             const int32_t *face_sides, const int32_t *face_group,
                             const double *face_shift, int degree) {
   if (degree < 1 || degree > 3 || n_cells <= 0) return NULL;
@@ -263,7 +263,17 @@ orc_modal *orc_modal_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
   m->center = (double *)malloc(sizeof(double) * n_cells * 3);
   m->s = (double *)calloc(n_cells * M * M, sizeof(double));
   m->length = (double *)malloc(sizeof(double) * n_cells);
-  m->corners = (double *)calloc(n_cells * 24, sizeof(double));
+  m->corners = (double *)calloc(n_cells * 81, sizeof(double));
+  const int64_t NS = stride > 0 ? stride : 8;
+  for (int64_t c = 0; c < n_cells; ++c) {
+    int t = cell_type ? cell_type[c] : ORC_CELL_HEX8;
+    if (orc_type_nodes(t) == 0 || orc_type_nodes(t) > NS) {
+      free(m->corners);
+      m->corners = NULL;
+      orc_modal_destroy(m);
+      return NULL;
+    }
+  }
   m->type = (int32_t *)malloc(sizeof(int32_t) * n_cells);
   double gx[4], gw[4];
   gauss_rule(Q, gx, gw);
@@ -275,19 +285,44 @@ orc_modal *orc_modal_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
 #pragma omp parallel for schedule(static) num_threads(orc_get_threads())
   for (int64_t c = 0; c < n_cells; ++c) {
     int t = cell_type ? cell_type[c] : ORC_CELL_HEX8;
-    int nv = t == ORC_CELL_HEX8 ? 8 : 4;
-    double xn[24];
+    int nv = orc_type_nodes(t);
+    double xn[81];
     for (int v = 0; v < nv; ++v) {
-      int64_t id = cell_nodes[c * 8 + v];
+      int64_t id = cell_nodes[c * NS + v];
       if (id < 0 || id >= n_nodes) { bad = 1; id = 0; }
       for (int d = 0; d < 3; ++d) xn[v * 3 + d] = xyz[id * 3 + d];
     }
-    memcpy(&m->corners[c * 24], xn, sizeof(double) * 3 * nv);
+    memcpy(&m->corners[c * 81], xn, sizeof(double) * 3 * nv);
     m->type[c] = t;
     double *ctr = &m->center[c * 3];
     double *X = &m->vx[m->vp_off[c] * 3], *W = &m->vw[m->vp_off[c]];
     double volume = 0;
-    if (t == ORC_CELL_HEX8) {
+    if (t == ORC_CELL_HEX27 || t == ORC_CELL_HEX20 || t == ORC_CELL_TET10) {
+      /* quadratic map: points and det J from the shape functions; the centre
+       * at the local centre (hex (0,0,0), tet (1/4,1/4,1/4)) */
+      const int tet = t == ORC_CELL_TET10;
+      const double cl[3] = {tet ? 0.25 : 0.0, tet ? 0.25 : 0.0, tet ? 0.25 : 0.0};
+      double J[9];
+      orc_map_point(t, xn, cl, ctr, J);
+      int nq = (int)(m->vp_off[c + 1] - m->vp_off[c]);
+      for (int q = 0; q < nq; ++q) {
+        double loc[3], wl;
+        if (tet) {
+          loc[0] = tx[q][0]; loc[1] = tx[q][1]; loc[2] = tx[q][2];
+          wl = tw[q];
+        } else {
+          int i = q / (Q * Q), j = (q / Q) % Q, k = q % Q;
+          loc[0] = gx[i]; loc[1] = gx[j]; loc[2] = gx[k];
+          wl = gw[i] * gw[j] * gw[k];
+        }
+        orc_map_point(t, xn, loc, &X[q * 3], J);
+        double det = J[0] * (J[4] * J[8] - J[5] * J[7]) - J[1] * (J[3] * J[8] - J[5] * J[6]) +
+                     J[2] * (J[3] * J[7] - J[4] * J[6]);
+        if (det == 0) bad = 1;
+        W[q] = wl * fabs(det);
+        volume += W[q];
+      }
+    } else if (t == ORC_CELL_HEX8) {
       const double zero[3] = {0, 0, 0};
       hex8_global(xn, zero, ctr);
       for (int i = 0; i < Q; ++i)
@@ -362,12 +397,52 @@ orc_modal *orc_modal_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
     int t = cell_type ? cell_type[h] : ORC_CELL_HEX8;
     double *X = &m->fx[m->fp_off[f] * 3], *W = &m->fw[m->fp_off[f]];
     double *F = &m->ff[m->fp_off[f] * 9];
-    if (t == ORC_CELL_HEX8) {
+    if (t == ORC_CELL_HEX27 || t == ORC_CELL_HEX20 || t == ORC_CELL_TET10) {
+      /* curved holder: face points from its cell map at the face's local
+       * points; tangents J^T dloc/da, J^T dloc/db (quad: corner 0 -> 1,
+       * 0 -> 3; triangle: corner 0 - corner 2, corner 1 - corner 2) */
+      const int hex = t != ORC_CELL_TET10;
+      if (side < 0 || side > (hex ? 5 : 3)) { bad = 1; continue; }
+      double lc[4][3], da[3], db[3];
+      for (int v = 0; v < (hex ? 4 : 3); ++v)
+        orc_local_of_node(t, hex ? kHexFace[side][v] : kTetFace[side][v], lc[v]);
+      for (int d = 0; d < 3; ++d) {
+        da[d] = hex ? (lc[1][d] - lc[0][d]) / 2 : lc[0][d] - lc[2][d];
+        db[d] = hex ? (lc[3][d] - lc[0][d]) / 2 : lc[1][d] - lc[2][d];
+      }
+      int nq = hex ? Q * Q : ntri;
+      for (int q = 0; q < nq; ++q) {
+        double loc[3], wl;
+        if (hex) {
+          int i = q / Q, j = q % Q;
+          for (int d = 0; d < 3; ++d) loc[d] = lc[0][d] + (gx[i] + 1) * da[d] + (gx[j] + 1) * db[d];
+          wl = gw[i] * gw[j];
+        } else {
+          double x = sx[q][0], y = sx[q][1], z = 1.0 - x - y;
+          for (int d = 0; d < 3; ++d) loc[d] = lc[0][d] * x + lc[1][d] * y + lc[2][d] * z;
+          wl = sw[q];
+        }
+        double J[9], jac[6];
+        orc_map_point(t, &m->corners[h * 81], loc, &X[q * 3], J);
+        for (int d = 0; d < 3; ++d) {
+          jac[d] = J[0 * 3 + d] * da[0] + J[1 * 3 + d] * da[1] + J[2 * 3 + d] * da[2];
+          jac[3 + d] = J[0 * 3 + d] * db[0] + J[1 * 3 + d] * db[1] + J[2 * 3 + d] * db[2];
+        }
+        double *fr = &F[q * 9];
+        cross(&jac[0], &jac[3], &fr[0]);
+        double nn = norm3(&fr[0]);
+        W[q] = wl * nn;
+        for (int d = 0; d < 3; ++d) fr[d] /= nn;
+        double tn = norm3(&jac[0]);
+        for (int d = 0; d < 3; ++d) fr[3 + d] = jac[d] / tn;
+        cross(&fr[0], &fr[3], &fr[6]);
+      }
+    } else if (t == ORC_CELL_HEX8) {
       if (side < 0 || side > 5) { bad = 1; continue; }
       double xn[12];
       for (int v = 0; v < 4; ++v)
         for (int d = 0; d < 3; ++d)
-          xn[v * 3 + d] = xyz[cell_nodes[h * 8 + kHexFace[side][v]] * 3 + d];
+          xn[v * 3 + d] = xyz[cell_nodes[h * NS + kHexFace[side][v]] * 3 + d];
       for (int i = 0; i < Q; ++i)
         for (int j = 0; j < Q; ++j) {
           int q = i * Q + j;
@@ -399,7 +474,7 @@ orc_modal *orc_modal_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
       double xn[9];
       for (int v = 0; v < 3; ++v)
         for (int d = 0; d < 3; ++d)
-          xn[v * 3 + d] = xyz[cell_nodes[h * 8 + kTetFace[side][v]] * 3 + d];
+          xn[v * 3 + d] = xyz[cell_nodes[h * NS + kTetFace[side][v]] * 3 + d];
       /* Triangle3: shapes (x, y, 1 - x - y); Jacobian rows X0 - X2, X1 - X2 */
       double jac[6];
       for (int d = 0; d < 3; ++d) {
@@ -670,13 +745,17 @@ int64_t orc_modal_vtk_sample(const orc_modal *m, const double *u, double *xyz,
   int64_t pt = 0;
   double psi[MAXM];
   for (int64_t c = 0; c < m->n_cells; ++c) {
-    const double *xn = &m->corners[c * 24];
-    const int tet = m->type[c] == ORC_CELL_TET4;
+    const double *xn = &m->corners[c * 81];
+    const int tet = orc_type_is_tet(m->type[c]);
     types[c] = tet ? 24 : 29;
     const int n = tet ? 10 : 27;
     for (int s = 0; s < n; ++s, ++pt) {
       double *g = &xyz[pt * 3];
-      if (!tet) {
+      if (m->type[c] != ORC_CELL_HEX8 && m->type[c] != ORC_CELL_TET4) {
+        double loc[3], J[9];
+        for (int d = 0; d < 3; ++d) loc[d] = tet ? kTet10[s][d] : orc_vtk_hex27[s][d];
+        orc_map_point(m->type[c], xn, loc, g, J);
+      } else if (!tet) {
         double loc[3] = {orc_vtk_hex27[s][0], orc_vtk_hex27[s][1], orc_vtk_hex27[s][2]};
         hex8_global(xn, loc, g);
       } else {

@@ -39,6 +39,7 @@ class MeshDesc(C.Structure):
         ("face_sides", C.POINTER(C.c_int32)),
         ("face_group", C.POINTER(C.c_int32)),
         ("face_shift", C.POINTER(C.c_double)),
+        ("cell_node_stride", C.c_int32),
     ]
 
 
@@ -93,7 +94,7 @@ SIGNATURES = {
     "mcfd_advance": (C.c_int, [_P, C.c_int32, C.c_double, C.c_int32, _D]),
     "mcfd_face_slot_count": (C.c_int64, [C.c_int64, C.POINTER(C.c_int32)]),
     "mcfd_build_faces": (C.c_int, [C.c_int64, _D, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
-                                   C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.c_int32,
+                                   C.c_int32, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.c_int32,
                                    C.POINTER(C.c_int32), _D, C.c_int64, C.POINTER(C.c_int64),
                                    C.POINTER(C.c_int32), C.POINTER(C.c_int32), _D, C.POINTER(C.c_int64)]),
     "mcfd_build_error": (C.c_char_p, []),

@@ -27,6 +27,7 @@
 
 #include "../../include/mcfd.h"
 #include "euler.cuh"
+#include "geometry.hpp"
 #include "handle.hpp"
 
 namespace {
@@ -193,18 +194,32 @@ void release(mcfd_handle *h) {
 // Cell corners and types for output sampling (Tet4 cells: the first four
 // cell_nodes entries, the rest zero).
 int upload_corners(mcfd_handle *h, const mcfd_mesh_desc *d) {
-  const int64_t nc = d->n_cells;
+  const int64_t nc = d->n_cells, S = d->cell_node_stride > 0 ? d->cell_node_stride : 8;
   std::vector<double> corners(nc * 24, 0.0);
   auto &types = h->mesh.host_types;
+  auto &m = h->mesh;
   types.assign(nc, 0);
+  m.host_cell_type.assign(nc, MCFD_HEX8);
+  m.curved = false;
   for (int64_t c = 0; c < nc; ++c) {
     const int t = d->cell_type ? d->cell_type[c] : 0;
-    types[c] = (uint8_t)(t == 1 ? 1 : 0);
-    const int nv = t == 1 ? 4 : 8;
+    m.host_cell_type[c] = (uint8_t)t;
+    m.curved = m.curved || mcfd::geo::curved(t);
+    types[c] = (uint8_t)(mcfd::geo::is_tet(t) ? 1 : 0);
+    const int nv = mcfd::geo::is_tet(t) ? 4 : 8;
     for (int v = 0; v < nv; ++v) {
-      const int64_t id = d->cell_nodes[c * 8 + v];
+      const int64_t id = d->cell_nodes[c * S + v];
       if (id < 0 || id >= d->n_nodes) return fail(h, MCFD_ERR_ARGUMENT, "cell node index out of range");
       for (int e = 0; e < 3; ++e) corners[(c * 8 + v) * 3 + e] = d->xyz[id * 3 + e];
+    }
+  }
+  if (m.curved) {  // every node of every cell, for the output sampling points
+    m.host_nodes.assign((size_t)nc * mcfd::geo::kMaxNodes * 3, 0.0);
+    for (int64_t c = 0; c < nc; ++c) {
+      const int nv = mcfd::geo::node_count(m.host_cell_type[c]);
+      for (int v = 0; v < nv; ++v)
+        for (int e = 0; e < 3; ++e)
+          m.host_nodes[((size_t)c * mcfd::geo::kMaxNodes + v) * 3 + e] = d->xyz[d->cell_nodes[c * S + v] * 3 + e];
     }
   }
   int rc = upload(h, &h->mesh.corners, corners);
@@ -253,30 +268,49 @@ int build_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
   gll(Q, xq, wq);
   for (int i = 0; i < Q; ++i) h->mesh.xq[i] = xq[i];
   diff_matrix(Q, xq, dm);
+  const int64_t S = d->cell_node_stride > 0 ? d->cell_node_stride : 8;
+  std::vector<int> ctype(d->n_cells, MCFD_HEX8);
   for (int64_t c = 0; c < d->n_cells; ++c) {
-    if (d->cell_type && d->cell_type[c] != MCFD_HEX8)
-      return fail(h, MCFD_ERR_UNSUPPORTED, "only Hex8 cells are supported by the DGSEM scheme");
-    for (int v = 0; v < 8; ++v) {
-      int64_t id = d->cell_nodes[c * 8 + v];
+    const int t = d->cell_type ? d->cell_type[c] : MCFD_HEX8;
+    if (!mcfd::geo::is_hex(t))
+      return fail(h, MCFD_ERR_UNSUPPORTED, "the nodal schemes take hexahedra (Hex8, Hex20, Hex27) only");
+    if (mcfd::geo::node_count(t) > S)
+      return fail(h, MCFD_ERR_MESH, "cell_node_stride is below the node count of cell " + std::to_string(c));
+    ctype[c] = t;
+    for (int v = 0; v < mcfd::geo::node_count(t); ++v) {
+      int64_t id = d->cell_nodes[c * S + v];
       if (id < 0 || id >= d->n_nodes)
         return fail(h, MCFD_ERR_MESH, "cell node index out of range in cell " + std::to_string(c));
     }
   }
+  // all nodes of cell c, [n][3]
+  auto gather = [&](int64_t c, double *xn) {
+    for (int v = 0; v < mcfd::geo::node_count(ctype[c]); ++v)
+      for (int e = 0; e < 3; ++e) xn[v * 3 + e] = d->xyz[d->cell_nodes[c * S + v] * 3 + e];
+  };
+  // x and J at a local point of cell c (Hex8 through the trilinear map)
+  auto cell_point = [&](int64_t c, const double *xn, double a, double b, double cc, double *x, double *J) {
+    if (ctype[c] == MCFD_HEX8) {
+      hex8_point(xn, a, b, cc, x, J);
+    } else {
+      const double loc[3] = {a, b, cc};
+      mcfd::geo::map_point(ctype[c], xn, loc, x, J);
+    }
+  };
   // ---- per node geometry
   std::vector<double> geo((size_t)d->n_cells * N * 10);
   std::vector<double> rate(d->n_cells);
   int bad_jac = 0;
 #pragma omp parallel for schedule(static)
   for (int64_t c = 0; c < d->n_cells; ++c) {
-    double xn[24];
-    for (int v = 0; v < 8; ++v)
-      for (int e = 0; e < 3; ++e) xn[v * 3 + e] = d->xyz[d->cell_nodes[c * 8 + v] * 3 + e];
+    double xn[mcfd::geo::kMaxNodes * 3];
+    gather(c, xn);
     double volume = 0;
     for (int i = 0; i < Q; ++i)
       for (int j = 0; j < Q; ++j)
         for (int k = 0; k < Q; ++k) {
           double x[3], J[9];
-          hex8_point(xn, xq[i], xq[j], xq[k], x, J);
+          cell_point(c, xn, xq[i], xq[j], xq[k], x, J);
           double det = J[0] * (J[4] * J[8] - J[5] * J[7]) -
                        J[1] * (J[3] * J[8] - J[5] * J[6]) +
                        J[2] * (J[3] * J[7] - J[4] * J[6]);
@@ -334,7 +368,23 @@ int build_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
     for (int v = 0; v < 4; ++v) {
       int hv = kHexFace[sh][v];
       corner_grid(hv, Q, hg[v]);
-      for (int e = 0; e < 3; ++e) xn[v * 3 + e] = d->xyz[d->cell_nodes[hc * 8 + hv] * 3 + e];
+      for (int e = 0; e < 3; ++e) xn[v * 3 + e] = d->xyz[d->cell_nodes[hc * S + hv] * 3 + e];
+    }
+    // curved holder: face points from the cell map at the face's local
+    // points, tangents J^T dloc/da and J^T dloc/db (the face is a square of
+    // the local cube, corner 0 -> 1 along a, corner 0 -> 3 along b)
+    const bool curved_face = ctype[hc] != MCFD_HEX8;
+    double xc[mcfd::geo::kMaxNodes * 3], l0[3], da[3], db[3];
+    if (curved_face) {
+      gather(hc, xc);
+      double l1[3], l3[3];
+      for (int e = 0; e < 3; ++e) {
+        l0[e] = kHexLocal[kHexFace[sh][0]][e];
+        l1[e] = kHexLocal[kHexFace[sh][1]][e];
+        l3[e] = kHexLocal[kHexFace[sh][3]][e];
+        da[e] = (l1[e] - l0[e]) / 2;
+        db[e] = (l3[e] - l0[e]) / 2;
+      }
     }
     double shift[3] = {0, 0, 0};
     if (d->face_shift)
@@ -343,12 +393,12 @@ int build_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
     int sg[4][3];
     if (sc >= 0) {
       for (int v = 0; v < 4; ++v) {
-        int64_t hid = d->cell_nodes[hc * 8 + kHexFace[sh][v]];
+        int64_t hid = d->cell_nodes[hc * S + kHexFace[sh][v]];
         int best = -1;
         double best_d = 1e300;
         for (int w = 0; w < 4; ++w) {
           int sv = kHexFace[ss][w];
-          int64_t sid = d->cell_nodes[sc * 8 + sv];
+          int64_t sid = d->cell_nodes[sc * S + sv];
           double dd = 0;
           for (int e = 0; e < 3; ++e) {
             double diff = d->xyz[sid * 3 + e] + shift[e] - d->xyz[hid * 3 + e];
@@ -368,7 +418,15 @@ int build_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
         int fp = a * Q + b;
         int64_t pt = f * QF + fp;
         double x[3], ta[3], tb[3];
-        quad4_point(xn, xq[a], xq[b], x, ta, tb);
+        if (curved_face) {
+          double loc[3], J[9];
+          for (int e = 0; e < 3; ++e) loc[e] = l0[e] + (xq[a] + 1) * da[e] + (xq[b] + 1) * db[e];
+          mcfd::geo::map_point(ctype[hc], xc, loc, x, J);
+          mcfd::geo::tangent(J, da, ta);
+          mcfd::geo::tangent(J, db, tb);
+        } else {
+          quad4_point(xn, xq[a], xq[b], x, ta, tb);
+        }
         double nrm[3] = {ta[1] * tb[2] - ta[2] * tb[1], ta[2] * tb[0] - ta[0] * tb[2],
                          ta[0] * tb[1] - ta[1] * tb[0]};
         double area = std::sqrt(nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2]);
@@ -428,12 +486,9 @@ int build_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
 #pragma omp parallel for schedule(static)
   for (int64_t f = 0; f < d->n_faces; ++f) {
     int64_t hc = d->face_cells[f * 2], sc = d->face_cells[f * 2 + 1];
-    double xh[24], xs[24];
-    for (int v = 0; v < 8; ++v)
-      for (int e = 0; e < 3; ++e) {
-        xh[v * 3 + e] = d->xyz[d->cell_nodes[hc * 8 + v] * 3 + e];
-        if (sc >= 0) xs[v * 3 + e] = d->xyz[d->cell_nodes[sc * 8 + v] * 3 + e];
-      }
+    double xh[mcfd::geo::kMaxNodes * 3], xs[mcfd::geo::kMaxNodes * 3];
+    gather(hc, xh);
+    if (sc >= 0) gather(sc, xs);
     double shift[3] = {0, 0, 0};
     if (d->face_shift)
       for (int e = 0; e < 3; ++e) shift[e] = d->face_shift[f * 3 + e];
@@ -443,13 +498,13 @@ int build_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
       double scale = 1 + std::fabs(x[0]) + std::fabs(x[1]) + std::fabs(x[2]);
       double p[3], J[9];
       int node = m.map_h[pt];
-      hex8_point(xh, xq[node / QF], xq[(node / Q) % Q], xq[node % Q], p, J);
+      cell_point(hc, xh, xq[node / QF], xq[(node / Q) % Q], xq[node % Q], p, J);
       double e2 = 0;
       for (int e = 0; e < 3; ++e) e2 += (p[e] - x[e]) * (p[e] - x[e]);
       if (std::sqrt(e2) > 1e-10 * scale) bad_match = 1;
       if (sc >= 0) {
         node = m.map_s[pt];
-        hex8_point(xs, xq[node / QF], xq[(node / Q) % Q], xq[node % Q], p, J);
+        cell_point(sc, xs, xq[node / QF], xq[(node / Q) % Q], xq[node % Q], p, J);
         e2 = 0;
         for (int e = 0; e < 3; ++e) e2 += (p[e] + shift[e] - x[e]) * (p[e] + shift[e] - x[e]);
         if (std::sqrt(e2) > 1e-10 * scale) bad_match = 1;
@@ -538,6 +593,11 @@ int build_limiter(mcfd_handle *h, const mcfd_mesh_desc *d, int kind, double w0,
   auto &l = h->lim;
   const int Q = m.q, N = m.n, p = m.p;
   const int M = (p + 1) * (p + 2) * (p + 3) / 6;
+  const int64_t S = d->cell_node_stride > 0 ? d->cell_node_stride : 8;
+  if (d->cell_type)
+    for (int64_t c = 0; c < d->n_cells; ++c)
+      if (d->cell_type[c] != MCFD_HEX8)
+        return fail(h, MCFD_ERR_UNSUPPORTED, "the WENO limiter takes Hex8 cells only");
   l.kind = kind;
   l.m = M;
   l.w0 = w0 > 0 ? w0 : 0.001;
@@ -562,7 +622,7 @@ int build_limiter(mcfd_handle *h, const mcfd_mesh_desc *d, int kind, double w0,
     double xn[12], x[3], ta[3], tb[3], fr[9];
     const int side = d->face_sides[f * 2];
     for (int v = 0; v < 4; ++v)
-      for (int e = 0; e < 3; ++e) xn[v * 3 + e] = d->xyz[d->cell_nodes[hc * 8 + kHexFace[side][v]] * 3 + e];
+      for (int e = 0; e < 3; ++e) xn[v * 3 + e] = d->xyz[d->cell_nodes[hc * S + kHexFace[side][v]] * 3 + e];
     quad4_point(xn, -1.0, -1.0, x, ta, tb);
     fr[0] = ta[1] * tb[2] - ta[2] * tb[1];
     fr[1] = ta[2] * tb[0] - ta[0] * tb[2];
@@ -593,7 +653,7 @@ int build_limiter(mcfd_handle *h, const mcfd_mesh_desc *d, int kind, double w0,
   for (int64_t c = 0; c < C; ++c) {
     double xn[24], J[9];
     for (int v = 0; v < 8; ++v)
-      for (int e = 0; e < 3; ++e) xn[v * 3 + e] = d->xyz[d->cell_nodes[c * 8 + v] * 3 + e];
+      for (int e = 0; e < 3; ++e) xn[v * 3 + e] = d->xyz[d->cell_nodes[c * S + v] * 3 + e];
     CellBasis &b = basis[c];
     hex8_point(xn, 0, 0, 0, b.center, J);
     double vol = 0;

@@ -67,12 +67,28 @@ struct OutFace {
   double shift[3];
 };
 
-int face_node_ids(const int64_t *cell_nodes, const int32_t *cell_type, int64_t c, int side,
-                  int64_t *ids) {
-  const bool tet = cell_type && cell_type[c] == 1;
+bool tet_type(const int32_t *cell_type, int64_t c) {
+  return cell_type && (cell_type[c] == MCFD_TET4 || cell_type[c] == MCFD_TET10);
+}
+
+int type_nodes(int t) {
+  switch (t) {
+    case MCFD_HEX8: return 8;
+    case MCFD_TET4: return 4;
+    case MCFD_HEX27: return 27;
+    case MCFD_TET10: return 10;
+    case MCFD_HEX20: return 20;
+    default: return 0;
+  }
+}
+
+// corner ids of a local face (faces are keyed and matched by their corners)
+int face_node_ids(const int64_t *cell_nodes, int64_t stride, const int32_t *cell_type, int64_t c,
+                  int side, int64_t *ids) {
+  const bool tet = tet_type(cell_type, c);
   const int n = tet ? 3 : 4;
   for (int v = 0; v < n; ++v)
-    ids[v] = cell_nodes[c * 8 + (tet ? kTetFace[side][v] : kHexFace[side][v])];
+    ids[v] = cell_nodes[c * stride + (tet ? kTetFace[side][v] : kHexFace[side][v])];
   return n;
 }
 
@@ -112,17 +128,19 @@ const char *mcfd_build_error(void) { return g_build_error.c_str(); }
 int64_t mcfd_face_slot_count(int64_t n_cells, const int32_t *cell_type) {
   if (n_cells < 0) return -1;
   int64_t n = 0;
-  for (int64_t c = 0; c < n_cells; ++c) n += (cell_type && cell_type[c] == 1) ? 4 : 6;
+  for (int64_t c = 0; c < n_cells; ++c) n += tet_type(cell_type, c) ? 4 : 6;
   return n;
 }
 
 int mcfd_build_faces(int64_t n_nodes, const double *xyz, int64_t n_cells,
-                     const int64_t *cell_nodes, const int32_t *cell_type, int64_t n_bfaces,
+                     const int64_t *cell_nodes, const int32_t *cell_type,
+                     int32_t cell_node_stride, int64_t n_bfaces,
                      const int64_t *bface_nodes, const int32_t *bface_group, int32_t n_periodic,
                      const int32_t *periodic_groups, const double *periodic_shift, int64_t cap,
                      int64_t *face_cells, int32_t *face_sides, int32_t *face_group,
                      double *face_shift, int64_t *n_faces) {
   g_build_error.clear();
+  const int64_t stride = cell_node_stride > 0 ? cell_node_stride : 8;
   if (n_nodes <= 0 || !xyz || n_cells <= 0 || !cell_nodes || n_bfaces < 0 ||
       (n_bfaces > 0 && (!bface_nodes || !bface_group)) || n_periodic < 0 ||
       (n_periodic > 0 && (!periodic_groups || !periodic_shift)) || !face_cells || !face_sides ||
@@ -134,17 +152,17 @@ int mcfd_build_faces(int64_t n_nodes, const double *xyz, int64_t n_cells,
   std::vector<Slot> slots;
   slots.reserve(mcfd_face_slot_count(n_cells, cell_type));
   for (int64_t c = 0; c < n_cells; ++c) {
-    const bool tet = cell_type && cell_type[c] == 1;
-    if (cell_type && cell_type[c] != 0 && cell_type[c] != 1)
-      return build_fail("cell " + std::to_string(c) + ": unknown cell type");
-    const int nv = tet ? 4 : 8;
+    const bool tet = tet_type(cell_type, c);
+    const int nv = type_nodes(cell_type ? cell_type[c] : MCFD_HEX8);
+    if (nv == 0) return build_fail("cell " + std::to_string(c) + ": unknown cell type");
+    if (nv > stride) return build_fail("cell " + std::to_string(c) + ": more nodes than cell_node_stride");
     for (int v = 0; v < nv; ++v) {
-      const int64_t id = cell_nodes[c * 8 + v];
+      const int64_t id = cell_nodes[c * stride + v];
       if (id < 0 || id >= n_nodes) return build_fail("cell " + std::to_string(c) + ": node index out of range");
     }
     for (int s = 0; s < (tet ? 4 : 6); ++s) {
       int64_t ids[4];
-      const int n = face_node_ids(cell_nodes, cell_type, c, s, ids);
+      const int n = face_node_ids(cell_nodes, stride, cell_type, c, s, ids);
       slots.push_back({make_key(ids, n), c, s});
     }
   }
@@ -190,7 +208,7 @@ int mcfd_build_faces(int64_t n_nodes, const double *xyz, int64_t n_cells,
   auto centroid = [&](int64_t li, double *x) {
     const Slot &s = slots[lone[li]];
     int64_t ids[4];
-    const int n = face_node_ids(cell_nodes, cell_type, s.cell, s.side, ids);
+    const int n = face_node_ids(cell_nodes, stride, cell_type, s.cell, s.side, ids);
     x[0] = x[1] = x[2] = 0;
     for (int v = 0; v < n; ++v)
       for (int e = 0; e < 3; ++e) x[e] += xyz[ids[v] * 3 + e] / n;

@@ -812,6 +812,7 @@ struct ModalSampleArgs {
   double *xyz;
   double *values;
   int64_t n_cells;
+  int points_given;  // curved cells: xyz holds the points already (host-mapped)
 };
 
 template <int M>
@@ -823,8 +824,12 @@ __global__ void __launch_bounds__(256) modal_vtk_sample_kernel(ModalSampleArgs a
   const bool tet = a.type[c] == 1;
   if (tet && s >= 10) return;
   const double *xn = a.corners + c * 24;
+  const int64_t pt = a.off[c] + s;
   double g[3];
-  if (!tet) {
+  if (a.points_given) {
+#pragma unroll
+    for (int e = 0; e < 3; ++e) g[e] = a.xyz[pt * 3 + e];
+  } else if (!tet) {
     const double loc[3] = {(double)kVtkHex27[s][0], (double)kVtkHex27[s][1],
                            (double)kVtkHex27[s][2]};
     g[0] = g[1] = g[2] = 0;
@@ -848,9 +853,10 @@ __global__ void __launch_bounds__(256) modal_vtk_sample_kernel(ModalSampleArgs a
   double t[M], v[kK];
   taylor_values<M>(g[0] - ch.x, g[1] - ch.y, g[2] - ch.z, t);
   eval_taylor<M>(a.taylor + c * M * kK, t, v);
-  const int64_t pt = a.off[c] + s;
+  if (!a.points_given) {
 #pragma unroll
-  for (int e = 0; e < 3; ++e) a.xyz[pt * 3 + e] = g[e];
+    for (int e = 0; e < 3; ++e) a.xyz[pt * 3 + e] = g[e];
+  }
 #pragma unroll
   for (int e = 0; e < kK; ++e) a.values[pt * kK + e] = v[e];
 }
@@ -869,7 +875,7 @@ int launch_modal_vtk_sample(mcfd_handle *h, const double *u, const int64_t *off,
                             double *values) {
   const Modal &md = h->modal;
   ModalSampleArgs sa{md.taylor, md.center, h->mesh.corners, h->mesh.cell_type, off, xyz, values,
-                     h->mesh.n_cells};
+                     h->mesh.n_cells, h->mesh.curved ? 1 : 0};
   switch (md.m) {
     case 4: return modal_vtk_launch<4>(h, u, sa);
     case 10: return modal_vtk_launch<10>(h, u, sa);

@@ -39,6 +39,7 @@
 
 #include "../../include/mcfd.h"
 #include "euler.cuh"
+#include "geometry.hpp"
 #include "handle.hpp"
 
 namespace mcfd {
@@ -203,18 +204,19 @@ int build_modal_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
   std::vector<int32_t> type(C), vol_off(C + 1, 0);
   TetRule tet = tet_rule(p);
   const int n_hex_pts = Q * Q * Q, n_tet_pts = (int)tet.w.size();
+  const int64_t NS = d->cell_node_stride > 0 ? d->cell_node_stride : 8;
   for (int64_t c = 0; c < C; ++c) {
     int t = d->cell_type ? d->cell_type[c] : MCFD_HEX8;
-    if (t != MCFD_HEX8 && t != MCFD_TET4)
-      return fail(h, MCFD_ERR_MESH, "unknown cell type in cell " + std::to_string(c));
+    const int nv = geo::node_count(t);
+    if (nv == 0) return fail(h, MCFD_ERR_MESH, "unknown cell type in cell " + std::to_string(c));
+    if (nv > NS) return fail(h, MCFD_ERR_MESH, "cell_node_stride is below the node count of cell " + std::to_string(c));
     type[c] = t;
-    int nv = t == MCFD_HEX8 ? 8 : 4;
     for (int v = 0; v < nv; ++v) {
-      int64_t id = d->cell_nodes[c * 8 + v];
+      int64_t id = d->cell_nodes[c * NS + v];
       if (id < 0 || id >= d->n_nodes)
         return fail(h, MCFD_ERR_MESH, "cell node index out of range in cell " + std::to_string(c));
     }
-    int64_t next = (int64_t)vol_off[c] + (t == MCFD_HEX8 ? n_hex_pts : n_tet_pts);
+    int64_t next = (int64_t)vol_off[c] + (geo::is_hex(t) ? n_hex_pts : n_tet_pts);
     if (next > INT32_MAX) return fail(h, MCFD_ERR_UNSUPPORTED, "more than 2^31 volume points");
     vol_off[c + 1] = (int32_t)next;
   }
@@ -228,14 +230,39 @@ int build_modal_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
   int bad_jac = 0, bad_gram = 0;
 #pragma omp parallel for schedule(static)
   for (int64_t c = 0; c < C; ++c) {
-    double xn[24];
-    int nv = type[c] == MCFD_HEX8 ? 8 : 4;
+    double xn[geo::kMaxNodes * 3];
+    const int nv = geo::node_count(type[c]);
     for (int v = 0; v < nv; ++v)
-      for (int e = 0; e < 3; ++e) xn[v * 3 + e] = d->xyz[d->cell_nodes[c * 8 + v] * 3 + e];
+      for (int e = 0; e < 3; ++e) xn[v * 3 + e] = d->xyz[d->cell_nodes[c * NS + v] * 3 + e];
     double ctr[3], volume = 0;
     double *X = &md.host_points[(size_t)vol_off[c] * 3];
     std::vector<double> W(vol_off[c + 1] - vol_off[c]);
-    if (type[c] == MCFD_HEX8) {
+    if (geo::curved(type[c])) {
+      // quadratic map: x, det J from the shape functions at every point;
+      // centre at the local centre (hex (0,0,0), tet (1/4,1/4,1/4))
+      const bool is_t = geo::is_tet(type[c]);
+      double J[9];
+      const double cl[3] = {is_t ? 0.25 : 0.0, is_t ? 0.25 : 0.0, is_t ? 0.25 : 0.0};
+      geo::map_point(type[c], xn, cl, ctr, J);
+      const int nq = (int)W.size();
+      for (int q = 0; q < nq; ++q) {
+        double loc[3];
+        double wl;
+        if (is_t) {
+          for (int e = 0; e < 3; ++e) loc[e] = tet.x[q][e];
+          wl = tet.w[q];
+        } else {
+          const int i = q / (Q * Q), j = (q / Q) % Q, k = q % Q;
+          loc[0] = gx[i]; loc[1] = gx[j]; loc[2] = gx[k];
+          wl = gw[i] * gw[j] * gw[k];
+        }
+        geo::map_point(type[c], xn, loc, &X[q * 3], J);
+        const double det = geo::det3(J);
+        if (is_t ? !(det != 0) : !(det > 0)) bad_jac = 1;
+        W[q] = wl * (is_t ? std::fabs(det) : det);
+        volume += W[q];
+      }
+    } else if (type[c] == MCFD_HEX8) {
       const double zero[3] = {0, 0, 0};
       double det;
       hex8_map(xn, zero, ctr, &det);
@@ -327,15 +354,16 @@ int build_modal_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
     int64_t hc = d->face_cells[f * 2], sc = d->face_cells[f * 2 + 1];
     int sh = d->face_sides[f * 2], ss = d->face_sides[f * 2 + 1];
     bool ok = hc >= 0 && hc < C && sc < C && hc <= INT32_MAX;
-    if (ok) ok = sh >= 0 && sh < (type[hc] == MCFD_HEX8 ? 6 : 4);
-    if (ok && sc >= 0) ok = ss >= 0 && ss < (type[sc] == MCFD_HEX8 ? 6 : 4) && type[sc] == type[hc];
+    if (ok) ok = sh >= 0 && sh < (geo::is_hex(type[hc]) ? 6 : 4);
+    if (ok && sc >= 0)
+      ok = ss >= 0 && ss < (geo::is_hex(type[sc]) ? 6 : 4) && geo::is_hex(type[sc]) == geo::is_hex(type[hc]);
     if (!ok) return fail(h, MCFD_ERR_MESH, "bad face record " + std::to_string(f));
     fcells[f] = make_int2((int)hc, (int)sc);
     fgroup[f] = d->face_group ? d->face_group[f] : -1;
     if (sc < 0) max_group = std::max(max_group, fgroup[f]);
     if (d->face_shift)
       fshift[f] = make_double4(d->face_shift[f * 3], d->face_shift[f * 3 + 1], d->face_shift[f * 3 + 2], 0);
-    int64_t next = (int64_t)face_off[f] + (type[hc] == MCFD_HEX8 ? Q * Q : (int)tw.size());
+    int64_t next = (int64_t)face_off[f] + (geo::is_hex(type[hc]) ? Q * Q : (int)tw.size());
     if (next > INT32_MAX) return fail(h, MCFD_ERR_UNSUPPORTED, "more than 2^31 face points");
     face_off[f + 1] = (int32_t)next;
     const int64_t owners[2] = {hc, sc};
@@ -357,16 +385,16 @@ int build_modal_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
   for (int64_t f = 0; f < F; ++f) {
     int64_t hc = fcells[f].x, sc = fcells[f].y;
     int sh = d->face_sides[f * 2], ss = d->face_sides[f * 2 + 1];
-    const bool hex = type[hc] == MCFD_HEX8;
+    const bool hex = geo::is_hex(type[hc]);
     const int nfv = hex ? 4 : 3;
     double xn[12], xs[12];
     for (int v = 0; v < nfv; ++v)
       for (int e = 0; e < 3; ++e) {
         int slot = hex ? kHexFace[sh][v] : kTetFace[sh][v];
-        xn[v * 3 + e] = d->xyz[d->cell_nodes[hc * 8 + slot] * 3 + e];
+        xn[v * 3 + e] = d->xyz[d->cell_nodes[hc * NS + slot] * 3 + e];
         if (sc >= 0) {
           int sslot = hex ? kHexFace[ss][v] : kTetFace[ss][v];
-          xs[v * 3 + e] = d->xyz[d->cell_nodes[sc * 8 + sslot] * 3 + e];
+          xs[v * 3 + e] = d->xyz[d->cell_nodes[sc * NS + sslot] * 3 + e];
         }
       }
     // the sharer's face must hold the same corners (after the shift)
@@ -388,7 +416,43 @@ int build_modal_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
       }
     }
     int32_t base = face_off[f];
-    if (hex) {
+    if (geo::curved(type[hc])) {
+      // face points from the holder's cell map at the face's local points;
+      // tangents J^T dloc/da, J^T dloc/db (hex: corner 0 -> 1, 0 -> 3; tet:
+      // corner 0 - corner 2, corner 1 - corner 2 of the face)
+      double xc[geo::kMaxNodes * 3];
+      for (int v = 0; v < geo::node_count(type[hc]); ++v)
+        for (int e = 0; e < 3; ++e) xc[v * 3 + e] = d->xyz[d->cell_nodes[hc * NS + v] * 3 + e];
+      double lc[4][3];
+      for (int v = 0; v < nfv; ++v) geo::local_of_node(type[hc], hex ? kHexFace[sh][v] : kTetFace[sh][v], lc[v]);
+      double da[3], db[3];
+      for (int e = 0; e < 3; ++e) {
+        da[e] = hex ? (lc[1][e] - lc[0][e]) / 2 : lc[0][e] - lc[2][e];
+        db[e] = hex ? (lc[3][e] - lc[0][e]) / 2 : lc[1][e] - lc[2][e];
+      }
+      const int nq = hex ? Q * Q : (int)tw.size();
+      for (int q = 0; q < nq; ++q) {
+        double loc[3], wl;
+        if (hex) {
+          const int i = q / Q, j = q % Q;
+          for (int e = 0; e < 3; ++e) loc[e] = lc[0][e] + (gx[i] + 1) * da[e] + (gx[j] + 1) * db[e];
+          wl = gw[i] * gw[j];
+        } else {
+          const double x = tx[q][0], y = tx[q][1], z = 1.0 - x - y;
+          for (int e = 0; e < 3; ++e) loc[e] = lc[0][e] * x + lc[1][e] * y + lc[2][e] * z;
+          wl = tw[q];
+        }
+        double X[3], J[9], ta[3], tb[3], nn[3];
+        geo::map_point(type[hc], xc, loc, X, J);
+        geo::tangent(J, da, ta);
+        geo::tangent(J, db, tb);
+        cross(ta, tb, nn);
+        const double len = norm3(nn);
+        point_face[base + q] = (int32_t)f;
+        fpt[base + q] = make_double4(X[0], X[1], X[2], wl * len);
+        fnrm[base + q] = make_double4(nn[0] / len, nn[1] / len, nn[2] / len, 0);
+      }
+    } else if (hex) {
       for (int i = 0; i < Q; ++i)
         for (int j = 0; j < Q; ++j) {
           int q = i * Q + j;

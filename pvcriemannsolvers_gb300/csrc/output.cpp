@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "../../include/mcfd.h"
+#include "geometry.hpp"
 #include "handle.hpp"
 
 namespace {
@@ -138,6 +139,32 @@ struct RestartHeader {
   uint64_t checksum;
 };
 const char kRestartMagic[8] = {'M', 'C', 'F', 'D', 'R', 'S', 'T', '\0'};
+
+// VTK local coordinates of the written elements (mesh/vtk.hpp:214-224,
+// 310-330), for the host-side points of curved cells: Hexahedron27 in
+// [-1, 1]^3 and Tetrahedron10 in units of 1/2, VTK node order.
+const signed char kHostHex27[27][3] = {
+    {-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1}, {-1, -1, 1}, {1, -1, 1}, {1, 1, 1},
+    {-1, 1, 1},   {0, -1, -1}, {1, 0, -1}, {0, 1, -1},  {-1, 0, -1}, {0, -1, 1},  {1, 0, 1},
+    {0, 1, 1},    {-1, 0, 1},  {-1, -1, 0}, {1, -1, 0}, {1, 1, 0},   {-1, 1, 0},  {-1, 0, 0},
+    {1, 0, 0},    {0, -1, 0},  {0, 1, 0},  {0, 0, -1},  {0, 0, 1},   {0, 0, 0}};
+const signed char kHostTet10Half[10][3] = {{2, 0, 0}, {0, 2, 0}, {0, 0, 2}, {0, 0, 0}, {1, 1, 0},
+                                           {0, 1, 1}, {1, 0, 1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+
+// The VTK points of every cell through its own map (curved meshes).
+void host_vtk_points(const mcfd_handle *h, const std::vector<int64_t> &off, double *xyz) {
+  const auto &m = h->mesh;
+  for (int64_t c = 0; c < m.n_cells; ++c) {
+    const int t = m.host_cell_type[c];
+    const bool tet = mcfd::geo::is_tet(t);
+    const double *xn = &m.host_nodes[(size_t)c * mcfd::geo::kMaxNodes * 3];
+    for (int s = 0; s < (tet ? 10 : 27); ++s) {
+      double loc[3], J[9];
+      for (int e = 0; e < 3; ++e) loc[e] = tet ? 0.5 * kHostTet10Half[s][e] : kHostHex27[s][e];
+      mcfd::geo::map_point(t, xn, loc, &xyz[(off[c] + s) * 3], J);
+    }
+  }
+}
 
 // VTK point offsets of the cells (27 per Hex8, 10 per Tet4).
 std::vector<int64_t> vtk_offsets(const mcfd_handle *h) {
@@ -258,6 +285,10 @@ int mcfd_vtk_sample(mcfd_handle *h, double *xyz, double *values, uint8_t *types,
   if (e == cudaSuccess) e = cudaMalloc(&d_val, sizeof(double) * kK5 * np);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(d_off, off.data(), sizeof(int64_t) * (nc + 1), cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess && h->mesh.curved) {  // points through the quadratic maps, on the host
+    host_vtk_points(h, off, xyz);
+    e = cudaMemcpyAsync(d_xyz, xyz, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, h->stream);
+  }
   if (e == cudaSuccess) {
     h->launches += mcfd::launch_vtk_sample(h, h->buf.u, d_off, d_xyz, d_val);
     e = cudaGetLastError();

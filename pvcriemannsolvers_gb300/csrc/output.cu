@@ -71,6 +71,7 @@ struct SampleArgs {
   double *values;
   int64_t n_cells;
   double xq[4];
+  int points_given;  // curved cells: xyz holds the points already (host-mapped)
 };
 
 template <int Q>
@@ -118,8 +119,10 @@ __global__ void __launch_bounds__(256) vtk_sample_kernel(SampleArgs a) {
         for (int e = 0; e < kK; ++e) v[e] += w * un[e];
       }
   const int64_t pt = (a.off ? a.off[c] : c * 27) + s;
+  if (!a.points_given) {
 #pragma unroll
-  for (int e = 0; e < 3; ++e) a.xyz[pt * 3 + e] = g[e];
+    for (int e = 0; e < 3; ++e) a.xyz[pt * 3 + e] = g[e];
+  }
 #pragma unroll
   for (int e = 0; e < kK; ++e) a.values[pt * kK + e] = v[e];
 }
@@ -142,7 +145,8 @@ int launch_vtk_sample(mcfd_handle *h, const double *u, const int64_t *off, doubl
                       double *values) {
   if (h->opt.scheme == 2) return launch_modal_vtk_sample(h, u, off, xyz, values);
   const Mesh &m = h->mesh;
-  SampleArgs a{u, m.corners, off, xyz, values, m.n_cells, {m.xq[0], m.xq[1], m.xq[2], m.xq[3]}};
+  SampleArgs a{u, m.corners, off, xyz, values, m.n_cells, {m.xq[0], m.xq[1], m.xq[2], m.xq[3]},
+               m.curved ? 1 : 0};
   const int64_t threads = m.n_cells * 27;
   const unsigned blocks = (unsigned)((threads + 255) / 256);
   switch (m.q) {

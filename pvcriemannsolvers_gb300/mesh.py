@@ -170,15 +170,113 @@ def gll_points(q: int) -> np.ndarray:
 
 def node_coordinates(mesh: Mesh, degree: int) -> np.ndarray:
     """Global coordinates of the (p+1)^3 GLL nodes of every cell, [cells, N, 3],
-    node order i*Q*Q + j*Q + k (integrator/hexahedron.hpp:66-80)."""
+    node order i*Q*Q + j*Q + k (integrator/hexahedron.hpp:66-80), through
+    each cell's map (Hex8, Hex20 or Hex27)."""
     x = gll_points(degree + 1)
     a, b, c = np.meshgrid(x, x, x, indexing="ij")
     loc = np.stack([a.ravel(), b.ravel(), c.ravel()], axis=1)  # [N, 3]
-    corners = np.array([[-1, -1, -1], [1, -1, -1], [1, 1, -1], [-1, 1, -1],
-                        [-1, -1, 1], [1, -1, 1], [1, 1, 1], [-1, 1, 1]], dtype=np.float64)
-    shape = np.prod(1 + loc[:, None, :] * corners[None, :, :], axis=2) / 8  # [N, 8]
-    xn = mesh.xyz[mesh.cell_nodes]  # [cells, 8, 3]
-    return np.einsum("nv,cvd->cnd", shape, xn)
+    types = np.zeros(mesh.n_cells, np.int32) if mesh.cell_type is None else mesh.cell_type
+    out = np.empty((mesh.n_cells, loc.shape[0], 3))
+    for t in np.unique(types):
+        sel = types == t
+        shape = hex_shapes(int(t), loc)  # [N, nodes]
+        xn = mesh.xyz[mesh.cell_nodes[sel, :shape.shape[1]]]
+        out[sel] = np.einsum("nv,cvd->cnd", shape, xn)
+    return out
+
+
+HEX27, TET10, HEX20 = 2, 3, 4
+# CGNS HEXA_27 local coordinates (coordinate/hexahedron.hpp Hexahedron27):
+# corners, mid-edges bottom / vertical / top, face centres, centre
+HEX27_LOCAL = np.array([
+    [-1, -1, -1], [1, -1, -1], [1, 1, -1], [-1, 1, -1], [-1, -1, 1], [1, -1, 1], [1, 1, 1], [-1, 1, 1],
+    [0, -1, -1], [1, 0, -1], [0, 1, -1], [-1, 0, -1], [-1, -1, 0], [1, -1, 0], [1, 1, 0], [-1, 1, 0],
+    [0, -1, 1], [1, 0, 1], [0, 1, 1], [-1, 0, 1], [0, 0, -1], [0, -1, 0], [1, 0, 0], [0, 1, 0],
+    [-1, 0, 0], [0, 0, 1], [0, 0, 0]], dtype=np.float64)
+HEX_EDGES = np.array([[0, 1], [1, 2], [2, 3], [3, 0], [0, 4], [1, 5], [2, 6], [3, 7],
+                      [4, 5], [5, 6], [6, 7], [7, 4]])
+HEX_FACE_CORNERS = np.array([[0, 3, 2, 1], [0, 1, 5, 4], [1, 2, 6, 5], [2, 3, 7, 6], [0, 4, 7, 3], [4, 5, 6, 7]])
+TET_EDGES = np.array([[0, 1], [1, 2], [2, 0], [3, 0], [3, 1], [3, 2]])  # AB BC CA DA DB DC
+
+
+def hex_shapes(cell_type: int, loc: np.ndarray) -> np.ndarray:
+    """Shape functions [points, nodes] of a hexahedron type at local points."""
+    L = HEX27_LOCAL
+    x, y, z = loc[:, 0:1], loc[:, 1:2], loc[:, 2:3]
+    if cell_type == HEX8:
+        return (1 + x * L[None, :8, 0]) * (1 + y * L[None, :8, 1]) * (1 + z * L[None, :8, 2]) / 8
+
+    def q1(c, t):
+        return np.where(c == 0, 1 - t * t, 0.5 * t * (t + c))
+    if cell_type == HEX27:
+        return q1(L[None, :, 0], x) * q1(L[None, :, 1], y) * q1(L[None, :, 2], z)
+    if cell_type == HEX20:
+        l = L[:20]
+        f = [1 + x * l[None, :, 0], 1 + y * l[None, :, 1], 1 + z * l[None, :, 2]]
+        corner = f[0] * f[1] * f[2] * (x * l[None, :, 0] + y * l[None, :, 1] + z * l[None, :, 2] - 2) / 8
+        t = [x, y, z]
+        out = corner.copy()
+        for ax in range(3):
+            mid = (l[:, ax] == 0)[None, :]
+            o1, o2 = f[(ax + 1) % 3], f[(ax + 2) % 3]
+            out = np.where(mid, (1 - t[ax] * t[ax]) * o1 * o2 / 4, out)
+        return out
+    raise ValueError("not a hexahedron type")
+
+
+def quadratic(m: Mesh, serendipity: bool = False) -> Mesh:
+    """The same mesh with quadratic cells (Hex8 -> Hex27, or Hex20 with
+    serendipity=True; Tet4 -> Tet10): mid-edge, mid-face and centre nodes at
+    the averages of their corners, shared between neighbours, so the geometry
+    is unchanged until the nodes are moved (see deform())."""
+    types = np.zeros(m.n_cells, np.int32) if m.cell_type is None else m.cell_type.astype(np.int32)
+    tet = types == TET4
+    xyz = [m.xyz]
+    n_nodes = m.xyz.shape[0]
+    stride = 27 if not serendipity or tet.any() else 20
+    cn = np.full((m.n_cells, max(stride, 10 if tet.any() else 0, 20)), -1, dtype=np.int64)
+    cn[:, :8] = m.cell_nodes[:, :8]
+
+    def shared(groups):  # groups [k, n]: corner sets -> new node ids (shared by sorted key)
+        nonlocal n_nodes
+        key = np.sort(groups, axis=1)
+        uniq, inv = np.unique(key, axis=0, return_inverse=True)
+        pos = m.xyz[uniq].mean(axis=1)
+        ids = n_nodes + np.arange(uniq.shape[0])
+        xyz.append(pos)
+        n_nodes += uniq.shape[0]
+        return ids[inv.ravel()]
+    hexes = np.flatnonzero(~tet)
+    if hexes.size:
+        corners = m.cell_nodes[hexes, :8]
+        e = shared(corners[:, HEX_EDGES].reshape(-1, 2)).reshape(hexes.size, 12)
+        cn[hexes, 8:20] = e
+        if not serendipity:
+            f = shared(corners[:, HEX_FACE_CORNERS].reshape(-1, 4)).reshape(hexes.size, 6)
+            # CGNS centre order: bottom, -y, +x, +y, -x, top = local faces 0..5
+            cn[hexes, 20:26] = f
+            c = shared(corners)
+            cn[hexes, 26] = c
+    tets = np.flatnonzero(tet)
+    if tets.size:
+        corners = m.cell_nodes[tets, :4]
+        cn[tets, 4:10] = shared(corners[:, TET_EDGES].reshape(-1, 2)).reshape(tets.size, 6)
+        cn[tets, 10:] = -1
+    new_types = np.where(tet, TET10, HEX20 if serendipity else HEX27).astype(np.int32)
+    cn = cn[:, :max(27 if (not serendipity and hexes.size) else 20 if hexes.size else 10, 1)]
+    return Mesh(xyz=np.ascontiguousarray(np.concatenate(xyz)), cell_nodes=np.ascontiguousarray(cn),
+                face_cells=m.face_cells, face_sides=m.face_sides, face_group=m.face_group,
+                face_shift=m.face_shift, cell_type=new_types, shape=m.shape, lengths=m.lengths,
+                origin=m.origin, periodic=m.periodic, meta=dict(m.meta))
+
+
+def deform(m: Mesh, fn) -> Mesh:
+    """The mesh with every node moved to fn(xyz) (vectorised over [n, 3]);
+    keep fn periodic with the box for periodic meshes."""
+    return Mesh(xyz=np.ascontiguousarray(fn(m.xyz), dtype=np.float64), cell_nodes=m.cell_nodes,
+                face_cells=m.face_cells, face_sides=m.face_sides, face_group=m.face_group,
+                face_shift=m.face_shift, cell_type=m.cell_type, shape=m.shape, lengths=m.lengths,
+                origin=m.origin, periodic=m.periodic, meta=dict(m.meta))
 
 
 # Tetrahedron4::faces_ (coordinate/tetrahedron.hpp:141-147): local face ->
@@ -304,9 +402,11 @@ def concat(*meshes: Mesh) -> Mesh:
     b * 6 + group."""
     xyz, cn, fc, fs, fg, fsh, ct = [], [], [], [], [], [], []
     n_off = c_off = 0
+    stride = max(m.cell_nodes.shape[1] for m in meshes)
     for b, m in enumerate(meshes):
         xyz.append(m.xyz)
-        nodes = m.cell_nodes.copy()
+        nodes = np.full((m.n_cells, stride), -1, dtype=np.int64)
+        nodes[:, :m.cell_nodes.shape[1]] = m.cell_nodes
         nodes[nodes >= 0] += n_off
         cn.append(nodes)
         f = m.face_cells.copy()
@@ -362,7 +462,7 @@ def build(xyz, cell_nodes, cell_type=None, bface_nodes=None, bface_group=None,
     fsh = np.empty((cap, 3), np.float64)
     n = C.c_int64()
     rc = lib.mcfd_build_faces(xyz.shape[0], xyz.ctypes.data_as(PD), cn.shape[0], cn.ctypes.data_as(P64), ct_p,
-                              bf.shape[0], bf.ctypes.data_as(P64), bg.ctypes.data_as(P32), pg.shape[0],
+                              cn.shape[1], bf.shape[0], bf.ctypes.data_as(P64), bg.ctypes.data_as(P32), pg.shape[0],
                               pg.ctypes.data_as(P32), ps.ctypes.data_as(PD), cap, fc.ctypes.data_as(P64),
                               fs.ctypes.data_as(P32), fg.ctypes.data_as(P32), fsh.ctypes.data_as(PD),
                               C.byref(n))
@@ -377,10 +477,10 @@ def build(xyz, cell_nodes, cell_type=None, bface_nodes=None, bface_group=None,
 def cell_centroids(m: Mesh) -> np.ndarray:
     """Mean of each cell's corner nodes (8 for Hex8, 4 for Tet4)."""
     if m.cell_type is None:
-        return m.xyz[m.cell_nodes].mean(axis=1)
-    tet = m.cell_type == TET4
+        return m.xyz[m.cell_nodes[:, :8]].mean(axis=1)
+    tet = (m.cell_type == TET4) | (m.cell_type == TET10)
     out = m.xyz[m.cell_nodes[:, :4].clip(0)].mean(axis=1)
-    out[~tet] = m.xyz[m.cell_nodes[~tet]].mean(axis=1)
+    out[~tet] = m.xyz[m.cell_nodes[~tet, :8]].mean(axis=1)
     return out
 
 

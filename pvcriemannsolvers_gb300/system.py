@@ -102,6 +102,7 @@ class Lobatto:
         desc.face_sides = fs.ctypes.data_as(C.POINTER(C.c_int32))
         desc.face_group = fg.ctypes.data_as(C.POINTER(C.c_int32))
         desc.face_shift = capi.dptr(fsh)
+        desc.cell_node_stride = cn.shape[1]
         opt = capi.Options()
         opt.degree = self.degree
         if scheme not in capi.SCHEME:
