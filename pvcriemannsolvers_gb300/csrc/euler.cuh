@@ -531,6 +531,69 @@ MCFD_HD void flux_roe(const Prim &l, const Prim &r, const double *n,
           (t0 * u + t1 * v + t2 * w);
 }
 
+// Roe on conservative inputs, times the face weight w, for two admissible
+// states (rho > 0, E >= 0, p >= 0 on both sides; false otherwise and the
+// caller takes flux_roe on the converted primitives).  The same flux as
+// flux_roe, regrouped: the physical fluxes from the conservative variables
+// (m u_n + p n, (E + p) u_n), the total enthalpy as (E + p) / rho, the Roe
+// weights from lambda = sqrt(rho_R / rho_L) (u~ = (u_L + lambda u_R) /
+// (1 + lambda), rho~ = lambda rho_L: one square root instead of two), the
+// acoustic pair combined as (a1 + a5) (u, h0) + (a5 - a1) a (n, u_n), and the
+// halves of the average and of the wave strengths folded into one w / 2.
+// FAST_SQRT (the mixed form) takes both square roots from sqrt_seeded.
+template <bool FAST_SQRT>
+MCFD_HD bool flux_roe_cons_weighted(const double *cl, const double *cr, const double *n,
+                                    double w, double *f) {
+  const double rl = cl[0], rr = cr[0], el = cl[4], er = cr[4];
+  if (!bits_positive(rl) || !bits_positive(rr) || bits_negative(el) || bits_negative(er)) return false;
+  const double il = rcp_newton(rl), ir = rcp_newton(rr);
+  const double ul = cl[1] * il, vl = cl[2] * il, wl = cl[3] * il;
+  const double ur = cr[1] * ir, vr = cr[2] * ir, wr = cr[3] * ir;
+  const double pl = (el - 0.5 * (cl[1] * ul + cl[2] * vl + cl[3] * wl)) * kGm1;
+  const double pr = (er - 0.5 * (cr[1] * ur + cr[2] * vr + cr[3] * wr)) * kGm1;
+  if (bits_negative(pl) || bits_negative(pr)) return false;
+  const double unl = ul * n[0] + vl * n[1] + wl * n[2];
+  const double unr = ur * n[0] + vr * n[1] + wr * n[2];
+  // F(U_L) + F(U_R)
+  const double s0 = rl * unl + rr * unr;
+  const double s1 = (cl[1] * unl + pl * n[0]) + (cr[1] * unr + pr * n[0]);
+  const double s2 = (cl[2] * unl + pl * n[1]) + (cr[2] * unr + pr * n[1]);
+  const double s3 = (cl[3] * unl + pl * n[2]) + (cr[3] * unr + pr * n[2]);
+  const double s4 = (el + pl) * unl + (er + pr) * unr;
+  // Roe averages
+  double lam;
+  if constexpr (FAST_SQRT) lam = sqrt_seeded(rr * il);
+  else lam = sqrt(rr * il);
+  const double inv = rcp_newton(1 + lam);
+  const double rho = lam * rl;
+  const double u = (ul + lam * ur) * inv, v = (vl + lam * vr) * inv, ww = (wl + lam * wr) * inv;
+  const double h0 = ((el + pl) * il + lam * ((er + pr) * ir)) * inv;
+  const double un = u * n[0] + v * n[1] + ww * n[2];
+  const double ke = 0.5 * (u * u + v * v + ww * ww);
+  const double aa = kGm1 * (h0 - ke);
+  double a;
+  if constexpr (FAST_SQRT) a = sqrt_seeded(aa);
+  else a = sqrt(aa);
+  const double i2aa = rcp_newton(2 * aa);
+  // twice the wave strengths times |lambda_k|
+  const double dp = pr - pl, rau = rho * a * (unr - unl);
+  const double a1 = ((dp - rau) * i2aa) * fabs(un - a);
+  const double a2 = ((rr - rl) - dp * (2 * i2aa)) * fabs(un);
+  const double a5 = ((dp + rau) * i2aa) * fabs(un + a);
+  const double dv0 = ur - ul, dv1 = vr - vl, dv2 = wr - wl;
+  const double dvn = dv0 * n[0] + dv1 * n[1] + dv2 * n[2];
+  const double st = rho * fabs(un);
+  const double t0 = st * (dv0 - dvn * n[0]), t1 = st * (dv1 - dvn * n[1]), t2 = st * (dv2 - dvn * n[2]);
+  const double S = a1 + a5, Sa = S + a2, D = (a5 - a1) * a;
+  const double hw = 0.5 * w;
+  f[0] = hw * (s0 - Sa);
+  f[1] = hw * (s1 - (Sa * u + D * n[0] + t0));
+  f[2] = hw * (s2 - (Sa * v + D * n[1] + t1));
+  f[3] = hw * (s3 - (Sa * ww + D * n[2] + t2));
+  f[4] = hw * (s4 - (S * h0 + D * un + a2 * ke + (t0 * u + t1 * v + t2 * ww)));
+  return true;
+}
+
 // ---------------------------------------------------------------- Exact
 // exact.hpp:62-320 on the normal component; the tangential velocity comes
 // from the left state if u* > 0 else the right (SetPassiveScalars).  The
