@@ -81,18 +81,34 @@ weno_modal_kernel(const double *__restrict__ u, const double *__restrict__ mn,
 // the conservative state of primitive w in the frame {nu, mu, pi}:
 // e < 25 is L[e / 5][e % 5], otherwise R[(e - 25) / 5][(e - 25) % 5].
 // Columns of R: u - a, u (entropy), two shear waves, u + a; L = R^-1.
-__device__ double eigen_entry(const Prim &w, const double *nu, const double *mu,
+// Frame-independent scalars of EigenMatrices at one state, computed once per
+// cell: velocity, a, 1/a, b1 = 1/e0 (e0 = a^2 / (gamma - 1)), ek, h0 = e0 + ek.
+struct EigenState {
+  double vel[3], a, ia, b1, ek, h0;
+};
+
+__device__ EigenState eigen_state(const Prim &w) {
+  EigenState s;
+  s.vel[0] = w.u; s.vel[1] = w.v; s.vel[2] = w.w;
+  s.a = sqrt(kGamma * w.p / w.rho);
+  s.ia = 1 / s.a;
+  s.ek = (w.u * w.u + w.v * w.v + w.w * w.w) / 2;
+  const double e0 = s.a * s.a * (1 / kGm1);
+  s.b1 = 1 / e0;
+  s.h0 = e0 + s.ek;
+  return s;
+}
+
+__device__ double eigen_entry(const EigenState &s, const double *nu, const double *mu,
                               const double *pi, int e) {
-  const double vel[3] = {w.u, w.v, w.w};
+  const double *vel = s.vel;
   const double u_nu = vel[0] * nu[0] + vel[1] * nu[1] + vel[2] * nu[2];
-  const double a = sqrt(kGamma * w.p / w.rho);
-  const double ek = (vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]) / 2;
-  const double e0 = a * a * (1 / kGm1);
+  const double a = s.a, ek = s.ek;
   if (e >= 25) {
     const int row = (e - 25) / 5, col = (e - 25) % 5;
     if (row == 0) return (col == 2 || col == 3) ? 0.0 : 1.0;
     if (row == 4) {
-      const double h0 = e0 + ek;
+      const double h0 = s.h0;
       if (col == 0) return h0 - a * u_nu;
       if (col == 1) return ek;
       if (col == 2) return vel[0] * mu[0] + vel[1] * mu[1] + vel[2] * mu[2];
@@ -107,13 +123,13 @@ __device__ double eigen_entry(const Prim &w, const double *nu, const double *mu,
     return vel[d] + a * nu[d];
   }
   const int row = e / 5, col = e % 5;
-  const double b1 = 1 / e0, b2 = b1 * ek;
+  const double b1 = s.b1, b2 = b1 * ek;
   if (col == 0) {
-    if (row == 0) return (b2 + u_nu / a) / 2;
+    if (row == 0) return (b2 + u_nu * s.ia) / 2;
     if (row == 1) return 1 - b2;
     if (row == 2) return -(vel[0] * mu[0] + vel[1] * mu[1] + vel[2] * mu[2]);
     if (row == 3) return -(vel[0] * pi[0] + vel[1] * pi[1] + vel[2] * pi[2]);
-    return (b2 - u_nu / a) / 2;
+    return (b2 - u_nu * s.ia) / 2;
   }
   if (col == 4) {
     if (row == 0 || row == 4) return b1 / 2;
@@ -121,11 +137,11 @@ __device__ double eigen_entry(const Prim &w, const double *nu, const double *mu,
     return 0.0;
   }
   const int d = col - 1;
-  if (row == 0) return -(b1 * vel[d] + nu[d] / a) / 2;
+  if (row == 0) return -(b1 * vel[d] + nu[d] * s.ia) / 2;
   if (row == 1) return b1 * vel[d];
   if (row == 2) return mu[d];
   if (row == 3) return pi[d];
-  return -(b1 * vel[d] - nu[d] / a) / 2;
+  return -(b1 * vel[d] - nu[d] * s.ia) / 2;
 }
 
 // weno::Eigen reconstruction of cell c from its candidates (slots 0..n_adj-1
@@ -146,6 +162,7 @@ __device__ void eigen_reconstruct(const Args &a, int64_t c, int n_adj,
   __shared__ double s_w[6][7][kK];
   __shared__ double s_nw[6][kK][M];
   __shared__ double s_vol[6];
+  __shared__ EigenState s_es;
   const int t = threadIdx.x, nt = blockDim.x;
   const int nc = n_adj + 1;  // candidates: 0..n_adj-1 neighbours, then own (slot 6)
   const double *B = a.beta + c * M * M;
@@ -157,16 +174,20 @@ __device__ void eigen_reconstruct(const Args &a, int64_t c, int n_adj,
     for (int j = 0; j < M; ++j) v += s_cand[src][k][j] * B[j * M + m];
     s_cb[cand][k][m] = v;
   }
-  {
+  if (t == 0) {
     const double s00 = a.s00[c];
-    const Prim w = cons_to_prim(s_cand[6][0][0] * s00, s_cand[6][1][0] * s00, s_cand[6][2][0] * s00,
-                                s_cand[6][3][0] * s00, s_cand[6][4][0] * s00);
+    s_es = eigen_state(cons_to_prim(s_cand[6][0][0] * s00, s_cand[6][1][0] * s00, s_cand[6][2][0] * s00,
+                                    s_cand[6][3][0] * s00, s_cand[6][4][0] * s00));
+  }
+  if (t < n_adj) s_vol[t] = a.volume[a.adj[c * 6 + t]];
+  __syncthreads();
+  {
+    const EigenState es = s_es;
     for (int i = t; i < n_adj * 50; i += nt) {
       const int f = i / 50, e = i - f * 50;
       const double *fr = a.frame + (c * 6 + f) * 9;
-      s_LR[f][e] = eigen_entry(w, fr, fr + 3, fr + 6, e);
+      s_LR[f][e] = eigen_entry(es, fr, fr + 3, fr + 6, e);
     }
-    if (t < n_adj) s_vol[t] = a.volume[a.adj[c * 6 + t]];
   }
   __syncthreads();
   for (int i = t; i < nc * kK * kK; i += nt) {
@@ -204,11 +225,12 @@ __device__ void eigen_reconstruct(const Args &a, int64_t c, int n_adj,
       }
       double b = s_beta[f][cand][k] + a.eps;
       b *= b;
-      w /= b;
+      w *= rcp_newton(b);
       s_w[f][cand][k] = w;
       sum += w;
     }
-    for (int cand = 0; cand < nc; ++cand) s_w[f][cand][k] /= sum;
+    const double isum = rcp_newton(sum);
+    for (int cand = 0; cand < nc; ++cand) s_w[f][cand][k] *= isum;
   }
   __syncthreads();
   // nw[f] = w_own (L_f C_own) + sum_i w_i (L_f C_i)   (weno.hpp:327-333)
@@ -240,7 +262,7 @@ __device__ void eigen_reconstruct(const Args &a, int64_t c, int n_adj,
       acc += v * s_vol[f];
       total += s_vol[f];
     }
-    s_new[k][m] = acc / total;
+    s_new[k][m] = acc * rcp_newton(total);
   }
   __syncthreads();
 }
