@@ -166,6 +166,14 @@ __global__ void __launch_bounds__(512) face_flux_kernel(FaceArgs a) {
           return;
         }
       }
+      if constexpr (R == kHllc) {
+        if (flux_hllc_cons<FAST_SQRT>(ch, cs, n, out)) {
+#pragma unroll
+          for (int k = 0; k < kK; ++k) out[k] *= g.w;
+          store_flux(a.flux, a.f32_out, gid, out);
+          return;
+        }
+      }
       Prim l = cons_to_prim(ch[0], ch[1], ch[2], ch[3], ch[4]);
       Prim r = cons_to_prim(cs[0], cs[1], cs[2], cs[3], cs[4]);
       flux_upwind<R>(l, r, n, out, &not_converged);
@@ -653,7 +661,7 @@ template <int Q, int R>
 void face_launch(mcfd_handle *h, const FaceArgs &fa) {
   const int bs = h->tune.face_block;
   int64_t blocks = (fa.n_points + bs - 1) / bs;
-  if constexpr (R == kRusanov || R == kRoe) {
+  if constexpr (R == kRusanov || R == kRoe || R == kHllc) {
     if (h->opt.precision == 1) {
       face_flux_kernel<Q, R, true><<<(unsigned)blocks, bs, 0, h->stream>>>(fa);
       return;

@@ -531,6 +531,81 @@ MCFD_HD void flux_roe(const Prim &l, const Prim &r, const double *n,
           (t0 * u + t1 * v + t2 * w);
 }
 
+// HLLC on conservative inputs for two states with rho > 0, E >= 0 and
+// p > 0 on both sides (false otherwise: the caller takes flux_hllc on the
+// converted primitives).  The same flux as flux_hllc with the energy and
+// momenta taken from the inputs instead of being rebuilt from primitives;
+// FAST_SQRT (the mixed form) takes the sound speeds and the pressure-ratio
+// roots from sqrt_seeded.
+template <bool FAST_SQRT>
+MCFD_HD double sqrt_form(double x) {
+  if constexpr (FAST_SQRT) return sqrt_seeded(x);
+  else return sqrt(x);
+}
+
+template <bool FAST_SQRT>
+MCFD_HD double hllc_q_form(double p_estimate, double p_k) {
+  if (p_estimate <= p_k) return 1.0;
+  double temp = 1 + kGp1Over2 * (p_estimate * rcp_newton(p_k) - 1) * kOneOverGamma;
+  return sqrt_form<FAST_SQRT>(temp);
+}
+
+// one side's flux, plus the star correction when wk is finite (hllc_star)
+MCFD_HD void hllc_side_cons(const double *c, double rinv, double u, double v, double w,
+                            double p, double un, const double *n, bool star, double wk,
+                            double ws, double *f) {
+  const double rho = c[0], e = c[4];
+  f[0] = rho * un;
+  f[1] = c[1] * un + p * n[0];
+  f[2] = c[2] * un + p * n[1];
+  f[3] = c[3] * un + p * n[2];
+  f[4] = (e + p) * un;
+  if (!star) return;
+  const double temp = rho * (wk - un) * rcp_signed(wk - ws);
+  double es = e * rinv + (ws - un) * (ws + p * rcp_signed(rho * (wk - un)));
+  es *= temp;
+  const double dm = temp * (ws - un);
+  f[0] += wk * (temp - rho);
+  f[1] += wk * ((temp * u + dm * n[0]) - c[1]);
+  f[2] += wk * ((temp * v + dm * n[1]) - c[2]);
+  f[3] += wk * ((temp * w + dm * n[2]) - c[3]);
+  f[4] += wk * (es - e);
+}
+
+template <bool FAST_SQRT>
+MCFD_HD bool flux_hllc_cons(const double *cl, const double *cr, const double *n, double *f) {
+  const double rl = cl[0], rr = cr[0];
+  if (!bits_positive(rl) || !bits_positive(rr) || bits_negative(cl[4]) || bits_negative(cr[4])) return false;
+  const double il = rcp_newton(rl), ir = rcp_newton(rr);
+  const double ul = cl[1] * il, vl = cl[2] * il, wl = cl[3] * il;
+  const double ur = cr[1] * ir, vr = cr[2] * ir, wr = cr[3] * ir;
+  const double pl = (cl[4] - rl * (0.5 * (ul * ul + vl * vl + wl * wl))) * kGm1;
+  const double pr = (cr[4] - rr * (0.5 * (ur * ur + vr * vr + wr * wr))) * kGm1;
+  if (!bits_positive(pl) || !bits_positive(pr)) return false;
+  const double unl = ul * n[0] + vl * n[1] + wl * n[2];
+  const double unr = ur * n[0] + vr * n[1] + wr * n[2];
+  const double al = sqrt_form<FAST_SQRT>(kGamma * pl * il), ar = sqrt_form<FAST_SQRT>(kGamma * pr * ir);
+  const double rho_average = (rl + rr) / 2, a_average = (al + ar) / 2;
+  const double p_pvrs = (pl + pr - (unr - unl) * rho_average * a_average) / 2;
+  const double p_estimate = fmax(0.0, p_pvrs);
+  const double wave_left = unl - al * hllc_q_form<FAST_SQRT>(p_estimate, pl);
+  const double wave_right = unr + ar * hllc_q_form<FAST_SQRT>(p_estimate, pr);
+  const double wave_star = (pr - pl + rl * unl * (wave_left - unl) - rr * unr * (wave_right - unr)) *
+                           rcp_signed(rl * (wave_left - unl) - rr * (wave_right - unr));
+  if (0.0 <= wave_left) {
+    hllc_side_cons(cl, il, ul, vl, wl, pl, unl, n, false, 0, 0, f);
+  } else if (wave_right <= 0.0) {
+    hllc_side_cons(cr, ir, ur, vr, wr, pr, unr, n, false, 0, 0, f);
+  } else if (0.0 <= wave_star) {
+    hllc_side_cons(cl, il, ul, vl, wl, pl, unl, n, true, wave_left, wave_star, f);
+  } else if (wave_star < 0.0) {
+    hllc_side_cons(cr, ir, ur, vr, wr, pr, unr, n, true, wave_right, wave_star, f);
+  } else {
+    for (int k = 0; k < kK; ++k) f[k] = NAN;
+  }
+  return true;
+}
+
 // Roe on conservative inputs, times the face weight w, for two admissible
 // states (rho > 0, E >= 0, p >= 0 on both sides; false otherwise and the
 // caller takes flux_roe on the converted primitives).  The same flux as

@@ -159,16 +159,22 @@ __global__ void __launch_bounds__(512) modal_face_kernel(ModalFaceArgs a) {
   taylor_values<M>(x.x - ch.x, x.y - ch.y, x.z - ch.z, t);
   eval_taylor<M>(a.taylor + (int64_t)cells.x * M * kK, t, uh);
   bool not_converged = false;
-  Prim l = cons_to_prim(uh[0], uh[1], uh[2], uh[3], uh[4]);
   if (cells.y >= 0) {
     const double4 sh = a.fshift[f];
     const double4 cs = a.center[cells.y];
     double us[kK];
     taylor_values<M>((x.x - sh.x) - cs.x, (x.y - sh.y) - cs.y, (x.z - sh.z) - cs.z, t);
     eval_taylor<M>(a.taylor + (int64_t)cells.y * M * kK, t, us);
-    Prim r = cons_to_prim(us[0], us[1], us[2], us[3], us[4]);
-    flux_upwind<R>(l, r, n, out, &not_converged);
+    bool done = false;
+    if constexpr (R == kHllc) done = flux_hllc_cons<false>(uh, us, n, out);
+    if constexpr (R == kRoe) done = flux_roe_cons_weighted<false>(uh, us, n, 1.0, out);
+    if (!done) {
+      Prim l = cons_to_prim(uh[0], uh[1], uh[2], uh[3], uh[4]);
+      Prim r = cons_to_prim(us[0], us[1], us[2], us[3], us[4]);
+      flux_upwind<R>(l, r, n, out, &not_converged);
+    }
   } else {
+    Prim l = cons_to_prim(uh[0], uh[1], uh[2], uh[3], uh[4]);
     const int grp = a.face_group[f];
     if (grp >= 0 && grp < a.n_groups && a.bcs[grp].kind != kBcNone) {
       const BcDev &bc = a.bcs[grp];
@@ -503,7 +509,6 @@ __global__ void __launch_bounds__(512) modal_face32_kernel(ModalFace32Args a) {
 #pragma unroll
   for (int k = 0; k < kK; ++k) uh[k] = f32_to_f64(v[k]);
   bool not_converged = false;
-  Prim l = cons_to_prim(uh[0], uh[1], uh[2], uh[3], uh[4]);
   if (cells.y >= 0) {
     const float4 os = a.foff32[gid * 2 + 1];
     double us[kK];
@@ -511,9 +516,16 @@ __global__ void __launch_bounds__(512) modal_face32_kernel(ModalFace32Args a) {
     eval_taylor<M, float>(a.taylor32 + (int64_t)cells.y * M * kK, t, v);
 #pragma unroll
     for (int k = 0; k < kK; ++k) us[k] = f32_to_f64(v[k]);
-    Prim r = cons_to_prim(us[0], us[1], us[2], us[3], us[4]);
-    flux_upwind<R>(l, r, n, out, &not_converged);
+    bool done = false;
+    if constexpr (R == kHllc) done = flux_hllc_cons<true>(uh, us, n, out);
+    if constexpr (R == kRoe) done = flux_roe_cons_weighted<true>(uh, us, n, 1.0, out);
+    if (!done) {
+      Prim l = cons_to_prim(uh[0], uh[1], uh[2], uh[3], uh[4]);
+      Prim r = cons_to_prim(us[0], us[1], us[2], us[3], us[4]);
+      flux_upwind<R>(l, r, n, out, &not_converged);
+    }
   } else {
+    Prim l = cons_to_prim(uh[0], uh[1], uh[2], uh[3], uh[4]);
     const int grp = a.face_group[f];
     if (grp >= 0 && grp < a.n_groups && a.bcs[grp].kind != kBcNone) {
       const BcDev &bc = a.bcs[grp];
