@@ -70,7 +70,7 @@ __device__ __forceinline__ void add_gradient(const Real *t, Real gx, Real gy, Re
   rt(2) += gy;
   rt(3) += gz;
   if constexpr (M >= 10) {
-    const double x = t[1], y = t[2], z = t[3];
+    const Real x = t[1], y = t[2], z = t[3];
     rt(4) += gx * (2 * x);
     rt(5) += gx * y + gy * x;
     rt(6) += gx * z + gz * x;
@@ -79,7 +79,7 @@ __device__ __forceinline__ void add_gradient(const Real *t, Real gx, Real gy, Re
     rt(9) += gz * (2 * z);
   }
   if constexpr (M >= 20) {
-    const double xx = t[4], xy = t[5], xz = t[6], yy = t[7], yz = t[8], zz = t[9];
+    const Real xx = t[4], xy = t[5], xz = t[6], yy = t[7], yz = t[8], zz = t[9];
     rt(10) += gx * (3 * xx);
     rt(11) += gx * (2 * xy) + gy * xx;
     rt(12) += gx * (2 * xz) + gz * xx;
