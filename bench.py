@@ -568,7 +568,7 @@ def ensemble_mesh(spec):
     return make((spec["n"],) * 3, periodic=(True,) * 3)
 
 
-def build_ensemble(specs, device=0):
+def build_ensemble(specs, device=0, precision="fp64"):
     """Group the cases by (scheme, p); one handle per group with its cases."""
     from pvcriemannsolvers_gb300 import General, Lobatto, mesh as meshlib
     groups = {}
@@ -578,8 +578,8 @@ def build_ensemble(specs, device=0):
     for (scheme, p), sps in sorted(groups.items()):
         meshes = [ensemble_mesh(sp) for sp in sps]
         m = meshlib.concat(*meshes)
-        sysm = General(m, p, "rusanov", device=device) if scheme == "modal" else \
-            Lobatto(m, p, "rusanov", device=device)
+        sysm = General(m, p, "rusanov", device=device, precision=precision) if scheme == "modal" else \
+            Lobatto(m, p, "rusanov", device=device, precision=precision)
         if scheme == "modal":
             # volume points come cell by cell; a case's cells are one type
             pts = sysm.points()
@@ -631,14 +631,10 @@ def ensemble_cpu_sample(specs, seconds=12.0, threads=None):
                       f"oracle (plain C restatement, OpenMP)"}
 
 
-def run_ensemble(args, rank, world, local_rank):
-    import torch
-    from pvcriemannsolvers_gb300 import Ensemble, build
-    build.build()
-    torch.cuda.set_device(local_rank)
-    dev = torch.device("cuda", local_rank)
-    specs = ensemble_spec(scale=args.ensemble_scale)
-    members = build_ensemble(specs, device=local_rank)
+def ensemble_form(args, torch, dev, local_rank, specs, precision):
+    """Time one precision form of the ensemble: device-resident steps, e2e."""
+    from pvcriemannsolvers_gb300 import Ensemble
+    members = build_ensemble(specs, device=local_rank, precision=precision)
     for mb in members:
         mb["system"].autotune()
     ens = Ensemble([mb["system"] for mb in members])
@@ -657,13 +653,14 @@ def run_ensemble(args, rank, world, local_rank):
         e1.synchronize()
     ms = e0.elapsed_time(e1)
     launches = sum(mb["system"].launch_count() for mb in members) - launches0
+    solution = [mb["system"].GetSolutionColumn() for mb in members]
     # end to end: every member's column from / to pinned host memory each step
     hosts = []
-    for mb in members:
+    for mb, sol in zip(members, solution):
         n = mb["dofs"]
         hin = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
         hout = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
-        hin[:] = mb["system"].GetSolutionColumn()
+        hin[:] = sol
         hosts.append((hin, hout))
     e2e_steps = max(1, min(args.steps, 10))
     torch.cuda.synchronize(dev)
@@ -686,30 +683,54 @@ def run_ensemble(args, rank, world, local_rank):
     ens.close()
     for mb in members:
         mb["system"].close()
+    return {"value": 3 * L * args.steps / (ms * 1e-3), "ms_per_step": ms / args.steps,
+            "e2e": 3 * L * e2e_steps / e2e_s, "e2e_steps": e2e_steps, "launches": launches,
+            "clocks": clocks.summary(), "members": per_member, "solution": solution, "L": L}
+
+
+def run_ensemble(args, rank, world, local_rank):
+    import torch
+    from pvcriemannsolvers_gb300 import build
+    build.build()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    specs = ensemble_spec(scale=args.ensemble_scale)
+    res = {f: ensemble_form(args, torch, dev, local_rank, specs, f) for f in ("fp64", "mixed")}
+    r, pf = res["mixed"], res["fp64"]
+    L = r["L"]
+    # density of every member: nodal values (DGSEM) or the coefficients on the
+    # orthonormal basis (modal), whose L2 is the field's L2
+    a = np.concatenate([s.reshape(-1, K)[:, 0] for s in r["solution"]])
+    b = np.concatenate([s.reshape(-1, K)[:, 0] for s in pf["solution"]])
     fp64_peak = fp64_peak_tflops(torch, dev)
     hbm_peak, peak_src = measured_peaks()
-    dom = max(per_member, key=lambda r: r["kernel_ms"]["rk3_step"])
+    dom = max(pf["members"], key=lambda m: m["kernel_ms"]["rk3_step"])
     cpu = None
     if not args.no_cpu:
         cpu = ensemble_cpu_sample(specs)
     line = {
-        "metric": METRIC, "value": 3 * L * args.steps / (ms * 1e-3), "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
         "config": {"workload": f"ensemble of {len(specs)} periodic unit-cube cases (seed 1), counts log-uniform "
                                f"in [4k, 200k] x {args.ensemble_scale}, Hex8 DGSEM / Hex8 modal / Tet4 modal, "
                                f"p in 1..3, Rusanov, SSP-RK3, own dt per case",
-                   "cases": len(specs), "cells": sum(mb["cells"] for mb in members), "dofs": L,
-                   "handles": len(members), "form": "plain FP64",
+                   "cases": len(specs), "cells": sum(m["cells"] for m in r["members"]), "dofs": L,
+                   "handles": len(r["members"]),
+                   "form": "mixed (FP32 contractions; FP64 Riemann fluxes and RK)",
                    "step": "one CUDA graph per step: every handle's dt reduction + 3 RK stages",
                    "l2_flush": f"inputs larger than L2 (all columns {8 * L / 1e9:.2f} GB)"},
-        "clocks": clocks.summary(),
-        "e2e": {"value": 3 * L * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * L,
-                "d2h_bytes_per_step": 8 * L, "steps": e2e_steps,
+        "accuracy": {"mixed_vs_fp64_density_rel_l2": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
+                     "finite": bool(np.isfinite(a).all())},
+        "clocks": r["clocks"],
+        "e2e": {"value": r["e2e"], "unit": UNIT, "h2d_bytes_per_step": 8 * L,
+                "d2h_bytes_per_step": 8 * L, "steps": r["e2e_steps"],
                 "path": "mcfd_set_solution per handle + mcfd_ensemble_advance(1) + mcfd_get_solution per handle"},
-        "gpu_launches": launches,
-        "members": per_member,
-        "roofline": {"bound": "fp64", "kernel": f"step of the {dom['scheme']} p={dom['p']} handle",
+        "gpu_launches": r["launches"],
+        "members": r["members"],
+        "plain_fp64": {"value": pf["value"], "ms_per_step": pf["ms_per_step"], "e2e": pf["e2e"],
+                       "launches": pf["launches"], "clocks": pf["clocks"], "members": pf["members"]},
+        "roofline": {"bound": "fp64", "kernel": f"step of the {dom['scheme']} p={dom['p']} handle (FP64 form)",
                      "achieved": None, "peak": fp64_peak, "unit": "TFLOP/s", "frac": None,
                      "traffic": None, "peak_source": "measured in this run: cuBLAS DGEMM 4096^3",
                      "hbm_peak": hbm_peak, "hbm_peak_source": peak_src,
