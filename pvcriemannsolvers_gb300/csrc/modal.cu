@@ -168,6 +168,10 @@ __global__ void __launch_bounds__(512) modal_face_kernel(ModalFaceArgs a) {
     bool done = false;
     if constexpr (R == kHllc) done = flux_hllc_cons<false>(uh, us, n, out);
     if constexpr (R == kRoe) done = flux_roe_cons_weighted<false>(uh, us, n, 1.0, out);
+    if constexpr (R == kRusanov) {
+      flux_rusanov_cons_weighted<false>(uh, us, n, 1.0, out);
+      done = true;
+    }
     if (!done) {
       Prim l = cons_to_prim(uh[0], uh[1], uh[2], uh[3], uh[4]);
       Prim r = cons_to_prim(us[0], us[1], us[2], us[3], us[4]);
@@ -519,6 +523,10 @@ __global__ void __launch_bounds__(512) modal_face32_kernel(ModalFace32Args a) {
     bool done = false;
     if constexpr (R == kHllc) done = flux_hllc_cons<true>(uh, us, n, out);
     if constexpr (R == kRoe) done = flux_roe_cons_weighted<true>(uh, us, n, 1.0, out);
+    if constexpr (R == kRusanov) {
+      flux_rusanov_cons_weighted<true>(uh, us, n, 1.0, out);
+      done = true;
+    }
     if (!done) {
       Prim l = cons_to_prim(uh[0], uh[1], uh[2], uh[3], uh[4]);
       Prim r = cons_to_prim(us[0], us[1], us[2], us[3], us[4]);
