@@ -173,7 +173,7 @@ void release(mcfd_handle *h) {
   for (void *p : ptrs)
     if (p) cudaFree(p);
   auto &l = h->lim;
-  void *lptrs[] = {l.psi, l.mn, l.proj, l.beta, l.eval, l.s00, l.divisor, l.adj,
+  void *lptrs[] = {l.psi, l.mn, l.mn32, l.proj, l.beta, l.eval, l.s00, l.divisor, l.adj,
                    l.frame, l.volume, l.modal, l.list, l.list_count, l.troubled};
   for (void *p : lptrs)
     if (p) cudaFree(p);
@@ -764,6 +764,11 @@ int build_limiter(mcfd_handle *h, const mcfd_mesh_desc *d, int kind, double w0,
   int rc;
   if ((rc = upload(h, &l.psi, psi))) return rc;
   if ((rc = upload(h, &l.mn, mn))) return rc;
+  if (h->opt.precision == MCFD_MIXED) {  // the mixed form's nodal -> modal map in FP32
+    std::vector<float> mn32(mn.size());
+    for (size_t i = 0; i < mn.size(); ++i) mn32[i] = (float)mn[i];
+    if ((rc = upload(h, &l.mn32, mn32))) return rc;
+  }
   if ((rc = upload(h, &l.proj, proj))) return rc;
   if ((rc = upload(h, &l.beta, beta))) return rc;
   if ((rc = upload(h, &l.eval, eval))) return rc;

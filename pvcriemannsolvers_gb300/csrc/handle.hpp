@@ -83,6 +83,7 @@ struct Limiter {
   double w0 = 0.001, eps = 1e-6;
   double *psi = nullptr;     // [cells][N][M] orthonormal basis at the cell's nodes
   double *mn = nullptr;      // [cells][N][M] w_n psi_m(x_n) (modal_to_nodal)
+  float *mn32 = nullptr;     // FP32 copy of mn (mixed form)
   double *proj = nullptr;    // [cells][6][M][M] neighbour -> own basis projection
   double *beta = nullptr;    // [cells][M][M] smoothness quadratic form
   double *eval = nullptr;    // [cells][7][M] basis values at this cell's centre:

@@ -77,6 +77,47 @@ weno_modal_kernel(const double *__restrict__ u, const double *__restrict__ mn,
   for (int k = 0; k < kK; ++k) modal[(c * kK + k) * M + m] = s[k];
 }
 
+// Mixed form: the same product in FP32.  A block holds CB cells: their
+// nodal states are converted to FP32 once into shared memory (integer-pipe
+// conversions), then one thread per (cell, mode) accumulates with FP32 FMAs
+// over the FP32 copy of the table; the modal coefficients are stored in FP64
+// for the FP64 smoothness indicators and reconstruction.
+template <int N, int M>
+struct Modal32Cfg {
+  static constexpr int kCells = M >= 20 ? 16 : 32;
+  static constexpr int kThreads = kCells * M;
+};
+
+template <int N, int M>
+__global__ void __launch_bounds__(Modal32Cfg<N, M>::kThreads)
+weno_modal32_kernel(const double *__restrict__ u, const float *__restrict__ mn32,
+                    double *__restrict__ modal, int64_t n_cells) {
+  constexpr int CB = Modal32Cfg<N, M>::kCells, NT = Modal32Cfg<N, M>::kThreads;
+  __shared__ float s_u[CB][N * kK];
+  const int64_t c0 = (int64_t)blockIdx.x * CB;
+  const int t = threadIdx.x;
+  const int64_t avail = n_cells - c0;
+  const int nc = avail < CB ? (int)avail : CB;
+  for (int i = t; i < nc * N * kK; i += NT) {
+    const int cl = i / (N * kK), r = i - cl * (N * kK);
+    s_u[cl][r] = f64_to_f32(u[(c0 + cl) * N * kK + r]);
+  }
+  __syncthreads();
+  const int cl = t / M, m = t - cl * M;
+  if (cl >= nc) return;
+  const int64_t c = c0 + cl;
+  const float *mc = mn32 + c * N * M;
+  float s[kK] = {0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll 4
+  for (int q = 0; q < N; ++q) {
+    const float w = mc[q * M + m];
+#pragma unroll
+    for (int k = 0; k < kK; ++k) s[k] = fmaf(s_u[cl][q * kK + k], w, s[k]);
+  }
+#pragma unroll
+  for (int k = 0; k < kK; ++k) modal[(c * kK + k) * M + m] = f32_to_f64(s[k]);
+}
+
 // One entry of L or R of EigenMatrices (riemann/euler/eigen.hpp:27-56) for
 // the conservative state of primitive w in the frame {nu, mu, pi}:
 // e < 25 is L[e / 5][e % 5], otherwise R[(e - 25) / 5][(e - 25) % 5].
@@ -420,8 +461,14 @@ int limiter_dispatch(mcfd_handle *h, double *u) {
   const Mesh &mesh = h->mesh;
   Limiter &l = h->lim;
   int64_t total = mesh.n_cells * M;
-  weno_modal_kernel<N, M><<<(unsigned)((total + 255) / 256), 256, 0, h->stream>>>(
-      u, l.mn, l.modal, mesh.n_cells);
+  if (l.mn32) {
+    constexpr int CB = Modal32Cfg<N, M>::kCells;
+    weno_modal32_kernel<N, M><<<(unsigned)((mesh.n_cells + CB - 1) / CB), Modal32Cfg<N, M>::kThreads, 0,
+                                h->stream>>>(u, l.mn32, l.modal, mesh.n_cells);
+  } else {
+    weno_modal_kernel<N, M><<<(unsigned)((total + 255) / 256), 256, 0, h->stream>>>(
+        u, l.mn, l.modal, mesh.n_cells);
+  }
   WenoArgs wa{u, l.modal, l.psi, l.proj, l.beta, l.eval, l.s00, l.divisor, l.adj,
               l.frame, l.volume, l.troubled, mesh.n_cells, l.w0, l.eps, (Q - 1) < 3 ? 1.0 : 3.0};
   // persistent grid: limiter_blocks_per_sm blocks of 64 threads per SM

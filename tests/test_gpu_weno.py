@@ -123,3 +123,26 @@ def test_limited_fr_rk3_parity(gpu):
     err = rel_l2(s.GetSolutionColumn(), u)
     assert err <= RTOL, err
     s.close()
+
+
+@pytest.mark.parametrize("mode", ["eigen", "detect_lazy"])
+def test_mixed_form_limiter_close_to_fp64(gpu, mode):
+    """The mixed form's limiter (FP32 nodal-to-modal products, FP64 smoothness
+    and reconstruction) tracks the FP64 form on the Sod tube: same troubled
+    cells, density within 1e-6 after 10 steps."""
+    p = 2
+    m = cases.sod_mesh(40, 2, 2)
+    x = meshlib.node_coordinates(m, p).reshape(-1, 3)
+    u0 = cases.sod_ic(x).ravel()
+    out = {}
+    for precision in ("fp64", "mixed"):
+        s = Lobatto(m, p, "roe", cfl=0.1, limiter=mode, precision=precision)
+        cases.sod_bc(s)
+        s.SetSolutionColumn(u0)
+        s.troubled_cells()
+        s.advance(10, 1.0, 3, 0.0)
+        out[precision] = (s.GetSolutionColumn(), s.troubled_cells())
+        s.close()
+    a, b = out["mixed"][0].reshape(-1, 5)[:, 0], out["fp64"][0].reshape(-1, 5)[:, 0]
+    assert rel_l2(a, b) <= 1e-6
+    assert abs(out["mixed"][1] - out["fp64"][1]) <= 0.02 * out["fp64"][1] + 2
