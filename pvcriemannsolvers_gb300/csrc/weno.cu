@@ -77,11 +77,14 @@ weno_modal_kernel(const double *__restrict__ u, const double *__restrict__ mn,
   for (int k = 0; k < kK; ++k) modal[(c * kK + k) * M + m] = s[k];
 }
 
-// Mixed form: the same product in FP32.  A block holds CB cells: their
-// nodal states are converted to FP32 once into shared memory (integer-pipe
-// conversions), then one thread per (cell, mode) accumulates with FP32 FMAs
-// over the FP32 copy of the table; the modal coefficients are stored in FP64
-// for the FP64 smoothness indicators and reconstruction.
+// Mixed form: the momenta's product in FP32, density and energy in FP64.
+// The jump detector reads only density and energy, so its decisions are the
+// FP64 form's; the momenta enter only the reconstruction of troubled cells.
+// A block holds CB cells: their nodal momenta are converted to FP32 once into
+// shared memory (integer-pipe conversions), then one thread per (cell, mode)
+// accumulates them with FP32 FMAs over the FP32 copy of the table, and
+// density and energy with FP64 FMAs over the FP64 table; all coefficients
+// are stored in FP64.
 template <int N, int M>
 struct Modal32Cfg {
   static constexpr int kCells = M >= 20 ? 16 : 32;
@@ -90,32 +93,40 @@ struct Modal32Cfg {
 
 template <int N, int M>
 __global__ void __launch_bounds__(Modal32Cfg<N, M>::kThreads)
-weno_modal32_kernel(const double *__restrict__ u, const float *__restrict__ mn32,
-                    double *__restrict__ modal, int64_t n_cells) {
+weno_modal32_kernel(const double *__restrict__ u, const double *__restrict__ mn,
+                    const float *__restrict__ mn32, double *__restrict__ modal, int64_t n_cells) {
   constexpr int CB = Modal32Cfg<N, M>::kCells, NT = Modal32Cfg<N, M>::kThreads;
-  __shared__ float s_u[CB][N * kK];
+  __shared__ float s_m[CB][N * 3];  // momenta, FP32
   const int64_t c0 = (int64_t)blockIdx.x * CB;
   const int t = threadIdx.x;
   const int64_t avail = n_cells - c0;
   const int nc = avail < CB ? (int)avail : CB;
-  for (int i = t; i < nc * N * kK; i += NT) {
-    const int cl = i / (N * kK), r = i - cl * (N * kK);
-    s_u[cl][r] = f64_to_f32(u[(c0 + cl) * N * kK + r]);
+  for (int i = t; i < nc * N * 3; i += NT) {
+    const int cl = i / (N * 3), r = i - cl * (N * 3), q = r / 3, d = r - q * 3;
+    s_m[cl][r] = f64_to_f32(u[((c0 + cl) * N + q) * kK + 1 + d]);
   }
   __syncthreads();
   const int cl = t / M, m = t - cl * M;
   if (cl >= nc) return;
   const int64_t c = c0 + cl;
-  const float *mc = mn32 + c * N * M;
-  float s[kK] = {0.f, 0.f, 0.f, 0.f, 0.f};
-#pragma unroll 4
+  const float *mc32 = mn32 + c * N * M;
+  const double *mc = mn + c * N * M;
+  const double *uc = u + c * kK * N;
+  float s[3] = {0.f, 0.f, 0.f};
+  double rho = 0, e = 0;
+#pragma unroll 3
   for (int q = 0; q < N; ++q) {
-    const float w = mc[q * M + m];
+    const float w = mc32[q * M + m];
 #pragma unroll
-    for (int k = 0; k < kK; ++k) s[k] = fmaf(s_u[cl][q * kK + k], w, s[k]);
+    for (int d = 0; d < 3; ++d) s[d] = fmaf(s_m[cl][q * 3 + d], w, s[d]);
+    const double wd = mc[q * M + m];
+    rho += uc[q * kK] * wd;
+    e += uc[q * kK + 4] * wd;
   }
+  modal[(c * kK + 0) * M + m] = rho;
 #pragma unroll
-  for (int k = 0; k < kK; ++k) modal[(c * kK + k) * M + m] = f32_to_f64(s[k]);
+  for (int d = 0; d < 3; ++d) modal[(c * kK + 1 + d) * M + m] = f32_to_f64(s[d]);
+  modal[(c * kK + 4) * M + m] = e;
 }
 
 // One entry of L or R of EigenMatrices (riemann/euler/eigen.hpp:27-56) for
@@ -464,7 +475,7 @@ int limiter_dispatch(mcfd_handle *h, double *u) {
   if (l.mn32) {
     constexpr int CB = Modal32Cfg<N, M>::kCells;
     weno_modal32_kernel<N, M><<<(unsigned)((mesh.n_cells + CB - 1) / CB), Modal32Cfg<N, M>::kThreads, 0,
-                                h->stream>>>(u, l.mn32, l.modal, mesh.n_cells);
+                                h->stream>>>(u, l.mn, l.mn32, l.modal, mesh.n_cells);
   } else {
     weno_modal_kernel<N, M><<<(unsigned)((total + 255) / 256), 256, 0, h->stream>>>(
         u, l.mn, l.modal, mesh.n_cells);

@@ -127,9 +127,10 @@ def test_limited_fr_rk3_parity(gpu):
 
 @pytest.mark.parametrize("mode", ["eigen", "detect_lazy"])
 def test_mixed_form_limiter_close_to_fp64(gpu, mode):
-    """The mixed form's limiter (FP32 nodal-to-modal products, FP64 smoothness
-    and reconstruction) tracks the FP64 form on the Sod tube: same troubled
-    cells, density within 1e-6 after 10 steps."""
+    """The mixed form's limiter (FP32 nodal-to-modal products of the momenta;
+    density, energy, smoothness and reconstruction in FP64) tracks the FP64
+    form on the Sod tube: about the same troubled cells, density within 1e-6
+    after 10 steps."""
     p = 2
     m = cases.sod_mesh(40, 2, 2)
     x = meshlib.node_coordinates(m, p).reshape(-1, 3)
