@@ -303,6 +303,18 @@ int mcfd_build_faces(int64_t n_nodes, const double *xyz, int64_t n_cells,
                      int64_t cap, int64_t *face_cells, int32_t *face_sides,
                      int32_t *face_group, double *face_shift, int64_t *n_faces);
 const char *mcfd_build_error(void);
+/* The same faces, index for index, with the keying and pairing of the face
+ * slots on GPU `device` (hash table + prefix sums); the free slots (O(n^(2/3)))
+ * are grouped and ordered on the host as above.  Needs n_nodes < 2^32;
+ * MCFD_ERR_CUDA for device errors. */
+int mcfd_build_faces_gpu(int32_t device, int64_t n_nodes, const double *xyz,
+                         int64_t n_cells, const int64_t *cell_nodes,
+                         const int32_t *cell_type, int32_t cell_node_stride,
+                         int64_t n_bfaces, const int64_t *bface_nodes,
+                         const int32_t *bface_group, int32_t n_periodic,
+                         const int32_t *periodic_groups, const double *periodic_shift,
+                         int64_t cap, int64_t *face_cells, int32_t *face_sides,
+                         int32_t *face_group, double *face_shift, int64_t *n_faces);
 /* Legacy VTK unstructured grid reader (ASCII or BINARY; CELLS in the classic
  * or the version-5 OFFSETS / CONNECTIVITY layout): hexahedra (12) and
  * tetrahedra (10) become cells in mcfd_mesh_desc form (VTK and CGNS share

@@ -98,6 +98,11 @@ SIGNATURES = {
                                    C.POINTER(C.c_int32), _D, C.c_int64, C.POINTER(C.c_int64),
                                    C.POINTER(C.c_int32), C.POINTER(C.c_int32), _D, C.POINTER(C.c_int64)]),
     "mcfd_build_error": (C.c_char_p, []),
+    "mcfd_build_faces_gpu": (C.c_int, [C.c_int32, C.c_int64, _D, C.c_int64, C.POINTER(C.c_int64),
+                                       C.POINTER(C.c_int32), C.c_int32, C.c_int64, C.POINTER(C.c_int64),
+                                       C.POINTER(C.c_int32), C.c_int32, C.POINTER(C.c_int32), _D, C.c_int64,
+                                       C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int32), _D,
+                                       C.POINTER(C.c_int64)]),
     "mcfd_vtk_read": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(C.c_void_p)]),
     "mcfd_vtk_mesh_sizes": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                       C.POINTER(C.c_int64)]),

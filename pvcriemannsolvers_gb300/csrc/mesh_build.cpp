@@ -22,6 +22,7 @@
 //                      coalesce.  It takes the place of the reference's METIS
 //                      renumbering (mesh/shuffler.hpp) on one GPU.
 #include <algorithm>
+#include <climits>
 #include <array>
 #include <cmath>
 #include <cstdint>
@@ -32,6 +33,7 @@
 #include <vector>
 
 #include "../../include/mcfd.h"
+#include "mesh_build_gpu.hpp"
 
 namespace {
 
@@ -119,6 +121,13 @@ uint64_t hilbert_key(uint32_t x, uint32_t y, uint32_t z, int b) {
   return key;
 }
 
+int finish_faces(int64_t n_nodes, const double *xyz, const int64_t *cell_nodes, int64_t stride,
+                 const int32_t *cell_type, int64_t n_bfaces, const int64_t *bface_nodes,
+                 const int32_t *bface_group, int32_t n_periodic, const int32_t *periodic_groups,
+                 const double *periodic_shift, std::vector<OutFace> &inner, const std::vector<Slot> &lone,
+                 int64_t *face_cells, int32_t *face_sides, int32_t *face_group, double *face_shift,
+                 int64_t *n_faces);
+
 }  // namespace
 
 extern "C" {
@@ -189,6 +198,27 @@ int mcfd_build_faces(int64_t n_nodes, const double *xyz, int64_t n_cells,
     }
     i = j;
   }
+  std::vector<Slot> lone_slots;
+  lone_slots.reserve(lone.size());
+  for (int64_t i : lone) lone_slots.push_back(slots[i]);
+  return finish_faces(n_nodes, xyz, cell_nodes, stride, cell_type, n_bfaces, bface_nodes, bface_group,
+                      n_periodic, periodic_groups, periodic_shift, inner, lone_slots, face_cells,
+                      face_sides, face_group, face_shift, n_faces);
+}
+
+}  // extern "C"
+
+namespace {
+
+// Boundary groups, periodic pairs, order and output of the faces, given the
+// interior pairs and the free slots (sorted by key): shared by the host and
+// the GPU builder.
+int finish_faces(int64_t n_nodes, const double *xyz, const int64_t *cell_nodes, int64_t stride,
+                 const int32_t *cell_type, int64_t n_bfaces, const int64_t *bface_nodes,
+                 const int32_t *bface_group, int32_t n_periodic, const int32_t *periodic_groups,
+                 const double *periodic_shift, std::vector<OutFace> &inner, const std::vector<Slot> &lone,
+                 int64_t *face_cells, int32_t *face_sides, int32_t *face_group, double *face_shift,
+                 int64_t *n_faces) {
   // boundary elements -> groups of the lone slots
   std::vector<int32_t> lone_group(lone.size(), -1);
   for (int64_t f = 0; f < n_bfaces; ++f) {
@@ -198,15 +228,15 @@ int mcfd_build_faces(int64_t n_nodes, const double *xyz, int64_t n_cells,
         return build_fail("boundary face " + std::to_string(f) + ": node index out of range");
     const Key k = make_key(bface_nodes + f * 4, n);
     auto it = std::lower_bound(lone.begin(), lone.end(), k,
-                               [&](int64_t i, const Key &key) { return slots[i].key < key; });
-    if (it == lone.end() || slots[*it].key != k)
+                               [&](const Slot &sl, const Key &key) { return sl.key < key; });
+    if (it == lone.end() || it->key != k)
       return build_fail("boundary face " + std::to_string(f) + " is not a free face of any cell");
     lone_group[it - lone.begin()] = bface_group[f];
   }
   // periodic pairs: group a faces matched with group b faces translated by the shift
   std::vector<char> used(lone.size(), 0);
   auto centroid = [&](int64_t li, double *x) {
-    const Slot &s = slots[lone[li]];
+    const Slot &s = lone[li];
     int64_t ids[4];
     const int n = face_node_ids(cell_nodes, stride, cell_type, s.cell, s.side, ids);
     x[0] = x[1] = x[2] = 0;
@@ -267,7 +297,7 @@ int mcfd_build_faces(int64_t n_nodes, const double *xyz, int64_t n_cells,
         return build_fail("periodic group " + std::to_string(gb) + ": a face has no partner in group " +
                           std::to_string(ga));
       taken[match] = 1;
-      const Slot &sa = slots[lone[fa[match]]], &sb = slots[lone[fb[j]]];
+      const Slot &sa = lone[fa[match]], &sb = lone[fb[j]];
       used[fa[match]] = used[fb[j]] = 1;
       // x(sharer) + shift = x(holder); the holder is the lower cell id
       OutFace f;
@@ -288,7 +318,7 @@ int mcfd_build_faces(int64_t n_nodes, const double *xyz, int64_t n_cells,
   std::vector<OutFace> bnd;
   for (size_t i = 0; i < lone.size(); ++i) {
     if (used[i]) continue;
-    const Slot &s = slots[lone[i]];
+    const Slot &s = lone[i];
     bnd.push_back({s.cell, -1, s.side, -1, lone_group[i], {0, 0, 0}});
   }
   std::sort(bnd.begin(), bnd.end(), [](const OutFace &a, const OutFace &b) {
@@ -309,6 +339,76 @@ int mcfd_build_faces(int64_t n_nodes, const double *xyz, int64_t n_cells,
     }
   *n_faces = n;
   return MCFD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mcfd_build_faces_gpu(int32_t device, int64_t n_nodes, const double *xyz, int64_t n_cells,
+                         const int64_t *cell_nodes, const int32_t *cell_type,
+                         int32_t cell_node_stride, int64_t n_bfaces, const int64_t *bface_nodes,
+                         const int32_t *bface_group, int32_t n_periodic,
+                         const int32_t *periodic_groups, const double *periodic_shift, int64_t cap,
+                         int64_t *face_cells, int32_t *face_sides, int32_t *face_group,
+                         double *face_shift, int64_t *n_faces) {
+  g_build_error.clear();
+  const int64_t stride = cell_node_stride > 0 ? cell_node_stride : 8;
+  if (n_nodes <= 0 || !xyz || n_cells <= 0 || !cell_nodes || n_bfaces < 0 ||
+      (n_bfaces > 0 && (!bface_nodes || !bface_group)) || n_periodic < 0 ||
+      (n_periodic > 0 && (!periodic_groups || !periodic_shift)) || !face_cells || !face_sides ||
+      !face_group || !face_shift || !n_faces) {
+    g_build_error = "null or negative argument";
+    return MCFD_ERR_ARGUMENT;
+  }
+  if (n_nodes >= (int64_t)UINT32_MAX) {
+    g_build_error = "the GPU builder keys faces by 32-bit node ids";
+    return MCFD_ERR_UNSUPPORTED;
+  }
+  std::vector<int64_t> slot_off(n_cells + 1, 0);
+  for (int64_t c = 0; c < n_cells; ++c) {
+    const int nv = type_nodes(cell_type ? cell_type[c] : MCFD_HEX8);
+    if (nv == 0) return build_fail("cell " + std::to_string(c) + ": unknown cell type");
+    if (nv > stride) return build_fail("cell " + std::to_string(c) + ": more nodes than cell_node_stride");
+    for (int v = 0; v < nv; ++v) {
+      const int64_t id = cell_nodes[c * stride + v];
+      if (id < 0 || id >= n_nodes) return build_fail("cell " + std::to_string(c) + ": node index out of range");
+    }
+    slot_off[c + 1] = slot_off[c] + (tet_type(cell_type, c) ? 4 : 6);
+  }
+  if (cap < slot_off.back()) {
+    g_build_error = "output capacity below the face slot count (mcfd_face_slot_count)";
+    return MCFD_ERR_ARGUMENT;
+  }
+  if (slot_off.back() >= (int64_t)UINT32_MAX) {
+    g_build_error = "more than 2^32 face slots";
+    return MCFD_ERR_UNSUPPORTED;
+  }
+  mcfd::GpuPairs pr;
+  std::string err;
+  const int rc = mcfd::gpu_pair_slots(device, cell_nodes, stride, cell_type, n_cells, slot_off, &pr, &err);
+  if (rc == 2) return build_fail(err);
+  if (rc) {
+    g_build_error = err;
+    return MCFD_ERR_CUDA;
+  }
+  const int64_t n_inner = (int64_t)pr.inner_sides.size() / 2;
+  std::vector<OutFace> inner(n_inner);
+  for (int64_t f = 0; f < n_inner; ++f)
+    inner[f] = {pr.inner_cells[2 * f], pr.inner_cells[2 * f + 1], pr.inner_sides[2 * f],
+                pr.inner_sides[2 * f + 1], -1, {0, 0, 0}};
+  std::vector<Slot> lone(pr.lone_cells.size());
+  for (size_t i = 0; i < lone.size(); ++i) {
+    int64_t ids[4];
+    const int n = face_node_ids(cell_nodes, stride, cell_type, pr.lone_cells[i], pr.lone_sides[i], ids);
+    lone[i] = {make_key(ids, n), pr.lone_cells[i], pr.lone_sides[i]};
+  }
+  std::sort(lone.begin(), lone.end(), [](const Slot &a, const Slot &b) {
+    return a.key != b.key ? a.key < b.key : (a.cell != b.cell ? a.cell < b.cell : a.side < b.side);
+  });
+  return finish_faces(n_nodes, xyz, cell_nodes, stride, cell_type, n_bfaces, bface_nodes, bface_group,
+                      n_periodic, periodic_groups, periodic_shift, inner, lone, face_cells, face_sides,
+                      face_group, face_shift, n_faces);
 }
 
 int mcfd_hilbert_order(int64_t n, const double *points, int64_t *order) {

@@ -437,12 +437,13 @@ def concat(*meshes: Mesh) -> Mesh:
 # and the Hilbert cell order (mcfd_hilbert_order).
 
 def build(xyz, cell_nodes, cell_type=None, bface_nodes=None, bface_group=None,
-          periodic=()) -> Mesh:
+          periodic=(), device: int | None = None) -> Mesh:
     """Mesh with faces built from the cells alone (Part::BuildLocalFaces /
-    BuildBoundaryFaces).  cell_nodes [cells, 8] (Tet4: first 4, rest -1);
+    BuildBoundaryFaces).  cell_nodes [cells, stride] (CGNS order);
     bface_nodes [n, 4] boundary elements (triangles end in -1) with groups
     bface_group; periodic: ((group_a, group_b, shift), ...) with
-    x(face of b) + shift = x(face of a)."""
+    x(face of b) + shift = x(face of a).  device: pair the face slots on that
+    GPU (mcfd_build_faces_gpu; the same faces)."""
     import ctypes as C
     from . import capi
     lib = capi.load()
@@ -461,7 +462,9 @@ def build(xyz, cell_nodes, cell_type=None, bface_nodes=None, bface_group=None,
     fg = np.empty(cap, np.int32)
     fsh = np.empty((cap, 3), np.float64)
     n = C.c_int64()
-    rc = lib.mcfd_build_faces(xyz.shape[0], xyz.ctypes.data_as(PD), cn.shape[0], cn.ctypes.data_as(P64), ct_p,
+    fn = lib.mcfd_build_faces if device is None else \
+        (lambda *a: lib.mcfd_build_faces_gpu(int(device), *a))
+    rc = fn(xyz.shape[0], xyz.ctypes.data_as(PD), cn.shape[0], cn.ctypes.data_as(P64), ct_p,
                               cn.shape[1], bf.shape[0], bf.ctypes.data_as(P64), bg.ctypes.data_as(P32), pg.shape[0],
                               pg.ctypes.data_as(P32), ps.ctypes.data_as(PD), cap, fc.ctypes.data_as(P64),
                               fs.ctypes.data_as(P32), fg.ctypes.data_as(P32), fsh.ctypes.data_as(PD),
