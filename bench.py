@@ -1055,6 +1055,23 @@ def run_reorder(args, rank, world, local_rank):
         sysm.close()
     ref = sols["lexicographic"]
     agree = {k: float(np.linalg.norm(v - ref) / np.linalg.norm(ref)) for k, v in sols.items()}
+    # mesh ingest: the faces of the same mesh from its cells and boundary
+    # elements, host builder against GPU builder (the same faces)
+    open_mesh = meshlib.box((args.cells,) * 3, lengths=(10.0,) * 3)
+    bn, bg = meshlib.boundary_elements(open_mesh)
+    spec = [(2 * ax, 2 * ax + 1, tuple(-10.0 if e == ax else 0.0 for e in range(3))) for ax in range(3)]
+    ingest = {}
+    built = {}
+    for name, device in (("host", None), ("gpu", local_rank)):
+        times = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            built[name] = meshlib.build(open_mesh.xyz, open_mesh.cell_nodes, None, bn, bg, spec, device=device)
+            times.append(time.perf_counter() - t0)
+        ingest[name + "_s"] = sorted(times)[1]
+    ingest["same_faces"] = bool(all(np.array_equal(getattr(built["host"], f), getattr(built["gpu"], f))
+                                    for f in ("face_cells", "face_sides", "face_group", "face_shift")))
+    ingest["faces"] = built["gpu"].n_faces
     r = res["hilbert_of_random"]
     line = {
         "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -1063,7 +1080,7 @@ def run_reorder(args, rank, world, local_rank):
         "config": {"workload": f"vortex {args.cells}^3 Hex8 DGSEM p={DEGREE} mixed, cells renumbered",
                    "numbering": "Hilbert order (mcfd_hilbert_order) of a random renumbering",
                    "l2_flush": f"inputs larger than L2 ({8 * L / 1e9:.2f} GB)"},
-        "clocks": r["clocks"], "hilbert_order_s": order_s,
+        "clocks": r["clocks"], "hilbert_order_s": order_s, "face_builder": ingest,
         "variants": res, "solution_rel_l2_vs_lexicographic": agree,
     }
     if rank == 0:
