@@ -220,6 +220,18 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def max_over_ranks(torch, dist, dev, x: float) -> float:
+    """The maximum of a per-rank time over all ranks (the job's time)."""
+    tt = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def whole_job_rate(units_per_rank: float, world: int, seconds: float) -> float:
+    """value = the units all ranks processed / the max-over-ranks time."""
+    return units_per_rank * world / seconds
+
+
 def e2e_runs(torch, dev, sysm, sol, t, steps, dt_guess, dist=None):
     """End-to-end stepping through the C ABI from / to pinned host memory.
 
@@ -258,9 +270,7 @@ def e2e_runs(torch, dev, sysm, sol, t, steps, dt_guess, dist=None):
         torch.cuda.synchronize(dev)
         el = time.perf_counter() - t0
         if dist:
-            tt = torch.tensor([el], dtype=torch.float64, device=dev)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            el = float(tt.item())
+            el = max_over_ranks(torch, dist, dev, el)
         out.append(el)
     return out[0], out[1]
 
@@ -297,9 +307,7 @@ def measure_form(args, torch, dist, dev, local_rank, m, u0, precision):
     launches = sysm.launch_count() - launches0
     ms = e0.elapsed_time(e1)
     if dist:
-        tt = torch.tensor([ms], dtype=torch.float64, device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
+        ms = max_over_ranks(torch, dist, dev, ms)
     sol = sysm.GetSolutionColumn()
     kt = sysm.kernel_times(reps=5)
     # end to end through the C ABI with pinned host buffers
