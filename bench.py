@@ -353,7 +353,22 @@ def roofline_of(kt, L, cells, hbm_peak, peak_src, fp64_peak, precision):
                      "frac": alg_flops / t_dom / 1e12 / fp64_peak,
                      "peak_source": "measured in this run: cuBLAS DGEMM 4096^3",
                      "alg_flops_per_launch": alg_flops},
-            "binding": "fp64 pipe (see fp64.frac)", "kernel_ms": kt}
+            "binding": "fp64 pipe", "pipe_utilisation": NCU_PIPE_40.get((precision, dom)),
+            "kernel_ms": kt}
+
+
+# FP64-pipe utilisation of the dominant kernels (ncu --set full on the 40^3
+# p = 3 case; profiles/mixed_kernels_vortex40_p3.md,
+# profiles/cell_face_kernels_vortex40_p3_fp64.md): the mixed form's
+# algorithmic FP64 flops (RK accumulation, 4 per DOF) understate the FP64
+# instruction stream (conversions, node traces, positivity), which is what
+# binds the kernel.
+NCU_PIPE_40 = {
+    ("mixed", "cell_update"): {"sm__pipe_fp64_cycles_active_pct": 68.0, "issue_active_pct": 47.8,
+                               "source": "profiles/mixed_kernels_vortex40_p3.md"},
+    ("mixed", "face_flux"): {"sm__pipe_fp64_cycles_active_pct": 87.7, "issue_active_pct": 9.5,
+                             "source": "profiles/mixed_kernels_vortex40_p3.md"},
+}
 
 
 # ---------------------------------------------------------------------------
