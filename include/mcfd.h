@@ -455,6 +455,19 @@ int mcfd_ensemble_destroy(mcfd_ensemble *e);
  * released); the caller keeps ownership of the stream. */
 int mcfd_ensemble_set_stream(mcfd_ensemble *e, void *cuda_stream);
 const char *mcfd_ensemble_last_error(const mcfd_ensemble *e);
+/* Streamed ensemble stepping: each job loads every member's column from
+ * host_in[i], runs n_steps ensemble steps and stores the columns to
+ * host_out[i]; the uploads of job k+1 and the downloads of job k-1 overlap
+ * job k (staging of two columns per member and direction, allocated by the
+ * first begin and kept until mcfd_ensemble_destroy).  As mcfd_stream_*: the
+ * host arrays stay untouched until mcfd_ensemble_stream_end, which waits and
+ * reports the first member status.  Member times continue from job to job,
+ * as with set-solution + mcfd_ensemble_advance. */
+int mcfd_ensemble_stream_begin(mcfd_ensemble *e);
+int mcfd_ensemble_stream_step(mcfd_ensemble *e, const double *const *host_in,
+                              double *const *host_out, int32_t n_steps,
+                              double dt_guess, int32_t rk_order);
+int mcfd_ensemble_stream_end(mcfd_ensemble *e);
 
 /* Launch-shape autotuner (no reference counterpart).  Times the candidate
  * launch shapes of this handle's kernels on its own mesh and current solution

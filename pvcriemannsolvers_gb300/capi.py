@@ -122,6 +122,9 @@ SIGNATURES = {
     "mcfd_scatter_fields": (C.c_int, [_P, _P, C.c_int64]),
     "mcfd_write_restart": (C.c_int, [_P, C.c_char_p, C.c_double]),
     "mcfd_read_restart": (C.c_int, [_P, C.c_char_p, _D]),
+    "mcfd_ensemble_stream_begin": (C.c_int, [_P]),
+    "mcfd_ensemble_stream_step": (C.c_int, [_P, C.POINTER(_D), C.POINTER(_D), C.c_int32, C.c_double, C.c_int32]),
+    "mcfd_ensemble_stream_end": (C.c_int, [_P]),
     "mcfd_stream_begin": (C.c_int, [_P]),
     "mcfd_stream_step": (C.c_int, [_P, _D, _D, C.c_int64, C.c_double, C.c_int32, C.c_double, C.c_int32]),
     "mcfd_stream_end": (C.c_int, [_P]),

@@ -1211,6 +1211,14 @@ struct mcfd_ensemble {
   int order = 0;
   std::vector<int> kernels;
   std::string err;
+  // streamed stepping (mcfd_ensemble_stream_*): per member and slot b the
+  // staged input / output columns; one copy stream per direction
+  bool streaming = false;
+  std::vector<double *> in[2], out[2];
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  cudaEvent_t in_ready[2] = {nullptr, nullptr}, in_free[2] = {nullptr, nullptr};
+  cudaEvent_t out_ready[2] = {nullptr, nullptr}, out_free[2] = {nullptr, nullptr};
+  int64_t k = 0;
 };
 
 namespace {
@@ -1220,7 +1228,52 @@ int ens_fail(mcfd_ensemble *e, int code, const std::string &msg) {
   return code;
 }
 
+void ens_stream_release(mcfd_ensemble *e) {
+  for (int b = 0; b < 2; ++b) {
+    for (double *p : e->in[b]) if (p) cudaFree(p);
+    for (double *p : e->out[b]) if (p) cudaFree(p);
+    e->in[b].clear();
+    e->out[b].clear();
+    cudaEvent_t evs[] = {e->in_ready[b], e->in_free[b], e->out_ready[b], e->out_free[b]};
+    for (cudaEvent_t ev : evs) if (ev) cudaEventDestroy(ev);
+    e->in_ready[b] = e->in_free[b] = e->out_ready[b] = e->out_free[b] = nullptr;
+  }
+  if (e->copy_in) cudaStreamDestroy(e->copy_in);
+  if (e->copy_out) cudaStreamDestroy(e->copy_out);
+  e->copy_in = e->copy_out = nullptr;
+  e->streaming = false;
+}
+
+// Capture (once per RK order) the fork/join graph of one ensemble step.
+int ens_ensure_graph(mcfd_ensemble *e, int32_t rk_order) {
+  if (e->graph && e->order == rk_order) return MCFD_OK;
+  if (e->graph) { cudaGraphExecDestroy(e->graph); e->graph = nullptr; }
+  e->kernels.assign(e->members.size(), 0);
+  cudaGraph_t graph;
+  cudaError_t err = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
+  if (err == cudaSuccess) err = cudaEventRecord(e->fork, e->stream);
+  for (size_t i = 0; i < e->members.size() && err == cudaSuccess; ++i) {
+    mcfd_handle *h = e->members[i];
+    err = cudaStreamWaitEvent(h->stream, e->fork, 0);
+    if (err != cudaSuccess) break;
+    int k = mcfd::launch_dt(h, h->buf.u);
+    k += mcfd::launch_rk_stage_sequence(h, rk_order);
+    e->kernels[i] = k;
+    err = cudaEventRecord(e->join[i], h->stream);
+    if (err == cudaSuccess) err = cudaStreamWaitEvent(e->stream, e->join[i], 0);
+  }
+  cudaError_t end = cudaStreamEndCapture(e->stream, &graph);
+  if (err == cudaSuccess) err = end;
+  if (err != cudaSuccess) return ens_fail(e, MCFD_ERR_CUDA, std::string("ensemble capture: ") + cudaGetErrorString(err));
+  err = cudaGraphInstantiate(&e->graph, graph, 0);
+  cudaGraphDestroy(graph);
+  if (err != cudaSuccess) return ens_fail(e, MCFD_ERR_CUDA, std::string("ensemble graph: ") + cudaGetErrorString(err));
+  e->order = rk_order;
+  return MCFD_OK;
+}
+
 void ens_release(mcfd_ensemble *e) {
+  ens_stream_release(e);
   if (e->graph) cudaGraphExecDestroy(e->graph);
   for (cudaEvent_t ev : e->join)
     if (ev) cudaEventDestroy(ev);
@@ -1299,29 +1352,9 @@ int mcfd_ensemble_advance(mcfd_ensemble *e, int32_t n_steps, double dt_guess, in
     if (err == cudaSuccess) err = cudaStreamSynchronize(h->stream);
     if (err != cudaSuccess) return ens_fail(e, MCFD_ERR_CUDA, std::string("member set-up: ") + cudaGetErrorString(err));
   }
-  if (!e->graph || e->order != rk_order) {
-    if (e->graph) { cudaGraphExecDestroy(e->graph); e->graph = nullptr; }
-    e->kernels.assign(e->members.size(), 0);
-    cudaGraph_t graph;
-    cudaError_t err = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
-    if (err == cudaSuccess) err = cudaEventRecord(e->fork, e->stream);
-    for (size_t i = 0; i < e->members.size() && err == cudaSuccess; ++i) {
-      mcfd_handle *h = e->members[i];
-      err = cudaStreamWaitEvent(h->stream, e->fork, 0);
-      if (err != cudaSuccess) break;
-      int k = mcfd::launch_dt(h, h->buf.u);
-      k += mcfd::launch_rk_stage_sequence(h, rk_order);
-      e->kernels[i] = k;
-      err = cudaEventRecord(e->join[i], h->stream);
-      if (err == cudaSuccess) err = cudaStreamWaitEvent(e->stream, e->join[i], 0);
-    }
-    cudaError_t end = cudaStreamEndCapture(e->stream, &graph);
-    if (err == cudaSuccess) err = end;
-    if (err != cudaSuccess) return ens_fail(e, MCFD_ERR_CUDA, std::string("ensemble capture: ") + cudaGetErrorString(err));
-    err = cudaGraphInstantiate(&e->graph, graph, 0);
-    cudaGraphDestroy(graph);
-    if (err != cudaSuccess) return ens_fail(e, MCFD_ERR_CUDA, std::string("ensemble graph: ") + cudaGetErrorString(err));
-    e->order = rk_order;
+  {
+    const int grc = ens_ensure_graph(e, rk_order);
+    if (grc) return grc;
   }
   for (int s = 0; s < n_steps; ++s) {
     cudaError_t err = cudaGraphLaunch(e->graph, e->stream);
@@ -1336,6 +1369,109 @@ int mcfd_ensemble_advance(mcfd_ensemble *e, int32_t n_steps, double dt_guess, in
     mcfd::DevState st;
     if (cudaMemcpy(&st, h->buf.state, sizeof(st), cudaMemcpyDeviceToHost) == cudaSuccess) h->t_host = st.t;
     int r = check_status(h);
+    if (r && !rc) {
+      rc = r;
+      e->err = "member " + std::to_string(i) + ": " + h->err;
+    }
+  }
+  return rc;
+}
+
+int mcfd_ensemble_stream_begin(mcfd_ensemble *e) {
+  if (!e) return MCFD_ERR_ARGUMENT;
+  if (e->streaming) return MCFD_OK;
+  cudaSetDevice(e->device);
+  cudaError_t err = cudaSuccess;
+  if (!e->copy_out) {
+    for (int b = 0; b < 2 && err == cudaSuccess; ++b) {
+      for (mcfd_handle *h : e->members) {
+        double *pi = nullptr, *po = nullptr;
+        if (err == cudaSuccess) err = cudaMalloc(&pi, sizeof(double) * h->mesh.column);
+        if (err == cudaSuccess) e->in[b].push_back(pi);
+        if (err == cudaSuccess) err = cudaMalloc(&po, sizeof(double) * h->mesh.column);
+        if (err == cudaSuccess) e->out[b].push_back(po);
+      }
+      cudaEvent_t *evs[] = {&e->in_ready[b], &e->in_free[b], &e->out_ready[b], &e->out_free[b]};
+      for (cudaEvent_t *ev : evs)
+        if (err == cudaSuccess) err = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+    }
+    if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&e->copy_in, cudaStreamNonBlocking);
+    if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&e->copy_out, cudaStreamNonBlocking);
+    if (err != cudaSuccess) {
+      ens_stream_release(e);
+      return ens_fail(e, MCFD_ERR_CUDA, std::string("ensemble stream set-up: ") + cudaGetErrorString(err));
+    }
+  }
+  e->streaming = true;
+  e->k = 0;
+  return MCFD_OK;
+}
+
+int mcfd_ensemble_stream_step(mcfd_ensemble *e, const double *const *host_in, double *const *host_out,
+                              int32_t n_steps, double dt_guess, int32_t rk_order) {
+  if (!e || !host_in || !host_out || n_steps < 1 || rk_order < 1 || rk_order > 3) return MCFD_ERR_ARGUMENT;
+  if (!e->streaming) return ens_fail(e, MCFD_ERR_STATE, "mcfd_ensemble_stream_begin first");
+  cudaSetDevice(e->device);
+  const int b = (int)(e->k & 1);
+  const size_t nm = e->members.size();
+  cudaError_t err = cudaStreamWaitEvent(e->copy_in, e->in_free[b], 0);
+  for (size_t i = 0; i < nm && err == cudaSuccess; ++i)
+    err = cudaMemcpyAsync(e->in[b][i], host_in[i], sizeof(double) * e->members[i]->mesh.column,
+                          cudaMemcpyHostToDevice, e->copy_in);
+  if (err == cudaSuccess) err = cudaEventRecord(e->in_ready[b], e->copy_in);
+  if (err == cudaSuccess) err = cudaStreamWaitEvent(e->stream, e->in_ready[b], 0);
+  if (err == cudaSuccess) err = cudaStreamWaitEvent(e->stream, e->out_free[b], 0);
+  // load every member's column and set its step bounds, ordered on the
+  // ensemble stream ahead of the replays that fork from it
+  for (size_t i = 0; i < nm && err == cudaSuccess; ++i) {
+    mcfd_handle *h = e->members[i];
+    err = cudaMemcpyAsync(h->buf.u, e->in[b][i], sizeof(double) * h->mesh.column, cudaMemcpyDeviceToDevice,
+                          e->stream);
+    if (err != cudaSuccess) break;
+    mcfd::invalidate_trace(h, h->buf.u);
+    const cudaStream_t own = h->stream;
+    h->stream = e->stream;
+    const double cfl = h->opt.cfl > 0 ? h->opt.cfl : cfl_table(rk_order, h->mesh.p);
+    h->launches += mcfd::launch_set_bounds(h, dt_guess, cfl);  // times continue on the device
+    h->launches += mcfd::launch_trace(h, h->buf.u);
+    h->stream = own;
+    err = cudaGetLastError();
+  }
+  if (err == cudaSuccess) err = cudaEventRecord(e->in_free[b], e->stream);
+  if (err != cudaSuccess) return ens_fail(e, MCFD_ERR_CUDA, std::string("ensemble stream load: ") + cudaGetErrorString(err));
+  const int grc = ens_ensure_graph(e, rk_order);
+  if (grc) return grc;
+  for (int s = 0; s < n_steps && err == cudaSuccess; ++s) err = cudaGraphLaunch(e->graph, e->stream);
+  for (size_t i = 0; i < nm; ++i) e->members[i]->launches += (int64_t)e->kernels[i] * n_steps;
+  for (size_t i = 0; i < nm && err == cudaSuccess; ++i)
+    err = cudaMemcpyAsync(e->out[b][i], e->members[i]->buf.u, sizeof(double) * e->members[i]->mesh.column,
+                          cudaMemcpyDeviceToDevice, e->stream);
+  if (err == cudaSuccess) err = cudaEventRecord(e->out_ready[b], e->stream);
+  if (err == cudaSuccess) err = cudaStreamWaitEvent(e->copy_out, e->out_ready[b], 0);
+  for (size_t i = 0; i < nm && err == cudaSuccess; ++i)
+    err = cudaMemcpyAsync(host_out[i], e->out[b][i], sizeof(double) * e->members[i]->mesh.column,
+                          cudaMemcpyDeviceToHost, e->copy_out);
+  if (err == cudaSuccess) err = cudaEventRecord(e->out_free[b], e->copy_out);
+  if (err != cudaSuccess) return ens_fail(e, MCFD_ERR_CUDA, std::string("ensemble stream step: ") + cudaGetErrorString(err));
+  ++e->k;
+  return MCFD_OK;
+}
+
+int mcfd_ensemble_stream_end(mcfd_ensemble *e) {
+  if (!e) return MCFD_ERR_ARGUMENT;
+  if (!e->streaming) return MCFD_OK;
+  cudaSetDevice(e->device);
+  cudaError_t err = cudaStreamSynchronize(e->copy_in);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(e->stream);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(e->copy_out);
+  e->streaming = false;
+  if (err != cudaSuccess) return ens_fail(e, MCFD_ERR_CUDA, std::string("ensemble stream end: ") + cudaGetErrorString(err));
+  int rc = MCFD_OK;
+  for (size_t i = 0; i < e->members.size(); ++i) {
+    mcfd_handle *h = e->members[i];
+    mcfd::DevState st;
+    if (cudaMemcpy(&st, h->buf.state, sizeof(st), cudaMemcpyDeviceToHost) == cudaSuccess) h->t_host = st.t;
+    const int r = check_status(h);
     if (r && !rc) {
       rc = r;
       e->err = "member " + std::to_string(i) + ": " + h->err;

@@ -719,6 +719,18 @@ void cell_dispatch_s(mcfd_handle *h, int stage, const CellArgs &ca) {
 
 }  // namespace
 
+// Step bounds only (dt guess, CFL, rate reset), the device time kept.
+__global__ void set_bounds_kernel(DevState *state, double dt_guess, double cfl) {
+  state->dt_guess = dt_guess;
+  state->cfl = cfl;
+  state->max_rate_bits = 0ull;
+}
+
+int launch_set_bounds(mcfd_handle *h, double dt_guess, double cfl) {
+  set_bounds_kernel<<<1, 1, 0, h->stream>>>(h->buf.state, dt_guess, cfl);
+  return 1;
+}
+
 int launch_set_state(mcfd_handle *h, double t, double dt, double dt_guess,
                      double cfl, int reset_rate) {
   set_state_kernel<<<1, 1, 0, h->stream>>>(h->buf.state, t, dt, dt_guess, cfl,

@@ -232,6 +232,8 @@ inline void drop_graphs(mcfd_handle *h) {
 // Kernel launchers (dgsem.cu).  Each returns the number of kernels launched.
 int launch_set_state(mcfd_handle *h, double t, double dt, double dt_guess,
                      double cfl, int reset_rate);
+// dt guess and CFL of the next steps with the device time left as it is.
+int launch_set_bounds(mcfd_handle *h, double dt_guess, double cfl);
 int launch_face_flux(mcfd_handle *h, const double *u, double stage_c);
 int launch_cell_update(mcfd_handle *h, int stage, const double *u_in,
                        const double *u0, double *u_out, int advance_time);

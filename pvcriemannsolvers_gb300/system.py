@@ -396,6 +396,33 @@ class Ensemble:
             msg = self._lib.mcfd_ensemble_last_error(self._e)
             raise capi.McfdError(code, msg.decode() if msg else "")
 
+    def _ens_check(self, code: int) -> None:
+        if code != capi.OK:
+            msg = self._lib.mcfd_ensemble_last_error(self._e)
+            raise capi.McfdError(code, msg.decode() if msg else "")
+
+    def stream_begin(self) -> None:
+        self._ens_check(self._lib.mcfd_ensemble_stream_begin(self._e))
+
+    def stream_step(self, host_in, host_out, n_steps: int, dt_guess: float, rk_order: int) -> None:
+        """Enqueue one job: every member's column from host_in[i], n_steps
+        ensemble steps, the columns into host_out[i] (arrays kept alive and
+        unread until stream_end; page-locked for asynchronous copies)."""
+        n = len(self.systems)
+        if len(host_in) != n or len(host_out) != n:
+            raise ValueError("one input and one output column per member")
+        for s, a, b in zip(self.systems, host_in, host_out):
+            for x in (a, b):
+                if x.dtype != np.float64 or not x.flags.c_contiguous or x.size != s.column_size:
+                    raise ValueError("stream buffers must be contiguous float64 arrays of each column size")
+        ins = (capi._D * n)(*[capi.dptr(a) for a in host_in])
+        outs = (capi._D * n)(*[capi.dptr(b) for b in host_out])
+        self._ens_check(self._lib.mcfd_ensemble_stream_step(self._e, ins, outs, int(n_steps), float(dt_guess),
+                                                            int(rk_order)))
+
+    def stream_end(self) -> None:
+        self._ens_check(self._lib.mcfd_ensemble_stream_end(self._e))
+
     def set_stream(self, stream_ptr: int) -> None:
         code = self._lib.mcfd_ensemble_set_stream(self._e, C.c_void_p(stream_ptr))
         if code != capi.OK:

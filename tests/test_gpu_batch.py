@@ -113,3 +113,54 @@ def test_cases_must_not_share_faces(gpu):
     with pytest.raises(capi.McfdError):
         s.set_cases([0, 20])
     s.close()
+
+
+def test_ensemble_stream_matches_sequential(gpu):
+    """Streamed ensemble jobs (mcfd_ensemble_stream_*) give the columns of
+    set-solution + mcfd_ensemble_advance + get-solution, bit for bit."""
+    import torch
+
+    def members():
+        a, _ = batched("hex", 2, "dgsem", [(3, 3, 3), (2, 3, 2)], [4, 5])
+        b, _ = batched("tet", 2, "modal", [(3, 3, 2), (3, 2, 3)], [6, 7], riemann="hllc")
+        c = Lobatto(meshlib.box((3, 3, 3), periodic=(True,) * 3, jitter=0.05, seed=8), 3, "rusanov",
+                    precision="mixed")
+        load(c, meshlib.box((3, 3, 3), periodic=(True,) * 3, jitter=0.05, seed=8), 8, False)
+        return [a, b, c]
+
+    def pinned(n):
+        return torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+
+    seq = members()
+    start = [s.GetSolutionColumn() for s in seq]
+    ens = Ensemble(seq)
+    want = []
+    cols = start
+    for job in range(4):
+        for s, col in zip(seq, cols):
+            s.SetSolutionColumn(col)
+        ens.advance(1, 1e9, 3)
+        cols = [s.GetSolutionColumn() for s in seq]
+        want.append(cols)
+    ens.close()
+    for s in seq:
+        s.close()
+    # streamed: job k's input is job k-1's expected output
+    stm = members()
+    ens = Ensemble(stm)
+    ins = [[pinned(c.size) for c in start] for _ in range(4)]
+    outs = [[pinned(c.size) for c in start] for _ in range(4)]
+    for j in range(4):
+        src = start if j == 0 else want[j - 1]
+        for dst, col in zip(ins[j], src):
+            dst[:] = col
+    ens.stream_begin()
+    for j in range(4):
+        ens.stream_step(ins[j], outs[j], 1, 1e9, 3)
+    ens.stream_end()
+    for j in range(4):
+        for got, ref in zip(outs[j], want[j]):
+            assert np.array_equal(got, ref), f"job {j}"
+    ens.close()
+    for s in stm:
+        s.close()
