@@ -685,8 +685,19 @@ def ensemble_form(args, torch, dev, local_rank, specs, precision):
         hout = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
         hin[:] = sol
         hosts.append((hin, hout))
-    e2e_steps = max(1, min(args.steps, 10))
+    e2e_steps = max(1, min(args.steps, 20))
+    ins, outs = [h[0] for h in hosts], [h[1] for h in hosts]
+    ens.stream_begin()  # staging allocation and the job set-up, untimed
+    ens.stream_step(ins, outs, 1, 1e9, 3)
+    ens.stream_end()
     torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    ens.stream_begin()
+    for _ in range(e2e_steps):
+        ens.stream_step(ins, outs, 1, 1e9, 3)
+    ens.stream_end()
+    torch.cuda.synchronize(dev)
+    e2e_s = time.perf_counter() - t0
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         for mb, (hin, _) in zip(members, hosts):
@@ -695,7 +706,7 @@ def ensemble_form(args, torch, dev, local_rank, specs, precision):
         for mb, (_, hout) in zip(members, hosts):
             mb["system"].get_solution_into(hout)
     torch.cuda.synchronize(dev)
-    e2e_s = time.perf_counter() - t0
+    seq_s = time.perf_counter() - t0
     per_member = []
     for mb in members:
         kt = mb["system"].kernel_times(reps=3)
@@ -707,7 +718,8 @@ def ensemble_form(args, torch, dev, local_rank, specs, precision):
     for mb in members:
         mb["system"].close()
     return {"value": 3 * L * args.steps / (ms * 1e-3), "ms_per_step": ms / args.steps,
-            "e2e": 3 * L * e2e_steps / e2e_s, "e2e_steps": e2e_steps, "launches": launches,
+            "e2e": 3 * L * e2e_steps / e2e_s, "e2e_sequential": 3 * L * e2e_steps / seq_s,
+            "e2e_steps": e2e_steps, "launches": launches,
             "clocks": clocks.summary(), "members": per_member, "solution": solution, "L": L}
 
 
@@ -748,7 +760,11 @@ def run_ensemble(args, rank, world, local_rank):
         "clocks": r["clocks"],
         "e2e": {"value": r["e2e"], "unit": UNIT, "h2d_bytes_per_step": 8 * L,
                 "d2h_bytes_per_step": 8 * L, "steps": r["e2e_steps"],
-                "path": "mcfd_set_solution per handle + mcfd_ensemble_advance(1) + mcfd_get_solution per handle"},
+                "path": "mcfd_ensemble_stream_step per step (every member's column in from pinned host memory, "
+                        "one ensemble step, the columns out; neighbouring steps' copies overlap the compute)",
+                "sequential": {"value": r["e2e_sequential"],
+                               "path": "mcfd_set_solution per handle + mcfd_ensemble_advance(1) + "
+                                       "mcfd_get_solution per handle"}},
         "gpu_launches": r["launches"],
         "members": r["members"],
         "plain_fp64": {"value": pf["value"], "ms_per_step": pf["ms_per_step"], "e2e": pf["e2e"],
