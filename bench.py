@@ -1041,27 +1041,32 @@ def run_sod(args, rank, world, local_rank):
     cpu_s = time.perf_counter() - t0_cpu
     chk.close()
     cpu_rate = 3 * L * (n_cpu - n0) / cpu_s
-    r, pf = res["mixed"], res["fp64"]
-    a, b = r["solution"].reshape(-1, K)[:, 0], pf["solution"].reshape(-1, K)[:, 0]
+    # the plain FP64 form is the line's value: with weno::Lazy on every cell
+    # this case amplifies perturbations exponentially (the FP64 GPU run and
+    # the FP64 oracle drift apart from 1e-13 at 100 steps to 1e-8 at 400), so
+    # the mixed form's FP32 rounding grows to percent-level differences by
+    # t = 0.2 and is reported beside it, not as the result
+    r, pm = res["fp64"], res["mixed"]
+    a, b = pm["solution"].reshape(-1, K)[:, 0], r["solution"].reshape(-1, K)[:, 0]
     line = {
         "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": r["steps"],
         "warmup": args.warmup, "ms_per_step": r["seconds"] * 1e3 / r["steps"], "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "Sod shock tube 100x4x4 Hex8 on [0,1]x[0,0.04]^2, DGSEM p=2, Roe, weno::Lazy "
                                "on every cell after every stage, SSP-RK3, CFL 0.1, t = 0 -> 0.2",
-                   "cells": m.n_cells, "dofs": L, "form": "mixed; plain FP64 beside it",
+                   "cells": m.n_cells, "dofs": L, "form": "plain FP64 (mixed beside it)",
                    "l2_flush": "none: the whole case (1.7 MB) lives in L2, as it does on the CPU"},
-        "time_to_solution_s": {"gpu_mixed": r["seconds"], "gpu_fp64": pf["seconds"],
-                               "cpu_oracle_extrapolated": pf["steps"] * (cpu_s / (n_cpu - n0))},
+        "time_to_solution_s": {"gpu_fp64": r["seconds"], "gpu_mixed": pm["seconds"],
+                               "cpu_oracle_extrapolated": r["steps"] * (cpu_s / (n_cpu - n0))},
         "accuracy": {"gpu_fp64_vs_oracle_rel_l2_after_5_steps": parity,
                      "mixed_vs_fp64_density_rel_l2_at_t_end": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
-                     "t_end": r["t"]},
+                     "t_end_fp64": r["t"], "t_end_mixed": pm["t"]},
         "clocks": r["clocks"], "gpu_launches": r["launches"],
-        "plain_fp64": {k: pf[k] for k in ("value", "steps", "seconds", "launches", "kernel_ms", "clocks")},
+        "mixed": {k: pm[k] for k in ("value", "steps", "seconds", "launches", "kernel_ms", "clocks")},
         "roofline": {"bound": "launch", "note": "1,600 cells: every kernel is a few microseconds; the step "
                                                 "graph removes launch gaps", "kernel_ms": r["kernel_ms"]},
         "cpu_baseline": {"value": cpu_rate, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"the same case, steps 6..{n_cpu} of {pf['steps']}, {cpu_s:.1f} s, oracle "
+                         "sample": f"the same case, steps 6..{n_cpu} of {r['steps']}, {cpu_s:.1f} s, oracle "
                                    f"(plain C restatement, OpenMP)"},
     }
     if rank == 0:
