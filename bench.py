@@ -870,26 +870,31 @@ def run_quadrant(args, rank, world, local_rank):
     cpu = None
     if not args.no_cpu:
         cpu = quadrant_cpu_sample()
-    r = res["mixed"]
+    # the plain FP64 form is the line's value: with the limiter switching on
+    # shocks this case amplifies perturbations over the steps (mixed vs FP64
+    # density 4.8e-7 after 53 steps, 4.4e-4 after 203), so the mixed form is
+    # reported beside it with its deviation, not as the result
+    r = res["fp64"]
     line = {
         "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"four-quadrant Riemann problem, {nx}x{ny}x{nz} Hex8, DGSEM p={QUAD_DEGREE}, Roe, "
                                f"SSP-RK3, CFL 0.209, weno::Eigen limiter after every stage",
                    "cells": m.n_cells, "dofs": L,
-                   "form": "mixed (FP32 volume flux + contraction; FP64 Riemann fluxes, limiter, RK)",
+                   "form": "plain FP64 (mixed beside it: FP32 volume flux + contraction, FP64 Riemann "
+                           "fluxes, limiter smoothness and reconstruction, RK)",
                    "step": "dt reduction + 3 x (RK stage + limiter pass)",
                    "l2_flush": "inputs larger than L2 (solution column 1.13 GB)"},
         "accuracy": {"t_end": r["t"], "mixed_vs_fp64_density_rel_l2": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
-                     "troubled_fraction_mixed": r["troubled_fraction"],
+                     "troubled_fraction_mixed": res["mixed"]["troubled_fraction"],
                      "troubled_fraction_fp64": res["fp64"]["troubled_fraction"]},
         "clocks": r["clocks"],
         "e2e": {"value": r["e2e"], "unit": UNIT, "h2d_bytes_per_step": 8 * L, "d2h_bytes_per_step": 8 * L,
                 "steps": e2e_steps, "path": E2E_PATH,
                 "sequential": {"value": r["e2e_sequential"], "path": E2E_SEQ_PATH}},
         "gpu_launches": r["launches"],
-        "plain_fp64": {k: res["fp64"][k] for k in ("value", "ms_per_step", "e2e", "e2e_sequential", "launches",
+        "mixed": {k: res["mixed"][k] for k in ("value", "ms_per_step", "e2e", "e2e_sequential", "launches",
                                                    "kernel_ms", "clocks")},
         "roofline": {"bound": "fp64", "kernel": "step", "kernel_ms": r["kernel_ms"], "peak": fp64_peak,
                      "unit": "TFLOP/s", "achieved": None, "frac": None, "traffic": None,
