@@ -46,7 +46,8 @@ enum {
   ORC_BC_SUPERSONIC_OUTLET = 3,
   ORC_BC_SUBSONIC_INLET = 4,
   ORC_BC_SUBSONIC_OUTLET = 5,
-  ORC_BC_SMART = 6
+  ORC_BC_SMART = 6,
+  ORC_BC_NO_SLIP_WALL = 7 /* viscous fr::Lobatto only (spatial/fr/lobatto.hpp:298-317) */
 };
 
 /* Given-state programs for boundaries that need an exterior value. */
@@ -207,6 +208,48 @@ int orc_vtk_sample(const orc_mesh *m, const double *u, double *xyz, double *valu
  * 24), cell by cell; returns the number of points */
 int64_t orc_modal_vtk_sample(const orc_modal *m, const double *u, double *xyz,
                              double *values, uint8_t *types);
+
+/* ---- energy-based artificial viscosity on fr::Lobatto (orc_visc.c) ----
+ * EnergyBasedViscosity<Part, ConvectionDiffusion<rotated::Euler<...>,
+ * Direct<Isotropic>>> with WithViscosity<fr::Lobatto> (spatial/viscosity.hpp,
+ * spatial/with_viscosity.hpp, riemann/diffusive/direct.hpp), Hex8 cells.
+ * The mesh must use ORC_SCHEME_FR.  Creating the object builds the damping
+ * matrices the way BuildDampingMatrices does (viscosity.hpp:299-384). */
+typedef struct orc_visc orc_visc;
+orc_visc *orc_visc_create(const orc_mesh *m, double beta0, double beta1, double time_scale);
+void orc_visc_destroy(orc_visc *v);
+/* damping matrices [cells][N][N] (row-major) */
+const double *orc_visc_damping(const orc_visc *v);
+/* IntegrateJumpOnFaces (viscosity.hpp:446-475): [cells][K] */
+void orc_visc_jumps(const orc_visc *v, const double *u, double *jumps);
+/* UpdateProperties: GetViscosityValues (viscosity.hpp:477-544) of the
+ * solution u; nu [cells][K]; *min_dt = GetMinimumTimeStep() */
+void orc_visc_properties(const orc_visc *v, const double *u, double *nu, double *min_dt);
+/* GetResidualColumn of fr::Lobatto over the viscous Riemann object with
+ * given cell viscosities nu [cells][K] (fr/general.hpp:249-515). */
+int orc_visc_residual(const orc_visc *v, int riemann, int n_bc, const orc_bc *bcs,
+                      double t, const double *u, const double *nu, double *r);
+/* WithViscosity::GetTimeStep (with_viscosity.hpp:67-71) after
+ * UpdateProperties on u: min(2 cfl min_dt, dt_guess); cfl <= 0 selects the
+ * table. */
+double orc_visc_time_step(const orc_visc *v, const double *u, double dt_guess, int rk_order,
+                          double cfl);
+/* RungeKutta<order>::Update on WithViscosity<fr::Lobatto>: every residual
+ * uses the viscosities of its own input (SetSolutionColumn runs
+ * UpdateProperties, with_viscosity.hpp:56-59). */
+int orc_visc_rk_update(const orc_visc *v, int riemann, int n_bc, const orc_bc *bcs, int order,
+                       double t, double dt, double *u);
+/* Global value, gradient [3][K] and Hessian [6][K] (XX XY XZ YY YZ ZZ) at
+ * node q of cell c (Hexahedron::GetGlobalValueGradientHessian, kLocal =
+ * false, polynomial/hexahedron.hpp:586-595). */
+void orc_visc_node_derivatives(const orc_visc *v, const double *u, int64_t c, int q,
+                               double *grad, double *hess);
+/* Initial limiters of the viscous demos: limiter::average::Reconstruct and
+ * limiter::majority::Reconstruct (limiter/average.hpp:11-28,
+ * limiter/majority.hpp:14-42), in place.  Returns the number of cells that
+ * have a component without a strict majority value (left unchanged). */
+enum { ORC_INIT_AVERAGE = 1, ORC_INIT_MAJORITY = 2 };
+int64_t orc_initial_limiter(const orc_mesh *m, int kind, double *u);
 
 #ifdef __cplusplus
 }

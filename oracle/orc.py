@@ -18,7 +18,7 @@ LIB = HERE / "liborc.so"
 
 EXACT, HLLC, AUSM, ROE, RUSANOV = range(5)
 BC_NONE, BC_INVISCID_WALL, BC_SUPERSONIC_INLET, BC_SUPERSONIC_OUTLET, BC_SUBSONIC_INLET, \
-    BC_SUBSONIC_OUTLET, BC_SMART = range(7)
+    BC_SUBSONIC_OUTLET, BC_SMART, BC_NO_SLIP_WALL = range(8)
 STATE_CONSTANT, STATE_MOVING_SPLIT = 0, 1
 
 _D = C.POINTER(C.c_double)
@@ -332,6 +332,102 @@ class Limiter:
         self.lib.orc_rk_update_limited(self.mesh._m, riemann, n, arr, order, t, dt, _p(u), self._l,
                                        self.mode, self.w0, self.eps)
         return u
+
+
+def _visc_sigs(lib):
+    sig = {
+        "orc_visc_create": (C.c_void_p, [C.c_void_p, C.c_double, C.c_double, C.c_double]),
+        "orc_visc_destroy": (None, [C.c_void_p]),
+        "orc_visc_damping": (_D, [C.c_void_p]),
+        "orc_visc_jumps": (None, [C.c_void_p, _D, _D]),
+        "orc_visc_properties": (None, [C.c_void_p, _D, _D, _D]),
+        "orc_visc_residual": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(OrcBc), C.c_double, _D, _D, _D]),
+        "orc_visc_time_step": (C.c_double, [C.c_void_p, _D, C.c_double, C.c_int, C.c_double]),
+        "orc_visc_rk_update": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(OrcBc), C.c_int, C.c_double,
+                                         C.c_double, _D]),
+        "orc_visc_node_derivatives": (None, [C.c_void_p, _D, C.c_int64, C.c_int, _D, _D]),
+        "orc_initial_limiter": (C.c_int64, [C.c_void_p, C.c_int, _D]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+INIT_AVERAGE, INIT_MAJORITY = 1, 2
+
+
+class Viscosity:
+    """EnergyBasedViscosity on the fr::Lobatto system of an oracle Mesh built
+    with scheme="fr" (WithViscosity<fr::Lobatto>, Hex8 cells)."""
+
+    def __init__(self, mesh: "Mesh", beta0: float = 2.0, beta1: float = 1.0 / 12, time_scale: float = 1.0):
+        self.lib = load()
+        _visc_sigs(self.lib)
+        self.mesh = mesh
+        self._v = self.lib.orc_visc_create(mesh._m, beta0, beta1, time_scale)
+        if not self._v:
+            raise RuntimeError("oracle viscosity needs an fr mesh of Hex8 cells")
+        self.n = (mesh.degree + 1) ** 3
+
+    def __del__(self):
+        if getattr(self, "_v", None):
+            self.lib.orc_visc_destroy(self._v)
+            self._v = None
+
+    def damping(self) -> np.ndarray:
+        n, nc = self.n, self.mesh.n_cells
+        ptr = self.lib.orc_visc_damping(self._v)
+        return np.ctypeslib.as_array(ptr, shape=(nc, n, n)).copy()
+
+    def jumps(self, u: np.ndarray) -> np.ndarray:
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        out = np.empty((self.mesh.n_cells, 5))
+        self.lib.orc_visc_jumps(self._v, _p(u), _p(out))
+        return out
+
+    def properties(self, u: np.ndarray) -> tuple[np.ndarray, float]:
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        nu = np.empty((self.mesh.n_cells, 5))
+        dt = np.zeros(1)
+        self.lib.orc_visc_properties(self._v, _p(u), _p(nu), _p(dt))
+        return nu, float(dt[0])
+
+    def residual(self, riemann: int, u: np.ndarray, nu: np.ndarray | None = None, t: float = 0.0) -> np.ndarray:
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        if nu is None:
+            nu = self.properties(u)[0]
+        nu = np.ascontiguousarray(nu, dtype=np.float64)
+        r = np.empty_like(u)
+        n, arr = self.mesh.bcs
+        self.lib.orc_visc_residual(self._v, riemann, n, arr, t, _p(u), _p(nu), _p(r))
+        return r
+
+    def time_step(self, u: np.ndarray, dt_guess: float, rk_order: int, cfl: float = 0.0) -> float:
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        return float(self.lib.orc_visc_time_step(self._v, _p(u), dt_guess, rk_order, cfl))
+
+    def rk_update(self, riemann: int, order: int, t: float, dt: float, u: np.ndarray) -> np.ndarray:
+        u = np.array(u, dtype=np.float64, copy=True)
+        n, arr = self.mesh.bcs
+        self.lib.orc_visc_rk_update(self._v, riemann, n, arr, order, t, dt, _p(u))
+        return u
+
+    def node_derivatives(self, u: np.ndarray, cell: int, node: int) -> tuple[np.ndarray, np.ndarray]:
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        g = np.empty((3, 5))
+        h = np.empty((6, 5))
+        self.lib.orc_visc_node_derivatives(self._v, _p(u), cell, node, _p(g), _p(h))
+        return g, h
+
+
+def initial_limiter(mesh: "Mesh", kind: int, u: np.ndarray) -> tuple[np.ndarray, int]:
+    """limiter::average / limiter::majority Reconstruct on a copy of u."""
+    lib = load()
+    _visc_sigs(lib)
+    u = np.array(u, dtype=np.float64, copy=True)
+    missing = lib.orc_initial_limiter(mesh._m, kind, _p(u))
+    return u, int(missing)
 
 
 def _modal_sigs(lib):

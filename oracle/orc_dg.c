@@ -37,7 +37,7 @@
 #include "orc_internal.h"
 
 #define K ORC_K
-#define MAXQ 6
+#define MAXQ ORC_MAXQ
 #define MAXN (MAXQ * MAXQ * MAXQ)
 
 static int g_threads = 0;
@@ -141,6 +141,30 @@ static void lagrange_derivatives(int q, const double *x, double *d) {
   }
 }
 
+/* Second derivatives D2[a][i] = l_i''(x_a) the same way: the Taylor second
+ * derivative row times the inverse Vandermonde matrix (lagrange.hpp:130-133,
+ * polynomial/hexahedron.hpp:155-170). */
+void orc_lagrange_second(int q, const double *x, double *d2) {
+  double v[MAXQ * MAXQ];
+  for (int j = 0; j < q; ++j) {
+    double p = 1;
+    for (int m = 0; m < q; ++m) { v[j * q + m] = p; p *= x[j]; }
+  }
+  invert(q, v);
+  for (int a = 0; a < q; ++a) {
+    double trow[MAXQ];
+    trow[0] = 0;
+    if (q > 1) trow[1] = 0;
+    double p = 1;
+    for (int m = 2; m < q; ++m) { trow[m] = m * (m - 1) * p; p *= x[a]; }
+    for (int i = 0; i < q; ++i) {
+      double s = 0;
+      for (int m = 0; m < q; ++m) s += trow[m] * v[m * q + i];
+      d2[a * q + i] = s;
+    }
+  }
+}
+
 /* ---------------- Hex8 / Quad4 maps ---------------- */
 
 static const int kHexLocal[8][3] = {
@@ -229,31 +253,7 @@ static void normalize(double *a) {
 
 /* ---------------- mesh ---------------- */
 
-struct orc_mesh {
-  int p, q, n, qf; /* degree, line points, nodes per cell, points per face */
-  int64_t n_cells, n_faces;
-  double xq[MAXQ], wq[MAXQ], d[MAXQ * MAXQ];
-  /* per cell */
-  double *node_xyz;   /* [cells][N][3] */
-  double *node_w;     /* [cells][N]  global weights */
-  double *grad;       /* [cells][N][3][N]  basis global gradients */
-  double *length;     /* [cells] */
-  double *cell_center; /* [cells][3] Hex8 LocalToGlobal(0, 0, 0) */
-  double *corners;    /* [cells][27][3] node coordinates (the type's first n) */
-  int32_t *type;      /* [cells] ORC_CELL_HEX8 / HEX27 / HEX20 */
-  double *jdi;        /* [cells][N][9] det(J) J^-1 (GetJacobianAssociated) */
-  double *detj;       /* [cells][N] det(J) */
-  int32_t *face_sides; /* [faces][2] local face index in holder / sharer */
-  int scheme;          /* ORC_SCHEME_DGSEM or ORC_SCHEME_FR */
-  /* per face */
-  int64_t *face_cells; /* [faces][2] */
-  int32_t *face_group; /* [faces] */
-  double *face_shift;  /* [faces][3] periodic shift (zeros when absent) */
-  double *face_xyz;    /* [faces][QF][3] */
-  double *face_w;      /* [faces][QF] */
-  double *face_frame;  /* [faces][QF][9] */
-  int16_t *map_h, *map_s; /* [faces][QF] */
-};
+/* struct orc_mesh: orc_internal.h */
 
 int64_t orc_column_size(const orc_mesh *m) { return m->n_cells * m->n * K; }
 int orc_mesh_degree(const orc_mesh *m) { return m->p; }
@@ -493,7 +493,7 @@ void orc_mesh_set_scheme(orc_mesh *m, int scheme) { m->scheme = scheme; }
 /* Vincent::LocalToRightDerivative(1) with c_next = HuynhLumpingLobatto(p)
  * (basis/vincent.hpp:30-32, 73-89): Legendre derivatives by the recurrence
  * P'_{k+1}(x) = (k+1) P_k(x) + x P'_k(x) at x = 1, where P_k(1) = 1. */
-static double fr_g_prime(int p) {
+double orc_fr_g_prime(int p) {
   double c_next = p / (2.0 * p + 1), c_prev = 1 - c_next;
   double prev = 0, curr = 0, next = 0;
   for (int k = 0; k <= p; ++k) {
@@ -514,7 +514,7 @@ static int fr_residual(const orc_mesh *m, int riemann, int n_bc,
   const int Q = m->q, N = m->n, QF = m->qf, KN = K * m->n;
   int64_t L = orc_column_size(m);
   memset(r, 0, sizeof(double) * L);
-  const double g1 = fr_g_prime(m->p);
+  const double g1 = orc_fr_g_prime(m->p);
   double *cflux = (double *)malloc(sizeof(double) * m->n_cells * N * 15);
   /* AddFluxDivergence */
 #pragma omp parallel for schedule(static) num_threads(orc_get_threads())
@@ -552,6 +552,8 @@ static int fr_residual(const orc_mesh *m, int riemann, int n_bc,
     int64_t h = m->face_cells[f * 2], s = m->face_cells[f * 2 + 1];
     int g = m->face_group[f];
     if (s < 0 && !(g >= 0 && g < n_bc && bcs[g].kind != ORC_BC_NONE)) continue;
+    /* a no-slip wall without viscosity: zero correction (fr/general.hpp:455-459) */
+    if (s < 0 && bcs[g].kind == ORC_BC_NO_SLIP_WALL) continue;
     int sh = m->face_sides[f * 2], ss = s >= 0 ? m->face_sides[f * 2 + 1] : 0;
     for (int fp = 0; fp < QF; ++fp) {
       const double *fr = &m->face_frame[(f * QF + fp) * 9];

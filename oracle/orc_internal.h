@@ -7,6 +7,41 @@
 
 #include "orc.h"
 
+#define ORC_MAXQ 6
+
+/* Mesh of the nodal schemes (built by orc_mesh_create, orc_dg.c). */
+struct orc_mesh {
+  int p, q, n, qf; /* degree, line points, nodes per cell, points per face */
+  int64_t n_cells, n_faces;
+  double xq[ORC_MAXQ], wq[ORC_MAXQ], d[ORC_MAXQ * ORC_MAXQ];
+  /* per cell */
+  double *node_xyz;   /* [cells][N][3] */
+  double *node_w;     /* [cells][N]  global weights */
+  double *grad;       /* [cells][N][3][N]  basis global gradients */
+  double *length;     /* [cells] */
+  double *cell_center; /* [cells][3] Hex8 LocalToGlobal(0, 0, 0) */
+  double *corners;    /* [cells][27][3] node coordinates (the type's first n) */
+  int32_t *type;      /* [cells] ORC_CELL_HEX8 / HEX27 / HEX20 */
+  double *jdi;        /* [cells][N][9] det(J) J^-1 (GetJacobianAssociated) */
+  double *detj;       /* [cells][N] det(J) */
+  int32_t *face_sides; /* [faces][2] local face index in holder / sharer */
+  int scheme;          /* ORC_SCHEME_DGSEM or ORC_SCHEME_FR */
+  /* per face */
+  int64_t *face_cells; /* [faces][2] */
+  int32_t *face_group; /* [faces] */
+  double *face_shift;  /* [faces][3] periodic shift (zeros when absent) */
+  double *face_xyz;    /* [faces][QF][3] */
+  double *face_w;      /* [faces][QF] */
+  double *face_frame;  /* [faces][QF][9] */
+  int16_t *map_h, *map_s; /* [faces][QF] */
+};
+
+/* Lagrange derivative of the FR correction at the right end, g_R'(1)
+ * (basis/vincent.hpp:30-32, 73-89). */
+double orc_fr_g_prime(int p);
+/* Lagrange second derivatives on the line points x [q]: d2[a * q + i] = l_i''(x_a). */
+void orc_lagrange_second(int q, const double *x, double *d2);
+
 int orc_mesh_degree(const orc_mesh *m);
 int64_t orc_mesh_cells(const orc_mesh *m);
 int64_t orc_mesh_faces(const orc_mesh *m);
