@@ -72,7 +72,11 @@ enum mcfd_bc_kind {
   MCFD_BC_SUPERSONIC_OUTLET = 3, /* SetSupersonicOutlet */
   MCFD_BC_SUBSONIC_INLET = 4,    /* SetSubsonicInlet(p0, cos x/y/z, T0) */
   MCFD_BC_SUBSONIC_OUTLET = 5,   /* SetSubsonicOutlet(value[4] = p) */
-  MCFD_BC_SMART = 6              /* SetSmartBoundary(value) */
+  MCFD_BC_SMART = 6,             /* SetSmartBoundary(value) */
+  MCFD_BC_NO_SLIP_WALL = 7       /* SetNoSlipWall (fem.hpp:213-219); MCFD_FR only: with
+                                    the artificial viscosity the wall flux minus
+                                    nu n . grad(u) (fr/general.hpp:460-476), without
+                                    it no correction (:455-459) */
 };
 
 /* The reference passes a std::function<Value(Global, double t)> per boundary
@@ -387,6 +391,34 @@ int mcfd_read_restart(mcfd_handle *h, const char *path, double *t);
  * current solution with the handle's limiter (no-op when none is set).
  * *troubled (may be NULL) receives the number of reconstructed cells. */
 int mcfd_limit(mcfd_handle *h, int64_t *troubled);
+
+/* Energy-based artificial viscosity, the shock capturing of the reference's
+ * viscous demos: WithViscosity<fr::Lobatto<Part, EnergyBasedViscosity<Part,
+ * ConvectionDiffusion<Riemann, Direct<Isotropic>>>>> (spatial/viscosity.hpp:
+ * 35-602, spatial/with_viscosity.hpp:20-72, riemann/diffusive/direct.hpp).
+ * Replaces Direct::SetBetaValues(ddg_beta0, ddg_beta1),
+ * EnergyBasedViscosity::SetTimeScale(time_scale) and the construction of
+ * WithViscosity (demo/euler/sourceless.cpp:117-121).  From then on every
+ * residual, stage and time step of the handle uses the viscosities of its
+ * own input state (SetSolutionColumn runs UpdateProperties) and
+ * mcfd_time_step returns min(2 cfl min_dt, dt_guess).  Needs MCFD_FR, the
+ * plain FP64 form, no limiter, no cases and Hex8 cells
+ * (MCFD_ERR_UNSUPPORTED otherwise). */
+int mcfd_set_viscosity(mcfd_handle *h, double ddg_beta0, double ddg_beta1, double time_scale);
+
+/* The viscosity of every cell and component, [cells][5], of the current
+ * solution (GetPropertyOnCell(cell, 0), the demos' CellViscosity fields). */
+int mcfd_get_viscosity(mcfd_handle *h, double *nu, int64_t n);
+
+/* Initial limiters of the viscous demos on the current solution of a nodal
+ * handle (sourceless.cpp:146-153): MCFD_INIT_AVERAGE sets every node to the
+ * cell average (limiter/average.hpp:11-28); MCFD_INIT_MAJORITY sets every
+ * node to the value a strict majority of the cell's nodes hold, per
+ * component (limiter/majority.hpp:14-42; no-op for p < 2).  A cell with a
+ * component without such a value stays unchanged and the call returns
+ * MCFD_ERR_STATE after treating the others. */
+enum mcfd_initial_limiter_kind { MCFD_INIT_AVERAGE = 1, MCFD_INIT_MAJORITY = 2 };
+int mcfd_initial_limiter(mcfd_handle *h, int32_t kind);
 
 /* Cells reconstructed by limiter passes since the last call (reset on read). */
 int mcfd_troubled_cells(mcfd_handle *h, int64_t *count);

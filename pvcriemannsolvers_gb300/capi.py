@@ -19,7 +19,8 @@ ERR_ARGUMENT, ERR_MESH, ERR_CUDA, ERR_STATE, ERR_NOT_CONVERGED, ERR_UNSUPPORTED,
 EXACT, HLLC, AUSM, ROE, RUSANOV = range(5)
 RIEMANN = {"exact": EXACT, "hllc": HLLC, "ausm": AUSM, "roe": ROE, "rusanov": RUSANOV}
 BC_NONE, BC_INVISCID_WALL, BC_SUPERSONIC_INLET, BC_SUPERSONIC_OUTLET, BC_SUBSONIC_INLET, \
-    BC_SUBSONIC_OUTLET, BC_SMART = range(7)
+    BC_SUBSONIC_OUTLET, BC_SMART, BC_NO_SLIP_WALL = range(8)
+INIT_AVERAGE, INIT_MAJORITY = 1, 2
 STATE_CONSTANT, STATE_MOVING_SPLIT = 0, 1
 HEX8, TET4 = 0, 1
 DGSEM, FR, MODAL = 0, 1, 2
@@ -134,6 +135,9 @@ SIGNATURES = {
     "mcfd_launch_count": (C.c_int64, [_P]),
     "mcfd_kernel_times": (C.c_int, [_P, C.c_int32, _D]),
     "mcfd_limit": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "mcfd_set_viscosity": (C.c_int, [_P, C.c_double, C.c_double, C.c_double]),
+    "mcfd_get_viscosity": (C.c_int, [_P, _D, C.c_int64]),
+    "mcfd_initial_limiter": (C.c_int, [_P, C.c_int32]),
     "mcfd_troubled_cells": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "mcfd_set_cases": (C.c_int, [_P, C.c_int32, C.POINTER(C.c_int64)]),
     "mcfd_case_times": (C.c_int, [_P, _D, _D, C.c_int32]),

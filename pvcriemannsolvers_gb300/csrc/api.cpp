@@ -187,6 +187,8 @@ void release(mcfd_handle *h) {
                    md.s32, md.vol32, md.foff32, md.taylor32};
   for (void *p : mptrs)
     if (p) cudaFree(p);
+  mcfd::release_viscosity(h);
+  if (h->mesh.node_w) cudaFree(h->mesh.node_w);
   mcfd::drop_graphs(h);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
 }
@@ -223,7 +225,9 @@ int upload_corners(mcfd_handle *h, const mcfd_mesh_desc *d) {
     }
   }
   int rc = upload(h, &h->mesh.corners, corners);
-  return rc ? rc : upload(h, &h->mesh.cell_type, types);
+  if (!rc) rc = upload(h, &h->mesh.cell_type, types);
+  m.host_corners = std::move(corners);
+  return rc;
 }
 
 int check_status(mcfd_handle *h) {
@@ -347,6 +351,9 @@ int build_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
   std::vector<int32_t> cflux((size_t)d->n_cells * 6 * QF, INT32_MIN);
   int max_group = -1;
   std::string mesh_error;
+  m.host_face_sides.assign((size_t)d->n_faces * 2, -1);
+  if (d->face_shift) m.host_shift.assign(d->face_shift, d->face_shift + d->n_faces * 3);
+  else m.host_shift.clear();
   for (int64_t f = 0; f < d->n_faces; ++f) {
     int64_t hc = d->face_cells[f * 2], sc = d->face_cells[f * 2 + 1];
     int sh = d->face_sides[f * 2], ss = d->face_sides[f * 2 + 1];
@@ -356,6 +363,8 @@ int build_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
     }
     fcells[f] = make_int2((int)hc, (int)sc);
     fgroup[f] = d->face_group ? d->face_group[f] : -1;
+    m.host_face_sides[f * 2] = (int8_t)sh;
+    m.host_face_sides[f * 2 + 1] = (int8_t)(sc >= 0 ? ss : -1);
     if (sc < 0) max_group = std::max(max_group, fgroup[f]);
   }
   m.n_groups = max_group + 1;
@@ -886,7 +895,9 @@ int mcfd_set_bc(mcfd_handle *h, int32_t group, const mcfd_bc_state *s) {
   if (!h || !s) return MCFD_ERR_ARGUMENT;
   if (group < 0 || group >= h->mesh.n_groups)
     return fail(h, MCFD_ERR_ARGUMENT, "boundary group out of range");
-  if (s->kind < MCFD_BC_NONE || s->kind > MCFD_BC_SMART ||
+  if (s->kind == MCFD_BC_NO_SLIP_WALL && h->opt.scheme != MCFD_FR)
+    return fail(h, MCFD_ERR_UNSUPPORTED, "no-slip walls run on the fr::Lobatto scheme only");
+  if (s->kind < MCFD_BC_NONE || s->kind > MCFD_BC_NO_SLIP_WALL ||
       (s->program != MCFD_STATE_CONSTANT && s->program != MCFD_STATE_MOVING_SPLIT) ||
       s->axis < 0 || s->axis > 2)
     return fail(h, MCFD_ERR_ARGUMENT, "bad boundary description");
@@ -952,6 +963,91 @@ int mcfd_limit(mcfd_handle *h, int64_t *troubled) {
   return MCFD_OK;
 }
 
+int mcfd_set_viscosity(mcfd_handle *h, double ddg_beta0, double ddg_beta1, double time_scale) {
+  if (!h) return MCFD_ERR_ARGUMENT;
+  if (!std::isfinite(ddg_beta0) || !std::isfinite(ddg_beta1) || !std::isfinite(time_scale))
+    return fail(h, MCFD_ERR_ARGUMENT, "viscosity parameters must be finite");
+  if (h->opt.scheme != MCFD_FR)
+    return fail(h, MCFD_ERR_UNSUPPORTED, "the artificial viscosity runs on the fr::Lobatto scheme (MCFD_FR)");
+  if (h->opt.precision != MCFD_FP64)
+    return fail(h, MCFD_ERR_UNSUPPORTED, "the artificial viscosity runs in the plain FP64 form");
+  if (h->lim.kind != MCFD_LIMITER_NONE)
+    return fail(h, MCFD_ERR_UNSUPPORTED, "a handle has either a limiter or the artificial viscosity");
+  if (h->cases.n)
+    return fail(h, MCFD_ERR_UNSUPPORTED, "the artificial viscosity takes a handle without cases");
+  for (uint8_t t : h->mesh.host_cell_type)
+    if (t != MCFD_HEX8) return fail(h, MCFD_ERR_UNSUPPORTED, "the artificial viscosity takes Hex8 cells");
+  cudaSetDevice(h->device);
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  const int rc = mcfd::build_viscosity(h, ddg_beta0, ddg_beta1, time_scale);
+  if (rc) return fail(h, rc, h->err);
+  // the viscous face kernel evaluates its own states: no Rusanov node traces
+  h->use_trace = false;
+  h->trace_for = nullptr;
+  mcfd::drop_graphs(h);
+  return MCFD_OK;
+}
+
+int mcfd_get_viscosity(mcfd_handle *h, double *nu, int64_t n) {
+  if (!h || !nu) return MCFD_ERR_ARGUMENT;
+  if (!h->visc.on) return fail(h, MCFD_ERR_ARGUMENT, "no artificial viscosity on this handle");
+  if (n != h->mesh.n_cells * mcfd::kK) return fail(h, MCFD_ERR_ARGUMENT, "viscosity array length mismatch");
+  cudaSetDevice(h->device);
+  h->launches += mcfd::launch_visc_properties(h, h->buf.u, 0);
+  CUDA_TRY(h, cudaMemcpyAsync(nu, h->visc.nu, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
+  return check_status(h);
+}
+
+int mcfd_initial_limiter(mcfd_handle *h, int32_t kind) {
+  if (!h) return MCFD_ERR_ARGUMENT;
+  if (kind != MCFD_INIT_AVERAGE && kind != MCFD_INIT_MAJORITY)
+    return fail(h, MCFD_ERR_ARGUMENT, "unknown initial limiter");
+  if (h->opt.scheme == mcfd::kSchemeModal)
+    return fail(h, MCFD_ERR_UNSUPPORTED, "the initial limiters take the nodal schemes");
+  cudaSetDevice(h->device);
+  auto &m = h->mesh;
+  if (kind == MCFD_INIT_MAJORITY && m.p < 2) return MCFD_OK;
+  if (kind == MCFD_INIT_AVERAGE && !m.node_w) {
+    // global weights w_i w_j w_k det(J) of every node (integrator/element.hpp:102-115)
+    const int Q = m.q, N = m.n;
+    double xq[4], wq[4];
+    gll(Q, xq, wq);
+    std::vector<double> w((size_t)m.n_cells * N);
+    for (int64_t c = 0; c < m.n_cells; ++c) {
+      const int t = m.host_cell_type[c];
+      for (int i = 0; i < Q; ++i)
+        for (int j = 0; j < Q; ++j)
+          for (int k = 0; k < Q; ++k) {
+            double x[3], J[9];
+            if (t == MCFD_HEX8) {
+              hex8_point(&m.host_corners[c * 24], xq[i], xq[j], xq[k], x, J);
+            } else {
+              const double loc[3] = {xq[i], xq[j], xq[k]};
+              mcfd::geo::map_point(t, &m.host_nodes[(size_t)c * mcfd::geo::kMaxNodes * 3], loc, x, J);
+            }
+            const double det = J[0] * (J[4] * J[8] - J[5] * J[7]) - J[1] * (J[3] * J[8] - J[5] * J[6]) +
+                               J[2] * (J[3] * J[7] - J[4] * J[6]);
+            w[(size_t)c * N + (i * Q + j) * Q + k] = wq[i] * wq[j] * wq[k] * det;
+          }
+    }
+    int rc = upload(h, &m.node_w, w);
+    if (rc) return rc;
+  }
+  unsigned long long *missing = nullptr, count = 0;
+  CUDA_TRY(h, cudaMalloc(&missing, sizeof(unsigned long long)));
+  cudaMemsetAsync(missing, 0, sizeof(unsigned long long), h->stream);
+  h->launches += mcfd::launch_initial_limiter(h, kind, h->buf.u, missing);
+  mcfd::invalidate_trace(h, h->buf.u);
+  cudaMemcpyAsync(&count, missing, sizeof(count), cudaMemcpyDeviceToHost, h->stream);
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  cudaFree(missing);
+  if (e != cudaSuccess) return cuda_fail(h, e, "initial limiter");
+  if (count)
+    return fail(h, MCFD_ERR_STATE, std::to_string(count) +
+                " cells have a component without a strict majority value (left unchanged)");
+  return check_status(h);
+}
+
 int mcfd_troubled_cells(mcfd_handle *h, int64_t *count) {
   if (!h || !count) return MCFD_ERR_ARGUMENT;
   *count = 0;
@@ -1005,6 +1101,8 @@ int mcfd_residual_device_noalloc(mcfd_handle *h, const double *d_u,
   if (n != h->mesh.column) return fail(h, MCFD_ERR_ARGUMENT, "column size mismatch");
   if (h->opt.scheme == MCFD_MODAL)
     return fail(h, MCFD_ERR_UNSUPPORTED, "the no-allocation residual covers the nodal schemes");
+  if (h->visc.on)
+    return fail(h, MCFD_ERR_UNSUPPORTED, "the no-allocation residual does not cover the artificial viscosity");
   if (h->mesh.n_points * mcfd::kK > mcfd::kStaticFluxCapacity)
     return fail(h, MCFD_ERR_ARGUMENT,
                 "mesh too large for the no-allocation residual: " +
@@ -1513,6 +1611,7 @@ int64_t mcfd_launch_count(const mcfd_handle *h) { return h ? h->launches : -1; }
 
 int mcfd_set_cases(mcfd_handle *h, int32_t n_cases, const int64_t *case_offsets) {
   if (!h || n_cases < 1 || !case_offsets) return MCFD_ERR_ARGUMENT;
+  if (h->visc.on) return fail(h, MCFD_ERR_UNSUPPORTED, "cases take a handle without the artificial viscosity");
   const int64_t C = h->mesh.n_cells;
   if (n_cases > 1024) return fail(h, MCFD_ERR_UNSUPPORTED, "at most 1024 cases per handle");
   if (case_offsets[0] != 0 || case_offsets[n_cases] != C)

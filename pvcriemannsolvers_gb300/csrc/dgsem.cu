@@ -92,6 +92,7 @@ struct CellArgs {
   double g1;  // FR: g_R'(1) of the Huynh g2 correction
   CaseView cs;
   double *trace;  // write the node traces of u_out here (surface nodes), or null
+  const double *nu;  // artificial viscosity [cells][K] (VISC variant), else null
 };
 
 // Step of the case that owns cell c (the handle's step without cases).
@@ -181,7 +182,8 @@ __global__ void __launch_bounds__(512) face_flux_kernel(FaceArgs a) {
   } else {
     Prim l = cons_to_prim(ch[0], ch[1], ch[2], ch[3], ch[4]);
     int grp = a.face_group[f];
-    if (grp >= 0 && grp < a.n_groups && a.bcs[grp].kind != kBcNone) {
+    if (grp >= 0 && grp < a.n_groups && a.bcs[grp].kind != kBcNone &&
+        a.bcs[grp].kind != kBcNoSlipWall) {
       const BcDev &bc = a.bcs[grp];
       double t = stage_time(a.cs, a.state, cells.x, a.stage_c);
       double given[kK];
@@ -199,13 +201,17 @@ __global__ void __launch_bounds__(512) face_flux_kernel(FaceArgs a) {
   store_flux(a.flux, a.f32_out, gid, out);
 }
 
-template <int Q, int STAGE>
+// VISC: fr::Lobatto with the energy-based artificial viscosity: the volume
+// flux carries -nu_k grad(u_k) (spatial/fem.hpp:393-403), so every node also
+// needs its gradient, from the cell's states staged in shared memory.
+template <int Q, int STAGE, bool VISC = false>
 __global__ void __launch_bounds__(CellCfg<Q>::kThreads)
 cell_update_kernel(CellArgs a) {
   constexpr int N = Q * Q * Q, QF = Q * Q, KN = kK * N;
   constexpr int CPB = CellCfg<Q>::kCells;
   __shared__ double s_ft[CPB][15][N];
   __shared__ double s_d[Q * Q];
+  __shared__ double s_u[VISC ? CPB : 1][VISC ? KN : 1];
   const int tid = threadIdx.x;
   if (tid < Q * Q) s_d[tid] = a.dmat[tid];
   const int lc = tid / N, q = tid - lc * N;
@@ -216,6 +222,13 @@ cell_update_kernel(CellArgs a) {
     const double *up = a.u_in + c * KN + q * kK;
 #pragma unroll
     for (int k = 0; k < kK; ++k) uq[k] = up[k];
+    if constexpr (VISC) {
+#pragma unroll
+      for (int k = 0; k < kK; ++k) s_u[lc][q * kK + k] = uq[k];
+    }
+  }
+  if constexpr (VISC) __syncthreads();
+  if (active) {
     const double *geo = a.cell_geo + (c * N + q) * 10;
     double A[9];
 #pragma unroll
@@ -240,6 +253,30 @@ cell_update_kernel(CellArgs a) {
       ft[2 * 3 + e] = uq[2] * ve + w.p * A[1 * 3 + e];
       ft[3 * 3 + e] = uq[3] * ve + w.p * A[2 * 3 + e];
       ft[4 * 3 + e] = (uq[4] + w.p) * ve;
+    }
+    if constexpr (VISC) {
+      // -nu_k grad(u_k), grad = det(J)^-1 adj(J) g_local, in contravariant form
+      const int i = q / QF, j = (q / Q) % Q, l = q % Q;
+      const double inv_det = geo[9];
+      const double *nu = a.nu + c * kK;
+#pragma unroll
+      for (int r = 0; r < kK; ++r) {
+        double g0 = 0, g1 = 0, g2 = 0;
+#pragma unroll
+        for (int m = 0; m < Q; ++m) {
+          g0 += s_d[i * Q + m] * s_u[lc][((m * Q + j) * Q + l) * kK + r];
+          g1 += s_d[j * Q + m] * s_u[lc][((i * Q + m) * Q + l) * kK + r];
+          g2 += s_d[l * Q + m] * s_u[lc][((i * Q + j) * Q + m) * kK + r];
+        }
+        double gu[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+          gu[d] = inv_det * (A[d * 3 + 0] * g0 + A[d * 3 + 1] * g1 + A[d * 3 + 2] * g2);
+        const double nr = nu[r];
+#pragma unroll
+        for (int e = 0; e < 3; ++e)
+          ft[r * 3 + e] -= nr * (gu[0] * A[0 * 3 + e] + gu[1] * A[1 * 3 + e] + gu[2] * A[2 * 3 + e]);
+      }
     }
 #pragma unroll
     for (int r = 0; r < 15; ++r) s_ft[lc][r][q] = ft[r];
@@ -685,7 +722,10 @@ template <int Q, int S>
 void cell_launch(mcfd_handle *h, const CellArgs &ca) {
   constexpr int CPB = CellCfg<Q>::kCells;
   int64_t blocks = (ca.n_cells + CPB - 1) / CPB;
-  cell_update_kernel<Q, S><<<(unsigned)blocks, CellCfg<Q>::kThreads, 0, h->stream>>>(ca);
+  if (ca.nu)
+    cell_update_kernel<Q, S, true><<<(unsigned)blocks, CellCfg<Q>::kThreads, 0, h->stream>>>(ca);
+  else
+    cell_update_kernel<Q, S><<<(unsigned)blocks, CellCfg<Q>::kThreads, 0, h->stream>>>(ca);
 }
 
 template <int Q, int S>
@@ -740,6 +780,9 @@ int launch_set_state(mcfd_handle *h, double t, double dt, double dt_guess,
 
 int launch_face_flux(mcfd_handle *h, const double *u, double stage_c) {
   if (h->opt.scheme == kSchemeModal) return launch_modal_face_flux(h, u, stage_c);
+  // viscosity: the properties of this stage input first (SetSolutionColumn
+  // runs UpdateProperties, with_viscosity.hpp:56-59)
+  if (h->visc.on) return launch_visc_properties(h, u, 0) + launch_visc_face_flux(h, u, stage_c);
   const Mesh &m = h->mesh;
   FaceArgs fa{u, m.face_cells, m.face_group, m.face_geo, m.face_xyz,
               m.face_map, m.bcs, h->buf.flux, h->buf.state, stage_c,
@@ -763,7 +806,7 @@ int launch_cell_update(mcfd_handle *h, int stage, const double *u_in,
   double *trace = (h->use_trace && stage != kStageResidual) ? h->buf.trace : nullptr;
   CellArgs ca{u_in, u0, u_out, m.cell_geo, m.cell_flux, h->buf.flux, m.dmat,
               h->buf.state, m.n_cells, advance_time, h->opt.scheme == 1, h->opt.fr_g1,
-              case_view(h), trace};
+              case_view(h), trace, h->visc.on ? h->visc.nu : nullptr};
   if (trace) h->trace_for = u_out;
   switch (m.q) {
     case 2: cell_dispatch_s<2>(h, stage, ca); break;
@@ -787,6 +830,7 @@ int launch_dt_finalize(mcfd_handle *h) {
 
 int launch_dt(mcfd_handle *h, const double *u) {
   if (h->opt.scheme == kSchemeModal) return launch_modal_dt(h, u);
+  if (h->visc.on) return launch_visc_properties(h, u, 1) + launch_visc_dt_finalize(h);
   const Mesh &m = h->mesh;
   int64_t nodes = m.n_cells * m.n;
   const int bs = h->tune.dt_block;
@@ -882,7 +926,8 @@ int launch_residual_static_scratch(mcfd_handle *h, const double *d_u,
               m.n_points, m.n_groups, h->opt.scheme == 1, case_view(h), nullptr,
               h->opt.precision == 1};
   CellArgs ca{d_u, nullptr, d_r, m.cell_geo, m.cell_flux, scratch, m.dmat,
-              h->buf.state, m.n_cells, 0, h->opt.scheme == 1, h->opt.fr_g1, case_view(h), nullptr};
+              h->buf.state, m.n_cells, 0, h->opt.scheme == 1, h->opt.fr_g1, case_view(h), nullptr,
+              nullptr};
   int n = 0;
   if (m.n_points > 0) {
     switch (m.q) {

@@ -49,7 +49,8 @@ enum Riemann { kExact = 0, kHllc = 1, kAusm = 2, kRoe = 3, kRusanov = 4 };
 enum BcKind {
   kBcNone = 0, kBcInviscidWall = 1, kBcSupersonicInlet = 2,
   kBcSupersonicOutlet = 3, kBcSubsonicInlet = 4, kBcSubsonicOutlet = 5,
-  kBcSmart = 6
+  kBcSmart = 6,
+  kBcNoSlipWall = 7  // viscous fr::Lobatto only (fr/general.hpp:455-476)
 };
 
 // Status bits raised by kernels (read back by the host).

@@ -23,6 +23,7 @@ struct DevState {
   unsigned long long max_rate_bits;  // max over cells of max_speed / length (bits of a positive double)
   unsigned int status;    // StatusBits
   unsigned int pad;
+  unsigned long long min_dt_bits;  // viscosity: min over cells of the stable step (bits of a positive double)
 };
 
 // One boundary group on the device (mirror of mcfd_bc_state).
@@ -73,6 +74,28 @@ struct Mesh {
   // host copies for parity queries
   std::vector<int16_t> map_h, map_s;
   std::vector<BcDev> host_bcs;
+  double *node_w = nullptr;         // [cells][N] global weights (initial limiters; built on first use)
+  std::vector<double> host_corners;  // [cells][8][3] (as uploaded to corners)
+  std::vector<double> host_shift;    // [faces][3] periodic shifts (empty: none)
+  std::vector<int8_t> host_face_sides;  // [faces][2] local face on the holder / sharer side
+};
+
+// Energy-based artificial viscosity on fr::Lobatto (spatial/viscosity.hpp,
+// spatial/with_viscosity.hpp, riemann/diffusive/direct.hpp), Hex8 cells.
+// Per stage a properties kernel turns the stage input into one viscosity per
+// cell and component and, for every face point side, the normal derivative
+// n . grad(u) and the normal curvature n^T H n that the DDG common gradient
+// needs; the face and cell kernels then add the viscous fluxes.
+struct Visc {
+  bool on = false;
+  double beta0 = 2.0, beta1 = 1.0 / 12, time_scale = 1.0;
+  double *nu = nullptr;     // [cells][K] viscosity of the last properties pass
+  double *trace = nullptr;  // [points][2 sides][2K]: n . grad(u_k), n^T H_k n
+  double *side = nullptr;   // [points][2 sides][6]: m = J^-T n, q (Hessian chain-rule term)
+  double *pt = nullptr;     // [points][4]: beta0 / d, beta1 d, w h_holder, w h_sharer
+  double *cell = nullptr;   // [cells][2]: length, length^(p + 4)
+  double *d2 = nullptr;     // [Q][Q] second derivatives l_i''(x_a)
+  double *wloc = nullptr;   // [N] local GLL weights of the nodes
 };
 
 // Device tables of the WENO limiter (built when a limiter is requested).
@@ -208,6 +231,7 @@ struct mcfd_handle {
   mcfd::Limiter lim;
   mcfd::Modal modal;
   mcfd::Cases cases;
+  mcfd::Visc visc;
   double t_host = 0;
   int64_t launches = 0;
   bool use_trace = false;            // see Buffers::trace
@@ -279,6 +303,19 @@ int launch_modal_dt(mcfd_handle *h, const double *u);
 int launch_modal_project(mcfd_handle *h, double *u);
 // Host set-up of the modal tables (modal_setup.cpp); returns an mcfd status.
 int build_modal_mesh(mcfd_handle *h, const ::mcfd_mesh_desc *d, int degree);
+
+// Artificial viscosity (viscosity.cu / visc_setup.cpp).  The properties
+// pass writes Visc::nu and Visc::trace from the state u; with dt_mode it also
+// folds every cell's stable step into DevState::min_dt_bits, and
+// launch_visc_dt turns that into the step (with_viscosity.hpp:67-71).
+int build_viscosity(mcfd_handle *h, double beta0, double beta1, double time_scale);
+void release_viscosity(mcfd_handle *h);
+int launch_visc_properties(mcfd_handle *h, const double *u, int dt_mode);
+int launch_visc_face_flux(mcfd_handle *h, const double *u, double stage_c);
+int launch_visc_dt_finalize(mcfd_handle *h);
+// Initial limiters of the viscous demos (limiter/average.hpp,
+// limiter/majority.hpp), in place; majority counts the cells without one.
+int launch_initial_limiter(mcfd_handle *h, int kind, double *u, unsigned long long *missing);
 
 // Residual whose face-flux scratch is a fixed file-scope device array
 // (mcfd_residual_device_noalloc).  Capacity in doubles: 2 Mi = 16 MiB, i.e.

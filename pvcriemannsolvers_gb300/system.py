@@ -171,6 +171,29 @@ class Lobatto:
     def SetSmartBoundary(self, group: int, value) -> None:
         self._check(self._lib.mcfd_set_bc(self._h, group, C.byref(_bc_state(capi.BC_SMART, value))))
 
+    def SetNoSlipWall(self, group: int) -> None:
+        """fr::Lobatto only; with the artificial viscosity the wall flux minus
+        nu n . grad(u) (fr/general.hpp:460-476), without it no correction."""
+        self._check(self._lib.mcfd_set_bc(self._h, group, C.byref(_bc_state(capi.BC_NO_SLIP_WALL, None))))
+
+    # -- energy-based artificial viscosity (spatial/viscosity.hpp, with_viscosity.hpp)
+    def SetViscosity(self, ddg_beta0: float = 2.0, ddg_beta1: float = 1.0 / 12, time_scale: float = 1.0) -> None:
+        """Direct::SetBetaValues + EnergyBasedViscosity::SetTimeScale + the
+        WithViscosity construction (demo/euler/sourceless.cpp:117-121)."""
+        self._check(self._lib.mcfd_set_viscosity(self._h, float(ddg_beta0), float(ddg_beta1), float(time_scale)))
+
+    def GetViscosity(self) -> np.ndarray:
+        """[cells, 5] viscosity of the current solution (GetPropertyOnCell)."""
+        out = np.empty((self.mesh.n_cells, 5), dtype=np.float64)
+        self._check(self._lib.mcfd_get_viscosity(self._h, capi.dptr(out), out.size))
+        return out
+
+    def InitialLimiter(self, kind: str) -> None:
+        """limiter::average ("average") or limiter::majority ("majority")
+        Reconstruct on the current solution."""
+        code = {"average": capi.INIT_AVERAGE, "majority": capi.INIT_MAJORITY}[kind]
+        self._check(self._lib.mcfd_initial_limiter(self._h, code))
+
     # -- System quartet (ode.hpp:17-48)
     def SetTime(self, t_curr: float) -> None:
         self._check(self._lib.mcfd_set_time(self._h, float(t_curr)))
