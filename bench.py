@@ -1079,6 +1079,176 @@ def run_sod(args, rank, world, local_rank):
 
 
 # ---------------------------------------------------------------------------
+# Energy-based artificial viscosity on fr::Lobatto (the reference's default
+# shock capturing in its viscous demos: demo/euler/sourceless.hpp FR +
+# VISCOSITY, Exact Riemann solver, DDG beta0 = 2, beta1 = 0.0833333333,
+# time_scale = 0.05 from riemann2d.json / shock_tube_sod.json).
+#   value: the four-quadrant demo (riemann2d, average initial limiter) on the
+#          four-quadrant mesh, SSP-RK3 with the viscous time step
+#   sod:   the Sod demo (majority initial limiter) on the 100x4x4 tube to
+#          t = 0.2, GPU time to solution against the oracle's
+
+VISC_BETA0, VISC_BETA1, VISC_TIME_SCALE = 2.0, 0.0833333333, 0.05
+VISC_SAMPLE = (48, 48, 2)
+
+
+def viscous_cpu_sample(seconds=12.0, threads=None):
+    """The oracle (EnergyBasedViscosity on fr::Lobatto) on a slice of the
+    four-quadrant demo; the damping matrices are built before the clock."""
+    import oracle.orc as orc
+    from pvcriemannsolvers_gb300 import cases, mesh as meshlib
+    orc.build()
+    threads = threads or os.cpu_count() or 1
+    orc.set_threads(threads)
+    m = cases.quadrant_mesh(*VISC_SAMPLE)
+    om = orc.Mesh(m, QUAD_DEGREE, scheme="fr")
+    om.set_bcs(quadrant_oracle_bcs())
+    ov = orc.Viscosity(om, VISC_BETA0, VISC_BETA1, VISC_TIME_SCALE)
+    u, _ = orc.initial_limiter(om, orc.INIT_AVERAGE,
+                               cases.quadrant_ic(meshlib.node_coordinates(m, QUAD_DEGREE).reshape(-1, 3)).ravel())
+    t, n, t0 = 0.0, 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds or n == 0:
+        dt = ov.time_step(u, 1.0, 3)
+        u = ov.rk_update(orc.EXACT, 3, t, dt, u)
+        t += dt
+        n += 1
+    el = time.perf_counter() - t0
+    return {"value": 3 * u.size * n / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{VISC_SAMPLE[0]}x{VISC_SAMPLE[1]}x{VISC_SAMPLE[2]} cells of the same case "
+                      f"(L = {u.size} DOFs), {n} SSP-RK3 steps with viscous time steps, {el:.1f} s, "
+                      f"oracle (OpenMP over cells; the damping matrices are built before the clock)"}
+
+
+def run_viscous(args, rank, world, local_rank):
+    import torch
+    import oracle.orc as orc
+    from pvcriemannsolvers_gb300 import Lobatto, build, cases, mesh as meshlib
+    build.build()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    p = QUAD_DEGREE
+    # ---- four-quadrant demo with the viscosity
+    nx, ny, nz = args.quadrant_cells
+    m = cases.quadrant_mesh(nx, ny, nz)
+    u0 = np.ascontiguousarray(cases.quadrant_ic(meshlib.node_coordinates(m, p).reshape(-1, 3)).ravel())
+    L = u0.size
+    sysm = Lobatto(m, p, "exact", device=local_rank, scheme="fr")
+    cases.quadrant_bc(sysm)
+    sysm.SetViscosity(VISC_BETA0, VISC_BETA1, VISC_TIME_SCALE)
+    stream = torch.cuda.Stream(device=dev)
+    sysm.set_stream(stream.cuda_stream)
+    sysm.SetSolutionColumn(u0)
+    sysm.InitialLimiter("average")
+    t = sysm.advance(args.warmup, 1.0, 3, 0.0)
+    torch.cuda.synchronize(dev)
+    launches0 = sysm.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clocks:
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            t = sysm.advance(args.steps, 1.0, 3, t)
+            e1.record(stream)
+        e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = sysm.launch_count() - launches0
+    sol = sysm.GetSolutionColumn()
+    nu = sysm.GetViscosity()
+    kt = sysm.kernel_times(reps=3)
+    e2e_steps = max(1, min(args.steps, 10))
+    e2e_s, seq_s = e2e_runs(torch, dev, sysm, sol, t, e2e_steps, 1.0)
+    sysm.close()
+    value = 3 * L * args.steps / (ms * 1e-3)
+    fp64_peak = fp64_peak_tflops(torch, dev)
+    # ---- the Sod demo with the viscosity, to t = 0.2
+    ms_ = cases.sod_mesh()
+    us0 = np.ascontiguousarray(cases.sod_ic(meshlib.node_coordinates(ms_, p).reshape(-1, 3)).ravel())
+    Ls = us0.size
+    sod = Lobatto(ms_, p, "exact", device=local_rank, scheme="fr")
+    cases.sod_bc(sod)
+    sod.SetViscosity(VISC_BETA0, VISC_BETA1, VISC_TIME_SCALE)
+    sstream = torch.cuda.Stream(device=dev)
+    sod.set_stream(sstream.cuda_stream)
+    sod.SetSolutionColumn(us0)
+    sod.InitialLimiter("majority")
+    start = sod.GetSolutionColumn()
+    sod.advance(args.warmup, 1.0, 3, 0.0)
+    sod.SetSolutionColumn(start)
+    torch.cuda.synchronize(dev)
+    t_end, ts, n_sod = 0.2, 0.0, 0
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(sstream):
+        s0.record(sstream)
+        while ts < t_end - 1e-12:
+            ts = sod.advance(10, t_end - ts if t_end - ts < 1.0 else 1.0, 3, ts)
+            n_sod += 10
+        s1.record(sstream)
+    s1.synchronize()
+    sod_s = s0.elapsed_time(s1) * 1e-3
+    # oracle: parity of the first 5 steps from the same start, then a timing sample
+    orc.build()
+    threads = os.cpu_count() or 1
+    orc.set_threads(threads)
+    om = orc.Mesh(ms_, p, scheme="fr")
+    om.set_bcs({0: (orc.BC_SMART, cases.SOD_LEFT), 1: (orc.BC_SMART, cases.SOD_RIGHT),
+                2: (orc.BC_INVISCID_WALL, None), 3: (orc.BC_INVISCID_WALL, None),
+                4: (orc.BC_INVISCID_WALL, None), 5: (orc.BC_INVISCID_WALL, None)})
+    ov = orc.Viscosity(om, VISC_BETA0, VISC_BETA1, VISC_TIME_SCALE)
+    u = start.copy()
+    tt, n_cpu, t0 = 0.0, 0, time.perf_counter()
+    parity, n0, t0_cpu = None, 0, t0
+    while True:
+        dt = ov.time_step(u, 1.0, 3)
+        u = ov.rk_update(orc.EXACT, 3, tt, dt, u)
+        tt += dt
+        n_cpu += 1
+        if n_cpu == 5:
+            sod.SetSolutionColumn(start)
+            sod.advance(5, 1.0, 3, 0.0)
+            g = sod.GetSolutionColumn()
+            parity = float(np.linalg.norm(g - u) / np.linalg.norm(u))
+            t0_cpu, n0 = time.perf_counter(), n_cpu
+        if n_cpu >= 5 and (time.perf_counter() - t0 >= 12.0 or n_cpu >= n_sod):
+            break
+    cpu_sod_s = time.perf_counter() - t0_cpu
+    sod.close()
+    cpu = None
+    if not args.no_cpu:
+        cpu = viscous_cpu_sample()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"four-quadrant Riemann problem with energy-based artificial viscosity, "
+                               f"{nx}x{ny}x{nz} Hex8, fr::Lobatto p={p} (Huynh g2), Exact Riemann solver, "
+                               f"DDG beta0 = {VISC_BETA0}, beta1 = {VISC_BETA1}, time scale {VISC_TIME_SCALE}, "
+                               f"average initial limiter, SSP-RK3 with the viscous time step",
+                   "cells": m.n_cells, "dofs": L, "form": "plain FP64",
+                   "step": "viscosity properties + viscous dt + 3 x (properties + face flux + cell update)",
+                   "l2_flush": "inputs larger than L2 (solution column 1.13 GB)"},
+        "accuracy": {"t_end": t, "cells_with_viscosity": int((nu.max(axis=1) > 0).sum()),
+                     "max_viscosity": float(nu.max())},
+        "clocks": clocks.summary(),
+        "e2e": {"value": 3 * L * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * L,
+                "d2h_bytes_per_step": 8 * L, "steps": e2e_steps, "path": E2E_PATH,
+                "sequential": {"value": 3 * L * e2e_steps / seq_s, "path": E2E_SEQ_PATH}},
+        "gpu_launches": launches,
+        "sod": {"workload": "Sod shock tube 100x4x4 Hex8, fr::Lobatto p=2, Exact, the same viscosity, majority "
+                            "initial limiter, t = 0 -> 0.2",
+                "steps": n_sod, "t_end": ts, "gpu_s": sod_s, "value": 3 * Ls * n_sod / sod_s,
+                "cpu_oracle_extrapolated_s": n_sod * (cpu_sod_s / max(n_cpu - n0, 1)),
+                "cpu_sample": f"steps 6..{n_cpu}, {cpu_sod_s:.1f} s, {threads} threads",
+                "gpu_vs_oracle_rel_l2_after_5_steps": parity},
+        "roofline": {"bound": "fp64", "kernel": "step", "kernel_ms": kt, "peak": fp64_peak, "unit": "TFLOP/s",
+                     "achieved": None, "frac": None, "traffic": None,
+                     "peak_source": "measured in this run: cuBLAS DGEMM 4096^3",
+                     "note": "face_flux includes the viscosity properties pass of the stage"},
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
 # Output and restart on the headline mesh (64^3 Hex8, DGSEM p = 3, 83.9 M
 # values): the DataOnCells field transposition (Part::GatherSolutions /
 # ScatterSolutions) against HBM, the VTK sampling (Writer::Prepare) and the
@@ -1250,10 +1420,11 @@ def main():
     ap.add_argument("--form", default="both", choices=["both", "fp64", "mixed"],
                     help="precision form(s) to time; the line's value is the mixed form when timed")
     ap.add_argument("--workload", default="vortex",
-                    choices=["vortex", "mixed_box", "ensemble", "quadrant", "output", "reorder", "sod"],
+                    choices=["vortex", "mixed_box", "ensemble", "quadrant", "output", "reorder", "sod", "viscous"],
                     help="vortex: the headline DGSEM case; mixed_box: modal DG on hex + tet blocks; "
                          "ensemble: 64 independent cases in one graph per step; output: field "
-                         "gather/scatter, VTK sampling and restart on the headline column")
+                         "gather/scatter, VTK sampling and restart on the headline column; viscous: fr::Lobatto "
+                         "with the energy-based artificial viscosity (four-quadrant and Sod demos)")
     ap.add_argument("--quadrant-cells", type=int, nargs=3, default=[256, 256, 16], metavar=("NX", "NY", "NZ"),
                     help="mesh of the four-quadrant workload")
     ap.add_argument("--ensemble-scale", type=float, default=1.0,
@@ -1286,6 +1457,9 @@ def main():
         return
     if args.workload == "sod":
         run_sod(args, rank, world, local_rank)
+        return
+    if args.workload == "viscous":
+        run_viscous(args, rank, world, local_rank)
         return
     if world > 1:
         import torch

@@ -413,6 +413,7 @@ void orc_visc_properties(const orc_visc *v, const double *u, double *nu, double 
   double *jumps = (double *)malloc(sizeof(double) * m->n_cells * K);
   orc_visc_jumps(v, u, jumps);
   double min_dt = 1.e+100;
+#pragma omp parallel for schedule(static) reduction(min : min_dt) num_threads(orc_get_threads())
   for (int64_t c = 0; c < m->n_cells; ++c) {
     const double *uc = u + c * N * K;
     double max_speed = 1e-5, max_sq[K];
@@ -512,17 +513,21 @@ int orc_visc_residual(const orc_visc *v, int riemann, int n_bc, const orc_bc *bc
       for (int k = 0; k < K; ++k) r[c * KN + q * K + k] -= value[k];
     }
   }
-  /* face corrections (fr/lobatto.hpp:232-428 over fr/general.hpp:316-515) */
+  /* face corrections (fr/lobatto.hpp:232-428 over fr/general.hpp:316-515):
+   * the upwind fluxes of every face point in parallel, then the corrections
+   * in face order */
+  double *fup = (double *)malloc(sizeof(double) * (m->n_faces * QF * K + 1));
+  char *skip = (char *)calloc(m->n_faces + 1, 1);
+#pragma omp parallel for schedule(dynamic, 64) num_threads(orc_get_threads())
   for (int64_t f = 0; f < m->n_faces; ++f) {
     const int64_t h = m->face_cells[f * 2], s = m->face_cells[f * 2 + 1];
     const int g = m->face_group[f];
-    if (s < 0 && !(g >= 0 && g < n_bc && bcs[g].kind != ORC_BC_NONE)) continue;
-    const int sh = m->face_sides[f * 2], ss = s >= 0 ? m->face_sides[f * 2 + 1] : 0;
+    if (s < 0 && !(g >= 0 && g < n_bc && bcs[g].kind != ORC_BC_NONE)) { skip[f] = 1; continue; }
     for (int fp = 0; fp < QF; ++fp) {
       const double *fr = &m->face_frame[(f * QF + fp) * 9];
       const int nh = m->map_h[f * QF + fp];
       const double *uh = u + h * KN + nh * K;
-      double flux[K];
+      double *flux = &fup[(f * QF + fp) * K];
       if (s >= 0) {
         const int ns = m->map_s[f * QF + fp];
         const double *us = u + s * KN + ns * K;
@@ -554,6 +559,15 @@ int orc_visc_residual(const orc_visc *v, int riemann, int n_bc, const orc_bc *bc
         given_value(&bcs[g], &m->face_xyz[(f * QF + fp) * 3], t, given);
         orc_flux_boundary(riemann, bcs[g].kind, fr, uh, given, flux);
       }
+    }
+  }
+  for (int64_t f = 0; f < m->n_faces; ++f) {
+    if (skip[f]) continue;
+    const int64_t h = m->face_cells[f * 2], s = m->face_cells[f * 2 + 1];
+    const int sh = m->face_sides[f * 2], ss = s >= 0 ? m->face_sides[f * 2 + 1] : 0;
+    for (int fp = 0; fp < QF; ++fp) {
+      const int nh = m->map_h[f * QF + fp];
+      const double *flux = &fup[(f * QF + fp) * K];
       {
         const double *jd = &m->jdi[(h * N + nh) * 9];
         const int dir = kDir[sh];
@@ -579,6 +593,8 @@ int orc_visc_residual(const orc_visc *v, int riemann, int n_bc, const orc_bc *bc
       }
     }
   }
+  free(fup);
+  free(skip);
   free(cflux);
 #pragma omp parallel for schedule(static) num_threads(orc_get_threads())
   for (int64_t c = 0; c < m->n_cells; ++c)

@@ -1157,7 +1157,7 @@ static int ensure_step_graph(mcfd_handle *h, int32_t rk_order) {
     cudaGraph_t graph;
     CUDA_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     int n = mcfd::launch_dt(h, h->buf.u);
-    n += mcfd::launch_rk_stage_sequence(h, rk_order);
+    n += mcfd::launch_rk_stage_sequence(h, rk_order, nullptr, nullptr, true);
     cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
     if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamEndCapture");
     e = cudaGraphInstantiate(&h->step_graph, graph, 0);
@@ -1183,7 +1183,7 @@ static int ensure_job_graph(mcfd_handle *h, int b, int32_t n_steps, int32_t rk_o
   for (int s = 0; s < n_steps; ++s) {
     const double *src = s == 0 ? st.in[b] : st.out[b];
     n += mcfd::launch_dt(h, src);
-    n += mcfd::launch_rk_stage_sequence(h, rk_order, src, st.out[b]);
+    n += mcfd::launch_rk_stage_sequence(h, rk_order, src, st.out[b], true);
   }
   cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
   if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamEndCapture");
@@ -1355,7 +1355,7 @@ int ens_ensure_graph(mcfd_ensemble *e, int32_t rk_order) {
     err = cudaStreamWaitEvent(h->stream, e->fork, 0);
     if (err != cudaSuccess) break;
     int k = mcfd::launch_dt(h, h->buf.u);
-    k += mcfd::launch_rk_stage_sequence(h, rk_order);
+    k += mcfd::launch_rk_stage_sequence(h, rk_order, nullptr, nullptr, true);
     e->kernels[i] = k;
     err = cudaEventRecord(e->join[i], h->stream);
     if (err == cudaSuccess) err = cudaStreamWaitEvent(e->stream, e->join[i], 0);

@@ -55,6 +55,7 @@ struct FaceArgs {
   CaseView cs;
   const double *trace;  // node traces of u (Rusanov), or null
   int f32_out;          // mixed form: the flux buffer holds FP32 values
+  int visc;             // artificial viscosity: no-slip walls take the wall flux
 };
 
 // Face-point flux store: FP64, or FP32 for the mixed form's FP32 lift (one
@@ -183,12 +184,14 @@ __global__ void __launch_bounds__(512) face_flux_kernel(FaceArgs a) {
     Prim l = cons_to_prim(ch[0], ch[1], ch[2], ch[3], ch[4]);
     int grp = a.face_group[f];
     if (grp >= 0 && grp < a.n_groups && a.bcs[grp].kind != kBcNone &&
-        a.bcs[grp].kind != kBcNoSlipWall) {
+        (a.bcs[grp].kind != kBcNoSlipWall || a.visc)) {
       const BcDev &bc = a.bcs[grp];
       double t = stage_time(a.cs, a.state, cells.x, a.stage_c);
       double given[kK];
       given_value(bc, a.face_xyz + gid * 3, t, given);
-      flux_boundary<R>(bc.kind, l, given, n, out, &not_converged);
+      // a no-slip wall's convective part is the inviscid wall flux
+      flux_boundary<R>(bc.kind == kBcNoSlipWall ? (int)kBcInviscidWall : bc.kind, l, given, n, out,
+                       &not_converged);
     } else {
 #pragma unroll
       for (int k = 0; k < kK; ++k) out[k] = 0;
@@ -254,11 +257,11 @@ cell_update_kernel(CellArgs a) {
       ft[3 * 3 + e] = uq[3] * ve + w.p * A[2 * 3 + e];
       ft[4 * 3 + e] = (uq[4] + w.p) * ve;
     }
-    if constexpr (VISC) {
+    const double *nu = VISC ? a.nu + c * kK : nullptr;
+    if (VISC && (nu[0] != 0 || nu[1] != 0 || nu[2] != 0 || nu[3] != 0 || nu[4] != 0)) {
       // -nu_k grad(u_k), grad = det(J)^-1 adj(J) g_local, in contravariant form
       const int i = q / QF, j = (q / Q) % Q, l = q % Q;
       const double inv_det = geo[9];
-      const double *nu = a.nu + c * kK;
 #pragma unroll
       for (int r = 0; r < kK; ++r) {
         double g0 = 0, g1 = 0, g2 = 0;
@@ -778,24 +781,27 @@ int launch_set_state(mcfd_handle *h, double t, double dt, double dt_guess,
   return 1;
 }
 
-int launch_face_flux(mcfd_handle *h, const double *u, double stage_c) {
+int launch_face_flux(mcfd_handle *h, const double *u, double stage_c, bool props_fresh) {
   if (h->opt.scheme == kSchemeModal) return launch_modal_face_flux(h, u, stage_c);
   // viscosity: the properties of this stage input first (SetSolutionColumn
   // runs UpdateProperties, with_viscosity.hpp:56-59)
-  if (h->visc.on) return launch_visc_properties(h, u, 0) + launch_visc_face_flux(h, u, stage_c);
+  int n = 0;
+  if (h->visc.on && !props_fresh) n += launch_visc_properties(h, u, 0);
   const Mesh &m = h->mesh;
   FaceArgs fa{u, m.face_cells, m.face_group, m.face_geo, m.face_xyz,
               m.face_map, m.bcs, h->buf.flux, h->buf.state, stage_c,
               m.n_points, m.n_groups, h->opt.scheme == 1, case_view(h),
               (h->use_trace && h->trace_for == u) ? h->buf.trace : nullptr,
-              h->opt.precision == 1};
-  if (m.n_points == 0) return 0;
+              h->opt.precision == 1, h->visc.on ? 1 : 0};
+  if (m.n_points == 0) return n;
   switch (m.q) {
     case 2: face_dispatch_r<2>(h, fa); break;
     case 3: face_dispatch_r<3>(h, fa); break;
     default: face_dispatch_r<4>(h, fa); break;
   }
-  return 1;
+  ++n;
+  if (h->visc.on) n += launch_visc_face_flux(h, u);
+  return n;
 }
 
 int launch_cell_update(mcfd_handle *h, int stage, const double *u_in,
@@ -924,7 +930,7 @@ int launch_residual_static_scratch(mcfd_handle *h, const double *d_u,
   FaceArgs fa{d_u, m.face_cells, m.face_group, m.face_geo, m.face_xyz,
               m.face_map, m.bcs, scratch, h->buf.state, 0.0,
               m.n_points, m.n_groups, h->opt.scheme == 1, case_view(h), nullptr,
-              h->opt.precision == 1};
+              h->opt.precision == 1, 0};
   CellArgs ca{d_u, nullptr, d_r, m.cell_geo, m.cell_flux, scratch, m.dmat,
               h->buf.state, m.n_cells, 0, h->opt.scheme == 1, h->opt.fr_g1, case_view(h), nullptr,
               nullptr};
@@ -948,7 +954,8 @@ int launch_residual_static_scratch(mcfd_handle *h, const double *d_u,
 // The stages of RungeKutta<order>::Update with the result left in buf.u.
 // Stage times: t, t + dt, t + dt/2 (rk.hpp:34-42).  The last stage also
 // advances the device time by dt.
-int launch_rk_stage_sequence(mcfd_handle *h, int order, const double *u_in, double *u_out) {
+int launch_rk_stage_sequence(mcfd_handle *h, int order, const double *u_in, double *u_out,
+                             bool after_dt) {
   Buffers &b = h->buf;
   const double *u = u_in ? u_in : b.u;
   double *out = u_out ? u_out : b.u;
@@ -956,18 +963,18 @@ int launch_rk_stage_sequence(mcfd_handle *h, int order, const double *u_in, doub
   // Each stage result is a SetSolutionColumn in the reference, which runs the
   // limiter when one is installed (spatial/with_limiter.hpp:56-59).
   if (order == 1) {
-    n += launch_face_flux(h, u, 0.0);
+    n += launch_face_flux(h, u, 0.0, after_dt);
     n += launch_cell_update(h, kStageEuler, u, nullptr, out, 1);
     n += launch_limiter(h, out);
   } else if (order == 2) {
-    n += launch_face_flux(h, u, 0.0);
+    n += launch_face_flux(h, u, 0.0, after_dt);
     n += launch_cell_update(h, kStageEuler, u, nullptr, b.u1, 0);
     n += launch_limiter(h, b.u1);
     n += launch_face_flux(h, b.u1, 1.0);
     n += launch_cell_update(h, kStageRk2Last, b.u1, u, out, 1);
     n += launch_limiter(h, out);
   } else {
-    n += launch_face_flux(h, u, 0.0);
+    n += launch_face_flux(h, u, 0.0, after_dt);
     n += launch_cell_update(h, kStageEuler, u, nullptr, b.u1, 0);
     n += launch_limiter(h, b.u1);
     n += launch_face_flux(h, b.u1, 1.0);

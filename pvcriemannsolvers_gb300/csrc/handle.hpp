@@ -83,14 +83,12 @@ struct Mesh {
 // Energy-based artificial viscosity on fr::Lobatto (spatial/viscosity.hpp,
 // spatial/with_viscosity.hpp, riemann/diffusive/direct.hpp), Hex8 cells.
 // Per stage a properties kernel turns the stage input into one viscosity per
-// cell and component and, for every face point side, the normal derivative
-// n . grad(u) and the normal curvature n^T H n that the DDG common gradient
-// needs; the face and cell kernels then add the viscous fluxes.
+// cell and component; the face and cell kernels then add the viscous fluxes
+// where it is not zero.
 struct Visc {
   bool on = false;
   double beta0 = 2.0, beta1 = 1.0 / 12, time_scale = 1.0;
   double *nu = nullptr;     // [cells][K] viscosity of the last properties pass
-  double *trace = nullptr;  // [points][2 sides][2K]: n . grad(u_k), n^T H_k n
   double *side = nullptr;   // [points][2 sides][6]: m = J^-T n, q (Hessian chain-rule term)
   double *pt = nullptr;     // [points][4]: beta0 / d, beta1 d, w h_holder, w h_sharer
   double *cell = nullptr;   // [cells][2]: length, length^(p + 4)
@@ -258,7 +256,8 @@ int launch_set_state(mcfd_handle *h, double t, double dt, double dt_guess,
                      double cfl, int reset_rate);
 // dt guess and CFL of the next steps with the device time left as it is.
 int launch_set_bounds(mcfd_handle *h, double dt_guess, double cfl);
-int launch_face_flux(mcfd_handle *h, const double *u, double stage_c);
+// props_fresh: the viscosity properties of u were just computed by launch_dt
+int launch_face_flux(mcfd_handle *h, const double *u, double stage_c, bool props_fresh = false);
 int launch_cell_update(mcfd_handle *h, int stage, const double *u_in,
                        const double *u0, double *u_out, int advance_time);
 int launch_dt(mcfd_handle *h, const double *u);
@@ -278,9 +277,11 @@ int launch_vtk_sample(mcfd_handle *h, const double *u, const int64_t *off, doubl
                       double *values);
 int launch_modal_vtk_sample(mcfd_handle *h, const double *u, const int64_t *off, double *xyz,
                             double *values);
-// One RK step's stages from u_in to u_out (both default to buf.u).
+// One RK step's stages from u_in to u_out (both default to buf.u);
+// after_dt: launch_dt(u_in) ran right before (its viscosity properties are
+// the first stage's).
 int launch_rk_stage_sequence(mcfd_handle *h, int order, const double *u_in = nullptr,
-                             double *u_out = nullptr);
+                             double *u_out = nullptr, bool after_dt = false);
 // WENO limiter pass on a solution buffer, in place (weno.cu).
 int launch_limiter(mcfd_handle *h, double *u);
 
@@ -311,7 +312,7 @@ int build_modal_mesh(mcfd_handle *h, const ::mcfd_mesh_desc *d, int degree);
 int build_viscosity(mcfd_handle *h, double beta0, double beta1, double time_scale);
 void release_viscosity(mcfd_handle *h);
 int launch_visc_properties(mcfd_handle *h, const double *u, int dt_mode);
-int launch_visc_face_flux(mcfd_handle *h, const double *u, double stage_c);
+int launch_visc_face_flux(mcfd_handle *h, const double *u);
 int launch_visc_dt_finalize(mcfd_handle *h);
 // Initial limiters of the viscous demos (limiter/average.hpp,
 // limiter/majority.hpp), in place; majority counts the cells without one.

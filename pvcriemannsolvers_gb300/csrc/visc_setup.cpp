@@ -114,7 +114,7 @@ cudaError_t download_vec(std::vector<T> *dst, const T *src, size_t n) {
 
 void release_viscosity(mcfd_handle *h) {
   Visc &v = h->visc;
-  void *ptrs[] = {v.nu, v.trace, v.side, v.pt, v.cell, v.d2, v.wloc};
+  void *ptrs[] = {v.nu, v.side, v.pt, v.cell, v.d2, v.wloc};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   v = Visc{};
@@ -259,8 +259,6 @@ int build_viscosity(mcfd_handle *h, double beta0, double beta1, double time_scal
   if (e == cudaSuccess) e = upload_vec(&v.wloc, wloc);
   if (e == cudaSuccess) e = cudaMalloc(&v.nu, sizeof(double) * kK * std::max<int64_t>(nc, 1));
   if (e == cudaSuccess) e = cudaMemset(v.nu, 0, sizeof(double) * kK * std::max<int64_t>(nc, 1));
-  if (e == cudaSuccess) e = cudaMalloc(&v.trace, sizeof(double) * 4 * kK * std::max<int64_t>(np, 1));
-  if (e == cudaSuccess) e = cudaMemset(v.trace, 0, sizeof(double) * 4 * kK * std::max<int64_t>(np, 1));
   if (e == cudaSuccess) {
     const double init = 1.e+100;
     unsigned long long bits;
