@@ -699,7 +699,8 @@ struct SpeedChange {
       double divisor = sqrt(rho_before * P(p_after));
       return (p_after - p_before) / divisor;
     }
-    double v = pow(p_after / p_before, kGm1Over2 / kGamma) - 1;
+    // pow(+0, y > 0) is +0: the vacuum test at p = 0 needs no power
+    double v = (p_after == 0 ? 0.0 : pow(p_after / p_before, kGm1Over2 / kGamma)) - 1;
     return v * (kGm1Under2 * a_before);
   }
   MCFD_HD double prime(double p_after) const {
@@ -711,6 +712,23 @@ struct SpeedChange {
     }
     double divisor = rho_before * a_before;
     return pow(p_after / p_before, -kGp1Over2 / kGamma) / divisor;
+  }
+  // value and prime at the same pressure, sharing the square root of the
+  // shock branch and, in the expansion branch, the power r^((g-1)/(2g)) of
+  // r = p_after / p_before: r^(-(g+1)/(2g)) = r^((g-1)/(2g)) / r.
+  MCFD_HD void value_prime(double p_after, double *v, double *d) const {
+    if (p_after >= p_before) {
+      const double p = P(p_after);
+      const double divisor = sqrt(rho_before * p);
+      *v = (p_after - p_before) / divisor;
+      const double w = kGp1Over4 * (p_before - p_after);
+      *d = (1 + w / p) / divisor;
+      return;
+    }
+    const double r = p_after / p_before;
+    const double s = pow(r, kGm1Over2 / kGamma);
+    *v = (s - 1) * (kGm1Under2 * a_before);
+    *d = (s / r) / (rho_before * a_before);
   }
 };
 
@@ -806,14 +824,21 @@ MCFD_HD Exact1D exact_upwind(const Exact1D &l, const Exact1D &r,
     }
     if (it == kExactMaxIter) *not_converged = true;
     it = 0;
-    double fx;
-    while ((fx = cl.value(x) + cr.value(x) + du) < -1e-8 && it < kExactMaxIter) {
-      x -= fx / (cl.prime(x) + cr.prime(x));
+    // Newton: value and prime of both sides at each x together
+    double vl, dl, vr, dr;
+    cl.value_prime(x, &vl, &dl);
+    cr.value_prime(x, &vr, &dr);
+    double fx = vl + vr + du;
+    while (fx < -1e-8 && it < kExactMaxIter) {
+      x -= fx / (dl + dr);
       ++it;
+      cl.value_prime(x, &vl, &dl);
+      cr.value_prime(x, &vr, &dr);
+      fx = vl + vr + du;
     }
     if (it == kExactMaxIter) *not_converged = true;
     Exact1D star{0, 0, x};
-    star.u = 0.5 * (r.u + cr.value(x) + l.u - cl.value(x));
+    star.u = 0.5 * (r.u + vr + l.u - vl);
     *star_u = star.u;
     if (0 < star.u) {
       return star.p >= l.p ? ex_near_shock(1, l, star)
