@@ -113,7 +113,9 @@ enum mcfd_cell_type {
   MCFD_TET4 = 1,
   MCFD_HEX27 = 2,
   MCFD_TET10 = 3,
-  MCFD_HEX20 = 4
+  MCFD_HEX20 = 4,
+  MCFD_WEDGE6 = 5, /* coordinate/wedge.hpp Wedge6 (modal scheme): local (a, b, z), c = 1 - a - b */
+  MCFD_PYRA5 = 6   /* coordinate/pyramid.hpp Pyramid5 (modal scheme): collapsed local cube */
 };
 
 /* Unstructured mesh, the input that replaces mesh::part::Part

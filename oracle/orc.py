@@ -547,6 +547,8 @@ class Modal:
         types = np.empty(self.n_cells, dtype=np.uint8)
         n = int(self.lib.orc_modal_vtk_sample(self._m, _p(u), _p(xyz), _p(v),
                                               types.ctypes.data_as(C.POINTER(C.c_uint8))))
+        if n < 0:
+            raise RuntimeError("the VTK writer has no pyramid cell")
         return xyz[:n].copy(), v[:n].copy(), types
 
 
@@ -595,7 +597,8 @@ def vtu_text(xyz: np.ndarray, values: np.ndarray, types: np.ndarray) -> str:
             '        <DataArray type="Int32" Name="connectivity" format="ascii">\n',
             "".join(f"{i} " for i in range(n_points)), "\n        </DataArray>\n",
             '        <DataArray type="Int32" Name="offsets" format="ascii">\n']
-    sizes = np.where(np.asarray(types) == 29, 27, 10)
+    t_ = np.asarray(types)
+    sizes = np.where(t_ == 29, 27, np.where(t_ == 26, 15, 10))
     out.append("".join(f"{o} " for o in np.cumsum(sizes)))
     out += ["\n        </DataArray>\n", '        <DataArray type="UInt8" Name="types" format="ascii">\n',
             "".join(f"{int(t)} " for t in types), "\n        </DataArray>\n", "      </Cells>\n",

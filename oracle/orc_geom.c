@@ -7,7 +7,13 @@
  * shapes (1+xx_a)(1+yy_a)(1+zz_a)(xx_a+yy_a+zz_a-2)/8, mid-edge shapes
  * (1-x^2)(1+yy_a)(1+zz_a)/4 and permutations); Tet10 the quadratic simplex
  * element (corner shapes L(2L-1), mid-edge shapes 4 L_i L_j) with barycentric
- * coordinates (x, y, z, 1 - x - y - z) for corners A, B, C, D.
+ * coordinates (x, y, z, 1 - x - y - z) for corners A, B, C, D.  Wedge6
+ * (coordinate/wedge.hpp:127-138): {a, b, 1 - a - b} times {(1 - z)/2,
+ * (1 + z)/2}; Pyra5 (coordinate/pyramid.hpp:124-135): trilinear shapes of the
+ * base corners (+-1, +-1, -1) of the local cube and (1 + z)/2 for the apex.
+ * Local faces (orc_type_face_corners) in the reference's node order:
+ * hexahedron.hpp:353-390, tetrahedron.hpp:141-147, wedge.hpp:211-223,
+ * pyramid.hpp:110-121 and 199-208.
  */
 #include <math.h>
 
@@ -29,14 +35,56 @@ int orc_type_nodes(int type) {
     case ORC_CELL_HEX27: return 27;
     case ORC_CELL_TET10: return 10;
     case ORC_CELL_HEX20: return 20;
+    case ORC_CELL_WEDGE6: return 6;
+    case ORC_CELL_PYRA5: return 5;
     default: return 0;
+  }
+}
+
+int orc_type_faces(int type) {
+  if (orc_type_is_tet(type)) return 4;
+  return (type == ORC_CELL_WEDGE6 || type == ORC_CELL_PYRA5) ? 5 : 6;
+}
+
+int orc_type_face_corners(int type, int side, int *v) {
+  static const int hex[6][4] = {{0, 3, 2, 1}, {0, 1, 5, 4}, {1, 2, 6, 5},
+                                {2, 3, 7, 6}, {0, 4, 7, 3}, {4, 5, 6, 7}};
+  static const int tet[4][4] = {{0, 2, 1, -1}, {0, 1, 3, -1}, {0, 3, 2, -1}, {1, 2, 3, -1}};
+  static const int wedge[5][4] = {{0, 2, 1, -1}, {3, 4, 5, -1}, {0, 1, 4, 3}, {1, 2, 5, 4}, {0, 3, 5, 2}};
+  static const int pyra[5][4] = {{0, 3, 2, 1}, {0, 1, 4, -1}, {1, 2, 4, -1}, {2, 3, 4, -1}, {3, 0, 4, -1}};
+  const int *row = orc_type_is_tet(type) ? tet[side]
+                   : type == ORC_CELL_WEDGE6 ? wedge[side]
+                   : type == ORC_CELL_PYRA5  ? pyra[side]
+                                             : hex[side];
+  int n = row[3] < 0 ? 3 : 4;
+  for (int i = 0; i < n; ++i) v[i] = row[i];
+  return n;
+}
+
+void orc_type_center(int type, double *loc) {
+  if (orc_type_is_tet(type)) {
+    loc[0] = loc[1] = loc[2] = 0.25;
+  } else if (type == ORC_CELL_WEDGE6) {
+    loc[0] = loc[1] = 1.0 / 3;
+    loc[2] = 0;
+  } else if (type == ORC_CELL_PYRA5) {
+    loc[0] = loc[1] = 0;
+    loc[2] = -0.5;
+  } else {
+    loc[0] = loc[1] = loc[2] = 0;
   }
 }
 
 int orc_type_is_tet(int type) { return type == ORC_CELL_TET4 || type == ORC_CELL_TET10; }
 
 void orc_local_of_node(int type, int a, double *loc) {
-  if (orc_type_is_tet(type)) {
+  static const double wedge[6][3] = {{1, 0, -1}, {0, 1, -1}, {0, 0, -1}, {1, 0, 1}, {0, 1, 1}, {0, 0, 1}};
+  static const double pyra[5][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1}, {0, 0, 1}};
+  if (type == ORC_CELL_WEDGE6) {
+    for (int e = 0; e < 3; ++e) loc[e] = wedge[a][e];
+  } else if (type == ORC_CELL_PYRA5) {
+    for (int e = 0; e < 3; ++e) loc[e] = pyra[a][e];
+  } else if (orc_type_is_tet(type)) {
     double b[4] = {0, 0, 0, 0};
     if (a < 4) {
       b[a] = 1;
@@ -70,6 +118,27 @@ static void shapes(int type, const double *p, double *N, double (*G)[3]) {
       G[a][1] = kHex27[a][1] * fx * fz / 8;
       G[a][2] = kHex27[a][2] * fx * fy / 8;
     }
+  } else if (type == ORC_CELL_WEDGE6) {
+    const double c = 1 - x - y, lo = (1 - z) / 2, hi = (1 + z) / 2;
+    const double L[3] = {x, y, c};
+    const double dL[3][2] = {{1, 0}, {0, 1}, {-1, -1}};
+    for (int a = 0; a < 3; ++a) {
+      N[a] = L[a] * lo;
+      N[3 + a] = L[a] * hi;
+      G[a][0] = dL[a][0] * lo; G[a][1] = dL[a][1] * lo; G[a][2] = -0.5 * L[a];
+      G[3 + a][0] = dL[a][0] * hi; G[3 + a][1] = dL[a][1] * hi; G[3 + a][2] = 0.5 * L[a];
+    }
+  } else if (type == ORC_CELL_PYRA5) {
+    for (int a = 0; a < 4; ++a) {
+      double fx = 1 + kHex27[a][0] * x, fy = 1 + kHex27[a][1] * y, fz = 1 + kHex27[a][2] * z;
+      N[a] = fx * fy * fz / 8;
+      G[a][0] = kHex27[a][0] * fy * fz / 8;
+      G[a][1] = kHex27[a][1] * fx * fz / 8;
+      G[a][2] = kHex27[a][2] * fx * fy / 8;
+    }
+    N[4] = (1 + z) / 2;
+    G[4][0] = G[4][1] = 0;
+    G[4][2] = 0.5;
   } else if (type == ORC_CELL_HEX27) {
     for (int a = 0; a < 27; ++a) {
       double qx = quad1(kHex27[a][0], x), qy = quad1(kHex27[a][1], y), qz = quad1(kHex27[a][2], z);

@@ -71,5 +71,10 @@ int orc_type_nodes(int type);
 int orc_type_is_tet(int type);
 void orc_local_of_node(int type, int a, double *loc);
 void orc_map_point(int type, const double *xn, const double *loc, double *x, double *jac);
+/* local faces of a type (4, 5 or 6), the corners of local face `side` in v
+ * (the return value: 3 or 4), and the type's local centre (BuildCenter). */
+int orc_type_faces(int type);
+int orc_type_face_corners(int type, int side, int *v);
+void orc_type_center(int type, double *loc);
 
 #endif /* MCFD_ORACLE_ORC_INTERNAL_H_ */

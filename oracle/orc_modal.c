@@ -1,7 +1,7 @@
 /*
  * ORACLE (test infrastructure only): modal DG (dg::General over
- * polynomial::Projection) on Hex8 and Tet4 cells, restated from the
- * reference project.  Parity checker and CPU baseline; the product library
+ * polynomial::Projection) on Hex8, Tet4, Wedge6 and Pyra5 cells (and the
+ * curved Hex20 / Hex27 / Tet10), restated from the reference project.  Parity checker and CPU baseline; the product library
  * never calls it.
  *
  *   residual (volume, faces, boundaries)  spatial/dg/general.hpp:58-202
@@ -22,7 +22,13 @@
  * (p+1)^2; Tet4 cells the 14-point degree-5 rule for p <= 2 and the
  * 24-point degree-6 rule for p = 3; Tri3 faces the 6-point degree-4 rule for
  * p <= 2 and the 12-point degree-6 rule for p = 3
- * (integrator/tetrahedron.hpp:149-275, integrator/triangle.hpp:163-228).
+ * (integrator/tetrahedron.hpp:149-275, integrator/triangle.hpp:163-228);
+ * Wedge6 cells the triangle rule times Gauss-Legendre p+1 in z, triangle
+ * point outer (integrator/wedge.hpp:63-88); Pyra5 cells Gauss-Legendre
+ * (p+1)^2 times Gauss-Jacobi (alpha 2, beta 0) p+1 in z, local weight
+ * w_x w_y w_z (1 - z)^-2 (integrator/pyramid.hpp:63-91); the Gauss-Jacobi
+ * points are the roots of P_{p+1}^(2,0) found by bisection and Newton, the
+ * weights 8 / ((1 - x^2) P'(x)^2).
  *
  * Periodic faces (an extension; the reference has none): the sharer's
  * polynomial is evaluated at x - shift.
@@ -158,11 +164,7 @@ static int tri_rule(int p, double (*x)[2], double *w) {
 static const int kHexLocal[8][3] = {
     {-1, -1, -1}, {+1, -1, -1}, {+1, +1, -1}, {-1, +1, -1},
     {-1, -1, +1}, {+1, -1, +1}, {+1, +1, +1}, {-1, +1, +1}};
-static const int kHexFace[6][4] = {
-    {0, 3, 2, 1}, {0, 1, 5, 4}, {1, 2, 6, 5},
-    {2, 3, 7, 6}, {0, 4, 7, 3}, {4, 5, 6, 7}};
-/* Tetrahedron4::faces_ (coordinate/tetrahedron.hpp:141-147) */
-static const int kTetFace[4][3] = {{0, 2, 1}, {0, 1, 3}, {0, 3, 2}, {1, 2, 3}};
+
 static const int kQuadLocal[4][2] = {{-1, -1}, {+1, -1}, {+1, +1}, {-1, +1}};
 
 static void hex8_global(const double *xn, const double *loc, double *g) {
@@ -233,14 +235,70 @@ void orc_modal_destroy(orc_modal *m) {
 }
 
 static int cell_points(int type, int p) {
+  if (type == ORC_CELL_WEDGE6) return (p <= 2 ? 6 : 12) * (p + 1);
   if (!orc_type_is_tet(type)) return (p + 1) * (p + 1) * (p + 1);
   return p <= 2 ? 14 : 24;
 }
 
-static int face_points(int type, int p) {
-  if (!orc_type_is_tet(type)) return (p + 1) * (p + 1);
+/* points of local face `side` of a cell of the type: quadrangle or triangle */
+static int face_points(int type, int side, int p) {
+  int v[4];
+  if (orc_type_face_corners(type, side, v) == 4) return (p + 1) * (p + 1);
   return p <= 2 ? 6 : 12;
 }
+
+/* P_n^(2,0)(x) by the three-term recurrence and its derivative from
+ * (2n+a+b)(1-x^2) P_n' = n((a-b) - (2n+a+b)x) P_n + 2(n+a)(n+b) P_{n-1} */
+static void jacobi20(int n, double x, double *pn, double *dpn) {
+  const double a = 2, b = 0;
+  double p0 = 1, p1 = ((a + b + 2) * x + (a - b)) / 2;
+  for (int k = 2; k <= n; ++k) {
+    const double c = 2 * k + a + b;
+    const double p2 = (((c - 1) * (a * a - b * b) + (c - 2) * (c - 1) * c * x) * p1 -
+                       2 * (k + a - 1) * (k + b - 1) * c * p0) /
+                      (2 * k * (k + a + b) * (c - 2));
+    p0 = p1;
+    p1 = p2;
+  }
+  const double c = 2 * n + a + b;
+  *pn = p1;
+  *dpn = (n * ((a - b) - c * x) * p1 + 2 * (n + a) * (n + b) * p0) / (c * (1 - x * x));
+}
+
+/* Gauss-Jacobi rule of the weight (1 - x)^2, n points ascending */
+static void gauss_jacobi20(int n, double *x, double *w) {
+  int found = 0;
+  double xl = -1 + 1e-12, fl, d;
+  jacobi20(n, xl, &fl, &d);
+  for (int g = 1; g <= 4000 && found < n; ++g) {
+    double xr = -1 + 2.0 * g / 4000 - (g == 4000 ? 1e-12 : 0.0), fr;
+    jacobi20(n, xr, &fr, &d);
+    if ((fl < 0) != (fr < 0)) {
+      double lo = xl, hi = xr, flo = fl;
+      for (int it = 0; it < 200 && hi - lo > 1e-15; ++it) {
+        double mid = 0.5 * (lo + hi), fm;
+        jacobi20(n, mid, &fm, &d);
+        if ((fm < 0) == (flo < 0)) { lo = mid; flo = fm; } else { hi = mid; }
+      }
+      double r = 0.5 * (lo + hi);
+      for (int it = 0; it < 3; ++it) {
+        double f, df;
+        jacobi20(n, r, &f, &df);
+        if (df != 0) r -= f / df;
+      }
+      x[found++] = r;
+    }
+    xl = xr;
+    fl = fr;
+  }
+  for (int i = 0; i < n; ++i) {
+    double f, df;
+    jacobi20(n, x[i], &f, &df);
+    w[i] = 8.0 / ((1 - x[i] * x[i]) * df * df);
+  }
+}
+
+void orc_gauss_jacobi20(int n, double *x, double *w) { gauss_jacobi20(n, x, w); }
 
 orc_modal *orc_modal_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
                             const int64_t *cell_nodes, const int32_t *cell_type,
@@ -281,6 +339,8 @@ orc_modal *orc_modal_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
   int ntet = tet_rule(p, tx, tw);
   double sx[12][2], sw[12];
   int ntri = tri_rule(p, sx, sw);
+  double jx[4], jw[4];
+  gauss_jacobi20(Q, jx, jw);
   int bad = 0;
 #pragma omp parallel for schedule(static) num_threads(orc_get_threads())
   for (int64_t c = 0; c < n_cells; ++c) {
@@ -297,12 +357,13 @@ orc_modal *orc_modal_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
     double *ctr = &m->center[c * 3];
     double *X = &m->vx[m->vp_off[c] * 3], *W = &m->vw[m->vp_off[c]];
     double volume = 0;
-    if (t == ORC_CELL_HEX27 || t == ORC_CELL_HEX20 || t == ORC_CELL_TET10) {
-      /* quadratic map: points and det J from the shape functions; the centre
-       * at the local centre (hex (0,0,0), tet (1/4,1/4,1/4)) */
+    if (t == ORC_CELL_HEX27 || t == ORC_CELL_HEX20 || t == ORC_CELL_TET10 ||
+        t == ORC_CELL_WEDGE6 || t == ORC_CELL_PYRA5) {
+      /* points and det J from the shape functions; the centre at the type's
+       * local centre */
       const int tet = t == ORC_CELL_TET10;
-      const double cl[3] = {tet ? 0.25 : 0.0, tet ? 0.25 : 0.0, tet ? 0.25 : 0.0};
-      double J[9];
+      double cl[3], J[9];
+      orc_type_center(t, cl);
       orc_map_point(t, xn, cl, ctr, J);
       int nq = (int)(m->vp_off[c + 1] - m->vp_off[c]);
       for (int q = 0; q < nq; ++q) {
@@ -310,6 +371,14 @@ orc_modal *orc_modal_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
         if (tet) {
           loc[0] = tx[q][0]; loc[1] = tx[q][1]; loc[2] = tx[q][2];
           wl = tw[q];
+        } else if (t == ORC_CELL_WEDGE6) {
+          int i = q / Q, k = q % Q;
+          loc[0] = sx[i][0]; loc[1] = sx[i][1]; loc[2] = gx[k];
+          wl = sw[i] * gw[k];
+        } else if (t == ORC_CELL_PYRA5) {
+          int i = q / (Q * Q), j = (q / Q) % Q, k = q % Q;
+          loc[0] = gx[i]; loc[1] = gx[j]; loc[2] = jx[k];
+          wl = gw[i] * gw[j] * jw[k] * pow(1 - jx[k], -2);
         } else {
           int i = q / (Q * Q), j = (q / Q) % Q, k = q % Q;
           loc[0] = gx[i]; loc[1] = gx[j]; loc[2] = gx[k];
@@ -375,7 +444,9 @@ orc_modal *orc_modal_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
   for (int64_t f = 0; f < n_faces; ++f) {
     int64_t h = face_cells[f * 2];
     int t = (cell_type && h >= 0 && h < n_cells) ? cell_type[h] : ORC_CELL_HEX8;
-    m->fp_off[f + 1] = m->fp_off[f] + face_points(t, p);
+    int sd = face_sides[f * 2];
+    if (sd < 0 || sd >= orc_type_faces(t)) sd = 0;
+    m->fp_off[f + 1] = m->fp_off[f] + face_points(t, sd, p);
   }
   int64_t NF = m->fp_off[n_faces];
   m->fx = (double *)malloc(sizeof(double) * (NF * 3 + 1));
@@ -397,15 +468,17 @@ orc_modal *orc_modal_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
     int t = cell_type ? cell_type[h] : ORC_CELL_HEX8;
     double *X = &m->fx[m->fp_off[f] * 3], *W = &m->fw[m->fp_off[f]];
     double *F = &m->ff[m->fp_off[f] * 9];
+    int fvs[4] = {0, 0, 0, 0};
+    const int nfvs = (side >= 0 && side < orc_type_faces(t)) ? orc_type_face_corners(t, side, fvs) : 0;
     if (t == ORC_CELL_HEX27 || t == ORC_CELL_HEX20 || t == ORC_CELL_TET10) {
-      /* curved holder: face points from its cell map at the face's local
+      /* quadratic holder through its cell map: face points at the face's local
        * points; tangents J^T dloc/da, J^T dloc/db (quad: corner 0 -> 1,
        * 0 -> 3; triangle: corner 0 - corner 2, corner 1 - corner 2) */
-      const int hex = t != ORC_CELL_TET10;
-      if (side < 0 || side > (hex ? 5 : 3)) { bad = 1; continue; }
+      if (side < 0 || side >= orc_type_faces(t)) { bad = 1; continue; }
+      int fv[4];
+      const int hex = orc_type_face_corners(t, side, fv) == 4;  /* quadrangle face */
       double lc[4][3], da[3], db[3];
-      for (int v = 0; v < (hex ? 4 : 3); ++v)
-        orc_local_of_node(t, hex ? kHexFace[side][v] : kTetFace[side][v], lc[v]);
+      for (int v = 0; v < (hex ? 4 : 3); ++v) orc_local_of_node(t, fv[v], lc[v]);
       for (int d = 0; d < 3; ++d) {
         da[d] = hex ? (lc[1][d] - lc[0][d]) / 2 : lc[0][d] - lc[2][d];
         db[d] = hex ? (lc[3][d] - lc[0][d]) / 2 : lc[1][d] - lc[2][d];
@@ -437,12 +510,12 @@ orc_modal *orc_modal_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
         for (int d = 0; d < 3; ++d) fr[3 + d] = jac[d] / tn;
         cross(&fr[0], &fr[3], &fr[6]);
       }
-    } else if (t == ORC_CELL_HEX8) {
-      if (side < 0 || side > 5) { bad = 1; continue; }
+    } else if (nfvs == 4) {
+      /* Quadrangle4 map of the holder's face corners (Hex8, Wedge6, Pyra5) */
       double xn[12];
       for (int v = 0; v < 4; ++v)
         for (int d = 0; d < 3; ++d)
-          xn[v * 3 + d] = xyz[cell_nodes[h * NS + kHexFace[side][v]] * 3 + d];
+          xn[v * 3 + d] = xyz[cell_nodes[h * NS + fvs[v]] * 3 + d];
       for (int i = 0; i < Q; ++i)
         for (int j = 0; j < Q; ++j) {
           int q = i * Q + j;
@@ -470,11 +543,12 @@ orc_modal *orc_modal_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
           cross(&fr[0], &fr[3], &fr[6]);
         }
     } else {
-      if (side < 0 || side > 3) { bad = 1; continue; }
+      /* Triangle3 map of the holder's face corners (Tet4, Wedge6, Pyra5) */
+      if (nfvs != 3) { bad = 1; continue; }
       double xn[9];
       for (int v = 0; v < 3; ++v)
         for (int d = 0; d < 3; ++d)
-          xn[v * 3 + d] = xyz[cell_nodes[h * NS + kTetFace[side][v]] * 3 + d];
+          xn[v * 3 + d] = xyz[cell_nodes[h * NS + fvs[v]] * 3 + d];
       /* Triangle3: shapes (x, y, 1 - x - y); Jacobian rows X0 - X2, X1 - X2 */
       double jac[6];
       for (int d = 0; d < 3; ++d) {
@@ -736,6 +810,11 @@ int orc_modal_rk_update(const orc_modal *m, int riemann, int n_bc,
  * Tetrahedron10 locals (vtk.hpp:214-224); global point from the cell map,
  * value = Projection::GlobalToValue there.  Points cell by cell. */
 extern const signed char orc_vtk_hex27[27][3];
+/* Wedge15 locals (vtk.hpp:251-270) */
+static const double kWedge15[15][3] = {
+    {1, 0, -1}, {0, 1, -1}, {0, 0, -1}, {1, 0, 1}, {0, 1, 1}, {0, 0, 1},
+    {0.5, 0.5, -1}, {0, 0.5, -1}, {0.5, 0, -1}, {0.5, 0.5, 1}, {0, 0.5, 1}, {0.5, 0, 1},
+    {1, 0, 0}, {0, 1, 0}, {0, 0, 0}};
 static const double kTet10[10][3] = {
     {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {0, 0, 0}, {0.5, 0.5, 0},
     {0, 0.5, 0.5}, {0.5, 0, 0.5}, {0.5, 0, 0}, {0, 0.5, 0}, {0, 0, 0.5}};
@@ -746,14 +825,15 @@ int64_t orc_modal_vtk_sample(const orc_modal *m, const double *u, double *xyz,
   double psi[MAXM];
   for (int64_t c = 0; c < m->n_cells; ++c) {
     const double *xn = &m->corners[c * 81];
-    const int tet = orc_type_is_tet(m->type[c]);
-    types[c] = tet ? 24 : 29;
-    const int n = tet ? 10 : 27;
+    const int tet = orc_type_is_tet(m->type[c]), wedge = m->type[c] == ORC_CELL_WEDGE6;
+    if (m->type[c] == ORC_CELL_PYRA5) return -1; /* no pyramid in the writer (vtk.hpp:400-414) */
+    types[c] = tet ? 24 : wedge ? 26 : 29;
+    const int n = tet ? 10 : wedge ? 15 : 27;
     for (int s = 0; s < n; ++s, ++pt) {
       double *g = &xyz[pt * 3];
       if (m->type[c] != ORC_CELL_HEX8 && m->type[c] != ORC_CELL_TET4) {
         double loc[3], J[9];
-        for (int d = 0; d < 3; ++d) loc[d] = tet ? kTet10[s][d] : orc_vtk_hex27[s][d];
+        for (int d = 0; d < 3; ++d) loc[d] = tet ? kTet10[s][d] : wedge ? kWedge15[s][d] : orc_vtk_hex27[s][d];
         orc_map_point(m->type[c], xn, loc, g, J);
       } else if (!tet) {
         double loc[3] = {orc_vtk_hex27[s][0], orc_vtk_hex27[s][1], orc_vtk_hex27[s][2]};

@@ -206,9 +206,9 @@ int upload_corners(mcfd_handle *h, const mcfd_mesh_desc *d) {
   for (int64_t c = 0; c < nc; ++c) {
     const int t = d->cell_type ? d->cell_type[c] : 0;
     m.host_cell_type[c] = (uint8_t)t;
-    m.curved = m.curved || mcfd::geo::curved(t);
-    types[c] = (uint8_t)(mcfd::geo::is_tet(t) ? 1 : 0);
-    const int nv = mcfd::geo::is_tet(t) ? 4 : 8;
+    m.curved = m.curved || mcfd::geo::curved(t) || mcfd::geo::is_wedge(t) || mcfd::geo::is_pyramid(t);
+    types[c] = (uint8_t)(mcfd::geo::is_tet(t) ? 1 : mcfd::geo::is_wedge(t) ? 2 : mcfd::geo::is_pyramid(t) ? 3 : 0);
+    const int nv = mcfd::geo::corner_count(t);
     for (int v = 0; v < nv; ++v) {
       const int64_t id = d->cell_nodes[c * S + v];
       if (id < 0 || id >= d->n_nodes) return fail(h, MCFD_ERR_ARGUMENT, "cell node index out of range");

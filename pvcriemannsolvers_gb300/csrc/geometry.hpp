@@ -12,6 +12,21 @@
 //   Tet4   (a, b, c, 1 - a - b - c) for corners A (1,0,0), B (0,1,0),
 //          C (0,0,1), D (0,0,0)
 //   Tet10  quadratic: corners, then mid-edges AB, BC, CA, DA, DB, DC
+//   Wedge6 (coordinate/wedge.hpp:127-138): local (a, b, z) with c = 1 - a - b,
+//          nodes (1,0,-1) (0,1,-1) (0,0,-1) (1,0,1) (0,1,1) (0,0,1);
+//          N = {a, b, c} x {(1 - z) / 2, (1 + z) / 2}
+//   Pyra5  (coordinate/pyramid.hpp:124-135): the base corners of the local
+//          cube (+-1, +-1, -1) with the trilinear shape functions, the apex
+//          (0, 0, 1) with (1 + z) / 2: the cube collapses onto the pyramid
+//
+// Local faces of every type (cell_face_corners) in the reference's node
+// order, each parametrised so that its normal points out of the cell:
+//   hexahedron  coordinate/hexahedron.hpp:353-390 (6 quadrangles)
+//   tetrahedron coordinate/tetrahedron.hpp:141-147 (4 triangles)
+//   wedge       coordinate/wedge.hpp:211-223: triangles {0,2,1} {3,4,5}, then
+//               quadrangles {0,1,4,3} {1,2,5,4} {0,3,5,2}
+//   pyramid     coordinate/pyramid.hpp:110-121, 199-208: the base {0,3,2,1},
+//               then triangles {0,1,4} {1,2,4} {2,3,4} {3,0,4}
 #pragma once
 
 #include <cmath>
@@ -25,6 +40,8 @@ constexpr int kMaxNodes = 27;
 
 inline bool is_tet(int type) { return type == MCFD_TET4 || type == MCFD_TET10; }
 inline bool is_hex(int type) { return type == MCFD_HEX8 || type == MCFD_HEX27 || type == MCFD_HEX20; }
+inline bool is_wedge(int type) { return type == MCFD_WEDGE6; }
+inline bool is_pyramid(int type) { return type == MCFD_PYRA5; }
 inline bool curved(int type) { return type == MCFD_HEX27 || type == MCFD_HEX20 || type == MCFD_TET10; }
 inline int node_count(int type) {
   switch (type) {
@@ -33,8 +50,34 @@ inline int node_count(int type) {
     case MCFD_HEX27: return 27;
     case MCFD_TET10: return 10;
     case MCFD_HEX20: return 20;
+    case MCFD_WEDGE6: return 6;
+    case MCFD_PYRA5: return 5;
     default: return 0;
   }
+}
+// corner count (the straight-sided type the corners span)
+inline int corner_count(int type) {
+  return is_tet(type) ? 4 : is_wedge(type) ? 6 : is_pyramid(type) ? 5 : 8;
+}
+
+// Number of local faces, and the corners of local face `side` in v[] (3 or
+// 4 entries; the return value).
+inline int face_count(int type) { return is_tet(type) ? 4 : (is_wedge(type) || is_pyramid(type)) ? 5 : 6; }
+inline int cell_face_corners(int type, int side, int *v) {
+  static const int hex[6][4] = {{0, 3, 2, 1}, {0, 1, 5, 4}, {1, 2, 6, 5},
+                                {2, 3, 7, 6}, {0, 4, 7, 3}, {4, 5, 6, 7}};
+  static const int tet[4][3] = {{0, 2, 1}, {0, 1, 3}, {0, 3, 2}, {1, 2, 3}};
+  static const int wedge[5][4] = {{0, 2, 1, -1}, {3, 4, 5, -1}, {0, 1, 4, 3}, {1, 2, 5, 4}, {0, 3, 5, 2}};
+  static const int pyra[5][4] = {{0, 3, 2, 1}, {0, 1, 4, -1}, {1, 2, 4, -1}, {2, 3, 4, -1}, {3, 0, 4, -1}};
+  const int *row;
+  if (is_tet(type)) {
+    for (int i = 0; i < 3; ++i) v[i] = tet[side][i];
+    return 3;
+  }
+  row = is_wedge(type) ? wedge[side] : is_pyramid(type) ? pyra[side] : hex[side];
+  const int n = row[3] < 0 ? 3 : 4;
+  for (int i = 0; i < n; ++i) v[i] = row[i];
+  return n;
 }
 
 // CGNS local coordinates of the Hex27 nodes (Hex8 and Hex20 are prefixes).
@@ -56,10 +99,33 @@ inline const int (*tet10_local_half())[3] {
 }
 
 inline void local_of_node(int type, int a, double *loc) {
+  static const double wedge[6][3] = {{1, 0, -1}, {0, 1, -1}, {0, 0, -1}, {1, 0, 1}, {0, 1, 1}, {0, 0, 1}};
+  static const double pyra[5][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1}, {0, 0, 1}};
   if (is_tet(type)) {
     for (int e = 0; e < 3; ++e) loc[e] = 0.5 * tet10_local_half()[a][e];
+  } else if (is_wedge(type)) {
+    for (int e = 0; e < 3; ++e) loc[e] = wedge[a][e];
+  } else if (is_pyramid(type)) {
+    for (int e = 0; e < 3; ++e) loc[e] = pyra[a][e];
   } else {
     for (int e = 0; e < 3; ++e) loc[e] = hex27_local()[a][e];
+  }
+}
+
+// Local centre of a type (the reference's BuildCenter): hexahedron (0, 0, 0),
+// tetrahedron (1/4, 1/4, 1/4), wedge (1/3, 1/3, 0), pyramid (0, 0, -1/2)
+// (coordinate/{hexahedron,tetrahedron,wedge,pyramid}.hpp).
+inline void local_center(int type, double *loc) {
+  if (is_tet(type)) {
+    loc[0] = loc[1] = loc[2] = 0.25;
+  } else if (is_wedge(type)) {
+    loc[0] = loc[1] = 1.0 / 3;
+    loc[2] = 0;
+  } else if (is_pyramid(type)) {
+    loc[0] = loc[1] = 0;
+    loc[2] = -0.5;
+  } else {
+    loc[0] = loc[1] = loc[2] = 0;
   }
 }
 
@@ -124,6 +190,28 @@ inline void shapes(int type, const double *loc, double *N, double (*G)[3]) {
           G[a][2] = -2 * z * fx * fy / 4;
         }
       }
+      break;
+    case MCFD_WEDGE6: {
+      const double c = 1 - x - y, lo = (1 - z) / 2, hi = lo + z;
+      N[0] = x * lo; N[1] = y * lo; N[2] = c * lo;
+      N[3] = x * hi; N[4] = y * hi; N[5] = c * hi;
+      const double g[6][3] = {{lo, 0, -0.5 * x}, {0, lo, -0.5 * y}, {-lo, -lo, -0.5 * c},
+                              {hi, 0, 0.5 * x},  {0, hi, 0.5 * y},  {-hi, -hi, 0.5 * c}};
+      for (int a = 0; a < 6; ++a)
+        for (int e = 0; e < 3; ++e) G[a][e] = g[a][e];
+      break;
+    }
+    case MCFD_PYRA5:
+      for (int a = 0; a < 4; ++a) {
+        const double fx = 1 + L[a][0] * x, fy = 1 + L[a][1] * y, fz = 1 + L[a][2] * z;
+        N[a] = fx * fy * fz / 8;
+        G[a][0] = L[a][0] * fy * fz / 8;
+        G[a][1] = L[a][1] * fx * fz / 8;
+        G[a][2] = L[a][2] * fx * fy / 8;
+      }
+      N[4] = (1 + z) / 2;
+      G[4][0] = G[4][1] = 0;
+      G[4][2] = 0.5;
       break;
     case MCFD_TET4: {
       N[0] = x; N[1] = y; N[2] = z; N[3] = 1 - x - y - z;

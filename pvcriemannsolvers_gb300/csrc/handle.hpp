@@ -66,9 +66,9 @@ struct Mesh {
   // output sampling (mcfd_vtk_sample): cell corners and types
   double *corners = nullptr;        // [cells][8][3] corner coordinates (Tet4: first 4)
   uint8_t *cell_type = nullptr;     // [cells] 0 Hex8, 1 Tet4
-  std::vector<uint8_t> host_types;  // [cells] 0 hexahedron, 1 tetrahedron
+  std::vector<uint8_t> host_types;  // [cells] 0 hexahedron, 1 tetrahedron, 2 wedge, 3 pyramid
   std::vector<uint8_t> host_cell_type;  // [cells] enum mcfd_cell_type
-  bool curved = false;              // some cell has a quadratic map
+  bool curved = false;              // output points come from the host maps (quadratic, wedge or pyramid cells)
   std::vector<double> host_nodes;   // [cells][27][3] all nodes (curved meshes only)
   double xq[4] = {0, 0, 0, 0};      // GLL abscissae of the nodal schemes
   // host copies for parity queries

@@ -33,13 +33,10 @@
 #include <vector>
 
 #include "../../include/mcfd.h"
+#include "geometry.hpp"
 #include "mesh_build_gpu.hpp"
 
 namespace {
-
-const int kHexFace[6][4] = {{0, 3, 2, 1}, {0, 1, 5, 4}, {1, 2, 6, 5},
-                            {2, 3, 7, 6}, {0, 4, 7, 3}, {4, 5, 6, 7}};
-const int kTetFace[4][3] = {{0, 2, 1}, {0, 1, 3}, {0, 3, 2}, {1, 2, 3}};
 
 thread_local std::string g_build_error;
 
@@ -69,28 +66,19 @@ struct OutFace {
   double shift[3];
 };
 
-bool tet_type(const int32_t *cell_type, int64_t c) {
-  return cell_type && (cell_type[c] == MCFD_TET4 || cell_type[c] == MCFD_TET10);
-}
+int type_of(const int32_t *cell_type, int64_t c) { return cell_type ? cell_type[c] : MCFD_HEX8; }
 
-int type_nodes(int t) {
-  switch (t) {
-    case MCFD_HEX8: return 8;
-    case MCFD_TET4: return 4;
-    case MCFD_HEX27: return 27;
-    case MCFD_TET10: return 10;
-    case MCFD_HEX20: return 20;
-    default: return 0;
-  }
-}
+int type_nodes(int t) { return mcfd::geo::node_count(t); }
+
+// local faces of cell c (6 hexahedron, 4 tetrahedron, 5 wedge or pyramid)
+int n_sides(const int32_t *cell_type, int64_t c) { return mcfd::geo::face_count(type_of(cell_type, c)); }
 
 // corner ids of a local face (faces are keyed and matched by their corners)
 int face_node_ids(const int64_t *cell_nodes, int64_t stride, const int32_t *cell_type, int64_t c,
                   int side, int64_t *ids) {
-  const bool tet = tet_type(cell_type, c);
-  const int n = tet ? 3 : 4;
-  for (int v = 0; v < n; ++v)
-    ids[v] = cell_nodes[c * stride + (tet ? kTetFace[side][v] : kHexFace[side][v])];
+  int v[4];
+  const int n = mcfd::geo::cell_face_corners(type_of(cell_type, c), side, v);
+  for (int i = 0; i < n; ++i) ids[i] = cell_nodes[c * stride + v[i]];
   return n;
 }
 
@@ -137,7 +125,7 @@ const char *mcfd_build_error(void) { return g_build_error.c_str(); }
 int64_t mcfd_face_slot_count(int64_t n_cells, const int32_t *cell_type) {
   if (n_cells < 0) return -1;
   int64_t n = 0;
-  for (int64_t c = 0; c < n_cells; ++c) n += tet_type(cell_type, c) ? 4 : 6;
+  for (int64_t c = 0; c < n_cells; ++c) n += n_sides(cell_type, c);
   return n;
 }
 
@@ -161,7 +149,6 @@ int mcfd_build_faces(int64_t n_nodes, const double *xyz, int64_t n_cells,
   std::vector<Slot> slots;
   slots.reserve(mcfd_face_slot_count(n_cells, cell_type));
   for (int64_t c = 0; c < n_cells; ++c) {
-    const bool tet = tet_type(cell_type, c);
     const int nv = type_nodes(cell_type ? cell_type[c] : MCFD_HEX8);
     if (nv == 0) return build_fail("cell " + std::to_string(c) + ": unknown cell type");
     if (nv > stride) return build_fail("cell " + std::to_string(c) + ": more nodes than cell_node_stride");
@@ -169,7 +156,7 @@ int mcfd_build_faces(int64_t n_nodes, const double *xyz, int64_t n_cells,
       const int64_t id = cell_nodes[c * stride + v];
       if (id < 0 || id >= n_nodes) return build_fail("cell " + std::to_string(c) + ": node index out of range");
     }
-    for (int s = 0; s < (tet ? 4 : 6); ++s) {
+    for (int s = 0; s < n_sides(cell_type, c); ++s) {
       int64_t ids[4];
       const int n = face_node_ids(cell_nodes, stride, cell_type, c, s, ids);
       slots.push_back({make_key(ids, n), c, s});
@@ -374,7 +361,7 @@ int mcfd_build_faces_gpu(int32_t device, int64_t n_nodes, const double *xyz, int
       const int64_t id = cell_nodes[c * stride + v];
       if (id < 0 || id >= n_nodes) return build_fail("cell " + std::to_string(c) + ": node index out of range");
     }
-    slot_off[c + 1] = slot_off[c] + (tet_type(cell_type, c) ? 4 : 6);
+    slot_off[c + 1] = slot_off[c] + n_sides(cell_type, c);
   }
   if (cap < slot_off.back()) {
     g_build_error = "output capacity below the face slot count (mcfd_face_slot_count)";

@@ -29,15 +29,24 @@
 namespace mcfd {
 namespace {
 
-__constant__ int8_t kHexFaceD[6][4] = {{0, 3, 2, 1}, {0, 1, 5, 4}, {1, 2, 6, 5},
-                                       {2, 3, 7, 6}, {0, 4, 7, 3}, {4, 5, 6, 7}};
-__constant__ int8_t kTetFaceD[4][3] = {{0, 2, 1}, {0, 1, 3}, {0, 3, 2}, {1, 2, 3}};
+// Local faces by family (hexahedron, tetrahedron, wedge, pyramid), the
+// tables of geometry.hpp cell_face_corners; -1 ends a triangle.
+__constant__ int8_t kFacesD[4][6][4] = {
+    {{0, 3, 2, 1}, {0, 1, 5, 4}, {1, 2, 6, 5}, {2, 3, 7, 6}, {0, 4, 7, 3}, {4, 5, 6, 7}},
+    {{0, 2, 1, -1}, {0, 1, 3, -1}, {0, 3, 2, -1}, {1, 2, 3, -1}, {-1, -1, -1, -1}, {-1, -1, -1, -1}},
+    {{0, 2, 1, -1}, {3, 4, 5, -1}, {0, 1, 4, 3}, {1, 2, 5, 4}, {0, 3, 5, 2}, {-1, -1, -1, -1}},
+    {{0, 3, 2, 1}, {0, 1, 4, -1}, {1, 2, 4, -1}, {2, 3, 4, -1}, {3, 0, 4, -1}, {-1, -1, -1, -1}}};
+__constant__ int8_t kNFacesD[4] = {6, 4, 5, 5};
 
 constexpr uint64_t kNone = ~0ull;
 enum : unsigned { kErrThree = 1u, kErrProbe = 2u, kErrSameCell = 4u };
 
-__device__ __forceinline__ bool is_tet(const int32_t *type, int64_t c) {
-  return type && (type[c] == 1 || type[c] == 3);
+// family of a cell: 0 hexahedron (Hex8/20/27), 1 tetrahedron (Tet4/10),
+// 2 wedge, 3 pyramid (enum mcfd_cell_type)
+__device__ __forceinline__ int family(const int32_t *type, int64_t c) {
+  if (!type) return 0;
+  const int t = type[c];
+  return (t == 1 || t == 3) ? 1 : t == 5 ? 2 : t == 6 ? 3 : 0;
 }
 
 __device__ __forceinline__ void sort4(uint32_t *k) {
@@ -66,12 +75,12 @@ __global__ void slot_keys_kernel(const int64_t *cell_nodes, int64_t stride, cons
                                  int64_t *slot_cell, int8_t *slot_side) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= n_cells) return;
-  const bool tet = is_tet(type, c);
+  const int fam = family(type, c);
   const int64_t base = slot_off[c];
-  for (int s = 0; s < (tet ? 4 : 6); ++s) {
+  for (int s = 0; s < kNFacesD[fam]; ++s) {
     uint32_t k[4] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu};
-    for (int v = 0; v < (tet ? 3 : 4); ++v)
-      k[v] = (uint32_t)cell_nodes[c * stride + (tet ? kTetFaceD[s][v] : kHexFaceD[s][v])];
+    for (int v = 0; v < 4 && kFacesD[fam][s][v] >= 0; ++v)
+      k[v] = (uint32_t)cell_nodes[c * stride + kFacesD[fam][s][v]];
     sort4(k);
     keys[base + s] = make_uint4(k[0], k[1], k[2], k[3]);
     slot_cell[base + s] = c;

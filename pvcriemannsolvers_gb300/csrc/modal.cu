@@ -832,7 +832,7 @@ struct ModalSampleArgs {
   double *xyz;
   double *values;
   int64_t n_cells;
-  int points_given;  // curved cells: xyz holds the points already (host-mapped)
+  int points_given;  // quadratic / wedge cells: xyz holds the points already (host-mapped)
 };
 
 template <int M>
@@ -842,7 +842,8 @@ __global__ void __launch_bounds__(256) modal_vtk_sample_kernel(ModalSampleArgs a
   const int s = (int)(gid - c * 27);
   if (c >= a.n_cells) return;
   const bool tet = a.type[c] == 1;
-  if (tet && s >= 10) return;
+  // VTK points per cell: Tetrahedron10, Wedge15 (host-mapped), Hexahedron27
+  if (s >= (tet ? 10 : a.type[c] == 2 ? 15 : 27)) return;
   const double *xn = a.corners + c * 24;
   const int64_t pt = a.off[c] + s;
   double g[3];

@@ -1,5 +1,6 @@
 // Host set-up of the modal DG scheme (dg::General over polynomial::Projection)
-// on Hex8 and Tet4 cells: everything the reference's Part / Cell / Face
+// on Hex8, Tet4, Wedge6 and Pyra5 cells (and the curved Hex20 / Hex27 /
+// Tet10): everything the reference's Part / Cell / Face
 // constructors and OrthoNormal bases compute, built once in FP64 and
 // uploaded.
 //
@@ -7,15 +8,27 @@
 //                       integrator/hexahedron.hpp:66-93); Tet4: the 14-point
 //                       degree-5 rule for p <= 2 and the 24-point degree-6
 //                       rule for p = 3 (integrator/tetrahedron.hpp:149-275);
+//                       Wedge6: the triangle rule of the faces (below) times
+//                       Gauss-Legendre p+1 in z, triangle point outer
+//                       (integrator/wedge.hpp:63-88); Pyra5: Gauss-Legendre
+//                       (p+1)^2 times Gauss-Jacobi (alpha 2, beta 0) p+1 in
+//                       z with local weight w_x w_y w_z (1 - z)^-2
+//                       (integrator/pyramid.hpp:63-91, integrator/jacobi.hpp);
 //                       global weight = local weight * det J
 //                       (integrator/element.hpp:102-115)
 //   face quadrature     Quad4: Gauss-Legendre (p+1)^2; Tri3: the 6-point
 //                       degree-4 rule for p <= 2 and the 12-point degree-6
 //                       rule for p = 3 (integrator/triangle.hpp:163-228);
-//                       points, weights and normals on the holder's local
-//                       face (coordinate/face.hpp:50-62)
+//                       points, weights and normals from the face's own
+//                       Quadrangle4 / Triangle3 map of the holder's local
+//                       face corners (coordinate/face.hpp:50-62) — also for
+//                       wedges and pyramids, whose collapsed local cube does
+//                       not hold a pyramid's triangles as local triangles;
+//                       quadratic cells map their faces through the cell
 //   cell centre         Hex8 LocalToGlobal(0, 0, 0); Tet4 LocalToGlobal(1/4,
-//                       1/4, 1/4) (coordinate/tetrahedron.hpp:40-44)
+//                       1/4, 1/4) (coordinate/tetrahedron.hpp:40-44); Wedge6
+//                       (1/3, 1/3, 0) (coordinate/wedge.hpp:41-44); Pyra5
+//                       (0, 0, -1/2) (coordinate/pyramid.hpp:36-38)
 //   orthonormal basis   psi = S T(x - centre), S lower triangular with
 //                       S^-1 S^-T the Gram matrix of the Taylor monomials
 //                       under the cell quadrature, i.e. S = L^-1 of its
@@ -48,9 +61,6 @@ namespace {
 const int kHexLocal[8][3] = {{-1, -1, -1}, {+1, -1, -1}, {+1, +1, -1},
                              {-1, +1, -1}, {-1, -1, +1}, {+1, -1, +1},
                              {+1, +1, +1}, {-1, +1, +1}};
-const int kHexFace[6][4] = {{0, 3, 2, 1}, {0, 1, 5, 4}, {1, 2, 6, 5},
-                            {2, 3, 7, 6}, {0, 4, 7, 3}, {4, 5, 6, 7}};
-const int kTetFace[4][3] = {{0, 2, 1}, {0, 1, 3}, {0, 3, 2}, {1, 2, 3}};
 const int kQuadLocal[4][2] = {{-1, -1}, {+1, -1}, {+1, +1}, {-1, +1}};
 
 // exponents of the Taylor monomials in the reference's order
@@ -144,6 +154,65 @@ void tri_rule(int p, std::vector<std::array<double, 2>> *x, std::vector<double> 
   }
 }
 
+// Gauss-Jacobi rule for the weight (1 - x)^2 on [-1, 1] (alpha = 2, beta =
+// 0) with n points, ascending: the roots of P_n^(2,0) bracketed on a grid and
+// polished by bisection and Newton (three-term recurrence and the derivative
+// identity (2n+a+b)(1-x^2) P_n' = n ((a-b) - (2n+a+b) x) P_n
+// + 2 (n+a)(n+b) P_{n-1}); w_i = 8 / ((1 - x_i^2) P_n'(x_i)^2).
+void jacobi20(int n, double x, double *pn, double *dpn) {
+  const double a = 2, b = 0;
+  double p0 = 1, p1 = ((a + b + 2) * x + (a - b)) / 2;
+  if (n == 0) { *pn = 1; *dpn = 0; return; }
+  for (int k = 2; k <= n; ++k) {
+    const double c = 2 * k + a + b;
+    const double a1 = 2 * k * (k + a + b) * (c - 2);
+    const double a2 = (c - 1) * (a * a - b * b);
+    const double a3 = (c - 2) * (c - 1) * c;
+    const double a4 = 2 * (k + a - 1) * (k + b - 1) * c;
+    const double p2 = ((a2 + a3 * x) * p1 - a4 * p0) / a1;
+    p0 = p1;
+    p1 = p2;
+  }
+  *pn = p1;
+  const double c = 2 * n + a + b;
+  *dpn = (n * ((a - b) - c * x) * p1 + 2 * (n + a) * (n + b) * p0) / (c * (1 - x * x));
+}
+
+void gauss_jacobi20(int n, double *x, double *w) {
+  const int grid = 4000;
+  int found = 0;
+  double xl = -1 + 1e-12, fl, dummy;
+  jacobi20(n, xl, &fl, &dummy);
+  for (int g = 1; g <= grid && found < n; ++g) {
+    const double xr = -1 + 2.0 * g / grid - (g == grid ? 1e-12 : 0.0);
+    double fr;
+    jacobi20(n, xr, &fr, &dummy);
+    if ((fl < 0) != (fr < 0)) {
+      double lo = xl, hi = xr, flo = fl;
+      for (int it = 0; it < 200 && hi - lo > 1e-15; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        double fm;
+        jacobi20(n, mid, &fm, &dummy);
+        if ((fm < 0) == (flo < 0)) { lo = mid; flo = fm; } else { hi = mid; }
+      }
+      double r = 0.5 * (lo + hi);
+      for (int it = 0; it < 3; ++it) {
+        double f, df;
+        jacobi20(n, r, &f, &df);
+        if (df != 0) r -= f / df;
+      }
+      x[found++] = r;
+    }
+    xl = xr;
+    fl = fr;
+  }
+  for (int i = 0; i < n; ++i) {
+    double f, df;
+    jacobi20(n, x[i], &f, &df);
+    w[i] = 8.0 / ((1 - x[i] * x[i]) * df * df);
+  }
+}
+
 void hex8_map(const double *xn, const double *loc, double *x, double *det) {
   double j[9] = {0};
   x[0] = x[1] = x[2] = 0;
@@ -203,7 +272,16 @@ int build_modal_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
   // ---- cells: types, node ids, point counts
   std::vector<int32_t> type(C), vol_off(C + 1, 0);
   TetRule tet = tet_rule(p);
+  std::vector<std::array<double, 2>> tx;
+  std::vector<double> tw;
+  tri_rule(p, &tx, &tw);
+  double jx[8], jw[8];
+  gauss_jacobi20(Q, jx, jw);
   const int n_hex_pts = Q * Q * Q, n_tet_pts = (int)tet.w.size();
+  const int n_wedge_pts = (int)tw.size() * Q, n_pyra_pts = Q * Q * Q;
+  auto n_vol_pts = [&](int t) {
+    return geo::is_hex(t) ? n_hex_pts : geo::is_tet(t) ? n_tet_pts : geo::is_wedge(t) ? n_wedge_pts : n_pyra_pts;
+  };
   const int64_t NS = d->cell_node_stride > 0 ? d->cell_node_stride : 8;
   for (int64_t c = 0; c < C; ++c) {
     int t = d->cell_type ? d->cell_type[c] : MCFD_HEX8;
@@ -216,7 +294,7 @@ int build_modal_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
       if (id < 0 || id >= d->n_nodes)
         return fail(h, MCFD_ERR_MESH, "cell node index out of range in cell " + std::to_string(c));
     }
-    int64_t next = (int64_t)vol_off[c] + (geo::is_hex(t) ? n_hex_pts : n_tet_pts);
+    int64_t next = (int64_t)vol_off[c] + n_vol_pts(t);
     if (next > INT32_MAX) return fail(h, MCFD_ERR_UNSUPPORTED, "more than 2^31 volume points");
     vol_off[c + 1] = (int32_t)next;
   }
@@ -237,12 +315,12 @@ int build_modal_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
     double ctr[3], volume = 0;
     double *X = &md.host_points[(size_t)vol_off[c] * 3];
     std::vector<double> W(vol_off[c + 1] - vol_off[c]);
-    if (geo::curved(type[c])) {
-      // quadratic map: x, det J from the shape functions at every point;
-      // centre at the local centre (hex (0,0,0), tet (1/4,1/4,1/4))
+    if (geo::curved(type[c]) || geo::is_wedge(type[c]) || geo::is_pyramid(type[c])) {
+      // x, det J from the shape functions at every point; centre at the
+      // type's local centre
       const bool is_t = geo::is_tet(type[c]);
-      double J[9];
-      const double cl[3] = {is_t ? 0.25 : 0.0, is_t ? 0.25 : 0.0, is_t ? 0.25 : 0.0};
+      double J[9], cl[3];
+      geo::local_center(type[c], cl);
       geo::map_point(type[c], xn, cl, ctr, J);
       const int nq = (int)W.size();
       for (int q = 0; q < nq; ++q) {
@@ -251,6 +329,14 @@ int build_modal_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
         if (is_t) {
           for (int e = 0; e < 3; ++e) loc[e] = tet.x[q][e];
           wl = tet.w[q];
+        } else if (geo::is_wedge(type[c])) {
+          const int i = q / Q, k = q % Q;
+          loc[0] = tx[i][0]; loc[1] = tx[i][1]; loc[2] = gx[k];
+          wl = tw[i] * gw[k];
+        } else if (geo::is_pyramid(type[c])) {
+          const int i = q / (Q * Q), j = (q / Q) % Q, k = q % Q;
+          loc[0] = gx[i]; loc[1] = gx[j]; loc[2] = jx[k];
+          wl = gw[i] * gw[j] * jw[k] * std::pow(1 - jx[k], -2);
         } else {
           const int i = q / (Q * Q), j = (q / Q) % Q, k = q % Q;
           loc[0] = gx[i]; loc[1] = gx[j]; loc[2] = gx[k];
@@ -346,24 +432,23 @@ int build_modal_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
   std::vector<int32_t> fgroup(F), face_off(F + 1, 0), cell_faces((size_t)C * 6, -1);
   std::vector<int> n_slot(C, 0);
   std::vector<double4> fshift(std::max<int64_t>(F, 1), make_double4(0, 0, 0, 0));
-  std::vector<std::array<double, 2>> tx;
-  std::vector<double> tw;
-  tri_rule(p, &tx, &tw);
   int max_group = -1;
   for (int64_t f = 0; f < F; ++f) {
     int64_t hc = d->face_cells[f * 2], sc = d->face_cells[f * 2 + 1];
     int sh = d->face_sides[f * 2], ss = d->face_sides[f * 2 + 1];
     bool ok = hc >= 0 && hc < C && sc < C && hc <= INT32_MAX;
-    if (ok) ok = sh >= 0 && sh < (geo::is_hex(type[hc]) ? 6 : 4);
+    if (ok) ok = sh >= 0 && sh < geo::face_count(type[hc]);
+    int fv[4];
+    const int nfv_h = ok ? geo::cell_face_corners(type[hc], sh, fv) : 0;
     if (ok && sc >= 0)
-      ok = ss >= 0 && ss < (geo::is_hex(type[sc]) ? 6 : 4) && geo::is_hex(type[sc]) == geo::is_hex(type[hc]);
+      ok = ss >= 0 && ss < geo::face_count(type[sc]) && geo::cell_face_corners(type[sc], ss, fv) == nfv_h;
     if (!ok) return fail(h, MCFD_ERR_MESH, "bad face record " + std::to_string(f));
     fcells[f] = make_int2((int)hc, (int)sc);
     fgroup[f] = d->face_group ? d->face_group[f] : -1;
     if (sc < 0) max_group = std::max(max_group, fgroup[f]);
     if (d->face_shift)
       fshift[f] = make_double4(d->face_shift[f * 3], d->face_shift[f * 3 + 1], d->face_shift[f * 3 + 2], 0);
-    int64_t next = (int64_t)face_off[f] + (geo::is_hex(type[hc]) ? Q * Q : (int)tw.size());
+    int64_t next = (int64_t)face_off[f] + (nfv_h == 4 ? Q * Q : (int)tw.size());
     if (next > INT32_MAX) return fail(h, MCFD_ERR_UNSUPPORTED, "more than 2^31 face points");
     face_off[f + 1] = (int32_t)next;
     const int64_t owners[2] = {hc, sc};
@@ -385,17 +470,15 @@ int build_modal_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
   for (int64_t f = 0; f < F; ++f) {
     int64_t hc = fcells[f].x, sc = fcells[f].y;
     int sh = d->face_sides[f * 2], ss = d->face_sides[f * 2 + 1];
-    const bool hex = geo::is_hex(type[hc]);
-    const int nfv = hex ? 4 : 3;
+    int hv[4], sv[4] = {0, 0, 0, 0};
+    const int nfv = geo::cell_face_corners(type[hc], sh, hv);
+    if (sc >= 0) geo::cell_face_corners(type[sc], ss, sv);
+    const bool hex = nfv == 4;  // quadrangle face
     double xn[12], xs[12];
     for (int v = 0; v < nfv; ++v)
       for (int e = 0; e < 3; ++e) {
-        int slot = hex ? kHexFace[sh][v] : kTetFace[sh][v];
-        xn[v * 3 + e] = d->xyz[d->cell_nodes[hc * NS + slot] * 3 + e];
-        if (sc >= 0) {
-          int sslot = hex ? kHexFace[ss][v] : kTetFace[ss][v];
-          xs[v * 3 + e] = d->xyz[d->cell_nodes[sc * NS + sslot] * 3 + e];
-        }
+        xn[v * 3 + e] = d->xyz[d->cell_nodes[hc * NS + hv[v]] * 3 + e];
+        if (sc >= 0) xs[v * 3 + e] = d->xyz[d->cell_nodes[sc * NS + sv[v]] * 3 + e];
       }
     // the sharer's face must hold the same corners (after the shift)
     if (sc >= 0) {
@@ -418,13 +501,13 @@ int build_modal_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
     int32_t base = face_off[f];
     if (geo::curved(type[hc])) {
       // face points from the holder's cell map at the face's local points;
-      // tangents J^T dloc/da, J^T dloc/db (hex: corner 0 -> 1, 0 -> 3; tet:
-      // corner 0 - corner 2, corner 1 - corner 2 of the face)
+      // tangents J^T dloc/da, J^T dloc/db (quadrangle: corner 0 -> 1, 0 -> 3;
+      // triangle: corner 0 - corner 2, corner 1 - corner 2 of the face)
       double xc[geo::kMaxNodes * 3];
       for (int v = 0; v < geo::node_count(type[hc]); ++v)
         for (int e = 0; e < 3; ++e) xc[v * 3 + e] = d->xyz[d->cell_nodes[hc * NS + v] * 3 + e];
       double lc[4][3];
-      for (int v = 0; v < nfv; ++v) geo::local_of_node(type[hc], hex ? kHexFace[sh][v] : kTetFace[sh][v], lc[v]);
+      for (int v = 0; v < nfv; ++v) geo::local_of_node(type[hc], hv[v], lc[v]);
       double da[3], db[3];
       for (int e = 0; e < 3; ++e) {
         da[e] = hex ? (lc[1][e] - lc[0][e]) / 2 : lc[0][e] - lc[2][e];

@@ -37,7 +37,7 @@ namespace {
 
 const char *const kFieldNames[5] = {"Density", "MomentumX", "MomentumY", "MomentumZ",
                                     "EnergyStagnationDensity"};
-constexpr int kVtkHex27Type = 29, kVtkTet10Type = 24;
+constexpr int kVtkHex27Type = 29, kVtkTet10Type = 24, kVtkWedge15Type = 26;
 constexpr int kK5 = 5;  // conservative variables
 
 int fail(mcfd_handle *h, int code, const std::string &msg) {
@@ -151,27 +151,45 @@ const signed char kHostHex27[27][3] = {
 const signed char kHostTet10Half[10][3] = {{2, 0, 0}, {0, 2, 0}, {0, 0, 2}, {0, 0, 0}, {1, 1, 0},
                                            {0, 1, 1}, {1, 0, 1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
 
-// The VTK points of every cell through its own map (curved meshes).
+// Wedge15 local coordinates (a, b, z) of Writer<Part> (mesh/vtk.hpp:251-270):
+// corners, bottom and top edge midpoints, vertical edge midpoints.
+const double kHostWedge15[15][3] = {
+    {1, 0, -1},   {0, 1, -1},   {0, 0, -1},   {1, 0, 1},     {0, 1, 1},
+    {0, 0, 1},    {0.5, 0.5, -1}, {0, 0.5, -1}, {0.5, 0, -1}, {0.5, 0.5, 1},
+    {0, 0.5, 1},  {0.5, 0, 1},  {1, 0, 0},    {0, 1, 0},     {0, 0, 0}};
+
+// VTK points per cell: Hexahedron27, Tetrahedron10, Wedge15 (host_types 0, 1, 2).
+int vtk_cell_points(uint8_t type) { return type == 1 ? 10 : type == 2 ? 15 : 27; }
+
+// The VTK points of every cell through its own map (quadratic and wedge cells).
 void host_vtk_points(const mcfd_handle *h, const std::vector<int64_t> &off, double *xyz) {
   const auto &m = h->mesh;
   for (int64_t c = 0; c < m.n_cells; ++c) {
     const int t = m.host_cell_type[c];
-    const bool tet = mcfd::geo::is_tet(t);
+    const bool tet = mcfd::geo::is_tet(t), wedge = mcfd::geo::is_wedge(t);
     const double *xn = &m.host_nodes[(size_t)c * mcfd::geo::kMaxNodes * 3];
-    for (int s = 0; s < (tet ? 10 : 27); ++s) {
+    for (int s = 0; s < vtk_cell_points(m.host_types[c]); ++s) {
       double loc[3], J[9];
-      for (int e = 0; e < 3; ++e) loc[e] = tet ? 0.5 * kHostTet10Half[s][e] : kHostHex27[s][e];
+      for (int e = 0; e < 3; ++e)
+        loc[e] = tet ? 0.5 * kHostTet10Half[s][e] : wedge ? kHostWedge15[s][e] : kHostHex27[s][e];
       mcfd::geo::map_point(t, xn, loc, &xyz[(off[c] + s) * 3], J);
     }
   }
 }
 
-// VTK point offsets of the cells (27 per Hex8, 10 per Tet4).
+// VTK point offsets of the cells.
 std::vector<int64_t> vtk_offsets(const mcfd_handle *h) {
   const auto &types = h->mesh.host_types;
   std::vector<int64_t> off(types.size() + 1, 0);
-  for (size_t c = 0; c < types.size(); ++c) off[c + 1] = off[c] + (types[c] == 1 ? 10 : 27);
+  for (size_t c = 0; c < types.size(); ++c) off[c + 1] = off[c] + vtk_cell_points(types[c]);
   return off;
+}
+
+// The reference's writer has no pyramid element (mesh/vtk.hpp:400-414).
+bool has_pyramid(const mcfd_handle *h) {
+  for (uint8_t t : h->mesh.host_types)
+    if (t == 3) return true;
+  return false;
 }
 
 }  // namespace
@@ -195,9 +213,11 @@ int mcfd_write_vtu_arrays(const char *directory, const char *soln_name, int64_t 
       (n_points > 0 && (!xyz || !values)) || (n_cells > 0 && !types))
     return MCFD_ERR_ARGUMENT;
   int64_t total = 0;
+  auto points_of = [](uint8_t t) { return t == kVtkHex27Type ? 27 : t == kVtkWedge15Type ? 15 : 10; };
   for (int64_t c = 0; c < n_cells; ++c) {
-    if (types[c] != kVtkHex27Type && types[c] != kVtkTet10Type) return MCFD_ERR_ARGUMENT;
-    total += types[c] == kVtkHex27Type ? 27 : 10;
+    if (types[c] != kVtkHex27Type && types[c] != kVtkTet10Type && types[c] != kVtkWedge15Type)
+      return MCFD_ERR_ARGUMENT;
+    total += points_of(types[c]);
   }
   if (total != n_points) return MCFD_ERR_ARGUMENT;
   const std::string dir(directory), name(soln_name);
@@ -251,7 +271,7 @@ int mcfd_write_vtu_arrays(const char *directory, const char *soln_name, int64_t 
   {
     std::vector<int32_t> off(n_cells);
     int64_t o = 0;
-    for (int64_t c = 0; c < n_cells; ++c) off[c] = (int32_t)(o += types[c] == kVtkHex27Type ? 27 : 10);
+    for (int64_t c = 0; c < n_cells; ++c) off[c] = (int32_t)(o += points_of(types[c]));
     write_list<int32_t>(vtu, n_cells, [&](int64_t c) { return off[c]; }, binary);
   }
   vtu << "\n        </DataArray>\n";
@@ -267,6 +287,7 @@ int mcfd_write_vtu_arrays(const char *directory, const char *soln_name, int64_t 
 
 int mcfd_vtk_point_count(const mcfd_handle *h, int64_t *n_points) {
   if (!h || !n_points) return MCFD_ERR_ARGUMENT;
+  if (has_pyramid(h)) return MCFD_ERR_UNSUPPORTED;
   *n_points = vtk_offsets(h).back();
   return MCFD_OK;
 }
@@ -274,6 +295,7 @@ int mcfd_vtk_point_count(const mcfd_handle *h, int64_t *n_points) {
 int mcfd_vtk_sample(mcfd_handle *h, double *xyz, double *values, uint8_t *types,
                     int64_t n_points) {
   if (!h || !xyz || !values || !types) return MCFD_ERR_ARGUMENT;
+  if (has_pyramid(h)) return fail(h, MCFD_ERR_UNSUPPORTED, "the VTK writer has no pyramid cell (mesh/vtk.hpp:400-414)");
   const std::vector<int64_t> off = vtk_offsets(h);
   const int64_t np = off.back(), nc = h->mesh.n_cells;
   if (n_points != np) return fail(h, MCFD_ERR_ARGUMENT, "point count mismatch (mcfd_vtk_point_count)");
@@ -302,14 +324,18 @@ int mcfd_vtk_sample(mcfd_handle *h, double *xyz, double *values, uint8_t *types,
   cudaFree(d_xyz);
   cudaFree(d_val);
   if (e != cudaSuccess) return cuda_fail(h, e, "vtk sample");
-  for (int64_t c = 0; c < nc; ++c) types[c] = h->mesh.host_types[c] == 1 ? kVtkTet10Type : kVtkHex27Type;
+  for (int64_t c = 0; c < nc; ++c) {
+    const uint8_t t = h->mesh.host_types[c];
+    types[c] = t == 1 ? kVtkTet10Type : t == 2 ? kVtkWedge15Type : kVtkHex27Type;
+  }
   return MCFD_OK;
 }
 
 int mcfd_write_vtu(mcfd_handle *h, const char *directory, const char *soln_name, int32_t binary) {
   if (!h || !directory || !soln_name) return MCFD_ERR_ARGUMENT;
   int64_t np = 0;
-  mcfd_vtk_point_count(h, &np);
+  if (mcfd_vtk_point_count(h, &np))
+    return fail(h, MCFD_ERR_UNSUPPORTED, "the VTK writer has no pyramid cell (mesh/vtk.hpp:400-414)");
   std::vector<double> xyz(3 * np), values(kK5 * np);
   std::vector<uint8_t> types(h->mesh.n_cells);
   int rc = mcfd_vtk_sample(h, xyz.data(), values.data(), types.data(), np);

@@ -22,7 +22,7 @@
 struct mcfd_vtk_mesh {
   std::vector<double> xyz;
   std::vector<int64_t> cell_nodes;  // [cells][8]
-  std::vector<int32_t> cell_type;   // 0 Hex8, 1 Tet4
+  std::vector<int32_t> cell_type;   // enum mcfd_cell_type (Hex8, Tet4, Wedge6, Pyra5)
   std::vector<int64_t> bface_nodes; // [bfaces][4]
   std::vector<int32_t> bface_group;
 };
@@ -266,9 +266,15 @@ int mcfd_vtk_read(const char *path, const char *group_array, mcfd_vtk_mesh **out
         return vtk_fail("cell " + std::to_string(c) + ": node index out of range");
       }
     const int vt = (int)types[c];
-    if ((vt == 12 && k == 8) || (vt == 10 && k == 4)) {
+    if ((vt == 12 && k == 8) || (vt == 10 && k == 4) || (vt == 14 && k == 5)) {
+      // hexahedron, tetrahedron and pyramid: VTK and CGNS orders agree
       for (int i = 0; i < 8; ++i) m->cell_nodes.push_back(i < k ? node(i) : -1);
-      m->cell_type.push_back(vt == 10 ? 1 : 0);
+      m->cell_type.push_back(vt == 10 ? MCFD_TET4 : vt == 14 ? MCFD_PYRA5 : MCFD_HEX8);
+    } else if (vt == 13 && k == 6) {
+      // wedge: VTK's 0, 1, 2, 3, 4, 5 are CGNS's 0, 2, 1, 3, 5, 4 (mesh/vtk.hpp:236-243)
+      const int perm[6] = {0, 2, 1, 3, 5, 4};
+      for (int i = 0; i < 8; ++i) m->cell_nodes.push_back(i < 6 ? node(perm[i]) : -1);
+      m->cell_type.push_back(MCFD_WEDGE6);
     } else if ((vt == 9 && k == 4) || (vt == 5 && k == 3)) {
       for (int i = 0; i < 4; ++i) m->bface_nodes.push_back(i < k ? node(i) : -1);
       const double g = have_groups ? groups[c] : 0.0;

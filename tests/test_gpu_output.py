@@ -35,10 +35,25 @@ def rel(a, b):
     return np.linalg.norm(a - b) / np.linalg.norm(b)
 
 
+def modal_wedges(p):
+    m = meshlib.concat(meshlib.box((2, 2, 2), periodic=(True,) * 3, jitter=0.1, seed=1),
+                       meshlib.wedge_box((3, 2, 2), periodic=(True,) * 3, jitter=0.1, seed=3))
+    s = General(m, p, "hllc")
+    om = orc.Modal(m, p)
+    u = om.project(cases.smooth_ic(om.points()[0]))
+    s.SetSolutionColumn(u)
+    return s, om, u
+
+
 @pytest.mark.parametrize("p", [1, 2, 3])
-@pytest.mark.parametrize("kind", ["dgsem", "fr", "modal"])
+@pytest.mark.parametrize("kind", ["dgsem", "fr", "modal", "modal_wedges"])
 def test_vtk_sample_matches_oracle(kind, p):
-    s, om, u = modal(p) if kind == "modal" else nodal(p, kind)
+    """Writer<Part>::Prepare: Hexahedron27 / Tetrahedron10 / Wedge15 points
+    (mesh/vtk.hpp:400-493)."""
+    if kind == "modal_wedges":
+        s, om, u = modal_wedges(p)
+    else:
+        s, om, u = modal(p) if kind == "modal" else nodal(p, kind)
     xyz, values, types = s.vtk_sample()
     oxyz, ovalues, otypes = om.vtk_sample(u)
     assert np.array_equal(types, otypes)
@@ -122,3 +137,15 @@ def test_restart_refuses_other_mesh(tmp_path):
         other.read_restart(tmp_path / "missing.rst")
     s.close()
     other.close()
+
+
+def test_pyramids_have_no_vtk_cell(tmp_path):
+    """The reference's writer has no pyramid element (mesh/vtk.hpp:400-414):
+    sampling or writing a mesh with pyramids is refused."""
+    m = meshlib.pyramid_box((2, 2, 2), periodic=(True,) * 3)
+    s = General(m, 2, "hllc")
+    with pytest.raises(capi.McfdError):
+        s.vtk_sample()
+    with pytest.raises(capi.McfdError):
+        s.WriteSolutions(str(tmp_path), "frame")
+    s.close()
