@@ -407,12 +407,38 @@ def mixed_box_config(n_hex, n_tet):
             "l2_flush": "inputs larger than L2 (solution column 1.03 GB)"}
 
 
-def mixed_box_cpu_sample(seconds=12.0, threads=None, fixed_steps=None):
+# All four cell types of the modal scheme: independent periodic unit-cube
+# blocks of Hex8, Tet4 (Kuhn split), Wedge6 (2 per hex) and Pyra5 (6 per hex,
+# apex at the hex's centroid), jitter 0.1 h, the mixed box's initial state.
+ALL_TYPES = (60, 32, 48, 32)
+ALL_TYPES_SAMPLE = (8, 6, 8, 6)
+
+
+def all_types_mesh(n_hex, n_tet, n_wedge, n_pyr):
+    from pvcriemannsolvers_gb300 import mesh as meshlib
+    kw = dict(periodic=(True,) * 3, jitter=0.1, seed=0)
+    return meshlib.concat(meshlib.box((n_hex,) * 3, **kw), meshlib.tet_box((n_tet,) * 3, **kw),
+                          meshlib.wedge_box((n_wedge,) * 3, **kw), meshlib.pyramid_box((n_pyr,) * 3, **kw))
+
+
+def all_types_config(n_hex, n_tet, n_wedge, n_pyr):
+    cells = n_hex ** 3 + 6 * n_tet ** 3 + 2 * n_wedge ** 3 + 6 * n_pyr ** 3
+    m = (MIXED_DEGREE + 1) * (MIXED_DEGREE + 2) * (MIXED_DEGREE + 3) // 6
+    return {"workload": f"all cell types: periodic unit cubes {n_hex}^3 Hex8 + {n_tet}^3 x 6 Tet4 + "
+                        f"{n_wedge}^3 x 2 Wedge6 + {n_pyr}^3 x 6 Pyra5, jitter 0.1 h, modal DG p={MIXED_DEGREE} "
+                        f"(dg::General + Projection), HLLC, SSP-RK3, CFL 0.209 (reference table)",
+            "cells": cells, "dofs": cells * m * K, "form": "plain FP64",
+            "quadrature": "Hex8 Gauss 3^3; Tet4 14; Wedge6 6 x 3; Pyra5 3^2 x Gauss-Jacobi 3; faces Quad4 3^2 / Tri3 6",
+            "step": "dt reduction + 3 RK stages (3 kernels each)",
+            "l2_flush": f"inputs larger than L2 (solution column {8 * cells * m * K / 1e6:.0f} MB)"}
+
+
+def mixed_box_cpu_sample(seconds=12.0, threads=None, fixed_steps=None, kind="mixed_box"):
     import oracle.orc as orc
     orc.build()
     threads = threads or os.cpu_count() or 1
     orc.set_threads(threads)
-    m = mixed_box_mesh(*MIXED_SAMPLE)
+    m = mixed_box_mesh(*MIXED_SAMPLE) if kind == "mixed_box" else all_types_mesh(*ALL_TYPES_SAMPLE)
     o = orc.Modal(m, MIXED_DEGREE)
     x, _ = o.points()
     u = o.project(mixed_box_ic(x))
@@ -427,9 +453,10 @@ def mixed_box_cpu_sample(seconds=12.0, threads=None, fixed_steps=None):
         if (fixed_steps is not None and n >= fixed_steps) or (fixed_steps is None and el >= seconds):
             break
     el = time.perf_counter() - t0
+    what = (f"mixed box {MIXED_SAMPLE[0]}^3 Hex8 + {MIXED_SAMPLE[1]}^3 x 6 Tet4" if kind == "mixed_box" else
+            "all types {}^3 Hex8 + {}^3 x 6 Tet4 + {}^3 x 2 Wedge6 + {}^3 x 6 Pyra5".format(*ALL_TYPES_SAMPLE))
     return {"value": 3 * L * n / el, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"mixed box {MIXED_SAMPLE[0]}^3 Hex8 + {MIXED_SAMPLE[1]}^3 x 6 Tet4 (L = {L} DOFs), "
-                      f"{n} SSP-RK3 steps, {el:.1f} s, oracle (plain C restatement, OpenMP)",
+            "sample": f"{what} (L = {L} DOFs), {n} SSP-RK3 steps, {el:.1f} s, oracle (plain C restatement, OpenMP)",
             "seconds": el, "steps": n}
 
 
@@ -439,19 +466,24 @@ def modal_roofline(kt, m, L, fp64_peak, hbm_peak, peak_src):
     2 K M per face point and side, stage 4 per DOF; bytes: 3 column
     accesses + Hex8 192 B / Tet4 96 B of geometry + 4 B per face slot.
     face kernel: 2 x 2 K M (both traces) + c_R per face point."""
+    from pvcriemannsolvers_gb300 import mesh as meshlib
     M = (MIXED_DEGREE + 1) * (MIXED_DEGREE + 2) * (MIXED_DEGREE + 3) // 6
     Q = MIXED_DEGREE + 1
     ct = m.cell_type
-    n_hex = int((ct == 0).sum())
-    n_tet = int((ct == 1).sum())
-    nq = n_hex * Q ** 3 + n_tet * 14
+    # per type: volume points, geometry bytes (3 doubles per corner), face slots
+    per = {0: (Q ** 3, 192, 6), 1: (14, 96, 4), meshlib.WEDGE6: (6 * Q, 144, 5), meshlib.PYRA5: (Q ** 3, 120, 5)}
+    counts = {t: int((ct == t).sum()) for t in per}
+    nq = sum(counts[t] * per[t][0] for t in per)
     interior = m.face_cells[:, 1] >= 0
-    fq_face = np.where(ct[m.face_cells[:, 0]] == 0, Q * Q, 6)
+    hold = ct[m.face_cells[:, 0]]
+    quad = np.array([meshlib.CELL_FACES[meshlib.family(t)][sd][3] >= 0
+                     for t, sd in zip(hold, m.face_sides[:, 0])]) if (hold > 1).any() else hold == 0
+    fq_face = np.where(quad, Q * Q, 6)
     face_pts = int(fq_face.sum())
     face_sides = int(fq_face.sum() + fq_face[interior].sum())
     cell_flops = 2 * K * 3 * M * nq + 2 * K * M * face_sides + 4 * L
     face_flops = face_pts * (4 * K * M + C_HLLC)
-    cell_bytes = 24 * L + 192 * n_hex + 96 * n_tet + 4 * (6 * n_hex + 4 * n_tet)
+    cell_bytes = 24 * L + sum(counts[t] * per[t][1] for t in per) + 4 * sum(counts[t] * per[t][2] for t in per)
     dom = "cell_update" if kt["cell_update"] >= kt["face_flux"] else "face_flux"
     flops = cell_flops if dom == "cell_update" else face_flops
     t = kt[dom] * 1e-3
@@ -465,14 +497,14 @@ def modal_roofline(kt, m, L, fp64_peak, hbm_peak, peak_src):
             "note": "face_flux includes the Taylor-coefficient kernel a = S^T c"}
 
 
-def run_mixed_box(args, rank, world, local_rank):
+def run_mixed_box(args, rank, world, local_rank, kind="mixed_box"):
     import torch
     from pvcriemannsolvers_gb300 import General, build
     build.build()
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     n_hex, n_tet = args.mixed_cells
-    m = mixed_box_mesh(n_hex, n_tet)
+    m = mixed_box_mesh(n_hex, n_tet) if kind == "mixed_box" else all_types_mesh(*ALL_TYPES)
     res = {}
     u0 = None
     for form in ("fp64", "mixed"):
@@ -512,13 +544,13 @@ def run_mixed_box(args, rank, world, local_rank):
     fp64_peak = fp64_peak_tflops(torch, dev)
     cpu = None
     if not args.no_cpu:
-        cpu = mixed_box_cpu_sample()
+        cpu = mixed_box_cpu_sample(kind=kind)
         cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
     a = res["mixed"]["solution"].reshape(-1, K)[:, 0]
     b = res["fp64"]["solution"].reshape(-1, K)[:, 0]
     r = res["mixed"]
     L = u0.size
-    cfg = mixed_box_config(n_hex, n_tet)
+    cfg = mixed_box_config(n_hex, n_tet) if kind == "mixed_box" else all_types_config(*ALL_TYPES)
     cfg["form"] = "mixed (FP32 contractions; FP64 face states, Riemann fluxes, RK)"
     line = {
         "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world,
@@ -1420,11 +1452,13 @@ def main():
     ap.add_argument("--form", default="both", choices=["both", "fp64", "mixed"],
                     help="precision form(s) to time; the line's value is the mixed form when timed")
     ap.add_argument("--workload", default="vortex",
-                    choices=["vortex", "mixed_box", "ensemble", "quadrant", "output", "reorder", "sod", "viscous"],
+                    choices=["vortex", "mixed_box", "all_types", "ensemble", "quadrant", "output", "reorder", "sod",
+                             "viscous"],
                     help="vortex: the headline DGSEM case; mixed_box: modal DG on hex + tet blocks; "
                          "ensemble: 64 independent cases in one graph per step; output: field "
                          "gather/scatter, VTK sampling and restart on the headline column; viscous: fr::Lobatto "
-                         "with the energy-based artificial viscosity (four-quadrant and Sod demos)")
+                         "with the energy-based artificial viscosity (four-quadrant and Sod demos); all_types: "
+                         "modal DG on Hex8, Tet4, Wedge6 and Pyra5 blocks")
     ap.add_argument("--quadrant-cells", type=int, nargs=3, default=[256, 256, 16], metavar=("NX", "NY", "NZ"),
                     help="mesh of the four-quadrant workload")
     ap.add_argument("--ensemble-scale", type=float, default=1.0,
@@ -1440,8 +1474,8 @@ def main():
     if args.impl == "reference":
         run_reference(args, rank, world)
         return
-    if args.workload == "mixed_box":
-        run_mixed_box(args, rank, world, local_rank)
+    if args.workload in ("mixed_box", "all_types"):
+        run_mixed_box(args, rank, world, local_rank, args.workload)
         return
     if args.workload == "ensemble":
         run_ensemble(args, rank, world, local_rank)
