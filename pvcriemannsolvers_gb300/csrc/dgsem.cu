@@ -58,6 +58,14 @@ struct FaceArgs {
   int visc;             // artificial viscosity: no-slip walls take the wall flux
 };
 
+// FR: a boundary face point without a registered boundary gets no correction
+// (the reference skips such faces); the face kernel marks its flux with this
+// exact NaN bit pattern (kNoFluxBits32 in an FP32 flux buffer: the FP32
+// conversion canonicalises every other NaN) and the FR lift skips exactly
+// that pattern, so a NaN from a degenerate state still reaches the residual.
+constexpr unsigned long long kNoFluxBits = 0x7ff8dead0000beefull;
+constexpr unsigned kNoFluxBits32 = 0x7fbeef01u;
+
 // Face-point flux store: FP64, or FP32 for the mixed form's FP32 lift (one
 // conversion per face point instead of one per lifting cell).
 __device__ __forceinline__ void store_flux(double *flux, int f32_out, int64_t gid,
@@ -66,6 +74,7 @@ __device__ __forceinline__ void store_flux(double *flux, int f32_out, int64_t gi
     float *d = reinterpret_cast<float *>(flux) + gid * kK;
 #pragma unroll
     for (int k = 0; k < kK; ++k) d[k] = f64_to_f32(v[k]);
+    if ((unsigned long long)__double_as_longlong(v[0]) == kNoFluxBits) d[0] = __uint_as_float(kNoFluxBits32);
   } else {
     double *d = flux + gid * kK;
 #pragma unroll
@@ -73,10 +82,6 @@ __device__ __forceinline__ void store_flux(double *flux, int f32_out, int64_t gi
   }
 }
 
-// FR: a boundary face point without a registered boundary gets no correction
-// (the reference skips such faces); the face kernel marks its flux with this
-// NaN payload and the FR lift skips it.
-constexpr unsigned long long kNoFluxBits = 0x7ff8dead0000beefull;
 
 struct CellArgs {
   const double *u_in;
@@ -143,7 +148,7 @@ __global__ void __launch_bounds__(512) face_flux_kernel(FaceArgs a) {
 #pragma unroll
   for (int k = 0; k < kK; ++k) ch[k] = uh[k];
   double out[kK];
-  bool not_converged = false;
+  bool not_converged = false, no_flux = false;
   if (cells.y >= 0) {
     const double *us = a.u + (int64_t)cells.y * KN + map.y * kK;
     double cs[kK];
@@ -195,12 +200,13 @@ __global__ void __launch_bounds__(512) face_flux_kernel(FaceArgs a) {
     } else {
 #pragma unroll
       for (int k = 0; k < kK; ++k) out[k] = 0;
-      if (a.fr) out[0] = __longlong_as_double((long long)kNoFluxBits);
+      no_flux = a.fr != 0;
     }
   }
   if (not_converged) atomicOr(&a.state->status, (unsigned)kStatusNotConverged);
 #pragma unroll
   for (int k = 0; k < kK; ++k) out[k] *= g.w;
+  if (no_flux) out[0] = __longlong_as_double((long long)kNoFluxBits);
   store_flux(a.flux, a.f32_out, gid, out);
 }
 
@@ -325,8 +331,7 @@ cell_update_kernel(CellArgs a) {
     if (v == INT32_MIN) return;
     const double *fl = a.flux + (int64_t)(v >= 0 ? v : ~v) * kK;
     if (a.fr) {
-      const long long b0 = __double_as_longlong(fl[0]);
-      if (((b0 >> 52) & 0x7ff) == 0x7ff && (b0 & 0xFFFFFFFFFFFFFll)) return;  // no boundary
+      if ((unsigned long long)__double_as_longlong(fl[0]) == kNoFluxBits) return;  // no boundary
       const int dir = fr_dir(side);
       const double sigma = fr_sign(side), out_sign = v >= 0 ? 1.0 : -1.0;
 #pragma unroll
@@ -485,8 +490,7 @@ cell_update_mixed_kernel(CellArgs a, const float *__restrict__ geo32) {
     // FP32 face fluxes (the face kernel converts once per face point)
     const float *fl = reinterpret_cast<const float *>(a.flux) + (int64_t)(vv >= 0 ? vv : ~vv) * kK;
     if (a.fr) {
-      const unsigned b0 = __float_as_uint(fl[0]);
-      if (((b0 >> 23) & 0xffu) == 0xffu && (b0 & 0x7fffffu)) return;  // no boundary
+      if (__float_as_uint(fl[0]) == kNoFluxBits32) return;  // no boundary
       const int dir = fr_dir(side);
       const float sigma = fr_sign(side) > 0 ? 1.f : -1.f, out_sign = vv >= 0 ? 1.f : -1.f;
 #pragma unroll

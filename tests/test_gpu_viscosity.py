@@ -230,3 +230,84 @@ def test_viscosity_rejections(gpu):
     with pytest.raises(capi.McfdError):
         s.SetViscosity()
     s.close()
+
+
+def _background_tube(p, nx=16, periodic=(False, True, True)):
+    m = meshlib.box((nx, 2, 2), lengths=(1.0, 0.1, 0.1), periodic=periodic, jitter=0.05, seed=9)
+    x = meshlib.node_coordinates(m, p).reshape(-1, 3)
+    left = cases.prim_to_cons(1.0, 0.1, 0.05, -0.07, 1.0)
+    right = cases.prim_to_cons(0.125, 0.1, 0.05, -0.07, 0.1)
+    u0 = np.where((x[:, 0] < 0.5)[:, None], left[None, :], right[None, :]).ravel()
+    return m, u0, left, right
+
+
+@pytest.mark.parametrize("p", [1, 3])
+def test_viscous_rk3_parity_other_degrees(gpu, p):
+    """p = 1 and p = 3 (spatial factors 4 and 40, viscosity.hpp:581-601),
+    HLLC, on a jittered tube with a background flow."""
+    m, u0, left, right = _background_tube(p)
+    s, om, ov = pair(m, p, "hllc", bcs={0: (orc.BC_SMART, left), 1: (orc.BC_SMART, right)})
+    # the demos' initial limiter puts the jump on cell faces (majority is a
+    # no-op below p = 2, limiter/majority.hpp:17-19)
+    kind = "majority" if p >= 2 else "average"
+    s.SetSolutionColumn(u0)
+    s.InitialLimiter(kind)
+    u, _ = orc.initial_limiter(om, orc.INIT_MAJORITY if p >= 2 else orc.INIT_AVERAGE, u0)
+    assert np.abs(s.GetSolutionColumn() - u).max() <= 1e-14 * np.abs(u).max()
+    s.SetSolutionColumn(u)
+    t = 0.0
+    for _ in range(3):
+        dt = ov.time_step(u, 1.0, 3)
+        assert abs(s.GetTimeStep(1.0, 3) - dt) <= 1e-13 * dt
+        RungeKutta(3).Update(s, t, dt)
+        u = ov.rk_update(orc.HLLC, 3, t, dt, u)
+        t += dt
+    assert ov.properties(u)[0].max() > 0
+    err = rel_l2(s.GetSolutionColumn(), u)
+    assert err <= RTOL, err
+    s.close()
+
+
+def test_viscous_stream_matches_advance(gpu):
+    """mcfd_stream_step (per-slot job graphs: dt pass, then the stages reusing
+    its viscosity properties) gives the columns of mcfd_advance."""
+    p = 2
+    m, u0, left, right = _background_tube(p)
+    s, _, _ = pair(m, p, "roe", bcs={0: (orc.BC_SMART, left), 1: (orc.BC_SMART, right)})
+    s.SetSolutionColumn(u0)
+    s.InitialLimiter("majority")
+    u0 = s.GetSolutionColumn()
+    want = []
+    t = 0.0
+    for _ in range(3):
+        t = s.advance(1, 1.0, 3, t)
+        want.append(s.GetSolutionColumn())
+    host_in = [u0.copy(), want[0].copy(), want[1].copy()]
+    host_out = [np.empty_like(u0) for _ in range(3)]
+    s.stream_begin()
+    for k in range(3):
+        s.stream_step(host_in[k], host_out[k], 0.0, 1, 1.0, 3)
+    s.stream_end()
+    for k in range(3):
+        assert rel_l2(host_out[k], want[k]) <= 1e-15, k
+    s.close()
+
+
+def test_fr_degenerate_state_is_reported(gpu):
+    """A state with negative pressure at a face point (clamped to zero
+    primitives, riemann/euler/types.hpp:194-202) makes the HLLC flux NaN in the
+    oracle; the GPU residual reports the non-finite value instead of treating
+    that face as one without a boundary condition."""
+    p = 2
+    m = meshlib.box((4, 2, 2), lengths=(1.0, 0.5, 0.5), periodic=(True,) * 3)
+    x = meshlib.node_coordinates(m, p).reshape(-1, 3)
+    u = np.tile(cases.prim_to_cons(1.0, 0.1, 0.0, 0.0, 1.0), (x.shape[0], 1))
+    u[0] = [0.16, 0.38, 0.008, -0.011, 0.379]   # kinetic energy above the total
+    u = u.ravel()
+    om = orc.Mesh(m, p, scheme="fr")
+    assert not np.isfinite(om.residual(orc.HLLC, u)).all()
+    s = Lobatto(m, p, "hllc", scheme="fr")
+    s.SetSolutionColumn(u)
+    with pytest.raises(capi.McfdError):
+        s.GetResidualColumn()
+    s.close()
