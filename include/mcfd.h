@@ -115,7 +115,11 @@ enum mcfd_cell_type {
   MCFD_TET10 = 3,
   MCFD_HEX20 = 4,
   MCFD_WEDGE6 = 5, /* coordinate/wedge.hpp Wedge6 (modal scheme): local (a, b, z), c = 1 - a - b */
-  MCFD_PYRA5 = 6   /* coordinate/pyramid.hpp Pyramid5 (modal scheme): collapsed local cube */
+  MCFD_PYRA5 = 6,  /* coordinate/pyramid.hpp Pyramid5 (modal scheme): collapsed local cube */
+  MCFD_WEDGE15 = 7, /* coordinate/wedge.hpp Wedge15 (modal scheme), CGNS PENTA_15 node order */
+  MCFD_WEDGE18 = 8, /* coordinate/wedge.hpp Wedge18 (modal scheme), CGNS PENTA_18 node order */
+  MCFD_PYRA13 = 9,  /* coordinate/pyramid.hpp Pyramid13 (modal scheme), CGNS PYRA_13 node order */
+  MCFD_PYRA14 = 10  /* coordinate/pyramid.hpp Pyramid14 (modal scheme), CGNS PYRA_14 node order */
 };
 
 /* Unstructured mesh, the input that replaces mesh::part::Part

@@ -168,7 +168,8 @@ int orc_rk_update_limited(const orc_mesh *m, int riemann, int n_bc,
 
 /* ---- modal DG: dg::General over Projection on Hex8 / Tet4 (orc_modal.c) ---- */
 enum { ORC_CELL_HEX8 = 0, ORC_CELL_TET4 = 1, ORC_CELL_HEX27 = 2, ORC_CELL_TET10 = 3,
-       ORC_CELL_HEX20 = 4, ORC_CELL_WEDGE6 = 5, ORC_CELL_PYRA5 = 6 };
+       ORC_CELL_HEX20 = 4, ORC_CELL_WEDGE6 = 5, ORC_CELL_PYRA5 = 6, ORC_CELL_WEDGE15 = 7,
+       ORC_CELL_WEDGE18 = 8, ORC_CELL_PYRA13 = 9, ORC_CELL_PYRA14 = 10 };
 typedef struct orc_modal orc_modal;
 /* Same mesh description as orc_mesh_create plus cell types (NULL: all Hex8);
  * a Tet4 cell uses the first 4 of its 8 cell_nodes entries (CGNS order) and

@@ -69,6 +69,12 @@ int orc_rk_generic(orc_residual_fn fn, void *ctx, int64_t L, int order, double t
  * jac[r * 3 + d] = d x_d / d loc_r for the type's nodes xn [n][3]. */
 int orc_type_nodes(int type);
 int orc_type_is_tet(int type);
+int orc_type_is_wedge(int type);
+int orc_type_is_pyramid(int type);
+/* nodes of a quadratic pyramid's face in its face map's order; the point and
+ * tangents of a Triangle6 (n = 6) / Quadrangle8 (8) / Quadrangle9 (9) map */
+int orc_pyramid_face_nodes(int type, int side, int *v);
+void orc_face_map(int n, const double *xf, double s, double t, double *x, double *ts, double *tt);
 void orc_local_of_node(int type, int a, double *loc);
 void orc_map_point(int type, const double *xn, const double *loc, double *x, double *jac);
 /* local faces of a type (4, 5 or 6), the corners of local face `side` in v

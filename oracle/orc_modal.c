@@ -235,7 +235,7 @@ void orc_modal_destroy(orc_modal *m) {
 }
 
 static int cell_points(int type, int p) {
-  if (type == ORC_CELL_WEDGE6) return (p <= 2 ? 6 : 12) * (p + 1);
+  if (orc_type_is_wedge(type)) return (p <= 2 ? 6 : 12) * (p + 1);
   if (!orc_type_is_tet(type)) return (p + 1) * (p + 1) * (p + 1);
   return p <= 2 ? 14 : 24;
 }
@@ -357,8 +357,7 @@ orc_modal *orc_modal_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
     double *ctr = &m->center[c * 3];
     double *X = &m->vx[m->vp_off[c] * 3], *W = &m->vw[m->vp_off[c]];
     double volume = 0;
-    if (t == ORC_CELL_HEX27 || t == ORC_CELL_HEX20 || t == ORC_CELL_TET10 ||
-        t == ORC_CELL_WEDGE6 || t == ORC_CELL_PYRA5) {
+    if (t != ORC_CELL_HEX8 && t != ORC_CELL_TET4) {
       /* points and det J from the shape functions; the centre at the type's
        * local centre */
       const int tet = t == ORC_CELL_TET10;
@@ -371,11 +370,11 @@ orc_modal *orc_modal_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
         if (tet) {
           loc[0] = tx[q][0]; loc[1] = tx[q][1]; loc[2] = tx[q][2];
           wl = tw[q];
-        } else if (t == ORC_CELL_WEDGE6) {
+        } else if (orc_type_is_wedge(t)) {
           int i = q / Q, k = q % Q;
           loc[0] = sx[i][0]; loc[1] = sx[i][1]; loc[2] = gx[k];
           wl = sw[i] * gw[k];
-        } else if (t == ORC_CELL_PYRA5) {
+        } else if (orc_type_is_pyramid(t)) {
           int i = q / (Q * Q), j = (q / Q) % Q, k = q % Q;
           loc[0] = gx[i]; loc[1] = gx[j]; loc[2] = jx[k];
           wl = gw[i] * gw[j] * jw[k] * pow(1 - jx[k], -2);
@@ -470,7 +469,31 @@ orc_modal *orc_modal_create(int64_t n_nodes, const double *xyz, int64_t n_cells,
     double *F = &m->ff[m->fp_off[f] * 9];
     int fvs[4] = {0, 0, 0, 0};
     const int nfvs = (side >= 0 && side < orc_type_faces(t)) ? orc_type_face_corners(t, side, fvs) : 0;
-    if (t == ORC_CELL_HEX27 || t == ORC_CELL_HEX20 || t == ORC_CELL_TET10) {
+    if (t == ORC_CELL_PYRA13 || t == ORC_CELL_PYRA14) {
+      /* quadratic pyramid: the face's own Triangle6 / Quadrangle8 / 9 map */
+      if (side < 0 || side >= 5) { bad = 1; continue; }
+      int fn[9];
+      const int n = orc_pyramid_face_nodes(t, side, fn), quad = n != 6;
+      double xf[27];
+      for (int v = 0; v < n; ++v)
+        for (int d = 0; d < 3; ++d) xf[v * 3 + d] = xyz[cell_nodes[h * NS + fn[v]] * 3 + d];
+      int nq = quad ? Q * Q : ntri;
+      for (int q = 0; q < nq; ++q) {
+        double s = quad ? gx[q / Q] : sx[q][0], tt = quad ? gx[q % Q] : sx[q][1];
+        double wl = quad ? gw[q / Q] * gw[q % Q] : sw[q];
+        double jac[6];
+        orc_face_map(n, xf, s, tt, &X[q * 3], &jac[0], &jac[3]);
+        double *fr = &F[q * 9];
+        cross(&jac[0], &jac[3], &fr[0]);
+        double nn = norm3(&fr[0]);
+        W[q] = wl * nn;
+        for (int d = 0; d < 3; ++d) fr[d] /= nn;
+        double tn = norm3(&jac[0]);
+        for (int d = 0; d < 3; ++d) fr[3 + d] = jac[d] / tn;
+        cross(&fr[0], &fr[3], &fr[6]);
+      }
+    } else if (t == ORC_CELL_HEX27 || t == ORC_CELL_HEX20 || t == ORC_CELL_TET10 || t == ORC_CELL_WEDGE15 ||
+               t == ORC_CELL_WEDGE18) {
       /* quadratic holder through its cell map: face points at the face's local
        * points; tangents J^T dloc/da, J^T dloc/db (quad: corner 0 -> 1,
        * 0 -> 3; triangle: corner 0 - corner 2, corner 1 - corner 2) */
@@ -825,8 +848,8 @@ int64_t orc_modal_vtk_sample(const orc_modal *m, const double *u, double *xyz,
   double psi[MAXM];
   for (int64_t c = 0; c < m->n_cells; ++c) {
     const double *xn = &m->corners[c * 81];
-    const int tet = orc_type_is_tet(m->type[c]), wedge = m->type[c] == ORC_CELL_WEDGE6;
-    if (m->type[c] == ORC_CELL_PYRA5) return -1; /* no pyramid in the writer (vtk.hpp:400-414) */
+    const int tet = orc_type_is_tet(m->type[c]), wedge = orc_type_is_wedge(m->type[c]);
+    if (orc_type_is_pyramid(m->type[c])) return -1; /* no pyramid in the writer (vtk.hpp:400-414) */
     types[c] = tet ? 24 : wedge ? 26 : 29;
     const int n = tet ? 10 : wedge ? 15 : 27;
     for (int s = 0; s < n; ++s, ++pt) {

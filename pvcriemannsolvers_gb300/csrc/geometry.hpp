@@ -18,6 +18,18 @@
 //   Pyra5  (coordinate/pyramid.hpp:124-135): the base corners of the local
 //          cube (+-1, +-1, -1) with the trilinear shape functions, the apex
 //          (0, 0, 1) with (1 + z) / 2: the cube collapses onto the pyramid
+//   Wedge15 (coordinate/wedge.hpp:234-449): Wedge6 plus mid-edge nodes of the
+//          bottom triangle (ab, bc, ca), the vertical edges, the top triangle;
+//          built hierarchically: the new nodes' functions 4ab (1 - z) / 2,
+//          a (1 - z^2), ... and N_a -= N6_a(node j) B_j for the corners
+//   Wedge18 (coordinate/wedge.hpp:456-690): the quadratic triangle times the
+//          quadratic Lagrange polynomials in z; nodes 15-17 at the centres of
+//          the quadrangles (ab, bc, ca at z = 0)
+//   Pyra13 (coordinate/pyramid.hpp:219-412): Pyra5 plus mid-edge nodes of the
+//          base (5-8) and of the lateral edges (9-12, at z = 0 of the local
+//          cube), hierarchically as Wedge15
+//   Pyra14 (coordinate/pyramid.hpp:415-560): Pyra13 plus the base centre (13)
+//          with (1 - x^2)(1 - y^2)(1 - z) / 2
 //
 // Local faces of every type (cell_face_corners) in the reference's node
 // order, each parametrised so that its normal points out of the cell:
@@ -40,9 +52,12 @@ constexpr int kMaxNodes = 27;
 
 inline bool is_tet(int type) { return type == MCFD_TET4 || type == MCFD_TET10; }
 inline bool is_hex(int type) { return type == MCFD_HEX8 || type == MCFD_HEX27 || type == MCFD_HEX20; }
-inline bool is_wedge(int type) { return type == MCFD_WEDGE6; }
-inline bool is_pyramid(int type) { return type == MCFD_PYRA5; }
-inline bool curved(int type) { return type == MCFD_HEX27 || type == MCFD_HEX20 || type == MCFD_TET10; }
+inline bool is_wedge(int type) { return type == MCFD_WEDGE6 || type == MCFD_WEDGE15 || type == MCFD_WEDGE18; }
+inline bool is_pyramid(int type) { return type == MCFD_PYRA5 || type == MCFD_PYRA13 || type == MCFD_PYRA14; }
+inline bool curved(int type) {
+  return type == MCFD_HEX27 || type == MCFD_HEX20 || type == MCFD_TET10 || type == MCFD_WEDGE15 ||
+         type == MCFD_WEDGE18 || type == MCFD_PYRA13 || type == MCFD_PYRA14;
+}
 inline int node_count(int type) {
   switch (type) {
     case MCFD_HEX8: return 8;
@@ -52,6 +67,10 @@ inline int node_count(int type) {
     case MCFD_HEX20: return 20;
     case MCFD_WEDGE6: return 6;
     case MCFD_PYRA5: return 5;
+    case MCFD_WEDGE15: return 15;
+    case MCFD_WEDGE18: return 18;
+    case MCFD_PYRA13: return 13;
+    case MCFD_PYRA14: return 14;
     default: return 0;
   }
 }
@@ -80,6 +99,76 @@ inline int cell_face_corners(int type, int side, int *v) {
   return n;
 }
 
+inline double lq(int c, double x);
+inline double dlq(int c, double x);
+
+// Nodes of local face `side` of a quadratic pyramid in its face map's order
+// (coordinate/pyramid.hpp Pyramid13::faces_ and SortNodesOnFace): the base
+// Quadrangle8 / Quadrangle9 {0, 3, 2, 1, 8, 7, 6, 5 (, 13)}, the lateral
+// Triangle6 faces {i, i + 1, 4, mid(i, i + 1), mid(i + 1, 4), mid(4, i)}.
+inline int pyramid_face_nodes(int type, int side, int *v) {
+  static const int tri[4][6] = {{0, 1, 4, 5, 10, 9}, {1, 2, 4, 6, 11, 10}, {2, 3, 4, 7, 12, 11}, {3, 0, 4, 8, 9, 12}};
+  static const int base[9] = {0, 3, 2, 1, 8, 7, 6, 5, 13};
+  if (side == 0) {
+    const int n = type == MCFD_PYRA14 ? 9 : 8;
+    for (int i = 0; i < n; ++i) v[i] = base[i];
+    return n;
+  }
+  for (int i = 0; i < 6; ++i) v[i] = tri[side - 1][i];
+  return 6;
+}
+
+// Point X and tangents dX/ds, dX/dt of a quadratic face map with n nodes
+// xf[n][3] at face-local (s, t): n = 6 Triangle6 (coordinate/triangle.hpp:
+// nodes (1, 0) (0, 1) (0, 0), then the mid-edges 01, 12, 20), n = 8 / 9
+// Quadrangle8 / Quadrangle9 (coordinate/quadrangle.hpp: corners (-1, -1)
+// (1, -1) (1, 1) (-1, 1), the mid-edges 01, 12, 23, 30, the centre).
+inline void face_map(int n, const double *xf, double s, double t, double *X, double *ts, double *tt) {
+  double N[9], Ds[9], Dt[9];
+  if (n == 6) {
+    const double L[3] = {s, t, 1 - s - t}, dLs[3] = {1, 0, -1}, dLt[3] = {0, 1, -1};
+    for (int i = 0; i < 3; ++i) {
+      const int j = (i + 1) % 3;
+      N[i] = L[i] * (2 * L[i] - 1);
+      Ds[i] = (4 * L[i] - 1) * dLs[i];
+      Dt[i] = (4 * L[i] - 1) * dLt[i];
+      N[3 + i] = 4 * L[i] * L[j];
+      Ds[3 + i] = 4 * (dLs[i] * L[j] + L[i] * dLs[j]);
+      Dt[3 + i] = 4 * (dLt[i] * L[j] + L[i] * dLt[j]);
+    }
+  } else {
+    static const int q[9][2] = {{-1, -1}, {1, -1}, {1, 1}, {-1, 1}, {0, -1}, {1, 0}, {0, 1}, {-1, 0}, {0, 0}};
+    for (int a = 0; a < n; ++a) {
+      const int qs = q[a][0], qt = q[a][1];
+      if (n == 9) {
+        N[a] = lq(qs, s) * lq(qt, t);
+        Ds[a] = dlq(qs, s) * lq(qt, t);
+        Dt[a] = lq(qs, s) * dlq(qt, t);
+      } else if (a < 4) {  // serendipity corner (1 + s qs)(1 + t qt)(s qs + t qt - 1) / 4
+        const double fs = 1 + qs * s, ft = 1 + qt * t, w = qs * s + qt * t - 1;
+        N[a] = fs * ft * w / 4;
+        Ds[a] = qs * ft * (w + fs) / 4;
+        Dt[a] = qt * fs * (w + ft) / 4;
+      } else if (qs == 0) {  // (1 - s^2)(1 + t qt) / 2
+        N[a] = (1 - s * s) * (1 + qt * t) / 2;
+        Ds[a] = -s * (1 + qt * t);
+        Dt[a] = (1 - s * s) * qt / 2;
+      } else {  // (1 + s qs)(1 - t^2) / 2
+        N[a] = (1 + qs * s) * (1 - t * t) / 2;
+        Ds[a] = qs * (1 - t * t) / 2;
+        Dt[a] = -t * (1 + qs * s);
+      }
+    }
+  }
+  for (int e = 0; e < 3; ++e) X[e] = ts[e] = tt[e] = 0;
+  for (int a = 0; a < n; ++a)
+    for (int e = 0; e < 3; ++e) {
+      X[e] += N[a] * xf[a * 3 + e];
+      ts[e] += Ds[a] * xf[a * 3 + e];
+      tt[e] += Dt[a] * xf[a * 3 + e];
+    }
+}
+
 // CGNS local coordinates of the Hex27 nodes (Hex8 and Hex20 are prefixes).
 inline const int (*hex27_local())[3] {
   static const int l[27][3] = {
@@ -98,15 +187,28 @@ inline const int (*tet10_local_half())[3] {
   return l;
 }
 
+// Wedge18 / Pyra14 local coordinates (the lower orders are prefixes).
+inline const double (*wedge18_local())[3] {
+  static const double l[18][3] = {{1, 0, -1},    {0, 1, -1},   {0, 0, -1},    {1, 0, 1},   {0, 1, 1},
+                                  {0, 0, 1},     {.5, .5, -1}, {0, .5, -1},   {.5, 0, -1}, {1, 0, 0},
+                                  {0, 1, 0},     {0, 0, 0},    {.5, .5, 1},   {0, .5, 1},  {.5, 0, 1},
+                                  {.5, .5, 0},   {0, .5, 0},   {.5, 0, 0}};
+  return l;
+}
+inline const double (*pyra14_local())[3] {
+  static const double l[14][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1}, {0, 0, 1},
+                                  {0, -1, -1},  {1, 0, -1},  {0, 1, -1}, {-1, 0, -1}, {-1, -1, 0},
+                                  {1, -1, 0},   {1, 1, 0},   {-1, 1, 0}, {0, 0, -1}};
+  return l;
+}
+
 inline void local_of_node(int type, int a, double *loc) {
-  static const double wedge[6][3] = {{1, 0, -1}, {0, 1, -1}, {0, 0, -1}, {1, 0, 1}, {0, 1, 1}, {0, 0, 1}};
-  static const double pyra[5][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1}, {0, 0, 1}};
   if (is_tet(type)) {
     for (int e = 0; e < 3; ++e) loc[e] = 0.5 * tet10_local_half()[a][e];
   } else if (is_wedge(type)) {
-    for (int e = 0; e < 3; ++e) loc[e] = wedge[a][e];
+    for (int e = 0; e < 3; ++e) loc[e] = wedge18_local()[a][e];
   } else if (is_pyramid(type)) {
-    for (int e = 0; e < 3; ++e) loc[e] = pyra[a][e];
+    for (int e = 0; e < 3; ++e) loc[e] = pyra14_local()[a][e];
   } else {
     for (int e = 0; e < 3; ++e) loc[e] = hex27_local()[a][e];
   }
@@ -135,6 +237,23 @@ inline double lq(int c, double x) {
 }
 inline double dlq(int c, double x) {
   return c == 0 ? -2 * x : x + 0.5 * c;
+}
+
+inline void shapes(int type, const double *loc, double *N, double (*G)[3]);
+
+// Hierarchical enrichment: with the functions B_j of the new nodes
+// j in [n0, n1) (at locals l[j]) already in N / G, the functions of the
+// lower type's nodes a < n0 become N_a - sum_j N_lower,a(l_j) B_j, so every
+// function is 1 at its own node and 0 at the others.
+inline void enrich(int lower, int n0, int n1, const double (*l)[3], double *N, double (*G)[3]) {
+  double Nl[kMaxNodes], Gl[kMaxNodes][3];
+  for (int j = n0; j < n1; ++j) {
+    shapes(lower, l[j], Nl, Gl);
+    for (int a = 0; a < n0; ++a) {
+      N[a] -= Nl[a] * N[j];
+      for (int e = 0; e < 3; ++e) G[a][e] -= Nl[a] * G[j][e];
+    }
+  }
 }
 
 // Shape functions N[a] and gradients G[a][3] at loc.
@@ -213,6 +332,93 @@ inline void shapes(int type, const double *loc, double *N, double (*G)[3]) {
       G[4][0] = G[4][1] = 0;
       G[4][2] = 0.5;
       break;
+    case MCFD_WEDGE15: {
+      shapes(MCFD_WEDGE6, loc, N, G);
+      // the new nodes' functions: 4 L_i L_j (1 -+ z) / 2 on the triangles,
+      // L_i (1 - z^2) on the vertical edges
+      const double L[3] = {x, y, 1 - x - y}, dL[3][2] = {{1, 0}, {0, 1}, {-1, -1}};
+      const double fz[3] = {(1 - z) / 2, 1 - z * z, (1 + z) / 2}, dfz[3] = {-0.5, -2 * z, 0.5};
+      for (int lev = 0; lev < 3; ++lev)
+        for (int i = 0; i < 3; ++i) {
+          const int a = 6 + lev * 3 + i, j = (i + 1) % 3;
+          const double t = lev == 1 ? L[i] : 4 * L[i] * L[j];
+          for (int r = 0; r < 2; ++r)
+            G[a][r] = (lev == 1 ? dL[i][r] : 4 * (dL[i][r] * L[j] + L[i] * dL[j][r])) * fz[lev];
+          N[a] = t * fz[lev];
+          G[a][2] = t * dfz[lev];
+        }
+      enrich(MCFD_WEDGE6, 6, 15, wedge18_local(), N, G);
+      break;
+    }
+    case MCFD_WEDGE18: {
+      // quadratic triangle (corners, then mid-edges ab, bc, ca) x quadratic
+      // Lagrange in z on {-1, 0, 1}
+      const double L[3] = {x, y, 1 - x - y}, dL[3][2] = {{1, 0}, {0, 1}, {-1, -1}};
+      double T[6], dT[6][2];
+      for (int i = 0; i < 3; ++i) {
+        const int j = (i + 1) % 3;
+        T[i] = L[i] * (2 * L[i] - 1);
+        T[3 + i] = 4 * L[i] * L[j];
+        for (int r = 0; r < 2; ++r) {
+          dT[i][r] = (4 * L[i] - 1) * dL[i][r];
+          dT[3 + i][r] = 4 * (dL[i][r] * L[j] + L[i] * dL[j][r]);
+        }
+      }
+      // node -> (triangle node, z level): 0-2 / 3-5 corners at z = -1 / +1,
+      // 6-8 / 12-14 mid-edges at -1 / +1, 9-11 corners at 0, 15-17 mid-edges at 0
+      static const int tri[18] = {0, 1, 2, 0, 1, 2, 3, 4, 5, 0, 1, 2, 3, 4, 5, 3, 4, 5};
+      static const int lev[18] = {-1, -1, -1, 1, 1, 1, -1, -1, -1, 0, 0, 0, 1, 1, 1, 0, 0, 0};
+      for (int a = 0; a < 18; ++a) {
+        const double bz = lq(lev[a], z);
+        N[a] = T[tri[a]] * bz;
+        G[a][0] = dT[tri[a]][0] * bz;
+        G[a][1] = dT[tri[a]][1] * bz;
+        G[a][2] = T[tri[a]] * dlq(lev[a], z);
+      }
+      break;
+    }
+    case MCFD_PYRA13: {
+      shapes(MCFD_PYRA5, loc, N, G);
+      const auto P = pyra14_local();
+      const double qx = 1 - x * x, qy = 1 - y * y, qz = (1 - z * z) / 4;
+      for (int a = 5; a < 13; ++a) {
+        const double ax = P[a][0], ay = P[a][1], az = P[a][2];
+        if (a >= 9) {  // lateral mid-edges: (1 + x ax)(1 + y ay)(1 - z^2) / 4
+          const double fx = 1 + ax * x, fy = 1 + ay * y;
+          N[a] = fx * fy * qz;
+          G[a][0] = ax * fy * qz;
+          G[a][1] = ay * fx * qz;
+          G[a][2] = fx * fy * (-z / 2);
+        } else {  // base mid-edges: bubble of one axis x (1 + t at) / 2 x ((1 + z az) / 2 - qz)
+          const double fz = (1 + az * z) / 2 - qz, dfz = (az + z) / 2;
+          if (ax == 0) {
+            const double fy = (1 + ay * y) / 2;
+            N[a] = qx * fy * fz;
+            G[a][0] = -2 * x * fy * fz;
+            G[a][1] = ay / 2 * qx * fz;
+            G[a][2] = qx * fy * dfz;
+          } else {
+            const double fx = (1 + ax * x) / 2;
+            N[a] = fx * qy * fz;
+            G[a][0] = ax / 2 * qy * fz;
+            G[a][1] = -2 * y * fx * fz;
+            G[a][2] = fx * qy * dfz;
+          }
+        }
+      }
+      enrich(MCFD_PYRA5, 5, 13, P, N, G);
+      break;
+    }
+    case MCFD_PYRA14: {
+      shapes(MCFD_PYRA13, loc, N, G);
+      const double qx = 1 - x * x, qy = 1 - y * y, fz = (1 - z) / 2;
+      N[13] = qx * qy * fz;
+      G[13][0] = -2 * x * qy * fz;
+      G[13][1] = -2 * y * qx * fz;
+      G[13][2] = -qx * qy / 2;
+      enrich(MCFD_PYRA13, 13, 14, pyra14_local(), N, G);
+      break;
+    }
     case MCFD_TET4: {
       N[0] = x; N[1] = y; N[2] = z; N[3] = 1 - x - y - z;
       const double g[4][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {-1, -1, -1}};

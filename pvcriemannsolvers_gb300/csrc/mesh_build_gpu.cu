@@ -42,11 +42,11 @@ constexpr uint64_t kNone = ~0ull;
 enum : unsigned { kErrThree = 1u, kErrProbe = 2u, kErrSameCell = 4u };
 
 // family of a cell: 0 hexahedron (Hex8/20/27), 1 tetrahedron (Tet4/10),
-// 2 wedge, 3 pyramid (enum mcfd_cell_type)
+// 2 wedge (Wedge6/15/18), 3 pyramid (Pyra5/13/14) (enum mcfd_cell_type)
 __device__ __forceinline__ int family(const int32_t *type, int64_t c) {
   if (!type) return 0;
   const int t = type[c];
-  return (t == 1 || t == 3) ? 1 : t == 5 ? 2 : t == 6 ? 3 : 0;
+  return (t == 1 || t == 3) ? 1 : (t == 5 || t == 7 || t == 8) ? 2 : (t == 6 || t == 9 || t == 10) ? 3 : 0;
 }
 
 __device__ __forceinline__ void sort4(uint32_t *k) {

@@ -499,7 +499,27 @@ int build_modal_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
       }
     }
     int32_t base = face_off[f];
-    if (geo::curved(type[hc])) {
+    if (geo::is_pyramid(type[hc]) && geo::curved(type[hc])) {
+      // quadratic pyramid: the face's own Triangle6 / Quadrangle8 / 9 map (the
+      // collapsed cube of the cell map does not hold the lateral triangles)
+      int fn[9];
+      const int n = geo::pyramid_face_nodes(type[hc], sh, fn);
+      double xf[27];
+      for (int v = 0; v < n; ++v)
+        for (int e = 0; e < 3; ++e) xf[v * 3 + e] = d->xyz[d->cell_nodes[hc * NS + fn[v]] * 3 + e];
+      const int nq = hex ? Q * Q : (int)tw.size();
+      for (int q = 0; q < nq; ++q) {
+        const double s = hex ? gx[q / Q] : tx[q][0], t = hex ? gx[q % Q] : tx[q][1];
+        const double wl = hex ? gw[q / Q] * gw[q % Q] : tw[q];
+        double X[3], ta[3], tb[3], nn[3];
+        geo::face_map(n, xf, s, t, X, ta, tb);
+        cross(ta, tb, nn);
+        const double len = norm3(nn);
+        point_face[base + q] = (int32_t)f;
+        fpt[base + q] = make_double4(X[0], X[1], X[2], wl * len);
+        fnrm[base + q] = make_double4(nn[0] / len, nn[1] / len, nn[2] / len, 0);
+      }
+    } else if (geo::curved(type[hc])) {
       // face points from the holder's cell map at the face's local points;
       // tangents J^T dloc/da, J^T dloc/db (quadrangle: corner 0 -> 1, 0 -> 3;
       // triangle: corner 0 - corner 2, corner 1 - corner 2 of the face)

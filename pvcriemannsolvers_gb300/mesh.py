@@ -224,50 +224,85 @@ def hex_shapes(cell_type: int, loc: np.ndarray) -> np.ndarray:
     raise ValueError("not a hexahedron type")
 
 
+# CGNS PENTA_15 / PENTA_18 (coordinate/wedge.hpp Wedge15 / Wedge18): mid-edges
+# 6-14 of the bottom triangle, the vertical edges and the top triangle, then
+# the centres 15-17 of the quadrangles; PYRA_13 / PYRA_14 (coordinate/
+# pyramid.hpp Pyramid13 / Pyramid14): mid-edges 5-8 of the base, 9-12 of the
+# lateral edges, then the base centre 13.
+WEDGE_EDGES = np.array([[0, 1], [1, 2], [2, 0], [0, 3], [1, 4], [2, 5], [3, 4], [4, 5], [5, 3]])
+WEDGE_QUAD_CORNERS = np.array([[0, 1, 4, 3], [1, 2, 5, 4], [2, 0, 3, 5]])
+PYRA_EDGES = np.array([[0, 1], [1, 2], [2, 3], [3, 0], [0, 4], [1, 4], [2, 4], [3, 4]])
+PYRA_BASE = np.array([[0, 1, 2, 3]])
+
+
 def quadratic(m: Mesh, serendipity: bool = False) -> Mesh:
-    """The same mesh with quadratic cells (Hex8 -> Hex27, or Hex20 with
-    serendipity=True; Tet4 -> Tet10): mid-edge, mid-face and centre nodes at
-    the averages of their corners, shared between neighbours, so the geometry
-    is unchanged until the nodes are moved (see deform())."""
+    """The same mesh with quadratic cells: Hex8 -> Hex27 (Hex20 with
+    serendipity=True), Tet4 -> Tet10, Wedge6 -> Wedge18 (Wedge15), Pyra5 ->
+    Pyra14 (Pyra13).  Mid-edge, mid-face and centre nodes sit at the averages
+    of their corners and are shared between neighbours, so the geometry is
+    unchanged until the nodes are moved (see deform())."""
     types = np.zeros(m.n_cells, np.int32) if m.cell_type is None else m.cell_type.astype(np.int32)
-    tet = types == TET4
+    fams = np.array([family(t) for t in types]) if m.cell_type is not None else np.full(m.n_cells, "hex")
+    # family -> (corners, edges, quadrangles with centre nodes, cell centre?, new type, nodes)
+    spec = {
+        "hex": (8, HEX_EDGES, None if serendipity else HEX_FACE_CORNERS, not serendipity,
+                HEX20 if serendipity else HEX27, 20 if serendipity else 27),
+        "tet": (4, TET_EDGES, None, False, TET10, 10),
+        "wedge": (6, WEDGE_EDGES, None if serendipity else WEDGE_QUAD_CORNERS, False,
+                  WEDGE15 if serendipity else WEDGE18, 15 if serendipity else 18),
+        "pyramid": (5, PYRA_EDGES, None if serendipity else PYRA_BASE, False,
+                    PYRA13 if serendipity else PYRA14, 13 if serendipity else 14),
+    }
+    present = [f for f in spec if (fams == f).any()]
+    width = max(spec[f][5] for f in present)
+    cn = np.full((m.n_cells, width), -1, dtype=np.int64)
+    new_types = types.copy()
     xyz = [m.xyz]
     n_nodes = m.xyz.shape[0]
-    stride = 27 if not serendipity or tet.any() else 20
-    cn = np.full((m.n_cells, max(stride, 10 if tet.any() else 0, 20)), -1, dtype=np.int64)
-    cn[:, :8] = m.cell_nodes[:, :8]
 
     def shared(groups):  # groups [k, n]: corner sets -> new node ids (shared by sorted key)
         nonlocal n_nodes
         key = np.sort(groups, axis=1)
         uniq, inv = np.unique(key, axis=0, return_inverse=True)
-        pos = m.xyz[uniq].mean(axis=1)
+        xyz.append(m.xyz[uniq].mean(axis=1))
         ids = n_nodes + np.arange(uniq.shape[0])
-        xyz.append(pos)
         n_nodes += uniq.shape[0]
         return ids[inv.ravel()]
-    hexes = np.flatnonzero(~tet)
-    if hexes.size:
-        corners = m.cell_nodes[hexes, :8]
-        e = shared(corners[:, HEX_EDGES].reshape(-1, 2)).reshape(hexes.size, 12)
-        cn[hexes, 8:20] = e
-        if not serendipity:
-            f = shared(corners[:, HEX_FACE_CORNERS].reshape(-1, 4)).reshape(hexes.size, 6)
-            # CGNS centre order: bottom, -y, +x, +y, -x, top = local faces 0..5
-            cn[hexes, 20:26] = f
-            c = shared(corners)
-            cn[hexes, 26] = c
-    tets = np.flatnonzero(tet)
-    if tets.size:
-        corners = m.cell_nodes[tets, :4]
-        cn[tets, 4:10] = shared(corners[:, TET_EDGES].reshape(-1, 2)).reshape(tets.size, 6)
-        cn[tets, 10:] = -1
-    new_types = np.where(tet, TET10, HEX20 if serendipity else HEX27).astype(np.int32)
-    cn = cn[:, :max(27 if (not serendipity and hexes.size) else 20 if hexes.size else 10, 1)]
+
+    def gather(which):  # corner sets of every present family's table, one shared() call
+        rows, where = [], []
+        for f in present:
+            table = spec[f][which]
+            if table is None:
+                continue
+            cells = np.flatnonzero(fams == f)
+            rows.append(m.cell_nodes[cells][:, table].reshape(-1, table.shape[1]))
+            where.append((f, cells, table.shape[0]))
+        return rows, where
+
+    for f in present:
+        cells = np.flatnonzero(fams == f)
+        nc = spec[f][0]
+        cn[cells, :nc] = m.cell_nodes[cells, :nc]
+        new_types[cells] = spec[f][4]
+    for which in (1, 2):  # mid-edges, then quadrangle centres
+        rows, where = gather(which)
+        if not rows:
+            continue
+        ids = shared(np.concatenate(rows))
+        pos = 0
+        for f, cells, k in where:
+            nc, edges = spec[f][0], spec[f][1]
+            first = nc + (0 if which == 1 else edges.shape[0])
+            cn[cells, first:first + k] = ids[pos:pos + cells.size * k].reshape(cells.size, k)
+            pos += cells.size * k
+    hexes = np.flatnonzero(fams == "hex")
+    if hexes.size and spec["hex"][3]:
+        cn[hexes, 26] = shared(m.cell_nodes[hexes, :8])
     return Mesh(xyz=np.ascontiguousarray(np.concatenate(xyz)), cell_nodes=np.ascontiguousarray(cn),
                 face_cells=m.face_cells, face_sides=m.face_sides, face_group=m.face_group,
-                face_shift=m.face_shift, cell_type=new_types, shape=m.shape, lengths=m.lengths,
-                origin=m.origin, periodic=m.periodic, meta=dict(m.meta))
+                face_shift=m.face_shift, cell_type=new_types.astype(np.int32), shape=m.shape,
+                lengths=m.lengths, origin=m.origin, periodic=m.periodic, meta=dict(m.meta))
 
 
 def deform(m: Mesh, fn) -> Mesh:
@@ -285,6 +320,7 @@ def deform(m: Mesh, fn) -> Mesh:
 TET_FACES = np.array([[0, 2, 1], [0, 1, 3], [0, 3, 2], [1, 2, 3]], dtype=np.int64)
 HEX8, TET4 = 0, 1
 WEDGE6, PYRA5 = 5, 6
+WEDGE15, WEDGE18, PYRA13, PYRA14 = 7, 8, 9, 10
 # local faces of every cell type in the reference's node order (triangles end
 # in -1): coordinate/hexahedron.hpp:353-390, tetrahedron.hpp:141-147,
 # wedge.hpp:211-223, pyramid.hpp:110-121, 199-208
@@ -299,7 +335,8 @@ CORNERS = {"hex": 8, "tet": 4, "wedge": 6, "pyramid": 5}
 
 
 def family(cell_type: int) -> str:
-    return {TET4: "tet", 3: "tet", WEDGE6: "wedge", PYRA5: "pyramid"}.get(int(cell_type), "hex")
+    return {TET4: "tet", 3: "tet", WEDGE6: "wedge", 7: "wedge", 8: "wedge", PYRA5: "pyramid",
+            9: "pyramid", 10: "pyramid"}.get(int(cell_type), "hex")
 
 # Kuhn split of a hex into 6 tetrahedra sharing the (0,0,0)-(1,1,1) diagonal:
 # for each axis permutation (a, b, c) the path 0 -> e_a -> e_a + e_b -> 1.
@@ -616,8 +653,9 @@ def boundary_elements(m: Mesh) -> tuple[np.ndarray, np.ndarray]:
 
 
 def write_vtk(path, m: Mesh, binary: bool = False, classic: bool = False) -> None:
-    """Legacy VTK unstructured grid of m: its cells (Hex8 -> 12, Tet4 -> 10,
-    Wedge6 -> 13 in VTK's node order, Pyra5 -> 14), its boundary faces as
+    """Legacy VTK unstructured grid of m: its cells by their corners (Hex8 ->
+    12, Tet4 -> 10, Wedge6 -> 13 in VTK's node order, Pyra5 -> 14; the
+    quadratic types as the linear cell of their family), its boundary faces as
     quads / triangles (9 / 5) and a CELL_DATA int array "group" (-1 on volume
     cells).  Version-5 OFFSETS / CONNECTIVITY layout, or the classic CELLS
     layout with classic=True (ASCII only)."""
@@ -625,13 +663,13 @@ def write_vtk(path, m: Mesh, binary: bool = False, classic: bool = False) -> Non
     ct = np.zeros(m.n_cells, np.int32) if m.cell_type is None else np.asarray(m.cell_type)
     conn, offs, types = [], [0], []
     for c in range(m.n_cells):
-        t = int(ct[c])
-        if t == WEDGE6:
+        fam = family(int(ct[c]))
+        if fam == "wedge":
             nodes = m.cell_nodes[c, [0, 2, 1, 3, 5, 4]]
         else:
-            nodes = m.cell_nodes[c, :{TET4: 4, PYRA5: 5}.get(t, 8)]
+            nodes = m.cell_nodes[c, :CORNERS[fam]]
         conn.append(nodes); offs.append(offs[-1] + nodes.size)
-        types.append({TET4: 10, WEDGE6: 13, PYRA5: 14}.get(t, 12))
+        types.append({"tet": 10, "wedge": 13, "pyramid": 14}.get(fam, 12))
     for f in range(bn.shape[0]):
         k = 3 if bn[f, 3] < 0 else 4
         conn.append(bn[f, :k]); offs.append(offs[-1] + k); types.append(5 if k == 3 else 9)

@@ -116,3 +116,58 @@ def test_undeformed_quadratic_runs_like_straight():
 def test_curved_limiter_refused():
     with pytest.raises(capi.McfdError):
         Lobatto(nodal_mesh(False), 2, "roe", limiter="eigen")
+
+
+@pytest.mark.parametrize("serendipity", [False, True])
+@pytest.mark.parametrize("p", [1, 2, 3])
+def test_curved_wedge_pyramid_modal_parity(p, serendipity):
+    """Wedge15 / Wedge18 (faces through the cell map) and Pyra13 / Pyra14
+    (faces through their own Triangle6 / Quadrangle8 / 9 maps) in one deformed
+    mesh with Hex27 / Tet10 blocks: residual, SSP-RK3 step and dt against the
+    oracle's nodal (serendipity / Vandermonde) form of the same maps."""
+    m = meshlib.deform(meshlib.quadratic(meshlib.concat(
+        meshlib.wedge_box((2, 3, 2), periodic=(True,) * 3, jitter=0.05, seed=1),
+        meshlib.pyramid_box((2, 2, 2), periodic=(True,) * 3, jitter=0.05, seed=2),
+        meshlib.box((2, 2, 2), periodic=(True,) * 3, jitter=0.05, seed=3)), serendipity=serendipity),
+        wavy(0.02))
+    g = General(m, p, "hllc")
+    om = orc.Modal(m, p)
+    assert np.allclose(g.points(), om.points()[0], rtol=0, atol=1e-13)
+    u = om.project(cases.smooth_ic(om.points()[0]))
+    g.SetSolutionColumn(u)
+    assert rel(g.GetResidualColumn(), om.residual(orc.HLLC, u)) <= 1e-12
+    dt = om.time_step(u, 1.0, 3)
+    g.advance(1, dt, 3, 0.0)
+    u1 = om.rk_update(orc.HLLC, 3, 0.0, dt, u)
+    assert rel(g.GetSolutionColumn(), u1) <= 1e-12
+    g.close()
+
+
+@pytest.mark.parametrize("serendipity", [False, True])
+def test_curved_wedge_vtk_sample(serendipity):
+    """Quadratic wedges write Wedge15 samples through their own maps."""
+    m = meshlib.deform(meshlib.quadratic(meshlib.wedge_box((3, 2, 2), periodic=(True,) * 3, jitter=0.05,
+                                                           seed=6), serendipity=serendipity), wavy(0.02))
+    g = General(m, 2, "hllc")
+    om = orc.Modal(m, 2)
+    u = om.project(cases.smooth_ic(om.points()[0]))
+    g.SetSolutionColumn(u)
+    xyz, values, types = g.vtk_sample()
+    oxyz, ovalues, otypes = om.vtk_sample(u)
+    assert np.array_equal(types, otypes) and set(types.tolist()) == {26}
+    assert rel(xyz, oxyz) <= 1e-14 and rel(values, ovalues) <= 1e-13
+    g.close()
+
+
+def test_undeformed_quadratic_wedge_pyramid_runs_like_straight():
+    m = meshlib.concat(meshlib.wedge_box((3, 2, 2), periodic=(True,) * 3, jitter=0.1, seed=7),
+                       meshlib.pyramid_box((2, 2, 2), periodic=(True,) * 3, jitter=0.1, seed=8))
+    q = meshlib.quadratic(m)
+    om = orc.Modal(m, 3)
+    u = om.project(cases.smooth_ic(om.points()[0]))
+    a, b = General(m, 3, "rusanov"), General(q, 3, "rusanov")
+    for s in (a, b):
+        s.SetSolutionColumn(u)
+    assert rel(b.GetResidualColumn(), a.GetResidualColumn()) <= 1e-12
+    a.close()
+    b.close()

@@ -51,13 +51,16 @@ def test_gpu_builder_errors():
         meshlib.build(m.xyz, bad, device=0)
 
 
+@pytest.mark.parametrize("quad", [False, True])
 @pytest.mark.parametrize("maker", ["wedge_box", "pyramid_box"])
 @pytest.mark.parametrize("periodic", [(False, False, False), (True, False, True)])
-def test_gpu_builder_wedges_and_pyramids(maker, periodic):
-    """Wedge6 and Pyra5 cells (triangle and quadrangle faces of one cell)."""
+def test_gpu_builder_wedges_and_pyramids(maker, periodic, quad):
+    """Wedge6 / Pyra5 cells (triangle and quadrangle faces of one cell) and
+    their quadratic Wedge18 / Pyra14 forms."""
     host = getattr(meshlib, maker)((4, 3, 3), lengths=(1.0, 0.8, 1.3), periodic=periodic, jitter=0.1, seed=5)
     bn, bg = meshlib.boundary_elements(getattr(meshlib, maker)((4, 3, 3), lengths=(1.0, 0.8, 1.3),
                                                                jitter=0.1, seed=5))
     spec = periodic_spec(host, periodic)
-    gpu = meshlib.build(host.xyz, host.cell_nodes, host.cell_type, bn, bg, spec, device=0)
+    src = meshlib.quadratic(host) if quad else host
+    gpu = meshlib.build(src.xyz, src.cell_nodes, src.cell_type, bn, bg, spec, device=0)
     same(gpu, host)

@@ -160,3 +160,21 @@ def test_vtk_reader_errors(tmp_path):
     bad.write_text(text)
     with pytest.raises(capi.McfdError, match="unexpected keyword"):
         meshlib.read_vtk(bad)
+
+
+@pytest.mark.parametrize("serendipity", [False, True])
+@pytest.mark.parametrize("maker", ["wedge_box", "pyramid_box"])
+def test_builder_quadratic_wedges_and_pyramids(maker, serendipity):
+    """Wedge15 / Wedge18 / Pyra13 / Pyra14 cells (corners first, in CGNS
+    order) give the faces of their linear cells."""
+    make = getattr(meshlib, maker)
+    periodic = (True, False, True)
+    open_mesh = make((3, 2, 2), lengths=(1.0, 0.8, 1.3), jitter=0.1, seed=7)
+    want = make((3, 2, 2), lengths=(1.0, 0.8, 1.3), periodic=periodic, jitter=0.1, seed=7)
+    q = meshlib.quadratic(open_mesh, serendipity=serendipity)
+    want_type = {("wedge_box", True): 7, ("wedge_box", False): 8, ("pyramid_box", True): 9,
+                 ("pyramid_box", False): 10}[(maker, serendipity)]
+    assert set(np.unique(q.cell_type).tolist()) == {want_type}
+    bn, bg = meshlib.boundary_elements(open_mesh)
+    got = meshlib.build(q.xyz, q.cell_nodes, q.cell_type, bn, bg, periodic_spec(want, periodic))
+    same_faces(got, want)
