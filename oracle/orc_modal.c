@@ -1,7 +1,8 @@
 /*
  * ORACLE (test infrastructure only): modal DG (dg::General over
  * polynomial::Projection) on Hex8, Tet4, Wedge6 and Pyra5 cells (and the
- * curved Hex20 / Hex27 / Tet10), restated from the reference project.  Parity checker and CPU baseline; the product library
+ * curved Hex20 / Hex27 / Tet10 / Wedge15 / Wedge18 / Pyra13 / Pyra14),
+ * restated from the reference project.  Parity checker and CPU baseline; the product library
  * never calls it.
  *
  *   residual (volume, faces, boundaries)  spatial/dg/general.hpp:58-202

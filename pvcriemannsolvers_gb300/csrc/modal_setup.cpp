@@ -1,6 +1,9 @@
 // Host set-up of the modal DG scheme (dg::General over polynomial::Projection)
 // on Hex8, Tet4, Wedge6 and Pyra5 cells (and the curved Hex20 / Hex27 /
-// Tet10): everything the reference's Part / Cell / Face
+// Tet10 / Wedge15 / Wedge18 / Pyra13 / Pyra14; quadratic pyramids take their
+// face points from the faces' own Triangle6 / Quadrangle8 / Quadrangle9
+// maps, every other curved cell from its cell map): everything the
+// reference's Part / Cell / Face
 // constructors and OrthoNormal bases compute, built once in FP64 and
 // uploaded.
 //
