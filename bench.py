@@ -414,21 +414,41 @@ ALL_TYPES = (60, 32, 48, 32)
 ALL_TYPES_SAMPLE = (8, 6, 8, 6)
 
 
-def all_types_mesh(n_hex, n_tet, n_wedge, n_pyr):
+def _wavy(eps):
+    """x + eps (sin 2 pi y sin 2 pi z, ...): smooth and periodic on the unit cube"""
+    def fn(x):
+        s = np.sin(2 * np.pi * x)
+        y = x.copy()
+        y[:, 0] += eps * s[:, 1] * s[:, 2]
+        y[:, 1] += eps * s[:, 2] * s[:, 0]
+        y[:, 2] += eps * s[:, 0] * s[:, 1]
+        return y
+    return fn
+
+
+def all_types_mesh(n_hex, n_tet, n_wedge, n_pyr, curved=False):
+    """curved: every block quadratic (Hex27, Tet10, Wedge18, Pyra14) with its
+    nodes moved by a smooth periodic deformation of amplitude 0.02."""
     from pvcriemannsolvers_gb300 import mesh as meshlib
     kw = dict(periodic=(True,) * 3, jitter=0.1, seed=0)
-    return meshlib.concat(meshlib.box((n_hex,) * 3, **kw), meshlib.tet_box((n_tet,) * 3, **kw),
-                          meshlib.wedge_box((n_wedge,) * 3, **kw), meshlib.pyramid_box((n_pyr,) * 3, **kw))
+    m = meshlib.concat(meshlib.box((n_hex,) * 3, **kw), meshlib.tet_box((n_tet,) * 3, **kw),
+                       meshlib.wedge_box((n_wedge,) * 3, **kw), meshlib.pyramid_box((n_pyr,) * 3, **kw))
+    return meshlib.deform(meshlib.quadratic(m), _wavy(0.02)) if curved else m
 
 
-def all_types_config(n_hex, n_tet, n_wedge, n_pyr):
+def all_types_config(n_hex, n_tet, n_wedge, n_pyr, curved=False):
     cells = n_hex ** 3 + 6 * n_tet ** 3 + 2 * n_wedge ** 3 + 6 * n_pyr ** 3
     m = (MIXED_DEGREE + 1) * (MIXED_DEGREE + 2) * (MIXED_DEGREE + 3) // 6
-    return {"workload": f"all cell types: periodic unit cubes {n_hex}^3 Hex8 + {n_tet}^3 x 6 Tet4 + "
-                        f"{n_wedge}^3 x 2 Wedge6 + {n_pyr}^3 x 6 Pyra5, jitter 0.1 h, modal DG p={MIXED_DEGREE} "
+    names = ("Hex27", "Tet10", "Wedge18", "Pyra14") if curved else ("Hex8", "Tet4", "Wedge6", "Pyra5")
+    shape = ", quadratic nodes moved by a periodic deformation of amplitude 0.02" if curved else ""
+    return {"workload": f"{'curved' if curved else 'all'} cell types: periodic unit cubes {n_hex}^3 {names[0]} + "
+                        f"{n_tet}^3 x 6 {names[1]} + {n_wedge}^3 x 2 {names[2]} + {n_pyr}^3 x 6 {names[3]}, "
+                        f"jitter 0.1 h{shape}, modal DG p={MIXED_DEGREE} "
                         f"(dg::General + Projection), HLLC, SSP-RK3, CFL 0.209 (reference table)",
             "cells": cells, "dofs": cells * m * K, "form": "plain FP64",
-            "quadrature": "Hex8 Gauss 3^3; Tet4 14; Wedge6 6 x 3; Pyra5 3^2 x Gauss-Jacobi 3; faces Quad4 3^2 / Tri3 6",
+            "quadrature": "hexahedra Gauss 3^3; tetrahedra 14; wedges 6 x 3; pyramids 3^2 x Gauss-Jacobi 3; faces "
+                          "3^2 / 6" + (" (curved: cell maps, pyramid faces on their own Triangle6 / Quadrangle9 maps)"
+                                       if curved else ""),
             "step": "dt reduction + 3 RK stages (3 kernels each)",
             "l2_flush": f"inputs larger than L2 (solution column {8 * cells * m * K / 1e6:.0f} MB)"}
 
@@ -438,7 +458,8 @@ def mixed_box_cpu_sample(seconds=12.0, threads=None, fixed_steps=None, kind="mix
     orc.build()
     threads = threads or os.cpu_count() or 1
     orc.set_threads(threads)
-    m = mixed_box_mesh(*MIXED_SAMPLE) if kind == "mixed_box" else all_types_mesh(*ALL_TYPES_SAMPLE)
+    m = mixed_box_mesh(*MIXED_SAMPLE) if kind == "mixed_box" else \
+        all_types_mesh(*ALL_TYPES_SAMPLE, curved=kind == "curved_types")
     o = orc.Modal(m, MIXED_DEGREE)
     x, _ = o.points()
     u = o.project(mixed_box_ic(x))
@@ -454,7 +475,8 @@ def mixed_box_cpu_sample(seconds=12.0, threads=None, fixed_steps=None, kind="mix
             break
     el = time.perf_counter() - t0
     what = (f"mixed box {MIXED_SAMPLE[0]}^3 Hex8 + {MIXED_SAMPLE[1]}^3 x 6 Tet4" if kind == "mixed_box" else
-            "all types {}^3 Hex8 + {}^3 x 6 Tet4 + {}^3 x 2 Wedge6 + {}^3 x 6 Pyra5".format(*ALL_TYPES_SAMPLE))
+            "all types {}^3 Hex8 + {}^3 x 6 Tet4 + {}^3 x 2 Wedge6 + {}^3 x 6 Pyra5".format(*ALL_TYPES_SAMPLE) +
+            (", quadratic and deformed" if kind == "curved_types" else ""))
     return {"value": 3 * L * n / el, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{what} (L = {L} DOFs), {n} SSP-RK3 steps, {el:.1f} s, oracle (plain C restatement, OpenMP)",
             "seconds": el, "steps": n}
@@ -469,7 +491,10 @@ def modal_roofline(kt, m, L, fp64_peak, hbm_peak, peak_src):
     from pvcriemannsolvers_gb300 import mesh as meshlib
     M = (MIXED_DEGREE + 1) * (MIXED_DEGREE + 2) * (MIXED_DEGREE + 3) // 6
     Q = MIXED_DEGREE + 1
-    ct = m.cell_type
+    # the quadratic types by their family (the kernels read the same
+    # precomputed point data)
+    ct = np.array([0, 1, 0, 1, 0, meshlib.WEDGE6, meshlib.PYRA5, meshlib.WEDGE6, meshlib.WEDGE6, meshlib.PYRA5,
+                   meshlib.PYRA5])[m.cell_type]
     # per type: volume points, geometry bytes (3 doubles per corner), face slots
     per = {0: (Q ** 3, 192, 6), 1: (14, 96, 4), meshlib.WEDGE6: (6 * Q, 144, 5), meshlib.PYRA5: (Q ** 3, 120, 5)}
     counts = {t: int((ct == t).sum()) for t in per}
@@ -504,7 +529,8 @@ def run_mixed_box(args, rank, world, local_rank, kind="mixed_box"):
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     n_hex, n_tet = args.mixed_cells
-    m = mixed_box_mesh(n_hex, n_tet) if kind == "mixed_box" else all_types_mesh(*ALL_TYPES)
+    m = mixed_box_mesh(n_hex, n_tet) if kind == "mixed_box" else \
+        all_types_mesh(*ALL_TYPES, curved=kind == "curved_types")
     res = {}
     u0 = None
     for form in ("fp64", "mixed"):
@@ -550,7 +576,8 @@ def run_mixed_box(args, rank, world, local_rank, kind="mixed_box"):
     b = res["fp64"]["solution"].reshape(-1, K)[:, 0]
     r = res["mixed"]
     L = u0.size
-    cfg = mixed_box_config(n_hex, n_tet) if kind == "mixed_box" else all_types_config(*ALL_TYPES)
+    cfg = mixed_box_config(n_hex, n_tet) if kind == "mixed_box" else \
+        all_types_config(*ALL_TYPES, curved=kind == "curved_types")
     cfg["form"] = "mixed (FP32 contractions; FP64 face states, Riemann fluxes, RK)"
     line = {
         "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world,
@@ -1452,13 +1479,14 @@ def main():
     ap.add_argument("--form", default="both", choices=["both", "fp64", "mixed"],
                     help="precision form(s) to time; the line's value is the mixed form when timed")
     ap.add_argument("--workload", default="vortex",
-                    choices=["vortex", "mixed_box", "all_types", "ensemble", "quadrant", "output", "reorder", "sod",
-                             "viscous"],
+                    choices=["vortex", "mixed_box", "all_types", "curved_types", "ensemble", "quadrant", "output",
+                             "reorder", "sod", "viscous"],
                     help="vortex: the headline DGSEM case; mixed_box: modal DG on hex + tet blocks; "
                          "ensemble: 64 independent cases in one graph per step; output: field "
                          "gather/scatter, VTK sampling and restart on the headline column; viscous: fr::Lobatto "
                          "with the energy-based artificial viscosity (four-quadrant and Sod demos); all_types: "
-                         "modal DG on Hex8, Tet4, Wedge6 and Pyra5 blocks")
+                         "modal DG on Hex8, Tet4, Wedge6 and Pyra5 blocks; curved_types: the same blocks as "
+                         "deformed Hex27, Tet10, Wedge18 and Pyra14 cells")
     ap.add_argument("--quadrant-cells", type=int, nargs=3, default=[256, 256, 16], metavar=("NX", "NY", "NZ"),
                     help="mesh of the four-quadrant workload")
     ap.add_argument("--ensemble-scale", type=float, default=1.0,
@@ -1474,7 +1502,7 @@ def main():
     if args.impl == "reference":
         run_reference(args, rank, world)
         return
-    if args.workload in ("mixed_box", "all_types"):
+    if args.workload in ("mixed_box", "all_types", "curved_types"):
         run_mixed_box(args, rank, world, local_rank, args.workload)
         return
     if args.workload == "ensemble":
