@@ -336,8 +336,14 @@ typedef struct mcfd_vtk_mesh mcfd_vtk_mesh;
 int mcfd_vtk_read(const char *path, const char *group_array, mcfd_vtk_mesh **out);
 int mcfd_vtk_mesh_sizes(const mcfd_vtk_mesh *m, int64_t *n_nodes, int64_t *n_cells,
                         int64_t *n_bfaces);
-/* xyz [n_nodes][3], cell_nodes [n_cells][8] (Tet4: 4 then -1), cell_type
- * [n_cells], bface_nodes [n_bfaces][4] (triangles end in -1), bface_group. */
+/* Slots per cell of cell_nodes: 8, or up to 27 when the file holds quadratic
+ * cells (VTK 25 / 29 hexahedra, 24 tetrahedra, 26 / 32 wedges, 27
+ * pyramids), which are read into CGNS node order (MCFD_HEX20 / HEX27 /
+ * TET10 / WEDGE15 / WEDGE18 / PYRA13). */
+int mcfd_vtk_mesh_stride(const mcfd_vtk_mesh *m, int32_t *stride);
+/* xyz [n_nodes][3], cell_nodes [n_cells][stride] (unused slots -1),
+ * cell_type [n_cells], bface_nodes [n_bfaces][4] (triangles end in -1),
+ * bface_group. */
 int mcfd_vtk_mesh_arrays(const mcfd_vtk_mesh *m, double *xyz, int64_t *cell_nodes,
                          int32_t *cell_type, int64_t *bface_nodes, int32_t *bface_group);
 void mcfd_vtk_mesh_destroy(mcfd_vtk_mesh *m);

@@ -107,6 +107,7 @@ SIGNATURES = {
     "mcfd_vtk_read": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(C.c_void_p)]),
     "mcfd_vtk_mesh_sizes": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                       C.POINTER(C.c_int64)]),
+    "mcfd_vtk_mesh_stride": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "mcfd_vtk_mesh_arrays": (C.c_int, [C.c_void_p, _D, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
                                        C.POINTER(C.c_int64), C.POINTER(C.c_int32)]),
     "mcfd_vtk_mesh_destroy": (None, [C.c_void_p]),

@@ -17,17 +17,49 @@
 #include <string>
 #include <vector>
 
+#include "geometry.hpp"
+
 #include "../../include/mcfd.h"
 
 struct mcfd_vtk_mesh {
   std::vector<double> xyz;
-  std::vector<int64_t> cell_nodes;  // [cells][8]
-  std::vector<int32_t> cell_type;   // enum mcfd_cell_type (Hex8, Tet4, Wedge6, Pyra5)
+  std::vector<int64_t> cell_nodes;  // [cells][stride]
+  std::vector<int32_t> cell_type;   // enum mcfd_cell_type
+  int32_t stride = 8;               // slots per cell: 8, or the most nodes of a quadratic cell
   std::vector<int64_t> bface_nodes; // [bfaces][4]
   std::vector<int32_t> bface_group;
 };
 
 namespace {
+
+// Quadratic VTK cells in CGNS node order: slot i of the CGNS cell holds VTK
+// node vtk[i].  Hexahedra: VTK lists the top mid-edges (12-15) before the
+// vertical ones (16-19) and its face centres as -x, +x, -y, +y, -z, +z
+// (20-25); CGNS HEXA_20 / HEXA_27 the vertical mid-edges first and the
+// centres bottom, -y, +x, +y, -x, top.  Quadratic wedges in the order the
+// reference's solution writer emits them (mesh/vtk.hpp Wedge15): the CGNS
+// corners unflipped (unlike VTK_WEDGE), the mid-edges of the bottom and the
+// top triangles, then the vertical ones (VTK 32 adds the quadrangle centres
+// in CGNS order).  Tetrahedra and pyramids:
+// VTK_QUADRATIC_TETRA / VTK_QUADRATIC_PYRAMID agree with TETRA_10 / PYRA_13.
+struct QuadraticVtk {
+  int vtk_type, n, type;
+  int vtk[27];
+};
+const QuadraticVtk kQuadraticVtk[] = {
+    {25, 20, MCFD_HEX20, {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 16, 17, 18, 19, 12, 13, 14, 15}},
+    {29, 27, MCFD_HEX27, {0,  1,  2,  3,  4,  5,  6,  7,  8,  9,  10, 11, 16, 17,
+                          18, 19, 12, 13, 14, 15, 24, 22, 21, 23, 20, 25, 26}},
+    {24, 10, MCFD_TET10, {0, 1, 2, 3, 4, 5, 6, 7, 8, 9}},
+    {26, 15, MCFD_WEDGE15, {0, 1, 2, 3, 4, 5, 6, 7, 8, 12, 13, 14, 9, 10, 11}},
+    {32, 18, MCFD_WEDGE18, {0, 1, 2, 3, 4, 5, 6, 7, 8, 12, 13, 14, 9, 10, 11, 15, 16, 17}},
+    {27, 13, MCFD_PYRA13, {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12}},
+};
+const QuadraticVtk *quadratic_vtk(int vtk_type, int64_t k) {
+  for (const auto &q : kQuadraticVtk)
+    if (q.vtk_type == vtk_type && q.n == k) return &q;
+  return nullptr;
+}
 
 thread_local std::string g_vtk_error;
 
@@ -266,7 +298,14 @@ int mcfd_vtk_read(const char *path, const char *group_array, mcfd_vtk_mesh **out
         return vtk_fail("cell " + std::to_string(c) + ": node index out of range");
       }
     const int vt = (int)types[c];
-    if ((vt == 12 && k == 8) || (vt == 10 && k == 4) || (vt == 14 && k == 5)) {
+    const QuadraticVtk *qv = quadratic_vtk(vt, k);
+    if (qv) {
+      // CGNS slot i holds VTK node qv->vtk[i]
+      for (int i = 0; i < qv->n; ++i) m->cell_nodes.push_back(node(qv->vtk[i]));
+      for (int i = qv->n; i < 8; ++i) m->cell_nodes.push_back(-1);
+      m->cell_type.push_back(qv->type);
+      m->stride = std::max<int32_t>(m->stride, qv->n);
+    } else if ((vt == 12 && k == 8) || (vt == 10 && k == 4) || (vt == 14 && k == 5)) {
       // hexahedron, tetrahedron and pyramid: VTK and CGNS orders agree
       for (int i = 0; i < 8; ++i) m->cell_nodes.push_back(i < k ? node(i) : -1);
       m->cell_type.push_back(vt == 10 ? MCFD_TET4 : vt == 14 ? MCFD_PYRA5 : MCFD_HEX8);
@@ -281,7 +320,24 @@ int mcfd_vtk_read(const char *path, const char *group_array, mcfd_vtk_mesh **out
       m->bface_group.push_back((int32_t)std::lround(g));
     }
   }
+  if (m->stride > 8) {  // re-lay the cells at the widest cell's stride
+    std::vector<int64_t> wide;
+    wide.reserve(m->cell_type.size() * m->stride);
+    size_t at = 0;
+    for (int32_t t : m->cell_type) {
+      const int n = std::max(8, mcfd::geo::node_count(t));
+      for (int i = 0; i < m->stride; ++i) wide.push_back(i < n ? m->cell_nodes[at + i] : -1);
+      at += n;
+    }
+    m->cell_nodes.swap(wide);
+  }
   *out = m;
+  return MCFD_OK;
+}
+
+int mcfd_vtk_mesh_stride(const mcfd_vtk_mesh *m, int32_t *stride) {
+  if (!m || !stride) return MCFD_ERR_ARGUMENT;
+  *stride = m->stride;
   return MCFD_OK;
 }
 

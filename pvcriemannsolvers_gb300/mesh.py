@@ -652,10 +652,25 @@ def boundary_elements(m: Mesh) -> tuple[np.ndarray, np.ndarray]:
     return nodes, m.face_group[b].astype(np.int32)
 
 
+# Quadratic cells in VTK node order: type -> (VTK type, the CGNS slot of each
+# VTK node); the inverse of the reader's tables (csrc/vtk_reader.cpp).  VTK
+# has no 14-node pyramid: Pyra14 cells are written by their corners.  The
+# quadratic wedges follow the solution writer's Wedge15 (mesh/vtk.hpp): CGNS
+# corners unflipped, bottom, top, then vertical mid-edges.
+_VTK_QUADRATIC = {
+    HEX20: (25, [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 16, 17, 18, 19, 12, 13, 14, 15]),
+    HEX27: (29, [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 16, 17, 18, 19, 12, 13, 14, 15, 24, 22, 21, 23, 20, 25, 26]),
+    TET10: (24, list(range(10))),
+    WEDGE15: (26, [0, 1, 2, 3, 4, 5, 6, 7, 8, 12, 13, 14, 9, 10, 11]),
+    WEDGE18: (32, [0, 1, 2, 3, 4, 5, 6, 7, 8, 12, 13, 14, 9, 10, 11, 15, 16, 17]),
+    PYRA13: (27, list(range(13))),
+}
+
+
 def write_vtk(path, m: Mesh, binary: bool = False, classic: bool = False) -> None:
     """Legacy VTK unstructured grid of m: its cells by their corners (Hex8 ->
     12, Tet4 -> 10, Wedge6 -> 13 in VTK's node order, Pyra5 -> 14; the
-    quadratic types as the linear cell of their family), its boundary faces as
+    quadratic types in VTK's quadratic cells, Pyra14 by its corners), its boundary faces as
     quads / triangles (9 / 5) and a CELL_DATA int array "group" (-1 on volume
     cells).  Version-5 OFFSETS / CONNECTIVITY layout, or the classic CELLS
     layout with classic=True (ASCII only)."""
@@ -663,13 +678,17 @@ def write_vtk(path, m: Mesh, binary: bool = False, classic: bool = False) -> Non
     ct = np.zeros(m.n_cells, np.int32) if m.cell_type is None else np.asarray(m.cell_type)
     conn, offs, types = [], [0], []
     for c in range(m.n_cells):
-        fam = family(int(ct[c]))
-        if fam == "wedge":
+        t = int(ct[c])
+        fam = family(t)
+        if t in _VTK_QUADRATIC:
+            vtk_type, cgns_of_vtk = _VTK_QUADRATIC[t]
+            nodes = m.cell_nodes[c, cgns_of_vtk]
+        elif fam == "wedge":
             nodes = m.cell_nodes[c, [0, 2, 1, 3, 5, 4]]
         else:
             nodes = m.cell_nodes[c, :CORNERS[fam]]
         conn.append(nodes); offs.append(offs[-1] + nodes.size)
-        types.append({"tet": 10, "wedge": 13, "pyramid": 14}.get(fam, 12))
+        types.append(vtk_type if t in _VTK_QUADRATIC else {"tet": 10, "wedge": 13, "pyramid": 14}.get(fam, 12))
     for f in range(bn.shape[0]):
         k = 3 if bn[f, 3] < 0 else 4
         conn.append(bn[f, :k]); offs.append(offs[-1] + k); types.append(5 if k == 3 else 9)
@@ -729,7 +748,9 @@ def read_vtk(path, periodic=(), group_array: str | None = None) -> Mesh:
         nn, nc, nb = C.c_int64(), C.c_int64(), C.c_int64()
         capi.check(lib.mcfd_vtk_mesh_sizes(h, C.byref(nn), C.byref(nc), C.byref(nb)))
         xyz = np.empty((nn.value, 3))
-        cn = np.empty((nc.value, 8), np.int64)
+        stride = C.c_int32()
+        capi.check(lib.mcfd_vtk_mesh_stride(h, C.byref(stride)))
+        cn = np.empty((nc.value, stride.value), np.int64)
         ct = np.empty(nc.value, np.int32)
         bf = np.empty((nb.value, 4), np.int64)
         bg = np.empty(nb.value, np.int32)
@@ -738,4 +759,4 @@ def read_vtk(path, periodic=(), group_array: str | None = None) -> Mesh:
                                             ct.ctypes.data_as(P32), bf.ctypes.data_as(P64), bg.ctypes.data_as(P32)))
     finally:
         lib.mcfd_vtk_mesh_destroy(h)
-    return build(xyz, cn, ct if np.any(ct == TET4) else None, bf, bg, periodic)
+    return build(xyz, cn, ct if np.any(ct != HEX8) else None, bf, bg, periodic)

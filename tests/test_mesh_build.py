@@ -178,3 +178,42 @@ def test_builder_quadratic_wedges_and_pyramids(maker, serendipity):
     bn, bg = meshlib.boundary_elements(open_mesh)
     got = meshlib.build(q.xyz, q.cell_nodes, q.cell_type, bn, bg, periodic_spec(want, periodic))
     same_faces(got, want)
+
+
+@pytest.mark.parametrize("maker", ["box", "tet_box", "wedge_box", "pyramid_box"])
+@pytest.mark.parametrize("serendipity", [False, True])
+def test_vtk_round_trip_quadratic(tmp_path, maker, serendipity):
+    """Quadratic cells through the legacy VTK writer and reader: VTK 25 / 29
+    hexahedra, 24 tetrahedra, 26 / 32 wedges and 27 pyramids come back in CGNS
+    order with their types (Pyra14, which VTK lacks, is written by its
+    corners and comes back as Pyra5)."""
+    q = meshlib.quadratic(getattr(meshlib, maker)((3, 3, 2), jitter=0.1, seed=4), serendipity=serendipity)
+    path = tmp_path / "q.vtk"
+    meshlib.write_vtk(path, q)
+    got = meshlib.read_vtk(path)
+    if maker == "pyramid_box" and not serendipity:
+        assert np.all(got.cell_type == meshlib.PYRA5)
+        assert np.array_equal(got.cell_nodes[:, :5], q.cell_nodes[:, :5])
+    else:
+        assert np.array_equal(got.cell_type, q.cell_type)
+        assert np.array_equal(got.cell_nodes, q.cell_nodes)
+    same_faces(got, q)
+
+
+@pytest.mark.parametrize("maker", ["box", "tet_box", "wedge_box"])
+def test_vtk_quadratic_order_matches_the_writer(maker):
+    """The VTK orders of the quadratic cells are the orders in which the
+    solution writer (mesh/vtk.hpp Hexahedron27 / Tetrahedron10 / Wedge15,
+    restated by the oracle) emits its sample points: on an undeformed
+    quadratic mesh node k of a cell in VTK order sits at sample point k."""
+    m = getattr(meshlib, maker)((3, 3, 3), jitter=0.1, seed=5)
+    q = meshlib.quadratic(m)
+    om = orc.Modal(m, 1)
+    u = om.project(cases.smooth_ic(om.points()[0]))
+    xyz, _, types = om.vtk_sample(u)
+    t = int(q.cell_type[0])
+    _, order = meshlib._VTK_QUADRATIC[t]
+    n = {29: 27, 24: 10, 26: 15}[int(types[0])]
+    pts = xyz.reshape(m.n_cells, n, 3)
+    want = q.xyz[q.cell_nodes[:, order[:n]]]
+    assert np.allclose(pts, want, rtol=0, atol=1e-13)
