@@ -525,6 +525,42 @@ int mcfd_ensemble_stream_end(mcfd_ensemble *e);
  * ensemble from them. */
 int mcfd_autotune(mcfd_handle *h, const char *cache_path, int32_t *choice);
 
+/* ---- device probes (for verification; no handle) ----
+ * mcfd_probe_flux evaluates, on GPU `device`, the flux that a face kernel
+ * computes at one face point, for n points given on caller-owned device
+ * memory: d_left [n][5] the holder's conservative state, d_right [n][5] the
+ * sharer's state (bc_kind == MCFD_BC_NONE: an interior face, the rotated
+ * solver's GetFluxUpwind, riemann/rotated/euler.hpp:153-159) or the given
+ * boundary value (bc_kind = MCFD_BC_INVISCID_WALL .. MCFD_BC_SMART: the
+ * boundary fluxes of rotated/euler.hpp:144-318), d_normal [n][3] unit
+ * normals, d_flux [n][5] the flux through the normal (face weight 1).  The
+ * same device code and template instance as the face kernels of `precision`
+ * (MCFD_MIXED: the seeded square roots of the mixed form), including the
+ * conservative-input fast paths and their primitive fallbacks.  *status
+ * (may be NULL) receives the device status bits (2: the Exact solver hit
+ * its iteration cap, also returned as MCFD_ERR_NOT_CONVERGED).  Restores the
+ * caller's current device. */
+int mcfd_probe_flux(int32_t device, int32_t riemann, int32_t precision,
+                    int32_t bc_kind, int64_t n, const double *d_left,
+                    const double *d_right, const double *d_normal,
+                    double *d_flux, uint32_t *status);
+/* mcfd_probe_numerics applies one operation elementwise to n device values:
+ * the arithmetic that the kernels use in place of CUDA's operators on their
+ * FP64-bound paths, and CUDA's own operators for comparison. */
+enum mcfd_probe_op {
+  MCFD_PROBE_RCP = 0,             /* double -> double: Newton reciprocal 1/x, x > 0 */
+  MCFD_PROBE_RCP_SIGNED = 1,      /* double -> double: Newton reciprocal of either sign */
+  MCFD_PROBE_SQRT_SEEDED = 2,     /* double -> double: FP32-seeded square root, x >= 0 */
+  MCFD_PROBE_F64_TO_F32 = 3,      /* double -> float: integer-pipe rounding conversion */
+  MCFD_PROBE_F32_TO_F64 = 4,      /* float -> double: integer-pipe widening */
+  MCFD_PROBE_CUDA_RCP = 5,        /* double -> double: 1.0 / x */
+  MCFD_PROBE_CUDA_SQRT = 6,       /* double -> double: sqrt(x) */
+  MCFD_PROBE_CUDA_F64_TO_F32 = 7, /* double -> float: __double2float_rn */
+  MCFD_PROBE_CUDA_F32_TO_F64 = 8  /* float -> double: (double)f */
+};
+int mcfd_probe_numerics(int32_t device, int32_t op, int64_t n, const void *d_in,
+                        void *d_out);
+
 /* Message describing the last failure on this handle (or of mcfd_create when
  * h is NULL).  Valid until the next call on the handle. */
 const char *mcfd_last_error(const mcfd_handle *h);

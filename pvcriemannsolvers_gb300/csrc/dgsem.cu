@@ -155,36 +155,20 @@ __global__ void __launch_bounds__(512) face_flux_kernel(FaceArgs a) {
 #pragma unroll
     for (int k = 0; k < kK; ++k) cs[k] = us[k];
     if constexpr (R == kRusanov) {
-      // already multiplied by the face weight
       if (a.trace) {
         const double *th = a.trace + ((int64_t)cells.x * (Q * Q * Q) + map.x) * 3;
         const double *ts = a.trace + ((int64_t)cells.y * (Q * Q * Q) + map.y) * 3;
         const double trh[3] = {th[0], th[1], th[2]}, trs[3] = {ts[0], ts[1], ts[2]};
         flux_rusanov_traced_weighted(ch, trh, cs, trs, n, g.w, out);
-      } else {
-        flux_rusanov_cons_weighted<FAST_SQRT>(ch, cs, n, g.w, out);
+        store_flux(a.flux, a.f32_out, gid, out);
+        return;
       }
-      store_flux(a.flux, a.f32_out, gid, out);
-      return;
-    } else {
-      if constexpr (R == kRoe) {
-        if (flux_roe_cons_weighted<FAST_SQRT>(ch, cs, n, g.w, out)) {
-          store_flux(a.flux, a.f32_out, gid, out);
-          return;
-        }
-      }
-      if constexpr (R == kHllc) {
-        if (flux_hllc_cons<FAST_SQRT>(ch, cs, n, out)) {
-#pragma unroll
-          for (int k = 0; k < kK; ++k) out[k] *= g.w;
-          store_flux(a.flux, a.f32_out, gid, out);
-          return;
-        }
-      }
-      Prim l = cons_to_prim(ch[0], ch[1], ch[2], ch[3], ch[4]);
-      Prim r = cons_to_prim(cs[0], cs[1], cs[2], cs[3], cs[4]);
-      flux_upwind<R>(l, r, n, out, &not_converged);
     }
+    // already multiplied by the face weight
+    interior_flux_weighted<R, FAST_SQRT>(ch, cs, n, g.w, out, &not_converged);
+    if (not_converged) atomicOr(&a.state->status, (unsigned)kStatusNotConverged);
+    store_flux(a.flux, a.f32_out, gid, out);
+    return;
   } else {
     Prim l = cons_to_prim(ch[0], ch[1], ch[2], ch[3], ch[4]);
     int grp = a.face_group[f];

@@ -494,8 +494,13 @@ MCFD_HD void flux_roe(const Prim &l, const Prim &r, const double *n,
   normal_flux(l, el, n, unl, fl);
   normal_flux(r, er, n, unr, fr);
   for (int k = 0; k < kK; ++k) f[k] = (fl[k] + fr[k]) / 2;
-  double h0_l = kGammaOverGm1 * l.p * l.rinv + kinetic(l);
-  double h0_r = kGammaOverGm1 * r.p * r.rinv + kinetic(r);
+  // h0 = gamma p / rho / (gamma - 1) + |u|^2 / 2 (python/equation.py): a
+  // zero density (a vacuum or unconverted state) divides by zero there, so
+  // the flux becomes non-finite as in the prototype
+  const double il = l.rho != 0 ? l.rinv : 1.0 / l.rho;
+  const double ir = r.rho != 0 ? r.rinv : 1.0 / r.rho;
+  double h0_l = kGammaOverGm1 * l.p * il + kinetic(l);
+  double h0_r = kGammaOverGm1 * r.p * ir + kinetic(r);
   double sl = sqrt(l.rho), sr = sqrt(r.rho);
   double inv_sum = rcp_newton(sl + sr);
   double rho = sl * sr;
@@ -884,6 +889,38 @@ MCFD_HD void flux_upwind(const Prim &l, const Prim &r, const double *n,
     flux_roe(l, r, n, f);
   } else {
     flux_exact(l, r, n, f, not_converged);
+  }
+}
+
+// Interior face flux of the face kernels times the face weight w, from the
+// two conservative states: Rusanov, Roe and HLLC take their conservative-
+// input forms, which return false on degenerate states (rho <= 0, E < 0,
+// p < 0; HLLC also p == 0); those states, and the Exact and AUSM solvers,
+// take flux_upwind on the clamped primitives (ConservativeToPrimitive with
+// SetZeroIfNegative).  FAST_SQRT selects the mixed form's seeded roots.
+template <int R, bool FAST_SQRT>
+MCFD_HD void interior_flux_weighted(const double *cl, const double *cr, const double *n,
+                                    double w, double *f, bool *not_converged) {
+  if constexpr (R == kRusanov) {
+    flux_rusanov_cons_weighted<FAST_SQRT>(cl, cr, n, w, f);
+    return;
+  }
+  if constexpr (R == kRoe) {
+    if (flux_roe_cons_weighted<FAST_SQRT>(cl, cr, n, w, f)) return;
+  }
+  if constexpr (R == kHllc) {
+    if (flux_hllc_cons<FAST_SQRT>(cl, cr, n, f)) {
+#pragma unroll
+      for (int k = 0; k < kK; ++k) f[k] *= w;
+      return;
+    }
+  }
+  if constexpr (R != kRusanov) {
+    Prim l = cons_to_prim(cl[0], cl[1], cl[2], cl[3], cl[4]);
+    Prim r = cons_to_prim(cr[0], cr[1], cr[2], cr[3], cr[4]);
+    flux_upwind<R>(l, r, n, f, not_converged);
+#pragma unroll
+    for (int k = 0; k < kK; ++k) f[k] *= w;
   }
 }
 

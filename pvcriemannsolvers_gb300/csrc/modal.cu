@@ -165,18 +165,8 @@ __global__ void __launch_bounds__(512) modal_face_kernel(ModalFaceArgs a) {
     double us[kK];
     taylor_values<M>((x.x - sh.x) - cs.x, (x.y - sh.y) - cs.y, (x.z - sh.z) - cs.z, t);
     eval_taylor<M>(a.taylor + (int64_t)cells.y * M * kK, t, us);
-    bool done = false;
-    if constexpr (R == kHllc) done = flux_hllc_cons<false>(uh, us, n, out);
-    if constexpr (R == kRoe) done = flux_roe_cons_weighted<false>(uh, us, n, 1.0, out);
-    if constexpr (R == kRusanov) {
-      flux_rusanov_cons_weighted<false>(uh, us, n, 1.0, out);
-      done = true;
-    }
-    if (!done) {
-      Prim l = cons_to_prim(uh[0], uh[1], uh[2], uh[3], uh[4]);
-      Prim r = cons_to_prim(us[0], us[1], us[2], us[3], us[4]);
-      flux_upwind<R>(l, r, n, out, &not_converged);
-    }
+    // unit weight (exact): the point weight is applied below
+    interior_flux_weighted<R, false>(uh, us, n, 1.0, out, &not_converged);
   } else {
     Prim l = cons_to_prim(uh[0], uh[1], uh[2], uh[3], uh[4]);
     const int grp = a.face_group[f];
@@ -520,18 +510,8 @@ __global__ void __launch_bounds__(512) modal_face32_kernel(ModalFace32Args a) {
     eval_taylor<M, float>(a.taylor32 + (int64_t)cells.y * M * kK, t, v);
 #pragma unroll
     for (int k = 0; k < kK; ++k) us[k] = f32_to_f64(v[k]);
-    bool done = false;
-    if constexpr (R == kHllc) done = flux_hllc_cons<true>(uh, us, n, out);
-    if constexpr (R == kRoe) done = flux_roe_cons_weighted<true>(uh, us, n, 1.0, out);
-    if constexpr (R == kRusanov) {
-      flux_rusanov_cons_weighted<true>(uh, us, n, 1.0, out);
-      done = true;
-    }
-    if (!done) {
-      Prim l = cons_to_prim(uh[0], uh[1], uh[2], uh[3], uh[4]);
-      Prim r = cons_to_prim(us[0], us[1], us[2], us[3], us[4]);
-      flux_upwind<R>(l, r, n, out, &not_converged);
-    }
+    // unit weight (exact): the point weight is applied below
+    interior_flux_weighted<R, true>(uh, us, n, 1.0, out, &not_converged);
   } else {
     Prim l = cons_to_prim(uh[0], uh[1], uh[2], uh[3], uh[4]);
     const int grp = a.face_group[f];
