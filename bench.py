@@ -321,8 +321,7 @@ def measure_form(args, torch, dist, dev, local_rank, m, u0, precision):
 
 # DRAM bytes (read + write) per launch measured by one ncu capture on the
 # 40^3 p = 3 case (64 000 cells); scaled linearly with the cell count.  Mixed
-# form: profiles/mixed_kernels_vortex40_p3.md (traced face kernel, cell
-# kernel writing the node traces).
+# form: the traced face kernel and the cell kernel writing the node traces.
 NCU_TRAFFIC_40 = {
     ("mixed", "face_flux"): 380.929024e6 + 102.737152e6,
     ("mixed", "cell_update"): 491.185664e6 + 220.190208e6,
@@ -358,16 +357,15 @@ def roofline_of(kt, L, cells, hbm_peak, peak_src, fp64_peak, precision):
 
 
 # FP64-pipe utilisation of the dominant kernels (ncu --set full on the 40^3
-# p = 3 case; profiles/mixed_kernels_vortex40_p3.md,
-# profiles/cell_face_kernels_vortex40_p3_fp64.md): the mixed form's
+# p = 3 case, one capture per kernel): the mixed form's
 # algorithmic FP64 flops (RK accumulation, 4 per DOF) understate the FP64
 # instruction stream (conversions, node traces, positivity), which is what
 # binds the kernel.
 NCU_PIPE_40 = {
     ("mixed", "cell_update"): {"sm__pipe_fp64_cycles_active_pct": 68.0, "issue_active_pct": 47.8,
-                               "source": "profiles/mixed_kernels_vortex40_p3.md"},
+                               "source": "ncu --set full, 40^3 p = 3 case"},
     ("mixed", "face_flux"): {"sm__pipe_fp64_cycles_active_pct": 87.7, "issue_active_pct": 9.5,
-                             "source": "profiles/mixed_kernels_vortex40_p3.md"},
+                             "source": "ncu --set full, 40^3 p = 3 case"},
 }
 
 
@@ -382,17 +380,13 @@ C_HLLC = 120
 
 
 def mixed_box_mesh(n_hex, n_tet):
-    from pvcriemannsolvers_gb300 import mesh as meshlib
-    a = meshlib.box((n_hex,) * 3, periodic=(True,) * 3, jitter=0.1, seed=0)
-    b = meshlib.tet_box((n_tet,) * 3, periodic=(True,) * 3, jitter=0.1, seed=0)
-    return meshlib.concat(a, b)
+    from pvcriemannsolvers_gb300 import cases
+    return cases.mixed_box_mesh(n_hex, n_tet)
 
 
 def mixed_box_ic(x):
     from pvcriemannsolvers_gb300 import cases
-    rho = 1 + 0.2 * np.sin(2 * np.pi * x[:, 0]) * np.cos(2 * np.pi * x[:, 1])
-    n = rho.size
-    return cases.prim_to_cons(rho, np.full(n, 0.5), np.full(n, 0.3), np.full(n, 0.1), np.ones(n))
+    return cases.mixed_box_ic(x)
 
 
 def mixed_box_config(n_hex, n_tet):
@@ -618,36 +612,18 @@ ENSEMBLE_CASES = 64
 
 
 def ensemble_spec(n_cases=ENSEMBLE_CASES, seed=1, scale=1.0):
-    rng = np.random.default_rng(seed)
-    specs = []
-    for k in range(n_cases):
-        count = float(np.exp(rng.uniform(np.log(4000), np.log(200000)))) * scale
-        tet = bool(rng.integers(0, 2))
-        p = int(rng.integers(1, 4))
-        modal_hex = bool(rng.integers(0, 2))
-        waves = [(rng.uniform(0, 0.1), rng.integers(-3, 4, 3), rng.uniform(0, 2 * np.pi)) for _ in range(3)]
-        d = rng.normal(size=3)
-        vel = rng.uniform(0, 0.5) * d / np.linalg.norm(d)
-        n = max(3, int(round((count / 6) ** (1 / 3)))) if tet else max(3, int(round(count ** (1 / 3))))
-        scheme = "modal" if (tet or modal_hex) else "dgsem"
-        specs.append({"case": k, "tet": tet, "p": p, "scheme": scheme, "n": n, "waves": waves, "vel": vel})
-    return specs
+    from pvcriemannsolvers_gb300 import cases
+    return cases.ensemble_spec(n_cases, seed, scale)
 
 
 def ensemble_state(x, spec):
     from pvcriemannsolvers_gb300 import cases
-    rho = np.ones(len(x))
-    for a, kv, phi in spec["waves"]:
-        rho += a * np.sin(2 * np.pi * (x @ kv) + phi)
-    n = len(x)
-    v = spec["vel"]
-    return cases.prim_to_cons(rho, np.full(n, v[0]), np.full(n, v[1]), np.full(n, v[2]), np.ones(n))
+    return cases.ensemble_state(x, spec)
 
 
 def ensemble_mesh(spec):
-    from pvcriemannsolvers_gb300 import mesh as meshlib
-    make = meshlib.tet_box if spec["tet"] else meshlib.box
-    return make((spec["n"],) * 3, periodic=(True,) * 3)
+    from pvcriemannsolvers_gb300 import cases
+    return cases.ensemble_mesh(spec)
 
 
 def build_ensemble(specs, device=0, precision="fp64"):

@@ -112,3 +112,56 @@ def smooth_ic(x: np.ndarray) -> np.ndarray:
     """rho = 1 + 0.2 sin(2 pi x) cos(2 pi y), u = (0.5, 0.3, 0.1), p = 1."""
     rho = 1 + 0.2 * np.sin(2 * math.pi * x[:, 0]) * np.cos(2 * math.pi * x[:, 1])
     return prim_to_cons(rho, 0.5, 0.3, 0.1, 1.0)
+
+
+# ---------------------------------------------------------------- mixed box
+def mixed_box_mesh(n_hex: int, n_tet: int) -> meshlib.Mesh:
+    """Two independent periodic unit-cube blocks: n_hex^3 Hex8 and
+    n_tet^3 x 6 Tet4 (Kuhn split), interior nodes jittered U(-0.1 h, 0.1 h)
+    with seed 0 (the mixed-element box; 100 / 64 at full size)."""
+    a = meshlib.box((n_hex,) * 3, periodic=(True,) * 3, jitter=0.1, seed=0)
+    b = meshlib.tet_box((n_tet,) * 3, periodic=(True,) * 3, jitter=0.1, seed=0)
+    return meshlib.concat(a, b)
+
+
+mixed_box_ic = smooth_ic
+
+
+# ---------------------------------------------------------------- ensemble
+def ensemble_spec(n_cases: int = 64, seed: int = 1, scale: float = 1.0) -> list[dict]:
+    """The batched ensemble's draw (numpy PCG64): per case an element count
+    log-uniform in [4k, 200k] (times scale), Hex8 or 6-tet-split (fair
+    draw), p in {1, 2, 3}, DGSEM or modal DG for Hex8 cases (fair draw;
+    Tet4 cases are modal), rho = 1 + sum of 3 modes a sin(2 pi k.x + phi)
+    with a ~ U(0, 0.1), |k|_inf <= 3, phi ~ U(0, 2 pi), and a uniform
+    velocity of magnitude U(0, 0.5) in a direction on the sphere; p = 1."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for k in range(n_cases):
+        count = float(np.exp(rng.uniform(np.log(4000), np.log(200000)))) * scale
+        tet = bool(rng.integers(0, 2))
+        p = int(rng.integers(1, 4))
+        modal_hex = bool(rng.integers(0, 2))
+        waves = [(rng.uniform(0, 0.1), rng.integers(-3, 4, 3), rng.uniform(0, 2 * np.pi)) for _ in range(3)]
+        d = rng.normal(size=3)
+        vel = rng.uniform(0, 0.5) * d / np.linalg.norm(d)
+        n = max(3, int(round((count / 6) ** (1 / 3)))) if tet else max(3, int(round(count ** (1 / 3))))
+        scheme = "modal" if (tet or modal_hex) else "dgsem"
+        specs.append({"case": k, "tet": tet, "p": p, "scheme": scheme, "n": n, "waves": waves, "vel": vel})
+    return specs
+
+
+def ensemble_state(x: np.ndarray, spec: dict) -> np.ndarray:
+    """Initial state of one ensemble case at points x."""
+    rho = np.ones(len(x))
+    for a, kv, phi in spec["waves"]:
+        rho += a * np.sin(2 * np.pi * (x @ kv) + phi)
+    n = len(x)
+    v = spec["vel"]
+    return prim_to_cons(rho, np.full(n, v[0]), np.full(n, v[1]), np.full(n, v[2]), np.ones(n))
+
+
+def ensemble_mesh(spec: dict) -> meshlib.Mesh:
+    """Periodic unit cube of one ensemble case (n^3 Hex8 or n^3 x 6 Tet4)."""
+    make = meshlib.tet_box if spec["tet"] else meshlib.box
+    return make((spec["n"],) * 3, periodic=(True,) * 3)

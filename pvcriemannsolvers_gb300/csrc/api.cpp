@@ -1110,7 +1110,9 @@ int mcfd_residual_device_noalloc(mcfd_handle *h, const double *d_u,
                     std::to_string(h->mesh.n_points * mcfd::kK) +
                     " scratch doubles, the static capacity is " +
                     std::to_string(mcfd::kStaticFluxCapacity) + " (16 MiB)");
-  CUDA_TRY(h, cudaSetDevice(h->device));
+  // the caller's current device is restored on return
+  mcfd::DeviceGuard guard(h->device);
+  CUDA_TRY(h, cudaGetLastError());
   double *scratch = nullptr;
   std::string why;
   if (mcfd::static_flux_scratch(h->device, &scratch, &why))

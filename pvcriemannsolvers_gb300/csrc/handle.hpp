@@ -13,6 +13,20 @@ struct mcfd_mesh_desc;
 
 namespace mcfd {
 
+// Makes `device` current for a scope and restores the caller's device.
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int device) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    cudaSetDevice(device);
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+  DeviceGuard(const DeviceGuard &) = delete;
+  DeviceGuard &operator=(const DeviceGuard &) = delete;
+};
+
 // Device-side scalars of the time loop.  t and dt live on the device so a
 // whole step (dt reduction + 3 stages) runs without a host round trip.
 struct DevState {

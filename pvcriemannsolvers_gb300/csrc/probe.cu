@@ -20,20 +20,10 @@
 
 #include "../../include/mcfd.h"
 #include "euler.cuh"
+#include "handle.hpp"
 
 namespace mcfd {
 namespace {
-
-struct DeviceGuard {
-  int prev = -1;
-  explicit DeviceGuard(int device) {
-    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-    cudaSetDevice(device);
-  }
-  ~DeviceGuard() {
-    if (prev >= 0) cudaSetDevice(prev);
-  }
-};
 
 template <int R, bool FAST_SQRT>
 __global__ void __launch_bounds__(256)

@@ -1,7 +1,7 @@
 """Generates the golden fixtures under tests/golden/ from the reference project.
 
-Run in a checkout that has the reference project at REFERENCE (default
-/root/reference).  Two sources:
+Run as `python tests/golden/make_golden.py <path of the reference project>`
+(or with the path in the environment variable MCFD_REFERENCE).  Two sources:
 
 1. Known-answer tests of the reference's C++ test suite, transcribed below
    with their file:line.  The script re-reads each cited line and checks that
@@ -25,7 +25,16 @@ from pathlib import Path
 
 import numpy as np
 
-REFERENCE = Path(os.environ.get("MCFD_REFERENCE", "/root/reference"))
+def _reference_path() -> Path:
+    """The reference checkout: the first argument, else $MCFD_REFERENCE."""
+    if len(sys.argv) > 1:
+        return Path(sys.argv[1])
+    if os.environ.get("MCFD_REFERENCE"):
+        return Path(os.environ["MCFD_REFERENCE"])
+    sys.exit("usage: make_golden.py <path of the reference project> (or set MCFD_REFERENCE)")
+
+
+REFERENCE = _reference_path() if __name__ == "__main__" else Path(os.environ.get("MCFD_REFERENCE", "."))
 OUT = Path(__file__).resolve().parent
 
 # ----------------------------------------------------------------------------

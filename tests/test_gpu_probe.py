@@ -172,11 +172,27 @@ def test_exact_vacuum_kat_through_device_flux(gpu, case, form):
         want = flux_of(rw)
     else:
         want = flux_of(to3d(case["expect"], dim))
-    # the reference's absolute tolerance on the Godunov state, or 1e-14
-    # relative for the flux components assembled from it
+    # The reference's absolute tolerance on the Godunov state, or a relative
+    # one for the flux assembled from it.  The device takes conservative
+    # inputs and recovers p = (gamma - 1)(E - |m|^2 / 2 rho), whose condition
+    # number is E / (rho e): 817 for the state of exact.cpp:320 (tangential
+    # speed 54 against a sound speed of 1), so rounding of the inputs reaches
+    # the result amplified by that factor.
+    kappa = max(input_condition(w) for w in (lw, rw))
+    rel = max(1e-14, 16 * np.finfo(float).eps * kappa)
     for comp in components(dim):
-        assert abs(got[0, comp] - want[comp]) <= max(case["atol"], 1e-14 * abs(want[comp])), \
+        assert abs(got[0, comp] - want[comp]) <= max(case["atol"], rel * abs(want[comp])), \
             (comp, got[0], want)
+
+
+def input_condition(prim):
+    """E / (rho e) of a primitive state: the amplification of relative
+    rounding in the conservative variables into the recovered pressure."""
+    rho, u, v, w, p = prim
+    if rho <= 0 or p <= 0:
+        return 1.0
+    internal = p / (G - 1)
+    return (internal + 0.5 * rho * (u * u + v * v + w * w)) / internal
 
 
 def kat_state_pairs():
