@@ -36,12 +36,17 @@ namespace {
 // node vtk[i].  Hexahedra: VTK lists the top mid-edges (12-15) before the
 // vertical ones (16-19) and its face centres as -x, +x, -y, +y, -z, +z
 // (20-25); CGNS HEXA_20 / HEXA_27 the vertical mid-edges first and the
-// centres bottom, -y, +x, +y, -x, top.  Quadratic wedges in the order the
-// reference's solution writer emits them (mesh/vtk.hpp Wedge15): the CGNS
-// corners unflipped (unlike VTK_WEDGE), the mid-edges of the bottom and the
-// top triangles, then the vertical ones (VTK 32 adds the quadrangle centres
-// in CGNS order).  Tetrahedra and pyramids:
-// VTK_QUADRATIC_TETRA / VTK_QUADRATIC_PYRAMID agree with TETRA_10 / PYRA_13.
+// centres bottom, -y, +x, +y, -x, top.  Quadratic wedges come in two
+// layouts: VTK's own (VTK_QUADRATIC_WEDGE / VTK_BIQUADRATIC_QUADRATIC_WEDGE
+// share VTK_WEDGE's corner orientation, so CGNS corners 0, 1, 2, 3, 4, 5 are
+// VTK's 0, 2, 1, 3, 5, 4 as for VTK_WEDGE, mesh/vtk.hpp:236-243, with the
+// mid-edge and quadrangle-centre slots permuted to match), and the order the
+// reference's solution writer emits (mesh/vtk.hpp Wedge15: the CGNS corners
+// unflipped, the mid-edges of the bottom and the top triangles, then the
+// vertical ones, VTK 32 adding the quadrangle centres in CGNS order).  The
+// reader takes the layout in which the cell's corner wedge has a positive
+// volume.  Tetrahedra and pyramids: VTK_QUADRATIC_TETRA /
+// VTK_QUADRATIC_PYRAMID agree with TETRA_10 / PYRA_13.
 struct QuadraticVtk {
   int vtk_type, n, type;
   int vtk[27];
@@ -54,6 +59,11 @@ const QuadraticVtk kQuadraticVtk[] = {
     {26, 15, MCFD_WEDGE15, {0, 1, 2, 3, 4, 5, 6, 7, 8, 12, 13, 14, 9, 10, 11}},
     {32, 18, MCFD_WEDGE18, {0, 1, 2, 3, 4, 5, 6, 7, 8, 12, 13, 14, 9, 10, 11, 15, 16, 17}},
     {27, 13, MCFD_PYRA13, {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12}},
+};
+// VTK's own quadratic wedge layouts (corners flipped as VTK_WEDGE).
+const QuadraticVtk kVtkWedge[] = {
+    {26, 15, MCFD_WEDGE15, {0, 2, 1, 3, 5, 4, 8, 7, 6, 12, 14, 13, 11, 10, 9}},
+    {32, 18, MCFD_WEDGE18, {0, 2, 1, 3, 5, 4, 8, 7, 6, 12, 14, 13, 11, 10, 9, 17, 16, 15}},
 };
 const QuadraticVtk *quadratic_vtk(int vtk_type, int64_t k) {
   for (const auto &q : kQuadraticVtk)
@@ -299,6 +309,19 @@ int mcfd_vtk_read(const char *path, const char *group_array, mcfd_vtk_mesh **out
       }
     const int vt = (int)types[c];
     const QuadraticVtk *qv = quadratic_vtk(vt, k);
+    if (qv && (qv->type == MCFD_WEDGE15 || qv->type == MCFD_WEDGE18)) {
+      // VTK's layout when its flipped corners give a positive corner wedge
+      // ((x1 - x0) x (x2 - x0) . (x3 - x0) > 0 in CGNS order), else the
+      // reference writer's
+      const QuadraticVtk *vq = &kVtkWedge[qv->type == MCFD_WEDGE15 ? 0 : 1];
+      const double *x0 = &m->xyz[3 * node(vq->vtk[0])], *x1 = &m->xyz[3 * node(vq->vtk[1])];
+      const double *x2 = &m->xyz[3 * node(vq->vtk[2])], *x3 = &m->xyz[3 * node(vq->vtk[3])];
+      double a[3], b[3], d[3];
+      for (int i = 0; i < 3; ++i) a[i] = x1[i] - x0[i], b[i] = x2[i] - x0[i], d[i] = x3[i] - x0[i];
+      const double vol = (a[1] * b[2] - a[2] * b[1]) * d[0] + (a[2] * b[0] - a[0] * b[2]) * d[1] +
+                         (a[0] * b[1] - a[1] * b[0]) * d[2];
+      if (vol > 0) qv = vq;
+    }
     if (qv) {
       // CGNS slot i holds VTK node qv->vtk[i]
       for (int i = 0; i < qv->n; ++i) m->cell_nodes.push_back(node(qv->vtk[i]));
@@ -314,10 +337,21 @@ int mcfd_vtk_read(const char *path, const char *group_array, mcfd_vtk_mesh **out
       const int perm[6] = {0, 2, 1, 3, 5, 4};
       for (int i = 0; i < 8; ++i) m->cell_nodes.push_back(i < 6 ? node(perm[i]) : -1);
       m->cell_type.push_back(MCFD_WEDGE6);
-    } else if ((vt == 9 && k == 4) || (vt == 5 && k == 3)) {
-      for (int i = 0; i < 4; ++i) m->bface_nodes.push_back(i < k ? node(i) : -1);
+    } else if ((vt == 9 && k == 4) || (vt == 5 && k == 3) || (vt == 22 && k == 6) ||
+               (vt == 23 && k == 8) || (vt == 28 && k == 9)) {
+      // boundary elements: quads and triangles, the quadratic ones (VTK 22
+      // triangle, 23 / 28 quadrangles) by their corners, which VTK lists first
+      const int nc = (vt == 5 || vt == 22) ? 3 : 4;
+      for (int i = 0; i < 4; ++i) m->bface_nodes.push_back(i < nc ? node(i) : -1);
       const double g = have_groups ? groups[c] : 0.0;
       m->bface_group.push_back((int32_t)std::lround(g));
+    } else if (vt == 1 || vt == 2 || vt == 3 || vt == 4 || vt == 21) {
+      // vertices and lines (mesh generators' physical points and curves)
+      // bound no volume and no face: skipped
+    } else {
+      delete m;
+      return vtk_fail("cell " + std::to_string(c) + ": unsupported VTK cell type " + std::to_string(vt) +
+                      " with " + std::to_string(k) + " nodes");
     }
   }
   if (m->stride > 8) {  // re-lay the cells at the widest cell's stride

@@ -676,6 +676,10 @@ def write_vtk(path, m: Mesh, binary: bool = False, classic: bool = False) -> Non
     layout with classic=True (ASCII only)."""
     bn, bg = boundary_elements(m)
     ct = np.zeros(m.n_cells, np.int32) if m.cell_type is None else np.asarray(m.cell_type)
+    if np.any(ct == PYRA14):
+        import warnings
+        warnings.warn("write_vtk: VTK has no 14-node pyramid; Pyra14 cells are written by their 5 corners "
+                      "and read back as straight-sided Pyra5 cells", stacklevel=2)
     conn, offs, types = [], [0], []
     for c in range(m.n_cells):
         t = int(ct[c])

@@ -189,7 +189,11 @@ def test_vtk_round_trip_quadratic(tmp_path, maker, serendipity):
     corners and comes back as Pyra5)."""
     q = meshlib.quadratic(getattr(meshlib, maker)((3, 3, 2), jitter=0.1, seed=4), serendipity=serendipity)
     path = tmp_path / "q.vtk"
-    meshlib.write_vtk(path, q)
+    if maker == "pyramid_box" and not serendipity:
+        with pytest.warns(UserWarning, match="Pyra14 cells are written by their 5 corners"):
+            meshlib.write_vtk(path, q)
+    else:
+        meshlib.write_vtk(path, q)
     got = meshlib.read_vtk(path)
     if maker == "pyramid_box" and not serendipity:
         assert np.all(got.cell_type == meshlib.PYRA5)
@@ -217,3 +221,72 @@ def test_vtk_quadratic_order_matches_the_writer(maker):
     pts = xyz.reshape(m.n_cells, n, 3)
     want = q.xyz[q.cell_nodes[:, order[:n]]]
     assert np.allclose(pts, want, rtol=0, atol=1e-13)
+
+
+def write_classic_vtk(path, xyz, cells):
+    """A legacy ASCII VTK file written directly: cells = [(vtk type, node
+    ids, group)], CELL_DATA "group"."""
+    lines = ["# vtk DataFile Version 3.0", "hand-written", "ASCII", "DATASET UNSTRUCTURED_GRID",
+             f"POINTS {len(xyz)} double"]
+    lines += [" ".join(repr(float(v)) for v in p) for p in xyz]
+    size = sum(1 + len(n) for _, n, _ in cells)
+    lines.append(f"CELLS {len(cells)} {size}")
+    lines += [" ".join(str(int(v)) for v in [len(n), *n]) for _, n, _ in cells]
+    lines.append(f"CELL_TYPES {len(cells)}")
+    lines += [str(t) for t, _, _ in cells]
+    lines += [f"CELL_DATA {len(cells)}", "SCALARS group int 1", "LOOKUP_TABLE default"]
+    lines += [str(g) for _, _, g in cells]
+    path.write_text("\n".join(lines) + "\n")
+
+
+# VTK_QUADRATIC_WEDGE / VTK_BIQUADRATIC_QUADRATIC_WEDGE in VTK's own layout:
+# CGNS slot i of the cell is VTK node VTK_WEDGE_OF_CGNS[i] (corners flipped
+# as for VTK_WEDGE, mid-edges and quadrangle centres following them).
+VTK_WEDGE_OF_CGNS = [0, 2, 1, 3, 5, 4, 8, 7, 6, 12, 14, 13, 11, 10, 9, 17, 16, 15]
+
+
+def corner_wedge_volume(xyz, nodes):
+    x0, x1, x2, x3 = (xyz[nodes[i]] for i in range(4))
+    return float(np.dot(np.cross(x1 - x0, x2 - x0), x3 - x0))
+
+
+@pytest.mark.parametrize("serendipity", [False, True])
+def test_vtk_quadratic_wedges_in_vtk_layout(tmp_path, serendipity):
+    """Quadratic wedges as ParaView, gmsh or meshio write them (VTK 26 / 32
+    with VTK_WEDGE's corner orientation) and quadratic boundary elements
+    (VTK 22 triangles, 23 / 28 quadrangles) come back in CGNS order with
+    positive volumes, the same faces and the boundary groups."""
+    m = meshlib.wedge_box((3, 2, 2), jitter=0.1, seed=9)
+    q = meshlib.quadratic(m, serendipity=serendipity)
+    n = 15 if serendipity else 18
+    vtk_type = 26 if serendipity else 32
+    cells = []
+    for c in range(q.n_cells):
+        vtk_nodes = np.empty(n, np.int64)
+        vtk_nodes[VTK_WEDGE_OF_CGNS[:n]] = q.cell_nodes[c, :n]
+        cells.append((vtk_type, vtk_nodes, -1))
+    bn, bg = meshlib.boundary_elements(m)
+    for nodes, g in zip(bn, bg):
+        if nodes[3] < 0:  # quadratic triangle: corners, then any three mid-edge ids
+            cells.append((22, [*nodes[:3], *nodes[:3]], int(g)))
+        else:  # quadratic and biquadratic quadrangles
+            cells.append((23 if g % 2 else 28, [*nodes, *nodes] + ([nodes[0]] if g % 2 == 0 else []), int(g)))
+    cells.append((3, [0, 1], -1))  # a line: skipped
+    path = tmp_path / "w.vtk"
+    write_classic_vtk(path, q.xyz, cells)
+    got = meshlib.read_vtk(path)
+    assert np.array_equal(got.cell_nodes[:, :n], q.cell_nodes[:, :n])
+    assert np.array_equal(got.cell_type, q.cell_type)
+    assert all(corner_wedge_volume(got.xyz, got.cell_nodes[c]) > 0 for c in range(got.n_cells))
+    same_faces(got, q)
+
+
+def test_vtk_reader_rejects_unsupported_cells(tmp_path):
+    m = meshlib.box((1, 1, 1))
+    path = tmp_path / "u.vtk"
+    write_classic_vtk(path, m.xyz, [(12, m.cell_nodes[0], -1), (38, list(range(8)), -1)])
+    with pytest.raises(capi.McfdError, match="unsupported VTK cell type 38 with 8 nodes"):
+        meshlib.read_vtk(path)
+    write_classic_vtk(path, m.xyz, [(29, list(range(8)) * 2 + [0, 1, 2, 3], -1)])
+    with pytest.raises(capi.McfdError, match="unsupported VTK cell type 29 with 20 nodes"):
+        meshlib.read_vtk(path)
