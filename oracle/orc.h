@@ -159,6 +159,10 @@ void orc_limiter_smoothness(const orc_limiter *l, int64_t c, const double *cm,
 /* jump-detector flags [cells]; returns the troubled count */
 int64_t orc_limiter_troubled(const orc_limiter *l, const double *u,
                              char *flags);
+/* The limiter on the modal scheme's cells (WithLimiter<dg::General> over
+ * Projection); orc_limit then works on the modal column [cells][M][K]. */
+typedef struct orc_modal orc_modal;
+orc_limiter *orc_modal_limiter_create(const orc_modal *m);
 /* RungeKutta<order>::Update on WithLimiter<dg::Lobatto>: the limiter runs
  * after every SetSolutionColumn (spatial/with_limiter.hpp:56-59). */
 int orc_rk_update_limited(const orc_mesh *m, int riemann, int n_bc,
@@ -170,7 +174,6 @@ int orc_rk_update_limited(const orc_mesh *m, int riemann, int n_bc,
 enum { ORC_CELL_HEX8 = 0, ORC_CELL_TET4 = 1, ORC_CELL_HEX27 = 2, ORC_CELL_TET10 = 3,
        ORC_CELL_HEX20 = 4, ORC_CELL_WEDGE6 = 5, ORC_CELL_PYRA5 = 6, ORC_CELL_WEDGE15 = 7,
        ORC_CELL_WEDGE18 = 8, ORC_CELL_PYRA13 = 9, ORC_CELL_PYRA14 = 10 };
-typedef struct orc_modal orc_modal;
 /* Same mesh description as orc_mesh_create plus cell types (NULL: all Hex8);
  * a Tet4 cell uses the first 4 of its 8 cell_nodes entries (CGNS order) and
  * local faces 0..3 of Tetrahedron4::faces_.  Column layout per cell: [M][K]. */
@@ -200,6 +203,12 @@ double orc_modal_time_step(const orc_modal *m, const double *u, double dt_guess,
 int orc_modal_rk_update(const orc_modal *m, int riemann, int n_bc,
                         const orc_bc *bcs, int order, double t, double dt,
                         double *u);
+/* RungeKutta<order>::Update on WithLimiter<dg::General>: the limiter runs
+ * after every SetSolutionColumn (spatial/with_limiter.hpp:56-59). */
+int orc_modal_rk_update_limited(const orc_modal *m, int riemann, int n_bc,
+                                const orc_bc *bcs, int order, double t, double dt,
+                                double *u, const orc_limiter *l, int mode, double w0,
+                                double eps);
 
 /* ---- output sampling, Writer<Part>::Prepare (mesh/vtk.hpp:428-493) ---- */
 /* nodal mesh: every cell at the 27 VTK Hexahedron27 locals; xyz

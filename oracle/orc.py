@@ -279,6 +279,10 @@ def _limiter_sigs(lib):
         "orc_limiter_smoothness": (None, [C.c_void_p, C.c_int64, _D, _D]),
         "orc_rk_update_limited": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(OrcBc), C.c_int, C.c_double,
                                             C.c_double, _D, C.c_void_p, C.c_int, C.c_double, C.c_double]),
+        "orc_modal_limiter_create": (C.c_void_p, [C.c_void_p]),
+        "orc_modal_rk_update_limited": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(OrcBc), C.c_int,
+                                                  C.c_double, C.c_double, _D, C.c_void_p, C.c_int, C.c_double,
+                                                  C.c_double]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -331,6 +335,27 @@ class Limiter:
         n, arr = self.mesh.bcs
         self.lib.orc_rk_update_limited(self.mesh._m, riemann, n, arr, order, t, dt, _p(u), self._l,
                                        self.mode, self.w0, self.eps)
+        return u
+
+
+class ModalLimiter(Limiter):
+    """The same WENO limiter on the cells of an oracle Modal system
+    (WithLimiter<dg::General> over Projection): the column holds the modal
+    coefficients, [cells][M][5]."""
+
+    def __init__(self, modal: "Modal", mode: int = LIMITER_LAZY, w0: float = 0.001, eps: float = 1e-6):
+        self.lib = load()
+        _limiter_sigs(self.lib)
+        self.mesh = modal
+        self._l = self.lib.orc_modal_limiter_create(modal._m)
+        self.mode, self.w0, self.eps = mode, w0, eps
+        self.m = modal.m
+
+    def rk_update(self, riemann: int, order: int, t: float, dt: float, u: np.ndarray) -> np.ndarray:
+        u = np.array(u, dtype=np.float64, copy=True)
+        n, arr = self.mesh.bcs
+        self.lib.orc_modal_rk_update_limited(self.mesh._m, riemann, n, arr, order, t, dt, _p(u), self._l,
+                                             self.mode, self.w0, self.eps)
         return u
 
 

@@ -36,6 +36,24 @@ struct orc_mesh {
   int16_t *map_h, *map_s; /* [faces][QF] */
 };
 
+/* Mesh of the modal scheme (built by orc_modal_create, orc_modal.c). */
+struct orc_modal {
+  int p, m;
+  int64_t n_cells, n_faces;
+  int64_t *vp_off;     /* [cells + 1] volume point offsets */
+  double *vx, *vw;     /* [points][3] global coordinates, [points] global weights */
+  double *center;      /* [cells][3] */
+  double *s;           /* [cells][M][M] */
+  double *length;      /* [cells] */
+  int64_t *fp_off;     /* [faces + 1] */
+  double *fx, *fw, *ff; /* face points: coordinates, weights, frames [9] */
+  int64_t *face_cells;
+  int32_t *face_group;
+  double *face_shift;
+  double *corners;     /* [cells][8][3] (Tet4: first 4) */
+  int32_t *type;       /* [cells] ORC_CELL_* */
+};
+
 /* Lagrange derivative of the FR correction at the right end, g_R'(1)
  * (basis/vincent.hpp:30-32, 73-89). */
 double orc_fr_g_prime(int p);

@@ -204,23 +204,6 @@ static double norm3(const double *a) { return sqrt(a[0] * a[0] + a[1] * a[1] + a
 
 /* ---------------- mesh ---------------- */
 
-struct orc_modal {
-  int p, m;
-  int64_t n_cells, n_faces;
-  int64_t *vp_off;     /* [cells + 1] volume point offsets */
-  double *vx, *vw;     /* [points][3] global coordinates, [points] global weights */
-  double *center;      /* [cells][3] */
-  double *s;           /* [cells][M][M] */
-  double *length;      /* [cells] */
-  int64_t *fp_off;     /* [faces + 1] */
-  double *fx, *fw, *ff; /* face points: coordinates, weights, frames [9] */
-  int64_t *face_cells;
-  int32_t *face_group;
-  double *face_shift;
-  double *corners;     /* [cells][8][3] (Tet4: first 4) */
-  int32_t *type;       /* [cells] ORC_CELL_* */
-};
-
 int64_t orc_modal_column_size(const orc_modal *m) { return m->n_cells * m->m * K; }
 int orc_modal_basis_count(const orc_modal *m) { return m->m; }
 int64_t orc_modal_point_count(const orc_modal *m) { return m->vp_off[m->n_cells]; }
@@ -827,6 +810,27 @@ int orc_modal_rk_update(const orc_modal *m, int riemann, int n_bc,
   modal_ctx ctx = {m, riemann, n_bc, bcs};
   return orc_rk_generic(modal_residual_fn, &ctx, orc_modal_column_size(m), order,
                         t, dt, u, NULL, NULL);
+}
+
+typedef struct {
+  const orc_limiter *l;
+  int mode;
+  double w0, eps;
+} modal_limit_ctx;
+
+static void modal_limit_hook(void *ctx, double *u) {
+  modal_limit_ctx *c = (modal_limit_ctx *)ctx;
+  orc_limit(c->l, c->mode, c->w0, c->eps, u);
+}
+
+int orc_modal_rk_update_limited(const orc_modal *m, int riemann, int n_bc,
+                                const orc_bc *bcs, int order, double t, double dt,
+                                double *u, const orc_limiter *l, int mode, double w0,
+                                double eps) {
+  modal_ctx ctx = {m, riemann, n_bc, bcs};
+  modal_limit_ctx lc = {l, mode, w0, eps};
+  return orc_rk_generic(modal_residual_fn, &ctx, orc_modal_column_size(m), order, t, dt, u,
+                        (l && mode != ORC_LIMITER_NONE) ? modal_limit_hook : NULL, &lc);
 }
 
 /* ---- output sampling: Writer<Part>::Prepare (mesh/vtk.hpp:428-493) ----

@@ -128,11 +128,16 @@ static int degree_of(int j) {
 struct orc_limiter {
   int p, n, m;
   int64_t n_cells;
+  int modal_column; /* 1: the column holds the modal coefficients [cells][M][K]
+                       (dg::General over Projection); 0: nodal values [cells][N][K]
+                       with Extrapolation (DGSEM) */
+  int64_t *off;    /* [cells + 1] quadrature points of cell c: off[c] .. off[c+1]-1
+                      (DGSEM: its N nodes; modal: its volume quadrature) */
   double *center;  /* [cells][3] */
   double *s;       /* [cells][M][M] lower triangular */
-  double *psi;     /* [cells][N][M] basis values at own nodes */
-  double *w;       /* [cells][N] global weights */
-  double *xyz;     /* [cells][N][3] */
+  double *psi;     /* [points][M] basis values at the cell's own points */
+  double *w;       /* [points] global weights */
+  double *xyz;     /* [points][3] */
   double *volume;  /* [cells] */
   int *adj;        /* [cells][6] */
   int *n_adj;      /* [cells] */
@@ -149,6 +154,8 @@ orc_limiter *orc_limiter_create(const orc_mesh *mesh) {
   const int64_t C = orc_mesh_cells(mesh);
   orc_limiter *l = (orc_limiter *)calloc(1, sizeof(orc_limiter));
   l->p = p; l->n = N; l->m = M; l->n_cells = C;
+  l->off = (int64_t *)malloc(sizeof(int64_t) * (C + 1));
+  for (int64_t c = 0; c <= C; ++c) l->off[c] = c * N;
   l->center = (double *)malloc(sizeof(double) * C * 3);
   l->s = (double *)calloc(C * M * M, sizeof(double));
   l->psi = (double *)malloc(sizeof(double) * C * N * M);
@@ -207,9 +214,70 @@ orc_limiter *orc_limiter_create(const orc_mesh *mesh) {
   return l;
 }
 
+/* The limiter of WithLimiter<dg::General> over Projection (the reference's
+ * DGFEM build, demo/euler/sourceless.hpp:28-32, 74-80): the cells' own
+ * orthonormal bases and volume quadratures (any cell type), neighbours in
+ * face order, frames of the shared faces at their first quadrature point. */
+orc_limiter *orc_modal_limiter_create(const orc_modal *mm) {
+  const int p = mm->p, M = mm->m;
+  const int64_t C = mm->n_cells, NP = mm->vp_off[C];
+  orc_limiter *l = (orc_limiter *)calloc(1, sizeof(orc_limiter));
+  l->p = p; l->n = 0; l->m = M; l->n_cells = C; l->modal_column = 1;
+  l->off = (int64_t *)malloc(sizeof(int64_t) * (C + 1));
+  memcpy(l->off, mm->vp_off, sizeof(int64_t) * (C + 1));
+  l->center = (double *)malloc(sizeof(double) * C * 3);
+  memcpy(l->center, mm->center, sizeof(double) * C * 3);
+  l->s = (double *)malloc(sizeof(double) * C * M * M);
+  memcpy(l->s, mm->s, sizeof(double) * C * M * M);
+  l->psi = (double *)malloc(sizeof(double) * NP * M);
+  l->w = (double *)malloc(sizeof(double) * NP);
+  memcpy(l->w, mm->vw, sizeof(double) * NP);
+  l->xyz = (double *)malloc(sizeof(double) * NP * 3);
+  memcpy(l->xyz, mm->vx, sizeof(double) * NP * 3);
+  l->volume = (double *)malloc(sizeof(double) * C);
+  l->adj = (int *)malloc(sizeof(int) * C * 6);
+  l->n_adj = (int *)calloc(C, sizeof(int));
+  l->adj_shift = (double *)calloc(C * 6 * 3, sizeof(double));
+  l->adj_frame = (double *)calloc(C * 6 * 9, sizeof(double));
+  for (int64_t f = 0; f < mm->n_faces; ++f) {
+    int64_t h = mm->face_cells[f * 2], s = mm->face_cells[f * 2 + 1];
+    if (s < 0) continue;
+    const double *fs = &mm->face_shift[f * 3];
+    const double *fr = &mm->ff[mm->fp_off[f] * 9];
+    if (l->n_adj[h] < 6) {
+      for (int e = 0; e < 3; ++e) l->adj_shift[(h * 6 + l->n_adj[h]) * 3 + e] = fs[e];
+      memcpy(&l->adj_frame[(h * 6 + l->n_adj[h]) * 9], fr, sizeof(double) * 9);
+      l->adj[h * 6 + l->n_adj[h]++] = (int)s;
+    }
+    if (l->n_adj[s] < 6) {
+      for (int e = 0; e < 3; ++e) l->adj_shift[(s * 6 + l->n_adj[s]) * 3 + e] = -fs[e];
+      memcpy(&l->adj_frame[(s * 6 + l->n_adj[s]) * 9], fr, sizeof(double) * 9);
+      l->adj[s * 6 + l->n_adj[s]++] = (int)h;
+    }
+  }
+#pragma omp parallel for schedule(static) num_threads(orc_get_threads())
+  for (int64_t c = 0; c < C; ++c) {
+    const double *S = &l->s[c * M * M];
+    double vol = 0;
+    for (int64_t q = l->off[c]; q < l->off[c + 1]; ++q) {
+      double d[3], t[20];
+      for (int e = 0; e < 3; ++e) d[e] = l->xyz[q * 3 + e] - l->center[c * 3 + e];
+      orc_taylor_values(M, d, t);
+      for (int m = 0; m < M; ++m) {
+        double s = 0;
+        for (int j = 0; j <= m; ++j) s += S[m * M + j] * t[j];
+        l->psi[q * M + m] = s;
+      }
+      vol += l->w[q];
+    }
+    l->volume[c] = vol;
+  }
+  return l;
+}
+
 void orc_limiter_destroy(orc_limiter *l) {
   if (!l) return;
-  free(l->center); free(l->s); free(l->psi); free(l->w); free(l->xyz);
+  free(l->off); free(l->center); free(l->s); free(l->psi); free(l->w); free(l->xyz);
   free(l->volume); free(l->adj); free(l->n_adj); free(l->adj_shift); free(l->adj_frame);
   free(l);
 }
@@ -236,16 +304,21 @@ static void modal_value(const orc_limiter *l, int64_t c, const double *cm,
   }
 }
 
-/* UpdateModalCoeff: modal (K x M) = nodal values (K x N) * modal_to_nodal. */
+/* UpdateModalCoeff: modal (K x M) = nodal values (K x N) * modal_to_nodal;
+ * for the modal scheme the coefficients are the column itself. */
 void orc_limiter_modal(const orc_limiter *l, const double *u, double *modal) {
-  const int N = l->n, M = l->m;
+  const int M = l->m;
 #pragma omp parallel for schedule(static) num_threads(orc_get_threads())
   for (int64_t c = 0; c < l->n_cells; ++c) {
     for (int k = 0; k < K; ++k)
       for (int m = 0; m < M; ++m) {
+        if (l->modal_column) {
+          modal[(c * K + k) * M + m] = u[(c * M + m) * K + k];
+          continue;
+        }
         double s = 0;
-        for (int q = 0; q < N; ++q)
-          s += u[(c * N + q) * K + k] * (l->w[c * N + q] * l->psi[(c * N + q) * M + m]);
+        for (int64_t q = l->off[c]; q < l->off[c + 1]; ++q)
+          s += u[q * K + k] * (l->w[q] * l->psi[q * M + m]);
         modal[(c * K + k) * M + m] = s;
       }
   }
@@ -254,7 +327,7 @@ void orc_limiter_modal(const orc_limiter *l, const double *u, double *modal) {
 /* GetSmoothness (weno.hpp:78-95) of modal coeff cm on cell c. */
 static void smoothness(const orc_limiter *l, int64_t c, const double *cm,
                        double *beta) {
-  const int N = l->n, M = l->m, P = l->p;
+  const int M = l->m, P = l->p;
   const double *S = &l->s[c * M * M];
   double tc[K * 20], integral[K * 20];
   for (int k = 0; k < K; ++k)
@@ -264,10 +337,10 @@ static void smoothness(const orc_limiter *l, int64_t c, const double *cm,
       tc[k * M + j] = s;
     }
   memset(integral, 0, sizeof(integral));
-  for (int q = 0; q < N; ++q) {
+  for (int64_t q = l->off[c]; q < l->off[c + 1]; ++q) {
     double d[3], pdv[20];
-    for (int e = 0; e < 3; ++e) d[e] = l->xyz[(c * N + q) * 3 + e] - l->center[c * 3 + e];
-    double w = l->w[c * N + q];
+    for (int e = 0; e < 3; ++e) d[e] = l->xyz[q * 3 + e] - l->center[c * 3 + e];
+    double w = l->w[q];
     for (int k = 0; k < K; ++k) {
       taylor_pdv(M, d, &tc[k * M], pdv);
       for (int a = 0; a < M; ++a) integral[k * M + a] += pdv[a] * pdv[a] * w;
@@ -332,7 +405,7 @@ static int is_not_smooth(const orc_limiter *l, int64_t c, const double *modal) {
 static void lazy_reconstruct(const orc_limiter *l, int64_t c,
                              const double *modal, double w0, double eps,
                              double *out) {
-  const int N = l->n, M = l->m;
+  const int M = l->m;
   const int n_adj = l->n_adj[c];
   double cand[7][K * 20];
   const double *own = &modal[c * K * M];
@@ -343,13 +416,13 @@ static void lazy_reconstruct(const orc_limiter *l, int64_t c,
     const double *sh = &l->adj_shift[(c * 6 + a) * 3];
     double *pj = cand[a];
     memset(pj, 0, sizeof(double) * K * M);
-    for (int q = 0; q < N; ++q) {
+    for (int64_t q = l->off[c]; q < l->off[c + 1]; ++q) {
       double v[K], xq[3];
-      for (int e = 0; e < 3; ++e) xq[e] = l->xyz[(c * N + q) * 3 + e] - sh[e];
+      for (int e = 0; e < 3; ++e) xq[e] = l->xyz[q * 3 + e] - sh[e];
       modal_value(l, b, &modal[b * K * M], xq, v);
-      double w = l->w[c * N + q];
+      double w = l->w[q];
       for (int k = 0; k < K; ++k)
-        for (int m = 0; m < M; ++m) pj[k * M + m] += v[k] * l->psi[(c * N + q) * M + m] * w;
+        for (int m = 0; m < M; ++m) pj[k * M + m] += v[k] * l->psi[q * M + m] * w;
     }
     for (int k = 0; k < K; ++k) {
       double my_avg = own[k * M] * s00;
@@ -424,7 +497,7 @@ void orc_eigen_matrices(const double *cons, const double *frame9, double *L, dou
 static void eigen_reconstruct(const orc_limiter *l, int64_t c,
                               const double *modal, double w0, double eps,
                               double *out) {
-  const int N = l->n, M = l->m;
+  const int M = l->m;
   const int n_adj = l->n_adj[c];
   double cand[7][K * 20], rot[7][K * 20];
   const double *own = &modal[c * K * M];
@@ -435,13 +508,13 @@ static void eigen_reconstruct(const orc_limiter *l, int64_t c,
     const double *sh = &l->adj_shift[(c * 6 + a) * 3];
     double *pj = cand[a];
     memset(pj, 0, sizeof(double) * K * M);
-    for (int q = 0; q < N; ++q) {
+    for (int64_t q = l->off[c]; q < l->off[c + 1]; ++q) {
       double v[K], xq[3];
-      for (int e = 0; e < 3; ++e) xq[e] = l->xyz[(c * N + q) * 3 + e] - sh[e];
+      for (int e = 0; e < 3; ++e) xq[e] = l->xyz[q * 3 + e] - sh[e];
       modal_value(l, b, &modal[b * K * M], xq, v);
-      double w = l->w[c * N + q];
+      double w = l->w[q];
       for (int k = 0; k < K; ++k)
-        for (int m = 0; m < M; ++m) pj[k * M + m] += v[k] * l->psi[(c * N + q) * M + m] * w;
+        for (int m = 0; m < M; ++m) pj[k * M + m] += v[k] * l->psi[q * M + m] * w;
     }
     for (int k = 0; k < K; ++k) {
       double my_avg = own[k * M] * s00;
@@ -508,7 +581,7 @@ static void eigen_reconstruct(const orc_limiter *l, int64_t c,
  * jump detector flags).  Returns the number of reconstructed cells. */
 int64_t orc_limit(const orc_limiter *l, int mode, double w0, double eps,
                   double *u) {
-  const int N = l->n, M = l->m;
+  const int M = l->m;
   const int64_t C = l->n_cells;
   double *modal = (double *)malloc(sizeof(double) * C * K * M);
   double *fresh = (double *)malloc(sizeof(double) * C * K * M);
@@ -527,15 +600,21 @@ int64_t orc_limit(const orc_limiter *l, int mode, double w0, double eps,
       ++count;
     }
   }
-  /* SetCoeff(modal) -> UpdateNodalCoeff: nodal = modal at the nodes */
+  /* SetCoeff(modal): the modal column takes the coefficients; with
+   * Extrapolation UpdateNodalCoeff sets nodal = modal at the nodes */
 #pragma omp parallel for schedule(static) num_threads(orc_get_threads())
   for (int64_t c = 0; c < C; ++c) {
     if (!troubled[c]) continue;
-    for (int q = 0; q < N; ++q)
+    if (l->modal_column) {
+      for (int m = 0; m < M; ++m)
+        for (int k = 0; k < K; ++k) u[(c * M + m) * K + k] = fresh[(c * K + k) * M + m];
+      continue;
+    }
+    for (int64_t q = l->off[c]; q < l->off[c + 1]; ++q)
       for (int k = 0; k < K; ++k) {
         double s = 0;
-        for (int m = 0; m < M; ++m) s += fresh[(c * K + k) * M + m] * l->psi[(c * N + q) * M + m];
-        u[(c * N + q) * K + k] = s;
+        for (int m = 0; m < M; ++m) s += fresh[(c * K + k) * M + m] * l->psi[q * M + m];
+        u[q * K + k] = s;
       }
   }
   free(modal); free(fresh); free(troubled);

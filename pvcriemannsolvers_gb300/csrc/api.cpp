@@ -816,8 +816,6 @@ int mcfd_create(const mcfd_mesh_desc *mesh, const mcfd_options *options,
     return fail(nullptr, MCFD_ERR_UNSUPPORTED, "degree must be 1, 2 or 3");
   if (options->scheme != MCFD_DGSEM && options->scheme != MCFD_FR && options->scheme != MCFD_MODAL)
     return fail(nullptr, MCFD_ERR_UNSUPPORTED, "unknown scheme");
-  if (options->scheme == MCFD_MODAL && options->limiter != MCFD_LIMITER_NONE)
-    return fail(nullptr, MCFD_ERR_UNSUPPORTED, "the modal scheme is built without a limiter");
   if (options->riemann < MCFD_EXACT || options->riemann > MCFD_RUSANOV)
     return fail(nullptr, MCFD_ERR_ARGUMENT, "unknown Riemann solver");
   if (options->precision != MCFD_FP64 && options->precision != MCFD_MIXED)
@@ -841,6 +839,7 @@ int mcfd_create(const mcfd_mesh_desc *mesh, const mcfd_options *options,
   if (!rc && cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
     rc = fail(h, MCFD_ERR_CUDA, "cudaStreamCreate failed");
   h->own_stream = true;
+  h->modal.keep_host = options->scheme == MCFD_MODAL && options->limiter != MCFD_LIMITER_NONE;
   if (!rc)
     rc = options->scheme == MCFD_MODAL ? mcfd::build_modal_mesh(h, mesh, options->degree)
                                        : build_mesh(h, mesh, options->degree);
@@ -849,6 +848,8 @@ int mcfd_create(const mcfd_mesh_desc *mesh, const mcfd_options *options,
     if (options->limiter != MCFD_LIMITER_LAZY && options->limiter != MCFD_LIMITER_DETECT_LAZY &&
         options->limiter != MCFD_LIMITER_EIGEN)
       rc = fail(h, MCFD_ERR_ARGUMENT, "unknown limiter");
+    else if (options->scheme == MCFD_MODAL)
+      rc = mcfd::build_modal_limiter(h, mesh, options->limiter, options->weno_w0, options->weno_eps);
     else
       rc = build_limiter(h, mesh, options->limiter, options->weno_w0, options->weno_eps);
   }
@@ -1688,7 +1689,8 @@ int mcfd_project(mcfd_handle *h, const double *values, int64_t n) {
   h->launches += mcfd::launch_modal_project(h, h->buf.u);
   CUDA_TRY(h, cudaGetLastError());
   CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-  return MCFD_OK;
+  // WithLimiter::Approximate reconstructs after projecting (with_limiter.hpp:61-65)
+  return limit_current(h);
 }
 
 int mcfd_kernel_times(mcfd_handle *h, int32_t reps, double *out_ms) {

@@ -160,6 +160,12 @@ struct Modal {
   float4 *foff32 = nullptr;         // [face points][2] x - centre (holder), x - shift - centre (sharer)
   float *taylor32 = nullptr;        // [cells][M][K]
   std::vector<double> host_points;  // [volume points][3] global coordinates
+  // kept by build_modal_mesh for build_modal_limiter when a limiter is set,
+  // then released: per point weights, per cell centre, full S and volume,
+  // per cell point offsets, per face the frame at its first point
+  bool keep_host = false;
+  std::vector<double> host_weights, host_center, host_s, host_volume, host_frame0;
+  std::vector<int32_t> host_vol_off;
 };
 
 // Independent cases inside one handle (an ensemble member: disjoint meshes
@@ -318,6 +324,9 @@ int launch_modal_dt(mcfd_handle *h, const double *u);
 int launch_modal_project(mcfd_handle *h, double *u);
 // Host set-up of the modal tables (modal_setup.cpp); returns an mcfd status.
 int build_modal_mesh(mcfd_handle *h, const ::mcfd_mesh_desc *d, int degree);
+// The WENO limiter tables of the modal scheme from the cells' own bases and
+// volume quadratures (after build_modal_mesh with modal.keep_host set).
+int build_modal_limiter(mcfd_handle *h, const ::mcfd_mesh_desc *d, int kind, double w0, double eps);
 
 // Artificial viscosity (viscosity.cu / visc_setup.cpp).  The properties
 // pass writes Visc::nu and Visc::trace from the state u; with dt_mode it also

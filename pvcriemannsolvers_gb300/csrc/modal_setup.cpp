@@ -428,6 +428,25 @@ int build_modal_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
     for (int i = 0; i < M; ++i)
       for (int j = 0; j <= i; ++j) Sp[i * (i + 1) / 2 + j] = Sc[i * M + j];
   }
+  if (md.keep_host) {
+    md.host_weights.resize(NV);
+    md.host_center.resize((size_t)C * 3);
+    md.host_s.assign((size_t)C * M * M, 0.0);
+    md.host_volume.assign(C, 0.0);
+    md.host_vol_off = vol_off;
+    for (int64_t c = 0; c < C; ++c) {
+      md.host_center[c * 3] = center[c].x;
+      md.host_center[c * 3 + 1] = center[c].y;
+      md.host_center[c * 3 + 2] = center[c].z;
+      const double *Sp = &S[(size_t)c * M * (M + 1) / 2];
+      for (int i = 0; i < M; ++i)
+        for (int j = 0; j <= i; ++j) md.host_s[((size_t)c * M + i) * M + j] = Sp[i * (i + 1) / 2 + j];
+      for (int32_t q = vol_off[c]; q < vol_off[c + 1]; ++q) {
+        md.host_weights[q] = vol[q].w;
+        md.host_volume[c] += vol[q].w;
+      }
+    }
+  }
   if (bad_jac) return fail(h, MCFD_ERR_MESH, "non-positive Jacobian in a modal cell");
   if (bad_gram) return fail(h, MCFD_ERR_MESH, "degenerate cell quadrature (Gram matrix not positive)");
   // ---- faces
@@ -468,6 +487,13 @@ int build_modal_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
   m.n_points = NF;
   std::vector<int32_t> point_face(NF);
   std::vector<double4> fpt(NF), fnrm(NF);
+  // tangent (first row of the face map's Jacobian) at each face's first point:
+  // with the normal, the frame of that point (coordinate/face.hpp:54-62)
+  std::vector<double> ftan0(md.keep_host ? (size_t)F * 3 : 0);
+  auto keep_tangent = [&](int64_t f, int q, const double *ta) {
+    if (md.keep_host && q == 0)
+      for (int e = 0; e < 3; ++e) ftan0[f * 3 + e] = ta[e];
+  };
   int bad_face = 0;
 #pragma omp parallel for schedule(static)
   for (int64_t f = 0; f < F; ++f) {
@@ -516,6 +542,7 @@ int build_modal_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
         const double wl = hex ? gw[q / Q] * gw[q % Q] : tw[q];
         double X[3], ta[3], tb[3], nn[3];
         geo::face_map(n, xf, s, t, X, ta, tb);
+        keep_tangent(f, q, ta);
         cross(ta, tb, nn);
         const double len = norm3(nn);
         point_face[base + q] = (int32_t)f;
@@ -552,6 +579,7 @@ int build_modal_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
         geo::map_point(type[hc], xc, loc, X, J);
         geo::tangent(J, da, ta);
         geo::tangent(J, db, tb);
+        keep_tangent(f, q, ta);
         cross(ta, tb, nn);
         const double len = norm3(nn);
         point_face[base + q] = (int32_t)f;
@@ -577,6 +605,7 @@ int build_modal_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
           double cc = jac[3] * jac[3] + jac[4] * jac[4] + jac[5] * jac[5];
           double nn[3];
           cross(&jac[0], &jac[3], nn);
+          keep_tangent(f, q, &jac[0]);
           double len = norm3(nn);
           point_face[base + q] = (int32_t)f;
           fpt[base + q] = make_double4(X[0], X[1], X[2], gw[i] * gw[j] * std::sqrt(a * cc - b * b));
@@ -589,6 +618,7 @@ int build_modal_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
         jac[3 + e] = xn[1 * 3 + e] - xn[2 * 3 + e];
       }
       cross(&jac[0], &jac[3], nn);
+      keep_tangent(f, 0, &jac[0]);
       double area2 = norm3(nn);
       for (size_t q = 0; q < tw.size(); ++q) {
         double x = tx[q][0], y = tx[q][1], z = 1.0 - x - y, X[3];
@@ -600,6 +630,17 @@ int build_modal_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
     }
   }
   if (bad_face) return fail(h, MCFD_ERR_MESH, "a sharer face does not match its holder face");
+  if (md.keep_host) {
+    md.host_frame0.assign((size_t)F * 9, 0.0);
+    for (int64_t f = 0; f < F; ++f) {
+      double *fr = &md.host_frame0[f * 9];
+      const double4 nv = fnrm[face_off[f]];
+      fr[0] = nv.x; fr[1] = nv.y; fr[2] = nv.z;
+      const double tn = norm3(&ftan0[f * 3]);
+      for (int e = 0; e < 3; ++e) fr[3 + e] = ftan0[f * 3 + e] / tn;
+      cross(&fr[0], &fr[3], &fr[6]);
+    }
+  }
   // ---- upload
   int rc;
   if ((rc = upload(h, &md.center, center))) return rc;
@@ -647,6 +688,158 @@ int build_modal_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
   if (e != cudaSuccess) return fail(h, MCFD_ERR_CUDA, std::string("modal tables: ") + cudaGetErrorString(e));
   m.host_bcs.assign(std::max(m.n_groups, 1), BcDev{});
   if ((rc = upload(h, &m.bcs, m.host_bcs))) return rc;
+  return MCFD_OK;
+}
+
+namespace {
+
+// d^a T_j (the Taylor monomial j differentiated by multi-index a) at d.
+double taylor_pdv(int j, int a, const double *d) {
+  double f = 1;
+  for (int e = 0; e < 3; ++e) {
+    const int ej = kTaylorExp[j][e], ea = kTaylorExp[a][e];
+    if (ej < ea) return 0;
+    double fall = 1;
+    for (int i = 0; i < ea; ++i) fall *= (ej - i);
+    f *= fall * ipow(d[e], ej - ea);
+  }
+  return f;
+}
+
+// psi of a cell (centre ctr, full lower-triangular S [M][M]) at global x.
+void modal_basis(const double *ctr, const double *S, int M, const double *x, double *psi) {
+  const double d[3] = {x[0] - ctr[0], x[1] - ctr[1], x[2] - ctr[2]};
+  double t[20];
+  for (int j = 0; j < M; ++j) t[j] = ipow(d[0], kTaylorExp[j][0]) * ipow(d[1], kTaylorExp[j][1]) *
+                                     ipow(d[2], kTaylorExp[j][2]);
+  for (int i = 0; i < M; ++i) {
+    double s = 0;
+    for (int j = 0; j <= i; ++j) s += S[i * M + j] * t[j];
+    psi[i] = s;
+  }
+}
+
+}  // namespace
+
+// WithLimiter<dg::General> over Projection: the tables of the WENO kernels
+// (weno.cu) from each cell's own orthonormal basis and volume quadrature,
+// the quantities limiter/weno.hpp computes on the fly:
+//   proj [cells][6][M][M]  neighbour basis -> own basis over the own
+//                          quadrature (Borrow: adj_proj.Approximate of the
+//                          neighbour's GlobalToValue, weno.hpp:138-166)
+//   beta [cells][M][M]     the smoothness quadratic form: sum over Taylor
+//                          multi-indices a, |a| >= 1, of vol^(2|a|/3 - 1) /
+//                          (|a|!)^2 * integral of d^a psi_i d^a psi_j
+//                          (weno.hpp:25-95)
+//   eval [cells][7][M]     neighbour bases (slots 0..5) and the own basis
+//                          (slot 6) at the cell centre (IsNotSmooth,
+//                          weno.hpp:230-258)
+//   s00, divisor = vol^((p+1)/6) * n_adj, volume, adjacency in face order
+//   with the periodic shifts, and each shared face's frame at its first
+//   quadrature point (weno::Eigen, weno.hpp:297-336).
+int build_modal_limiter(mcfd_handle *h, const mcfd_mesh_desc *d, int kind, double w0, double eps) {
+  auto &md = h->modal;
+  auto &l = h->lim;
+  const int p = h->mesh.p, M = md.m;
+  const int64_t C = h->mesh.n_cells;
+  l.kind = kind;
+  l.m = M;
+  l.w0 = w0 > 0 ? w0 : 0.001;
+  l.eps = eps > 0 ? eps : 1e-6;
+  std::vector<int32_t> adj((size_t)C * 6, -1);
+  std::vector<double> adj_shift((size_t)C * 6 * 3, 0.0), adj_frame((size_t)C * 6 * 9, 0.0);
+  std::vector<int> n_adj(C, 0);
+  for (int64_t f = 0; f < d->n_faces; ++f) {
+    const int64_t hc = d->face_cells[f * 2], sc = d->face_cells[f * 2 + 1];
+    if (sc < 0) continue;
+    double sh[3] = {0, 0, 0};
+    if (d->face_shift)
+      for (int e = 0; e < 3; ++e) sh[e] = d->face_shift[f * 3 + e];
+    const double *fr = &md.host_frame0[f * 9];
+    const int64_t owner[2] = {hc, sc}, other[2] = {sc, hc};
+    for (int side = 0; side < 2; ++side) {
+      const int64_t c = owner[side];
+      if (n_adj[c] >= 6) continue;
+      const size_t slot = (size_t)c * 6 + n_adj[c];
+      for (int e = 0; e < 3; ++e) adj_shift[slot * 3 + e] = side == 0 ? sh[e] : -sh[e];
+      for (int e = 0; e < 9; ++e) adj_frame[slot * 9 + e] = fr[e];
+      adj[slot] = (int32_t)other[side];
+      ++n_adj[c];
+    }
+  }
+  const double *X = md.host_points.data(), *W = md.host_weights.data();
+  const double *ctr = md.host_center.data(), *S = md.host_s.data();
+  std::vector<double> proj((size_t)C * 6 * M * M, 0.0), beta((size_t)C * M * M, 0.0);
+  std::vector<double> eval((size_t)C * 7 * M, 0.0), s00(C), divisor(C);
+#pragma omp parallel for schedule(static)
+  for (int64_t c = 0; c < C; ++c) {
+    const double *Sc = &S[(size_t)c * M * M];
+    const double vol = md.host_volume[c];
+    s00[c] = Sc[0];
+    divisor[c] = std::pow(vol, (p + 1.0) / 2.0 / 3) * n_adj[c];
+    double weight[4] = {0, 0, 0, 0};
+    const double measure = 1 / (Sc[0] * Sc[0]);
+    for (int deg = 1; deg <= p; ++deg) {
+      const double kf = std::tgamma(deg + 1);
+      weight[deg] = std::pow(measure, deg * 2. / 3 - 1) / (kf * kf);
+    }
+    double *B = &beta[(size_t)c * M * M];
+    double psi[20], pb[20], dpsi[20];
+    for (int32_t q = md.host_vol_off[c]; q < md.host_vol_off[c + 1]; ++q) {
+      const double *x = &X[(size_t)q * 3];
+      const double dd[3] = {x[0] - ctr[c * 3], x[1] - ctr[c * 3 + 1], x[2] - ctr[c * 3 + 2]};
+      for (int a = 1; a < M; ++a) {
+        const int deg = kTaylorExp[a][0] + kTaylorExp[a][1] + kTaylorExp[a][2];
+        for (int i = 0; i < M; ++i) {
+          double s = 0;
+          for (int j = 0; j <= i; ++j) s += Sc[i * M + j] * taylor_pdv(j, a, dd);
+          dpsi[i] = s;
+        }
+        for (int i = 0; i < M; ++i)
+          for (int j = 0; j < M; ++j) B[i * M + j] += W[q] * weight[deg] * dpsi[i] * dpsi[j];
+      }
+      modal_basis(&ctr[c * 3], Sc, M, x, psi);
+      for (int s = 0; s < n_adj[c]; ++s) {
+        const int32_t nb = adj[(size_t)c * 6 + s];
+        const double *sh = &adj_shift[((size_t)c * 6 + s) * 3];
+        const double xs[3] = {x[0] - sh[0], x[1] - sh[1], x[2] - sh[2]};
+        modal_basis(&ctr[(size_t)nb * 3], &S[(size_t)nb * M * M], M, xs, pb);
+        double *P = &proj[(((size_t)c * 6 + s) * M) * M];
+        for (int i = 0; i < M; ++i)
+          for (int j = 0; j < M; ++j) P[i * M + j] += pb[i] * (W[q] * psi[j]);
+      }
+    }
+    for (int s = 0; s < n_adj[c]; ++s) {
+      const int32_t nb = adj[(size_t)c * 6 + s];
+      const double *sh = &adj_shift[((size_t)c * 6 + s) * 3];
+      const double xc[3] = {ctr[c * 3] - sh[0], ctr[c * 3 + 1] - sh[1], ctr[c * 3 + 2] - sh[2]};
+      modal_basis(&ctr[(size_t)nb * 3], &S[(size_t)nb * M * M], M, xc, &eval[((size_t)c * 7 + s) * M]);
+    }
+    modal_basis(&ctr[c * 3], Sc, M, &ctr[c * 3], &eval[((size_t)c * 7 + 6) * M]);
+  }
+  int rc;
+  if ((rc = upload(h, &l.proj, proj))) return rc;
+  if ((rc = upload(h, &l.beta, beta))) return rc;
+  if ((rc = upload(h, &l.eval, eval))) return rc;
+  if ((rc = upload(h, &l.s00, s00))) return rc;
+  if ((rc = upload(h, &l.divisor, divisor))) return rc;
+  if ((rc = upload(h, &l.adj, adj))) return rc;
+  if ((rc = upload(h, &l.frame, adj_frame))) return rc;
+  if ((rc = upload(h, &l.volume, md.host_volume))) return rc;
+  cudaError_t e = cudaMalloc(&l.modal, sizeof(double) * C * kK * M);
+  if (e == cudaSuccess) e = cudaMalloc(&l.list, sizeof(int32_t) * C);
+  if (e == cudaSuccess) e = cudaMalloc(&l.list_count, sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMalloc(&l.troubled, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemset(l.troubled, 0, sizeof(unsigned long long));
+  if (e != cudaSuccess) return fail(h, MCFD_ERR_CUDA, std::string("limiter tables: ") + cudaGetErrorString(e));
+  // the host copies are no longer needed
+  std::vector<double>().swap(md.host_weights);
+  std::vector<double>().swap(md.host_center);
+  std::vector<double>().swap(md.host_s);
+  std::vector<double>().swap(md.host_frame0);
+  std::vector<double>().swap(md.host_volume);
+  std::vector<int32_t>().swap(md.host_vol_off);
+  md.keep_host = false;
   return MCFD_OK;
 }
 

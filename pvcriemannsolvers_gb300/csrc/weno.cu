@@ -26,6 +26,13 @@
 // Every cell reads the modal buffer only, so the in-place write is safe and
 // the pass is Jacobi-like, as in limiter::Reconstruct (all new projections
 // are computed before any is written back).
+// The modal scheme (WithLimiter<dg::General> over Projection, the reference's
+// DGFEM build) runs the same kernels on the cells' own orthonormal bases: its
+// column already holds the modal coefficients ([M][K] per cell), so
+// weno_transpose_kernel replaces the nodal -> modal product and the
+// reconstruction writes the new coefficients back in the column's order
+// (MODAL); the tables come from each cell's own volume quadrature, for every
+// cell type (hexahedra, tetrahedra, wedges, pyramids, curved or straight).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -75,6 +82,19 @@ weno_modal_kernel(const double *__restrict__ u, const double *__restrict__ mn,
   }
 #pragma unroll
   for (int k = 0; k < kK; ++k) modal[(c * kK + k) * M + m] = s[k];
+}
+
+// Modal scheme: modal[c][k][m] = column[c][m][k], one thread per (cell, mode).
+template <int M>
+__global__ void __launch_bounds__(256)
+weno_transpose_kernel(const double *__restrict__ u, double *__restrict__ modal, int64_t n_cells) {
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= n_cells * M) return;
+  const int64_t c = gid / M;
+  const int m = (int)(gid - c * M);
+  const double *src = u + gid * kK;
+#pragma unroll
+  for (int k = 0; k < kK; ++k) modal[(c * kK + k) * M + m] = src[k];
 }
 
 // Mixed form: the momenta's product in FP32, density and energy in FP64.
@@ -357,8 +377,10 @@ weno_detect_kernel(WenoArgs a, int32_t *list, unsigned *count) {
 }
 
 // Reconstruction of the listed cells (every cell when list is null) by a
-// persistent grid of 64-thread blocks, one cell at a time per block.
-template <int N, int M, int MODE>
+// persistent grid of 64-thread blocks, one cell at a time per block.  MODAL:
+// the new coefficients go to the modal column; otherwise the new nodal
+// values (UpdateNodalCoeff).
+template <int N, int M, int MODE, bool MODAL = false>
 __global__ void __launch_bounds__(64)
 weno_reconstruct_kernel(WenoArgs a, const int32_t *list, const unsigned *count) {
   const int t = threadIdx.x;
@@ -451,15 +473,24 @@ weno_reconstruct_kernel(WenoArgs a, const int32_t *list, const unsigned *count) 
   }
   }
   __syncthreads();
-  // UpdateNodalCoeff: nodal values = modal expansion at the nodes
-  const double *pc = a.psi + c * N * M;
-  double *uc = a.u + c * kK * N;
-  for (int i = t; i < N * kK; i += blockDim.x) {
-    const int q = i / kK, k = i - q * kK;
-    double v = 0;
+  if constexpr (MODAL) {
+    // SetCoeff: the column block [M][K] takes the new coefficients
+    double *uc = a.u + c * kK * M;
+    for (int i = t; i < M * kK; i += blockDim.x) {
+      const int m = i / kK, k = i - m * kK;
+      uc[i] = s_new[k][m];
+    }
+  } else {
+    // UpdateNodalCoeff: nodal values = modal expansion at the nodes
+    const double *pc = a.psi + c * N * M;
+    double *uc = a.u + c * kK * N;
+    for (int i = t; i < N * kK; i += blockDim.x) {
+      const int q = i / kK, k = i - q * kK;
+      double v = 0;
 #pragma unroll
-    for (int m = 0; m < M; ++m) v += s_new[k][m] * pc[q * M + m];
-    uc[q * kK + k] = v;
+      for (int m = 0; m < M; ++m) v += s_new[k][m] * pc[q * M + m];
+      uc[q * kK + k] = v;
+    }
   }
   __syncthreads();  // the shared arrays are reused by the next cell
   }
@@ -501,10 +532,44 @@ int limiter_dispatch(mcfd_handle *h, double *u) {
   return 3;
 }
 
+// The modal scheme's limiter pass (M = basis size of degree p).
+template <int M>
+int limiter_dispatch_modal(mcfd_handle *h, double *u) {
+  const Mesh &mesh = h->mesh;
+  Limiter &l = h->lim;
+  const int64_t total = mesh.n_cells * M;
+  weno_transpose_kernel<M><<<(unsigned)((total + 255) / 256), 256, 0, h->stream>>>(u, l.modal, mesh.n_cells);
+  WenoArgs wa{u, l.modal, nullptr, l.proj, l.beta, l.eval, l.s00, l.divisor, l.adj,
+              l.frame, l.volume, l.troubled, mesh.n_cells, l.w0, l.eps, mesh.p < 3 ? 1.0 : 3.0};
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+  const unsigned grid =
+      (unsigned)std::min<int64_t>(mesh.n_cells, (int64_t)std::max(sms, 1) * h->tune.limiter_blocks_per_sm);
+  if (l.kind == 1 /* MCFD_LIMITER_LAZY: every cell */) {
+    weno_reconstruct_kernel<0, M, 1, true><<<grid, 64, 0, h->stream>>>(wa, nullptr, nullptr);
+    return 2;
+  }
+  cudaMemsetAsync(l.list_count, 0, sizeof(unsigned), h->stream);
+  weno_detect_kernel<M><<<(unsigned)((mesh.n_cells + 255) / 256), 256, 0, h->stream>>>(
+      wa, l.list, l.list_count);
+  if (l.kind == 2 /* MCFD_LIMITER_DETECT_LAZY */)
+    weno_reconstruct_kernel<0, M, 2, true><<<grid, 64, 0, h->stream>>>(wa, l.list, l.list_count);
+  else
+    weno_reconstruct_kernel<0, M, 3, true><<<grid, 64, 0, h->stream>>>(wa, l.list, l.list_count);
+  return 3;
+}
+
 }  // namespace
 
 int launch_limiter(mcfd_handle *h, double *u) {
   if (h->lim.kind == 0) return 0;
+  if (h->opt.scheme == kSchemeModal) {
+    switch (h->mesh.p) {
+      case 1: return limiter_dispatch_modal<4>(h, u);
+      case 2: return limiter_dispatch_modal<10>(h, u);
+      default: return limiter_dispatch_modal<20>(h, u);
+    }
+  }
   switch (h->mesh.q) {
     case 2: return limiter_dispatch<2>(h, u);
     case 3: return limiter_dispatch<3>(h, u);

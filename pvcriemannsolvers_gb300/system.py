@@ -363,16 +363,19 @@ class Lobatto:
 
 class General(Lobatto):
     """Modal DG (dg::General over polynomial::Projection) Euler system on one
-    GPU, on Hex8 and Tet4 cells.  The column holds, per cell, the M x 5
+    GPU, on every cell type (hexahedra, tetrahedra, wedges, pyramids).  The column holds, per cell, the M x 5
     coefficients on the cell's orthonormal Taylor basis (m-major)."""
 
     def __init__(self, mesh: Mesh, degree: int, riemann: str | int = "rusanov",
-                 cfl: float = 0.0, device: int = 0, precision: str = "fp64"):
+                 cfl: float = 0.0, device: int = 0, precision: str = "fp64",
+                 limiter: str = "none", weno_w0: float = 0.001, weno_eps: float = 1e-6):
         """precision: "fp64", or "mixed" (FP32 contractions on FP32 copies of
         the basis and point offsets; FP64 face states, Riemann fluxes and RK
-        accumulation)."""
+        accumulation).  limiter: as for Lobatto, on the cells' own bases
+        (WithLimiter<dg::General> over Projection, every cell type); it runs
+        after every solution update and after Approximate / project."""
         super().__init__(mesh, degree, riemann, cfl=cfl, device=device, scheme="modal",
-                         precision=precision)
+                         precision=precision, limiter=limiter, weno_w0=weno_w0, weno_eps=weno_eps)
         self.n_points = int(self._lib.mcfd_point_count(self._h))
 
     def points(self) -> np.ndarray:

@@ -128,3 +128,91 @@ def test_eigen_reconstruction_preserves_means_and_linear_fields(p):
                              1 + 0.05 * x[:, 1]).ravel()
     out_l, _ = lim.limit(lin)
     assert np.abs(out_l - lin).max() < 1e-12 * np.abs(lin).max()
+
+
+# ---------------------------------------------------------------- modal scheme
+# WithLimiter<dg::General> over Projection (the reference's DGFEM build,
+# demo/euler/sourceless.hpp:28-32, 74-80): the same limiter on every cell
+# type of the modal scheme, the column holding the modal coefficients.
+
+def modal_mesh(kind, periodic=False, shape=(3, 3, 2), seed=0, lengths=(1.0, 1.0, 1.0)):
+    per = (periodic,) * 3
+    kw = dict(lengths=lengths, periodic=per, jitter=0.1)
+    if kind == "mixed":
+        return meshlib.concat(meshlib.box(shape, seed=seed, **kw),
+                              meshlib.tet_box(shape, origin=(2.0, 0, 0), seed=seed + 1, **kw))
+    make = {"hex": meshlib.box, "tet": meshlib.tet_box, "wedge": meshlib.wedge_box,
+            "pyramid": meshlib.pyramid_box}[kind]
+    return make(shape, seed=seed, **kw)
+
+
+@pytest.mark.parametrize("kind", ["hex", "tet", "wedge", "pyramid", "mixed"])
+@pytest.mark.parametrize("p", [1, 2, 3])
+def test_modal_lazy_preserves_averages_and_reproduces_linear_fields(kind, p):
+    m = modal_mesh(kind)
+    om = orc.Modal(m, p)
+    lim = orc.ModalLimiter(om, orc.LIMITER_LAZY)
+    x, _ = om.points()
+    n = len(x)
+    rng = np.random.default_rng(p)
+    u = om.project(cases.prim_to_cons(1 + 0.3 * rng.uniform(-1, 1, n), 0.2, 0.1, 0.0,
+                                      1 + 0.3 * rng.uniform(-1, 1, n)))
+    v, count = lim.limit(u)
+    assert count == m.n_cells
+    # the constant mode carries the average: psi_0 is the only basis function
+    # with a non-zero mean, so the mean of every component is preserved iff
+    # coefficient 0 is (limiter/weno.hpp:172-176, 301-305: 1e-13)
+    c0_u, c0_v = u.reshape(-1, om.m, 5)[:, 0], v.reshape(-1, om.m, 5)[:, 0]
+    assert np.abs(c0_v - c0_u).max() <= 1e-13 * np.abs(c0_u).max()
+    assert not np.allclose(v, u)
+    # every candidate of a globally linear field is that field
+    lin = om.project(cases.prim_to_cons(1 + 0.1 * x[:, 0] - 0.2 * x[:, 1], 0.0, 0.0, 0.0, 1 + 0.05 * x[:, 2]))
+    w, _ = lim.limit(lin)
+    assert np.abs(w - lin).max() <= 1e-12 * np.abs(lin).max()
+
+
+@pytest.mark.parametrize("kind", ["tet", "wedge", "pyramid"])
+def test_modal_smoothness_of_linear_fields(kind):
+    """beta of a linear field g.x on any cell is vol^(2/3 - 1) * vol * |g|^2
+    per component (limiter/weno.hpp:25-95 with only first derivatives)."""
+    m = modal_mesh(kind, shape=(2, 2, 2))
+    om = orc.Modal(m, 2)
+    lim = orc.ModalLimiter(om)
+    x, w = om.points()
+    g = np.array([[0.3, -0.2, 0.5], [1.0, 0.0, 0.0], [0.0, 2.0, 0.0], [0.0, 0.0, -1.5], [0.7, 0.7, 0.7]])
+    u = om.project(x @ g.T)
+    modal = lim.modal(u)
+    # cell volumes from the quadrature: psi_0 = S00 is constant, 1 / S00^2 = vol
+    for c in range(m.n_cells):
+        vol = 1.0 / lim_s00(modal, u, om, c) ** 2
+        beta = lim.smoothness(c, modal[c])
+        want = vol ** (2 / 3) * (g * g).sum(axis=1)
+        np.testing.assert_allclose(beta, want, rtol=1e-12)
+
+
+def lim_s00(modal, u, om, c):
+    """psi_0 of cell c from a projected constant: coefficient 0 of the
+    constant 1 is integral(psi_0) = psi_0 * vol = 1 / psi_0."""
+    one = om.project(np.ones((om.n_points, 5)))
+    return 1.0 / one.reshape(-1, om.m, 5)[c, 0, 0]
+
+
+@pytest.mark.parametrize("kind", ["hex", "tet", "mixed"])
+def test_modal_eigen_preserves_means_and_detector_flags_the_jump(kind):
+    m = modal_mesh(kind, shape=(12, 2, 2), lengths=(1.0, 0.2, 0.2))
+    om = orc.Modal(m, 2)
+    x, _ = om.points()
+    n = len(x)
+    smooth = om.project(cases.prim_to_cons(1 + 0.01 * x[:, 0], 0.1, 0.0, 0.0, 1.0 + 0.0 * x[:, 0]))
+    lim = orc.ModalLimiter(om, orc.LIMITER_EIGEN)
+    assert not lim.troubled(smooth).any()
+    jump = om.project(cases.prim_to_cons(1 + 0.8 * (x[:, 0] > 0.53), 0.1, 0.0, 0.0, 1 + 0.5 * (x[:, 0] > 0.53)))
+    flags = lim.troubled(jump)
+    assert flags.any() and not flags.all()
+    out, count = lim.limit(jump)
+    assert count == flags.sum()
+    c0_in, c0_out = jump.reshape(-1, om.m, 5)[:, 0], out.reshape(-1, om.m, 5)[:, 0]
+    assert np.abs(c0_out - c0_in).max() <= 1e-12 * np.abs(c0_in).max()
+    # unflagged cells are untouched
+    keep = ~flags
+    assert np.array_equal(out.reshape(-1, om.m * 5)[keep], jump.reshape(-1, om.m * 5)[keep])
