@@ -329,6 +329,50 @@ NCU_TRAFFIC_40 = {
 NCU_CELLS = 40 ** 3
 
 
+# Whole-step roofline (the fixed convention of the workload's algorithmic
+# counts): T_roof = max(B / BW_HBM, F64 / P_FP64, F32 / P_FP32) for one SSP-RK3
+# step of three stages, achieved = T_roof / T_measured.  The dt reduction and
+# limiter passes add measured time but no algorithmic counts.  B: per stage
+# 8 L (stage input) + 8 L (u_n, stages 2-3) + 8 L (output) + geometry (Hex8
+# 192 B, Tet4 96 B, Wedge6 144 B, Pyra5 120 B per cell) + 4 B per face slot.
+# FP64 / FP32 flops per the form: the plain form counts every flop as FP64;
+# the mixed form moves the contractions (volume flux and contravariant
+# transform, differentiation, lift) to FP32 and keeps the Riemann fluxes and
+# the RK accumulation in FP64.  P_FP32 is the nominal SIMT rate (152 SMs x 128
+# lanes x 2 flops x 2.07 GHz); the contractions run on the FP32 SIMT pipe.
+FP32_SIMT_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
+C_R = {"rusanov": 60, "hllc": 120, "roe": 200, "exact": 400, "ausm": 80}
+
+
+def step_roofline(bytes_step, f64_step, f32_step, ms_per_step, hbm_peak, fp64_peak, peak_src):
+    terms = {"hbm": bytes_step / (hbm_peak * 1e9), "fp64": f64_step / (fp64_peak * 1e12),
+             "fp32": f32_step / (FP32_SIMT_PEAK_TFLOPS * 1e12)}
+    bound = max(terms, key=terms.get)
+    t_roof = terms[bound]
+    return {"t_roof_ms": t_roof * 1e3, "t_measured_ms": ms_per_step, "achieved": t_roof / (ms_per_step * 1e-3),
+            "bound": bound, "alg_bytes_per_step": bytes_step, "alg_fp64_flops_per_step": f64_step,
+            "alg_fp32_flops_per_step": f32_step, "terms_ms": {k: v * 1e3 for k, v in terms.items()},
+            "peaks": {"hbm_gbs": hbm_peak, "hbm_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+                      "fp64_tflops": fp64_peak, "fp64_source": "cuBLAS DGEMM 4096^3 measured in this run",
+                      "fp32_tflops": FP32_SIMT_PEAK_TFLOPS, "fp32_source": "nominal SIMT rate at 2070 MHz"}}
+
+
+def nodal_step_counts(L, cells, degree, riemann, precision):
+    """Algorithmic bytes and FP64 / FP32 flops of one SSP-RK3 step of DGSEM
+    (Hex8 cells, the three stages)."""
+    Q = degree + 1
+    N = Q ** 3
+    per_stage_bytes = 24 * L + (192 + 4 * 6) * cells
+    bytes_step = 3 * per_stage_bytes - 8 * L  # stage 1 reads no u_n
+    contraction = 130 / K + 6 * Q            # per DOF: volume flux + transform, differentiation
+    riemann_f = 3 * Q * Q * C_R[riemann] / (N * K)
+    if precision == "mixed":
+        f64, f32 = riemann_f + 4, contraction
+    else:
+        f64, f32 = contraction + riemann_f + 4, 0.0
+    return bytes_step, 3 * f64 * L, 3 * f32 * L
+
+
 def roofline_of(kt, L, cells, hbm_peak, peak_src, fp64_peak, precision):
     """Roofline of the dominant kernel (algorithmic counts per launch)."""
     N = (DEGREE + 1) ** 3
@@ -503,6 +547,10 @@ def modal_roofline(kt, m, L, fp64_peak, hbm_peak, peak_src):
     cell_flops = 2 * K * 3 * M * nq + 2 * K * M * face_sides + 4 * L
     face_flops = face_pts * (4 * K * M + C_HLLC)
     cell_bytes = 24 * L + sum(counts[t] * per[t][1] for t in per) + 4 * sum(counts[t] * per[t][2] for t in per)
+    if kt is None:  # the counts of one SSP-RK3 step for step_roofline: (bytes, FP64, FP32) per form
+        f64_mixed = face_pts * C_HLLC + 4 * L
+        return {"fp64": (3 * cell_bytes - 8 * L, 3 * (cell_flops + face_flops), 0.0),
+                "mixed": (3 * cell_bytes - 8 * L, 3 * f64_mixed, 3 * (cell_flops + face_flops) - 3 * f64_mixed)}
     dom = "cell_update" if kt["cell_update"] >= kt["face_flux"] else "face_flux"
     flops = cell_flops if dom == "cell_update" else face_flops
     t = kt[dom] * 1e-3
@@ -594,6 +642,10 @@ def run_mixed_box(args, rank, world, local_rank, kind="mixed_box"):
     line["roofline"]["note"] = ("FP64 form's dominant kernel (the mixed form moves the contractions "
                                 "to FP32); face_flux includes the Taylor-coefficient kernel a = S^T c")
     line["roofline"]["mixed_kernel_ms"] = r["kernel_ms"]
+    counts = modal_roofline(None, m, L, fp64_peak, hbm_peak, peak_src)
+    line["roofline"]["step"] = step_roofline(*counts["mixed"], r["ms_per_step"], hbm_peak, fp64_peak, peak_src)
+    line["plain_fp64"]["roofline_step"] = step_roofline(*counts["fp64"], res["fp64"]["ms_per_step"], hbm_peak,
+                                                        fp64_peak, peak_src)
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -937,6 +989,12 @@ def run_quadrant(args, rank, world, local_rank):
                      "note": "per-kernel rooflines of the DGSEM kernels: the vortex line"},
         "cpu_baseline": cpu,
     }
+    line["roofline"]["step"] = step_roofline(*nodal_step_counts(L, m.n_cells, QUAD_DEGREE, "roe", "fp64"),
+                                             r["ms_per_step"], *measured_peaks()[:1], fp64_peak,
+                                             measured_peaks()[1])
+    line["mixed"]["roofline_step"] = step_roofline(
+        *nodal_step_counts(L, m.n_cells, QUAD_DEGREE, "roe", "mixed"), res["mixed"]["ms_per_step"],
+        *measured_peaks()[:1], fp64_peak, measured_peaks()[1])
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -995,6 +1053,8 @@ def run_gpu(args, rank, world, local_rank):
             "roofline": roofline_of(r["kernel_ms"], L, m.n_cells, hbm_peak, peak_src, fp64_peak, head),
             "cpu_baseline": cpu,
         }
+        line["roofline"]["step"] = step_roofline(*nodal_step_counts(L, m.n_cells, DEGREE, "rusanov", head),
+                                                 r["ms_per_step"], hbm_peak, fp64_peak, peak_src)
         if head == "mixed" and "fp64" in res:
             p = res["fp64"]
             line["plain_fp64"] = {"value": p["value"], "ms_per_step": p["ms_per_step"], "e2e": p["e2e"],
@@ -1002,6 +1062,9 @@ def run_gpu(args, rank, world, local_rank):
                                   "gpu_launches": p["launches"], "clocks": p["clocks"],
                                   "roofline": roofline_of(p["kernel_ms"], L, m.n_cells, hbm_peak, peak_src,
                                                           fp64_peak, "fp64")}
+            line["plain_fp64"]["roofline"]["step"] = step_roofline(
+                *nodal_step_counts(L, m.n_cells, DEGREE, "rusanov", "fp64"), p["ms_per_step"], hbm_peak,
+                fp64_peak, peak_src)
         print(json.dumps(line), flush=True)
 
 

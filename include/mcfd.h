@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define MCFD_ABI_VERSION 1
+#define MCFD_ABI_VERSION 2
 #define MCFD_K 5
 
 /* Status codes. */
@@ -80,16 +80,28 @@ enum mcfd_bc_kind {
 };
 
 /* The reference passes a std::function<Value(Global, double t)> per boundary
- * name.  The ABI carries that function as a small program evaluated on the
- * device at every boundary face point and stage time:
- *   CONSTANT:     value = a
- *   MOVING_SPLIT: value = (x[axis] - speed * t) < position ? a : b
- * (the second form is the moving-shock boundary of demo/euler/riemann2d.cpp).
+ * name (spatial/fem.hpp:196-222).  The ABI carries that function as a small
+ * program evaluated on the device at every boundary face point and stage
+ * time:
+ *   CONSTANT:       value = a
+ *   MOVING_SPLIT:   value = (x[axis] - speed * t) < position ? a : b
+ *                   (the moving-shock boundaries of demo/euler/riemann2d.cpp)
+ *   OBLIQUE_SPLIT:  value = (normal . x - speed * t) < position ? a : b
+ *                   (the oblique moving shock of demo/euler/double_mach.cpp:
+ *                   normal = (tan 60, -1, 0), speed = tan 60 * u_x,
+ *                   position = tan 60 * x_gap, a = post-shock, b = pre-shock)
+ *   TABLE:          a value per face point of the group, set by
+ *                   mcfd_set_bc_table: any function of the position alone,
+ *                   sampled once by the caller at mcfd_bc_points (e.g. the
+ *                   right boundary of demo/euler/shu_osher.cpp, whose state
+ *                   is the initial sine profile)
  * a and b are conservative states, or for SUBSONIC_INLET the tuple
  * (p_total, cos_x, cos_y, cos_z, T_total), as in the reference. */
 enum mcfd_state_program {
   MCFD_STATE_CONSTANT = 0,
-  MCFD_STATE_MOVING_SPLIT = 1
+  MCFD_STATE_MOVING_SPLIT = 1,
+  MCFD_STATE_OBLIQUE_SPLIT = 2,
+  MCFD_STATE_TABLE = 3
 };
 
 typedef struct mcfd_bc_state {
@@ -101,6 +113,7 @@ typedef struct mcfd_bc_state {
   double speed;
   double a[MCFD_K];
   double b[MCFD_K];
+  double normal[3]; /* OBLIQUE_SPLIT only (need not be a unit vector) */
 } mcfd_bc_state;
 
 /* Element types and their maps (coordinate/hexahedron.hpp Hexahedron8 /
@@ -219,6 +232,16 @@ int64_t mcfd_column_size(const mcfd_handle *h);
 
 /* Boundary registration for one face group (fem.hpp:196-222). */
 int mcfd_set_bc(mcfd_handle *h, int32_t group, const mcfd_bc_state *state);
+
+/* Face points of boundary group `group` in the order a TABLE program takes
+ * its values: the group's faces in mesh order, each face's quadrature points
+ * in order.  xyz [n][3] host memory. */
+int mcfd_bc_point_count(const mcfd_handle *h, int32_t group, int64_t *n);
+int mcfd_bc_points(const mcfd_handle *h, int32_t group, double *xyz, int64_t n);
+/* The values [n][5] of a group registered with program MCFD_STATE_TABLE, at
+ * mcfd_bc_points (host memory, copied to the device; call after
+ * mcfd_set_bc).  Until set, such a group's value is its state a. */
+int mcfd_set_bc_table(mcfd_handle *h, int32_t group, const double *values, int64_t n);
 
 /* System<Scalar> quartet (ode.hpp:17-48): host columns of length n. */
 int mcfd_set_time(mcfd_handle *h, double t);

@@ -50,18 +50,27 @@ enum {
   ORC_BC_NO_SLIP_WALL = 7 /* viscous fr::Lobatto only (spatial/fr/lobatto.hpp:298-317) */
 };
 
-/* Given-state programs for boundaries that need an exterior value. */
-enum { ORC_STATE_CONSTANT = 0, ORC_STATE_MOVING_SPLIT = 1 };
+/* Given-state programs for boundaries that need an exterior value: the
+ * std::function<Value(Global, double)> of spatial/fem.hpp:196-222 for the
+ * demos' functions. */
+enum { ORC_STATE_CONSTANT = 0, ORC_STATE_MOVING_SPLIT = 1, ORC_STATE_OBLIQUE_SPLIT = 2,
+       ORC_STATE_TABLE = 3 };
 
 /* One boundary group: kind, and the given value program
- * value(x, t) = (x[axis] - speed * t) < position ? a : b   (MOVING_SPLIT)
- * value(x, t) = a                                           (CONSTANT)   */
+ * value(x, t) = (x[axis] - speed * t) < position ? a : b         (MOVING_SPLIT)
+ * value(x, t) = (normal . x - speed * t) < position ? a : b      (OBLIQUE_SPLIT)
+ * value(x, t) = table[point] (the function sampled at every face
+ *               point of the mesh, [face points][K], by global face-point
+ *               index)                                             (TABLE)
+ * value(x, t) = a                                                  (CONSTANT)   */
 typedef struct {
   int kind;
   int program;
   int axis;
   double position, speed;
   double a[ORC_K], b[ORC_K];
+  double normal[3];
+  const double *table;
 } orc_bc;
 
 /* ---- point functions (used by the golden-vector tests) ---- */

@@ -19,7 +19,7 @@ LIB = HERE / "liborc.so"
 EXACT, HLLC, AUSM, ROE, RUSANOV = range(5)
 BC_NONE, BC_INVISCID_WALL, BC_SUPERSONIC_INLET, BC_SUPERSONIC_OUTLET, BC_SUBSONIC_INLET, \
     BC_SUBSONIC_OUTLET, BC_SMART, BC_NO_SLIP_WALL = range(8)
-STATE_CONSTANT, STATE_MOVING_SPLIT = 0, 1
+STATE_CONSTANT, STATE_MOVING_SPLIT, STATE_OBLIQUE_SPLIT, STATE_TABLE = 0, 1, 2, 3
 
 _D = C.POINTER(C.c_double)
 
@@ -27,7 +27,8 @@ _D = C.POINTER(C.c_double)
 class OrcBc(C.Structure):
     _fields_ = [("kind", C.c_int), ("program", C.c_int), ("axis", C.c_int),
                 ("position", C.c_double), ("speed", C.c_double),
-                ("a", C.c_double * 5), ("b", C.c_double * 5)]
+                ("a", C.c_double * 5), ("b", C.c_double * 5),
+                ("normal", C.c_double * 3), ("table", _D)]
 
 
 def build(force: bool = False) -> Path:
@@ -140,16 +141,33 @@ def flux_boundary(riemann: int, bc_kind: int, frame, cons_in, given) -> np.ndarr
     return out
 
 
-def make_bcs(specs: dict[int, tuple]) -> tuple[int, C.Array]:
-    """specs: group -> (kind, value) with value None, a 5-vector, or an object
-    with axis/position/speed/a/b (moving split)."""
+def make_bcs(specs: dict[int, tuple], face_points=None) -> tuple[int, C.Array]:
+    """specs: group -> (kind, value) with value None, a 5-vector, an object
+    with axis/position/speed/a/b (moving split), one with
+    normal/position/speed/a/b (oblique split), or a callable of the points
+    [n, 3] -> states [n, 5] (sampled at face_points, every face point of the
+    mesh by global index, into a table)."""
     n = max(specs) + 1 if specs else 1
     arr = (OrcBc * n)()
+    keep = []
     for g, (kind, value) in specs.items():
         b = arr[g]
         b.kind = kind
         if value is None:
             b.program = STATE_CONSTANT
+        elif callable(value):
+            table = np.ascontiguousarray(value(np.asarray(face_points).reshape(-1, 3)), dtype=np.float64)
+            keep.append(table)
+            b.program = STATE_TABLE
+            b.table = table.ctypes.data_as(_D)
+        elif hasattr(value, "normal"):
+            b.program = STATE_OBLIQUE_SPLIT
+            b.position, b.speed = float(value.position), float(value.speed)
+            for k in range(3):
+                b.normal[k] = float(value.normal[k])
+            for k in range(5):
+                b.a[k] = float(value.a[k])
+                b.b[k] = float(value.b[k])
         elif hasattr(value, "axis"):
             b.program = STATE_MOVING_SPLIT
             b.axis, b.position, b.speed = int(value.axis), float(value.position), float(value.speed)
@@ -160,6 +178,7 @@ def make_bcs(specs: dict[int, tuple]) -> tuple[int, C.Array]:
             b.program = STATE_CONSTANT
             for k in range(5):
                 b.a[k] = float(value[k])
+    arr._keep = keep  # the tables live as long as the array
     return n, arr
 
 
@@ -198,7 +217,12 @@ class Mesh:
             self._m = None
 
     def set_bcs(self, specs: dict[int, tuple]) -> None:
-        self.bcs = make_bcs(specs)
+        pts = None
+        if any(callable(v) for _, v in specs.values()):
+            qf = (self.degree + 1) ** 2
+            pts = np.empty((self.n_faces * qf, 3))
+            self.lib.orc_face_geometry(self._m, _p(pts), None, None)
+        self.bcs = make_bcs(specs, pts)
 
     def face_node_maps(self):
         qf = (self.degree + 1) ** 2
@@ -518,7 +542,8 @@ class Modal:
             self._m = None
 
     def set_bcs(self, specs: dict[int, tuple]) -> None:
-        self.bcs = make_bcs(specs)
+        pts = self.face_points()[0] if any(callable(v) for _, v in specs.values()) else None
+        self.bcs = make_bcs(specs, pts)
 
     def points(self):
         xyz = np.empty((self.n_points, 3))

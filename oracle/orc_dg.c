@@ -479,11 +479,16 @@ int orc_face_geometry(const orc_mesh *m, double *xyz, double *weights,
 
 /* ---------------- residual ---------------- */
 
-static void given_value(const orc_bc *bc, const double *x, double t,
+static void given_value(const orc_bc *bc, const double *x, double t, int64_t point,
                         double *v) {
   const double *src = bc->a;
   if (bc->program == ORC_STATE_MOVING_SPLIT) {
     src = (x[bc->axis] - bc->speed * t) < bc->position ? bc->a : bc->b;
+  } else if (bc->program == ORC_STATE_OBLIQUE_SPLIT) {
+    src = (bc->normal[0] * x[0] + bc->normal[1] * x[1] + bc->normal[2] * x[2] - bc->speed * t) < bc->position
+              ? bc->a : bc->b;
+  } else if (bc->program == ORC_STATE_TABLE && bc->table) {
+    src = &bc->table[point * K];
   }
   memcpy(v, src, sizeof(double) * K);
 }
@@ -565,7 +570,7 @@ static int fr_residual(const orc_mesh *m, int riemann, int n_bc,
         orc_flux_rotated(riemann, fr, uh, us, flux);
       } else {
         double given[K];
-        given_value(&bcs[g], &m->face_xyz[(f * QF + fp) * 3], t, given);
+        given_value(&bcs[g], &m->face_xyz[(f * QF + fp) * 3], t, f * QF + fp, given);
         orc_flux_boundary(riemann, bcs[g].kind, fr, uh, given, flux);
       }
       {
@@ -646,7 +651,7 @@ int orc_dgsem_residual(const orc_mesh *m, int riemann, int n_bc,
         orc_flux_rotated(riemann, fr, uh, us, out);
       } else if (g >= 0 && g < n_bc && bcs[g].kind != ORC_BC_NONE) {
         double given[K];
-        given_value(&bcs[g], &m->face_xyz[(f * QF + fp) * 3], t, given);
+        given_value(&bcs[g], &m->face_xyz[(f * QF + fp) * 3], t, f * QF + fp, given);
         orc_flux_boundary(riemann, bcs[g].kind, fr, uh, given, out);
       } else {
         memset(out, 0, sizeof(double) * K);

@@ -656,10 +656,16 @@ int orc_modal_project(const orc_modal *m, const double *values, double *u) {
   return 0;
 }
 
-static void given_value(const orc_bc *bc, const double *x, double t, double *v) {
+static void given_value(const orc_bc *bc, const double *x, double t, int64_t point, double *v) {
   const double *src = bc->a;
-  if (bc->program == ORC_STATE_MOVING_SPLIT)
+  if (bc->program == ORC_STATE_MOVING_SPLIT) {
     src = (x[bc->axis] - bc->speed * t) < bc->position ? bc->a : bc->b;
+  } else if (bc->program == ORC_STATE_OBLIQUE_SPLIT) {
+    src = (bc->normal[0] * x[0] + bc->normal[1] * x[1] + bc->normal[2] * x[2] - bc->speed * t) < bc->position
+              ? bc->a : bc->b;
+  } else if (bc->program == ORC_STATE_TABLE && bc->table) {
+    src = &bc->table[point * K];
+  }
   memcpy(v, src, sizeof(double) * K);
 }
 
@@ -717,7 +723,7 @@ int orc_modal_residual(const orc_modal *m, int riemann, int n_bc,
         orc_flux_rotated(riemann, &m->ff[q * 9], uh, us, out);
       } else if (g >= 0 && g < n_bc && bcs[g].kind != ORC_BC_NONE) {
         double given[K];
-        given_value(&bcs[g], x, t, given);
+        given_value(&bcs[g], x, t, q, given);
         orc_flux_boundary(riemann, bcs[g].kind, &m->ff[q * 9], uh, given, out);
       } else {
         memset(out, 0, sizeof(double) * K);

@@ -461,11 +461,18 @@ void orc_visc_properties(const orc_visc *v, const double *u, double *nu, double 
   if (min_dt_out) *min_dt_out = min_dt;
 }
 
-static void given_value(const orc_bc *bc, const double *x, double t, double *g) {
+static void given_value(const orc_bc *bc, const double *x, double t, int64_t point,
+                        double *v) {
   const double *src = bc->a;
-  if (bc->program == ORC_STATE_MOVING_SPLIT && (x[bc->axis] - bc->speed * t) >= bc->position)
-    src = bc->b;
-  memcpy(g, src, sizeof(double) * K);
+  if (bc->program == ORC_STATE_MOVING_SPLIT) {
+    src = (x[bc->axis] - bc->speed * t) < bc->position ? bc->a : bc->b;
+  } else if (bc->program == ORC_STATE_OBLIQUE_SPLIT) {
+    src = (bc->normal[0] * x[0] + bc->normal[1] * x[1] + bc->normal[2] * x[2] - bc->speed * t) < bc->position
+              ? bc->a : bc->b;
+  } else if (bc->program == ORC_STATE_TABLE && bc->table) {
+    src = &bc->table[point * K];
+  }
+  memcpy(v, src, sizeof(double) * K);
 }
 
 int orc_visc_residual(const orc_visc *v, int riemann, int n_bc, const orc_bc *bcs, double t,
@@ -556,7 +563,7 @@ int orc_visc_residual(const orc_visc *v, int riemann, int n_bc, const orc_bc *bc
         }
       } else {
         double given[K];
-        given_value(&bcs[g], &m->face_xyz[(f * QF + fp) * 3], t, given);
+        given_value(&bcs[g], &m->face_xyz[(f * QF + fp) * 3], t, f * QF + fp, given);
         orc_flux_boundary(riemann, bcs[g].kind, fr, uh, given, flux);
       }
     }

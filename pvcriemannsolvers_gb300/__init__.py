@@ -8,7 +8,7 @@ reference interface.  There is no CPU fallback: constructing a system without
 the built library or without a GPU raises.
 """
 from . import capi, cases, mesh
-from .system import Ensemble, General, Lobatto, MovingSplit, RungeKutta, base64_encode, write_vtu_arrays
+from .system import Ensemble, General, Lobatto, MovingSplit, ObliqueSplit, RungeKutta, base64_encode, write_vtu_arrays
 
-__all__ = ["capi", "cases", "mesh", "Ensemble", "General", "Lobatto", "MovingSplit", "RungeKutta",
+__all__ = ["capi", "cases", "mesh", "Ensemble", "General", "Lobatto", "MovingSplit", "ObliqueSplit", "RungeKutta",
            "base64_encode", "write_vtu_arrays"]

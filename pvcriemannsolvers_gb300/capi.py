@@ -21,7 +21,7 @@ RIEMANN = {"exact": EXACT, "hllc": HLLC, "ausm": AUSM, "roe": ROE, "rusanov": RU
 BC_NONE, BC_INVISCID_WALL, BC_SUPERSONIC_INLET, BC_SUPERSONIC_OUTLET, BC_SUBSONIC_INLET, \
     BC_SUBSONIC_OUTLET, BC_SMART, BC_NO_SLIP_WALL = range(8)
 INIT_AVERAGE, INIT_MAJORITY = 1, 2
-STATE_CONSTANT, STATE_MOVING_SPLIT = 0, 1
+STATE_CONSTANT, STATE_MOVING_SPLIT, STATE_OBLIQUE_SPLIT, STATE_TABLE = 0, 1, 2, 3
 HEX8, TET4 = 0, 1
 DGSEM, FR, MODAL = 0, 1, 2
 SCHEME = {"dgsem": DGSEM, "fr": FR, "modal": MODAL}
@@ -69,6 +69,7 @@ class BcState(C.Structure):
         ("speed", C.c_double),
         ("a", C.c_double * 5),
         ("b", C.c_double * 5),
+        ("normal", C.c_double * 3),
     ]
 
 
@@ -83,6 +84,9 @@ SIGNATURES = {
     "mcfd_column_size": (C.c_int64, [_P]),
     "mcfd_set_bc": (C.c_int, [_P, C.c_int32, C.POINTER(BcState)]),
     "mcfd_set_time": (C.c_int, [_P, C.c_double]),
+    "mcfd_bc_point_count": (C.c_int, [_P, C.c_int32, C.POINTER(C.c_int64)]),
+    "mcfd_bc_points": (C.c_int, [_P, C.c_int32, _D, C.c_int64]),
+    "mcfd_set_bc_table": (C.c_int, [_P, C.c_int32, _D, C.c_int64]),
     "mcfd_set_solution": (C.c_int, [_P, _D, C.c_int64]),
     "mcfd_get_solution": (C.c_int, [_P, _D, C.c_int64]),
     "mcfd_residual": (C.c_int, [_P, _D, C.c_int64]),

@@ -189,6 +189,9 @@ void release(mcfd_handle *h) {
     if (p) cudaFree(p);
   mcfd::release_viscosity(h);
   if (h->mesh.node_w) cudaFree(h->mesh.node_w);
+  if (m.bc_row) cudaFree(m.bc_row);
+  for (double *t : m.bc_tables)
+    if (t) cudaFree(t);
   mcfd::drop_graphs(h);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
 }
@@ -863,10 +866,11 @@ int mcfd_create(const mcfd_mesh_desc *mesh, const mcfd_options *options,
     if (e == cudaSuccess) e = cudaMalloc(&h->buf.state, sizeof(mcfd::DevState));
     if (e == cudaSuccess) e = cudaMemset(h->buf.u, 0, col);
     if (e == cudaSuccess) e = cudaMemset(h->buf.state, 0, sizeof(mcfd::DevState));
-    // node traces for the Rusanov face flux of the nodal schemes (a limiter
-    // rewrites states after the cell kernel, so it turns them off)
-    h->use_trace = options->scheme != MCFD_MODAL && options->riemann == MCFD_RUSANOV &&
-                   options->limiter == MCFD_LIMITER_NONE;
+    // node traces for the Rusanov, Roe and HLLC face fluxes of the nodal
+    // schemes (the limiter rewrites the traces of the cells it reconstructs)
+    h->use_trace = options->scheme != MCFD_MODAL &&
+                   (options->riemann == MCFD_RUSANOV || options->riemann == MCFD_ROE ||
+                    options->riemann == MCFD_HLLC);
     if (e == cudaSuccess && h->use_trace)
       e = cudaMalloc(&h->buf.trace, sizeof(double) * 3 * h->mesh.n_cells * h->mesh.n);
     if (e != cudaSuccess) rc = cuda_fail(h, e, "device allocation");
@@ -899,8 +903,7 @@ int mcfd_set_bc(mcfd_handle *h, int32_t group, const mcfd_bc_state *s) {
   if (s->kind == MCFD_BC_NO_SLIP_WALL && h->opt.scheme != MCFD_FR)
     return fail(h, MCFD_ERR_UNSUPPORTED, "no-slip walls run on the fr::Lobatto scheme only");
   if (s->kind < MCFD_BC_NONE || s->kind > MCFD_BC_NO_SLIP_WALL ||
-      (s->program != MCFD_STATE_CONSTANT && s->program != MCFD_STATE_MOVING_SPLIT) ||
-      s->axis < 0 || s->axis > 2)
+      s->program < MCFD_STATE_CONSTANT || s->program > MCFD_STATE_TABLE || s->axis < 0 || s->axis > 2)
     return fail(h, MCFD_ERR_ARGUMENT, "bad boundary description");
   BcDev bc{};
   bc.kind = s->kind;
@@ -909,11 +912,113 @@ int mcfd_set_bc(mcfd_handle *h, int32_t group, const mcfd_bc_state *s) {
   bc.position = s->position;
   bc.speed = s->speed;
   for (int k = 0; k < 5; ++k) { bc.a[k] = s->a[k]; bc.b[k] = s->b[k]; }
+  for (int e = 0; e < 3; ++e) bc.normal[e] = s->normal[e];
+  // a table registered earlier for this group stays until replaced
+  if (s->program == MCFD_STATE_TABLE && (size_t)group < h->mesh.bc_tables.size())
+    bc.table = h->mesh.bc_tables[group];
   h->mesh.host_bcs[group] = bc;
   cudaSetDevice(h->device);
   CUDA_TRY(h, cudaMemcpyAsync(h->mesh.bcs + group, &h->mesh.host_bcs[group], sizeof(BcDev),
                               cudaMemcpyHostToDevice, h->stream));
   CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  return MCFD_OK;
+}
+
+// The face points of boundary group `group` (global point ids, in order).
+static int group_points(const mcfd_handle *h, int32_t group, std::vector<int64_t> *gids,
+                        std::vector<double> *xyz) {
+  const auto &m = h->mesh;
+  std::vector<int32_t> fg(m.n_faces);
+  cudaSetDevice(h->device);
+  if (m.n_faces && cudaMemcpy(fg.data(), m.face_group, sizeof(int32_t) * m.n_faces,
+                              cudaMemcpyDeviceToHost) != cudaSuccess)
+    return MCFD_ERR_CUDA;
+  std::vector<int32_t> off(m.n_faces + 1);
+  const bool modal = h->opt.scheme == MCFD_MODAL;
+  if (modal) {
+    if (cudaMemcpy(off.data(), h->modal.face_off, sizeof(int32_t) * (m.n_faces + 1), cudaMemcpyDeviceToHost) !=
+        cudaSuccess)
+      return MCFD_ERR_CUDA;
+  } else {
+    for (int64_t f = 0; f <= m.n_faces; ++f) off[f] = (int32_t)(f * m.qf);
+  }
+  gids->clear();
+  for (int64_t f = 0; f < m.n_faces; ++f)
+    if (fg[f] == group)
+      for (int32_t q = off[f]; q < off[f + 1]; ++q) gids->push_back(q);
+  if (!xyz) return MCFD_OK;
+  xyz->assign(gids->size() * 3, 0.0);
+  if (modal) {
+    std::vector<double4> fpt(m.n_points);
+    if (m.n_points && cudaMemcpy(fpt.data(), h->modal.fpt, sizeof(double4) * m.n_points,
+                                 cudaMemcpyDeviceToHost) != cudaSuccess)
+      return MCFD_ERR_CUDA;
+    for (size_t i = 0; i < gids->size(); ++i) {
+      const double4 x = fpt[(*gids)[i]];
+      (*xyz)[i * 3] = x.x; (*xyz)[i * 3 + 1] = x.y; (*xyz)[i * 3 + 2] = x.z;
+    }
+  } else {
+    std::vector<double> fx(m.n_points * 3);
+    if (m.n_points && cudaMemcpy(fx.data(), m.face_xyz, sizeof(double) * 3 * m.n_points,
+                                 cudaMemcpyDeviceToHost) != cudaSuccess)
+      return MCFD_ERR_CUDA;
+    for (size_t i = 0; i < gids->size(); ++i)
+      for (int e = 0; e < 3; ++e) (*xyz)[i * 3 + e] = fx[(*gids)[i] * 3 + e];
+  }
+  return MCFD_OK;
+}
+
+int mcfd_bc_point_count(const mcfd_handle *h, int32_t group, int64_t *n) {
+  if (!h || !n || group < 0 || group >= h->mesh.n_groups) return MCFD_ERR_ARGUMENT;
+  std::vector<int64_t> gids;
+  int rc = group_points(h, group, &gids, nullptr);
+  if (rc) return rc;
+  *n = (int64_t)gids.size();
+  return MCFD_OK;
+}
+
+int mcfd_bc_points(const mcfd_handle *h, int32_t group, double *xyz, int64_t n) {
+  if (!h || !xyz || group < 0 || group >= h->mesh.n_groups) return MCFD_ERR_ARGUMENT;
+  std::vector<int64_t> gids;
+  std::vector<double> pts;
+  int rc = group_points(h, group, &gids, &pts);
+  if (rc) return rc;
+  if ((int64_t)gids.size() != n) return MCFD_ERR_ARGUMENT;
+  std::copy(pts.begin(), pts.end(), xyz);
+  return MCFD_OK;
+}
+
+int mcfd_set_bc_table(mcfd_handle *h, int32_t group, const double *values, int64_t n) {
+  if (!h || !values) return MCFD_ERR_ARGUMENT;
+  if (group < 0 || group >= h->mesh.n_groups) return fail(h, MCFD_ERR_ARGUMENT, "boundary group out of range");
+  auto &m = h->mesh;
+  if (m.host_bcs[group].program != MCFD_STATE_TABLE)
+    return fail(h, MCFD_ERR_ARGUMENT, "the group's state program is not MCFD_STATE_TABLE");
+  std::vector<int64_t> gids;
+  int rc = group_points(h, group, &gids, nullptr);
+  if (rc) return fail(h, rc, "reading the face table");
+  if ((int64_t)gids.size() != n) return fail(h, MCFD_ERR_ARGUMENT, "table size != the group's face points");
+  for (int64_t i = 0; i < n * mcfd::kK; ++i)
+    if (!std::isfinite(values[i])) return fail(h, MCFD_ERR_ARGUMENT, "non-finite boundary table value");
+  cudaSetDevice(h->device);
+  if (m.bc_tables.size() < (size_t)m.n_groups) m.bc_tables.resize(m.n_groups, nullptr);
+  if (!m.bc_row) {
+    CUDA_TRY(h, cudaMalloc(&m.bc_row, sizeof(int32_t) * std::max<int64_t>(m.n_points, 1)));
+    m.host_bc_row.assign(std::max<int64_t>(m.n_points, 1), -1);
+  }
+  for (int64_t i = 0; i < n; ++i) m.host_bc_row[gids[i]] = (int32_t)i;
+  CUDA_TRY(h, cudaMemcpy(m.bc_row, m.host_bc_row.data(), sizeof(int32_t) * m.host_bc_row.size(),
+                         cudaMemcpyHostToDevice));
+  if (m.bc_tables[group]) {
+    cudaFree(m.bc_tables[group]);
+    m.bc_tables[group] = nullptr;
+  }
+  CUDA_TRY(h, cudaMalloc(&m.bc_tables[group], sizeof(double) * mcfd::kK * std::max<int64_t>(n, 1)));
+  CUDA_TRY(h, cudaMemcpy(m.bc_tables[group], values, sizeof(double) * mcfd::kK * n, cudaMemcpyHostToDevice));
+  m.host_bcs[group].table = m.bc_tables[group];
+  CUDA_TRY(h, cudaMemcpy(m.bcs + group, &m.host_bcs[group], sizeof(BcDev), cudaMemcpyHostToDevice));
+  // captured step graphs hold the old bc_row pointer only if it changed: recapture
+  mcfd::drop_graphs(h);
   return MCFD_OK;
 }
 

@@ -56,6 +56,7 @@ struct FaceArgs {
   const double *trace;  // node traces of u (Rusanov), or null
   int f32_out;          // mixed form: the flux buffer holds FP32 values
   int visc;             // artificial viscosity: no-slip walls take the wall flux
+  const int32_t *bc_row;  // [points] row in the group's boundary table, or null
 };
 
 // FR: a boundary face point without a registered boundary gets no correction
@@ -99,6 +100,7 @@ struct CellArgs {
   CaseView cs;
   double *trace;  // write the node traces of u_out here (surface nodes), or null
   const double *nu;  // artificial viscosity [cells][K] (VISC variant), else null
+  int trace_roe;     // the traces' third entry is sqrt(rho) (Roe), else the sound speed
 };
 
 // Step of the case that owns cell c (the handle's step without cases).
@@ -123,13 +125,6 @@ __device__ __forceinline__ double fr_sign(int side) {
   return ((0x2c >> side) & 1) ? 1.0 : -1.0;  // + for faces 2, 3, 5
 }
 
-__device__ __forceinline__ void given_value(const BcDev &bc, const double *x,
-                                            double t, double *g) {
-  const double *src = bc.a;
-  if (bc.program == 1 && (x[bc.axis] - bc.speed * t) >= bc.position) src = bc.b;
-#pragma unroll
-  for (int k = 0; k < kK; ++k) g[k] = src[k];
-}
 
 // FAST_SQRT (the mixed form): the Rusanov wave speed's square root from an
 // FP32 seed and one FP64 Newton step (sqrt_seeded, relative error ~1e-13).
@@ -154,14 +149,28 @@ __global__ void __launch_bounds__(512) face_flux_kernel(FaceArgs a) {
     double cs[kK];
 #pragma unroll
     for (int k = 0; k < kK; ++k) cs[k] = us[k];
-    if constexpr (R == kRusanov) {
+    if constexpr (R == kRusanov || R == kRoe || R == kHllc) {
       if (a.trace) {
+        // both sides' node traces: 1/rho, p and the sound speed (Roe: sqrt(rho))
         const double *th = a.trace + ((int64_t)cells.x * (Q * Q * Q) + map.x) * 3;
         const double *ts = a.trace + ((int64_t)cells.y * (Q * Q * Q) + map.y) * 3;
         const double trh[3] = {th[0], th[1], th[2]}, trs[3] = {ts[0], ts[1], ts[2]};
-        flux_rusanov_traced_weighted(ch, trh, cs, trs, n, g.w, out);
-        store_flux(a.flux, a.f32_out, gid, out);
-        return;
+        bool done = true;
+        if constexpr (R == kRusanov) {
+          flux_rusanov_traced_weighted(ch, trh, cs, trs, n, g.w, out);
+        } else if constexpr (R == kRoe) {
+          done = flux_roe_traced_weighted<FAST_SQRT>(ch, trh, cs, trs, n, g.w, out);
+        } else {
+          done = flux_hllc_traced<FAST_SQRT>(ch, trh, cs, trs, n, out);
+          if (done) {
+#pragma unroll
+            for (int k = 0; k < kK; ++k) out[k] *= g.w;
+          }
+        }
+        if (done) {
+          store_flux(a.flux, a.f32_out, gid, out);
+          return;
+        }
       }
     }
     // already multiplied by the face weight
@@ -177,7 +186,8 @@ __global__ void __launch_bounds__(512) face_flux_kernel(FaceArgs a) {
       const BcDev &bc = a.bcs[grp];
       double t = stage_time(a.cs, a.state, cells.x, a.stage_c);
       double given[kK];
-      given_value(bc, a.face_xyz + gid * 3, t, given);
+      const double *xp = a.face_xyz + gid * 3;
+      boundary_given(bc, xp[0], xp[1], xp[2], t, a.bc_row ? a.bc_row[gid] : -1, given);
       // a no-slip wall's convective part is the inviscid wall flux
       flux_boundary<R>(bc.kind == kBcNoSlipWall ? (int)kBcInviscidWall : bc.kind, l, given, n, out,
                        &not_converged);
@@ -370,7 +380,7 @@ cell_update_kernel(CellArgs a) {
     const bool surface = i == 0 || i == Q - 1 || j == 0 || j == Q - 1 || k == 0 || k == Q - 1;
     if (a.trace && surface) {
       double tr[3];
-      node_trace<false>(nv, tr);
+      node_trace<false>(nv, tr, a.trace_roe != 0);
       double *dst = a.trace + (c * N + q) * 3;
       dst[0] = tr[0]; dst[1] = tr[1]; dst[2] = tr[2];
     }
@@ -524,7 +534,7 @@ cell_update_mixed_kernel(CellArgs a, const float *__restrict__ geo32) {
     const bool surface = i == 0 || i == Q - 1 || j == 0 || j == Q - 1 || k == 0 || k == Q - 1;
     if (a.trace && surface) {
       double tr[3];
-      node_trace<true>(nv, tr);
+      node_trace<true>(nv, tr, a.trace_roe != 0);
       double *dst = a.trace + (c * N + q) * 3;
       dst[0] = tr[0]; dst[1] = tr[1]; dst[2] = tr[2];
     }
@@ -666,11 +676,11 @@ __global__ void set_cases_kernel(double *case_t, double *case_dt, int n, double 
 // Node traces of a state (Buffers::trace), one thread per node.
 template <bool FAST_SQRT>
 __global__ void __launch_bounds__(256)
-trace_kernel(const double *u, double *trace, int64_t n_nodes) {
+trace_kernel(const double *u, double *trace, int64_t n_nodes, int roe) {
   const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= n_nodes) return;
   double tr[3];
-  node_trace<FAST_SQRT>(u + gid * kK, tr);
+  node_trace<FAST_SQRT>(u + gid * kK, tr, roe != 0);
   trace[gid * 3 + 0] = tr[0];
   trace[gid * 3 + 1] = tr[1];
   trace[gid * 3 + 2] = tr[2];
@@ -780,7 +790,7 @@ int launch_face_flux(mcfd_handle *h, const double *u, double stage_c, bool props
               m.face_map, m.bcs, h->buf.flux, h->buf.state, stage_c,
               m.n_points, m.n_groups, h->opt.scheme == 1, case_view(h),
               (h->use_trace && h->trace_for == u) ? h->buf.trace : nullptr,
-              h->opt.precision == 1, h->visc.on ? 1 : 0};
+              h->opt.precision == 1, h->visc.on ? 1 : 0, m.bc_row};
   if (m.n_points == 0) return n;
   switch (m.q) {
     case 2: face_dispatch_r<2>(h, fa); break;
@@ -800,7 +810,7 @@ int launch_cell_update(mcfd_handle *h, int stage, const double *u_in,
   double *trace = (h->use_trace && stage != kStageResidual) ? h->buf.trace : nullptr;
   CellArgs ca{u_in, u0, u_out, m.cell_geo, m.cell_flux, h->buf.flux, m.dmat,
               h->buf.state, m.n_cells, advance_time, h->opt.scheme == 1, h->opt.fr_g1,
-              case_view(h), trace, h->visc.on ? h->visc.nu : nullptr};
+              case_view(h), trace, h->visc.on ? h->visc.nu : nullptr, h->opt.riemann == kRoe};
   if (trace) h->trace_for = u_out;
   switch (m.q) {
     case 2: cell_dispatch_s<2>(h, stage, ca); break;
@@ -851,10 +861,11 @@ int launch_trace(mcfd_handle *h, const double *u) {
   if (!h->use_trace) return 0;
   const int64_t nodes = h->mesh.n_cells * h->mesh.n;
   const unsigned blocks = (unsigned)((nodes + 255) / 256);
+  const int roe = h->opt.riemann == kRoe;
   if (h->opt.precision == 1)
-    trace_kernel<true><<<blocks, 256, 0, h->stream>>>(u, h->buf.trace, nodes);
+    trace_kernel<true><<<blocks, 256, 0, h->stream>>>(u, h->buf.trace, nodes, roe);
   else
-    trace_kernel<false><<<blocks, 256, 0, h->stream>>>(u, h->buf.trace, nodes);
+    trace_kernel<false><<<blocks, 256, 0, h->stream>>>(u, h->buf.trace, nodes, roe);
   h->trace_for = u;
   return 1;
 }
@@ -918,10 +929,10 @@ int launch_residual_static_scratch(mcfd_handle *h, const double *d_u,
   FaceArgs fa{d_u, m.face_cells, m.face_group, m.face_geo, m.face_xyz,
               m.face_map, m.bcs, scratch, h->buf.state, 0.0,
               m.n_points, m.n_groups, h->opt.scheme == 1, case_view(h), nullptr,
-              h->opt.precision == 1, 0};
+              h->opt.precision == 1, 0, m.bc_row};
   CellArgs ca{d_u, nullptr, d_r, m.cell_geo, m.cell_flux, scratch, m.dmat,
               h->buf.state, m.n_cells, 0, h->opt.scheme == 1, h->opt.fr_g1, case_view(h), nullptr,
-              nullptr};
+              nullptr, 0};
   int n = 0;
   if (m.n_points > 0) {
     switch (m.q) {

@@ -265,11 +265,13 @@ MCFD_HD bool rusanov_side(const double *c, const double *n, double *f,
   return true;
 }
 
-// The per-node part of rusanov_side, stored once per stage state ("trace"):
-// tr = {1/rho, p, sound speed}; p = -1 marks a state that takes the
-// primitive fallback (non-positive density, negative energy or pressure).
+// The per-node part of the conservative-input face fluxes, stored once per
+// stage state ("trace"): tr = {1/rho, p, third}, third = the sound speed
+// (Rusanov, HLLC) or sqrt(rho) (Roe, roe_sqrt_rho); p = -1 marks a state that
+// takes the primitive fallback (non-positive density, negative energy or
+// pressure).
 template <bool FAST_SQRT = false>
-MCFD_HD void node_trace(const double *c, double *tr) {
+MCFD_HD void node_trace(const double *c, double *tr, bool roe_sqrt_rho = false) {
   double r = c[0], e = c[4];
   if (!bits_positive(r) || bits_negative(e)) {
     tr[0] = 0; tr[1] = -1; tr[2] = 0;
@@ -283,8 +285,13 @@ MCFD_HD void node_trace(const double *c, double *tr) {
     tr[1] = -1; tr[2] = 0;
     return;
   }
-  const double c2 = kGamma * p * rinv;
   tr[1] = p;
+  if (roe_sqrt_rho) {
+    if constexpr (FAST_SQRT) tr[2] = sqrt_seeded(r);
+    else tr[2] = sqrt(r);
+    return;
+  }
+  const double c2 = kGamma * p * rinv;
   if constexpr (FAST_SQRT) {
     tr[2] = bits_positive(p) ? sqrt_seeded(c2) : 0.0;
   } else {
@@ -578,19 +585,15 @@ MCFD_HD void hllc_side_cons(const double *c, double rinv, double u, double v, do
   f[4] += wk * (es - e);
 }
 
+// HLLC from both sides' 1/rho, pressure and sound speed (p > 0 on both).
 template <bool FAST_SQRT>
-MCFD_HD bool flux_hllc_cons(const double *cl, const double *cr, const double *n, double *f) {
+MCFD_HD void hllc_core(const double *cl, const double *cr, double il, double ir, double pl,
+                       double pr, double al, double ar, const double *n, double *f) {
   const double rl = cl[0], rr = cr[0];
-  if (!bits_positive(rl) || !bits_positive(rr) || bits_negative(cl[4]) || bits_negative(cr[4])) return false;
-  const double il = rcp_newton(rl), ir = rcp_newton(rr);
   const double ul = cl[1] * il, vl = cl[2] * il, wl = cl[3] * il;
   const double ur = cr[1] * ir, vr = cr[2] * ir, wr = cr[3] * ir;
-  const double pl = (cl[4] - rl * (0.5 * (ul * ul + vl * vl + wl * wl))) * kGm1;
-  const double pr = (cr[4] - rr * (0.5 * (ur * ur + vr * vr + wr * wr))) * kGm1;
-  if (!bits_positive(pl) || !bits_positive(pr)) return false;
   const double unl = ul * n[0] + vl * n[1] + wl * n[2];
   const double unr = ur * n[0] + vr * n[1] + wr * n[2];
-  const double al = sqrt_form<FAST_SQRT>(kGamma * pl * il), ar = sqrt_form<FAST_SQRT>(kGamma * pr * ir);
   const double rho_average = (rl + rr) / 2, a_average = (al + ar) / 2;
   const double p_pvrs = (pl + pr - (unr - unl) * rho_average * a_average) / 2;
   const double p_estimate = fmax(0.0, p_pvrs);
@@ -609,6 +612,30 @@ MCFD_HD bool flux_hllc_cons(const double *cl, const double *cr, const double *n,
   } else {
     for (int k = 0; k < kK; ++k) f[k] = NAN;
   }
+}
+
+template <bool FAST_SQRT>
+MCFD_HD bool flux_hllc_cons(const double *cl, const double *cr, const double *n, double *f) {
+  const double rl = cl[0], rr = cr[0];
+  if (!bits_positive(rl) || !bits_positive(rr) || bits_negative(cl[4]) || bits_negative(cr[4])) return false;
+  const double il = rcp_newton(rl), ir = rcp_newton(rr);
+  const double ul = cl[1] * il, vl = cl[2] * il, wl = cl[3] * il;
+  const double ur = cr[1] * ir, vr = cr[2] * ir, wr = cr[3] * ir;
+  const double pl = (cl[4] - rl * (0.5 * (ul * ul + vl * vl + wl * wl))) * kGm1;
+  const double pr = (cr[4] - rr * (0.5 * (ur * ur + vr * vr + wr * wr))) * kGm1;
+  if (!bits_positive(pl) || !bits_positive(pr)) return false;
+  const double al = sqrt_form<FAST_SQRT>(kGamma * pl * il), ar = sqrt_form<FAST_SQRT>(kGamma * pr * ir);
+  hllc_core<FAST_SQRT>(cl, cr, il, ir, pl, pr, al, ar, n, f);
+  return true;
+}
+
+// flux_hllc_cons with both sides' node traces {1/rho, p, sound speed}: false
+// (primitive fallback) unless p > 0 on both sides.
+template <bool FAST_SQRT>
+MCFD_HD bool flux_hllc_traced(const double *cl, const double *trl, const double *cr,
+                              const double *trr, const double *n, double *f) {
+  if (!bits_positive(trl[1]) || !bits_positive(trr[1])) return false;
+  hllc_core<FAST_SQRT>(cl, cr, trl[0], trr[0], trl[1], trr[1], trl[2], trr[2], n, f);
   return true;
 }
 
@@ -622,17 +649,14 @@ MCFD_HD bool flux_hllc_cons(const double *cl, const double *cr, const double *n,
 // acoustic pair combined as (a1 + a5) (u, h0) + (a5 - a1) a (n, u_n), and the
 // halves of the average and of the wave strengths folded into one w / 2.
 // FAST_SQRT (the mixed form) takes both square roots from sqrt_seeded.
+// Roe from both sides' 1/rho and pressure and lambda = sqrt(rho_R / rho_L).
 template <bool FAST_SQRT>
-MCFD_HD bool flux_roe_cons_weighted(const double *cl, const double *cr, const double *n,
-                                    double w, double *f) {
+MCFD_HD void roe_core_weighted(const double *cl, const double *cr, double il, double ir,
+                               double pl, double pr, double lam, const double *n, double w,
+                               double *f) {
   const double rl = cl[0], rr = cr[0], el = cl[4], er = cr[4];
-  if (!bits_positive(rl) || !bits_positive(rr) || bits_negative(el) || bits_negative(er)) return false;
-  const double il = rcp_newton(rl), ir = rcp_newton(rr);
   const double ul = cl[1] * il, vl = cl[2] * il, wl = cl[3] * il;
   const double ur = cr[1] * ir, vr = cr[2] * ir, wr = cr[3] * ir;
-  const double pl = (el - 0.5 * (cl[1] * ul + cl[2] * vl + cl[3] * wl)) * kGm1;
-  const double pr = (er - 0.5 * (cr[1] * ur + cr[2] * vr + cr[3] * wr)) * kGm1;
-  if (bits_negative(pl) || bits_negative(pr)) return false;
   const double unl = ul * n[0] + vl * n[1] + wl * n[2];
   const double unr = ur * n[0] + vr * n[1] + wr * n[2];
   // F(U_L) + F(U_R)
@@ -642,9 +666,6 @@ MCFD_HD bool flux_roe_cons_weighted(const double *cl, const double *cr, const do
   const double s3 = (cl[3] * unl + pl * n[2]) + (cr[3] * unr + pr * n[2]);
   const double s4 = (el + pl) * unl + (er + pr) * unr;
   // Roe averages
-  double lam;
-  if constexpr (FAST_SQRT) lam = sqrt_seeded(rr * il);
-  else lam = sqrt(rr * il);
   const double inv = rcp_newton(1 + lam);
   const double rho = lam * rl;
   const double u = (ul + lam * ur) * inv, v = (vl + lam * vr) * inv, ww = (wl + lam * wr) * inv;
@@ -672,6 +693,35 @@ MCFD_HD bool flux_roe_cons_weighted(const double *cl, const double *cr, const do
   f[2] = hw * (s2 - (Sa * v + D * n[1] + t1));
   f[3] = hw * (s3 - (Sa * ww + D * n[2] + t2));
   f[4] = hw * (s4 - (S * h0 + D * un + a2 * ke + (t0 * u + t1 * v + t2 * ww)));
+}
+
+template <bool FAST_SQRT>
+MCFD_HD bool flux_roe_cons_weighted(const double *cl, const double *cr, const double *n,
+                                    double w, double *f) {
+  const double rl = cl[0], rr = cr[0], el = cl[4], er = cr[4];
+  if (!bits_positive(rl) || !bits_positive(rr) || bits_negative(el) || bits_negative(er)) return false;
+  const double il = rcp_newton(rl), ir = rcp_newton(rr);
+  const double ul = cl[1] * il, vl = cl[2] * il, wl = cl[3] * il;
+  const double ur = cr[1] * ir, vr = cr[2] * ir, wr = cr[3] * ir;
+  const double pl = (el - 0.5 * (cl[1] * ul + cl[2] * vl + cl[3] * wl)) * kGm1;
+  const double pr = (er - 0.5 * (cr[1] * ur + cr[2] * vr + cr[3] * wr)) * kGm1;
+  if (bits_negative(pl) || bits_negative(pr)) return false;
+  double lam;
+  if constexpr (FAST_SQRT) lam = sqrt_seeded(rr * il);
+  else lam = sqrt(rr * il);
+  roe_core_weighted<FAST_SQRT>(cl, cr, il, ir, pl, pr, lam, n, w, f);
+  return true;
+}
+
+// flux_roe_cons_weighted with both sides' node traces {1/rho, p, sqrt(rho)}:
+// lambda = sqrt(rho_R) sqrt(rho_L) / rho_L without a square root; false
+// (primitive fallback) when a side is marked (p = -1).
+template <bool FAST_SQRT>
+MCFD_HD bool flux_roe_traced_weighted(const double *cl, const double *trl, const double *cr,
+                                      const double *trr, const double *n, double w, double *f) {
+  if (bits_negative(trl[1]) || bits_negative(trr[1])) return false;
+  const double lam = (trr[2] * trl[2]) * trl[0];
+  roe_core_weighted<FAST_SQRT>(cl, cr, trl[0], trr[0], trl[1], trr[1], lam, n, w, f);
   return true;
 }
 

@@ -45,7 +45,28 @@ struct BcDev {
   int kind, program, axis, pad;
   double position, speed;
   double a[5], b[5];
+  double normal[3];      // OBLIQUE_SPLIT
+  const double *table;   // TABLE: [group points][5] (device), or null
 };
+
+#ifdef __CUDACC__
+// The given value of boundary group bc at face point (x, y, z) and time t;
+// row = the point's index within its group (TABLE programs), or -1.
+__device__ __forceinline__ void boundary_given(const BcDev &bc, double x, double y, double z,
+                                               double t, int32_t row, double *g) {
+  const double *src = bc.a;
+  if (bc.program == 1) {
+    const double pos[3] = {x, y, z};
+    if ((pos[bc.axis] - bc.speed * t) >= bc.position) src = bc.b;
+  } else if (bc.program == 2) {
+    if ((bc.normal[0] * x + bc.normal[1] * y + bc.normal[2] * z - bc.speed * t) >= bc.position) src = bc.b;
+  } else if (bc.program == 3 && bc.table && row >= 0) {
+    src = bc.table + (int64_t)row * 5;
+  }
+#pragma unroll
+  for (int k = 0; k < 5; ++k) g[k] = src[k];
+}
+#endif
 
 // Stage combinations of RungeKutta<1|2|3> (temporal/rk.hpp:16-49):
 //   kStageEuler:    u + R dt                          (Euler::NextSolution)
@@ -88,6 +109,11 @@ struct Mesh {
   // host copies for parity queries
   std::vector<int16_t> map_h, map_s;
   std::vector<BcDev> host_bcs;
+  // TABLE boundary programs: per face point its row in its group's table
+  // (-1 elsewhere), allocated with the first table; per group the table
+  int32_t *bc_row = nullptr;          // [points] (device)
+  std::vector<int32_t> host_bc_row;   // [points]
+  std::vector<double *> bc_tables;    // [n_groups] device tables (owned)
   double *node_w = nullptr;         // [cells][N] global weights (initial limiters; built on first use)
   std::vector<double> host_corners;  // [cells][8][3] (as uploaded to corners)
   std::vector<double> host_shift;    // [faces][3] periodic shifts (empty: none)

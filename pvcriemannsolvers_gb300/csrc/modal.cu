@@ -93,15 +93,6 @@ __device__ __forceinline__ void add_gradient(const Real *t, Real gx, Real gy, Re
   }
 }
 
-__device__ __forceinline__ void modal_given(const BcDev &bc, double x, double y,
-                                            double z, double t, double *g) {
-  const double pos[3] = {x, y, z};
-  const double *src = bc.a;
-  if (bc.program == 1 && (pos[bc.axis] - bc.speed * t) >= bc.position) src = bc.b;
-#pragma unroll
-  for (int k = 0; k < kK; ++k) g[k] = src[k];
-}
-
 // a[c][j][k] = sum_{m >= j} S[m][j] u[c][m][k]
 template <int M>
 __global__ void __launch_bounds__(256)
@@ -132,6 +123,7 @@ struct ModalFaceArgs {
   int64_t n_points;
   int n_groups;
   CaseView cs;
+  const int32_t *bc_row;  // [points] row in the group's boundary table, or null
 };
 
 template <int M, class Real>
@@ -178,7 +170,7 @@ __global__ void __launch_bounds__(512) modal_face_kernel(ModalFaceArgs a) {
         const int k = a.cs.cell_case[cells.x];
         t = a.cs.t[k] + a.stage_c * a.cs.dt[k];
       }
-      modal_given(bc, x.x, x.y, x.z, t, given);
+      boundary_given(bc, x.x, x.y, x.z, t, a.bc_row ? a.bc_row[gid] : -1, given);
       flux_boundary<R>(bc.kind, l, given, n, out, &not_converged);
     } else {
 #pragma unroll
@@ -484,6 +476,7 @@ struct ModalFace32Args {
   int64_t n_points;
   int n_groups;
   CaseView cs;
+  const int32_t *bc_row;  // [points] row in the group's boundary table, or null
 };
 
 template <int M, int R>
@@ -523,7 +516,7 @@ __global__ void __launch_bounds__(512) modal_face32_kernel(ModalFace32Args a) {
         const int k = a.cs.cell_case[cells.x];
         tt = a.cs.t[k] + a.stage_c * a.cs.dt[k];
       }
-      modal_given(bc, x.x, x.y, x.z, tt, given);
+      boundary_given(bc, x.x, x.y, x.z, tt, a.bc_row ? a.bc_row[gid] : -1, given);
       flux_boundary<R>(bc.kind, l, given, n, out, &not_converged);
     } else {
 #pragma unroll
@@ -897,7 +890,7 @@ int launch_modal_face_flux(mcfd_handle *h, const double *u, double stage_c) {
     if (md.n_fpts == 0) return n;
     ModalFace32Args fa{md.taylor32, m.face_cells, m.face_group, md.point_face, md.fpt, md.fnrm,
                        md.foff32, m.bcs, reinterpret_cast<float *>(h->buf.flux), h->buf.state,
-                       stage_c, md.n_fpts, m.n_groups, case_view(h)};
+                       stage_c, md.n_fpts, m.n_groups, case_view(h), m.bc_row};
     switch (md.m) {
       case 4: modal_face32_dispatch<4>(h, fa); break;
       case 10: modal_face32_dispatch<10>(h, fa); break;
@@ -913,7 +906,7 @@ int launch_modal_face_flux(mcfd_handle *h, const double *u, double stage_c) {
   if (md.n_fpts == 0) return n;
   ModalFaceArgs fa{md.taylor, md.center, m.face_cells, m.face_group, md.point_face,
                    md.fpt, md.fnrm, md.fshift, m.bcs, h->buf.flux, h->buf.state,
-                   stage_c, md.n_fpts, m.n_groups, case_view(h)};
+                   stage_c, md.n_fpts, m.n_groups, case_view(h), m.bc_row};
   switch (md.m) {
     case 4: modal_face_dispatch<4>(h, fa); break;
     case 10: modal_face_dispatch<10>(h, fa); break;

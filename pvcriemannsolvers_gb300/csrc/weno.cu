@@ -59,6 +59,9 @@ struct WenoArgs {
   unsigned long long *troubled;
   int64_t n_cells;
   double w0, eps, smooth_ref;
+  double *trace;   // node traces of u to rewrite for the reconstructed cells, or null
+  int trace_fast;  // the mixed form's seeded roots in the traces
+  int trace_roe;   // third trace entry sqrt(rho) (Roe), else the sound speed
 };
 
 // one thread per (cell, mode): all five components, so each modal_to_nodal
@@ -339,41 +342,66 @@ __device__ void eigen_reconstruct(const Args &a, int64_t c, int n_adj,
   __syncthreads();
 }
 
-// weno::Eigen::IsNotSmooth (weno.hpp:230-258) on density and energy, one
-// thread per cell; flagged cells are appended to the troubled list (their
-// order does not matter: each reconstruction writes only its own cell).
+// weno::Eigen::IsNotSmooth (weno.hpp:230-258) on density and energy, eight
+// lanes per cell (four cells per warp): the lanes split the M modes of every
+// value at the cell centre (own polynomial and each neighbour's, coalesced
+// reads of the [K][M] modal blocks and the [7][M] centre values) and combine
+// their partial sums with warp shuffles; flagged cells are appended to the
+// troubled list (their order does not matter: each reconstruction writes
+// only its own cell).
+constexpr int kDetectLanes = 8;
+
+__device__ __forceinline__ double group_sum(double v) {
+#pragma unroll
+  for (int o = kDetectLanes / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, kDetectLanes);
+  return v;
+}
+
 template <int M>
 __global__ void __launch_bounds__(256)
 weno_detect_kernel(WenoArgs a, int32_t *list, unsigned *count) {
-  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= a.n_cells) return;
-  const double s00 = a.s00[c];
-  const double *ev = a.eval + c * 7 * M;
-  const double *own = a.modal + c * kK * M;
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t c = gid / kDetectLanes;
+  const int lane = (int)(gid % kDetectLanes);
+  const bool live = c < a.n_cells;
+  const int64_t cc = live ? c : a.n_cells - 1;  // idle lanes shadow the last cell
+  const double s00 = a.s00[cc];
+  const double *ev = a.eval + cc * 7 * M;
+  const double *own = a.modal + cc * kK * M;
   int adj[6], n = 0;
+#pragma unroll
   for (int s = 0; s < 6; ++s) {
-    adj[s] = a.adj[c * 6 + s];
+    adj[s] = a.adj[cc * 6 + s];
     n += adj[s] >= 0;
   }
   bool troubled = false;
   const int comps[2] = {0, kK - 1};
+#pragma unroll
   for (int ci = 0; ci < 2; ++ci) {
     const int k = comps[ci];
+    double part = 0;
+    for (int m = lane; m < M; m += kDetectLanes) part += own[k * M + m] * ev[6 * M + m];
+    const double mine = group_sum(part);
     double max_abs = fmax(1e-9, fabs(own[k * M] * s00));
-    double mine = 0;
-    for (int m = 0; m < M; ++m) mine += own[k * M + m] * ev[6 * M + m];
     double sum_abs = 0;
-    for (int s = 0; s < n; ++s) {
+    // every lane runs all six slots so that the shuffles stay warp-uniform
+#pragma unroll
+    for (int s = 0; s < 6; ++s) {
       const int b = adj[s];
-      const double *cb = a.modal + ((int64_t)b * kK + k) * M;
+      const bool used = s < n;
+      const double *cb = a.modal + ((int64_t)(used ? b : 0) * kK + k) * M;
       double v = 0;
-      for (int m = 0; m < M; ++m) v += cb[m] * ev[s * M + m];
-      sum_abs += fabs(mine - v);
-      max_abs = fmax(max_abs, fabs(cb[0] * a.s00[b]));
+      if (used)
+        for (int m = lane; m < M; m += kDetectLanes) v += cb[m] * ev[s * M + m];
+      v = group_sum(v);
+      if (used) {
+        sum_abs += fabs(mine - v);
+        max_abs = fmax(max_abs, fabs(cb[0] * a.s00[b]));
+      }
     }
-    if (sum_abs / max_abs / a.divisor[c] > a.smooth_ref) troubled = true;
+    if (sum_abs / max_abs / a.divisor[cc] > a.smooth_ref) troubled = true;
   }
-  if (troubled) list[atomicAdd(count, 1u)] = (int32_t)c;
+  if (live && lane == 0 && troubled) list[atomicAdd(count, 1u)] = (int32_t)c;
 }
 
 // Reconstruction of the listed cells (every cell when list is null) by a
@@ -480,6 +508,28 @@ weno_reconstruct_kernel(WenoArgs a, const int32_t *list, const unsigned *count) 
       const int m = i / kK, k = i - m * kK;
       uc[i] = s_new[k][m];
     }
+  } else if (a.trace) {
+    // UpdateNodalCoeff, one node per thread, and the node's new trace
+    const double *pc = a.psi + c * N * M;
+    double *uc = a.u + c * kK * N;
+    for (int q = t; q < N; q += blockDim.x) {
+      double v[kK];
+#pragma unroll
+      for (int k = 0; k < kK; ++k) {
+        double s = 0;
+#pragma unroll
+        for (int m = 0; m < M; ++m) s += s_new[k][m] * pc[q * M + m];
+        v[k] = s;
+        uc[q * kK + k] = s;
+      }
+      double tr[3];
+      if (a.trace_fast)
+        node_trace<true>(v, tr, a.trace_roe != 0);
+      else
+        node_trace<false>(v, tr, a.trace_roe != 0);
+      double *dst = a.trace + (c * N + q) * 3;
+      dst[0] = tr[0]; dst[1] = tr[1]; dst[2] = tr[2];
+    }
   } else {
     // UpdateNodalCoeff: nodal values = modal expansion at the nodes
     const double *pc = a.psi + c * N * M;
@@ -511,8 +561,12 @@ int limiter_dispatch(mcfd_handle *h, double *u) {
     weno_modal_kernel<N, M><<<(unsigned)((total + 255) / 256), 256, 0, h->stream>>>(
         u, l.mn, l.modal, mesh.n_cells);
   }
+  // a stage state whose node traces the face kernels will read gets the
+  // reconstructed cells' traces rewritten
+  double *trace = (h->use_trace && h->trace_for == u) ? h->buf.trace : nullptr;
   WenoArgs wa{u, l.modal, l.psi, l.proj, l.beta, l.eval, l.s00, l.divisor, l.adj,
-              l.frame, l.volume, l.troubled, mesh.n_cells, l.w0, l.eps, (Q - 1) < 3 ? 1.0 : 3.0};
+              l.frame, l.volume, l.troubled, mesh.n_cells, l.w0, l.eps, (Q - 1) < 3 ? 1.0 : 3.0,
+              trace, h->opt.precision == 1, h->opt.riemann == kRoe};
   // persistent grid: limiter_blocks_per_sm blocks of 64 threads per SM
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
@@ -523,7 +577,7 @@ int limiter_dispatch(mcfd_handle *h, double *u) {
     return 2;
   }
   cudaMemsetAsync(l.list_count, 0, sizeof(unsigned), h->stream);
-  weno_detect_kernel<M><<<(unsigned)((mesh.n_cells + 255) / 256), 256, 0, h->stream>>>(
+  weno_detect_kernel<M><<<(unsigned)((mesh.n_cells * kDetectLanes + 255) / 256), 256, 0, h->stream>>>(
       wa, l.list, l.list_count);
   if (l.kind == 2 /* MCFD_LIMITER_DETECT_LAZY */)
     weno_reconstruct_kernel<N, M, 2><<<grid, 64, 0, h->stream>>>(wa, l.list, l.list_count);
@@ -540,7 +594,8 @@ int limiter_dispatch_modal(mcfd_handle *h, double *u) {
   const int64_t total = mesh.n_cells * M;
   weno_transpose_kernel<M><<<(unsigned)((total + 255) / 256), 256, 0, h->stream>>>(u, l.modal, mesh.n_cells);
   WenoArgs wa{u, l.modal, nullptr, l.proj, l.beta, l.eval, l.s00, l.divisor, l.adj,
-              l.frame, l.volume, l.troubled, mesh.n_cells, l.w0, l.eps, mesh.p < 3 ? 1.0 : 3.0};
+              l.frame, l.volume, l.troubled, mesh.n_cells, l.w0, l.eps, mesh.p < 3 ? 1.0 : 3.0,
+              nullptr, 0, 0};
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
   const unsigned grid =
@@ -550,7 +605,7 @@ int limiter_dispatch_modal(mcfd_handle *h, double *u) {
     return 2;
   }
   cudaMemsetAsync(l.list_count, 0, sizeof(unsigned), h->stream);
-  weno_detect_kernel<M><<<(unsigned)((mesh.n_cells + 255) / 256), 256, 0, h->stream>>>(
+  weno_detect_kernel<M><<<(unsigned)((mesh.n_cells * kDetectLanes + 255) / 256), 256, 0, h->stream>>>(
       wa, l.list, l.list_count);
   if (l.kind == 2 /* MCFD_LIMITER_DETECT_LAZY */)
     weno_reconstruct_kernel<0, M, 2, true><<<grid, 64, 0, h->stream>>>(wa, l.list, l.list_count);

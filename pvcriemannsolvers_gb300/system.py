@@ -39,11 +39,33 @@ class MovingSplit:
     b: np.ndarray
 
 
+@dataclass
+class ObliqueSplit:
+    """value(x, t) = (normal . x - speed t) < position ? a : b, e.g. the
+    oblique moving shock of demo/euler/double_mach.cpp:28-31."""
+    normal: np.ndarray
+    position: float
+    speed: float
+    a: np.ndarray
+    b: np.ndarray
+
+
 def _bc_state(kind: int, value) -> capi.BcState:
     s = capi.BcState()
     s.kind = kind
     if value is None:
         s.program = capi.STATE_CONSTANT
+    elif callable(value):
+        s.program = capi.STATE_TABLE  # values set by _set_bc afterwards
+    elif isinstance(value, ObliqueSplit):
+        s.program = capi.STATE_OBLIQUE_SPLIT
+        s.position = float(value.position)
+        s.speed = float(value.speed)
+        for k in range(3):
+            s.normal[k] = float(value.normal[k])
+        for k in range(5):
+            s.a[k] = float(value.a[k])
+            s.b[k] = float(value.b[k])
     elif isinstance(value, MovingSplit):
         s.program = capi.STATE_MOVING_SPLIT
         s.axis = int(value.axis)
@@ -152,24 +174,44 @@ class Lobatto:
     def _check(self, code: int) -> None:
         capi.check(code, self._h)
 
-    # -- boundary registration (fem.hpp:196-222)
+    # -- boundary registration (fem.hpp:196-222).  value: a 5-component
+    # state, a MovingSplit or ObliqueSplit (moving shocks, evaluated on the
+    # device at every stage time), or a callable of the points [n, 3] ->
+    # states [n, 5], sampled once at the group's face points (bc_points).
+    def _set_bc(self, kind: int, group: int, value) -> None:
+        self._check(self._lib.mcfd_set_bc(self._h, group, C.byref(_bc_state(kind, value))))
+        if callable(value):
+            pts = self.bc_points(group)
+            vals = np.ascontiguousarray(value(pts), dtype=np.float64)
+            if vals.shape != (pts.shape[0], 5):
+                raise ValueError("a boundary function maps points [n, 3] to states [n, 5]")
+            self._check(self._lib.mcfd_set_bc_table(self._h, group, capi.dptr(vals), pts.shape[0]))
+
+    def bc_points(self, group: int) -> np.ndarray:
+        """Face points [n, 3] of a boundary group (mcfd_bc_points)."""
+        n = C.c_int64()
+        self._check(self._lib.mcfd_bc_point_count(self._h, group, C.byref(n)))
+        out = np.empty((n.value, 3))
+        self._check(self._lib.mcfd_bc_points(self._h, group, capi.dptr(out), n.value))
+        return out
+
     def SetInviscidWall(self, group: int) -> None:
-        self._check(self._lib.mcfd_set_bc(self._h, group, C.byref(_bc_state(capi.BC_INVISCID_WALL, None))))
+        self._set_bc(capi.BC_INVISCID_WALL, group, None)
 
     def SetSupersonicOutlet(self, group: int) -> None:
-        self._check(self._lib.mcfd_set_bc(self._h, group, C.byref(_bc_state(capi.BC_SUPERSONIC_OUTLET, None))))
+        self._set_bc(capi.BC_SUPERSONIC_OUTLET, group, None)
 
     def SetSupersonicInlet(self, group: int, value) -> None:
-        self._check(self._lib.mcfd_set_bc(self._h, group, C.byref(_bc_state(capi.BC_SUPERSONIC_INLET, value))))
+        self._set_bc(capi.BC_SUPERSONIC_INLET, group, value)
 
     def SetSubsonicInlet(self, group: int, value) -> None:
-        self._check(self._lib.mcfd_set_bc(self._h, group, C.byref(_bc_state(capi.BC_SUBSONIC_INLET, value))))
+        self._set_bc(capi.BC_SUBSONIC_INLET, group, value)
 
     def SetSubsonicOutlet(self, group: int, value) -> None:
-        self._check(self._lib.mcfd_set_bc(self._h, group, C.byref(_bc_state(capi.BC_SUBSONIC_OUTLET, value))))
+        self._set_bc(capi.BC_SUBSONIC_OUTLET, group, value)
 
     def SetSmartBoundary(self, group: int, value) -> None:
-        self._check(self._lib.mcfd_set_bc(self._h, group, C.byref(_bc_state(capi.BC_SMART, value))))
+        self._set_bc(capi.BC_SMART, group, value)
 
     def SetNoSlipWall(self, group: int) -> None:
         """fr::Lobatto only; with the artificial viscosity the wall flux minus

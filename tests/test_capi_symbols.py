@@ -37,7 +37,7 @@ def test_library_exports_every_declared_symbol(mcfd_lib):
 
 def test_abi_version_and_create_errors_without_gpu(mcfd_lib):
     """Calls that touch no device memory: version, argument validation."""
-    assert mcfd_lib.mcfd_abi_version() == 1
+    assert mcfd_lib.mcfd_abi_version() == 2
     h = ctypes.c_void_p()
     assert mcfd_lib.mcfd_create(None, None, ctypes.byref(h)) == 1  # MCFD_ERR_ARGUMENT
     assert b"null" in mcfd_lib.mcfd_last_error(None)
