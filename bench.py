@@ -137,14 +137,15 @@ def fp64_peak_tflops(torch, device) -> float:
     return best
 
 
-def cpu_sample(steps_min=1, seconds=12.0, max_steps=200, threads=None, fixed_steps=None):
-    """The oracle on the 16^3 sample of the workload, all host cores."""
+def cpu_sample(steps_min=1, seconds=12.0, max_steps=200, threads=None, fixed_steps=None, n1d=SAMPLE_1D):
+    """The oracle on n1d^3 cells of the workload (the 16^3 sample by
+    default), all host cores."""
     import oracle.orc as orc
     from pvcriemannsolvers_gb300 import cases, mesh as meshlib
     orc.build()
     threads = threads or os.cpu_count() or 1
     orc.set_threads(threads)
-    m = meshlib.box((SAMPLE_1D,) * 3, lengths=(10.0,) * 3, periodic=(True,) * 3)
+    m = meshlib.box((n1d,) * 3, lengths=(10.0,) * 3, periodic=(True,) * 3)
     om = orc.Mesh(m, DEGREE)
     x = meshlib.node_coordinates(m, DEGREE).reshape(-1, 3)
     u = cases.vortex_ic(x).ravel()
@@ -163,7 +164,7 @@ def cpu_sample(steps_min=1, seconds=12.0, max_steps=200, threads=None, fixed_ste
             break
     el = time.perf_counter() - t0
     return {"value": 3 * L * n / el, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{SAMPLE_1D}^3 cells of the same case (L = {L} DOFs), {n} SSP-RK3 steps, "
+            "sample": f"{n1d}^3 cells of the same case (L = {L} DOFs), {n} SSP-RK3 steps, "
                       f"{el:.1f} s, oracle (plain C restatement, OpenMP)", "seconds": el, "steps": n}
 
 
@@ -205,15 +206,17 @@ def convergence(forms, device, dt_cfl, n_steps, finest):
 
 
 def run_reference(args, rank, world):
+    """The reference algorithm (the oracle, all host cores) on the GPU arm's
+    own configuration: the 64^3 mesh, every one of the W + K steps timed."""
     if rank != 0:
         return
-    res = cpu_sample(threads=os.cpu_count(), fixed_steps=args.warmup + args.steps)
+    res = cpu_sample(threads=os.cpu_count(), fixed_steps=args.warmup + args.steps, n1d=args.cells)
     line = {
         "impl": "reference", "metric": METRIC, "value": res["value"], "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": res["seconds"] / res["steps"] * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": workload(SAMPLE_1D),
+        "config": workload(args.cells),
         "cpu_baseline": {k: res[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "e2e": {"value": res["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -887,27 +890,51 @@ def quadrant_oracle_bcs():
             3: (orc.BC_INVISCID_WALL, None), 4: (orc.BC_INVISCID_WALL, None), 5: (orc.BC_INVISCID_WALL, None)}
 
 
-def quadrant_cpu_sample(seconds=12.0, threads=None):
+QUAD_FLOOR_STEPS = 200
+
+
+def quadrant_cpu_sample(threads=None, steps=QUAD_FLOOR_STEPS, device=0):
+    """The oracle on the 32 x 32 x 2 cells of the same case (all host cores)
+    for the case's 200 steps, timed; the same steps on the GPU in both forms
+    from the same initial state give the FP64 floor of the comparison: how far
+    the FP64 GPU run drifts from the FP64 oracle (the same algorithm in
+    another rounding order) on this limited shock problem, next to the mixed
+    form's deviation."""
     import oracle.orc as orc
-    from pvcriemannsolvers_gb300 import cases, mesh as meshlib
+    from pvcriemannsolvers_gb300 import Lobatto, cases, mesh as meshlib
     orc.build()
     threads = threads or os.cpu_count() or 1
     orc.set_threads(threads)
     m = cases.quadrant_mesh(*QUAD_SAMPLE)
+    u0 = cases.quadrant_ic(meshlib.node_coordinates(m, QUAD_DEGREE).reshape(-1, 3)).ravel()
     om = orc.Mesh(m, QUAD_DEGREE)
     om.set_bcs(quadrant_oracle_bcs())
     lim = orc.Limiter(om, orc.LIMITER_EIGEN)
-    u, _ = lim.limit(cases.quadrant_ic(meshlib.node_coordinates(m, QUAD_DEGREE).reshape(-1, 3)).ravel())
-    t, n, t0 = 0.0, 0, time.perf_counter()
-    while time.perf_counter() - t0 < seconds:
+    u, _ = lim.limit(u0)
+    t, t0 = 0.0, time.perf_counter()
+    for _ in range(steps):
         dt = om.time_step(u, 1.0, 3, 0.0)
         u = lim.rk_update(orc.ROE, 3, t, dt, u)
         t += dt
-        n += 1
     el = time.perf_counter() - t0
-    return {"value": 3 * u.size * n / el, "unit": UNIT, "cores": threads, "kind": "port",
+    gpu = {}
+    for form in ("fp64", "mixed"):
+        s = Lobatto(m, QUAD_DEGREE, "roe", device=device, precision=form, limiter="eigen")
+        cases.quadrant_bc(s)
+        s.SetSolutionColumn(u0)
+        s.advance(steps, 1.0, 3, 0.0)
+        gpu[form] = s.GetSolutionColumn().reshape(-1, K)[:, 0]
+        s.close()
+    rho = u.reshape(-1, K)[:, 0]
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    floor = {"steps": steps, "mesh": "x".join(map(str, QUAD_SAMPLE)),
+             "fp64_gpu_vs_fp64_oracle_density_rel_l2": rel(gpu["fp64"], rho),
+             "mixed_gpu_vs_fp64_gpu_density_rel_l2": rel(gpu["mixed"], gpu["fp64"]),
+             "mixed_gpu_vs_fp64_oracle_density_rel_l2": rel(gpu["mixed"], rho)}
+    return {"value": 3 * u.size * steps / el, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{QUAD_SAMPLE[0]}x{QUAD_SAMPLE[1]}x{QUAD_SAMPLE[2]} cells of the same case "
-                      f"(L = {u.size} DOFs), {n} SSP-RK3 steps with the limiter, {el:.1f} s, oracle (OpenMP)"}
+                      f"(L = {u.size} DOFs), {steps} SSP-RK3 steps with the limiter, {el:.1f} s, oracle (OpenMP)",
+            "floor": floor}
 
 
 def run_quadrant(args, rank, world, local_rank):
@@ -955,8 +982,10 @@ def run_quadrant(args, rank, world, local_rank):
     fp64_peak = fp64_peak_tflops(torch, dev)
     a, b = res["mixed"]["solution"].reshape(-1, K)[:, 0], res["fp64"]["solution"].reshape(-1, K)[:, 0]
     cpu = None
+    floor = None
     if not args.no_cpu:
-        cpu = quadrant_cpu_sample()
+        cpu = quadrant_cpu_sample(device=local_rank)
+        floor = cpu.pop("floor")
     # the plain FP64 form is the line's value: with the limiter switching on
     # shocks this case amplifies perturbations over the steps (mixed vs FP64
     # density 4.8e-7 after 53 steps, 4.4e-4 after 203), so the mixed form is
@@ -975,7 +1004,8 @@ def run_quadrant(args, rank, world, local_rank):
                    "l2_flush": "inputs larger than L2 (solution column 1.13 GB)"},
         "accuracy": {"t_end": r["t"], "mixed_vs_fp64_density_rel_l2": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
                      "troubled_fraction_mixed": res["mixed"]["troubled_fraction"],
-                     "troubled_fraction_fp64": res["fp64"]["troubled_fraction"]},
+                     "troubled_fraction_fp64": res["fp64"]["troubled_fraction"],
+                     "fp64_floor": floor},
         "clocks": r["clocks"],
         "e2e": {"value": r["e2e"], "unit": UNIT, "h2d_bytes_per_step": 8 * L, "d2h_bytes_per_step": 8 * L,
                 "steps": e2e_steps, "path": E2E_PATH,

@@ -69,11 +69,23 @@ def jump_state(x, rng):
     return cases.prim_to_cons(rho, np.full(n, 0.1), np.full(n, -0.05), np.full(n, 0.02), p)
 
 
-def load_pair(m, p, mode, precision="fp64", seed=1, riemann="hllc"):
+def mild_jump_state(x, rng):
+    """A jump of density ratio 2 and pressure ratio 2.5: the limited scheme
+    stays positive over the stepping tests' steps (with the 5:1 jump of
+    jump_state the oracle's own limited run of the hexahedral and pyramid
+    blocks turns non-finite within three steps)."""
+    xl = np.mod(x[:, 0], 2.0)
+    rho = np.where(xl < 0.45, 1.0, 0.5) * (1 + 0.02 * rng.uniform(-1, 1, len(x)))
+    p = np.where(xl < 0.45, 1.0, 0.4)
+    n = len(x)
+    return cases.prim_to_cons(rho, np.full(n, 0.1), np.full(n, -0.05), np.full(n, 0.02), p)
+
+
+def load_pair(m, p, mode, precision="fp64", seed=1, riemann="hllc", state=jump_state):
     s = General(m, p, riemann, precision=precision, limiter=mode)
     om = orc.Modal(m, p)
     lim = orc.ModalLimiter(om, MODES[mode])
-    u = om.project(jump_state(om.points()[0], np.random.default_rng(seed)))
+    u = om.project(state(om.points()[0], np.random.default_rng(seed)))
     return s, om, lim, u
 
 
@@ -120,10 +132,11 @@ BC = {0: (orc.BC_SMART, cases.SOD_LEFT), 1: (orc.BC_SUPERSONIC_OUTLET, None),
       4: (orc.BC_INVISCID_WALL, None), 5: (orc.BC_INVISCID_WALL, None)}
 
 
-def set_bcs(s, om, n_blocks):
+def set_bcs(s, om, n_blocks, groups=tuple(BC)):
     specs = {}
     for b in range(n_blocks):
-        for g, spec in BC.items():
+        for g in groups:
+            spec = BC[g]
             specs[b * 6 + g] = spec
             kind, value = spec
             if kind == orc.BC_SMART:
@@ -142,7 +155,7 @@ def test_limited_rk3_parity(gpu, kind, mode):
     smart inlet, outlet and walls; the GPU's own time step."""
     p = 2
     m = make_mesh(kind, periodic=False)
-    s, om, lim, u = load_pair(m, p, mode, riemann="roe")
+    s, om, lim, u = load_pair(m, p, mode, riemann="roe", state=mild_jump_state)
     set_bcs(s, om, {"tet": 1, "mixed": 2, "all": 4}[kind])
     s.SetSolutionColumn(u)
     u, _ = lim.limit(u)
@@ -167,8 +180,8 @@ def test_limited_advance_graph_equals_stepwise_and_is_deterministic(gpu):
     m = make_mesh("mixed", periodic=True)
     outs = []
     for run in range(2):
-        s, om, lim, u = load_pair(m, p, "eigen", riemann="hllc")
-        set_bcs(s, om, 2)
+        s, om, lim, u = load_pair(m, p, "eigen", riemann="hllc", state=mild_jump_state)
+        set_bcs(s, om, 2, groups=(0, 1))  # y and z are periodic
         s.SetSolutionColumn(u)
         t = s.advance(4, 1.0, 3, 0.0)
         outs.append(s.GetSolutionColumn())
@@ -189,8 +202,9 @@ def test_mixed_form_limited_density_close_to_fp64(gpu):
     m = make_mesh("mixed", periodic=True)
     res = {}
     for precision in ("fp64", "mixed"):
-        s, om, lim, u = load_pair(m, p, "detect_lazy", precision=precision, riemann="hllc")
-        set_bcs(s, om, 2)
+        s, om, lim, u = load_pair(m, p, "detect_lazy", precision=precision, riemann="hllc",
+                                  state=mild_jump_state)
+        set_bcs(s, om, 2, groups=(0, 1))  # y and z are periodic
         s.SetSolutionColumn(u)
         s.advance(5, 1.0, 3, 0.0)
         res[precision] = s.GetSolutionColumn().reshape(-1, om.m, 5)[:, :, 0]
