@@ -212,8 +212,14 @@ typedef struct mcfd_options {
   int32_t limiter;   /* enum mcfd_limiter */
   double weno_w0;    /* linear weight of a neighbour; <= 0 selects 0.001 */
   double weno_eps;   /* smoothness offset; <= 0 selects 1e-6 */
-  int32_t reserved[4];
+  int32_t contraction; /* enum mcfd_contraction (mixed form) */
+  int32_t reserved[3];
 } mcfd_options;
+
+/* Where the mixed form's DGSEM differentiation runs: the FP32 SIMT pipes
+ * (default), or the tensor cores as TF32x3 compensated products with FP32
+ * accumulation (mma.sync m16n8k8; DGSEM, p = 3, mixed form only). */
+enum mcfd_contraction { MCFD_CONTRACTION_SIMT = 0, MCFD_CONTRACTION_TENSOR = 1 };
 
 typedef struct mcfd_handle mcfd_handle;
 

@@ -26,6 +26,7 @@ HEX8, TET4 = 0, 1
 DGSEM, FR, MODAL = 0, 1, 2
 SCHEME = {"dgsem": DGSEM, "fr": FR, "modal": MODAL}
 FP64, MIXED = 0, 1
+CONTRACTION = {"simt": 0, "tensor": 1}
 
 
 class MeshDesc(C.Structure):
@@ -55,7 +56,8 @@ class Options(C.Structure):
         ("limiter", C.c_int32),
         ("weno_w0", C.c_double),
         ("weno_eps", C.c_double),
-        ("reserved", C.c_int32 * 4),
+        ("contraction", C.c_int32),
+        ("reserved", C.c_int32 * 3),
     ]
 
 

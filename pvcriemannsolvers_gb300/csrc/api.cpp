@@ -823,6 +823,11 @@ int mcfd_create(const mcfd_mesh_desc *mesh, const mcfd_options *options,
     return fail(nullptr, MCFD_ERR_ARGUMENT, "unknown Riemann solver");
   if (options->precision != MCFD_FP64 && options->precision != MCFD_MIXED)
     return fail(nullptr, MCFD_ERR_UNSUPPORTED, "unknown precision form");
+  if (options->contraction != MCFD_CONTRACTION_SIMT &&
+      (options->contraction != MCFD_CONTRACTION_TENSOR || options->precision != MCFD_MIXED ||
+       options->scheme != MCFD_DGSEM || options->degree != 3))
+    return fail(nullptr, MCFD_ERR_UNSUPPORTED,
+                "the tensor-core contraction is built for the mixed DGSEM form at p = 3");
   int n_dev = 0;
   if (cudaGetDeviceCount(&n_dev) != cudaSuccess || n_dev <= options->device || options->device < 0)
     return fail(nullptr, MCFD_ERR_NO_DEVICE, "no CUDA device available");
@@ -837,6 +842,7 @@ int mcfd_create(const mcfd_mesh_desc *mesh, const mcfd_options *options,
   h->opt.cfl = options->cfl;
   h->opt.scheme = options->scheme;
   h->opt.fr_g1 = fr_correction_slope(options->degree);
+  h->opt.tensor_contraction = options->contraction == MCFD_CONTRACTION_TENSOR;
   int rc = MCFD_OK;
   if (cudaSetDevice(h->device) != cudaSuccess) rc = fail(h, MCFD_ERR_CUDA, "cudaSetDevice failed");
   if (!rc && cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)

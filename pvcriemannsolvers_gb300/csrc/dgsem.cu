@@ -396,12 +396,112 @@ cell_update_kernel(CellArgs a) {
 // energy (exact, on the bit patterns), the stage accumulation u + dt R and the
 // RK combinations.  Conversions between the two formats run on the integer
 // pipes, so a node issues ~15 FP64 instructions instead of ~145.
-template <int Q, int STAGE>
+// ---- tensor-core differentiation (TC variant of the mixed cell kernel, Q = 4)
+// The DGSEM derivative along axis d applies the transposed 1D matrix D^T
+// (4 x 4, shared by every cell) to the 4-point lines of each contravariant
+// flux component: R_d[(p, i), n] = sum_m D[m][i] F_d[p][m][n], p one of the
+// block's 20 (cell, component) pairs and n the 16 positions of the line
+// across the other two axes.  Four pairs share one m16n8k8 product: A =
+// diag(D^T, D^T, D^T, D^T) (16 x 16, two k-steps), B the four pairs' lines
+// (16 x 8 per n-tile).  Operands are split as x = tf32(x) + tf32(x - tf32(x))
+// and each product takes three TF32 MMAs (hi hi, hi lo, lo hi) with FP32
+// accumulation, which keeps the FP32 SIMT path's accuracy.
+__device__ __forceinline__ unsigned tf32_of(float x) {
+  unsigned r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ void split_tf32(float x, unsigned *hi, unsigned *lo) {
+  *hi = tf32_of(x);
+  *lo = tf32_of(x - __uint_as_float(*hi));
+}
+
+__device__ __forceinline__ void mma_tf32(float *c, const unsigned *a, unsigned b0, unsigned b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// s_ft [4 cells][15][64] -> s_res [4 cells][5][64] = sum over the three axes
+// of the line derivatives (the weak-form volume term before the lift), for
+// the block's 4 cells; every thread of the 256-thread block takes part.
+__device__ __forceinline__ void tc_differentiate(const float (*s_ft)[15][64], const float *s_d,
+                                                 float (*s_res)[kK][64]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int gid = lane >> 2, tig = lane & 3;
+  // A fragments of diag(D^T, ...) for both k-steps: element (row r, col kk)
+  // of k-step s is D[m][i] when r / 4 == (8 s + kk) / 4, with i = r % 4,
+  // m = kk % 4 (a0: (gid, tig), a1: (gid + 8, tig), a2: (gid, tig + 4),
+  // a3: (gid + 8, tig + 4))
+  unsigned ahi[2][4], alo[2][4];
+#pragma unroll
+  for (int st = 0; st < 2; ++st) {
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int r = gid + ((e & 1) ? 8 : 0), kk = tig + ((e & 2) ? 4 : 0);
+      const int col = st * 8 + kk;
+      const float v = (r / 4 == col / 4) ? s_d[(col % 4) * 4 + (r % 4)] : 0.f;
+      split_tf32(v, &ahi[st][e], &alo[st][e]);
+    }
+  }
+  // one direction at a time: each output element is written by one lane
+#pragma unroll 1
+  for (int d = 0; d < 3; ++d) {
+#pragma unroll 1
+    for (int item = warp; item < 10; item += 8) {
+      const int g = item >> 1, t = item & 1;  // pair group (4 pairs), n-tile
+      float c[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int st = 0; st < 2; ++st) {
+        // B (8 x 8): row kk = (pair pb, m), col n; b0: (tig, gid), b1: (tig + 4, gid)
+        unsigned bhi[2], blo[2];
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+          const int kk = tig + 4 * e;
+          const int pb = st * 2 + kk / 4, m = kk % 4;
+          const int pr = g * 4 + pb, cell = pr / kK, comp = pr % kK;
+          const int col = t * 8 + gid, hi = col / 4, lo = col % 4;
+          int node;
+          if (d == 0) node = (m * 4 + hi) * 4 + lo;        // (m, j, k)
+          else if (d == 1) node = (hi * 4 + m) * 4 + lo;   // (i, m, k)
+          else node = (hi * 4 + lo) * 4 + m;               // (i, j, m)
+          split_tf32(s_ft[cell][comp * 3 + d][node], &bhi[e], &blo[e]);
+        }
+        mma_tf32(c, alo[st], bhi[0], bhi[1]);
+        mma_tf32(c, ahi[st], blo[0], blo[1]);
+        mma_tf32(c, ahi[st], bhi[0], bhi[1]);
+      }
+      // C (16 x 8): c0, c1 at (gid, 2 tig + 0/1), c2, c3 at (gid + 8, ...)
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int r = gid + ((e & 2) ? 8 : 0), n = t * 8 + 2 * tig + (e & 1);
+        const int pr = g * 4 + r / 4, cell = pr / kK, comp = pr % kK, i = r % 4;
+        const int hi = n / 4, lo = n % 4;
+        int node;
+        if (d == 0) node = (i * 4 + hi) * 4 + lo;
+        else if (d == 1) node = (hi * 4 + i) * 4 + lo;
+        else node = (hi * 4 + lo) * 4 + i;
+        if (d == 0) s_res[cell][comp][node] = c[e];
+        else s_res[cell][comp][node] += c[e];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// TC (Q = 4, dg::Lobatto only): the differentiation on the tensor cores
+// (tc_differentiate), everything else as the SIMT form.
+template <int Q, int STAGE, bool TC = false>
 __global__ void __launch_bounds__(CellCfg<Q>::kThreads)
 cell_update_mixed_kernel(CellArgs a, const float *__restrict__ geo32) {
   constexpr int N = Q * Q * Q, QF = Q * Q, KN = kK * N;
   constexpr int CPB = CellCfg<Q>::kCells;
+  static_assert(!TC || (Q == 4 && CPB == 4), "the tensor-core form is built for Q = 4");
   __shared__ float s_ft[CPB][15][N];
+  __shared__ float s_res[TC ? CPB : 1][kK][TC ? N : 1];
   __shared__ float s_d[Q * Q];
   const int tid = threadIdx.x;
   if (tid < Q * Q) s_d[tid] = f64_to_f32(a.dmat[tid]);
@@ -446,12 +546,22 @@ cell_update_mixed_kernel(CellArgs a, const float *__restrict__ geo32) {
     }
 #pragma unroll
     for (int rr = 0; rr < 15; ++rr) s_ft[lc][rr][q] = ft[rr];
+  } else if constexpr (TC) {
+#pragma unroll
+    for (int rr = 0; rr < 15; ++rr) s_ft[lc][rr][q] = 0.f;
   }
   __syncthreads();
+  float res[kK];
+  if constexpr (TC) {
+    tc_differentiate(s_ft, s_d, s_res);
+    if (!active) return;
+#pragma unroll
+    for (int rr = 0; rr < kK; ++rr) res[rr] = s_res[lc][rr][q];
+  }
   if (!active) return;
   const int i = q / QF, j = (q / Q) % Q, k = q % Q;
-  float res[kK];
-  if (!a.fr) {
+  if constexpr (TC) {
+  } else if (!a.fr) {
 #pragma unroll
     for (int rr = 0; rr < kK; ++rr) {
       float s = 0.f;
@@ -733,6 +843,13 @@ template <int Q, int S>
 void cell_launch_mixed(mcfd_handle *h, const CellArgs &ca) {
   constexpr int CPB = CellCfg<Q>::kCells;
   int64_t blocks = (ca.n_cells + CPB - 1) / CPB;
+  if constexpr (Q == 4) {
+    if (h->opt.tensor_contraction && !ca.fr) {
+      cell_update_mixed_kernel<Q, S, true><<<(unsigned)blocks, CellCfg<Q>::kThreads, 0, h->stream>>>(
+          ca, h->mesh.cell_geo32);
+      return;
+    }
+  }
   cell_update_mixed_kernel<Q, S><<<(unsigned)blocks, CellCfg<Q>::kThreads, 0, h->stream>>>(
       ca, h->mesh.cell_geo32);
 }

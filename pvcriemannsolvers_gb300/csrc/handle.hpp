@@ -233,6 +233,7 @@ struct Options {
   int scheme = 0;     // 0 dg::Lobatto (DGSEM), 1 fr::Lobatto (Huynh g2), 2 dg::General (modal)
   double cfl = 0;
   double fr_g1 = 0;   // g_R'(1) of the FR correction function
+  int tensor_contraction = 0;  // mixed DGSEM p = 3: differentiation on the tensor cores
 };
 
 }  // namespace mcfd
