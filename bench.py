@@ -283,11 +283,12 @@ E2E_PATH = ("mcfd_stream_step per step (pinned host column in, one SSP-RK3 step,
 E2E_SEQ_PATH = "mcfd_set_solution (pinned host) + mcfd_advance(1) + mcfd_get_solution (pinned host)"
 
 
-def measure_form(args, torch, dist, dev, local_rank, m, u0, precision):
+def measure_form(args, torch, dist, dev, local_rank, m, u0, precision, contraction="simt", e2e=True):
     """Time one precision form: device-resident stepping, kernel times, e2e."""
     from pvcriemannsolvers_gb300 import Lobatto
     world = dist.get_world_size() if dist else 1
-    sysm = Lobatto(m, DEGREE, "rusanov", cfl=CFL, device=local_rank, precision=precision)
+    sysm = Lobatto(m, DEGREE, "rusanov", cfl=CFL, device=local_rank, precision=precision,
+                   contraction=contraction)
     stream = torch.cuda.Stream(device=dev)
     sysm.set_stream(stream.cuda_stream)
     L = u0.size
@@ -314,7 +315,7 @@ def measure_form(args, torch, dist, dev, local_rank, m, u0, precision):
     sol = sysm.GetSolutionColumn()
     kt = sysm.kernel_times(reps=5)
     # end to end through the C ABI with pinned host buffers
-    e2e_s, seq_s = e2e_runs(torch, dev, sysm, sol, t, args.steps, 1e9, dist)
+    e2e_s, seq_s = e2e_runs(torch, dev, sysm, sol, t, args.steps, 1e9, dist) if e2e else (1.0, 1.0)
     sysm.close()
     return {"value": 3 * L * args.steps * world / (ms * 1e-3), "ms_per_step": ms / args.steps,
             "e2e": 3 * L * args.steps * world / e2e_s, "e2e_sequential": 3 * L * args.steps * world / seq_s,
@@ -1045,6 +1046,13 @@ def run_gpu(args, rank, world, local_rank):
     L = u0.size
     forms = ["fp64", "mixed"] if args.form == "both" else [args.form]
     res = {f: measure_form(args, torch, dist, dev, local_rank, m, u0, f) for f in forms}
+    tensor = None
+    if "mixed" in res and DEGREE == 3:
+        # the same mixed form with the differentiation on the tensor cores
+        # (TF32x3 mma.sync): timed beside the SIMT path, which stays the
+        # headline unless the tensor path is faster
+        tensor = measure_form(args, torch, dist, dev, local_rank, m, u0, "mixed", contraction="tensor",
+                              e2e=False)
     head = "mixed" if "mixed" in res else "fp64"
     r = res[head]
     accuracy = {"density_rel_l2_vs_exact": density_l2_vs_exact(r["solution"], m, r["t"]), "t_end": r["t"],
@@ -1085,6 +1093,16 @@ def run_gpu(args, rank, world, local_rank):
         }
         line["roofline"]["step"] = step_roofline(*nodal_step_counts(L, m.n_cells, DEGREE, "rusanov", head),
                                                  r["ms_per_step"], hbm_peak, fp64_peak, peak_src)
+        if tensor is not None:
+            ta = tensor["solution"].reshape(-1, K)[:, 0]
+            tb = (res["fp64"] if "fp64" in res else res["mixed"])["solution"].reshape(-1, K)[:, 0]
+            line["mixed_tensor_contraction"] = {
+                "value": tensor["value"], "ms_per_step": tensor["ms_per_step"], "kernel_ms": tensor["kernel_ms"],
+                "gpu_launches": tensor["launches"], "clocks": tensor["clocks"],
+                "density_rel_l2_vs_fp64": float(np.linalg.norm(ta - tb) / np.linalg.norm(tb)),
+                "vs_simt": tensor["value"] / r["value"],
+                "note": "DGSEM differentiation as TF32x3 mma.sync m16n8k8 products (FP32 accumulation); "
+                        "the line's value is the FP32 SIMT path unless this one is faster"}
         if head == "mixed" and "fp64" in res:
             p = res["fp64"]
             line["plain_fp64"] = {"value": p["value"], "ms_per_step": p["ms_per_step"], "e2e": p["e2e"],
