@@ -693,7 +693,9 @@ dt_reduce_kernel(const double *u, const double *cell_rate, int64_t n_nodes,
   reduce_rate(rate, (case_rate && gid < n_nodes) ? cell_case[gid / N] : -1, state, case_rate);
 }
 
-// Mixed-precision dt reduction: wave speeds in FP32.
+// Mixed-precision dt reduction: wave speeds in FP32, the state converted on
+// the integer pipes (f64_to_f32; the hardware conversion issues on the FP64
+// unit, the bottleneck of this part).
 template <int Q>
 __global__ void __launch_bounds__(512)
 dt_reduce_mixed_kernel(const double *u, const double *cell_rate, int64_t n_nodes,
@@ -704,8 +706,8 @@ dt_reduce_mixed_kernel(const double *u, const double *cell_rate, int64_t n_nodes
   double rate = 0;
   if (gid < n_nodes) {
     const double *p = u + gid * kK;
-    float r = (float)p[0], mx = (float)p[1], my = (float)p[2], mz = (float)p[3],
-          en = (float)p[4];
+    float r = f64_to_f32(p[0]), mx = f64_to_f32(p[1]), my = f64_to_f32(p[2]), mz = f64_to_f32(p[3]),
+          en = f64_to_f32(p[4]);
     float speed = 0.f;
     if (r > 0.f && en >= 0.f) {
       float inv = 1.0f / r;
@@ -716,7 +718,7 @@ dt_reduce_mixed_kernel(const double *u, const double *cell_rate, int64_t n_nodes
     } else if (r == 0.f && en >= 0.f) {
       speed = sqrtf(mx * mx + my * my + mz * mz);
     }
-    rate = (double)fmaxf(speed, 1e-5f) * cell_rate[gid / N];
+    rate = f32_to_f64(fmaxf(speed, 1e-5f)) * cell_rate[gid / N];
   }
   reduce_rate(rate, (case_rate && gid < n_nodes) ? cell_case[gid / N] : -1, state, case_rate);
 }
