@@ -342,66 +342,45 @@ __device__ void eigen_reconstruct(const Args &a, int64_t c, int n_adj,
   __syncthreads();
 }
 
-// weno::Eigen::IsNotSmooth (weno.hpp:230-258) on density and energy, eight
-// lanes per cell (four cells per warp): the lanes split the M modes of every
-// value at the cell centre (own polynomial and each neighbour's, coalesced
-// reads of the [K][M] modal blocks and the [7][M] centre values) and combine
-// their partial sums with warp shuffles; flagged cells are appended to the
-// troubled list (their order does not matter: each reconstruction writes
-// only its own cell).
-constexpr int kDetectLanes = 8;
-
-__device__ __forceinline__ double group_sum(double v) {
-#pragma unroll
-  for (int o = kDetectLanes / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, kDetectLanes);
-  return v;
-}
-
+// weno::Eigen::IsNotSmooth (weno.hpp:230-258) on density and energy, one
+// thread per cell; flagged cells are appended to the troubled list (their
+// order does not matter: each reconstruction writes only its own cell).
+// A warp-cooperative form (eight lanes per cell splitting the modes, shuffle
+// reductions) measured five times slower on the four-quadrant case: on this
+// FP64-bound part the shuffle trees replicate the FP64 adds and the per-cell
+// bookkeeping on every lane, which costs more than the coalescing gains.
 template <int M>
 __global__ void __launch_bounds__(256)
 weno_detect_kernel(WenoArgs a, int32_t *list, unsigned *count) {
-  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t c = gid / kDetectLanes;
-  const int lane = (int)(gid % kDetectLanes);
-  const bool live = c < a.n_cells;
-  const int64_t cc = live ? c : a.n_cells - 1;  // idle lanes shadow the last cell
-  const double s00 = a.s00[cc];
-  const double *ev = a.eval + cc * 7 * M;
-  const double *own = a.modal + cc * kK * M;
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.n_cells) return;
+  const double s00 = a.s00[c];
+  const double *ev = a.eval + c * 7 * M;
+  const double *own = a.modal + c * kK * M;
   int adj[6], n = 0;
-#pragma unroll
   for (int s = 0; s < 6; ++s) {
-    adj[s] = a.adj[cc * 6 + s];
+    adj[s] = a.adj[c * 6 + s];
     n += adj[s] >= 0;
   }
   bool troubled = false;
   const int comps[2] = {0, kK - 1};
-#pragma unroll
   for (int ci = 0; ci < 2; ++ci) {
     const int k = comps[ci];
-    double part = 0;
-    for (int m = lane; m < M; m += kDetectLanes) part += own[k * M + m] * ev[6 * M + m];
-    const double mine = group_sum(part);
     double max_abs = fmax(1e-9, fabs(own[k * M] * s00));
+    double mine = 0;
+    for (int m = 0; m < M; ++m) mine += own[k * M + m] * ev[6 * M + m];
     double sum_abs = 0;
-    // every lane runs all six slots so that the shuffles stay warp-uniform
-#pragma unroll
-    for (int s = 0; s < 6; ++s) {
+    for (int s = 0; s < n; ++s) {
       const int b = adj[s];
-      const bool used = s < n;
-      const double *cb = a.modal + ((int64_t)(used ? b : 0) * kK + k) * M;
+      const double *cb = a.modal + ((int64_t)b * kK + k) * M;
       double v = 0;
-      if (used)
-        for (int m = lane; m < M; m += kDetectLanes) v += cb[m] * ev[s * M + m];
-      v = group_sum(v);
-      if (used) {
-        sum_abs += fabs(mine - v);
-        max_abs = fmax(max_abs, fabs(cb[0] * a.s00[b]));
-      }
+      for (int m = 0; m < M; ++m) v += cb[m] * ev[s * M + m];
+      sum_abs += fabs(mine - v);
+      max_abs = fmax(max_abs, fabs(cb[0] * a.s00[b]));
     }
-    if (sum_abs / max_abs / a.divisor[cc] > a.smooth_ref) troubled = true;
+    if (sum_abs / max_abs / a.divisor[c] > a.smooth_ref) troubled = true;
   }
-  if (live && lane == 0 && troubled) list[atomicAdd(count, 1u)] = (int32_t)c;
+  if (troubled) list[atomicAdd(count, 1u)] = (int32_t)c;
 }
 
 // Reconstruction of the listed cells (every cell when list is null) by a
@@ -577,7 +556,7 @@ int limiter_dispatch(mcfd_handle *h, double *u) {
     return 2;
   }
   cudaMemsetAsync(l.list_count, 0, sizeof(unsigned), h->stream);
-  weno_detect_kernel<M><<<(unsigned)((mesh.n_cells * kDetectLanes + 255) / 256), 256, 0, h->stream>>>(
+  weno_detect_kernel<M><<<(unsigned)((mesh.n_cells + 255) / 256), 256, 0, h->stream>>>(
       wa, l.list, l.list_count);
   if (l.kind == 2 /* MCFD_LIMITER_DETECT_LAZY */)
     weno_reconstruct_kernel<N, M, 2><<<grid, 64, 0, h->stream>>>(wa, l.list, l.list_count);
@@ -605,7 +584,7 @@ int limiter_dispatch_modal(mcfd_handle *h, double *u) {
     return 2;
   }
   cudaMemsetAsync(l.list_count, 0, sizeof(unsigned), h->stream);
-  weno_detect_kernel<M><<<(unsigned)((mesh.n_cells * kDetectLanes + 255) / 256), 256, 0, h->stream>>>(
+  weno_detect_kernel<M><<<(unsigned)((mesh.n_cells + 255) / 256), 256, 0, h->stream>>>(
       wa, l.list, l.list_count);
   if (l.kind == 2 /* MCFD_LIMITER_DETECT_LAZY */)
     weno_reconstruct_kernel<0, M, 2, true><<<grid, 64, 0, h->stream>>>(wa, l.list, l.list_count);
