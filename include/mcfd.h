@@ -213,7 +213,13 @@ typedef struct mcfd_options {
   double weno_w0;    /* linear weight of a neighbour; <= 0 selects 0.001 */
   double weno_eps;   /* smoothness offset; <= 0 selects 1e-6 */
   int32_t contraction; /* enum mcfd_contraction (mixed form) */
-  int32_t reserved[3];
+  int32_t shock_cells_fp64; /* mixed form with a WENO limiter on a nodal scheme:
+                               1 runs the cells that the last limiter pass
+                               flagged, and their face neighbours, through the
+                               FP64 cell update (FP64 face fluxes and FP64
+                               nodal-to-modal products); the other cells stay
+                               mixed */
+  int32_t reserved[2];
 } mcfd_options;
 
 /* Where the mixed form's DGSEM differentiation runs: the FP32 SIMT pipes

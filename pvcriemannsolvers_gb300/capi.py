@@ -57,7 +57,8 @@ class Options(C.Structure):
         ("weno_w0", C.c_double),
         ("weno_eps", C.c_double),
         ("contraction", C.c_int32),
-        ("reserved", C.c_int32 * 3),
+        ("shock_cells_fp64", C.c_int32),
+        ("reserved", C.c_int32 * 2),
     ]
 
 

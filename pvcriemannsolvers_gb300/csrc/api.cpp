@@ -174,7 +174,8 @@ void release(mcfd_handle *h) {
     if (p) cudaFree(p);
   auto &l = h->lim;
   void *lptrs[] = {l.psi, l.mn, l.mn32, l.proj, l.beta, l.eval, l.s00, l.divisor, l.adj,
-                   l.frame, l.volume, l.modal, l.list, l.list_count, l.troubled};
+                   l.frame, l.volume, l.modal, l.list, l.list_count, l.troubled, l.cell_hot,
+                   l.block_hot};
   for (void *p : lptrs)
     if (p) cudaFree(p);
   auto &cs = h->cases;
@@ -791,6 +792,14 @@ int build_limiter(mcfd_handle *h, const mcfd_mesh_desc *d, int kind, double w0,
   if ((rc = upload(h, &l.volume, volume))) return rc;
   CUDA_TRY(h, cudaMalloc(&l.modal, sizeof(double) * C * mcfd::kK * M));
   CUDA_TRY(h, cudaMalloc(&l.list, sizeof(int32_t) * C));
+  if (h->opt.shock_fp64) {
+    const int cpb = Q == 4 ? 4 : (Q == 3 ? 9 : 32);  // CellCfg<Q>::kCells of the cell kernels
+    l.n_blocks = (C + cpb - 1) / cpb;
+    CUDA_TRY(h, cudaMalloc(&l.cell_hot, C));
+    CUDA_TRY(h, cudaMalloc(&l.block_hot, l.n_blocks));
+    CUDA_TRY(h, cudaMemset(l.cell_hot, 0, C));
+    CUDA_TRY(h, cudaMemset(l.block_hot, 0, l.n_blocks));
+  }
   CUDA_TRY(h, cudaMalloc(&l.list_count, sizeof(unsigned)));
   CUDA_TRY(h, cudaMalloc(&l.troubled, sizeof(unsigned long long)));
   CUDA_TRY(h, cudaMemset(l.troubled, 0, sizeof(unsigned long long)));
@@ -823,6 +832,11 @@ int mcfd_create(const mcfd_mesh_desc *mesh, const mcfd_options *options,
     return fail(nullptr, MCFD_ERR_ARGUMENT, "unknown Riemann solver");
   if (options->precision != MCFD_FP64 && options->precision != MCFD_MIXED)
     return fail(nullptr, MCFD_ERR_UNSUPPORTED, "unknown precision form");
+  if (options->shock_cells_fp64 &&
+      (options->precision != MCFD_MIXED || options->scheme == MCFD_MODAL ||
+       options->limiter == MCFD_LIMITER_NONE))
+    return fail(nullptr, MCFD_ERR_UNSUPPORTED,
+                "FP64 shock cells need the mixed form, a nodal scheme and a WENO limiter");
   if (options->contraction != MCFD_CONTRACTION_SIMT &&
       (options->contraction != MCFD_CONTRACTION_TENSOR || options->precision != MCFD_MIXED ||
        options->scheme != MCFD_DGSEM || options->degree != 3))
@@ -843,6 +857,7 @@ int mcfd_create(const mcfd_mesh_desc *mesh, const mcfd_options *options,
   h->opt.scheme = options->scheme;
   h->opt.fr_g1 = fr_correction_slope(options->degree);
   h->opt.tensor_contraction = options->contraction == MCFD_CONTRACTION_TENSOR;
+  h->opt.shock_fp64 = options->shock_cells_fp64 != 0;
   int rc = MCFD_OK;
   if (cudaSetDevice(h->device) != cudaSuccess) rc = fail(h, MCFD_ERR_CUDA, "cudaSetDevice failed");
   if (!rc && cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)

@@ -101,7 +101,20 @@ struct CellArgs {
   double *trace;  // write the node traces of u_out here (surface nodes), or null
   const double *nu;  // artificial viscosity [cells][K] (VISC variant), else null
   int trace_roe;     // the traces' third entry is sqrt(rho) (Roe), else the sound speed
+  // FP64 shock cells (mixed form): the blocks flagged in block_hot take the
+  // FP64 kernel, the others the mixed one; hot_mode 1 skips flagged blocks,
+  // 2 skips the others.  flux64: the face fluxes are stored in FP64.
+  const uint8_t *block_hot;
+  int hot_mode;
+  int flux64;
 };
+
+// Whether this block of a cell kernel sits out under the FP64 shock-cell split.
+__device__ __forceinline__ bool skip_block(const CellArgs &a) {
+  if (!a.block_hot) return false;
+  const bool hot = a.block_hot[blockIdx.x] != 0;
+  return a.hot_mode == 1 ? hot : !hot;
+}
 
 // Step of the case that owns cell c (the handle's step without cases).
 __device__ __forceinline__ double cell_dt(const CaseView &cs, const DevState *state, int64_t c) {
@@ -212,6 +225,7 @@ __global__ void __launch_bounds__(CellCfg<Q>::kThreads)
 cell_update_kernel(CellArgs a) {
   constexpr int N = Q * Q * Q, QF = Q * Q, KN = kK * N;
   constexpr int CPB = CellCfg<Q>::kCells;
+  if (skip_block(a)) return;
   __shared__ double s_ft[CPB][15][N];
   __shared__ double s_d[Q * Q];
   __shared__ double s_u[VISC ? CPB : 1][VISC ? KN : 1];
@@ -500,6 +514,7 @@ cell_update_mixed_kernel(CellArgs a, const float *__restrict__ geo32) {
   constexpr int N = Q * Q * Q, QF = Q * Q, KN = kK * N;
   constexpr int CPB = CellCfg<Q>::kCells;
   static_assert(!TC || (Q == 4 && CPB == 4), "the tensor-core form is built for Q = 4");
+  if (skip_block(a)) return;
   __shared__ float s_ft[CPB][15][N];
   __shared__ float s_res[TC ? CPB : 1][kK][TC ? N : 1];
   __shared__ float s_d[Q * Q];
@@ -591,10 +606,24 @@ cell_update_mixed_kernel(CellArgs a, const float *__restrict__ geo32) {
   auto lift = [&](int side, int t) {
     int32_t vv = cf[side * QF + t];
     if (vv == INT32_MIN) return;
-    // FP32 face fluxes (the face kernel converts once per face point)
-    const float *fl = reinterpret_cast<const float *>(a.flux) + (int64_t)(vv >= 0 ? vv : ~vv) * kK;
+    // FP32 face fluxes (the face kernel converts once per face point), or
+    // FP64 ones converted here (FP64 shock cells: one flux buffer format)
+    const int64_t slot = (int64_t)(vv >= 0 ? vv : ~vv) * kK;
+    float fl[kK];
+    bool no_flux;
+    if (a.flux64) {
+      const double *fd = a.flux + slot;
+#pragma unroll
+      for (int rr = 0; rr < kK; ++rr) fl[rr] = f64_to_f32(fd[rr]);
+      no_flux = (unsigned long long)__double_as_longlong(fd[0]) == kNoFluxBits;
+    } else {
+      const float *fs = reinterpret_cast<const float *>(a.flux) + slot;
+#pragma unroll
+      for (int rr = 0; rr < kK; ++rr) fl[rr] = fs[rr];
+      no_flux = __float_as_uint(fl[0]) == kNoFluxBits32;
+    }
     if (a.fr) {
-      if (__float_as_uint(fl[0]) == kNoFluxBits32) return;  // no boundary
+      if (no_flux) return;  // no boundary
       const int dir = fr_dir(side);
       const float sigma = fr_sign(side) > 0 ? 1.f : -1.f, out_sign = vv >= 0 ? 1.f : -1.f;
 #pragma unroll
@@ -909,7 +938,7 @@ int launch_face_flux(mcfd_handle *h, const double *u, double stage_c, bool props
               m.face_map, m.bcs, h->buf.flux, h->buf.state, stage_c,
               m.n_points, m.n_groups, h->opt.scheme == 1, case_view(h),
               (h->use_trace && h->trace_for == u) ? h->buf.trace : nullptr,
-              h->opt.precision == 1, h->visc.on ? 1 : 0, m.bc_row};
+              h->opt.precision == 1 && !h->opt.shock_fp64, h->visc.on ? 1 : 0, m.bc_row};
   if (m.n_points == 0) return n;
   switch (m.q) {
     case 2: face_dispatch_r<2>(h, fa); break;
@@ -931,6 +960,29 @@ int launch_cell_update(mcfd_handle *h, int stage, const double *u_in,
               h->buf.state, m.n_cells, advance_time, h->opt.scheme == 1, h->opt.fr_g1,
               case_view(h), trace, h->visc.on ? h->visc.nu : nullptr, h->opt.riemann == kRoe};
   if (trace) h->trace_for = u_out;
+  if (h->opt.shock_fp64 && h->opt.precision == 1 && h->lim.block_hot) {
+    // the mixed kernel on the quiet blocks, the FP64 kernel on the blocks of
+    // the last limiter pass's flagged cells and their neighbours; one FP64
+    // flux buffer for both
+    CellArgs mixed = ca, fp64 = ca;
+    mixed.block_hot = fp64.block_hot = h->lim.block_hot;
+    mixed.hot_mode = 1;
+    fp64.hot_mode = 2;
+    mixed.flux64 = fp64.flux64 = 1;
+    h->opt.precision = 0;
+    switch (m.q) {
+      case 2: cell_dispatch_s<2>(h, stage, fp64); break;
+      case 3: cell_dispatch_s<3>(h, stage, fp64); break;
+      default: cell_dispatch_s<4>(h, stage, fp64); break;
+    }
+    h->opt.precision = 1;
+    switch (m.q) {
+      case 2: cell_dispatch_s<2>(h, stage, mixed); break;
+      case 3: cell_dispatch_s<3>(h, stage, mixed); break;
+      default: cell_dispatch_s<4>(h, stage, mixed); break;
+    }
+    return 2;
+  }
   switch (m.q) {
     case 2: cell_dispatch_s<2>(h, stage, ca); break;
     case 3: cell_dispatch_s<3>(h, stage, ca); break;

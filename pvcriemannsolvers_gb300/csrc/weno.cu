@@ -62,7 +62,24 @@ struct WenoArgs {
   double *trace;   // node traces of u to rewrite for the reconstructed cells, or null
   int trace_fast;  // the mixed form's seeded roots in the traces
   int trace_roe;   // third trace entry sqrt(rho) (Roe), else the sound speed
+  uint8_t *cell_hot;  // per cell the detector's flag (FP64 shock cells), or null
 };
+
+// FP64 shock cells of the mixed form: a block of the cell kernel is hot when
+// one of its cells, or a face neighbour of one, was flagged.
+__global__ void __launch_bounds__(256)
+weno_mark_blocks_kernel(const int32_t *__restrict__ adj, const uint8_t *__restrict__ cell_hot,
+                        uint8_t *__restrict__ block_hot, int64_t n_cells, int cells_per_block) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n_cells) return;
+  bool hot = cell_hot[c] != 0;
+#pragma unroll
+  for (int s = 0; s < 6; ++s) {
+    const int b = adj[c * 6 + s];
+    hot |= b >= 0 && cell_hot[b] != 0;
+  }
+  if (hot) block_hot[c / cells_per_block] = 1;
+}
 
 // one thread per (cell, mode): all five components, so each modal_to_nodal
 // entry is loaded once
@@ -380,6 +397,7 @@ weno_detect_kernel(WenoArgs a, int32_t *list, unsigned *count) {
     }
     if (sum_abs / max_abs / a.divisor[c] > a.smooth_ref) troubled = true;
   }
+  if (a.cell_hot) a.cell_hot[c] = troubled ? 1 : 0;
   if (troubled) list[atomicAdd(count, 1u)] = (int32_t)c;
 }
 
@@ -532,7 +550,8 @@ int limiter_dispatch(mcfd_handle *h, double *u) {
   const Mesh &mesh = h->mesh;
   Limiter &l = h->lim;
   int64_t total = mesh.n_cells * M;
-  if (l.mn32) {
+  // FP64 shock cells: the troubled region's momenta take the FP64 product too
+  if (l.mn32 && !l.block_hot) {
     constexpr int CB = Modal32Cfg<N, M>::kCells;
     weno_modal32_kernel<N, M><<<(unsigned)((mesh.n_cells + CB - 1) / CB), Modal32Cfg<N, M>::kThreads, 0,
                                 h->stream>>>(u, l.mn, l.mn32, l.modal, mesh.n_cells);
@@ -545,7 +564,7 @@ int limiter_dispatch(mcfd_handle *h, double *u) {
   double *trace = (h->use_trace && h->trace_for == u) ? h->buf.trace : nullptr;
   WenoArgs wa{u, l.modal, l.psi, l.proj, l.beta, l.eval, l.s00, l.divisor, l.adj,
               l.frame, l.volume, l.troubled, mesh.n_cells, l.w0, l.eps, (Q - 1) < 3 ? 1.0 : 3.0,
-              trace, h->opt.precision == 1, h->opt.riemann == kRoe};
+              trace, h->opt.precision == 1, h->opt.riemann == kRoe, l.cell_hot};
   // persistent grid: limiter_blocks_per_sm blocks of 64 threads per SM
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
@@ -553,16 +572,24 @@ int limiter_dispatch(mcfd_handle *h, double *u) {
       (unsigned)std::min<int64_t>(mesh.n_cells, (int64_t)std::max(sms, 1) * h->tune.limiter_blocks_per_sm);
   if (l.kind == 1 /* MCFD_LIMITER_LAZY: every cell */) {
     weno_reconstruct_kernel<N, M, 1><<<grid, 64, 0, h->stream>>>(wa, nullptr, nullptr);
+    if (l.block_hot) cudaMemsetAsync(l.block_hot, 1, l.n_blocks, h->stream);
     return 2;
   }
   cudaMemsetAsync(l.list_count, 0, sizeof(unsigned), h->stream);
   weno_detect_kernel<M><<<(unsigned)((mesh.n_cells + 255) / 256), 256, 0, h->stream>>>(
       wa, l.list, l.list_count);
+  int n = 3;
+  if (l.block_hot) {
+    cudaMemsetAsync(l.block_hot, 0, l.n_blocks, h->stream);
+    weno_mark_blocks_kernel<<<(unsigned)((mesh.n_cells + 255) / 256), 256, 0, h->stream>>>(
+        l.adj, l.cell_hot, l.block_hot, mesh.n_cells, Q == 4 ? 4 : (Q == 3 ? 9 : 32));
+    ++n;
+  }
   if (l.kind == 2 /* MCFD_LIMITER_DETECT_LAZY */)
     weno_reconstruct_kernel<N, M, 2><<<grid, 64, 0, h->stream>>>(wa, l.list, l.list_count);
   else
     weno_reconstruct_kernel<N, M, 3><<<grid, 64, 0, h->stream>>>(wa, l.list, l.list_count);
-  return 3;
+  return n;
 }
 
 // The modal scheme's limiter pass (M = basis size of degree p).
@@ -574,7 +601,7 @@ int limiter_dispatch_modal(mcfd_handle *h, double *u) {
   weno_transpose_kernel<M><<<(unsigned)((total + 255) / 256), 256, 0, h->stream>>>(u, l.modal, mesh.n_cells);
   WenoArgs wa{u, l.modal, nullptr, l.proj, l.beta, l.eval, l.s00, l.divisor, l.adj,
               l.frame, l.volume, l.troubled, mesh.n_cells, l.w0, l.eps, mesh.p < 3 ? 1.0 : 3.0,
-              nullptr, 0, 0};
+              nullptr, 0, 0, nullptr};
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
   const unsigned grid =

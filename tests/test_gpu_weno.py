@@ -168,3 +168,53 @@ def test_limited_steps_bitwise_reproducible(gpu, precision):
         outs.append((s.GetSolutionColumn().tobytes(), t, s.troubled_cells()))
         s.close()
     assert outs[0] == outs[1]
+
+
+def test_shock_cells_fp64_with_every_block_flagged_is_the_fp64_form(gpu):
+    """weno::Lazy flags every cell, so with FP64 shock cells every block takes
+    the FP64 cell update: with the same steps the result is the FP64 form's
+    up to the mixed form's seeded square roots in the Riemann fluxes."""
+    p = 2
+    m = cases.sod_mesh(20, 2, 2)
+    u0 = cases.sod_ic(meshlib.node_coordinates(m, p).reshape(-1, 3)).ravel()
+    out = {}
+    for name, kw in (("fp64", dict(precision="fp64")),
+                     ("hybrid", dict(precision="mixed", shock_cells_fp64=True))):
+        s = Lobatto(m, p, "roe", limiter="lazy", **kw)
+        cases.sod_bc(s)
+        s.SetSolutionColumn(u0)
+        t = 0.0
+        for _ in range(5):
+            RungeKutta(3).Update(s, t, 2e-4)
+            t += 2e-4
+        out[name] = s.GetSolutionColumn()
+        s.close()
+    assert rel_l2(out["hybrid"], out["fp64"]) <= 1e-11, rel_l2(out["hybrid"], out["fp64"])
+
+
+def test_shock_cells_fp64_track_the_fp64_form_closer(gpu):
+    """The four-quadrant problem with weno::Eigen: the mixed form with FP64
+    shock cells stays closer to the FP64 form than the plain mixed form."""
+    p = 2
+    m = cases.quadrant_mesh(32, 32, 2)
+    u0 = cases.quadrant_ic(meshlib.node_coordinates(m, p).reshape(-1, 3)).ravel()
+    out = {}
+    for name, kw in (("fp64", dict(precision="fp64")), ("mixed", dict(precision="mixed")),
+                     ("hybrid", dict(precision="mixed", shock_cells_fp64=True))):
+        s = Lobatto(m, p, "roe", limiter="eigen", **kw)
+        cases.quadrant_bc(s)
+        s.SetSolutionColumn(u0)
+        s.advance(60, 1.0, 3, 0.0)
+        out[name] = s.GetSolutionColumn().reshape(-1, 5)[:, 0]
+        s.close()
+    e_mixed = rel_l2(out["mixed"], out["fp64"])
+    e_hybrid = rel_l2(out["hybrid"], out["fp64"])
+    assert e_hybrid < e_mixed and e_hybrid <= 1e-6, (e_hybrid, e_mixed)
+
+
+def test_shock_cells_fp64_rejected_without_limiter(gpu):
+    m = cases.sod_mesh(4, 2, 2)
+    with pytest.raises(Exception):
+        Lobatto(m, 2, "roe", precision="mixed", shock_cells_fp64=True)
+    with pytest.raises(Exception):
+        Lobatto(m, 2, "roe", precision="fp64", limiter="eigen", shock_cells_fp64=True)
