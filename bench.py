@@ -895,7 +895,8 @@ QUAD_FLOOR_STEPS = 200
 # the forms of the four-quadrant workload: plain FP64 (the result), mixed,
 # and mixed with the flagged cells and their neighbours in FP64
 QUAD_FORMS = {"fp64": dict(precision="fp64"), "mixed": dict(precision="mixed"),
-              "mixed_shock_fp64": dict(precision="mixed", shock_cells_fp64=True)}
+              "mixed_shock_fp64": dict(precision="mixed", shock_cells_fp64=1),
+              "mixed_shock_fp64_2": dict(precision="mixed", shock_cells_fp64=2)}
 
 
 def quadrant_cpu_sample(threads=None, steps=QUAD_FLOOR_STEPS, device=0):
@@ -936,7 +937,8 @@ def quadrant_cpu_sample(threads=None, steps=QUAD_FLOOR_STEPS, device=0):
              "fp64_gpu_vs_fp64_oracle_density_rel_l2": rel(gpu["fp64"], rho),
              "mixed_gpu_vs_fp64_gpu_density_rel_l2": rel(gpu["mixed"], gpu["fp64"]),
              "mixed_gpu_vs_fp64_oracle_density_rel_l2": rel(gpu["mixed"], rho),
-             "mixed_shock_fp64_gpu_vs_fp64_gpu_density_rel_l2": rel(gpu["mixed_shock_fp64"], gpu["fp64"])}
+             "mixed_shock_fp64_gpu_vs_fp64_gpu_density_rel_l2": rel(gpu["mixed_shock_fp64"], gpu["fp64"]),
+             "mixed_shock_fp64_2_gpu_vs_fp64_gpu_density_rel_l2": rel(gpu["mixed_shock_fp64_2"], gpu["fp64"])}
     return {"value": 3 * u.size * steps / el, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{QUAD_SAMPLE[0]}x{QUAD_SAMPLE[1]}x{QUAD_SAMPLE[2]} cells of the same case "
                       f"(L = {u.size} DOFs), {steps} SSP-RK3 steps with the limiter, {el:.1f} s, oracle (OpenMP)",
@@ -1026,6 +1028,12 @@ def run_quadrant(args, rank, world, local_rank):
                                      / np.linalg.norm(b)),
                                  note="the mixed form with the cells of the last limiter pass's flags "
                                       "and their face neighbours through the FP64 cell update"),
+        "mixed_shock_fp64_2": dict({k: res["mixed_shock_fp64_2"][k] for k in ("value", "ms_per_step", "launches",
+                                                                              "kernel_ms", "clocks")},
+                                   density_rel_l2_vs_fp64=float(np.linalg.norm(
+                                       res["mixed_shock_fp64_2"]["solution"].reshape(-1, K)[:, 0] - b)
+                                       / np.linalg.norm(b)),
+                                   note="as mixed_shock_fp64 with two layers of neighbours"),
         "roofline": {"bound": "fp64", "kernel": "step", "kernel_ms": r["kernel_ms"], "peak": fp64_peak,
                      "unit": "TFLOP/s", "achieved": None, "frac": None, "traffic": None,
                      "peak_source": "measured in this run: cuBLAS DGEMM 4096^3",
@@ -1057,9 +1065,11 @@ def run_gpu(args, rank, world, local_rank):
     del x
     L = u0.size
     forms = ["fp64", "mixed"] if args.form == "both" else [args.form]
-    res = {f: measure_form(args, torch, dist, dev, local_rank, m, u0, f) for f in forms}
+    res = {f: measure_form(args, torch, dist, dev, local_rank, m, u0, f,
+                           contraction="tensor" if (f == "mixed" and args.contraction == "tensor") else "simt")
+           for f in forms}
     tensor = None
-    if "mixed" in res and DEGREE == 3:
+    if "mixed" in res and DEGREE == 3 and args.contraction == "both":
         # the same mixed form with the differentiation on the tensor cores
         # (TF32x3 mma.sync): timed beside the SIMT path, which stays the
         # headline unless the tensor path is faster
@@ -1577,6 +1587,9 @@ def main():
     ap.add_argument("--cells", type=int, default=N_CELLS_1D, help="cells per direction (profiling runs a smaller case)")
     ap.add_argument("--form", default="both", choices=["both", "fp64", "mixed"],
                     help="precision form(s) to time; the line's value is the mixed form when timed")
+    ap.add_argument("--contraction", default="both", choices=["both", "simt", "tensor"],
+                    help="the mixed form's differentiation: FP32 SIMT, tensor cores (TF32x3), or both "
+                         "(SIMT for the line's value, the tensor path timed beside it)")
     ap.add_argument("--workload", default="vortex",
                     choices=["vortex", "mixed_box", "all_types", "curved_types", "ensemble", "quadrant", "output",
                              "reorder", "sod", "viscous"],

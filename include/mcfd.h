@@ -214,11 +214,11 @@ typedef struct mcfd_options {
   double weno_eps;   /* smoothness offset; <= 0 selects 1e-6 */
   int32_t contraction; /* enum mcfd_contraction (mixed form) */
   int32_t shock_cells_fp64; /* mixed form with a WENO limiter on a nodal scheme:
-                               1 runs the cells that the last limiter pass
-                               flagged, and their face neighbours, through the
-                               FP64 cell update (FP64 face fluxes and FP64
-                               nodal-to-modal products); the other cells stay
-                               mixed */
+                               n = 1 or 2 runs the cells that the last limiter
+                               pass flagged, and n layers of face neighbours,
+                               through the FP64 cell update (with FP64 face
+                               fluxes, nodal-to-modal products and time step);
+                               the other cells stay mixed; 0 = off */
   int32_t reserved[2];
 } mcfd_options;
 

@@ -175,7 +175,7 @@ void release(mcfd_handle *h) {
   auto &l = h->lim;
   void *lptrs[] = {l.psi, l.mn, l.mn32, l.proj, l.beta, l.eval, l.s00, l.divisor, l.adj,
                    l.frame, l.volume, l.modal, l.list, l.list_count, l.troubled, l.cell_hot,
-                   l.block_hot};
+                   l.cell_hot2, l.block_hot};
   for (void *p : lptrs)
     if (p) cudaFree(p);
   auto &cs = h->cases;
@@ -796,6 +796,7 @@ int build_limiter(mcfd_handle *h, const mcfd_mesh_desc *d, int kind, double w0,
     const int cpb = Q == 4 ? 4 : (Q == 3 ? 9 : 32);  // CellCfg<Q>::kCells of the cell kernels
     l.n_blocks = (C + cpb - 1) / cpb;
     CUDA_TRY(h, cudaMalloc(&l.cell_hot, C));
+    CUDA_TRY(h, cudaMalloc(&l.cell_hot2, C));
     CUDA_TRY(h, cudaMalloc(&l.block_hot, l.n_blocks));
     CUDA_TRY(h, cudaMemset(l.cell_hot, 0, C));
     CUDA_TRY(h, cudaMemset(l.block_hot, 0, l.n_blocks));
@@ -857,7 +858,7 @@ int mcfd_create(const mcfd_mesh_desc *mesh, const mcfd_options *options,
   h->opt.scheme = options->scheme;
   h->opt.fr_g1 = fr_correction_slope(options->degree);
   h->opt.tensor_contraction = options->contraction == MCFD_CONTRACTION_TENSOR;
-  h->opt.shock_fp64 = options->shock_cells_fp64 != 0;
+  h->opt.shock_fp64 = options->shock_cells_fp64 > 0 ? std::min(options->shock_cells_fp64, 2) : 0;
   int rc = MCFD_OK;
   if (cudaSetDevice(h->device) != cudaSuccess) rc = fail(h, MCFD_ERR_CUDA, "cudaSetDevice failed");
   if (!rc && cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)

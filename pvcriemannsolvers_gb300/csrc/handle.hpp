@@ -162,6 +162,7 @@ struct Limiter {
   // the cell kernel (CellCfg cells) whether it holds a flagged cell or a
   // face neighbour of one (those blocks take the FP64 cell update)
   uint8_t *cell_hot = nullptr;   // [cells]
+  uint8_t *cell_hot2 = nullptr;  // [cells] after the first dilation (two layers)
   uint8_t *block_hot = nullptr;  // [cell-kernel blocks]
   int64_t n_blocks = 0;
   unsigned long long *troubled = nullptr;  // counter of reconstructed cells
@@ -240,7 +241,7 @@ struct Options {
   double cfl = 0;
   double fr_g1 = 0;   // g_R'(1) of the FR correction function
   int tensor_contraction = 0;  // mixed DGSEM p = 3: differentiation on the tensor cores
-  int shock_fp64 = 0;  // mixed + limiter: flagged cells and neighbours in FP64
+  int shock_fp64 = 0;  // mixed + limiter: flagged cells and 1 or 2 neighbour layers in FP64
 };
 
 }  // namespace mcfd

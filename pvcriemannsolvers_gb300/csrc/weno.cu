@@ -65,8 +65,24 @@ struct WenoArgs {
   uint8_t *cell_hot;  // per cell the detector's flag (FP64 shock cells), or null
 };
 
-// FP64 shock cells of the mixed form: a block of the cell kernel is hot when
-// one of its cells, or a face neighbour of one, was flagged.
+// FP64 shock cells of the mixed form: a cell is hot when it or a face
+// neighbour was flagged (one layer); with two layers, when it or a face
+// neighbour is hot after the first.  A block of the cell kernel is hot when
+// one of its cells is.
+__global__ void __launch_bounds__(256)
+weno_dilate_kernel(const int32_t *__restrict__ adj, const uint8_t *__restrict__ in,
+                   uint8_t *__restrict__ out, int64_t n_cells) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n_cells) return;
+  bool hot = in[c] != 0;
+#pragma unroll
+  for (int s = 0; s < 6; ++s) {
+    const int b = adj[c * 6 + s];
+    hot |= b >= 0 && in[b] != 0;
+  }
+  out[c] = hot ? 1 : 0;
+}
+
 __global__ void __launch_bounds__(256)
 weno_mark_blocks_kernel(const int32_t *__restrict__ adj, const uint8_t *__restrict__ cell_hot,
                         uint8_t *__restrict__ block_hot, int64_t n_cells, int cells_per_block) {
@@ -580,9 +596,16 @@ int limiter_dispatch(mcfd_handle *h, double *u) {
       wa, l.list, l.list_count);
   int n = 3;
   if (l.block_hot) {
+    const unsigned cgrid = (unsigned)((mesh.n_cells + 255) / 256);
+    const uint8_t *flags = l.cell_hot;
+    if (h->opt.shock_fp64 > 1) {  // a second layer of neighbours
+      weno_dilate_kernel<<<cgrid, 256, 0, h->stream>>>(l.adj, l.cell_hot, l.cell_hot2, mesh.n_cells);
+      flags = l.cell_hot2;
+      ++n;
+    }
     cudaMemsetAsync(l.block_hot, 0, l.n_blocks, h->stream);
-    weno_mark_blocks_kernel<<<(unsigned)((mesh.n_cells + 255) / 256), 256, 0, h->stream>>>(
-        l.adj, l.cell_hot, l.block_hot, mesh.n_cells, Q == 4 ? 4 : (Q == 3 ? 9 : 32));
+    weno_mark_blocks_kernel<<<cgrid, 256, 0, h->stream>>>(l.adj, flags, l.block_hot, mesh.n_cells,
+                                                           Q == 4 ? 4 : (Q == 3 ? 9 : 32));
     ++n;
   }
   if (l.kind == 2 /* MCFD_LIMITER_DETECT_LAZY */)

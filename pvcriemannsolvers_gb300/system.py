@@ -90,7 +90,7 @@ class Lobatto:
     def __init__(self, mesh: Mesh, degree: int, riemann: str | int = "rusanov",
                  cfl: float = 0.0, device: int = 0, precision: str = "fp64",
                  limiter: str = "none", weno_w0: float = 0.001, weno_eps: float = 1e-6,
-                 scheme: str = "dgsem", contraction: str = "simt", shock_cells_fp64: bool = False):
+                 scheme: str = "dgsem", contraction: str = "simt", shock_cells_fp64: int = 0):
         """precision: "fp64" (plain form) or "mixed" (FP32 volume flux and
         contraction; FP64 Riemann fluxes, lift and RK accumulation).
         limiter: "none", "lazy" (weno::Lazy on every cell) or "detect_lazy"
@@ -98,9 +98,10 @@ class Lobatto:
         after every solution update as WithLimiter does.
         contraction: "simt" (FP32 SIMT) or "tensor" (TF32x3 on the tensor
         cores; mixed DGSEM at p = 3) for the mixed form's differentiation.
-        shock_cells_fp64 (mixed form with a limiter): the cells the last
-        limiter pass flagged and their face neighbours take the FP64 cell
-        update, the rest stays mixed."""
+        shock_cells_fp64 (mixed form with a limiter): 1 or 2 — the cells the
+        last limiter pass flagged and that many layers of face neighbours take
+        the FP64 cell update (and the time step is FP64), the rest stays
+        mixed."""
         lib = capi.load()
         self.mesh = mesh
         self.degree = int(degree)
@@ -145,7 +146,7 @@ class Lobatto:
         opt.weno_w0 = float(weno_w0)
         opt.weno_eps = float(weno_eps)
         opt.contraction = capi.CONTRACTION[contraction]
-        opt.shock_cells_fp64 = 1 if shock_cells_fp64 else 0
+        opt.shock_cells_fp64 = int(shock_cells_fp64)
         self.limiter = limiter
         h = C.c_void_p()
         capi.check(lib.mcfd_create(C.byref(desc), C.byref(opt), C.byref(h)), None)
