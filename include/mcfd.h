@@ -217,7 +217,7 @@ typedef struct mcfd_options {
                                n = 1 or 2 runs the cells that the last limiter
                                pass flagged, and n layers of face neighbours,
                                through the FP64 cell update (with FP64 face
-                               fluxes, nodal-to-modal products and time step);
+                               fluxes and nodal-to-modal products);
                                the other cells stay mixed; 0 = off */
   int32_t reserved[2];
 } mcfd_options;

@@ -1012,9 +1012,9 @@ int launch_dt(mcfd_handle *h, const double *u) {
   unsigned blocks = (unsigned)((nodes + bs - 1) / bs);
   const int32_t *cc = h->cases.cell_case;
   unsigned long long *cr = h->cases.n ? h->cases.rate : nullptr;
-  // FP64 shock cells take the FP64 time step as well (the step size is the
-  // FP64 form's when the states are)
-  if (h->opt.precision == 1 && !h->opt.shock_fp64) {
+  // (with FP64 shock cells too: an FP64 time step measured no closer to the
+  // FP64 form over 200 limited steps and costs 1.6 ms per four-quadrant step)
+  if (h->opt.precision == 1) {
     switch (m.q) {
       case 2: dt_reduce_mixed_kernel<2><<<blocks, bs, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr); break;
       case 3: dt_reduce_mixed_kernel<3><<<blocks, bs, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr); break;

@@ -100,8 +100,7 @@ class Lobatto:
         cores; mixed DGSEM at p = 3) for the mixed form's differentiation.
         shock_cells_fp64 (mixed form with a limiter): 1 or 2 — the cells the
         last limiter pass flagged and that many layers of face neighbours take
-        the FP64 cell update (and the time step is FP64), the rest stays
-        mixed."""
+        the FP64 cell update, the rest stays mixed."""
         lib = capi.load()
         self.mesh = mesh
         self.degree = int(degree)
