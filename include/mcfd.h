@@ -120,7 +120,8 @@ typedef struct mcfd_bc_state {
  * Hexahedron20 / Hexahedron27, coordinate/tetrahedron.hpp Tetrahedron4 /
  * Tetrahedron10), nodes in CGNS order.  The quadratic types give curved
  * cells and faces; the hexahedra run every scheme, the tetrahedra the MODAL
- * scheme; the WENO limiter takes Hex8 cells only. */
+ * scheme; the WENO limiter takes every cell type on the MODAL scheme and
+ * Hex8 cells on the nodal schemes. */
 enum mcfd_cell_type {
   MCFD_HEX8 = 0,
   MCFD_TET4 = 1,
@@ -175,13 +176,14 @@ typedef struct mcfd_mesh_desc {
  *          (spatial/fr/general.hpp, spatial/fr/lobatto.hpp, basis/vincent.hpp);
  *          its time step is twice the DGSEM one (fr/lobatto.hpp:220-222)
  *   MODAL: dg::General over polynomial::Projection (spatial/dg/general.hpp,
- *          polynomial/projection.hpp) on Hex8 and Tet4 cells: per-cell
+ *          polynomial/projection.hpp) on every cell type: per-cell
  *          orthonormal Taylor basis, column block [M][K] per cell with
  *          M = (p+1)(p+2)(p+3)/6.  Quadrature: Hex8 Gauss-Legendre (p+1)^3,
  *          Quad4 faces (p+1)^2; Tet4 14 points (p <= 2) or 24 points (p = 3),
  *          Tri3 faces 6 points (p <= 2) or 12 points (p = 3)
  *          (integrator/{legendre,tetrahedron,triangle}.hpp).  FP64 or mixed
- *          (FP32 contractions, FP64 face states / Riemann / RK); no limiter. */
+ *          (FP32 contractions, FP64 face states / Riemann / RK); any
+ *          limiter (WithLimiter<dg::General>, demo/euler/sourceless.hpp). */
 enum mcfd_scheme { MCFD_DGSEM = 0, MCFD_FR = 1, MCFD_MODAL = 2 };
 enum mcfd_precision { MCFD_FP64 = 0, MCFD_MIXED = 1 };
 
