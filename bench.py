@@ -44,6 +44,7 @@ N_CELLS_1D = 64
 DEGREE = 3
 CFL = 0.1
 SAMPLE_1D = 16
+VORTEX_ACCURACY_STEPS = 100  # SSP-RK3 steps of the convergence and accuracy runs
 K = 5
 
 
@@ -190,6 +191,7 @@ def convergence(forms, device, dt_cfl, n_steps, finest):
     dt = 0.5 * dt_cfl
     out = {"dt": dt, "steps": n_steps, "t_end": dt * n_steps}
     sizes = [n for n in (16, 32) if n < finest] + [finest]
+    finest_rho = {}
     for form in forms:
         errs = []
         for n1d in sizes:
@@ -197,11 +199,17 @@ def convergence(forms, device, dt_cfl, n_steps, finest):
             s = Lobatto(m, DEGREE, "rusanov", cfl=CFL, device=device, precision=form)
             s.SetSolutionColumn(cases.vortex_ic(meshlib.node_coordinates(m, DEGREE).reshape(-1, 3)).ravel())
             t = s.advance(n_steps, dt, 3, 0.0)
-            errs.append(density_l2_vs_exact(s.GetSolutionColumn(), m, t))
+            sol = s.GetSolutionColumn()
+            errs.append(density_l2_vs_exact(sol, m, t))
+            if n1d == finest:
+                finest_rho[form] = sol.reshape(-1, K)[:, 0].copy()
             s.close()
         orders = [math.log2(errs[i] / errs[i + 1]) * math.log(2) / math.log(sizes[i + 1] / sizes[i])
                   for i in range(len(errs) - 1)]
         out[form] = {"cells_1d": sizes, "density_rel_l2_vs_exact": errs, "observed_order": orders}
+    if "fp64" in finest_rho and "mixed" in finest_rho:
+        a, b = finest_rho["mixed"], finest_rho["fp64"]
+        out["mixed_vs_fp64_density_rel_l2_finest"] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
     return out
 
 
@@ -955,8 +963,11 @@ def run_quadrant(args, rank, world, local_rank):
     m = cases.quadrant_mesh(nx, ny, nz)
     u0 = np.ascontiguousarray(cases.quadrant_ic(meshlib.node_coordinates(m, QUAD_DEGREE).reshape(-1, 3)).ravel())
     L = u0.size
+    # --form fp64 / mixed times that form alone (profiling runs); the line
+    # then carries no comparison between the forms
+    forms = QUAD_FORMS if args.form == "both" else {args.form: QUAD_FORMS[args.form]}
     res = {}
-    for form, kw in QUAD_FORMS.items():
+    for form, kw in forms.items():
         sysm = Lobatto(m, QUAD_DEGREE, "roe", device=local_rank, limiter="eigen", **kw)
         cases.quadrant_bc(sysm)
         stream = torch.cuda.Stream(device=dev)
@@ -988,6 +999,22 @@ def run_quadrant(args, rank, world, local_rank):
                      "clocks": clocks.summary(), "t": t, "solution": sol,
                      "troubled_fraction": troubled / (3.0 * args.steps * m.n_cells)}
     fp64_peak = fp64_peak_tflops(torch, dev)
+    if args.form != "both":
+        r = res[args.form]
+        line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.form == "fp64" else "f64+f32",
+                "data": "synthetic",
+                "config": {"workload": f"four-quadrant Riemann problem, {nx}x{ny}x{nz} Hex8, DGSEM "
+                                       f"p={QUAD_DEGREE}, Roe, weno::Eigen, {args.form} form alone",
+                           "cells": m.n_cells, "dofs": L},
+                "clocks": r["clocks"], "gpu_launches": r["launches"], "kernel_ms": r["kernel_ms"],
+                "e2e": {"value": r["e2e"], "unit": UNIT, "h2d_bytes_per_step": 8 * L,
+                        "d2h_bytes_per_step": 8 * L, "steps": min(args.steps, 20), "path": E2E_PATH},
+                "troubled_fraction": r["troubled_fraction"]}
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        return
     a, b = res["mixed"]["solution"].reshape(-1, K)[:, 0], res["fp64"]["solution"].reshape(-1, K)[:, 0]
     # the workload's stated step count on the full mesh: each form from the
     # initial state for 200 steps, densities against the FP64 form's
@@ -1010,7 +1037,7 @@ def run_quadrant(args, rank, world, local_rank):
         floor = cpu.pop("floor")
     # the plain FP64 form is the line's value: with the limiter switching on
     # shocks this case amplifies perturbations over the steps (mixed vs FP64
-    # density 4.8e-7 after 53 steps, 4.4e-4 after 203), so the mixed form is
+    # density 4.9e-7 after 53 steps, 4.7e-4 after 200), so the mixed form is
     # reported beside it with its deviation, not as the result
     r = res["fp64"]
     line = {
@@ -1098,8 +1125,10 @@ def run_gpu(args, rank, world, local_rank):
         a, b = res["mixed"]["solution"].reshape(-1, K)[:, 0], res["fp64"]["solution"].reshape(-1, K)[:, 0]
         accuracy["mixed_vs_fp64_density_rel_l2"] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
         accuracy["fp64_density_rel_l2_vs_exact"] = density_l2_vs_exact(res["fp64"]["solution"], m, res["fp64"]["t"])
+    # the workload's stated 100 steps, at half the timed run's CFL step on
+    # every mesh
     accuracy["convergence"] = convergence(forms, local_rank, r["t"] / (args.warmup + args.steps),
-                                          args.warmup + args.steps, args.cells)
+                                          VORTEX_ACCURACY_STEPS, args.cells)
     hbm_peak, peak_src = measured_peaks()
     fp64_peak = fp64_peak_tflops(torch, dev)
     cpu = None

@@ -368,7 +368,7 @@ cell_update_kernel(CellArgs a) {
 #pragma unroll
     for (int r = 0; r < kK; ++r) {
       double v = res[r] * inv_w;
-      bad |= !isfinite(v);
+      bad |= !finite64(v);
       out[r] = v;
     }
   } else {
@@ -387,7 +387,7 @@ cell_update_kernel(CellArgs a) {
       } else {  // kStageRk3Last; division by 3 as a multiplication
         v = (next * 2 + a.u0[c * KN + q * kK + r]) * (1.0 / 3.0);
       }
-      bad |= !isfinite(v);
+      bad |= !finite64(v);
       out[r] = v;
       nv[r] = v;
     }

@@ -75,6 +75,25 @@ MCFD_HD Prim make_prim(double rho, double u, double v, double w, double p) {
   return Prim{rho, u, v, w, p, rho > 0 ? rcp_newton(rho) : 0.0};
 }
 
+// x < 0, x > 0 and x != 0 with IEEE results (-0, infinities, NaN) decided on
+// the bit pattern: on the device these run on the integer pipes instead of
+// taking FP64 compare slots on the FP64 unit, which bounds the FP64 kernels.
+#ifdef __CUDA_ARCH__
+__device__ __forceinline__ bool lt_zero(double x) {
+  // negative finite or -inf: bit patterns 0x8000000000000001 .. 0xfff0000000000000
+  return (unsigned long long)__double_as_longlong(x) - 0x8000000000000001ull < 0x7ff0000000000000ull;
+}
+__device__ __forceinline__ bool gt_zero(double x) {
+  // positive finite or +inf: 0x0000000000000001 .. 0x7ff0000000000000
+  return (unsigned long long)__double_as_longlong(x) - 1ull < 0x7ff0000000000000ull;
+}
+__device__ __forceinline__ bool ne_zero(double x) { return (__double_as_longlong(x) << 1) != 0; }
+#else
+inline bool lt_zero(double x) { return x < 0; }
+inline bool gt_zero(double x) { return x > 0; }
+inline bool ne_zero(double x) { return x != 0; }
+#endif
+
 // ConservativeToPrimitive with SetZeroIfNegative (types.hpp:194-202,288-301):
 // a negative density or (first) energy, or a negative pressure after the
 // conversion, zeroes the whole primitive state.  The three velocity
@@ -82,8 +101,8 @@ MCFD_HD Prim make_prim(double rho, double u, double v, double w, double p) {
 MCFD_HD Prim cons_to_prim(double r, double mx, double my, double mz,
                           double e) {
   Prim w{r, mx, my, mz, e, 0.0};
-  if (r < 0 || e < 0) return Prim{0, 0, 0, 0, 0, 0};
-  if (r != 0) {
+  if (lt_zero(r) || lt_zero(e)) return Prim{0, 0, 0, 0, 0, 0};
+  if (ne_zero(r)) {
     double inv = rcp_newton(r);
     w.rinv = inv;
     w.u = mx * inv;
@@ -91,7 +110,7 @@ MCFD_HD Prim cons_to_prim(double r, double mx, double my, double mz,
     w.w = mz * inv;
     double ke = 0.5 * (w.u * w.u + w.v * w.v + w.w * w.w);
     w.p = (e - r * ke) * kGm1;
-    if (w.p < 0) return Prim{0, 0, 0, 0, 0, 0};
+    if (lt_zero(w.p)) return Prim{0, 0, 0, 0, 0, 0};
   }
   return w;
 }
@@ -102,7 +121,7 @@ MCFD_HD double kinetic(const Prim &w) {
 
 // GetSpeedOfSound(rho, p) (types.hpp:252-254).
 MCFD_HD double sound_speed(const Prim &w) {
-  return (w.rho > 0 && w.p > 0) ? sqrt(kGamma * w.p * w.rinv) : 0.0;
+  return (gt_zero(w.rho) && gt_zero(w.p)) ? sqrt(kGamma * w.p * w.rinv) : 0.0;
 }
 
 // Total energy of a primitive state (PrimitiveToConservative, types.hpp:302-311).
@@ -383,16 +402,27 @@ MCFD_HD void flux_rusanov_cons_weighted(const double *cl, const double *cr,
   for (int k = 0; k < kK; ++k) f[k] *= w;
 }
 
+// The two sides' physical fluxes are summed as they are formed: the momentum
+// rows share (p_L + p_R) nh, the energy row is one product plus one FMA, so a
+// face point takes 40 FP64 operations instead of 46 for the side-by-side
+// form.
 MCFD_HD void flux_rusanov_traced_weighted(const double *cl, const double *trl,
                                           const double *cr, const double *trr,
                                           const double *n, double w, double *f) {
-  const double hw = 0.5 * w;
-  const double nh[3] = {hw * n[0], hw * n[1], hw * n[2]};
-  double fl[kK], fr[kK], sl[2], sr[2];
-  if (rusanov_side_traced(cl, trl, nh, fl, sl) && rusanov_side_traced(cr, trr, nh, fr, sr)) {
-    double lam = fmax(fma(sl[0], hw, sl[1]), fma(sr[0], hw, sr[1]));
+  const double pl = trl[1], pr = trr[1];
+  if (!bits_negative(pl) && !bits_negative(pr)) {
+    const double hw = 0.5 * w;
+    const double nh[3] = {hw * n[0], hw * n[1], hw * n[2]};
+    const double mnl = cl[1] * nh[0] + cl[2] * nh[1] + cl[3] * nh[2];
+    const double mnr = cr[1] * nh[0] + cr[2] * nh[1] + cr[3] * nh[2];
+    const double unl = mnl * trl[0], unr = mnr * trr[0];
+    const double lam = fmax(fma(trl[2], hw, fabs(unl)), fma(trr[2], hw, fabs(unr)));
+    const double ps = pl + pr;
+    f[0] = (mnr + mnl) - lam * (cr[0] - cl[0]);
 #pragma unroll
-    for (int k = 0; k < kK; ++k) f[k] = (fr[k] + fl[k]) - lam * (cr[k] - cl[k]);
+    for (int d = 0; d < 3; ++d)
+      f[1 + d] = fma(cr[1 + d], unr, fma(cl[1 + d], unl, ps * nh[d])) - lam * (cr[1 + d] - cl[1 + d]);
+    f[4] = fma(cr[4] + pr, unr, (cl[4] + pl) * unl) - lam * (cr[4] - cl[4]);
     return;
   }
   flux_rusanov(cons_to_prim(cl[0], cl[1], cl[2], cl[3], cl[4]),

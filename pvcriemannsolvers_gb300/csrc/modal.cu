@@ -305,7 +305,7 @@ __global__ void __launch_bounds__(ModalCfg<M>::kBlock) modal_cell_kernel(ModalCe
           v = (next * 2 + a.u0[c * KM + m * kK + k]) * (1.0 / 3.0);
         }
       }
-      bad |= !isfinite(v);
+      bad |= !finite64(v);
       out[m * kK + k] = v;
     }
   }
