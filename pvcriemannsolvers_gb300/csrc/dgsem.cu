@@ -258,14 +258,22 @@ cell_update_kernel(CellArgs a) {
     //   Ft[4][e] = (E + p) V_e.
     // For a converted state (rho > 0) the mass row equals rho V_e; clamped
     // (all-zero primitives) and rho == 0 (unconverted) states take the
-    // general form.
-    double ft[15];
-    const bool converted = w.rho != 0;
+    // general form (a branch, not a select: the common path issues one
+    // multiplication per direction).
+    double ft[15], vel[3];
+#pragma unroll
+    for (int e = 0; e < 3; ++e) vel[e] = w.u * A[0 * 3 + e] + w.v * A[1 * 3 + e] + w.w * A[2 * 3 + e];
+    if (ne_zero(w.rho)) {
+#pragma unroll
+      for (int e = 0; e < 3; ++e) ft[0 * 3 + e] = w.rho * vel[e];
+    } else {
+#pragma unroll
+      for (int e = 0; e < 3; ++e)
+        ft[0 * 3 + e] = uq[1] * A[0 * 3 + e] + uq[2] * A[1 * 3 + e] + uq[3] * A[2 * 3 + e];
+    }
 #pragma unroll
     for (int e = 0; e < 3; ++e) {
-      double ve = w.u * A[0 * 3 + e] + w.v * A[1 * 3 + e] + w.w * A[2 * 3 + e];
-      ft[0 * 3 + e] = converted ? w.rho * ve
-                                : uq[1] * A[0 * 3 + e] + uq[2] * A[1 * 3 + e] + uq[3] * A[2 * 3 + e];
+      const double ve = vel[e];
       ft[1 * 3 + e] = uq[1] * ve + w.p * A[0 * 3 + e];
       ft[2 * 3 + e] = uq[2] * ve + w.p * A[1 * 3 + e];
       ft[3 * 3 + e] = uq[3] * ve + w.p * A[2 * 3 + e];
@@ -347,20 +355,18 @@ cell_update_kernel(CellArgs a) {
         res[r] -= a.g1 * (out_sign * fl[r] - sigma * s_ft[lc][r * 3 + dir][q]);
       return;
     }
-    if (v >= 0) {
+    // -fl or +fl as one FMA with a +-1 factor (exact, and no divergence
+    // between holder and sharer lanes)
+    const double sign = v >= 0 ? -1.0 : 1.0;
 #pragma unroll
-      for (int r = 0; r < kK; ++r) res[r] -= fl[r];
-    } else {
-#pragma unroll
-      for (int r = 0; r < kK; ++r) res[r] += fl[r];
-    }
+    for (int r = 0; r < kK; ++r) res[r] = fma(sign, fl[r], res[r]);
   };
-  if (k == 0) lift(0, i * Q + j);
-  if (k == Q - 1) lift(5, i * Q + j);
-  if (j == 0) lift(1, i * Q + k);
-  if (j == Q - 1) lift(3, i * Q + k);
-  if (i == 0) lift(4, j * Q + k);
-  if (i == Q - 1) lift(2, j * Q + k);
+  // A node touches at most one of the two faces normal to each axis, so the
+  // six faces are visited as three axes (sides 0/5, 1/3, 4/2: the order of
+  // the per-face form), and a warp issues three flux additions, not six.
+  if (k == 0 || k == Q - 1) lift(k == 0 ? 0 : 5, i * Q + j);
+  if (j == 0 || j == Q - 1) lift(j == 0 ? 1 : 3, i * Q + k);
+  if (i == 0 || i == Q - 1) lift(i == 0 ? 4 : 2, j * Q + k);
   const double inv_w = a.cell_geo[(c * N + q) * 10 + 9];
   double *out = a.u_out + c * KN + q * kK;
   bool bad = false;
@@ -372,20 +378,16 @@ cell_update_kernel(CellArgs a) {
       out[r] = v;
     }
   } else {
-    const double dt = cell_dt(a.cs, a.state, c);
+    using SC = StageCoef<STAGE>;
+    const double scale = (SC::cd * cell_dt(a.cs, a.state, c)) * inv_w;
     double nv[kK];
 #pragma unroll
     for (int r = 0; r < kK; ++r) {
-      double next = uq[r] + (res[r] * inv_w) * dt;
       double v;
       if (STAGE == kStageEuler) {
-        v = next;
-      } else if (STAGE == kStageRk2Last) {
-        v = (next + a.u0[c * KN + q * kK + r]) * 0.5;
-      } else if (STAGE == kStageRk3Mid) {
-        v = (a.u0[c * KN + q * kK + r] * 3 + next) * 0.25;
-      } else {  // kStageRk3Last; division by 3 as a multiplication
-        v = (next * 2 + a.u0[c * KN + q * kK + r]) * (1.0 / 3.0);
+        v = fma(res[r], scale, uq[r]);
+      } else {
+        v = fma(SC::c0, a.u0[c * KN + q * kK + r], fma(SC::cu, uq[r], res[r] * scale));
       }
       bad |= !finite64(v);
       out[r] = v;
@@ -635,12 +637,10 @@ cell_update_mixed_kernel(CellArgs a, const float *__restrict__ geo32) {
 #pragma unroll
     for (int rr = 0; rr < kK; ++rr) res[rr] = fmaf(sign, fl[rr], res[rr]);
   };
-  if (k == 0) lift(0, i * Q + j);
-  if (k == Q - 1) lift(5, i * Q + j);
-  if (j == 0) lift(1, i * Q + k);
-  if (j == Q - 1) lift(3, i * Q + k);
-  if (i == 0) lift(4, j * Q + k);
-  if (i == Q - 1) lift(2, j * Q + k);
+  // three axes, at most one face each (the per-face order: sides 0/5, 1/3, 4/2)
+  if (k == 0 || k == Q - 1) lift(k == 0 ? 0 : 5, i * Q + j);
+  if (j == 0 || j == Q - 1) lift(j == 0 ? 1 : 3, i * Q + k);
+  if (i == 0 || i == Q - 1) lift(i == 0 ? 4 : 2, j * Q + k);
   double *out = a.u_out + c * KN + q * kK;
   bool bad = false;
   if (STAGE == kStageResidual) {
@@ -651,20 +651,19 @@ cell_update_mixed_kernel(CellArgs a, const float *__restrict__ geo32) {
       out[rr] = val;
     }
   } else {
-    const float wdt = inv_w * f64_to_f32(cell_dt(a.cs, a.state, c));
+    // the stage's increment weight folded into the FP32 scale (exact for
+    // 1, 1/2 and 1/4; 2/3 rounds to FP32 like the increment itself)
+    using SC = StageCoef<STAGE>;
+    const float wdt = inv_w * f64_to_f32(cell_dt(a.cs, a.state, c)) * (float)SC::cd;
     double nv[kK];
 #pragma unroll
     for (int rr = 0; rr < kK; ++rr) {
-      double next = uq[rr] + f32_to_f64(res[rr] * wdt);
+      const double d = f32_to_f64(res[rr] * wdt);
       double val;
       if (STAGE == kStageEuler) {
-        val = next;
-      } else if (STAGE == kStageRk2Last) {
-        val = (next + a.u0[c * KN + q * kK + rr]) * 0.5;
-      } else if (STAGE == kStageRk3Mid) {
-        val = (a.u0[c * KN + q * kK + rr] * 3 + next) * 0.25;
+        val = uq[rr] + d;
       } else {
-        val = (next * 2 + a.u0[c * KN + q * kK + rr]) * (1.0 / 3.0);
+        val = fma(SC::c0, a.u0[c * KN + q * kK + rr], fma(SC::cu, uq[rr], d));
       }
       bad |= !finite64(val);
       out[rr] = val;

@@ -88,10 +88,28 @@ __device__ __forceinline__ bool gt_zero(double x) {
   return (unsigned long long)__double_as_longlong(x) - 1ull < 0x7ff0000000000000ull;
 }
 __device__ __forceinline__ bool ne_zero(double x) { return (__double_as_longlong(x) << 1) != 0; }
+__device__ __forceinline__ bool ge_zero(double x) {
+  // +0 .. +inf, or -0
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return b <= 0x7ff0000000000000ull || b == 0x8000000000000000ull;
+}
+__device__ __forceinline__ bool le_zero(double x) {
+  // -0 .. -inf, or +0
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return b - 0x8000000000000000ull <= 0x7ff0000000000000ull || b == 0ull;
+}
+// a <= b for a, b >= 0 (either zero's sign), compared as unsigned integers
+__device__ __forceinline__ bool le_nonneg(double a, double b) {
+  return ((unsigned long long)__double_as_longlong(a) & 0x7fffffffffffffffull) <=
+         ((unsigned long long)__double_as_longlong(b) & 0x7fffffffffffffffull);
+}
 #else
 inline bool lt_zero(double x) { return x < 0; }
 inline bool gt_zero(double x) { return x > 0; }
 inline bool ne_zero(double x) { return x != 0; }
+inline bool ge_zero(double x) { return 0.0 <= x; }
+inline bool le_zero(double x) { return x <= 0.0; }
+inline bool le_nonneg(double a, double b) { return a <= b; }
 #endif
 
 // ConservativeToPrimitive with SetZeroIfNegative (types.hpp:194-202,288-301):
@@ -298,7 +316,7 @@ MCFD_HD void node_trace(const double *c, double *tr, bool roe_sqrt_rho = false) 
   }
   double rinv = rcp_newton(r);
   double m2 = c[1] * c[1] + c[2] * c[2] + c[3] * c[3];
-  double p = (e - 0.5 * m2 * rinv) * kGm1;
+  double p = fma(-0.5 * m2, rinv, e) * kGm1;
   tr[0] = rinv;
   if (bits_negative(p)) {
     tr[1] = -1; tr[2] = 0;
@@ -588,7 +606,7 @@ MCFD_HD double sqrt_form(double x) {
 
 template <bool FAST_SQRT>
 MCFD_HD double hllc_q_form(double p_estimate, double p_k) {
-  if (p_estimate <= p_k) return 1.0;
+  if (le_nonneg(p_estimate, p_k)) return 1.0;  // both >= 0 here
   double temp = 1 + kGp1Over2 * (p_estimate * rcp_newton(p_k) - 1) * kOneOverGamma;
   return sqrt_form<FAST_SQRT>(temp);
 }
@@ -626,18 +644,20 @@ MCFD_HD void hllc_core(const double *cl, const double *cr, double il, double ir,
   const double unr = ur * n[0] + vr * n[1] + wr * n[2];
   const double rho_average = (rl + rr) / 2, a_average = (al + ar) / 2;
   const double p_pvrs = (pl + pr - (unr - unl) * rho_average * a_average) / 2;
-  const double p_estimate = fmax(0.0, p_pvrs);
+  // fmax(0, p_pvrs) and the wave-sign tests on the bit patterns (integer
+  // pipes; the same results, NaN included)
+  const double p_estimate = gt_zero(p_pvrs) ? p_pvrs : 0.0;
   const double wave_left = unl - al * hllc_q_form<FAST_SQRT>(p_estimate, pl);
   const double wave_right = unr + ar * hllc_q_form<FAST_SQRT>(p_estimate, pr);
   const double wave_star = (pr - pl + rl * unl * (wave_left - unl) - rr * unr * (wave_right - unr)) *
                            rcp_signed(rl * (wave_left - unl) - rr * (wave_right - unr));
-  if (0.0 <= wave_left) {
+  if (ge_zero(wave_left)) {
     hllc_side_cons(cl, il, ul, vl, wl, pl, unl, n, false, 0, 0, f);
-  } else if (wave_right <= 0.0) {
+  } else if (le_zero(wave_right)) {
     hllc_side_cons(cr, ir, ur, vr, wr, pr, unr, n, false, 0, 0, f);
-  } else if (0.0 <= wave_star) {
+  } else if (ge_zero(wave_star)) {
     hllc_side_cons(cl, il, ul, vl, wl, pl, unl, n, true, wave_left, wave_star, f);
-  } else if (wave_star < 0.0) {
+  } else if (lt_zero(wave_star)) {
     hllc_side_cons(cr, ir, ur, vr, wr, pr, unr, n, true, wave_right, wave_star, f);
   } else {
     for (int k = 0; k < kK; ++k) f[k] = NAN;

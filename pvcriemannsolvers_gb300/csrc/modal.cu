@@ -279,6 +279,7 @@ __global__ void __launch_bounds__(ModalCfg<M>::kBlock) modal_cell_kernel(ModalCe
   double *out = a.u_out + c * KM;
   const double dt = STAGE == kStageResidual ? 0.0
                     : (a.cs.dt ? a.cs.dt[a.cs.cell_case[c]] : a.state->dt);
+  const double dts = StageCoef<STAGE>::cd * dt;  // the increment's stage weight folded in
   bool bad = false;
 #pragma unroll
   for (int m = 0; m < M; ++m) {
@@ -293,17 +294,11 @@ __global__ void __launch_bounds__(ModalCfg<M>::kBlock) modal_cell_kernel(ModalCe
       double v;
       if (STAGE == kStageResidual) {
         v = r;
+      } else if (STAGE == kStageEuler) {
+        v = fma(r, dts, uin[m * kK + k]);
       } else {
-        const double next = uin[m * kK + k] + r * dt;
-        if (STAGE == kStageEuler) {
-          v = next;
-        } else if (STAGE == kStageRk2Last) {
-          v = (next + a.u0[c * KM + m * kK + k]) * 0.5;
-        } else if (STAGE == kStageRk3Mid) {
-          v = (a.u0[c * KM + m * kK + k] * 3 + next) * 0.25;
-        } else {
-          v = (next * 2 + a.u0[c * KM + m * kK + k]) * (1.0 / 3.0);
-        }
+        v = fma(StageCoef<STAGE>::c0, a.u0[c * KM + m * kK + k],
+                fma(StageCoef<STAGE>::cu, uin[m * kK + k], r * dts));
       }
       bad |= !finite64(v);
       out[m * kK + k] = v;
@@ -633,7 +628,8 @@ __global__ void __launch_bounds__(ModalCfg32<M>::kBlock) modal_cell32_kernel(Mod
   double *out = a.u_out + c * KM;
   const double dt = STAGE == kStageResidual ? 0.0
                     : (a.cs.dt ? a.cs.dt[a.cs.cell_case[c]] : a.state->dt);
-  const float dt32 = f64_to_f32(dt);
+  // the increment's stage weight folded in (2/3 rounds to FP32 like the increment)
+  const float dt32 = f64_to_f32(dt) * (float)StageCoef<STAGE>::cd;
   bool bad = false;
 #pragma unroll
   for (int m = 0; m < M; ++m) {
@@ -648,17 +644,11 @@ __global__ void __launch_bounds__(ModalCfg32<M>::kBlock) modal_cell32_kernel(Mod
       double v;
       if (STAGE == kStageResidual) {
         v = f32_to_f64(r);
+      } else if (STAGE == kStageEuler) {
+        v = uin[m * kK + k] + f32_to_f64(r * dt32);
       } else {
-        const double next = uin[m * kK + k] + f32_to_f64(r * dt32);
-        if (STAGE == kStageEuler) {
-          v = next;
-        } else if (STAGE == kStageRk2Last) {
-          v = (next + a.u0[c * KM + m * kK + k]) * 0.5;
-        } else if (STAGE == kStageRk3Mid) {
-          v = (a.u0[c * KM + m * kK + k] * 3 + next) * 0.25;
-        } else {
-          v = (next * 2 + a.u0[c * KM + m * kK + k]) * (1.0 / 3.0);
-        }
+        v = fma(StageCoef<STAGE>::c0, a.u0[c * KM + m * kK + k],
+                fma(StageCoef<STAGE>::cu, uin[m * kK + k], f32_to_f64(r * dt32)));
       }
       bad |= !finite64(v);
       out[m * kK + k] = v;
