@@ -651,17 +651,23 @@ MCFD_HD void hllc_core(const double *cl, const double *cr, double il, double ir,
   const double wave_right = unr + ar * hllc_q_form<FAST_SQRT>(p_estimate, pr);
   const double wave_star = (pr - pl + rl * unl * (wave_left - unl) - rr * unr * (wave_right - unr)) *
                            rcp_signed(rl * (wave_left - unl) - rr * (wave_right - unr));
-  if (ge_zero(wave_left)) {
-    hllc_side_cons(cl, il, ul, vl, wl, pl, unl, n, false, 0, 0, f);
-  } else if (le_zero(wave_right)) {
-    hllc_side_cons(cr, ir, ur, vr, wr, pr, unr, n, false, 0, 0, f);
-  } else if (ge_zero(wave_star)) {
-    hllc_side_cons(cl, il, ul, vl, wl, pl, unl, n, true, wave_left, wave_star, f);
-  } else if (lt_zero(wave_star)) {
-    hllc_side_cons(cr, ir, ur, vr, wr, pr, unr, n, true, wave_right, wave_star, f);
-  } else {
+  // The reference's four cases (left, right, left star, right star) pick a
+  // side and whether the star correction applies; the side's values are
+  // selected (integer selects) and one side evaluation follows, so lanes of a
+  // warp whose star speeds differ in sign share one pass through the FP64
+  // arithmetic instead of one per case.
+  const bool sup_l = ge_zero(wave_left), sup_r = le_zero(wave_right);
+  const bool star = !sup_l && !sup_r;
+  if (star && !ge_zero(wave_star) && !lt_zero(wave_star)) {  // wave_star is NaN
     for (int k = 0; k < kK; ++k) f[k] = NAN;
+    return;
   }
+  const bool left = sup_l || (!sup_r && ge_zero(wave_star));
+  double cs[kK];
+#pragma unroll
+  for (int k = 0; k < kK; ++k) cs[k] = left ? cl[k] : cr[k];
+  hllc_side_cons(cs, left ? il : ir, left ? ul : ur, left ? vl : vr, left ? wl : wr, left ? pl : pr,
+                 left ? unl : unr, n, star, left ? wave_left : wave_right, wave_star, f);
 }
 
 template <bool FAST_SQRT>

@@ -185,12 +185,10 @@ weno_modal32_kernel(const double *__restrict__ u, const double *__restrict__ mn,
   modal[(c * kK + 4) * M + m] = e;
 }
 
-// One entry of L or R of EigenMatrices (riemann/euler/eigen.hpp:27-56) for
-// the conservative state of primitive w in the frame {nu, mu, pi}:
-// e < 25 is L[e / 5][e % 5], otherwise R[(e - 25) / 5][(e - 25) % 5].
-// Columns of R: u - a, u (entropy), two shear waves, u + a; L = R^-1.
-// Frame-independent scalars of EigenMatrices at one state, computed once per
-// cell: velocity, a, 1/a, b1 = 1/e0 (e0 = a^2 / (gamma - 1)), ek, h0 = e0 + ek.
+// Frame-independent scalars of EigenMatrices (riemann/euler/eigen.hpp:27-56)
+// at one state, computed once per cell: velocity, a, 1/a, b1 = 1/e0
+// (e0 = a^2 / (gamma - 1)), ek, h0 = e0 + ek.  Columns of R: u - a,
+// u (entropy), two shear waves, u + a; L = R^-1.
 struct EigenState {
   double vel[3], a, ia, b1, ek, h0;
 };
@@ -207,49 +205,53 @@ __device__ EigenState eigen_state(const Prim &w) {
   return s;
 }
 
-__device__ double eigen_entry(const EigenState &s, const double *nu, const double *mu,
-                              const double *pi, int e) {
+// L (row-major, entries 0..24) and R (25..49) of EigenMatrices
+// (riemann/euler/eigen.hpp:27-56) for the frame {nu, mu, pi}, by one thread in
+// straight-line code: the frame's dot products once, every entry at most two
+// FP64 operations from them.  (Spread over the block entry by entry, the
+// entries' different formulas made each warp step through all of them.)
+__device__ void eigen_matrices(const EigenState &s, const double *nu, const double *mu,
+                               const double *pi, double *lr) {
   const double *vel = s.vel;
   const double u_nu = vel[0] * nu[0] + vel[1] * nu[1] + vel[2] * nu[2];
-  const double a = s.a, ek = s.ek;
-  if (e >= 25) {
-    const int row = (e - 25) / 5, col = (e - 25) % 5;
-    if (row == 0) return (col == 2 || col == 3) ? 0.0 : 1.0;
-    if (row == 4) {
-      const double h0 = s.h0;
-      if (col == 0) return h0 - a * u_nu;
-      if (col == 1) return ek;
-      if (col == 2) return vel[0] * mu[0] + vel[1] * mu[1] + vel[2] * mu[2];
-      if (col == 3) return vel[0] * pi[0] + vel[1] * pi[1] + vel[2] * pi[2];
-      return h0 + a * u_nu;
-    }
-    const int d = row - 1;
-    if (col == 0) return vel[d] - a * nu[d];
-    if (col == 1) return vel[d];
-    if (col == 2) return mu[d];
-    if (col == 3) return pi[d];
-    return vel[d] + a * nu[d];
+  const double u_mu = vel[0] * mu[0] + vel[1] * mu[1] + vel[2] * mu[2];
+  const double u_pi = vel[0] * pi[0] + vel[1] * pi[1] + vel[2] * pi[2];
+  const double a = s.a, ek = s.ek, b1 = s.b1, b2 = b1 * ek, ia = s.ia;
+  double *L = lr, *R = lr + 25;
+  // L: columns 0 and 4
+  L[0 * 5 + 0] = (b2 + u_nu * ia) / 2;
+  L[1 * 5 + 0] = 1 - b2;
+  L[2 * 5 + 0] = -u_mu;
+  L[3 * 5 + 0] = -u_pi;
+  L[4 * 5 + 0] = (b2 - u_nu * ia) / 2;
+  L[0 * 5 + 4] = b1 / 2;
+  L[1 * 5 + 4] = -b1;
+  L[2 * 5 + 4] = 0.0;
+  L[3 * 5 + 4] = 0.0;
+  L[4 * 5 + 4] = b1 / 2;
+  // R: rows 0 and 4
+  R[0 * 5 + 0] = 1.0; R[0 * 5 + 1] = 1.0; R[0 * 5 + 2] = 0.0; R[0 * 5 + 3] = 0.0; R[0 * 5 + 4] = 1.0;
+  R[4 * 5 + 0] = s.h0 - a * u_nu;
+  R[4 * 5 + 1] = ek;
+  R[4 * 5 + 2] = u_mu;
+  R[4 * 5 + 3] = u_pi;
+  R[4 * 5 + 4] = s.h0 + a * u_nu;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const double bv = b1 * vel[d], ni = nu[d] * ia, an = a * nu[d];
+    // L column 1 + d
+    L[0 * 5 + 1 + d] = -(bv + ni) / 2;
+    L[1 * 5 + 1 + d] = bv;
+    L[2 * 5 + 1 + d] = mu[d];
+    L[3 * 5 + 1 + d] = pi[d];
+    L[4 * 5 + 1 + d] = -(bv - ni) / 2;
+    // R row 1 + d
+    R[(1 + d) * 5 + 0] = vel[d] - an;
+    R[(1 + d) * 5 + 1] = vel[d];
+    R[(1 + d) * 5 + 2] = mu[d];
+    R[(1 + d) * 5 + 3] = pi[d];
+    R[(1 + d) * 5 + 4] = vel[d] + an;
   }
-  const int row = e / 5, col = e % 5;
-  const double b1 = s.b1, b2 = b1 * ek;
-  if (col == 0) {
-    if (row == 0) return (b2 + u_nu * s.ia) / 2;
-    if (row == 1) return 1 - b2;
-    if (row == 2) return -(vel[0] * mu[0] + vel[1] * mu[1] + vel[2] * mu[2]);
-    if (row == 3) return -(vel[0] * pi[0] + vel[1] * pi[1] + vel[2] * pi[2]);
-    return (b2 - u_nu * s.ia) / 2;
-  }
-  if (col == 4) {
-    if (row == 0 || row == 4) return b1 / 2;
-    if (row == 1) return -b1;
-    return 0.0;
-  }
-  const int d = col - 1;
-  if (row == 0) return -(b1 * vel[d] + nu[d] * s.ia) / 2;
-  if (row == 1) return b1 * vel[d];
-  if (row == 2) return mu[d];
-  if (row == 3) return pi[d];
-  return -(b1 * vel[d] - nu[d] * s.ia) / 2;
 }
 
 // weno::Eigen reconstruction of cell c from its candidates (slots 0..n_adj-1
@@ -289,13 +291,9 @@ __device__ void eigen_reconstruct(const Args &a, int64_t c, int n_adj,
   }
   if (t < n_adj) s_vol[t] = a.volume[a.adj[c * 6 + t]];
   __syncthreads();
-  {
-    const EigenState es = s_es;
-    for (int i = t; i < n_adj * 50; i += nt) {
-      const int f = i / 50, e = i - f * 50;
-      const double *fr = a.frame + (c * 6 + f) * 9;
-      s_LR[f][e] = eigen_entry(es, fr, fr + 3, fr + 6, e);
-    }
+  if (t < n_adj) {
+    const double *fr = a.frame + (c * 6 + t) * 9;
+    eigen_matrices(s_es, fr, fr + 3, fr + 6, s_LR[t]);
   }
   __syncthreads();
   for (int i = t; i < nc * kK * kK; i += nt) {
