@@ -167,7 +167,7 @@ void release(mcfd_handle *h) {
   stream_release(h);
   auto &m = h->mesh;
   auto &b = h->buf;
-  void *ptrs[] = {m.cell_geo, m.cell_geo32, m.cell_rate, m.cell_flux, m.face_cells,
+  void *ptrs[] = {m.cell_geo, m.cell_geo32, m.cell_rate, m.cell_rate32, m.cell_flux, m.face_cells,
                   m.face_group, m.face_geo, m.face_xyz, m.face_map, m.dmat,
                   m.bcs, m.corners, m.cell_type, b.u, b.u1, b.u2, b.res, b.flux, b.trace, b.state};
   for (void *p : ptrs)
@@ -533,6 +533,8 @@ int build_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
     for (int64_t i = 0; i < d->n_cells * N; ++i)
       for (int e = 0; e < 10; ++e) geo32[(size_t)i * 10 + e] = (float)geo[(size_t)i * 10 + e];
     if ((rc = upload(h, &m.cell_geo32, geo32))) return rc;
+    std::vector<float> rate32(rate.begin(), rate.end());
+    if ((rc = upload(h, &m.cell_rate32, rate32))) return rc;
   }
   if ((rc = upload(h, &m.cell_geo, geo))) return rc;
   if ((rc = upload(h, &m.cell_rate, rate))) return rc;

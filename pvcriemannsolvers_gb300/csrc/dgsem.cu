@@ -685,22 +685,25 @@ cell_update_mixed_kernel(CellArgs a, const float *__restrict__ geo32) {
 // a positive double (monotone as an unsigned integer).
 // Max of `rate` into the handle's word, or into the word of each lane's case.
 // Cases are contiguous runs of cells, so almost every warp is uniform.
+// (rates are >= 1e-5 / length, or 0 for idle lanes: never negative or NaN;
+// FP32 rates of the mixed form are widened exactly first)
 __device__ __forceinline__ void reduce_rate(double rate, int key, DevState *state,
                                             unsigned long long *case_rate) {
-  if (case_rate) {
-    const int key0 = __shfl_sync(0xffffffffu, key, 0);
-    if (__all_sync(0xffffffffu, key == key0)) {
-      for (int o = 16; o > 0; o >>= 1) rate = fmax(rate, __shfl_xor_sync(0xffffffffu, rate, o));
-      if ((threadIdx.x & 31) == 0 && key0 >= 0 && rate > 0)
-        atomicMax(&case_rate[key0], (unsigned long long)__double_as_longlong(rate));
-    } else if (key >= 0 && rate > 0) {
-      atomicMax(&case_rate[key], (unsigned long long)__double_as_longlong(rate));
-    }
-    return;
-  }
-  for (int o = 16; o > 0; o >>= 1) rate = fmax(rate, __shfl_xor_sync(0xffffffffu, rate, o));
-  if ((threadIdx.x & 31) == 0 && rate > 0)
-    atomicMax(&state->max_rate_bits, (unsigned long long)__double_as_longlong(rate));
+  block_max_bits((unsigned long long)__double_as_longlong(rate), key, &state->max_rate_bits, case_rate);
+}
+
+// FP64 -> FP32 by truncating the mantissa (|result| within 2^-23 below |x|),
+// a third of f64_to_f32's integer work: for the mixed time step's wave-speed
+// estimate.  Magnitudes below the normal FP32 range give a signed zero, above
+// it (and infinities, NaN) a signed infinity.
+__device__ __forceinline__ float f64_to_f32_trunc(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const unsigned e = (hi >> 20) & 0x7ffu;
+  unsigned bits = ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+  bits = e <= 896u ? 0u : bits;
+  bits = e >= 1151u ? 0x7f800000u : bits;
+  return __uint_as_float((hi & 0x80000000u) | bits);
 }
 
 template <int Q>
@@ -721,21 +724,23 @@ dt_reduce_kernel(const double *u, const double *cell_rate, int64_t n_nodes,
   reduce_rate(rate, (case_rate && gid < n_nodes) ? cell_case[gid / N] : -1, state, case_rate);
 }
 
-// Mixed-precision dt reduction: wave speeds in FP32, the state converted on
-// the integer pipes (f64_to_f32; the hardware conversion issues on the FP64
-// unit, the bottleneck of this part).
+// Mixed-precision dt reduction: wave speeds and rates in FP32 (the FP32 copy
+// of the cell rates), the state converted by mantissa truncation on the
+// integer pipes (the hardware conversion issues on the FP64 unit, the
+// bottleneck of this part), the maximum by integer reductions: no FP64
+// instruction per node.
 template <int Q>
 __global__ void __launch_bounds__(512)
-dt_reduce_mixed_kernel(const double *u, const double *cell_rate, int64_t n_nodes,
+dt_reduce_mixed_kernel(const double *u, const float *cell_rate32, int64_t n_nodes,
                        DevState *state, const int32_t *cell_case,
                        unsigned long long *case_rate) {
   constexpr int N = Q * Q * Q;
   int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  double rate = 0;
+  float rate = 0.f;
   if (gid < n_nodes) {
     const double *p = u + gid * kK;
-    float r = f64_to_f32(p[0]), mx = f64_to_f32(p[1]), my = f64_to_f32(p[2]), mz = f64_to_f32(p[3]),
-          en = f64_to_f32(p[4]);
+    float r = f64_to_f32_trunc(p[0]), mx = f64_to_f32_trunc(p[1]), my = f64_to_f32_trunc(p[2]),
+          mz = f64_to_f32_trunc(p[3]), en = f64_to_f32_trunc(p[4]);
     float speed = 0.f;
     if (r > 0.f && en >= 0.f) {
       float inv = 1.0f / r;
@@ -746,9 +751,9 @@ dt_reduce_mixed_kernel(const double *u, const double *cell_rate, int64_t n_nodes
     } else if (r == 0.f && en >= 0.f) {
       speed = sqrtf(mx * mx + my * my + mz * mz);
     }
-    rate = f32_to_f64(fmaxf(speed, 1e-5f)) * cell_rate[gid / N];
+    rate = fmaxf(speed, 1e-5f) * cell_rate32[gid / N];
   }
-  reduce_rate(rate, (case_rate && gid < n_nodes) ? cell_case[gid / N] : -1, state, case_rate);
+  reduce_rate(f32_to_f64(rate), (case_rate && gid < n_nodes) ? cell_case[gid / N] : -1, state, case_rate);
 }
 
 __global__ void dt_finalize_kernel(DevState *state, int fr) {
@@ -1015,9 +1020,9 @@ int launch_dt(mcfd_handle *h, const double *u) {
   // FP64 form over 200 limited steps and costs 1.6 ms per four-quadrant step)
   if (h->opt.precision == 1) {
     switch (m.q) {
-      case 2: dt_reduce_mixed_kernel<2><<<blocks, bs, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr); break;
-      case 3: dt_reduce_mixed_kernel<3><<<blocks, bs, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr); break;
-      default: dt_reduce_mixed_kernel<4><<<blocks, bs, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr); break;
+      case 2: dt_reduce_mixed_kernel<2><<<blocks, bs, 0, h->stream>>>(u, m.cell_rate32, nodes, h->buf.state, cc, cr); break;
+      case 3: dt_reduce_mixed_kernel<3><<<blocks, bs, 0, h->stream>>>(u, m.cell_rate32, nodes, h->buf.state, cc, cr); break;
+      default: dt_reduce_mixed_kernel<4><<<blocks, bs, 0, h->stream>>>(u, m.cell_rate32, nodes, h->buf.state, cc, cr); break;
     }
   } else {
     switch (m.q) {

@@ -66,6 +66,54 @@ __device__ __forceinline__ void boundary_given(const BcDev &bc, double x, double
 #pragma unroll
   for (int k = 0; k < 5; ++k) g[k] = src[k];
 }
+
+// Warp maximum of non-negative, non-NaN doubles given as bit patterns, which
+// order like the values as unsigned integers: shuffles and integer compares,
+// no FP64 max (the FP64 unit bounds these kernels).
+__device__ __forceinline__ unsigned long long warp_max_bits(unsigned long long b) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long other = __shfl_xor_sync(0xffffffffu, b, o);
+    b = other > b ? other : b;
+  }
+  return b;
+}
+
+// The block's maximum of such bit patterns into *word (the handle's rate) or
+// case_word[key] (the case of every thread, when the block is one case),
+// with one atomic per block: every warp's atomic on one address serialised
+// in L2 and bounded the time-step passes.  A block that spans cases (case
+// boundaries) takes one atomic per warp, or per lane where a warp spans them
+// too.  Every thread of the block calls this (it synchronises the block).
+__device__ __forceinline__ void block_max_bits(unsigned long long b, int key, unsigned long long *word,
+                                               unsigned long long *case_word) {
+  __shared__ unsigned long long s_max[32];
+  __shared__ int s_key;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) s_key = key;
+  __syncthreads();
+  const int key0 = s_key;
+  if (case_word && !__syncthreads_and(key == key0)) {
+    const int wkey = __shfl_sync(0xffffffffu, key, 0);
+    if (__all_sync(0xffffffffu, key == wkey)) {
+      const unsigned long long m = warp_max_bits(b);
+      if (lane == 0 && wkey >= 0 && m > 0) atomicMax(&case_word[wkey], m);
+    } else if (key >= 0 && b > 0) {
+      atomicMax(&case_word[key], b);
+    }
+    return;
+  }
+  const unsigned long long m = warp_max_bits(b);
+  if (lane == 0) s_max[warp] = m;
+  __syncthreads();
+  if (warp == 0) {
+    const unsigned long long v = warp_max_bits(lane < (int)(blockDim.x >> 5) ? s_max[lane] : 0ull);
+    if (lane == 0 && v > 0) {
+      if (!case_word) atomicMax(word, v);
+      else if (key0 >= 0) atomicMax(&case_word[key0], v);
+    }
+  }
+}
 #endif
 
 // Stage combinations of RungeKutta<1|2|3> (temporal/rk.hpp:16-49):
@@ -105,6 +153,7 @@ struct Mesh {
   double *cell_geo = nullptr;       // [cells][N][10]: w*J^-1 (3x3 row-major), 1/w
   float *cell_geo32 = nullptr;      // [cells][N][10]: FP32 w*J^-1, 1/w (mixed form only)
   double *cell_rate = nullptr;      // [cells] 1 / length  (length = cbrt(V)/2)
+  float *cell_rate32 = nullptr;     // [cells] FP32 copy (mixed form's time step)
   int32_t *cell_flux = nullptr;     // [cells][6][QF] flux slot: >=0 subtract, <0 add (~slot), INT32_MIN none
   int2 *face_cells = nullptr;       // [faces] holder, sharer
   int32_t *face_group = nullptr;    // [faces]

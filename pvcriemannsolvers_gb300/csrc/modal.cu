@@ -313,21 +313,9 @@ __global__ void __launch_bounds__(ModalCfg<M>::kBlock) modal_cell_kernel(ModalCe
 __device__ __forceinline__ void reduce_cell_rate(double rate, int64_t c, int64_t n_cells,
                                                  DevState *state, const int32_t *cell_case,
                                                  unsigned long long *case_rate) {
-  if (case_rate) {
-    const int key = c < n_cells ? cell_case[c] : -1;
-    const int key0 = __shfl_sync(0xffffffffu, key, 0);
-    if (__all_sync(0xffffffffu, key == key0)) {
-      for (int o = 16; o > 0; o >>= 1) rate = fmax(rate, __shfl_xor_sync(0xffffffffu, rate, o));
-      if ((threadIdx.x & 31) == 0 && key0 >= 0 && rate > 0)
-        atomicMax(&case_rate[key0], (unsigned long long)__double_as_longlong(rate));
-    } else if (key >= 0 && rate > 0) {
-      atomicMax(&case_rate[key], (unsigned long long)__double_as_longlong(rate));
-    }
-    return;
-  }
-  for (int o = 16; o > 0; o >>= 1) rate = fmax(rate, __shfl_xor_sync(0xffffffffu, rate, o));
-  if ((threadIdx.x & 31) == 0 && rate > 0)
-    atomicMax(&state->max_rate_bits, (unsigned long long)__double_as_longlong(rate));
+  // (rates are >= 1e-5 / length, or 0 for idle lanes: never negative or NaN)
+  block_max_bits((unsigned long long)__double_as_longlong(rate),
+                 (case_rate && c < n_cells) ? cell_case[c] : -1, &state->max_rate_bits, case_rate);
 }
 
 __device__ __forceinline__ double point_speed(const double *v) {

@@ -98,8 +98,10 @@ weno_mark_blocks_kernel(const int32_t *__restrict__ adj, const uint8_t *__restri
 }
 
 // one thread per (cell, mode): all five components, so each modal_to_nodal
-// entry is loaded once
-template <int N, int M>
+// entry is loaded once.  RHO_E: density and energy only (the jump detector's
+// inputs); the momenta of the cells that a reconstruction reads follow in
+// weno_modal_momenta_kernel once the troubled cells are known.
+template <int N, int M, bool RHO_E = false>
 __global__ void __launch_bounds__(256)
 weno_modal_kernel(const double *__restrict__ u, const double *__restrict__ mn,
                   double *__restrict__ modal, int64_t n_cells) {
@@ -114,10 +116,44 @@ weno_modal_kernel(const double *__restrict__ u, const double *__restrict__ mn,
   for (int q = 0; q < N; ++q) {
     const double w = mc[q * M + m];
 #pragma unroll
-    for (int k = 0; k < kK; ++k) s[k] += uc[q * kK + k] * w;
+    for (int k = 0; k < kK; ++k)
+      if (!RHO_E || k == 0 || k == kK - 1) s[k] += uc[q * kK + k] * w;
   }
 #pragma unroll
-  for (int k = 0; k < kK; ++k) modal[(c * kK + k) * M + m] = s[k];
+  for (int k = 0; k < kK; ++k)
+    if (!RHO_E || k == 0 || k == kK - 1) modal[(c * kK + k) * M + m] = s[k];
+}
+
+// The momenta's modal coefficients of every troubled cell and of its face
+// neighbours (the reconstruction's candidates), after the detector: a
+// grid-stride loop over (troubled cell, slot 0..5 neighbour or 6 own, mode).
+// A cell next to several troubled cells is computed once per such cell, each
+// time to the same values.
+template <int N, int M>
+__global__ void __launch_bounds__(256)
+weno_modal_momenta_kernel(const double *__restrict__ u, const double *__restrict__ mn,
+                          double *__restrict__ modal, const int32_t *__restrict__ adj,
+                          const int32_t *__restrict__ list, const unsigned *count) {
+  const int64_t n_items = (int64_t)*count * 7 * M;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_items;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t l = i / (7 * M);
+    const int r = (int)(i - l * 7 * M), slot = r / M, m = r - slot * M;
+    const int64_t own = list[l];
+    const int64_t c = slot == 6 ? own : adj[own * 6 + slot];
+    if (c < 0) continue;
+    const double *uc = u + c * kK * N;
+    const double *mc = mn + c * N * M;
+    double s[3] = {0, 0, 0};
+#pragma unroll 3
+    for (int q = 0; q < N; ++q) {
+      const double w = mc[q * M + m];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) s[d] += uc[q * kK + 1 + d] * w;
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) modal[(c * kK + 1 + d) * M + m] = s[d];
+  }
 }
 
 // Modal scheme: modal[c][k][m] = column[c][m][k], one thread per (cell, mode).
@@ -374,8 +410,9 @@ __device__ void eigen_reconstruct(const Args &a, int64_t c, int n_adj,
 }
 
 // weno::Eigen::IsNotSmooth (weno.hpp:230-258) on density and energy, one
-// thread per cell; flagged cells are appended to the troubled list (their
-// order does not matter: each reconstruction writes only its own cell).
+// thread per cell; flagged cells are appended to the troubled list, one
+// atomic per warp (their order does not matter: each reconstruction writes
+// only its own cell).
 // A warp-cooperative form (eight lanes per cell splitting the modes, shuffle
 // reductions) measured five times slower on the four-quadrant case: on this
 // FP64-bound part the shuffle trees replicate the FP64 adds and the per-cell
@@ -412,7 +449,16 @@ weno_detect_kernel(WenoArgs a, int32_t *list, unsigned *count) {
     if (sum_abs / max_abs / a.divisor[c] > a.smooth_ref) troubled = true;
   }
   if (a.cell_hot) a.cell_hot[c] = troubled ? 1 : 0;
-  if (troubled) list[atomicAdd(count, 1u)] = (int32_t)c;
+  // one atomic per warp for its troubled cells (the list's order is free)
+  const unsigned active = __activemask();
+  const unsigned mask = __ballot_sync(active, troubled);
+  if (mask) {
+    const int lane = threadIdx.x & 31, leader = __ffs(mask) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(count, (unsigned)__popc(mask));
+    base = __shfl_sync(active, base, leader);
+    if (troubled) list[base + __popc(mask & ((1u << lane) - 1u))] = (int32_t)c;
+  }
 }
 
 // Reconstruction of the listed cells (every cell when list is null) by a
@@ -565,10 +611,16 @@ int limiter_dispatch(mcfd_handle *h, double *u) {
   Limiter &l = h->lim;
   int64_t total = mesh.n_cells * M;
   // FP64 shock cells: the troubled region's momenta take the FP64 product too
+  // FP64 products with a detector: density and energy of every cell now, the
+  // momenta of the reconstructions' candidates after the detector
+  const bool deferred = !(l.mn32 && !l.block_hot) && l.kind != 1;
   if (l.mn32 && !l.block_hot) {
     constexpr int CB = Modal32Cfg<N, M>::kCells;
     weno_modal32_kernel<N, M><<<(unsigned)((mesh.n_cells + CB - 1) / CB), Modal32Cfg<N, M>::kThreads, 0,
                                 h->stream>>>(u, l.mn, l.mn32, l.modal, mesh.n_cells);
+  } else if (deferred) {
+    weno_modal_kernel<N, M, true><<<(unsigned)((total + 255) / 256), 256, 0, h->stream>>>(
+        u, l.mn, l.modal, mesh.n_cells);
   } else {
     weno_modal_kernel<N, M><<<(unsigned)((total + 255) / 256), 256, 0, h->stream>>>(
         u, l.mn, l.modal, mesh.n_cells);
@@ -604,6 +656,11 @@ int limiter_dispatch(mcfd_handle *h, double *u) {
     cudaMemsetAsync(l.block_hot, 0, l.n_blocks, h->stream);
     weno_mark_blocks_kernel<<<cgrid, 256, 0, h->stream>>>(l.adj, flags, l.block_hot, mesh.n_cells,
                                                            Q == 4 ? 4 : (Q == 3 ? 9 : 32));
+    ++n;
+  }
+  if (deferred) {
+    weno_modal_momenta_kernel<N, M><<<(unsigned)std::max(sms, 1) * 8, 256, 0, h->stream>>>(
+        u, l.mn, l.modal, l.adj, l.list, l.list_count);
     ++n;
   }
   if (l.kind == 2 /* MCFD_LIMITER_DETECT_LAZY */)
