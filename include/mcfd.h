@@ -593,7 +593,9 @@ enum mcfd_probe_op {
   MCFD_PROBE_CUDA_RCP = 5,        /* double -> double: 1.0 / x */
   MCFD_PROBE_CUDA_SQRT = 6,       /* double -> double: sqrt(x) */
   MCFD_PROBE_CUDA_F64_TO_F32 = 7, /* double -> float: __double2float_rn */
-  MCFD_PROBE_CUDA_F32_TO_F64 = 8  /* float -> double: (double)f */
+  MCFD_PROBE_CUDA_F32_TO_F64 = 8, /* float -> double: (double)f */
+  MCFD_PROBE_RCP1 = 9             /* double -> double: one-step Newton reciprocal, x > 0
+                                     (the mixed form's node traces) */
 };
 int mcfd_probe_numerics(int32_t device, int32_t op, int64_t n, const void *d_in,
                         void *d_out);

@@ -168,7 +168,7 @@ void release(mcfd_handle *h) {
   auto &m = h->mesh;
   auto &b = h->buf;
   void *ptrs[] = {m.cell_geo, m.cell_geo32, m.cell_rate, m.cell_rate32, m.cell_flux, m.face_cells,
-                  m.face_group, m.face_geo, m.face_xyz, m.face_map, m.dmat,
+                  m.face_group, m.face_geo, m.face_nh, m.face_xyz, m.face_map, m.dmat,
                   m.bcs, m.corners, m.cell_type, b.u, b.u1, b.u2, b.res, b.flux, b.trace, b.state};
   for (void *p : ptrs)
     if (p) cudaFree(p);
@@ -542,6 +542,16 @@ int build_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
   if ((rc = upload(h, &m.face_cells, fcells))) return rc;
   if ((rc = upload(h, &m.face_group, fgroup))) return rc;
   if ((rc = upload(h, &m.face_geo, fgeo))) return rc;
+  if (h->opt.riemann == MCFD_RUSANOV) {
+    // the half-weighted normals of the traced Rusanov flux, formed as the
+    // face kernel formed them: (0.5 w) n_i
+    std::vector<double4> fnh(m.n_points);
+    for (int64_t i = 0; i < m.n_points; ++i) {
+      const double hw = 0.5 * fgeo[i].w;
+      fnh[i] = make_double4(hw * fgeo[i].x, hw * fgeo[i].y, hw * fgeo[i].z, hw);
+    }
+    if ((rc = upload(h, &m.face_nh, fnh))) return rc;
+  }
   if ((rc = upload(h, &m.face_xyz, fxyz))) return rc;
   if ((rc = upload(h, &m.face_map, fmap))) return rc;
   std::vector<double> dvec(dm, dm + Q * Q);

@@ -57,6 +57,7 @@ struct FaceArgs {
   int f32_out;          // mixed form: the flux buffer holds FP32 values
   int visc;             // artificial viscosity: no-slip walls take the wall flux
   const int32_t *bc_row;  // [points] row in the group's boundary table, or null
+  const double4 *face_nh; // [points] (w/2) n, w/2 (Rusanov handles), or null
 };
 
 // FR: a boundary face point without a registered boundary gets no correction
@@ -149,8 +150,6 @@ __global__ void __launch_bounds__(512) face_flux_kernel(FaceArgs a) {
   int64_t f = gid / QF;
   int2 cells = a.face_cells[f];
   short2 map = a.face_map[gid];
-  double4 g = a.face_geo[gid];
-  double n[3] = {g.x, g.y, g.z};
   const double *uh = a.u + (int64_t)cells.x * KN + map.x * kK;
   double ch[kK];
 #pragma unroll
@@ -162,6 +161,23 @@ __global__ void __launch_bounds__(512) face_flux_kernel(FaceArgs a) {
     double cs[kK];
 #pragma unroll
     for (int k = 0; k < kK; ++k) cs[k] = us[k];
+    // Rusanov with traces and precomputed half-weighted normals: neither the
+    // unit normal nor the weight is loaded
+    if constexpr (R == kRusanov) {
+      if (a.trace && a.face_nh) {
+        const double *th = a.trace + ((int64_t)cells.x * (Q * Q * Q) + map.x) * 3;
+        const double *ts = a.trace + ((int64_t)cells.y * (Q * Q * Q) + map.y) * 3;
+        const double trh[3] = {th[0], th[1], th[2]}, trs[3] = {ts[0], ts[1], ts[2]};
+        const double4 h4 = a.face_nh[gid];
+        const double nh[3] = {h4.x, h4.y, h4.z};
+        if (rusanov_traced_nh(ch, trh, cs, trs, nh, h4.w, out)) {
+          store_flux(a.flux, a.f32_out, gid, out);
+          return;
+        }
+      }
+    }
+    const double4 g = a.face_geo[gid];
+    const double n[3] = {g.x, g.y, g.z};
     if constexpr (R == kRusanov || R == kRoe || R == kHllc) {
       if (a.trace) {
         // both sides' node traces: 1/rho, p and the sound speed (Roe: sqrt(rho))
@@ -191,7 +207,10 @@ __global__ void __launch_bounds__(512) face_flux_kernel(FaceArgs a) {
     if (not_converged) atomicOr(&a.state->status, (unsigned)kStatusNotConverged);
     store_flux(a.flux, a.f32_out, gid, out);
     return;
-  } else {
+  }
+  const double4 g = a.face_geo[gid];
+  const double n[3] = {g.x, g.y, g.z};
+  {
     Prim l = cons_to_prim(ch[0], ch[1], ch[2], ch[3], ch[4]);
     int grp = a.face_group[f];
     if (grp >= 0 && grp < a.n_groups && a.bcs[grp].kind != kBcNone &&
@@ -942,7 +961,7 @@ int launch_face_flux(mcfd_handle *h, const double *u, double stage_c, bool props
               m.face_map, m.bcs, h->buf.flux, h->buf.state, stage_c,
               m.n_points, m.n_groups, h->opt.scheme == 1, case_view(h),
               (h->use_trace && h->trace_for == u) ? h->buf.trace : nullptr,
-              h->opt.precision == 1 && !h->opt.shock_fp64, h->visc.on ? 1 : 0, m.bc_row};
+              h->opt.precision == 1 && !h->opt.shock_fp64, h->visc.on ? 1 : 0, m.bc_row, m.face_nh};
   if (m.n_points == 0) return n;
   switch (m.q) {
     case 2: face_dispatch_r<2>(h, fa); break;
@@ -1106,7 +1125,7 @@ int launch_residual_static_scratch(mcfd_handle *h, const double *d_u,
   FaceArgs fa{d_u, m.face_cells, m.face_group, m.face_geo, m.face_xyz,
               m.face_map, m.bcs, scratch, h->buf.state, 0.0,
               m.n_points, m.n_groups, h->opt.scheme == 1, case_view(h), nullptr,
-              h->opt.precision == 1, 0, m.bc_row};
+              h->opt.precision == 1, 0, m.bc_row, nullptr};
   CellArgs ca{d_u, nullptr, d_r, m.cell_geo, m.cell_flux, scratch, m.dmat,
               h->buf.state, m.n_cells, 0, h->opt.scheme == 1, h->opt.fr_g1, case_view(h), nullptr,
               nullptr, 0};

@@ -232,6 +232,22 @@ __device__ __forceinline__ double rcp_newton(double x) {
   d = fma(-x, y, 1.0);
   return fma(y, d, y);
 }
+// rcp_newton with one Newton-Raphson step (relative error below 4e-14, the
+// square of the FP32 seed's 1.8e-7): the mixed form's node traces, where the
+// seeded square root beside it carries 1.4e-13.
+__device__ __forceinline__ double rcp_newton1(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7ff) - (1023 - 127);
+  if (e <= 1 || e >= 253) return 1.0 / x;
+  const unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
+  const float xf = __uint_as_float(((unsigned)e << 23) + (unsigned)(mant >> 29));
+  const unsigned yb = __float_as_uint(__frcp_rn(xf));
+  const unsigned ye = (yb >> 23) & 0xffu;
+  const double y = __longlong_as_double((long long)(
+      ((unsigned long long)(ye + (1023u - 127u)) << 52) |
+      ((unsigned long long)(yb & 0x7fffffu) << 29)));
+  return fma(y, fma(-x, y, 1.0), y);
+}
 // Square root for the mixed form's wave speed: one Newton-Raphson step on
 // the reciprocal square root, y <- y + y (1 - x y^2) / 2, from the FP32
 // hardware estimate of 1/sqrt(x) (relative error below 3e-7, so ~1.4e-13
@@ -268,6 +284,7 @@ __device__ __forceinline__ double rcp_signed(double x) {
 }
 #else
 inline double rcp_newton(double x) { return 1.0 / x; }
+inline double rcp_newton1(double x) { return 1.0 / x; }
 inline double rcp_signed(double x) { return 1.0 / x; }
 inline double sqrt_seeded(double x) { return std::sqrt(x); }
 inline bool bits_positive(double x) { return x > 0; }
@@ -314,7 +331,8 @@ MCFD_HD void node_trace(const double *c, double *tr, bool roe_sqrt_rho = false) 
     tr[0] = 0; tr[1] = -1; tr[2] = 0;
     return;
   }
-  double rinv = rcp_newton(r);
+  // FAST_SQRT (the mixed form): one Newton step for 1/rho as well
+  double rinv = FAST_SQRT ? rcp_newton1(r) : rcp_newton(r);
   double m2 = c[1] * c[1] + c[2] * c[2] + c[3] * c[3];
   double p = fma(-0.5 * m2, rinv, e) * kGm1;
   tr[0] = rinv;
@@ -424,25 +442,34 @@ MCFD_HD void flux_rusanov_cons_weighted(const double *cl, const double *cr,
 // rows share (p_L + p_R) nh, the energy row is one product plus one FMA, so a
 // face point takes 40 FP64 operations instead of 46 for the side-by-side
 // form.
+// The same from the half-weighted normal nh = (w/2) n and hw = w/2 (the
+// face kernels of Rusanov handles read them precomputed); false when a side's
+// trace is marked (the caller takes the primitive fallback).  The larger of
+// the two wave speeds (both >= 0) is chosen on the bit patterns.
+MCFD_HD bool rusanov_traced_nh(const double *cl, const double *trl, const double *cr,
+                               const double *trr, const double *nh, double hw, double *f) {
+  const double pl = trl[1], pr = trr[1];
+  if (bits_negative(pl) || bits_negative(pr)) return false;
+  const double mnl = cl[1] * nh[0] + cl[2] * nh[1] + cl[3] * nh[2];
+  const double mnr = cr[1] * nh[0] + cr[2] * nh[1] + cr[3] * nh[2];
+  const double unl = mnl * trl[0], unr = mnr * trr[0];
+  const double sl = fma(trl[2], hw, fabs(unl)), sr = fma(trr[2], hw, fabs(unr));
+  const double lam = le_nonneg(sr, sl) ? sl : sr;
+  const double ps = pl + pr;
+  f[0] = (mnr + mnl) - lam * (cr[0] - cl[0]);
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+    f[1 + d] = fma(cr[1 + d], unr, fma(cl[1 + d], unl, ps * nh[d])) - lam * (cr[1 + d] - cl[1 + d]);
+  f[4] = fma(cr[4] + pr, unr, (cl[4] + pl) * unl) - lam * (cr[4] - cl[4]);
+  return true;
+}
+
 MCFD_HD void flux_rusanov_traced_weighted(const double *cl, const double *trl,
                                           const double *cr, const double *trr,
                                           const double *n, double w, double *f) {
-  const double pl = trl[1], pr = trr[1];
-  if (!bits_negative(pl) && !bits_negative(pr)) {
-    const double hw = 0.5 * w;
-    const double nh[3] = {hw * n[0], hw * n[1], hw * n[2]};
-    const double mnl = cl[1] * nh[0] + cl[2] * nh[1] + cl[3] * nh[2];
-    const double mnr = cr[1] * nh[0] + cr[2] * nh[1] + cr[3] * nh[2];
-    const double unl = mnl * trl[0], unr = mnr * trr[0];
-    const double lam = fmax(fma(trl[2], hw, fabs(unl)), fma(trr[2], hw, fabs(unr)));
-    const double ps = pl + pr;
-    f[0] = (mnr + mnl) - lam * (cr[0] - cl[0]);
-#pragma unroll
-    for (int d = 0; d < 3; ++d)
-      f[1 + d] = fma(cr[1 + d], unr, fma(cl[1 + d], unl, ps * nh[d])) - lam * (cr[1 + d] - cl[1 + d]);
-    f[4] = fma(cr[4] + pr, unr, (cl[4] + pl) * unl) - lam * (cr[4] - cl[4]);
-    return;
-  }
+  const double hw = 0.5 * w;
+  const double nh[3] = {hw * n[0], hw * n[1], hw * n[2]};
+  if (rusanov_traced_nh(cl, trl, cr, trr, nh, hw, f)) return;
   flux_rusanov(cons_to_prim(cl[0], cl[1], cl[2], cl[3], cl[4]),
                cons_to_prim(cr[0], cr[1], cr[2], cr[3], cr[4]), n, f);
 #pragma unroll

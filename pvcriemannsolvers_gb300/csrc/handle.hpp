@@ -158,6 +158,7 @@ struct Mesh {
   int2 *face_cells = nullptr;       // [faces] holder, sharer
   int32_t *face_group = nullptr;    // [faces]
   double4 *face_geo = nullptr;      // [points] unit normal, weight
+  double4 *face_nh = nullptr;       // [points] (w/2) n, w/2: Rusanov handles' face kernel
   double *face_xyz = nullptr;       // [points][3]
   short2 *face_map = nullptr;       // [points] holder node, sharer node
   double *dmat = nullptr;           // [Q][Q] D[a][i] = l_i'(x_a)

@@ -157,8 +157,9 @@ __global__ void __launch_bounds__(512) modal_face_kernel(ModalFaceArgs a) {
     double us[kK];
     taylor_values<M>((x.x - sh.x) - cs.x, (x.y - sh.y) - cs.y, (x.z - sh.z) - cs.z, t);
     eval_taylor<M>(a.taylor + (int64_t)cells.y * M * kK, t, us);
-    // unit weight (exact): the point weight is applied below
-    interior_flux_weighted<R, false>(uh, us, n, 1.0, out, &not_converged);
+    // the point weight folded into the flux (Rusanov and Roe through the
+    // half-weighted normal, the others by one multiplication)
+    interior_flux_weighted<R, false>(uh, us, n, x.w, out, &not_converged);
   } else {
     Prim l = cons_to_prim(uh[0], uh[1], uh[2], uh[3], uh[4]);
     const int grp = a.face_group[f];
@@ -176,11 +177,13 @@ __global__ void __launch_bounds__(512) modal_face_kernel(ModalFaceArgs a) {
 #pragma unroll
       for (int k = 0; k < kK; ++k) out[k] = 0;
     }
+#pragma unroll
+    for (int k = 0; k < kK; ++k) out[k] *= x.w;
   }
   if (not_converged) atomicOr(&a.state->status, (unsigned)kStatusNotConverged);
   double *dst = a.flux + gid * kK;
 #pragma unroll
-  for (int k = 0; k < kK; ++k) dst[k] = out[k] * x.w;
+  for (int k = 0; k < kK; ++k) dst[k] = out[k];
 }
 
 struct ModalCellArgs {
@@ -486,8 +489,8 @@ __global__ void __launch_bounds__(512) modal_face32_kernel(ModalFace32Args a) {
     eval_taylor<M, float>(a.taylor32 + (int64_t)cells.y * M * kK, t, v);
 #pragma unroll
     for (int k = 0; k < kK; ++k) us[k] = f32_to_f64(v[k]);
-    // unit weight (exact): the point weight is applied below
-    interior_flux_weighted<R, true>(uh, us, n, 1.0, out, &not_converged);
+    // the point weight folded into the flux (as in modal_face_kernel)
+    interior_flux_weighted<R, true>(uh, us, n, x.w, out, &not_converged);
   } else {
     Prim l = cons_to_prim(uh[0], uh[1], uh[2], uh[3], uh[4]);
     const int grp = a.face_group[f];
@@ -505,11 +508,13 @@ __global__ void __launch_bounds__(512) modal_face32_kernel(ModalFace32Args a) {
 #pragma unroll
       for (int k = 0; k < kK; ++k) out[k] = 0;
     }
+#pragma unroll
+    for (int k = 0; k < kK; ++k) out[k] *= x.w;
   }
   if (not_converged) atomicOr(&a.state->status, (unsigned)kStatusNotConverged);
   float *dst = a.flux32 + gid * kK;
 #pragma unroll
-  for (int k = 0; k < kK; ++k) dst[k] = f64_to_f32(out[k] * x.w);
+  for (int k = 0; k < kK; ++k) dst[k] = f64_to_f32(out[k]);
 }
 
 struct ModalCell32Args {

@@ -68,6 +68,7 @@ probe_numerics_kernel(int op, int64_t n, const void *in, void *out) {
     case MCFD_PROBE_CUDA_SQRT: y[i] = sqrt(x[i]); break;
     case MCFD_PROBE_CUDA_F64_TO_F32: yf[i] = __double2float_rn(x[i]); break;
     case MCFD_PROBE_CUDA_F32_TO_F64: y[i] = (double)xf[i]; break;
+    case MCFD_PROBE_RCP1: y[i] = rcp_newton1(x[i]); break;
     default: break;
   }
 }
@@ -120,7 +121,7 @@ extern "C" int mcfd_probe_flux(int32_t device, int32_t riemann, int32_t precisio
 
 extern "C" int mcfd_probe_numerics(int32_t device, int32_t op, int64_t n, const void *d_in,
                                    void *d_out) {
-  if (n < 0 || n > (int64_t)INT32_MAX * 256 || op < MCFD_PROBE_RCP || op > MCFD_PROBE_CUDA_F32_TO_F64)
+  if (n < 0 || n > (int64_t)INT32_MAX * 256 || op < MCFD_PROBE_RCP || op > MCFD_PROBE_RCP1)
     return MCFD_ERR_ARGUMENT;
   if (n == 0) return MCFD_OK;
   if (!d_in || !d_out) return MCFD_ERR_ARGUMENT;

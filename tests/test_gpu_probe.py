@@ -18,7 +18,8 @@ instances (solver x FP64 / mixed form) on given states.  Checked here:
 * every boundary kind (rotated/euler.hpp:144-318) against the oracle;
 * rcp_newton / rcp_signed (Newton reciprocals from an FP32 seed) within one
   ulp of CUDA's correctly rounded 1.0 / x over the whole exponent range and
-  at the seed guards; sqrt_seeded within its stated relative bound of
+  at the seed guards; rcp_newton1 (one Newton step, the mixed form's node
+  traces) and sqrt_seeded within their stated relative bounds of 1.0 / x and
   sqrt; f64_to_f32 / f32_to_f64 bit-equal to __double2float_rn and
   (double)f except the stated flush of magnitudes below 2^-126 to a signed
   zero (NaN stays NaN, infinities stay infinite).
@@ -375,6 +376,31 @@ def test_rcp_signed_within_one_ulp_of_cuda_division(gpu):
     err = np.abs(got[fin] - ref[fin])
     bad = err > ulp(ref[fin])
     assert not bad.any(), (x[fin][bad][:5], got[fin][bad][:5], ref[fin][bad][:5])
+
+
+RCP1_RTOL = 4e-14  # one Newton step on an FP32 seed of relative error < 1.8e-7
+
+
+def test_rcp_newton1_within_its_bound_of_cuda_division(gpu):
+    """The mixed form's node-trace reciprocal (one Newton step): within its
+    stated relative bound of CUDA's 1.0 / x over the exponent range, the
+    FP64 division itself outside the seed's range."""
+    import torch
+    rng = np.random.default_rng(8)
+    x = np.concatenate([f64_sweep(rng, positive_only=True), guard_values()])
+    got = probe_numerics(capi.PROBE_RCP1, x, torch.float64)
+    with np.errstate(divide="ignore", over="ignore", invalid="ignore"):
+        ref = 1.0 / x
+    nan = np.isnan(ref)
+    assert np.array_equal(np.isnan(got), nan)
+    special = nan | np.isinf(ref) | (ref == 0)
+    assert np.array_equal(got[special & ~nan], ref[special & ~nan])
+    fin = ~special
+    rel = np.abs(got[fin] - ref[fin]) / np.abs(ref[fin])
+    assert rel.max() <= RCP1_RTOL, (rel.max(), x[fin][np.argmax(rel)])
+    ex = (x.view(np.uint64) >> np.uint64(52)) & np.uint64(0x7FF)
+    outside = fin & ((ex <= 897) | (ex >= 1149))
+    assert np.array_equal(got[outside], ref[outside])
 
 
 SQRT_SEEDED_RTOL = 2e-13  # one Newton step on an FP32 seed of relative error < 3e-7
