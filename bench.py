@@ -335,8 +335,8 @@ def measure_form(args, torch, dist, dev, local_rank, m, u0, precision, contracti
 # 40^3 p = 3 case (64 000 cells); scaled linearly with the cell count.  Mixed
 # form: the traced face kernel and the cell kernel writing the node traces.
 NCU_TRAFFIC_40 = {
-    ("mixed", "face_flux"): 380.929024e6 + 102.737152e6,
-    ("mixed", "cell_update"): 491.185664e6 + 220.190208e6,
+    ("mixed", "face_flux"): 380.940800e6 + 50.558464e6,
+    ("mixed", "cell_update"): 594.870272e6 + 226.026496e6,  # the RK3 middle stage
 }
 NCU_CELLS = 40 ** 3
 
@@ -418,9 +418,9 @@ def roofline_of(kt, L, cells, hbm_peak, peak_src, fp64_peak, precision):
 # instruction stream (conversions, node traces, positivity), which is what
 # binds the kernel.
 NCU_PIPE_40 = {
-    ("mixed", "cell_update"): {"sm__pipe_fp64_cycles_active_pct": 68.0, "issue_active_pct": 47.8,
+    ("mixed", "cell_update"): {"sm__pipe_fp64_cycles_active_pct": 74.2, "issue_active_pct": 34.6,
                                "source": "ncu --set full, 40^3 p = 3 case"},
-    ("mixed", "face_flux"): {"sm__pipe_fp64_cycles_active_pct": 87.7, "issue_active_pct": 9.5,
+    ("mixed", "face_flux"): {"sm__pipe_fp64_cycles_active_pct": 87.9, "issue_active_pct": 13.4,
                              "source": "ncu --set full, 40^3 p = 3 case"},
 }
 
