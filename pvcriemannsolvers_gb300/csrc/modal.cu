@@ -12,7 +12,7 @@
 // sparse update of Rt (each monomial has at most three non-zero partials);
 // S is applied once per cell.  Per RK stage three kernels run:
 //   modal_taylor_kernel  a = S^T c of the stage input, one thread per
-//                        (cell, monomial, component)
+//                        (cell, pair of monomials j and M - 1 - j, component)
 //   modal_face_kernel    one thread per face point: u on both sides from a,
 //                        the rotated Riemann or boundary flux, times w
 //   modal_cell_kernel    one thread per cell: volume quadrature, lift of its
@@ -93,20 +93,26 @@ __device__ __forceinline__ void add_gradient(const Real *t, Real gx, Real gy, Re
   }
 }
 
-// a[c][j][k] = sum_{m >= j} S[m][j] u[c][m][k]
+// a[c][j][k] = sum_{m >= j} S[m][j] u[c][m][k].  A thread takes the rows j
+// and M - 1 - j (M is even), M + 1 products in all: the same count on every
+// lane (one row per thread gave lanes M - j products, and the FP64 pipe spent
+// the longest row's slots on the whole warp).
 template <int M>
 __global__ void __launch_bounds__(256)
 modal_taylor_kernel(const double *u, const double *s, double *a, int64_t n) {
-  constexpr int KM = kK * M, NS = M * (M + 1) / 2;
+  static_assert(M % 2 == 0, "paired rows need an even basis size");
+  constexpr int KM = kK * M, KH = kK * (M / 2), NS = M * (M + 1) / 2;
   int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= n) return;
-  const int64_t c = gid / KM;
-  const int r = (int)(gid - c * KM), j = r / kK, k = r - j * kK;
+  const int64_t c = gid / KH;
+  const int r = (int)(gid - c * KH), j0 = r / kK, k = r - j0 * kK, j1 = M - 1 - j0;
   const double *uc = u + c * KM;
   const double *sc = s + c * NS;
-  double acc = 0;
-  for (int m = j; m < M; ++m) acc += sc[m * (m + 1) / 2 + j] * uc[m * kK + k];
-  a[gid] = acc;
+  double acc0 = 0, acc1 = 0;
+  for (int m = j0; m < M; ++m) acc0 += sc[m * (m + 1) / 2 + j0] * uc[m * kK + k];
+  for (int m = j1; m < M; ++m) acc1 += sc[m * (m + 1) / 2 + j1] * uc[m * kK + k];
+  a[c * KM + j0 * kK + k] = acc0;
+  a[c * KM + j1 * kK + k] = acc1;
 }
 
 struct ModalFaceArgs {
@@ -732,7 +738,7 @@ void modal_cell32_dispatch(mcfd_handle *h, int stage, const ModalCell32Args &ca)
 
 template <int M>
 int taylor_launch(mcfd_handle *h, const double *u) {
-  const int64_t n = h->mesh.n_cells * kK * M;
+  const int64_t n = h->mesh.n_cells * kK * (M / 2);  // one thread per row pair
   modal_taylor_kernel<M><<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(
       u, h->modal.s, h->modal.taylor, n);
   return 1;
