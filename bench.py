@@ -1280,8 +1280,10 @@ def run_sod(args, rank, world, local_rank):
                      "t_end_fp64": r["t"], "t_end_mixed": pm["t"]},
         "clocks": r["clocks"], "gpu_launches": r["launches"],
         "mixed": {k: pm[k] for k in ("value", "steps", "seconds", "launches", "kernel_ms", "clocks")},
-        "roofline": {"bound": "launch", "note": "1,600 cells: every kernel is a few microseconds; the step "
-                                                "graph removes launch gaps", "kernel_ms": r["kernel_ms"]},
+        "roofline": {"bound": "latency",
+                     "note": "1,600 cells: each kernel fills few SMs; three weno::Lazy passes over every "
+                             "cell (one 64-thread block per cell, dependent FP64 phases) take most of the "
+                             "step; the step graph removes launch gaps", "kernel_ms": r["kernel_ms"]},
         "cpu_baseline": {"value": cpu_rate, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"the same case, steps 6..{n_cpu} of {r['steps']}, {cpu_s:.1f} s, oracle "
                                    f"(plain C restatement, OpenMP)"},

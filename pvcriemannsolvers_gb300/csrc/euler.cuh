@@ -631,51 +631,56 @@ MCFD_HD double sqrt_form(double x) {
   else return sqrt(x);
 }
 
-template <bool FAST_SQRT>
-MCFD_HD double hllc_q_form(double p_estimate, double p_k) {
-  if (le_nonneg(p_estimate, p_k)) return 1.0;  // both >= 0 here
-  double temp = 1 + kGp1Over2 * (p_estimate * rcp_newton(p_k) - 1) * kOneOverGamma;
-  return sqrt_form<FAST_SQRT>(temp);
-}
-
-// one side's flux, plus the star correction when wk is finite (hllc_star)
-MCFD_HD void hllc_side_cons(const double *c, double rinv, double u, double v, double w,
-                            double p, double un, const double *n, bool star, double wk,
-                            double ws, double *f) {
+// one side's flux, plus the star correction (hllc_star) when `star`; the
+// state enters as its conservative variables, 1/rho, p, the normal momentum
+// mn = m . n and un = mn / rho (the star momentum temp u + dm n is formed as
+// (temp / rho) m + dm n, so no velocity vector is needed)
+MCFD_HD void hllc_side_cons(const double *c, double rinv, double p, double mn, double un,
+                            const double *n, bool star, double wk, double ws, double *f) {
   const double rho = c[0], e = c[4];
-  f[0] = rho * un;
+  f[0] = mn;
   f[1] = c[1] * un + p * n[0];
   f[2] = c[2] * un + p * n[1];
   f[3] = c[3] * un + p * n[2];
   f[4] = (e + p) * un;
   if (!star) return;
-  const double temp = rho * (wk - un) * rcp_signed(wk - ws);
-  double es = e * rinv + (ws - un) * (ws + p * rcp_signed(rho * (wk - un)));
+  const double rdk = rho * (wk - un);
+  const double temp = rdk * rcp_signed(wk - ws);
+  double es = e * rinv + (ws - un) * (ws + p * rcp_signed(rdk));
   es *= temp;
-  const double dm = temp * (ws - un);
+  const double dm = temp * (ws - un), ti = temp * rinv;
   f[0] += wk * (temp - rho);
-  f[1] += wk * ((temp * u + dm * n[0]) - c[1]);
-  f[2] += wk * ((temp * v + dm * n[1]) - c[2]);
-  f[3] += wk * ((temp * w + dm * n[2]) - c[3]);
+  f[1] += wk * ((ti * c[1] + dm * n[0]) - c[1]);
+  f[2] += wk * ((ti * c[2] + dm * n[1]) - c[2]);
+  f[3] += wk * ((ti * c[3] + dm * n[2]) - c[3]);
   f[4] += wk * (es - e);
 }
 
+// (gamma + 1) / (2 gamma): the pressure ratio's weight in the wave-speed factor
+constexpr double kHllcQ = kGp1Over2 * kOneOverGamma;
+
 // HLLC from both sides' 1/rho, pressure and sound speed (p > 0 on both).
+// The wave speeds of hllc.hpp, u_n -/+ a_k q_k with
+// q_k = sqrt(1 + (gamma+1)/(2 gamma) (p*/p_k - 1)) for p* > p_k, are formed as
+// a_k q_k = sqrt(gamma / rho_k (p_k + (gamma+1)/(2 gamma) (p* - p_k))): the same
+// number without the reciprocal of p_k.
 template <bool FAST_SQRT>
 MCFD_HD void hllc_core(const double *cl, const double *cr, double il, double ir, double pl,
                        double pr, double al, double ar, const double *n, double *f) {
   const double rl = cl[0], rr = cr[0];
-  const double ul = cl[1] * il, vl = cl[2] * il, wl = cl[3] * il;
-  const double ur = cr[1] * ir, vr = cr[2] * ir, wr = cr[3] * ir;
-  const double unl = ul * n[0] + vl * n[1] + wl * n[2];
-  const double unr = ur * n[0] + vr * n[1] + wr * n[2];
+  const double mnl = cl[1] * n[0] + cl[2] * n[1] + cl[3] * n[2];
+  const double mnr = cr[1] * n[0] + cr[2] * n[1] + cr[3] * n[2];
+  const double unl = mnl * il, unr = mnr * ir;
   const double rho_average = (rl + rr) / 2, a_average = (al + ar) / 2;
   const double p_pvrs = (pl + pr - (unr - unl) * rho_average * a_average) / 2;
   // fmax(0, p_pvrs) and the wave-sign tests on the bit patterns (integer
   // pipes; the same results, NaN included)
   const double p_estimate = gt_zero(p_pvrs) ? p_pvrs : 0.0;
-  const double wave_left = unl - al * hllc_q_form<FAST_SQRT>(p_estimate, pl);
-  const double wave_right = unr + ar * hllc_q_form<FAST_SQRT>(p_estimate, pr);
+  double aql = al, aqr = ar;  // a_k q_k, q_k = 1 unless p* > p_k (both >= 0 here)
+  if (!le_nonneg(p_estimate, pl)) aql = sqrt_form<FAST_SQRT>(kGamma * il * fma(kHllcQ, p_estimate - pl, pl));
+  if (!le_nonneg(p_estimate, pr)) aqr = sqrt_form<FAST_SQRT>(kGamma * ir * fma(kHllcQ, p_estimate - pr, pr));
+  const double wave_left = unl - aql;
+  const double wave_right = unr + aqr;
   const double wave_star = (pr - pl + rl * unl * (wave_left - unl) - rr * unr * (wave_right - unr)) *
                            rcp_signed(rl * (wave_left - unl) - rr * (wave_right - unr));
   // The reference's four cases (left, right, left star, right star) pick a
@@ -693,8 +698,8 @@ MCFD_HD void hllc_core(const double *cl, const double *cr, double il, double ir,
   double cs[kK];
 #pragma unroll
   for (int k = 0; k < kK; ++k) cs[k] = left ? cl[k] : cr[k];
-  hllc_side_cons(cs, left ? il : ir, left ? ul : ur, left ? vl : vr, left ? wl : wr, left ? pl : pr,
-                 left ? unl : unr, n, star, left ? wave_left : wave_right, wave_star, f);
+  hllc_side_cons(cs, left ? il : ir, left ? pl : pr, left ? mnl : mnr, left ? unl : unr, n, star,
+                 left ? wave_left : wave_right, wave_star, f);
 }
 
 template <bool FAST_SQRT>
@@ -702,10 +707,11 @@ MCFD_HD bool flux_hllc_cons(const double *cl, const double *cr, const double *n,
   const double rl = cl[0], rr = cr[0];
   if (!bits_positive(rl) || !bits_positive(rr) || bits_negative(cl[4]) || bits_negative(cr[4])) return false;
   const double il = rcp_newton(rl), ir = rcp_newton(rr);
-  const double ul = cl[1] * il, vl = cl[2] * il, wl = cl[3] * il;
-  const double ur = cr[1] * ir, vr = cr[2] * ir, wr = cr[3] * ir;
-  const double pl = (cl[4] - rl * (0.5 * (ul * ul + vl * vl + wl * wl))) * kGm1;
-  const double pr = (cr[4] - rr * (0.5 * (ur * ur + vr * vr + wr * wr))) * kGm1;
+  // p = (E - |m|^2 / (2 rho)) (gamma - 1)
+  const double ml = cl[1] * cl[1] + cl[2] * cl[2] + cl[3] * cl[3];
+  const double mr = cr[1] * cr[1] + cr[2] * cr[2] + cr[3] * cr[3];
+  const double pl = fma(-0.5 * ml, il, cl[4]) * kGm1;
+  const double pr = fma(-0.5 * mr, ir, cr[4]) * kGm1;
   if (!bits_positive(pl) || !bits_positive(pr)) return false;
   const double al = sqrt_form<FAST_SQRT>(kGamma * pl * il), ar = sqrt_form<FAST_SQRT>(kGamma * pr * ir);
   hllc_core<FAST_SQRT>(cl, cr, il, ir, pl, pr, al, ar, n, f);
