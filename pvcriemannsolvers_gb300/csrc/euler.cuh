@@ -420,18 +420,21 @@ MCFD_HD void flux_rusanov_cons(const double *cl, const double *cr,
 // fluxes and |u.nh| + a|nh| = (w/2)(|u.n| + a), so
 //   w F_hat = F_L(nh) + F_R(nh) - lambda(nh) (U_R - U_L)
 // without the separate averaging and weighting multiplies.
+MCFD_HD bool rusanov_traced_nh(const double *cl, const double *trl, const double *cr,
+                               const double *trr, const double *nh, double hw, double *f);
+
 template <bool FAST_SQRT>
 MCFD_HD void flux_rusanov_cons_weighted(const double *cl, const double *cr,
                                         const double *n, double w, double *f) {
+  // both sides' {1/rho, p, sound speed} as the node traces form them, then the
+  // traced flux (summed side fluxes); a marked side (rho <= 0, E < 0 or
+  // p < 0) takes the primitive form
+  double trl[3], trr[3];
+  node_trace<FAST_SQRT>(cl, trl);
+  node_trace<FAST_SQRT>(cr, trr);
   const double hw = 0.5 * w;
   const double nh[3] = {hw * n[0], hw * n[1], hw * n[2]};
-  double fl[kK], fr[kK], sl[2], sr[2];
-  if (rusanov_side<FAST_SQRT>(cl, nh, fl, sl) && rusanov_side<FAST_SQRT>(cr, nh, fr, sr)) {
-    double lam = fmax(fma(sl[0], hw, sl[1]), fma(sr[0], hw, sr[1]));
-#pragma unroll
-    for (int k = 0; k < kK; ++k) f[k] = (fr[k] + fl[k]) - lam * (cr[k] - cl[k]);
-    return;
-  }
+  if (rusanov_traced_nh(cl, trl, cr, trr, nh, hw, f)) return;
   flux_rusanov(cons_to_prim(cl[0], cl[1], cl[2], cl[3], cl[4]),
                cons_to_prim(cr[0], cr[1], cr[2], cr[3], cr[4]), n, f);
 #pragma unroll
