@@ -831,6 +831,7 @@ const char *mcfd_last_error(const mcfd_handle *h) {
 
 int mcfd_create(const mcfd_mesh_desc *mesh, const mcfd_options *options,
                 mcfd_handle **out) {
+  mcfd::NvtxRange nvtx_range("mcfd_create");
   g_create_error.clear();
   if (!mesh || !options || !out) return fail(nullptr, MCFD_ERR_ARGUMENT, "null argument");
   *out = nullptr;
@@ -1084,12 +1085,14 @@ static int limit_current(mcfd_handle *h) {
 }
 
 int mcfd_set_solution(mcfd_handle *h, const double *column, int64_t n) {
+  mcfd::NvtxRange nvtx_range("mcfd_set_solution");
   if (!h) return MCFD_ERR_ARGUMENT;
   int rc = copy_column(h, h->buf.u, column, n, cudaMemcpyHostToDevice);
   return rc ? rc : limit_current(h);
 }
 
 int mcfd_limit(mcfd_handle *h, int64_t *troubled) {
+  mcfd::NvtxRange nvtx_range("mcfd_limit");
   if (!h) return MCFD_ERR_ARGUMENT;
   cudaSetDevice(h->device);
   int64_t before = 0, after = 0;
@@ -1200,6 +1203,7 @@ int mcfd_troubled_cells(mcfd_handle *h, int64_t *count) {
 }
 
 int mcfd_get_solution(mcfd_handle *h, double *column, int64_t n) {
+  mcfd::NvtxRange nvtx_range("mcfd_get_solution");
   if (!h) return MCFD_ERR_ARGUMENT;
   return copy_column(h, column, h->buf.u, n, cudaMemcpyDeviceToHost);
 }
@@ -1228,10 +1232,12 @@ static int residual_into(mcfd_handle *h, double *dst, int64_t n, cudaMemcpyKind 
 }
 
 int mcfd_residual(mcfd_handle *h, double *residual, int64_t n) {
+  mcfd::NvtxRange nvtx_range("mcfd_residual");
   return residual_into(h, residual, n, cudaMemcpyDeviceToHost);
 }
 
 int mcfd_residual_device(mcfd_handle *h, double *d_residual, int64_t n) {
+  mcfd::NvtxRange nvtx_range("mcfd_residual_device");
   return residual_into(h, d_residual, n, cudaMemcpyDeviceToDevice);
 }
 
@@ -1264,6 +1270,7 @@ int mcfd_residual_device_noalloc(mcfd_handle *h, const double *d_u,
 }
 
 int mcfd_time_step(mcfd_handle *h, double dt_guess, int32_t rk_order, double *dt) {
+  mcfd::NvtxRange nvtx_range("mcfd_time_step");
   if (!h || !dt) return MCFD_ERR_ARGUMENT;
   cudaSetDevice(h->device);
   double cfl = h->opt.cfl > 0 ? h->opt.cfl : cfl_table(rk_order, h->mesh.p);
@@ -1278,6 +1285,7 @@ int mcfd_time_step(mcfd_handle *h, double dt_guess, int32_t rk_order, double *dt
 }
 
 int mcfd_rk_step(mcfd_handle *h, double t, double dt, int32_t order) {
+  mcfd::NvtxRange nvtx_range("mcfd_rk_step");
   if (!h || order < 1 || order > 3) return h ? fail(h, MCFD_ERR_ARGUMENT, "order must be 1, 2 or 3") : MCFD_ERR_ARGUMENT;
   cudaSetDevice(h->device);
   h->launches += mcfd::launch_set_state(h, t, dt, dt, 0.0, 0);
@@ -1339,6 +1347,7 @@ static int ensure_job_graph(mcfd_handle *h, int b, int32_t n_steps, int32_t rk_o
 }
 
 int mcfd_advance(mcfd_handle *h, int32_t n_steps, double dt_guess, int32_t rk_order, double *t) {
+  mcfd::NvtxRange nvtx_range("mcfd_advance");
   if (!h || !t || n_steps < 0 || rk_order < 1 || rk_order > 3) return MCFD_ERR_ARGUMENT;
   cudaSetDevice(h->device);
   double cfl = h->opt.cfl > 0 ? h->opt.cfl : cfl_table(rk_order, h->mesh.p);
@@ -1389,6 +1398,7 @@ int mcfd_stream_begin(mcfd_handle *h) {
 
 int mcfd_stream_step(mcfd_handle *h, const double *host_in, double *host_out, int64_t n,
                      double t, int32_t n_steps, double dt_guess, int32_t rk_order) {
+  mcfd::NvtxRange nvtx_range("mcfd_stream_step");
   if (!h || !host_in || !host_out || n_steps < 1 || rk_order < 1 || rk_order > 3)
     return MCFD_ERR_ARGUMENT;
   if (!h->streamer.on) return fail(h, MCFD_ERR_STATE, "mcfd_stream_begin first");
@@ -1581,6 +1591,7 @@ const char *mcfd_ensemble_last_error(const mcfd_ensemble *e) {
 }
 
 int mcfd_ensemble_advance(mcfd_ensemble *e, int32_t n_steps, double dt_guess, int32_t rk_order) {
+  mcfd::NvtxRange nvtx_range("mcfd_ensemble_advance");
   if (!e || n_steps < 0 || rk_order < 1 || rk_order > 3) return MCFD_ERR_ARGUMENT;
   cudaSetDevice(e->device);
   // per-member step bounds, ordered before the replays
@@ -1649,6 +1660,7 @@ int mcfd_ensemble_stream_begin(mcfd_ensemble *e) {
 
 int mcfd_ensemble_stream_step(mcfd_ensemble *e, const double *const *host_in, double *const *host_out,
                               int32_t n_steps, double dt_guess, int32_t rk_order) {
+  mcfd::NvtxRange nvtx_range("mcfd_ensemble_stream_step");
   if (!e || !host_in || !host_out || n_steps < 1 || rk_order < 1 || rk_order > 3) return MCFD_ERR_ARGUMENT;
   if (!e->streaming) return ens_fail(e, MCFD_ERR_STATE, "mcfd_ensemble_stream_begin first");
   cudaSetDevice(e->device);
@@ -1816,6 +1828,7 @@ int mcfd_points(const mcfd_handle *h, double *xyz, int64_t n) {
 }
 
 int mcfd_project(mcfd_handle *h, const double *values, int64_t n) {
+  mcfd::NvtxRange nvtx_range("mcfd_project");
   if (!h || !values) return MCFD_ERR_ARGUMENT;
   if (h->opt.scheme != MCFD_MODAL)
     return fail(h, MCFD_ERR_UNSUPPORTED, "mcfd_project belongs to the modal scheme");

@@ -27,6 +27,26 @@ struct DeviceGuard {
   DeviceGuard &operator=(const DeviceGuard &) = delete;
 };
 
+// An NVTX range for the lifetime of a scope (the C-ABI calls open one named
+// after the call), so that a timeline tool shows the host phases around the
+// kernels and graph replays; a function-pointer test when no tool is attached.
+#if defined(__has_include)
+#if __has_include(<nvtx3/nvToolsExt.h>)
+#include <nvtx3/nvToolsExt.h>
+#define MCFD_HAVE_NVTX 1
+#endif
+#endif
+struct NvtxRange {
+#ifdef MCFD_HAVE_NVTX
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+#else
+  explicit NvtxRange(const char *) {}
+#endif
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
 // Device-side scalars of the time loop.  t and dt live on the device so a
 // whole step (dt reduction + 3 stages) runs without a host round trip.
 struct DevState {
