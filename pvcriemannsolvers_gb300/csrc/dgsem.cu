@@ -529,10 +529,19 @@ __device__ __forceinline__ void tc_differentiate(const float (*s_ft)[15][64], co
 
 // TC (Q = 4, dg::Lobatto only): the differentiation on the tensor cores
 // (tc_differentiate), everything else as the SIMT form.
-// (p = 3, SIMT: eight resident blocks per SM, 32 registers; measured 1.6 %
-// faster per launch than the unconstrained 48-register form on the 64^3 case)
+// Resident blocks per SM the compiler is held to: p = 3 SIMT eight (32
+// registers; 1.6 % faster per launch than its unconstrained 48 registers on
+// the 64^3 case); the other instances at the register counts they take
+// unconstrained (p = 2 and the tensor form 48, p = 1 40), since a looser
+// bound lets the compiler trade occupancy for registers (90 at p = 2, and
+// 66 % slower).
+template <int Q, bool TC>
+constexpr int mixed_cell_min_blocks() {
+  return Q == 4 ? (TC ? 5 : 8) : (Q == 3 ? 5 : 6);
+}
+
 template <int Q, int STAGE, bool TC = false>
-__global__ void __launch_bounds__(CellCfg<Q>::kThreads, (Q == 4 && !TC) ? 8 : 1)
+__global__ void __launch_bounds__(CellCfg<Q>::kThreads, mixed_cell_min_blocks<Q, TC>())
 cell_update_mixed_kernel(CellArgs a, const float *__restrict__ geo32) {
   constexpr int N = Q * Q * Q, QF = Q * Q, KN = kK * N;
   constexpr int CPB = CellCfg<Q>::kCells;
