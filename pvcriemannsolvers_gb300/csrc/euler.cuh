@@ -415,14 +415,14 @@ MCFD_HD void flux_rusanov_cons(const double *cl, const double *cr,
                cons_to_prim(cr[0], cr[1], cr[2], cr[3], cr[4]), n, f);
 }
 
+MCFD_HD bool rusanov_traced_nh(const double *cl, const double *trl, const double *cr,
+                               const double *trr, const double *nh, double hw, double *f);
+
 // w * Rusanov(n) for a unit normal n and face weight w > 0, evaluated with
 // the half-weighted normal nh = (w/2) n: F(nh) = (w/2) F(n) for the physical
 // fluxes and |u.nh| + a|nh| = (w/2)(|u.n| + a), so
 //   w F_hat = F_L(nh) + F_R(nh) - lambda(nh) (U_R - U_L)
 // without the separate averaging and weighting multiplies.
-MCFD_HD bool rusanov_traced_nh(const double *cl, const double *trl, const double *cr,
-                               const double *trr, const double *nh, double hw, double *f);
-
 template <bool FAST_SQRT>
 MCFD_HD void flux_rusanov_cons_weighted(const double *cl, const double *cr,
                                         const double *n, double w, double *f) {
