@@ -489,51 +489,90 @@ weno_reconstruct_kernel(WenoArgs a, const int32_t *list, const unsigned *count) 
   __syncthreads();
   const int n_adj = s_nadj;
   // Borrow: neighbour coefficients projected onto the own basis, shifted to
-  // the own average (weno.hpp:138-166, projection.hpp:260-264)
-  if (t < 6 * kK) {
-    const int slot = t / kK, k = t - slot * kK;
-    if (slot < n_adj) {
-      const int b = s_adj[slot];
-      const double *P = a.proj + ((c * 6 + slot) * M) * M;
-      const double *cb = a.modal + ((int64_t)b * kK + k) * M;
-      double cbl[M];
+  // the own average (weno.hpp:138-166, projection.hpp:260-264).  weno::Eigen
+  // (throughput-bound: many cells per SM) takes one thread per (neighbour,
+  // field) with the neighbour's coefficients in registers; the Lazy modes
+  // (every cell of small meshes: latency-bound) one thread per (neighbour,
+  // field, mode), ten times shorter dependent chains, the mode-0 thread
+  // applying the shift.
+  if constexpr (MODE == 3) {
+    if (t < 6 * kK) {
+      const int slot = t / kK, k = t - slot * kK;
+      if (slot < n_adj) {
+        const int b = s_adj[slot];
+        const double *P = a.proj + ((c * 6 + slot) * M) * M;
+        const double *cb = a.modal + ((int64_t)b * kK + k) * M;
+        double cbl[M];
 #pragma unroll
-      for (int j = 0; j < M; ++j) cbl[j] = cb[j];
+        for (int j = 0; j < M; ++j) cbl[j] = cb[j];
 #pragma unroll
-      for (int m = 0; m < M; ++m) {
+        for (int m = 0; m < M; ++m) {
+          double s = 0;
+#pragma unroll
+          for (int j = 0; j < M; ++j) s += cbl[j] * P[j * M + m];
+          s_cand[slot][k][m] = s;
+        }
+        const double s00 = a.s00[c];
+        const double my_avg = s_cand[6][k][0] * s00;
+        const double adj_avg = s_cand[slot][k][0] * s00;
+        s_cand[slot][k][0] += (my_avg - adj_avg) / s00;
+      }
+    }
+  } else {
+    for (int i = t; i < 6 * kK * M; i += blockDim.x) {
+      const int slot = i / (kK * M), r = i - slot * (kK * M), k = r / M, m = r - k * M;
+      if (slot < n_adj) {
+        const int b = s_adj[slot];
+        const double *P = a.proj + ((c * 6 + slot) * M) * M;
+        const double *cb = a.modal + ((int64_t)b * kK + k) * M;
         double s = 0;
 #pragma unroll
-        for (int j = 0; j < M; ++j) s += cbl[j] * P[j * M + m];
+        for (int j = 0; j < M; ++j) s += cb[j] * P[j * M + m];
+        if (m == 0) {
+          const double s00 = a.s00[c];
+          const double my_avg = s_cand[6][k][0] * s00;
+          const double adj_avg = s * s00;
+          s += (my_avg - adj_avg) / s00;
+        }
         s_cand[slot][k][m] = s;
       }
-      const double s00 = a.s00[c];
-      const double my_avg = s_cand[6][k][0] * s00;
-      const double adj_avg = s_cand[slot][k][0] * s00;
-      s_cand[slot][k][0] += (my_avg - adj_avg) / s00;
     }
   }
   __syncthreads();
   if constexpr (MODE == 3) {
     eigen_reconstruct<M>(a, c, n_adj, s_cand, s_new);
   } else {
+  // The phases are spread over the block so that the warps' FP64 lanes stay
+  // busy: the rows B c by (candidate, field, mode), the quadratic forms by
+  // (candidate, field), the weights by field, the new projection by (field,
+  // mode).
+  __shared__ double s_row[7][kK][M];
+  __shared__ double s_wt[kK][7];
   // smoothness indicators beta = c^T B c (weno.hpp:25-95)
+  const double *B = a.beta + c * M * M;
+  for (int i = t; i < 7 * kK * M; i += blockDim.x) {
+    const int slot = i / (kK * M), r = i - slot * (kK * M), k = r / M, m = r - k * M;
+    if (slot == 6 || slot < n_adj) {
+      double row = 0;
+#pragma unroll
+      for (int j = 0; j < M; ++j) row += B[m * M + j] * s_cand[slot][k][j];
+      s_row[slot][k][m] = row;
+    }
+  }
+  __syncthreads();
   if (t < 7 * kK) {
     const int slot = t / kK, k = t - slot * kK;
     if (slot == 6 || slot < n_adj) {
-      const double *B = a.beta + c * M * M;
       double b = 0;
 #pragma unroll
-      for (int m = 0; m < M; ++m) {
-        double row = 0;
-#pragma unroll
-        for (int j = 0; j < M; ++j) row += B[m * M + j] * s_cand[slot][k][j];
-        b += s_cand[slot][k][m] * row;
-      }
+      for (int m = 0; m < M; ++m) b += s_cand[slot][k][m] * s_row[slot][k][m];
       s_beta[slot][k] = b;
     }
   }
   __syncthreads();
-  // weights and the new projection (weno.hpp:167-194)
+  // weights (weno.hpp:167-194): w0 for the neighbours, 1 - n w0 for the own
+  // candidate, divided by (beta + eps)^2 and normalised per field (the
+  // divisions as Newton reciprocals)
   if (t < kK) {
     const int k = t;
     double w[7];
@@ -546,15 +585,19 @@ weno_reconstruct_kernel(WenoArgs a, const int32_t *list, const unsigned *count) 
     for (int s = 0; s <= n_adj; ++s) {
       double b = (s < n_adj ? s_beta[s][k] : s_beta[6][k]) + a.eps;
       b *= b;
-      w[s] /= b;
+      w[s] *= rcp_newton(b);
     }
     for (int s = 0; s <= n_adj; ++s) sum += w[s];
-    for (int s = 0; s <= n_adj; ++s) w[s] /= sum;
-    for (int m = 0; m < M; ++m) {
-      double v = s_cand[6][k][m] * w[n_adj];
-      for (int s = 0; s < n_adj; ++s) v += s_cand[s][k][m] * w[s];
-      s_new[k][m] = v;
-    }
+    const double isum = rcp_newton(sum);
+    for (int s = 0; s <= n_adj; ++s) s_wt[k][s] = w[s] * isum;
+  }
+  __syncthreads();
+  // the new projection (weno.hpp:182-194)
+  for (int i = t; i < kK * M; i += blockDim.x) {
+    const int k = i / M, m = i - k * M;
+    double v = s_cand[6][k][m] * s_wt[k][n_adj];
+    for (int s = 0; s < n_adj; ++s) v += s_cand[s][k][m] * s_wt[k][s];
+    s_new[k][m] = v;
   }
   }
   __syncthreads();
