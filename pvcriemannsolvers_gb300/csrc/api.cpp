@@ -169,7 +169,7 @@ void release(mcfd_handle *h) {
   auto &b = h->buf;
   void *ptrs[] = {m.cell_geo, m.cell_geo32, m.cell_rate, m.cell_rate32, m.cell_flux, m.face_cells,
                   m.face_group, m.face_geo, m.face_nh, m.face_xyz, m.face_map, m.dmat,
-                  m.bcs, m.corners, m.cell_type, b.u, b.u1, b.u2, b.res, b.flux, b.trace, b.state};
+                  m.bcs, m.corners, m.cell_type, b.u, b.u1, b.u2, b.res, b.flux, b.trace, b.state, b.dt_hi};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   auto &l = h->lim;
@@ -908,6 +908,8 @@ int mcfd_create(const mcfd_mesh_desc *mesh, const mcfd_options *options,
                     options->riemann == MCFD_HLLC);
     if (e == cudaSuccess && h->use_trace)
       e = cudaMalloc(&h->buf.trace, sizeof(double) * 3 * h->mesh.n_cells * h->mesh.n);
+    if (e == cudaSuccess && options->scheme != MCFD_MODAL && options->precision != MCFD_MIXED)
+      e = cudaMalloc(&h->buf.dt_hi, sizeof(unsigned) * ((h->mesh.n_cells * h->mesh.n + 127) / 128));
     if (e != cudaSuccess) rc = cuda_fail(h, e, "device allocation");
   }
   if (rc) {

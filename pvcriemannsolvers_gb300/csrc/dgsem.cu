@@ -756,6 +756,153 @@ dt_reduce_kernel(const double *u, const double *cell_rate, int64_t n_nodes,
   reduce_rate(rate, (case_rate && gid < n_nodes) ? cell_case[gid / N] : -1, state, case_rate);
 }
 
+// ---- FP64 time step at FP32 cost: the exact FP64 maximum of the rates is
+// found in two passes.  Pass 1 brackets every node's rate [lo, hi] in FP32
+// interval arithmetic (directed roundings), reduces max(lo) into the handle's
+// (or the case's) rate word and stores each block's max(hi).  Pass 2 reads
+// that word as a threshold: a block whose max(hi) is below it returns at
+// once, without reading the solution; in the other blocks a node forms the
+// FP64 rate, with exactly dt_reduce_kernel's arithmetic, when its own hi is
+// not below the threshold, and those rates reduce into the same word.  The
+// node of the largest FP64 rate always passes (its hi is above its rate,
+// which is above every lo), every value the word holds during pass 2 is at
+// most that rate, and a node that fails the test has a rate below it, so the
+// word ends at the same FP64 maximum as dt_reduce_kernel's.  Nodes whose
+// bracket is uncertain (a value above the FP32 range, a density or energy the
+// clamp might zero, a pressure that cancels to below 2^-20 of the energy)
+// take hi = +inf and always pass.
+
+// [lo, hi] in FP32 around a double: the magnitude truncated and, unless
+// exact, the next float up; below the normal FP32 range [0, FLT_MIN] with the
+// sign.  False above the FP32 range (and for infinities and NaN).
+__device__ __forceinline__ bool f32_bracket(double x, float *lo, float *hi) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned h = (unsigned)(b >> 32), l = (unsigned)b;
+  const unsigned e = (h >> 20) & 0x7ffu;
+  if (e >= 1151u) return false;
+  float t = 0.f, tu = 0.f;
+  if ((b << 1) == 0ull) {
+  } else if (e <= 896u) {
+    tu = __uint_as_float(0x00800000u);  // FLT_MIN
+  } else {
+    const unsigned mag = ((e - 896u) << 23) | ((h & 0xfffffu) << 3) | (l >> 29);
+    t = __uint_as_float(mag);
+    tu = (l & 0x1fffffffu) == 0u ? t : __uint_as_float(mag + 1u);
+  }
+  if (h & 0x80000000u) {
+    *lo = -tu;
+    *hi = -t;
+  } else {
+    *lo = t;
+    *hi = tu;
+  }
+  return true;
+}
+
+// FP32 bounds of the FP64 rate max(|u| + c, 1e-5) * cell_rate of a node;
+// false when the node must take the FP64 path.  The FP64 arithmetic (one
+// Newton reciprocal, products, two square roots) stays within 2^-30 relative
+// of the exact rate once the pressure does not cancel below 2^-20 of the
+// energy, and the bounds are widened by 2^-20 relative on top of that.
+__device__ __forceinline__ bool rate_bracket(const double *p, double cell_rate, float *lo, float *hi) {
+  // the double constants gamma - 1 = 0.4, gamma = 1.4 and 1e-5 bracketed
+  const float g1l = __uint_as_float(0x3ecccccc), g1h = __uint_as_float(0x3ecccccd);
+  const float gl = __uint_as_float(0x3fb33333), gh = __uint_as_float(0x3fb33334);
+  const float fl = __uint_as_float(0x3727c5ac), fh = __uint_as_float(0x3727c5ad);
+  constexpr float kTol = 9.5367431640625e-7f;  // 2^-20
+  float rl, rh, el, eh, crl, crh;
+  if (!f32_bracket(p[0], &rl, &rh) || !f32_bracket(p[4], &el, &eh) || !f32_bracket(cell_rate, &crl, &crh))
+    return false;
+  if (!(rl > 0.f) || !(el >= 0.f) || !(crl > 0.f)) return false;
+  float m2l = 0.f, m2h = 0.f;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    float ml, mh;
+    if (!f32_bracket(p[1 + d], &ml, &mh)) return false;
+    const float al = ml >= 0.f ? ml : (mh <= 0.f ? -mh : 0.f);
+    const float ah = fmaxf(-ml, mh);
+    m2l = __fadd_rd(m2l, __fmul_rd(al, al));
+    m2h = __fadd_ru(m2h, __fmul_ru(ah, ah));
+  }
+  const float irl = __frcp_rd(rh), irh = __frcp_ru(rl);  // bounds of 1 / rho
+  const float kel = __fmul_rd(__fmul_rd(m2l, 0.5f), irl), keh = __fmul_ru(__fmul_ru(m2h, 0.5f), irh);
+  const float pl = __fmul_rd(__fsub_rd(el, keh), g1l), ph = __fmul_ru(__fsub_ru(eh, kel), g1h);
+  if (!(pl > __fmul_ru(__fadd_ru(eh, keh), kTol))) return false;
+  const float c2l = __fmul_rd(__fmul_rd(gl, pl), irl), c2h = __fmul_ru(__fmul_ru(gh, ph), irh);
+  const float ul = __fmul_rd(__fsqrt_rd(m2l), irl), uh = __fmul_ru(__fsqrt_ru(m2h), irh);
+  const float sl = fmaxf(__fadd_rd(__fsqrt_rd(c2l), ul), fl);
+  const float sh = fmaxf(__fadd_ru(__fsqrt_ru(c2h), uh), fh);
+  *lo = __fmul_rd(__fmul_rd(sl, crl), 1.f - kTol);
+  *hi = __fmul_ru(__fmul_ru(sh, crh), 1.f + kTol);
+  return true;
+}
+
+template <int Q>
+__global__ void __launch_bounds__(512)
+dt_bound_kernel(const double *u, const double *cell_rate, int64_t n_nodes, DevState *state,
+                const int32_t *cell_case, unsigned long long *case_rate, unsigned *block_hi) {
+  constexpr int N = Q * Q * Q;
+  __shared__ unsigned s_hi[16];
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double lo64 = 0;
+  unsigned hib = 0u;
+  if (gid < n_nodes) {
+    float lo, hi;
+    if (rate_bracket(u + gid * kK, cell_rate[gid / N], &lo, &hi)) {
+      lo64 = f32_to_f64(lo);
+      hib = __float_as_uint(hi);
+    } else {
+      hib = 0x7f800000u;  // +inf
+    }
+  }
+  // the block's max(hi): non-negative floats order as their bit patterns
+  hib = __reduce_max_sync(0xffffffffu, hib);
+  if ((threadIdx.x & 31) == 0) s_hi[threadIdx.x >> 5] = hib;
+  reduce_rate(lo64, (case_rate && gid < n_nodes) ? cell_case[gid / N] : -1, state, case_rate);
+  // reduce_rate's barrier orders the s_hi writes before this read
+  if (threadIdx.x == 0) {
+    unsigned m = 0u;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = max(m, s_hi[w]);
+    block_hi[blockIdx.x] = m;
+  }
+}
+
+template <int Q>
+__global__ void __launch_bounds__(512)
+dt_exact_kernel(const double *u, const double *cell_rate, int64_t n_nodes, DevState *state,
+                const int32_t *cell_case, unsigned long long *case_rate, const unsigned *block_hi) {
+  constexpr int N = Q * Q * Q;
+  __shared__ int s_skip;
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const double bh = f32_to_f64(__uint_as_float(block_hi[blockIdx.x]));
+  if (!case_rate) {
+    // one decision for the block (the word may grow while its threads read it)
+    if (threadIdx.x == 0)
+      s_skip = bh < __longlong_as_double((long long)*(volatile const unsigned long long *)&state->max_rate_bits);
+    __syncthreads();
+    if (s_skip) return;
+  }
+  double rate = 0;
+  int key = -1;
+  if (gid < n_nodes) {
+    if (case_rate) key = cell_case[gid / N];
+    const unsigned long long *word = case_rate ? &case_rate[key] : &state->max_rate_bits;
+    const double threshold = __longlong_as_double((long long)*(volatile const unsigned long long *)word);
+    if (!(bh < threshold)) {
+      const double *p = u + gid * kK;
+      const double cr = cell_rate[gid / N];
+      float lo, hi;
+      if (!rate_bracket(p, cr, &lo, &hi) || !(f32_to_f64(hi) < threshold)) {
+        Prim w = cons_to_prim(p[0], p[1], p[2], p[3], p[4]);
+        double c = sound_speed(w);
+        double speed = c + sqrt(w.u * w.u + w.v * w.v + w.w * w.w);
+        rate = fmax(speed, 1e-5) * cr;
+      }
+    }
+  }
+  reduce_rate(rate, key, state, case_rate);
+}
+
 // Mixed-precision dt reduction: wave speeds and rates in FP32 (the FP32 copy
 // of the cell rates), the state converted by mantissa truncation on the
 // integer pipes (the hardware conversion issues on the FP64 unit, the
@@ -1057,11 +1204,25 @@ int launch_dt(mcfd_handle *h, const double *u) {
       default: dt_reduce_mixed_kernel<4><<<blocks, bs, 0, h->stream>>>(u, m.cell_rate32, nodes, h->buf.state, cc, cr); break;
     }
   } else {
+    // the exact FP64 maximum in two passes (FP32 brackets, then FP64 only
+    // for the nodes that can hold it); buf.dt_hi holds a word per block of
+    // at least 128 threads
+    unsigned *bh = h->buf.dt_hi;
     switch (m.q) {
-      case 2: dt_reduce_kernel<2><<<blocks, bs, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr); break;
-      case 3: dt_reduce_kernel<3><<<blocks, bs, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr); break;
-      default: dt_reduce_kernel<4><<<blocks, bs, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr); break;
+      case 2:
+        dt_bound_kernel<2><<<blocks, bs, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr, bh);
+        dt_exact_kernel<2><<<blocks, bs, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr, bh);
+        break;
+      case 3:
+        dt_bound_kernel<3><<<blocks, bs, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr, bh);
+        dt_exact_kernel<3><<<blocks, bs, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr, bh);
+        break;
+      default:
+        dt_bound_kernel<4><<<blocks, bs, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr, bh);
+        dt_exact_kernel<4><<<blocks, bs, 0, h->stream>>>(u, m.cell_rate, nodes, h->buf.state, cc, cr, bh);
+        break;
     }
+    return 2 + launch_dt_finalize(h);
   }
   return 1 + launch_dt_finalize(h);
 }

@@ -317,6 +317,9 @@ struct Buffers {
   // state, read by the next face kernel instead of recomputing per face point
   double *trace = nullptr;
   DevState *state = nullptr;
+  // FP64 nodal forms: the FP32 upper bound of each dt block's largest rate
+  // (one word per 128 nodes), from the first pass of the two-pass dt
+  unsigned *dt_hi = nullptr;
 };
 
 struct Options {

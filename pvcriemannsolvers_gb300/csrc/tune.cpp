@@ -51,8 +51,11 @@ bool load_cached(const char *path, const std::string &key, mcfd::Tune *t) {
   std::string line;
   while (std::getline(in, line)) {
     if (line.find(tag) == std::string::npos) continue;
-    t->face_block = read_int(line, "face_block", t->face_block);
-    t->dt_block = read_int(line, "dt_block", t->dt_block);
+    // block sizes other than the tuner's own (a damaged file) keep the defaults:
+    // the dt kernels' per-block words assume 128 to 512 threads
+    const auto block = [](int v, int fallback) { return (v == 128 || v == 256 || v == 512) ? v : fallback; };
+    t->face_block = block(read_int(line, "face_block", t->face_block), t->face_block);
+    t->dt_block = block(read_int(line, "dt_block", t->dt_block), t->dt_block);
     t->limiter_blocks_per_sm = read_int(line, "limiter_blocks_per_sm", t->limiter_blocks_per_sm);
     return true;
   }
