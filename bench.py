@@ -335,8 +335,8 @@ def measure_form(args, torch, dist, dev, local_rank, m, u0, precision, contracti
 # 40^3 p = 3 case (64 000 cells); scaled linearly with the cell count.  Mixed
 # form: the traced face kernel and the cell kernel writing the node traces.
 NCU_TRAFFIC_40 = {
-    ("mixed", "face_flux"): 380.940800e6 + 50.558464e6,
-    ("mixed", "cell_update"): 594.870272e6 + 226.026496e6,  # the RK3 middle stage
+    ("mixed", "face_flux"): 380.926720e6 + 50.025984e6,
+    ("mixed", "cell_update"): 591.940608e6 + 229.314048e6,  # the RK3 last stage
 }
 NCU_CELLS = 40 ** 3
 
@@ -418,10 +418,10 @@ def roofline_of(kt, L, cells, hbm_peak, peak_src, fp64_peak, precision):
 # instruction stream (conversions, node traces, positivity), which is what
 # binds the kernel.
 NCU_PIPE_40 = {
-    ("mixed", "cell_update"): {"sm__pipe_fp64_cycles_active_pct": 74.2, "issue_active_pct": 34.6,
-                               "source": "ncu --set full, 40^3 p = 3 case"},
-    ("mixed", "face_flux"): {"sm__pipe_fp64_cycles_active_pct": 87.9, "issue_active_pct": 13.4,
-                             "source": "ncu --set full, 40^3 p = 3 case"},
+    ("mixed", "cell_update"): {"sm__pipe_fp64_cycles_active_pct": 80.1, "issue_active_pct": 50.4,
+                               "source": "ncu --metrics, 40^3 p = 3 case, RK3 last stage"},
+    ("mixed", "face_flux"): {"sm__pipe_fp64_cycles_active_pct": 89.4, "issue_active_pct": 17.0,
+                             "source": "ncu --metrics, 40^3 p = 3 case"},
 }
 
 

@@ -76,7 +76,7 @@ __device__ __forceinline__ void store_flux(double *flux, int f32_out, int64_t gi
     float *d = reinterpret_cast<float *>(flux) + gid * kK;
 #pragma unroll
     for (int k = 0; k < kK; ++k) d[k] = f64_to_f32(v[k]);
-    if ((unsigned long long)__double_as_longlong(v[0]) == kNoFluxBits) d[0] = __uint_as_float(kNoFluxBits32);
+    if (bits64(v[0]) == kNoFluxBits) d[0] = __uint_as_float(kNoFluxBits32);
   } else {
     double *d = flux + gid * kK;
 #pragma unroll
@@ -366,7 +366,7 @@ cell_update_kernel(CellArgs a) {
     if (v == INT32_MIN) return;
     const double *fl = a.flux + (int64_t)(v >= 0 ? v : ~v) * kK;
     if (a.fr) {
-      if ((unsigned long long)__double_as_longlong(fl[0]) == kNoFluxBits) return;  // no boundary
+      if (bits64(fl[0]) == kNoFluxBits) return;  // no boundary
       const int dir = fr_dir(side);
       const double sigma = fr_sign(side), out_sign = v >= 0 ? 1.0 : -1.0;
 #pragma unroll
@@ -649,7 +649,7 @@ cell_update_mixed_kernel(CellArgs a, const float *__restrict__ geo32) {
       const double *fd = a.flux + slot;
 #pragma unroll
       for (int rr = 0; rr < kK; ++rr) fl[rr] = f64_to_f32(fd[rr]);
-      no_flux = (unsigned long long)__double_as_longlong(fd[0]) == kNoFluxBits;
+      no_flux = bits64(fd[0]) == kNoFluxBits;
     } else {
       const float *fs = reinterpret_cast<const float *>(a.flux) + slot;
 #pragma unroll
@@ -721,7 +721,7 @@ cell_update_mixed_kernel(CellArgs a, const float *__restrict__ geo32) {
 // FP32 rates of the mixed form are widened exactly first)
 __device__ __forceinline__ void reduce_rate(double rate, int key, DevState *state,
                                             unsigned long long *case_rate) {
-  block_max_bits((unsigned long long)__double_as_longlong(rate), key, &state->max_rate_bits, case_rate);
+  block_max_bits(bits64(rate), key, &state->max_rate_bits, case_rate);
 }
 
 // FP64 -> FP32 by truncating the mantissa (|result| within 2^-23 below |x|),
@@ -729,7 +729,7 @@ __device__ __forceinline__ void reduce_rate(double rate, int key, DevState *stat
 // estimate.  Magnitudes below the normal FP32 range give a signed zero, above
 // it (and infinities, NaN) a signed infinity.
 __device__ __forceinline__ float f64_to_f32_trunc(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long b = bits64(x);
   const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
   const unsigned e = (hi >> 20) & 0x7ffu;
   unsigned bits = ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
@@ -776,7 +776,7 @@ dt_reduce_kernel(const double *u, const double *cell_rate, int64_t n_nodes,
 // exact, the next float up; below the normal FP32 range [0, FLT_MIN] with the
 // sign.  False above the FP32 range (and for infinities and NaN).
 __device__ __forceinline__ bool f32_bracket(double x, float *lo, float *hi) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long b = bits64(x);
   const unsigned h = (unsigned)(b >> 32), l = (unsigned)b;
   const unsigned e = (h >> 20) & 0x7ffu;
   if (e >= 1151u) return false;

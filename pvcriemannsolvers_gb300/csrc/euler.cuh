@@ -78,30 +78,43 @@ MCFD_HD Prim make_prim(double rho, double u, double v, double w, double p) {
 // x < 0, x > 0 and x != 0 with IEEE results (-0, infinities, NaN) decided on
 // the bit pattern: on the device these run on the integer pipes instead of
 // taking FP64 compare slots on the FP64 unit, which bounds the FP64 kernels.
+#ifdef __CUDACC__
+// The bit pattern of x through an opaque move: the integer tests below stay
+// integer operations instead of being folded back into FP64 compares, which
+// would issue on the FP64 pipe.
+__device__ __forceinline__ unsigned long long bits64(double x) {
+#ifdef __CUDA_ARCH__
+  unsigned long long r;
+  asm("mov.b64 %0, %1;" : "=l"(r) : "d"(x));
+  return r;
+#else
+  return (unsigned long long)__double_as_longlong(x);
+#endif
+}
+#endif
 #ifdef __CUDA_ARCH__
 __device__ __forceinline__ bool lt_zero(double x) {
   // negative finite or -inf: bit patterns 0x8000000000000001 .. 0xfff0000000000000
-  return (unsigned long long)__double_as_longlong(x) - 0x8000000000000001ull < 0x7ff0000000000000ull;
+  return bits64(x) - 0x8000000000000001ull < 0x7ff0000000000000ull;
 }
 __device__ __forceinline__ bool gt_zero(double x) {
   // positive finite or +inf: 0x0000000000000001 .. 0x7ff0000000000000
-  return (unsigned long long)__double_as_longlong(x) - 1ull < 0x7ff0000000000000ull;
+  return bits64(x) - 1ull < 0x7ff0000000000000ull;
 }
-__device__ __forceinline__ bool ne_zero(double x) { return (__double_as_longlong(x) << 1) != 0; }
+__device__ __forceinline__ bool ne_zero(double x) { return (bits64(x) << 1) != 0; }
 __device__ __forceinline__ bool ge_zero(double x) {
   // +0 .. +inf, or -0
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long b = bits64(x);
   return b <= 0x7ff0000000000000ull || b == 0x8000000000000000ull;
 }
 __device__ __forceinline__ bool le_zero(double x) {
   // -0 .. -inf, or +0
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long b = bits64(x);
   return b - 0x8000000000000000ull <= 0x7ff0000000000000ull || b == 0ull;
 }
 // a <= b for a, b >= 0 (either zero's sign), compared as unsigned integers
 __device__ __forceinline__ bool le_nonneg(double a, double b) {
-  return ((unsigned long long)__double_as_longlong(a) & 0x7fffffffffffffffull) <=
-         ((unsigned long long)__double_as_longlong(b) & 0x7fffffffffffffffull);
+  return (bits64(a) & 0x7fffffffffffffffull) <= (bits64(b) & 0x7fffffffffffffffull);
 }
 #else
 inline bool lt_zero(double x) { return x < 0; }
@@ -175,7 +188,7 @@ MCFD_HD void normal_flux(const Prim &w, double e, const double *n, double un,
 // round to nearest even, subnormal results flushed to a signed zero,
 // overflow to infinity, NaN kept NaN.
 __device__ __forceinline__ float f64_to_f32(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long b = bits64(x);
   const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
   const int ex = (int)((b >> 52) & 0x7ff);
   const int e = ex - (1023 - 127);
@@ -201,23 +214,23 @@ __device__ __forceinline__ double f32_to_f64(float f) {
 
 // x != 0 on the bit pattern.
 __device__ __forceinline__ bool nonzero64(double x) {
-  return (__double_as_longlong(x) << 1) != 0;
+  return (bits64(x) << 1) != 0;
 }
 
 // x < 0 for a finite or infinite double, tested on the bit pattern.
 __device__ __forceinline__ bool negative64(double x) {
-  const long long b = __double_as_longlong(x);
+  const long long b = (long long)bits64(x);
   return b < 0 && (b << 1) != 0;
 }
 
 // isfinite on the bit pattern (exponent field not all ones).
 __device__ __forceinline__ bool finite64(double x) {
-  return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff;
+  return ((bits64(x) >> 52) & 0x7ff) != 0x7ff;
 }
 
 #ifdef __CUDA_ARCH__
 __device__ __forceinline__ double rcp_newton(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long b = bits64(x);
   const int e = (int)((b >> 52) & 0x7ff) - (1023 - 127);
   if (e <= 1 || e >= 253) return 1.0 / x;
   const unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
@@ -236,7 +249,7 @@ __device__ __forceinline__ double rcp_newton(double x) {
 // square of the FP32 seed's 1.8e-7): the mixed form's node traces, where the
 // seeded square root beside it carries 1.4e-13.
 __device__ __forceinline__ double rcp_newton1(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long b = bits64(x);
   const int e = (int)((b >> 52) & 0x7ff) - (1023 - 127);
   if (e <= 1 || e >= 253) return 1.0 / x;
   const unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
@@ -251,36 +264,50 @@ __device__ __forceinline__ double rcp_newton1(double x) {
 // Square root for the mixed form's wave speed: one Newton-Raphson step on
 // the reciprocal square root, y <- y + y (1 - x y^2) / 2, from the FP32
 // hardware estimate of 1/sqrt(x) (relative error below 3e-7, so ~1.4e-13
-// after the step), then sqrt(x) = x y.  Outside the normal FP32 range the
-// FP64 square root is used.
+// after the step), then sqrt(x) = x y.  Written on t = x y0:
+//   sqrt(x) = t + t (1/2 - t y0 / 2),
+// three FP64 operations, with -y0/2 scaled in FP32 (exact) before its
+// conversion.  Outside the normal FP32 range the FP64 square root is used.
 __device__ __forceinline__ double sqrt_seeded(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long b = bits64(x);
   const int e = (int)((b >> 52) & 0x7ff) - (1023 - 127);
   if (e <= 1 || e >= 253) return sqrt(x);
   const unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
   const float xf = __uint_as_float(((unsigned)e << 23) + (unsigned)(mant >> 29));
-  const unsigned yb = __float_as_uint(rsqrtf(xf));
-  const unsigned ye = (yb >> 23) & 0xffu;
+  const float yf = rsqrtf(xf);
+  // both normal: 1/sqrt(x) of a normal x in [2^-125, 2^126) is within [2^-63, 2^63)
+  const unsigned yb = __float_as_uint(yf), hb = __float_as_uint(-0.5f * yf);
   const double y0 = __longlong_as_double((long long)(
-      ((unsigned long long)(ye + (1023u - 127u)) << 52) |
+      ((unsigned long long)(((yb >> 23) & 0xffu) + (1023u - 127u)) << 52) |
       ((unsigned long long)(yb & 0x7fffffu) << 29)));
-  const double r = fma(-(x * y0), y0, 1.0);
-  const double y1 = fma(y0 * r, 0.5, y0);
-  return x * y1;
+  const double yh = __longlong_as_double((long long)(
+      0x8000000000000000ull |
+      ((unsigned long long)(((hb >> 23) & 0xffu) + (1023u - 127u)) << 52) |
+      ((unsigned long long)(hb & 0x7fffffu) << 29)));
+  const double t = x * y0;
+  return fma(t, fma(t, yh, 0.5), t);
 }
 
 // Sign tests on the bit patterns (integer pipes): x > 0 and x < 0 for
 // finite or infinite x.
-__device__ __forceinline__ bool bits_positive(double x) { return __double_as_longlong(x) > 0; }
+__device__ __forceinline__ bool bits_positive(double x) { return (long long)bits64(x) > 0; }
+// |x| by clearing the sign bit of the high word (an integer operation, where
+// fabs feeding an FMA's addend issues on the FP64 pipe)
+__device__ __forceinline__ double abs_bits(double x) {
+  double r;
+  asm("{\n\t.reg .b32 lo, hi;\n\tmov.b64 {lo, hi}, %1;\n\tand.b32 hi, hi, 0x7fffffff;\n\t"
+      "mov.b64 %0, {lo, hi};\n\t}" : "=d"(r) : "d"(x));
+  return r;
+}
 __device__ __forceinline__ bool bits_negative(double x) {
-  const long long b = __double_as_longlong(x);
+  const long long b = (long long)bits64(x);
   return b < 0 && (b << 1) != 0;
 }
 // 1/x of either sign: rcp_newton of |x| with x's sign.
 __device__ __forceinline__ double rcp_signed(double x) {
-  const long long b = __double_as_longlong(x);
+  const long long b = (long long)bits64(x);
   const double y = rcp_newton(__longlong_as_double(b & 0x7fffffffffffffffll));
-  return __longlong_as_double(__double_as_longlong(y) ^ (b & (long long)0x8000000000000000ull));
+  return __longlong_as_double((long long)bits64(y) ^ (b & (long long)0x8000000000000000ull));
 }
 #else
 inline double rcp_newton(double x) { return 1.0 / x; }
@@ -288,6 +315,7 @@ inline double rcp_newton1(double x) { return 1.0 / x; }
 inline double rcp_signed(double x) { return 1.0 / x; }
 inline double sqrt_seeded(double x) { return std::sqrt(x); }
 inline bool bits_positive(double x) { return x > 0; }
+inline double abs_bits(double x) { return std::fabs(x); }
 inline bool bits_negative(double x) { return x < 0; }
 #endif
 
@@ -458,7 +486,7 @@ MCFD_HD bool rusanov_traced_nh(const double *cl, const double *trl, const double
   const double mnl = cl[1] * nh[0] + cl[2] * nh[1] + cl[3] * nh[2];
   const double mnr = cr[1] * nh[0] + cr[2] * nh[1] + cr[3] * nh[2];
   const double unl = mnl * trl[0], unr = mnr * trr[0];
-  const double sl = fma(trl[2], hw, fabs(unl)), sr = fma(trr[2], hw, fabs(unr));
+  const double sl = fma(trl[2], hw, abs_bits(unl)), sr = fma(trr[2], hw, abs_bits(unr));
   const double lam = le_nonneg(sr, sl) ? sl : sr;
   const double al = unl + lam, ar = unr - lam;
   const double ps = pl + pr;

@@ -323,7 +323,7 @@ __device__ __forceinline__ void reduce_cell_rate(double rate, int64_t c, int64_t
                                                  DevState *state, const int32_t *cell_case,
                                                  unsigned long long *case_rate) {
   // (rates are >= 1e-5 / length, or 0 for idle lanes: never negative or NaN)
-  block_max_bits((unsigned long long)__double_as_longlong(rate),
+  block_max_bits(bits64(rate),
                  (case_rate && c < n_cells) ? cell_case[c] : -1, &state->max_rate_bits, case_rate);
 }
 

@@ -317,7 +317,7 @@ __global__ void __launch_bounds__(32 * kWarps) visc_properties_kernel(PropArgs a
     }
     a.nu[c * kK + k] = val;
   }
-  if (a.dt_mode) atomicMin(&a.state->min_dt_bits, (unsigned long long)__double_as_longlong(min_dt));
+  if (a.dt_mode) atomicMin(&a.state->min_dt_bits, bits64(min_dt));
 }
 
 struct ViscFaceArgs {
