@@ -167,7 +167,7 @@ void release(mcfd_handle *h) {
   stream_release(h);
   auto &m = h->mesh;
   auto &b = h->buf;
-  void *ptrs[] = {m.cell_geo, m.cell_geo32, m.cell_rate, m.cell_rate32, m.cell_flux, m.face_cells,
+  void *ptrs[] = {m.cell_geo, m.cell_geo32, m.node_w32, m.cell_rate, m.cell_rate32, m.cell_flux, m.face_cells,
                   m.face_group, m.face_geo, m.face_nh, m.face_xyz, m.face_map, m.dmat,
                   m.bcs, m.corners, m.cell_type, b.u, b.u1, b.u2, b.res, b.flux, b.trace, b.state, b.dt_hi};
   for (void *p : ptrs)
@@ -308,6 +308,11 @@ int build_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
   // ---- per node geometry
   std::vector<double> geo((size_t)d->n_cells * N * 10);
   std::vector<double> rate(d->n_cells);
+  // per cell adj(J) and det(J) at its first node, and whether every node of
+  // the cell has the same ones (an affine cell: the mixed form then stores its
+  // FP32 metric terms once per cell)
+  std::vector<double> adj0((size_t)d->n_cells * 10);
+  std::vector<uint8_t> affine(d->n_cells, 1);
   int bad_jac = 0;
 #pragma omp parallel for schedule(static)
   for (int64_t c = 0; c < d->n_cells; ++c) {
@@ -330,16 +335,24 @@ int build_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
           const bool fr = h->opt.scheme == MCFD_FR;
           double s = fr ? 1.0 : w / det;
           double *g = &geo[((size_t)c * N + (i * Q + j) * Q + k) * 10];
-          g[0] = s * (J[4] * J[8] - J[5] * J[7]);
-          g[1] = s * (J[2] * J[7] - J[1] * J[8]);
-          g[2] = s * (J[1] * J[5] - J[2] * J[4]);
-          g[3] = s * (J[5] * J[6] - J[3] * J[8]);
-          g[4] = s * (J[0] * J[8] - J[2] * J[6]);
-          g[5] = s * (J[2] * J[3] - J[0] * J[5]);
-          g[6] = s * (J[3] * J[7] - J[4] * J[6]);
-          g[7] = s * (J[1] * J[6] - J[0] * J[7]);
-          g[8] = s * (J[0] * J[4] - J[1] * J[3]);
+          const double adj[9] = {J[4] * J[8] - J[5] * J[7], J[2] * J[7] - J[1] * J[8],
+                                 J[1] * J[5] - J[2] * J[4], J[5] * J[6] - J[3] * J[8],
+                                 J[0] * J[8] - J[2] * J[6], J[2] * J[3] - J[0] * J[5],
+                                 J[3] * J[7] - J[4] * J[6], J[1] * J[6] - J[0] * J[7],
+                                 J[0] * J[4] - J[1] * J[3]};
+          for (int e = 0; e < 9; ++e) g[e] = s * adj[e];
           g[9] = fr ? 1.0 / det : 1.0 / w;
+          double *a0 = &adj0[(size_t)c * 10];
+          if (i == 0 && j == 0 && k == 0) {
+            for (int e = 0; e < 9; ++e) a0[e] = adj[e];
+            a0[9] = det;
+          } else {
+            double scale = 0;
+            for (int e = 0; e < 9; ++e) scale = std::max(scale, std::fabs(a0[e]));
+            for (int e = 0; e < 9; ++e)
+              if (std::fabs(adj[e] - a0[e]) > 1e-13 * scale) affine[c] = 0;
+            if (std::fabs(det - a0[9]) > 1e-13 * std::fabs(a0[9])) affine[c] = 0;
+          }
         }
     rate[c] = 1.0 / (std::cbrt(volume) * 0.5);
   }
@@ -528,11 +541,35 @@ int build_mesh(mcfd_handle *h, const mcfd_mesh_desc *d, int degree) {
   // ---- upload
   int rc;
   if (h->opt.precision == MCFD_MIXED) {
-    std::vector<float> geo32((size_t)d->n_cells * N * 10);
+    m.geo32_affine = d->n_cells > 0;
+    for (int64_t c = 0; c < d->n_cells && m.geo32_affine; ++c) m.geo32_affine = affine[c] != 0;
+    if (m.geo32_affine) {
+      // per cell adj(J) and 1/det(J); per node w_q and 1/w_q (DGSEM: the
+      // node's metric terms are w_q adj(J) and 1/(w_q det(J))) or 1 (FR)
+      std::vector<float> geo32((size_t)d->n_cells * 10);
 #pragma omp parallel for schedule(static)
-    for (int64_t i = 0; i < d->n_cells * N; ++i)
-      for (int e = 0; e < 10; ++e) geo32[(size_t)i * 10 + e] = (float)geo[(size_t)i * 10 + e];
-    if ((rc = upload(h, &m.cell_geo32, geo32))) return rc;
+      for (int64_t c = 0; c < d->n_cells; ++c) {
+        for (int e = 0; e < 9; ++e) geo32[(size_t)c * 10 + e] = (float)adj0[(size_t)c * 10 + e];
+        geo32[(size_t)c * 10 + 9] = (float)(1.0 / adj0[(size_t)c * 10 + 9]);
+      }
+      if ((rc = upload(h, &m.cell_geo32, geo32))) return rc;
+      std::vector<float> w32(2 * (size_t)N);
+      const bool fr = h->opt.scheme == MCFD_FR;
+      for (int i = 0; i < Q; ++i)
+        for (int j = 0; j < Q; ++j)
+          for (int k = 0; k < Q; ++k) {
+            const double w = wq[i] * wq[j] * wq[k];
+            w32[(i * Q + j) * Q + k] = fr ? 1.f : (float)w;
+            w32[N + (i * Q + j) * Q + k] = fr ? 1.f : (float)(1.0 / w);
+          }
+      if ((rc = upload(h, &m.node_w32, w32))) return rc;
+    } else {
+      std::vector<float> geo32((size_t)d->n_cells * N * 10);
+#pragma omp parallel for schedule(static)
+      for (int64_t i = 0; i < d->n_cells * N; ++i)
+        for (int e = 0; e < 10; ++e) geo32[(size_t)i * 10 + e] = (float)geo[(size_t)i * 10 + e];
+      if ((rc = upload(h, &m.cell_geo32, geo32))) return rc;
+    }
     std::vector<float> rate32(rate.begin(), rate.end());
     if ((rc = upload(h, &m.cell_rate32, rate32))) return rc;
   }

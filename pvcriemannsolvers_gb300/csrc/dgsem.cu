@@ -544,7 +544,8 @@ constexpr int mixed_cell_min_blocks() {
 
 template <int Q, int STAGE, bool TC = false>
 __global__ void __launch_bounds__(CellCfg<Q>::kThreads, mixed_cell_min_blocks<Q, TC>())
-cell_update_mixed_kernel(CellArgs a, const float *__restrict__ geo32) {
+cell_update_mixed_kernel(CellArgs a, const float *__restrict__ geo32,
+                         const float *__restrict__ node_w32) {
   constexpr int N = Q * Q * Q, QF = Q * Q, KN = kK * N;
   constexpr int CPB = CellCfg<Q>::kCells;
   static_assert(!TC || (Q == 4 && CPB == 4), "the tensor-core form is built for Q = 4");
@@ -563,11 +564,21 @@ cell_update_mixed_kernel(CellArgs a, const float *__restrict__ geo32) {
     const double *up = a.u_in + c * KN + q * kK;
 #pragma unroll
     for (int k = 0; k < kK; ++k) uq[k] = up[k];
-    const float *g = geo32 + (c * N + q) * 10;
+    // metric terms: per node, or (every cell affine) adj(J) and 1/det(J) of
+    // the cell scaled by the node's weight
     float A[9];
+    if (node_w32) {
+      const float *g = geo32 + c * 10;
+      const float wn = node_w32[q];
 #pragma unroll
-    for (int e = 0; e < 9; ++e) A[e] = g[e];
-    inv_w = g[9];
+      for (int e = 0; e < 9; ++e) A[e] = wn * g[e];
+      inv_w = node_w32[N + q] * g[9];
+    } else {
+      const float *g = geo32 + (c * N + q) * 10;
+#pragma unroll
+      for (int e = 0; e < 9; ++e) A[e] = g[e];
+      inv_w = g[9];
+    }
     const float r = f64_to_f32(uq[0]), mx = f64_to_f32(uq[1]), my = f64_to_f32(uq[2]),
                 mz = f64_to_f32(uq[3]), en = f64_to_f32(uq[4]);
     // ConservativeToPrimitive with its clamp; rho < 0 and E < 0 are decided
@@ -1057,15 +1068,16 @@ template <int Q, int S>
 void cell_launch_mixed(mcfd_handle *h, const CellArgs &ca) {
   constexpr int CPB = CellCfg<Q>::kCells;
   int64_t blocks = (ca.n_cells + CPB - 1) / CPB;
+  const float *w32 = h->mesh.geo32_affine ? h->mesh.node_w32 : nullptr;
   if constexpr (Q == 4) {
     if (h->opt.tensor_contraction && !ca.fr) {
       cell_update_mixed_kernel<Q, S, true><<<(unsigned)blocks, CellCfg<Q>::kThreads, 0, h->stream>>>(
-          ca, h->mesh.cell_geo32);
+          ca, h->mesh.cell_geo32, w32);
       return;
     }
   }
   cell_update_mixed_kernel<Q, S><<<(unsigned)blocks, CellCfg<Q>::kThreads, 0, h->stream>>>(
-      ca, h->mesh.cell_geo32);
+      ca, h->mesh.cell_geo32, w32);
 }
 
 template <int Q>

@@ -171,7 +171,10 @@ struct Mesh {
   int n_groups = 0;
   // device arrays
   double *cell_geo = nullptr;       // [cells][N][10]: w*J^-1 (3x3 row-major), 1/w
-  float *cell_geo32 = nullptr;      // [cells][N][10]: FP32 w*J^-1, 1/w (mixed form only)
+  float *cell_geo32 = nullptr;      // [cells][N][10]: FP32 w*J^-1, 1/w (mixed form only); with
+                                    // geo32_affine [cells][10]: adj(J), 1/det(J)
+  float *node_w32 = nullptr;        // [2][N] with geo32_affine: w_q, 1/w_q (DGSEM) or 1, 1 (FR)
+  bool geo32_affine = false;        // every cell affine: the FP32 metric terms stored per cell
   double *cell_rate = nullptr;      // [cells] 1 / length  (length = cbrt(V)/2)
   float *cell_rate32 = nullptr;     // [cells] FP32 copy (mixed form's time step)
   int32_t *cell_flux = nullptr;     // [cells][6][QF] flux slot: >=0 subtract, <0 add (~slot), INT32_MIN none

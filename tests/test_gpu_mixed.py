@@ -119,3 +119,30 @@ def test_mixed_fr_vortex_density_error(gpu):
     assert abs(out["mixed"][1] - out["fp64"][1]) <= 1e-6 * out["fp64"][1]
     err = density_l2(out["mixed"][0], out["fp64"][0])
     assert err <= MIXED_L2_BAR, err
+
+
+@pytest.mark.parametrize("scheme", ["dg", "fr"])
+@pytest.mark.parametrize("p", [1, 2, 3])
+def test_mixed_affine_metric_terms(gpu, scheme, p):
+    """Uniform boxes have affine cells, and the mixed form then keeps its FP32
+    metric terms once per cell (adj(J), 1/det(J)) scaled by the node weights.
+    Its residual must match the oracle to FP32 accuracy, and match the
+    per-node metric path of a box whose nodes moved by 1e-9 of a cell (not
+    affine any more) to the size of that move."""
+    kw = {} if scheme == "dg" else {"scheme": "fr"}
+    om_kw = () if scheme == "dg" else ("fr",)
+    res = {}
+    for jitter in (0.0, 1e-9):
+        m = meshlib.box((5, 4, 3), lengths=(10.0, 8.0, 6.0), periodic=(True,) * 3, jitter=jitter, seed=3)
+        s = Lobatto(m, p, "rusanov", precision="mixed", **kw)
+        x = meshlib.node_coordinates(m, p).reshape(-1, 3)
+        u = cases.vortex_ic(x).ravel()
+        s.SetSolutionColumn(u)
+        res[jitter] = s.GetResidualColumn()
+        if jitter == 0.0:
+            ro = orc.Mesh(m, p, *om_kw).residual(orc.RUSANOV, u)
+            err = np.linalg.norm(res[jitter] - ro) / np.linalg.norm(ro)
+            assert err < 1e-5, err
+        s.close()
+    d = np.linalg.norm(res[0.0] - res[1e-9]) / np.linalg.norm(res[1e-9])
+    assert d < 1e-5, d
