@@ -190,11 +190,7 @@ __global__ void __launch_bounds__(512) face_flux_kernel(FaceArgs a) {
         } else if constexpr (R == kRoe) {
           done = flux_roe_traced_weighted<FAST_SQRT>(ch, trh, cs, trs, n, g.w, out);
         } else {
-          done = flux_hllc_traced<FAST_SQRT>(ch, trh, cs, trs, n, out);
-          if (done) {
-#pragma unroll
-            for (int k = 0; k < kK; ++k) out[k] *= g.w;
-          }
+          done = flux_hllc_traced_weighted<FAST_SQRT>(ch, trh, cs, trs, n, g.w, out);
         }
         if (done) {
           store_flux(a.flux, a.f32_out, gid, out);

@@ -299,6 +299,13 @@ __device__ __forceinline__ double abs_bits(double x) {
       "mov.b64 %0, {lo, hi};\n\t}" : "=d"(r) : "d"(x));
   return r;
 }
+// -x by flipping the sign bit of the high word (an integer operation)
+__device__ __forceinline__ double neg_bits(double x) {
+  double r;
+  asm("{\n\t.reg .b32 lo, hi;\n\tmov.b64 {lo, hi}, %1;\n\txor.b32 hi, hi, 0x80000000;\n\t"
+      "mov.b64 %0, {lo, hi};\n\t}" : "=d"(r) : "d"(x));
+  return r;
+}
 __device__ __forceinline__ bool bits_negative(double x) {
   const long long b = (long long)bits64(x);
   return b < 0 && (b << 1) != 0;
@@ -316,6 +323,7 @@ inline double rcp_signed(double x) { return 1.0 / x; }
 inline double sqrt_seeded(double x) { return std::sqrt(x); }
 inline bool bits_positive(double x) { return x > 0; }
 inline double abs_bits(double x) { return std::fabs(x); }
+inline double neg_bits(double x) { return -x; }
 inline bool bits_negative(double x) { return x < 0; }
 #endif
 
@@ -664,42 +672,34 @@ MCFD_HD double sqrt_form(double x) {
   else return sqrt(x);
 }
 
-// one side's flux, plus the star correction (hllc_star) when `star`; the
-// state enters as its conservative variables, 1/rho, p, the normal momentum
-// mn = m . n and un = mn / rho (the star momentum temp u + dm n is formed as
-// (temp / rho) m + dm n, so no velocity vector is needed)
-MCFD_HD void hllc_side_cons(const double *c, double rinv, double p, double mn, double un,
-                            const double *n, bool star, double wk, double ws, double *f) {
-  const double rho = c[0], e = c[4];
-  f[0] = mn;
-  f[1] = c[1] * un + p * n[0];
-  f[2] = c[2] * un + p * n[1];
-  f[3] = c[3] * un + p * n[2];
-  f[4] = (e + p) * un;
-  if (!star) return;
-  const double rdk = rho * (wk - un);
-  const double temp = rdk * rcp_signed(wk - ws);
-  double es = e * rinv + (ws - un) * (ws + p * rcp_signed(rdk));
-  es *= temp;
-  const double dm = temp * (ws - un), ti = temp * rinv;
-  f[0] += wk * (temp - rho);
-  f[1] += wk * ((ti * c[1] + dm * n[0]) - c[1]);
-  f[2] += wk * ((ti * c[2] + dm * n[1]) - c[2]);
-  f[3] += wk * ((ti * c[3] + dm * n[2]) - c[3]);
-  f[4] += wk * (es - e);
-}
-
 // (gamma + 1) / (2 gamma): the pressure ratio's weight in the wave-speed factor
 constexpr double kHllcQ = kGp1Over2 * kOneOverGamma;
 
-// HLLC from both sides' 1/rho, pressure and sound speed (p > 0 on both).
+// HLLC times the face weight w, from both sides' conservative variables,
+// 1/rho, pressure and sound speed (p > 0 on both).
 // The wave speeds of hllc.hpp, u_n -/+ a_k q_k with
 // q_k = sqrt(1 + (gamma+1)/(2 gamma) (p*/p_k - 1)) for p* > p_k, are formed as
 // a_k q_k = sqrt(gamma / rho_k (p_k + (gamma+1)/(2 gamma) (p* - p_k))): the same
 // number without the reciprocal of p_k.
+// The flux of the side that the reference's four cases pick (left, right,
+// left star, right star), with S_k that side's wave speed and S* the contact
+// speed, is
+//   F*_k = (S* (S_k U_k - F_k) + S_k p*_k D) / (S_k - S*),  D = (0, n, S*),
+//   p*_k = p_k + rho_k (S_k - u_k) (S* - u_k),
+// which is F_k + S_k (U*_k - U_k) with the star state of hllc.hpp: the jump
+// conditions across the S_k wave (S_k U* - F* = S_k U - F) and across the
+// contact (F* = S* U* + p* D) give it.  A supersonic side (no star
+// correction) takes the same arithmetic with S_k = 0, S* = 1, which yields
+// F_k.  Per component, with g = w / (S_k - S*),
+//   rho:  rho A,   m_i:  m_i A + n_i B,   E:  E A + g S* (S_k p*_k - p_k u_k),
+//   A = g S* (S_k - u_k),   B = g (S_k p*_k - S* p_k),
+// so neither F_k nor U*_k is formed: 24 FP64 operations after the wave
+// speeds (the side flux, the star correction and the weight took 50), and
+// lanes of a warp in different cases share one pass through them.
 template <bool FAST_SQRT>
-MCFD_HD void hllc_core(const double *cl, const double *cr, double il, double ir, double pl,
-                       double pr, double al, double ar, const double *n, double *f) {
+MCFD_HD void hllc_core_weighted(const double *cl, const double *cr, double il, double ir,
+                                double pl, double pr, double al, double ar, const double *n,
+                                double w, double *f) {
   const double rl = cl[0], rr = cr[0];
   const double mnl = cl[1] * n[0] + cl[2] * n[1] + cl[3] * n[2];
   const double mnr = cr[1] * n[0] + cr[2] * n[1] + cr[3] * n[2];
@@ -714,13 +714,8 @@ MCFD_HD void hllc_core(const double *cl, const double *cr, double il, double ir,
   if (!le_nonneg(p_estimate, pr)) aqr = sqrt_form<FAST_SQRT>(kGamma * ir * fma(kHllcQ, p_estimate - pr, pr));
   const double wave_left = unl - aql;
   const double wave_right = unr + aqr;
-  const double wave_star = (pr - pl + rl * unl * (wave_left - unl) - rr * unr * (wave_right - unr)) *
-                           rcp_signed(rl * (wave_left - unl) - rr * (wave_right - unr));
-  // The reference's four cases (left, right, left star, right star) pick a
-  // side and whether the star correction applies; the side's values are
-  // selected (integer selects) and one side evaluation follows, so lanes of a
-  // warp whose star speeds differ in sign share one pass through the FP64
-  // arithmetic instead of one per case.
+  const double dl = wave_left - unl, dr = wave_right - unr;  // S_k - u_k
+  const double wave_star = (pr - pl + rl * unl * dl - rr * unr * dr) * rcp_signed(rl * dl - rr * dr);
   const bool sup_l = ge_zero(wave_left), sup_r = le_zero(wave_right);
   const bool star = !sup_l && !sup_r;
   if (star && !ge_zero(wave_star) && !lt_zero(wave_star)) {  // wave_star is NaN
@@ -728,15 +723,31 @@ MCFD_HD void hllc_core(const double *cl, const double *cr, double il, double ir,
     return;
   }
   const bool left = sup_l || (!sup_r && ge_zero(wave_star));
-  double cs[kK];
+  // the side's values (integer selects); S_k = 0, S* = 1 without the star
+  // correction, where S_k - u_k is then -u_k
+  double c[kK];
 #pragma unroll
-  for (int k = 0; k < kK; ++k) cs[k] = left ? cl[k] : cr[k];
-  hllc_side_cons(cs, left ? il : ir, left ? pl : pr, left ? mnl : mnr, left ? unl : unr, n, star,
-                 left ? wave_left : wave_right, wave_star, f);
+  for (int k = 0; k < kK; ++k) c[k] = left ? cl[k] : cr[k];
+  const double p = left ? pl : pr, un = left ? unl : unr;
+  const double sk = star ? (left ? wave_left : wave_right) : 0.0;
+  const double ss = star ? wave_star : 1.0;
+  const double skun = star ? (left ? dl : dr) : neg_bits(un);
+  const double g = w * rcp_signed(sk - ss);
+  const double pstar = fma(c[0] * skun, ss - un, p);
+  const double sp = star ? sk * pstar : 0.0;  // S_k p*_k
+  const double gs = g * ss;
+  const double A = gs * skun;
+  const double B = g * fma(-ss, p, sp);
+  f[0] = c[0] * A;
+  f[1] = fma(c[1], A, n[0] * B);
+  f[2] = fma(c[2], A, n[1] * B);
+  f[3] = fma(c[3], A, n[2] * B);
+  f[4] = fma(c[4], A, gs * fma(-p, un, sp));
 }
 
 template <bool FAST_SQRT>
-MCFD_HD bool flux_hllc_cons(const double *cl, const double *cr, const double *n, double *f) {
+MCFD_HD bool flux_hllc_cons_weighted(const double *cl, const double *cr, const double *n,
+                                     double w, double *f) {
   const double rl = cl[0], rr = cr[0];
   if (!bits_positive(rl) || !bits_positive(rr) || bits_negative(cl[4]) || bits_negative(cr[4])) return false;
   const double il = rcp_newton(rl), ir = rcp_newton(rr);
@@ -747,17 +758,17 @@ MCFD_HD bool flux_hllc_cons(const double *cl, const double *cr, const double *n,
   const double pr = fma(-0.5 * mr, ir, cr[4]) * kGm1;
   if (!bits_positive(pl) || !bits_positive(pr)) return false;
   const double al = sqrt_form<FAST_SQRT>(kGamma * pl * il), ar = sqrt_form<FAST_SQRT>(kGamma * pr * ir);
-  hllc_core<FAST_SQRT>(cl, cr, il, ir, pl, pr, al, ar, n, f);
+  hllc_core_weighted<FAST_SQRT>(cl, cr, il, ir, pl, pr, al, ar, n, w, f);
   return true;
 }
 
-// flux_hllc_cons with both sides' node traces {1/rho, p, sound speed}: false
-// (primitive fallback) unless p > 0 on both sides.
+// flux_hllc_cons_weighted with both sides' node traces {1/rho, p, sound
+// speed}: false (primitive fallback) unless p > 0 on both sides.
 template <bool FAST_SQRT>
-MCFD_HD bool flux_hllc_traced(const double *cl, const double *trl, const double *cr,
-                              const double *trr, const double *n, double *f) {
+MCFD_HD bool flux_hllc_traced_weighted(const double *cl, const double *trl, const double *cr,
+                                       const double *trr, const double *n, double w, double *f) {
   if (!bits_positive(trl[1]) || !bits_positive(trr[1])) return false;
-  hllc_core<FAST_SQRT>(cl, cr, trl[0], trr[0], trl[1], trr[1], trl[2], trr[2], n, f);
+  hllc_core_weighted<FAST_SQRT>(cl, cr, trl[0], trr[0], trl[1], trr[1], trl[2], trr[2], n, w, f);
   return true;
 }
 
@@ -1081,11 +1092,7 @@ MCFD_HD void interior_flux_weighted(const double *cl, const double *cr, const do
     if (flux_roe_cons_weighted<FAST_SQRT>(cl, cr, n, w, f)) return;
   }
   if constexpr (R == kHllc) {
-    if (flux_hllc_cons<FAST_SQRT>(cl, cr, n, f)) {
-#pragma unroll
-      for (int k = 0; k < kK; ++k) f[k] *= w;
-      return;
-    }
+    if (flux_hllc_cons_weighted<FAST_SQRT>(cl, cr, n, w, f)) return;
   }
   if constexpr (R != kRusanov) {
     Prim l = cons_to_prim(cl[0], cl[1], cl[2], cl[3], cl[4]);
