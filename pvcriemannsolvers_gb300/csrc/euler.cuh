@@ -775,12 +775,18 @@ MCFD_HD bool flux_hllc_traced_weighted(const double *cl, const double *trl, cons
 // Roe on conservative inputs, times the face weight w, for two admissible
 // states (rho > 0, E >= 0, p >= 0 on both sides; false otherwise and the
 // caller takes flux_roe on the converted primitives).  The same flux as
-// flux_roe, regrouped: the physical fluxes from the conservative variables
+// flux_roe, regrouped: the physical flux from the conservative variables
 // (m u_n + p n, (E + p) u_n), the total enthalpy as (E + p) / rho, the Roe
 // weights from lambda = sqrt(rho_R / rho_L) (u~ = (u_L + lambda u_R) /
-// (1 + lambda), rho~ = lambda rho_L: one square root instead of two), the
-// acoustic pair combined as (a1 + a5) (u, h0) + (a5 - a1) a (n, u_n), and the
-// halves of the average and of the wave strengths folded into one w / 2.
+// (1 + lambda), rho~ = lambda rho_L: one square root instead of two), and the
+// acoustic pair combined as (a1 + a5) (u, h0) + (a5 - a1) a (n, u_n).
+// The reference's average 0.5 (F_L + F_R) - 0.5 sum_k |l_k| alpha_k r_k is
+// taken in its upwind form F_L + sum_k min(l_k, 0) alpha_k r_k: with Roe
+// averages the wave strengths decompose the jumps exactly,
+// F_R - F_L = sum_k l_k alpha_k r_k (Roe's property), so the two are the
+// same flux, and the right state's physical flux and normal velocity are
+// never formed (u_n,R - u_n,L is the normal part of the velocity jump that
+// the shear waves need anyway).
 // FAST_SQRT (the mixed form) takes both square roots from sqrt_seeded.
 // Roe from both sides' 1/rho and pressure and lambda = sqrt(rho_R / rho_L).
 template <bool FAST_SQRT>
@@ -791,18 +797,18 @@ MCFD_HD void roe_core_weighted(const double *cl, const double *cr, double il, do
   const double ul = cl[1] * il, vl = cl[2] * il, wl = cl[3] * il;
   const double ur = cr[1] * ir, vr = cr[2] * ir, wr = cr[3] * ir;
   const double unl = ul * n[0] + vl * n[1] + wl * n[2];
-  const double unr = ur * n[0] + vr * n[1] + wr * n[2];
-  // F(U_L) + F(U_R)
-  const double s0 = rl * unl + rr * unr;
-  const double s1 = (cl[1] * unl + pl * n[0]) + (cr[1] * unr + pr * n[0]);
-  const double s2 = (cl[2] * unl + pl * n[1]) + (cr[2] * unr + pr * n[1]);
-  const double s3 = (cl[3] * unl + pl * n[2]) + (cr[3] * unr + pr * n[2]);
-  const double s4 = (el + pl) * unl + (er + pr) * unr;
+  // F(U_L)
+  const double hl = el + pl;
+  const double s0 = rl * unl;
+  const double s1 = cl[1] * unl + pl * n[0];
+  const double s2 = cl[2] * unl + pl * n[1];
+  const double s3 = cl[3] * unl + pl * n[2];
+  const double s4 = hl * unl;
   // Roe averages
   const double inv = rcp_newton(1 + lam);
   const double rho = lam * rl;
   const double u = (ul + lam * ur) * inv, v = (vl + lam * vr) * inv, ww = (wl + lam * wr) * inv;
-  const double h0 = ((el + pl) * il + lam * ((er + pr) * ir)) * inv;
+  const double h0 = (hl * il + lam * ((er + pr) * ir)) * inv;
   const double un = u * n[0] + v * n[1] + ww * n[2];
   const double ke = 0.5 * (u * u + v * v + ww * ww);
   const double aa = kGm1 * (h0 - ke);
@@ -810,22 +816,24 @@ MCFD_HD void roe_core_weighted(const double *cl, const double *cr, double il, do
   if constexpr (FAST_SQRT) a = sqrt_seeded(aa);
   else a = sqrt(aa);
   const double i2aa = rcp_newton(2 * aa);
-  // twice the wave strengths times |lambda_k|
-  const double dp = pr - pl, rau = rho * a * (unr - unl);
-  const double a1 = ((dp - rau) * i2aa) * fabs(un - a);
-  const double a2 = ((rr - rl) - dp * (2 * i2aa)) * fabs(un);
-  const double a5 = ((dp + rau) * i2aa) * fabs(un + a);
+  // min(l_k, 0) on the bit patterns (integer selects; NaN stays NaN)
+  const double l1 = un - a, l5 = un + a;
+  const double m1 = gt_zero(l1) ? 0.0 : l1, m2 = gt_zero(un) ? 0.0 : un, m5 = gt_zero(l5) ? 0.0 : l5;
   const double dv0 = ur - ul, dv1 = vr - vl, dv2 = wr - wl;
-  const double dvn = dv0 * n[0] + dv1 * n[1] + dv2 * n[2];
-  const double st = rho * fabs(un);
+  const double dvn = dv0 * n[0] + dv1 * n[1] + dv2 * n[2];  // u_n,R - u_n,L
+  // the wave strengths times min(l_k, 0)
+  const double dp = pr - pl, rau = rho * a * dvn;
+  const double a1 = ((dp - rau) * i2aa) * m1;
+  const double a2 = ((rr - rl) - dp * (2 * i2aa)) * m2;
+  const double a5 = ((dp + rau) * i2aa) * m5;
+  const double st = rho * m2;
   const double t0 = st * (dv0 - dvn * n[0]), t1 = st * (dv1 - dvn * n[1]), t2 = st * (dv2 - dvn * n[2]);
   const double S = a1 + a5, Sa = S + a2, D = (a5 - a1) * a;
-  const double hw = 0.5 * w;
-  f[0] = hw * (s0 - Sa);
-  f[1] = hw * (s1 - (Sa * u + D * n[0] + t0));
-  f[2] = hw * (s2 - (Sa * v + D * n[1] + t1));
-  f[3] = hw * (s3 - (Sa * ww + D * n[2] + t2));
-  f[4] = hw * (s4 - (S * h0 + D * un + a2 * ke + (t0 * u + t1 * v + t2 * ww)));
+  f[0] = w * (s0 + Sa);
+  f[1] = w * (s1 + (Sa * u + D * n[0] + t0));
+  f[2] = w * (s2 + (Sa * v + D * n[1] + t1));
+  f[3] = w * (s3 + (Sa * ww + D * n[2] + t2));
+  f[4] = w * (s4 + (S * h0 + D * un + a2 * ke + (t0 * u + t1 * v + t2 * ww)));
 }
 
 template <bool FAST_SQRT>
