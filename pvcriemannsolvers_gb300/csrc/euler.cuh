@@ -883,12 +883,73 @@ MCFD_HD double ex_sound(double rho, double p) {
   return (rho > 0 && p > 0) ? sqrt(kGamma * p / rho) : 0.0;
 }
 
+// The Exact solver's powers have rational exponents for gamma = 1.4:
+// (gamma - 1) / (2 gamma) = 1/7 and gamma = 7/5.  On the device they come
+// from inverse roots z = x^(-1/K) (K = 7, 5): an FP32 seed exp2(-log2(x) / K)
+// (relative error below 1e-6), then two Newton steps on z^-K = x in the
+// division-free form z <- z + z (1 - x z^K) / K, each taking a relative error
+// e to about (K + 1) / 2 e^2 (1e-12, then the FP64 rounding level).  Outside
+// x in [2^-120, 2^120] (FP32 cannot seed it) pow is taken.
+#ifdef __CUDA_ARCH__
+template <int K>
+__device__ __forceinline__ double zpow(double z) {
+  const double z2 = z * z;
+  if constexpr (K == 5) return (z2 * z2) * z;
+  const double z3 = z2 * z;
+  return (z3 * z3) * z;  // K == 7
+}
+template <int K>
+__device__ __forceinline__ bool inv_root(double x, double *z_out) {
+  const int e = (int)((bits64(x) >> 52) & 0x7ff) - 1023;
+  if (e < -120 || e > 120 || (long long)bits64(x) < 0) return false;
+  const float xf = f64_to_f32(x);
+  double z = f32_to_f64(exp2f(log2f(xf) * (-1.0f / K)));
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const double err = fma(-x, zpow<K>(z), 1.0);
+    z = fma(z * err, 1.0 / K, z);
+  }
+  *z_out = z;
+  return true;
+}
+#endif
+
+// r^(1/7) for the expansion branch (r = p_after / p_before >= 0); with
+// *r67 = r^(-6/7) = r^(1/7) / r for its derivative when asked.
+MCFD_HD double ex_root7(double r, double *r67 = nullptr) {
+#ifdef __CUDA_ARCH__
+  double z;
+  if (inv_root<7>(r, &z)) {
+    const double z3 = (z * z) * z, z6 = z3 * z3;
+    if (r67) *r67 = z6;
+    return r * z6;
+  }
+#endif
+  const double s = pow(r, kGm1Over2 / kGamma);
+  if (r67) *r67 = s / r;
+  return s;
+}
+
+// p / rho^gamma (the isentrope constant of ex_near_expansion and the vacuum
+// cases), rho^-gamma = (rho^(-1/5))^7.
+MCFD_HD double ex_isentrope(double p, double rho) {
+#ifdef __CUDA_ARCH__
+  double z;
+  if (inv_root<5>(rho, &z)) return p * zpow<7>(z);
+#endif
+  return p / pow(rho, kGamma);
+}
+
 struct SpeedChange {
   double rho_before, p_before, a_before, p_const;
+  // 1 / p_before and 1 / (rho_before a_before), once per side (IEEE
+  // reciprocals: a zero gives the infinity the reference's quotients give)
+  double inv_p, inv_rho_a;
   MCFD_HD SpeedChange(double rho, double p)
       : rho_before(rho), p_before(p),
         a_before(rho == 0 ? 0 : ex_sound(rho, p)),
-        p_const(p * kGm1Over2) {}
+        p_const(p * kGm1Over2),
+        inv_p(1.0 / p), inv_rho_a(1.0 / (rho * a_before)) {}
   MCFD_HD double P(double p_after) const { return kGp1Over2 * p_after + p_const; }
   MCFD_HD double value(double p_after) const {
     if (p_after >= p_before) {
@@ -896,35 +957,26 @@ struct SpeedChange {
       return (p_after - p_before) / divisor;
     }
     // pow(+0, y > 0) is +0: the vacuum test at p = 0 needs no power
-    double v = (p_after == 0 ? 0.0 : pow(p_after / p_before, kGm1Over2 / kGamma)) - 1;
+    double v = (p_after == 0 ? 0.0 : ex_root7(p_after * inv_p)) - 1;
     return v * (kGm1Under2 * a_before);
   }
-  MCFD_HD double prime(double p_after) const {
-    if (p_after >= p_before) {
-      double p = P(p_after);
-      double v = kGp1Over4 * (p_before - p_after);
-      double divisor = sqrt(rho_before * p);
-      return (1 + v / p) / divisor;
-    }
-    double divisor = rho_before * a_before;
-    return pow(p_after / p_before, -kGp1Over2 / kGamma) / divisor;
-  }
-  // value and prime at the same pressure, sharing the square root of the
-  // shock branch and, in the expansion branch, the power r^((g-1)/(2g)) of
-  // r = p_after / p_before: r^(-(g+1)/(2g)) = r^((g-1)/(2g)) / r.
+  // value and prime at the same pressure: in the shock branch one reciprocal
+  // of the square root D = sqrt(rho P) serves both (1 / P = rho / D^2); in the
+  // expansion branch r^(1/7) and r^(-6/7) = r^(1/7) / r of r = p_after /
+  // p_before come from one inverse root.
   MCFD_HD void value_prime(double p_after, double *v, double *d) const {
     if (p_after >= p_before) {
-      const double p = P(p_after);
-      const double divisor = sqrt(rho_before * p);
-      *v = (p_after - p_before) / divisor;
+      const double divisor = sqrt(rho_before * P(p_after));
+      const double inv = 1.0 / divisor;
+      *v = (p_after - p_before) * inv;
       const double w = kGp1Over4 * (p_before - p_after);
-      *d = (1 + w / p) / divisor;
+      *d = fma(w * rho_before, inv * inv, 1.0) * inv;
       return;
     }
-    const double r = p_after / p_before;
-    const double s = pow(r, kGm1Over2 / kGamma);
+    double r67;
+    const double s = ex_root7(p_after * inv_p, &r67);
     *v = (s - 1) * (kGm1Under2 * a_before);
-    *d = (s / r) / (rho_before * a_before);
+    *d = r67 * inv_rho_a;
   }
 };
 
@@ -932,7 +984,9 @@ MCFD_HD Exact1D ex_inside_expansion(double gri_1, double gri_2) {
   constexpr double r = kGm1 / kGp1;
   double a = r * gri_2;
   double a_square = a * a;
-  double rho = pow(a_square / gri_1 * kOneOverGamma, kOneOverGm1);
+  // q^(1 / (gamma - 1)) = q^(5/2) = q^2 sqrt(q)
+  const double q = a_square / gri_1 * kOneOverGamma;
+  double rho = (q * q) * sqrt(q);
   return Exact1D{rho, a, a_square * rho * kOneOverGamma};
 }
 
@@ -952,7 +1006,7 @@ MCFD_HD Exact1D ex_near_shock(int field, const Exact1D &before,
 MCFD_HD Exact1D ex_near_expansion(int field, const Exact1D &before,
                                   Exact1D after) {
   double a_before = ex_sound(before.rho, before.p);
-  double gri_1 = before.p / pow(before.rho, kGamma);
+  double gri_1 = ex_isentrope(before.p, before.rho);
   double gri_2, a_after;
   if (field == 1) {
     gri_2 = before.u + kGm1Under2 * a_before;
@@ -978,10 +1032,10 @@ MCFD_HD Exact1D ex_near_vacuum(const Exact1D &l, const Exact1D &r) {
   if (l.u > left_a) return l;
   double right_a = ex_sound(r.rho, r.p);
   if (r.u + right_a < 0) return r;
-  double gri_1 = l.p / pow(l.rho, kGamma);
+  double gri_1 = ex_isentrope(l.p, l.rho);
   double gri_2 = l.u + left_a * kGm1Under2;
   if (gri_2 >= 0) return ex_inside_expansion(gri_1, gri_2);
-  gri_1 = r.p / pow(r.rho, kGamma);
+  gri_1 = ex_isentrope(r.p, r.rho);
   gri_2 = r.u - right_a * kGm1Under2;
   if (gri_2 < 0) return ex_inside_expansion(gri_1, gri_2);
   return Exact1D{0, 0, 0};
@@ -996,7 +1050,7 @@ MCFD_HD Exact1D exact_upwind(const Exact1D &l, const Exact1D &r,
       if (l.u >= a_left) return l;
       double u_star = l.u + a_left * kGm1Under2;
       if (u_star <= 0) return Exact1D{0, 0, 0};
-      return ex_inside_expansion(l.p / pow(l.rho, kGamma), u_star);
+      return ex_inside_expansion(ex_isentrope(l.p, l.rho), u_star);
     }
   } else {
     if (r.rho > 0) {
@@ -1004,7 +1058,7 @@ MCFD_HD Exact1D exact_upwind(const Exact1D &l, const Exact1D &r,
       if (r.u + a_right <= 0) return r;
       double u_star = r.u - a_right * kGm1Under2;
       if (u_star >= 0) return Exact1D{0, 0, 0};
-      return ex_inside_expansion(r.p / pow(r.rho, kGamma), u_star);
+      return ex_inside_expansion(ex_isentrope(r.p, r.rho), u_star);
     }
     return Exact1D{0, 0, 0};
   }
