@@ -222,7 +222,14 @@ struct Visc {
   double *cell = nullptr;   // [cells][2]: length, length^(p + 4)
   double *d2 = nullptr;     // [Q][Q] second derivatives l_i''(x_a)
   double *wloc = nullptr;   // [N] local GLL weights of the nodes
+  // work list of the damping-rate pass (cells whose jump reaches the
+  // reference square): count, cells, kViscRateData doubles per entry
+  unsigned *rate_count = nullptr;
+  int32_t *rate_cell = nullptr;
+  double *rate_data = nullptr;
+  int rate_blocks = 1;  // persistent grid of the damping-rate kernel
 };
+constexpr int kViscRateData = 8;  // wave speed, 5 jump integrals, flags, pad
 
 // Device tables of the WENO limiter (built when a limiter is requested).
 // M = (p+1)(p+2)(p+3)/6 modal basis functions per cell.
@@ -461,6 +468,9 @@ int build_modal_limiter(mcfd_handle *h, const ::mcfd_mesh_desc *d, int kind, dou
 int build_viscosity(mcfd_handle *h, double beta0, double beta1, double time_scale);
 void release_viscosity(mcfd_handle *h);
 int launch_visc_properties(mcfd_handle *h, const double *u, int dt_mode);
+// resident blocks per SM of the damping-rate kernel for Q nodes per direction
+// (its persistent grid; queried once at set-up, outside any stream capture)
+int visc_rate_blocks_per_sm(int q);
 int launch_visc_face_flux(mcfd_handle *h, const double *u);
 int launch_visc_dt_finalize(mcfd_handle *h);
 // Initial limiters of the viscous demos (limiter/average.hpp,

@@ -114,7 +114,7 @@ cudaError_t download_vec(std::vector<T> *dst, const T *src, size_t n) {
 
 void release_viscosity(mcfd_handle *h) {
   Visc &v = h->visc;
-  void *ptrs[] = {v.nu, v.side, v.pt, v.cell, v.d2, v.wloc};
+  void *ptrs[] = {v.nu, v.side, v.pt, v.cell, v.d2, v.wloc, v.rate_count, v.rate_cell, v.rate_data};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   v = Visc{};
@@ -259,6 +259,14 @@ int build_viscosity(mcfd_handle *h, double beta0, double beta1, double time_scal
   if (e == cudaSuccess) e = upload_vec(&v.wloc, wloc);
   if (e == cudaSuccess) e = cudaMalloc(&v.nu, sizeof(double) * kK * std::max<int64_t>(nc, 1));
   if (e == cudaSuccess) e = cudaMemset(v.nu, 0, sizeof(double) * kK * std::max<int64_t>(nc, 1));
+  if (e == cudaSuccess) e = cudaMalloc(&v.rate_count, sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMalloc(&v.rate_cell, sizeof(int32_t) * std::max<int64_t>(nc, 1));
+  if (e == cudaSuccess) e = cudaMalloc(&v.rate_data, sizeof(double) * kViscRateData * std::max<int64_t>(nc, 1));
+  if (e == cudaSuccess) {
+    int sms = 0;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+    v.rate_blocks = std::max(sms, 1) * visc_rate_blocks_per_sm(Q);
+  }
   if (e == cudaSuccess) {
     const double init = 1.e+100;
     unsigned long long bits;

@@ -10,14 +10,20 @@
 //                                (IntegrateJumpOnFaces, :446-475);
 //                              * maximum wave speed and reference squares
 //                                over the nodes (:490-503);
-//                              * only for a cell with a component whose jump
-//                                reaches its reference square: the damping
-//                                rate -u_k^T D u_k, where D u is the viscous
-//                                FR residual of the cell with nu = 1 and zero
-//                                neighbours (BuildDampingMatrices, :299-384),
-//                                evaluated matrix-free (no N x N matrix per
-//                                cell is stored or read);
-//                              * nu_k and the stable step (:504-536).
+//                              * nu_k = 0 and the stable step (:504-536) of
+//                                a cell none of whose components has a jump
+//                                reaching its reference square; the other
+//                                cells go to a work list.
+//   visc_rate_kernel<Q>        persistent grid over the work list, one warp
+//                              per listed cell: the damping rate
+//                              -u_k^T D u_k, where D u is the viscous FR
+//                              residual of the cell with nu = 1 and zero
+//                              neighbours (BuildDampingMatrices, :299-384),
+//                              evaluated matrix-free (no N x N matrix per
+//                              cell is stored or read), then nu_k and the
+//                              stable step.  Apart from the pass over every
+//                              cell so that its registers do not bound that
+//                              pass's occupancy.
 //   visc_face_kernel<Q>        one thread per face point, after the
 //                              convective face kernel: minus nu_avg n .
 //                              common_gradient (fr/general.hpp:316-350).  The DDG common
@@ -39,6 +45,7 @@
 //                              demos (limiter/average.hpp, limiter/majority.hpp).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <climits>
 #include <cstdint>
 
@@ -65,6 +72,11 @@ struct PropArgs {
   const double *side, *pt, *cell;
   double *nu;
   DevState *state;
+  // cells whose jump reaches the reference square: count, cell, and per
+  // entry the wave speed, the five jump integrals and the component flags
+  unsigned *rate_count;
+  int32_t *rate_cell;
+  double *rate_data;
   int64_t n_cells;
   double g1, time_scale, spatial_factor;
   int p;
@@ -126,6 +138,17 @@ __device__ __forceinline__ void normal_traces(const double (&g)[3][kK], const do
   }
 }
 
+// the slots (local face side, point) of node (i, j, l) on the cell surface
+template <int Q, class F>
+__device__ __forceinline__ void for_slots(int i, int j, int l, F &&fn) {
+  if (l == 0) fn(0, i * Q + j);
+  if (l == Q - 1) fn(5, i * Q + j);
+  if (j == 0) fn(1, i * Q + l);
+  if (j == Q - 1) fn(3, i * Q + l);
+  if (i == 0) fn(4, j * Q + l);
+  if (i == Q - 1) fn(2, j * Q + l);
+}
+
 template <int Q>
 __global__ void __launch_bounds__(32 * kWarps) visc_properties_kernel(PropArgs a) {
   constexpr int N = Q * Q * Q, QF = Q * Q, KN = kK * N;
@@ -146,15 +169,6 @@ __global__ void __launch_bounds__(32 * kWarps) visc_properties_kernel(PropArgs a
   if (!active) return;
   const double *U = s_u[warp];
   const int32_t *cf = a.cell_flux + c * 6 * QF;
-  // the slots (local face side, point) of node (i, j, l) on the cell surface
-  auto for_slots = [&](int i, int j, int l, auto &&fn) {
-    if (l == 0) fn(0, i * Q + j);
-    if (l == Q - 1) fn(5, i * Q + j);
-    if (j == 0) fn(1, i * Q + l);
-    if (j == Q - 1) fn(3, i * Q + l);
-    if (i == 0) fn(4, j * Q + l);
-    if (i == Q - 1) fn(2, j * Q + l);
-  };
   // cheap pass: wave speeds, reference squares and the face jump integral
   double speed_max = 1e-5, sq_max[kK], jump_acc[kK];
 #pragma unroll
@@ -174,7 +188,7 @@ __global__ void __launch_bounds__(32 * kWarps) visc_properties_kernel(PropArgs a
 #pragma unroll
     for (int k = 0; k < kK; ++k) sq_max[k] = (sq_max[k] < sq[k]) ? sq[k] : sq_max[k];
     const int i = q / QF, j = (q / Q) % Q, l = q % Q;
-    for_slots(i, j, l, [&](int side, int t) {
+    for_slots<Q>(i, j, l, [&](int side, int t) {
       const int32_t v = cf[side * QF + t];
       if (v == INT32_MIN) return;
       const int64_t pt = v >= 0 ? v : ~(int64_t)v;
@@ -211,10 +225,59 @@ __global__ void __launch_bounds__(32 * kWarps) visc_properties_kernel(PropArgs a
 #pragma unroll
   for (int k = 0; k < kK; ++k)
     if (!(jump_acc[k] < sq_max[k] * Lp)) flagged |= 1u << k;
-  double rate_acc[kK];
-#pragma unroll
-  for (int k = 0; k < kK; ++k) rate_acc[k] = 0;
+  if (lane != 0) return;
   if (flagged) {
+    // the damping rate follows in visc_rate_kernel
+    const unsigned idx = atomicAdd(a.rate_count, 1u);
+    a.rate_cell[idx] = (int32_t)c;
+    double *d = a.rate_data + (int64_t)idx * kViscRateData;
+    d[0] = speed_max;
+#pragma unroll
+    for (int k = 0; k < kK; ++k) d[1 + k] = jump_acc[k];
+    d[1 + kK] = (double)flagged;
+    return;
+  }
+  const double min_dt = L / speed_max;
+#pragma unroll
+  for (int k = 0; k < kK; ++k) a.nu[c * kK + k] = 0.0;
+  if (a.dt_mode) atomicMin(&a.state->min_dt_bits, bits64(min_dt));
+}
+
+// The damping rate, nu and the stable step of the cells that the properties
+// kernel listed (a persistent grid, one warp per listed cell at a time).
+// Kept apart from the cheap pass so that its register count (the gradient,
+// flux and Hessian arrays of the matrix-free rate) does not bound the
+// occupancy of the pass over every cell.
+template <int Q>
+__global__ void __launch_bounds__(32 * kWarps) visc_rate_kernel(PropArgs a) {
+  constexpr int N = Q * Q * Q, QF = Q * Q, KN = kK * N;
+  __shared__ double s_u[kWarps][KN];
+  __shared__ double s_ft[kWarps][3 * kK][N];
+  __shared__ double s_d[Q * Q], s_d2[Q * Q], s_w[N];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int e = threadIdx.x; e < Q * Q; e += blockDim.x) {
+    s_d[e] = a.dmat[e];
+    s_d2[e] = a.d2[e];
+  }
+  for (int e = threadIdx.x; e < N; e += blockDim.x) s_w[e] = a.wloc[e];
+  __syncthreads();
+  const unsigned count = *a.rate_count;
+  for (unsigned idx = blockIdx.x * kWarps + warp; idx < count; idx += gridDim.x * kWarps) {
+    const int64_t c = a.rate_cell[idx];
+    for (int e = lane; e < KN; e += 32) s_u[warp][e] = a.u[c * KN + e];
+    __syncwarp();
+    const double *U = s_u[warp];
+    const int32_t *cf = a.cell_flux + c * 6 * QF;
+    const double *d = a.rate_data + (int64_t)idx * kViscRateData;
+    const double speed_max = d[0];
+    double jump_acc[kK];
+#pragma unroll
+    for (int k = 0; k < kK; ++k) jump_acc[k] = d[1 + k];
+    const unsigned flagged = (unsigned)d[1 + kK];
+    const double L = a.cell[c * 2];
+    double rate_acc[kK];
+#pragma unroll
+    for (int k = 0; k < kK; ++k) rate_acc[k] = 0;
     // damping rate -u^T D u: D u is the viscous residual of this cell alone
     // (nu = 1, zero neighbours, before the det(J) scaling), weighted by the
     // local GLL weights.  Pass 1: the contravariant flux of -grad(u).
@@ -269,7 +332,7 @@ __global__ void __launch_bounds__(32 * kWarps) visc_properties_kernel(PropArgs a
       if (surface) {
         double g[3][kK], h[6][kK];
         local_grad_hess<Q>(U, s_d, s_d2, i, j, l, g, h);
-        for_slots(i, j, l, [&](int side, int t) {
+        for_slots<Q>(i, j, l, [&](int side, int t) {
           const int32_t v = cf[side * QF + t];
           if (v == INT32_MIN) return;
           const int64_t pt = v >= 0 ? v : ~(int64_t)v;
@@ -298,27 +361,30 @@ __global__ void __launch_bounds__(32 * kWarps) visc_properties_kernel(PropArgs a
     for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
       for (int k = 0; k < kK; ++k) rate_acc[k] += __shfl_xor_sync(0xffffffffu, rate_acc[k], o);
-  }
-  if (lane != 0) return;
-  double min_dt = L / speed_max;
-  const double max_visc = speed_max * L / a.p;
-  const double time_base = L / speed_max;
-#pragma unroll
-  for (int k = 0; k < kK; ++k) {
-    double val = 0.0;
-    if (flagged & (1u << k)) {
-      const double rate = -rate_acc[k];
-      const double damping_time = time_base * a.time_scale;
-      const double ratio = jump_acc[k] / (rate * damping_time);
-      const double lo = (0.0 < ratio) ? ratio : 0.0;
-      val = (lo < max_visc) ? lo : max_visc;
-      const double t1 = L / (speed_max + a.spatial_factor * val / L);
-      min_dt = (t1 < min_dt) ? t1 : min_dt;
+    if (lane == 0) {
+    double min_dt = L / speed_max;
+    const double max_visc = speed_max * L / a.p;
+    const double time_base = L / speed_max;
+  #pragma unroll
+    for (int k = 0; k < kK; ++k) {
+      double val = 0.0;
+      if (flagged & (1u << k)) {
+        const double rate = -rate_acc[k];
+        const double damping_time = time_base * a.time_scale;
+        const double ratio = jump_acc[k] / (rate * damping_time);
+        const double lo = (0.0 < ratio) ? ratio : 0.0;
+        val = (lo < max_visc) ? lo : max_visc;
+        const double t1 = L / (speed_max + a.spatial_factor * val / L);
+        min_dt = (t1 < min_dt) ? t1 : min_dt;
+      }
+      a.nu[c * kK + k] = val;
     }
-    a.nu[c * kK + k] = val;
+    if (a.dt_mode) atomicMin(&a.state->min_dt_bits, bits64(min_dt));
+    }
+    __syncwarp();  // s_u and s_ft are rewritten for the next listed cell
   }
-  if (a.dt_mode) atomicMin(&a.state->min_dt_bits, bits64(min_dt));
 }
+
 
 struct ViscFaceArgs {
   const double *u;
@@ -491,8 +557,21 @@ __global__ void majority_kernel(double *u, int64_t n_cells, int n, unsigned long
 template <int Q>
 int props_launch(mcfd_handle *h, const PropArgs &pa) {
   const unsigned blocks = (unsigned)((pa.n_cells + kWarps - 1) / kWarps);
+  cudaMemsetAsync(pa.rate_count, 0, sizeof(unsigned), h->stream);
   visc_properties_kernel<Q><<<blocks, 32 * kWarps, 0, h->stream>>>(pa);
-  return 1;
+  // persistent grid of the rate kernel: the blocks that fit on the device at once
+  const unsigned grid = (unsigned)std::min<int64_t>(blocks, h->visc.rate_blocks);
+  visc_rate_kernel<Q><<<grid, 32 * kWarps, 0, h->stream>>>(pa);
+  return 2;
+}
+
+template <int Q>
+int rate_blocks_per_sm() {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, visc_rate_kernel<Q>, 32 * kWarps, 0) !=
+      cudaSuccess)
+    return 1;
+  return std::max(per_sm, 1);
 }
 
 template <int Q>
@@ -510,12 +589,20 @@ double spatial_factor(int p) {
 
 }  // namespace
 
+int visc_rate_blocks_per_sm(int q) {
+  switch (q) {
+    case 2: return rate_blocks_per_sm<2>();
+    case 3: return rate_blocks_per_sm<3>();
+    default: return rate_blocks_per_sm<4>();
+  }
+}
+
 int launch_visc_properties(mcfd_handle *h, const double *u, int dt_mode) {
   const Mesh &m = h->mesh;
   const Visc &v = h->visc;
   PropArgs pa{u, m.cell_geo, m.cell_flux, m.face_cells, m.face_map, m.face_geo,
               m.dmat, v.d2, v.wloc, v.side, v.pt, v.cell, v.nu, h->buf.state,
-              m.n_cells, h->opt.fr_g1, v.time_scale, spatial_factor(m.p), m.p, dt_mode};
+              v.rate_count, v.rate_cell, v.rate_data, m.n_cells, h->opt.fr_g1, v.time_scale, spatial_factor(m.p), m.p, dt_mode};
   switch (m.q) {
     case 2: return props_launch<2>(h, pa);
     case 3: return props_launch<3>(h, pa);

@@ -68,6 +68,26 @@ def test_viscosity_values_parity(gpu, p, periodic):
     s.close()
 
 
+def test_viscosity_values_parity_many_listed_cells(gpu):
+    """More cells over the jump threshold than the damping-rate kernel's
+    persistent grid has warps (152 SMs x a few resident blocks x 4 warps), so
+    its warps each take several listed cells; two passes are bitwise equal
+    (the list's order does not reach the values)."""
+    m = meshlib.box((40, 40, 4), lengths=(1.0, 1.0, 0.1), periodic=(True,) * 3, jitter=0.1, seed=5)
+    s, om, ov = pair(m, 2)
+    x = meshlib.node_coordinates(m, 2).reshape(-1, 3)
+    u = shock_state(x, np.random.default_rng(11))
+    s.SetSolutionColumn(u)
+    got = s.GetViscosity()
+    want, _ = ov.properties(u)
+    assert (want.reshape(-1, 5).max(axis=1) > 0).sum() > 4000
+    assert np.array_equal(got > 0, want > 0)
+    assert np.abs(got - want).max() <= RTOL * want.max(), np.abs(got - want).max() / want.max()
+    s.SetSolutionColumn(u)
+    assert np.array_equal(s.GetViscosity(), got)
+    s.close()
+
+
 @pytest.mark.parametrize("riemann", ["exact", "hllc", "roe", "rusanov"])
 @pytest.mark.parametrize("p", [2, 3])
 def test_viscous_residual_parity(gpu, riemann, p):
