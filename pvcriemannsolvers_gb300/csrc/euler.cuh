@@ -693,7 +693,7 @@ constexpr double kHllcQ = kGp1Over2 * kOneOverGamma;
 // F_k.  Per component, with g = w / (S_k - S*),
 //   rho:  rho A,   m_i:  m_i A + n_i B,   E:  E A + g S* (S_k p*_k - p_k u_k),
 //   A = g S* (S_k - u_k),   B = g (S_k p*_k - S* p_k),
-// so neither F_k nor U*_k is formed: 24 FP64 operations after the wave
+// so neither F_k nor U*_k is formed: 23 FP64 operations after the wave
 // speeds (the side flux, the star correction and the weight took 50), and
 // lanes of a warp in different cases share one pass through them.
 template <bool FAST_SQRT>
@@ -704,8 +704,9 @@ MCFD_HD void hllc_core_weighted(const double *cl, const double *cr, double il, d
   const double mnl = cl[1] * n[0] + cl[2] * n[1] + cl[3] * n[2];
   const double mnr = cr[1] * n[0] + cr[2] * n[1] + cr[3] * n[2];
   const double unl = mnl * il, unr = mnr * ir;
-  const double rho_average = (rl + rr) / 2, a_average = (al + ar) / 2;
-  const double p_pvrs = (pl + pr - (unr - unl) * rho_average * a_average) / 2;
+  // (p_L + p_R - (u_R - u_L) rho_average a_average) / 2 with the averages'
+  // halves taken out as one exact factor 1/8
+  const double p_pvrs = fma(((unr - unl) * (rl + rr)) * (al + ar), -0.125, 0.5 * (pl + pr));
   // fmax(0, p_pvrs) and the wave-sign tests on the bit patterns (integer
   // pipes; the same results, NaN included)
   const double p_estimate = gt_zero(p_pvrs) ? p_pvrs : 0.0;
@@ -715,7 +716,8 @@ MCFD_HD void hllc_core_weighted(const double *cl, const double *cr, double il, d
   const double wave_left = unl - aql;
   const double wave_right = unr + aqr;
   const double dl = wave_left - unl, dr = wave_right - unr;  // S_k - u_k
-  const double wave_star = (pr - pl + rl * unl * dl - rr * unr * dr) * rcp_signed(rl * dl - rr * dr);
+  const double rdl = rl * dl, rdr = rr * dr;                  // rho_k (S_k - u_k)
+  const double wave_star = fma(unl, rdl, fma(-unr, rdr, pr - pl)) * rcp_signed(rdl - rdr);
   const bool sup_l = ge_zero(wave_left), sup_r = le_zero(wave_right);
   const bool star = !sup_l && !sup_r;
   if (star && !ge_zero(wave_star) && !lt_zero(wave_star)) {  // wave_star is NaN
@@ -733,7 +735,8 @@ MCFD_HD void hllc_core_weighted(const double *cl, const double *cr, double il, d
   const double ss = star ? wave_star : 1.0;
   const double skun = star ? (left ? dl : dr) : neg_bits(un);
   const double g = w * rcp_signed(sk - ss);
-  const double pstar = fma(c[0] * skun, ss - un, p);
+  // p*_k = p_k + rho_k (S_k - u_k)(S* - u_k) (used only with the star correction)
+  const double pstar = fma(left ? rdl : rdr, ss - un, p);
   const double sp = star ? sk * pstar : 0.0;  // S_k p*_k
   const double gs = g * ss;
   const double A = gs * skun;
@@ -750,7 +753,10 @@ MCFD_HD bool flux_hllc_cons_weighted(const double *cl, const double *cr, const d
                                      double w, double *f) {
   const double rl = cl[0], rr = cr[0];
   if (!bits_positive(rl) || !bits_positive(rr) || bits_negative(cl[4]) || bits_negative(cr[4])) return false;
-  const double il = rcp_newton(rl), ir = rcp_newton(rr);
+  // the mixed form: one Newton step (relative error below 4e-14, as its node
+  // traces take it, beside the seeded square roots' 1.4e-13)
+  const double il = FAST_SQRT ? rcp_newton1(rl) : rcp_newton(rl);
+  const double ir = FAST_SQRT ? rcp_newton1(rr) : rcp_newton(rr);
   // p = (E - |m|^2 / (2 rho)) (gamma - 1)
   const double ml = cl[1] * cl[1] + cl[2] * cl[2] + cl[3] * cl[3];
   const double mr = cr[1] * cr[1] + cr[2] * cr[2] + cr[3] * cr[3];

@@ -472,7 +472,7 @@ struct ModalFace32Args {
 };
 
 template <int M, int R>
-__global__ void __launch_bounds__(512) modal_face32_kernel(ModalFace32Args a) {
+__global__ void __launch_bounds__(512, R == kHllc ? 2 : 0) modal_face32_kernel(ModalFace32Args a) {
   int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= a.n_points) return;
   const int f = a.point_face[gid];
