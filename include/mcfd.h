@@ -594,8 +594,15 @@ enum mcfd_probe_op {
   MCFD_PROBE_CUDA_SQRT = 6,       /* double -> double: sqrt(x) */
   MCFD_PROBE_CUDA_F64_TO_F32 = 7, /* double -> float: __double2float_rn */
   MCFD_PROBE_CUDA_F32_TO_F64 = 8, /* float -> double: (double)f */
-  MCFD_PROBE_RCP1 = 9             /* double -> double: one-step Newton reciprocal, x > 0
+  MCFD_PROBE_RCP1 = 9,            /* double -> double: one-step Newton reciprocal, x > 0
                                      (the mixed form's node traces) */
+  /* the Exact solver's powers for gamma = 1.4, from FP32-seeded inverse roots
+     refined by Newton steps (pow outside x in [2^-120, 2^120]) */
+  MCFD_PROBE_ROOT7 = 10,          /* double -> double: x^((gamma-1)/(2 gamma)) = x^(1/7) */
+  MCFD_PROBE_ROOT7_OVER_X = 11,   /* double -> double: x^(1/7) / x */
+  MCFD_PROBE_POW_NEG_GAMMA = 12,  /* double -> double: x^(-gamma) */
+  MCFD_PROBE_CUDA_POW_ROOT7 = 13, /* double -> double: pow(x, (gamma-1)/(2 gamma)) */
+  MCFD_PROBE_CUDA_POW_NEG_GAMMA = 14 /* double -> double: 1 / pow(x, gamma) */
 };
 int mcfd_probe_numerics(int32_t device, int32_t op, int64_t n, const void *d_in,
                         void *d_out);

@@ -163,7 +163,9 @@ SIGNATURES = {
     "mcfd_probe_numerics": (C.c_int, [C.c_int32, C.c_int32, C.c_int64, _P, _P]),
 }
 PROBE_RCP, PROBE_RCP_SIGNED, PROBE_SQRT_SEEDED, PROBE_F64_TO_F32, PROBE_F32_TO_F64, \
-    PROBE_CUDA_RCP, PROBE_CUDA_SQRT, PROBE_CUDA_F64_TO_F32, PROBE_CUDA_F32_TO_F64, PROBE_RCP1 = range(10)
+    PROBE_CUDA_RCP, PROBE_CUDA_SQRT, PROBE_CUDA_F64_TO_F32, PROBE_CUDA_F32_TO_F64, PROBE_RCP1, \
+    PROBE_ROOT7, PROBE_ROOT7_OVER_X, PROBE_POW_NEG_GAMMA, PROBE_CUDA_POW_ROOT7, \
+    PROBE_CUDA_POW_NEG_GAMMA = range(15)
 LIMITER = {"none": 0, "lazy": 1, "detect_lazy": 2, "eigen": 3}
 
 _lib = None

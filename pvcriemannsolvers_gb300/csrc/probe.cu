@@ -12,8 +12,8 @@
 //
 // mcfd_probe_numerics evaluates the arithmetic that replaces CUDA's own
 // operators on the FP64-bound paths (Newton reciprocals, the seeded square
-// root, the integer-pipe FP64 <-> FP32 conversions) next to CUDA's operators
-// on the same inputs.
+// root, the integer-pipe FP64 <-> FP32 conversions, the Exact solver's
+// inverse-root powers) next to CUDA's operators on the same inputs.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -69,6 +69,16 @@ probe_numerics_kernel(int op, int64_t n, const void *in, void *out) {
     case MCFD_PROBE_CUDA_F64_TO_F32: yf[i] = __double2float_rn(x[i]); break;
     case MCFD_PROBE_CUDA_F32_TO_F64: y[i] = (double)xf[i]; break;
     case MCFD_PROBE_RCP1: y[i] = rcp_newton1(x[i]); break;
+    case MCFD_PROBE_ROOT7: y[i] = ex_root7(x[i]); break;
+    case MCFD_PROBE_ROOT7_OVER_X: {
+      double r67;
+      ex_root7(x[i], &r67);
+      y[i] = r67;
+      break;
+    }
+    case MCFD_PROBE_POW_NEG_GAMMA: y[i] = ex_isentrope(1.0, x[i]); break;
+    case MCFD_PROBE_CUDA_POW_ROOT7: y[i] = pow(x[i], kGm1Over2 / kGamma); break;
+    case MCFD_PROBE_CUDA_POW_NEG_GAMMA: y[i] = 1.0 / pow(x[i], kGamma); break;
     default: break;
   }
 }
@@ -121,7 +131,7 @@ extern "C" int mcfd_probe_flux(int32_t device, int32_t riemann, int32_t precisio
 
 extern "C" int mcfd_probe_numerics(int32_t device, int32_t op, int64_t n, const void *d_in,
                                    void *d_out) {
-  if (n < 0 || n > (int64_t)INT32_MAX * 256 || op < MCFD_PROBE_RCP || op > MCFD_PROBE_RCP1)
+  if (n < 0 || n > (int64_t)INT32_MAX * 256 || op < MCFD_PROBE_RCP || op > MCFD_PROBE_CUDA_POW_NEG_GAMMA)
     return MCFD_ERR_ARGUMENT;
   if (n == 0) return MCFD_OK;
   if (!d_in || !d_out) return MCFD_ERR_ARGUMENT;

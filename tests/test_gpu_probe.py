@@ -378,6 +378,44 @@ def test_rcp_signed_within_one_ulp_of_cuda_division(gpu):
     assert not bad.any(), (x[fin][bad][:5], got[fin][bad][:5], ref[fin][bad][:5])
 
 
+ROOT_RTOL = 2e-14  # two Newton steps on an FP32 seed, then up to seven roundings
+
+
+def seeded_root_range(x):
+    """Inputs that the Exact solver's inverse roots take: positive normal x
+    with 2^-120 <= x < 2^121 (binary64 exponent fields 903..1143)."""
+    ex = (x.view(np.uint64) >> np.uint64(52)) & np.uint64(0x7FF)
+    return (x > 0) & (ex >= 903) & (ex <= 1143)
+
+
+@pytest.mark.parametrize("op, cuda_op, what", [
+    (capi.PROBE_ROOT7, capi.PROBE_CUDA_POW_ROOT7, "x^(1/7)"),
+    (capi.PROBE_ROOT7_OVER_X, capi.PROBE_CUDA_POW_ROOT7, "x^(1/7) / x"),
+    (capi.PROBE_POW_NEG_GAMMA, capi.PROBE_CUDA_POW_NEG_GAMMA, "x^-gamma"),
+])
+def test_exact_solver_roots_within_their_bound_of_cuda_pow(gpu, op, cuda_op, what):
+    """The Exact solver's powers (gamma = 1.4: r^(1/7) of the expansion
+    branch, its derivative's r^(1/7) / r, the isentrope's rho^-gamma) from
+    FP32-seeded inverse roots: within ROOT_RTOL of CUDA's pow over the seeded
+    range, and CUDA's pow itself (bit for bit) outside it: zero, subnormals,
+    the extreme exponents, infinities, NaN and negative inputs."""
+    import torch
+    rng = np.random.default_rng(12)
+    dense = 2.0 ** rng.uniform(-120, 121, 30000)
+    x = np.concatenate([f64_sweep(rng), dense,
+                        [0.0, -0.0, np.inf, -np.inf, np.nan, 1.0, 2.0 ** -120, 2.0 ** 121]])
+    got = probe_numerics(op, x, torch.float64)
+    ref = probe_numerics(cuda_op, x, torch.float64)
+    if op == capi.PROBE_ROOT7_OVER_X:
+        with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+            ref = ref / x
+    inside = seeded_root_range(x)
+    assert inside.sum() > 30000
+    rel = np.abs(got[inside] - ref[inside]) / np.abs(ref[inside])
+    assert rel.max() <= ROOT_RTOL, (what, rel.max(), x[inside][np.argmax(rel)])
+    assert np.array_equal(got[~inside], ref[~inside], equal_nan=True), what
+
+
 RCP1_RTOL = 4e-14  # one Newton step on an FP32 seed of relative error < 1.8e-7
 
 
