@@ -153,14 +153,7 @@ template <int Q>
 __global__ void __launch_bounds__(32 * kWarps) visc_properties_kernel(PropArgs a) {
   constexpr int N = Q * Q * Q, QF = Q * Q, KN = kK * N;
   __shared__ double s_u[kWarps][KN];
-  __shared__ double s_ft[kWarps][3 * kK][N];
-  __shared__ double s_d[Q * Q], s_d2[Q * Q], s_w[N];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int e = threadIdx.x; e < Q * Q; e += blockDim.x) {
-    s_d[e] = a.dmat[e];
-    s_d2[e] = a.d2[e];
-  }
-  for (int e = threadIdx.x; e < N; e += blockDim.x) s_w[e] = a.wloc[e];
   const int64_t c = (int64_t)blockIdx.x * kWarps + warp;
   const bool active = c < a.n_cells;
   if (active)
