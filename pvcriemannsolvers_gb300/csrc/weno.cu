@@ -293,7 +293,8 @@ __device__ void eigen_matrices(const EigenState &s, const double *nu, const doub
 // weno::Eigen reconstruction of cell c from its candidates (slots 0..n_adj-1
 // neighbours, slot 6 own) into s_new, all adjacent faces at once so that the
 // 64 threads stay busy:
-//   G_i = C_i B C_i^T     (K x K, face-independent) for each candidate
+//   G_i = C_i B C_i^T     (K x K, face-independent, symmetric: its upper
+//                          triangle) for each candidate
 //   L_f, R_f              every entry of every face's eigen-matrices
 //   beta[f][i][k] = L_f[k] G_i L_f[k]^T   (= GetSmoothness of L_f C_i)
 //   w[f][i][k]            the reference's weights per face and field
@@ -332,12 +333,21 @@ __device__ void eigen_reconstruct(const Args &a, int64_t c, int n_adj,
     eigen_matrices(s_es, fr, fr + 3, fr + 6, s_LR[t]);
   }
   __syncthreads();
-  for (int i = t; i < nc * kK * kK; i += nt) {
-    const int cand = i / (kK * kK), r = i - cand * kK * kK, j = r / kK, l = r - j * kK;
+  // G is symmetric (B is): its upper triangle only, the off-diagonal entries
+  // doubled, so that L G L^T = sum_j L_j (G_jj L_j + sum_{l > j} 2 G_jl L_l)
+  constexpr int kUpper = kK * (kK + 1) / 2;  // 15 entries l >= j
+  for (int i = t; i < nc * kUpper; i += nt) {
+    const int cand = i / kUpper;
+    int r = i - cand * kUpper, j = 0;
+    while (r >= kK - j) {  // row j holds the kK - j entries l = j .. kK - 1
+      r -= kK - j;
+      ++j;
+    }
+    const int l = j + r;
     const int src = cand < n_adj ? cand : 6;
     double v = 0;
     for (int m = 0; m < M; ++m) v += s_cb[cand][j][m] * s_cand[src][l][m];
-    s_G[cand][j][l] = v;
+    s_G[cand][j][l] = l == j ? v : 2 * v;
   }
   __syncthreads();
   for (int i = t; i < n_adj * nc * kK; i += nt) {
@@ -346,9 +356,9 @@ __device__ void eigen_reconstruct(const Args &a, int64_t c, int n_adj,
     double b = 0;
 #pragma unroll
     for (int j = 0; j < kK; ++j) {
-      double row = 0;
+      double row = s_G[cand][j][j] * Lk[j];
 #pragma unroll
-      for (int l = 0; l < kK; ++l) row += s_G[cand][j][l] * Lk[l];
+      for (int l = j + 1; l < kK; ++l) row += s_G[cand][j][l] * Lk[l];
       b += Lk[j] * row;
     }
     s_beta[f][cand][k] = b;
